@@ -1,0 +1,245 @@
+"""ctypes binding of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Loaded by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs to
+check (or time beside) the CUDA path.  Nothing in the product package imports
+this module.  See sph_oracle.h for the pinning status of the restatement.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+
+
+def build(quiet: bool = True) -> None:
+    """Compile liboracle_f64.so / liboracle_f32.so with the committed Makefile."""
+    out = subprocess.run(["make", "-C", HERE, "-s"], capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
+
+
+class OrcParams(ctypes.Structure):
+    _fields_ = [
+        ("radius", ctypes.c_double),
+        ("density0", ctypes.c_double),
+        ("gravity", ctypes.c_double * 3),
+        ("cfl_method", ctypes.c_int),
+        ("cfl_factor", ctypes.c_double),
+        ("cfl_min", ctypes.c_double),
+        ("cfl_max", ctypes.c_double),
+        ("min_iterations", ctypes.c_uint),
+        ("max_iterations", ctypes.c_uint),
+        ("max_error", ctypes.c_double),
+        ("enable_divergence_solver", ctypes.c_int),
+        ("max_iterations_v", ctypes.c_uint),
+        ("max_error_v", ctypes.c_double),
+        ("xsph_fluid", ctypes.c_double),
+        ("xsph_boundary", ctypes.c_double),
+        ("viscosity_method", ctypes.c_int),
+        ("viscosity", ctypes.c_double),
+        ("viscosity_boundary", ctypes.c_double),
+        ("visco_max_iter", ctypes.c_uint),
+        ("visco_max_error", ctypes.c_double),
+        ("fp32_predicate", ctypes.c_int),
+        ("num_threads", ctypes.c_int),
+    ]
+
+
+class OrcState(ctypes.Structure):
+    _fields_ = [
+        ("n", ctypes.c_uint),
+        ("nb", ctypes.c_uint),
+        ("x", ctypes.c_void_p),
+        ("v", ctypes.c_void_p),
+        ("a", ctypes.c_void_p),
+        ("density", ctypes.c_void_p),
+        ("factor", ctypes.c_void_p),
+        ("density_adv", ctypes.c_void_p),
+        ("kappa", ctypes.c_void_p),
+        ("kappa_v", ctypes.c_void_p),
+        ("pressure_accel", ctypes.c_void_p),
+        ("vdiff", ctypes.c_void_p),
+        ("xb", ctypes.c_void_p),
+        ("Vb", ctypes.c_void_p),
+        ("dt", ctypes.c_double),
+        ("time", ctypes.c_double),
+        ("iterations", ctypes.c_uint),
+        ("iterations_v", ctypes.c_uint),
+        ("visco_iterations", ctypes.c_uint),
+        ("avg_density_err", ctypes.c_double),
+        ("avg_density_err_v", ctypes.c_double),
+        ("visco_error", ctypes.c_double),
+        ("dt_old", ctypes.c_double),
+        ("factor_raw", ctypes.c_void_p),
+        ("density_adv_v", ctypes.c_void_p),
+        ("num_fluid_neighbors", ctypes.c_void_p),
+        ("num_boundary_neighbors", ctypes.c_void_p),
+    ]
+
+
+_LIBS = {}
+
+
+def lib(precision: str = "f64") -> ctypes.CDLL:
+    if precision not in _LIBS:
+        path = os.path.join(BUILD, f"liboracle_{precision}.so")
+        if not os.path.exists(path):
+            build()
+        L = ctypes.CDLL(path)
+        L.orc_step.argtypes = [ctypes.POINTER(OrcState), ctypes.POINTER(OrcParams)]
+        L.orc_step.restype = ctypes.c_int
+        L.orc_kernel_W.argtypes = [ctypes.c_double, ctypes.c_double]
+        L.orc_kernel_W.restype = ctypes.c_double
+        L.orc_kernel_gradW.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p]
+        L.orc_kernel_gradW.restype = None
+        L.orc_neighbors.argtypes = [ctypes.c_uint, ctypes.c_void_p, ctypes.c_uint, ctypes.c_void_p,
+                                    ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                    ctypes.c_void_p, ctypes.c_uint]
+        L.orc_neighbors.restype = ctypes.c_int
+        L.orc_boundary_volume.argtypes = [ctypes.c_uint, ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
+                                          ctypes.c_void_p]
+        L.orc_boundary_volume.restype = ctypes.c_int
+        for name in ("orc_weiler_system",):
+            f = getattr(L, name)
+            f.argtypes = [ctypes.POINTER(OrcState), ctypes.POINTER(OrcParams), ctypes.c_double,
+                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+            f.restype = ctypes.c_int
+        L.orc_weiler_matvec.argtypes = [ctypes.POINTER(OrcState), ctypes.POINTER(OrcParams), ctypes.c_double,
+                                        ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_weiler_matvec.restype = ctypes.c_int
+        L.orc_weiler_solve.argtypes = [ctypes.POINTER(OrcState), ctypes.POINTER(OrcParams), ctypes.c_double,
+                                       ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint),
+                                       ctypes.POINTER(ctypes.c_double)]
+        L.orc_weiler_solve.restype = ctypes.c_int
+        _LIBS[precision] = L
+    return _LIBS[precision]
+
+
+def make_params(p, fp32_predicate: bool = True, num_threads: int = 0) -> OrcParams:
+    """Convert an SPHParams (splishsplash_gb300.scenes) into the oracle's struct."""
+    q = OrcParams()
+    q.radius = p.particleRadius
+    q.density0 = p.density0
+    q.gravity = (ctypes.c_double * 3)(*p.gravitation)
+    q.cfl_method = p.cflMethod
+    q.cfl_factor = p.cflFactor
+    q.cfl_min = p.cflMinTimeStepSize
+    q.cfl_max = p.cflMaxTimeStepSize
+    q.min_iterations = p.minIterations
+    q.max_iterations = p.maxIterations
+    q.max_error = p.maxError
+    q.enable_divergence_solver = int(p.enableDivergenceSolver)
+    q.max_iterations_v = p.maxIterationsV
+    q.max_error_v = p.maxErrorV
+    q.xsph_fluid = p.xsph
+    q.xsph_boundary = p.xsphBoundary
+    q.viscosity_method = p.viscosityMethod
+    q.viscosity = p.viscosity
+    q.viscosity_boundary = p.viscosityBoundary
+    q.visco_max_iter = p.viscoMaxIter
+    q.visco_max_error = p.viscoMaxError
+    q.fp32_predicate = int(fp32_predicate)
+    q.num_threads = num_threads
+    return q
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+class OracleSim:
+    """A scene advanced by the oracle; arrays live in numpy (AoS, n x 3)."""
+
+    def __init__(self, scene, precision: str = "f64", fp32_predicate: bool = True, num_threads: int = 0):
+        self.precision = precision
+        dt = np.float64 if precision == "f64" else np.float32
+        self.dtype = dt
+        self.lib = lib(precision)
+        self.params = scene.params
+        self.cp = make_params(scene.params, fp32_predicate, num_threads)
+        n, nb = scene.n, scene.nb
+        self.n, self.nb = n, nb
+        self.x = np.ascontiguousarray(scene.x, dtype=dt)
+        self.v = np.ascontiguousarray(scene.v, dtype=dt)
+        self.a = np.zeros((n, 3), dt)
+        self.density = np.zeros(n, dt)
+        self.factor = np.zeros(n, dt)
+        self.density_adv = np.zeros(n, dt)
+        self.kappa = np.zeros(n, dt)
+        self.kappa_v = np.zeros(n, dt)
+        self.pressure_accel = np.zeros((n, 3), dt)
+        self.vdiff = np.zeros((n, 3), dt)
+        self.xb = np.ascontiguousarray(scene.xb, dtype=dt)
+        self.Vb = np.zeros(nb, dt)
+        self.factor_raw = np.zeros(n, dt)
+        self.density_adv_v = np.zeros(n, dt)
+        self.nf = np.zeros(n, np.uint32)
+        self.nbn = np.zeros(n, np.uint32)
+        rc = self.lib.orc_boundary_volume(nb, _ptr(self.xb), scene.params.supportRadius,
+                                          int(fp32_predicate), _ptr(self.Vb))
+        if rc != 0:
+            raise RuntimeError(f"orc_boundary_volume failed: {rc}")
+        self.st = OrcState()
+        self.st.n, self.st.nb = n, nb
+        for name in ("x", "v", "a", "density", "factor", "density_adv", "kappa", "kappa_v",
+                     "pressure_accel", "vdiff", "xb", "Vb", "factor_raw", "density_adv_v"):
+            setattr(self.st, name, _ptr(getattr(self, name)))
+        self.st.num_fluid_neighbors = _ptr(self.nf)
+        self.st.num_boundary_neighbors = _ptr(self.nbn)
+        self.st.dt = scene.params.timeStepSize
+        self.st.time = 0.0
+
+    def step(self):
+        rc = self.lib.orc_step(ctypes.byref(self.st), ctypes.byref(self.cp))
+        if rc != 0:
+            raise RuntimeError(f"orc_step failed: {rc}")
+
+    @property
+    def dt(self):
+        return self.st.dt
+
+    @dt.setter
+    def dt(self, value):
+        self.st.dt = value
+
+    def stats(self):
+        s = self.st
+        return dict(iterations=s.iterations, iterations_v=s.iterations_v, visco_iterations=s.visco_iterations,
+                    avg_density_err=s.avg_density_err, avg_density_err_v=s.avg_density_err_v,
+                    visco_error=s.visco_error, dt_old=s.dt_old, dt=s.dt, time=s.time)
+
+
+def neighbors(x, y, support, same_set, fp32=True, precision="f64"):
+    """CSR neighbour lists (offsets, indices) of points x against y."""
+    L = lib(precision)
+    dt = np.float64 if precision == "f64" else np.float32
+    x = np.ascontiguousarray(x, dtype=dt)
+    y = np.ascontiguousarray(y, dtype=dt)
+    n, m = x.shape[0], y.shape[0]
+    off = np.zeros(n + 1, np.uint32)
+    rc = L.orc_neighbors(n, _ptr(x), m, _ptr(y), support, int(same_set), int(fp32), _ptr(off), None, 0)
+    if rc != 0:
+        raise RuntimeError(f"orc_neighbors failed: {rc}")
+    idx = np.zeros(max(1, int(off[-1])), np.uint32)
+    rc = L.orc_neighbors(n, _ptr(x), m, _ptr(y), support, int(same_set), int(fp32), _ptr(off), _ptr(idx),
+                         idx.size)
+    if rc != 0:
+        raise RuntimeError(f"orc_neighbors failed: {rc}")
+    return off, idx[: int(off[-1])]
+
+
+def kernel_W(r, support):
+    return lib().orc_kernel_W(float(r), float(support))
+
+
+def kernel_gradW(r, support):
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    out = np.zeros(3, np.float64)
+    lib().orc_kernel_gradW(_ptr(r), float(support), _ptr(out))
+    return out

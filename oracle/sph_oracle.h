@@ -1,0 +1,108 @@
+/*
+ * CPU oracle for the DFSPH time-step hot path -- TEST INFRASTRUCTURE ONLY.
+ *
+ * This is a plain-C restatement of the reference algorithm (SPlisHSPlasH 2.16.0)
+ * used as the checker for the CUDA path.  Only tests/, __graft_entry__.smoke()
+ * and bench.py's cpu_baseline / --impl reference legs may load it.  The product
+ * path (splishsplash_gb300, libsphgb300.so) never calls into it.
+ *
+ * Pinning status:
+ *   - Cubic spline W / gradW: pinned against values produced by the reference's
+ *     own SPHKernels.{h,cpp} (compiled from the reference tree by
+ *     oracle/build_ref.sh into oracle/_ref/), stored in tests/golden/.
+ *   - 3x3 block-Jacobi preconditioned CG: pinned against the reference's
+ *     MatrixFreeSolver.h + vendored Eigen 3.4 ConjugateGradient, run on the
+ *     oracle's own Weiler2018 operator (tests/golden/).
+ *   - DFSPH / Akinci2012 / XSPH / Weiler2018 per-particle sums and the solver
+ *     loops: parity unpinned.  The reference has no golden vectors for them and
+ *     its full library cannot be built here (it needs the CompactNSearch,
+ *     GenericParameters and Discregrid external projects, which are absent).
+ *     Every function below cites the reference file:line it restates.
+ *
+ * Build: two precisions from one source (ORC_REAL = double | float).  The FP64
+ * build is the parity oracle; the FP32 build is the CPU timing baseline (a
+ * port of the reference's FP32 OpenMP path, not the reference binary).
+ */
+#ifndef SPH_ORACLE_H
+#define SPH_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#ifndef ORC_REAL
+#define ORC_REAL double
+#endif
+typedef ORC_REAL orc_real;
+
+typedef struct orc_params {
+    double radius;               /* particle radius r; support radius = 4r (Simulation.cpp:283) */
+    double density0;             /* rest density (FluidModel density0) */
+    double gravity[3];           /* Simulation::GRAVITATION */
+    int cfl_method;              /* 0 none, 1 CFL, 2 CFL + iteration heuristic (Simulation.cpp:395-413) */
+    double cfl_factor, cfl_min, cfl_max;
+    unsigned min_iterations, max_iterations;   /* DFSPH minIterations / maxIterations */
+    double max_error;                          /* DFSPH maxError (percent) */
+    int enable_divergence_solver;
+    unsigned max_iterations_v;                 /* DFSPH maxIterationsV */
+    double max_error_v;                        /* DFSPH maxErrorV (percent) */
+    double xsph_fluid, xsph_boundary;          /* XSPH xsph / xsphBoundary */
+    int viscosity_method;                      /* 0 none, 6 Weiler et al. 2018 */
+    double viscosity, viscosity_boundary;      /* Weiler viscosity / viscosityBoundary */
+    unsigned visco_max_iter;                   /* Weiler viscoMaxIter */
+    double visco_max_error;                    /* Weiler viscoMaxError */
+    int fp32_predicate;          /* evaluate |xi-xj|^2 < h^2 in float (as the FP32 device path) */
+    int num_threads;             /* OpenMP threads (0 = runtime default) */
+} orc_params;
+
+typedef struct orc_state {
+    unsigned n, nb;
+    orc_real *x, *v, *a;                  /* 3n, AoS (x0,y0,z0,x1,...) like Vector3r */
+    orc_real *density, *factor, *density_adv, *kappa, *kappa_v;   /* n */
+    orc_real *pressure_accel, *vdiff;     /* 3n */
+    orc_real *xb, *Vb;                    /* 3nb, nb (static boundary, v_b = 0) */
+    double dt, time;
+    /* written by orc_step */
+    unsigned iterations, iterations_v, visco_iterations;
+    double avg_density_err, avg_density_err_v, visco_error;
+    double dt_old;
+    /* optional outputs (may be NULL) */
+    orc_real *factor_raw;                 /* alpha right after computeDFSPHFactor */
+    orc_real *density_adv_v;              /* divergence source (unclamped) */
+    unsigned *num_fluid_neighbors, *num_boundary_neighbors;
+} orc_state;
+
+/* Cubic spline (SPHKernels.h:16-91). */
+double orc_kernel_W(double r, double support);
+void orc_kernel_gradW(const double r[3], double support, double out[3]);
+
+/* Neighbour lists as CSR sorted ascending per particle.  For query points x (n)
+ * against points y (m); self excluded when same_set != 0.  Returns 0 on success.
+ * offsets must hold n+1 entries; when indices == NULL only the counts/offsets are
+ * produced.  Predicate: squared distance < support^2, evaluated in float when
+ * fp32 != 0 (separate multiplies and adds, no fused multiply-add). */
+int orc_neighbors(unsigned n, const orc_real *x, unsigned m, const orc_real *y,
+                  double support, int same_set, int fp32,
+                  unsigned *offsets, unsigned *indices, unsigned capacity);
+
+/* Akinci2012 boundary volume V_b = 1 / (W0 + sum_b' W(x_b - x_b'))
+ * (BoundaryModel_Akinci2012.cpp:48-75). */
+int orc_boundary_volume(unsigned nb, const orc_real *xb, double support, int fp32, orc_real *Vb);
+
+/* One TimeStepDFSPH::step() (TimeStepDFSPH.cpp:117-249). */
+int orc_step(orc_state *s, const orc_params *p);
+
+/* Weiler2018 operator pieces for the CG pin (Viscosity_Weiler2018.cpp:271-443,
+ * 605-742).  Lists are rebuilt from state positions. */
+int orc_weiler_system(const orc_state *s, const orc_params *p, double dt,
+                      orc_real *b, orc_real *g, orc_real *diag9);
+int orc_weiler_matvec(const orc_state *s, const orc_params *p, double dt,
+                      const orc_real *vec, orc_real *result);
+/* CG restatement (ConjugateGradient.h:29-90 with MatrixFreeSolver.h:201-272). */
+int orc_weiler_solve(const orc_state *s, const orc_params *p, double dt,
+                     orc_real *x_out, unsigned *iters, double *err);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
