@@ -1,0 +1,171 @@
+/*
+ * sphgb300 -- GB300-native (sm_103a) DFSPH time step behind a C ABI.
+ *
+ * One context holds one fluid model (one fluid phase) with static Akinci2012
+ * boundary particles, device-resident for the life of the context.  Every call
+ * returns an int status (SPHGB_OK = 0); no C++ exception crosses the ABI and no
+ * kernel traps.  A context is driven by one host thread and owns one CUDA
+ * stream.  Arrays are plain host pointers, AoS Vector3 layout (x0,y0,z0,x1,...)
+ * exactly like the reference's std::vector<Vector3r> storage.
+ *
+ * Reference interfaces replaced (SPlisHSPlasH 2.16.0, paths relative to the
+ * project root):
+ *   sphgb_step            TimeStepDFSPH::step           SPlisHSPlasH/DFSPH/TimeStepDFSPH.cpp:117-249
+ *                         (neighbour search Simulation.cpp:606-619, densities TimeStep.cpp:54-169,
+ *                          DFSPH factor :735-825, divergence solve :386-541, non-pressure forces
+ *                          Simulation.cpp:495-509 with XSPH XSPH.cpp:46-216 and Weiler2018
+ *                          Viscosity/Viscosity_Weiler2018.cpp:891-1089, CFL Simulation.cpp:395-493,
+ *                          pressure solve TimeStepDFSPH.cpp:252-384)
+ *   sphgb_upload_fluid    FluidModel::initModel          SPlisHSPlasH/FluidModel.cpp:285-327
+ *   sphgb_upload_boundary BoundaryModel_Akinci2012::initModel + computeBoundaryVolume
+ *                                                        SPlisHSPlasH/BoundaryModel_Akinci2012.cpp:48-110,
+ *                                                        Simulation::updateBoundaryVolume Simulation.cpp:696-756
+ *   sphgb_download /      FluidModel::getFieldBuffer     pySPlisHSPlasH/FluidModelModule.cpp:86-118,
+ *   sphgb_upload_field    field registry                 FluidModel.cpp:694-710, TimeStepDFSPH.cpp:49-53,
+ *                                                        Viscosity_Weiler2018.cpp:33
+ *   sphgb_neighbors       Simulation::getNeighborList    SPlisHSPlasH/Simulation.h:451-473
+ *   sphgb_set_params      ParameterObject set/getValue   TimeStepDFSPH.cpp:73-115, Simulation.cpp:163-277,
+ *                                                        XSPH.cpp:27-42, Viscosity_Weiler2018.cpp:43-74
+ */
+#ifndef SPHGB300_H
+#define SPHGB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPHGB_ABI_VERSION 1
+
+/* status codes */
+#define SPHGB_OK 0
+#define SPHGB_ERR_ARGUMENT 1      /* bad pointer / size / enum */
+#define SPHGB_ERR_CUDA 2          /* a CUDA runtime call failed (message in sphgb_last_error) */
+#define SPHGB_ERR_CAPACITY 3      /* neighbour-list or particle capacity exceeded */
+#define SPHGB_ERR_NONFINITE 4     /* NaN/Inf velocity detected during the step */
+#define SPHGB_ERR_STATE 5         /* call out of order (e.g. step before upload) */
+#define SPHGB_ERR_GRID 6          /* scene extent too large for the cell grid */
+
+/* precision of the bulk arithmetic */
+#define SPHGB_PRECISION_FP32 0    /* FP32 neighbour sums; FP64 reductions, dt, time and positions */
+#define SPHGB_PRECISION_FP64 1    /* everything in FP64 */
+
+typedef struct sphgb_config {
+    int abi_version;                 /* must be SPHGB_ABI_VERSION */
+    int device;                      /* CUDA device ordinal */
+    int precision;                   /* SPHGB_PRECISION_* */
+    uint32_t max_fluid_neighbors;    /* per-particle list capacity (0 = default 80) */
+    uint32_t max_boundary_neighbors; /* per-particle list capacity (0 = default 128) */
+    int use_graph;                   /* 1: capture the step in a CUDA graph with device-side
+                                        solver loops (conditional while nodes); 0: host-driven loops */
+} sphgb_config;
+
+typedef struct sphgb_params {
+    double particle_radius;          /* Simulation "particleRadius"; support radius = 4 r */
+    double density0;                 /* FluidModel "density0" */
+    double gravity[3];               /* Simulation "gravitation" */
+    int cfl_method;                  /* "cflMethod": 0 none, 1 CFL, 2 CFL + iteration heuristic */
+    double cfl_factor;               /* "cflFactor" */
+    double cfl_min_time_step;        /* "cflMinTimeStepSize" */
+    double cfl_max_time_step;        /* "cflMaxTimeStepSize" */
+    uint32_t min_iterations;         /* DFSPH "minIterations" */
+    uint32_t max_iterations;         /* DFSPH "maxIterations" */
+    double max_error;                /* DFSPH "maxError" (percent) */
+    int enable_divergence_solver;    /* DFSPH "enableDivergenceSolver" */
+    uint32_t max_iterations_v;       /* DFSPH "maxIterationsV" */
+    double max_error_v;              /* DFSPH "maxErrorV" (percent) */
+    double xsph;                     /* XSPH "xsph" */
+    double xsph_boundary;            /* XSPH "xsphBoundary" */
+    int viscosity_method;            /* 0 none, 6 "Weiler et al. 2018" */
+    double viscosity;                /* Weiler "viscosity" */
+    double viscosity_boundary;       /* Weiler "viscosityBoundary" */
+    uint32_t visco_max_iter;         /* Weiler "viscoMaxIter" */
+    double visco_max_error;          /* Weiler "viscoMaxError" */
+} sphgb_params;
+
+typedef struct sphgb_stats {
+    uint32_t iterations;             /* DFSPH "iterations" (pressure solve) */
+    uint32_t iterations_v;           /* DFSPH "iterationsV" (divergence solve) */
+    uint32_t visco_iterations;       /* Weiler "viscoIterations" (Eigen CG iteration count) */
+    uint32_t max_fluid_neighbors;    /* largest fluid neighbour count seen this step */
+    uint32_t max_boundary_neighbors; /* largest boundary neighbour count seen this step */
+    uint32_t flags;                  /* bit 0 capacity overflow, bit 1 non-finite */
+    double avg_density_err;          /* last pressure-solve average density error (FP64) */
+    double avg_density_err_v;        /* last divergence-solve average error (FP64) */
+    double visco_error;              /* CG relative residual */
+    double dt_used;                  /* step size used for the kick and the position update */
+    double dt_next;                  /* CFL step size (used by the pressure solve) */
+    double time;                     /* simulated time after the step */
+} sphgb_stats;
+
+/* field ids for sphgb_download / sphgb_upload_field; names are the reference's field names */
+#define SPHGB_FIELD_POSITION 0        /* "position", 3 */
+#define SPHGB_FIELD_VELOCITY 1        /* "velocity", 3 */
+#define SPHGB_FIELD_ACCELERATION 2    /* "acceleration" (non-pressure), 3 */
+#define SPHGB_FIELD_DENSITY 3         /* "density" */
+#define SPHGB_FIELD_FACTOR 4          /* "factor" as stored after step(): alpha / dt_next^2 */
+#define SPHGB_FIELD_DENSITY_ADV 5     /* "advected density" */
+#define SPHGB_FIELD_PRESSURE_RHO2 6   /* "p / rho^2" (kappa, stored * dt^2) */
+#define SPHGB_FIELD_PRESSURE_RHO2_V 7 /* "p_v / rho^2" (kappa_v, stored * dt) */
+#define SPHGB_FIELD_PRESSURE_ACCEL 8  /* "pressure acceleration", 3 */
+#define SPHGB_FIELD_VDIFF 9           /* Weiler "velocity difference", 3 */
+#define SPHGB_FIELD_PARTICLE_ID 10    /* "id" (uint32) */
+#define SPHGB_FIELD_FACTOR_RAW 11     /* alpha as computed by computeDFSPHFactor */
+#define SPHGB_FIELD_NUM_FLUID_NEIGHBORS 12     /* uint32 */
+#define SPHGB_FIELD_NUM_BOUNDARY_NEIGHBORS 13  /* uint32 */
+#define SPHGB_FIELD_BOUNDARY_VOLUME 14         /* boundary "volume" V_b (nb entries) */
+#define SPHGB_FIELD_BOUNDARY_POSITION 15       /* boundary "position" (nb x 3) */
+
+#define SPHGB_DTYPE_F32 0
+#define SPHGB_DTYPE_F64 1
+#define SPHGB_DTYPE_U32 2
+
+typedef struct sphgb_ctx sphgb_ctx;
+
+/* lifetime */
+int sphgb_create(const sphgb_config *cfg, sphgb_ctx **out);
+int sphgb_destroy(sphgb_ctx *ctx);
+const char *sphgb_last_error(const sphgb_ctx *ctx);
+int sphgb_abi_version(void);
+
+/* parameters (may be called between steps) */
+int sphgb_default_params(sphgb_params *p);
+int sphgb_set_params(sphgb_ctx *ctx, const sphgb_params *p);
+int sphgb_get_params(const sphgb_ctx *ctx, sphgb_params *p);
+
+/* scene set-up.  Positions/velocities AoS n x 3; ids may be NULL (0..n-1).
+ * upload_boundary computes the Akinci2012 volumes on the device. */
+int sphgb_upload_boundary(sphgb_ctx *ctx, const double *xb, uint32_t nb);
+int sphgb_upload_boundary_f32(sphgb_ctx *ctx, const float *xb, uint32_t nb);
+int sphgb_upload_fluid(sphgb_ctx *ctx, const double *x, const double *v, const uint32_t *id, uint32_t n);
+int sphgb_upload_fluid_f32(sphgb_ctx *ctx, const float *x, const float *v, const uint32_t *id, uint32_t n);
+
+/* time step size (TimeManager::get/setTimeStepSize) and time */
+int sphgb_set_time_step(sphgb_ctx *ctx, double dt);
+int sphgb_get_time_step(const sphgb_ctx *ctx, double *dt);
+int sphgb_set_time(sphgb_ctx *ctx, double t);
+
+/* one TimeStepDFSPH::step(); stats may be NULL (then the call does not wait for the GPU) */
+int sphgb_step(sphgb_ctx *ctx, sphgb_stats *stats);
+/* blocks until the last step finished and fills stats */
+int sphgb_sync(sphgb_ctx *ctx, sphgb_stats *stats);
+
+/* field transfer in particle-id order (the host std::vector order); count = n (or nb for the
+ * boundary fields) x components */
+int sphgb_download(sphgb_ctx *ctx, int field, void *dst, int dtype);
+int sphgb_upload_field(sphgb_ctx *ctx, int field, const void *src, int dtype);
+
+/* neighbour lists of the last step in particle-id order, CSR: offsets[n+1], indices are particle
+ * ids.  kind 0 = fluid-fluid, 1 = fluid-boundary (boundary indices in upload order).  Pass
+ * indices == NULL to query offsets only. */
+int sphgb_neighbors(sphgb_ctx *ctx, int kind, uint32_t *offsets, uint32_t *indices, size_t capacity);
+
+/* counts */
+int sphgb_num_particles(const sphgb_ctx *ctx, uint32_t *n, uint32_t *nb);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1016 @@
+// C-ABI entry points (include/sphgb300.h) and the host orchestration of one
+// TimeStepDFSPH::step() (SPlisHSPlasH/DFSPH/TimeStepDFSPH.cpp:117-249) on the GPU.
+//
+// The step is a fixed sequence of kernel launches on one stream.  Solver loops
+// (divergence, pressure, viscosity CG) decide on the device whether to continue;
+// the host either reads that decision after each iteration (use_graph = 0) or
+// the whole step is captured once into a CUDA graph whose loops are conditional
+// WHILE nodes driven by the kernels (use_graph = 1), so a step is one graph
+// launch with no host round trip.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/sphgb300.h"
+#include "sph_ctx.h"
+
+using namespace sphgb;
+
+struct sphgb_ctx {
+    sphgb_config cfg{};
+    sphgb_params prm{};
+    cudaStream_t stream = nullptr;
+    cudaStream_t body_stream = nullptr;
+    std::string err;
+    bool fp64 = false;
+    uint32_t n = 0, nb = 0;
+    // host-side extents of the uploaded data
+    double fmin[3] = {0, 0, 0}, fmax[3] = {0, 0, 0}, bmin[3] = {0, 0, 0}, bmax[3] = {0, 0, 0};
+    bool have_fluid = false, have_boundary = false, prepared = false;
+    // grid
+    double org[3] = {0, 0, 0}, cell = 0;
+    int dim[3] = {0, 0, 0};
+    int key_bits = 0;
+    size_t ncell = 0;
+    // allocations
+    std::vector<void *> allocs;
+    void *set_x[2] = {}, *set_v[2] = {}, *set_vdiff[2] = {}, *set_kappa[2] = {}, *set_kappa_v[2] = {};
+    float4 *set_xlo[2] = {};
+    uint32_t *set_id[2] = {};
+    void *a = nullptr, *pa = nullptr, *density = nullptr, *factor = nullptr, *dadv = nullptr;
+    uint32_t *nfc = nullptr, *nbc = nullptr, *lf = nullptr, *lb = nullptr;
+    uint32_t *key = nullptr, *key2 = nullptr, *perm = nullptr, *perm2 = nullptr, *cell0 = nullptr, *cell1 = nullptr;
+    uint32_t *cstart = nullptr, *cend = nullptr, *bcstart = nullptr, *bcend = nullptr;
+    void *xb = nullptr, *xb_raw = nullptr, *bscratch = nullptr;
+    uint32_t *bid = nullptr;
+    void *cg[5] = {}, *inv[3] = {};
+    double *partials = nullptr;
+    unsigned *counter = nullptr;
+    StepScalars *sc = nullptr;
+    StepScalars *hsc = nullptr;   // pinned mirror
+    uint32_t *hist = nullptr;
+    uint32_t *inv_perm = nullptr;
+    void *staging = nullptr;
+    size_t staging_bytes = 0;
+    int parity = 0;
+    bool scalars_dirty = true;    // host dt/time changed since the last upload of scalars
+    double dt = 0.001, time = 0.0;
+    // graphs (one per parity)
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    bool graph_ok = false;
+    bool step_pending = false;
+};
+
+namespace {
+
+const sphgb_params kDefaults = {
+    0.025, 1000.0, {0.0, -9.81, 0.0}, 1, 0.5, 1e-4, 5e-3, 2, 100, 0.01, 1, 100, 0.1, 0.0, 0.0, 0, 0.01, 0.0, 100, 0.01,
+};
+
+int fail(sphgb_ctx *c, int code, const std::string &msg)
+{
+    if (c) c->err = msg;
+    return code;
+}
+
+#define CK(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return fail(c, SPHGB_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));   \
+    } while (0)
+
+template <class P> int dalloc(sphgb_ctx *c, P **p, size_t bytes)
+{
+    void *q = nullptr;
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(&q, bytes);
+    if (e != cudaSuccess) return fail(c, SPHGB_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    c->allocs.push_back(q);
+    *p = static_cast<P *>(q);
+    return SPHGB_OK;
+}
+
+void free_all(sphgb_ctx *c)
+{
+    for (void *p : c->allocs) cudaFree(p);
+    c->allocs.clear();
+    for (int k = 0; k < 2; k++)
+        if (c->exec[k]) { cudaGraphExecDestroy(c->exec[k]); c->exec[k] = nullptr; }
+    c->graph_ok = false;
+}
+
+void invalidate_graphs(sphgb_ctx *c)
+{
+    for (int k = 0; k < 2; k++)
+        if (c->exec[k]) { cudaGraphExecDestroy(c->exec[k]); c->exec[k] = nullptr; }
+    c->graph_ok = false;
+}
+
+size_t real_size(const sphgb_ctx *c) { return c->fp64 ? sizeof(double) : sizeof(float); }
+size_t vec_size(const sphgb_ctx *c) { return c->fp64 ? sizeof(dquad) : sizeof(float4); }
+
+template <class T> DevParams<T> make_params(const sphgb_ctx *c)
+{
+    DevParams<T> P{};
+    const sphgb_params &q = c->prm;
+    const double h = 4.0 * q.particle_radius;
+    P.K.h = (T)h;
+    P.K.invh = (T)(1.0 / h);
+    P.K.invh2 = (T)(1.0 / (h * h));
+    P.K.k = (T)(8.0 / (M_PI * h * h * h));
+    P.K.l = (T)(48.0 / (M_PI * h * h * h));
+    P.K.w0 = P.K.k;
+    P.K.h2 = (T)(h * h);
+    const double d = 2.0 * q.particle_radius;
+    const double V = 0.8 * d * d * d;
+    P.V = (T)V;
+    P.mass = (T)(V * q.density0);
+    P.rho0 = (T)q.density0;
+    P.eps = (T)1.0e-5;
+    P.gx = (T)q.gravity[0];
+    P.gy = (T)q.gravity[1];
+    P.gz = (T)q.gravity[2];
+    P.xsph = (T)q.xsph;
+    P.xsph_b = (T)q.xsph_boundary;
+    P.mu = (T)(q.viscosity * q.density0);
+    P.mub = (T)(q.viscosity_boundary * q.density0);
+    P.vd = (T)10.0;
+    P.h2 = (T)(h * h);
+    P.max_error = q.max_error;
+    P.max_error_v = q.max_error_v;
+    P.cfl_factor = q.cfl_factor;
+    P.cfl_min = q.cfl_min_time_step;
+    P.cfl_max = q.cfl_max_time_step;
+    P.radius = q.particle_radius;
+    P.visc_tol = q.visco_max_error;
+    P.min_iter = q.min_iterations;
+    P.max_iter = q.max_iterations;
+    P.max_iter_v = q.max_iterations_v;
+    P.visc_max_iter = q.visco_max_iter;
+    P.cfl_method = q.cfl_method;
+    P.visc_on = q.viscosity_method == 6 ? 1 : 0;
+    P.div_on = q.enable_divergence_solver ? 1 : 0;
+    P.ox = (T)c->org[0];
+    P.oy = (T)c->org[1];
+    P.oz = (T)c->org[2];
+    P.inv_cell = (T)(1.0 / c->cell);
+    P.dimx = c->dim[0];
+    P.dimy = c->dim[1];
+    P.dimz = c->dim[2];
+    P.n = c->n;
+    P.nb = c->nb;
+    P.capf = c->cfg.max_fluid_neighbors;
+    P.capb = c->cfg.max_boundary_neighbors;
+    return P;
+}
+
+// view 0: x = state set of the previous step (sort source), x2 = gather target
+// view 1: x = the gathered set (working set of this step)
+template <class T> DevBufs<T> make_bufs(const sphgb_ctx *c, int view)
+{
+    using v4 = v4_t<T>;
+    DevBufs<T> B{};
+    const int cur = view == 0 ? c->parity : 1 - c->parity;
+    const int alt = 1 - cur;
+    B.x = (v4 *)c->set_x[cur];
+    B.v = (v4 *)c->set_v[cur];
+    B.vdiff = (v4 *)c->set_vdiff[cur];
+    B.xlo = c->set_xlo[cur];
+    B.kappa = (T *)c->set_kappa[cur];
+    B.kappa_v = (T *)c->set_kappa_v[cur];
+    B.id = c->set_id[cur];
+    B.x2 = (v4 *)c->set_x[alt];
+    B.v2 = (v4 *)c->set_v[alt];
+    B.vdiff2 = (v4 *)c->set_vdiff[alt];
+    B.xlo2 = c->set_xlo[alt];
+    B.kappa2 = (T *)c->set_kappa[alt];
+    B.kappa_v2 = (T *)c->set_kappa_v[alt];
+    B.id2 = c->set_id[alt];
+    B.a = (v4 *)c->a;
+    B.pa = (v4 *)c->pa;
+    B.density = (T *)c->density;
+    B.factor = (T *)c->factor;
+    B.dadv = (T *)c->dadv;
+    B.nf = c->nfc;
+    B.nbn = c->nbc;
+    B.lf = c->lf;
+    B.lb = c->lb;
+    B.key = c->key;
+    B.key2 = c->key2;
+    B.perm = c->perm;
+    B.perm2 = c->perm2;
+    B.cellid = view == 0 ? c->cell0 : c->cell1;
+    B.cellid2 = c->cell1;
+    B.cstart = c->cstart;
+    B.cend = c->cend;
+    B.bcstart = c->bcstart;
+    B.bcend = c->bcend;
+    B.xb = (v4 *)c->xb;
+    B.bscratch = (T *)c->bscratch;
+    B.bid = c->bid;
+    B.cg_x = (v4 *)c->cg[0];
+    B.cg_r = (v4 *)c->cg[1];
+    B.cg_p = (v4 *)c->cg[2];
+    B.cg_z = (v4 *)c->cg[3];
+    B.cg_t = (v4 *)c->cg[4];
+    B.inv0 = (v4 *)c->inv[0];
+    B.inv1 = (v4 *)c->inv[1];
+    B.inv2 = (v4 *)c->inv[2];
+    B.partials = c->partials;
+    B.counter = c->counter;
+    B.sc = c->sc;
+    B.hist = c->hist;
+    B.num_tiles = (c->n + kSortTile - 1) / kSortTile;
+    return B;
+}
+
+int upload_scalars(sphgb_ctx *c)
+{
+    if (!c->scalars_dirty) return SPHGB_OK;
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(c->hsc, c->sc, sizeof(StepScalars), cudaMemcpyDeviceToHost));
+    c->hsc->dt = c->dt;
+    c->hsc->dt_next = c->dt;
+    c->hsc->time = c->time;
+    CK(cudaMemcpy(c->sc, c->hsc, sizeof(StepScalars), cudaMemcpyHostToDevice));
+    c->scalars_dirty = false;
+    return SPHGB_OK;
+}
+
+// Build the cell grid over the union of fluid and boundary extents, sort the
+// boundary particles into it and compute their Akinci2012 volumes.
+template <class T> int prepare(sphgb_ctx *c)
+{
+    if (!c->have_fluid) return fail(c, SPHGB_ERR_STATE, "no fluid uploaded");
+    const double h = 4.0 * c->prm.particle_radius;
+    // slightly larger than the support radius: keeps |dx| < h => |cell delta| <= 1 under float rounding
+    c->cell = h * 1.001;
+    double lo[3], hi[3];
+    for (int d = 0; d < 3; d++) {
+        lo[d] = c->fmin[d];
+        hi[d] = c->fmax[d];
+        if (c->have_boundary && c->nb > 0) {
+            lo[d] = std::min(lo[d], c->bmin[d]);
+            hi[d] = std::max(hi[d], c->bmax[d]);
+        }
+    }
+    size_t ncell = 1;
+    int maxdim = 1;
+    for (int d = 0; d < 3; d++) {
+        c->org[d] = lo[d] - c->cell;
+        const double ext = hi[d] - c->org[d];
+        c->dim[d] = (int)std::floor(ext / c->cell) + 2;
+        if (c->dim[d] > 1024) return fail(c, SPHGB_ERR_GRID, "scene extent exceeds 1024 cells per axis");
+        maxdim = std::max(maxdim, c->dim[d]);
+        ncell *= (size_t)c->dim[d];
+    }
+    int bits = 1;
+    while ((1 << bits) < maxdim) bits++;
+    c->key_bits = 3 * bits;
+    c->ncell = ncell;
+    int rc;
+    if ((rc = dalloc(c, &c->cstart, ncell * 4))) return rc;
+    if ((rc = dalloc(c, &c->cend, ncell * 4))) return rc;
+    if ((rc = dalloc(c, &c->bcstart, ncell * 4))) return rc;
+    if ((rc = dalloc(c, &c->bcend, ncell * 4))) return rc;
+    CK(cudaMemsetAsync(c->bcstart, 0xff, ncell * 4, c->stream));
+    const uint32_t nb = c->nb;
+    if ((rc = dalloc(c, &c->xb, (size_t)std::max(nb, 1u) * vec_size(c)))) return rc;
+    if ((rc = dalloc(c, &c->bid, (size_t)std::max(nb, 1u) * 4))) return rc;
+    if ((rc = dalloc(c, &c->bscratch, (size_t)std::max(nb, 1u) * real_size(c)))) return rc;
+    if (nb > 0) {
+        DevParams<T> P = make_params<T>(c);
+        DevBufs<T> B = make_bufs<T>(c, 1);
+        // sort boundary by cell Morton code; reuse fluid sort scratch sized for max(n, nb)
+        uint32_t *k1, *k2, *v1, *v2, *cells, *hist;
+        if ((rc = dalloc(c, &k1, (size_t)nb * 4))) return rc;
+        if ((rc = dalloc(c, &k2, (size_t)nb * 4))) return rc;
+        if ((rc = dalloc(c, &v1, (size_t)nb * 4))) return rc;
+        if ((rc = dalloc(c, &v2, (size_t)nb * 4))) return rc;
+        if ((rc = dalloc(c, &cells, (size_t)nb * 4))) return rc;
+        const uint32_t tiles = (nb + kSortTile - 1) / kSortTile;
+        if ((rc = dalloc(c, &hist, (size_t)tiles * 256 * 4))) return rc;
+        launch_boundary_keys<T>(P, B, (const v4_t<T> *)c->xb_raw, k1, v1, c->stream);
+        const bool sw = radix_sort_pairs(k1, v1, k2, v2, nb, c->key_bits, hist, tiles, c->stream);
+        launch_boundary_gather<T>(P, B, (const v4_t<T> *)c->xb_raw, sw ? v2 : v1, cells, c->stream);
+        launch_boundary_volume<T>(P, B, c->stream);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    c->prepared = true;
+    return SPHGB_OK;
+}
+
+template <class T> void enqueue_solver_loop_body(sphgb_ctx *c, const DevParams<T> &P, const DevBufs<T> &B, bool div,
+                                                 cudaGraphConditionalHandle h, bool use_handle, cudaStream_t s)
+{
+    launch_pressure_accel<T>(P, B, div, s);
+    launch_jacobi<T>(P, B, div, h, use_handle, s);
+}
+
+int read_cont(sphgb_ctx *c, unsigned *cont)
+{
+    CK(cudaMemcpyAsync(&c->hsc->cont, &c->sc->cont, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    *cont = c->hsc->cont;
+    return SPHGB_OK;
+}
+
+// Enqueue the launches that precede / follow the solver loops.
+template <class T> void enqueue_prologue(sphgb_ctx *c, const DevParams<T> &P, const DevBufs<T> &B0, const DevBufs<T> &B1,
+                                         cudaStream_t s)
+{
+    launch_step_begin<T>(P, B1, s);
+    launch_keys<T>(P, B0, s);
+    const uint32_t tiles = (c->n + kSortTile - 1) / kSortTile;
+    const bool sw = radix_sort_pairs(c->key, c->perm, c->key2, c->perm2, c->n, c->key_bits, c->hist, tiles, s);
+    launch_gather<T>(P, B0, sw ? c->perm2 : c->perm, s);
+    cudaMemsetAsync(c->cstart, 0xff, c->ncell * 4, s);
+    launch_cell_ranges<T>(P, B1, s);
+    launch_build<T>(P, B1, s);
+}
+
+template <class T> int step_host_loop(sphgb_ctx *c)
+{
+    const DevParams<T> P = make_params<T>(c);
+    const DevBufs<T> B0 = make_bufs<T>(c, 0);
+    const DevBufs<T> B1 = make_bufs<T>(c, 1);
+    cudaStream_t s = c->stream;
+    int rc;
+    unsigned cont = 0;
+    enqueue_prologue<T>(c, P, B0, B1, s);
+    if (P.div_on) {
+        launch_loop_begin<T>(P, B1, true, s);
+        if (P.max_iter_v > 0) {
+            do {
+                enqueue_solver_loop_body<T>(c, P, B1, true, 0, false, s);
+                if ((rc = read_cont(c, &cont))) return rc;
+            } while (cont);
+        }
+        launch_solver_finalize<T>(P, B1, true, s);
+    }
+    launch_xsph<T>(P, B1, s);
+    if (P.visc_on) {
+        launch_visc_setup<T>(P, B1, 0, false, s);
+        if ((rc = read_cont(c, &cont))) return rc;
+        while (cont) {
+            launch_cg_matvec<T>(P, B1, s);
+            launch_cg_update<T>(P, B1, 0, false, s);
+            if ((rc = read_cont(c, &cont))) return rc;
+            if (!cont) break;
+            launch_cg_p<T>(P, B1, s);
+        }
+    }
+    launch_kick<T>(P, B1, s);
+    launch_press_init<T>(P, B1, s);
+    launch_loop_begin<T>(P, B1, false, s);
+    if (P.max_iter > 0) {
+        do {
+            enqueue_solver_loop_body<T>(c, P, B1, false, 0, false, s);
+            if ((rc = read_cont(c, &cont))) return rc;
+        } while (cont);
+    }
+    launch_solver_finalize<T>(P, B1, false, s);
+    launch_integrate<T>(P, B1, s);
+    CK(cudaGetLastError());
+    return SPHGB_OK;
+}
+
+// --- graph capture with conditional WHILE nodes ----------------------------
+// Adds a WHILE node after the current capture tail of c->stream and captures
+// body(stream) into it on the body stream.  default_value is the condition
+// value on entry (the kernels before the loop may also set it).
+template <class F>
+cudaError_t add_while(sphgb_ctx *c, cudaGraphConditionalHandle *handle_out, unsigned default_value, F body)
+{
+    cudaStreamCaptureStatus st;
+    cudaGraph_t g;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t ndeps = 0;
+    cudaError_t e = cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &g, &deps, nullptr, &ndeps);
+    if (e != cudaSuccess) return e;
+    cudaGraphConditionalHandle h;
+    e = cudaGraphConditionalHandleCreate(&h, g, default_value, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) return e;
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    e = cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &np);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    if (e != cudaSuccess) return e;
+    cudaGraph_t bodyg = np.conditional.phGraph_out[0];
+    e = cudaStreamBeginCaptureToGraph(c->body_stream, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) return e;
+    body(c->body_stream, h);
+    e = cudaStreamEndCapture(c->body_stream, &bodyg);
+    *handle_out = h;
+    return e;
+}
+
+}  // namespace
+
+// The viscosity set-up kernel must set the CG loop's condition, so the graph is
+// built in one capture where the handle exists before the set-up launch.  This
+// helper does the whole capture (prologue, loops, epilogue) for one parity.
+namespace {
+template <class T> int build_graph(sphgb_ctx *c, int parity, cudaGraphExec_t *out)
+{
+    const int saved = c->parity;
+    c->parity = parity;
+    const DevParams<T> P = make_params<T>(c);
+    const DevBufs<T> B0 = make_bufs<T>(c, 0);
+    const DevBufs<T> B1 = make_bufs<T>(c, 1);
+    c->parity = saved;
+    cudaStream_t s = c->stream;
+    cudaGraph_t graph = nullptr;
+    CK(cudaGraphCreate(&graph, 0));
+    cudaError_t e = cudaStreamBeginCaptureToGraph(s, graph, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) { cudaGraphDestroy(graph); return fail(c, SPHGB_ERR_CUDA, cudaGetErrorString(e)); }
+    enqueue_prologue<T>(c, P, B0, B1, s);
+    cudaGraphConditionalHandle h = 0;
+    if (P.div_on) {
+        launch_loop_begin<T>(P, B1, true, s);
+        if (e == cudaSuccess)
+            e = add_while(c, &h, P.max_iter_v > 0 ? 1u : 0u, [&](cudaStream_t bs, cudaGraphConditionalHandle hh) {
+                enqueue_solver_loop_body<T>(c, P, B1, true, hh, true, bs);
+            });
+        launch_solver_finalize<T>(P, B1, true, s);
+    }
+    launch_xsph<T>(P, B1, s);
+    if (P.visc_on && e == cudaSuccess) {
+        // create the CG handle first so that the set-up kernel can set it
+        cudaStreamCaptureStatus st;
+        cudaGraph_t g;
+        const cudaGraphNode_t *deps = nullptr;
+        size_t ndeps = 0;
+        e = cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &ndeps);
+        cudaGraphConditionalHandle hcg = 0;
+        if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hcg, g, 0u, 0);
+        if (e == cudaSuccess) {
+            launch_visc_setup<T>(P, B1, hcg, true, s);
+            e = cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &ndeps);
+        }
+        if (e == cudaSuccess) {
+            cudaGraphNodeParams np{};
+            np.type = cudaGraphNodeTypeConditional;
+            np.conditional.handle = hcg;
+            np.conditional.type = cudaGraphCondTypeWhile;
+            np.conditional.size = 1;
+            cudaGraphNode_t node;
+            e = cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &np);
+            if (e == cudaSuccess)
+                e = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+            if (e == cudaSuccess) {
+                cudaGraph_t bodyg = np.conditional.phGraph_out[0];
+                e = cudaStreamBeginCaptureToGraph(c->body_stream, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+                if (e == cudaSuccess) {
+                    launch_cg_matvec<T>(P, B1, c->body_stream);
+                    launch_cg_update<T>(P, B1, hcg, true, c->body_stream);
+                    launch_cg_p<T>(P, B1, c->body_stream);
+                    e = cudaStreamEndCapture(c->body_stream, &bodyg);
+                }
+            }
+        }
+    }
+    launch_kick<T>(P, B1, s);
+    launch_press_init<T>(P, B1, s);
+    launch_loop_begin<T>(P, B1, false, s);
+    if (e == cudaSuccess)
+        e = add_while(c, &h, P.max_iter > 0 ? 1u : 0u, [&](cudaStream_t bs, cudaGraphConditionalHandle hh) {
+            enqueue_solver_loop_body<T>(c, P, B1, false, hh, true, bs);
+        });
+    launch_solver_finalize<T>(P, B1, false, s);
+    launch_integrate<T>(P, B1, s);
+    cudaGraph_t done = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(s, &done);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaGraphInstantiate(out, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(c, SPHGB_ERR_CUDA, std::string("graph build: ") + cudaGetErrorString(e));
+    }
+    return SPHGB_OK;
+}
+}  // namespace
+
+namespace {
+
+template <class T> int do_step(sphgb_ctx *c)
+{
+    int rc;
+    if (!c->prepared && (rc = prepare<T>(c))) return rc;
+    if ((rc = upload_scalars(c))) return rc;
+    if (c->cfg.use_graph) {
+        if (!c->graph_ok) {
+            invalidate_graphs(c);
+            if ((rc = build_graph<T>(c, 0, &c->exec[0]))) return rc;
+            if ((rc = build_graph<T>(c, 1, &c->exec[1]))) return rc;
+            c->graph_ok = true;
+        }
+        CK(cudaGraphLaunch(c->exec[c->parity], c->stream));
+    } else {
+        if ((rc = step_host_loop<T>(c))) return rc;
+    }
+    c->parity = 1 - c->parity;
+    CK(cudaMemcpyAsync(c->hsc, c->sc, sizeof(StepScalars), cudaMemcpyDeviceToHost, c->stream));
+    c->step_pending = true;
+    return SPHGB_OK;
+}
+
+int fill_stats(sphgb_ctx *c, sphgb_stats *st)
+{
+    CK(cudaStreamSynchronize(c->stream));
+    const StepScalars &h = *c->hsc;
+    if (c->step_pending) {
+        c->dt = h.dt;
+        c->time = h.time;
+        c->step_pending = false;
+    }
+    if (st) {
+        st->iterations = h.iters;
+        st->iterations_v = h.iters_v;
+        st->visco_iterations = c->prm.viscosity_method == 6 ? h.iters_cg : 0;
+        st->max_fluid_neighbors = h.max_nf;
+        st->max_boundary_neighbors = h.max_nb;
+        st->flags = h.flags;
+        st->avg_density_err = h.avg_err;
+        st->avg_density_err_v = h.avg_err_v;
+        st->visco_error = c->prm.viscosity_method == 6 ? h.cg_err : 0.0;
+        st->dt_used = h.dt_used;
+        st->dt_next = h.dt_next;
+        st->time = h.time;
+    }
+    if (h.flags & kFlagOverflow)
+        return fail(c, SPHGB_ERR_CAPACITY, "neighbour list capacity exceeded (raise max_fluid/boundary_neighbors)");
+    if (h.flags & kFlagNonFinite) return fail(c, SPHGB_ERR_NONFINITE, "non-finite velocity");
+    return SPHGB_OK;
+}
+
+template <class T> int init_fluid(sphgb_ctx *c, const double *x, const double *v, const uint32_t *id, uint32_t n)
+{
+    int rc;
+    // (re)allocate every per-particle buffer
+    free_all(c);
+    c->prepared = false;
+    c->n = n;
+    const size_t N = std::max<uint32_t>(n, 1);
+    const size_t vs = vec_size(c), rs = real_size(c);
+    for (int k = 0; k < 2; k++) {
+        if ((rc = dalloc(c, &c->set_x[k], N * vs))) return rc;
+        if ((rc = dalloc(c, &c->set_v[k], N * vs))) return rc;
+        if ((rc = dalloc(c, &c->set_vdiff[k], N * vs))) return rc;
+        if ((rc = dalloc(c, &c->set_kappa[k], N * rs))) return rc;
+        if ((rc = dalloc(c, &c->set_kappa_v[k], N * rs))) return rc;
+        if ((rc = dalloc(c, &c->set_id[k], N * 4))) return rc;
+        c->set_xlo[k] = nullptr;
+        if (!c->fp64 && (rc = dalloc(c, &c->set_xlo[k], N * sizeof(float4)))) return rc;
+    }
+    if ((rc = dalloc(c, &c->a, N * vs))) return rc;
+    if ((rc = dalloc(c, &c->pa, N * vs))) return rc;
+    if ((rc = dalloc(c, &c->density, N * rs))) return rc;
+    if ((rc = dalloc(c, &c->factor, N * rs))) return rc;
+    if ((rc = dalloc(c, &c->dadv, N * rs))) return rc;
+    if ((rc = dalloc(c, &c->nfc, N * 4))) return rc;
+    if ((rc = dalloc(c, &c->nbc, N * 4))) return rc;
+    const size_t NW = (N + 31) / 32 * 32;
+    if ((rc = dalloc(c, &c->lf, NW * c->cfg.max_fluid_neighbors * 4))) return rc;
+    if ((rc = dalloc(c, &c->lb, NW * c->cfg.max_boundary_neighbors * 4))) return rc;
+    if ((rc = dalloc(c, &c->key, N * 4))) return rc;
+    if ((rc = dalloc(c, &c->key2, N * 4))) return rc;
+    if ((rc = dalloc(c, &c->perm, N * 4))) return rc;
+    if ((rc = dalloc(c, &c->perm2, N * 4))) return rc;
+    if ((rc = dalloc(c, &c->cell0, N * 4))) return rc;
+    if ((rc = dalloc(c, &c->cell1, N * 4))) return rc;
+    for (int k = 0; k < 5; k++)
+        if ((rc = dalloc(c, &c->cg[k], N * vs))) return rc;
+    for (int k = 0; k < 3; k++)
+        if ((rc = dalloc(c, &c->inv[k], N * vs))) return rc;
+    const size_t blocks = (N + kBlock - 1) / kBlock;
+    if ((rc = dalloc(c, &c->partials, blocks * 4 * sizeof(double)))) return rc;
+    if ((rc = dalloc(c, &c->counter, 64))) return rc;
+    CK(cudaMemset(c->counter, 0, 64));
+    if ((rc = dalloc(c, &c->sc, sizeof(StepScalars)))) return rc;
+    CK(cudaMemset(c->sc, 0, sizeof(StepScalars)));
+    const size_t tiles = (N + kSortTile - 1) / kSortTile;
+    if ((rc = dalloc(c, &c->hist, tiles * 256 * 4))) return rc;
+    if ((rc = dalloc(c, &c->inv_perm, N * 4))) return rc;
+    // zero per-step fields so that downloads before the first step are defined
+    CK(cudaMemset(c->a, 0, N * vs));
+    CK(cudaMemset(c->pa, 0, N * vs));
+    CK(cudaMemset(c->density, 0, N * rs));
+    CK(cudaMemset(c->factor, 0, N * rs));
+    CK(cudaMemset(c->dadv, 0, N * rs));
+    CK(cudaMemset(c->nfc, 0, N * 4));
+    CK(cudaMemset(c->nbc, 0, N * 4));
+    // staging copy of x/v (double) and ids
+    double *dx, *dv;
+    uint32_t *did = nullptr;
+    if ((rc = dalloc(c, &dx, N * 3 * sizeof(double)))) return rc;
+    if ((rc = dalloc(c, &dv, N * 3 * sizeof(double)))) return rc;
+    if (n) {
+        CK(cudaMemcpy(dx, x, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(dv, v, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    if (id) {
+        if ((rc = dalloc(c, &did, N * 4))) return rc;
+        CK(cudaMemcpy(did, id, (size_t)n * 4, cudaMemcpyHostToDevice));
+    }
+    c->parity = 0;
+    DevParams<T> P = make_params<T>(c);
+    DevBufs<T> B = make_bufs<T>(c, 0);
+    launch_init_state<T>(P, B, dx, dv, did, c->stream);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->stream));
+    // extents
+    for (int d = 0; d < 3; d++) {
+        c->fmin[d] = n ? x[d] : 0.0;
+        c->fmax[d] = n ? x[d] : 0.0;
+    }
+    for (uint32_t i = 1; i < n; i++)
+        for (int d = 0; d < 3; d++) {
+            c->fmin[d] = std::min(c->fmin[d], x[3 * (size_t)i + d]);
+            c->fmax[d] = std::max(c->fmax[d], x[3 * (size_t)i + d]);
+        }
+    c->have_fluid = true;
+    c->scalars_dirty = true;
+    return SPHGB_OK;
+}
+
+template <class T> int init_boundary(sphgb_ctx *c, const double *xb, uint32_t nb)
+{
+    int rc;
+    c->nb = nb;
+    std::vector<char> host((size_t)std::max<uint32_t>(nb, 1) * vec_size(c));
+    for (uint32_t i = 0; i < nb; i++) {
+        if (c->fp64) {
+            dquad q{xb[3 * (size_t)i], xb[3 * (size_t)i + 1], xb[3 * (size_t)i + 2], 0.0};
+            std::memcpy(host.data() + (size_t)i * sizeof(dquad), &q, sizeof(q));
+        } else {
+            float4 q = make_float4((float)xb[3 * (size_t)i], (float)xb[3 * (size_t)i + 1], (float)xb[3 * (size_t)i + 2], 0.f);
+            std::memcpy(host.data() + (size_t)i * sizeof(float4), &q, sizeof(q));
+        }
+    }
+    if ((rc = dalloc(c, &c->xb_raw, host.size()))) return rc;
+    CK(cudaMemcpy(c->xb_raw, host.data(), host.size(), cudaMemcpyHostToDevice));
+    for (int d = 0; d < 3; d++) {
+        c->bmin[d] = nb ? xb[d] : 0.0;
+        c->bmax[d] = nb ? xb[d] : 0.0;
+    }
+    for (uint32_t i = 1; i < nb; i++)
+        for (int d = 0; d < 3; d++) {
+            c->bmin[d] = std::min(c->bmin[d], xb[3 * (size_t)i + d]);
+            c->bmax[d] = std::max(c->bmax[d], xb[3 * (size_t)i + d]);
+        }
+    c->have_boundary = true;
+    c->prepared = false;
+    invalidate_graphs(c);
+    return SPHGB_OK;
+}
+
+int ensure_staging(sphgb_ctx *c, size_t bytes)
+{
+    if (c->staging_bytes >= bytes) return SPHGB_OK;
+    int rc = dalloc(c, &c->staging, bytes);
+    if (rc) return rc;
+    c->staging_bytes = bytes;
+    return SPHGB_OK;
+}
+
+int field_components(int field)
+{
+    switch (field) {
+    case SPHGB_FIELD_POSITION: case SPHGB_FIELD_VELOCITY: case SPHGB_FIELD_ACCELERATION:
+    case SPHGB_FIELD_PRESSURE_ACCEL: case SPHGB_FIELD_VDIFF: case SPHGB_FIELD_BOUNDARY_POSITION:
+        return 3;
+    default:
+        return 1;
+    }
+}
+
+size_t dtype_size(int dt) { return dt == SPHGB_DTYPE_F64 ? 8 : 4; }
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+int sphgb_abi_version(void) { return SPHGB_ABI_VERSION; }
+
+int sphgb_default_params(sphgb_params *p)
+{
+    if (!p) return SPHGB_ERR_ARGUMENT;
+    *p = kDefaults;
+    return SPHGB_OK;
+}
+
+int sphgb_create(const sphgb_config *cfg, sphgb_ctx **out)
+{
+    if (!cfg || !out) return SPHGB_ERR_ARGUMENT;
+    if (cfg->abi_version != SPHGB_ABI_VERSION) return SPHGB_ERR_ARGUMENT;
+    if (cfg->precision != SPHGB_PRECISION_FP32 && cfg->precision != SPHGB_PRECISION_FP64) return SPHGB_ERR_ARGUMENT;
+    sphgb_ctx *c = new sphgb_ctx();
+    c->cfg = *cfg;
+    if (c->cfg.max_fluid_neighbors == 0) c->cfg.max_fluid_neighbors = 80;
+    if (c->cfg.max_boundary_neighbors == 0) c->cfg.max_boundary_neighbors = 128;
+    c->fp64 = cfg->precision == SPHGB_PRECISION_FP64;
+    c->prm = kDefaults;
+    cudaError_t e = cudaSetDevice(cfg->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->body_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMallocHost(&c->hsc, sizeof(StepScalars));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        delete c;
+        return SPHGB_ERR_CUDA;
+    }
+    std::memset(c->hsc, 0, sizeof(StepScalars));
+    *out = c;
+    return SPHGB_OK;
+}
+
+int sphgb_destroy(sphgb_ctx *c)
+{
+    if (!c) return SPHGB_ERR_ARGUMENT;
+    cudaSetDevice(c->cfg.device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    free_all(c);
+    if (c->hsc) cudaFreeHost(c->hsc);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->body_stream) cudaStreamDestroy(c->body_stream);
+    delete c;
+    return SPHGB_OK;
+}
+
+const char *sphgb_last_error(const sphgb_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+int sphgb_set_params(sphgb_ctx *c, const sphgb_params *p)
+{
+    if (!c || !p) return SPHGB_ERR_ARGUMENT;
+    if (!(p->particle_radius > 0) || !(p->density0 > 0)) return fail(c, SPHGB_ERR_ARGUMENT, "radius/density0 must be > 0");
+    if (p->viscosity_method != 0 && p->viscosity_method != 6)
+        return fail(c, SPHGB_ERR_ARGUMENT, "viscosity_method must be 0 (none) or 6 (Weiler et al. 2018)");
+    if (p->cfl_method < 0 || p->cfl_method > 2) return fail(c, SPHGB_ERR_ARGUMENT, "cfl_method must be 0, 1 or 2");
+    const bool radius_changed = c->prm.particle_radius != p->particle_radius;
+    c->prm = *p;
+    invalidate_graphs(c);
+    if (radius_changed && c->prepared) {
+        // the cell grid and boundary volumes depend on the support radius
+        c->prepared = false;
+    }
+    return SPHGB_OK;
+}
+
+int sphgb_get_params(const sphgb_ctx *c, sphgb_params *p)
+{
+    if (!c || !p) return SPHGB_ERR_ARGUMENT;
+    *p = c->prm;
+    return SPHGB_OK;
+}
+
+int sphgb_upload_boundary(sphgb_ctx *c, const double *xb, uint32_t nb)
+{
+    if (!c || (!xb && nb)) return SPHGB_ERR_ARGUMENT;
+    cudaSetDevice(c->cfg.device);
+    return c->fp64 ? init_boundary<double>(c, xb, nb) : init_boundary<float>(c, xb, nb);
+}
+
+int sphgb_upload_boundary_f32(sphgb_ctx *c, const float *xb, uint32_t nb)
+{
+    if (!c || (!xb && nb)) return SPHGB_ERR_ARGUMENT;
+    std::vector<double> d((size_t)nb * 3);
+    for (size_t k = 0; k < d.size(); k++) d[k] = xb[k];
+    return sphgb_upload_boundary(c, d.data(), nb);
+}
+
+int sphgb_upload_fluid(sphgb_ctx *c, const double *x, const double *v, const uint32_t *id, uint32_t n)
+{
+    if (!c || (n && (!x || !v))) return SPHGB_ERR_ARGUMENT;
+    cudaSetDevice(c->cfg.device);
+    // keep the staged boundary across the re-allocation of the fluid buffers
+    std::vector<double> xb;
+    uint32_t nb = 0;
+    if (c->have_boundary && c->nb) {
+        nb = c->nb;
+        xb.resize((size_t)nb * 3);
+        if (c->fp64) {
+            std::vector<dquad> t(nb);
+            if (cudaMemcpy(t.data(), c->xb_raw, nb * sizeof(dquad), cudaMemcpyDeviceToHost) != cudaSuccess)
+                return fail(c, SPHGB_ERR_CUDA, "boundary readback");
+            for (uint32_t i = 0; i < nb; i++) { xb[3 * i] = t[i].x; xb[3 * i + 1] = t[i].y; xb[3 * i + 2] = t[i].z; }
+        } else {
+            std::vector<float4> t(nb);
+            if (cudaMemcpy(t.data(), c->xb_raw, nb * sizeof(float4), cudaMemcpyDeviceToHost) != cudaSuccess)
+                return fail(c, SPHGB_ERR_CUDA, "boundary readback");
+            for (uint32_t i = 0; i < nb; i++) { xb[3 * i] = t[i].x; xb[3 * i + 1] = t[i].y; xb[3 * i + 2] = t[i].z; }
+        }
+    }
+    const bool had_boundary = c->have_boundary;
+    int rc = c->fp64 ? init_fluid<double>(c, x, v, id, n) : init_fluid<float>(c, x, v, id, n);
+    if (rc) return rc;
+    if (had_boundary) {
+        rc = c->fp64 ? init_boundary<double>(c, xb.data(), nb) : init_boundary<float>(c, xb.data(), nb);
+        if (rc) return rc;
+    }
+    c->time = 0.0;
+    c->scalars_dirty = true;
+    invalidate_graphs(c);
+    return SPHGB_OK;
+}
+
+int sphgb_upload_fluid_f32(sphgb_ctx *c, const float *x, const float *v, const uint32_t *id, uint32_t n)
+{
+    if (!c || (n && (!x || !v))) return SPHGB_ERR_ARGUMENT;
+    std::vector<double> dx((size_t)n * 3), dv((size_t)n * 3);
+    for (size_t k = 0; k < dx.size(); k++) { dx[k] = x[k]; dv[k] = v[k]; }
+    return sphgb_upload_fluid(c, dx.data(), dv.data(), id, n);
+}
+
+int sphgb_set_time_step(sphgb_ctx *c, double dt)
+{
+    if (!c || !(dt > 0)) return SPHGB_ERR_ARGUMENT;
+    sphgb_stats st;
+    if (c->step_pending) fill_stats(c, &st);
+    c->dt = dt;
+    c->scalars_dirty = true;
+    return SPHGB_OK;
+}
+
+int sphgb_get_time_step(const sphgb_ctx *c, double *dt)
+{
+    if (!c || !dt) return SPHGB_ERR_ARGUMENT;
+    if (c->step_pending) {
+        cudaStreamSynchronize(c->stream);
+        *dt = c->hsc->dt;
+    } else {
+        *dt = c->dt;
+    }
+    return SPHGB_OK;
+}
+
+int sphgb_set_time(sphgb_ctx *c, double t)
+{
+    if (!c) return SPHGB_ERR_ARGUMENT;
+    sphgb_stats st;
+    if (c->step_pending) fill_stats(c, &st);
+    c->time = t;
+    c->scalars_dirty = true;
+    return SPHGB_OK;
+}
+
+int sphgb_step(sphgb_ctx *c, sphgb_stats *stats)
+{
+    if (!c) return SPHGB_ERR_ARGUMENT;
+    if (!c->have_fluid) return fail(c, SPHGB_ERR_STATE, "sphgb_step before sphgb_upload_fluid");
+    cudaSetDevice(c->cfg.device);
+    if (c->step_pending && c->scalars_dirty) {
+        sphgb_stats st;
+        fill_stats(c, &st);
+    }
+    int rc = c->fp64 ? do_step<double>(c) : do_step<float>(c);
+    if (rc) return rc;
+    if (stats) return fill_stats(c, stats);
+    return SPHGB_OK;
+}
+
+int sphgb_sync(sphgb_ctx *c, sphgb_stats *stats)
+{
+    if (!c) return SPHGB_ERR_ARGUMENT;
+    return fill_stats(c, stats);
+}
+
+int sphgb_num_particles(const sphgb_ctx *c, uint32_t *n, uint32_t *nb)
+{
+    if (!c) return SPHGB_ERR_ARGUMENT;
+    if (n) *n = c->n;
+    if (nb) *nb = c->nb;
+    return SPHGB_OK;
+}
+
+int sphgb_download(sphgb_ctx *c, int field, void *dst, int dtype)
+{
+    if (!c || !dst) return SPHGB_ERR_ARGUMENT;
+    if (field < 0 || field > SPHGB_FIELD_BOUNDARY_POSITION) return fail(c, SPHGB_ERR_ARGUMENT, "unknown field");
+    if (dtype < SPHGB_DTYPE_F32 || dtype > SPHGB_DTYPE_U32) return fail(c, SPHGB_ERR_ARGUMENT, "unknown dtype");
+    if (!c->have_fluid) return fail(c, SPHGB_ERR_STATE, "no fluid uploaded");
+    cudaSetDevice(c->cfg.device);
+    const bool bfield = field == SPHGB_FIELD_BOUNDARY_VOLUME || field == SPHGB_FIELD_BOUNDARY_POSITION;
+    if (bfield && !c->prepared) {
+        int rc = c->fp64 ? prepare<double>(c) : prepare<float>(c);
+        if (rc) return rc;
+    }
+    const size_t m = bfield ? c->nb : c->n;
+    const size_t bytes = m * field_components(field) * dtype_size(dtype);
+    if (bytes == 0) return SPHGB_OK;
+    int rc = ensure_staging(c, bytes);
+    if (rc) return rc;
+    if (c->fp64) {
+        DevParams<double> P = make_params<double>(c);
+        DevBufs<double> B = make_bufs<double>(c, 0);
+        launch_scatter_field<double>(P, B, field, c->staging, dtype, c->stream);
+    } else {
+        DevParams<float> P = make_params<float>(c);
+        DevBufs<float> B = make_bufs<float>(c, 0);
+        launch_scatter_field<float>(P, B, field, c->staging, dtype, c->stream);
+    }
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(dst, c->staging, bytes, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SPHGB_OK;
+}
+
+int sphgb_upload_field(sphgb_ctx *c, int field, const void *src, int dtype)
+{
+    if (!c || !src) return SPHGB_ERR_ARGUMENT;
+    if (field != SPHGB_FIELD_POSITION && field != SPHGB_FIELD_VELOCITY && field != SPHGB_FIELD_VDIFF &&
+        field != SPHGB_FIELD_PRESSURE_RHO2 && field != SPHGB_FIELD_PRESSURE_RHO2_V)
+        return fail(c, SPHGB_ERR_ARGUMENT, "field is not uploadable");
+    if (dtype != SPHGB_DTYPE_F32 && dtype != SPHGB_DTYPE_F64) return fail(c, SPHGB_ERR_ARGUMENT, "bad dtype");
+    if (!c->have_fluid) return fail(c, SPHGB_ERR_STATE, "no fluid uploaded");
+    cudaSetDevice(c->cfg.device);
+    sphgb_stats st;
+    if (c->step_pending) fill_stats(c, &st);
+    const size_t bytes = (size_t)c->n * field_components(field) * dtype_size(dtype);
+    if (bytes == 0) return SPHGB_OK;
+    int rc = ensure_staging(c, bytes);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(c->staging, src, bytes, cudaMemcpyHostToDevice, c->stream));
+    launch_inverse_perm(c->set_id[c->parity], c->inv_perm, c->n, c->stream);
+    if (c->fp64) {
+        DevParams<double> P = make_params<double>(c);
+        DevBufs<double> B = make_bufs<double>(c, 0);
+        launch_upload_field<double>(P, B, field, c->staging, dtype, c->inv_perm, c->stream);
+    } else {
+        DevParams<float> P = make_params<float>(c);
+        DevBufs<float> B = make_bufs<float>(c, 0);
+        launch_upload_field<float>(P, B, field, c->staging, dtype, c->inv_perm, c->stream);
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->stream));
+    if (field == SPHGB_FIELD_POSITION) {
+        // positions may have moved outside the grid used so far: rebuild it at the next step
+        const double *d = static_cast<const double *>(src);
+        const float *f = static_cast<const float *>(src);
+        for (int k = 0; k < 3; k++) { c->fmin[k] = 1e300; c->fmax[k] = -1e300; }
+        for (uint32_t i = 0; i < c->n; i++)
+            for (int k = 0; k < 3; k++) {
+                const double val = dtype == SPHGB_DTYPE_F64 ? d[3 * (size_t)i + k] : (double)f[3 * (size_t)i + k];
+                c->fmin[k] = std::min(c->fmin[k], val);
+                c->fmax[k] = std::max(c->fmax[k], val);
+            }
+    }
+    return SPHGB_OK;
+}
+
+int sphgb_neighbors(sphgb_ctx *c, int kind, uint32_t *offsets, uint32_t *indices, size_t capacity)
+{
+    if (!c || !offsets || (kind != 0 && kind != 1)) return SPHGB_ERR_ARGUMENT;
+    if (!c->have_fluid) return fail(c, SPHGB_ERR_STATE, "no fluid uploaded");
+    cudaSetDevice(c->cfg.device);
+    sphgb_stats st;
+    if (c->step_pending) fill_stats(c, &st);
+    const uint32_t n = c->n;
+    std::vector<uint32_t> cnt(n);
+    int rc = sphgb_download(c, kind == 0 ? SPHGB_FIELD_NUM_FLUID_NEIGHBORS : SPHGB_FIELD_NUM_BOUNDARY_NEIGHBORS,
+                            cnt.data(), SPHGB_DTYPE_U32);
+    if (rc) return rc;
+    const uint32_t cap = kind == 0 ? c->cfg.max_fluid_neighbors : c->cfg.max_boundary_neighbors;
+    offsets[0] = 0;
+    for (uint32_t i = 0; i < n; i++) offsets[i + 1] = offsets[i] + std::min(cnt[i], cap);
+    if (!indices) return SPHGB_OK;
+    if (capacity < offsets[n]) return fail(c, SPHGB_ERR_CAPACITY, "index buffer too small");
+    // the lists of the last step are indexed by the sorted order of that step,
+    // which is the current state order (parity already flipped to it)
+    uint32_t *doff, *dout;
+    if ((rc = dalloc(c, &doff, ((size_t)n + 1) * 4))) return rc;
+    if ((rc = dalloc(c, &dout, (size_t)std::max<uint32_t>(offsets[n], 1) * 4))) return rc;
+    CK(cudaMemcpy(doff, offsets, ((size_t)n + 1) * 4, cudaMemcpyHostToDevice));
+    const uint32_t *id = c->set_id[c->parity];
+    launch_inverse_perm(id, c->inv_perm, n, c->stream);
+    launch_lists_to_ids(kind == 0 ? c->lf : c->lb, kind == 0 ? c->nfc : c->nbc, cap, id, c->inv_perm, c->bid, kind,
+                        doff, dout, n, c->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(indices, dout, (size_t)offsets[n] * 4, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    // release the temporaries (last two allocations)
+    cudaFree(dout);
+    cudaFree(doff);
+    c->allocs.pop_back();
+    c->allocs.pop_back();
+    return SPHGB_OK;
+}
+
+}  // extern "C"

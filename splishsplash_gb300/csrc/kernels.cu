@@ -1,0 +1,1193 @@
+// sm_103a kernels of the DFSPH time step.  One thread per fluid particle, in
+// the cell-sorted order of the current step.  Neighbour lists are built once per
+// step (fused with densities, the DFSPH factor and the divergence source) and
+// then re-read by every later pass; kernel gradients are recomputed from the
+// positions in each pass (the whole position array stays in L2).
+//
+// Reference restated (SPlisHSPlasH 2.16.0): TimeStep.cpp:35-169,
+// DFSPH/TimeStepDFSPH.cpp:117-706 and the scalar kernels :1106-1420,
+// XSPH.cpp:138-216, Viscosity/Viscosity_Weiler2018.cpp:271-443,605-742,891-1254,
+// Simulation.cpp:395-493, BoundaryModel_Akinci2012.cpp:48-75.
+#include "sph_ctx.h"
+
+#include "../../include/sphgb300.h"
+
+namespace sphgb {
+
+namespace {
+
+inline unsigned grid_for(uint32_t n) { return (n + kBlock - 1) / kBlock; }
+
+// ---- list access --------------------------------------------------------
+__device__ __forceinline__ const uint32_t *list_ptr(const uint32_t *L, uint32_t i, uint32_t cap)
+{
+    return L + (size_t)(i >> 5) * cap * 32u + (i & 31u);
+}
+__device__ __forceinline__ uint32_t *list_ptr(uint32_t *L, uint32_t i, uint32_t cap)
+{
+    return L + (size_t)(i >> 5) * cap * 32u + (i & 31u);
+}
+
+template <class T> struct Pair {
+    V3<T> r;    // xi - xj
+    T rl;       // |r|
+};
+
+template <class T> __device__ __forceinline__ Pair<T> pair_of(const v4_t<T> &xi, const v4_t<T> &xj)
+{
+    T dx, dy, dz;
+    const T d2 = pair_d2(xi, xj, dx, dy, dz);
+    Pair<T> p;
+    p.r = V3<T>{dx, dy, dz};
+    p.rl = dev_sqrt(d2);
+    return p;
+}
+
+template <class T> __device__ __forceinline__ V3<T> gradW(const Kernel<T> &K, const Pair<T> &p)
+{
+    return scl(p.r, kernel_gradW_coef(K, p.rl));
+}
+
+__device__ __forceinline__ void cell_coords(uint32_t c, int dimx, int dimy, int &cx, int &cy, int &cz)
+{
+    cx = (int)(c % (uint32_t)dimx);
+    const uint32_t t = c / (uint32_t)dimx;
+    cy = (int)(t % (uint32_t)dimy);
+    cz = (int)(t / (uint32_t)dimy);
+}
+
+template <class T> __device__ __forceinline__ void cell_of(const DevParams<T> &P, const v4_t<T> &x, int &cx, int &cy, int &cz)
+{
+    cx = (int)floor(((T)x.x - P.ox) * P.inv_cell);
+    cy = (int)floor(((T)x.y - P.oy) * P.inv_cell);
+    cz = (int)floor(((T)x.z - P.oz) * P.inv_cell);
+    cx = min(max(cx, 0), P.dimx - 1);
+    cy = min(max(cy, 0), P.dimy - 1);
+    cz = min(max(cz, 0), P.dimz - 1);
+}
+
+// block-wide max of two counters, one atomic per block
+__device__ __forceinline__ void block_max_atomic(uint32_t a, uint32_t b, unsigned *da, unsigned *db)
+{
+    __shared__ uint32_t sa[32], sb[32];
+    a = __reduce_max_sync(0xffffffffu, a);
+    b = __reduce_max_sync(0xffffffffu, b);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) { sa[warp] = a; sb[warp] = b; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) { a = max(a, sa[w]); b = max(b, sb[w]); }
+        atomicMax(da, a);
+        atomicMax(db, b);
+    }
+}
+
+// ==========================================================================
+// neighbour structure
+// ==========================================================================
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_keys(DevParams<T> P, DevBufs<T> B)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    int cx, cy, cz;
+    const v4_t<T> xi = ldv(B.x, i);
+    cell_of(P, xi, cx, cy, cz);
+    B.key[i] = morton3((uint32_t)cx, (uint32_t)cy, (uint32_t)cz);
+    B.perm[i] = i;
+    B.cellid[i] = ((uint32_t)cz * (uint32_t)P.dimy + (uint32_t)cy) * (uint32_t)P.dimx + (uint32_t)cx;
+}
+
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_gather(DevParams<T> P, DevBufs<T> B, const uint32_t *__restrict__ perm)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= P.n) return;
+    const uint32_t s = perm[k];
+    stv(B.x2, k, ldv(B.x, s));
+    stv(B.v2, k, ldv(B.v, s));
+    stv(B.vdiff2, k, ldv(B.vdiff, s));
+    if (B.xlo) B.xlo2[k] = B.xlo[s];
+    B.kappa2[k] = B.kappa[s];
+    B.kappa_v2[k] = B.kappa_v[s];
+    B.id2[k] = B.id[s];
+    B.cellid2[k] = B.cellid[s];
+}
+
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_cell_ranges(DevParams<T> P, const uint32_t *__restrict__ cellid,
+                                                         uint32_t *__restrict__ cstart, uint32_t *__restrict__ cend, uint32_t n)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t c = cellid[k];
+    if (k == 0 || cellid[k - 1] != c) cstart[c] = k;
+    if (k == n - 1 || cellid[k + 1] != c) cend[c] = k + 1;
+}
+
+// Build the fluid and boundary neighbour lists of particle i and, in the same
+// pass, compute (TimeStep.cpp:116-169) the density, (TimeStepDFSPH.cpp:1106-1186)
+// the DFSPH factor alpha, (TimeStepDFSPH.cpp:1247-1295) the divergence source and
+// (TimeStepDFSPH.cpp:402-463) the warm-started kappa_v.
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_build(DevParams<T> P, DevBufs<T> B)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const v4_t<T> xi = ldv(B.x, i);
+    const V3<T> vi = xyz<T>(ldv(B.v, i));
+    int cx, cy, cz;
+    cell_coords(B.cellid[i], P.dimx, P.dimy, cx, cy, cz);
+
+    uint32_t *Lf = list_ptr(B.lf, i, P.capf);
+    uint32_t *Lb = list_ptr(B.lb, i, P.capb);
+    uint32_t nf = 0, nb = 0;
+    T wf = T(0), wb = T(0), gsq = T(0), divf = T(0), divb = T(0);
+    V3<T> gf = mk3<T>(0, 0, 0), gb = mk3<T>(0, 0, 0);
+
+    for (int dz = -1; dz <= 1; dz++) {
+        const int z = cz + dz;
+        if (z < 0 || z >= P.dimz) continue;
+        for (int dy = -1; dy <= 1; dy++) {
+            const int y = cy + dy;
+            if (y < 0 || y >= P.dimy) continue;
+            for (int dx = -1; dx <= 1; dx++) {
+                const int x = cx + dx;
+                if (x < 0 || x >= P.dimx) continue;
+                const uint32_t c = ((uint32_t)z * (uint32_t)P.dimy + (uint32_t)y) * (uint32_t)P.dimx + (uint32_t)x;
+                // fluid
+                uint32_t s = B.cstart[c];
+                if (s != kEmpty) {
+                    const uint32_t e = B.cend[c];
+                    for (uint32_t j = s; j < e; j++) {
+                        if (j == i) continue;
+                        const v4_t<T> xj = ldv(B.x, j);
+                        T ddx, ddy, ddz;
+                        const T d2 = pair_d2(xi, xj, ddx, ddy, ddz);
+                        if (!(d2 < P.K.h2)) continue;
+                        if (nf < P.capf) Lf[nf * 32u] = j;
+                        nf++;
+                        const T rl = dev_sqrt(d2);
+                        wf += kernel_W(P.K, rl);
+                        const T cg = kernel_gradW_coef(P.K, rl);
+                        const V3<T> g = V3<T>{ddx * cg, ddy * cg, ddz * cg};
+                        gsq += dot(g, g);
+                        gf = add(gf, g);
+                        const V3<T> vj = xyz<T>(ldv(B.v, j));
+                        divf += dot(sub(vi, vj), g);
+                    }
+                }
+                // boundary
+                s = B.bcstart[c];
+                if (s != kEmpty) {
+                    const uint32_t e = B.bcend[c];
+                    for (uint32_t j = s; j < e; j++) {
+                        const v4_t<T> xj = ldv(B.xb, j);
+                        T ddx, ddy, ddz;
+                        const T d2 = pair_d2(xi, xj, ddx, ddy, ddz);
+                        if (!(d2 < P.K.h2)) continue;
+                        if (nb < P.capb) Lb[nb * 32u] = j;
+                        nb++;
+                        const T Vb = (T)xj.w;
+                        const T rl = dev_sqrt(d2);
+                        wb += Vb * kernel_W(P.K, rl);
+                        const T cg = kernel_gradW_coef(P.K, rl);
+                        const V3<T> g = V3<T>{ddx * cg, ddy * cg, ddz * cg};
+                        gb = add(gb, scl(g, Vb));
+                        divb += Vb * dot(vi, g);
+                    }
+                }
+            }
+        }
+    }
+    B.nf[i] = nf;
+    B.nbn[i] = nb;
+    if (nf > P.capf || nb > P.capb) atomicOr(&B.sc->flags, kFlagOverflow);
+    block_max_atomic(nf, nb, &B.sc->max_nf, &B.sc->max_nb);
+
+    // density: rho0 * (V W0 + sum_f V W + sum_b Vb W)
+    B.density[i] = P.rho0 * (P.V * P.K.w0 + P.V * wf + wb);
+    // factor: 1 / (sum_f |V gradW|^2 + |sum_f V gradW + sum_b Vb gradW|^2)
+    const V3<T> gpi = add(scl(gf, P.V), gb);
+    const T sum_grad = P.V * P.V * gsq + dot(gpi, gpi);
+    const T alpha = sum_grad > P.eps ? T(1) / sum_grad : T(0);
+    B.factor[i] = alpha;
+    // divergence source (unclamped, as stored by computeDensityChange) and kappa_v warm start
+    const T dsrc = divf * P.V + divb;
+    B.dadv[i] = dsrc;
+    if (P.div_on) {
+        T densityAdv = dsrc > T(0) ? dsrc : T(0);
+        if (nf + nb < 20u) densityAdv = T(0);
+        const T invH = T(1) / (T)B.sc->dt;
+        const T kv = B.kappa_v[i];
+        B.kappa_v[i] = densityAdv > T(0) ? T(0.5) * (kv < T(0.5) ? kv : T(0.5)) * invH : T(0);
+    }
+}
+
+// ==========================================================================
+// DFSPH solver passes
+// ==========================================================================
+// computePressureAccel, scalar path (TimeStepDFSPH.cpp:1299-1367)
+template <class T>
+__device__ __forceinline__ V3<T> pressure_accel_i(const DevParams<T> &P, const DevBufs<T> &B, uint32_t i,
+                                                  const T *__restrict__ kap)
+{
+    const v4_t<T> xi = ldv(B.x, i);
+    const T pi = kap[i];
+    V3<T> ai = mk3<T>(0, 0, 0);
+    const uint32_t nf = min(B.nf[i], P.capf);
+    const uint32_t *Lf = list_ptr(B.lf, i, P.capf);
+    for (uint32_t k = 0; k < nf; k++) {
+        const uint32_t j = Lf[k * 32u];
+        const T psum = pi + kap[j];
+        if (fabs(psum) > P.eps) {
+            const Pair<T> pr = pair_of<T>(xi, ldv(B.x, j));
+            const V3<T> g = gradW(P.K, pr);
+            ai = add(ai, scl(g, -P.V * psum));
+        }
+    }
+    if (fabs(pi) > P.eps) {
+        const uint32_t nb = min(B.nbn[i], P.capb);
+        const uint32_t *Lb = list_ptr(B.lb, i, P.capb);
+        for (uint32_t k = 0; k < nb; k++) {
+            const uint32_t j = Lb[k * 32u];
+            const v4_t<T> xj = ldv(B.xb, j);
+            const Pair<T> pr = pair_of<T>(xi, xj);
+            const V3<T> g = gradW(P.K, pr);
+            ai = add(ai, scl(g, -(T)xj.w * pi));
+        }
+    }
+    return ai;
+}
+
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_pressure_accel(DevParams<T> P, DevBufs<T> B, const T *__restrict__ kap)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    stv(B.pa, i, pack(pressure_accel_i(P, B, i, kap), T(0)));
+}
+
+// compute_aij_pj, scalar path (TimeStepDFSPH.cpp:1370-1420)
+template <class T> __device__ __forceinline__ T aij_pj_i(const DevParams<T> &P, const DevBufs<T> &B, uint32_t i)
+{
+    const v4_t<T> xi = ldv(B.x, i);
+    const V3<T> ai = xyz<T>(ldv(B.pa, i));
+    T accf = T(0), accb = T(0);
+    const uint32_t nf = min(B.nf[i], P.capf);
+    const uint32_t *Lf = list_ptr(B.lf, i, P.capf);
+    for (uint32_t k = 0; k < nf; k++) {
+        const uint32_t j = Lf[k * 32u];
+        const Pair<T> pr = pair_of<T>(xi, ldv(B.x, j));
+        const V3<T> g = gradW(P.K, pr);
+        const V3<T> aj = xyz<T>(ldv(B.pa, j));
+        accf += dot(sub(ai, aj), g);
+    }
+    const uint32_t nb = min(B.nbn[i], P.capb);
+    const uint32_t *Lb = list_ptr(B.lb, i, P.capb);
+    for (uint32_t k = 0; k < nb; k++) {
+        const uint32_t j = Lb[k * 32u];
+        const v4_t<T> xj = ldv(B.xb, j);
+        const Pair<T> pr = pair_of<T>(xi, xj);
+        accb += (T)xj.w * dot(ai, gradW(P.K, pr));
+    }
+    return accf * P.V + accb;
+}
+
+// divergenceSolveIteration (TimeStepDFSPH.cpp:621-706) / pressureSolveIteration (:544-619):
+// Jacobi update of kappa_v / kappa plus the FP64 average-error reduction and the
+// loop decision (the while conditions of :477 and :324).
+template <class T, bool DIV>
+__global__ void __launch_bounds__(kBlock) k_jacobi(DevParams<T> P, DevBufs<T> B, ReduceSlot slot,
+                                                     cudaGraphConditionalHandle handle, int use_handle)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    double err = 0.0;
+    if (i < P.n) {
+        const double hd = DIV ? B.sc->dt : B.sc->dt_next;
+        const T h = (T)hd;
+        T apj = aij_pj_i(P, B, i);
+        T *kap = DIV ? B.kappa_v : B.kappa;
+        if (DIV) {
+            apj *= h;
+            const T si = -B.dadv[i];
+            T residuum = (si - apj) < T(0) ? (si - apj) : T(0);
+            if (B.nf[i] + B.nbn[i] < 20u) residuum = T(0);
+            const T fac = B.factor[i] * (T(1) / h);
+            const T kv = kap[i] - T(0.5) * (si - apj) * fac;
+            kap[i] = kv > T(0) ? kv : T(0);
+            err = -(double)P.rho0 * (double)residuum;
+        } else {
+            apj *= h * h;
+            const T si = T(1) - B.dadv[i];
+            const T residuum = (si - apj) < T(0) ? (si - apj) : T(0);
+            const T fac = B.factor[i] * (T(1) / (h * h));
+            const T kv = kap[i] - T(0.5) * (si - apj) * fac;
+            kap[i] = kv > T(0) ? kv : T(0);
+            err = -(double)P.rho0 * (double)residuum;
+        }
+    }
+    DSum<1> mine;
+    mine.v[0] = err;
+    StepScalars *sc = B.sc;
+    const DevParams<T> &PP = P;
+    grid_sum_finalize<1>(mine, slot, [&](const DSum<1> &tot) {
+        const double avg = tot.v[0] / (double)PP.n;
+        unsigned it;
+        bool cont;
+        if (DIV) {
+            it = ++sc->iters_v;
+            sc->avg_err_v = avg;
+            const double eta = (1.0 / sc->dt) * PP.max_error_v * 0.01 * (double)PP.rho0;
+            const bool chk = avg <= eta;
+            cont = (!chk || it < 1u) && it < PP.max_iter_v;
+        } else {
+            it = ++sc->iters;
+            sc->avg_err = avg;
+            const double eta = PP.max_error * 0.01 * (double)PP.rho0;
+            const bool chk = avg <= eta;
+            cont = (!chk || it < PP.min_iter) && it < PP.max_iter;
+        }
+        sc->cont = cont ? 1u : 0u;
+        if (use_handle) cudaGraphSetConditional(handle, cont ? 1u : 0u);
+    });
+}
+
+// final pressure acceleration and velocity update of both solvers
+// (TimeStepDFSPH.cpp:500-520 and :345-363)
+template <class T, bool DIV>
+__global__ void __launch_bounds__(kBlock) k_solver_finalize(DevParams<T> P, DevBufs<T> B)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const T h = (T)(DIV ? B.sc->dt : B.sc->dt_next);
+    const V3<T> a = pressure_accel_i(P, B, i, DIV ? B.kappa_v : B.kappa);
+    stv(B.pa, i, pack(a, T(0)));
+    v4_t<T> v = ldv(B.v, i);
+    v.x += h * a.x;
+    v.y += h * a.y;
+    v.z += h * a.z;
+    stv(B.v, i, v);
+}
+
+__global__ void k_step_begin(StepScalars *sc)
+{
+    if (threadIdx.x == 0) {
+        sc->flags = 0;
+        sc->max_nf = 0;
+        sc->max_nb = 0;
+        sc->maxvel_bits = 0;
+        sc->iters_cg = 0;
+        sc->cg_err = 0.0;
+        sc->cg_state = 1;
+    }
+}
+
+template <class T>
+__global__ void k_loop_begin(StepScalars *sc, int div, unsigned max_iter)
+{
+    if (threadIdx.x == 0) {
+        if (div) { sc->iters_v = 0; sc->avg_err_v = 0.0; }
+        else { sc->iters = 0; sc->avg_err = 0.0; }
+        sc->cont = max_iter > 0 ? 1u : 0u;
+    }
+}
+
+// ==========================================================================
+// non-pressure forces
+// ==========================================================================
+// clearAccelerations (TimeStep.cpp:35-50) + XSPH::step scalar path (XSPH.cpp:138-211).
+// Also finishes the divergence solve's kappa_v *= h (TimeStepDFSPH.cpp:522-540),
+// which must wait until no thread reads kappa_v of its neighbours any more.
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_xsph(DevParams<T> P, DevBufs<T> B, int div_on)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const T h = (T)B.sc->dt;
+    const T invH = T(1) / h;
+    const v4_t<T> xi = ldv(B.x, i);
+    const V3<T> vi = xyz<T>(ldv(B.v, i));
+    V3<T> ai = mk3<T>(P.gx, P.gy, P.gz);
+    if (P.xsph != T(0)) {
+        V3<T> acc = mk3<T>(0, 0, 0);
+        const uint32_t nf = min(B.nf[i], P.capf);
+        const uint32_t *Lf = list_ptr(B.lf, i, P.capf);
+        for (uint32_t k = 0; k < nf; k++) {
+            const uint32_t j = Lf[k * 32u];
+            const Pair<T> pr = pair_of<T>(xi, ldv(B.x, j));
+            const V3<T> vj = xyz<T>(ldv(B.v, j));
+            const T w = (P.mass / B.density[j]) * kernel_W(P.K, pr.rl);
+            acc = add(acc, scl(sub(vi, vj), w));
+        }
+        ai = sub(ai, scl(acc, invH * P.xsph));
+    }
+    if (P.xsph_b != T(0)) {
+        const T rhoi = B.density[i];
+        T wsum = T(0);
+        const uint32_t nb = min(B.nbn[i], P.capb);
+        const uint32_t *Lb = list_ptr(B.lb, i, P.capb);
+        for (uint32_t k = 0; k < nb; k++) {
+            const uint32_t j = Lb[k * 32u];
+            const v4_t<T> xj = ldv(B.xb, j);
+            const Pair<T> pr = pair_of<T>(xi, xj);
+            wsum += (P.rho0 * (T)xj.w / rhoi) * kernel_W(P.K, pr.rl);
+        }
+        ai = sub(ai, scl(vi, invH * P.xsph_b * wsum));
+    }
+    stv(B.a, i, pack(ai, T(0)));
+    if (div_on) B.kappa_v[i] *= h;
+}
+
+// ---- Weiler et al. 2018 ---------------------------------------------------
+// (A v)_i = v_i - dt/rho_i * sum_j d mu (m_j/rho_j) ((v_i - v_j).x_ij) / (|x_ij|^2 + 0.01 h^2) gradW_ij
+// (Viscosity_Weiler2018.cpp:271-443); boundary term when mub != 0.
+template <class T, class VF>
+__device__ __forceinline__ V3<T> weiler_Av(const DevParams<T> &P, const DevBufs<T> &B, uint32_t i, V3<T> vi, VF vec_of)
+{
+    const v4_t<T> xi = ldv(B.x, i);
+    const T rhoi = B.density[i];
+    V3<T> acc = mk3<T>(0, 0, 0);
+    const uint32_t nf = min(B.nf[i], P.capf);
+    const uint32_t *Lf = list_ptr(B.lf, i, P.capf);
+    const T eps2 = T(0.01) * P.h2;
+    for (uint32_t k = 0; k < nf; k++) {
+        const uint32_t j = Lf[k * 32u];
+        const Pair<T> pr = pair_of<T>(xi, ldv(B.x, j));
+        const V3<T> g = gradW(P.K, pr);
+        const V3<T> vj = vec_of(j);
+        const T f = P.vd * P.mu * (P.mass / B.density[j]) * dot(sub(vi, vj), pr.r) / (pr.rl * pr.rl + eps2);
+        acc = add(acc, scl(g, f));
+    }
+    if (P.mub != T(0)) {
+        const uint32_t nb = min(B.nbn[i], P.capb);
+        const uint32_t *Lb = list_ptr(B.lb, i, P.capb);
+        for (uint32_t k = 0; k < nb; k++) {
+            const uint32_t j = Lb[k * 32u];
+            const v4_t<T> xj = ldv(B.xb, j);
+            const Pair<T> pr = pair_of<T>(xi, xj);
+            const V3<T> g = gradW(P.K, pr);
+            const T f = P.vd * P.mub * (P.rho0 * (T)xj.w / rhoi) * dot(vi, pr.r) / (pr.rl * pr.rl + eps2);
+            acc = add(acc, scl(g, f));
+        }
+    }
+    const T dt = (T)B.sc->dt;
+    return sub(vi, scl(acc, dt / rhoi));
+}
+
+template <class T> __device__ __forceinline__ V3<T> mat3_mul(const v4_t<T> &r0, const v4_t<T> &r1, const v4_t<T> &r2, V3<T> v)
+{
+    return V3<T>{(T)r0.x * v.x + (T)r0.y * v.y + (T)r0.z * v.z, (T)r1.x * v.x + (T)r1.y * v.y + (T)r1.z * v.z,
+                 (T)r2.x * v.x + (T)r2.y * v.y + (T)r2.z * v.z};
+}
+
+// Set-up of the CG solve (Viscosity_Weiler2018.cpp:891-926): block-Jacobi inverse
+// of the diagonal 3x3 blocks (diagonalMatrixElement :605-742, inverse taken in
+// MatrixFreeSolver.h:231-244), right-hand side b = v (computeRHS :1091-1254 with
+// static boundary), warm start g = v + vDiff, initial residual r = b - A g,
+// p = M^-1 r and the first reductions of Eigen's conjugate_gradient
+// (ConjugateGradient.h:29-70).
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T> B, ReduceSlot slot,
+                                                        cudaGraphConditionalHandle handle, int use_handle)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    DSum<3> mine;
+    mine.v[0] = mine.v[1] = mine.v[2] = 0.0;
+    if (i < P.n) {
+        const v4_t<T> xi = ldv(B.x, i);
+        const T rhoi = B.density[i];
+        const T dt = (T)B.sc->dt;
+        const T eps2 = T(0.01) * P.h2;
+        T R[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        const uint32_t nf = min(B.nf[i], P.capf);
+        const uint32_t *Lf = list_ptr(B.lf, i, P.capf);
+        for (uint32_t k = 0; k < nf; k++) {
+            const uint32_t j = Lf[k * 32u];
+            const Pair<T> pr = pair_of<T>(xi, ldv(B.x, j));
+            const V3<T> g = gradW(P.K, pr);
+            const T f = P.vd * P.mu * (P.mass / B.density[j]) / (pr.rl * pr.rl + eps2);
+            const T gg[3] = {g.x, g.y, g.z}, rr[3] = {pr.r.x, pr.r.y, pr.r.z};
+#pragma unroll
+            for (int a = 0; a < 3; a++)
+#pragma unroll
+                for (int b = 0; b < 3; b++) R[3 * a + b] += f * gg[a] * rr[b];
+        }
+        if (P.mub != T(0)) {
+            const uint32_t nb = min(B.nbn[i], P.capb);
+            const uint32_t *Lb = list_ptr(B.lb, i, P.capb);
+            for (uint32_t k = 0; k < nb; k++) {
+                const uint32_t j = Lb[k * 32u];
+                const v4_t<T> xj = ldv(B.xb, j);
+                const Pair<T> pr = pair_of<T>(xi, xj);
+                const V3<T> g = gradW(P.K, pr);
+                const T f = P.vd * P.mub * (P.rho0 * (T)xj.w / rhoi) / (pr.rl * pr.rl + eps2);
+                const T gg[3] = {g.x, g.y, g.z}, rr[3] = {pr.r.x, pr.r.y, pr.r.z};
+#pragma unroll
+                for (int a = 0; a < 3; a++)
+#pragma unroll
+                    for (int b = 0; b < 3; b++) R[3 * a + b] += f * gg[a] * rr[b];
+            }
+        }
+        T M[9];
+        const T s = dt / rhoi;
+#pragma unroll
+        for (int a = 0; a < 9; a++) M[a] = ((a % 4) == 0 ? T(1) : T(0)) - s * R[a];
+        const T c00 = M[4] * M[8] - M[5] * M[7];
+        const T c01 = M[5] * M[6] - M[3] * M[8];
+        const T c02 = M[3] * M[7] - M[4] * M[6];
+        const T det = M[0] * c00 + M[1] * c01 + M[2] * c02;
+        const T id = T(1) / det;
+        v4_t<T> r0, r1, r2;
+        r0.x = c00 * id; r0.y = (M[2] * M[7] - M[1] * M[8]) * id; r0.z = (M[1] * M[5] - M[2] * M[4]) * id; r0.w = 0;
+        r1.x = c01 * id; r1.y = (M[0] * M[8] - M[2] * M[6]) * id; r1.z = (M[2] * M[3] - M[0] * M[5]) * id; r1.w = 0;
+        r2.x = c02 * id; r2.y = (M[1] * M[6] - M[0] * M[7]) * id; r2.z = (M[0] * M[4] - M[1] * M[3]) * id; r2.w = 0;
+        stv(B.inv0, i, r0);
+        stv(B.inv1, i, r1);
+        stv(B.inv2, i, r2);
+
+        const V3<T> vi = xyz<T>(ldv(B.v, i));
+        const V3<T> gi = add(vi, xyz<T>(ldv(B.vdiff, i)));
+        const V3<T> Ag = weiler_Av(P, B, i, gi, [&](uint32_t j) { return add(xyz<T>(ldv(B.v, j)), xyz<T>(ldv(B.vdiff, j))); });
+        const V3<T> r = sub(vi, Ag);
+        const V3<T> p = mat3_mul<T>(r0, r1, r2, r);
+        stv(B.cg_x, i, pack(gi, T(0)));
+        stv(B.cg_r, i, pack(r, T(0)));
+        stv(B.cg_p, i, pack(p, T(0)));
+        mine.v[0] = (double)vi.x * vi.x + (double)vi.y * vi.y + (double)vi.z * vi.z;
+        mine.v[1] = (double)r.x * r.x + (double)r.y * r.y + (double)r.z * r.z;
+        mine.v[2] = (double)r.x * p.x + (double)r.y * p.y + (double)r.z * p.z;
+    }
+    StepScalars *sc = B.sc;
+    const double tol = P.visc_tol;
+    const unsigned maxit = P.visc_max_iter;
+    grid_sum_finalize<3>(mine, slot, [&](const DSum<3> &tot) {
+        sc->cg_rhs2 = tot.v[0];
+        sc->iters_cg = 0;
+        sc->cg_err = 0.0;
+        if (tot.v[0] == 0.0) {
+            sc->cg_state = 2;
+        } else {
+            double thr = tol * tol * tot.v[0];
+            if (thr < 2.2250738585072014e-308) thr = 2.2250738585072014e-308;
+            sc->cg_thresh = thr;
+            sc->cg_res2 = tot.v[1];
+            if (tot.v[1] < thr) {
+                sc->cg_state = 1;
+                sc->cg_err = sqrt(tot.v[1] / tot.v[0]);
+            } else {
+                sc->cg_state = 0;
+                sc->cg_absnew = tot.v[2];
+            }
+        }
+        const bool cont = sc->cg_state == 0 && maxit > 0;
+        if (sc->cg_state == 0 && maxit == 0) sc->cg_err = sqrt(tot.v[1] / tot.v[0]);
+        sc->cont = cont ? 1u : 0u;
+        if (use_handle) cudaGraphSetConditional(handle, cont ? 1u : 0u);
+    });
+}
+
+// tmp = A p and p.tmp -> alpha (ConjugateGradient.h:74-76)
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_cg_matvec(DevParams<T> P, DevBufs<T> B, ReduceSlot slot)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    DSum<1> mine;
+    mine.v[0] = 0.0;
+    if (i < P.n) {
+        const V3<T> pi = xyz<T>(ldv(B.cg_p, i));
+        const V3<T> t = weiler_Av(P, B, i, pi, [&](uint32_t j) { return xyz<T>(ldv(B.cg_p, j)); });
+        stv(B.cg_t, i, pack(t, T(0)));
+        mine.v[0] = (double)pi.x * t.x + (double)pi.y * t.y + (double)pi.z * t.z;
+    }
+    StepScalars *sc = B.sc;
+    grid_sum_finalize<1>(mine, slot, [&](const DSum<1> &tot) { sc->cg_alpha = sc->cg_absnew / tot.v[0]; });
+}
+
+// x += alpha p; r -= alpha tmp; |r|^2; z = M^-1 r; r.z -> beta (ConjugateGradient.h:77-88)
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_cg_update(DevParams<T> P, DevBufs<T> B, ReduceSlot slot,
+                                                       cudaGraphConditionalHandle handle, int use_handle)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    DSum<2> mine;
+    mine.v[0] = mine.v[1] = 0.0;
+    if (i < P.n) {
+        const double alpha = B.sc->cg_alpha;
+        const V3<T> p = xyz<T>(ldv(B.cg_p, i));
+        const V3<T> t = xyz<T>(ldv(B.cg_t, i));
+        V3<T> x = xyz<T>(ldv(B.cg_x, i));
+        V3<T> r = xyz<T>(ldv(B.cg_r, i));
+        x = V3<T>{(T)((double)x.x + alpha * p.x), (T)((double)x.y + alpha * p.y), (T)((double)x.z + alpha * p.z)};
+        r = V3<T>{(T)((double)r.x - alpha * t.x), (T)((double)r.y - alpha * t.y), (T)((double)r.z - alpha * t.z)};
+        const V3<T> z = mat3_mul<T>(ldv(B.inv0, i), ldv(B.inv1, i), ldv(B.inv2, i), r);
+        stv(B.cg_x, i, pack(x, T(0)));
+        stv(B.cg_r, i, pack(r, T(0)));
+        stv(B.cg_z, i, pack(z, T(0)));
+        mine.v[0] = (double)r.x * r.x + (double)r.y * r.y + (double)r.z * r.z;
+        mine.v[1] = (double)r.x * z.x + (double)r.y * z.y + (double)r.z * z.z;
+    }
+    StepScalars *sc = B.sc;
+    const unsigned maxit = P.visc_max_iter;
+    grid_sum_finalize<2>(mine, slot, [&](const DSum<2> &tot) {
+        sc->cg_res2 = tot.v[0];
+        sc->cg_err = sqrt(tot.v[0] / sc->cg_rhs2);
+        bool cont;
+        if (tot.v[0] < sc->cg_thresh) {
+            sc->cg_state = 1;
+            cont = false;
+        } else {
+            const double absOld = sc->cg_absnew;
+            sc->cg_absnew = tot.v[1];
+            sc->cg_beta = tot.v[1] / absOld;
+            sc->iters_cg += 1;
+            cont = sc->iters_cg < maxit;
+        }
+        sc->cont = cont ? 1u : 0u;
+        if (use_handle) cudaGraphSetConditional(handle, cont ? 1u : 0u);
+    });
+}
+
+// p = z + beta p (ConjugateGradient.h:88)
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_cg_p(DevParams<T> P, DevBufs<T> B)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    if (B.sc->cg_state != 0) return;
+    const double beta = B.sc->cg_beta;
+    const V3<T> z = xyz<T>(ldv(B.cg_z, i));
+    const V3<T> p = xyz<T>(ldv(B.cg_p, i));
+    stv(B.cg_p, i, pack(V3<T>{(T)(z.x + beta * p.x), (T)(z.y + beta * p.y), (T)(z.z + beta * p.z)}, T(0)));
+}
+
+// ==========================================================================
+// viscosity forces + CFL + velocity kick
+// ==========================================================================
+// applyForces (Viscosity_Weiler2018.cpp:928-936): a += (x - v)/dt, vDiff = x - v;
+// updateTimeStepSizeCFL (Simulation.cpp:415-492): max |v + a h|^2 over particles;
+// kick v += h a (TimeStepDFSPH.cpp:192-208).  The last block computes dt_next.
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_kick(DevParams<T> P, DevBufs<T> B)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float m = 0.0f;
+    const double hd = B.sc->dt;
+    if (i < P.n) {
+        const T h = (T)hd;
+        V3<T> a = xyz<T>(ldv(B.a, i));
+        v4_t<T> v4 = ldv(B.v, i);
+        const V3<T> v = xyz<T>(v4);
+        if (P.visc_on) {
+            const V3<T> x = B.sc->cg_state == 2 ? mk3<T>(0, 0, 0) : xyz<T>(ldv(B.cg_x, i));
+            const V3<T> dv = sub(x, v);
+            a = add(a, scl(dv, T(1) / h));
+            stv(B.vdiff, i, pack(dv, T(0)));
+            stv(B.a, i, pack(a, T(0)));
+        }
+        const V3<T> vn = add(v, scl(a, h));
+        const T m2 = dot(vn, vn);
+        if (!(m2 <= T(3.0e38))) atomicOr(&B.sc->flags, kFlagNonFinite);
+        m = (float)m2;
+        if (!(m >= 0.0f)) m = 0.0f;
+        v4.x = vn.x; v4.y = vn.y; v4.z = vn.z;
+        stv(B.v, i, v4);
+    }
+    // block max -> atomicMax on the float bits (non-negative floats order like uint)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+    __shared__ float wm[32];
+    __shared__ bool amLast;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) wm[warp] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float bm = 0.0f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) bm = fmaxf(bm, wm[w]);
+        atomicMax(&B.sc->maxvel_bits, __float_as_uint(bm));
+        __threadfence();
+        const unsigned t = atomicAdd(B.counter, 1u);
+        amLast = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (amLast && threadIdx.x == 0) {
+        __threadfence();
+        StepScalars *sc = B.sc;
+        double maxVel = (double)__uint_as_float(atomicAdd(&sc->maxvel_bits, 0u));
+        sc->maxvel_bits = 0;
+        *B.counter = 0;
+        double hn = hd;
+        if (P.cfl_method != 0) {
+            if (maxVel < 1.0e-9) maxVel = 1.0e-9;
+            hn = P.cfl_factor * 0.4 * (2.0 * P.radius / sqrt(maxVel));
+            hn = fmin(hn, P.cfl_max);
+            hn = fmax(hn, P.cfl_min);
+            if (P.cfl_method == 2 && sc->prev_iters != 0) {
+                double hh = hd;
+                if (sc->prev_iters > 10) hh *= 0.9;
+                else if (sc->prev_iters < 5) hh *= 1.1;
+                hn = fmin(hh, hn);
+            }
+        }
+        sc->dt_next = hn;
+    }
+}
+
+// computeDensityAdv (TimeStepDFSPH.cpp:1190-1243) and the pressure-solve set-up
+// (:264-309): advected density, warm-started kappa (USE_WARMSTART).
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_press_init(DevParams<T> P, DevBufs<T> B)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const T h = (T)B.sc->dt_next;
+    const v4_t<T> xi = ldv(B.x, i);
+    const V3<T> vi = xyz<T>(ldv(B.v, i));
+    T accf = T(0), accb = T(0);
+    const uint32_t nf = min(B.nf[i], P.capf);
+    const uint32_t *Lf = list_ptr(B.lf, i, P.capf);
+    for (uint32_t k = 0; k < nf; k++) {
+        const uint32_t j = Lf[k * 32u];
+        const Pair<T> pr = pair_of<T>(xi, ldv(B.x, j));
+        accf += dot(sub(vi, xyz<T>(ldv(B.v, j))), gradW(P.K, pr));
+    }
+    const uint32_t nb = min(B.nbn[i], P.capb);
+    const uint32_t *Lb = list_ptr(B.lb, i, P.capb);
+    for (uint32_t k = 0; k < nb; k++) {
+        const uint32_t j = Lb[k * 32u];
+        const v4_t<T> xj = ldv(B.xb, j);
+        const Pair<T> pr = pair_of<T>(xi, xj);
+        accb += (T)xj.w * dot(vi, gradW(P.K, pr));
+    }
+    const T dadv = B.density[i] / P.rho0 + h * (accf * P.V + accb);
+    B.dadv[i] = dadv;
+    const T invH2 = T(1) / (h * h);
+    const T k = B.kappa[i];
+    B.kappa[i] = dadv > T(1) ? T(0.5) * (k < T(0.00025) ? k : T(0.00025)) * invH2 : T(0);
+}
+
+// x += h_old v (TimeStepDFSPH.cpp:220-237) accumulated in FP64 (double-float
+// compensated positions in FP32 mode), kappa *= h_new^2 (:365-383); the last
+// block advances time (:248) and makes dt_next the step size of the next step.
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_integrate(DevParams<T> P, DevBufs<T> B)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const double h = B.sc->dt;
+    const double hn = B.sc->dt_next;
+    if (i < P.n) {
+        v4_t<T> x = ldv(B.x, i);
+        const v4_t<T> v = ldv(B.v, i);
+        if (B.xlo) {
+            const float4 lo = B.xlo[i];
+            const double px = (double)x.x + (double)lo.x + h * (double)v.x;
+            const double py = (double)x.y + (double)lo.y + h * (double)v.y;
+            const double pz = (double)x.z + (double)lo.z + h * (double)v.z;
+            x.x = (T)px; x.y = (T)py; x.z = (T)pz;
+            B.xlo[i] = make_float4((float)(px - (double)x.x), (float)(py - (double)x.y), (float)(pz - (double)x.z), 0.f);
+        } else {
+            x.x = (T)((double)x.x + h * (double)v.x);
+            x.y = (T)((double)x.y + h * (double)v.y);
+            x.z = (T)((double)x.z + h * (double)v.z);
+        }
+        stv(B.x, i, x);
+        B.kappa[i] = (T)((double)B.kappa[i] * (hn * hn));
+    }
+    __shared__ bool amLast;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned t = atomicAdd(B.counter, 1u);
+        amLast = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (amLast && threadIdx.x == 0) {
+        StepScalars *sc = B.sc;
+        *B.counter = 0;
+        sc->time += h;
+        sc->dt_used = h;
+        sc->dt = hn;
+        sc->prev_iters = sc->iters;
+    }
+}
+
+// ==========================================================================
+// boundary set-up
+// ==========================================================================
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_boundary_keys(DevParams<T> P, const v4_t<T> *__restrict__ xb,
+                                                           uint32_t *keys, uint32_t *vals, uint32_t nb)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nb) return;
+    int cx, cy, cz;
+    cell_of(P, ldv(xb, i), cx, cy, cz);
+    keys[i] = morton3((uint32_t)cx, (uint32_t)cy, (uint32_t)cz);
+    vals[i] = i;
+}
+
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_boundary_gather(DevParams<T> P, DevBufs<T> B, const v4_t<T> *__restrict__ xb_in,
+                                                             const uint32_t *__restrict__ perm, uint32_t *cells)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= P.nb) return;
+    const uint32_t s = perm[k];
+    v4_t<T> x = ldv(xb_in, s);
+    x.w = 0;
+    stv(B.xb, k, x);
+    B.bid[k] = s;
+    int cx, cy, cz;
+    cell_of(P, x, cx, cy, cz);
+    cells[k] = ((uint32_t)cz * (uint32_t)P.dimy + (uint32_t)cy) * (uint32_t)P.dimx + (uint32_t)cx;
+}
+
+// BoundaryModel_Akinci2012::computeBoundaryVolume (BoundaryModel_Akinci2012.cpp:48-75):
+// V_b = 1 / (W0 + sum over boundary neighbours of W)
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_boundary_volume(DevParams<T> P, DevBufs<T> B)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.nb) return;
+    v4_t<T> xi = ldv(B.xb, i);
+    int cx, cy, cz;
+    cell_of(P, xi, cx, cy, cz);
+    T delta = P.K.w0;
+    for (int dz = -1; dz <= 1; dz++) {
+        const int z = cz + dz;
+        if (z < 0 || z >= P.dimz) continue;
+        for (int dy = -1; dy <= 1; dy++) {
+            const int y = cy + dy;
+            if (y < 0 || y >= P.dimy) continue;
+            for (int dx = -1; dx <= 1; dx++) {
+                const int x = cx + dx;
+                if (x < 0 || x >= P.dimx) continue;
+                const uint32_t c = ((uint32_t)z * (uint32_t)P.dimy + (uint32_t)y) * (uint32_t)P.dimx + (uint32_t)x;
+                const uint32_t s = B.bcstart[c];
+                if (s == kEmpty) continue;
+                const uint32_t e = B.bcend[c];
+                for (uint32_t j = s; j < e; j++) {
+                    if (j == i) continue;
+                    T ddx, ddy, ddz;
+                    const T d2 = pair_d2(xi, ldv(B.xb, j), ddx, ddy, ddz);
+                    if (d2 < P.K.h2) delta += kernel_W(P.K, dev_sqrt(d2));
+                }
+            }
+        }
+    }
+    // stored by a second pass: the w lane of xb is read by other threads here
+    B.bscratch[i] = T(1) / delta;
+}
+
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_boundary_volume_store(DevParams<T> P, DevBufs<T> B)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.nb) return;
+    v4_t<T> x = ldv(B.xb, i);
+    x.w = B.bscratch[i];
+    stv(B.xb, i, x);
+}
+
+// ==========================================================================
+// host <-> device field transfer helpers
+// ==========================================================================
+template <class T>
+__global__ void k_init_state(DevParams<T> P, DevBufs<T> B, const double *__restrict__ x, const double *__restrict__ v,
+                             const uint32_t *__restrict__ id)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    v4_t<T> xx, vv, zz;
+    xx.x = (T)x[3 * i]; xx.y = (T)x[3 * i + 1]; xx.z = (T)x[3 * i + 2]; xx.w = 0;
+    vv.x = (T)v[3 * i]; vv.y = (T)v[3 * i + 1]; vv.z = (T)v[3 * i + 2]; vv.w = 0;
+    zz.x = zz.y = zz.z = zz.w = 0;
+    stv(B.x, i, xx);
+    stv(B.v, i, vv);
+    stv(B.vdiff, i, zz);
+    if (B.xlo)
+        B.xlo[i] = make_float4((float)(x[3 * i] - (double)xx.x), (float)(x[3 * i + 1] - (double)xx.y),
+                               (float)(x[3 * i + 2] - (double)xx.z), 0.f);
+    B.kappa[i] = 0;
+    B.kappa_v[i] = 0;
+    B.id[i] = id ? id[i] : i;
+}
+
+__global__ void k_inverse_perm(const uint32_t *__restrict__ id, uint32_t *__restrict__ inv, uint32_t n)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n && id[k] < n) inv[id[k]] = k;
+}
+
+template <class T> __device__ __forceinline__ void put(void *out, int dt, size_t idx, double v)
+{
+    if (dt == SPHGB_DTYPE_F32) static_cast<float *>(out)[idx] = (float)v;
+    else if (dt == SPHGB_DTYPE_F64) static_cast<double *>(out)[idx] = v;
+    else static_cast<uint32_t *>(out)[idx] = (uint32_t)v;
+}
+template <class T> __device__ __forceinline__ double get(const void *in, int dt, size_t idx)
+{
+    if (dt == SPHGB_DTYPE_F32) return (double)static_cast<const float *>(in)[idx];
+    if (dt == SPHGB_DTYPE_F64) return static_cast<const double *>(in)[idx];
+    return (double)static_cast<const uint32_t *>(in)[idx];
+}
+
+// field value of sorted particle k, component c, written at id order
+template <class T>
+__global__ void k_scatter_field(DevParams<T> P, DevBufs<T> B, int field, void *out, int odt)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (field == SPHGB_FIELD_BOUNDARY_VOLUME || field == SPHGB_FIELD_BOUNDARY_POSITION) {
+        if (k >= P.nb) return;
+        const v4_t<T> x = ldv(B.xb, k);
+        const uint32_t d = B.bid[k];
+        if (field == SPHGB_FIELD_BOUNDARY_VOLUME) put<T>(out, odt, d, (double)x.w);
+        else {
+            put<T>(out, odt, 3 * (size_t)d, (double)x.x);
+            put<T>(out, odt, 3 * (size_t)d + 1, (double)x.y);
+            put<T>(out, odt, 3 * (size_t)d + 2, (double)x.z);
+        }
+        return;
+    }
+    if (k >= P.n) return;
+    const uint32_t d = B.id[k];
+    const double hn = B.sc->dt_next;
+    auto vec = [&](const v4_t<T> *arr, const float4 *lo) {
+        const v4_t<T> a = ldv(arr, k);
+        double ax = (double)a.x, ay = (double)a.y, az = (double)a.z;
+        if (lo) { const float4 l = lo[k]; ax += l.x; ay += l.y; az += l.z; }
+        put<T>(out, odt, 3 * (size_t)d, ax);
+        put<T>(out, odt, 3 * (size_t)d + 1, ay);
+        put<T>(out, odt, 3 * (size_t)d + 2, az);
+    };
+    switch (field) {
+    case SPHGB_FIELD_POSITION: vec(B.x, B.xlo); break;
+    case SPHGB_FIELD_VELOCITY: vec(B.v, nullptr); break;
+    case SPHGB_FIELD_ACCELERATION: vec(B.a, nullptr); break;
+    case SPHGB_FIELD_PRESSURE_ACCEL: vec(B.pa, nullptr); break;
+    case SPHGB_FIELD_VDIFF: vec(B.vdiff, nullptr); break;
+    case SPHGB_FIELD_DENSITY: put<T>(out, odt, d, (double)B.density[k]); break;
+    case SPHGB_FIELD_FACTOR_RAW: put<T>(out, odt, d, (double)B.factor[k]); break;
+    case SPHGB_FIELD_FACTOR: put<T>(out, odt, d, (double)B.factor[k] / (hn * hn)); break;
+    case SPHGB_FIELD_DENSITY_ADV: put<T>(out, odt, d, (double)B.dadv[k]); break;
+    case SPHGB_FIELD_PRESSURE_RHO2: put<T>(out, odt, d, (double)B.kappa[k]); break;
+    case SPHGB_FIELD_PRESSURE_RHO2_V: put<T>(out, odt, d, (double)B.kappa_v[k]); break;
+    case SPHGB_FIELD_PARTICLE_ID: put<T>(out, odt, d, (double)B.id[k]); break;
+    case SPHGB_FIELD_NUM_FLUID_NEIGHBORS: put<T>(out, odt, d, (double)B.nf[k]); break;
+    case SPHGB_FIELD_NUM_BOUNDARY_NEIGHBORS: put<T>(out, odt, d, (double)B.nbn[k]); break;
+    default: break;
+    }
+}
+
+template <class T>
+__global__ void k_upload_field(DevParams<T> P, DevBufs<T> B, int field, const void *in, int idt, const uint32_t *__restrict__ inv)
+{
+    const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;   // particle id
+    if (d >= P.n) return;
+    const uint32_t k = inv[d];
+    auto vec = [&](v4_t<T> *arr, float4 *lo) {
+        const double ax = get<T>(in, idt, 3 * (size_t)d), ay = get<T>(in, idt, 3 * (size_t)d + 1),
+                     az = get<T>(in, idt, 3 * (size_t)d + 2);
+        v4_t<T> a = ldv(arr, k);
+        a.x = (T)ax; a.y = (T)ay; a.z = (T)az;
+        stv(arr, k, a);
+        if (lo) lo[k] = make_float4((float)(ax - (double)a.x), (float)(ay - (double)a.y), (float)(az - (double)a.z), 0.f);
+    };
+    switch (field) {
+    case SPHGB_FIELD_POSITION: vec(B.x, B.xlo); break;
+    case SPHGB_FIELD_VELOCITY: vec(B.v, nullptr); break;
+    case SPHGB_FIELD_VDIFF: vec(B.vdiff, nullptr); break;
+    case SPHGB_FIELD_PRESSURE_RHO2: B.kappa[k] = (T)get<T>(in, idt, d); break;
+    case SPHGB_FIELD_PRESSURE_RHO2_V: B.kappa_v[k] = (T)get<T>(in, idt, d); break;
+    default: break;
+    }
+}
+
+// Neighbour lists to particle ids, CSR (debug / oracle comparison path)
+__global__ void k_lists_to_ids(const uint32_t *__restrict__ list, const uint32_t *__restrict__ cnt, uint32_t cap,
+                               const uint32_t *__restrict__ id, const uint32_t *__restrict__ inv,
+                               const uint32_t *__restrict__ bid, int kind, const uint32_t *__restrict__ offsets,
+                               uint32_t *__restrict__ out, uint32_t n)
+{
+    const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;   // particle id
+    if (d >= n) return;
+    const uint32_t k = inv[d];
+    const uint32_t c = min(cnt[k], cap);
+    const uint32_t *L = list_ptr(list, k, cap);
+    uint32_t *o = out + offsets[d];
+    for (uint32_t m = 0; m < c; m++) {
+        const uint32_t j = L[m * 32u];
+        o[m] = kind == 0 ? id[j] : bid[j];
+    }
+}
+
+}  // namespace
+
+// ==========================================================================
+// launchers
+// ==========================================================================
+template <class T> void launch_keys(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
+{
+    if (P.n) k_keys<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
+}
+template <class T> void launch_gather(const DevParams<T> &P, const DevBufs<T> &B, const uint32_t *perm, cudaStream_t s)
+{
+    if (P.n) k_gather<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B, perm);
+}
+template <class T> void launch_cell_ranges(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
+{
+    if (P.n) k_cell_ranges<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B.cellid, B.cstart, B.cend, P.n);
+}
+template <class T> void launch_build(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
+{
+    if (P.n) k_build<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
+}
+template <class T> void launch_pressure_accel(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s)
+{
+    if (P.n) k_pressure_accel<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B, div ? B.kappa_v : B.kappa);
+}
+template <class T>
+void launch_jacobi(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaGraphConditionalHandle h, bool use_handle,
+                   cudaStream_t s)
+{
+    if (!P.n) return;
+    ReduceSlot slot{B.partials, B.counter};
+    if (div) k_jacobi<T, true><<<grid_for(P.n), kBlock, 0, s>>>(P, B, slot, h, use_handle ? 1 : 0);
+    else k_jacobi<T, false><<<grid_for(P.n), kBlock, 0, s>>>(P, B, slot, h, use_handle ? 1 : 0);
+}
+template <class T> void launch_solver_finalize(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s)
+{
+    if (!P.n) return;
+    if (div) k_solver_finalize<T, true><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
+    else k_solver_finalize<T, false><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
+}
+template <class T> void launch_step_begin(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
+{
+    k_step_begin<<<1, 32, 0, s>>>(B.sc);
+}
+template <class T> void launch_loop_begin(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s)
+{
+    k_loop_begin<T><<<1, 32, 0, s>>>(B.sc, div ? 1 : 0, div ? P.max_iter_v : P.max_iter);
+}
+template <class T> void launch_xsph(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
+{
+    if (P.n) k_xsph<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B, P.div_on);
+}
+template <class T>
+void launch_visc_setup(const DevParams<T> &P, const DevBufs<T> &B, cudaGraphConditionalHandle h, bool use_handle,
+                       cudaStream_t s)
+{
+    if (!P.n) return;
+    ReduceSlot slot{B.partials, B.counter};
+    k_visc_setup<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B, slot, h, use_handle ? 1 : 0);
+}
+template <class T> void launch_cg_matvec(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
+{
+    if (!P.n) return;
+    ReduceSlot slot{B.partials, B.counter};
+    k_cg_matvec<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B, slot);
+}
+template <class T>
+void launch_cg_update(const DevParams<T> &P, const DevBufs<T> &B, cudaGraphConditionalHandle h, bool use_handle,
+                      cudaStream_t s)
+{
+    if (!P.n) return;
+    ReduceSlot slot{B.partials, B.counter};
+    k_cg_update<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B, slot, h, use_handle ? 1 : 0);
+}
+template <class T> void launch_cg_p(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
+{
+    if (P.n) k_cg_p<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
+}
+template <class T> void launch_kick(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
+{
+    k_kick<T><<<grid_for(P.n > 0 ? P.n : 1), kBlock, 0, s>>>(P, B);
+}
+template <class T> void launch_press_init(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
+{
+    if (P.n) k_press_init<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
+}
+template <class T> void launch_integrate(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
+{
+    k_integrate<T><<<grid_for(P.n > 0 ? P.n : 1), kBlock, 0, s>>>(P, B);
+}
+template <class T> void launch_boundary_keys(const DevParams<T> &P, const DevBufs<T> &B, const v4_t<T> *xb_in,
+                                             uint32_t *keys, uint32_t *vals, cudaStream_t s)
+{
+    if (P.nb) k_boundary_keys<T><<<grid_for(P.nb), kBlock, 0, s>>>(P, xb_in, keys, vals, P.nb);
+}
+template <class T> void launch_boundary_gather(const DevParams<T> &P, const DevBufs<T> &B, const v4_t<T> *xb_in,
+                                               const uint32_t *perm, const uint32_t *cells, cudaStream_t s)
+{
+    if (!P.nb) return;
+    k_boundary_gather<T><<<grid_for(P.nb), kBlock, 0, s>>>(P, B, xb_in, perm, const_cast<uint32_t *>(cells));
+    k_cell_ranges<T><<<grid_for(P.nb), kBlock, 0, s>>>(P, cells, B.bcstart, B.bcend, P.nb);
+}
+template <class T> void launch_boundary_volume(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
+{
+    if (!P.nb) return;
+    k_boundary_volume<T><<<grid_for(P.nb), kBlock, 0, s>>>(P, B);
+    k_boundary_volume_store<T><<<grid_for(P.nb), kBlock, 0, s>>>(P, B);
+}
+template <class T> void launch_scatter_field(const DevParams<T> &P, const DevBufs<T> &B, int field, void *out,
+                                             int odt, cudaStream_t s)
+{
+    const uint32_t m = (field == SPHGB_FIELD_BOUNDARY_VOLUME || field == SPHGB_FIELD_BOUNDARY_POSITION) ? P.nb : P.n;
+    if (m) k_scatter_field<T><<<grid_for(m), kBlock, 0, s>>>(P, B, field, out, odt);
+}
+template <class T> void launch_upload_field(const DevParams<T> &P, const DevBufs<T> &B, int field, const void *in,
+                                            int idt, const uint32_t *inv, cudaStream_t s)
+{
+    if (P.n) k_upload_field<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B, field, in, idt, inv);
+}
+template <class T> void launch_init_state(const DevParams<T> &P, const DevBufs<T> &B, const double *x, const double *v,
+                                          const uint32_t *id, cudaStream_t s)
+{
+    if (P.n) k_init_state<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B, x, v, id);
+}
+void launch_inverse_perm(const uint32_t *id, uint32_t *inv, uint32_t n, cudaStream_t s)
+{
+    if (n) k_inverse_perm<<<grid_for(n), kBlock, 0, s>>>(id, inv, n);
+}
+void launch_lists_to_ids(const uint32_t *list, const uint32_t *cnt, uint32_t cap, const uint32_t *id, const uint32_t *inv,
+                         const uint32_t *bid, int kind, const uint32_t *offsets, uint32_t *out, uint32_t n, cudaStream_t s)
+{
+    if (n) k_lists_to_ids<<<grid_for(n), kBlock, 0, s>>>(list, cnt, cap, id, inv, bid, kind, offsets, out, n);
+}
+
+#define SPHGB_INSTANTIATE(T)                                                                                        \
+    template void launch_keys<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                           \
+    template void launch_gather<T>(const DevParams<T> &, const DevBufs<T> &, const uint32_t *, cudaStream_t);       \
+    template void launch_cell_ranges<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                    \
+    template void launch_build<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                          \
+    template void launch_pressure_accel<T>(const DevParams<T> &, const DevBufs<T> &, bool, cudaStream_t);           \
+    template void launch_jacobi<T>(const DevParams<T> &, const DevBufs<T> &, bool, cudaGraphConditionalHandle, bool, \
+                                   cudaStream_t);                                                                   \
+    template void launch_solver_finalize<T>(const DevParams<T> &, const DevBufs<T> &, bool, cudaStream_t);          \
+    template void launch_loop_begin<T>(const DevParams<T> &, const DevBufs<T> &, bool, cudaStream_t);               \
+    template void launch_step_begin<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                     \
+    template void launch_xsph<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                           \
+    template void launch_visc_setup<T>(const DevParams<T> &, const DevBufs<T> &, cudaGraphConditionalHandle, bool,  \
+                                       cudaStream_t);                                                               \
+    template void launch_cg_matvec<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                      \
+    template void launch_cg_update<T>(const DevParams<T> &, const DevBufs<T> &, cudaGraphConditionalHandle, bool,   \
+                                      cudaStream_t);                                                                \
+    template void launch_cg_p<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                           \
+    template void launch_kick<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                           \
+    template void launch_press_init<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                     \
+    template void launch_integrate<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                      \
+    template void launch_boundary_keys<T>(const DevParams<T> &, const DevBufs<T> &, const v4_t<T> *, uint32_t *,    \
+                                          uint32_t *, cudaStream_t);                                                \
+    template void launch_boundary_gather<T>(const DevParams<T> &, const DevBufs<T> &, const v4_t<T> *,              \
+                                            const uint32_t *, const uint32_t *, cudaStream_t);                      \
+    template void launch_boundary_volume<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                \
+    template void launch_scatter_field<T>(const DevParams<T> &, const DevBufs<T> &, int, void *, int, cudaStream_t); \
+    template void launch_upload_field<T>(const DevParams<T> &, const DevBufs<T> &, int, const void *, int,          \
+                                         const uint32_t *, cudaStream_t);                                           \
+    template void launch_init_state<T>(const DevParams<T> &, const DevBufs<T> &, const double *, const double *,    \
+                                       const uint32_t *, cudaStream_t);
+
+SPHGB_INSTANTIATE(float)
+SPHGB_INSTANTIATE(double)
+
+}  // namespace sphgb

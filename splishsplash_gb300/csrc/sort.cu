@@ -1,0 +1,128 @@
+// Stable LSD radix sort of (uint32 key, uint32 value) pairs with 8-bit digits.
+// Used to order particles by the Morton code of their cell every step.
+//
+// Per pass: (1) per-tile digit histograms, stored digit-major so that one
+// exclusive scan over [digit][tile] yields every tile's global base per digit
+// in stable order; (2) a single-block scan; (3) a stable scatter that ranks the
+// items of a tile with warp match masks and per-warp digit counts.
+#include "sph_ctx.h"
+
+namespace sphgb {
+
+namespace {
+
+constexpr int kSortThreads = 256;
+constexpr int kItems = kSortTile / kSortThreads;   // 8
+constexpr int kRadix = 256;
+constexpr int kWarps = kSortThreads / 32;
+
+__global__ void __launch_bounds__(kSortThreads) k_hist(const uint32_t *__restrict__ keys, uint32_t n, int shift,
+                                                      uint32_t *__restrict__ hist, uint32_t num_tiles)
+{
+    __shared__ uint32_t h[kRadix];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t base = blockIdx.x * kSortTile;
+#pragma unroll
+    for (int r = 0; r < kItems; r++) {
+        const uint32_t idx = base + r * kSortThreads + threadIdx.x;
+        if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 0xffu], 1u);
+    }
+    __syncthreads();
+    hist[(size_t)threadIdx.x * num_tiles + blockIdx.x] = h[threadIdx.x];
+}
+
+// exclusive scan of m entries by one block of 1024 threads
+__global__ void __launch_bounds__(1024) k_scan(uint32_t *__restrict__ data, uint32_t m)
+{
+    __shared__ uint32_t sums[1024];
+    const uint32_t per = (m + 1023) / 1024;
+    const uint32_t lo = threadIdx.x * per;
+    const uint32_t hi = min(lo + per, m);
+    uint32_t s = 0;
+    for (uint32_t i = lo; i < hi; i++) s += data[i];
+    sums[threadIdx.x] = s;
+    __syncthreads();
+    // Hillis-Steele inclusive scan over 1024 partial sums
+    for (int off = 1; off < 1024; off <<= 1) {
+        const uint32_t v = (threadIdx.x >= (unsigned)off) ? sums[threadIdx.x - off] : 0u;
+        __syncthreads();
+        sums[threadIdx.x] += v;
+        __syncthreads();
+    }
+    uint32_t run = sums[threadIdx.x] - s;   // exclusive prefix of this chunk
+    for (uint32_t i = lo; i < hi; i++) {
+        const uint32_t v = data[i];
+        data[i] = run;
+        run += v;
+    }
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_scatter(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin,
+                                                         uint32_t *__restrict__ kout, uint32_t *__restrict__ vout,
+                                                         uint32_t n, int shift, const uint32_t *__restrict__ scanned,
+                                                         uint32_t num_tiles)
+{
+    __shared__ uint32_t base[kRadix];
+    __shared__ uint32_t run[kRadix];
+    __shared__ uint32_t wcnt[kWarps][kRadix];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    base[t] = scanned[(size_t)t * num_tiles + blockIdx.x];
+    run[t] = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; w++) wcnt[w][t] = 0;
+    __syncthreads();
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    const uint32_t tile0 = blockIdx.x * kSortTile;
+    for (int r = 0; r < kItems; r++) {
+        const uint32_t idx = tile0 + r * kSortThreads + t;
+        const bool valid = idx < n;
+        const uint32_t key = valid ? kin[idx] : 0u;
+        const uint32_t val = valid ? vin[idx] : 0u;
+        const uint32_t d = valid ? ((key >> shift) & 0xffu) : 0x100u;
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t lrank = __popc(peers & lt_mask);
+        const bool leader = lane == (__ffs(peers) - 1);
+        if (valid && leader) wcnt[warp][d] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+            uint32_t pre = run[d];
+            for (int w = 0; w < warp; w++) pre += wcnt[w][d];
+            const uint32_t dst = base[d] + pre + lrank;
+            kout[dst] = key;
+            vout[dst] = val;
+        }
+        __syncthreads();
+        uint32_t s = 0;
+#pragma unroll
+        for (int w = 0; w < kWarps; w++) {
+            s += wcnt[w][t];
+            wcnt[w][t] = 0;
+        }
+        run[t] += s;
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+bool radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *keys2, uint32_t *vals2, uint32_t n, int key_bits,
+                      uint32_t *hist, uint32_t num_tiles, cudaStream_t s)
+{
+    if (n == 0) return false;
+    const uint32_t tiles = (n + kSortTile - 1) / kSortTile;
+    (void)num_tiles;
+    bool swapped = false;
+    uint32_t *ki = keys, *vi = vals, *ko = keys2, *vo = vals2;
+    for (int shift = 0; shift < key_bits; shift += 8) {
+        k_hist<<<tiles, kSortThreads, 0, s>>>(ki, n, shift, hist, tiles);
+        k_scan<<<1, 1024, 0, s>>>(hist, kRadix * tiles);
+        k_scatter<<<tiles, kSortThreads, 0, s>>>(ki, vi, ko, vo, n, shift, hist, tiles);
+        uint32_t *tk = ki, *tv = vi;
+        ki = ko; vi = vo; ko = tk; vo = tv;
+        swapped = !swapped;
+    }
+    return swapped;
+}
+
+}  // namespace sphgb

@@ -1,0 +1,132 @@
+// Internal structures shared by the host orchestration (api.cu) and the kernel
+// translation units.  Not part of the public ABI (include/sphgb300.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sph_common.cuh"
+
+namespace sphgb {
+
+// Scalars that live in device memory so that a captured step can be replayed
+// without host updates.  All solver control (iteration counters, convergence
+// flags, the CFL step size) is decided on the device.
+struct StepScalars {
+    double dt;          // step size of the current step (used by kick / position update)
+    double dt_next;     // CFL result, used by the pressure solve and the next step
+    double time;
+    double dt_used;     // step size the last completed step used
+    double avg_err;     // pressure solve
+    double avg_err_v;   // divergence solve
+    double cg_rhs2, cg_thresh, cg_res2, cg_absnew, cg_alpha, cg_beta, cg_err;
+    unsigned iters, iters_v, iters_cg;
+    unsigned cont;      // 1 while the running solver loop continues
+    unsigned cg_state;  // 0 running, 1 converged / no iteration, 2 zero right-hand side
+    unsigned maxvel_bits;
+    unsigned flags;     // bit 0 list overflow, bit 1 non-finite velocity
+    unsigned max_nf, max_nb;
+    unsigned prev_iters;
+    unsigned pad[3];
+};
+
+constexpr unsigned kFlagOverflow = 1u;
+constexpr unsigned kFlagNonFinite = 2u;
+
+template <class T> struct DevParams {
+    Kernel<T> K;
+    T V, mass, rho0, eps;
+    T gx, gy, gz;
+    T xsph, xsph_b;
+    T mu, mub, vd, h2;            // Weiler: mu = nu rho0, d = 10, h^2 (support)
+    double max_error, max_error_v;
+    double cfl_factor, cfl_min, cfl_max, radius;
+    double visc_tol;
+    unsigned min_iter, max_iter, max_iter_v, visc_max_iter;
+    int cfl_method, visc_on, div_on;
+    // grid
+    T ox, oy, oz, inv_cell;
+    int dimx, dimy, dimz;
+    uint32_t n, nb, capf, capb;
+};
+
+template <class T> struct DevBufs {
+    using v4 = v4_t<T>;
+    // state, current order
+    v4 *x, *v, *vdiff;
+    float4 *xlo;                 // FP32 mode: low part of the double-float position
+    T *kappa, *kappa_v;
+    uint32_t *id;
+    // state, alternate (gather target)
+    v4 *x2, *v2, *vdiff2;
+    float4 *xlo2;
+    T *kappa2, *kappa_v2;
+    uint32_t *id2;
+    // per-step fields
+    v4 *a, *pa;
+    T *density, *factor, *dadv;
+    uint32_t *nf, *nbn;
+    uint32_t *lf, *lb;
+    // cell grid
+    uint32_t *key, *key2, *perm, *perm2, *cellid, *cellid2;
+    uint32_t *cstart, *cend;
+    uint32_t *bcstart, *bcend;
+    v4 *xb;                      // sorted boundary positions, w = volume
+    T *bscratch;                 // nb scratch values (boundary volume set-up)
+    uint32_t *bid;               // upload index of each sorted boundary particle
+    // CG
+    v4 *cg_x, *cg_r, *cg_p, *cg_z, *cg_t;
+    v4 *inv0, *inv1, *inv2;
+    // reductions
+    double *partials;
+    unsigned *counter;
+    StepScalars *sc;
+    // radix sort scratch
+    uint32_t *hist;
+    uint32_t num_tiles;
+};
+
+// ---- launchers (defined in kernels.cu / sort.cu, instantiated for float and double)
+template <class T> void launch_keys(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
+template <class T> void launch_gather(const DevParams<T> &P, const DevBufs<T> &B, const uint32_t *perm, cudaStream_t s);
+template <class T> void launch_cell_ranges(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
+template <class T> void launch_build(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
+template <class T> void launch_pressure_accel(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s);
+template <class T> void launch_jacobi(const DevParams<T> &P, const DevBufs<T> &B, bool div,
+                                      cudaGraphConditionalHandle h, bool use_handle, cudaStream_t s);
+template <class T> void launch_solver_finalize(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s);
+template <class T> void launch_xsph(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
+template <class T> void launch_visc_setup(const DevParams<T> &P, const DevBufs<T> &B,
+                                          cudaGraphConditionalHandle h, bool use_handle, cudaStream_t s);
+template <class T> void launch_cg_matvec(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
+template <class T> void launch_cg_update(const DevParams<T> &P, const DevBufs<T> &B,
+                                         cudaGraphConditionalHandle h, bool use_handle, cudaStream_t s);
+template <class T> void launch_cg_p(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
+template <class T> void launch_kick(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
+template <class T> void launch_press_init(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
+template <class T> void launch_integrate(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
+template <class T> void launch_step_begin(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
+template <class T> void launch_loop_begin(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s);
+template <class T> void launch_boundary_volume(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
+template <class T> void launch_boundary_keys(const DevParams<T> &P, const DevBufs<T> &B, const v4_t<T> *xb_in,
+                                             uint32_t *keys, uint32_t *vals, cudaStream_t s);
+template <class T> void launch_boundary_gather(const DevParams<T> &P, const DevBufs<T> &B, const v4_t<T> *xb_in,
+                                               const uint32_t *perm, const uint32_t *cells, cudaStream_t s);
+template <class T> void launch_scatter_field(const DevParams<T> &P, const DevBufs<T> &B, int field, void *out,
+                                             int out_dtype, cudaStream_t s);
+template <class T> void launch_upload_field(const DevParams<T> &P, const DevBufs<T> &B, int field, const void *in,
+                                            int in_dtype, const uint32_t *inv, cudaStream_t s);
+template <class T> void launch_init_state(const DevParams<T> &P, const DevBufs<T> &B, const double *x,
+                                          const double *v, const uint32_t *id, cudaStream_t s);
+void launch_inverse_perm(const uint32_t *id, uint32_t *inv, uint32_t n, cudaStream_t s);
+void launch_lists_to_ids(const uint32_t *list, const uint32_t *cnt, uint32_t cap, const uint32_t *id,
+                         const uint32_t *inv, const uint32_t *bid, int kind, const uint32_t *offsets,
+                         uint32_t *out, uint32_t n, cudaStream_t s);
+
+// radix sort of (key, value) pairs, LSD, 8-bit digits, stable.  keys/vals are
+// ping-ponged with keys2/vals2; returns true if the result ended in keys2/vals2.
+bool radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *keys2, uint32_t *vals2, uint32_t n,
+                      int key_bits, uint32_t *hist, uint32_t num_tiles, cudaStream_t s);
+constexpr uint32_t kSortTile = 2048;   // items per radix-sort tile (256 threads x 8)
+
+}  // namespace sphgb

@@ -1,0 +1,292 @@
+"""ctypes binding of libsphgb300.so (include/sphgb300.h).
+
+There is no CPU fallback: if the library cannot be loaded, or no CUDA device is
+visible, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+SPHGB_ABI_VERSION = 1
+OK = 0
+ERR_NAMES = {1: "ARGUMENT", 2: "CUDA", 3: "CAPACITY", 4: "NONFINITE", 5: "STATE", 6: "GRID"}
+
+PRECISION_FP32 = 0
+PRECISION_FP64 = 1
+
+FIELDS = {
+    "position": (0, 3),
+    "velocity": (1, 3),
+    "acceleration": (2, 3),
+    "density": (3, 1),
+    "factor": (4, 1),
+    "advected density": (5, 1),
+    "p / rho^2": (6, 1),
+    "p_v / rho^2": (7, 1),
+    "pressure acceleration": (8, 3),
+    "velocity difference": (9, 3),
+    "id": (10, 1),
+    "factor raw": (11, 1),
+    "fluid neighbors": (12, 1),
+    "boundary neighbors": (13, 1),
+    "boundary volume": (14, 1),
+    "boundary position": (15, 3),
+}
+DTYPE_F32, DTYPE_F64, DTYPE_U32 = 0, 1, 2
+
+
+class SphgbError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"sphgb error {code} ({ERR_NAMES.get(code, '?')}): {msg}")
+        self.code = code
+
+
+class Config(ctypes.Structure):
+    _fields_ = [
+        ("abi_version", ctypes.c_int),
+        ("device", ctypes.c_int),
+        ("precision", ctypes.c_int),
+        ("max_fluid_neighbors", ctypes.c_uint32),
+        ("max_boundary_neighbors", ctypes.c_uint32),
+        ("use_graph", ctypes.c_int),
+    ]
+
+
+class Params(ctypes.Structure):
+    _fields_ = [
+        ("particle_radius", ctypes.c_double),
+        ("density0", ctypes.c_double),
+        ("gravity", ctypes.c_double * 3),
+        ("cfl_method", ctypes.c_int),
+        ("cfl_factor", ctypes.c_double),
+        ("cfl_min_time_step", ctypes.c_double),
+        ("cfl_max_time_step", ctypes.c_double),
+        ("min_iterations", ctypes.c_uint32),
+        ("max_iterations", ctypes.c_uint32),
+        ("max_error", ctypes.c_double),
+        ("enable_divergence_solver", ctypes.c_int),
+        ("max_iterations_v", ctypes.c_uint32),
+        ("max_error_v", ctypes.c_double),
+        ("xsph", ctypes.c_double),
+        ("xsph_boundary", ctypes.c_double),
+        ("viscosity_method", ctypes.c_int),
+        ("viscosity", ctypes.c_double),
+        ("viscosity_boundary", ctypes.c_double),
+        ("visco_max_iter", ctypes.c_uint32),
+        ("visco_max_error", ctypes.c_double),
+    ]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [
+        ("iterations", ctypes.c_uint32),
+        ("iterations_v", ctypes.c_uint32),
+        ("visco_iterations", ctypes.c_uint32),
+        ("max_fluid_neighbors", ctypes.c_uint32),
+        ("max_boundary_neighbors", ctypes.c_uint32),
+        ("flags", ctypes.c_uint32),
+        ("avg_density_err", ctypes.c_double),
+        ("avg_density_err_v", ctypes.c_double),
+        ("visco_error", ctypes.c_double),
+        ("dt_used", ctypes.c_double),
+        ("dt_next", ctypes.c_double),
+        ("time", ctypes.c_double),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+EXPORTS = [
+    "sphgb_abi_version", "sphgb_create", "sphgb_destroy", "sphgb_last_error", "sphgb_default_params",
+    "sphgb_set_params", "sphgb_get_params", "sphgb_upload_boundary", "sphgb_upload_boundary_f32",
+    "sphgb_upload_fluid", "sphgb_upload_fluid_f32", "sphgb_set_time_step", "sphgb_get_time_step",
+    "sphgb_set_time", "sphgb_step", "sphgb_sync", "sphgb_download", "sphgb_upload_field", "sphgb_neighbors",
+    "sphgb_num_particles",
+]
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Load libsphgb300.so (building it in-tree first if needed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_missing and not _build.up_to_date():
+        _build.build()
+    if not os.path.exists(_build.LIB):
+        raise RuntimeError("libsphgb300.so is missing; run splishsplash_gb300.build.build()")
+    L = ctypes.CDLL(_build.LIB)
+    vp, u32, i32, dbl = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int, ctypes.c_double
+    L.sphgb_abi_version.restype = i32
+    L.sphgb_create.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(vp)]
+    L.sphgb_destroy.argtypes = [vp]
+    L.sphgb_last_error.argtypes = [vp]
+    L.sphgb_last_error.restype = ctypes.c_char_p
+    L.sphgb_default_params.argtypes = [ctypes.POINTER(Params)]
+    L.sphgb_set_params.argtypes = [vp, ctypes.POINTER(Params)]
+    L.sphgb_get_params.argtypes = [vp, ctypes.POINTER(Params)]
+    L.sphgb_upload_boundary.argtypes = [vp, vp, u32]
+    L.sphgb_upload_boundary_f32.argtypes = [vp, vp, u32]
+    L.sphgb_upload_fluid.argtypes = [vp, vp, vp, vp, u32]
+    L.sphgb_upload_fluid_f32.argtypes = [vp, vp, vp, vp, u32]
+    L.sphgb_set_time_step.argtypes = [vp, dbl]
+    L.sphgb_get_time_step.argtypes = [vp, ctypes.POINTER(dbl)]
+    L.sphgb_set_time.argtypes = [vp, dbl]
+    L.sphgb_step.argtypes = [vp, ctypes.POINTER(Stats)]
+    L.sphgb_sync.argtypes = [vp, ctypes.POINTER(Stats)]
+    L.sphgb_download.argtypes = [vp, i32, vp, i32]
+    L.sphgb_upload_field.argtypes = [vp, i32, vp, i32]
+    L.sphgb_neighbors.argtypes = [vp, i32, vp, vp, ctypes.c_size_t]
+    L.sphgb_num_particles.argtypes = [vp, ctypes.POINTER(u32), ctypes.POINTER(u32)]
+    for name in EXPORTS:
+        if name != "sphgb_last_error":
+            getattr(L, name).restype = i32
+    _lib = L
+    return L
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def params_from(sp) -> Params:
+    """SPHParams (scene-key names) -> sphgb_params."""
+    q = Params()
+    q.particle_radius = sp.particleRadius
+    q.density0 = sp.density0
+    q.gravity = (ctypes.c_double * 3)(*sp.gravitation)
+    q.cfl_method = sp.cflMethod
+    q.cfl_factor = sp.cflFactor
+    q.cfl_min_time_step = sp.cflMinTimeStepSize
+    q.cfl_max_time_step = sp.cflMaxTimeStepSize
+    q.min_iterations = sp.minIterations
+    q.max_iterations = sp.maxIterations
+    q.max_error = sp.maxError
+    q.enable_divergence_solver = int(sp.enableDivergenceSolver)
+    q.max_iterations_v = sp.maxIterationsV
+    q.max_error_v = sp.maxErrorV
+    q.xsph = sp.xsph
+    q.xsph_boundary = sp.xsphBoundary
+    q.viscosity_method = sp.viscosityMethod
+    q.viscosity = sp.viscosity
+    q.viscosity_boundary = sp.viscosityBoundary
+    q.visco_max_iter = sp.viscoMaxIter
+    q.visco_max_error = sp.viscoMaxError
+    return q
+
+
+class Context:
+    """One device-resident fluid model + static boundary (one sphgb_ctx)."""
+
+    def __init__(self, precision: str = "fp32", device: int = 0, use_graph: bool = False,
+                 max_fluid_neighbors: int = 0, max_boundary_neighbors: int = 0):
+        self.L = load()
+        cfg = Config()
+        cfg.abi_version = SPHGB_ABI_VERSION
+        cfg.device = device
+        cfg.precision = PRECISION_FP64 if precision == "fp64" else PRECISION_FP32
+        cfg.max_fluid_neighbors = max_fluid_neighbors
+        cfg.max_boundary_neighbors = max_boundary_neighbors
+        cfg.use_graph = int(use_graph)
+        h = ctypes.c_void_p()
+        rc = self.L.sphgb_create(ctypes.byref(cfg), ctypes.byref(h))
+        if rc != OK:
+            raise SphgbError(rc, "sphgb_create failed (no CUDA device?)")
+        self.h = h
+        self.precision = precision
+
+    def _check(self, rc):
+        if rc != OK:
+            raise SphgbError(rc, self.L.sphgb_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.sphgb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, sp):
+        self._check(self.L.sphgb_set_params(self.h, ctypes.byref(params_from(sp))))
+
+    def get_params(self) -> Params:
+        q = Params()
+        self._check(self.L.sphgb_get_params(self.h, ctypes.byref(q)))
+        return q
+
+    def upload_boundary(self, xb):
+        xb = np.ascontiguousarray(xb, dtype=np.float64)
+        self._check(self.L.sphgb_upload_boundary(self.h, _p(xb), xb.shape[0]))
+
+    def upload_fluid(self, x, v, ids=None):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        idp = None if ids is None else np.ascontiguousarray(ids, dtype=np.uint32)
+        self._check(self.L.sphgb_upload_fluid(self.h, _p(x), _p(v), _p(idp), x.shape[0]))
+
+    def set_time_step(self, dt):
+        self._check(self.L.sphgb_set_time_step(self.h, float(dt)))
+
+    def get_time_step(self):
+        d = ctypes.c_double()
+        self._check(self.L.sphgb_get_time_step(self.h, ctypes.byref(d)))
+        return d.value
+
+    def set_time(self, t):
+        self._check(self.L.sphgb_set_time(self.h, float(t)))
+
+    def step(self, wait: bool = True):
+        st = Stats()
+        self._check(self.L.sphgb_step(self.h, ctypes.byref(st) if wait else None))
+        return st.as_dict() if wait else None
+
+    def sync(self):
+        st = Stats()
+        self._check(self.L.sphgb_sync(self.h, ctypes.byref(st)))
+        return st.as_dict()
+
+    def num_particles(self):
+        n, nb = ctypes.c_uint32(), ctypes.c_uint32()
+        self._check(self.L.sphgb_num_particles(self.h, ctypes.byref(n), ctypes.byref(nb)))
+        return n.value, nb.value
+
+    def download(self, name: str, dtype=np.float64) -> np.ndarray:
+        fid, comp = FIELDS[name]
+        n, nb = self.num_particles()
+        m = nb if name.startswith("boundary") and name != "boundary neighbors" else n
+        if name in ("id", "fluid neighbors", "boundary neighbors"):
+            dtype = np.uint32
+        dt = {np.dtype(np.float32): DTYPE_F32, np.dtype(np.float64): DTYPE_F64,
+              np.dtype(np.uint32): DTYPE_U32}[np.dtype(dtype)]
+        out = np.zeros((m, comp) if comp > 1 else (m,), dtype=dtype)
+        self._check(self.L.sphgb_download(self.h, fid, _p(out), dt))
+        return out
+
+    def upload_field(self, name: str, values):
+        fid, comp = FIELDS[name]
+        a = np.ascontiguousarray(values, dtype=np.float64)
+        self._check(self.L.sphgb_upload_field(self.h, fid, _p(a), DTYPE_F64))
+
+    def neighbors(self, kind: int = 0):
+        """CSR (offsets, indices) of the last step's lists, in particle-id numbering."""
+        n, _ = self.num_particles()
+        off = np.zeros(n + 1, np.uint32)
+        self._check(self.L.sphgb_neighbors(self.h, kind, _p(off), None, 0))
+        idx = np.zeros(max(1, int(off[-1])), np.uint32)
+        self._check(self.L.sphgb_neighbors(self.h, kind, _p(off), _p(idx), idx.size))
+        return off, idx[: int(off[-1])]

@@ -1,0 +1,197 @@
+"""Parity of the CUDA path (through the C ABI) against the FP64 CPU oracle.
+
+Protocol: the same state (positions/velocities/warm starts rounded to float32 so
+both sides start from identical values) and the same dt; one step on each side;
+comparison by particle id.  Bars (max relative error):
+  density 1e-5, velocity after one step 1e-4 (denominator max(|v|, 1e-3 m/s)),
+  alpha 1e-4 (floor: median |alpha|), kappa/kappa_v 1e-3 of max|kappa|,
+  neighbour sets bit-exact (float predicate, self excluded).
+FP64 device mode is held to 1e-9.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from splishsplash_gb300 import scenes
+from splishsplash_gb300.dfsph import TimeStepDFSPH
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b, floor):
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b)) / np.maximum(np.abs(np.asarray(b)), floor)))
+
+
+def relv(a, b, floor):
+    d = np.linalg.norm(np.asarray(a) - np.asarray(b), axis=-1)
+    return float(np.max(d / np.maximum(np.linalg.norm(np.asarray(b), axis=-1), floor)))
+
+
+def f32(a):
+    return np.asarray(a, np.float64).astype(np.float32).astype(np.float64)
+
+
+def advanced_state(scene, steps):
+    """Run the oracle `steps` steps and return a float32-representable state."""
+    sim = oracle.OracleSim(scene)
+    for _ in range(steps):
+        sim.step()
+    return dict(x=f32(sim.x), v=f32(sim.v), kappa=f32(sim.kappa), kappa_v=f32(sim.kappa_v),
+                vdiff=f32(sim.vdiff), dt=sim.dt, time=sim.st.time, iterations=sim.st.iterations)
+
+
+def oracle_from_state(scene, state):
+    sim = oracle.OracleSim(scene)
+    sim.x[:] = state["x"]
+    sim.v[:] = state["v"]
+    sim.kappa[:] = state["kappa"]
+    sim.kappa_v[:] = state["kappa_v"]
+    sim.vdiff[:] = state["vdiff"]
+    sim.dt = state["dt"]
+    sim.st.iterations = state["iterations"]
+    return sim
+
+
+def gpu_from_state(scene, state, precision="fp32", use_graph=False):
+    ts = TimeStepDFSPH(scene, precision=precision, use_graph=use_graph)
+    m = ts.getFluidModel()
+    m.setFieldBuffer("position", state["x"])
+    m.setFieldBuffer("velocity", state["v"])
+    m.setFieldBuffer("p / rho^2", state["kappa"])
+    m.setFieldBuffer("p_v / rho^2", state["kappa_v"])
+    m.setFieldBuffer("velocity difference", state["vdiff"])
+    ts.setTimeStepSize(state["dt"])
+    return ts
+
+
+def compare(ts, sim, st_gpu, tol_scale=1.0):
+    m = ts.getFluidModel()
+    so = sim.stats()
+    assert st_gpu["iterations"] == so["iterations"], (st_gpu, so)
+    assert st_gpu["iterations_v"] == so["iterations_v"], (st_gpu, so)
+    rho = m.getFieldBuffer("density")
+    assert rel(rho, sim.density, 1e-6 * 1000) < 1e-5 * tol_scale
+    alpha = m.getFieldBuffer("factor raw")
+    assert rel(alpha, sim.factor_raw, np.median(np.abs(sim.factor_raw))) < 1e-4 * tol_scale
+    v = m.getFieldBuffer("velocity")
+    assert relv(v, sim.v, 1e-3) < 1e-4 * tol_scale
+    x = m.getFieldBuffer("position")
+    assert np.max(np.abs(x - sim.x)) < 1e-7 * tol_scale + 1e-6 * tol_scale * np.max(np.abs(sim.x))
+    kap = m.getFieldBuffer("p / rho^2")
+    if np.max(np.abs(sim.kappa)) > 0:
+        assert np.max(np.abs(kap - sim.kappa)) <= 1e-3 * tol_scale * np.max(np.abs(sim.kappa))
+    kv = m.getFieldBuffer("p_v / rho^2")
+    if np.max(np.abs(sim.kappa_v)) > 0:
+        assert np.max(np.abs(kv - sim.kappa_v)) <= 1e-3 * tol_scale * np.max(np.abs(sim.kappa_v))
+    assert st_gpu["dt_next"] == pytest.approx(so["dt"], rel=1e-5 * tol_scale)
+    assert st_gpu["time"] == pytest.approx(so["time"], rel=1e-12)
+
+
+def test_boundary_volume_matches_oracle():
+    sc = scenes.small_block(counts=(6, 6, 6)).as_float32()
+    ts = TimeStepDFSPH(sc)
+    Vb = ts.ctx.download("boundary volume")
+    sim = oracle.OracleSim(sc)
+    assert rel(Vb, sim.Vb, 1e-12) < 1e-6
+    ts.close()
+
+
+@pytest.mark.parametrize("jitter", [0.01, 0.0])
+def test_neighbor_sets_bit_exact(jitter):
+    sc = scenes.small_block(counts=(12, 10, 12), jitter=jitter, box=(1.0, 1.0, 1.0)).as_float32()
+    ts = TimeStepDFSPH(sc)
+    ts.step()
+    h = sc.params.supportRadius
+    for kind, (pts, same) in enumerate(((sc.x, True), (sc.xb, False))):
+        off_g, idx_g = ts.ctx.neighbors(kind)
+        off_o, idx_o = oracle.neighbors(sc.x, pts, h, same, fp32=True)
+        np.testing.assert_array_equal(off_g, off_o)
+        for i in range(sc.n):
+            np.testing.assert_array_equal(np.sort(idx_g[off_g[i]:off_g[i + 1]]), idx_o[off_o[i]:off_o[i + 1]])
+    ts.close()
+
+
+def test_first_step_matches_oracle():
+    sc = scenes.small_block(counts=(10, 10, 10), box=(0.8, 0.8, 0.8)).as_float32()
+    ts = TimeStepDFSPH(sc, use_graph=False)
+    st = ts.step()
+    sim = oracle.OracleSim(sc)
+    sim.step()
+    compare(ts, sim, st)
+    ts.close()
+
+
+@pytest.mark.parametrize("viscosity", [False, True])
+def test_step_from_compressed_state(viscosity):
+    sc = scenes.small_block(counts=(12, 12, 12), box=(0.8, 1.0, 0.8), viscosity=viscosity).as_float32()
+    state = advanced_state(sc, 60)
+    sim = oracle_from_state(sc, state)
+    ts = gpu_from_state(sc, state)
+    st = ts.step()
+    sim.step()
+    assert sim.stats()["iterations"] >= 2
+    compare(ts, sim, st)
+    if viscosity:
+        assert st["visco_iterations"] == sim.stats()["visco_iterations"]
+        vd = ts.getFluidModel().getFieldBuffer("velocity difference")
+        assert relv(vd, sim.vdiff, 1e-3) < 1e-3
+    ts.close()
+
+
+def test_fp64_device_path_matches_oracle_tightly():
+    sc = scenes.small_block(counts=(10, 10, 10), box=(0.8, 1.0, 0.8), viscosity=True).as_float32()
+    state = advanced_state(sc, 40)
+    sim = oracle_from_state(sc, state)
+    ts = gpu_from_state(sc, state, precision="fp64")
+    st = ts.step()
+    sim.step()
+    compare(ts, sim, st, tol_scale=1e-5)
+    ts.close()
+
+
+def test_graph_and_host_loops_agree_bitwise():
+    sc = scenes.small_block(counts=(10, 12, 10), box=(0.8, 1.0, 0.8), viscosity=True).as_float32()
+    outs = []
+    for graph in (False, True):
+        ts = TimeStepDFSPH(sc, use_graph=graph)
+        stats = [ts.step() for _ in range(25)]
+        m = ts.getFluidModel()
+        outs.append((m.getFieldBuffer("position"), m.getFieldBuffer("velocity"), m.getFieldBuffer("p / rho^2"),
+                     [(s["iterations"], s["iterations_v"], s["visco_iterations"]) for s in stats]))
+        ts.close()
+    for a, b in zip(outs[0], outs[1]):
+        if isinstance(a, list):
+            assert a == b
+        else:
+            np.testing.assert_array_equal(a, b)
+
+
+def test_repeat_runs_are_deterministic():
+    sc = scenes.small_block(counts=(10, 10, 10), box=(0.8, 0.8, 0.8)).as_float32()
+    res = []
+    for _ in range(2):
+        ts = TimeStepDFSPH(sc, use_graph=True)
+        for _ in range(20):
+            ts.step()
+        res.append(ts.getFluidModel().getFieldBuffer("position"))
+        ts.close()
+    np.testing.assert_array_equal(res[0], res[1])
+
+
+def test_dambreak_8k_tracks_oracle_statistically():
+    """50 steps of the 8k dam break: average density error under the solver tolerance and the
+    kinetic-energy curve within 2% of the oracle's."""
+    sc = scenes.dambreak_8k().as_float32()
+    ts = TimeStepDFSPH(sc, use_graph=True)
+    sim = oracle.OracleSim(sc)
+    ke_g, ke_o = [], []
+    for _ in range(50):
+        st = ts.step()
+        sim.step()
+        assert st["avg_density_err"] <= 0.01 * 0.01 * 1000 + 1e-9 or st["iterations"] == 100
+        v = ts.getFluidModel().getFieldBuffer("velocity")
+        ke_g.append(0.5 * np.sum(v * v))
+        ke_o.append(0.5 * np.sum(sim.v * sim.v))
+    ke_g, ke_o = np.array(ke_g), np.array(ke_o)
+    assert np.max(np.abs(ke_g - ke_o) / np.maximum(ke_o, 1e-3 * ke_o.max())) < 0.02
+    ts.close()
