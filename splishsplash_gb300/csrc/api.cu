@@ -310,7 +310,7 @@ template <class T> int prepare(sphgb_ctx *c)
 template <class T> void enqueue_solver_loop_body(sphgb_ctx *c, const DevParams<T> &P, const DevBufs<T> &B, bool div,
                                                  cudaGraphConditionalHandle h, bool use_handle, cudaStream_t s)
 {
-    launch_pressure_accel<T>(P, B, div, s);
+    launch_pressure_accel<T>(P, B, div, s, h, use_handle);
     launch_jacobi<T>(P, B, div, h, use_handle, s);
 }
 
@@ -348,10 +348,11 @@ template <class T> int step_host_loop(sphgb_ctx *c)
     if (P.div_on) {
         launch_loop_begin<T>(P, B1, true, s);
         if (P.max_iter_v > 0) {
+            unsigned guard = 0;
             do {
                 enqueue_solver_loop_body<T>(c, P, B1, true, 0, false, s);
                 if ((rc = read_cont(c, &cont))) return rc;
-            } while (cont);
+            } while (cont && ++guard <= P.max_iter_v);
         }
         launch_solver_finalize<T>(P, B1, true, s);
     }
@@ -359,7 +360,8 @@ template <class T> int step_host_loop(sphgb_ctx *c)
     if (P.visc_on) {
         launch_visc_setup<T>(P, B1, 0, false, s);
         if ((rc = read_cont(c, &cont))) return rc;
-        while (cont) {
+        unsigned guard = 0;
+        while (cont && guard++ <= P.visc_max_iter) {
             launch_cg_matvec<T>(P, B1, s);
             launch_cg_update<T>(P, B1, 0, false, s);
             if ((rc = read_cont(c, &cont))) return rc;
@@ -371,10 +373,11 @@ template <class T> int step_host_loop(sphgb_ctx *c)
     launch_press_init<T>(P, B1, s);
     launch_loop_begin<T>(P, B1, false, s);
     if (P.max_iter > 0) {
+        unsigned guard = 0;
         do {
             enqueue_solver_loop_body<T>(c, P, B1, false, 0, false, s);
             if ((rc = read_cont(c, &cont))) return rc;
-        } while (cont);
+        } while (cont && ++guard <= P.max_iter);
     }
     launch_solver_finalize<T>(P, B1, false, s);
     launch_integrate<T>(P, B1, s);
@@ -474,7 +477,7 @@ template <class T> int build_graph(sphgb_ctx *c, int parity, cudaGraphExec_t *ou
                 cudaGraph_t bodyg = np.conditional.phGraph_out[0];
                 e = cudaStreamBeginCaptureToGraph(c->body_stream, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
                 if (e == cudaSuccess) {
-                    launch_cg_matvec<T>(P, B1, c->body_stream);
+                    launch_cg_matvec<T>(P, B1, c->body_stream, hcg, true);
                     launch_cg_update<T>(P, B1, hcg, true, c->body_stream);
                     launch_cg_p<T>(P, B1, c->body_stream);
                     e = cudaStreamEndCapture(c->body_stream, &bodyg);
@@ -555,6 +558,7 @@ int fill_stats(sphgb_ctx *c, sphgb_stats *st)
     if (h.flags & kFlagOverflow)
         return fail(c, SPHGB_ERR_CAPACITY, "neighbour list capacity exceeded (raise max_fluid/boundary_neighbors)");
     if (h.flags & kFlagNonFinite) return fail(c, SPHGB_ERR_NONFINITE, "non-finite velocity");
+    if (h.flags & kFlagLoopGuard) return fail(c, SPHGB_ERR_STATE, "a device solver loop exceeded its iteration bound");
     return SPHGB_OK;
 }
 
@@ -799,6 +803,16 @@ int sphgb_upload_boundary_f32(sphgb_ctx *c, const float *xb, uint32_t nb)
 int sphgb_upload_fluid(sphgb_ctx *c, const double *x, const double *v, const uint32_t *id, uint32_t n)
 {
     if (!c || (n && (!x || !v))) return SPHGB_ERR_ARGUMENT;
+    if (id) {
+        // ids index the host arrays on download: they must be a permutation of 0..n-1
+        std::vector<char> seen(n, 0);
+        for (uint32_t i = 0; i < n; i++) {
+            if (id[i] >= n || seen[id[i]]) return fail(c, SPHGB_ERR_ARGUMENT, "particle ids must be a permutation of 0..n-1");
+            seen[id[i]] = 1;
+        }
+    }
+    for (size_t k = 0; k < (size_t)n * 3; k++)
+        if (!std::isfinite(x[k]) || !std::isfinite(v[k])) return fail(c, SPHGB_ERR_NONFINITE, "non-finite fluid state");
     cudaSetDevice(c->cfg.device);
     // keep the staged boundary across the re-allocation of the fluid buffers
     std::vector<double> xb;

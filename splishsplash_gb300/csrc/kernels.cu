@@ -260,9 +260,27 @@ __device__ __forceinline__ V3<T> pressure_accel_i(const DevParams<T> &P, const D
     return ai;
 }
 
-template <class T>
-__global__ void __launch_bounds__(kBlock) k_pressure_accel(DevParams<T> P, DevBufs<T> B, const T *__restrict__ kap)
+// Termination guard of a device-side loop: the first kernel of every loop body
+// counts body executions; past the bound (which the solver's own decision never
+// reaches) it clears the loop condition and raises a flag, so a loop can never
+// run on if its convergence decision was lost.
+__device__ __forceinline__ void loop_guard(StepScalars *sc, unsigned limit, cudaGraphConditionalHandle h, int use_handle)
 {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const unsigned g = ++sc->loop_guard;
+        if (g > limit) {
+            sc->flags |= kFlagLoopGuard;
+            sc->cont = 0;
+            if (use_handle) cudaGraphSetConditional(h, 0u);
+        }
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_pressure_accel(DevParams<T> P, DevBufs<T> B, const T *__restrict__ kap,
+                                                            unsigned limit, cudaGraphConditionalHandle h, int use_handle)
+{
+    loop_guard(B.sc, limit, h, use_handle);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     stv(B.pa, i, pack(pressure_accel_i(P, B, i, kap), T(0)));
@@ -374,6 +392,7 @@ __global__ void k_step_begin(StepScalars *sc)
 {
     if (threadIdx.x == 0) {
         sc->flags = 0;
+        sc->loop_guard = 0;
         sc->max_nf = 0;
         sc->max_nb = 0;
         sc->maxvel_bits = 0;
@@ -390,6 +409,7 @@ __global__ void k_loop_begin(StepScalars *sc, int div, unsigned max_iter)
         if (div) { sc->iters_v = 0; sc->avg_err_v = 0.0; }
         else { sc->iters = 0; sc->avg_err = 0.0; }
         sc->cont = max_iter > 0 ? 1u : 0u;
+        sc->loop_guard = 0;
     }
 }
 
@@ -565,6 +585,7 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T
         sc->cg_rhs2 = tot.v[0];
         sc->iters_cg = 0;
         sc->cg_err = 0.0;
+        sc->loop_guard = 0;
         if (tot.v[0] == 0.0) {
             sc->cg_state = 2;
         } else {
@@ -589,8 +610,10 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T
 
 // tmp = A p and p.tmp -> alpha (ConjugateGradient.h:74-76)
 template <class T>
-__global__ void __launch_bounds__(kBlock) k_cg_matvec(DevParams<T> P, DevBufs<T> B, ReduceSlot slot)
+__global__ void __launch_bounds__(kBlock) k_cg_matvec(DevParams<T> P, DevBufs<T> B, ReduceSlot slot,
+                                                       cudaGraphConditionalHandle h, int use_handle)
 {
+    loop_guard(B.sc, P.visc_max_iter + 1, h, use_handle);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     DSum<1> mine;
     mine.v[0] = 0.0;
@@ -1042,9 +1065,11 @@ template <class T> void launch_build(const DevParams<T> &P, const DevBufs<T> &B,
 {
     if (P.n) k_build<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
 }
-template <class T> void launch_pressure_accel(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s)
+template <class T> void launch_pressure_accel(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s,
+                                              cudaGraphConditionalHandle h, bool use_handle)
 {
-    if (P.n) k_pressure_accel<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B, div ? B.kappa_v : B.kappa);
+    const unsigned limit = (div ? P.max_iter_v : P.max_iter) + 1;
+    if (P.n) k_pressure_accel<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B, div ? B.kappa_v : B.kappa, limit, h, use_handle ? 1 : 0);
 }
 template <class T>
 void launch_jacobi(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaGraphConditionalHandle h, bool use_handle,
@@ -1081,11 +1106,12 @@ void launch_visc_setup(const DevParams<T> &P, const DevBufs<T> &B, cudaGraphCond
     ReduceSlot slot{B.partials, B.counter};
     k_visc_setup<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B, slot, h, use_handle ? 1 : 0);
 }
-template <class T> void launch_cg_matvec(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
+template <class T> void launch_cg_matvec(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s,
+                                         cudaGraphConditionalHandle h, bool use_handle)
 {
     if (!P.n) return;
     ReduceSlot slot{B.partials, B.counter};
-    k_cg_matvec<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B, slot);
+    k_cg_matvec<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B, slot, h, use_handle ? 1 : 0);
 }
 template <class T>
 void launch_cg_update(const DevParams<T> &P, const DevBufs<T> &B, cudaGraphConditionalHandle h, bool use_handle,
@@ -1160,7 +1186,8 @@ void launch_lists_to_ids(const uint32_t *list, const uint32_t *cnt, uint32_t cap
     template void launch_gather<T>(const DevParams<T> &, const DevBufs<T> &, const uint32_t *, cudaStream_t);       \
     template void launch_cell_ranges<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                    \
     template void launch_build<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                          \
-    template void launch_pressure_accel<T>(const DevParams<T> &, const DevBufs<T> &, bool, cudaStream_t);           \
+    template void launch_pressure_accel<T>(const DevParams<T> &, const DevBufs<T> &, bool, cudaStream_t,            \
+                                           cudaGraphConditionalHandle, bool);                                       \
     template void launch_jacobi<T>(const DevParams<T> &, const DevBufs<T> &, bool, cudaGraphConditionalHandle, bool, \
                                    cudaStream_t);                                                                   \
     template void launch_solver_finalize<T>(const DevParams<T> &, const DevBufs<T> &, bool, cudaStream_t);          \
@@ -1169,7 +1196,8 @@ void launch_lists_to_ids(const uint32_t *list, const uint32_t *cnt, uint32_t cap
     template void launch_xsph<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                           \
     template void launch_visc_setup<T>(const DevParams<T> &, const DevBufs<T> &, cudaGraphConditionalHandle, bool,  \
                                        cudaStream_t);                                                               \
-    template void launch_cg_matvec<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                      \
+    template void launch_cg_matvec<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t,                       \
+                                      cudaGraphConditionalHandle, bool);                                            \
     template void launch_cg_update<T>(const DevParams<T> &, const DevBufs<T> &, cudaGraphConditionalHandle, bool,   \
                                       cudaStream_t);                                                                \
     template void launch_cg_p<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                           \

@@ -27,11 +27,13 @@ struct StepScalars {
     unsigned flags;     // bit 0 list overflow, bit 1 non-finite velocity
     unsigned max_nf, max_nb;
     unsigned prev_iters;
-    unsigned pad[3];
+    unsigned loop_guard;   // body executions of the running device-side loop
+    unsigned pad[2];
 };
 
 constexpr unsigned kFlagOverflow = 1u;
 constexpr unsigned kFlagNonFinite = 2u;
+constexpr unsigned kFlagLoopGuard = 4u;   // a device loop ran past its iteration bound and was stopped
 
 template <class T> struct DevParams {
     Kernel<T> K;
@@ -91,14 +93,16 @@ template <class T> void launch_keys(const DevParams<T> &P, const DevBufs<T> &B, 
 template <class T> void launch_gather(const DevParams<T> &P, const DevBufs<T> &B, const uint32_t *perm, cudaStream_t s);
 template <class T> void launch_cell_ranges(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
 template <class T> void launch_build(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
-template <class T> void launch_pressure_accel(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s);
+template <class T> void launch_pressure_accel(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s,
+                                              cudaGraphConditionalHandle h = 0, bool use_handle = false);
 template <class T> void launch_jacobi(const DevParams<T> &P, const DevBufs<T> &B, bool div,
                                       cudaGraphConditionalHandle h, bool use_handle, cudaStream_t s);
 template <class T> void launch_solver_finalize(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s);
 template <class T> void launch_xsph(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
 template <class T> void launch_visc_setup(const DevParams<T> &P, const DevBufs<T> &B,
                                           cudaGraphConditionalHandle h, bool use_handle, cudaStream_t s);
-template <class T> void launch_cg_matvec(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
+template <class T> void launch_cg_matvec(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s,
+                                         cudaGraphConditionalHandle h = 0, bool use_handle = false);
 template <class T> void launch_cg_update(const DevParams<T> &P, const DevBufs<T> &B,
                                          cudaGraphConditionalHandle h, bool use_handle, cudaStream_t s);
 template <class T> void launch_cg_p(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
