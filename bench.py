@@ -1,0 +1,377 @@
+#!/usr/bin/env python
+"""Benchmark: DFSPH particle-steps/s on the 1M-particle dam break (one GB300).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (single-GPU configuration of the headline metric): 128x64x128 =
+1,048,576 fluid particles, r = 0.01 m, jitter +/-0.01 r, in a 6x3x3 m box of
+625,002 Akinci2012 boundary particles; DFSPH with the divergence solver, XSPH
+0.01, Weiler2018 viscosity nu = 0.01 (CG tol 1e-3), CFL (factor 1, dt in
+[1e-4, 5e-3]).  Synthetic seeded input; nothing is skipped inside a step.
+
+One JSON line on stdout.  `value` = fluid particles x timed steps / summed
+device time of the steps (CUDA events on the library's own stream, L2 flushed
+between steps), inputs resident in HBM.  `e2e` = the same metric through the
+C-ABI with host buffers: each step uploads positions/velocities from pinned
+host memory, steps, and downloads positions, velocities, density and both
+pressure warm starts.  `roofline` = the dominant kernel (by event-timed share
+of a profiled run) against the measured HBM copy bandwidth.  `cpu_baseline` =
+the CPU restatement (FP32 build, OpenMP over all host cores) timed for a
+bounded sample from the GPU's state.
+
+--impl reference times that CPU restatement of the reference's step (the
+reference library itself cannot be built: its build needs external projects
+that are not in its tree) on the same workload, all host threads.
+
+--gpus N > 1 (torchrun): independent replicas, one per GPU (the step does not
+shard); value = total particle-steps / max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DFSPH particle-steps/s at 1M; learned vs plain warm start at 0.01% rho error"
+UNIT = "particle-steps/s"
+WORKLOAD = "dambreak_1m"
+
+
+def baseline_metric():
+    try:
+        with open(os.path.join(ROOT, "BASELINE.json")) as f:
+            return json.load(f)["metric"]
+    except Exception:
+        return METRIC
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def workload_config(scene):
+    p = scene.params
+    return {
+        "workload": f"{WORKLOAD}: {scene.n} fluid + {scene.nb} Akinci2012 boundary particles, r={p.particleRadius}, "
+                    f"Weiler2018 nu={p.viscosity}, XSPH {p.xsph}, DFSPH maxError {p.maxError}% / maxErrorV "
+                    f"{p.maxErrorV}%, CFL factor {p.cflFactor} dt in [{p.cflMinTimeStepSize}, {p.cflMaxTimeStepSize}]",
+        "fluid_particles": scene.n,
+        "boundary_particles": scene.nb,
+        "precision": "fp32 bulk, fp64 reductions/dt/time/positions",
+        "l2": "flushed between timed steps (256 MB device write)",
+    }
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index=0):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+        self.index = index
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def run_oracle_sample(scene, state, budget_s, threads):
+    """FP32 CPU restatement from `state`; at least one step, then as many as fit in budget_s."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # CPU baseline only
+
+    sim = oracle.OracleSim(scene, precision="f32", num_threads=threads)
+    if state is not None:
+        sim.x[:] = state["x"]
+        sim.v[:] = state["v"]
+        sim.kappa[:] = state["kappa"]
+        sim.kappa_v[:] = state["kappa_v"]
+        sim.vdiff[:] = state["vdiff"]
+        sim.dt = state["dt"]
+    t0 = time.perf_counter()
+    steps = 0
+    iters = []
+    while True:
+        sim.step()
+        steps += 1
+        st = sim.stats()
+        iters.append((st["iterations"], st["iterations_v"], st["visco_iterations"]))
+        if time.perf_counter() - t0 >= budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return scene.n * steps / dt, steps, dt, iters
+
+
+def run_reference(args):
+    from splishsplash_gb300 import scenes
+
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    scene = scenes.dambreak_1m()
+    threads = cpu_cores()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    sim = oracle.OracleSim(scene, precision="f32", num_threads=threads)
+    t_w = time.perf_counter()
+    warm_done = 0
+    for _ in range(args.warmup):
+        sim.step()
+        warm_done += 1
+        if time.perf_counter() - t_w > args.cpu_warmup_budget:
+            break
+    t0 = time.perf_counter()
+    steps = 0
+    for _ in range(args.steps):
+        sim.step()
+        steps += 1
+        if time.perf_counter() - t0 > args.cpu_budget:
+            break
+    el = time.perf_counter() - t0
+    value = scene.n * steps / el
+    sample = (f"{steps} of {args.steps} requested steps after {warm_done} warm-up steps of the full {scene.n}-particle "
+              f"scene (stops once {args.cpu_budget:.0f} s of timed CPU work is exceeded)")
+    line = {
+        "impl": "reference", "metric": baseline_metric(), "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": steps, "warmup": warm_done, "ms_per_step": 1e3 * el / max(steps, 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam break)",
+        "config": workload_config(scene),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "CPU restatement of the reference DFSPH step (oracle/sph_oracle.c, FP32 build, OpenMP); the "
+                "reference library itself needs external projects absent from its tree and is not built",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=190)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--profile-steps", type=int, default=4)
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--cpu-warmup-budget", type=float, default=60.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--only-timed", action="store_true",
+                    help="run warm-up and the device-resident timed steps only (profiling captures)")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+
+    from splishsplash_gb300 import bytes_model, scenes
+    from splishsplash_gb300.dfsph import TimeStepDFSPH
+
+    scene = scenes.dambreak_1m()
+    ts = TimeStepDFSPH(scene, precision="fp32", use_graph=True, device=local)
+    ext = torch.cuda.ExternalStream(ts.ctx.stream())
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
+
+    for _ in range(args.warmup):
+        ts.step()
+
+    # ---------------- device-resident timed region ----------------
+    clocks = Clocks(local)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    iters = []
+    launches = 0
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks.start()
+    t_wall = time.perf_counter()
+    for k in range(args.steps):
+        with torch.cuda.stream(ext):
+            flush.zero_()
+            evs[k][0].record(ext)
+        st = ts.step()
+        with torch.cuda.stream(ext):
+            evs[k][1].record(ext)
+        iters.append((st["iterations"], st["iterations_v"], st["visco_iterations"]))
+        launches += int(st["kernel_launches"])
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    dev_s = sum(a.elapsed_time(b) for a, b in evs) / 1e3
+    t_max = dev_s
+    if dist:
+        t = torch.tensor([dev_s], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+        dist.barrier()
+    value = world * scene.n * args.steps / t_max
+    if args.only_timed:
+        if rank == 0:
+            print(json.dumps({"metric": baseline_metric(), "value": value, "unit": UNIT, "steps": args.steps,
+                              "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
+                              "note": "timed steps only"}), flush=True)
+        ts.close()
+        return
+
+    # ---------------- end-to-end through the C ABI with host buffers ----------------
+    n = scene.n
+    pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()
+    hx, hv = pin((n, 3), torch.float32), pin((n, 3), torch.float32)
+    hrho, hk, hkv = pin((n,), torch.float32), pin((n,), torch.float32), pin((n,), torch.float32)
+    ts.ctx.download("position", out=hx)
+    ts.ctx.download("velocity", out=hv)
+    torch.cuda.synchronize()
+    e2e_steps = max(1, args.e2e_steps)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ts.ctx.upload_field("position", hx)
+        ts.ctx.upload_field("velocity", hv)
+        ts.step()
+        ts.ctx.download("position", out=hx)
+        ts.ctx.download("velocity", out=hv)
+        ts.ctx.download("density", out=hrho)
+        ts.ctx.download("p / rho^2", out=hk)
+        ts.ctx.download("p_v / rho^2", out=hkv)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": world * n * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 2 * n * 3 * 4,
+           "d2h_bytes_per_step": 2 * n * 3 * 4 + 3 * n * 4, "steps": e2e_steps}
+
+    # ---------------- per-kernel event timing (roofline) ----------------
+    ts.ctx.profile(True)
+    ts.ctx.profile_reset()
+    for _ in range(max(1, args.profile_steps)):
+        ts.step()
+    prof = ts.ctx.profile_read()
+    ts.ctx.profile(False)
+    nf = float(np.mean(ts.ctx.download("fluid neighbors")))
+    nb = float(np.mean(ts.ctx.download("boundary neighbors")))
+    total_ms = sum(ms for _, ms in prof.values())
+    kernels = {}
+    for name, (cnt, ms) in prof.items():
+        if cnt == 0:
+            continue
+        avg = ms / cnt
+        byts = bytes_model.per_launch(name, n, nf, nb)
+        kernels[name] = {"launches": cnt, "avg_ms": avg, "share": ms / total_ms if total_ms else 0.0,
+                         "algorithmic_bytes": byts, "gbs": byts / (avg * 1e-3) / 1e9 if avg > 0 else 0.0}
+    dom = max(kernels, key=lambda k: kernels[k]["share"])
+    peak, peak_kind = peaks()
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", f"dram_bytes_{dom}.txt")
+    if os.path.exists(tf):
+        try:
+            traffic = float(open(tf).read().split()[0])
+        except Exception:
+            traffic = None
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": kernels[dom]["gbs"], "peak": peak, "unit": "GB/s",
+                "frac": kernels[dom]["gbs"] / peak, "peak_source": peak_kind, "traffic": traffic,
+                "algorithmic_bytes_per_launch": kernels[dom]["algorithmic_bytes"],
+                "avg_launch_ms": kernels[dom]["avg_ms"], "share_of_step": kernels[dom]["share"],
+                "mean_neighbors": {"fluid": nf, "boundary": nb}}
+
+    # ---------------- CPU baseline (rank 0, N = 1) ----------------
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        state = {k: ts.ctx.download(f) for k, f in (("x", "position"), ("v", "velocity"), ("kappa", "p / rho^2"),
+                                                     ("kappa_v", "p_v / rho^2"), ("vdiff", "velocity difference"))}
+        state["dt"] = ts.getTimeStepSize()
+        threads = cpu_cores()
+        v_cpu, s_cpu, t_cpu, it_cpu = run_oracle_sample(scene, state, args.cpu_budget, threads)
+        cpu = {"value": v_cpu, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{s_cpu} step(s) of the full scene from the GPU state after the timed region, {t_cpu:.1f} s "
+                         f"(FP32 build of the CPU restatement, OpenMP); solver iterations {it_cpu}"}
+
+    if rank == 0:
+        it = np.array(iters)
+        line = {
+            "metric": baseline_metric(), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam break)",
+            "config": workload_config(scene), "e2e": e2e, "gpu_launches": launches,
+            "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+            "wall_ms_per_step": 1e3 * wall / args.steps,
+            "solver_iterations_mean": {"pressure": float(it[:, 0].mean()), "divergence": float(it[:, 1].mean()),
+                                       "viscosity_cg": float(it[:, 2].mean())},
+            "kernels": kernels,
+        }
+        print(json.dumps(line), flush=True)
+    ts.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -98,6 +98,7 @@ typedef struct sphgb_stats {
     double dt_used;                  /* step size used for the kick and the position update */
     double dt_next;                  /* CFL step size (used by the pressure solve) */
     double time;                     /* simulated time after the step */
+    uint64_t kernel_launches;        /* kernels this step launched on the GPU */
 } sphgb_stats;
 
 /* field ids for sphgb_download / sphgb_upload_field; names are the reference's field names */
@@ -164,6 +165,17 @@ int sphgb_neighbors(sphgb_ctx *ctx, int kind, uint32_t *offsets, uint32_t *indic
 
 /* counts */
 int sphgb_num_particles(const sphgb_ctx *ctx, uint32_t *n, uint32_t *nb);
+
+/* the cudaStream_t every kernel of this context is launched on (for event timing by callers) */
+int sphgb_get_stream(const sphgb_ctx *ctx, void **stream);
+
+/* Per-kernel CUDA-event timing, the device-side counterpart of the reference's
+ * START_TIMING / STOP_TIMING_AVG scopes (Utilities/Timing.h:73-187).  While on,
+ * steps run with host-driven loops so every launch can be bracketed by events.
+ * profile_read walks kernel classes by index until it returns SPHGB_ERR_ARGUMENT. */
+int sphgb_profile_enable(sphgb_ctx *ctx, int on);
+int sphgb_profile_reset(sphgb_ctx *ctx);
+int sphgb_profile_read(const sphgb_ctx *ctx, int index, const char **name, uint64_t *launches, double *total_ms);
 
 #ifdef __cplusplus
 }

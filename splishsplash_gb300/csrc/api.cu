@@ -64,9 +64,69 @@ struct sphgb_ctx {
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
     bool graph_ok = false;
     bool step_pending = false;
+    uint64_t launches_last_step = 0;
+    // per-kernel CUDA-event timing (host-loop mode only)
+    bool profile = false;
+    std::vector<cudaEvent_t> ev_pool;
+    struct Rec { int kid, a, b; };
+    std::vector<Rec> recs;
+    uint64_t prof_count[32] = {};
+    double prof_ms[32] = {};
 };
 
 namespace {
+
+enum KernelId {
+    K_STEP_BEGIN, K_KEYS, K_SORT, K_GATHER, K_CELL_RANGES, K_BUILD, K_LOOP_BEGIN, K_PRESSURE_ACCEL, K_JACOBI,
+    K_SOLVER_FINALIZE, K_XSPH, K_VISC_SETUP, K_CG_MATVEC, K_CG_UPDATE, K_CG_P, K_KICK, K_PRESS_INIT, K_INTEGRATE,
+    K_COUNT
+};
+const char *kKernelNames[K_COUNT] = {
+    "step_begin", "keys", "radix_sort", "gather", "cell_ranges", "build_lists_density_alpha", "loop_begin",
+    "pressure_accel", "jacobi_update", "solver_finalize", "xsph_gravity", "visc_setup", "cg_matvec", "cg_update",
+    "cg_p", "kick_cfl", "press_init", "integrate",
+};
+
+// Brackets the launches of one kernel class with events on the context stream
+// when profiling is on.  Events are resolved after the step (no sync per launch).
+struct ProfScope {
+    sphgb_ctx *c;
+    int kid;
+    int a = -1;
+    ProfScope(sphgb_ctx *c_, int kid_, cudaStream_t s) : c(c_), kid(kid_)
+    {
+        if (!c->profile) return;
+        a = (int)c->recs.size() * 2;
+        while ((int)c->ev_pool.size() < a + 2) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            c->ev_pool.push_back(e);
+        }
+        cudaEventRecord(c->ev_pool[a], s);
+        stream = s;
+    }
+    ~ProfScope()
+    {
+        if (!c->profile || a < 0) return;
+        cudaEventRecord(c->ev_pool[a + 1], stream);
+        c->recs.push_back({kid, a, a + 1});
+    }
+    cudaStream_t stream = nullptr;
+};
+#define PROF(kid, s) ProfScope prof_scope_##kid(c, kid, s)
+
+void prof_resolve(sphgb_ctx *c)
+{
+    if (!c->profile || c->recs.empty()) return;
+    cudaEventSynchronize(c->ev_pool[c->recs.back().b]);
+    for (const auto &r : c->recs) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev_pool[r.a], c->ev_pool[r.b]);
+        c->prof_count[r.kid] += 1;
+        c->prof_ms[r.kid] += ms;
+    }
+    c->recs.clear();
+}
 
 const sphgb_params kDefaults = {
     0.025, 1000.0, {0.0, -9.81, 0.0}, 1, 0.5, 1e-4, 5e-3, 2, 100, 0.01, 1, 100, 0.1, 0.0, 0.0, 0, 0.01, 0.0, 100, 0.01,
@@ -310,8 +370,14 @@ template <class T> int prepare(sphgb_ctx *c)
 template <class T> void enqueue_solver_loop_body(sphgb_ctx *c, const DevParams<T> &P, const DevBufs<T> &B, bool div,
                                                  cudaGraphConditionalHandle h, bool use_handle, cudaStream_t s)
 {
-    launch_pressure_accel<T>(P, B, div, s, h, use_handle);
-    launch_jacobi<T>(P, B, div, h, use_handle, s);
+    {
+        PROF(K_PRESSURE_ACCEL, s);
+        launch_pressure_accel<T>(P, B, div, s, h, use_handle);
+    }
+    {
+        PROF(K_JACOBI, s);
+        launch_jacobi<T>(P, B, div, h, use_handle, s);
+    }
 }
 
 int read_cont(sphgb_ctx *c, unsigned *cont)
@@ -326,14 +392,18 @@ int read_cont(sphgb_ctx *c, unsigned *cont)
 template <class T> void enqueue_prologue(sphgb_ctx *c, const DevParams<T> &P, const DevBufs<T> &B0, const DevBufs<T> &B1,
                                          cudaStream_t s)
 {
-    launch_step_begin<T>(P, B1, s);
-    launch_keys<T>(P, B0, s);
+    { PROF(K_STEP_BEGIN, s); launch_step_begin<T>(P, B1, s); }
+    { PROF(K_KEYS, s); launch_keys<T>(P, B0, s); }
     const uint32_t tiles = (c->n + kSortTile - 1) / kSortTile;
-    const bool sw = radix_sort_pairs(c->key, c->perm, c->key2, c->perm2, c->n, c->key_bits, c->hist, tiles, s);
-    launch_gather<T>(P, B0, sw ? c->perm2 : c->perm, s);
-    cudaMemsetAsync(c->cstart, 0xff, c->ncell * 4, s);
-    launch_cell_ranges<T>(P, B1, s);
-    launch_build<T>(P, B1, s);
+    bool sw;
+    { PROF(K_SORT, s); sw = radix_sort_pairs(c->key, c->perm, c->key2, c->perm2, c->n, c->key_bits, c->hist, tiles, s, &c->sc->launches); }
+    { PROF(K_GATHER, s); launch_gather<T>(P, B0, sw ? c->perm2 : c->perm, s); }
+    {
+        PROF(K_CELL_RANGES, s);
+        cudaMemsetAsync(c->cstart, 0xff, c->ncell * 4, s);
+        launch_cell_ranges<T>(P, B1, s);
+    }
+    { PROF(K_BUILD, s); launch_build<T>(P, B1, s); }
 }
 
 template <class T> int step_host_loop(sphgb_ctx *c)
@@ -346,7 +416,7 @@ template <class T> int step_host_loop(sphgb_ctx *c)
     unsigned cont = 0;
     enqueue_prologue<T>(c, P, B0, B1, s);
     if (P.div_on) {
-        launch_loop_begin<T>(P, B1, true, s);
+        { PROF(K_LOOP_BEGIN, s); launch_loop_begin<T>(P, B1, true, s); }
         if (P.max_iter_v > 0) {
             unsigned guard = 0;
             do {
@@ -354,24 +424,24 @@ template <class T> int step_host_loop(sphgb_ctx *c)
                 if ((rc = read_cont(c, &cont))) return rc;
             } while (cont && ++guard <= P.max_iter_v);
         }
-        launch_solver_finalize<T>(P, B1, true, s);
+        { PROF(K_SOLVER_FINALIZE, s); launch_solver_finalize<T>(P, B1, true, s); }
     }
-    launch_xsph<T>(P, B1, s);
+    { PROF(K_XSPH, s); launch_xsph<T>(P, B1, s); }
     if (P.visc_on) {
-        launch_visc_setup<T>(P, B1, 0, false, s);
+        { PROF(K_VISC_SETUP, s); launch_visc_setup<T>(P, B1, 0, false, s); }
         if ((rc = read_cont(c, &cont))) return rc;
         unsigned guard = 0;
         while (cont && guard++ <= P.visc_max_iter) {
-            launch_cg_matvec<T>(P, B1, s);
-            launch_cg_update<T>(P, B1, 0, false, s);
+            { PROF(K_CG_MATVEC, s); launch_cg_matvec<T>(P, B1, s); }
+            { PROF(K_CG_UPDATE, s); launch_cg_update<T>(P, B1, 0, false, s); }
             if ((rc = read_cont(c, &cont))) return rc;
             if (!cont) break;
-            launch_cg_p<T>(P, B1, s);
+            { PROF(K_CG_P, s); launch_cg_p<T>(P, B1, s); }
         }
     }
-    launch_kick<T>(P, B1, s);
-    launch_press_init<T>(P, B1, s);
-    launch_loop_begin<T>(P, B1, false, s);
+    { PROF(K_KICK, s); launch_kick<T>(P, B1, s); }
+    { PROF(K_PRESS_INIT, s); launch_press_init<T>(P, B1, s); }
+    { PROF(K_LOOP_BEGIN, s); launch_loop_begin<T>(P, B1, false, s); }
     if (P.max_iter > 0) {
         unsigned guard = 0;
         do {
@@ -379,9 +449,10 @@ template <class T> int step_host_loop(sphgb_ctx *c)
             if ((rc = read_cont(c, &cont))) return rc;
         } while (cont && ++guard <= P.max_iter);
     }
-    launch_solver_finalize<T>(P, B1, false, s);
-    launch_integrate<T>(P, B1, s);
+    { PROF(K_SOLVER_FINALIZE, s); launch_solver_finalize<T>(P, B1, false, s); }
+    { PROF(K_INTEGRATE, s); launch_integrate<T>(P, B1, s); }
     CK(cudaGetLastError());
+    prof_resolve(c);
     return SPHGB_OK;
 }
 
@@ -435,6 +506,9 @@ template <class T> int build_graph(sphgb_ctx *c, int parity, cudaGraphExec_t *ou
     const DevBufs<T> B1 = make_bufs<T>(c, 1);
     c->parity = saved;
     cudaStream_t s = c->stream;
+    const bool prof_saved = c->profile;
+    c->profile = false;   // no event records inside the captured graph
+    struct Restore { sphgb_ctx *c; bool v; ~Restore() { c->profile = v; } } restore{c, prof_saved};
     cudaGraph_t graph = nullptr;
     CK(cudaGraphCreate(&graph, 0));
     cudaError_t e = cudaStreamBeginCaptureToGraph(s, graph, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
@@ -515,7 +589,7 @@ template <class T> int do_step(sphgb_ctx *c)
     int rc;
     if (!c->prepared && (rc = prepare<T>(c))) return rc;
     if ((rc = upload_scalars(c))) return rc;
-    if (c->cfg.use_graph) {
+    if (c->cfg.use_graph && !c->profile) {
         if (!c->graph_ok) {
             invalidate_graphs(c);
             if ((rc = build_graph<T>(c, 0, &c->exec[0]))) return rc;
@@ -554,6 +628,7 @@ int fill_stats(sphgb_ctx *c, sphgb_stats *st)
         st->dt_used = h.dt_used;
         st->dt_next = h.dt_next;
         st->time = h.time;
+        st->kernel_launches = h.launches;
     }
     if (h.flags & kFlagOverflow)
         return fail(c, SPHGB_ERR_CAPACITY, "neighbour list capacity exceeded (raise max_fluid/boundary_neighbors)");
@@ -753,6 +828,7 @@ int sphgb_destroy(sphgb_ctx *c)
     if (c->stream) cudaStreamSynchronize(c->stream);
     free_all(c);
     if (c->hsc) cudaFreeHost(c->hsc);
+    for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->body_stream) cudaStreamDestroy(c->body_stream);
     delete c;
@@ -906,6 +982,36 @@ int sphgb_sync(sphgb_ctx *c, sphgb_stats *stats)
     return fill_stats(c, stats);
 }
 
+int sphgb_get_stream(const sphgb_ctx *c, void **stream)
+{
+    if (!c || !stream) return SPHGB_ERR_ARGUMENT;
+    *stream = (void *)c->stream;
+    return SPHGB_OK;
+}
+
+int sphgb_profile_enable(sphgb_ctx *c, int on)
+{
+    if (!c) return SPHGB_ERR_ARGUMENT;
+    c->profile = on != 0;
+    return SPHGB_OK;
+}
+
+int sphgb_profile_reset(sphgb_ctx *c)
+{
+    if (!c) return SPHGB_ERR_ARGUMENT;
+    for (int k = 0; k < K_COUNT; k++) { c->prof_count[k] = 0; c->prof_ms[k] = 0.0; }
+    return SPHGB_OK;
+}
+
+int sphgb_profile_read(const sphgb_ctx *c, int index, const char **name, uint64_t *launches, double *total_ms)
+{
+    if (!c || index < 0 || index >= K_COUNT) return SPHGB_ERR_ARGUMENT;
+    if (name) *name = kKernelNames[index];
+    if (launches) *launches = c->prof_count[index];
+    if (total_ms) *total_ms = c->prof_ms[index];
+    return SPHGB_OK;
+}
+
 int sphgb_num_particles(const sphgb_ctx *c, uint32_t *n, uint32_t *nb)
 {
     if (!c) return SPHGB_ERR_ARGUMENT;
@@ -974,18 +1080,6 @@ int sphgb_upload_field(sphgb_ctx *c, int field, const void *src, int dtype)
     }
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(c->stream));
-    if (field == SPHGB_FIELD_POSITION) {
-        // positions may have moved outside the grid used so far: rebuild it at the next step
-        const double *d = static_cast<const double *>(src);
-        const float *f = static_cast<const float *>(src);
-        for (int k = 0; k < 3; k++) { c->fmin[k] = 1e300; c->fmax[k] = -1e300; }
-        for (uint32_t i = 0; i < c->n; i++)
-            for (int k = 0; k < 3; k++) {
-                const double val = dtype == SPHGB_DTYPE_F64 ? d[3 * (size_t)i + k] : (double)f[3 * (size_t)i + k];
-                c->fmin[k] = std::min(c->fmin[k], val);
-                c->fmax[k] = std::max(c->fmax[k], val);
-            }
-    }
     return SPHGB_OK;
 }
 

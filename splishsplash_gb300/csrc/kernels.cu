@@ -88,6 +88,7 @@ __device__ __forceinline__ void block_max_atomic(uint32_t a, uint32_t b, unsigne
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_keys(DevParams<T> P, DevBufs<T> B)
 {
+    count_launch(&B.sc->launches);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     int cx, cy, cz;
@@ -101,6 +102,7 @@ __global__ void __launch_bounds__(kBlock) k_keys(DevParams<T> P, DevBufs<T> B)
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_gather(DevParams<T> P, DevBufs<T> B, const uint32_t *__restrict__ perm)
 {
+    count_launch(&B.sc->launches);
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= P.n) return;
     const uint32_t s = perm[k];
@@ -116,8 +118,10 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevParams<T> P, DevBufs<T> B,
 
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_cell_ranges(DevParams<T> P, const uint32_t *__restrict__ cellid,
-                                                         uint32_t *__restrict__ cstart, uint32_t *__restrict__ cend, uint32_t n)
+                                                         uint32_t *__restrict__ cstart, uint32_t *__restrict__ cend, uint32_t n,
+                                                         unsigned *lc)
 {
+    count_launch(lc);
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const uint32_t c = cellid[k];
@@ -132,6 +136,7 @@ __global__ void __launch_bounds__(kBlock) k_cell_ranges(DevParams<T> P, const ui
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_build(DevParams<T> P, DevBufs<T> B)
 {
+    count_launch(&B.sc->launches);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const v4_t<T> xi = ldv(B.x, i);
@@ -280,6 +285,7 @@ template <class T>
 __global__ void __launch_bounds__(kBlock) k_pressure_accel(DevParams<T> P, DevBufs<T> B, const T *__restrict__ kap,
                                                             unsigned limit, cudaGraphConditionalHandle h, int use_handle)
 {
+    count_launch(&B.sc->launches);
     loop_guard(B.sc, limit, h, use_handle);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
@@ -319,6 +325,7 @@ template <class T, bool DIV>
 __global__ void __launch_bounds__(kBlock) k_jacobi(DevParams<T> P, DevBufs<T> B, ReduceSlot slot,
                                                      cudaGraphConditionalHandle handle, int use_handle)
 {
+    count_launch(&B.sc->launches);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     double err = 0.0;
     if (i < P.n) {
@@ -376,6 +383,7 @@ __global__ void __launch_bounds__(kBlock) k_jacobi(DevParams<T> P, DevBufs<T> B,
 template <class T, bool DIV>
 __global__ void __launch_bounds__(kBlock) k_solver_finalize(DevParams<T> P, DevBufs<T> B)
 {
+    count_launch(&B.sc->launches);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const T h = (T)(DIV ? B.sc->dt : B.sc->dt_next);
@@ -391,6 +399,7 @@ __global__ void __launch_bounds__(kBlock) k_solver_finalize(DevParams<T> P, DevB
 __global__ void k_step_begin(StepScalars *sc)
 {
     if (threadIdx.x == 0) {
+        sc->launches = 1;
         sc->flags = 0;
         sc->loop_guard = 0;
         sc->max_nf = 0;
@@ -405,6 +414,7 @@ __global__ void k_step_begin(StepScalars *sc)
 template <class T>
 __global__ void k_loop_begin(StepScalars *sc, int div, unsigned max_iter)
 {
+    count_launch(&sc->launches);
     if (threadIdx.x == 0) {
         if (div) { sc->iters_v = 0; sc->avg_err_v = 0.0; }
         else { sc->iters = 0; sc->avg_err = 0.0; }
@@ -422,6 +432,7 @@ __global__ void k_loop_begin(StepScalars *sc, int div, unsigned max_iter)
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_xsph(DevParams<T> P, DevBufs<T> B, int div_on)
 {
+    count_launch(&B.sc->launches);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const T h = (T)B.sc->dt;
@@ -511,6 +522,7 @@ template <class T>
 __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T> B, ReduceSlot slot,
                                                         cudaGraphConditionalHandle handle, int use_handle)
 {
+    count_launch(&B.sc->launches);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     DSum<3> mine;
     mine.v[0] = mine.v[1] = mine.v[2] = 0.0;
@@ -613,6 +625,7 @@ template <class T>
 __global__ void __launch_bounds__(kBlock) k_cg_matvec(DevParams<T> P, DevBufs<T> B, ReduceSlot slot,
                                                        cudaGraphConditionalHandle h, int use_handle)
 {
+    count_launch(&B.sc->launches);
     loop_guard(B.sc, P.visc_max_iter + 1, h, use_handle);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     DSum<1> mine;
@@ -632,6 +645,7 @@ template <class T>
 __global__ void __launch_bounds__(kBlock) k_cg_update(DevParams<T> P, DevBufs<T> B, ReduceSlot slot,
                                                        cudaGraphConditionalHandle handle, int use_handle)
 {
+    count_launch(&B.sc->launches);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     DSum<2> mine;
     mine.v[0] = mine.v[1] = 0.0;
@@ -675,6 +689,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(DevParams<T> P, DevBufs<T>
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_cg_p(DevParams<T> P, DevBufs<T> B)
 {
+    count_launch(&B.sc->launches);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     if (B.sc->cg_state != 0) return;
@@ -693,6 +708,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_p(DevParams<T> P, DevBufs<T> B)
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_kick(DevParams<T> P, DevBufs<T> B)
 {
+    count_launch(&B.sc->launches);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     float m = 0.0f;
     const double hd = B.sc->dt;
@@ -761,6 +777,7 @@ __global__ void __launch_bounds__(kBlock) k_kick(DevParams<T> P, DevBufs<T> B)
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_press_init(DevParams<T> P, DevBufs<T> B)
 {
+    count_launch(&B.sc->launches);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const T h = (T)B.sc->dt_next;
@@ -795,6 +812,7 @@ __global__ void __launch_bounds__(kBlock) k_press_init(DevParams<T> P, DevBufs<T
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_integrate(DevParams<T> P, DevBufs<T> B)
 {
+    count_launch(&B.sc->launches);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const double h = B.sc->dt;
     const double hn = B.sc->dt_next;
@@ -1059,7 +1077,7 @@ template <class T> void launch_gather(const DevParams<T> &P, const DevBufs<T> &B
 }
 template <class T> void launch_cell_ranges(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {
-    if (P.n) k_cell_ranges<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B.cellid, B.cstart, B.cend, P.n);
+    if (P.n) k_cell_ranges<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B.cellid, B.cstart, B.cend, P.n, &B.sc->launches);
 }
 template <class T> void launch_build(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {
@@ -1147,7 +1165,7 @@ template <class T> void launch_boundary_gather(const DevParams<T> &P, const DevB
 {
     if (!P.nb) return;
     k_boundary_gather<T><<<grid_for(P.nb), kBlock, 0, s>>>(P, B, xb_in, perm, const_cast<uint32_t *>(cells));
-    k_cell_ranges<T><<<grid_for(P.nb), kBlock, 0, s>>>(P, cells, B.bcstart, B.bcend, P.nb);
+    k_cell_ranges<T><<<grid_for(P.nb), kBlock, 0, s>>>(P, cells, B.bcstart, B.bcend, P.nb, nullptr);
 }
 template <class T> void launch_boundary_volume(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {

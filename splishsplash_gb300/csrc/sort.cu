@@ -17,8 +17,9 @@ constexpr int kRadix = 256;
 constexpr int kWarps = kSortThreads / 32;
 
 __global__ void __launch_bounds__(kSortThreads) k_hist(const uint32_t *__restrict__ keys, uint32_t n, int shift,
-                                                      uint32_t *__restrict__ hist, uint32_t num_tiles)
+                                                      uint32_t *__restrict__ hist, uint32_t num_tiles, unsigned *lc)
 {
+    count_launch(lc);
     __shared__ uint32_t h[kRadix];
     h[threadIdx.x] = 0;
     __syncthreads();
@@ -33,8 +34,9 @@ __global__ void __launch_bounds__(kSortThreads) k_hist(const uint32_t *__restric
 }
 
 // exclusive scan of m entries by one block of 1024 threads
-__global__ void __launch_bounds__(1024) k_scan(uint32_t *__restrict__ data, uint32_t m)
+__global__ void __launch_bounds__(1024) k_scan(uint32_t *__restrict__ data, uint32_t m, unsigned *lc)
 {
+    count_launch(lc);
     __shared__ uint32_t sums[1024];
     const uint32_t per = (m + 1023) / 1024;
     const uint32_t lo = threadIdx.x * per;
@@ -61,8 +63,9 @@ __global__ void __launch_bounds__(1024) k_scan(uint32_t *__restrict__ data, uint
 __global__ void __launch_bounds__(kSortThreads) k_scatter(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin,
                                                          uint32_t *__restrict__ kout, uint32_t *__restrict__ vout,
                                                          uint32_t n, int shift, const uint32_t *__restrict__ scanned,
-                                                         uint32_t num_tiles)
+                                                         uint32_t num_tiles, unsigned *lc)
 {
+    count_launch(lc);
     __shared__ uint32_t base[kRadix];
     __shared__ uint32_t run[kRadix];
     __shared__ uint32_t wcnt[kWarps][kRadix];
@@ -107,7 +110,7 @@ __global__ void __launch_bounds__(kSortThreads) k_scatter(const uint32_t *__rest
 }  // namespace
 
 bool radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *keys2, uint32_t *vals2, uint32_t n, int key_bits,
-                      uint32_t *hist, uint32_t num_tiles, cudaStream_t s)
+                      uint32_t *hist, uint32_t num_tiles, cudaStream_t s, unsigned *lc)
 {
     if (n == 0) return false;
     const uint32_t tiles = (n + kSortTile - 1) / kSortTile;
@@ -115,9 +118,9 @@ bool radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *keys2, uint32_t 
     bool swapped = false;
     uint32_t *ki = keys, *vi = vals, *ko = keys2, *vo = vals2;
     for (int shift = 0; shift < key_bits; shift += 8) {
-        k_hist<<<tiles, kSortThreads, 0, s>>>(ki, n, shift, hist, tiles);
-        k_scan<<<1, 1024, 0, s>>>(hist, kRadix * tiles);
-        k_scatter<<<tiles, kSortThreads, 0, s>>>(ki, vi, ko, vo, n, shift, hist, tiles);
+        k_hist<<<tiles, kSortThreads, 0, s>>>(ki, n, shift, hist, tiles, lc);
+        k_scan<<<1, 1024, 0, s>>>(hist, kRadix * tiles, lc);
+        k_scatter<<<tiles, kSortThreads, 0, s>>>(ki, vi, ko, vo, n, shift, hist, tiles, lc);
         uint32_t *tk = ki, *tv = vi;
         ki = ko; vi = vo; ko = tk; vo = tv;
         swapped = !swapped;

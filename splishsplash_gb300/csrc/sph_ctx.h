@@ -28,11 +28,17 @@ struct StepScalars {
     unsigned max_nf, max_nb;
     unsigned prev_iters;
     unsigned loop_guard;   // body executions of the running device-side loop
-    unsigned pad[2];
+    unsigned launches;     // kernels launched in the current step (counted on the device)
+    unsigned pad[1];
 };
 
 constexpr unsigned kFlagOverflow = 1u;
 constexpr unsigned kFlagNonFinite = 2u;
+__device__ __forceinline__ void count_launch(unsigned *ctr)
+{
+    if (ctr && blockIdx.x == 0 && threadIdx.x == 0) *ctr += 1u;
+}
+
 constexpr unsigned kFlagLoopGuard = 4u;   // a device loop ran past its iteration bound and was stopped
 
 template <class T> struct DevParams {
@@ -130,7 +136,8 @@ void launch_lists_to_ids(const uint32_t *list, const uint32_t *cnt, uint32_t cap
 // radix sort of (key, value) pairs, LSD, 8-bit digits, stable.  keys/vals are
 // ping-ponged with keys2/vals2; returns true if the result ended in keys2/vals2.
 bool radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *keys2, uint32_t *vals2, uint32_t n,
-                      int key_bits, uint32_t *hist, uint32_t num_tiles, cudaStream_t s);
+                      int key_bits, uint32_t *hist, uint32_t num_tiles, cudaStream_t s,
+                      unsigned *launch_counter = nullptr);
 constexpr uint32_t kSortTile = 2048;   // items per radix-sort tile (256 threads x 8)
 
 }  // namespace sphgb

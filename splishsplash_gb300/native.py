@@ -96,6 +96,7 @@ class Stats(ctypes.Structure):
         ("dt_used", ctypes.c_double),
         ("dt_next", ctypes.c_double),
         ("time", ctypes.c_double),
+        ("kernel_launches", ctypes.c_uint64),
     ]
 
     def as_dict(self):
@@ -107,7 +108,7 @@ EXPORTS = [
     "sphgb_set_params", "sphgb_get_params", "sphgb_upload_boundary", "sphgb_upload_boundary_f32",
     "sphgb_upload_fluid", "sphgb_upload_fluid_f32", "sphgb_set_time_step", "sphgb_get_time_step",
     "sphgb_set_time", "sphgb_step", "sphgb_sync", "sphgb_download", "sphgb_upload_field", "sphgb_neighbors",
-    "sphgb_num_particles",
+    "sphgb_num_particles", "sphgb_get_stream", "sphgb_profile_enable", "sphgb_profile_reset", "sphgb_profile_read",
 ]
 
 _lib = None
@@ -149,6 +150,11 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.sphgb_upload_field.argtypes = [vp, i32, vp, i32]
     L.sphgb_neighbors.argtypes = [vp, i32, vp, vp, ctypes.c_size_t]
     L.sphgb_num_particles.argtypes = [vp, ctypes.POINTER(u32), ctypes.POINTER(u32)]
+    L.sphgb_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
+    L.sphgb_profile_enable.argtypes = [vp, i32]
+    L.sphgb_profile_reset.argtypes = [vp]
+    L.sphgb_profile_read.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_uint64),
+                                     ctypes.POINTER(dbl)]
     for name in EXPORTS:
         if name != "sphgb_last_error":
             getattr(L, name).restype = i32
@@ -265,22 +271,58 @@ class Context:
         self._check(self.L.sphgb_num_particles(self.h, ctypes.byref(n), ctypes.byref(nb)))
         return n.value, nb.value
 
-    def download(self, name: str, dtype=np.float64) -> np.ndarray:
+    def download(self, name: str, dtype=np.float64, out: np.ndarray = None) -> np.ndarray:
+        """Field in particle-id order.  `out` (C-contiguous, right size and dtype, e.g. a
+        pinned buffer) is filled in place when given."""
         fid, comp = FIELDS[name]
         n, nb = self.num_particles()
         m = nb if name.startswith("boundary") and name != "boundary neighbors" else n
         if name in ("id", "fluid neighbors", "boundary neighbors"):
             dtype = np.uint32
+        if out is None:
+            out = np.zeros((m, comp) if comp > 1 else (m,), dtype=dtype)
+        if not out.flags["C_CONTIGUOUS"] or out.size != m * comp:
+            raise ValueError("download target must be C-contiguous with n x components elements")
         dt = {np.dtype(np.float32): DTYPE_F32, np.dtype(np.float64): DTYPE_F64,
-              np.dtype(np.uint32): DTYPE_U32}[np.dtype(dtype)]
-        out = np.zeros((m, comp) if comp > 1 else (m,), dtype=dtype)
+              np.dtype(np.uint32): DTYPE_U32}[out.dtype]
         self._check(self.L.sphgb_download(self.h, fid, _p(out), dt))
         return out
 
     def upload_field(self, name: str, values):
+        """Set a field from particle-id ordered values (float32 or float64, no conversion copy)."""
         fid, comp = FIELDS[name]
-        a = np.ascontiguousarray(values, dtype=np.float64)
-        self._check(self.L.sphgb_upload_field(self.h, fid, _p(a), DTYPE_F64))
+        a = np.asarray(values)
+        if a.dtype not in (np.float32, np.float64) or not a.flags["C_CONTIGUOUS"]:
+            a = np.ascontiguousarray(a, dtype=np.float64)
+        dt = DTYPE_F32 if a.dtype == np.float32 else DTYPE_F64
+        self._check(self.L.sphgb_upload_field(self.h, fid, _p(a), dt))
+
+    def stream(self) -> int:
+        """cudaStream_t (as an integer) that every kernel of this context runs on."""
+        p = ctypes.c_void_p()
+        self._check(self.L.sphgb_get_stream(self.h, ctypes.byref(p)))
+        return int(p.value or 0)
+
+    def profile(self, on: bool = True):
+        self._check(self.L.sphgb_profile_enable(self.h, int(on)))
+
+    def profile_reset(self):
+        self._check(self.L.sphgb_profile_reset(self.h))
+
+    def profile_read(self):
+        """{kernel name: (launches, total ms)} of the CUDA-event timing since the last reset."""
+        out = {}
+        k = 0
+        while True:
+            name = ctypes.c_char_p()
+            cnt = ctypes.c_uint64()
+            ms = ctypes.c_double()
+            rc = self.L.sphgb_profile_read(self.h, k, ctypes.byref(name), ctypes.byref(cnt), ctypes.byref(ms))
+            if rc != OK:
+                break
+            out[name.value.decode()] = (int(cnt.value), float(ms.value))
+            k += 1
+        return out
 
     def neighbors(self, kind: int = 0):
         """CSR (offsets, indices) of the last step's lists, in particle-id numbering."""
