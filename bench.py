@@ -212,6 +212,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--cpu-warmup-budget", type=float, default=60.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--host-loops", action="store_true",
+                    help="host-driven solver loops instead of the captured graph (kernels visible to ncu)")
     ap.add_argument("--only-timed", action="store_true",
                     help="run warm-up and the device-resident timed steps only (profiling captures)")
     args = ap.parse_args()
@@ -236,7 +238,7 @@ def main():
     from splishsplash_gb300.dfsph import TimeStepDFSPH
 
     scene = scenes.dambreak_1m()
-    ts = TimeStepDFSPH(scene, precision="fp32", use_graph=True, device=local)
+    ts = TimeStepDFSPH(scene, precision="fp32", use_graph=not args.host_loops, device=local)
     ext = torch.cuda.ExternalStream(ts.ctx.stream())
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
 

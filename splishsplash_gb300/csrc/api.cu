@@ -42,7 +42,7 @@ struct sphgb_ctx {
     void *set_x[2] = {}, *set_v[2] = {}, *set_vdiff[2] = {}, *set_kappa[2] = {}, *set_kappa_v[2] = {};
     float4 *set_xlo[2] = {};
     uint32_t *set_id[2] = {};
-    void *a = nullptr, *pa = nullptr, *density = nullptr, *factor = nullptr, *dadv = nullptr;
+    void *a = nullptr, *pa = nullptr, *xk = nullptr, *bg = nullptr, *density = nullptr, *factor = nullptr, *dadv = nullptr;
     uint32_t *nfc = nullptr, *nbc = nullptr, *lf = nullptr, *lb = nullptr;
     uint32_t *key = nullptr, *key2 = nullptr, *perm = nullptr, *perm2 = nullptr, *cell0 = nullptr, *cell1 = nullptr;
     uint32_t *cstart = nullptr, *cend = nullptr, *bcstart = nullptr, *bcend = nullptr;
@@ -254,6 +254,8 @@ template <class T> DevBufs<T> make_bufs(const sphgb_ctx *c, int view)
     B.id2 = c->set_id[alt];
     B.a = (v4 *)c->a;
     B.pa = (v4 *)c->pa;
+    B.xk = (v4 *)c->xk;
+    B.bg = (v4 *)c->bg;
     B.density = (T *)c->density;
     B.factor = (T *)c->factor;
     B.dadv = (T *)c->dadv;
@@ -658,6 +660,8 @@ template <class T> int init_fluid(sphgb_ctx *c, const double *x, const double *v
     }
     if ((rc = dalloc(c, &c->a, N * vs))) return rc;
     if ((rc = dalloc(c, &c->pa, N * vs))) return rc;
+    if ((rc = dalloc(c, &c->xk, N * vs))) return rc;
+    if ((rc = dalloc(c, &c->bg, N * vs))) return rc;
     if ((rc = dalloc(c, &c->density, N * rs))) return rc;
     if ((rc = dalloc(c, &c->factor, N * rs))) return rc;
     if ((rc = dalloc(c, &c->dadv, N * rs))) return rc;

@@ -48,6 +48,56 @@ template <class T> __device__ __forceinline__ V3<T> gradW(const Kernel<T> &K, co
     return scl(p.r, kernel_gradW_coef(K, p.rl));
 }
 
+// gradW(r) = c r from the squared distance.  FP32: one reciprocal square root
+// (MUFU) instead of a square root and a division; FP64: exact sqrt and division.
+__device__ __forceinline__ float grad_coef_d2(const Kernel<float> &K, float d2)
+{
+    const float rinv = rsqrtf(fmaxf(d2, 1e-36f));
+    const float rl = d2 * rinv;
+    const float q = rl * K.invh;
+    float c;
+    if (q <= 0.5f) {
+        c = K.l * K.invh2 * (3.0f * q - 2.0f);
+    } else {
+        const float f = 1.0f - q;
+        c = -K.l * f * f * K.invh * rinv;
+    }
+    return (rl > 1.0e-9f && q <= 1.0f) ? c : 0.0f;
+}
+__device__ __forceinline__ double grad_coef_d2(const Kernel<double> &K, double d2)
+{
+    return kernel_gradW_coef(K, sqrt(d2));
+}
+
+template <class T> __device__ __forceinline__ V3<T> diff3(const v4_t<T> &a, const v4_t<T> &b)
+{
+    return V3<T>{(T)a.x - (T)b.x, (T)a.y - (T)b.y, (T)a.z - (T)b.z};
+}
+
+// Neighbour loop with U independent index loads, then U dependent gathers, then
+// U computations, so that each thread keeps several loads in flight.
+template <int U, class Ld, class Cp>
+__device__ __forceinline__ void nbr_loop(const uint32_t *__restrict__ L, uint32_t cnt, Ld ld, Cp cp)
+{
+    uint32_t k = 0;
+    for (; k + U <= cnt; k += U) {
+        uint32_t j[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) j[u] = __ldg(L + (k + u) * 32u);
+        decltype(ld(0u)) d[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) d[u] = ld(j[u]);
+#pragma unroll
+        for (int u = 0; u < U; u++) cp(j[u], d[u]);
+    }
+    for (; k < cnt; k++) {
+        const uint32_t jj = __ldg(L + k * 32u);
+        cp(jj, ld(jj));
+    }
+}
+
+constexpr int kUnroll = 4;
+
 __device__ __forceinline__ void cell_coords(uint32_t c, int dimx, int dimy, int &cx, int &cy, int &cz)
 {
     cx = (int)(c % (uint32_t)dimx);
@@ -220,48 +270,46 @@ __global__ void __launch_bounds__(kBlock) k_build(DevParams<T> P, DevBufs<T> B)
     // divergence source (unclamped, as stored by computeDensityChange) and kappa_v warm start
     const T dsrc = divf * P.V + divb;
     B.dadv[i] = dsrc;
+    T kv = B.kappa_v[i];
     if (P.div_on) {
         T densityAdv = dsrc > T(0) ? dsrc : T(0);
         if (nf + nb < 20u) densityAdv = T(0);
         const T invH = T(1) / (T)B.sc->dt;
-        const T kv = B.kappa_v[i];
-        B.kappa_v[i] = densityAdv > T(0) ? T(0.5) * (kv < T(0.5) ? kv : T(0.5)) * invH : T(0);
+        kv = densityAdv > T(0) ? T(0.5) * (kv < T(0.5) ? kv : T(0.5)) * invH : T(0);
+        B.kappa_v[i] = kv;
     }
+    // boundary sums are fixed for the step (static boundary, fixed positions): every
+    // later pass uses them instead of re-walking the boundary list
+    stv(B.bg, i, pack(gb, wb));
+    v4_t<T> xk = xi;
+    xk.w = kv;
+    stv(B.xk, i, xk);
 }
 
 // ==========================================================================
 // DFSPH solver passes
 // ==========================================================================
-// computePressureAccel, scalar path (TimeStepDFSPH.cpp:1299-1367)
+// computePressureAccel, scalar path (TimeStepDFSPH.cpp:1299-1367):
+// a_i = -V sum_j [|k_i + k_j| > eps] (k_i + k_j) gradW_ij - [|k_i| > eps] k_i sum_b V_b gradW_ib
+// with kappa of the running solver read from xk.w and the boundary sum from bg.
 template <class T>
-__device__ __forceinline__ V3<T> pressure_accel_i(const DevParams<T> &P, const DevBufs<T> &B, uint32_t i,
-                                                  const T *__restrict__ kap)
+__device__ __forceinline__ V3<T> pressure_accel_i(const DevParams<T> &P, const DevBufs<T> &B, uint32_t i)
 {
-    const v4_t<T> xi = ldv(B.x, i);
-    const T pi = kap[i];
-    V3<T> ai = mk3<T>(0, 0, 0);
+    const v4_t<T> xi = ldv(B.xk, i);
+    const T pi = (T)xi.w;
+    V3<T> acc = mk3<T>(0, 0, 0);
     const uint32_t nf = min(B.nf[i], P.capf);
-    const uint32_t *Lf = list_ptr(B.lf, i, P.capf);
-    for (uint32_t k = 0; k < nf; k++) {
-        const uint32_t j = Lf[k * 32u];
-        const T psum = pi + kap[j];
-        if (fabs(psum) > P.eps) {
-            const Pair<T> pr = pair_of<T>(xi, ldv(B.x, j));
-            const V3<T> g = gradW(P.K, pr);
-            ai = add(ai, scl(g, -P.V * psum));
-        }
-    }
-    if (fabs(pi) > P.eps) {
-        const uint32_t nb = min(B.nbn[i], P.capb);
-        const uint32_t *Lb = list_ptr(B.lb, i, P.capb);
-        for (uint32_t k = 0; k < nb; k++) {
-            const uint32_t j = Lb[k * 32u];
-            const v4_t<T> xj = ldv(B.xb, j);
-            const Pair<T> pr = pair_of<T>(xi, xj);
-            const V3<T> g = gradW(P.K, pr);
-            ai = add(ai, scl(g, -(T)xj.w * pi));
-        }
-    }
+    nbr_loop<kUnroll>(list_ptr(B.lf, i, P.capf), nf, [&](uint32_t j) { return ldv(B.xk, j); },
+                      [&](uint32_t, const v4_t<T> &xj) {
+                          const T psum = pi + (T)xj.w;
+                          if (fabs(psum) > P.eps) {
+                              const V3<T> r = diff3<T>(xi, xj);
+                              const T c = grad_coef_d2(P.K, dot(r, r)) * psum;
+                              acc = add(acc, scl(r, c));
+                          }
+                      });
+    V3<T> ai = scl(acc, -P.V);
+    if (fabs(pi) > P.eps) ai = sub(ai, scl(xyz<T>(ldv(B.bg, i)), pi));
     return ai;
 }
 
@@ -282,40 +330,34 @@ __device__ __forceinline__ void loop_guard(StepScalars *sc, unsigned limit, cuda
 }
 
 template <class T>
-__global__ void __launch_bounds__(kBlock) k_pressure_accel(DevParams<T> P, DevBufs<T> B, const T *__restrict__ kap,
-                                                            unsigned limit, cudaGraphConditionalHandle h, int use_handle)
+__global__ void __launch_bounds__(kBlock) k_pressure_accel(DevParams<T> P, DevBufs<T> B, unsigned limit,
+                                                            cudaGraphConditionalHandle h, int use_handle)
 {
     count_launch(&B.sc->launches);
     loop_guard(B.sc, limit, h, use_handle);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
-    stv(B.pa, i, pack(pressure_accel_i(P, B, i, kap), T(0)));
+    stv(B.pa, i, pack(pressure_accel_i(P, B, i), T(0)));
 }
 
-// compute_aij_pj, scalar path (TimeStepDFSPH.cpp:1370-1420)
+// compute_aij_pj, scalar path (TimeStepDFSPH.cpp:1370-1420):
+// V sum_j (a_i - a_j).gradW_ij + a_i . sum_b V_b gradW_ib
 template <class T> __device__ __forceinline__ T aij_pj_i(const DevParams<T> &P, const DevBufs<T> &B, uint32_t i)
 {
     const v4_t<T> xi = ldv(B.x, i);
     const V3<T> ai = xyz<T>(ldv(B.pa, i));
-    T accf = T(0), accb = T(0);
+    T accf = T(0);
+    struct XA {
+        v4_t<T> x, a;
+    };
     const uint32_t nf = min(B.nf[i], P.capf);
-    const uint32_t *Lf = list_ptr(B.lf, i, P.capf);
-    for (uint32_t k = 0; k < nf; k++) {
-        const uint32_t j = Lf[k * 32u];
-        const Pair<T> pr = pair_of<T>(xi, ldv(B.x, j));
-        const V3<T> g = gradW(P.K, pr);
-        const V3<T> aj = xyz<T>(ldv(B.pa, j));
-        accf += dot(sub(ai, aj), g);
-    }
-    const uint32_t nb = min(B.nbn[i], P.capb);
-    const uint32_t *Lb = list_ptr(B.lb, i, P.capb);
-    for (uint32_t k = 0; k < nb; k++) {
-        const uint32_t j = Lb[k * 32u];
-        const v4_t<T> xj = ldv(B.xb, j);
-        const Pair<T> pr = pair_of<T>(xi, xj);
-        accb += (T)xj.w * dot(ai, gradW(P.K, pr));
-    }
-    return accf * P.V + accb;
+    nbr_loop<kUnroll>(list_ptr(B.lf, i, P.capf), nf, [&](uint32_t j) { return XA{ldv(B.x, j), ldv(B.pa, j)}; },
+                      [&](uint32_t, const XA &d) {
+                          const V3<T> r = diff3<T>(xi, d.x);
+                          const T c = grad_coef_d2(P.K, dot(r, r));
+                          accf += c * dot(sub(ai, xyz<T>(d.a)), r);
+                      });
+    return accf * P.V + dot(ai, xyz<T>(ldv(B.bg, i)));
 }
 
 // divergenceSolveIteration (TimeStepDFSPH.cpp:621-706) / pressureSolveIteration (:544-619):
@@ -341,6 +383,7 @@ __global__ void __launch_bounds__(kBlock) k_jacobi(DevParams<T> P, DevBufs<T> B,
             const T fac = B.factor[i] * (T(1) / h);
             const T kv = kap[i] - T(0.5) * (si - apj) * fac;
             kap[i] = kv > T(0) ? kv : T(0);
+            store_w(B.xk, i, kap[i]);
             err = -(double)P.rho0 * (double)residuum;
         } else {
             apj *= h * h;
@@ -349,6 +392,7 @@ __global__ void __launch_bounds__(kBlock) k_jacobi(DevParams<T> P, DevBufs<T> B,
             const T fac = B.factor[i] * (T(1) / (h * h));
             const T kv = kap[i] - T(0.5) * (si - apj) * fac;
             kap[i] = kv > T(0) ? kv : T(0);
+            store_w(B.xk, i, kap[i]);
             err = -(double)P.rho0 * (double)residuum;
         }
     }
@@ -387,7 +431,7 @@ __global__ void __launch_bounds__(kBlock) k_solver_finalize(DevParams<T> P, DevB
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const T h = (T)(DIV ? B.sc->dt : B.sc->dt_next);
-    const V3<T> a = pressure_accel_i(P, B, i, DIV ? B.kappa_v : B.kappa);
+    const V3<T> a = pressure_accel_i(P, B, i);
     stv(B.pa, i, pack(a, T(0)));
     v4_t<T> v = ldv(B.v, i);
     v.x += h * a.x;
@@ -442,28 +486,23 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams<T> P, DevBufs<T> B, i
     V3<T> ai = mk3<T>(P.gx, P.gy, P.gz);
     if (P.xsph != T(0)) {
         V3<T> acc = mk3<T>(0, 0, 0);
+        struct XVR {
+            v4_t<T> x, v;
+            T rho;
+        };
         const uint32_t nf = min(B.nf[i], P.capf);
-        const uint32_t *Lf = list_ptr(B.lf, i, P.capf);
-        for (uint32_t k = 0; k < nf; k++) {
-            const uint32_t j = Lf[k * 32u];
-            const Pair<T> pr = pair_of<T>(xi, ldv(B.x, j));
-            const V3<T> vj = xyz<T>(ldv(B.v, j));
-            const T w = (P.mass / B.density[j]) * kernel_W(P.K, pr.rl);
-            acc = add(acc, scl(sub(vi, vj), w));
-        }
+        nbr_loop<kUnroll>(list_ptr(B.lf, i, P.capf), nf,
+                          [&](uint32_t j) { return XVR{ldv(B.x, j), ldv(B.v, j), B.density[j]}; },
+                          [&](uint32_t, const XVR &d) {
+                              const V3<T> r = diff3<T>(xi, d.x);
+                              const T w = (P.mass / d.rho) * kernel_W(P.K, dev_sqrt(dot(r, r)));
+                              acc = add(acc, scl(sub(vi, xyz<T>(d.v)), w));
+                          });
         ai = sub(ai, scl(acc, invH * P.xsph));
     }
     if (P.xsph_b != T(0)) {
-        const T rhoi = B.density[i];
-        T wsum = T(0);
-        const uint32_t nb = min(B.nbn[i], P.capb);
-        const uint32_t *Lb = list_ptr(B.lb, i, P.capb);
-        for (uint32_t k = 0; k < nb; k++) {
-            const uint32_t j = Lb[k * 32u];
-            const v4_t<T> xj = ldv(B.xb, j);
-            const Pair<T> pr = pair_of<T>(xi, xj);
-            wsum += (P.rho0 * (T)xj.w / rhoi) * kernel_W(P.K, pr.rl);
-        }
+        // sum_b (rho0 V_b / rho_i) W_ib from the per-step boundary sum
+        const T wsum = P.rho0 * (T)ldv(B.bg, i).w / B.density[i];
         ai = sub(ai, scl(vi, invH * P.xsph_b * wsum));
     }
     stv(B.a, i, pack(ai, T(0)));
@@ -480,16 +519,20 @@ __device__ __forceinline__ V3<T> weiler_Av(const DevParams<T> &P, const DevBufs<
     const T rhoi = B.density[i];
     V3<T> acc = mk3<T>(0, 0, 0);
     const uint32_t nf = min(B.nf[i], P.capf);
-    const uint32_t *Lf = list_ptr(B.lf, i, P.capf);
     const T eps2 = T(0.01) * P.h2;
-    for (uint32_t k = 0; k < nf; k++) {
-        const uint32_t j = Lf[k * 32u];
-        const Pair<T> pr = pair_of<T>(xi, ldv(B.x, j));
-        const V3<T> g = gradW(P.K, pr);
-        const V3<T> vj = vec_of(j);
-        const T f = P.vd * P.mu * (P.mass / B.density[j]) * dot(sub(vi, vj), pr.r) / (pr.rl * pr.rl + eps2);
-        acc = add(acc, scl(g, f));
-    }
+    struct XVR {
+        v4_t<T> x;
+        V3<T> v;
+        T rho;
+    };
+    nbr_loop<kUnroll>(list_ptr(B.lf, i, P.capf), nf,
+                      [&](uint32_t j) { return XVR{ldv(B.x, j), vec_of(j), B.density[j]}; },
+                      [&](uint32_t, const XVR &d) {
+                          const V3<T> r = diff3<T>(xi, d.x);
+                          const T r2 = dot(r, r);
+                          const T f = P.vd * P.mu * (P.mass / d.rho) * dot(sub(vi, d.v), r) / (r2 + eps2);
+                          acc = add(acc, scl(r, grad_coef_d2(P.K, r2) * f));
+                      });
     if (P.mub != T(0)) {
         const uint32_t nb = min(B.nbn[i], P.capb);
         const uint32_t *Lb = list_ptr(B.lb, i, P.capb);
@@ -783,27 +826,24 @@ __global__ void __launch_bounds__(kBlock) k_press_init(DevParams<T> P, DevBufs<T
     const T h = (T)B.sc->dt_next;
     const v4_t<T> xi = ldv(B.x, i);
     const V3<T> vi = xyz<T>(ldv(B.v, i));
-    T accf = T(0), accb = T(0);
+    T accf = T(0);
+    struct XV {
+        v4_t<T> x, v;
+    };
     const uint32_t nf = min(B.nf[i], P.capf);
-    const uint32_t *Lf = list_ptr(B.lf, i, P.capf);
-    for (uint32_t k = 0; k < nf; k++) {
-        const uint32_t j = Lf[k * 32u];
-        const Pair<T> pr = pair_of<T>(xi, ldv(B.x, j));
-        accf += dot(sub(vi, xyz<T>(ldv(B.v, j))), gradW(P.K, pr));
-    }
-    const uint32_t nb = min(B.nbn[i], P.capb);
-    const uint32_t *Lb = list_ptr(B.lb, i, P.capb);
-    for (uint32_t k = 0; k < nb; k++) {
-        const uint32_t j = Lb[k * 32u];
-        const v4_t<T> xj = ldv(B.xb, j);
-        const Pair<T> pr = pair_of<T>(xi, xj);
-        accb += (T)xj.w * dot(vi, gradW(P.K, pr));
-    }
+    nbr_loop<kUnroll>(list_ptr(B.lf, i, P.capf), nf, [&](uint32_t j) { return XV{ldv(B.x, j), ldv(B.v, j)}; },
+                      [&](uint32_t, const XV &d) {
+                          const V3<T> r = diff3<T>(xi, d.x);
+                          accf += grad_coef_d2(P.K, dot(r, r)) * dot(sub(vi, xyz<T>(d.v)), r);
+                      });
+    const T accb = dot(vi, xyz<T>(ldv(B.bg, i)));
     const T dadv = B.density[i] / P.rho0 + h * (accf * P.V + accb);
     B.dadv[i] = dadv;
     const T invH2 = T(1) / (h * h);
     const T k = B.kappa[i];
-    B.kappa[i] = dadv > T(1) ? T(0.5) * (k < T(0.00025) ? k : T(0.00025)) * invH2 : T(0);
+    const T kn = dadv > T(1) ? T(0.5) * (k < T(0.00025) ? k : T(0.00025)) * invH2 : T(0);
+    B.kappa[i] = kn;
+    store_w(B.xk, i, kn);
 }
 
 // x += h_old v (TimeStepDFSPH.cpp:220-237) accumulated in FP64 (double-float
@@ -1087,7 +1127,7 @@ template <class T> void launch_pressure_accel(const DevParams<T> &P, const DevBu
                                               cudaGraphConditionalHandle h, bool use_handle)
 {
     const unsigned limit = (div ? P.max_iter_v : P.max_iter) + 1;
-    if (P.n) k_pressure_accel<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B, div ? B.kappa_v : B.kappa, limit, h, use_handle ? 1 : 0);
+    if (P.n) k_pressure_accel<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B, limit, h, use_handle ? 1 : 0);
 }
 template <class T>
 void launch_jacobi(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaGraphConditionalHandle h, bool use_handle,

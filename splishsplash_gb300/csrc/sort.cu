@@ -33,30 +33,45 @@ __global__ void __launch_bounds__(kSortThreads) k_hist(const uint32_t *__restric
     hist[(size_t)threadIdx.x * num_tiles + blockIdx.x] = h[threadIdx.x];
 }
 
-// exclusive scan of m entries by one block of 1024 threads
+// Exclusive scan of m entries by one block of 32 warps.  Warp w owns the
+// contiguous chunk [w*C, (w+1)*C) and walks it 32 entries at a time with
+// coalesced loads and warp shuffles; a scan of the 32 chunk totals gives each
+// warp its base.
 __global__ void __launch_bounds__(1024) k_scan(uint32_t *__restrict__ data, uint32_t m, unsigned *lc)
 {
     count_launch(lc);
-    __shared__ uint32_t sums[1024];
-    const uint32_t per = (m + 1023) / 1024;
-    const uint32_t lo = threadIdx.x * per;
-    const uint32_t hi = min(lo + per, m);
+    __shared__ uint32_t tot[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t C = ((m + 31) / 32 + 31) / 32 * 32;   // chunk per warp, multiple of 32
+    const uint32_t lo = min((uint32_t)warp * C, m), hi = min(lo + C, m);
     uint32_t s = 0;
-    for (uint32_t i = lo; i < hi; i++) s += data[i];
-    sums[threadIdx.x] = s;
+    for (uint32_t i = lo + lane; i < hi; i += 32) s += data[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) tot[warp] = s;
     __syncthreads();
-    // Hillis-Steele inclusive scan over 1024 partial sums
-    for (int off = 1; off < 1024; off <<= 1) {
-        const uint32_t v = (threadIdx.x >= (unsigned)off) ? sums[threadIdx.x - off] : 0u;
-        __syncthreads();
-        sums[threadIdx.x] += v;
-        __syncthreads();
+    if (warp == 0) {
+        uint32_t v = tot[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += u;
+        }
+        tot[lane] = v - tot[lane];   // exclusive
     }
-    uint32_t run = sums[threadIdx.x] - s;   // exclusive prefix of this chunk
-    for (uint32_t i = lo; i < hi; i++) {
-        const uint32_t v = data[i];
-        data[i] = run;
-        run += v;
+    __syncthreads();
+    uint32_t run = tot[warp];
+    for (uint32_t base = lo; base < hi; base += 32) {
+        const uint32_t i = base + lane;
+        const uint32_t x = i < hi ? data[i] : 0u;
+        uint32_t v = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += u;
+        }
+        if (i < hi) data[i] = run + v - x;
+        run += __shfl_sync(0xffffffffu, v, 31);
     }
 }
 

@@ -47,6 +47,10 @@ __device__ __forceinline__ void stv(dquad *p, uint32_t i, dquad v)
     q[1] = make_double2(v.z, v.w);
 }
 
+// store only the w lane of element i
+__device__ __forceinline__ void store_w(float4 *p, uint32_t i, float w) { reinterpret_cast<float *>(p + i)[3] = w; }
+__device__ __forceinline__ void store_w(dquad *p, uint32_t i, double w) { p[i].w = w; }
+
 template <class T> __device__ __forceinline__ V3<T> xyz(const v4_t<T> &v) { return V3<T>{(T)v.x, (T)v.y, (T)v.z}; }
 template <class T> __device__ __forceinline__ v4_t<T> pack(V3<T> a, T w)
 {

@@ -72,6 +72,8 @@ template <class T> struct DevBufs {
     uint32_t *id2;
     // per-step fields
     v4 *a, *pa;
+    v4 *xk;                      // x_i with the running solver's kappa_i in w (one gather per pair)
+    v4 *bg;                      // per-particle boundary sums: xyz = sum_b V_b gradW_ib, w = sum_b V_b W_ib
     T *density, *factor, *dadv;
     uint32_t *nf, *nbn;
     uint32_t *lf, *lb;
