@@ -102,6 +102,7 @@ struct ProfScope {
             cudaEventCreate(&e);
             c->ev_pool.push_back(e);
         }
+        launch_delay(s, 20000);   // GPU stays busy while the host enqueues event, kernel, event
         cudaEventRecord(c->ev_pool[a], s);
         stream = s;
     }

@@ -1229,6 +1229,15 @@ template <class T> void launch_init_state(const DevParams<T> &P, const DevBufs<T
 {
     if (P.n) k_init_state<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B, x, v, id);
 }
+// Keeps the GPU busy for about `ns` nanoseconds without touching memory, so that
+// the host can enqueue an event, a kernel and an event back to back behind it
+// (per-kernel event timing without host-submission gaps).  Bounded: one sleep.
+__global__ void k_delay(unsigned ns)
+{
+    if (threadIdx.x == 0) __nanosleep(ns);
+}
+void launch_delay(cudaStream_t s, unsigned ns) { k_delay<<<1, 32, 0, s>>>(ns); }
+
 void launch_inverse_perm(const uint32_t *id, uint32_t *inv, uint32_t n, cudaStream_t s)
 {
     if (n) k_inverse_perm<<<grid_for(n), kBlock, 0, s>>>(id, inv, n);

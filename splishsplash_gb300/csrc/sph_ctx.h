@@ -131,6 +131,7 @@ template <class T> void launch_upload_field(const DevParams<T> &P, const DevBufs
 template <class T> void launch_init_state(const DevParams<T> &P, const DevBufs<T> &B, const double *x,
                                           const double *v, const uint32_t *id, cudaStream_t s);
 void launch_inverse_perm(const uint32_t *id, uint32_t *inv, uint32_t n, cudaStream_t s);
+void launch_delay(cudaStream_t s, unsigned ns);
 void launch_lists_to_ids(const uint32_t *list, const uint32_t *cnt, uint32_t cap, const uint32_t *id,
                          const uint32_t *inv, const uint32_t *bid, int kind, const uint32_t *offsets,
                          uint32_t *out, uint32_t n, cudaStream_t s);

@@ -138,6 +138,20 @@ def test_step_from_compressed_state(viscosity):
     ts.close()
 
 
+def test_boundary_viscosity_and_xsph_boundary_terms():
+    sc = scenes.small_block(counts=(10, 10, 10), box=(0.8, 1.0, 0.8), viscosity=True).as_float32()
+    sc.params.viscosityBoundary = 0.05
+    sc.params.xsphBoundary = 0.1
+    state = advanced_state(sc, 40)
+    sim = oracle_from_state(sc, state)
+    ts = gpu_from_state(sc, state)
+    st = ts.step()
+    sim.step()
+    compare(ts, sim, st)
+    assert st["visco_iterations"] == sim.stats()["visco_iterations"]
+    ts.close()
+
+
 def test_fp64_device_path_matches_oracle_tightly():
     sc = scenes.small_block(counts=(10, 10, 10), box=(0.8, 1.0, 0.8), viscosity=True).as_float32()
     state = advanced_state(sc, 40)
