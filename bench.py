@@ -212,6 +212,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--cpu-warmup-budget", type=float, default=60.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--nz", type=int, default=128,
+                    help="fluid block depth (128 = the 1M workload; smaller for multi-pass profiler captures)")
     ap.add_argument("--host-loops", action="store_true",
                     help="host-driven solver loops instead of the captured graph (kernels visible to ncu)")
     ap.add_argument("--only-timed", action="store_true",
@@ -237,7 +239,7 @@ def main():
     from splishsplash_gb300 import bytes_model, scenes
     from splishsplash_gb300.dfsph import TimeStepDFSPH
 
-    scene = scenes.dambreak_1m()
+    scene = scenes.dambreak_1m(nz=args.nz)
     ts = TimeStepDFSPH(scene, precision="fp32", use_graph=not args.host_loops, device=local)
     ext = torch.cuda.ExternalStream(ts.ctx.stream())
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")

@@ -146,15 +146,17 @@ def dambreak_8k(seed: int = 1000) -> Scene:
     return Scene("dambreak_8k", x, np.zeros_like(x), xb, p, np.zeros(3), np.full(3, 2.0))
 
 
-def dambreak_1m(seed: int = 1001, viscosity: bool = True) -> Scene:
+def dambreak_1m(seed: int = 1001, viscosity: bool = True, nz: int = 128) -> Scene:
     """128x64x128 block (1,048,576), spacing 0.02, r=0.01, in a 6x3x3 m box; walls at 0.012 m
-    (625,002 boundary particles); Weiler2018 viscosity nu=0.01."""
+    (625,002 boundary particles); Weiler2018 viscosity nu=0.01.  `nz` < 128 gives the same
+    scene with a shorter block (profiling captures)."""
     p = SPHParams(particleRadius=0.01, viscosityMethod=6 if viscosity else 0, viscosity=0.01,
                   viscoMaxError=1e-3, viscoMaxIter=100)
     rng = np.random.default_rng(seed)
-    x = fluid_block((128, 64, 128), 0.02, (0.02, 0.02, 0.02), p.particleRadius, rng)
+    x = fluid_block((128, 64, nz), 0.02, (0.02, 0.02, 0.02), p.particleRadius, rng)
     xb = box_walls((0, 0, 0), (6, 3, 3), 0.012)
-    return Scene("dambreak_1m", x, np.zeros_like(x), xb, p, np.zeros(3), np.array([6.0, 3.0, 3.0]))
+    name = "dambreak_1m" if nz == 128 else f"dambreak_128x64x{nz}"
+    return Scene(name, x, np.zeros_like(x), xb, p, np.zeros(3), np.array([6.0, 3.0, 3.0]))
 
 
 def precision_4m(seed: int = 1002) -> Scene:
