@@ -32,14 +32,16 @@ def per_particle(kernel: str, nf: float, nb: float, visc_boundary: bool = False)
         "jacobi_update": 2 * V4 + counts + lists + 2 * S + 2 * S,
         # pressure_accel + v_i r/w
         "solver_finalize": V4 + S + counts + lists + V4 + 2 * V4,
-        # x_i, v_i, density_i, counts, lists (fluid, + boundary when xsphBoundary); writes a_i; kappa_v r/w
-        "xsph_gravity": 2 * V4 + S + counts + IDX * nf + V4 + 2 * S,
-        # x_i, v_i, vdiff_i, density_i, counts, lists; writes 3 inverse rows, x, r, p
-        "visc_setup": 3 * V4 + S + counts + lists_f + 3 * V4 + 3 * V4,
+        # x_i, v_i, density_i, counts, lists (fluid); writes a_i; kappa_v r/w; with viscosity
+        # also reads vDiff_i and writes the CG warm start
+        "xsph_gravity": 2 * V4 + S + counts + IDX * nf + V4 + 2 * S + 2 * V4,
+        # x_i, warm start g_i (+ weight), v_i, density_i, counts, lists; writes 2 symmetric
+        # inverse rows, r, p
+        "visc_setup": 3 * V4 + S + counts + lists_f + 2 * V4 + 2 * V4,
         # x_i, p_i, density_i, counts, lists; writes t_i
         "cg_matvec": 2 * V4 + S + counts + lists_f + V4,
-        # p, t, x, r, 3 inverse rows; writes x, r, z
-        "cg_update": 7 * V4 + 3 * V4,
+        # p, t, x, r, 2 inverse rows; writes x, r, z
+        "cg_update": 6 * V4 + 3 * V4,
         # z, p; writes p
         "cg_p": 3 * V4,
         # a, v, cg x; writes v, a, vdiff

@@ -284,7 +284,6 @@ template <class T> DevBufs<T> make_bufs(const sphgb_ctx *c, int view)
     B.cg_t = (v4 *)c->cg[4];
     B.inv0 = (v4 *)c->inv[0];
     B.inv1 = (v4 *)c->inv[1];
-    B.inv2 = (v4 *)c->inv[2];
     B.partials = c->partials;
     B.counter = c->counter;
     B.sc = c->sc;
@@ -679,7 +678,7 @@ template <class T> int init_fluid(sphgb_ctx *c, const double *x, const double *v
     if ((rc = dalloc(c, &c->cell1, N * 4))) return rc;
     for (int k = 0; k < 5; k++)
         if ((rc = dalloc(c, &c->cg[k], N * vs))) return rc;
-    for (int k = 0; k < 3; k++)
+    for (int k = 0; k < 2; k++)
         if ((rc = dalloc(c, &c->inv[k], N * vs))) return rc;
     const size_t blocks = (N + kBlock - 1) / kBlock;
     if ((rc = dalloc(c, &c->partials, blocks * 4 * sizeof(double)))) return rc;

@@ -69,6 +69,31 @@ __device__ __forceinline__ double grad_coef_d2(const Kernel<double> &K, double d
     return kernel_gradW_coef(K, sqrt(d2));
 }
 
+// W(r) and the gradient coefficient from the squared distance (FP32: one rsqrt)
+__device__ __forceinline__ void kernel_W_coef_d2(const Kernel<float> &K, float d2, float &W, float &c)
+{
+    const float rinv = rsqrtf(fmaxf(d2, 1e-36f));
+    const float rl = d2 * rinv;
+    const float q = rl * K.invh;
+    if (q <= 0.5f) {
+        const float q2 = q * q;
+        W = K.k * (6.0f * q2 * q - 6.0f * q2 + 1.0f);
+        c = K.l * K.invh2 * (3.0f * q - 2.0f);
+    } else {
+        const float f = 1.0f - q;
+        W = K.k * (2.0f * f * f * f);
+        c = -K.l * f * f * K.invh * rinv;
+    }
+    if (!(q <= 1.0f)) W = 0.0f;
+    if (!(rl > 1.0e-9f && q <= 1.0f)) c = 0.0f;
+}
+__device__ __forceinline__ void kernel_W_coef_d2(const Kernel<double> &K, double d2, double &W, double &c)
+{
+    const double rl = sqrt(d2);
+    W = kernel_W(K, rl);
+    c = kernel_gradW_coef(K, rl);
+}
+
 template <class T> __device__ __forceinline__ V3<T> diff3(const v4_t<T> &a, const v4_t<T> &b)
 {
     return V3<T>{(T)a.x - (T)b.x, (T)a.y - (T)b.y, (T)a.z - (T)b.z};
@@ -180,9 +205,14 @@ __global__ void __launch_bounds__(kBlock) k_cell_ranges(DevParams<T> P, const ui
 }
 
 // Build the fluid and boundary neighbour lists of particle i and, in the same
-// pass, compute (TimeStep.cpp:116-169) the density, (TimeStepDFSPH.cpp:1106-1186)
+// kernel, compute (TimeStep.cpp:116-169) the density, (TimeStepDFSPH.cpp:1106-1186)
 // the DFSPH factor alpha, (TimeStepDFSPH.cpp:1247-1295) the divergence source and
 // (TimeStepDFSPH.cpp:402-463) the warm-started kappa_v.
+//
+// Phase 1 scans the 27 surrounding cells with the exact predicate only and appends
+// accepted indices to the lists (cells whose box is farther than h are skipped).
+// Phase 2 walks the fresh lists densely for the kernel sums, so the kernel math
+// does not run inside the divergent candidate loop.
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_build(DevParams<T> P, DevBufs<T> B)
 {
@@ -190,71 +220,99 @@ __global__ void __launch_bounds__(kBlock) k_build(DevParams<T> P, DevBufs<T> B)
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const v4_t<T> xi = ldv(B.x, i);
-    const V3<T> vi = xyz<T>(ldv(B.v, i));
     int cx, cy, cz;
     cell_coords(B.cellid[i], P.dimx, P.dimy, cx, cy, cz);
+    const T cs = T(1) / P.inv_cell;
+    // squared distances from x_i to the lower / upper face of its cell, per axis
+    T slo[3], shi[3];
+    {
+        const T px[3] = {(T)xi.x - P.ox, (T)xi.y - P.oy, (T)xi.z - P.oz};
+        const int c3[3] = {cx, cy, cz};
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            const T lo = px[d] - (T)c3[d] * cs;
+            const T hi = (T)(c3[d] + 1) * cs - px[d];
+            slo[d] = lo > T(0) ? lo * lo : T(0);
+            shi[d] = hi > T(0) ? hi * hi : T(0);
+        }
+    }
+    const T cull = P.K.h2 * T(1.001);
 
     uint32_t *Lf = list_ptr(B.lf, i, P.capf);
     uint32_t *Lb = list_ptr(B.lb, i, P.capb);
     uint32_t nf = 0, nb = 0;
-    T wf = T(0), wb = T(0), gsq = T(0), divf = T(0), divb = T(0);
-    V3<T> gf = mk3<T>(0, 0, 0), gb = mk3<T>(0, 0, 0);
-
     for (int dz = -1; dz <= 1; dz++) {
         const int z = cz + dz;
         if (z < 0 || z >= P.dimz) continue;
+        const T sz = dz < 0 ? slo[2] : (dz > 0 ? shi[2] : T(0));
+        const bool inner_z = z > 0 && z < P.dimz - 1;
         for (int dy = -1; dy <= 1; dy++) {
             const int y = cy + dy;
             if (y < 0 || y >= P.dimy) continue;
+            const T syz = sz + (dy < 0 ? slo[1] : (dy > 0 ? shi[1] : T(0)));
+            const bool inner_yz = inner_z && y > 0 && y < P.dimy - 1;
             for (int dx = -1; dx <= 1; dx++) {
                 const int x = cx + dx;
                 if (x < 0 || x >= P.dimx) continue;
+                // border cells may hold clamped particles outside their box: never culled
+                const bool inner = inner_yz && x > 0 && x < P.dimx - 1;
+                if (inner && syz + (dx < 0 ? slo[0] : (dx > 0 ? shi[0] : T(0))) > cull) continue;
                 const uint32_t c = ((uint32_t)z * (uint32_t)P.dimy + (uint32_t)y) * (uint32_t)P.dimx + (uint32_t)x;
-                // fluid
                 uint32_t s = B.cstart[c];
                 if (s != kEmpty) {
                     const uint32_t e = B.cend[c];
                     for (uint32_t j = s; j < e; j++) {
-                        if (j == i) continue;
-                        const v4_t<T> xj = ldv(B.x, j);
                         T ddx, ddy, ddz;
-                        const T d2 = pair_d2(xi, xj, ddx, ddy, ddz);
-                        if (!(d2 < P.K.h2)) continue;
-                        if (nf < P.capf) Lf[nf * 32u] = j;
-                        nf++;
-                        const T rl = dev_sqrt(d2);
-                        wf += kernel_W(P.K, rl);
-                        const T cg = kernel_gradW_coef(P.K, rl);
-                        const V3<T> g = V3<T>{ddx * cg, ddy * cg, ddz * cg};
-                        gsq += dot(g, g);
-                        gf = add(gf, g);
-                        const V3<T> vj = xyz<T>(ldv(B.v, j));
-                        divf += dot(sub(vi, vj), g);
+                        if (j != i && pair_d2(xi, ldv(B.x, j), ddx, ddy, ddz) < P.K.h2) {
+                            if (nf < P.capf) Lf[nf * 32u] = j;
+                            nf++;
+                        }
                     }
                 }
-                // boundary
                 s = B.bcstart[c];
                 if (s != kEmpty) {
                     const uint32_t e = B.bcend[c];
                     for (uint32_t j = s; j < e; j++) {
-                        const v4_t<T> xj = ldv(B.xb, j);
                         T ddx, ddy, ddz;
-                        const T d2 = pair_d2(xi, xj, ddx, ddy, ddz);
-                        if (!(d2 < P.K.h2)) continue;
-                        if (nb < P.capb) Lb[nb * 32u] = j;
-                        nb++;
-                        const T Vb = (T)xj.w;
-                        const T rl = dev_sqrt(d2);
-                        wb += Vb * kernel_W(P.K, rl);
-                        const T cg = kernel_gradW_coef(P.K, rl);
-                        const V3<T> g = V3<T>{ddx * cg, ddy * cg, ddz * cg};
-                        gb = add(gb, scl(g, Vb));
-                        divb += Vb * dot(vi, g);
+                        if (pair_d2(xi, ldv(B.xb, j), ddx, ddy, ddz) < P.K.h2) {
+                            if (nb < P.capb) Lb[nb * 32u] = j;
+                            nb++;
+                        }
                     }
                 }
             }
         }
     }
+
+    // phase 2: kernel sums over the accepted neighbours
+    const V3<T> vi = xyz<T>(ldv(B.v, i));
+    T wf = T(0), wb = T(0), gsq = T(0), divf = T(0), divb = T(0);
+    V3<T> gf = mk3<T>(0, 0, 0), gb = mk3<T>(0, 0, 0);
+    struct XV {
+        v4_t<T> x, v;
+    };
+    nbr_loop<kUnroll>(Lf, min(nf, P.capf), [&](uint32_t j) { return XV{ldv(B.x, j), ldv(B.v, j)}; },
+                      [&](uint32_t, const XV &d) {
+                          const V3<T> r = diff3<T>(xi, d.x);
+                          T W, c;
+                          kernel_W_coef_d2(P.K, dot(r, r), W, c);
+                          wf += W;
+                          const V3<T> g = scl(r, c);
+                          gsq += dot(g, g);
+                          gf = add(gf, g);
+                          divf += dot(sub(vi, xyz<T>(d.v)), g);
+                      });
+    nbr_loop<kUnroll>(Lb, min(nb, P.capb), [&](uint32_t j) { return ldv(B.xb, j); },
+                      [&](uint32_t, const v4_t<T> &xj) {
+                          const V3<T> r = diff3<T>(xi, xj);
+                          T W, c;
+                          kernel_W_coef_d2(P.K, dot(r, r), W, c);
+                          const T Vb = (T)xj.w;
+                          wb += Vb * W;
+                          const V3<T> g = scl(r, c * Vb);
+                          gb = add(gb, g);
+                          divb += dot(vi, g);
+                      });
     B.nf[i] = nf;
     B.nbn[i] = nb;
     if (nf > P.capf || nb > P.capb) atomicOr(&B.sc->flags, kFlagOverflow);
@@ -507,60 +565,52 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams<T> P, DevBufs<T> B, i
     }
     stv(B.a, i, pack(ai, T(0)));
     if (div_on) B.kappa_v[i] *= h;
+    if (P.visc_on) {
+        // Weiler2018 warm start g = v + vDiff (Viscosity_Weiler2018.cpp:1247-1250) with the
+        // operator weight d mu m_i / rho_i in w
+        stv(B.cg_x, i, pack(add(vi, xyz<T>(ldv(B.vdiff, i))), P.vd * P.mu * P.mass / B.density[i]));
+    }
 }
 
 // ---- Weiler et al. 2018 ---------------------------------------------------
-// (A v)_i = v_i - dt/rho_i * sum_j d mu (m_j/rho_j) ((v_i - v_j).x_ij) / (|x_ij|^2 + 0.01 h^2) gradW_ij
-// (Viscosity_Weiler2018.cpp:271-443); boundary term when mub != 0.
-template <class T, class VF>
-__device__ __forceinline__ V3<T> weiler_Av(const DevParams<T> &P, const DevBufs<T> &B, uint32_t i, V3<T> vi, VF vec_of)
+// Operator (Viscosity_Weiler2018.cpp:271-443):
+//   (A v)_i = v_i - dt/rho_i * sum_j w_j ((v_i - v_j).x_ij) / (|x_ij|^2 + 0.01 h^2) gradW_ij
+// with w_j = d mu m_j / rho_j, constant during the solve.  Since gradW_ij = c_ij x_ij the
+// diagonal block (diagonalMatrixElement :605-742) I - dt/rho_i sum_j w_j c_ij x_ij x_ij^T /
+// (|x_ij|^2 + 0.01 h^2) is symmetric: 6 entries, and its inverse is symmetric too.
+// w_j travels in the w lane of the CG direction p (and of the warm start in cg_x), so one
+// 16-byte gather per neighbour gives both the vector and the weight.
+
+// Boundary term of the operator (mub != 0): sum_b d mub (rho0 V_b / rho_i) (v_i.x_ib) / (...) gradW_ib.
+template <class T>
+__device__ __forceinline__ V3<T> weiler_boundary(const DevParams<T> &P, const DevBufs<T> &B, uint32_t i, const v4_t<T> &xi,
+                                                 T rhoi, V3<T> vi)
 {
-    const v4_t<T> xi = ldv(B.x, i);
-    const T rhoi = B.density[i];
     V3<T> acc = mk3<T>(0, 0, 0);
-    const uint32_t nf = min(B.nf[i], P.capf);
     const T eps2 = T(0.01) * P.h2;
-    struct XVR {
-        v4_t<T> x;
-        V3<T> v;
-        T rho;
-    };
-    nbr_loop<kUnroll>(list_ptr(B.lf, i, P.capf), nf,
-                      [&](uint32_t j) { return XVR{ldv(B.x, j), vec_of(j), B.density[j]}; },
-                      [&](uint32_t, const XVR &d) {
-                          const V3<T> r = diff3<T>(xi, d.x);
-                          const T r2 = dot(r, r);
-                          const T f = P.vd * P.mu * (P.mass / d.rho) * dot(sub(vi, d.v), r) / (r2 + eps2);
-                          acc = add(acc, scl(r, grad_coef_d2(P.K, r2) * f));
-                      });
-    if (P.mub != T(0)) {
-        const uint32_t nb = min(B.nbn[i], P.capb);
-        const uint32_t *Lb = list_ptr(B.lb, i, P.capb);
-        for (uint32_t k = 0; k < nb; k++) {
-            const uint32_t j = Lb[k * 32u];
-            const v4_t<T> xj = ldv(B.xb, j);
-            const Pair<T> pr = pair_of<T>(xi, xj);
-            const V3<T> g = gradW(P.K, pr);
-            const T f = P.vd * P.mub * (P.rho0 * (T)xj.w / rhoi) * dot(vi, pr.r) / (pr.rl * pr.rl + eps2);
-            acc = add(acc, scl(g, f));
-        }
+    const uint32_t nb = min(B.nbn[i], P.capb);
+    const uint32_t *Lb = list_ptr(B.lb, i, P.capb);
+    for (uint32_t k = 0; k < nb; k++) {
+        const v4_t<T> xj = ldv(B.xb, Lb[k * 32u]);
+        const V3<T> r = diff3<T>(xi, xj);
+        const T r2 = dot(r, r);
+        const T f = P.vd * P.mub * (P.rho0 * (T)xj.w / rhoi) * dot(vi, r) / (r2 + eps2);
+        acc = add(acc, scl(r, grad_coef_d2(P.K, r2) * f));
     }
-    const T dt = (T)B.sc->dt;
-    return sub(vi, scl(acc, dt / rhoi));
+    return acc;
 }
 
-template <class T> __device__ __forceinline__ V3<T> mat3_mul(const v4_t<T> &r0, const v4_t<T> &r1, const v4_t<T> &r2, V3<T> v)
+// Symmetric 3x3 stored as (m00, m01, m02, m11) and (m12, m22, -, -).
+template <class T> __device__ __forceinline__ V3<T> sym_mul(const v4_t<T> &a, const v4_t<T> &b, V3<T> v)
 {
-    return V3<T>{(T)r0.x * v.x + (T)r0.y * v.y + (T)r0.z * v.z, (T)r1.x * v.x + (T)r1.y * v.y + (T)r1.z * v.z,
-                 (T)r2.x * v.x + (T)r2.y * v.y + (T)r2.z * v.z};
+    return V3<T>{(T)a.x * v.x + (T)a.y * v.y + (T)a.z * v.z, (T)a.y * v.x + (T)a.w * v.y + (T)b.x * v.z,
+                 (T)a.z * v.x + (T)b.x * v.y + (T)b.y * v.z};
 }
 
-// Set-up of the CG solve (Viscosity_Weiler2018.cpp:891-926): block-Jacobi inverse
-// of the diagonal 3x3 blocks (diagonalMatrixElement :605-742, inverse taken in
-// MatrixFreeSolver.h:231-244), right-hand side b = v (computeRHS :1091-1254 with
-// static boundary), warm start g = v + vDiff, initial residual r = b - A g,
-// p = M^-1 r and the first reductions of Eigen's conjugate_gradient
-// (ConjugateGradient.h:29-70).
+// Set-up of the CG solve (Viscosity_Weiler2018.cpp:891-926): block-Jacobi inverse of the
+// diagonal blocks (inverse taken in MatrixFreeSolver.h:231-244), b = v (computeRHS :1091-1254,
+// static boundary), warm start g = v + vDiff (already in cg_x), r = b - A g, p = M^-1 r, and
+// the first reductions of Eigen's conjugate_gradient (ConjugateGradient.h:29-70), one pass.
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T> B, ReduceSlot slot,
                                                         cudaGraphConditionalHandle handle, int use_handle)
@@ -574,64 +624,56 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T
         const T rhoi = B.density[i];
         const T dt = (T)B.sc->dt;
         const T eps2 = T(0.01) * P.h2;
-        T R[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        const v4_t<T> gi4 = ldv(B.cg_x, i);
+        const V3<T> gi = xyz<T>(gi4);
+        T m00 = 0, m01 = 0, m02 = 0, m11 = 0, m12 = 0, m22 = 0;
+        V3<T> acc = mk3<T>(0, 0, 0);
+        struct XG {
+            v4_t<T> x, g;
+        };
         const uint32_t nf = min(B.nf[i], P.capf);
-        const uint32_t *Lf = list_ptr(B.lf, i, P.capf);
-        for (uint32_t k = 0; k < nf; k++) {
-            const uint32_t j = Lf[k * 32u];
-            const Pair<T> pr = pair_of<T>(xi, ldv(B.x, j));
-            const V3<T> g = gradW(P.K, pr);
-            const T f = P.vd * P.mu * (P.mass / B.density[j]) / (pr.rl * pr.rl + eps2);
-            const T gg[3] = {g.x, g.y, g.z}, rr[3] = {pr.r.x, pr.r.y, pr.r.z};
-#pragma unroll
-            for (int a = 0; a < 3; a++)
-#pragma unroll
-                for (int b = 0; b < 3; b++) R[3 * a + b] += f * gg[a] * rr[b];
-        }
+        nbr_loop<kUnroll>(list_ptr(B.lf, i, P.capf), nf, [&](uint32_t j) { return XG{ldv(B.x, j), ldv(B.cg_x, j)}; },
+                          [&](uint32_t, const XG &d) {
+                              const V3<T> r = diff3<T>(xi, d.x);
+                              const T r2 = dot(r, r);
+                              const T f = (T)d.g.w / (r2 + eps2) * grad_coef_d2(P.K, r2);
+                              m00 += f * r.x * r.x; m01 += f * r.x * r.y; m02 += f * r.x * r.z;
+                              m11 += f * r.y * r.y; m12 += f * r.y * r.z; m22 += f * r.z * r.z;
+                              acc = add(acc, scl(r, f * dot(sub(gi, xyz<T>(d.g)), r)));
+                          });
         if (P.mub != T(0)) {
             const uint32_t nb = min(B.nbn[i], P.capb);
             const uint32_t *Lb = list_ptr(B.lb, i, P.capb);
             for (uint32_t k = 0; k < nb; k++) {
-                const uint32_t j = Lb[k * 32u];
-                const v4_t<T> xj = ldv(B.xb, j);
-                const Pair<T> pr = pair_of<T>(xi, xj);
-                const V3<T> g = gradW(P.K, pr);
-                const T f = P.vd * P.mub * (P.rho0 * (T)xj.w / rhoi) / (pr.rl * pr.rl + eps2);
-                const T gg[3] = {g.x, g.y, g.z}, rr[3] = {pr.r.x, pr.r.y, pr.r.z};
-#pragma unroll
-                for (int a = 0; a < 3; a++)
-#pragma unroll
-                    for (int b = 0; b < 3; b++) R[3 * a + b] += f * gg[a] * rr[b];
+                const v4_t<T> xj = ldv(B.xb, Lb[k * 32u]);
+                const V3<T> r = diff3<T>(xi, xj);
+                const T r2 = dot(r, r);
+                const T f = P.vd * P.mub * (P.rho0 * (T)xj.w / rhoi) / (r2 + eps2) * grad_coef_d2(P.K, r2);
+                m00 += f * r.x * r.x; m01 += f * r.x * r.y; m02 += f * r.x * r.z;
+                m11 += f * r.y * r.y; m12 += f * r.y * r.z; m22 += f * r.z * r.z;
             }
+            acc = add(acc, weiler_boundary(P, B, i, xi, rhoi, gi));
         }
-        T M[9];
         const T s = dt / rhoi;
-#pragma unroll
-        for (int a = 0; a < 9; a++) M[a] = ((a % 4) == 0 ? T(1) : T(0)) - s * R[a];
-        const T c00 = M[4] * M[8] - M[5] * M[7];
-        const T c01 = M[5] * M[6] - M[3] * M[8];
-        const T c02 = M[3] * M[7] - M[4] * M[6];
-        const T det = M[0] * c00 + M[1] * c01 + M[2] * c02;
-        const T id = T(1) / det;
-        v4_t<T> r0, r1, r2;
-        r0.x = c00 * id; r0.y = (M[2] * M[7] - M[1] * M[8]) * id; r0.z = (M[1] * M[5] - M[2] * M[4]) * id; r0.w = 0;
-        r1.x = c01 * id; r1.y = (M[0] * M[8] - M[2] * M[6]) * id; r1.z = (M[2] * M[3] - M[0] * M[5]) * id; r1.w = 0;
-        r2.x = c02 * id; r2.y = (M[1] * M[6] - M[0] * M[7]) * id; r2.z = (M[0] * M[4] - M[1] * M[3]) * id; r2.w = 0;
-        stv(B.inv0, i, r0);
-        stv(B.inv1, i, r1);
-        stv(B.inv2, i, r2);
+        const T a = T(1) - s * m00, b = -s * m01, c = -s * m02, d = T(1) - s * m11, e = -s * m12, f = T(1) - s * m22;
+        const T A00 = d * f - e * e, A01 = c * e - b * f, A02 = b * e - c * d;
+        const T A11 = a * f - c * c, A12 = b * c - a * e, A22 = a * d - b * b;
+        const T id = T(1) / (a * A00 + b * A01 + c * A02);
+        v4_t<T> i0, i1;
+        i0.x = A00 * id; i0.y = A01 * id; i0.z = A02 * id; i0.w = A11 * id;
+        i1.x = A12 * id; i1.y = A22 * id; i1.z = 0; i1.w = 0;
+        stv(B.inv0, i, i0);
+        stv(B.inv1, i, i1);
 
         const V3<T> vi = xyz<T>(ldv(B.v, i));
-        const V3<T> gi = add(vi, xyz<T>(ldv(B.vdiff, i)));
-        const V3<T> Ag = weiler_Av(P, B, i, gi, [&](uint32_t j) { return add(xyz<T>(ldv(B.v, j)), xyz<T>(ldv(B.vdiff, j))); });
+        const V3<T> Ag = sub(gi, scl(acc, s));
         const V3<T> r = sub(vi, Ag);
-        const V3<T> p = mat3_mul<T>(r0, r1, r2, r);
-        stv(B.cg_x, i, pack(gi, T(0)));
+        const V3<T> p = sym_mul<T>(i0, i1, r);
         stv(B.cg_r, i, pack(r, T(0)));
-        stv(B.cg_p, i, pack(p, T(0)));
-        mine.v[0] = (double)vi.x * vi.x + (double)vi.y * vi.y + (double)vi.z * vi.z;
-        mine.v[1] = (double)r.x * r.x + (double)r.y * r.y + (double)r.z * r.z;
-        mine.v[2] = (double)r.x * p.x + (double)r.y * p.y + (double)r.z * p.z;
+        stv(B.cg_p, i, pack(p, (T)gi4.w));
+        mine.v[0] = (double)dot(vi, vi);
+        mine.v[1] = (double)dot(r, r);
+        mine.v[2] = (double)dot(r, p);
     }
     StepScalars *sc = B.sc;
     const double tol = P.visc_tol;
@@ -674,16 +716,34 @@ __global__ void __launch_bounds__(kBlock) k_cg_matvec(DevParams<T> P, DevBufs<T>
     DSum<1> mine;
     mine.v[0] = 0.0;
     if (i < P.n) {
+        const v4_t<T> xi = ldv(B.x, i);
+        const T rhoi = B.density[i];
+        const T eps2 = T(0.01) * P.h2;
         const V3<T> pi = xyz<T>(ldv(B.cg_p, i));
-        const V3<T> t = weiler_Av(P, B, i, pi, [&](uint32_t j) { return xyz<T>(ldv(B.cg_p, j)); });
+        V3<T> acc = mk3<T>(0, 0, 0);
+        struct XP {
+            v4_t<T> x, p;
+        };
+        const uint32_t nf = min(B.nf[i], P.capf);
+        nbr_loop<kUnroll>(list_ptr(B.lf, i, P.capf), nf, [&](uint32_t j) { return XP{ldv(B.x, j), ldv(B.cg_p, j)}; },
+                          [&](uint32_t, const XP &d) {
+                              const V3<T> r = diff3<T>(xi, d.x);
+                              const T r2 = dot(r, r);
+                              const T f = (T)d.p.w / (r2 + eps2) * grad_coef_d2(P.K, r2);
+                              acc = add(acc, scl(r, f * dot(sub(pi, xyz<T>(d.p)), r)));
+                          });
+        if (P.mub != T(0)) acc = add(acc, weiler_boundary(P, B, i, xi, rhoi, pi));
+        const T dt = (T)B.sc->dt;
+        const V3<T> t = sub(pi, scl(acc, dt / rhoi));
         stv(B.cg_t, i, pack(t, T(0)));
-        mine.v[0] = (double)pi.x * t.x + (double)pi.y * t.y + (double)pi.z * t.z;
+        mine.v[0] = (double)dot(pi, t);
     }
     StepScalars *sc = B.sc;
     grid_sum_finalize<1>(mine, slot, [&](const DSum<1> &tot) { sc->cg_alpha = sc->cg_absnew / tot.v[0]; });
 }
 
-// x += alpha p; r -= alpha tmp; |r|^2; z = M^-1 r; r.z -> beta (ConjugateGradient.h:77-88)
+// x += alpha p; r -= alpha tmp; |r|^2; z = M^-1 r; r.z -> beta (ConjugateGradient.h:77-88).
+// Element arithmetic in the bulk precision, sums accumulated in FP64.
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_cg_update(DevParams<T> P, DevBufs<T> B, ReduceSlot slot,
                                                        cudaGraphConditionalHandle handle, int use_handle)
@@ -693,19 +753,19 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(DevParams<T> P, DevBufs<T>
     DSum<2> mine;
     mine.v[0] = mine.v[1] = 0.0;
     if (i < P.n) {
-        const double alpha = B.sc->cg_alpha;
+        const T alpha = (T)B.sc->cg_alpha;
         const V3<T> p = xyz<T>(ldv(B.cg_p, i));
         const V3<T> t = xyz<T>(ldv(B.cg_t, i));
-        V3<T> x = xyz<T>(ldv(B.cg_x, i));
-        V3<T> r = xyz<T>(ldv(B.cg_r, i));
-        x = V3<T>{(T)((double)x.x + alpha * p.x), (T)((double)x.y + alpha * p.y), (T)((double)x.z + alpha * p.z)};
-        r = V3<T>{(T)((double)r.x - alpha * t.x), (T)((double)r.y - alpha * t.y), (T)((double)r.z - alpha * t.z)};
-        const V3<T> z = mat3_mul<T>(ldv(B.inv0, i), ldv(B.inv1, i), ldv(B.inv2, i), r);
-        stv(B.cg_x, i, pack(x, T(0)));
+        v4_t<T> x4 = ldv(B.cg_x, i);
+        V3<T> x = add(xyz<T>(x4), scl(p, alpha));
+        const V3<T> r = sub(xyz<T>(ldv(B.cg_r, i)), scl(t, alpha));
+        const V3<T> z = sym_mul<T>(ldv(B.inv0, i), ldv(B.inv1, i), r);
+        x4.x = x.x; x4.y = x.y; x4.z = x.z;
+        stv(B.cg_x, i, x4);
         stv(B.cg_r, i, pack(r, T(0)));
         stv(B.cg_z, i, pack(z, T(0)));
-        mine.v[0] = (double)r.x * r.x + (double)r.y * r.y + (double)r.z * r.z;
-        mine.v[1] = (double)r.x * z.x + (double)r.y * z.y + (double)r.z * z.z;
+        mine.v[0] = (double)dot(r, r);
+        mine.v[1] = (double)dot(r, z);
     }
     StepScalars *sc = B.sc;
     const unsigned maxit = P.visc_max_iter;
@@ -728,7 +788,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(DevParams<T> P, DevBufs<T>
     });
 }
 
-// p = z + beta p (ConjugateGradient.h:88)
+// p = z + beta p (ConjugateGradient.h:88); the weight in p.w is kept
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_cg_p(DevParams<T> P, DevBufs<T> B)
 {
@@ -736,10 +796,13 @@ __global__ void __launch_bounds__(kBlock) k_cg_p(DevParams<T> P, DevBufs<T> B)
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     if (B.sc->cg_state != 0) return;
-    const double beta = B.sc->cg_beta;
+    const T beta = (T)B.sc->cg_beta;
     const V3<T> z = xyz<T>(ldv(B.cg_z, i));
-    const V3<T> p = xyz<T>(ldv(B.cg_p, i));
-    stv(B.cg_p, i, pack(V3<T>{(T)(z.x + beta * p.x), (T)(z.y + beta * p.y), (T)(z.z + beta * p.z)}, T(0)));
+    v4_t<T> p = ldv(B.cg_p, i);
+    p.x = z.x + beta * (T)p.x;
+    p.y = z.y + beta * (T)p.y;
+    p.z = z.z + beta * (T)p.z;
+    stv(B.cg_p, i, p);
 }
 
 // ==========================================================================

@@ -86,7 +86,7 @@ template <class T> struct DevBufs {
     uint32_t *bid;               // upload index of each sorted boundary particle
     // CG
     v4 *cg_x, *cg_r, *cg_p, *cg_z, *cg_t;
-    v4 *inv0, *inv1, *inv2;
+    v4 *inv0, *inv1;             // symmetric 3x3 inverse blocks: (m00,m01,m02,m11), (m12,m22,-,-)
     // reductions
     double *partials;
     unsigned *counter;
