@@ -166,6 +166,25 @@ int sphgb_neighbors(sphgb_ctx *ctx, int kind, uint32_t *offsets, uint32_t *indic
 /* counts */
 int sphgb_num_particles(const sphgb_ctx *ctx, uint32_t *n, uint32_t *nb);
 
+/* Akinci2012 boundary volumes that allocate nothing (no reference counterpart: the
+ * reference computes volumes on the host in BoundaryModel_Akinci2012::computeBoundaryVolume).
+ * For callers that may not allocate device memory: code running during CUDA stream capture,
+ * where cudaMalloc cannot be recorded, and hosts with a fixed device-memory budget that forbid
+ * allocation after start-up.  xb (nb x 3 floats, AoS) and volume (nb floats) are DEVICE
+ * pointers owned by the caller; stream is a cudaStream_t (NULL = default stream).  The box
+ * must contain every position (it sets the cell grid).  All scratch is one static device
+ * array of about 5.8 MiB that every GPU loading this library holds until exit.  Limits:
+ * nb <= SPHGB_NOALLOC_MAX_BOUNDARY (else SPHGB_ERR_CAPACITY) and at most
+ * SPHGB_NOALLOC_MAX_CELLS grid cells of 1.001 x 4 r (else SPHGB_ERR_GRID).  The first call on a
+ * device looks up the scratch address (cudaGetSymbolAddress) and should be made before any
+ * stream capture.  Calls share the scratch: calls that overlap on the GPU (other streams,
+ * other host threads) race; serialise them.  Returns without waiting for the GPU. */
+#define SPHGB_NOALLOC_MAX_BOUNDARY 65536
+#define SPHGB_NOALLOC_MAX_CELLS 262144
+int sphgb_boundary_volume_noalloc(const float *xb, uint32_t nb, double particle_radius,
+                                  const double box_min[3], const double box_max[3], float *volume,
+                                  void *stream);
+
 /* the cudaStream_t every kernel of this context is launched on (for event timing by callers) */
 int sphgb_get_stream(const sphgb_ctx *ctx, void **stream);
 
