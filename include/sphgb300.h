@@ -99,6 +99,11 @@ typedef struct sphgb_stats {
     double dt_next;                  /* CFL step size (used by the pressure solve) */
     double time;                     /* simulated time after the step */
     uint64_t kernel_launches;        /* kernels this step launched on the GPU */
+    uint32_t learned_used;           /* bit 0 / bit 1: predicted warm start used by the divergence /
+                                        pressure solve this step */
+    uint32_t reserved;
+    double ws_residual_classic[2];   /* initial average error with the classic warm start (div, pressure) */
+    double ws_residual_learned[2];   /* ... with the predicted warm start (0 when the network is off) */
 } sphgb_stats;
 
 /* field ids for sphgb_download / sphgb_upload_field; names are the reference's field names */
@@ -118,6 +123,7 @@ typedef struct sphgb_stats {
 #define SPHGB_FIELD_NUM_BOUNDARY_NEIGHBORS 13  /* uint32 */
 #define SPHGB_FIELD_BOUNDARY_VOLUME 14         /* boundary "volume" V_b (nb entries) */
 #define SPHGB_FIELD_BOUNDARY_POSITION 15       /* boundary "position" (nb x 3) */
+#define SPHGB_FIELD_FEATURES 16                /* warm-start network inputs of the last step (n x 10) */
 
 #define SPHGB_DTYPE_F32 0
 #define SPHGB_DTYPE_F64 1
@@ -165,6 +171,35 @@ int sphgb_neighbors(sphgb_ctx *ctx, int kind, uint32_t *offsets, uint32_t *indic
 
 /* counts */
 int sphgb_num_particles(const sphgb_ctx *ctx, uint32_t *n, uint32_t *nb);
+
+/* ---- learned warm start (no counterpart in the reference: new in this library) ----
+ * A per-particle network 10 -> 64 -> 64 -> 2 (GELU), BF16 weights and activations on the
+ * tensor cores with FP32 accumulation, predicting the stored warm starts kappa_v*dt and
+ * kappa*dt^2 (divergence and pressure solve) from 5 per-particle features and their
+ * cubic-spline-weighted neighbour means (sphgb_download SPHGB_FIELD_FEATURES).  Trained with
+ * Adam by hand-written kernels.  Host arrays: X n x 10, targets/mask n x 2, row-major float. */
+typedef struct sphgb_mlp sphgb_mlp;
+int sphgb_mlp_create(int device, uint32_t seed, sphgb_mlp **out);
+int sphgb_mlp_destroy(sphgb_mlp *m);
+const char *sphgb_mlp_last_error(const sphgb_mlp *m);
+int sphgb_mlp_num_params(void);
+int sphgb_mlp_get_params(sphgb_mlp *m, float *out);
+int sphgb_mlp_set_params(sphgb_mlp *m, const float *in);
+/* network output o_k x scale_k = stored warm start (kappa_v*dt, kappa*dt^2) */
+int sphgb_mlp_set_output_scale(sphgb_mlp *m, float scale_v, float scale_p);
+int sphgb_mlp_get_output_scale(const sphgb_mlp *m, float *scale_v, float *scale_p);
+int sphgb_mlp_forward(sphgb_mlp *m, const float *X, uint32_t n, float *Y);
+int sphgb_mlp_loss_grad(sphgb_mlp *m, const float *X, const float *Y, const float *mask, uint32_t n, float *loss,
+                        float *grad);
+int sphgb_mlp_train(sphgb_mlp *m, const float *X, const float *Y, const float *mask, uint32_t n, uint32_t epochs,
+                    uint32_t batch, float lr, uint32_t seed, float *epoch_loss);
+/* Use the network for both warm starts of this context (NULL: classic warm start only).  The
+ * solvers still iterate to their tolerances; per step and solver the predicted warm start is
+ * used only if its initial residual is lower than the classic one (sphgb_stats.learned_used). */
+int sphgb_set_warmstart_mlp(sphgb_ctx *ctx, const sphgb_mlp *m);
+/* compute the network inputs every step even without a network (training-data collection);
+ * they are read back with SPHGB_FIELD_FEATURES */
+int sphgb_set_feature_output(sphgb_ctx *ctx, int on);
 
 /* Akinci2012 boundary volumes that allocate nothing (no reference counterpart: the
  * reference computes volumes on the host in BoundaryModel_Akinci2012::computeBoundaryVolume).

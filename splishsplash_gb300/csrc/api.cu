@@ -17,9 +17,14 @@
 #include <vector>
 
 #include "../../include/sphgb300.h"
+#include "mlp.cuh"
 #include "sph_ctx.h"
 
 using namespace sphgb;
+
+namespace sphgb {
+void mlp_export(const sphgb_mlp *m, const float **params, const void **w, float scale[2], int *device);
+}
 
 struct sphgb_ctx {
     sphgb_config cfg{};
@@ -65,6 +70,13 @@ struct sphgb_ctx {
     bool graph_ok = false;
     bool step_pending = false;
     uint64_t launches_last_step = 0;
+    // learned warm start: network copy and per-particle buffers
+    bool learned = false, feat_on = false;
+    float *mlp_p = nullptr;
+    void *mlp_w = nullptr;
+    float ws_scale[2] = {kMlpDefaultScaleV, kMlpDefaultScaleP};
+    float *feat = nullptr, *mlp_x = nullptr, *mlp_y = nullptr;
+    void *kl = nullptr, *pa2 = nullptr;
     // per-kernel CUDA-event timing (host-loop mode only)
     bool profile = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -79,12 +91,13 @@ namespace {
 enum KernelId {
     K_STEP_BEGIN, K_KEYS, K_SORT, K_GATHER, K_CELL_RANGES, K_BUILD, K_LOOP_BEGIN, K_PRESSURE_ACCEL, K_JACOBI,
     K_SOLVER_FINALIZE, K_XSPH, K_VISC_SETUP, K_CG_MATVEC, K_CG_UPDATE, K_CG_P, K_KICK, K_PRESS_INIT, K_INTEGRATE,
+    K_FEATURES, K_MLP, K_WS_SELECT,
     K_COUNT
 };
 const char *kKernelNames[K_COUNT] = {
     "step_begin", "keys", "radix_sort", "gather", "cell_ranges", "build_lists_density_alpha", "loop_begin",
     "pressure_accel", "jacobi_update", "solver_finalize", "xsph_gravity", "visc_setup", "cg_matvec", "cg_update",
-    "cg_p", "kick_cfl", "press_init", "integrate",
+    "cg_p", "kick_cfl", "press_init", "integrate", "features", "mlp_infer", "warmstart_select",
 };
 
 // Brackets the launches of one kernel class with events on the context stream
@@ -217,6 +230,10 @@ template <class T> DevParams<T> make_params(const sphgb_ctx *c)
     P.cfl_method = q.cfl_method;
     P.visc_on = q.viscosity_method == 6 ? 1 : 0;
     P.div_on = q.enable_divergence_solver ? 1 : 0;
+    P.learned = c->learned ? 1 : 0;
+    P.feat_on = (c->learned || c->feat_on) ? 1 : 0;
+    P.ws_scale_v = c->ws_scale[0];
+    P.ws_scale_p = c->ws_scale[1];
     P.ox = (T)c->org[0];
     P.oy = (T)c->org[1];
     P.oz = (T)c->org[2];
@@ -276,6 +293,13 @@ template <class T> DevBufs<T> make_bufs(const sphgb_ctx *c, int view)
     B.bcend = c->bcend;
     B.xb = (v4 *)c->xb;
     B.bscratch = (T *)c->bscratch;
+    B.feat = c->feat;
+    B.mlp_x = c->mlp_x;
+    B.mlp_y = c->mlp_y;
+    B.kl = (T *)c->kl;
+    B.pa2 = (v4 *)c->pa2;
+    B.mlp_w = c->mlp_w;
+    B.mlp_p = c->mlp_p;
     B.bid = c->bid;
     B.cg_x = (v4 *)c->cg[0];
     B.cg_r = (v4 *)c->cg[1];
@@ -406,6 +430,8 @@ template <class T> void enqueue_prologue(sphgb_ctx *c, const DevParams<T> &P, co
         launch_cell_ranges<T>(P, B1, s);
     }
     { PROF(K_BUILD, s); launch_build<T>(P, B1, s); }
+    if (P.feat_on) { PROF(K_FEATURES, s); launch_features<T>(P, B1, s); }
+    if (P.learned) { PROF(K_MLP, s); mlp_infer_device(c->mlp_x, c->n, c->mlp_w, c->mlp_p, c->mlp_y, s); }
 }
 
 template <class T> int step_host_loop(sphgb_ctx *c)
@@ -418,6 +444,7 @@ template <class T> int step_host_loop(sphgb_ctx *c)
     unsigned cont = 0;
     enqueue_prologue<T>(c, P, B0, B1, s);
     if (P.div_on) {
+        if (P.learned) { PROF(K_WS_SELECT, s); launch_warmstart_select<T>(P, B1, true, s); }
         { PROF(K_LOOP_BEGIN, s); launch_loop_begin<T>(P, B1, true, s); }
         if (P.max_iter_v > 0) {
             unsigned guard = 0;
@@ -443,6 +470,7 @@ template <class T> int step_host_loop(sphgb_ctx *c)
     }
     { PROF(K_KICK, s); launch_kick<T>(P, B1, s); }
     { PROF(K_PRESS_INIT, s); launch_press_init<T>(P, B1, s); }
+    if (P.learned) { PROF(K_WS_SELECT, s); launch_warmstart_select<T>(P, B1, false, s); }
     { PROF(K_LOOP_BEGIN, s); launch_loop_begin<T>(P, B1, false, s); }
     if (P.max_iter > 0) {
         unsigned guard = 0;
@@ -518,6 +546,7 @@ template <class T> int build_graph(sphgb_ctx *c, int parity, cudaGraphExec_t *ou
     enqueue_prologue<T>(c, P, B0, B1, s);
     cudaGraphConditionalHandle h = 0;
     if (P.div_on) {
+        if (P.learned) launch_warmstart_select<T>(P, B1, true, s);
         launch_loop_begin<T>(P, B1, true, s);
         if (e == cudaSuccess)
             e = add_while(c, &h, P.max_iter_v > 0 ? 1u : 0u, [&](cudaStream_t bs, cudaGraphConditionalHandle hh) {
@@ -563,6 +592,7 @@ template <class T> int build_graph(sphgb_ctx *c, int parity, cudaGraphExec_t *ou
     }
     launch_kick<T>(P, B1, s);
     launch_press_init<T>(P, B1, s);
+    if (P.learned) launch_warmstart_select<T>(P, B1, false, s);
     launch_loop_begin<T>(P, B1, false, s);
     if (e == cudaSuccess)
         e = add_while(c, &h, P.max_iter > 0 ? 1u : 0u, [&](cudaStream_t bs, cudaGraphConditionalHandle hh) {
@@ -630,7 +660,13 @@ int fill_stats(sphgb_ctx *c, sphgb_stats *st)
         st->dt_used = h.dt_used;
         st->dt_next = h.dt_next;
         st->time = h.time;
-        st->kernel_launches = h.launches;
+        st->kernel_launches = h.launches + (c->learned ? 1 : 0);   // the network forward counts as one
+        st->learned_used = c->learned ? h.ws_used : 0;
+        st->reserved = 0;
+        for (int k = 0; k < 2; k++) {
+            st->ws_residual_classic[k] = c->learned ? h.ws_rc[k] : 0.0;
+            st->ws_residual_learned[k] = c->learned ? h.ws_rl[k] : 0.0;
+        }
     }
     if (h.flags & kFlagOverflow)
         return fail(c, SPHGB_ERR_CAPACITY, "neighbour list capacity exceeded (raise max_fluid/boundary_neighbors)");
@@ -639,11 +675,17 @@ int fill_stats(sphgb_ctx *c, sphgb_stats *st)
     return SPHGB_OK;
 }
 
+int alloc_learned_buffers(sphgb_ctx *c);
+
 template <class T> int init_fluid(sphgb_ctx *c, const double *x, const double *v, const uint32_t *id, uint32_t n)
 {
     int rc;
     // (re)allocate every per-particle buffer
     free_all(c);
+    c->feat = c->mlp_x = c->mlp_y = nullptr;
+    c->kl = c->pa2 = nullptr;
+    c->staging = nullptr;
+    c->staging_bytes = 0;
     c->prepared = false;
     c->n = n;
     const size_t N = std::max<uint32_t>(n, 1);
@@ -727,6 +769,7 @@ template <class T> int init_fluid(sphgb_ctx *c, const double *x, const double *v
             c->fmax[d] = std::max(c->fmax[d], x[3 * (size_t)i + d]);
         }
     c->have_fluid = true;
+    if ((c->learned || c->feat_on) && (rc = alloc_learned_buffers(c))) return rc;
     c->scalars_dirty = true;
     return SPHGB_OK;
 }
@@ -777,12 +820,28 @@ int field_components(int field)
     case SPHGB_FIELD_POSITION: case SPHGB_FIELD_VELOCITY: case SPHGB_FIELD_ACCELERATION:
     case SPHGB_FIELD_PRESSURE_ACCEL: case SPHGB_FIELD_VDIFF: case SPHGB_FIELD_BOUNDARY_POSITION:
         return 3;
+    case SPHGB_FIELD_FEATURES:
+        return 10;
     default:
         return 1;
     }
 }
 
 size_t dtype_size(int dt) { return dt == SPHGB_DTYPE_F64 ? 8 : 4; }
+
+int alloc_learned_buffers(sphgb_ctx *c)
+{
+    if (c->feat) return SPHGB_OK;
+    const size_t N = std::max<uint32_t>(c->n, 1);
+    int rc;
+    if ((rc = dalloc(c, &c->feat, N * 8 * sizeof(float)))) return rc;
+    if ((rc = dalloc(c, &c->mlp_x, N * 10 * sizeof(float)))) return rc;
+    if ((rc = dalloc(c, &c->mlp_y, N * 2 * sizeof(float)))) return rc;
+    if ((rc = dalloc(c, &c->kl, N * real_size(c)))) return rc;
+    if ((rc = dalloc(c, &c->pa2, N * vec_size(c)))) return rc;
+    CK(cudaMemset(c->mlp_x, 0, N * 10 * sizeof(float)));
+    return SPHGB_OK;
+}
 
 }  // namespace
 
@@ -832,6 +891,8 @@ int sphgb_destroy(sphgb_ctx *c)
     if (c->stream) cudaStreamSynchronize(c->stream);
     free_all(c);
     if (c->hsc) cudaFreeHost(c->hsc);
+    if (c->mlp_p) cudaFree(c->mlp_p);
+    if (c->mlp_w) cudaFree(c->mlp_w);
     for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->body_stream) cudaStreamDestroy(c->body_stream);
@@ -986,6 +1047,49 @@ int sphgb_sync(sphgb_ctx *c, sphgb_stats *stats)
     return fill_stats(c, stats);
 }
 
+int sphgb_set_feature_output(sphgb_ctx *c, int on)
+{
+    if (!c) return SPHGB_ERR_ARGUMENT;
+    if (on && !c->have_fluid) return fail(c, SPHGB_ERR_STATE, "upload the fluid first");
+    cudaSetDevice(c->cfg.device);
+    if (on) {
+        int rc = alloc_learned_buffers(c);
+        if (rc) return rc;
+    }
+    c->feat_on = on != 0;
+    invalidate_graphs(c);
+    return SPHGB_OK;
+}
+
+int sphgb_set_warmstart_mlp(sphgb_ctx *c, const sphgb_mlp *m)
+{
+    if (!c) return SPHGB_ERR_ARGUMENT;
+    cudaSetDevice(c->cfg.device);
+    invalidate_graphs(c);
+    if (!m) {
+        c->learned = false;
+        return SPHGB_OK;
+    }
+    if (!c->have_fluid) return fail(c, SPHGB_ERR_STATE, "upload the fluid first");
+    const float *mp;
+    const void *mw;
+    float scale[2];
+    int dev;
+    mlp_export(m, &mp, &mw, scale, &dev);
+    if (dev != c->cfg.device) return fail(c, SPHGB_ERR_ARGUMENT, "network and context are on different devices");
+    int rc = alloc_learned_buffers(c);
+    if (rc) return rc;
+    // the network copy outlives re-uploads of the fluid: not in the per-particle allocation list
+    if (!c->mlp_p) CK(cudaMalloc(&c->mlp_p, (size_t)kMlpParams * 4));
+    if (!c->mlp_w) CK(cudaMalloc(&c->mlp_w, (size_t)kMlpParams * 2));
+    CK(cudaMemcpy(c->mlp_p, mp, (size_t)kMlpParams * 4, cudaMemcpyDeviceToDevice));
+    CK(cudaMemcpy(c->mlp_w, mw, (size_t)kMlpParams * 2, cudaMemcpyDeviceToDevice));
+    c->ws_scale[0] = scale[0];
+    c->ws_scale[1] = scale[1];
+    c->learned = true;
+    return SPHGB_OK;
+}
+
 int sphgb_get_stream(const sphgb_ctx *c, void **stream)
 {
     if (!c || !stream) return SPHGB_ERR_ARGUMENT;
@@ -1027,7 +1131,8 @@ int sphgb_num_particles(const sphgb_ctx *c, uint32_t *n, uint32_t *nb)
 int sphgb_download(sphgb_ctx *c, int field, void *dst, int dtype)
 {
     if (!c || !dst) return SPHGB_ERR_ARGUMENT;
-    if (field < 0 || field > SPHGB_FIELD_BOUNDARY_POSITION) return fail(c, SPHGB_ERR_ARGUMENT, "unknown field");
+    if (field < 0 || field > SPHGB_FIELD_FEATURES) return fail(c, SPHGB_ERR_ARGUMENT, "unknown field");
+    if (field == SPHGB_FIELD_FEATURES && !c->mlp_x) return fail(c, SPHGB_ERR_STATE, "features are not computed");
     if (dtype < SPHGB_DTYPE_F32 || dtype > SPHGB_DTYPE_U32) return fail(c, SPHGB_ERR_ARGUMENT, "unknown dtype");
     if (!c->have_fluid) return fail(c, SPHGB_ERR_STATE, "no fluid uploaded");
     cudaSetDevice(c->cfg.device);

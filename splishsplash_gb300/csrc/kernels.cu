@@ -339,6 +339,17 @@ __global__ void __launch_bounds__(kBlock) k_build(DevParams<T> P, DevBufs<T> B)
     // boundary sums are fixed for the step (static boundary, fixed positions): every
     // later pass uses them instead of re-walking the boundary list
     stv(B.bg, i, pack(gb, wb));
+    if (P.feat_on) {
+        // raw warm-start features, scaled to O(1): density deviation, velocity divergence x dt,
+        // neighbour count, previous (stored) kappa, displacement per step in diameters
+        const float h = (float)B.sc->dt;
+        float *f = B.feat + (size_t)i * 8;
+        f[0] = 100.0f * ((float)B.density[i] / (float)P.rho0 - 1.0f);
+        f[1] = 100.0f * (float)dsrc * h;
+        f[2] = (float)(nf + nb) * (1.0f / 40.0f) - 1.0f;
+        f[3] = (float)B.kappa[i] / P.ws_scale_p;
+        f[4] = 10.0f * sqrtf((float)dot(vi, vi)) * h / (float)(2.0 * P.radius);
+    }
     v4_t<T> xk = xi;
     xk.w = kv;
     stv(B.xk, i, xk);
@@ -956,6 +967,169 @@ __global__ void __launch_bounds__(kBlock) k_integrate(DevParams<T> P, DevBufs<T>
 }
 
 // ==========================================================================
+// learned warm start
+// ==========================================================================
+// Network inputs: the 5 raw features of particle i and their cubic-spline-weighted mean
+// over i and its fluid neighbours (sum_j W_ij f_j / sum_j W_ij, self weight W(0)).
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_features(DevParams<T> P, DevBufs<T> B)
+{
+    count_launch(&B.sc->launches);
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const v4_t<T> xi = ldv(B.x, i);
+    const float4 f0 = *reinterpret_cast<const float4 *>(B.feat + (size_t)i * 8);
+    const float f4 = B.feat[(size_t)i * 8 + 4];
+    const float w0 = (float)P.K.w0;
+    float m[5] = {w0 * f0.x, w0 * f0.y, w0 * f0.z, w0 * f0.w, w0 * f4};
+    float wsum = w0;
+    struct XF {
+        v4_t<T> x;
+        float4 a;
+        float b;
+    };
+    nbr_loop<kUnroll>(list_ptr(B.lf, i, P.capf), min(B.nf[i], P.capf),
+                      [&](uint32_t j) {
+                          return XF{ldv(B.x, j), *reinterpret_cast<const float4 *>(B.feat + (size_t)j * 8),
+                                    B.feat[(size_t)j * 8 + 4]};
+                      },
+                      [&](uint32_t, const XF &d) {
+                          const V3<T> r = diff3<T>(xi, d.x);
+                          const float w = (float)kernel_W(P.K, dev_sqrt(dot(r, r)));
+                          m[0] += w * d.a.x; m[1] += w * d.a.y; m[2] += w * d.a.z; m[3] += w * d.a.w; m[4] += w * d.b;
+                          wsum += w;
+                      });
+    float *X = B.mlp_x + (size_t)i * 10;
+    X[0] = f0.x; X[1] = f0.y; X[2] = f0.z; X[3] = f0.w; X[4] = f4;
+    const float inv = 1.0f / wsum;
+#pragma unroll
+    for (int k = 0; k < 5; k++) X[5 + k] = m[k] * inv;
+}
+
+// Predicted warm start of one solver, with the same masks as the classic warm start:
+// divergence: kappa_v = out_v * s_v / h where the clamped source is positive and the
+// particle is not deficient (TimeStepDFSPH.cpp:424-453); pressure: kappa = out_p * s_p / h^2
+// where rho_adv > 1 (:293-296).  Negative predictions are clipped to zero.
+template <class T, bool DIV>
+__global__ void __launch_bounds__(kBlock) k_ws_kappa(DevParams<T> P, DevBufs<T> B)
+{
+    count_launch(&B.sc->launches);
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    T k = T(0);
+    if (DIV) {
+        const T h = (T)B.sc->dt;
+        if (B.dadv[i] > T(0) && B.nf[i] + B.nbn[i] >= 20u) k = (T)fmaxf(B.mlp_y[(size_t)i * 2] * P.ws_scale_v, 0.0f) / h;
+    } else {
+        const T h = (T)B.sc->dt_next;
+        if (B.dadv[i] > T(1)) k = (T)fmaxf(B.mlp_y[(size_t)i * 2 + 1] * P.ws_scale_p, 0.0f) / (h * h);
+    }
+    B.kl[i] = k;
+}
+
+// Pressure accelerations of both candidate warm starts: classic (xk.w) into pa, predicted (kl)
+// into pa2 (the computePressureAccel sum of TimeStepDFSPH.cpp:1299-1367 for each).
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_ws_accel2(DevParams<T> P, DevBufs<T> B)
+{
+    count_launch(&B.sc->launches);
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const v4_t<T> xi = ldv(B.xk, i);
+    const T pc = (T)xi.w, pl = B.kl[i];
+    V3<T> ac = mk3<T>(0, 0, 0), al = mk3<T>(0, 0, 0);
+    struct XK {
+        v4_t<T> x;
+        T kl;
+    };
+    nbr_loop<kUnroll>(list_ptr(B.lf, i, P.capf), min(B.nf[i], P.capf), [&](uint32_t j) { return XK{ldv(B.xk, j), B.kl[j]}; },
+                      [&](uint32_t, const XK &d) {
+                          const V3<T> r = diff3<T>(xi, d.x);
+                          const T c = grad_coef_d2(P.K, dot(r, r));
+                          const T sc_ = pc + (T)d.x.w, sl = pl + d.kl;
+                          if (fabs(sc_) > P.eps) ac = add(ac, scl(r, c * sc_));
+                          if (fabs(sl) > P.eps) al = add(al, scl(r, c * sl));
+                      });
+    const V3<T> gb = xyz<T>(ldv(B.bg, i));
+    V3<T> a1 = scl(ac, -P.V), a2 = scl(al, -P.V);
+    if (fabs(pc) > P.eps) a1 = sub(a1, scl(gb, pc));
+    if (fabs(pl) > P.eps) a2 = sub(a2, scl(gb, pl));
+    stv(B.pa, i, pack(a1, T(0)));
+    stv(B.pa2, i, pack(a2, T(0)));
+}
+
+// Initial residuals of both candidates (the error the first Jacobi iteration would report,
+// TimeStepDFSPH.cpp:621-706 / :544-619); the last block picks the predicted warm start only
+// if its residual is lower.
+template <class T, bool DIV>
+__global__ void __launch_bounds__(kBlock) k_ws_residual2(DevParams<T> P, DevBufs<T> B, ReduceSlot slot)
+{
+    count_launch(&B.sc->launches);
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    DSum<2> mine;
+    mine.v[0] = mine.v[1] = 0.0;
+    if (i < P.n) {
+        const v4_t<T> xi = ldv(B.x, i);
+        const V3<T> a1 = xyz<T>(ldv(B.pa, i)), a2 = xyz<T>(ldv(B.pa2, i));
+        T s1 = T(0), s2 = T(0);
+        struct XA {
+            v4_t<T> x, a, b;
+        };
+        nbr_loop<kUnroll>(list_ptr(B.lf, i, P.capf), min(B.nf[i], P.capf),
+                          [&](uint32_t j) { return XA{ldv(B.x, j), ldv(B.pa, j), ldv(B.pa2, j)}; },
+                          [&](uint32_t, const XA &d) {
+                              const V3<T> r = diff3<T>(xi, d.x);
+                              const T c = grad_coef_d2(P.K, dot(r, r));
+                              s1 += c * dot(sub(a1, xyz<T>(d.a)), r);
+                              s2 += c * dot(sub(a2, xyz<T>(d.b)), r);
+                          });
+        const V3<T> gb = xyz<T>(ldv(B.bg, i));
+        T ap1 = s1 * P.V + dot(a1, gb), ap2 = s2 * P.V + dot(a2, gb);
+        T si;
+        bool zero = false;
+        if (DIV) {
+            const T h = (T)B.sc->dt;
+            ap1 *= h;
+            ap2 *= h;
+            si = -B.dadv[i];
+            zero = B.nf[i] + B.nbn[i] < 20u;
+        } else {
+            const T h = (T)B.sc->dt_next;
+            ap1 *= h * h;
+            ap2 *= h * h;
+            si = T(1) - B.dadv[i];
+        }
+        const T r1 = (si - ap1) < T(0) ? (si - ap1) : T(0);
+        const T r2 = (si - ap2) < T(0) ? (si - ap2) : T(0);
+        if (!zero) {
+            mine.v[0] = -(double)P.rho0 * (double)r1;
+            mine.v[1] = -(double)P.rho0 * (double)r2;
+        }
+    }
+    StepScalars *sc = B.sc;
+    const uint32_t n = P.n;
+    grid_sum_finalize<2>(mine, slot, [&](const DSum<2> &tot) {
+        const int k = DIV ? 0 : 1;
+        sc->ws_rc[k] = tot.v[0] / (double)n;
+        sc->ws_rl[k] = tot.v[1] / (double)n;
+        if (tot.v[1] < tot.v[0]) sc->ws_used |= (1u << k);
+        else sc->ws_used &= ~(1u << k);
+    });
+}
+
+template <class T, bool DIV>
+__global__ void __launch_bounds__(kBlock) k_ws_apply(DevParams<T> P, DevBufs<T> B)
+{
+    count_launch(&B.sc->launches);
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    if (!(B.sc->ws_used & (1u << (DIV ? 0 : 1)))) return;
+    const T k = B.kl[i];
+    (DIV ? B.kappa_v : B.kappa)[i] = k;
+    store_w(B.xk, i, k);
+}
+
+// ==========================================================================
 // boundary set-up
 // ==========================================================================
 template <class T>
@@ -1119,6 +1293,10 @@ __global__ void k_scatter_field(DevParams<T> P, DevBufs<T> B, int field, void *o
     case SPHGB_FIELD_PARTICLE_ID: put<T>(out, odt, d, (double)B.id[k]); break;
     case SPHGB_FIELD_NUM_FLUID_NEIGHBORS: put<T>(out, odt, d, (double)B.nf[k]); break;
     case SPHGB_FIELD_NUM_BOUNDARY_NEIGHBORS: put<T>(out, odt, d, (double)B.nbn[k]); break;
+    case SPHGB_FIELD_FEATURES:
+        if (B.mlp_x)
+            for (int c = 0; c < 10; c++) put<T>(out, odt, 10 * (size_t)d + c, (double)B.mlp_x[(size_t)k * 10 + c]);
+        break;
     default: break;
     }
 }
@@ -1258,6 +1436,26 @@ template <class T> void launch_integrate(const DevParams<T> &P, const DevBufs<T>
 {
     k_integrate<T><<<grid_for(P.n > 0 ? P.n : 1), kBlock, 0, s>>>(P, B);
 }
+template <class T> void launch_features(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
+{
+    if (P.n) k_features<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
+}
+template <class T> void launch_warmstart_select(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s)
+{
+    if (!P.n) return;
+    ReduceSlot slot{B.partials, B.counter};
+    if (div) {
+        k_ws_kappa<T, true><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
+        k_ws_accel2<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
+        k_ws_residual2<T, true><<<grid_for(P.n), kBlock, 0, s>>>(P, B, slot);
+        k_ws_apply<T, true><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
+    } else {
+        k_ws_kappa<T, false><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
+        k_ws_accel2<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
+        k_ws_residual2<T, false><<<grid_for(P.n), kBlock, 0, s>>>(P, B, slot);
+        k_ws_apply<T, false><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
+    }
+}
 template <class T> void launch_boundary_keys(const DevParams<T> &P, const DevBufs<T> &B, const v4_t<T> *xb_in,
                                              uint32_t *keys, uint32_t *vals, cudaStream_t s)
 {
@@ -1323,6 +1521,8 @@ void launch_lists_to_ids(const uint32_t *list, const uint32_t *cnt, uint32_t cap
     template void launch_solver_finalize<T>(const DevParams<T> &, const DevBufs<T> &, bool, cudaStream_t);          \
     template void launch_loop_begin<T>(const DevParams<T> &, const DevBufs<T> &, bool, cudaStream_t);               \
     template void launch_step_begin<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                     \
+    template void launch_features<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                       \
+    template void launch_warmstart_select<T>(const DevParams<T> &, const DevBufs<T> &, bool, cudaStream_t);         \
     template void launch_xsph<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                           \
     template void launch_visc_setup<T>(const DevParams<T> &, const DevBufs<T> &, cudaGraphConditionalHandle, bool,  \
                                        cudaStream_t);                                                               \

@@ -20,6 +20,7 @@ struct StepScalars {
     double avg_err;     // pressure solve
     double avg_err_v;   // divergence solve
     double cg_rhs2, cg_thresh, cg_res2, cg_absnew, cg_alpha, cg_beta, cg_err;
+    double ws_rc[2], ws_rl[2];   // initial residuals of the classic / learned warm start (div, pressure)
     unsigned iters, iters_v, iters_cg;
     unsigned cont;      // 1 while the running solver loop continues
     unsigned cg_state;  // 0 running, 1 converged / no iteration, 2 zero right-hand side
@@ -29,7 +30,8 @@ struct StepScalars {
     unsigned prev_iters;
     unsigned loop_guard;   // body executions of the running device-side loop
     unsigned launches;     // kernels launched in the current step (counted on the device)
-    unsigned pad[1];
+    unsigned ws_used;      // bit 0: learned warm start used by the divergence solve, bit 1: pressure solve
+    unsigned pad[2];
 };
 
 constexpr unsigned kFlagOverflow = 1u;
@@ -52,6 +54,8 @@ template <class T> struct DevParams {
     double visc_tol;
     unsigned min_iter, max_iter, max_iter_v, visc_max_iter;
     int cfl_method, visc_on, div_on;
+    int learned, feat_on;         // learned warm start on; features computed
+    float ws_scale_v, ws_scale_p; // network output scales
     // grid
     T ox, oy, oz, inv_cell;
     int dimx, dimy, dimz;
@@ -83,6 +87,14 @@ template <class T> struct DevBufs {
     uint32_t *bcstart, *bcend;
     v4 *xb;                      // sorted boundary positions, w = volume
     T *bscratch;                 // nb scratch values (boundary volume set-up)
+    // learned warm start
+    float *feat;                 // raw features, 8 floats per particle (5 used)
+    float *mlp_x;                // network inputs, 10 floats per particle
+    float *mlp_y;                // network outputs, 2 floats per particle
+    T *kl;                       // predicted warm start of the running solver
+    v4 *pa2;                     // pressure acceleration of the predicted warm start
+    const void *mlp_w;           // BF16 weights
+    const float *mlp_p;          // FP32 parameters (biases)
     uint32_t *bid;               // upload index of each sorted boundary particle
     // CG
     v4 *cg_x, *cg_r, *cg_p, *cg_z, *cg_t;
@@ -120,6 +132,9 @@ template <class T> void launch_integrate(const DevParams<T> &P, const DevBufs<T>
 template <class T> void launch_step_begin(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
 template <class T> void launch_loop_begin(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s);
 template <class T> void launch_boundary_volume(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
+template <class T> void launch_features(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
+template <class T> void launch_warmstart_select(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s);
+void mlp_infer_device(const float *X, uint32_t n, const void *w, const float *p, float *Y, cudaStream_t s);
 template <class T> void launch_boundary_keys(const DevParams<T> &P, const DevBufs<T> &B, const v4_t<T> *xb_in,
                                              uint32_t *keys, uint32_t *vals, cudaStream_t s);
 template <class T> void launch_boundary_gather(const DevParams<T> &P, const DevBufs<T> &B, const v4_t<T> *xb_in,

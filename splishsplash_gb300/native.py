@@ -36,6 +36,7 @@ FIELDS = {
     "boundary neighbors": (13, 1),
     "boundary volume": (14, 1),
     "boundary position": (15, 3),
+    "features": (16, 10),
 }
 DTYPE_F32, DTYPE_F64, DTYPE_U32 = 0, 1, 2
 
@@ -97,10 +98,18 @@ class Stats(ctypes.Structure):
         ("dt_next", ctypes.c_double),
         ("time", ctypes.c_double),
         ("kernel_launches", ctypes.c_uint64),
+        ("learned_used", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
+        ("ws_residual_classic", ctypes.c_double * 2),
+        ("ws_residual_learned", ctypes.c_double * 2),
     ]
 
     def as_dict(self):
-        return {name: getattr(self, name) for name, _ in self._fields_}
+        out = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            out[name] = list(v) if isinstance(v, ctypes.Array) else v
+        return out
 
 
 EXPORTS = [
@@ -109,6 +118,7 @@ EXPORTS = [
     "sphgb_upload_fluid", "sphgb_upload_fluid_f32", "sphgb_set_time_step", "sphgb_get_time_step",
     "sphgb_set_time", "sphgb_step", "sphgb_sync", "sphgb_download", "sphgb_upload_field", "sphgb_neighbors",
     "sphgb_num_particles", "sphgb_get_stream", "sphgb_profile_enable", "sphgb_profile_reset", "sphgb_profile_read",
+    "sphgb_set_warmstart_mlp", "sphgb_set_feature_output",
 ]
 
 _lib = None
@@ -151,6 +161,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.sphgb_neighbors.argtypes = [vp, i32, vp, vp, ctypes.c_size_t]
     L.sphgb_num_particles.argtypes = [vp, ctypes.POINTER(u32), ctypes.POINTER(u32)]
     L.sphgb_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
+    L.sphgb_set_warmstart_mlp.argtypes = [vp, vp]
+    L.sphgb_set_feature_output.argtypes = [vp, i32]
     L.sphgb_profile_enable.argtypes = [vp, i32]
     L.sphgb_profile_reset.argtypes = [vp]
     L.sphgb_profile_read.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_uint64),
@@ -190,6 +202,94 @@ def params_from(sp) -> Params:
     q.visco_max_iter = sp.viscoMaxIter
     q.visco_max_error = sp.viscoMaxError
     return q
+
+
+class Mlp:
+    """The warm-start network (sphgb_mlp): BF16 tensor-core forward, hand-written backward/Adam."""
+
+    def __init__(self, device: int = 0, seed: int = 1):
+        self.L = load()
+        L = self.L
+        vp, u32, f32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_float
+        L.sphgb_mlp_create.argtypes = [ctypes.c_int, u32, ctypes.POINTER(vp)]
+        L.sphgb_mlp_destroy.argtypes = [vp]
+        L.sphgb_mlp_last_error.argtypes = [vp]
+        L.sphgb_mlp_last_error.restype = ctypes.c_char_p
+        L.sphgb_mlp_num_params.restype = ctypes.c_int
+        L.sphgb_mlp_get_params.argtypes = [vp, vp]
+        L.sphgb_mlp_set_params.argtypes = [vp, vp]
+        L.sphgb_mlp_set_output_scale.argtypes = [vp, f32, f32]
+        L.sphgb_mlp_get_output_scale.argtypes = [vp, ctypes.POINTER(f32), ctypes.POINTER(f32)]
+        L.sphgb_mlp_forward.argtypes = [vp, vp, u32, vp]
+        L.sphgb_mlp_loss_grad.argtypes = [vp, vp, vp, vp, u32, ctypes.POINTER(f32), vp]
+        L.sphgb_mlp_train.argtypes = [vp, vp, vp, vp, u32, u32, u32, f32, u32, vp]
+        for name in ("sphgb_mlp_create", "sphgb_mlp_destroy", "sphgb_mlp_get_params", "sphgb_mlp_set_params",
+                     "sphgb_mlp_set_output_scale", "sphgb_mlp_get_output_scale", "sphgb_mlp_forward",
+                     "sphgb_mlp_loss_grad", "sphgb_mlp_train"):
+            getattr(L, name).restype = ctypes.c_int
+        h = ctypes.c_void_p()
+        rc = L.sphgb_mlp_create(device, seed, ctypes.byref(h))
+        if rc != OK:
+            raise SphgbError(rc, "sphgb_mlp_create failed (no CUDA device?)")
+        self.h = h
+        self.n_params = int(L.sphgb_mlp_num_params())
+
+    def _check(self, rc):
+        if rc != OK:
+            raise SphgbError(rc, self.L.sphgb_mlp_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.sphgb_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self) -> np.ndarray:
+        out = np.zeros(self.n_params, np.float32)
+        self._check(self.L.sphgb_mlp_get_params(self.h, _p(out)))
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == self.n_params
+        self._check(self.L.sphgb_mlp_set_params(self.h, _p(p)))
+
+    def set_output_scale(self, scale_v: float, scale_p: float):
+        self._check(self.L.sphgb_mlp_set_output_scale(self.h, scale_v, scale_p))
+
+    def output_scale(self):
+        a, b = ctypes.c_float(), ctypes.c_float()
+        self._check(self.L.sphgb_mlp_get_output_scale(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def forward(self, X) -> np.ndarray:
+        X = np.ascontiguousarray(X, np.float32)
+        Y = np.zeros((X.shape[0], 2), np.float32)
+        self._check(self.L.sphgb_mlp_forward(self.h, _p(X), X.shape[0], _p(Y)))
+        return Y
+
+    def loss_grad(self, X, T, mask=None):
+        X = np.ascontiguousarray(X, np.float32)
+        T = np.ascontiguousarray(T, np.float32)
+        M = None if mask is None else np.ascontiguousarray(mask, np.float32)
+        g = np.zeros(self.n_params, np.float32)
+        loss = ctypes.c_float()
+        self._check(self.L.sphgb_mlp_loss_grad(self.h, _p(X), _p(T), _p(M), X.shape[0], ctypes.byref(loss), _p(g)))
+        return float(loss.value), g
+
+    def train(self, X, T, mask=None, epochs=10, batch=4096, lr=1e-3, seed=0):
+        X = np.ascontiguousarray(X, np.float32)
+        T = np.ascontiguousarray(T, np.float32)
+        M = None if mask is None else np.ascontiguousarray(mask, np.float32)
+        losses = np.zeros(epochs, np.float32)
+        self._check(self.L.sphgb_mlp_train(self.h, _p(X), _p(T), _p(M), X.shape[0], epochs, batch, lr, seed,
+                                           _p(losses)))
+        return losses
 
 
 class Context:
@@ -296,6 +396,13 @@ class Context:
             a = np.ascontiguousarray(a, dtype=np.float64)
         dt = DTYPE_F32 if a.dtype == np.float32 else DTYPE_F64
         self._check(self.L.sphgb_upload_field(self.h, fid, _p(a), dt))
+
+    def set_warmstart_mlp(self, mlp):
+        """Use a trained network for both warm starts (None: classic warm start only)."""
+        self._check(self.L.sphgb_set_warmstart_mlp(self.h, None if mlp is None else mlp.h))
+
+    def set_feature_output(self, on: bool = True):
+        self._check(self.L.sphgb_set_feature_output(self.h, int(on)))
 
     def stream(self) -> int:
         """cudaStream_t (as an integer) that every kernel of this context runs on."""

@@ -159,11 +159,12 @@ def dambreak_1m(seed: int = 1001, viscosity: bool = True, nz: int = 128) -> Scen
     return Scene(name, x, np.zeros_like(x), xb, p, np.zeros(3), np.array([6.0, 3.0, 3.0]))
 
 
-def precision_4m(seed: int = 1002) -> Scene:
-    """256x64x256 block (4,194,304) at 0.02 in an 11x3x11 m box, walls at 0.0125 m."""
+def precision_4m(seed: int = 1002, counts=(256, 64, 256)) -> Scene:
+    """256x64x256 block (4,194,304) at 0.02 in an 11x3x11 m box, walls at 0.0125 m
+    (2,393,602 boundary particles).  `counts` shrinks the block for quick runs."""
     p = SPHParams(particleRadius=0.01, viscosityMethod=6, viscosity=0.01)
     rng = np.random.default_rng(seed)
-    x = fluid_block((256, 64, 256), 0.02, (0.02, 0.02, 0.02), p.particleRadius, rng)
+    x = fluid_block(tuple(counts), 0.02, (0.02, 0.02, 0.02), p.particleRadius, rng)
     xb = box_walls((0, 0, 0), (11, 3, 11), 0.0125)
     return Scene("precision_4m", x, np.zeros_like(x), xb, p, np.zeros(3), np.array([11.0, 3.0, 11.0]))
 
