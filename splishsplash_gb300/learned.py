@@ -105,7 +105,12 @@ def run(scene, steps, net=None, warmup=0, use_graph=True):
 def summarize(stats, ms, rho, rho0=1000.0):
     it = np.array([[s["iterations"], s["iterations_v"]] for s in stats], float)
     used = np.array([s["learned_used"] for s in stats])
+    rc = np.array([s["ws_residual_classic"] for s in stats], float)
+    rl = np.array([s["ws_residual_learned"] for s in stats], float)
+    ratio = np.where(rc > 0, rl / np.maximum(rc, 1e-300), 1.0)
     return {
+        "initial_residual_ratio_learned_over_classic_median": [float(np.median(ratio[:, 0])),
+                                                                float(np.median(ratio[:, 1]))],
         "pressure_iterations_mean": float(it[:, 0].mean()),
         "divergence_iterations_mean": float(it[:, 1].mean()),
         "solver_iterations_total": float(it.sum()),
@@ -132,7 +137,8 @@ def evaluate(scene, net, steps=300, warmup=0):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=None, help="directory for the report (weights go to the package data dir)")
-    ap.add_argument("--scenes", type=int, default=24)
+    ap.add_argument("--scenes", type=int, default=12)
+    ap.add_argument("--settling", type=int, default=3)
     ap.add_argument("--steps", type=int, default=120)
     ap.add_argument("--epochs", type=int, default=40)
     ap.add_argument("--eval-steps", type=int, default=300)
@@ -140,7 +146,12 @@ def main():
     args = ap.parse_args()
     t0 = time.time()
     ens = scenes.ensemble(num_scenes=256)
-    train_scenes = ens[: args.scenes]
+    # ensemble dam breaks plus settling columns around a sphere (the evaluation scene's kind,
+    # smaller and with other seeds and proportions)
+    settle = [scenes.settling_sphere(counts=c, box=b, sphere_radius=r, seed=2000 + k)
+              for k, (c, b, r) in enumerate([((48, 48, 48), (2.4, 1.6, 2.4), 0.4), ((64, 56, 64), (3.0, 2.0, 3.0), 0.5),
+                                             ((40, 64, 56), (2.2, 2.0, 2.6), 0.45)][: args.settling])]
+    train_scenes = ens[: args.scenes] + settle
     X, Y = collect(train_scenes, steps=args.steps)
     t_collect = time.time() - t0
     net, losses = train(X, Y, epochs=args.epochs)
@@ -148,7 +159,7 @@ def main():
     save(net)
     sc = scenes.learned_2m() if args.eval_scene == "learned_2m" else scenes.dambreak_1m()
     res = evaluate(sc, net, steps=args.eval_steps)
-    report = {"training": {"scenes": args.scenes, "samples": int(X.shape[0]), "epochs": args.epochs,
+    report = {"training": {"scenes": [s.name for s in train_scenes], "samples": int(X.shape[0]), "epochs": args.epochs,
                            "loss_first": float(losses[0]), "loss_last": float(losses[-1]),
                            "collect_s": t_collect, "train_s": t_train},
               "evaluation_scene": f"{sc.name}: {sc.n} fluid + {sc.nb} boundary", **res}

@@ -212,6 +212,23 @@ def learned_2m(seed: int = 1004) -> Scene:
     return Scene("learned_2m", x, np.zeros_like(x), xb, p, np.zeros(3), np.array([6.0, 4.0, 6.0]))
 
 
+def settling_sphere(counts=(64, 64, 64), box=(3.0, 2.0, 3.0), sphere_radius=0.5, seed: int = 2000) -> Scene:
+    """A smaller scene of the learned-warm-start configuration's kind: a jittered block at
+    0.02 m (r = 0.01) falling around a sphere obstacle at the box centre (fluid within
+    radius + 2r of the centre removed), walls and sphere sampled at 0.012 m."""
+    p = SPHParams(particleRadius=0.01)
+    rng = np.random.default_rng(seed)
+    box = np.asarray(box, dtype=np.float64)
+    c = box / 2.0
+    ext = np.asarray(counts, dtype=np.float64) * 0.02
+    corner = c - ext / 2.0
+    corner[1] = 0.02
+    x = fluid_block(tuple(counts), 0.02, corner, p.particleRadius, rng)
+    x = x[np.linalg.norm(x - c, axis=1) > sphere_radius + 2 * p.particleRadius]
+    xb = np.concatenate([box_walls((0, 0, 0), box, 0.012), sphere_surface(c, sphere_radius, 0.012)], 0)
+    return Scene(f"settling_sphere_{seed}", x, np.zeros_like(x), xb, p, np.zeros(3), box)
+
+
 def small_block(counts=(8, 8, 8), radius=0.025, seed: int = 7, box=(0.8, 0.8, 0.8), corner=None,
                 jitter=0.01, viscosity=False, velocity=None) -> Scene:
     """A small jittered block in a closed box, for parity tests."""
