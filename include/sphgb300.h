@@ -169,8 +169,27 @@ int sphgb_upload_field(sphgb_ctx *ctx, int field, const void *src, int dtype);
  * indices == NULL to query offsets only. */
 int sphgb_neighbors(sphgb_ctx *ctx, int kind, uint32_t *offsets, uint32_t *indices, size_t capacity);
 
-/* counts */
+/* counts (all scenes of a batch) */
 int sphgb_num_particles(const sphgb_ctx *ctx, uint32_t *n, uint32_t *nb);
+
+/* ---- batched scenes (no counterpart in the reference: it simulates one scene per process,
+ * Simulation::getCurrent at Simulation.cpp:112-119) ----
+ * Replaces the fluid and the boundary of the context with nscenes independent scenes that
+ * advance together: every kernel launch of a step covers all scenes, each scene keeps its own
+ * cell grid, CFL step size, solver iteration counts and convergence decisions (a scene whose
+ * solver converged idles while the others iterate), and with use_graph = 1 a step of the whole
+ * batch is one graph launch.  n[s] >= 1 fluid and nb[s] >= 0 boundary particles per scene;
+ * x and v hold the scenes' fluid particles concatenated in scene order (sum(n) x 3), xb the
+ * boundary particles (sum(nb) x 3).  Particle ids (the download order of every field) are this
+ * concatenated order.  Parameters (sphgb_set_params) and the network are shared by all scenes;
+ * sphgb_set_time_step / sphgb_set_time set every scene.  sphgb_step's stats for a batch: scene
+ * 0's times, the maxima over the scenes of iteration counts and errors, the OR of the flags.
+ * sphgb_upload_fluid / sphgb_upload_boundary switch the context back to one scene. */
+int sphgb_upload_scenes(sphgb_ctx *ctx, uint32_t nscenes, const uint32_t *n, const uint32_t *nb, const double *x,
+                        const double *v, const double *xb);
+int sphgb_num_scenes(const sphgb_ctx *ctx, uint32_t *nscenes);
+/* statistics of scenes first .. first+count-1 of the last step (waits for it) */
+int sphgb_scene_stats(sphgb_ctx *ctx, uint32_t first, uint32_t count, sphgb_stats *out);
 
 /* ---- learned warm start (no counterpart in the reference: new in this library) ----
  * A per-particle network 10 -> 64 -> 64 -> 2 (GELU), BF16 weights and activations on the

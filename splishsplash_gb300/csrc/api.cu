@@ -7,6 +7,11 @@
 // the whole step is captured once into a CUDA graph whose loops are conditional
 // WHILE nodes driven by the kernels (use_graph = 1), so a step is one graph
 // launch with no host round trip.
+//
+// A context holds one scene (the reference's case) or a batch of independent
+// scenes.  Scene s owns the fluid slots [pstart_s, pstart_s + n_s) (pstart_s a
+// multiple of the block size for batches), its own cell grid inside shared cell
+// tables, its own step size and solver decisions; every launch covers all scenes.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -26,6 +31,19 @@ namespace sphgb {
 void mlp_export(const sphgb_mlp *m, const float **params, const void **w, float scale[2], int *device);
 }
 
+namespace {
+struct SceneHost {
+    uint32_t n = 0, nb = 0;            // fluid / boundary particles
+    uint32_t ustart = 0, bstart = 0;   // first fluid / boundary particle in upload order
+    uint32_t pstart = 0;               // first fluid slot
+    double fmin[3] = {0, 0, 0}, fmax[3] = {0, 0, 0}, bmin[3] = {0, 0, 0}, bmax[3] = {0, 0, 0};
+    double org[3] = {0, 0, 0};         // cell grid
+    int dim[3] = {1, 1, 1};
+    uint32_t cell_off = 0;
+    double dt = 0.001, time = 0.0;     // host copies, valid while no step is pending
+};
+}  // namespace
+
 struct sphgb_ctx {
     sphgb_config cfg{};
     sphgb_params prm{};
@@ -33,17 +51,19 @@ struct sphgb_ctx {
     cudaStream_t body_stream = nullptr;
     std::string err;
     bool fp64 = false;
-    uint32_t n = 0, nb = 0;
-    // host-side extents of the uploaded data
-    double fmin[3] = {0, 0, 0}, fmax[3] = {0, 0, 0}, bmin[3] = {0, 0, 0}, bmax[3] = {0, 0, 0};
+    // scenes
+    std::vector<SceneHost> scn;
+    uint32_t n = 0;                    // fluid particles of all scenes
+    uint32_t np = 0;                   // fluid slots (launch size)
+    uint32_t nb = 0;                   // boundary particles of all scenes
+    std::vector<double> hb;            // boundary positions (host copy, scene order)
     bool have_fluid = false, have_boundary = false, prepared = false;
     // grid
-    double org[3] = {0, 0, 0}, cell = 0;
-    int dim[3] = {0, 0, 0};
-    int key_bits = 0;
+    double cell = 0;
+    int key_bits = 0, morton_bits = 0;
     size_t ncell = 0;
-    // allocations
-    std::vector<void *> allocs;
+    // allocations: per-particle buffers (allocs) and the grid / boundary set-up (prep_allocs)
+    std::vector<void *> allocs, prep_allocs;
     void *set_x[2] = {}, *set_v[2] = {}, *set_vdiff[2] = {}, *set_kappa[2] = {}, *set_kappa_v[2] = {};
     float4 *set_xlo[2] = {};
     uint32_t *set_id[2] = {};
@@ -51,25 +71,27 @@ struct sphgb_ctx {
     uint32_t *nfc = nullptr, *nbc = nullptr, *lf = nullptr, *lb = nullptr;
     uint32_t *key = nullptr, *key2 = nullptr, *perm = nullptr, *perm2 = nullptr, *cell0 = nullptr, *cell1 = nullptr;
     uint32_t *cstart = nullptr, *cend = nullptr, *bcstart = nullptr, *bcend = nullptr;
-    void *xb = nullptr, *xb_raw = nullptr, *bscratch = nullptr;
-    uint32_t *bid = nullptr;
+    void *xb = nullptr, *bscratch = nullptr;
+    uint32_t *bid = nullptr, *bscene = nullptr;
+    void *d_scenes = nullptr;
+    uint4 *d_blk = nullptr;
     void *cg[5] = {}, *inv[3] = {};
     double *partials = nullptr;
-    unsigned *counter = nullptr;
-    StepScalars *sc = nullptr;
-    StepScalars *hsc = nullptr;   // pinned mirror
+    unsigned *counters = nullptr;      // [scenes + 1]
+    StepScalars *sc = nullptr;         // [scenes + 1]: per-scene records, then the global one
+    StepScalars *hsc = nullptr;        // pinned mirror
+    size_t hsc_cap = 0;
     uint32_t *hist = nullptr;
     uint32_t *inv_perm = nullptr;
     void *staging = nullptr;
     size_t staging_bytes = 0;
     int parity = 0;
-    bool scalars_dirty = true;    // host dt/time changed since the last upload of scalars
-    double dt = 0.001, time = 0.0;
+    bool scalars_dirty = true;         // host dt/time changed since the last upload of scalars
+    double dt = 0.001;                 // step size given to every scene on upload / set_time_step
     // graphs (one per parity)
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
     bool graph_ok = false;
     bool step_pending = false;
-    uint64_t launches_last_step = 0;
     // learned warm start: network copy and per-particle buffers
     bool learned = false, feat_on = false;
     float *mlp_p = nullptr;
@@ -84,6 +106,8 @@ struct sphgb_ctx {
     std::vector<Rec> recs;
     uint64_t prof_count[32] = {};
     double prof_ms[32] = {};
+
+    uint32_t nscenes() const { return scn.empty() ? 1u : (uint32_t)scn.size(); }
 };
 
 namespace {
@@ -159,24 +183,25 @@ int fail(sphgb_ctx *c, int code, const std::string &msg)
             return fail(c, SPHGB_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));   \
     } while (0)
 
-template <class P> int dalloc(sphgb_ctx *c, P **p, size_t bytes)
+template <class P> int dalloc_into(sphgb_ctx *c, std::vector<void *> &list, P **p, size_t bytes)
 {
     void *q = nullptr;
     if (bytes == 0) bytes = 16;
     cudaError_t e = cudaMalloc(&q, bytes);
     if (e != cudaSuccess) return fail(c, SPHGB_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
-    c->allocs.push_back(q);
+    list.push_back(q);
     *p = static_cast<P *>(q);
     return SPHGB_OK;
 }
+template <class P> int dalloc(sphgb_ctx *c, P **p, size_t bytes) { return dalloc_into(c, c->allocs, p, bytes); }
+template <class P> int palloc(sphgb_ctx *c, P **p, size_t bytes) { return dalloc_into(c, c->prep_allocs, p, bytes); }
 
-void free_all(sphgb_ctx *c)
+// free one allocation of a list (temporaries)
+void dfree(std::vector<void *> &list, void *p)
 {
-    for (void *p : c->allocs) cudaFree(p);
-    c->allocs.clear();
-    for (int k = 0; k < 2; k++)
-        if (c->exec[k]) { cudaGraphExecDestroy(c->exec[k]); c->exec[k] = nullptr; }
-    c->graph_ok = false;
+    auto it = std::find(list.begin(), list.end(), p);
+    if (it != list.end()) list.erase(it);
+    cudaFree(p);
 }
 
 void invalidate_graphs(sphgb_ctx *c)
@@ -186,8 +211,50 @@ void invalidate_graphs(sphgb_ctx *c)
     c->graph_ok = false;
 }
 
+void free_prepared(sphgb_ctx *c)
+{
+    for (void *p : c->prep_allocs) cudaFree(p);
+    c->prep_allocs.clear();
+    c->cstart = c->cend = c->bcstart = c->bcend = nullptr;
+    c->xb = c->bscratch = nullptr;
+    c->bid = c->bscene = nullptr;
+    c->prepared = false;
+}
+
+void free_all(sphgb_ctx *c)
+{
+    free_prepared(c);
+    for (void *p : c->allocs) cudaFree(p);
+    c->allocs.clear();
+    invalidate_graphs(c);
+}
+
 size_t real_size(const sphgb_ctx *c) { return c->fp64 ? sizeof(double) : sizeof(float); }
 size_t vec_size(const sphgb_ctx *c) { return c->fp64 ? sizeof(dquad) : sizeof(float4); }
+
+template <class T> SceneDev<T> scene_dev(const sphgb_ctx *c, uint32_t s)
+{
+    SceneDev<T> S{};
+    if (c->scn.empty()) {
+        S.dimx = S.dimy = S.dimz = 1;
+        S.inv_cell = T(1);
+        return S;
+    }
+    const SceneHost &h = c->scn[s];
+    S.ox = (T)h.org[0];
+    S.oy = (T)h.org[1];
+    S.oz = (T)h.org[2];
+    S.inv_cell = (T)(c->cell > 0 ? 1.0 / c->cell : 1.0);
+    S.dimx = h.dim[0];
+    S.dimy = h.dim[1];
+    S.dimz = h.dim[2];
+    S.cell_off = h.cell_off;
+    S.pstart = h.pstart;
+    S.n = h.n;
+    S.ustart = h.ustart;
+    S.key_prefix = c->scn.size() > 1 ? (s << c->morton_bits) : 0u;
+    return S;
+}
 
 template <class T> DevParams<T> make_params(const sphgb_ctx *c)
 {
@@ -234,14 +301,12 @@ template <class T> DevParams<T> make_params(const sphgb_ctx *c)
     P.feat_on = (c->learned || c->feat_on) ? 1 : 0;
     P.ws_scale_v = c->ws_scale[0];
     P.ws_scale_p = c->ws_scale[1];
-    P.ox = (T)c->org[0];
-    P.oy = (T)c->org[1];
-    P.oz = (T)c->org[2];
-    P.inv_cell = (T)(1.0 / c->cell);
-    P.dimx = c->dim[0];
-    P.dimy = c->dim[1];
-    P.dimz = c->dim[2];
-    P.n = c->n;
+    P.nscenes = c->nscenes();
+    P.s0 = scene_dev<T>(c, 0);
+    P.scenes = P.nscenes > 1 ? static_cast<const SceneDev<T> *>(c->d_scenes) : nullptr;
+    P.blk = P.nscenes > 1 ? c->d_blk : nullptr;
+    P.np = c->np;
+    P.nreal = c->n;
     P.nb = c->nb;
     P.capf = c->cfg.max_fluid_neighbors;
     P.capb = c->cfg.max_boundary_neighbors;
@@ -293,6 +358,8 @@ template <class T> DevBufs<T> make_bufs(const sphgb_ctx *c, int view)
     B.bcend = c->bcend;
     B.xb = (v4 *)c->xb;
     B.bscratch = (T *)c->bscratch;
+    B.bid = c->bid;
+    B.bscene = c->bscene;
     B.feat = c->feat;
     B.mlp_x = c->mlp_x;
     B.mlp_y = c->mlp_y;
@@ -300,7 +367,6 @@ template <class T> DevBufs<T> make_bufs(const sphgb_ctx *c, int view)
     B.pa2 = (v4 *)c->pa2;
     B.mlp_w = c->mlp_w;
     B.mlp_p = c->mlp_p;
-    B.bid = c->bid;
     B.cg_x = (v4 *)c->cg[0];
     B.cg_r = (v4 *)c->cg[1];
     B.cg_p = (v4 *)c->cg[2];
@@ -309,85 +375,139 @@ template <class T> DevBufs<T> make_bufs(const sphgb_ctx *c, int view)
     B.inv0 = (v4 *)c->inv[0];
     B.inv1 = (v4 *)c->inv[1];
     B.partials = c->partials;
-    B.counter = c->counter;
+    B.counters = c->counters;
     B.sc = c->sc;
+    B.gsc = c->sc ? c->sc + c->nscenes() : nullptr;
     B.hist = c->hist;
-    B.num_tiles = (c->n + kSortTile - 1) / kSortTile;
     return B;
+}
+
+template <class T> int upload_scene_table(sphgb_ctx *c)
+{
+    if (c->scn.size() <= 1) return SPHGB_OK;
+    std::vector<SceneDev<T>> t(c->scn.size());
+    for (uint32_t s = 0; s < c->scn.size(); s++) t[s] = scene_dev<T>(c, s);
+    CK(cudaMemcpy(c->d_scenes, t.data(), t.size() * sizeof(SceneDev<T>), cudaMemcpyHostToDevice));
+    return SPHGB_OK;
 }
 
 int upload_scalars(sphgb_ctx *c)
 {
     if (!c->scalars_dirty) return SPHGB_OK;
+    const uint32_t S = c->nscenes();
     CK(cudaStreamSynchronize(c->stream));
-    CK(cudaMemcpy(c->hsc, c->sc, sizeof(StepScalars), cudaMemcpyDeviceToHost));
-    c->hsc->dt = c->dt;
-    c->hsc->dt_next = c->dt;
-    c->hsc->time = c->time;
-    CK(cudaMemcpy(c->sc, c->hsc, sizeof(StepScalars), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->hsc, c->sc, (S + 1) * sizeof(StepScalars), cudaMemcpyDeviceToHost));
+    for (uint32_t s = 0; s < S; s++) {
+        const double dt = c->scn.empty() ? c->dt : c->scn[s].dt;
+        const double t = c->scn.empty() ? 0.0 : c->scn[s].time;
+        c->hsc[s].dt = dt;
+        c->hsc[s].dt_next = dt;
+        c->hsc[s].time = t;
+    }
+    CK(cudaMemcpy(c->sc, c->hsc, (S + 1) * sizeof(StepScalars), cudaMemcpyHostToDevice));
     c->scalars_dirty = false;
     return SPHGB_OK;
 }
 
-// Build the cell grid over the union of fluid and boundary extents, sort the
-// boundary particles into it and compute their Akinci2012 volumes.
+int bits_for(size_t v)
+{
+    int b = 0;
+    while (((size_t)1 << b) < v) b++;
+    return b;
+}
+
+// Build each scene's cell grid over the union of its fluid and boundary extents,
+// sort the boundary particles into it and compute their Akinci2012 volumes.
 template <class T> int prepare(sphgb_ctx *c)
 {
     if (!c->have_fluid) return fail(c, SPHGB_ERR_STATE, "no fluid uploaded");
+    free_prepared(c);
+    invalidate_graphs(c);
     const double h = 4.0 * c->prm.particle_radius;
     // slightly larger than the support radius: keeps |dx| < h => |cell delta| <= 1 under float rounding
     c->cell = h * 1.001;
-    double lo[3], hi[3];
-    for (int d = 0; d < 3; d++) {
-        lo[d] = c->fmin[d];
-        hi[d] = c->fmax[d];
-        if (c->have_boundary && c->nb > 0) {
-            lo[d] = std::min(lo[d], c->bmin[d]);
-            hi[d] = std::max(hi[d], c->bmax[d]);
-        }
-    }
-    size_t ncell = 1;
+    size_t off = 0;
     int maxdim = 1;
-    for (int d = 0; d < 3; d++) {
-        c->org[d] = lo[d] - c->cell;
-        const double ext = hi[d] - c->org[d];
-        c->dim[d] = (int)std::floor(ext / c->cell) + 2;
-        if (c->dim[d] > 1024) return fail(c, SPHGB_ERR_GRID, "scene extent exceeds 1024 cells per axis");
-        maxdim = std::max(maxdim, c->dim[d]);
-        ncell *= (size_t)c->dim[d];
+    for (SceneHost &S : c->scn) {
+        size_t nc = 1;
+        for (int d = 0; d < 3; d++) {
+            double lo = S.fmin[d], hi = S.fmax[d];
+            if (S.nb > 0) {
+                lo = std::min(lo, S.bmin[d]);
+                hi = std::max(hi, S.bmax[d]);
+            }
+            S.org[d] = lo - c->cell;
+            const double ext = hi - S.org[d];
+            const double nd = std::floor(ext / c->cell) + 2;
+            if (!(nd <= 1024.0)) return fail(c, SPHGB_ERR_GRID, "scene extent exceeds 1024 cells per axis");
+            S.dim[d] = (int)nd;
+            maxdim = std::max(maxdim, S.dim[d]);
+            nc *= (size_t)S.dim[d];
+        }
+        S.cell_off = (uint32_t)off;
+        off += nc;
+        if (off >= 0xffffffffull) return fail(c, SPHGB_ERR_GRID, "more than 2^32 cells in the scenes' grids");
     }
-    int bits = 1;
-    while ((1 << bits) < maxdim) bits++;
-    c->key_bits = 3 * bits;
-    c->ncell = ncell;
+    c->ncell = std::max<size_t>(off, 1);
+    c->morton_bits = 3 * std::max(1, bits_for((size_t)maxdim));
+    const int scene_bits = c->scn.size() > 1 ? bits_for(c->scn.size()) : 0;
+    c->key_bits = c->morton_bits + scene_bits;
+    if (c->key_bits > 32)
+        return fail(c, SPHGB_ERR_GRID, "scene count and grid size need more than 32 sort-key bits");
     int rc;
-    if ((rc = dalloc(c, &c->cstart, ncell * 4))) return rc;
-    if ((rc = dalloc(c, &c->cend, ncell * 4))) return rc;
-    if ((rc = dalloc(c, &c->bcstart, ncell * 4))) return rc;
-    if ((rc = dalloc(c, &c->bcend, ncell * 4))) return rc;
-    CK(cudaMemsetAsync(c->bcstart, 0xff, ncell * 4, c->stream));
+    if ((rc = palloc(c, &c->cstart, c->ncell * 4))) return rc;
+    if ((rc = palloc(c, &c->cend, c->ncell * 4))) return rc;
+    if ((rc = palloc(c, &c->bcstart, c->ncell * 4))) return rc;
+    if ((rc = palloc(c, &c->bcend, c->ncell * 4))) return rc;
+    CK(cudaMemsetAsync(c->bcstart, 0xff, c->ncell * 4, c->stream));
+    if ((rc = upload_scene_table<T>(c))) return rc;
     const uint32_t nb = c->nb;
-    if ((rc = dalloc(c, &c->xb, (size_t)std::max(nb, 1u) * vec_size(c)))) return rc;
-    if ((rc = dalloc(c, &c->bid, (size_t)std::max(nb, 1u) * 4))) return rc;
-    if ((rc = dalloc(c, &c->bscratch, (size_t)std::max(nb, 1u) * real_size(c)))) return rc;
+    if ((rc = palloc(c, &c->xb, (size_t)std::max(nb, 1u) * vec_size(c)))) return rc;
+    if ((rc = palloc(c, &c->bid, (size_t)std::max(nb, 1u) * 4))) return rc;
+    if ((rc = palloc(c, &c->bscratch, (size_t)std::max(nb, 1u) * real_size(c)))) return rc;
+    if (c->scn.size() > 1 && (rc = palloc(c, &c->bscene, (size_t)std::max(nb, 1u) * 4))) return rc;
     if (nb > 0) {
-        DevParams<T> P = make_params<T>(c);
-        DevBufs<T> B = make_bufs<T>(c, 1);
-        // sort boundary by cell Morton code; reuse fluid sort scratch sized for max(n, nb)
-        uint32_t *k1, *k2, *v1, *v2, *cells, *hist;
-        if ((rc = dalloc(c, &k1, (size_t)nb * 4))) return rc;
-        if ((rc = dalloc(c, &k2, (size_t)nb * 4))) return rc;
-        if ((rc = dalloc(c, &v1, (size_t)nb * 4))) return rc;
-        if ((rc = dalloc(c, &v2, (size_t)nb * 4))) return rc;
-        if ((rc = dalloc(c, &cells, (size_t)nb * 4))) return rc;
+        // upload-order boundary positions (and scenes), sorted by (scene, cell Morton code)
+        std::vector<char> host((size_t)nb * vec_size(c));
+        for (uint32_t i = 0; i < nb; i++) {
+            const double *p = c->hb.data() + 3 * (size_t)i;
+            if (c->fp64) {
+                dquad q{p[0], p[1], p[2], 0.0};
+                std::memcpy(host.data() + (size_t)i * sizeof(dquad), &q, sizeof(q));
+            } else {
+                float4 q = make_float4((float)p[0], (float)p[1], (float)p[2], 0.f);
+                std::memcpy(host.data() + (size_t)i * sizeof(float4), &q, sizeof(q));
+            }
+        }
+        void *xb_raw;
+        uint32_t *bscene_raw = nullptr, *k1, *k2, *v1, *v2, *cells, *hist;
+        if ((rc = palloc(c, &xb_raw, host.size()))) return rc;
+        CK(cudaMemcpy(xb_raw, host.data(), host.size(), cudaMemcpyHostToDevice));
+        if (c->scn.size() > 1) {
+            std::vector<uint32_t> bs(nb);
+            for (uint32_t s = 0; s < c->scn.size(); s++)
+                for (uint32_t k = 0; k < c->scn[s].nb; k++) bs[c->scn[s].bstart + k] = s;
+            if ((rc = palloc(c, &bscene_raw, (size_t)nb * 4))) return rc;
+            CK(cudaMemcpy(bscene_raw, bs.data(), (size_t)nb * 4, cudaMemcpyHostToDevice));
+        }
         const uint32_t tiles = (nb + kSortTile - 1) / kSortTile;
-        if ((rc = dalloc(c, &hist, (size_t)tiles * 256 * 4))) return rc;
-        launch_boundary_keys<T>(P, B, (const v4_t<T> *)c->xb_raw, k1, v1, c->stream);
+        if ((rc = palloc(c, &k1, (size_t)nb * 4))) return rc;
+        if ((rc = palloc(c, &k2, (size_t)nb * 4))) return rc;
+        if ((rc = palloc(c, &v1, (size_t)nb * 4))) return rc;
+        if ((rc = palloc(c, &v2, (size_t)nb * 4))) return rc;
+        if ((rc = palloc(c, &cells, (size_t)nb * 4))) return rc;
+        if ((rc = palloc(c, &hist, (size_t)tiles * 256 * 4))) return rc;
+        const DevParams<T> P = make_params<T>(c);
+        const DevBufs<T> B = make_bufs<T>(c, 1);
+        launch_boundary_keys<T>(P, (const v4_t<T> *)xb_raw, bscene_raw, k1, v1, c->stream);
         const bool sw = radix_sort_pairs(k1, v1, k2, v2, nb, c->key_bits, hist, tiles, c->stream);
-        launch_boundary_gather<T>(P, B, (const v4_t<T> *)c->xb_raw, sw ? v2 : v1, cells, c->stream);
+        launch_boundary_gather<T>(P, B, (const v4_t<T> *)xb_raw, bscene_raw, sw ? v2 : v1, cells, c->stream);
         launch_boundary_volume<T>(P, B, c->stream);
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(c->stream));
+        for (void *p : {(void *)xb_raw, (void *)bscene_raw, (void *)k1, (void *)k2, (void *)v1, (void *)v2,
+                        (void *)cells, (void *)hist})
+            if (p) dfree(c->prep_allocs, p);
     }
     c->prepared = true;
     return SPHGB_OK;
@@ -406,15 +526,18 @@ template <class T> void enqueue_solver_loop_body(sphgb_ctx *c, const DevParams<T
     }
 }
 
+// the batch's loop decision (global record)
 int read_cont(sphgb_ctx *c, unsigned *cont)
 {
-    CK(cudaMemcpyAsync(&c->hsc->cont, &c->sc->cont, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+    StepScalars *g = c->sc + c->nscenes();
+    StepScalars *hg = c->hsc + c->nscenes();
+    CK(cudaMemcpyAsync(&hg->cont, &g->cont, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    *cont = c->hsc->cont;
+    *cont = hg->cont;
     return SPHGB_OK;
 }
 
-// Enqueue the launches that precede / follow the solver loops.
+// Enqueue the launches that precede the solver loops.
 template <class T> void enqueue_prologue(sphgb_ctx *c, const DevParams<T> &P, const DevBufs<T> &B0, const DevBufs<T> &B1,
                                          cudaStream_t s)
 {
@@ -422,7 +545,10 @@ template <class T> void enqueue_prologue(sphgb_ctx *c, const DevParams<T> &P, co
     { PROF(K_KEYS, s); launch_keys<T>(P, B0, s); }
     const uint32_t tiles = (c->n + kSortTile - 1) / kSortTile;
     bool sw;
-    { PROF(K_SORT, s); sw = radix_sort_pairs(c->key, c->perm, c->key2, c->perm2, c->n, c->key_bits, c->hist, tiles, s, &c->sc->launches); }
+    {
+        PROF(K_SORT, s);
+        sw = radix_sort_pairs(c->key, c->perm, c->key2, c->perm2, c->n, c->key_bits, c->hist, tiles, s, &B1.gsc->launches);
+    }
     { PROF(K_GATHER, s); launch_gather<T>(P, B0, sw ? c->perm2 : c->perm, s); }
     {
         PROF(K_CELL_RANGES, s);
@@ -431,7 +557,7 @@ template <class T> void enqueue_prologue(sphgb_ctx *c, const DevParams<T> &P, co
     }
     { PROF(K_BUILD, s); launch_build<T>(P, B1, s); }
     if (P.feat_on) { PROF(K_FEATURES, s); launch_features<T>(P, B1, s); }
-    if (P.learned) { PROF(K_MLP, s); mlp_infer_device(c->mlp_x, c->n, c->mlp_w, c->mlp_p, c->mlp_y, s); }
+    if (P.learned) { PROF(K_MLP, s); mlp_infer_device(c->mlp_x, c->np, c->mlp_w, c->mlp_p, c->mlp_y, s); }
 }
 
 template <class T> int step_host_loop(sphgb_ctx *c)
@@ -521,12 +647,9 @@ cudaError_t add_while(sphgb_ctx *c, cudaGraphConditionalHandle *handle_out, unsi
     return e;
 }
 
-}  // namespace
-
 // The viscosity set-up kernel must set the CG loop's condition, so the graph is
 // built in one capture where the handle exists before the set-up launch.  This
 // helper does the whole capture (prologue, loops, epilogue) for one parity.
-namespace {
 template <class T> int build_graph(sphgb_ctx *c, int parity, cudaGraphExec_t *out)
 {
     const int saved = c->parity;
@@ -612,9 +735,6 @@ template <class T> int build_graph(sphgb_ctx *c, int parity, cudaGraphExec_t *ou
     }
     return SPHGB_OK;
 }
-}  // namespace
-
-namespace {
 
 template <class T> int do_step(sphgb_ctx *c)
 {
@@ -633,62 +753,130 @@ template <class T> int do_step(sphgb_ctx *c)
         if ((rc = step_host_loop<T>(c))) return rc;
     }
     c->parity = 1 - c->parity;
-    CK(cudaMemcpyAsync(c->hsc, c->sc, sizeof(StepScalars), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(c->hsc, c->sc, (c->nscenes() + 1) * sizeof(StepScalars), cudaMemcpyDeviceToHost, c->stream));
     c->step_pending = true;
     return SPHGB_OK;
+}
+
+// statistics of scene s from the host mirror (g: the global record)
+void scene_stats(const sphgb_ctx *c, const StepScalars &h, const StepScalars &g, sphgb_stats *st)
+{
+    st->iterations = h.iters;
+    st->iterations_v = h.iters_v;
+    st->visco_iterations = c->prm.viscosity_method == 6 ? h.iters_cg : 0;
+    st->max_fluid_neighbors = h.max_nf;
+    st->max_boundary_neighbors = h.max_nb;
+    st->flags = h.flags | g.flags;
+    st->avg_density_err = h.avg_err;
+    st->avg_density_err_v = h.avg_err_v;
+    st->visco_error = c->prm.viscosity_method == 6 ? h.cg_err : 0.0;
+    st->dt_used = h.dt_used;
+    st->dt_next = h.dt_next;
+    st->time = h.time;
+    st->kernel_launches = g.launches + (c->learned ? 1 : 0);   // the network forward counts as one
+    st->learned_used = c->learned ? h.ws_used : 0;
+    st->reserved = 0;
+    for (int k = 0; k < 2; k++) {
+        st->ws_residual_classic[k] = c->learned ? h.ws_rc[k] : 0.0;
+        st->ws_residual_learned[k] = c->learned ? h.ws_rl[k] : 0.0;
+    }
 }
 
 int fill_stats(sphgb_ctx *c, sphgb_stats *st)
 {
     CK(cudaStreamSynchronize(c->stream));
-    const StepScalars &h = *c->hsc;
+    const uint32_t S = c->nscenes();
+    const StepScalars &g = c->hsc[S];
     if (c->step_pending) {
-        c->dt = h.dt;
-        c->time = h.time;
+        for (uint32_t s = 0; s < c->scn.size(); s++) {
+            c->scn[s].dt = c->hsc[s].dt;
+            c->scn[s].time = c->hsc[s].time;
+        }
         c->step_pending = false;
     }
+    unsigned flags = g.flags;
+    for (uint32_t s = 0; s < S; s++) flags |= c->hsc[s].flags;
     if (st) {
-        st->iterations = h.iters;
-        st->iterations_v = h.iters_v;
-        st->visco_iterations = c->prm.viscosity_method == 6 ? h.iters_cg : 0;
-        st->max_fluid_neighbors = h.max_nf;
-        st->max_boundary_neighbors = h.max_nb;
-        st->flags = h.flags;
-        st->avg_density_err = h.avg_err;
-        st->avg_density_err_v = h.avg_err_v;
-        st->visco_error = c->prm.viscosity_method == 6 ? h.cg_err : 0.0;
-        st->dt_used = h.dt_used;
-        st->dt_next = h.dt_next;
-        st->time = h.time;
-        st->kernel_launches = h.launches + (c->learned ? 1 : 0);   // the network forward counts as one
-        st->learned_used = c->learned ? h.ws_used : 0;
-        st->reserved = 0;
-        for (int k = 0; k < 2; k++) {
-            st->ws_residual_classic[k] = c->learned ? h.ws_rc[k] : 0.0;
-            st->ws_residual_learned[k] = c->learned ? h.ws_rl[k] : 0.0;
+        // one scene: its statistics; a batch: scene 0's times, the maxima of counts and errors over the
+        // scenes (the iterations the batch's loops executed), mean initial residuals, OR of flags
+        scene_stats(c, c->hsc[0], g, st);
+        for (uint32_t s = 1; s < S; s++) {
+            sphgb_stats o;
+            scene_stats(c, c->hsc[s], g, &o);
+            st->iterations = std::max(st->iterations, o.iterations);
+            st->iterations_v = std::max(st->iterations_v, o.iterations_v);
+            st->visco_iterations = std::max(st->visco_iterations, o.visco_iterations);
+            st->max_fluid_neighbors = std::max(st->max_fluid_neighbors, o.max_fluid_neighbors);
+            st->max_boundary_neighbors = std::max(st->max_boundary_neighbors, o.max_boundary_neighbors);
+            st->avg_density_err = std::max(st->avg_density_err, o.avg_density_err);
+            st->avg_density_err_v = std::max(st->avg_density_err_v, o.avg_density_err_v);
+            st->visco_error = std::max(st->visco_error, o.visco_error);
+            st->learned_used |= o.learned_used;
+            for (int k = 0; k < 2; k++) {
+                st->ws_residual_classic[k] += o.ws_residual_classic[k];
+                st->ws_residual_learned[k] += o.ws_residual_learned[k];
+            }
         }
+        for (int k = 0; k < 2; k++) {
+            st->ws_residual_classic[k] /= S;
+            st->ws_residual_learned[k] /= S;
+        }
+        st->flags = flags;
     }
-    if (h.flags & kFlagOverflow)
+    if (flags & kFlagOverflow)
         return fail(c, SPHGB_ERR_CAPACITY, "neighbour list capacity exceeded (raise max_fluid/boundary_neighbors)");
-    if (h.flags & kFlagNonFinite) return fail(c, SPHGB_ERR_NONFINITE, "non-finite velocity");
-    if (h.flags & kFlagLoopGuard) return fail(c, SPHGB_ERR_STATE, "a device solver loop exceeded its iteration bound");
+    if (flags & kFlagNonFinite) return fail(c, SPHGB_ERR_NONFINITE, "non-finite velocity");
+    if (flags & kFlagLoopGuard) return fail(c, SPHGB_ERR_STATE, "a device solver loop exceeded its iteration bound");
     return SPHGB_OK;
 }
 
 int alloc_learned_buffers(sphgb_ctx *c);
 
-template <class T> int init_fluid(sphgb_ctx *c, const double *x, const double *v, const uint32_t *id, uint32_t n)
+int ensure_scalar_mirror(sphgb_ctx *c, size_t records)
+{
+    if (c->hsc_cap >= records) return SPHGB_OK;
+    if (c->hsc) cudaFreeHost(c->hsc);
+    c->hsc = nullptr;
+    c->hsc_cap = 0;
+    CK(cudaMallocHost(&c->hsc, records * sizeof(StepScalars)));
+    std::memset(c->hsc, 0, records * sizeof(StepScalars));
+    c->hsc_cap = records;
+    return SPHGB_OK;
+}
+
+// (Re)allocate every per-particle buffer for the scenes with fluid counts `counts` and
+// upload their state; x, v (and id) hold all scenes' particles in scene order.
+template <class T> int init_scenes(sphgb_ctx *c, const double *x, const double *v, const uint32_t *id,
+                                   const std::vector<uint32_t> &counts)
 {
     int rc;
-    // (re)allocate every per-particle buffer
     free_all(c);
     c->feat = c->mlp_x = c->mlp_y = nullptr;
     c->kl = c->pa2 = nullptr;
     c->staging = nullptr;
     c->staging_bytes = 0;
-    c->prepared = false;
-    c->n = n;
-    const size_t N = std::max<uint32_t>(n, 1);
+    c->d_scenes = nullptr;
+    c->d_blk = nullptr;
+    c->have_fluid = false;
+    const uint32_t S = (uint32_t)counts.size();
+    std::vector<SceneHost> old = c->scn;
+    c->scn.assign(S, SceneHost{});
+    uint32_t u = 0, p = 0;
+    for (uint32_t s = 0; s < S; s++) {
+        SceneHost &h = c->scn[s];
+        h.n = counts[s];
+        h.ustart = u;
+        h.pstart = p;
+        h.dt = c->dt;
+        h.time = 0.0;
+        if (s < old.size()) { h.nb = old[s].nb; h.bstart = old[s].bstart; }
+        for (int d = 0; d < 3; d++) { h.bmin[d] = s < old.size() ? old[s].bmin[d] : 0.0; h.bmax[d] = s < old.size() ? old[s].bmax[d] : 0.0; }
+        u += h.n;
+        p += S > 1 ? (h.n + kBlock - 1) / kBlock * kBlock : h.n;
+    }
+    c->n = u;
+    c->np = p;
+    const size_t N = std::max<uint32_t>(c->np, 1), NR = std::max<uint32_t>(c->n, 1);
     const size_t vs = vec_size(c), rs = real_size(c);
     for (int k = 0; k < 2; k++) {
         if ((rc = dalloc(c, &c->set_x[k], N * vs))) return rc;
@@ -699,6 +887,9 @@ template <class T> int init_fluid(sphgb_ctx *c, const double *x, const double *v
         if ((rc = dalloc(c, &c->set_id[k], N * 4))) return rc;
         c->set_xlo[k] = nullptr;
         if (!c->fp64 && (rc = dalloc(c, &c->set_xlo[k], N * sizeof(float4)))) return rc;
+        // idle slots of a batch hold zeros
+        CK(cudaMemset(c->set_x[k], 0, N * vs));
+        CK(cudaMemset(c->set_v[k], 0, N * vs));
     }
     if ((rc = dalloc(c, &c->a, N * vs))) return rc;
     if ((rc = dalloc(c, &c->pa, N * vs))) return rc;
@@ -712,10 +903,10 @@ template <class T> int init_fluid(sphgb_ctx *c, const double *x, const double *v
     const size_t NW = (N + 31) / 32 * 32;
     if ((rc = dalloc(c, &c->lf, NW * c->cfg.max_fluid_neighbors * 4))) return rc;
     if ((rc = dalloc(c, &c->lb, NW * c->cfg.max_boundary_neighbors * 4))) return rc;
-    if ((rc = dalloc(c, &c->key, N * 4))) return rc;
-    if ((rc = dalloc(c, &c->key2, N * 4))) return rc;
-    if ((rc = dalloc(c, &c->perm, N * 4))) return rc;
-    if ((rc = dalloc(c, &c->perm2, N * 4))) return rc;
+    if ((rc = dalloc(c, &c->key, NR * 4))) return rc;
+    if ((rc = dalloc(c, &c->key2, NR * 4))) return rc;
+    if ((rc = dalloc(c, &c->perm, NR * 4))) return rc;
+    if ((rc = dalloc(c, &c->perm2, NR * 4))) return rc;
     if ((rc = dalloc(c, &c->cell0, N * 4))) return rc;
     if ((rc = dalloc(c, &c->cell1, N * 4))) return rc;
     for (int k = 0; k < 5; k++)
@@ -724,13 +915,27 @@ template <class T> int init_fluid(sphgb_ctx *c, const double *x, const double *v
         if ((rc = dalloc(c, &c->inv[k], N * vs))) return rc;
     const size_t blocks = (N + kBlock - 1) / kBlock;
     if ((rc = dalloc(c, &c->partials, blocks * 4 * sizeof(double)))) return rc;
-    if ((rc = dalloc(c, &c->counter, 64))) return rc;
-    CK(cudaMemset(c->counter, 0, 64));
-    if ((rc = dalloc(c, &c->sc, sizeof(StepScalars)))) return rc;
-    CK(cudaMemset(c->sc, 0, sizeof(StepScalars)));
-    const size_t tiles = (N + kSortTile - 1) / kSortTile;
+    const size_t nrec = (size_t)std::max<uint32_t>(S, 1) + 1;
+    if ((rc = dalloc(c, &c->counters, std::max<size_t>(nrec * 4, 64)))) return rc;
+    CK(cudaMemset(c->counters, 0, std::max<size_t>(nrec * 4, 64)));
+    if ((rc = dalloc(c, &c->sc, nrec * sizeof(StepScalars)))) return rc;
+    CK(cudaMemset(c->sc, 0, nrec * sizeof(StepScalars)));
+    if ((rc = ensure_scalar_mirror(c, nrec))) return rc;
+    const size_t tiles = (NR + kSortTile - 1) / kSortTile;
     if ((rc = dalloc(c, &c->hist, tiles * 256 * 4))) return rc;
-    if ((rc = dalloc(c, &c->inv_perm, N * 4))) return rc;
+    if ((rc = dalloc(c, &c->inv_perm, NR * 4))) return rc;
+    if (S > 1) {
+        if ((rc = dalloc(c, &c->d_scenes, S * sizeof(SceneDev<T>)))) return rc;
+        std::vector<uint4> blk(blocks);
+        for (uint32_t s = 0; s < S; s++) {
+            const SceneHost &h = c->scn[s];
+            for (uint32_t b = h.pstart / kBlock; b < (h.pstart + h.n + kBlock - 1) / kBlock; b++)
+                blk[b] = make_uint4(s, h.pstart, h.pstart + h.n, 0u);
+        }
+        if ((rc = dalloc(c, &c->d_blk, blocks * sizeof(uint4)))) return rc;
+        CK(cudaMemcpy(c->d_blk, blk.data(), blocks * sizeof(uint4), cudaMemcpyHostToDevice));
+        if ((rc = upload_scene_table<T>(c))) return rc;
+    }
     // zero per-step fields so that downloads before the first step are defined
     CK(cudaMemset(c->a, 0, N * vs));
     CK(cudaMemset(c->pa, 0, N * vs));
@@ -742,15 +947,15 @@ template <class T> int init_fluid(sphgb_ctx *c, const double *x, const double *v
     // staging copy of x/v (double) and ids
     double *dx, *dv;
     uint32_t *did = nullptr;
-    if ((rc = dalloc(c, &dx, N * 3 * sizeof(double)))) return rc;
-    if ((rc = dalloc(c, &dv, N * 3 * sizeof(double)))) return rc;
-    if (n) {
-        CK(cudaMemcpy(dx, x, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(dv, v, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice));
+    if ((rc = dalloc(c, &dx, NR * 3 * sizeof(double)))) return rc;
+    if ((rc = dalloc(c, &dv, NR * 3 * sizeof(double)))) return rc;
+    if (c->n) {
+        CK(cudaMemcpy(dx, x, (size_t)c->n * 3 * sizeof(double), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(dv, v, (size_t)c->n * 3 * sizeof(double), cudaMemcpyHostToDevice));
     }
     if (id) {
-        if ((rc = dalloc(c, &did, N * 4))) return rc;
-        CK(cudaMemcpy(did, id, (size_t)n * 4, cudaMemcpyHostToDevice));
+        if ((rc = dalloc(c, &did, NR * 4))) return rc;
+        CK(cudaMemcpy(did, id, (size_t)c->n * 4, cudaMemcpyHostToDevice));
     }
     c->parity = 0;
     DevParams<T> P = make_params<T>(c);
@@ -758,49 +963,55 @@ template <class T> int init_fluid(sphgb_ctx *c, const double *x, const double *v
     launch_init_state<T>(P, B, dx, dv, did, c->stream);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(c->stream));
+    dfree(c->allocs, dx);
+    dfree(c->allocs, dv);
+    if (did) dfree(c->allocs, did);
     // extents
-    for (int d = 0; d < 3; d++) {
-        c->fmin[d] = n ? x[d] : 0.0;
-        c->fmax[d] = n ? x[d] : 0.0;
-    }
-    for (uint32_t i = 1; i < n; i++)
+    for (SceneHost &h : c->scn) {
         for (int d = 0; d < 3; d++) {
-            c->fmin[d] = std::min(c->fmin[d], x[3 * (size_t)i + d]);
-            c->fmax[d] = std::max(c->fmax[d], x[3 * (size_t)i + d]);
+            h.fmin[d] = h.n ? x[3 * (size_t)h.ustart + d] : 0.0;
+            h.fmax[d] = h.fmin[d];
         }
+        for (uint32_t i = h.ustart + 1; i < h.ustart + h.n; i++)
+            for (int d = 0; d < 3; d++) {
+                h.fmin[d] = std::min(h.fmin[d], x[3 * (size_t)i + d]);
+                h.fmax[d] = std::max(h.fmax[d], x[3 * (size_t)i + d]);
+            }
+    }
     c->have_fluid = true;
     if ((c->learned || c->feat_on) && (rc = alloc_learned_buffers(c))) return rc;
     c->scalars_dirty = true;
     return SPHGB_OK;
 }
 
-template <class T> int init_boundary(sphgb_ctx *c, const double *xb, uint32_t nb)
+// Host copy of the boundary particles (scene order) with per-scene counts; the device
+// copy, its sort and the volumes are made by prepare().
+int set_boundary(sphgb_ctx *c, const double *xb, const std::vector<uint32_t> &counts)
 {
-    int rc;
-    c->nb = nb;
-    std::vector<char> host((size_t)std::max<uint32_t>(nb, 1) * vec_size(c));
-    for (uint32_t i = 0; i < nb; i++) {
-        if (c->fp64) {
-            dquad q{xb[3 * (size_t)i], xb[3 * (size_t)i + 1], xb[3 * (size_t)i + 2], 0.0};
-            std::memcpy(host.data() + (size_t)i * sizeof(dquad), &q, sizeof(q));
-        } else {
-            float4 q = make_float4((float)xb[3 * (size_t)i], (float)xb[3 * (size_t)i + 1], (float)xb[3 * (size_t)i + 2], 0.f);
-            std::memcpy(host.data() + (size_t)i * sizeof(float4), &q, sizeof(q));
-        }
-    }
-    if ((rc = dalloc(c, &c->xb_raw, host.size()))) return rc;
-    CK(cudaMemcpy(c->xb_raw, host.data(), host.size(), cudaMemcpyHostToDevice));
-    for (int d = 0; d < 3; d++) {
-        c->bmin[d] = nb ? xb[d] : 0.0;
-        c->bmax[d] = nb ? xb[d] : 0.0;
-    }
-    for (uint32_t i = 1; i < nb; i++)
+    size_t total = 0;
+    for (uint32_t k : counts) total += k;
+    if (total > 0xffffffffull) return fail(c, SPHGB_ERR_ARGUMENT, "too many boundary particles");
+    c->hb.assign(xb, xb + 3 * total);
+    c->nb = (uint32_t)total;
+    if (c->scn.size() < counts.size()) c->scn.resize(counts.size());
+    uint32_t b = 0;
+    for (uint32_t s = 0; s < c->scn.size(); s++) {
+        SceneHost &h = c->scn[s];
+        h.nb = s < counts.size() ? counts[s] : 0;
+        h.bstart = b;
         for (int d = 0; d < 3; d++) {
-            c->bmin[d] = std::min(c->bmin[d], xb[3 * (size_t)i + d]);
-            c->bmax[d] = std::max(c->bmax[d], xb[3 * (size_t)i + d]);
+            h.bmin[d] = h.nb ? xb[3 * (size_t)b + d] : 0.0;
+            h.bmax[d] = h.bmin[d];
         }
+        for (uint32_t i = b + 1; i < b + h.nb; i++)
+            for (int d = 0; d < 3; d++) {
+                h.bmin[d] = std::min(h.bmin[d], xb[3 * (size_t)i + d]);
+                h.bmax[d] = std::max(h.bmax[d], xb[3 * (size_t)i + d]);
+            }
+        b += h.nb;
+    }
     c->have_boundary = true;
-    c->prepared = false;
+    free_prepared(c);
     invalidate_graphs(c);
     return SPHGB_OK;
 }
@@ -832,14 +1043,22 @@ size_t dtype_size(int dt) { return dt == SPHGB_DTYPE_F64 ? 8 : 4; }
 int alloc_learned_buffers(sphgb_ctx *c)
 {
     if (c->feat) return SPHGB_OK;
-    const size_t N = std::max<uint32_t>(c->n, 1);
+    const size_t N = std::max<uint32_t>(c->np, 1);
     int rc;
     if ((rc = dalloc(c, &c->feat, N * 8 * sizeof(float)))) return rc;
     if ((rc = dalloc(c, &c->mlp_x, N * 10 * sizeof(float)))) return rc;
     if ((rc = dalloc(c, &c->mlp_y, N * 2 * sizeof(float)))) return rc;
     if ((rc = dalloc(c, &c->kl, N * real_size(c)))) return rc;
     if ((rc = dalloc(c, &c->pa2, N * vec_size(c)))) return rc;
+    CK(cudaMemset(c->feat, 0, N * 8 * sizeof(float)));
     CK(cudaMemset(c->mlp_x, 0, N * 10 * sizeof(float)));
+    return SPHGB_OK;
+}
+
+int check_finite(sphgb_ctx *c, const double *a, size_t m, const char *what)
+{
+    for (size_t k = 0; k < m; k++)
+        if (!std::isfinite(a[k])) return fail(c, SPHGB_ERR_NONFINITE, std::string("non-finite ") + what);
     return SPHGB_OK;
 }
 
@@ -873,13 +1092,13 @@ int sphgb_create(const sphgb_config *cfg, sphgb_ctx **out)
     cudaError_t e = cudaSetDevice(cfg->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->body_stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaMallocHost(&c->hsc, sizeof(StepScalars));
+    if (e == cudaSuccess && ensure_scalar_mirror(c, 2) != SPHGB_OK) e = cudaErrorMemoryAllocation;
     if (e != cudaSuccess) {
         cudaGetLastError();
+        if (c->hsc) cudaFreeHost(c->hsc);
         delete c;
         return SPHGB_ERR_CUDA;
     }
-    std::memset(c->hsc, 0, sizeof(StepScalars));
     *out = c;
     return SPHGB_OK;
 }
@@ -912,10 +1131,8 @@ int sphgb_set_params(sphgb_ctx *c, const sphgb_params *p)
     const bool radius_changed = c->prm.particle_radius != p->particle_radius;
     c->prm = *p;
     invalidate_graphs(c);
-    if (radius_changed && c->prepared) {
-        // the cell grid and boundary volumes depend on the support radius
-        c->prepared = false;
-    }
+    // the cell grids and boundary volumes depend on the support radius
+    if (radius_changed && c->prepared) c->prepared = false;
     return SPHGB_OK;
 }
 
@@ -929,8 +1146,11 @@ int sphgb_get_params(const sphgb_ctx *c, sphgb_params *p)
 int sphgb_upload_boundary(sphgb_ctx *c, const double *xb, uint32_t nb)
 {
     if (!c || (!xb && nb)) return SPHGB_ERR_ARGUMENT;
+    if (c->scn.size() > 1) return fail(c, SPHGB_ERR_STATE, "a batch of scenes takes its boundary in sphgb_upload_scenes");
+    int rc = check_finite(c, xb, (size_t)nb * 3, "boundary position");
+    if (rc) return rc;
     cudaSetDevice(c->cfg.device);
-    return c->fp64 ? init_boundary<double>(c, xb, nb) : init_boundary<float>(c, xb, nb);
+    return set_boundary(c, xb, std::vector<uint32_t>{nb});
 }
 
 int sphgb_upload_boundary_f32(sphgb_ctx *c, const float *xb, uint32_t nb)
@@ -955,34 +1175,16 @@ int sphgb_upload_fluid(sphgb_ctx *c, const double *x, const double *v, const uin
     for (size_t k = 0; k < (size_t)n * 3; k++)
         if (!std::isfinite(x[k]) || !std::isfinite(v[k])) return fail(c, SPHGB_ERR_NONFINITE, "non-finite fluid state");
     cudaSetDevice(c->cfg.device);
-    // keep the staged boundary across the re-allocation of the fluid buffers
-    std::vector<double> xb;
-    uint32_t nb = 0;
-    if (c->have_boundary && c->nb) {
-        nb = c->nb;
-        xb.resize((size_t)nb * 3);
-        if (c->fp64) {
-            std::vector<dquad> t(nb);
-            if (cudaMemcpy(t.data(), c->xb_raw, nb * sizeof(dquad), cudaMemcpyDeviceToHost) != cudaSuccess)
-                return fail(c, SPHGB_ERR_CUDA, "boundary readback");
-            for (uint32_t i = 0; i < nb; i++) { xb[3 * i] = t[i].x; xb[3 * i + 1] = t[i].y; xb[3 * i + 2] = t[i].z; }
-        } else {
-            std::vector<float4> t(nb);
-            if (cudaMemcpy(t.data(), c->xb_raw, nb * sizeof(float4), cudaMemcpyDeviceToHost) != cudaSuccess)
-                return fail(c, SPHGB_ERR_CUDA, "boundary readback");
-            for (uint32_t i = 0; i < nb; i++) { xb[3 * i] = t[i].x; xb[3 * i + 1] = t[i].y; xb[3 * i + 2] = t[i].z; }
-        }
+    if (c->scn.size() > 1) {
+        // a single scene replaces a batch: the batch's boundary does not carry over
+        c->scn.clear();
+        c->hb.clear();
+        c->nb = 0;
+        c->have_boundary = false;
     }
-    const bool had_boundary = c->have_boundary;
-    int rc = c->fp64 ? init_fluid<double>(c, x, v, id, n) : init_fluid<float>(c, x, v, id, n);
+    int rc = c->fp64 ? init_scenes<double>(c, x, v, id, {n}) : init_scenes<float>(c, x, v, id, {n});
     if (rc) return rc;
-    if (had_boundary) {
-        rc = c->fp64 ? init_boundary<double>(c, xb.data(), nb) : init_boundary<float>(c, xb.data(), nb);
-        if (rc) return rc;
-    }
-    c->time = 0.0;
     c->scalars_dirty = true;
-    invalidate_graphs(c);
     return SPHGB_OK;
 }
 
@@ -994,12 +1196,62 @@ int sphgb_upload_fluid_f32(sphgb_ctx *c, const float *x, const float *v, const u
     return sphgb_upload_fluid(c, dx.data(), dv.data(), id, n);
 }
 
+int sphgb_upload_scenes(sphgb_ctx *c, uint32_t nscenes, const uint32_t *n, const uint32_t *nb, const double *x,
+                        const double *v, const double *xb)
+{
+    if (!c || nscenes == 0 || !n || !nb || !x || !v) return SPHGB_ERR_ARGUMENT;
+    size_t nt = 0, nbt = 0;
+    for (uint32_t s = 0; s < nscenes; s++) {
+        if (n[s] == 0) return fail(c, SPHGB_ERR_ARGUMENT, "every scene needs at least one fluid particle");
+        nt += n[s];
+        nbt += nb[s];
+    }
+    if (nbt && !xb) return SPHGB_ERR_ARGUMENT;
+    // slots of a batch are padded to whole blocks: the padded total must fit 32-bit indices
+    size_t padded = 0;
+    for (uint32_t s = 0; s < nscenes; s++) padded += (n[s] + kBlock - 1) / kBlock * (size_t)kBlock;
+    if (padded >= 0xffffffffull || nbt >= 0xffffffffull) return fail(c, SPHGB_ERR_CAPACITY, "too many particles");
+    int rc = check_finite(c, x, nt * 3, "fluid position");
+    if (!rc) rc = check_finite(c, v, nt * 3, "fluid velocity");
+    if (!rc && nbt) rc = check_finite(c, xb, nbt * 3, "boundary position");
+    if (rc) return rc;
+    cudaSetDevice(c->cfg.device);
+    c->scn.clear();
+    std::vector<uint32_t> counts(n, n + nscenes), bcounts(nb, nb + nscenes);
+    rc = c->fp64 ? init_scenes<double>(c, x, v, nullptr, counts) : init_scenes<float>(c, x, v, nullptr, counts);
+    if (rc) return rc;
+    static const double kNone[3] = {0, 0, 0};
+    rc = set_boundary(c, nbt ? xb : kNone, bcounts);
+    if (rc) return rc;
+    c->scalars_dirty = true;
+    return SPHGB_OK;
+}
+
+int sphgb_num_scenes(const sphgb_ctx *c, uint32_t *nscenes)
+{
+    if (!c || !nscenes) return SPHGB_ERR_ARGUMENT;
+    *nscenes = (uint32_t)c->scn.size();
+    return SPHGB_OK;
+}
+
+int sphgb_scene_stats(sphgb_ctx *c, uint32_t first, uint32_t count, sphgb_stats *out)
+{
+    if (!c || (!out && count)) return SPHGB_ERR_ARGUMENT;
+    if ((size_t)first + count > c->scn.size()) return fail(c, SPHGB_ERR_ARGUMENT, "scene index out of range");
+    sphgb_stats agg;
+    const int rc = fill_stats(c, &agg);
+    const StepScalars &g = c->hsc[c->nscenes()];
+    for (uint32_t k = 0; k < count; k++) scene_stats(c, c->hsc[first + k], g, out + k);
+    return rc;
+}
+
 int sphgb_set_time_step(sphgb_ctx *c, double dt)
 {
     if (!c || !(dt > 0)) return SPHGB_ERR_ARGUMENT;
     sphgb_stats st;
     if (c->step_pending) fill_stats(c, &st);
     c->dt = dt;
+    for (SceneHost &h : c->scn) h.dt = dt;
     c->scalars_dirty = true;
     return SPHGB_OK;
 }
@@ -1009,9 +1261,9 @@ int sphgb_get_time_step(const sphgb_ctx *c, double *dt)
     if (!c || !dt) return SPHGB_ERR_ARGUMENT;
     if (c->step_pending) {
         cudaStreamSynchronize(c->stream);
-        *dt = c->hsc->dt;
+        *dt = c->hsc[0].dt;
     } else {
-        *dt = c->dt;
+        *dt = c->scn.empty() ? c->dt : c->scn[0].dt;
     }
     return SPHGB_OK;
 }
@@ -1021,7 +1273,7 @@ int sphgb_set_time(sphgb_ctx *c, double t)
     if (!c) return SPHGB_ERR_ARGUMENT;
     sphgb_stats st;
     if (c->step_pending) fill_stats(c, &st);
-    c->time = t;
+    for (SceneHost &h : c->scn) h.time = t;
     c->scalars_dirty = true;
     return SPHGB_OK;
 }
@@ -1177,14 +1429,15 @@ int sphgb_upload_field(sphgb_ctx *c, int field, const void *src, int dtype)
     int rc = ensure_staging(c, bytes);
     if (rc) return rc;
     CK(cudaMemcpyAsync(c->staging, src, bytes, cudaMemcpyHostToDevice, c->stream));
-    launch_inverse_perm(c->set_id[c->parity], c->inv_perm, c->n, c->stream);
     if (c->fp64) {
         DevParams<double> P = make_params<double>(c);
         DevBufs<double> B = make_bufs<double>(c, 0);
+        launch_inverse_perm<double>(P, B.id, c->inv_perm, c->stream);
         launch_upload_field<double>(P, B, field, c->staging, dtype, c->inv_perm, c->stream);
     } else {
         DevParams<float> P = make_params<float>(c);
         DevBufs<float> B = make_bufs<float>(c, 0);
+        launch_inverse_perm<float>(P, B.id, c->inv_perm, c->stream);
         launch_upload_field<float>(P, B, field, c->staging, dtype, c->inv_perm, c->stream);
     }
     CK(cudaGetLastError());
@@ -1216,17 +1469,15 @@ int sphgb_neighbors(sphgb_ctx *c, int kind, uint32_t *offsets, uint32_t *indices
     if ((rc = dalloc(c, &dout, (size_t)std::max<uint32_t>(offsets[n], 1) * 4))) return rc;
     CK(cudaMemcpy(doff, offsets, ((size_t)n + 1) * 4, cudaMemcpyHostToDevice));
     const uint32_t *id = c->set_id[c->parity];
-    launch_inverse_perm(id, c->inv_perm, n, c->stream);
+    if (c->fp64) launch_inverse_perm<double>(make_params<double>(c), id, c->inv_perm, c->stream);
+    else launch_inverse_perm<float>(make_params<float>(c), id, c->inv_perm, c->stream);
     launch_lists_to_ids(kind == 0 ? c->lf : c->lb, kind == 0 ? c->nfc : c->nbc, cap, id, c->inv_perm, c->bid, kind,
                         doff, dout, n, c->stream);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(indices, dout, (size_t)offsets[n] * 4, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    // release the temporaries (last two allocations)
-    cudaFree(dout);
-    cudaFree(doff);
-    c->allocs.pop_back();
-    c->allocs.pop_back();
+    dfree(c->allocs, dout);
+    dfree(c->allocs, doff);
     return SPHGB_OK;
 }
 

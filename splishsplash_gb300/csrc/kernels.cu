@@ -1,8 +1,14 @@
-// sm_103a kernels of the DFSPH time step.  One thread per fluid particle, in
-// the cell-sorted order of the current step.  Neighbour lists are built once per
+// sm_103a kernels of the DFSPH time step.  One thread per fluid slot, in the
+// cell-sorted order of the current step.  Neighbour lists are built once per
 // step (fused with densities, the DFSPH factor and the divergence source) and
 // then re-read by every later pass; kernel gradients are recomputed from the
 // positions in each pass (the whole position array stays in L2).
+//
+// Every launch covers all scenes of the context.  Scene s owns the slots
+// [begin_s, end_s) of whole thread blocks, so all threads of a block belong to
+// one scene: per-scene reductions, step sizes and loop decisions are block
+// uniform.  Slots past a scene's last particle are idle (they hold no particle,
+// appear in no cell and in no list).
 //
 // Reference restated (SPlisHSPlasH 2.16.0): TimeStep.cpp:35-169,
 // DFSPH/TimeStepDFSPH.cpp:117-706 and the scalar kernels :1106-1420,
@@ -18,6 +24,74 @@ namespace {
 
 inline unsigned grid_for(uint32_t n) { return (n + kBlock - 1) / kBlock; }
 
+// ---- slots and scenes -----------------------------------------------------
+struct SlotInfo {
+    uint32_t s;            // scene
+    uint32_t i;            // slot
+    uint32_t begin, end;   // the scene's slots holding particles
+    bool act;              // slot i holds a particle
+};
+
+template <class T> __device__ __forceinline__ SlotInfo slot_info(const DevParams<T> &P)
+{
+    SlotInfo q;
+    q.i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (P.nscenes > 1) {
+        const uint4 b = __ldg(P.blk + blockIdx.x);
+        q.s = b.x;
+        q.begin = b.y;
+        q.end = b.z;
+    } else {
+        q.s = 0;
+        q.begin = 0;
+        q.end = P.s0.n;
+    }
+    q.act = q.i < q.end;   // blocks never span scenes: i >= begin
+    return q;
+}
+
+// reduction slot of the scene of this block
+template <class T> __device__ __forceinline__ ReduceSlot scene_reduce(const DevParams<T> &P, const DevBufs<T> &B,
+                                                                      const SlotInfo &q)
+{
+    ReduceSlot r;
+    r.partials = B.partials;
+    r.counter = B.counters + q.s;
+    if (P.nscenes > 1) {
+        r.first = q.begin / kBlock;
+        r.count = (q.end - q.begin + kBlock - 1) / kBlock;
+    } else {
+        r.first = 0;
+        r.count = gridDim.x;
+    }
+    return r;
+}
+
+// Loop decision of the batch.  Called by the thread that finalized a scene's
+// reduction, after it stored the scene's own decision in sc[s].cont; the last
+// scene to arrive stores the OR over all scenes in the global record and in the
+// graph's loop condition.  A loop stopped by the guard stays stopped.
+template <class T>
+__device__ __forceinline__ void batch_decide(const DevParams<T> &P, const DevBufs<T> &B, cudaGraphConditionalHandle h,
+                                             int use_handle)
+{
+    unsigned any;
+    if (P.nscenes == 1) {
+        any = B.sc[0].cont;
+    } else {
+        __threadfence();
+        const unsigned t = atomicAdd(B.counters + P.nscenes, 1u);
+        if (t != P.nscenes - 1) return;
+        __threadfence();
+        any = 0;
+        for (uint32_t s = 0; s < P.nscenes; s++) any |= __ldcg(&B.sc[s].cont);
+        B.counters[P.nscenes] = 0;
+    }
+    if (B.gsc->flags & kFlagLoopGuard) any = 0;
+    B.gsc->cont = any ? 1u : 0u;
+    if (use_handle) cudaGraphSetConditional(h, any ? 1u : 0u);
+}
+
 // ---- list access --------------------------------------------------------
 __device__ __forceinline__ const uint32_t *list_ptr(const uint32_t *L, uint32_t i, uint32_t cap)
 {
@@ -32,21 +106,6 @@ template <class T> struct Pair {
     V3<T> r;    // xi - xj
     T rl;       // |r|
 };
-
-template <class T> __device__ __forceinline__ Pair<T> pair_of(const v4_t<T> &xi, const v4_t<T> &xj)
-{
-    T dx, dy, dz;
-    const T d2 = pair_d2(xi, xj, dx, dy, dz);
-    Pair<T> p;
-    p.r = V3<T>{dx, dy, dz};
-    p.rl = dev_sqrt(d2);
-    return p;
-}
-
-template <class T> __device__ __forceinline__ V3<T> gradW(const Kernel<T> &K, const Pair<T> &p)
-{
-    return scl(p.r, kernel_gradW_coef(K, p.rl));
-}
 
 // gradW(r) = c r from the squared distance.  FP32: one reciprocal square root
 // (MUFU) instead of a square root and a division; FP64: exact sqrt and division.
@@ -131,17 +190,23 @@ __device__ __forceinline__ void cell_coords(uint32_t c, int dimx, int dimy, int 
     cz = (int)(t / (uint32_t)dimy);
 }
 
-template <class T> __device__ __forceinline__ void cell_of(const DevParams<T> &P, const v4_t<T> &x, int &cx, int &cy, int &cz)
+// cell of x in the scene's grid, clamped into the grid (border cells absorb outliers)
+template <class T> __device__ __forceinline__ void cell_of(const SceneDev<T> &S, const v4_t<T> &x, int &cx, int &cy, int &cz)
 {
-    cx = (int)floor(((T)x.x - P.ox) * P.inv_cell);
-    cy = (int)floor(((T)x.y - P.oy) * P.inv_cell);
-    cz = (int)floor(((T)x.z - P.oz) * P.inv_cell);
-    cx = min(max(cx, 0), P.dimx - 1);
-    cy = min(max(cy, 0), P.dimy - 1);
-    cz = min(max(cz, 0), P.dimz - 1);
+    cx = (int)floor(((T)x.x - S.ox) * S.inv_cell);
+    cy = (int)floor(((T)x.y - S.oy) * S.inv_cell);
+    cz = (int)floor(((T)x.z - S.oz) * S.inv_cell);
+    cx = min(max(cx, 0), S.dimx - 1);
+    cy = min(max(cy, 0), S.dimy - 1);
+    cz = min(max(cz, 0), S.dimz - 1);
 }
 
-// block-wide max of two counters, one atomic per block
+template <class T> __device__ __forceinline__ uint32_t local_cell(const SceneDev<T> &S, int cx, int cy, int cz)
+{
+    return ((uint32_t)cz * (uint32_t)S.dimy + (uint32_t)cy) * (uint32_t)S.dimx + (uint32_t)cx;
+}
+
+// block-wide max of two counters, one atomic per block (all threads of the block call it)
 __device__ __forceinline__ void block_max_atomic(uint32_t a, uint32_t b, unsigned *da, unsigned *db)
 {
     __shared__ uint32_t sa[32], sb[32];
@@ -160,27 +225,34 @@ __device__ __forceinline__ void block_max_atomic(uint32_t a, uint32_t b, unsigne
 // ==========================================================================
 // neighbour structure
 // ==========================================================================
+// Sort keys of the particles: (scene << Morton bits) | Morton code of the cell in
+// the scene's grid, one entry per particle in upload order of the scenes
+// (compact: idle slots have no entry).
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_keys(DevParams<T> P, DevBufs<T> B)
 {
-    count_launch(&B.sc->launches);
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
+    count_launch(&B.gsc->launches);
+    const SlotInfo q = slot_info(P);
+    if (!q.act) return;
+    const SceneDev<T> S = scene_get(P, q.s);
     int cx, cy, cz;
-    const v4_t<T> xi = ldv(B.x, i);
-    cell_of(P, xi, cx, cy, cz);
-    B.key[i] = morton3((uint32_t)cx, (uint32_t)cy, (uint32_t)cz);
-    B.perm[i] = i;
-    B.cellid[i] = ((uint32_t)cz * (uint32_t)P.dimy + (uint32_t)cy) * (uint32_t)P.dimx + (uint32_t)cx;
+    cell_of(S, ldv(B.x, q.i), cx, cy, cz);
+    const uint32_t u = S.ustart + (q.i - q.begin);
+    B.key[u] = S.key_prefix | morton3((uint32_t)cx, (uint32_t)cy, (uint32_t)cz);
+    B.perm[u] = q.i;
+    B.cellid[q.i] = S.cell_off + local_cell(S, cx, cy, cz);
 }
 
+// physical reorder: slot p of scene s receives the particle ranked (p - begin_s) in the scene's sorted keys
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_gather(DevParams<T> P, DevBufs<T> B, const uint32_t *__restrict__ perm)
 {
-    count_launch(&B.sc->launches);
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= P.n) return;
-    const uint32_t s = perm[k];
+    count_launch(&B.gsc->launches);
+    const SlotInfo q = slot_info(P);
+    if (!q.act) return;
+    const uint32_t ustart = P.nscenes > 1 ? P.scenes[q.s].ustart : 0u;
+    const uint32_t k = q.i;
+    const uint32_t s = perm[ustart + (k - q.begin)];
     stv(B.x2, k, ldv(B.x, s));
     stv(B.v2, k, ldv(B.v, s));
     stv(B.vdiff2, k, ldv(B.vdiff, s));
@@ -191,12 +263,23 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevParams<T> P, DevBufs<T> B,
     B.cellid2[k] = B.cellid[s];
 }
 
+// first / one-past-last slot of every non-empty cell (cells of a scene are sorted within the scene's slots)
 template <class T>
-__global__ void __launch_bounds__(kBlock) k_cell_ranges(DevParams<T> P, const uint32_t *__restrict__ cellid,
-                                                         uint32_t *__restrict__ cstart, uint32_t *__restrict__ cend, uint32_t n,
-                                                         unsigned *lc)
+__global__ void __launch_bounds__(kBlock) k_cell_ranges(DevParams<T> P, DevBufs<T> B)
 {
-    count_launch(lc);
+    count_launch(&B.gsc->launches);
+    const SlotInfo q = slot_info(P);
+    if (!q.act) return;
+    const uint32_t k = q.i;
+    const uint32_t c = B.cellid[k];
+    if (k == q.begin || B.cellid[k - 1] != c) B.cstart[c] = k;
+    if (k + 1 == q.end || B.cellid[k + 1] != c) B.cend[c] = k + 1;
+}
+
+// the same for a flat sorted array without idle entries (boundary particles)
+__global__ void __launch_bounds__(kBlock) k_cell_ranges_flat(const uint32_t *__restrict__ cellid, uint32_t *__restrict__ cstart,
+                                                              uint32_t *__restrict__ cend, uint32_t n)
+{
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const uint32_t c = cellid[k];
@@ -214,19 +297,17 @@ __global__ void __launch_bounds__(kBlock) k_cell_ranges(DevParams<T> P, const ui
 // Phase 2 walks the fresh lists densely for the kernel sums, so the kernel math
 // does not run inside the divergent candidate loop.
 template <class T>
-__global__ void __launch_bounds__(kBlock) k_build(DevParams<T> P, DevBufs<T> B)
+__device__ __forceinline__ void build_one(const DevParams<T> &P, const DevBufs<T> &B, const SceneDev<T> &S,
+                                          StepScalars *sc, uint32_t i, uint32_t &nf_out, uint32_t &nb_out)
 {
-    count_launch(&B.sc->launches);
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
     const v4_t<T> xi = ldv(B.x, i);
     int cx, cy, cz;
-    cell_coords(B.cellid[i], P.dimx, P.dimy, cx, cy, cz);
-    const T cs = T(1) / P.inv_cell;
+    cell_coords(B.cellid[i] - S.cell_off, S.dimx, S.dimy, cx, cy, cz);
+    const T cs = T(1) / S.inv_cell;
     // squared distances from x_i to the lower / upper face of its cell, per axis
     T slo[3], shi[3];
     {
-        const T px[3] = {(T)xi.x - P.ox, (T)xi.y - P.oy, (T)xi.z - P.oz};
+        const T px[3] = {(T)xi.x - S.ox, (T)xi.y - S.oy, (T)xi.z - S.oz};
         const int c3[3] = {cx, cy, cz};
 #pragma unroll
         for (int d = 0; d < 3; d++) {
@@ -243,21 +324,21 @@ __global__ void __launch_bounds__(kBlock) k_build(DevParams<T> P, DevBufs<T> B)
     uint32_t nf = 0, nb = 0;
     for (int dz = -1; dz <= 1; dz++) {
         const int z = cz + dz;
-        if (z < 0 || z >= P.dimz) continue;
+        if (z < 0 || z >= S.dimz) continue;
         const T sz = dz < 0 ? slo[2] : (dz > 0 ? shi[2] : T(0));
-        const bool inner_z = z > 0 && z < P.dimz - 1;
+        const bool inner_z = z > 0 && z < S.dimz - 1;
         for (int dy = -1; dy <= 1; dy++) {
             const int y = cy + dy;
-            if (y < 0 || y >= P.dimy) continue;
+            if (y < 0 || y >= S.dimy) continue;
             const T syz = sz + (dy < 0 ? slo[1] : (dy > 0 ? shi[1] : T(0)));
-            const bool inner_yz = inner_z && y > 0 && y < P.dimy - 1;
+            const bool inner_yz = inner_z && y > 0 && y < S.dimy - 1;
             for (int dx = -1; dx <= 1; dx++) {
                 const int x = cx + dx;
-                if (x < 0 || x >= P.dimx) continue;
+                if (x < 0 || x >= S.dimx) continue;
                 // border cells may hold clamped particles outside their box: never culled
-                const bool inner = inner_yz && x > 0 && x < P.dimx - 1;
+                const bool inner = inner_yz && x > 0 && x < S.dimx - 1;
                 if (inner && syz + (dx < 0 ? slo[0] : (dx > 0 ? shi[0] : T(0))) > cull) continue;
-                const uint32_t c = ((uint32_t)z * (uint32_t)P.dimy + (uint32_t)y) * (uint32_t)P.dimx + (uint32_t)x;
+                const uint32_t c = S.cell_off + local_cell(S, x, y, z);
                 uint32_t s = B.cstart[c];
                 if (s != kEmpty) {
                     const uint32_t e = B.cend[c];
@@ -315,11 +396,13 @@ __global__ void __launch_bounds__(kBlock) k_build(DevParams<T> P, DevBufs<T> B)
                       });
     B.nf[i] = nf;
     B.nbn[i] = nb;
-    if (nf > P.capf || nb > P.capb) atomicOr(&B.sc->flags, kFlagOverflow);
-    block_max_atomic(nf, nb, &B.sc->max_nf, &B.sc->max_nb);
+    if (nf > P.capf || nb > P.capb) atomicOr(&sc->flags, kFlagOverflow);
+    nf_out = nf;
+    nb_out = nb;
 
     // density: rho0 * (V W0 + sum_f V W + sum_b Vb W)
-    B.density[i] = P.rho0 * (P.V * P.K.w0 + P.V * wf + wb);
+    const T rho = P.rho0 * (P.V * P.K.w0 + P.V * wf + wb);
+    B.density[i] = rho;
     // factor: 1 / (sum_f |V gradW|^2 + |sum_f V gradW + sum_b Vb gradW|^2)
     const V3<T> gpi = add(scl(gf, P.V), gb);
     const T sum_grad = P.V * P.V * gsq + dot(gpi, gpi);
@@ -332,7 +415,7 @@ __global__ void __launch_bounds__(kBlock) k_build(DevParams<T> P, DevBufs<T> B)
     if (P.div_on) {
         T densityAdv = dsrc > T(0) ? dsrc : T(0);
         if (nf + nb < 20u) densityAdv = T(0);
-        const T invH = T(1) / (T)B.sc->dt;
+        const T invH = T(1) / (T)sc->dt;
         kv = densityAdv > T(0) ? T(0.5) * (kv < T(0.5) ? kv : T(0.5)) * invH : T(0);
         B.kappa_v[i] = kv;
     }
@@ -342,9 +425,9 @@ __global__ void __launch_bounds__(kBlock) k_build(DevParams<T> P, DevBufs<T> B)
     if (P.feat_on) {
         // raw warm-start features, scaled to O(1): density deviation, velocity divergence x dt,
         // neighbour count, previous (stored) kappa, displacement per step in diameters
-        const float h = (float)B.sc->dt;
+        const float h = (float)sc->dt;
         float *f = B.feat + (size_t)i * 8;
-        f[0] = 100.0f * ((float)B.density[i] / (float)P.rho0 - 1.0f);
+        f[0] = 100.0f * ((float)rho / (float)P.rho0 - 1.0f);
         f[1] = 100.0f * (float)dsrc * h;
         f[2] = (float)(nf + nb) * (1.0f / 40.0f) - 1.0f;
         f[3] = (float)B.kappa[i] / P.ws_scale_p;
@@ -353,6 +436,17 @@ __global__ void __launch_bounds__(kBlock) k_build(DevParams<T> P, DevBufs<T> B)
     v4_t<T> xk = xi;
     xk.w = kv;
     stv(B.xk, i, xk);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_build(DevParams<T> P, DevBufs<T> B)
+{
+    count_launch(&B.gsc->launches);
+    const SlotInfo q = slot_info(P);
+    StepScalars *const sc = B.sc + q.s;
+    uint32_t nf = 0, nb = 0;
+    if (q.act) build_one(P, B, scene_get(P, q.s), sc, q.i, nf, nb);
+    block_max_atomic(nf, nb, &sc->max_nf, &sc->max_nb);
 }
 
 // ==========================================================================
@@ -383,30 +477,37 @@ __device__ __forceinline__ V3<T> pressure_accel_i(const DevParams<T> &P, const D
 }
 
 // Termination guard of a device-side loop: the first kernel of every loop body
-// counts body executions; past the bound (which the solver's own decision never
-// reaches) it clears the loop condition and raises a flag, so a loop can never
-// run on if its convergence decision was lost.
-__device__ __forceinline__ void loop_guard(StepScalars *sc, unsigned limit, cudaGraphConditionalHandle h, int use_handle)
+// counts body executions; past the bound (which the solvers' own decisions never
+// reach) it clears the loop condition and raises a flag that also overrides the
+// decision of the same body, so a loop can never run on if its convergence
+// decision was lost.
+__device__ __forceinline__ void loop_guard(StepScalars *gsc, unsigned limit, cudaGraphConditionalHandle h, int use_handle)
 {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        const unsigned g = ++sc->loop_guard;
+        const unsigned g = ++gsc->loop_guard;
         if (g > limit) {
-            sc->flags |= kFlagLoopGuard;
-            sc->cont = 0;
+            gsc->flags |= kFlagLoopGuard;
+            gsc->cont = 0;
             if (use_handle) cudaGraphSetConditional(h, 0u);
         }
     }
+}
+
+// a scene whose solver loop already stopped skips the remaining bodies of the batch's loop
+template <class T> __device__ __forceinline__ bool scene_live(const DevParams<T> &P, const StepScalars *sc)
+{
+    return P.nscenes == 1 || sc->cont != 0u;
 }
 
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_pressure_accel(DevParams<T> P, DevBufs<T> B, unsigned limit,
                                                             cudaGraphConditionalHandle h, int use_handle)
 {
-    count_launch(&B.sc->launches);
-    loop_guard(B.sc, limit, h, use_handle);
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
-    stv(B.pa, i, pack(pressure_accel_i(P, B, i), T(0)));
+    count_launch(&B.gsc->launches);
+    loop_guard(B.gsc, limit, h, use_handle);
+    const SlotInfo q = slot_info(P);
+    if (!q.act || !scene_live(P, B.sc + q.s)) return;
+    stv(B.pa, q.i, pack(pressure_accel_i(P, B, q.i), T(0)));
 }
 
 // compute_aij_pj, scalar path (TimeStepDFSPH.cpp:1370-1420):
@@ -431,16 +532,19 @@ template <class T> __device__ __forceinline__ T aij_pj_i(const DevParams<T> &P, 
 
 // divergenceSolveIteration (TimeStepDFSPH.cpp:621-706) / pressureSolveIteration (:544-619):
 // Jacobi update of kappa_v / kappa plus the FP64 average-error reduction and the
-// loop decision (the while conditions of :477 and :324).
+// loop decision (the while conditions of :477 and :324), per scene.
 template <class T, bool DIV>
-__global__ void __launch_bounds__(kBlock) k_jacobi(DevParams<T> P, DevBufs<T> B, ReduceSlot slot,
-                                                     cudaGraphConditionalHandle handle, int use_handle)
+__global__ void __launch_bounds__(kBlock) k_jacobi(DevParams<T> P, DevBufs<T> B, cudaGraphConditionalHandle handle,
+                                                     int use_handle)
 {
-    count_launch(&B.sc->launches);
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    count_launch(&B.gsc->launches);
+    const SlotInfo q = slot_info(P);
+    StepScalars *const sc = B.sc + q.s;
+    const bool live = scene_live(P, sc);
     double err = 0.0;
-    if (i < P.n) {
-        const double hd = DIV ? B.sc->dt : B.sc->dt_next;
+    if (q.act && live) {
+        const uint32_t i = q.i;
+        const double hd = DIV ? sc->dt : sc->dt_next;
         const T h = (T)hd;
         T apj = aij_pj_i(P, B, i);
         T *kap = DIV ? B.kappa_v : B.kappa;
@@ -467,27 +571,30 @@ __global__ void __launch_bounds__(kBlock) k_jacobi(DevParams<T> P, DevBufs<T> B,
     }
     DSum<1> mine;
     mine.v[0] = err;
-    StepScalars *sc = B.sc;
     const DevParams<T> &PP = P;
-    grid_sum_finalize<1>(mine, slot, [&](const DSum<1> &tot) {
-        const double avg = tot.v[0] / (double)PP.n;
-        unsigned it;
-        bool cont;
-        if (DIV) {
-            it = ++sc->iters_v;
-            sc->avg_err_v = avg;
-            const double eta = (1.0 / sc->dt) * PP.max_error_v * 0.01 * (double)PP.rho0;
-            const bool chk = avg <= eta;
-            cont = (!chk || it < 1u) && it < PP.max_iter_v;
-        } else {
-            it = ++sc->iters;
-            sc->avg_err = avg;
-            const double eta = PP.max_error * 0.01 * (double)PP.rho0;
-            const bool chk = avg <= eta;
-            cont = (!chk || it < PP.min_iter) && it < PP.max_iter;
+    const DevBufs<T> &BB = B;
+    const uint32_t n_s = q.end - q.begin;
+    grid_sum_finalize<1>(mine, scene_reduce(P, B, q), [&](const DSum<1> &tot) {
+        if (live) {
+            const double avg = n_s ? tot.v[0] / (double)n_s : 0.0;
+            unsigned it;
+            bool cont;
+            if (DIV) {
+                it = ++sc->iters_v;
+                sc->avg_err_v = avg;
+                const double eta = (1.0 / sc->dt) * PP.max_error_v * 0.01 * (double)PP.rho0;
+                const bool chk = avg <= eta;
+                cont = (!chk || it < 1u) && it < PP.max_iter_v;
+            } else {
+                it = ++sc->iters;
+                sc->avg_err = avg;
+                const double eta = PP.max_error * 0.01 * (double)PP.rho0;
+                const bool chk = avg <= eta;
+                cont = (!chk || it < PP.min_iter) && it < PP.max_iter;
+            }
+            sc->cont = cont ? 1u : 0u;
         }
-        sc->cont = cont ? 1u : 0u;
-        if (use_handle) cudaGraphSetConditional(handle, cont ? 1u : 0u);
+        batch_decide(PP, BB, handle, use_handle);
     });
 }
 
@@ -496,43 +603,52 @@ __global__ void __launch_bounds__(kBlock) k_jacobi(DevParams<T> P, DevBufs<T> B,
 template <class T, bool DIV>
 __global__ void __launch_bounds__(kBlock) k_solver_finalize(DevParams<T> P, DevBufs<T> B)
 {
-    count_launch(&B.sc->launches);
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
-    const T h = (T)(DIV ? B.sc->dt : B.sc->dt_next);
-    const V3<T> a = pressure_accel_i(P, B, i);
-    stv(B.pa, i, pack(a, T(0)));
-    v4_t<T> v = ldv(B.v, i);
+    count_launch(&B.gsc->launches);
+    const SlotInfo q = slot_info(P);
+    if (!q.act) return;
+    const StepScalars *sc = B.sc + q.s;
+    const T h = (T)(DIV ? sc->dt : sc->dt_next);
+    const V3<T> a = pressure_accel_i(P, B, q.i);
+    stv(B.pa, q.i, pack(a, T(0)));
+    v4_t<T> v = ldv(B.v, q.i);
     v.x += h * a.x;
     v.y += h * a.y;
     v.z += h * a.z;
-    stv(B.v, i, v);
+    stv(B.v, q.i, v);
 }
 
-__global__ void k_step_begin(StepScalars *sc)
+__global__ void k_step_begin(StepScalars *sc, StepScalars *gsc, uint32_t nscenes)
 {
+    for (uint32_t s = threadIdx.x; s < nscenes; s += blockDim.x) {
+        StepScalars &r = sc[s];
+        r.flags = 0;
+        r.max_nf = 0;
+        r.max_nb = 0;
+        r.maxvel_bits = 0;
+        r.iters_cg = 0;
+        r.cg_err = 0.0;
+        r.cg_state = 1;
+    }
     if (threadIdx.x == 0) {
-        sc->launches = 1;
-        sc->flags = 0;
-        sc->loop_guard = 0;
-        sc->max_nf = 0;
-        sc->max_nb = 0;
-        sc->maxvel_bits = 0;
-        sc->iters_cg = 0;
-        sc->cg_err = 0.0;
-        sc->cg_state = 1;
+        gsc->launches = 1;
+        gsc->flags = 0;
+        gsc->loop_guard = 0;
     }
 }
 
-template <class T>
-__global__ void k_loop_begin(StepScalars *sc, int div, unsigned max_iter)
+__global__ void k_loop_begin(StepScalars *sc, StepScalars *gsc, uint32_t nscenes, int div, unsigned max_iter)
 {
-    count_launch(&sc->launches);
+    count_launch(&gsc->launches);
+    const unsigned cont = max_iter > 0 ? 1u : 0u;
+    for (uint32_t s = threadIdx.x; s < nscenes; s += blockDim.x) {
+        StepScalars &r = sc[s];
+        if (div) { r.iters_v = 0; r.avg_err_v = 0.0; }
+        else { r.iters = 0; r.avg_err = 0.0; }
+        r.cont = cont;
+    }
     if (threadIdx.x == 0) {
-        if (div) { sc->iters_v = 0; sc->avg_err_v = 0.0; }
-        else { sc->iters = 0; sc->avg_err = 0.0; }
-        sc->cont = max_iter > 0 ? 1u : 0u;
-        sc->loop_guard = 0;
+        gsc->cont = cont;
+        gsc->loop_guard = 0;
     }
 }
 
@@ -545,10 +661,11 @@ __global__ void k_loop_begin(StepScalars *sc, int div, unsigned max_iter)
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_xsph(DevParams<T> P, DevBufs<T> B, int div_on)
 {
-    count_launch(&B.sc->launches);
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
-    const T h = (T)B.sc->dt;
+    count_launch(&B.gsc->launches);
+    const SlotInfo q = slot_info(P);
+    if (!q.act) return;
+    const uint32_t i = q.i;
+    const T h = (T)B.sc[q.s].dt;
     const T invH = T(1) / h;
     const v4_t<T> xi = ldv(B.x, i);
     const V3<T> vi = xyz<T>(ldv(B.v, i));
@@ -623,17 +740,19 @@ template <class T> __device__ __forceinline__ V3<T> sym_mul(const v4_t<T> &a, co
 // static boundary), warm start g = v + vDiff (already in cg_x), r = b - A g, p = M^-1 r, and
 // the first reductions of Eigen's conjugate_gradient (ConjugateGradient.h:29-70), one pass.
 template <class T>
-__global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T> B, ReduceSlot slot,
-                                                        cudaGraphConditionalHandle handle, int use_handle)
+__global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T> B, cudaGraphConditionalHandle handle,
+                                                        int use_handle)
 {
-    count_launch(&B.sc->launches);
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    count_launch(&B.gsc->launches);
+    const SlotInfo q = slot_info(P);
+    StepScalars *const sc = B.sc + q.s;
     DSum<3> mine;
     mine.v[0] = mine.v[1] = mine.v[2] = 0.0;
-    if (i < P.n) {
+    if (q.act) {
+        const uint32_t i = q.i;
         const v4_t<T> xi = ldv(B.x, i);
         const T rhoi = B.density[i];
-        const T dt = (T)B.sc->dt;
+        const T dt = (T)sc->dt;
         const T eps2 = T(0.01) * P.h2;
         const v4_t<T> gi4 = ldv(B.cg_x, i);
         const V3<T> gi = xyz<T>(gi4);
@@ -686,14 +805,15 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T
         mine.v[1] = (double)dot(r, r);
         mine.v[2] = (double)dot(r, p);
     }
-    StepScalars *sc = B.sc;
     const double tol = P.visc_tol;
     const unsigned maxit = P.visc_max_iter;
-    grid_sum_finalize<3>(mine, slot, [&](const DSum<3> &tot) {
+    const DevParams<T> &PP = P;
+    const DevBufs<T> &BB = B;
+    grid_sum_finalize<3>(mine, scene_reduce(P, B, q), [&](const DSum<3> &tot) {
         sc->cg_rhs2 = tot.v[0];
         sc->iters_cg = 0;
         sc->cg_err = 0.0;
-        sc->loop_guard = 0;
+        BB.gsc->loop_guard = 0;
         if (tot.v[0] == 0.0) {
             sc->cg_state = 2;
         } else {
@@ -712,21 +832,24 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T
         const bool cont = sc->cg_state == 0 && maxit > 0;
         if (sc->cg_state == 0 && maxit == 0) sc->cg_err = sqrt(tot.v[1] / tot.v[0]);
         sc->cont = cont ? 1u : 0u;
-        if (use_handle) cudaGraphSetConditional(handle, cont ? 1u : 0u);
+        batch_decide(PP, BB, handle, use_handle);
     });
 }
 
 // tmp = A p and p.tmp -> alpha (ConjugateGradient.h:74-76)
 template <class T>
-__global__ void __launch_bounds__(kBlock) k_cg_matvec(DevParams<T> P, DevBufs<T> B, ReduceSlot slot,
-                                                       cudaGraphConditionalHandle h, int use_handle)
+__global__ void __launch_bounds__(kBlock) k_cg_matvec(DevParams<T> P, DevBufs<T> B, cudaGraphConditionalHandle h,
+                                                       int use_handle)
 {
-    count_launch(&B.sc->launches);
-    loop_guard(B.sc, P.visc_max_iter + 1, h, use_handle);
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    count_launch(&B.gsc->launches);
+    loop_guard(B.gsc, P.visc_max_iter + 1, h, use_handle);
+    const SlotInfo q = slot_info(P);
+    StepScalars *const sc = B.sc + q.s;
+    const bool live = scene_live(P, sc);
     DSum<1> mine;
     mine.v[0] = 0.0;
-    if (i < P.n) {
+    if (q.act && live) {
+        const uint32_t i = q.i;
         const v4_t<T> xi = ldv(B.x, i);
         const T rhoi = B.density[i];
         const T eps2 = T(0.01) * P.h2;
@@ -744,27 +867,31 @@ __global__ void __launch_bounds__(kBlock) k_cg_matvec(DevParams<T> P, DevBufs<T>
                               acc = add(acc, scl(r, f * dot(sub(pi, xyz<T>(d.p)), r)));
                           });
         if (P.mub != T(0)) acc = add(acc, weiler_boundary(P, B, i, xi, rhoi, pi));
-        const T dt = (T)B.sc->dt;
+        const T dt = (T)sc->dt;
         const V3<T> t = sub(pi, scl(acc, dt / rhoi));
         stv(B.cg_t, i, pack(t, T(0)));
         mine.v[0] = (double)dot(pi, t);
     }
-    StepScalars *sc = B.sc;
-    grid_sum_finalize<1>(mine, slot, [&](const DSum<1> &tot) { sc->cg_alpha = sc->cg_absnew / tot.v[0]; });
+    grid_sum_finalize<1>(mine, scene_reduce(P, B, q), [&](const DSum<1> &tot) {
+        if (live) sc->cg_alpha = sc->cg_absnew / tot.v[0];
+    });
 }
 
 // x += alpha p; r -= alpha tmp; |r|^2; z = M^-1 r; r.z -> beta (ConjugateGradient.h:77-88).
 // Element arithmetic in the bulk precision, sums accumulated in FP64.
 template <class T>
-__global__ void __launch_bounds__(kBlock) k_cg_update(DevParams<T> P, DevBufs<T> B, ReduceSlot slot,
-                                                       cudaGraphConditionalHandle handle, int use_handle)
+__global__ void __launch_bounds__(kBlock) k_cg_update(DevParams<T> P, DevBufs<T> B, cudaGraphConditionalHandle handle,
+                                                       int use_handle)
 {
-    count_launch(&B.sc->launches);
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    count_launch(&B.gsc->launches);
+    const SlotInfo q = slot_info(P);
+    StepScalars *const sc = B.sc + q.s;
+    const bool live = scene_live(P, sc);
     DSum<2> mine;
     mine.v[0] = mine.v[1] = 0.0;
-    if (i < P.n) {
-        const T alpha = (T)B.sc->cg_alpha;
+    if (q.act && live) {
+        const uint32_t i = q.i;
+        const T alpha = (T)sc->cg_alpha;
         const V3<T> p = xyz<T>(ldv(B.cg_p, i));
         const V3<T> t = xyz<T>(ldv(B.cg_t, i));
         v4_t<T> x4 = ldv(B.cg_x, i);
@@ -778,36 +905,41 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(DevParams<T> P, DevBufs<T>
         mine.v[0] = (double)dot(r, r);
         mine.v[1] = (double)dot(r, z);
     }
-    StepScalars *sc = B.sc;
     const unsigned maxit = P.visc_max_iter;
-    grid_sum_finalize<2>(mine, slot, [&](const DSum<2> &tot) {
-        sc->cg_res2 = tot.v[0];
-        sc->cg_err = sqrt(tot.v[0] / sc->cg_rhs2);
-        bool cont;
-        if (tot.v[0] < sc->cg_thresh) {
-            sc->cg_state = 1;
-            cont = false;
-        } else {
-            const double absOld = sc->cg_absnew;
-            sc->cg_absnew = tot.v[1];
-            sc->cg_beta = tot.v[1] / absOld;
-            sc->iters_cg += 1;
-            cont = sc->iters_cg < maxit;
+    const DevParams<T> &PP = P;
+    const DevBufs<T> &BB = B;
+    grid_sum_finalize<2>(mine, scene_reduce(P, B, q), [&](const DSum<2> &tot) {
+        if (live) {
+            sc->cg_res2 = tot.v[0];
+            sc->cg_err = sqrt(tot.v[0] / sc->cg_rhs2);
+            bool cont;
+            if (tot.v[0] < sc->cg_thresh) {
+                sc->cg_state = 1;
+                cont = false;
+            } else {
+                const double absOld = sc->cg_absnew;
+                sc->cg_absnew = tot.v[1];
+                sc->cg_beta = tot.v[1] / absOld;
+                sc->iters_cg += 1;
+                cont = sc->iters_cg < maxit;
+            }
+            sc->cont = cont ? 1u : 0u;
         }
-        sc->cont = cont ? 1u : 0u;
-        if (use_handle) cudaGraphSetConditional(handle, cont ? 1u : 0u);
+        batch_decide(PP, BB, handle, use_handle);
     });
 }
 
-// p = z + beta p (ConjugateGradient.h:88); the weight in p.w is kept
+// p = z + beta p (ConjugateGradient.h:88) for scenes whose CG continues; the weight in p.w is kept
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_cg_p(DevParams<T> P, DevBufs<T> B)
 {
-    count_launch(&B.sc->launches);
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
-    if (B.sc->cg_state != 0) return;
-    const T beta = (T)B.sc->cg_beta;
+    count_launch(&B.gsc->launches);
+    const SlotInfo q = slot_info(P);
+    if (!q.act) return;
+    const StepScalars *sc = B.sc + q.s;
+    if (sc->cg_state != 0 || sc->cont == 0) return;
+    const uint32_t i = q.i;
+    const T beta = (T)sc->cg_beta;
     const V3<T> z = xyz<T>(ldv(B.cg_z, i));
     v4_t<T> p = ldv(B.cg_p, i);
     p.x = z.x + beta * (T)p.x;
@@ -820,22 +952,24 @@ __global__ void __launch_bounds__(kBlock) k_cg_p(DevParams<T> P, DevBufs<T> B)
 // viscosity forces + CFL + velocity kick
 // ==========================================================================
 // applyForces (Viscosity_Weiler2018.cpp:928-936): a += (x - v)/dt, vDiff = x - v;
-// updateTimeStepSizeCFL (Simulation.cpp:415-492): max |v + a h|^2 over particles;
-// kick v += h a (TimeStepDFSPH.cpp:192-208).  The last block computes dt_next.
+// updateTimeStepSizeCFL (Simulation.cpp:415-492): max |v + a h|^2 over the scene's particles;
+// kick v += h a (TimeStepDFSPH.cpp:192-208).  The scene's last block computes its dt_next.
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_kick(DevParams<T> P, DevBufs<T> B)
 {
-    count_launch(&B.sc->launches);
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    count_launch(&B.gsc->launches);
+    const SlotInfo q = slot_info(P);
+    StepScalars *const sc = B.sc + q.s;
     float m = 0.0f;
-    const double hd = B.sc->dt;
-    if (i < P.n) {
+    const double hd = sc->dt;
+    if (q.act) {
+        const uint32_t i = q.i;
         const T h = (T)hd;
         V3<T> a = xyz<T>(ldv(B.a, i));
         v4_t<T> v4 = ldv(B.v, i);
         const V3<T> v = xyz<T>(v4);
         if (P.visc_on) {
-            const V3<T> x = B.sc->cg_state == 2 ? mk3<T>(0, 0, 0) : xyz<T>(ldv(B.cg_x, i));
+            const V3<T> x = sc->cg_state == 2 ? mk3<T>(0, 0, 0) : xyz<T>(ldv(B.cg_x, i));
             const V3<T> dv = sub(x, v);
             a = add(a, scl(dv, T(1) / h));
             stv(B.vdiff, i, pack(dv, T(0)));
@@ -843,7 +977,7 @@ __global__ void __launch_bounds__(kBlock) k_kick(DevParams<T> P, DevBufs<T> B)
         }
         const V3<T> vn = add(v, scl(a, h));
         const T m2 = dot(vn, vn);
-        if (!(m2 <= T(3.0e38))) atomicOr(&B.sc->flags, kFlagNonFinite);
+        if (!(m2 <= T(3.0e38))) atomicOr(&sc->flags, kFlagNonFinite);
         m = (float)m2;
         if (!(m >= 0.0f)) m = 0.0f;
         v4.x = vn.x; v4.y = vn.y; v4.z = vn.z;
@@ -857,21 +991,21 @@ __global__ void __launch_bounds__(kBlock) k_kick(DevParams<T> P, DevBufs<T> B)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0) wm[warp] = m;
     __syncthreads();
+    const ReduceSlot rs = scene_reduce(P, B, q);
     if (threadIdx.x == 0) {
         float bm = 0.0f;
         for (int w = 0; w < (int)(blockDim.x >> 5); w++) bm = fmaxf(bm, wm[w]);
-        atomicMax(&B.sc->maxvel_bits, __float_as_uint(bm));
+        atomicMax(&sc->maxvel_bits, __float_as_uint(bm));
         __threadfence();
-        const unsigned t = atomicAdd(B.counter, 1u);
-        amLast = (t == gridDim.x - 1);
+        const unsigned t = atomicAdd(rs.counter, 1u);
+        amLast = (t == rs.count - 1);
     }
     __syncthreads();
     if (amLast && threadIdx.x == 0) {
         __threadfence();
-        StepScalars *sc = B.sc;
         double maxVel = (double)__uint_as_float(atomicAdd(&sc->maxvel_bits, 0u));
         sc->maxvel_bits = 0;
-        *B.counter = 0;
+        *rs.counter = 0;
         double hn = hd;
         if (P.cfl_method != 0) {
             if (maxVel < 1.0e-9) maxVel = 1.0e-9;
@@ -894,10 +1028,11 @@ __global__ void __launch_bounds__(kBlock) k_kick(DevParams<T> P, DevBufs<T> B)
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_press_init(DevParams<T> P, DevBufs<T> B)
 {
-    count_launch(&B.sc->launches);
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
-    const T h = (T)B.sc->dt_next;
+    count_launch(&B.gsc->launches);
+    const SlotInfo q = slot_info(P);
+    if (!q.act) return;
+    const uint32_t i = q.i;
+    const T h = (T)B.sc[q.s].dt_next;
     const v4_t<T> xi = ldv(B.x, i);
     const V3<T> vi = xyz<T>(ldv(B.v, i));
     T accf = T(0);
@@ -921,16 +1056,18 @@ __global__ void __launch_bounds__(kBlock) k_press_init(DevParams<T> P, DevBufs<T
 }
 
 // x += h_old v (TimeStepDFSPH.cpp:220-237) accumulated in FP64 (double-float
-// compensated positions in FP32 mode), kappa *= h_new^2 (:365-383); the last
-// block advances time (:248) and makes dt_next the step size of the next step.
+// compensated positions in FP32 mode), kappa *= h_new^2 (:365-383); the scene's
+// last block advances its time (:248) and makes dt_next its next step size.
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_integrate(DevParams<T> P, DevBufs<T> B)
 {
-    count_launch(&B.sc->launches);
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const double h = B.sc->dt;
-    const double hn = B.sc->dt_next;
-    if (i < P.n) {
+    count_launch(&B.gsc->launches);
+    const SlotInfo q = slot_info(P);
+    StepScalars *const sc = B.sc + q.s;
+    const double h = sc->dt;
+    const double hn = sc->dt_next;
+    if (q.act) {
+        const uint32_t i = q.i;
         v4_t<T> x = ldv(B.x, i);
         const v4_t<T> v = ldv(B.v, i);
         if (B.xlo) {
@@ -950,15 +1087,15 @@ __global__ void __launch_bounds__(kBlock) k_integrate(DevParams<T> P, DevBufs<T>
     }
     __shared__ bool amLast;
     __syncthreads();
+    const ReduceSlot rs = scene_reduce(P, B, q);
     if (threadIdx.x == 0) {
         __threadfence();
-        const unsigned t = atomicAdd(B.counter, 1u);
-        amLast = (t == gridDim.x - 1);
+        const unsigned t = atomicAdd(rs.counter, 1u);
+        amLast = (t == rs.count - 1);
     }
     __syncthreads();
     if (amLast && threadIdx.x == 0) {
-        StepScalars *sc = B.sc;
-        *B.counter = 0;
+        *rs.counter = 0;
         sc->time += h;
         sc->dt_used = h;
         sc->dt = hn;
@@ -974,9 +1111,10 @@ __global__ void __launch_bounds__(kBlock) k_integrate(DevParams<T> P, DevBufs<T>
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_features(DevParams<T> P, DevBufs<T> B)
 {
-    count_launch(&B.sc->launches);
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
+    count_launch(&B.gsc->launches);
+    const SlotInfo q = slot_info(P);
+    if (!q.act) return;
+    const uint32_t i = q.i;
     const v4_t<T> xi = ldv(B.x, i);
     const float4 f0 = *reinterpret_cast<const float4 *>(B.feat + (size_t)i * 8);
     const float f4 = B.feat[(size_t)i * 8 + 4];
@@ -1013,15 +1151,17 @@ __global__ void __launch_bounds__(kBlock) k_features(DevParams<T> P, DevBufs<T> 
 template <class T, bool DIV>
 __global__ void __launch_bounds__(kBlock) k_ws_kappa(DevParams<T> P, DevBufs<T> B)
 {
-    count_launch(&B.sc->launches);
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
+    count_launch(&B.gsc->launches);
+    const SlotInfo q = slot_info(P);
+    if (!q.act) return;
+    const uint32_t i = q.i;
+    const StepScalars *sc = B.sc + q.s;
     T k = T(0);
     if (DIV) {
-        const T h = (T)B.sc->dt;
+        const T h = (T)sc->dt;
         if (B.dadv[i] > T(0) && B.nf[i] + B.nbn[i] >= 20u) k = (T)fmaxf(B.mlp_y[(size_t)i * 2] * P.ws_scale_v, 0.0f) / h;
     } else {
-        const T h = (T)B.sc->dt_next;
+        const T h = (T)sc->dt_next;
         if (B.dadv[i] > T(1)) k = (T)fmaxf(B.mlp_y[(size_t)i * 2 + 1] * P.ws_scale_p, 0.0f) / (h * h);
     }
     B.kl[i] = k;
@@ -1032,9 +1172,10 @@ __global__ void __launch_bounds__(kBlock) k_ws_kappa(DevParams<T> P, DevBufs<T> 
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_ws_accel2(DevParams<T> P, DevBufs<T> B)
 {
-    count_launch(&B.sc->launches);
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
+    count_launch(&B.gsc->launches);
+    const SlotInfo q = slot_info(P);
+    if (!q.act) return;
+    const uint32_t i = q.i;
     const v4_t<T> xi = ldv(B.xk, i);
     const T pc = (T)xi.w, pl = B.kl[i];
     V3<T> ac = mk3<T>(0, 0, 0), al = mk3<T>(0, 0, 0);
@@ -1059,16 +1200,18 @@ __global__ void __launch_bounds__(kBlock) k_ws_accel2(DevParams<T> P, DevBufs<T>
 }
 
 // Initial residuals of both candidates (the error the first Jacobi iteration would report,
-// TimeStepDFSPH.cpp:621-706 / :544-619); the last block picks the predicted warm start only
-// if its residual is lower.
+// TimeStepDFSPH.cpp:621-706 / :544-619); the scene's last block picks the predicted warm
+// start only if its residual is lower.
 template <class T, bool DIV>
-__global__ void __launch_bounds__(kBlock) k_ws_residual2(DevParams<T> P, DevBufs<T> B, ReduceSlot slot)
+__global__ void __launch_bounds__(kBlock) k_ws_residual2(DevParams<T> P, DevBufs<T> B)
 {
-    count_launch(&B.sc->launches);
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    count_launch(&B.gsc->launches);
+    const SlotInfo q = slot_info(P);
+    StepScalars *const sc = B.sc + q.s;
     DSum<2> mine;
     mine.v[0] = mine.v[1] = 0.0;
-    if (i < P.n) {
+    if (q.act) {
+        const uint32_t i = q.i;
         const v4_t<T> xi = ldv(B.x, i);
         const V3<T> a1 = xyz<T>(ldv(B.pa, i)), a2 = xyz<T>(ldv(B.pa2, i));
         T s1 = T(0), s2 = T(0);
@@ -1088,13 +1231,13 @@ __global__ void __launch_bounds__(kBlock) k_ws_residual2(DevParams<T> P, DevBufs
         T si;
         bool zero = false;
         if (DIV) {
-            const T h = (T)B.sc->dt;
+            const T h = (T)sc->dt;
             ap1 *= h;
             ap2 *= h;
             si = -B.dadv[i];
             zero = B.nf[i] + B.nbn[i] < 20u;
         } else {
-            const T h = (T)B.sc->dt_next;
+            const T h = (T)sc->dt_next;
             ap1 *= h * h;
             ap2 *= h * h;
             si = T(1) - B.dadv[i];
@@ -1106,12 +1249,12 @@ __global__ void __launch_bounds__(kBlock) k_ws_residual2(DevParams<T> P, DevBufs
             mine.v[1] = -(double)P.rho0 * (double)r2;
         }
     }
-    StepScalars *sc = B.sc;
-    const uint32_t n = P.n;
-    grid_sum_finalize<2>(mine, slot, [&](const DSum<2> &tot) {
+    const uint32_t n_s = q.end - q.begin;
+    grid_sum_finalize<2>(mine, scene_reduce(P, B, q), [&](const DSum<2> &tot) {
         const int k = DIV ? 0 : 1;
-        sc->ws_rc[k] = tot.v[0] / (double)n;
-        sc->ws_rl[k] = tot.v[1] / (double)n;
+        const double inv = n_s ? 1.0 / (double)n_s : 0.0;
+        sc->ws_rc[k] = tot.v[0] * inv;
+        sc->ws_rl[k] = tot.v[1] * inv;
         if (tot.v[1] < tot.v[0]) sc->ws_used |= (1u << k);
         else sc->ws_used &= ~(1u << k);
     });
@@ -1120,13 +1263,13 @@ __global__ void __launch_bounds__(kBlock) k_ws_residual2(DevParams<T> P, DevBufs
 template <class T, bool DIV>
 __global__ void __launch_bounds__(kBlock) k_ws_apply(DevParams<T> P, DevBufs<T> B)
 {
-    count_launch(&B.sc->launches);
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
-    if (!(B.sc->ws_used & (1u << (DIV ? 0 : 1)))) return;
-    const T k = B.kl[i];
-    (DIV ? B.kappa_v : B.kappa)[i] = k;
-    store_w(B.xk, i, k);
+    count_launch(&B.gsc->launches);
+    const SlotInfo q = slot_info(P);
+    if (!q.act) return;
+    if (!(B.sc[q.s].ws_used & (1u << (DIV ? 0 : 1)))) return;
+    const T k = B.kl[q.i];
+    (DIV ? B.kappa_v : B.kappa)[q.i] = k;
+    store_w(B.xk, q.i, k);
 }
 
 // ==========================================================================
@@ -1134,53 +1277,60 @@ __global__ void __launch_bounds__(kBlock) k_ws_apply(DevParams<T> P, DevBufs<T> 
 // ==========================================================================
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_boundary_keys(DevParams<T> P, const v4_t<T> *__restrict__ xb,
-                                                           uint32_t *keys, uint32_t *vals, uint32_t nb)
+                                                           const uint32_t *__restrict__ bscene, uint32_t *keys,
+                                                           uint32_t *vals)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nb) return;
+    if (i >= P.nb) return;
+    const SceneDev<T> S = scene_get(P, bscene ? bscene[i] : 0u);
     int cx, cy, cz;
-    cell_of(P, ldv(xb, i), cx, cy, cz);
-    keys[i] = morton3((uint32_t)cx, (uint32_t)cy, (uint32_t)cz);
+    cell_of(S, ldv(xb, i), cx, cy, cz);
+    keys[i] = S.key_prefix | morton3((uint32_t)cx, (uint32_t)cy, (uint32_t)cz);
     vals[i] = i;
 }
 
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_boundary_gather(DevParams<T> P, DevBufs<T> B, const v4_t<T> *__restrict__ xb_in,
+                                                             const uint32_t *__restrict__ bscene_in,
                                                              const uint32_t *__restrict__ perm, uint32_t *cells)
 {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= P.nb) return;
-    const uint32_t s = perm[k];
-    v4_t<T> x = ldv(xb_in, s);
+    const uint32_t src = perm[k];
+    v4_t<T> x = ldv(xb_in, src);
     x.w = 0;
     stv(B.xb, k, x);
-    B.bid[k] = s;
+    B.bid[k] = src;
+    const uint32_t s = bscene_in ? bscene_in[src] : 0u;
+    if (B.bscene) B.bscene[k] = s;
+    const SceneDev<T> S = scene_get(P, s);
     int cx, cy, cz;
-    cell_of(P, x, cx, cy, cz);
-    cells[k] = ((uint32_t)cz * (uint32_t)P.dimy + (uint32_t)cy) * (uint32_t)P.dimx + (uint32_t)cx;
+    cell_of(S, x, cx, cy, cz);
+    cells[k] = S.cell_off + local_cell(S, cx, cy, cz);
 }
 
 // BoundaryModel_Akinci2012::computeBoundaryVolume (BoundaryModel_Akinci2012.cpp:48-75):
-// V_b = 1 / (W0 + sum over boundary neighbours of W)
+// V_b = 1 / (W0 + sum over boundary neighbours of the same scene of W)
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_boundary_volume(DevParams<T> P, DevBufs<T> B)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.nb) return;
+    const SceneDev<T> S = scene_get(P, B.bscene ? B.bscene[i] : 0u);
     v4_t<T> xi = ldv(B.xb, i);
     int cx, cy, cz;
-    cell_of(P, xi, cx, cy, cz);
+    cell_of(S, xi, cx, cy, cz);
     T delta = P.K.w0;
     for (int dz = -1; dz <= 1; dz++) {
         const int z = cz + dz;
-        if (z < 0 || z >= P.dimz) continue;
+        if (z < 0 || z >= S.dimz) continue;
         for (int dy = -1; dy <= 1; dy++) {
             const int y = cy + dy;
-            if (y < 0 || y >= P.dimy) continue;
+            if (y < 0 || y >= S.dimy) continue;
             for (int dx = -1; dx <= 1; dx++) {
                 const int x = cx + dx;
-                if (x < 0 || x >= P.dimx) continue;
-                const uint32_t c = ((uint32_t)z * (uint32_t)P.dimy + (uint32_t)y) * (uint32_t)P.dimx + (uint32_t)x;
+                if (x < 0 || x >= S.dimx) continue;
+                const uint32_t c = S.cell_off + local_cell(S, x, y, z);
                 const uint32_t s = B.bcstart[c];
                 if (s == kEmpty) continue;
                 const uint32_t e = B.bcend[c];
@@ -1210,31 +1360,35 @@ __global__ void __launch_bounds__(kBlock) k_boundary_volume_store(DevParams<T> P
 // ==========================================================================
 // host <-> device field transfer helpers
 // ==========================================================================
+// slot i of scene s takes upload entry u = ustart_s + (i - begin_s); its id is id[u] (or u)
 template <class T>
 __global__ void k_init_state(DevParams<T> P, DevBufs<T> B, const double *__restrict__ x, const double *__restrict__ v,
                              const uint32_t *__restrict__ id)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
+    const SlotInfo q = slot_info(P);
+    if (!q.act) return;
+    const uint32_t i = q.i;
+    const uint32_t u = scene_get(P, q.s).ustart + (i - q.begin);
     v4_t<T> xx, vv, zz;
-    xx.x = (T)x[3 * i]; xx.y = (T)x[3 * i + 1]; xx.z = (T)x[3 * i + 2]; xx.w = 0;
-    vv.x = (T)v[3 * i]; vv.y = (T)v[3 * i + 1]; vv.z = (T)v[3 * i + 2]; vv.w = 0;
+    xx.x = (T)x[3 * (size_t)u]; xx.y = (T)x[3 * (size_t)u + 1]; xx.z = (T)x[3 * (size_t)u + 2]; xx.w = 0;
+    vv.x = (T)v[3 * (size_t)u]; vv.y = (T)v[3 * (size_t)u + 1]; vv.z = (T)v[3 * (size_t)u + 2]; vv.w = 0;
     zz.x = zz.y = zz.z = zz.w = 0;
     stv(B.x, i, xx);
     stv(B.v, i, vv);
     stv(B.vdiff, i, zz);
     if (B.xlo)
-        B.xlo[i] = make_float4((float)(x[3 * i] - (double)xx.x), (float)(x[3 * i + 1] - (double)xx.y),
-                               (float)(x[3 * i + 2] - (double)xx.z), 0.f);
+        B.xlo[i] = make_float4((float)(x[3 * (size_t)u] - (double)xx.x), (float)(x[3 * (size_t)u + 1] - (double)xx.y),
+                               (float)(x[3 * (size_t)u + 2] - (double)xx.z), 0.f);
     B.kappa[i] = 0;
     B.kappa_v[i] = 0;
-    B.id[i] = id ? id[i] : i;
+    B.id[i] = id ? id[u] : u;
 }
 
-__global__ void k_inverse_perm(const uint32_t *__restrict__ id, uint32_t *__restrict__ inv, uint32_t n)
+template <class T>
+__global__ void k_inverse_perm(DevParams<T> P, const uint32_t *__restrict__ id, uint32_t *__restrict__ inv)
 {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < n && id[k] < n) inv[id[k]] = k;
+    const SlotInfo q = slot_info(P);
+    if (q.act && id[q.i] < P.nreal) inv[id[q.i]] = q.i;
 }
 
 template <class T> __device__ __forceinline__ void put(void *out, int dt, size_t idx, double v)
@@ -1250,26 +1404,32 @@ template <class T> __device__ __forceinline__ double get(const void *in, int dt,
     return (double)static_cast<const uint32_t *>(in)[idx];
 }
 
-// field value of sorted particle k, component c, written at id order
+// boundary field of sorted boundary particle k, written at its upload index
+template <class T>
+__global__ void k_scatter_boundary(DevParams<T> P, DevBufs<T> B, int field, void *out, int odt)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= P.nb) return;
+    const v4_t<T> x = ldv(B.xb, k);
+    const uint32_t d = B.bid[k];
+    if (field == SPHGB_FIELD_BOUNDARY_VOLUME) {
+        put<T>(out, odt, d, (double)x.w);
+    } else {
+        put<T>(out, odt, 3 * (size_t)d, (double)x.x);
+        put<T>(out, odt, 3 * (size_t)d + 1, (double)x.y);
+        put<T>(out, odt, 3 * (size_t)d + 2, (double)x.z);
+    }
+}
+
+// field value of the particle in slot k, written at its particle id
 template <class T>
 __global__ void k_scatter_field(DevParams<T> P, DevBufs<T> B, int field, void *out, int odt)
 {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (field == SPHGB_FIELD_BOUNDARY_VOLUME || field == SPHGB_FIELD_BOUNDARY_POSITION) {
-        if (k >= P.nb) return;
-        const v4_t<T> x = ldv(B.xb, k);
-        const uint32_t d = B.bid[k];
-        if (field == SPHGB_FIELD_BOUNDARY_VOLUME) put<T>(out, odt, d, (double)x.w);
-        else {
-            put<T>(out, odt, 3 * (size_t)d, (double)x.x);
-            put<T>(out, odt, 3 * (size_t)d + 1, (double)x.y);
-            put<T>(out, odt, 3 * (size_t)d + 2, (double)x.z);
-        }
-        return;
-    }
-    if (k >= P.n) return;
+    const SlotInfo q = slot_info(P);
+    if (!q.act) return;
+    const uint32_t k = q.i;
     const uint32_t d = B.id[k];
-    const double hn = B.sc->dt_next;
+    const double hn = B.sc[q.s].dt_next;
     auto vec = [&](const v4_t<T> *arr, const float4 *lo) {
         const v4_t<T> a = ldv(arr, k);
         double ax = (double)a.x, ay = (double)a.y, az = (double)a.z;
@@ -1305,7 +1465,7 @@ template <class T>
 __global__ void k_upload_field(DevParams<T> P, DevBufs<T> B, int field, const void *in, int idt, const uint32_t *__restrict__ inv)
 {
     const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;   // particle id
-    if (d >= P.n) return;
+    if (d >= P.nreal) return;
     const uint32_t k = inv[d];
     auto vec = [&](v4_t<T> *arr, float4 *lo) {
         const double ax = get<T>(in, idt, 3 * (size_t)d), ay = get<T>(in, idt, 3 * (size_t)d + 1),
@@ -1343,130 +1503,132 @@ __global__ void k_lists_to_ids(const uint32_t *__restrict__ list, const uint32_t
     }
 }
 
+// Keeps the GPU busy for about `ns` nanoseconds without touching memory, so that
+// the host can enqueue an event, a kernel and an event back to back behind it
+// (per-kernel event timing without host-submission gaps).  Bounded: one sleep.
+__global__ void k_delay(unsigned ns)
+{
+    if (threadIdx.x == 0) __nanosleep(ns);
+}
+
 }  // namespace
 
 // ==========================================================================
-// launchers
+// launchers: every particle kernel runs over all slots of all scenes
 // ==========================================================================
 template <class T> void launch_keys(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {
-    if (P.n) k_keys<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
+    if (P.np) k_keys<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
 }
 template <class T> void launch_gather(const DevParams<T> &P, const DevBufs<T> &B, const uint32_t *perm, cudaStream_t s)
 {
-    if (P.n) k_gather<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B, perm);
+    if (P.np) k_gather<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B, perm);
 }
 template <class T> void launch_cell_ranges(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {
-    if (P.n) k_cell_ranges<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B.cellid, B.cstart, B.cend, P.n, &B.sc->launches);
+    if (P.np) k_cell_ranges<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
 }
 template <class T> void launch_build(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {
-    if (P.n) k_build<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
+    if (P.np) k_build<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
 }
 template <class T> void launch_pressure_accel(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s,
                                               cudaGraphConditionalHandle h, bool use_handle)
 {
     const unsigned limit = (div ? P.max_iter_v : P.max_iter) + 1;
-    if (P.n) k_pressure_accel<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B, limit, h, use_handle ? 1 : 0);
+    if (P.np) k_pressure_accel<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B, limit, h, use_handle ? 1 : 0);
 }
 template <class T>
 void launch_jacobi(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaGraphConditionalHandle h, bool use_handle,
                    cudaStream_t s)
 {
-    if (!P.n) return;
-    ReduceSlot slot{B.partials, B.counter};
-    if (div) k_jacobi<T, true><<<grid_for(P.n), kBlock, 0, s>>>(P, B, slot, h, use_handle ? 1 : 0);
-    else k_jacobi<T, false><<<grid_for(P.n), kBlock, 0, s>>>(P, B, slot, h, use_handle ? 1 : 0);
+    if (!P.np) return;
+    if (div) k_jacobi<T, true><<<grid_for(P.np), kBlock, 0, s>>>(P, B, h, use_handle ? 1 : 0);
+    else k_jacobi<T, false><<<grid_for(P.np), kBlock, 0, s>>>(P, B, h, use_handle ? 1 : 0);
 }
 template <class T> void launch_solver_finalize(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s)
 {
-    if (!P.n) return;
-    if (div) k_solver_finalize<T, true><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
-    else k_solver_finalize<T, false><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
+    if (!P.np) return;
+    if (div) k_solver_finalize<T, true><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
+    else k_solver_finalize<T, false><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
 }
 template <class T> void launch_step_begin(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {
-    k_step_begin<<<1, 32, 0, s>>>(B.sc);
+    k_step_begin<<<1, kBlock, 0, s>>>(B.sc, B.gsc, P.nscenes);
 }
 template <class T> void launch_loop_begin(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s)
 {
-    k_loop_begin<T><<<1, 32, 0, s>>>(B.sc, div ? 1 : 0, div ? P.max_iter_v : P.max_iter);
+    k_loop_begin<<<1, kBlock, 0, s>>>(B.sc, B.gsc, P.nscenes, div ? 1 : 0, div ? P.max_iter_v : P.max_iter);
 }
 template <class T> void launch_xsph(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {
-    if (P.n) k_xsph<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B, P.div_on);
+    if (P.np) k_xsph<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B, P.div_on);
 }
 template <class T>
 void launch_visc_setup(const DevParams<T> &P, const DevBufs<T> &B, cudaGraphConditionalHandle h, bool use_handle,
                        cudaStream_t s)
 {
-    if (!P.n) return;
-    ReduceSlot slot{B.partials, B.counter};
-    k_visc_setup<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B, slot, h, use_handle ? 1 : 0);
+    if (P.np) k_visc_setup<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B, h, use_handle ? 1 : 0);
 }
 template <class T> void launch_cg_matvec(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s,
                                          cudaGraphConditionalHandle h, bool use_handle)
 {
-    if (!P.n) return;
-    ReduceSlot slot{B.partials, B.counter};
-    k_cg_matvec<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B, slot, h, use_handle ? 1 : 0);
+    if (P.np) k_cg_matvec<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B, h, use_handle ? 1 : 0);
 }
 template <class T>
 void launch_cg_update(const DevParams<T> &P, const DevBufs<T> &B, cudaGraphConditionalHandle h, bool use_handle,
                       cudaStream_t s)
 {
-    if (!P.n) return;
-    ReduceSlot slot{B.partials, B.counter};
-    k_cg_update<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B, slot, h, use_handle ? 1 : 0);
+    if (P.np) k_cg_update<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B, h, use_handle ? 1 : 0);
 }
 template <class T> void launch_cg_p(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {
-    if (P.n) k_cg_p<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
+    if (P.np) k_cg_p<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
 }
 template <class T> void launch_kick(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {
-    k_kick<T><<<grid_for(P.n > 0 ? P.n : 1), kBlock, 0, s>>>(P, B);
+    k_kick<T><<<grid_for(P.np > 0 ? P.np : 1), kBlock, 0, s>>>(P, B);
 }
 template <class T> void launch_press_init(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {
-    if (P.n) k_press_init<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
+    if (P.np) k_press_init<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
 }
 template <class T> void launch_integrate(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {
-    k_integrate<T><<<grid_for(P.n > 0 ? P.n : 1), kBlock, 0, s>>>(P, B);
+    k_integrate<T><<<grid_for(P.np > 0 ? P.np : 1), kBlock, 0, s>>>(P, B);
 }
 template <class T> void launch_features(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {
-    if (P.n) k_features<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
+    if (P.np) k_features<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
 }
 template <class T> void launch_warmstart_select(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s)
 {
-    if (!P.n) return;
-    ReduceSlot slot{B.partials, B.counter};
+    if (!P.np) return;
+    const unsigned g = grid_for(P.np);
     if (div) {
-        k_ws_kappa<T, true><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
-        k_ws_accel2<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
-        k_ws_residual2<T, true><<<grid_for(P.n), kBlock, 0, s>>>(P, B, slot);
-        k_ws_apply<T, true><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
+        k_ws_kappa<T, true><<<g, kBlock, 0, s>>>(P, B);
+        k_ws_accel2<T><<<g, kBlock, 0, s>>>(P, B);
+        k_ws_residual2<T, true><<<g, kBlock, 0, s>>>(P, B);
+        k_ws_apply<T, true><<<g, kBlock, 0, s>>>(P, B);
     } else {
-        k_ws_kappa<T, false><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
-        k_ws_accel2<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
-        k_ws_residual2<T, false><<<grid_for(P.n), kBlock, 0, s>>>(P, B, slot);
-        k_ws_apply<T, false><<<grid_for(P.n), kBlock, 0, s>>>(P, B);
+        k_ws_kappa<T, false><<<g, kBlock, 0, s>>>(P, B);
+        k_ws_accel2<T><<<g, kBlock, 0, s>>>(P, B);
+        k_ws_residual2<T, false><<<g, kBlock, 0, s>>>(P, B);
+        k_ws_apply<T, false><<<g, kBlock, 0, s>>>(P, B);
     }
 }
-template <class T> void launch_boundary_keys(const DevParams<T> &P, const DevBufs<T> &B, const v4_t<T> *xb_in,
+template <class T> void launch_boundary_keys(const DevParams<T> &P, const v4_t<T> *xb_in, const uint32_t *bscene_in,
                                              uint32_t *keys, uint32_t *vals, cudaStream_t s)
 {
-    if (P.nb) k_boundary_keys<T><<<grid_for(P.nb), kBlock, 0, s>>>(P, xb_in, keys, vals, P.nb);
+    if (P.nb) k_boundary_keys<T><<<grid_for(P.nb), kBlock, 0, s>>>(P, xb_in, bscene_in, keys, vals);
 }
 template <class T> void launch_boundary_gather(const DevParams<T> &P, const DevBufs<T> &B, const v4_t<T> *xb_in,
-                                               const uint32_t *perm, const uint32_t *cells, cudaStream_t s)
+                                               const uint32_t *bscene_in, const uint32_t *perm, uint32_t *cells,
+                                               cudaStream_t s)
 {
     if (!P.nb) return;
-    k_boundary_gather<T><<<grid_for(P.nb), kBlock, 0, s>>>(P, B, xb_in, perm, const_cast<uint32_t *>(cells));
-    k_cell_ranges<T><<<grid_for(P.nb), kBlock, 0, s>>>(P, cells, B.bcstart, B.bcend, P.nb, nullptr);
+    k_boundary_gather<T><<<grid_for(P.nb), kBlock, 0, s>>>(P, B, xb_in, bscene_in, perm, cells);
+    k_cell_ranges_flat<<<grid_for(P.nb), kBlock, 0, s>>>(cells, B.bcstart, B.bcend, P.nb);
 }
 template <class T> void launch_boundary_volume(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {
@@ -1477,32 +1639,28 @@ template <class T> void launch_boundary_volume(const DevParams<T> &P, const DevB
 template <class T> void launch_scatter_field(const DevParams<T> &P, const DevBufs<T> &B, int field, void *out,
                                              int odt, cudaStream_t s)
 {
-    const uint32_t m = (field == SPHGB_FIELD_BOUNDARY_VOLUME || field == SPHGB_FIELD_BOUNDARY_POSITION) ? P.nb : P.n;
-    if (m) k_scatter_field<T><<<grid_for(m), kBlock, 0, s>>>(P, B, field, out, odt);
+    if (field == SPHGB_FIELD_BOUNDARY_VOLUME || field == SPHGB_FIELD_BOUNDARY_POSITION) {
+        if (P.nb) k_scatter_boundary<T><<<grid_for(P.nb), kBlock, 0, s>>>(P, B, field, out, odt);
+    } else if (P.np) {
+        k_scatter_field<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B, field, out, odt);
+    }
 }
 template <class T> void launch_upload_field(const DevParams<T> &P, const DevBufs<T> &B, int field, const void *in,
                                             int idt, const uint32_t *inv, cudaStream_t s)
 {
-    if (P.n) k_upload_field<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B, field, in, idt, inv);
+    if (P.nreal) k_upload_field<T><<<grid_for(P.nreal), kBlock, 0, s>>>(P, B, field, in, idt, inv);
 }
 template <class T> void launch_init_state(const DevParams<T> &P, const DevBufs<T> &B, const double *x, const double *v,
                                           const uint32_t *id, cudaStream_t s)
 {
-    if (P.n) k_init_state<T><<<grid_for(P.n), kBlock, 0, s>>>(P, B, x, v, id);
+    if (P.np) k_init_state<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B, x, v, id);
 }
-// Keeps the GPU busy for about `ns` nanoseconds without touching memory, so that
-// the host can enqueue an event, a kernel and an event back to back behind it
-// (per-kernel event timing without host-submission gaps).  Bounded: one sleep.
-__global__ void k_delay(unsigned ns)
+template <class T> void launch_inverse_perm(const DevParams<T> &P, const uint32_t *id, uint32_t *inv, cudaStream_t s)
 {
-    if (threadIdx.x == 0) __nanosleep(ns);
+    if (P.np) k_inverse_perm<T><<<grid_for(P.np), kBlock, 0, s>>>(P, id, inv);
 }
 void launch_delay(cudaStream_t s, unsigned ns) { k_delay<<<1, 32, 0, s>>>(ns); }
 
-void launch_inverse_perm(const uint32_t *id, uint32_t *inv, uint32_t n, cudaStream_t s)
-{
-    if (n) k_inverse_perm<<<grid_for(n), kBlock, 0, s>>>(id, inv, n);
-}
 void launch_lists_to_ids(const uint32_t *list, const uint32_t *cnt, uint32_t cap, const uint32_t *id, const uint32_t *inv,
                          const uint32_t *bid, int kind, const uint32_t *offsets, uint32_t *out, uint32_t n, cudaStream_t s)
 {
@@ -1534,16 +1692,17 @@ void launch_lists_to_ids(const uint32_t *list, const uint32_t *cnt, uint32_t cap
     template void launch_kick<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                           \
     template void launch_press_init<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                     \
     template void launch_integrate<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                      \
-    template void launch_boundary_keys<T>(const DevParams<T> &, const DevBufs<T> &, const v4_t<T> *, uint32_t *,    \
+    template void launch_boundary_keys<T>(const DevParams<T> &, const v4_t<T> *, const uint32_t *, uint32_t *,      \
                                           uint32_t *, cudaStream_t);                                                \
     template void launch_boundary_gather<T>(const DevParams<T> &, const DevBufs<T> &, const v4_t<T> *,              \
-                                            const uint32_t *, const uint32_t *, cudaStream_t);                      \
+                                            const uint32_t *, const uint32_t *, uint32_t *, cudaStream_t);          \
     template void launch_boundary_volume<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                \
     template void launch_scatter_field<T>(const DevParams<T> &, const DevBufs<T> &, int, void *, int, cudaStream_t); \
     template void launch_upload_field<T>(const DevParams<T> &, const DevBufs<T> &, int, const void *, int,          \
                                          const uint32_t *, cudaStream_t);                                           \
     template void launch_init_state<T>(const DevParams<T> &, const DevBufs<T> &, const double *, const double *,    \
-                                       const uint32_t *, cudaStream_t);
+                                       const uint32_t *, cudaStream_t);                                             \
+    template void launch_inverse_perm<T>(const DevParams<T> &, const uint32_t *, uint32_t *, cudaStream_t);
 
 SPHGB_INSTANTIATE(float)
 SPHGB_INSTANTIATE(double)

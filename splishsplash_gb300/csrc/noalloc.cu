@@ -128,13 +128,14 @@ extern "C" int sphgb_boundary_volume_noalloc(const float *xb, uint32_t nb, doubl
     P.K.l = (float)(48.0 / (M_PI * h * h * h));
     P.K.w0 = P.K.k;
     P.K.h2 = (float)(h * h);
-    P.ox = (float)org[0];
-    P.oy = (float)org[1];
-    P.oz = (float)org[2];
-    P.inv_cell = (float)(1.0 / cell);
-    P.dimx = dim[0];
-    P.dimy = dim[1];
-    P.dimz = dim[2];
+    P.nscenes = 1;
+    P.s0.ox = (float)org[0];
+    P.s0.oy = (float)org[1];
+    P.s0.oz = (float)org[2];
+    P.s0.inv_cell = (float)(1.0 / cell);
+    P.s0.dimx = dim[0];
+    P.s0.dimy = dim[1];
+    P.s0.dimz = dim[2];
     P.nb = nb;
     DevBufs<float> B{};
     float4 *xb_in = reinterpret_cast<float4 *>(base + kOffXbIn);
@@ -154,10 +155,10 @@ extern "C" int sphgb_boundary_volume_noalloc(const float *xb, uint32_t nb, doubl
     if (cudaMemsetAsync(B.bcstart, 0xff, ncell * 4, s) != cudaSuccess) return SPHGB_ERR_CUDA;
     const unsigned blocks = (nb + kBlock - 1) / kBlock;
     k_pack<<<blocks, kBlock, 0, s>>>(xb, xb_in, nb);
-    launch_boundary_keys<float>(P, B, xb_in, keys, vals, s);
+    launch_boundary_keys<float>(P, xb_in, nullptr, keys, vals, s);
     const uint32_t tiles = (nb + kSortTile - 1) / kSortTile;
     const bool sw = radix_sort_pairs(keys, vals, keys2, vals2, nb, 3 * bits, hist, tiles, s);
-    launch_boundary_gather<float>(P, B, xb_in, sw ? vals2 : vals, cells, s);
+    launch_boundary_gather<float>(P, B, xb_in, nullptr, sw ? vals2 : vals, cells, s);
     launch_boundary_volume<float>(P, B, s);
     k_unsort_volume<<<blocks, kBlock, 0, s>>>(B.xb, B.bid, volume, nb);
     if (cudaGetLastError() != cudaSuccess) return SPHGB_ERR_CUDA;

@@ -165,15 +165,18 @@ template <int NV> __device__ __forceinline__ DSum<NV> block_sum(DSum<NV> s)
     return r;
 }
 
-// Reduction slots used by the last-block pattern.
+// Reduction slot of one scene for the last-block pattern.  A scene owns the
+// consecutive blocks [first, first + count) of the launch.
 struct ReduceSlot {
-    double *partials;    // gridDim.x * NV
-    unsigned *counter;   // zero before the launch; reset by the last block
+    double *partials;    // NV x gridDim.x, indexed by block
+    unsigned *counter;   // the scene's arrival counter: zero before the launch, reset by its last block
+    unsigned first, count;
 };
 
-// Every block calls this once with its per-thread contributions.  The last block
-// to arrive receives the grid-wide sums (in thread 0 of that block) and calls
-// fin(total) from thread 0.  Returns true in the block that finalized.
+// Every block of the scene calls this once with its per-thread contributions
+// (all threads of the block, no early return before it).  The scene's last block
+// to arrive sums the scene's block partials in block order (deterministic) and
+// calls fin(total) from its thread 0.
 template <int NV, class Fin>
 __device__ __forceinline__ void grid_sum_finalize(DSum<NV> mine, ReduceSlot slot, Fin fin)
 {
@@ -184,7 +187,7 @@ __device__ __forceinline__ void grid_sum_finalize(DSum<NV> mine, ReduceSlot slot
         for (int k = 0; k < NV; k++) slot.partials[(size_t)k * gridDim.x + blockIdx.x] = b.v[k];
         __threadfence();
         const unsigned t = atomicAdd(slot.counter, 1u);
-        amLast = (t == gridDim.x - 1);
+        amLast = (t == slot.count - 1);
     }
     __syncthreads();
     if (!amLast) return;
@@ -192,9 +195,9 @@ __device__ __forceinline__ void grid_sum_finalize(DSum<NV> mine, ReduceSlot slot
     DSum<NV> acc;
 #pragma unroll
     for (int k = 0; k < NV; k++) acc.v[k] = 0.0;
-    for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x) {
+    for (unsigned i = threadIdx.x; i < slot.count; i += blockDim.x) {
 #pragma unroll
-        for (int k = 0; k < NV; k++) acc.v[k] += __ldcg(&slot.partials[(size_t)k * gridDim.x + i]);
+        for (int k = 0; k < NV; k++) acc.v[k] += __ldcg(&slot.partials[(size_t)k * gridDim.x + slot.first + i]);
     }
     DSum<NV> tot = block_sum<NV>(acc);
     if (threadIdx.x == 0) {

@@ -1,5 +1,12 @@
 // Internal structures shared by the host orchestration (api.cu) and the kernel
 // translation units.  Not part of the public ABI (include/sphgb300.h).
+//
+// A context advances one or more independent scenes together.  Scene s owns the
+// fluid slots [pstart_s, pstart_s + n_s) with pstart_s a multiple of the block
+// size, so a thread block never spans two scenes; it owns the cells
+// [cell_off_s, cell_off_s + ncell_s) of the shared cell tables and one
+// StepScalars record (its own dt, CFL, iteration counters and convergence flags).
+// Every kernel of a step covers all scenes in one launch.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -11,7 +18,8 @@ namespace sphgb {
 
 // Scalars that live in device memory so that a captured step can be replayed
 // without host updates.  All solver control (iteration counters, convergence
-// flags, the CFL step size) is decided on the device.
+// flags, the CFL step size) is decided on the device.  One record per scene and
+// one global record (launch counter, loop guard, OR of the scenes' loop flags).
 struct StepScalars {
     double dt;          // step size of the current step (used by kick / position update)
     double dt_next;     // CFL result, used by the pressure solve and the next step
@@ -22,26 +30,37 @@ struct StepScalars {
     double cg_rhs2, cg_thresh, cg_res2, cg_absnew, cg_alpha, cg_beta, cg_err;
     double ws_rc[2], ws_rl[2];   // initial residuals of the classic / learned warm start (div, pressure)
     unsigned iters, iters_v, iters_cg;
-    unsigned cont;      // 1 while the running solver loop continues
+    unsigned cont;      // 1 while the running solver loop continues (global record: any scene)
     unsigned cg_state;  // 0 running, 1 converged / no iteration, 2 zero right-hand side
     unsigned maxvel_bits;
-    unsigned flags;     // bit 0 list overflow, bit 1 non-finite velocity
+    unsigned flags;     // bit 0 list overflow, bit 1 non-finite velocity, bit 2 loop guard
     unsigned max_nf, max_nb;
     unsigned prev_iters;
-    unsigned loop_guard;   // body executions of the running device-side loop
-    unsigned launches;     // kernels launched in the current step (counted on the device)
+    unsigned loop_guard;   // body executions of the running device-side loop (global record)
+    unsigned launches;     // kernels launched in the current step (global record)
     unsigned ws_used;      // bit 0: learned warm start used by the divergence solve, bit 1: pressure solve
     unsigned pad[2];
 };
 
 constexpr unsigned kFlagOverflow = 1u;
 constexpr unsigned kFlagNonFinite = 2u;
+constexpr unsigned kFlagLoopGuard = 4u;   // a device loop ran past its iteration bound and was stopped
+
 __device__ __forceinline__ void count_launch(unsigned *ctr)
 {
     if (ctr && blockIdx.x == 0 && threadIdx.x == 0) *ctr += 1u;
 }
 
-constexpr unsigned kFlagLoopGuard = 4u;   // a device loop ran past its iteration bound and was stopped
+// Per-scene layout and cell grid.
+template <class T> struct SceneDev {
+    T ox, oy, oz, inv_cell;      // grid origin, 1 / cell size
+    int dimx, dimy, dimz;
+    uint32_t cell_off;           // first cell of the scene in the shared cell tables
+    uint32_t pstart;             // first fluid slot (multiple of kBlock)
+    uint32_t n;                  // fluid particles
+    uint32_t ustart;             // first particle of the scene in upload (particle id) order
+    uint32_t key_prefix;         // scene index << Morton bits
+};
 
 template <class T> struct DevParams {
     Kernel<T> K;
@@ -56,11 +75,23 @@ template <class T> struct DevParams {
     int cfl_method, visc_on, div_on;
     int learned, feat_on;         // learned warm start on; features computed
     float ws_scale_v, ws_scale_p; // network output scales
-    // grid
-    T ox, oy, oz, inv_cell;
-    int dimx, dimy, dimz;
-    uint32_t n, nb, capf, capb;
+    // scenes
+    uint32_t nscenes;
+    SceneDev<T> s0;               // the scene when nscenes == 1 (no device lookup)
+    const SceneDev<T> *scenes;    // device array [nscenes] when nscenes > 1
+    const uint4 *blk;             // device array [blocks] when nscenes > 1: (scene, first slot, end slot, -)
+    uint32_t np;                  // fluid slots (sum of padded scene ranges): launch size
+    uint32_t nreal;               // fluid particles of all scenes
+    uint32_t nb;                  // boundary particles of all scenes
+    uint32_t capf, capb;
 };
+
+// Scene descriptor by value: a kernel parameter for a single scene, a (cached) global load otherwise.
+template <class T> __device__ __forceinline__ SceneDev<T> scene_get(const DevParams<T> &P, uint32_t s)
+{
+    if (P.nscenes > 1) return P.scenes[s];
+    return P.s0;
+}
 
 template <class T> struct DevBufs {
     using v4 = v4_t<T>;
@@ -87,6 +118,8 @@ template <class T> struct DevBufs {
     uint32_t *bcstart, *bcend;
     v4 *xb;                      // sorted boundary positions, w = volume
     T *bscratch;                 // nb scratch values (boundary volume set-up)
+    uint32_t *bid;               // upload index of each sorted boundary particle
+    uint32_t *bscene;            // scene of each sorted boundary particle
     // learned warm start
     float *feat;                 // raw features, 8 floats per particle (5 used)
     float *mlp_x;                // network inputs, 10 floats per particle
@@ -95,17 +128,16 @@ template <class T> struct DevBufs {
     v4 *pa2;                     // pressure acceleration of the predicted warm start
     const void *mlp_w;           // BF16 weights
     const float *mlp_p;          // FP32 parameters (biases)
-    uint32_t *bid;               // upload index of each sorted boundary particle
     // CG
     v4 *cg_x, *cg_r, *cg_p, *cg_z, *cg_t;
     v4 *inv0, *inv1;             // symmetric 3x3 inverse blocks: (m00,m01,m02,m11), (m12,m22,-,-)
     // reductions
-    double *partials;
-    unsigned *counter;
-    StepScalars *sc;
+    double *partials;            // [4][blocks]
+    unsigned *counters;          // [nscenes + 1]: per-scene last-block counters, then the global one
+    StepScalars *sc;             // [nscenes]
+    StepScalars *gsc;            // global record
     // radix sort scratch
     uint32_t *hist;
-    uint32_t num_tiles;
 };
 
 // ---- launchers (defined in kernels.cu / sort.cu, instantiated for float and double)
@@ -135,21 +167,23 @@ template <class T> void launch_boundary_volume(const DevParams<T> &P, const DevB
 template <class T> void launch_features(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
 template <class T> void launch_warmstart_select(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s);
 void mlp_infer_device(const float *X, uint32_t n, const void *w, const float *p, float *Y, cudaStream_t s);
-template <class T> void launch_boundary_keys(const DevParams<T> &P, const DevBufs<T> &B, const v4_t<T> *xb_in,
+// boundary set-up: keys (scene prefix | Morton code) of the boundary particles in upload order
+template <class T> void launch_boundary_keys(const DevParams<T> &P, const v4_t<T> *xb_in, const uint32_t *bscene_in,
                                              uint32_t *keys, uint32_t *vals, cudaStream_t s);
 template <class T> void launch_boundary_gather(const DevParams<T> &P, const DevBufs<T> &B, const v4_t<T> *xb_in,
-                                               const uint32_t *perm, const uint32_t *cells, cudaStream_t s);
+                                               const uint32_t *bscene_in, const uint32_t *perm, uint32_t *cells,
+                                               cudaStream_t s);
 template <class T> void launch_scatter_field(const DevParams<T> &P, const DevBufs<T> &B, int field, void *out,
                                              int out_dtype, cudaStream_t s);
 template <class T> void launch_upload_field(const DevParams<T> &P, const DevBufs<T> &B, int field, const void *in,
                                             int in_dtype, const uint32_t *inv, cudaStream_t s);
 template <class T> void launch_init_state(const DevParams<T> &P, const DevBufs<T> &B, const double *x,
                                           const double *v, const uint32_t *id, cudaStream_t s);
-void launch_inverse_perm(const uint32_t *id, uint32_t *inv, uint32_t n, cudaStream_t s);
-void launch_delay(cudaStream_t s, unsigned ns);
+template <class T> void launch_inverse_perm(const DevParams<T> &P, const uint32_t *id, uint32_t *inv, cudaStream_t s);
 void launch_lists_to_ids(const uint32_t *list, const uint32_t *cnt, uint32_t cap, const uint32_t *id,
                          const uint32_t *inv, const uint32_t *bid, int kind, const uint32_t *offsets,
                          uint32_t *out, uint32_t n, cudaStream_t s);
+void launch_delay(cudaStream_t s, unsigned ns);
 
 // radix sort of (key, value) pairs, LSD, 8-bit digits, stable.  keys/vals are
 // ping-ponged with keys2/vals2; returns true if the result ended in keys2/vals2.

@@ -140,3 +140,53 @@ class TimeStepDFSPH:
 
     def close(self):
         self.ctx.close()
+
+
+class BatchedTimeStepDFSPH:
+    """Many independent scenes advanced together by one context: every kernel launch of a
+    step covers all scenes, each scene keeps its own CFL step size and solver decisions, and
+    with use_graph a step of the whole batch is one graph launch.  The scenes share the
+    parameter block (that of the first scene).  No reference counterpart: the reference runs
+    one scene per process (Simulation.cpp:112-119)."""
+
+    def __init__(self, scene_list, precision: str = "fp32", use_graph: bool = True, device: int = 0,
+                 max_fluid_neighbors: int = 0, max_boundary_neighbors: int = 0):
+        if not scene_list:
+            raise ValueError("empty batch")
+        self.params: SPHParams = dataclasses.replace(scene_list[0].params)
+        self.ctx = native.Context(precision=precision, device=device, use_graph=use_graph,
+                                  max_fluid_neighbors=max_fluid_neighbors,
+                                  max_boundary_neighbors=max_boundary_neighbors)
+        self.ctx.set_params(self.params)
+        self.ctx.upload_scenes([s.x for s in scene_list], [s.v for s in scene_list], [s.xb for s in scene_list])
+        self.ctx.set_time_step(self.params.timeStepSize)
+        self.sizes = np.array([s.n for s in scene_list], np.int64)
+        self.offsets = np.concatenate([[0], np.cumsum(self.sizes)])
+        self.last = None
+
+    @property
+    def num_scenes(self) -> int:
+        return int(self.sizes.size)
+
+    def step(self):
+        """One step of every scene; returns the batch statistics (maxima over the scenes)."""
+        self.last = self.ctx.step(wait=True)
+        return self.last
+
+    def step_async(self):
+        self.ctx.step(wait=False)
+
+    def sync(self):
+        self.last = self.ctx.sync()
+        return self.last
+
+    def scene_stats(self):
+        return self.ctx.scene_stats()
+
+    def getFieldBuffer(self, name: str, dtype=np.float64):
+        """A field of all scenes, split per scene (list of arrays in each scene's particle order)."""
+        a = self.ctx.download(name, dtype)
+        return [a[self.offsets[k]:self.offsets[k + 1]] for k in range(self.num_scenes)]
+
+    def close(self):
+        self.ctx.close()

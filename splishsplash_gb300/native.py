@@ -118,7 +118,8 @@ EXPORTS = [
     "sphgb_upload_fluid", "sphgb_upload_fluid_f32", "sphgb_set_time_step", "sphgb_get_time_step",
     "sphgb_set_time", "sphgb_step", "sphgb_sync", "sphgb_download", "sphgb_upload_field", "sphgb_neighbors",
     "sphgb_num_particles", "sphgb_get_stream", "sphgb_profile_enable", "sphgb_profile_reset", "sphgb_profile_read",
-    "sphgb_set_warmstart_mlp", "sphgb_set_feature_output",
+    "sphgb_set_warmstart_mlp", "sphgb_set_feature_output", "sphgb_upload_scenes", "sphgb_num_scenes",
+    "sphgb_scene_stats",
 ]
 
 _lib = None
@@ -163,6 +164,9 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.sphgb_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
     L.sphgb_set_warmstart_mlp.argtypes = [vp, vp]
     L.sphgb_set_feature_output.argtypes = [vp, i32]
+    L.sphgb_upload_scenes.argtypes = [vp, u32, vp, vp, vp, vp, vp]
+    L.sphgb_num_scenes.argtypes = [vp, ctypes.POINTER(u32)]
+    L.sphgb_scene_stats.argtypes = [vp, u32, u32, ctypes.POINTER(Stats)]
     L.sphgb_profile_enable.argtypes = [vp, i32]
     L.sphgb_profile_reset.argtypes = [vp]
     L.sphgb_profile_read.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_uint64),
@@ -344,6 +348,31 @@ class Context:
         v = np.ascontiguousarray(v, dtype=np.float64)
         idp = None if ids is None else np.ascontiguousarray(ids, dtype=np.uint32)
         self._check(self.L.sphgb_upload_fluid(self.h, _p(x), _p(v), _p(idp), x.shape[0]))
+
+    def upload_scenes(self, xs, vs, xbs):
+        """A batch of independent scenes: per scene fluid positions / velocities (n_s x 3) and
+        boundary positions (nb_s x 3).  Fields download in the concatenated scene order."""
+        n = np.array([len(x) for x in xs], np.uint32)
+        nb = np.array([len(b) for b in xbs], np.uint32)
+        x = np.ascontiguousarray(np.concatenate(xs), np.float64)
+        v = np.ascontiguousarray(np.concatenate(vs), np.float64)
+        xb = np.ascontiguousarray(np.concatenate([np.reshape(b, (-1, 3)) for b in xbs]), np.float64)
+        self._check(self.L.sphgb_upload_scenes(self.h, len(xs), _p(n), _p(nb), _p(x), _p(v),
+                                               _p(xb) if xb.size else None))
+        self.scene_sizes = n
+
+    def num_scenes(self):
+        k = ctypes.c_uint32()
+        self._check(self.L.sphgb_num_scenes(self.h, ctypes.byref(k)))
+        return k.value
+
+    def scene_stats(self, first: int = 0, count: int = None):
+        """Per-scene statistics of the last step (list of dicts)."""
+        if count is None:
+            count = self.num_scenes() - first
+        arr = (Stats * max(count, 1))()
+        self._check(self.L.sphgb_scene_stats(self.h, first, count, arr))
+        return [arr[k].as_dict() for k in range(count)]
 
     def set_time_step(self, dt):
         self._check(self.L.sphgb_set_time_step(self.h, float(dt)))
