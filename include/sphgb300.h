@@ -102,8 +102,9 @@ typedef struct sphgb_stats {
     uint32_t learned_used;           /* bit 0 / bit 1: predicted warm start used by the divergence /
                                         pressure solve this step */
     uint32_t reserved;
-    double ws_residual_classic[2];   /* initial average error with the classic warm start (div, pressure) */
-    double ws_residual_learned[2];   /* ... with the predicted warm start (0 when the network is off) */
+    double ws_residual_classic[2];   /* average error of the classic warm start after the gate iterations
+                                        (div, pressure; with a gate of 1: the initial residual) */
+    double ws_residual_learned[2];   /* ... of the predicted warm start (0 when the network is off) */
 } sphgb_stats;
 
 /* field ids for sphgb_download / sphgb_upload_field; names are the reference's field names */
@@ -193,10 +194,16 @@ int sphgb_scene_stats(sphgb_ctx *ctx, uint32_t first, uint32_t count, sphgb_stat
 
 /* ---- learned warm start (no counterpart in the reference: new in this library) ----
  * A per-particle network 10 -> 64 -> 64 -> 2 (GELU), BF16 weights and activations on the
- * tensor cores with FP32 accumulation, predicting the stored warm starts kappa_v*dt and
- * kappa*dt^2 (divergence and pressure solve) from 5 per-particle features and their
- * cubic-spline-weighted neighbour means (sphgb_download SPHGB_FIELD_FEATURES).  Trained with
- * Adam by hand-written kernels.  Host arrays: X n x 10, targets/mask n x 2, row-major float. */
+ * tensor cores with FP32 accumulation.  Its two outputs (times the output scales) are the
+ * multipliers that the divergence and the pressure warm start apply to the previous step's
+ * stored kappa_v and kappa, in place of the classic factor 0.5 (TimeStepDFSPH.cpp:449-453,
+ * :293-296; classic clamps and masks kept, multiplier limited to [0, 4]).  Inputs: 5
+ * dimensionless per-particle features (density deviation, velocity divergence x dt, neighbour
+ * count, previous kappa relative to its neighbourhood, |v| dt / 2r) and the cubic-spline-
+ * weighted neighbour means of the features (sphgb_download SPHGB_FIELD_FEATURES).  Trained
+ * with Adam by hand-written kernels; the loss is the mean over samples of
+ * sum_o mask_o (y_o - t_o)^2 (mask = per-output weight).  Host arrays: X n x 10,
+ * targets/mask n x 2, row-major float. */
 typedef struct sphgb_mlp sphgb_mlp;
 int sphgb_mlp_create(int device, uint32_t seed, sphgb_mlp **out);
 int sphgb_mlp_destroy(sphgb_mlp *m);
@@ -204,7 +211,7 @@ const char *sphgb_mlp_last_error(const sphgb_mlp *m);
 int sphgb_mlp_num_params(void);
 int sphgb_mlp_get_params(sphgb_mlp *m, float *out);
 int sphgb_mlp_set_params(sphgb_mlp *m, const float *in);
-/* network output o_k x scale_k = stored warm start (kappa_v*dt, kappa*dt^2) */
+/* network output o_k x scale_k = warm-start multiplier (k = 0 divergence, 1 pressure); default 1 */
 int sphgb_mlp_set_output_scale(sphgb_mlp *m, float scale_v, float scale_p);
 int sphgb_mlp_get_output_scale(const sphgb_mlp *m, float *scale_v, float *scale_p);
 int sphgb_mlp_forward(sphgb_mlp *m, const float *X, uint32_t n, float *Y);
@@ -213,9 +220,19 @@ int sphgb_mlp_loss_grad(sphgb_mlp *m, const float *X, const float *Y, const floa
 int sphgb_mlp_train(sphgb_mlp *m, const float *X, const float *Y, const float *mask, uint32_t n, uint32_t epochs,
                     uint32_t batch, float lr, uint32_t seed, float *epoch_loss);
 /* Use the network for both warm starts of this context (NULL: classic warm start only).  The
- * solvers still iterate to their tolerances; per step and solver the predicted warm start is
- * used only if its initial residual is lower than the classic one (sphgb_stats.learned_used). */
+ * solvers still iterate to their tolerances; per step, scene and solver the first Jacobi
+ * iterations (sphgb_set_warmstart_gate) run for both candidates and the predicted warm start
+ * is kept only if its error after them is lower than the classic one's (sphgb_stats
+ * learned_used; ws_residual_* hold both errors). */
 int sphgb_set_warmstart_mlp(sphgb_ctx *ctx, const sphgb_mlp *m);
+/* The gate of the learned warm start, per solver: both candidates (classic and predicted) run
+ * this many Jacobi iterations, then the one with the lower average error continues (the
+ * loser's iterations are not booked; a solver that converges during the gate still books the
+ * gate's iterations).  1 compares the candidates' initial residuals.  0 (default): 1 for the
+ * divergence solve and max(minIterations, 4) for the pressure solve, because a warm start's
+ * particle-scale error dominates the first residuals but decays within a few sweeps, while
+ * the low-frequency error that decides the iteration count does not. */
+int sphgb_set_warmstart_gate(sphgb_ctx *ctx, uint32_t div_sweeps, uint32_t pressure_sweeps);
 /* compute the network inputs every step even without a network (training-data collection);
  * they are read back with SPHGB_FIELD_FEATURES */
 int sphgb_set_feature_output(sphgb_ctx *ctx, int on);

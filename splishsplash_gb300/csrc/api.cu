@@ -97,6 +97,7 @@ struct sphgb_ctx {
     float *mlp_p = nullptr;
     void *mlp_w = nullptr;
     float ws_scale[2] = {kMlpDefaultScaleV, kMlpDefaultScaleP};
+    uint32_t ws_gate[2] = {0, 0};      // Jacobi sweeps before the candidates are compared (div, pressure; 0: default)
     float *feat = nullptr, *mlp_x = nullptr, *mlp_y = nullptr;
     void *kl = nullptr, *pa2 = nullptr;
     // per-kernel CUDA-event timing (host-loop mode only)
@@ -513,6 +514,20 @@ template <class T> int prepare(sphgb_ctx *c)
     return SPHGB_OK;
 }
 
+// Gate of the learned warm start: both candidates run this many Jacobi iterations of the
+// solver before they are compared.  Default: 1 for the divergence solve (the candidates'
+// initial residuals) and max(minIterations, 4) for the pressure solve: the first sweeps damp
+// the particle-scale error of a warm start, after four the errors compared reflect the
+// low-frequency error that decides the iteration count.  Never more than the solver's maximum.
+constexpr unsigned kDefaultPressureGate = 4;
+unsigned gate_sweeps(const sphgb_ctx *c, bool div)
+{
+    const unsigned max_iter = div ? c->prm.max_iterations_v : c->prm.max_iterations;
+    const uint32_t set = c->ws_gate[div ? 0 : 1];
+    const unsigned g = set ? set : (div ? 1u : std::max(kDefaultPressureGate, c->prm.min_iterations));
+    return std::min(g, max_iter);
+}
+
 template <class T> void enqueue_solver_loop_body(sphgb_ctx *c, const DevParams<T> &P, const DevBufs<T> &B, bool div,
                                                  cudaGraphConditionalHandle h, bool use_handle, cudaStream_t s)
 {
@@ -569,18 +584,31 @@ template <class T> int step_host_loop(sphgb_ctx *c)
     int rc;
     unsigned cont = 0;
     enqueue_prologue<T>(c, P, B0, B1, s);
-    if (P.div_on) {
-        if (P.learned) { PROF(K_WS_SELECT, s); launch_warmstart_select<T>(P, B1, true, s); }
-        { PROF(K_LOOP_BEGIN, s); launch_loop_begin<T>(P, B1, true, s); }
-        if (P.max_iter_v > 0) {
-            unsigned guard = 0;
+    // one solver loop: with the network, the warm-start selection is iteration 1
+    auto solve = [&](bool div) -> int {
+        const unsigned max_iter = div ? P.max_iter_v : P.max_iter;
+        { PROF(K_LOOP_BEGIN, s); launch_loop_begin<T>(P, B1, div, s); }
+        unsigned guard = 0, cont = 0;
+        int r;
+        if (max_iter > 0 && P.learned) {
+            const unsigned g = gate_sweeps(c, div);
+            guard = g - 1;
+            { PROF(K_WS_SELECT, s); launch_warmstart_select<T>(P, B1, div, g, 0, false, s); }
+            if ((r = read_cont(c, &cont))) return r;
+            while (cont && ++guard <= max_iter) {
+                enqueue_solver_loop_body<T>(c, P, B1, div, 0, false, s);
+                if ((r = read_cont(c, &cont))) return r;
+            }
+        } else if (max_iter > 0) {
             do {
-                enqueue_solver_loop_body<T>(c, P, B1, true, 0, false, s);
-                if ((rc = read_cont(c, &cont))) return rc;
-            } while (cont && ++guard <= P.max_iter_v);
+                enqueue_solver_loop_body<T>(c, P, B1, div, 0, false, s);
+                if ((r = read_cont(c, &cont))) return r;
+            } while (cont && ++guard <= max_iter);
         }
-        { PROF(K_SOLVER_FINALIZE, s); launch_solver_finalize<T>(P, B1, true, s); }
-    }
+        { PROF(K_SOLVER_FINALIZE, s); launch_solver_finalize<T>(P, B1, div, s); }
+        return SPHGB_OK;
+    };
+    if (P.div_on && (rc = solve(true))) return rc;
     { PROF(K_XSPH, s); launch_xsph<T>(P, B1, s); }
     if (P.visc_on) {
         { PROF(K_VISC_SETUP, s); launch_visc_setup<T>(P, B1, 0, false, s); }
@@ -596,16 +624,7 @@ template <class T> int step_host_loop(sphgb_ctx *c)
     }
     { PROF(K_KICK, s); launch_kick<T>(P, B1, s); }
     { PROF(K_PRESS_INIT, s); launch_press_init<T>(P, B1, s); }
-    if (P.learned) { PROF(K_WS_SELECT, s); launch_warmstart_select<T>(P, B1, false, s); }
-    { PROF(K_LOOP_BEGIN, s); launch_loop_begin<T>(P, B1, false, s); }
-    if (P.max_iter > 0) {
-        unsigned guard = 0;
-        do {
-            enqueue_solver_loop_body<T>(c, P, B1, false, 0, false, s);
-            if ((rc = read_cont(c, &cont))) return rc;
-        } while (cont && ++guard <= P.max_iter);
-    }
-    { PROF(K_SOLVER_FINALIZE, s); launch_solver_finalize<T>(P, B1, false, s); }
+    if ((rc = solve(false))) return rc;
     { PROF(K_INTEGRATE, s); launch_integrate<T>(P, B1, s); }
     CK(cudaGetLastError());
     prof_resolve(c);
@@ -613,11 +632,9 @@ template <class T> int step_host_loop(sphgb_ctx *c)
 }
 
 // --- graph capture with conditional WHILE nodes ----------------------------
-// Adds a WHILE node after the current capture tail of c->stream and captures
-// body(stream) into it on the body stream.  default_value is the condition
-// value on entry (the kernels before the loop may also set it).
-template <class F>
-cudaError_t add_while(sphgb_ctx *c, cudaGraphConditionalHandle *handle_out, unsigned default_value, F body)
+// A loop-condition handle of the graph being captured on c->stream, reset to
+// default_value at every launch of the graph (kernels before the loop may set it).
+cudaError_t make_handle(sphgb_ctx *c, cudaGraphConditionalHandle *h, unsigned default_value)
 {
     cudaStreamCaptureStatus st;
     cudaGraph_t g;
@@ -625,8 +642,18 @@ cudaError_t add_while(sphgb_ctx *c, cudaGraphConditionalHandle *handle_out, unsi
     size_t ndeps = 0;
     cudaError_t e = cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &g, &deps, nullptr, &ndeps);
     if (e != cudaSuccess) return e;
-    cudaGraphConditionalHandle h;
-    e = cudaGraphConditionalHandleCreate(&h, g, default_value, cudaGraphCondAssignDefault);
+    return cudaGraphConditionalHandleCreate(h, g, default_value, cudaGraphCondAssignDefault);
+}
+
+// Adds a WHILE node on handle h after the current capture tail of c->stream and
+// captures body(stream, h) into it on the body stream.
+template <class F> cudaError_t add_while_node(sphgb_ctx *c, cudaGraphConditionalHandle h, F body)
+{
+    cudaStreamCaptureStatus st;
+    cudaGraph_t g;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t ndeps = 0;
+    cudaError_t e = cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &g, &deps, nullptr, &ndeps);
     if (e != cudaSuccess) return e;
     cudaGraphNodeParams np{};
     np.type = cudaGraphNodeTypeConditional;
@@ -642,14 +669,12 @@ cudaError_t add_while(sphgb_ctx *c, cudaGraphConditionalHandle *handle_out, unsi
     e = cudaStreamBeginCaptureToGraph(c->body_stream, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
     if (e != cudaSuccess) return e;
     body(c->body_stream, h);
-    e = cudaStreamEndCapture(c->body_stream, &bodyg);
-    *handle_out = h;
-    return e;
+    return cudaStreamEndCapture(c->body_stream, &bodyg);
 }
 
-// The viscosity set-up kernel must set the CG loop's condition, so the graph is
-// built in one capture where the handle exists before the set-up launch.  This
-// helper does the whole capture (prologue, loops, epilogue) for one parity.
+// The whole step (prologue, loops, epilogue) captured for one parity.  Kernels
+// that decide a loop's first condition (the viscosity set-up, the learned
+// warm-start selection) are captured after the loop's handle exists.
 template <class T> int build_graph(sphgb_ctx *c, int parity, cudaGraphExec_t *out)
 {
     const int saved = c->parity;
@@ -667,61 +692,38 @@ template <class T> int build_graph(sphgb_ctx *c, int parity, cudaGraphExec_t *ou
     cudaError_t e = cudaStreamBeginCaptureToGraph(s, graph, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
     if (e != cudaSuccess) { cudaGraphDestroy(graph); return fail(c, SPHGB_ERR_CUDA, cudaGetErrorString(e)); }
     enqueue_prologue<T>(c, P, B0, B1, s);
-    cudaGraphConditionalHandle h = 0;
-    if (P.div_on) {
-        if (P.learned) launch_warmstart_select<T>(P, B1, true, s);
-        launch_loop_begin<T>(P, B1, true, s);
+    // one solver loop; with the network the warm-start selection (iteration 1) sets the condition
+    auto solve = [&](bool div) {
+        const unsigned max_iter = div ? P.max_iter_v : P.max_iter;
+        launch_loop_begin<T>(P, B1, div, s);
+        cudaGraphConditionalHandle h = 0;
+        const bool sel = max_iter > 0 && P.learned;
+        if (e == cudaSuccess) e = make_handle(c, &h, (!sel && max_iter > 0) ? 1u : 0u);
+        if (e == cudaSuccess && sel) launch_warmstart_select<T>(P, B1, div, gate_sweeps(c, div), h, true, s);
         if (e == cudaSuccess)
-            e = add_while(c, &h, P.max_iter_v > 0 ? 1u : 0u, [&](cudaStream_t bs, cudaGraphConditionalHandle hh) {
-                enqueue_solver_loop_body<T>(c, P, B1, true, hh, true, bs);
+            e = add_while_node(c, h, [&](cudaStream_t bs, cudaGraphConditionalHandle hh) {
+                enqueue_solver_loop_body<T>(c, P, B1, div, hh, true, bs);
             });
-        launch_solver_finalize<T>(P, B1, true, s);
-    }
+        launch_solver_finalize<T>(P, B1, div, s);
+    };
+    if (P.div_on) solve(true);
     launch_xsph<T>(P, B1, s);
     if (P.visc_on && e == cudaSuccess) {
-        // create the CG handle first so that the set-up kernel can set it
-        cudaStreamCaptureStatus st;
-        cudaGraph_t g;
-        const cudaGraphNode_t *deps = nullptr;
-        size_t ndeps = 0;
-        e = cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &ndeps);
+        // the set-up kernel sets the CG loop's condition
         cudaGraphConditionalHandle hcg = 0;
-        if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hcg, g, 0u, 0);
+        e = make_handle(c, &hcg, 0u);
         if (e == cudaSuccess) {
             launch_visc_setup<T>(P, B1, hcg, true, s);
-            e = cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &ndeps);
-        }
-        if (e == cudaSuccess) {
-            cudaGraphNodeParams np{};
-            np.type = cudaGraphNodeTypeConditional;
-            np.conditional.handle = hcg;
-            np.conditional.type = cudaGraphCondTypeWhile;
-            np.conditional.size = 1;
-            cudaGraphNode_t node;
-            e = cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &np);
-            if (e == cudaSuccess)
-                e = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
-            if (e == cudaSuccess) {
-                cudaGraph_t bodyg = np.conditional.phGraph_out[0];
-                e = cudaStreamBeginCaptureToGraph(c->body_stream, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
-                if (e == cudaSuccess) {
-                    launch_cg_matvec<T>(P, B1, c->body_stream, hcg, true);
-                    launch_cg_update<T>(P, B1, hcg, true, c->body_stream);
-                    launch_cg_p<T>(P, B1, c->body_stream);
-                    e = cudaStreamEndCapture(c->body_stream, &bodyg);
-                }
-            }
+            e = add_while_node(c, hcg, [&](cudaStream_t bs, cudaGraphConditionalHandle hh) {
+                launch_cg_matvec<T>(P, B1, bs, hh, true);
+                launch_cg_update<T>(P, B1, hh, true, bs);
+                launch_cg_p<T>(P, B1, bs);
+            });
         }
     }
     launch_kick<T>(P, B1, s);
     launch_press_init<T>(P, B1, s);
-    if (P.learned) launch_warmstart_select<T>(P, B1, false, s);
-    launch_loop_begin<T>(P, B1, false, s);
-    if (e == cudaSuccess)
-        e = add_while(c, &h, P.max_iter > 0 ? 1u : 0u, [&](cudaStream_t bs, cudaGraphConditionalHandle hh) {
-            enqueue_solver_loop_body<T>(c, P, B1, false, hh, true, bs);
-        });
-    launch_solver_finalize<T>(P, B1, false, s);
+    solve(false);
     launch_integrate<T>(P, B1, s);
     cudaGraph_t done = nullptr;
     cudaError_t e2 = cudaStreamEndCapture(s, &done);
@@ -1339,6 +1341,15 @@ int sphgb_set_warmstart_mlp(sphgb_ctx *c, const sphgb_mlp *m)
     c->ws_scale[0] = scale[0];
     c->ws_scale[1] = scale[1];
     c->learned = true;
+    return SPHGB_OK;
+}
+
+int sphgb_set_warmstart_gate(sphgb_ctx *c, uint32_t div_sweeps, uint32_t pressure_sweeps)
+{
+    if (!c) return SPHGB_ERR_ARGUMENT;
+    c->ws_gate[0] = div_sweeps;
+    c->ws_gate[1] = pressure_sweeps;
+    invalidate_graphs(c);
     return SPHGB_OK;
 }
 

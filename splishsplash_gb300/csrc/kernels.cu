@@ -423,14 +423,16 @@ __device__ __forceinline__ void build_one(const DevParams<T> &P, const DevBufs<T
     // later pass uses them instead of re-walking the boundary list
     stv(B.bg, i, pack(gb, wb));
     if (P.feat_on) {
-        // raw warm-start features, scaled to O(1): density deviation, velocity divergence x dt,
-        // neighbour count, previous (stored) kappa, displacement per step in diameters
+        // raw warm-start features, dimensionless and O(1): density deviation, velocity divergence
+        // x dt, neighbour count, whether the particle carried pressure in the last step (the
+        // previous kappa itself enters relative to its neighbourhood, in k_features),
+        // displacement per step in diameters
         const float h = (float)sc->dt;
         float *f = B.feat + (size_t)i * 8;
         f[0] = 100.0f * ((float)rho / (float)P.rho0 - 1.0f);
         f[1] = 100.0f * (float)dsrc * h;
         f[2] = (float)(nf + nb) * (1.0f / 40.0f) - 1.0f;
-        f[3] = (float)B.kappa[i] / P.ws_scale_p;
+        f[3] = B.kappa[i] > T(0) ? 1.0f : 0.0f;
         f[4] = 10.0f * sqrtf((float)dot(vi, vi)) * h / (float)(2.0 * P.radius);
     }
     v4_t<T> xk = xi;
@@ -530,6 +532,31 @@ template <class T> __device__ __forceinline__ T aij_pj_i(const DevParams<T> &P, 
     return accf * P.V + dot(ai, xyz<T>(ldv(B.bg, i)));
 }
 
+// Book one iteration of a scene's solver with average error avg and take its loop decision:
+// the while conditions of TimeStepDFSPH.cpp:477 (divergence: at least one iteration, error
+// below maxErrorV percent of rho0 per second) and :324 (pressure: at least minIterations,
+// error below maxError percent of rho0), both capped by the maximum iteration count.
+template <class T, bool DIV>
+__device__ __forceinline__ void solver_decide(const DevParams<T> &P, StepScalars *sc, double avg, unsigned inc = 1)
+{
+    unsigned it;
+    bool cont;
+    if (DIV) {
+        it = (sc->iters_v += inc);
+        sc->avg_err_v = avg;
+        const double eta = (1.0 / sc->dt) * P.max_error_v * 0.01 * (double)P.rho0;
+        const bool chk = avg <= eta;
+        cont = (!chk || it < 1u) && it < P.max_iter_v;
+    } else {
+        it = (sc->iters += inc);
+        sc->avg_err = avg;
+        const double eta = P.max_error * 0.01 * (double)P.rho0;
+        const bool chk = avg <= eta;
+        cont = (!chk || it < P.min_iter) && it < P.max_iter;
+    }
+    sc->cont = cont ? 1u : 0u;
+}
+
 // divergenceSolveIteration (TimeStepDFSPH.cpp:621-706) / pressureSolveIteration (:544-619):
 // Jacobi update of kappa_v / kappa plus the FP64 average-error reduction and the
 // loop decision (the while conditions of :477 and :324), per scene.
@@ -575,25 +602,7 @@ __global__ void __launch_bounds__(kBlock) k_jacobi(DevParams<T> P, DevBufs<T> B,
     const DevBufs<T> &BB = B;
     const uint32_t n_s = q.end - q.begin;
     grid_sum_finalize<1>(mine, scene_reduce(P, B, q), [&](const DSum<1> &tot) {
-        if (live) {
-            const double avg = n_s ? tot.v[0] / (double)n_s : 0.0;
-            unsigned it;
-            bool cont;
-            if (DIV) {
-                it = ++sc->iters_v;
-                sc->avg_err_v = avg;
-                const double eta = (1.0 / sc->dt) * PP.max_error_v * 0.01 * (double)PP.rho0;
-                const bool chk = avg <= eta;
-                cont = (!chk || it < 1u) && it < PP.max_iter_v;
-            } else {
-                it = ++sc->iters;
-                sc->avg_err = avg;
-                const double eta = PP.max_error * 0.01 * (double)PP.rho0;
-                const bool chk = avg <= eta;
-                cont = (!chk || it < PP.min_iter) && it < PP.max_iter;
-            }
-            sc->cont = cont ? 1u : 0u;
-        }
+        if (live) solver_decide<T, DIV>(PP, sc, n_s ? tot.v[0] / (double)n_s : 0.0);
         batch_decide(PP, BB, handle, use_handle);
     });
 }
@@ -1106,8 +1115,11 @@ __global__ void __launch_bounds__(kBlock) k_integrate(DevParams<T> P, DevBufs<T>
 // ==========================================================================
 // learned warm start
 // ==========================================================================
-// Network inputs: the 5 raw features of particle i and their cubic-spline-weighted mean
-// over i and its fluid neighbours (sum_j W_ij f_j / sum_j W_ij, self weight W(0)).
+// Network inputs (10, all dimensionless): the raw features f0..f4 of particle i, with f3
+// replaced by the previous stored kappa of i relative to its cubic-spline-weighted
+// neighbourhood mean, followed by the weighted means of f0..f4 over i and its fluid
+// neighbours (sum_j W_ij f_j / sum_j W_ij, self weight W(0)).  Runs before the pressure
+// solve overwrites kappa, so B.kappa still holds the previous step's stored value.
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_features(DevParams<T> P, DevBufs<T> B)
 {
@@ -1118,36 +1130,40 @@ __global__ void __launch_bounds__(kBlock) k_features(DevParams<T> P, DevBufs<T> 
     const v4_t<T> xi = ldv(B.x, i);
     const float4 f0 = *reinterpret_cast<const float4 *>(B.feat + (size_t)i * 8);
     const float f4 = B.feat[(size_t)i * 8 + 4];
+    const float ki = (float)B.kappa[i];
     const float w0 = (float)P.K.w0;
     float m[5] = {w0 * f0.x, w0 * f0.y, w0 * f0.z, w0 * f0.w, w0 * f4};
-    float wsum = w0;
+    float wsum = w0, km = w0 * ki;
     struct XF {
         v4_t<T> x;
         float4 a;
-        float b;
+        float b, k;
     };
     nbr_loop<kUnroll>(list_ptr(B.lf, i, P.capf), min(B.nf[i], P.capf),
                       [&](uint32_t j) {
                           return XF{ldv(B.x, j), *reinterpret_cast<const float4 *>(B.feat + (size_t)j * 8),
-                                    B.feat[(size_t)j * 8 + 4]};
+                                    B.feat[(size_t)j * 8 + 4], (float)B.kappa[j]};
                       },
                       [&](uint32_t, const XF &d) {
                           const V3<T> r = diff3<T>(xi, d.x);
                           const float w = (float)kernel_W(P.K, dev_sqrt(dot(r, r)));
                           m[0] += w * d.a.x; m[1] += w * d.a.y; m[2] += w * d.a.z; m[3] += w * d.a.w; m[4] += w * d.b;
+                          km += w * d.k;
                           wsum += w;
                       });
     float *X = B.mlp_x + (size_t)i * 10;
-    X[0] = f0.x; X[1] = f0.y; X[2] = f0.z; X[3] = f0.w; X[4] = f4;
+    X[0] = f0.x; X[1] = f0.y; X[2] = f0.z; X[4] = f4;
+    X[3] = km > 0.0f ? ki / km * wsum : 0.0f;   // kappa_i / (weighted mean of kappa)
     const float inv = 1.0f / wsum;
 #pragma unroll
     for (int k = 0; k < 5; k++) X[5 + k] = m[k] * inv;
 }
 
-// Predicted warm start of one solver, with the same masks as the classic warm start:
-// divergence: kappa_v = out_v * s_v / h where the clamped source is positive and the
-// particle is not deficient (TimeStepDFSPH.cpp:424-453); pressure: kappa = out_p * s_p / h^2
-// where rho_adv > 1 (:293-296).  Negative predictions are clipped to zero.
+// Predicted warm start of one solver: the network's output o times the output scale is a
+// multiplier on the previous step's stored kappa_v / kappa, in place of the classic factor
+// 0.5 (TimeStepDFSPH.cpp:449-453 divergence, :293-296 pressure), with the classic clamps and
+// masks.  Since the classic warm start is 0.5 min(stored, clamp) / h^k where the mask holds
+// (and 0 elsewhere), the prediction is 2 m x classic; m is limited to [0, 4].
 template <class T, bool DIV>
 __global__ void __launch_bounds__(kBlock) k_ws_kappa(DevParams<T> P, DevBufs<T> B)
 {
@@ -1155,16 +1171,10 @@ __global__ void __launch_bounds__(kBlock) k_ws_kappa(DevParams<T> P, DevBufs<T> 
     const SlotInfo q = slot_info(P);
     if (!q.act) return;
     const uint32_t i = q.i;
-    const StepScalars *sc = B.sc + q.s;
-    T k = T(0);
-    if (DIV) {
-        const T h = (T)sc->dt;
-        if (B.dadv[i] > T(0) && B.nf[i] + B.nbn[i] >= 20u) k = (T)fmaxf(B.mlp_y[(size_t)i * 2] * P.ws_scale_v, 0.0f) / h;
-    } else {
-        const T h = (T)sc->dt_next;
-        if (B.dadv[i] > T(1)) k = (T)fmaxf(B.mlp_y[(size_t)i * 2 + 1] * P.ws_scale_p, 0.0f) / (h * h);
-    }
-    B.kl[i] = k;
+    const float o = B.mlp_y[(size_t)i * 2 + (DIV ? 0 : 1)] * (DIV ? P.ws_scale_v : P.ws_scale_p);
+    const float mult = fminf(fmaxf(o, 0.0f), 4.0f);   // NaN -> 0 (fmaxf returns the non-NaN operand)
+    const T classic = DIV ? B.kappa_v[i] : B.kappa[i];
+    B.kl[i] = T(2) * (T)mult * classic;
 }
 
 // Pressure accelerations of both candidate warm starts: classic (xk.w) into pa, predicted (kl)
@@ -1199,11 +1209,17 @@ __global__ void __launch_bounds__(kBlock) k_ws_accel2(DevParams<T> P, DevBufs<T>
     stv(B.pa2, i, pack(a2, T(0)));
 }
 
-// Initial residuals of both candidates (the error the first Jacobi iteration would report,
-// TimeStepDFSPH.cpp:621-706 / :544-619); the scene's last block picks the predicted warm
-// start only if its residual is lower.
-template <class T, bool DIV>
-__global__ void __launch_bounds__(kBlock) k_ws_residual2(DevParams<T> P, DevBufs<T> B)
+// One Jacobi iteration of the solver (TimeStepDFSPH.cpp:621-706 divergence, :544-619
+// pressure) for both candidate warm starts at once: aij from the two pressure accelerations,
+// the updated kappa of each candidate (classic into kappa_v / kappa and xk.w, predicted into
+// kl) and, in the last of the `sweeps` gate iterations, both average errors.  The scene's
+// last block then keeps the predicted warm start only if its error is lower, books the
+// gate iterations of the chosen candidate and takes the loop decision, so the solver loop
+// continues with iteration sweeps + 1.  With one sweep the errors compared are the
+// candidates' initial residuals.
+template <class T, bool DIV, bool LAST>
+__global__ void __launch_bounds__(kBlock) k_ws_sweep(DevParams<T> P, DevBufs<T> B, unsigned sweeps,
+                                                      cudaGraphConditionalHandle handle, int use_handle)
 {
     count_launch(&B.gsc->launches);
     const SlotInfo q = slot_info(P);
@@ -1228,7 +1244,7 @@ __global__ void __launch_bounds__(kBlock) k_ws_residual2(DevParams<T> P, DevBufs
                           });
         const V3<T> gb = xyz<T>(ldv(B.bg, i));
         T ap1 = s1 * P.V + dot(a1, gb), ap2 = s2 * P.V + dot(a2, gb);
-        T si;
+        T si, fac;
         bool zero = false;
         if (DIV) {
             const T h = (T)sc->dt;
@@ -1236,39 +1252,59 @@ __global__ void __launch_bounds__(kBlock) k_ws_residual2(DevParams<T> P, DevBufs
             ap2 *= h;
             si = -B.dadv[i];
             zero = B.nf[i] + B.nbn[i] < 20u;
+            fac = B.factor[i] * (T(1) / h);
         } else {
             const T h = (T)sc->dt_next;
             ap1 *= h * h;
             ap2 *= h * h;
             si = T(1) - B.dadv[i];
+            fac = B.factor[i] * (T(1) / (h * h));
         }
-        const T r1 = (si - ap1) < T(0) ? (si - ap1) : T(0);
-        const T r2 = (si - ap2) < T(0) ? (si - ap2) : T(0);
-        if (!zero) {
+        T *kap = DIV ? B.kappa_v : B.kappa;
+        T k1 = kap[i] - T(0.5) * (si - ap1) * fac;
+        T k2 = B.kl[i] - T(0.5) * (si - ap2) * fac;
+        k1 = k1 > T(0) ? k1 : T(0);
+        k2 = k2 > T(0) ? k2 : T(0);
+        kap[i] = k1;
+        B.kl[i] = k2;
+        store_w(B.xk, i, k1);
+        if (LAST && !zero) {
+            const T r1 = (si - ap1) < T(0) ? (si - ap1) : T(0);
+            const T r2 = (si - ap2) < T(0) ? (si - ap2) : T(0);
             mine.v[0] = -(double)P.rho0 * (double)r1;
             mine.v[1] = -(double)P.rho0 * (double)r2;
         }
     }
+    if (!LAST) return;   // uniform over the grid: no block collective follows
     const uint32_t n_s = q.end - q.begin;
+    const DevParams<T> &PP = P;
+    const DevBufs<T> &BB = B;
     grid_sum_finalize<2>(mine, scene_reduce(P, B, q), [&](const DSum<2> &tot) {
         const int k = DIV ? 0 : 1;
         const double inv = n_s ? 1.0 / (double)n_s : 0.0;
         sc->ws_rc[k] = tot.v[0] * inv;
         sc->ws_rl[k] = tot.v[1] * inv;
-        if (tot.v[1] < tot.v[0]) sc->ws_used |= (1u << k);
+        const bool learned = tot.v[1] < tot.v[0];
+        if (learned) sc->ws_used |= (1u << k);
         else sc->ws_used &= ~(1u << k);
+        solver_decide<T, DIV>(PP, sc, (learned ? tot.v[1] : tot.v[0]) * inv, sweeps);
+        batch_decide(PP, BB, handle, use_handle);
     });
 }
 
+// kappa of the chosen candidate after the gate iterations into kappa_v / kappa and xk.w
 template <class T, bool DIV>
 __global__ void __launch_bounds__(kBlock) k_ws_apply(DevParams<T> P, DevBufs<T> B)
 {
     count_launch(&B.gsc->launches);
     const SlotInfo q = slot_info(P);
     if (!q.act) return;
-    if (!(B.sc[q.s].ws_used & (1u << (DIV ? 0 : 1)))) return;
-    const T k = B.kl[q.i];
-    (DIV ? B.kappa_v : B.kappa)[q.i] = k;
+    T *kap = DIV ? B.kappa_v : B.kappa;
+    T k = kap[q.i];
+    if (B.sc[q.s].ws_used & (1u << (DIV ? 0 : 1))) {
+        k = B.kl[q.i];
+        kap[q.i] = k;
+    }
     store_w(B.xk, q.i, k);
 }
 
@@ -1601,19 +1637,28 @@ template <class T> void launch_features(const DevParams<T> &P, const DevBufs<T> 
 {
     if (P.np) k_features<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
 }
-template <class T> void launch_warmstart_select(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s)
+template <class T>
+void launch_warmstart_select(const DevParams<T> &P, const DevBufs<T> &B, bool div, unsigned sweeps,
+                             cudaGraphConditionalHandle h, bool use_handle, cudaStream_t s)
 {
-    if (!P.np) return;
+    if (!P.np || sweeps == 0) return;
     const unsigned g = grid_for(P.np);
+    const int uh = use_handle ? 1 : 0;
     if (div) {
         k_ws_kappa<T, true><<<g, kBlock, 0, s>>>(P, B);
-        k_ws_accel2<T><<<g, kBlock, 0, s>>>(P, B);
-        k_ws_residual2<T, true><<<g, kBlock, 0, s>>>(P, B);
+        for (unsigned k = 1; k <= sweeps; k++) {
+            k_ws_accel2<T><<<g, kBlock, 0, s>>>(P, B);
+            if (k < sweeps) k_ws_sweep<T, true, false><<<g, kBlock, 0, s>>>(P, B, sweeps, h, uh);
+            else k_ws_sweep<T, true, true><<<g, kBlock, 0, s>>>(P, B, sweeps, h, uh);
+        }
         k_ws_apply<T, true><<<g, kBlock, 0, s>>>(P, B);
     } else {
         k_ws_kappa<T, false><<<g, kBlock, 0, s>>>(P, B);
-        k_ws_accel2<T><<<g, kBlock, 0, s>>>(P, B);
-        k_ws_residual2<T, false><<<g, kBlock, 0, s>>>(P, B);
+        for (unsigned k = 1; k <= sweeps; k++) {
+            k_ws_accel2<T><<<g, kBlock, 0, s>>>(P, B);
+            if (k < sweeps) k_ws_sweep<T, false, false><<<g, kBlock, 0, s>>>(P, B, sweeps, h, uh);
+            else k_ws_sweep<T, false, true><<<g, kBlock, 0, s>>>(P, B, sweeps, h, uh);
+        }
         k_ws_apply<T, false><<<g, kBlock, 0, s>>>(P, B);
     }
 }
@@ -1680,7 +1725,8 @@ void launch_lists_to_ids(const uint32_t *list, const uint32_t *cnt, uint32_t cap
     template void launch_loop_begin<T>(const DevParams<T> &, const DevBufs<T> &, bool, cudaStream_t);               \
     template void launch_step_begin<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                     \
     template void launch_features<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                       \
-    template void launch_warmstart_select<T>(const DevParams<T> &, const DevBufs<T> &, bool, cudaStream_t);         \
+    template void launch_warmstart_select<T>(const DevParams<T> &, const DevBufs<T> &, bool, unsigned,              \
+                                             cudaGraphConditionalHandle, bool, cudaStream_t);                       \
     template void launch_xsph<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                           \
     template void launch_visc_setup<T>(const DevParams<T> &, const DevBufs<T> &, cudaGraphConditionalHandle, bool,  \
                                        cudaStream_t);                                                               \

@@ -24,16 +24,17 @@ constexpr int kOffW3 = kOffB2 + kMlpH;
 constexpr int kOffB3 = kOffW3 + kMlpOutPad * kMlpH;
 constexpr int kMlpParams = kOffB3 + kMlpOutPad;   // 5768
 
-// Default scales of the stored warm starts: network output x scale = kappa_v*dt (divergence)
-// and kappa*dt^2 (pressure); the pressure scale also normalises the previous-kappa feature.
-constexpr float kMlpDefaultScaleV = 1.0e-2f;
-constexpr float kMlpDefaultScaleP = 1.0e-4f;
+// Default output scales: network output x scale = the multiplier that the predicted warm
+// start applies to the previous step's stored kappa_v (divergence) and kappa (pressure), in
+// place of the classic factor 0.5.
+constexpr float kMlpDefaultScaleV = 1.0f;
+constexpr float kMlpDefaultScaleP = 1.0f;
 
 // Device copy used by kernels: BF16 weights and FP32 biases, plus feature/output scales.
 struct MlpDev {
     const __nv_bfloat16 *w;   // kMlpParams bf16 (biases unused in this copy)
     const float *p;           // kMlpParams fp32 (biases read from here)
-    float out_scale[2];       // network output * scale = stored warm start (kappa_v*h, kappa*h^2)
+    float out_scale[2];       // network output * scale = warm-start multiplier (divergence, pressure)
 };
 
 __device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }

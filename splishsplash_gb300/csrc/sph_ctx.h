@@ -74,7 +74,7 @@ template <class T> struct DevParams {
     unsigned min_iter, max_iter, max_iter_v, visc_max_iter;
     int cfl_method, visc_on, div_on;
     int learned, feat_on;         // learned warm start on; features computed
-    float ws_scale_v, ws_scale_p; // network output scales
+    float ws_scale_v, ws_scale_p; // network output scales (output x scale = warm-start multiplier)
     // scenes
     uint32_t nscenes;
     SceneDev<T> s0;               // the scene when nscenes == 1 (no device lookup)
@@ -165,7 +165,10 @@ template <class T> void launch_step_begin(const DevParams<T> &P, const DevBufs<T
 template <class T> void launch_loop_begin(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s);
 template <class T> void launch_boundary_volume(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
 template <class T> void launch_features(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
-template <class T> void launch_warmstart_select(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s);
+// Learned warm start of one solver: both candidates, their first `sweeps` Jacobi iterations,
+// the choice and the loop decision after them (needs 1 <= sweeps <= max_iter of that solver).
+template <class T> void launch_warmstart_select(const DevParams<T> &P, const DevBufs<T> &B, bool div, unsigned sweeps,
+                                                cudaGraphConditionalHandle h, bool use_handle, cudaStream_t s);
 void mlp_infer_device(const float *X, uint32_t n, const void *w, const float *p, float *Y, cudaStream_t s);
 // boundary set-up: keys (scene prefix | Morton code) of the boundary particles in upload order
 template <class T> void launch_boundary_keys(const DevParams<T> &P, const v4_t<T> *xb_in, const uint32_t *bscene_in,

@@ -119,7 +119,7 @@ EXPORTS = [
     "sphgb_set_time", "sphgb_step", "sphgb_sync", "sphgb_download", "sphgb_upload_field", "sphgb_neighbors",
     "sphgb_num_particles", "sphgb_get_stream", "sphgb_profile_enable", "sphgb_profile_reset", "sphgb_profile_read",
     "sphgb_set_warmstart_mlp", "sphgb_set_feature_output", "sphgb_upload_scenes", "sphgb_num_scenes",
-    "sphgb_scene_stats",
+    "sphgb_scene_stats", "sphgb_set_warmstart_gate",
 ]
 
 _lib = None
@@ -167,6 +167,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.sphgb_upload_scenes.argtypes = [vp, u32, vp, vp, vp, vp, vp]
     L.sphgb_num_scenes.argtypes = [vp, ctypes.POINTER(u32)]
     L.sphgb_scene_stats.argtypes = [vp, u32, u32, ctypes.POINTER(Stats)]
+    L.sphgb_set_warmstart_gate.argtypes = [vp, u32, u32]
     L.sphgb_profile_enable.argtypes = [vp, i32]
     L.sphgb_profile_reset.argtypes = [vp]
     L.sphgb_profile_read.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_uint64),
@@ -429,6 +430,11 @@ class Context:
     def set_warmstart_mlp(self, mlp):
         """Use a trained network for both warm starts (None: classic warm start only)."""
         self._check(self.L.sphgb_set_warmstart_mlp(self.h, None if mlp is None else mlp.h))
+
+    def set_warmstart_gate(self, div_sweeps: int = 0, pressure_sweeps: int = 0):
+        """Jacobi iterations both warm-start candidates run before they are compared, per
+        solver (0: default, 1 divergence / max(minIterations, 4) pressure; 1: initial residuals)."""
+        self._check(self.L.sphgb_set_warmstart_gate(self.h, int(div_sweeps), int(pressure_sweeps)))
 
     def set_feature_output(self, on: bool = True):
         self._check(self.L.sphgb_set_feature_output(self.h, int(on)))
