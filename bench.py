@@ -12,12 +12,18 @@ Workload (single-GPU configuration of the headline metric): 128x64x128 =
 One JSON line on stdout.  `value` = fluid particles x timed steps / summed
 device time of the steps (CUDA events on the library's own stream, L2 flushed
 between steps), inputs resident in HBM.  `e2e` = the same metric through the
-C-ABI with host buffers: each step uploads positions/velocities from pinned
-host memory, steps, and downloads positions, velocities, density and both
-pressure warm starts.  `roofline` = the dominant kernel (by event-timed share
-of a profiled run) against the measured HBM copy bandwidth.  `cpu_baseline` =
-the CPU restatement (FP32 build, OpenMP over all host cores) timed for a
-bounded sample from the GPU's state.
+C-ABI with host buffers, on a second context over the same warm-up and step
+range (the solver's iteration counts change with the phase of the dam break):
+each step uploads positions/velocities from pinned host memory, steps, and
+downloads positions, velocities, density and both pressure warm starts.
+`roofline` = the dominant kernel (by event-timed share of a profiled run)
+against the measured HBM copy bandwidth.  `cpu_baseline` = the CPU
+restatement (FP32 build, OpenMP over all host cores) timed for a bounded
+sample from the GPU's state.  `learned_warmstart` = the metric's second part:
+the 2,097,152-lattice sphere scene for 300 steps with the classic and with the
+learned warm start (committed network), iterations and device time per step at
+the same tolerance.  `ensemble` = 256 independent dam breaks advanced by one
+batched context (one launch per kernel, one graph per step).
 
 --impl reference times that CPU restatement of the reference's step (the
 reference library itself cannot be built: its build needs external projects
@@ -201,13 +207,68 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def learned_line(steps):
+    """The 2,097,152-lattice sphere scene with the classic and the learned warm start."""
+    from splishsplash_gb300 import learned, scenes
+
+    sc = scenes.learned_2m()
+    net = learned.load()
+    res = learned.evaluate(sc, net, steps=steps, strict=False)
+    net.close()
+    keep = ("pressure_iterations_mean", "divergence_iterations_mean", "solver_iterations_total", "ms_per_step",
+            "final_avg_density_error_percent", "max_avg_density_error_percent", "learned_used_pressure_fraction",
+            "learned_used_div_fraction")
+    return {"workload": f"{sc.name}: {sc.n} fluid + {sc.nb} boundary particles, r=0.01, unit-sphere obstacle, "
+                        f"{steps} steps from rest, maxError 0.01%",
+            "plain": {k: res["plain"][k] for k in keep}, "learned": {k: res["learned"][k] for k in keep},
+            "iteration_reduction": res["gain"]["iteration_reduction"],
+            "time_per_step_reduction": res["gain"]["time_per_step_reduction"],
+            "gate": "1 divergence / 4 pressure Jacobi iterations of both candidates (default)",
+            "network": "splishsplash_gb300/data/warmstart_mlp.npz (python -m splishsplash_gb300.learned)"}
+
+
+def ensemble_line(steps, device):
+    """256 independent dam breaks (N_i log-uniform in [2000, 60000]) in one batched context:
+    particle-steps/s over `steps` steps after 10 warm-up steps (inputs far larger than L2)."""
+    import torch
+
+    from splishsplash_gb300 import scenes
+    from splishsplash_gb300.dfsph import BatchedTimeStepDFSPH
+
+    ens = scenes.ensemble(num_scenes=256)
+    b = BatchedTimeStepDFSPH(ens, use_graph=True, device=device)
+    for _ in range(10):
+        b.step()
+    ext = torch.cuda.ExternalStream(b.ctx.stream())
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    it = []
+    torch.cuda.synchronize()
+    for k in range(steps):
+        with torch.cuda.stream(ext):
+            evs[k][0].record(ext)
+        st = b.step()
+        with torch.cuda.stream(ext):
+            evs[k][1].record(ext)
+        per = b.scene_stats()
+        it.append((st["iterations"], float(np.mean([p["iterations"] for p in per]))))
+    torch.cuda.synchronize()
+    dev_s = sum(a.elapsed_time(c) for a, c in evs) / 1e3
+    n = int(b.sizes.sum())
+    b.close()
+    it = np.array(it)
+    return {"workload": f"256 dam-break scenes, {n} fluid particles in total, r=0.025, per-scene CFL dt",
+            "value": n * steps / dev_s, "unit": UNIT, "steps": steps, "warmup": 10,
+            "ms_per_step": 1e3 * dev_s / steps,
+            "pressure_iterations": {"batch_loop_mean": float(it[:, 0].mean()), "scene_mean": float(it[:, 1].mean())}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=190)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--e2e-steps", type=int, default=0, help="0: as many as --steps")
     ap.add_argument("--profile-steps", type=int, default=4)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--cpu-warmup-budget", type=float, default=60.0)
@@ -218,6 +279,11 @@ def main():
                     help="host-driven solver loops instead of the captured graph (kernels visible to ncu)")
     ap.add_argument("--only-timed", action="store_true",
                     help="run warm-up and the device-resident timed steps only (profiling captures)")
+    ap.add_argument("--no-extras", action="store_true", help="skip the learned-warm-start and ensemble lines")
+    ap.add_argument("--lanes", type=int, default=0, choices=[0, 1, 2, 4],
+                    help="lanes per particle of the neighbour passes (0: the library's autotuner)")
+    ap.add_argument("--learned-steps", type=int, default=300)
+    ap.add_argument("--ensemble-steps", type=int, default=60)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -241,6 +307,7 @@ def main():
 
     scene = scenes.dambreak_1m(nz=args.nz)
     ts = TimeStepDFSPH(scene, precision="fp32", use_graph=not args.host_loops, device=local)
+    ts.ctx.set_lanes_per_particle(args.lanes)
     ext = torch.cuda.ExternalStream(ts.ctx.stream())
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
 
@@ -277,6 +344,7 @@ def main():
         t_max = float(t.item())
         dist.barrier()
     value = world * scene.n * args.steps / t_max
+    lanes, trial_ms = ts.ctx.lanes_per_particle()
     if args.only_timed:
         if rank == 0:
             print(json.dumps({"metric": baseline_metric(), "value": value, "unit": UNIT, "steps": args.steps,
@@ -286,32 +354,41 @@ def main():
         return
 
     # ---------------- end-to-end through the C ABI with host buffers ----------------
+    # A second context over the same warm-up and step range as the device-resident run.
     n = scene.n
     pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()
     hx, hv = pin((n, 3), torch.float32), pin((n, 3), torch.float32)
     hrho, hk, hkv = pin((n,), torch.float32), pin((n,), torch.float32), pin((n,), torch.float32)
-    ts.ctx.download("position", out=hx)
-    ts.ctx.download("velocity", out=hv)
+    te = TimeStepDFSPH(scene, precision="fp32", use_graph=not args.host_loops, device=local)
+    te.ctx.set_lanes_per_particle(args.lanes)
+    for _ in range(args.warmup):
+        te.step()
+    te.ctx.download("position", out=hx)
+    te.ctx.download("velocity", out=hv)
     torch.cuda.synchronize()
-    e2e_steps = max(1, args.e2e_steps)
+    e2e_steps = args.steps if args.e2e_steps <= 0 else min(args.e2e_steps, args.steps)
+    if dist:
+        dist.barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        ts.ctx.upload_field("position", hx)
-        ts.ctx.upload_field("velocity", hv)
-        ts.step()
-        ts.ctx.download("position", out=hx)
-        ts.ctx.download("velocity", out=hv)
-        ts.ctx.download("density", out=hrho)
-        ts.ctx.download("p / rho^2", out=hk)
-        ts.ctx.download("p_v / rho^2", out=hkv)
+        te.ctx.upload_field("position", hx)
+        te.ctx.upload_field("velocity", hv)
+        te.step()
+        te.ctx.download("position", out=hx)
+        te.ctx.download("velocity", out=hv)
+        te.ctx.download("density", out=hrho)
+        te.ctx.download("p / rho^2", out=hk)
+        te.ctx.download("p_v / rho^2", out=hkv)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
+    te.close()
     if dist:
         t = torch.tensor([e2e_s], device=f"cuda:{local}")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
     e2e = {"value": world * n * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 2 * n * 3 * 4,
-           "d2h_bytes_per_step": 2 * n * 3 * 4 + 3 * n * 4, "steps": e2e_steps}
+           "d2h_bytes_per_step": 2 * n * 3 * 4 + 3 * n * 4, "steps": e2e_steps,
+           "region": f"steps {args.warmup + 1}..{args.warmup + e2e_steps} of a fresh context (same as the timed run)"}
 
     # ---------------- per-kernel event timing (roofline) ----------------
     ts.ctx.profile(True)
@@ -358,18 +435,26 @@ def main():
                "sample": f"{s_cpu} step(s) of the full scene from the GPU state after the timed region, {t_cpu:.1f} s "
                          f"(FP32 build of the CPU restatement, OpenMP); solver iterations {it_cpu}"}
 
+    extras = {}
+    if rank == 0 and world == 1 and not args.no_extras:
+        extras["learned_warmstart"] = learned_line(args.learned_steps)
+        extras["ensemble"] = ensemble_line(args.ensemble_steps, local)
+
     if rank == 0:
         it = np.array(iters)
         line = {
             "metric": baseline_metric(), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam break)",
-            "config": workload_config(scene), "e2e": e2e, "gpu_launches": launches,
+            "config": {**workload_config(scene), "lanes_per_particle": lanes,
+                       "lanes_autotune_trial_ms": dict(zip(("1", "2", "4"), trial_ms)) if args.lanes == 0 else None},
+            "e2e": e2e, "gpu_launches": launches,
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
             "wall_ms_per_step": 1e3 * wall / args.steps,
             "solver_iterations_mean": {"pressure": float(it[:, 0].mean()), "divergence": float(it[:, 1].mean()),
                                        "viscosity_cg": float(it[:, 2].mean())},
             "kernels": kernels,
+            **extras,
         }
         print(json.dumps(line), flush=True)
     ts.close()

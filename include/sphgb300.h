@@ -56,7 +56,7 @@ typedef struct sphgb_config {
     int abi_version;                 /* must be SPHGB_ABI_VERSION */
     int device;                      /* CUDA device ordinal */
     int precision;                   /* SPHGB_PRECISION_* */
-    uint32_t max_fluid_neighbors;    /* per-particle list capacity (0 = default 80) */
+    uint32_t max_fluid_neighbors;    /* per-particle list capacity (0 = default 80; rounded up to a multiple of 4) */
     uint32_t max_boundary_neighbors; /* per-particle list capacity (0 = default 128) */
     int use_graph;                   /* 1: capture the step in a CUDA graph with device-side
                                         solver loops (conditional while nodes); 0: host-driven loops */
@@ -255,6 +255,15 @@ int sphgb_set_feature_output(sphgb_ctx *ctx, int on);
 int sphgb_boundary_volume_noalloc(const float *xb, uint32_t nb, double particle_radius,
                                   const double box_min[3], const double box_max[3], float *volume,
                                   void *stream);
+
+/* Lanes per particle of the neighbour passes (1, 2 or 4; 32 / lanes particles per warp, kBlock /
+ * lanes particles per 256-thread block): the lanes of a particle walk interleaved parts of its
+ * fluid list, which is stored in the matching layout, and combine their sums with warp shuffles.
+ * 0 (default): an autotuner times one trial step per candidate on the first step after an
+ * upload (trials are undone) and keeps the fastest.  No reference counterpart. */
+int sphgb_set_lanes_per_particle(sphgb_ctx *ctx, uint32_t lanes);
+/* the lanes in use and the autotuner's trial step times in ms for 1, 2, 4 lanes (zeros when fixed) */
+int sphgb_get_lanes_per_particle(const sphgb_ctx *ctx, uint32_t *lanes, float trial_ms[3]);
 
 /* the cudaStream_t every kernel of this context is launched on (for event timing by callers) */
 int sphgb_get_stream(const sphgb_ctx *ctx, void **stream);

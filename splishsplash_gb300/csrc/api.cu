@@ -67,6 +67,7 @@ struct sphgb_ctx {
     void *set_x[2] = {}, *set_v[2] = {}, *set_vdiff[2] = {}, *set_kappa[2] = {}, *set_kappa_v[2] = {};
     float4 *set_xlo[2] = {};
     uint32_t *set_id[2] = {};
+    float4 *xa = nullptr;
     void *a = nullptr, *pa = nullptr, *xk = nullptr, *bg = nullptr, *density = nullptr, *factor = nullptr, *dadv = nullptr;
     uint32_t *nfc = nullptr, *nbc = nullptr, *lf = nullptr, *lb = nullptr;
     uint32_t *key = nullptr, *key2 = nullptr, *perm = nullptr, *perm2 = nullptr, *cell0 = nullptr, *cell1 = nullptr;
@@ -98,6 +99,11 @@ struct sphgb_ctx {
     void *mlp_w = nullptr;
     float ws_scale[2] = {kMlpDefaultScaleV, kMlpDefaultScaleP};
     uint32_t ws_gate[2] = {0, 0};      // Jacobi sweeps before the candidates are compared (div, pressure; 0: default)
+    // lanes per particle of the neighbour passes: 1 << lpp_log2; chosen by the autotuner unless fixed
+    uint32_t lpp_log2 = 2;
+    uint32_t lpp_fixed = 0;            // 0: autotune on the first step after an upload
+    bool tuned = false;
+    float tune_ms[3] = {0, 0, 0};      // trial step times of lanes per particle 1, 2, 4
     float *feat = nullptr, *mlp_x = nullptr, *mlp_y = nullptr;
     void *kl = nullptr, *pa2 = nullptr;
     // per-kernel CUDA-event timing (host-loop mode only)
@@ -311,6 +317,7 @@ template <class T> DevParams<T> make_params(const sphgb_ctx *c)
     P.nb = c->nb;
     P.capf = c->cfg.max_fluid_neighbors;
     P.capb = c->cfg.max_boundary_neighbors;
+    P.lpp_log2 = c->lpp_log2;
     return P;
 }
 
@@ -338,6 +345,7 @@ template <class T> DevBufs<T> make_bufs(const sphgb_ctx *c, int view)
     B.id2 = c->set_id[alt];
     B.a = (v4 *)c->a;
     B.pa = (v4 *)c->pa;
+    B.xa = c->xa;
     B.xk = (v4 *)c->xk;
     B.bg = (v4 *)c->bg;
     B.density = (T *)c->density;
@@ -738,11 +746,66 @@ template <class T> int build_graph(sphgb_ctx *c, int parity, cudaGraphExec_t *ou
     return SPHGB_OK;
 }
 
+// Lanes per particle of the neighbour passes (and with it the fluid-list layout), chosen by
+// timing one trial step per candidate (1, 2 and 4 lanes, twice each, the faster of the two
+// kept) from the current state.  A step never writes the state set it starts from (it
+// gathers into the other set), so a trial is undone by restoring the step scalars.
+template <class T> int autotune(sphgb_ctx *c)
+{
+    const uint32_t S = c->nscenes();
+    std::vector<StepScalars> saved(S + 1);
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(saved.data(), c->sc, (S + 1) * sizeof(StepScalars), cudaMemcpyDeviceToHost));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    const bool prof = c->profile;
+    c->profile = false;
+    float best[3] = {1e30f, 1e30f, 1e30f};
+    int rc = SPHGB_OK;
+    for (int rep = 0; rep < 2 && rc == SPHGB_OK; rep++)
+        for (uint32_t lg = 0; lg <= 2 && rc == SPHGB_OK; lg++) {
+            c->lpp_log2 = lg;
+            cudaEventRecord(e0, c->stream);
+            rc = step_host_loop<T>(c);
+            cudaEventRecord(e1, c->stream);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            best[lg] = std::min(best[lg], ms);
+            if (cudaMemcpy(c->sc, saved.data(), (S + 1) * sizeof(StepScalars), cudaMemcpyHostToDevice) != cudaSuccess)
+                rc = fail(c, SPHGB_ERR_CUDA, "autotune: restoring the step scalars");
+        }
+    c->profile = prof;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    CK(cudaGetLastError());
+    uint32_t pick = 2;
+    for (uint32_t lg = 0; lg <= 2; lg++) {
+        c->tune_ms[lg] = best[lg];
+        if (best[lg] < best[pick]) pick = lg;
+    }
+    c->lpp_log2 = pick;
+    c->tuned = true;
+    invalidate_graphs(c);
+    return SPHGB_OK;
+}
+
 template <class T> int do_step(sphgb_ctx *c)
 {
     int rc;
     if (!c->prepared && (rc = prepare<T>(c))) return rc;
     if ((rc = upload_scalars(c))) return rc;
+    if (!c->tuned) {
+        if (c->lpp_fixed) {
+            c->lpp_log2 = c->lpp_fixed == 1 ? 0u : (c->lpp_fixed == 2 ? 1u : 2u);
+            c->tuned = true;
+            invalidate_graphs(c);
+        } else if ((rc = autotune<T>(c))) {
+            return rc;
+        }
+    }
     if (c->cfg.use_graph && !c->profile) {
         if (!c->graph_ok) {
             invalidate_graphs(c);
@@ -895,6 +958,8 @@ template <class T> int init_scenes(sphgb_ctx *c, const double *x, const double *
     }
     if ((rc = dalloc(c, &c->a, N * vs))) return rc;
     if ((rc = dalloc(c, &c->pa, N * vs))) return rc;
+    c->xa = nullptr;
+    if (!c->fp64 && (rc = dalloc(c, &c->xa, N * 2 * sizeof(float4)))) return rc;
     if ((rc = dalloc(c, &c->xk, N * vs))) return rc;
     if ((rc = dalloc(c, &c->bg, N * vs))) return rc;
     if ((rc = dalloc(c, &c->density, N * rs))) return rc;
@@ -916,7 +981,8 @@ template <class T> int init_scenes(sphgb_ctx *c, const double *x, const double *
     for (int k = 0; k < 2; k++)
         if ((rc = dalloc(c, &c->inv[k], N * vs))) return rc;
     const size_t blocks = (N + kBlock - 1) / kBlock;
-    if ((rc = dalloc(c, &c->partials, blocks * 4 * sizeof(double)))) return rc;
+    // reductions index partials by block: up to 4 blocks per kBlock slots (4 lanes per particle)
+    if ((rc = dalloc(c, &c->partials, 4 * blocks * 4 * sizeof(double)))) return rc;
     const size_t nrec = (size_t)std::max<uint32_t>(S, 1) + 1;
     if ((rc = dalloc(c, &c->counters, std::max<size_t>(nrec * 4, 64)))) return rc;
     CK(cudaMemset(c->counters, 0, std::max<size_t>(nrec * 4, 64)));
@@ -981,6 +1047,7 @@ template <class T> int init_scenes(sphgb_ctx *c, const double *x, const double *
             }
     }
     c->have_fluid = true;
+    c->tuned = false;
     if ((c->learned || c->feat_on) && (rc = alloc_learned_buffers(c))) return rc;
     c->scalars_dirty = true;
     return SPHGB_OK;
@@ -1088,6 +1155,7 @@ int sphgb_create(const sphgb_config *cfg, sphgb_ctx **out)
     sphgb_ctx *c = new sphgb_ctx();
     c->cfg = *cfg;
     if (c->cfg.max_fluid_neighbors == 0) c->cfg.max_fluid_neighbors = 80;
+    c->cfg.max_fluid_neighbors = (c->cfg.max_fluid_neighbors + 3u) / 4u * 4u;   // fluid-list layout: lanes of 4
     if (c->cfg.max_boundary_neighbors == 0) c->cfg.max_boundary_neighbors = 128;
     c->fp64 = cfg->precision == SPHGB_PRECISION_FP64;
     c->prm = kDefaults;
@@ -1353,6 +1421,26 @@ int sphgb_set_warmstart_gate(sphgb_ctx *c, uint32_t div_sweeps, uint32_t pressur
     return SPHGB_OK;
 }
 
+int sphgb_set_lanes_per_particle(sphgb_ctx *c, uint32_t lanes)
+{
+    if (!c || (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 4)) return SPHGB_ERR_ARGUMENT;
+    sphgb_stats st;
+    if (c->step_pending) fill_stats(c, &st);
+    c->lpp_fixed = lanes;
+    c->tuned = false;
+    invalidate_graphs(c);
+    return SPHGB_OK;
+}
+
+int sphgb_get_lanes_per_particle(const sphgb_ctx *c, uint32_t *lanes, float trial_ms[3])
+{
+    if (!c || !lanes) return SPHGB_ERR_ARGUMENT;
+    *lanes = 1u << c->lpp_log2;
+    if (trial_ms)
+        for (int k = 0; k < 3; k++) trial_ms[k] = c->tune_ms[k];
+    return SPHGB_OK;
+}
+
 int sphgb_get_stream(const sphgb_ctx *c, void **stream)
 {
     if (!c || !stream) return SPHGB_ERR_ARGUMENT;
@@ -1483,7 +1571,7 @@ int sphgb_neighbors(sphgb_ctx *c, int kind, uint32_t *offsets, uint32_t *indices
     if (c->fp64) launch_inverse_perm<double>(make_params<double>(c), id, c->inv_perm, c->stream);
     else launch_inverse_perm<float>(make_params<float>(c), id, c->inv_perm, c->stream);
     launch_lists_to_ids(kind == 0 ? c->lf : c->lb, kind == 0 ? c->nfc : c->nbc, cap, id, c->inv_perm, c->bid, kind,
-                        doff, dout, n, c->stream);
+                        c->lpp_log2, doff, dout, n, c->stream);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(indices, dout, (size_t)offsets[n] * 4, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));

@@ -24,20 +24,28 @@ namespace {
 
 inline unsigned grid_for(uint32_t n) { return (n + kBlock - 1) / kBlock; }
 
-// ---- slots and scenes -----------------------------------------------------
+// ---- slots, scenes and lanes per particle ---------------------------------
+// A particle kernel runs LPP lanes per particle (LPP = 1 everywhere except the
+// neighbour passes, which take LPP in {1, 2, 4}): the kBlock threads of a block
+// cover kBlock / LPP consecutive slots, and the LPP lanes of a particle walk
+// interleaved parts of its fluid list and combine their partial sums with warp
+// shuffles.  A block never spans two scenes (scenes start at multiples of kBlock).
 struct SlotInfo {
     uint32_t s;            // scene
     uint32_t i;            // slot
+    uint32_t l;            // lane of the particle (0 .. LPP-1)
     uint32_t begin, end;   // the scene's slots holding particles
     bool act;              // slot i holds a particle
 };
 
-template <class T> __device__ __forceinline__ SlotInfo slot_info(const DevParams<T> &P)
+template <int LPP = 1, class T> __device__ __forceinline__ SlotInfo slot_info(const DevParams<T> &P)
 {
+    constexpr uint32_t SPB = kBlock / LPP;
     SlotInfo q;
-    q.i = blockIdx.x * blockDim.x + threadIdx.x;
+    q.i = blockIdx.x * SPB + threadIdx.x / LPP;
+    q.l = threadIdx.x % LPP;
     if (P.nscenes > 1) {
-        const uint4 b = __ldg(P.blk + blockIdx.x);
+        const uint4 b = __ldg(P.blk + blockIdx.x / LPP);
         q.s = b.x;
         q.begin = b.y;
         q.end = b.z;
@@ -51,20 +59,35 @@ template <class T> __device__ __forceinline__ SlotInfo slot_info(const DevParams
 }
 
 // reduction slot of the scene of this block
-template <class T> __device__ __forceinline__ ReduceSlot scene_reduce(const DevParams<T> &P, const DevBufs<T> &B,
-                                                                      const SlotInfo &q)
+template <int LPP = 1, class T>
+__device__ __forceinline__ ReduceSlot scene_reduce(const DevParams<T> &P, const DevBufs<T> &B, const SlotInfo &q)
 {
+    constexpr uint32_t SPB = kBlock / LPP;
     ReduceSlot r;
     r.partials = B.partials;
     r.counter = B.counters + q.s;
     if (P.nscenes > 1) {
-        r.first = q.begin / kBlock;
-        r.count = (q.end - q.begin + kBlock - 1) / kBlock;
+        // every block of the scene's padded slot range [begin, begin + kBlock * ceil(n / kBlock))
+        // takes part, also those that hold no particle
+        r.first = q.begin / SPB;
+        r.count = (q.end - q.begin + kBlock - 1) / kBlock * LPP;
     } else {
         r.first = 0;
         r.count = gridDim.x;
     }
     return r;
+}
+
+// sum over the LPP lanes of a particle (all 32 lanes of the warp must call it)
+template <int LPP, class T> __device__ __forceinline__ T gsum(T v)
+{
+#pragma unroll
+    for (int o = LPP >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+template <int LPP, class T> __device__ __forceinline__ V3<T> gsum3(V3<T> v)
+{
+    return V3<T>{gsum<LPP>(v.x), gsum<LPP>(v.y), gsum<LPP>(v.z)};
 }
 
 // Loop decision of the batch.  Called by the thread that finalized a scene's
@@ -93,6 +116,7 @@ __device__ __forceinline__ void batch_decide(const DevParams<T> &P, const DevBuf
 }
 
 // ---- list access --------------------------------------------------------
+// Boundary lists: warp-interleaved, entry k of particle i at (i / 32) 32 cap + 32 k + i % 32.
 __device__ __forceinline__ const uint32_t *list_ptr(const uint32_t *L, uint32_t i, uint32_t cap)
 {
     return L + (size_t)(i >> 5) * cap * 32u + (i & 31u);
@@ -101,11 +125,26 @@ __device__ __forceinline__ uint32_t *list_ptr(uint32_t *L, uint32_t i, uint32_t 
 {
     return L + (size_t)(i >> 5) * cap * 32u + (i & 31u);
 }
-
-template <class T> struct Pair {
-    V3<T> r;    // xi - xj
-    T rl;       // |r|
-};
+// Fluid lists in the layout of the neighbour passes' lanes per particle (lpp = 1 << lpp_log2):
+// entry k of particle i at (i / G) G cap + 32 (k / lpp) + lpp (i % G) + k % lpp, G = 32 / lpp,
+// so that one step of a warp (G particles x lpp entries) reads 32 consecutive words; lpp = 1
+// is the warp-interleaved layout of the boundary lists.  cap is a multiple of 4.
+__device__ __forceinline__ size_t fl_index(uint32_t i, uint32_t k, uint32_t cap, uint32_t lpp_log2)
+{
+    const uint32_t lpp = 1u << lpp_log2, G = 32u >> lpp_log2;
+    return (size_t)(i / G) * G * cap + 32u * (k >> lpp_log2) + lpp * (i % G) + (k & (lpp - 1u));
+}
+// first entry of lane l of particle i; the lane's following entries are 32 words apart
+template <int LPP> __device__ __forceinline__ const uint32_t *fl_lane(const uint32_t *L, uint32_t i, uint32_t l, uint32_t cap)
+{
+    constexpr uint32_t G = 32u / LPP;
+    return L + (size_t)(i / G) * G * cap + LPP * (i % G) + l;
+}
+// entries of lane l among cnt entries dealt round-robin to LPP lanes
+template <int LPP> __device__ __forceinline__ uint32_t lane_count(uint32_t cnt, uint32_t l)
+{
+    return cnt > l ? (cnt - l + LPP - 1) / LPP : 0u;
+}
 
 // gradW(r) = c r from the squared distance.  FP32: one reciprocal square root
 // (MUFU) instead of a square root and a division; FP64: exact sqrt and division.
@@ -160,14 +199,14 @@ template <class T> __device__ __forceinline__ V3<T> diff3(const v4_t<T> &a, cons
 
 // Neighbour loop with U independent index loads, then U dependent gathers, then
 // U computations, so that each thread keeps several loads in flight.
-template <int U, class Ld, class Cp>
+template <int U, uint32_t STRIDE = 32u, class Ld, class Cp>
 __device__ __forceinline__ void nbr_loop(const uint32_t *__restrict__ L, uint32_t cnt, Ld ld, Cp cp)
 {
     uint32_t k = 0;
     for (; k + U <= cnt; k += U) {
         uint32_t j[U];
 #pragma unroll
-        for (int u = 0; u < U; u++) j[u] = __ldg(L + (k + u) * 32u);
+        for (int u = 0; u < U; u++) j[u] = __ldg(L + (k + u) * STRIDE);
         decltype(ld(0u)) d[U];
 #pragma unroll
         for (int u = 0; u < U; u++) d[u] = ld(j[u]);
@@ -175,8 +214,28 @@ __device__ __forceinline__ void nbr_loop(const uint32_t *__restrict__ L, uint32_
         for (int u = 0; u < U; u++) cp(j[u], d[u]);
     }
     for (; k < cnt; k++) {
-        const uint32_t jj = __ldg(L + k * 32u);
+        const uint32_t jj = __ldg(L + k * STRIDE);
         cp(jj, ld(jj));
+    }
+}
+
+// The fluid neighbours of particle i that lane l of its LPP lanes handles
+template <int LPP, int U, class T, class Ld, class Cp>
+__device__ __forceinline__ void fluid_loop(const DevParams<T> &P, const DevBufs<T> &B, uint32_t i, uint32_t l, Ld ld, Cp cp)
+{
+    const uint32_t nf = min(B.nf[i], P.capf);
+    nbr_loop<U>(fl_lane<LPP>(B.lf, i, l, P.capf), lane_count<LPP>(nf, l), ld, cp);
+}
+// ... and its boundary neighbours (warp-interleaved boundary list, entries l, l + LPP, ...)
+template <int LPP, class T, class Cp>
+__device__ __forceinline__ void boundary_loop(const DevParams<T> &P, const DevBufs<T> &B, uint32_t i, uint32_t l, Cp cp)
+{
+    const uint32_t nb = min(B.nbn[i], P.capb);
+    const uint32_t *L = list_ptr(B.lb, i, P.capb) + 32u * l;
+    const uint32_t cnt = lane_count<LPP>(nb, l);
+    for (uint32_t k = 0; k < cnt; k++) {
+        const uint32_t j = __ldg(L + k * 32u * LPP);
+        cp(j, ldv(B.xb, j));
     }
 }
 
@@ -319,8 +378,9 @@ __device__ __forceinline__ void build_one(const DevParams<T> &P, const DevBufs<T
     }
     const T cull = P.K.h2 * T(1.001);
 
-    uint32_t *Lf = list_ptr(B.lf, i, P.capf);
+    uint32_t *Lf = B.lf + fl_index(i, 0, P.capf, P.lpp_log2);   // entry k at fl_index(i, k, ...)
     uint32_t *Lb = list_ptr(B.lb, i, P.capb);
+    const uint32_t lpp = 1u << P.lpp_log2;
     uint32_t nf = 0, nb = 0;
     for (int dz = -1; dz <= 1; dz++) {
         const int z = cz + dz;
@@ -345,7 +405,7 @@ __device__ __forceinline__ void build_one(const DevParams<T> &P, const DevBufs<T
                     for (uint32_t j = s; j < e; j++) {
                         T ddx, ddy, ddz;
                         if (j != i && pair_d2(xi, ldv(B.x, j), ddx, ddy, ddz) < P.K.h2) {
-                            if (nf < P.capf) Lf[nf * 32u] = j;
+                            if (nf < P.capf) Lf[32u * (nf >> P.lpp_log2) + (nf & (lpp - 1u))] = j;
                             nf++;
                         }
                     }
@@ -372,17 +432,21 @@ __device__ __forceinline__ void build_one(const DevParams<T> &P, const DevBufs<T
     struct XV {
         v4_t<T> x, v;
     };
-    nbr_loop<kUnroll>(Lf, min(nf, P.capf), [&](uint32_t j) { return XV{ldv(B.x, j), ldv(B.v, j)}; },
-                      [&](uint32_t, const XV &d) {
-                          const V3<T> r = diff3<T>(xi, d.x);
-                          T W, c;
-                          kernel_W_coef_d2(P.K, dot(r, r), W, c);
-                          wf += W;
-                          const V3<T> g = scl(r, c);
-                          gsq += dot(g, g);
-                          gf = add(gf, g);
-                          divf += dot(sub(vi, xyz<T>(d.v)), g);
-                      });
+    // the own list, sub-list by sub-list (entries l, l + lpp, ... are 32 words apart)
+    const uint32_t nfc = min(nf, P.capf);
+    for (uint32_t l = 0; l < lpp; l++)
+        nbr_loop<kUnroll>(Lf + l, nfc > l ? (nfc - l + lpp - 1u) >> P.lpp_log2 : 0u,
+                          [&](uint32_t j) { return XV{ldv(B.x, j), ldv(B.v, j)}; },
+                          [&](uint32_t, const XV &d) {
+                              const V3<T> r = diff3<T>(xi, d.x);
+                              T W, c;
+                              kernel_W_coef_d2(P.K, dot(r, r), W, c);
+                              wf += W;
+                              const V3<T> g = scl(r, c);
+                              gsq += dot(g, g);
+                              gf = add(gf, g);
+                              divf += dot(sub(vi, xyz<T>(d.v)), g);
+                          });
     nbr_loop<kUnroll>(Lb, min(nb, P.capb), [&](uint32_t j) { return ldv(B.xb, j); },
                       [&](uint32_t, const v4_t<T> &xj) {
                           const V3<T> r = diff3<T>(xi, xj);
@@ -454,27 +518,35 @@ __global__ void __launch_bounds__(kBlock) k_build(DevParams<T> P, DevBufs<T> B)
 // ==========================================================================
 // DFSPH solver passes
 // ==========================================================================
+// The neighbour passes run LPP lanes per particle.  All 32 lanes of a warp reach the
+// lane sums (gsum): inactive slots contribute zeros, and only whole blocks return early.
+
 // computePressureAccel, scalar path (TimeStepDFSPH.cpp:1299-1367):
 // a_i = -V sum_j [|k_i + k_j| > eps] (k_i + k_j) gradW_ij - [|k_i| > eps] k_i sum_b V_b gradW_ib
 // with kappa of the running solver read from xk.w and the boundary sum from bg.
-template <class T>
-__device__ __forceinline__ V3<T> pressure_accel_i(const DevParams<T> &P, const DevBufs<T> &B, uint32_t i)
+// Every lane of the particle returns the full acceleration.
+template <int LPP, class T>
+__device__ __forceinline__ V3<T> pressure_accel_g(const DevParams<T> &P, const DevBufs<T> &B, const SlotInfo &q)
 {
-    const v4_t<T> xi = ldv(B.xk, i);
-    const T pi = (T)xi.w;
     V3<T> acc = mk3<T>(0, 0, 0);
-    const uint32_t nf = min(B.nf[i], P.capf);
-    nbr_loop<kUnroll>(list_ptr(B.lf, i, P.capf), nf, [&](uint32_t j) { return ldv(B.xk, j); },
-                      [&](uint32_t, const v4_t<T> &xj) {
-                          const T psum = pi + (T)xj.w;
-                          if (fabs(psum) > P.eps) {
-                              const V3<T> r = diff3<T>(xi, xj);
-                              const T c = grad_coef_d2(P.K, dot(r, r)) * psum;
-                              acc = add(acc, scl(r, c));
-                          }
-                      });
+    T pi = T(0);
+    v4_t<T> xi{};
+    if (q.act) {
+        xi = ldv(B.xk, q.i);
+        pi = (T)xi.w;
+        fluid_loop<LPP, kUnroll>(P, B, q.i, q.l, [&](uint32_t j) { return ldv(B.xk, j); },
+                                 [&](uint32_t, const v4_t<T> &xj) {
+                                     const T psum = pi + (T)xj.w;
+                                     if (fabs(psum) > P.eps) {
+                                         const V3<T> r = diff3<T>(xi, xj);
+                                         const T c = grad_coef_d2(P.K, dot(r, r)) * psum;
+                                         acc = add(acc, scl(r, c));
+                                     }
+                                 });
+    }
+    acc = gsum3<LPP>(acc);
     V3<T> ai = scl(acc, -P.V);
-    if (fabs(pi) > P.eps) ai = sub(ai, scl(xyz<T>(ldv(B.bg, i)), pi));
+    if (q.act && fabs(pi) > P.eps) ai = sub(ai, scl(xyz<T>(ldv(B.bg, q.i)), pi));
     return ai;
 }
 
@@ -496,40 +568,88 @@ __device__ __forceinline__ void loop_guard(StepScalars *gsc, unsigned limit, cud
 }
 
 // a scene whose solver loop already stopped skips the remaining bodies of the batch's loop
+// (uniform over a block: a block belongs to one scene)
 template <class T> __device__ __forceinline__ bool scene_live(const DevParams<T> &P, const StepScalars *sc)
 {
     return P.nscenes == 1 || sc->cont != 0u;
 }
 
-template <class T>
+// One 32-byte record (two float4) with a single 256-bit load; p must be 32-byte aligned and
+// not written during the kernel.
+struct F8 {
+    float4 a, b;
+};
+__device__ __forceinline__ F8 ld_f8(const float4 *p)
+{
+    F8 r;
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(r.a.x), "=f"(r.a.y), "=f"(r.a.z), "=f"(r.a.w), "=f"(r.b.x), "=f"(r.b.y), "=f"(r.b.z), "=f"(r.b.w)
+        : "l"(p));
+    return r;
+}
+
+// Pressure accelerations of the running solver.  FP32: also the (x_i, a_i) record that the
+// Jacobi pass gathers with one 256-bit load per neighbour.
+template <class T, int LPP>
 __global__ void __launch_bounds__(kBlock) k_pressure_accel(DevParams<T> P, DevBufs<T> B, unsigned limit,
                                                             cudaGraphConditionalHandle h, int use_handle)
 {
     count_launch(&B.gsc->launches);
     loop_guard(B.gsc, limit, h, use_handle);
-    const SlotInfo q = slot_info(P);
-    if (!q.act || !scene_live(P, B.sc + q.s)) return;
-    stv(B.pa, q.i, pack(pressure_accel_i(P, B, q.i), T(0)));
+    const SlotInfo q = slot_info<LPP>(P);
+    if (!scene_live(P, B.sc + q.s)) return;
+    const V3<T> a = pressure_accel_g<LPP>(P, B, q);
+    if (!q.act || q.l != 0) return;
+    if constexpr (sizeof(T) == 4) {
+        B.xa[2 * (size_t)q.i] = ldv(B.x, q.i);
+        B.xa[2 * (size_t)q.i + 1] = make_float4(a.x, a.y, a.z, 0.0f);
+    } else {
+        stv(B.pa, q.i, pack(a, T(0)));
+    }
 }
 
 // compute_aij_pj, scalar path (TimeStepDFSPH.cpp:1370-1420):
-// V sum_j (a_i - a_j).gradW_ij + a_i . sum_b V_b gradW_ib
-template <class T> __device__ __forceinline__ T aij_pj_i(const DevParams<T> &P, const DevBufs<T> &B, uint32_t i)
+// V sum_j (a_i - a_j).gradW_ij + a_i . sum_b V_b gradW_ib, on every lane of the particle.
+// FP32: x_j and a_j from the packed record, one 256-bit load per neighbour.
+template <int LPP>
+__device__ __forceinline__ float aij_pj_g(const DevParams<float> &P, const DevBufs<float> &B, const SlotInfo &q)
 {
-    const v4_t<T> xi = ldv(B.x, i);
-    const V3<T> ai = xyz<T>(ldv(B.pa, i));
-    T accf = T(0);
-    struct XA {
-        v4_t<T> x, a;
-    };
-    const uint32_t nf = min(B.nf[i], P.capf);
-    nbr_loop<kUnroll>(list_ptr(B.lf, i, P.capf), nf, [&](uint32_t j) { return XA{ldv(B.x, j), ldv(B.pa, j)}; },
-                      [&](uint32_t, const XA &d) {
-                          const V3<T> r = diff3<T>(xi, d.x);
-                          const T c = grad_coef_d2(P.K, dot(r, r));
-                          accf += c * dot(sub(ai, xyz<T>(d.a)), r);
-                      });
-    return accf * P.V + dot(ai, xyz<T>(ldv(B.bg, i)));
+    float accf = 0.0f;
+    V3<float> ai = mk3<float>(0, 0, 0);
+    if (q.act) {
+        const F8 me = ld_f8(B.xa + 2 * (size_t)q.i);
+        const float4 xi = me.a;
+        ai = xyz<float>(me.b);
+        fluid_loop<LPP, kUnroll>(P, B, q.i, q.l, [&](uint32_t j) { return ld_f8(B.xa + 2 * (size_t)j); },
+                                 [&](uint32_t, const F8 &d) {
+                                     const V3<float> r = diff3<float>(xi, d.a);
+                                     const float c = grad_coef_d2(P.K, dot(r, r));
+                                     accf += c * dot(sub(ai, xyz<float>(d.b)), r);
+                                 });
+    }
+    accf = gsum<LPP>(accf);
+    return q.act ? accf * P.V + dot(ai, xyz<float>(ldv(B.bg, q.i))) : 0.0f;
+}
+template <int LPP>
+__device__ __forceinline__ double aij_pj_g(const DevParams<double> &P, const DevBufs<double> &B, const SlotInfo &q)
+{
+    double accf = 0.0;
+    V3<double> ai = mk3<double>(0, 0, 0);
+    if (q.act) {
+        const dquad xi = ldv(B.x, q.i);
+        ai = xyz<double>(ldv(B.pa, q.i));
+        struct XA {
+            dquad x, a;
+        };
+        fluid_loop<LPP, kUnroll>(P, B, q.i, q.l, [&](uint32_t j) { return XA{ldv(B.x, j), ldv(B.pa, j)}; },
+                                 [&](uint32_t, const XA &d) {
+                                     const V3<double> r = diff3<double>(xi, d.x);
+                                     const double c = grad_coef_d2(P.K, dot(r, r));
+                                     accf += c * dot(sub(ai, xyz<double>(d.a)), r);
+                                 });
+    }
+    accf = gsum<LPP>(accf);
+    return q.act ? accf * P.V + dot(ai, xyz<double>(ldv(B.bg, q.i))) : 0.0;
 }
 
 // Book one iteration of a scene's solver with average error avg and take its loop decision:
@@ -560,40 +680,42 @@ __device__ __forceinline__ void solver_decide(const DevParams<T> &P, StepScalars
 // divergenceSolveIteration (TimeStepDFSPH.cpp:621-706) / pressureSolveIteration (:544-619):
 // Jacobi update of kappa_v / kappa plus the FP64 average-error reduction and the
 // loop decision (the while conditions of :477 and :324), per scene.
-template <class T, bool DIV>
+template <class T, bool DIV, int LPP>
 __global__ void __launch_bounds__(kBlock) k_jacobi(DevParams<T> P, DevBufs<T> B, cudaGraphConditionalHandle handle,
                                                      int use_handle)
 {
     count_launch(&B.gsc->launches);
-    const SlotInfo q = slot_info(P);
+    const SlotInfo q = slot_info<LPP>(P);
     StepScalars *const sc = B.sc + q.s;
     const bool live = scene_live(P, sc);
     double err = 0.0;
-    if (q.act && live) {
-        const uint32_t i = q.i;
-        const double hd = DIV ? sc->dt : sc->dt_next;
-        const T h = (T)hd;
-        T apj = aij_pj_i(P, B, i);
-        T *kap = DIV ? B.kappa_v : B.kappa;
-        if (DIV) {
-            apj *= h;
-            const T si = -B.dadv[i];
-            T residuum = (si - apj) < T(0) ? (si - apj) : T(0);
-            if (B.nf[i] + B.nbn[i] < 20u) residuum = T(0);
-            const T fac = B.factor[i] * (T(1) / h);
-            const T kv = kap[i] - T(0.5) * (si - apj) * fac;
-            kap[i] = kv > T(0) ? kv : T(0);
-            store_w(B.xk, i, kap[i]);
-            err = -(double)P.rho0 * (double)residuum;
-        } else {
-            apj *= h * h;
-            const T si = T(1) - B.dadv[i];
-            const T residuum = (si - apj) < T(0) ? (si - apj) : T(0);
-            const T fac = B.factor[i] * (T(1) / (h * h));
-            const T kv = kap[i] - T(0.5) * (si - apj) * fac;
-            kap[i] = kv > T(0) ? kv : T(0);
-            store_w(B.xk, i, kap[i]);
-            err = -(double)P.rho0 * (double)residuum;
+    if (live) {
+        T apj = aij_pj_g<LPP>(P, B, q);
+        if (q.act && q.l == 0) {
+            const uint32_t i = q.i;
+            const double hd = DIV ? sc->dt : sc->dt_next;
+            const T h = (T)hd;
+            T *kap = DIV ? B.kappa_v : B.kappa;
+            if (DIV) {
+                apj *= h;
+                const T si = -B.dadv[i];
+                T residuum = (si - apj) < T(0) ? (si - apj) : T(0);
+                if (B.nf[i] + B.nbn[i] < 20u) residuum = T(0);
+                const T fac = B.factor[i] * (T(1) / h);
+                const T kv = kap[i] - T(0.5) * (si - apj) * fac;
+                kap[i] = kv > T(0) ? kv : T(0);
+                store_w(B.xk, i, kap[i]);
+                err = -(double)P.rho0 * (double)residuum;
+            } else {
+                apj *= h * h;
+                const T si = T(1) - B.dadv[i];
+                const T residuum = (si - apj) < T(0) ? (si - apj) : T(0);
+                const T fac = B.factor[i] * (T(1) / (h * h));
+                const T kv = kap[i] - T(0.5) * (si - apj) * fac;
+                kap[i] = kv > T(0) ? kv : T(0);
+                store_w(B.xk, i, kap[i]);
+                err = -(double)P.rho0 * (double)residuum;
+            }
         }
     }
     DSum<1> mine;
@@ -601,7 +723,7 @@ __global__ void __launch_bounds__(kBlock) k_jacobi(DevParams<T> P, DevBufs<T> B,
     const DevParams<T> &PP = P;
     const DevBufs<T> &BB = B;
     const uint32_t n_s = q.end - q.begin;
-    grid_sum_finalize<1>(mine, scene_reduce(P, B, q), [&](const DSum<1> &tot) {
+    grid_sum_finalize<1>(mine, scene_reduce<LPP>(P, B, q), [&](const DSum<1> &tot) {
         if (live) solver_decide<T, DIV>(PP, sc, n_s ? tot.v[0] / (double)n_s : 0.0);
         batch_decide(PP, BB, handle, use_handle);
     });
@@ -609,15 +731,15 @@ __global__ void __launch_bounds__(kBlock) k_jacobi(DevParams<T> P, DevBufs<T> B,
 
 // final pressure acceleration and velocity update of both solvers
 // (TimeStepDFSPH.cpp:500-520 and :345-363)
-template <class T, bool DIV>
+template <class T, bool DIV, int LPP>
 __global__ void __launch_bounds__(kBlock) k_solver_finalize(DevParams<T> P, DevBufs<T> B)
 {
     count_launch(&B.gsc->launches);
-    const SlotInfo q = slot_info(P);
-    if (!q.act) return;
+    const SlotInfo q = slot_info<LPP>(P);
+    const V3<T> a = pressure_accel_g<LPP>(P, B, q);
+    if (!q.act || q.l != 0) return;
     const StepScalars *sc = B.sc + q.s;
     const T h = (T)(DIV ? sc->dt : sc->dt_next);
-    const V3<T> a = pressure_accel_i(P, B, q.i);
     stv(B.pa, q.i, pack(a, T(0)));
     v4_t<T> v = ldv(B.v, q.i);
     v.x += h * a.x;
@@ -667,34 +789,34 @@ __global__ void k_loop_begin(StepScalars *sc, StepScalars *gsc, uint32_t nscenes
 // clearAccelerations (TimeStep.cpp:35-50) + XSPH::step scalar path (XSPH.cpp:138-211).
 // Also finishes the divergence solve's kappa_v *= h (TimeStepDFSPH.cpp:522-540),
 // which must wait until no thread reads kappa_v of its neighbours any more.
-template <class T>
+template <class T, int LPP>
 __global__ void __launch_bounds__(kBlock) k_xsph(DevParams<T> P, DevBufs<T> B, int div_on)
 {
     count_launch(&B.gsc->launches);
-    const SlotInfo q = slot_info(P);
-    if (!q.act) return;
-    const uint32_t i = q.i;
-    const T h = (T)B.sc[q.s].dt;
-    const T invH = T(1) / h;
-    const v4_t<T> xi = ldv(B.x, i);
-    const V3<T> vi = xyz<T>(ldv(B.v, i));
-    V3<T> ai = mk3<T>(P.gx, P.gy, P.gz);
-    if (P.xsph != T(0)) {
-        V3<T> acc = mk3<T>(0, 0, 0);
+    const SlotInfo q = slot_info<LPP>(P);
+    V3<T> acc = mk3<T>(0, 0, 0);
+    if (q.act && P.xsph != T(0)) {
+        const v4_t<T> xi = ldv(B.x, q.i);
+        const V3<T> vi = xyz<T>(ldv(B.v, q.i));
         struct XVR {
             v4_t<T> x, v;
             T rho;
         };
-        const uint32_t nf = min(B.nf[i], P.capf);
-        nbr_loop<kUnroll>(list_ptr(B.lf, i, P.capf), nf,
-                          [&](uint32_t j) { return XVR{ldv(B.x, j), ldv(B.v, j), B.density[j]}; },
-                          [&](uint32_t, const XVR &d) {
-                              const V3<T> r = diff3<T>(xi, d.x);
-                              const T w = (P.mass / d.rho) * kernel_W(P.K, dev_sqrt(dot(r, r)));
-                              acc = add(acc, scl(sub(vi, xyz<T>(d.v)), w));
-                          });
-        ai = sub(ai, scl(acc, invH * P.xsph));
+        fluid_loop<LPP, kUnroll>(P, B, q.i, q.l, [&](uint32_t j) { return XVR{ldv(B.x, j), ldv(B.v, j), B.density[j]}; },
+                                 [&](uint32_t, const XVR &d) {
+                                     const V3<T> r = diff3<T>(xi, d.x);
+                                     const T w = (P.mass / d.rho) * kernel_W(P.K, dev_sqrt(dot(r, r)));
+                                     acc = add(acc, scl(sub(vi, xyz<T>(d.v)), w));
+                                 });
     }
+    acc = gsum3<LPP>(acc);
+    if (!q.act || q.l != 0) return;
+    const uint32_t i = q.i;
+    const T h = (T)B.sc[q.s].dt;
+    const T invH = T(1) / h;
+    const V3<T> vi = xyz<T>(ldv(B.v, i));
+    V3<T> ai = mk3<T>(P.gx, P.gy, P.gz);
+    if (P.xsph != T(0)) ai = sub(ai, scl(acc, invH * P.xsph));
     if (P.xsph_b != T(0)) {
         // sum_b (rho0 V_b / rho_i) W_ib from the per-step boundary sum
         const T wsum = P.rho0 * (T)ldv(B.bg, i).w / B.density[i];
@@ -718,22 +840,20 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams<T> P, DevBufs<T> B, i
 // w_j travels in the w lane of the CG direction p (and of the warm start in cg_x), so one
 // 16-byte gather per neighbour gives both the vector and the weight.
 
-// Boundary term of the operator (mub != 0): sum_b d mub (rho0 V_b / rho_i) (v_i.x_ib) / (...) gradW_ib.
-template <class T>
-__device__ __forceinline__ V3<T> weiler_boundary(const DevParams<T> &P, const DevBufs<T> &B, uint32_t i, const v4_t<T> &xi,
-                                                 T rhoi, V3<T> vi)
+// Boundary term of the operator (mub != 0), this lane's share:
+// sum_b d mub (rho0 V_b / rho_i) (v_i.x_ib) / (...) gradW_ib.
+template <int LPP, class T>
+__device__ __forceinline__ V3<T> weiler_boundary(const DevParams<T> &P, const DevBufs<T> &B, const SlotInfo &q,
+                                                 const v4_t<T> &xi, T rhoi, V3<T> vi)
 {
     V3<T> acc = mk3<T>(0, 0, 0);
     const T eps2 = T(0.01) * P.h2;
-    const uint32_t nb = min(B.nbn[i], P.capb);
-    const uint32_t *Lb = list_ptr(B.lb, i, P.capb);
-    for (uint32_t k = 0; k < nb; k++) {
-        const v4_t<T> xj = ldv(B.xb, Lb[k * 32u]);
+    boundary_loop<LPP>(P, B, q.i, q.l, [&](uint32_t, const v4_t<T> &xj) {
         const V3<T> r = diff3<T>(xi, xj);
         const T r2 = dot(r, r);
         const T f = P.vd * P.mub * (P.rho0 * (T)xj.w / rhoi) * dot(vi, r) / (r2 + eps2);
         acc = add(acc, scl(r, grad_coef_d2(P.K, r2) * f));
-    }
+    });
     return acc;
 }
 
@@ -748,53 +868,59 @@ template <class T> __device__ __forceinline__ V3<T> sym_mul(const v4_t<T> &a, co
 // diagonal blocks (inverse taken in MatrixFreeSolver.h:231-244), b = v (computeRHS :1091-1254,
 // static boundary), warm start g = v + vDiff (already in cg_x), r = b - A g, p = M^-1 r, and
 // the first reductions of Eigen's conjugate_gradient (ConjugateGradient.h:29-70), one pass.
-template <class T>
+template <class T, int LPP>
 __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T> B, cudaGraphConditionalHandle handle,
                                                         int use_handle)
 {
     count_launch(&B.gsc->launches);
-    const SlotInfo q = slot_info(P);
+    const SlotInfo q = slot_info<LPP>(P);
     StepScalars *const sc = B.sc + q.s;
     DSum<3> mine;
     mine.v[0] = mine.v[1] = mine.v[2] = 0.0;
+    T m[6] = {0, 0, 0, 0, 0, 0};   // m00 m01 m02 m11 m12 m22
+    V3<T> acc = mk3<T>(0, 0, 0);
+    v4_t<T> xi{}, gi4{};
+    T rhoi = T(1);
     if (q.act) {
         const uint32_t i = q.i;
-        const v4_t<T> xi = ldv(B.x, i);
-        const T rhoi = B.density[i];
-        const T dt = (T)sc->dt;
+        xi = ldv(B.x, i);
+        rhoi = B.density[i];
         const T eps2 = T(0.01) * P.h2;
-        const v4_t<T> gi4 = ldv(B.cg_x, i);
+        gi4 = ldv(B.cg_x, i);
         const V3<T> gi = xyz<T>(gi4);
-        T m00 = 0, m01 = 0, m02 = 0, m11 = 0, m12 = 0, m22 = 0;
-        V3<T> acc = mk3<T>(0, 0, 0);
         struct XG {
             v4_t<T> x, g;
         };
-        const uint32_t nf = min(B.nf[i], P.capf);
-        nbr_loop<kUnroll>(list_ptr(B.lf, i, P.capf), nf, [&](uint32_t j) { return XG{ldv(B.x, j), ldv(B.cg_x, j)}; },
-                          [&](uint32_t, const XG &d) {
-                              const V3<T> r = diff3<T>(xi, d.x);
-                              const T r2 = dot(r, r);
-                              const T f = (T)d.g.w / (r2 + eps2) * grad_coef_d2(P.K, r2);
-                              m00 += f * r.x * r.x; m01 += f * r.x * r.y; m02 += f * r.x * r.z;
-                              m11 += f * r.y * r.y; m12 += f * r.y * r.z; m22 += f * r.z * r.z;
-                              acc = add(acc, scl(r, f * dot(sub(gi, xyz<T>(d.g)), r)));
-                          });
+        fluid_loop<LPP, kUnroll>(P, B, i, q.l, [&](uint32_t j) { return XG{ldv(B.x, j), ldv(B.cg_x, j)}; },
+                                 [&](uint32_t, const XG &d) {
+                                     const V3<T> r = diff3<T>(xi, d.x);
+                                     const T r2 = dot(r, r);
+                                     const T f = (T)d.g.w / (r2 + eps2) * grad_coef_d2(P.K, r2);
+                                     m[0] += f * r.x * r.x; m[1] += f * r.x * r.y; m[2] += f * r.x * r.z;
+                                     m[3] += f * r.y * r.y; m[4] += f * r.y * r.z; m[5] += f * r.z * r.z;
+                                     acc = add(acc, scl(r, f * dot(sub(gi, xyz<T>(d.g)), r)));
+                                 });
         if (P.mub != T(0)) {
-            const uint32_t nb = min(B.nbn[i], P.capb);
-            const uint32_t *Lb = list_ptr(B.lb, i, P.capb);
-            for (uint32_t k = 0; k < nb; k++) {
-                const v4_t<T> xj = ldv(B.xb, Lb[k * 32u]);
+            boundary_loop<LPP>(P, B, i, q.l, [&](uint32_t, const v4_t<T> &xj) {
                 const V3<T> r = diff3<T>(xi, xj);
                 const T r2 = dot(r, r);
                 const T f = P.vd * P.mub * (P.rho0 * (T)xj.w / rhoi) / (r2 + eps2) * grad_coef_d2(P.K, r2);
-                m00 += f * r.x * r.x; m01 += f * r.x * r.y; m02 += f * r.x * r.z;
-                m11 += f * r.y * r.y; m12 += f * r.y * r.z; m22 += f * r.z * r.z;
-            }
-            acc = add(acc, weiler_boundary(P, B, i, xi, rhoi, gi));
+                m[0] += f * r.x * r.x; m[1] += f * r.x * r.y; m[2] += f * r.x * r.z;
+                m[3] += f * r.y * r.y; m[4] += f * r.y * r.z; m[5] += f * r.z * r.z;
+            });
+            acc = add(acc, weiler_boundary<LPP>(P, B, q, xi, rhoi, gi));
         }
+    }
+#pragma unroll
+    for (int k = 0; k < 6; k++) m[k] = gsum<LPP>(m[k]);
+    acc = gsum3<LPP>(acc);
+    if (q.act && q.l == 0) {
+        const uint32_t i = q.i;
+        const T dt = (T)sc->dt;
+        const V3<T> gi = xyz<T>(gi4);
         const T s = dt / rhoi;
-        const T a = T(1) - s * m00, b = -s * m01, c = -s * m02, d = T(1) - s * m11, e = -s * m12, f = T(1) - s * m22;
+        const T a = T(1) - s * m[0], b = -s * m[1], c = -s * m[2], d = T(1) - s * m[3], e = -s * m[4],
+                f = T(1) - s * m[5];
         const T A00 = d * f - e * e, A01 = c * e - b * f, A02 = b * e - c * d;
         const T A11 = a * f - c * c, A12 = b * c - a * e, A22 = a * d - b * b;
         const T id = T(1) / (a * A00 + b * A01 + c * A02);
@@ -818,7 +944,7 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T
     const unsigned maxit = P.visc_max_iter;
     const DevParams<T> &PP = P;
     const DevBufs<T> &BB = B;
-    grid_sum_finalize<3>(mine, scene_reduce(P, B, q), [&](const DSum<3> &tot) {
+    grid_sum_finalize<3>(mine, scene_reduce<LPP>(P, B, q), [&](const DSum<3> &tot) {
         sc->cg_rhs2 = tot.v[0];
         sc->iters_cg = 0;
         sc->cg_err = 0.0;
@@ -846,42 +972,47 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T
 }
 
 // tmp = A p and p.tmp -> alpha (ConjugateGradient.h:74-76)
-template <class T>
+template <class T, int LPP>
 __global__ void __launch_bounds__(kBlock) k_cg_matvec(DevParams<T> P, DevBufs<T> B, cudaGraphConditionalHandle h,
                                                        int use_handle)
 {
     count_launch(&B.gsc->launches);
     loop_guard(B.gsc, P.visc_max_iter + 1, h, use_handle);
-    const SlotInfo q = slot_info(P);
+    const SlotInfo q = slot_info<LPP>(P);
     StepScalars *const sc = B.sc + q.s;
     const bool live = scene_live(P, sc);
     DSum<1> mine;
     mine.v[0] = 0.0;
-    if (q.act && live) {
-        const uint32_t i = q.i;
-        const v4_t<T> xi = ldv(B.x, i);
-        const T rhoi = B.density[i];
-        const T eps2 = T(0.01) * P.h2;
-        const V3<T> pi = xyz<T>(ldv(B.cg_p, i));
-        V3<T> acc = mk3<T>(0, 0, 0);
-        struct XP {
-            v4_t<T> x, p;
-        };
-        const uint32_t nf = min(B.nf[i], P.capf);
-        nbr_loop<kUnroll>(list_ptr(B.lf, i, P.capf), nf, [&](uint32_t j) { return XP{ldv(B.x, j), ldv(B.cg_p, j)}; },
-                          [&](uint32_t, const XP &d) {
-                              const V3<T> r = diff3<T>(xi, d.x);
-                              const T r2 = dot(r, r);
-                              const T f = (T)d.p.w / (r2 + eps2) * grad_coef_d2(P.K, r2);
-                              acc = add(acc, scl(r, f * dot(sub(pi, xyz<T>(d.p)), r)));
-                          });
-        if (P.mub != T(0)) acc = add(acc, weiler_boundary(P, B, i, xi, rhoi, pi));
-        const T dt = (T)sc->dt;
-        const V3<T> t = sub(pi, scl(acc, dt / rhoi));
-        stv(B.cg_t, i, pack(t, T(0)));
-        mine.v[0] = (double)dot(pi, t);
+    if (live) {   // uniform over the block
+        V3<T> acc = mk3<T>(0, 0, 0), pi = mk3<T>(0, 0, 0);
+        T rhoi = T(1);
+        if (q.act) {
+            const uint32_t i = q.i;
+            const v4_t<T> xi = ldv(B.x, i);
+            rhoi = B.density[i];
+            const T eps2 = T(0.01) * P.h2;
+            pi = xyz<T>(ldv(B.cg_p, i));
+            struct XP {
+                v4_t<T> x, p;
+            };
+            fluid_loop<LPP, kUnroll>(P, B, i, q.l, [&](uint32_t j) { return XP{ldv(B.x, j), ldv(B.cg_p, j)}; },
+                                     [&](uint32_t, const XP &d) {
+                                         const V3<T> r = diff3<T>(xi, d.x);
+                                         const T r2 = dot(r, r);
+                                         const T f = (T)d.p.w / (r2 + eps2) * grad_coef_d2(P.K, r2);
+                                         acc = add(acc, scl(r, f * dot(sub(pi, xyz<T>(d.p)), r)));
+                                     });
+            if (P.mub != T(0)) acc = add(acc, weiler_boundary<LPP>(P, B, q, xi, rhoi, pi));
+        }
+        acc = gsum3<LPP>(acc);
+        if (q.act && q.l == 0) {
+            const T dt = (T)sc->dt;
+            const V3<T> t = sub(pi, scl(acc, dt / rhoi));
+            stv(B.cg_t, q.i, pack(t, T(0)));
+            mine.v[0] = (double)dot(pi, t);
+        }
     }
-    grid_sum_finalize<1>(mine, scene_reduce(P, B, q), [&](const DSum<1> &tot) {
+    grid_sum_finalize<1>(mine, scene_reduce<LPP>(P, B, q), [&](const DSum<1> &tot) {
         if (live) sc->cg_alpha = sc->cg_absnew / tot.v[0];
     });
 }
@@ -1034,26 +1165,29 @@ __global__ void __launch_bounds__(kBlock) k_kick(DevParams<T> P, DevBufs<T> B)
 
 // computeDensityAdv (TimeStepDFSPH.cpp:1190-1243) and the pressure-solve set-up
 // (:264-309): advected density, warm-started kappa (USE_WARMSTART).
-template <class T>
+template <class T, int LPP>
 __global__ void __launch_bounds__(kBlock) k_press_init(DevParams<T> P, DevBufs<T> B)
 {
     count_launch(&B.gsc->launches);
-    const SlotInfo q = slot_info(P);
-    if (!q.act) return;
+    const SlotInfo q = slot_info<LPP>(P);
+    T accf = T(0);
+    V3<T> vi = mk3<T>(0, 0, 0);
+    if (q.act) {
+        const v4_t<T> xi = ldv(B.x, q.i);
+        vi = xyz<T>(ldv(B.v, q.i));
+        struct XV {
+            v4_t<T> x, v;
+        };
+        fluid_loop<LPP, kUnroll>(P, B, q.i, q.l, [&](uint32_t j) { return XV{ldv(B.x, j), ldv(B.v, j)}; },
+                                 [&](uint32_t, const XV &d) {
+                                     const V3<T> r = diff3<T>(xi, d.x);
+                                     accf += grad_coef_d2(P.K, dot(r, r)) * dot(sub(vi, xyz<T>(d.v)), r);
+                                 });
+    }
+    accf = gsum<LPP>(accf);
+    if (!q.act || q.l != 0) return;
     const uint32_t i = q.i;
     const T h = (T)B.sc[q.s].dt_next;
-    const v4_t<T> xi = ldv(B.x, i);
-    const V3<T> vi = xyz<T>(ldv(B.v, i));
-    T accf = T(0);
-    struct XV {
-        v4_t<T> x, v;
-    };
-    const uint32_t nf = min(B.nf[i], P.capf);
-    nbr_loop<kUnroll>(list_ptr(B.lf, i, P.capf), nf, [&](uint32_t j) { return XV{ldv(B.x, j), ldv(B.v, j)}; },
-                      [&](uint32_t, const XV &d) {
-                          const V3<T> r = diff3<T>(xi, d.x);
-                          accf += grad_coef_d2(P.K, dot(r, r)) * dot(sub(vi, xyz<T>(d.v)), r);
-                      });
     const T accb = dot(vi, xyz<T>(ldv(B.bg, i)));
     const T dadv = B.density[i] / P.rho0 + h * (accf * P.V + accb);
     B.dadv[i] = dadv;
@@ -1120,37 +1254,47 @@ __global__ void __launch_bounds__(kBlock) k_integrate(DevParams<T> P, DevBufs<T>
 // neighbourhood mean, followed by the weighted means of f0..f4 over i and its fluid
 // neighbours (sum_j W_ij f_j / sum_j W_ij, self weight W(0)).  Runs before the pressure
 // solve overwrites kappa, so B.kappa still holds the previous step's stored value.
-template <class T>
+template <class T, int LPP>
 __global__ void __launch_bounds__(kBlock) k_features(DevParams<T> P, DevBufs<T> B)
 {
     count_launch(&B.gsc->launches);
-    const SlotInfo q = slot_info(P);
-    if (!q.act) return;
+    const SlotInfo q = slot_info<LPP>(P);
+    float m[5] = {0, 0, 0, 0, 0};
+    float wsum = 0.0f, km = 0.0f;
+    if (q.act) {
+        const v4_t<T> xi = ldv(B.x, q.i);
+        struct XF {
+            v4_t<T> x;
+            float4 a;
+            float b, k;
+        };
+        fluid_loop<LPP, kUnroll>(P, B, q.i, q.l,
+                                 [&](uint32_t j) {
+                                     return XF{ldv(B.x, j), *reinterpret_cast<const float4 *>(B.feat + (size_t)j * 8),
+                                               B.feat[(size_t)j * 8 + 4], (float)B.kappa[j]};
+                                 },
+                                 [&](uint32_t, const XF &d) {
+                                     const V3<T> r = diff3<T>(xi, d.x);
+                                     const float w = (float)kernel_W(P.K, dev_sqrt(dot(r, r)));
+                                     m[0] += w * d.a.x; m[1] += w * d.a.y; m[2] += w * d.a.z; m[3] += w * d.a.w;
+                                     m[4] += w * d.b;
+                                     km += w * d.k;
+                                     wsum += w;
+                                 });
+    }
+#pragma unroll
+    for (int k = 0; k < 5; k++) m[k] = gsum<LPP>(m[k]);
+    wsum = gsum<LPP>(wsum);
+    km = gsum<LPP>(km);
+    if (!q.act || q.l != 0) return;
     const uint32_t i = q.i;
-    const v4_t<T> xi = ldv(B.x, i);
     const float4 f0 = *reinterpret_cast<const float4 *>(B.feat + (size_t)i * 8);
     const float f4 = B.feat[(size_t)i * 8 + 4];
     const float ki = (float)B.kappa[i];
     const float w0 = (float)P.K.w0;
-    float m[5] = {w0 * f0.x, w0 * f0.y, w0 * f0.z, w0 * f0.w, w0 * f4};
-    float wsum = w0, km = w0 * ki;
-    struct XF {
-        v4_t<T> x;
-        float4 a;
-        float b, k;
-    };
-    nbr_loop<kUnroll>(list_ptr(B.lf, i, P.capf), min(B.nf[i], P.capf),
-                      [&](uint32_t j) {
-                          return XF{ldv(B.x, j), *reinterpret_cast<const float4 *>(B.feat + (size_t)j * 8),
-                                    B.feat[(size_t)j * 8 + 4], (float)B.kappa[j]};
-                      },
-                      [&](uint32_t, const XF &d) {
-                          const V3<T> r = diff3<T>(xi, d.x);
-                          const float w = (float)kernel_W(P.K, dev_sqrt(dot(r, r)));
-                          m[0] += w * d.a.x; m[1] += w * d.a.y; m[2] += w * d.a.z; m[3] += w * d.a.w; m[4] += w * d.b;
-                          km += w * d.k;
-                          wsum += w;
-                      });
+    m[0] += w0 * f0.x; m[1] += w0 * f0.y; m[2] += w0 * f0.z; m[3] += w0 * f0.w; m[4] += w0 * f4;
+    wsum += w0;
+    km += w0 * ki;
     float *X = B.mlp_x + (size_t)i * 10;
     X[0] = f0.x; X[1] = f0.y; X[2] = f0.z; X[4] = f4;
     X[3] = km > 0.0f ? ki / km * wsum : 0.0f;   // kappa_i / (weighted mean of kappa)
@@ -1179,34 +1323,39 @@ __global__ void __launch_bounds__(kBlock) k_ws_kappa(DevParams<T> P, DevBufs<T> 
 
 // Pressure accelerations of both candidate warm starts: classic (xk.w) into pa, predicted (kl)
 // into pa2 (the computePressureAccel sum of TimeStepDFSPH.cpp:1299-1367 for each).
-template <class T>
+template <class T, int LPP>
 __global__ void __launch_bounds__(kBlock) k_ws_accel2(DevParams<T> P, DevBufs<T> B)
 {
     count_launch(&B.gsc->launches);
-    const SlotInfo q = slot_info(P);
-    if (!q.act) return;
-    const uint32_t i = q.i;
-    const v4_t<T> xi = ldv(B.xk, i);
-    const T pc = (T)xi.w, pl = B.kl[i];
+    const SlotInfo q = slot_info<LPP>(P);
     V3<T> ac = mk3<T>(0, 0, 0), al = mk3<T>(0, 0, 0);
-    struct XK {
-        v4_t<T> x;
-        T kl;
-    };
-    nbr_loop<kUnroll>(list_ptr(B.lf, i, P.capf), min(B.nf[i], P.capf), [&](uint32_t j) { return XK{ldv(B.xk, j), B.kl[j]}; },
-                      [&](uint32_t, const XK &d) {
-                          const V3<T> r = diff3<T>(xi, d.x);
-                          const T c = grad_coef_d2(P.K, dot(r, r));
-                          const T sc_ = pc + (T)d.x.w, sl = pl + d.kl;
-                          if (fabs(sc_) > P.eps) ac = add(ac, scl(r, c * sc_));
-                          if (fabs(sl) > P.eps) al = add(al, scl(r, c * sl));
-                      });
-    const V3<T> gb = xyz<T>(ldv(B.bg, i));
+    T pc = T(0), pl = T(0);
+    if (q.act) {
+        const v4_t<T> xi = ldv(B.xk, q.i);
+        pc = (T)xi.w;
+        pl = B.kl[q.i];
+        struct XK {
+            v4_t<T> x;
+            T kl;
+        };
+        fluid_loop<LPP, kUnroll>(P, B, q.i, q.l, [&](uint32_t j) { return XK{ldv(B.xk, j), B.kl[j]}; },
+                                 [&](uint32_t, const XK &d) {
+                                     const V3<T> r = diff3<T>(xi, d.x);
+                                     const T c = grad_coef_d2(P.K, dot(r, r));
+                                     const T sc_ = pc + (T)d.x.w, sl = pl + d.kl;
+                                     if (fabs(sc_) > P.eps) ac = add(ac, scl(r, c * sc_));
+                                     if (fabs(sl) > P.eps) al = add(al, scl(r, c * sl));
+                                 });
+    }
+    ac = gsum3<LPP>(ac);
+    al = gsum3<LPP>(al);
+    if (!q.act || q.l != 0) return;
+    const V3<T> gb = xyz<T>(ldv(B.bg, q.i));
     V3<T> a1 = scl(ac, -P.V), a2 = scl(al, -P.V);
     if (fabs(pc) > P.eps) a1 = sub(a1, scl(gb, pc));
     if (fabs(pl) > P.eps) a2 = sub(a2, scl(gb, pl));
-    stv(B.pa, i, pack(a1, T(0)));
-    stv(B.pa2, i, pack(a2, T(0)));
+    stv(B.pa, q.i, pack(a1, T(0)));
+    stv(B.pa2, q.i, pack(a2, T(0)));
 }
 
 // One Jacobi iteration of the solver (TimeStepDFSPH.cpp:621-706 divergence, :544-619
@@ -1217,31 +1366,36 @@ __global__ void __launch_bounds__(kBlock) k_ws_accel2(DevParams<T> P, DevBufs<T>
 // gate iterations of the chosen candidate and takes the loop decision, so the solver loop
 // continues with iteration sweeps + 1.  With one sweep the errors compared are the
 // candidates' initial residuals.
-template <class T, bool DIV, bool LAST>
+template <class T, bool DIV, bool LAST, int LPP>
 __global__ void __launch_bounds__(kBlock) k_ws_sweep(DevParams<T> P, DevBufs<T> B, unsigned sweeps,
                                                       cudaGraphConditionalHandle handle, int use_handle)
 {
     count_launch(&B.gsc->launches);
-    const SlotInfo q = slot_info(P);
+    const SlotInfo q = slot_info<LPP>(P);
     StepScalars *const sc = B.sc + q.s;
     DSum<2> mine;
     mine.v[0] = mine.v[1] = 0.0;
+    T s1 = T(0), s2 = T(0);
+    V3<T> a1 = mk3<T>(0, 0, 0), a2 = mk3<T>(0, 0, 0);
     if (q.act) {
-        const uint32_t i = q.i;
-        const v4_t<T> xi = ldv(B.x, i);
-        const V3<T> a1 = xyz<T>(ldv(B.pa, i)), a2 = xyz<T>(ldv(B.pa2, i));
-        T s1 = T(0), s2 = T(0);
+        const v4_t<T> xi = ldv(B.x, q.i);
+        a1 = xyz<T>(ldv(B.pa, q.i));
+        a2 = xyz<T>(ldv(B.pa2, q.i));
         struct XA {
             v4_t<T> x, a, b;
         };
-        nbr_loop<kUnroll>(list_ptr(B.lf, i, P.capf), min(B.nf[i], P.capf),
-                          [&](uint32_t j) { return XA{ldv(B.x, j), ldv(B.pa, j), ldv(B.pa2, j)}; },
-                          [&](uint32_t, const XA &d) {
-                              const V3<T> r = diff3<T>(xi, d.x);
-                              const T c = grad_coef_d2(P.K, dot(r, r));
-                              s1 += c * dot(sub(a1, xyz<T>(d.a)), r);
-                              s2 += c * dot(sub(a2, xyz<T>(d.b)), r);
-                          });
+        fluid_loop<LPP, kUnroll>(P, B, q.i, q.l, [&](uint32_t j) { return XA{ldv(B.x, j), ldv(B.pa, j), ldv(B.pa2, j)}; },
+                                 [&](uint32_t, const XA &d) {
+                                     const V3<T> r = diff3<T>(xi, d.x);
+                                     const T c = grad_coef_d2(P.K, dot(r, r));
+                                     s1 += c * dot(sub(a1, xyz<T>(d.a)), r);
+                                     s2 += c * dot(sub(a2, xyz<T>(d.b)), r);
+                                 });
+    }
+    s1 = gsum<LPP>(s1);
+    s2 = gsum<LPP>(s2);
+    if (q.act && q.l == 0) {
+        const uint32_t i = q.i;
         const V3<T> gb = xyz<T>(ldv(B.bg, i));
         T ap1 = s1 * P.V + dot(a1, gb), ap2 = s2 * P.V + dot(a2, gb);
         T si, fac;
@@ -1279,7 +1433,7 @@ __global__ void __launch_bounds__(kBlock) k_ws_sweep(DevParams<T> P, DevBufs<T> 
     const uint32_t n_s = q.end - q.begin;
     const DevParams<T> &PP = P;
     const DevBufs<T> &BB = B;
-    grid_sum_finalize<2>(mine, scene_reduce(P, B, q), [&](const DSum<2> &tot) {
+    grid_sum_finalize<2>(mine, scene_reduce<LPP>(P, B, q), [&](const DSum<2> &tot) {
         const int k = DIV ? 0 : 1;
         const double inv = n_s ? 1.0 / (double)n_s : 0.0;
         sc->ws_rc[k] = tot.v[0] * inv;
@@ -1521,21 +1675,21 @@ __global__ void k_upload_field(DevParams<T> P, DevBufs<T> B, int field, const vo
     }
 }
 
-// Neighbour lists to particle ids, CSR (debug / oracle comparison path)
+// Neighbour lists to particle ids, CSR (debug / oracle comparison path).  kind 0: fluid
+// list in the layout of lpp_log2, kind 1: boundary list.
 __global__ void k_lists_to_ids(const uint32_t *__restrict__ list, const uint32_t *__restrict__ cnt, uint32_t cap,
                                const uint32_t *__restrict__ id, const uint32_t *__restrict__ inv,
-                               const uint32_t *__restrict__ bid, int kind, const uint32_t *__restrict__ offsets,
-                               uint32_t *__restrict__ out, uint32_t n)
+                               const uint32_t *__restrict__ bid, int kind, uint32_t lpp_log2,
+                               const uint32_t *__restrict__ offsets, uint32_t *__restrict__ out, uint32_t n)
 {
     const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;   // particle id
     if (d >= n) return;
     const uint32_t k = inv[d];
     const uint32_t c = min(cnt[k], cap);
-    const uint32_t *L = list_ptr(list, k, cap);
     uint32_t *o = out + offsets[d];
     for (uint32_t m = 0; m < c; m++) {
-        const uint32_t j = L[m * 32u];
-        o[m] = kind == 0 ? id[j] : bid[j];
+        if (kind == 0) o[m] = id[list[fl_index(k, m, cap, lpp_log2)]];
+        else o[m] = bid[list_ptr(list, k, cap)[m * 32u]];
     }
 }
 
@@ -1550,8 +1704,20 @@ __global__ void k_delay(unsigned ns)
 }  // namespace
 
 // ==========================================================================
-// launchers: every particle kernel runs over all slots of all scenes
+// launchers: every particle kernel runs over all slots of all scenes; the neighbour
+// passes with the context's lanes per particle (1 << P.lpp_log2)
 // ==========================================================================
+inline unsigned grid_lpp(uint32_t n, int lpp) { return (n + kBlock / lpp - 1) / (kBlock / lpp); }
+
+#define LPP_DISPATCH(P, CALL)                                                                                      \
+    do {                                                                                                           \
+        switch ((P).lpp_log2) {                                                                                    \
+        case 0: { constexpr int L = 1; CALL; } break;                                                              \
+        case 1: { constexpr int L = 2; CALL; } break;                                                              \
+        default: { constexpr int L = 4; CALL; } break;                                                             \
+        }                                                                                                          \
+    } while (0)
+
 template <class T> void launch_keys(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {
     if (P.np) k_keys<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
@@ -1572,21 +1738,23 @@ template <class T> void launch_pressure_accel(const DevParams<T> &P, const DevBu
                                               cudaGraphConditionalHandle h, bool use_handle)
 {
     const unsigned limit = (div ? P.max_iter_v : P.max_iter) + 1;
-    if (P.np) k_pressure_accel<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B, limit, h, use_handle ? 1 : 0);
+    if (P.np)
+        LPP_DISPATCH(P, (k_pressure_accel<T, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B, limit, h, use_handle ? 1 : 0)));
 }
 template <class T>
 void launch_jacobi(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaGraphConditionalHandle h, bool use_handle,
                    cudaStream_t s)
 {
     if (!P.np) return;
-    if (div) k_jacobi<T, true><<<grid_for(P.np), kBlock, 0, s>>>(P, B, h, use_handle ? 1 : 0);
-    else k_jacobi<T, false><<<grid_for(P.np), kBlock, 0, s>>>(P, B, h, use_handle ? 1 : 0);
+    const int uh = use_handle ? 1 : 0;
+    if (div) LPP_DISPATCH(P, (k_jacobi<T, true, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B, h, uh)));
+    else LPP_DISPATCH(P, (k_jacobi<T, false, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B, h, uh)));
 }
 template <class T> void launch_solver_finalize(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s)
 {
     if (!P.np) return;
-    if (div) k_solver_finalize<T, true><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
-    else k_solver_finalize<T, false><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
+    if (div) LPP_DISPATCH(P, (k_solver_finalize<T, true, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B)));
+    else LPP_DISPATCH(P, (k_solver_finalize<T, false, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B)));
 }
 template <class T> void launch_step_begin(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {
@@ -1598,18 +1766,18 @@ template <class T> void launch_loop_begin(const DevParams<T> &P, const DevBufs<T
 }
 template <class T> void launch_xsph(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {
-    if (P.np) k_xsph<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B, P.div_on);
+    if (P.np) LPP_DISPATCH(P, (k_xsph<T, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B, P.div_on)));
 }
 template <class T>
 void launch_visc_setup(const DevParams<T> &P, const DevBufs<T> &B, cudaGraphConditionalHandle h, bool use_handle,
                        cudaStream_t s)
 {
-    if (P.np) k_visc_setup<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B, h, use_handle ? 1 : 0);
+    if (P.np) LPP_DISPATCH(P, (k_visc_setup<T, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B, h, use_handle ? 1 : 0)));
 }
 template <class T> void launch_cg_matvec(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s,
                                          cudaGraphConditionalHandle h, bool use_handle)
 {
-    if (P.np) k_cg_matvec<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B, h, use_handle ? 1 : 0);
+    if (P.np) LPP_DISPATCH(P, (k_cg_matvec<T, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B, h, use_handle ? 1 : 0)));
 }
 template <class T>
 void launch_cg_update(const DevParams<T> &P, const DevBufs<T> &B, cudaGraphConditionalHandle h, bool use_handle,
@@ -1627,7 +1795,7 @@ template <class T> void launch_kick(const DevParams<T> &P, const DevBufs<T> &B, 
 }
 template <class T> void launch_press_init(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {
-    if (P.np) k_press_init<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
+    if (P.np) LPP_DISPATCH(P, (k_press_init<T, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B)));
 }
 template <class T> void launch_integrate(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {
@@ -1635,7 +1803,7 @@ template <class T> void launch_integrate(const DevParams<T> &P, const DevBufs<T>
 }
 template <class T> void launch_features(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {
-    if (P.np) k_features<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
+    if (P.np) LPP_DISPATCH(P, (k_features<T, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B)));
 }
 template <class T>
 void launch_warmstart_select(const DevParams<T> &P, const DevBufs<T> &B, bool div, unsigned sweeps,
@@ -1647,17 +1815,21 @@ void launch_warmstart_select(const DevParams<T> &P, const DevBufs<T> &B, bool di
     if (div) {
         k_ws_kappa<T, true><<<g, kBlock, 0, s>>>(P, B);
         for (unsigned k = 1; k <= sweeps; k++) {
-            k_ws_accel2<T><<<g, kBlock, 0, s>>>(P, B);
-            if (k < sweeps) k_ws_sweep<T, true, false><<<g, kBlock, 0, s>>>(P, B, sweeps, h, uh);
-            else k_ws_sweep<T, true, true><<<g, kBlock, 0, s>>>(P, B, sweeps, h, uh);
+            LPP_DISPATCH(P, (k_ws_accel2<T, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B)));
+            if (k < sweeps)
+                LPP_DISPATCH(P, (k_ws_sweep<T, true, false, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B, sweeps, h, uh)));
+            else
+                LPP_DISPATCH(P, (k_ws_sweep<T, true, true, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B, sweeps, h, uh)));
         }
         k_ws_apply<T, true><<<g, kBlock, 0, s>>>(P, B);
     } else {
         k_ws_kappa<T, false><<<g, kBlock, 0, s>>>(P, B);
         for (unsigned k = 1; k <= sweeps; k++) {
-            k_ws_accel2<T><<<g, kBlock, 0, s>>>(P, B);
-            if (k < sweeps) k_ws_sweep<T, false, false><<<g, kBlock, 0, s>>>(P, B, sweeps, h, uh);
-            else k_ws_sweep<T, false, true><<<g, kBlock, 0, s>>>(P, B, sweeps, h, uh);
+            LPP_DISPATCH(P, (k_ws_accel2<T, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B)));
+            if (k < sweeps)
+                LPP_DISPATCH(P, (k_ws_sweep<T, false, false, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B, sweeps, h, uh)));
+            else
+                LPP_DISPATCH(P, (k_ws_sweep<T, false, true, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B, sweeps, h, uh)));
         }
         k_ws_apply<T, false><<<g, kBlock, 0, s>>>(P, B);
     }
@@ -1707,9 +1879,10 @@ template <class T> void launch_inverse_perm(const DevParams<T> &P, const uint32_
 void launch_delay(cudaStream_t s, unsigned ns) { k_delay<<<1, 32, 0, s>>>(ns); }
 
 void launch_lists_to_ids(const uint32_t *list, const uint32_t *cnt, uint32_t cap, const uint32_t *id, const uint32_t *inv,
-                         const uint32_t *bid, int kind, const uint32_t *offsets, uint32_t *out, uint32_t n, cudaStream_t s)
+                         const uint32_t *bid, int kind, uint32_t lpp_log2, const uint32_t *offsets, uint32_t *out,
+                         uint32_t n, cudaStream_t s)
 {
-    if (n) k_lists_to_ids<<<grid_for(n), kBlock, 0, s>>>(list, cnt, cap, id, inv, bid, kind, offsets, out, n);
+    if (n) k_lists_to_ids<<<grid_for(n), kBlock, 0, s>>>(list, cnt, cap, id, inv, bid, kind, lpp_log2, offsets, out, n);
 }
 
 #define SPHGB_INSTANTIATE(T)                                                                                        \

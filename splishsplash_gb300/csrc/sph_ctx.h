@@ -84,6 +84,8 @@ template <class T> struct DevParams {
     uint32_t nreal;               // fluid particles of all scenes
     uint32_t nb;                  // boundary particles of all scenes
     uint32_t capf, capb;
+    uint32_t lpp_log2;            // lanes per particle of the neighbour passes (1, 2 or 4) = 1 << lpp_log2;
+                                  // also fixes the layout of the fluid lists
 };
 
 // Scene descriptor by value: a kernel parameter for a single scene, a (cached) global load otherwise.
@@ -107,6 +109,8 @@ template <class T> struct DevBufs {
     uint32_t *id2;
     // per-step fields
     v4 *a, *pa;
+    float4 *xa;                  // FP32 solver loops: (x_i, a_i) as one 32-byte record per particle,
+                                 // written by the pressure-acceleration pass, read by the Jacobi pass
     v4 *xk;                      // x_i with the running solver's kappa_i in w (one gather per pair)
     v4 *bg;                      // per-particle boundary sums: xyz = sum_b V_b gradW_ib, w = sum_b V_b W_ib
     T *density, *factor, *dadv;
@@ -184,8 +188,8 @@ template <class T> void launch_init_state(const DevParams<T> &P, const DevBufs<T
                                           const double *v, const uint32_t *id, cudaStream_t s);
 template <class T> void launch_inverse_perm(const DevParams<T> &P, const uint32_t *id, uint32_t *inv, cudaStream_t s);
 void launch_lists_to_ids(const uint32_t *list, const uint32_t *cnt, uint32_t cap, const uint32_t *id,
-                         const uint32_t *inv, const uint32_t *bid, int kind, const uint32_t *offsets,
-                         uint32_t *out, uint32_t n, cudaStream_t s);
+                         const uint32_t *inv, const uint32_t *bid, int kind, uint32_t lpp_log2,
+                         const uint32_t *offsets, uint32_t *out, uint32_t n, cudaStream_t s);
 void launch_delay(cudaStream_t s, unsigned ns);
 
 // radix sort of (key, value) pairs, LSD, 8-bit digits, stable.  keys/vals are

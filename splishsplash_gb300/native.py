@@ -119,7 +119,7 @@ EXPORTS = [
     "sphgb_set_time", "sphgb_step", "sphgb_sync", "sphgb_download", "sphgb_upload_field", "sphgb_neighbors",
     "sphgb_num_particles", "sphgb_get_stream", "sphgb_profile_enable", "sphgb_profile_reset", "sphgb_profile_read",
     "sphgb_set_warmstart_mlp", "sphgb_set_feature_output", "sphgb_upload_scenes", "sphgb_num_scenes",
-    "sphgb_scene_stats", "sphgb_set_warmstart_gate",
+    "sphgb_scene_stats", "sphgb_set_warmstart_gate", "sphgb_set_lanes_per_particle", "sphgb_get_lanes_per_particle",
 ]
 
 _lib = None
@@ -168,6 +168,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.sphgb_num_scenes.argtypes = [vp, ctypes.POINTER(u32)]
     L.sphgb_scene_stats.argtypes = [vp, u32, u32, ctypes.POINTER(Stats)]
     L.sphgb_set_warmstart_gate.argtypes = [vp, u32, u32]
+    L.sphgb_set_lanes_per_particle.argtypes = [vp, u32]
+    L.sphgb_get_lanes_per_particle.argtypes = [vp, ctypes.POINTER(u32), vp]
     L.sphgb_profile_enable.argtypes = [vp, i32]
     L.sphgb_profile_reset.argtypes = [vp]
     L.sphgb_profile_read.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_uint64),
@@ -435,6 +437,17 @@ class Context:
         """Jacobi iterations both warm-start candidates run before they are compared, per
         solver (0: default, 1 divergence / max(minIterations, 4) pressure; 1: initial residuals)."""
         self._check(self.L.sphgb_set_warmstart_gate(self.h, int(div_sweeps), int(pressure_sweeps)))
+
+    def set_lanes_per_particle(self, lanes: int = 0):
+        """Lanes per particle of the neighbour passes (1, 2, 4; 0 = autotune on the next step)."""
+        self._check(self.L.sphgb_set_lanes_per_particle(self.h, int(lanes)))
+
+    def lanes_per_particle(self):
+        """(lanes in use, autotuner trial step times in ms for 1, 2, 4 lanes)."""
+        k = ctypes.c_uint32()
+        t = np.zeros(3, np.float32)
+        self._check(self.L.sphgb_get_lanes_per_particle(self.h, ctypes.byref(k), _p(t)))
+        return int(k.value), [float(v) for v in t]
 
     def set_feature_output(self, on: bool = True):
         self._check(self.L.sphgb_set_feature_output(self.h, int(on)))

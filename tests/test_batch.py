@@ -25,19 +25,21 @@ def _batch(viscosity=False):
     return sc
 
 
-def _run_single(sc, steps, use_graph=True):
+def _run_single(sc, steps, use_graph=True, lanes=1):
     ts = TimeStepDFSPH(sc, use_graph=use_graph)
+    ts.ctx.set_lanes_per_particle(lanes)   # same summation order as the batch
     stats = [ts.step() for _ in range(steps)]
     out = {f: ts.getFluidModel().getFieldBuffer(f, np.float64) for f in FIELDS}
     ts.close()
     return stats, out
 
 
-@pytest.mark.parametrize("viscosity", [False, True])
-def test_batch_matches_separate_contexts_bitwise(viscosity):
+@pytest.mark.parametrize("viscosity,lanes", [(False, 1), (True, 1), (False, 4), (True, 2)])
+def test_batch_matches_separate_contexts_bitwise(viscosity, lanes):
     sc = _batch(viscosity)
     steps = 12
     b = BatchedTimeStepDFSPH(sc, use_graph=True)
+    b.ctx.set_lanes_per_particle(lanes)
     for _ in range(steps):
         agg = b.step()
     per = b.scene_stats()
@@ -45,7 +47,7 @@ def test_batch_matches_separate_contexts_bitwise(viscosity):
     b.close()
     iters = []
     for k, s in enumerate(sc):
-        stats, ref = _run_single(s, steps)
+        stats, ref = _run_single(s, steps, lanes=lanes)
         st = stats[-1]
         for key in ("iterations", "iterations_v", "visco_iterations", "dt_used", "dt_next", "time",
                     "avg_density_err", "avg_density_err_v", "max_fluid_neighbors", "max_boundary_neighbors"):
@@ -63,6 +65,7 @@ def test_batch_host_loops_match_graph():
     out = []
     for g in (True, False):
         b = BatchedTimeStepDFSPH(sc, use_graph=g)
+        b.ctx.set_lanes_per_particle(4)
         for _ in range(8):
             b.step()
         out.append((b.scene_stats(), b.ctx.download("position"), b.ctx.download("velocity")))

@@ -163,11 +163,13 @@ def test_fp64_device_path_matches_oracle_tightly():
     ts.close()
 
 
-def test_graph_and_host_loops_agree_bitwise():
+@pytest.mark.parametrize("lanes", [1, 4])
+def test_graph_and_host_loops_agree_bitwise(lanes):
     sc = scenes.small_block(counts=(10, 12, 10), box=(0.8, 1.0, 0.8), viscosity=True).as_float32()
     outs = []
     for graph in (False, True):
         ts = TimeStepDFSPH(sc, use_graph=graph)
+        ts.ctx.set_lanes_per_particle(lanes)   # the summation order depends on the lanes per particle
         stats = [ts.step() for _ in range(25)]
         m = ts.getFluidModel()
         outs.append((m.getFieldBuffer("position"), m.getFieldBuffer("velocity"), m.getFieldBuffer("p / rho^2"),
@@ -185,6 +187,7 @@ def test_repeat_runs_are_deterministic():
     res = []
     for _ in range(2):
         ts = TimeStepDFSPH(sc, use_graph=True)
+        ts.ctx.set_lanes_per_particle(2)
         for _ in range(20):
             ts.step()
         res.append(ts.getFluidModel().getFieldBuffer("position"))

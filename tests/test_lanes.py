@@ -1,0 +1,70 @@
+"""Lanes per particle of the neighbour passes: every variant (1, 2, 4 lanes, with the matching
+fluid-list layout) gives the same neighbour sets and the same step within FP32 summation-order
+tolerance, and the autotuner's trial steps leave no trace in the simulation."""
+import numpy as np
+import pytest
+
+from splishsplash_gb300 import scenes
+from splishsplash_gb300.dfsph import BatchedTimeStepDFSPH, TimeStepDFSPH
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(sc, lanes, steps, viscosity_fields=False):
+    ts = TimeStepDFSPH(sc)
+    ts.ctx.set_lanes_per_particle(lanes)
+    st = [ts.step() for _ in range(steps)]
+    m = ts.getFluidModel()
+    out = {f: m.getFieldBuffer(f) for f in ("position", "velocity", "density", "factor", "p / rho^2", "p_v / rho^2")}
+    nbr = ts.ctx.neighbors(0)
+    assert ts.ctx.lanes_per_particle()[0] == lanes
+    ts.close()
+    return st, out, nbr
+
+
+@pytest.mark.parametrize("viscosity", [False, True])
+def test_lane_variants_agree(viscosity):
+    sc = scenes.small_block(counts=(12, 12, 12), box=(0.8, 1.0, 0.8), viscosity=viscosity)
+    ref_st, ref, ref_nbr = _run(sc, 1, 3)
+    for lanes in (2, 4):
+        st, out, nbr = _run(sc, lanes, 3)
+        off0, idx0 = ref_nbr
+        off1, idx1 = nbr
+        np.testing.assert_array_equal(off0, off1)
+        for i in range(sc.n):
+            np.testing.assert_array_equal(np.sort(idx0[off0[i]:off0[i + 1]]), np.sort(idx1[off1[i]:off1[i + 1]]))
+        np.testing.assert_allclose(out["density"], ref["density"], rtol=2e-6)
+        np.testing.assert_allclose(out["velocity"], ref["velocity"], rtol=0, atol=1e-5)
+        np.testing.assert_allclose(out["position"], ref["position"], rtol=0, atol=1e-7)
+        assert [s["iterations"] for s in st] == [s["iterations"] for s in ref_st]
+
+
+def test_autotune_trials_are_undone():
+    sc = scenes.small_block(counts=(14, 14, 14), box=(0.9, 1.0, 0.9), velocity=(0.5, 0.0, 0.0))
+    a = TimeStepDFSPH(sc)
+    sa = [a.step() for _ in range(10)]
+    lanes, trial_ms = a.ctx.lanes_per_particle()
+    assert lanes in (1, 2, 4) and all(t > 0 for t in trial_ms)
+    b = TimeStepDFSPH(sc)
+    b.ctx.set_lanes_per_particle(lanes)
+    sb = [b.step() for _ in range(10)]
+    for f in ("position", "velocity", "p / rho^2"):
+        np.testing.assert_array_equal(a.getFluidModel().getFieldBuffer(f), b.getFluidModel().getFieldBuffer(f))
+    for x, y in zip(sa, sb):
+        assert x["iterations"] == y["iterations"] and x["time"] == y["time"] and x["dt_used"] == y["dt_used"]
+    a.close()
+    b.close()
+
+
+def test_batch_lane_variants_agree():
+    ens = scenes.ensemble(num_scenes=5, seed=9, n_min=2000, n_max=5000)
+    res = []
+    for lanes in (1, 4):
+        b = BatchedTimeStepDFSPH(ens)
+        b.ctx.set_lanes_per_particle(lanes)
+        for _ in range(3):
+            b.step()
+        res.append((b.scene_stats(), b.ctx.download("density")))
+        b.close()
+    assert [s["iterations"] for s in res[0][0]] == [s["iterations"] for s in res[1][0]]
+    np.testing.assert_allclose(res[0][1], res[1][1], rtol=2e-6)
