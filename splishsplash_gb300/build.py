@@ -18,6 +18,9 @@ CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "_lib")
 OBJDIR = os.path.join(PKG, "_build")
 LIB = os.path.join(LIBDIR, "libsphgb300.so")
+HOSTDIR = os.path.join(PKG, "host")
+HOST_LIB = os.path.join(LIBDIR, "libsphgb300_host.so")      # C++ plugin-interface layer over the C ABI
+HOST_DEMO = os.path.join(LIBDIR, "sphgb_host_demo")          # driver of the C++ layer (tests)
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-O3"]
 
@@ -35,14 +38,35 @@ def sources():
 
 def _deps():
     return sources() + glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) + \
-        glob.glob(os.path.join(ROOT, "include", "*.h")) + [os.path.abspath(__file__)]
+        glob.glob(os.path.join(HOSTDIR, "*")) + glob.glob(os.path.join(ROOT, "include", "*.h")) + \
+        [os.path.abspath(__file__)]
 
 
 def up_to_date() -> bool:
-    if not os.path.exists(LIB):
+    if not all(os.path.exists(f) for f in (LIB, HOST_LIB, HOST_DEMO)):
         return False
-    t = os.path.getmtime(LIB)
+    t = min(os.path.getmtime(f) for f in (LIB, HOST_LIB, HOST_DEMO))
     return all(os.path.getmtime(d) <= t for d in _deps())
+
+
+def build_host(verbose: bool = False) -> None:
+    """g++: the C++ host layer (libsphgb300_host.so) and its driver, linked to libsphgb300.so."""
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    inc = ["-I", os.path.join(ROOT, "include"), "-I", HOSTDIR]
+    rpath = "-Wl,-rpath,$ORIGIN"
+    cmds = [
+        [cxx, "-std=c++17", "-O2", "-Wall", "-fPIC", "-shared", *inc, os.path.join(HOSTDIR, "sphgb_host.cpp"),
+         "-L", LIBDIR, "-lsphgb300", rpath, "-o", HOST_LIB + ".tmp"],
+        [cxx, "-std=c++17", "-O2", "-Wall", *inc, os.path.join(HOSTDIR, "sphgb_host_demo.cpp"), "-L", LIBDIR,
+         "-lsphgb300_host", "-lsphgb300", rpath, "-o", HOST_DEMO + ".tmp"],
+    ]
+    for cmd, out in zip(cmds, (HOST_LIB, HOST_DEMO)):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"host build failed:\n{r.stdout}{r.stderr}")
+        if verbose and (r.stdout or r.stderr):
+            print(r.stdout, r.stderr)
+        os.replace(out + ".tmp", out)
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
@@ -70,6 +94,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}{r.stderr}")
     os.replace(tmp, LIB)
+    build_host(verbose)
     return LIB
 
 

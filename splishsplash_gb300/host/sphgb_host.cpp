@@ -1,0 +1,279 @@
+// Implementation of the C++ host side (sphgb_host.h) over the C ABI of libsphgb300.so.
+#include "sphgb_host.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace sphgb_host {
+
+// parameter ids: the order of TimeStepDFSPH::initParameters (TimeStepDFSPH.cpp:77-114)
+int TimeStepDFSPH_GB300::SOLVER_ITERATIONS = 0;
+int TimeStepDFSPH_GB300::MIN_ITERATIONS = 1;
+int TimeStepDFSPH_GB300::MAX_ITERATIONS = 2;
+int TimeStepDFSPH_GB300::MAX_ERROR = 3;
+int TimeStepDFSPH_GB300::SOLVER_ITERATIONS_V = 4;
+int TimeStepDFSPH_GB300::MAX_ITERATIONS_V = 5;
+int TimeStepDFSPH_GB300::MAX_ERROR_V = 6;
+int TimeStepDFSPH_GB300::USE_DIVERGENCE_SOLVER = 7;
+const std::string TimeStepDFSPH_GB300::METHOD_NAME = "DFSPH";
+
+// Viscosity_Weiler2018::initParameters order (Viscosity_Weiler2018.cpp:47-73)
+int Viscosity_Weiler2018_GB300::VISCOSITY_COEFFICIENT = 100;
+int Viscosity_Weiler2018_GB300::ITERATIONS = 101;
+int Viscosity_Weiler2018_GB300::MAX_ITERATIONS = 102;
+int Viscosity_Weiler2018_GB300::MAX_ERROR = 103;
+int Viscosity_Weiler2018_GB300::VISCOSITY_COEFFICIENT_BOUNDARY = 104;
+const std::string Viscosity_Weiler2018_GB300::METHOD_NAME = "Weiler et al. 2018";
+
+namespace {
+
+// the reference's parameter names (TimeStepDFSPH.cpp:77-114, Viscosity_Weiler2018.cpp:47-73)
+struct NamedId {
+    const char *name;
+    int *id;
+};
+const NamedId kNames[] = {
+    {"iterations", &TimeStepDFSPH_GB300::SOLVER_ITERATIONS},
+    {"minIterations", &TimeStepDFSPH_GB300::MIN_ITERATIONS},
+    {"maxIterations", &TimeStepDFSPH_GB300::MAX_ITERATIONS},
+    {"maxError", &TimeStepDFSPH_GB300::MAX_ERROR},
+    {"iterationsV", &TimeStepDFSPH_GB300::SOLVER_ITERATIONS_V},
+    {"maxIterationsV", &TimeStepDFSPH_GB300::MAX_ITERATIONS_V},
+    {"maxErrorV", &TimeStepDFSPH_GB300::MAX_ERROR_V},
+    {"enableDivergenceSolver", &TimeStepDFSPH_GB300::USE_DIVERGENCE_SOLVER},
+    {"viscosity", &Viscosity_Weiler2018_GB300::VISCOSITY_COEFFICIENT},
+    {"viscoIterations", &Viscosity_Weiler2018_GB300::ITERATIONS},
+    {"viscoMaxIter", &Viscosity_Weiler2018_GB300::MAX_ITERATIONS},
+    {"viscoMaxError", &Viscosity_Weiler2018_GB300::MAX_ERROR},
+    {"viscosityBoundary", &Viscosity_Weiler2018_GB300::VISCOSITY_COEFFICIENT_BOUNDARY},
+};
+
+constexpr int kDtype = sizeof(Real) == 8 ? SPHGB_DTYPE_F64 : SPHGB_DTYPE_F32;
+
+std::vector<double> to_double(const std::vector<Vector3r> &a)
+{
+    std::vector<double> d(a.size() * 3);
+    for (size_t i = 0; i < a.size(); i++)
+        for (int k = 0; k < 3; k++) d[3 * i + k] = (double)a[i][k];
+    return d;
+}
+
+}  // namespace
+
+void FluidModel::initModel(const std::string &id, unsigned int n, const Vector3r *x, const Vector3r *v)
+{
+    // FluidModel::initModel (FluidModel.cpp:285-327): x0 = x, v0 = v, a = 0, id = creation index;
+    // volume V = 0.8 (2r)^3 is set by the time step from the particle radius (FluidModel.cpp:234-253)
+    m_id = id;
+    m_x.assign(x, x + n);
+    m_x0 = m_x;
+    m_v.assign(v, v + n);
+    m_v0 = m_v;
+    m_a.assign(n, Vector3r());
+    m_density.assign(n, Real(0));
+    m_particleId.resize(n);
+    for (unsigned int i = 0; i < n; i++) m_particleId[i] = i;
+}
+
+void BoundaryModel_Akinci2012::initModel(unsigned int n, const Vector3r *x)
+{
+    m_x.assign(x, x + n);
+    m_V.assign(n, Real(0));
+}
+
+TimeStepDFSPH_GB300::TimeStepDFSPH_GB300(FluidModel &model, BoundaryModel_Akinci2012 &boundary,
+                                         const SimulationParameters &sim, Viscosity_Weiler2018_GB300 *viscosity,
+                                         int device, bool useGraph)
+    : m_model(model), m_boundary(boundary), m_sim(sim), m_visco(viscosity)
+{
+    sphgb_config cfg{};
+    cfg.abi_version = SPHGB_ABI_VERSION;
+    cfg.device = device;
+    cfg.precision = sizeof(Real) == 8 ? SPHGB_PRECISION_FP64 : SPHGB_PRECISION_FP32;
+    cfg.use_graph = useGraph ? 1 : 0;
+    const int rc = sphgb_create(&cfg, &m_ctx);
+    if (rc != SPHGB_OK) throw Error(rc, "sphgb_create failed (no CUDA device?)");
+    const Real d = Real(2) * m_sim.particleRadius;
+    m_model.m_V = Real(0.8) * d * d * d;
+    m_model.m_density0 = m_sim.density0;
+    applyParameters();
+}
+
+TimeStepDFSPH_GB300::~TimeStepDFSPH_GB300()
+{
+    if (m_ctx) sphgb_destroy(m_ctx);
+}
+
+void TimeStepDFSPH_GB300::check(int rc, const char *what)
+{
+    if (rc != SPHGB_OK) throw Error(rc, std::string(what) + ": " + sphgb_last_error(m_ctx));
+}
+
+void TimeStepDFSPH_GB300::applyParameters()
+{
+    sphgb_params p;
+    sphgb_default_params(&p);
+    p.particle_radius = m_sim.particleRadius;
+    p.density0 = m_sim.density0;
+    for (int k = 0; k < 3; k++) p.gravity[k] = m_sim.gravitation[k];
+    p.cfl_method = m_sim.cflMethod;
+    p.cfl_factor = m_sim.cflFactor;
+    p.cfl_min_time_step = m_sim.cflMinTimeStepSize;
+    p.cfl_max_time_step = m_sim.cflMaxTimeStepSize;
+    p.min_iterations = m_minIterations;
+    p.max_iterations = m_maxIterations;
+    p.max_error = m_maxError;
+    p.enable_divergence_solver = m_enableDivergenceSolver ? 1 : 0;
+    p.max_iterations_v = m_maxIterationsV;
+    p.max_error_v = m_maxErrorV;
+    p.xsph = m_sim.xsph;
+    p.xsph_boundary = m_sim.xsphBoundary;
+    p.viscosity_method = (m_visco && m_sim.viscosityMethod == 6) ? 6 : 0;
+    if (m_visco) {
+        p.viscosity = m_visco->m_viscosity;
+        p.viscosity_boundary = m_visco->m_boundaryViscosity;
+        p.visco_max_iter = m_visco->m_maxIter;
+        p.visco_max_error = m_visco->m_maxError;
+    }
+    check(sphgb_set_params(m_ctx, &p), "sphgb_set_params");
+}
+
+void TimeStepDFSPH_GB300::resize()
+{
+    const unsigned int n = m_model.numParticles();
+    m_factor.resize(n, Real(0));
+    m_densityAdv.resize(n, Real(0));
+    m_pressureRho2.resize(n, Real(0));
+    m_pressureRho2V.resize(n, Real(0));
+    m_pressureAccel.resize(n, Vector3r());
+    if (m_visco) m_visco->m_vDiff.resize(n, Vector3r());
+    m_dirty = true;
+}
+
+void TimeStepDFSPH_GB300::reset()
+{
+    // TimeStepDFSPH::reset (TimeStepDFSPH.cpp:709-717): warm starts and iteration counts cleared
+    std::fill(m_pressureRho2.begin(), m_pressureRho2.end(), Real(0));
+    std::fill(m_pressureRho2V.begin(), m_pressureRho2V.end(), Real(0));
+    if (m_visco) std::fill(m_visco->m_vDiff.begin(), m_visco->m_vDiff.end(), Vector3r());
+    m_iterations = m_iterationsV = 0;
+    m_time = 0;
+    m_dirty = true;
+}
+
+void TimeStepDFSPH_GB300::emittedParticles(FluidModel *, const unsigned int)
+{
+    resize();   // new particles were appended to the host vectors: upload before the next step
+}
+
+void TimeStepDFSPH_GB300::setTimeStepSize(Real dt)
+{
+    m_dt = dt;
+    if (!m_dirty) check(sphgb_set_time_step(m_ctx, dt), "sphgb_set_time_step");
+}
+
+// Host vectors -> device (the host vectors are the system of record).  Particle ids are the
+// host indices, so downloads come back in host order.
+void TimeStepDFSPH_GB300::upload()
+{
+    const unsigned int n = m_model.numParticles();
+    if (m_factor.size() != n) resize();
+    if (m_boundaryDirty) {
+        const std::vector<double> xb = to_double(m_boundary.m_x);
+        check(sphgb_upload_boundary(m_ctx, xb.data(), m_boundary.numberOfParticles()), "sphgb_upload_boundary");
+        m_boundaryDirty = false;
+    }
+    const std::vector<double> x = to_double(m_model.m_x), v = to_double(m_model.m_v);
+    check(sphgb_upload_fluid(m_ctx, x.data(), v.data(), nullptr, n), "sphgb_upload_fluid");
+    if (n) {
+        check(sphgb_upload_field(m_ctx, SPHGB_FIELD_PRESSURE_RHO2, m_pressureRho2.data(), kDtype), "upload p / rho^2");
+        check(sphgb_upload_field(m_ctx, SPHGB_FIELD_PRESSURE_RHO2_V, m_pressureRho2V.data(), kDtype), "upload p_v / rho^2");
+        if (m_visco)
+            check(sphgb_upload_field(m_ctx, SPHGB_FIELD_VDIFF, &m_visco->m_vDiff[0][0], kDtype), "upload velocity difference");
+    }
+    check(sphgb_set_time_step(m_ctx, m_dt), "sphgb_set_time_step");
+    check(sphgb_set_time(m_ctx, m_time), "sphgb_set_time");
+    m_dirty = false;
+}
+
+void TimeStepDFSPH_GB300::step()
+{
+    if (m_dirty) upload();
+    check(sphgb_step(m_ctx, &m_stats), "sphgb_step");
+    m_iterations = m_stats.iterations;
+    m_iterationsV = m_stats.iterations_v;
+    if (m_visco) m_visco->m_iterations = m_stats.visco_iterations;
+    m_dt = (Real)m_stats.dt_next;   // TimeManager::setTimeStepSize of the CFL update
+    m_time = (Real)m_stats.time;
+    if (m_hostSync) syncToHost();
+}
+
+void TimeStepDFSPH_GB300::syncToHost()
+{
+    const unsigned int n = m_model.numParticles();
+    if (n == 0) return;
+    auto dl = [&](int field, void *dst, const char *what) { check(sphgb_download(m_ctx, field, dst, kDtype), what); };
+    dl(SPHGB_FIELD_POSITION, &m_model.m_x[0][0], "download position");
+    dl(SPHGB_FIELD_VELOCITY, &m_model.m_v[0][0], "download velocity");
+    dl(SPHGB_FIELD_ACCELERATION, &m_model.m_a[0][0], "download acceleration");
+    dl(SPHGB_FIELD_DENSITY, m_model.m_density.data(), "download density");
+    dl(SPHGB_FIELD_FACTOR, m_factor.data(), "download factor");
+    dl(SPHGB_FIELD_DENSITY_ADV, m_densityAdv.data(), "download advected density");
+    dl(SPHGB_FIELD_PRESSURE_RHO2, m_pressureRho2.data(), "download p / rho^2");
+    dl(SPHGB_FIELD_PRESSURE_RHO2_V, m_pressureRho2V.data(), "download p_v / rho^2");
+    dl(SPHGB_FIELD_PRESSURE_ACCEL, &m_pressureAccel[0][0], "download pressure acceleration");
+    if (m_visco) dl(SPHGB_FIELD_VDIFF, &m_visco->m_vDiff[0][0], "download velocity difference");
+    const unsigned int nb = m_boundary.numberOfParticles();
+    if (nb) dl(SPHGB_FIELD_BOUNDARY_VOLUME, m_boundary.m_V.data(), "download boundary volume");
+}
+
+int TimeStepDFSPH_GB300::getParameterId(const std::string &name)
+{
+    for (const NamedId &p : kNames)
+        if (name == p.name) return *p.id;
+    return -1;
+}
+
+double TimeStepDFSPH_GB300::getValue(int id) const
+{
+    if (id == SOLVER_ITERATIONS) return m_iterations;
+    if (id == MIN_ITERATIONS) return m_minIterations;
+    if (id == MAX_ITERATIONS) return m_maxIterations;
+    if (id == MAX_ERROR) return m_maxError;
+    if (id == SOLVER_ITERATIONS_V) return m_iterationsV;
+    if (id == MAX_ITERATIONS_V) return m_maxIterationsV;
+    if (id == MAX_ERROR_V) return m_maxErrorV;
+    if (id == USE_DIVERGENCE_SOLVER) return m_enableDivergenceSolver ? 1.0 : 0.0;
+    if (m_visco) {
+        if (id == Viscosity_Weiler2018_GB300::VISCOSITY_COEFFICIENT) return m_visco->m_viscosity;
+        if (id == Viscosity_Weiler2018_GB300::ITERATIONS) return m_visco->m_iterations;
+        if (id == Viscosity_Weiler2018_GB300::MAX_ITERATIONS) return m_visco->m_maxIter;
+        if (id == Viscosity_Weiler2018_GB300::MAX_ERROR) return m_visco->m_maxError;
+        if (id == Viscosity_Weiler2018_GB300::VISCOSITY_COEFFICIENT_BOUNDARY) return m_visco->m_boundaryViscosity;
+    }
+    throw Error(SPHGB_ERR_ARGUMENT, "unknown parameter id " + std::to_string(id));
+}
+
+void TimeStepDFSPH_GB300::setValue(int id, double value)
+{
+    // the iteration counters are read-only, as in the reference (setReadOnly(true))
+    if (id == SOLVER_ITERATIONS || id == SOLVER_ITERATIONS_V ||
+        (m_visco && id == Viscosity_Weiler2018_GB300::ITERATIONS))
+        throw Error(SPHGB_ERR_ARGUMENT, "parameter is read-only");
+    if (id == MIN_ITERATIONS) m_minIterations = (unsigned int)value;
+    else if (id == MAX_ITERATIONS) m_maxIterations = (unsigned int)value;
+    else if (id == MAX_ERROR) m_maxError = (Real)value;
+    else if (id == MAX_ITERATIONS_V) m_maxIterationsV = (unsigned int)value;
+    else if (id == MAX_ERROR_V) m_maxErrorV = (Real)value;
+    else if (id == USE_DIVERGENCE_SOLVER) m_enableDivergenceSolver = value != 0.0;
+    else if (m_visco && id == Viscosity_Weiler2018_GB300::VISCOSITY_COEFFICIENT) m_visco->m_viscosity = (Real)value;
+    else if (m_visco && id == Viscosity_Weiler2018_GB300::MAX_ITERATIONS) m_visco->m_maxIter = (unsigned int)value;
+    else if (m_visco && id == Viscosity_Weiler2018_GB300::MAX_ERROR) m_visco->m_maxError = (Real)value;
+    else if (m_visco && id == Viscosity_Weiler2018_GB300::VISCOSITY_COEFFICIENT_BOUNDARY)
+        m_visco->m_boundaryViscosity = (Real)value;
+    else throw Error(SPHGB_ERR_ARGUMENT, "unknown parameter id " + std::to_string(id));
+    applyParameters();
+}
+
+}  // namespace sphgb_host

@@ -1,0 +1,211 @@
+// C++ host side of the GB300 DFSPH step: the reference's plugin interface for this path,
+// restated without the reference's headers and implemented over the C ABI
+// (include/sphgb300.h).
+//
+// Names, parameter names, field names and argument meaning follow SPlisHSPlasH 2.16.0:
+//   TimeStep                   SPlisHSPlasH/TimeStep.h:13-59
+//   TimeStepDFSPH parameters   SPlisHSPlasH/DFSPH/TimeStepDFSPH.h:57-64, TimeStepDFSPH.cpp:77-114
+//   DFSPH fields               TimeStepDFSPH.cpp:49-53, SimulationDataDFSPH.h:55-120
+//   FluidModel field layout    SPlisHSPlasH/FluidModel.h:113-124, 247-300
+//   Akinci2012 boundary        SPlisHSPlasH/BoundaryModel_Akinci2012.h:32-35
+//   Weiler2018 viscosity       SPlisHSPlasH/Viscosity/Viscosity_Weiler2018.h:44-48, .cpp:33,47-73
+//   time step size             SPlisHSPlasH/TimeManager.h
+// The host vectors are the system of record, as in the reference: step() uploads them when
+// they changed, advances the device copy and (with host sync on, the default) downloads the
+// fields back in particle-id order.  Errors from the C ABI are thrown as sphgb_host::Error.
+#pragma once
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "sphgb300.h"
+
+namespace sphgb_host {
+
+#ifdef USE_DOUBLE
+using Real = double;
+#else
+using Real = float;
+#endif
+
+// Vector3r stored as three packed Reals (the reference uses Eigen with DontAlign, Common.h:41)
+struct Vector3r {
+    Real v[3] = {0, 0, 0};
+    Vector3r() = default;
+    Vector3r(Real x, Real y, Real z) : v{x, y, z} {}
+    Real &operator[](int k) { return v[k]; }
+    Real operator[](int k) const { return v[k]; }
+    Real x() const { return v[0]; }
+    Real y() const { return v[1]; }
+    Real z() const { return v[2]; }
+};
+static_assert(sizeof(Vector3r) == 3 * sizeof(Real), "Vector3r must be packed like the reference's");
+
+class Error : public std::runtime_error {
+public:
+    Error(int code, const std::string &msg) : std::runtime_error(msg), code(code) {}
+    int code;
+};
+
+// Scene-level parameters (Simulation.cpp:163-277 keys, XSPH.cpp:27-42)
+struct SimulationParameters {
+    Real particleRadius = Real(0.025);
+    Real density0 = Real(1000);
+    Vector3r gravitation{0, Real(-9.81), 0};
+    int cflMethod = 1;
+    Real cflFactor = Real(0.5);
+    Real cflMinTimeStepSize = Real(1e-4);
+    Real cflMaxTimeStepSize = Real(5e-3);
+    Real xsph = Real(0.01);
+    Real xsphBoundary = Real(0);
+    int viscosityMethod = 0;   // 0 none, 6 "Weiler et al. 2018"
+};
+
+// Per-particle data of one fluid phase (FluidModel.h:113-124)
+class FluidModel {
+public:
+    std::vector<Vector3r> m_x0, m_x, m_v0, m_v, m_a;
+    std::vector<Real> m_density;
+    std::vector<unsigned int> m_particleId;
+    Real m_V = 0;
+    Real m_density0 = Real(1000);
+
+    void initModel(const std::string &id, unsigned int nFluidParticles, const Vector3r *fluidParticles,
+                   const Vector3r *fluidVelocities);
+    const std::string &getId() const { return m_id; }
+    unsigned int numParticles() const { return (unsigned int)m_x.size(); }
+    unsigned int numActiveParticles() const { return numParticles(); }
+    Vector3r &getPosition(unsigned int i) { return m_x[i]; }
+    Vector3r &getVelocity(unsigned int i) { return m_v[i]; }
+    Vector3r &getAcceleration(unsigned int i) { return m_a[i]; }
+    Real &getDensity(unsigned int i) { return m_density[i]; }
+    Real getDensity0() const { return m_density0; }
+    Real getVolume(unsigned int) const { return m_V; }
+    Real getMass(unsigned int) const { return m_V * m_density0; }
+
+private:
+    std::string m_id;
+};
+
+// Static boundary sampled with particles; volumes computed on the device (BoundaryModel_Akinci2012.cpp:48-75)
+class BoundaryModel_Akinci2012 {
+public:
+    std::vector<Vector3r> m_x;
+    std::vector<Real> m_V;
+    void initModel(unsigned int numBoundaryParticles, const Vector3r *boundaryParticles);
+    unsigned int numberOfParticles() const { return (unsigned int)m_x.size(); }
+    Vector3r &getPosition(unsigned int i) { return m_x[i]; }
+    Real getVolume(unsigned int i) const { return m_V[i]; }
+};
+
+// TimeStep.h:13-59
+class TimeStep {
+public:
+    virtual ~TimeStep() = default;
+    virtual std::string getMethodName() = 0;
+    virtual void step() = 0;
+    virtual void reset() {}
+    virtual void init() {}
+    virtual void resize() = 0;
+    virtual void emittedParticles(FluidModel *, const unsigned int) {}
+    virtual void performNeighborhoodSearchSort() {}
+    virtual int getNumIterations() = 0;
+};
+
+// Weiler et al. 2018 parameters and "velocity difference" field (Viscosity_Weiler2018.h:44-48)
+class Viscosity_Weiler2018_GB300 {
+public:
+    static int VISCOSITY_COEFFICIENT;
+    static int ITERATIONS;
+    static int MAX_ITERATIONS;
+    static int MAX_ERROR;
+    static int VISCOSITY_COEFFICIENT_BOUNDARY;
+    static const std::string METHOD_NAME;   // "Weiler et al. 2018"
+
+    Real m_viscosity = Real(0.01);
+    Real m_boundaryViscosity = Real(0);
+    unsigned int m_maxIter = 100;
+    Real m_maxError = Real(0.01);
+    unsigned int m_iterations = 0;
+    std::vector<Vector3r> m_vDiff;
+    Vector3r &getVDiff(unsigned int i) { return m_vDiff[i]; }
+};
+
+// The DFSPH time step on the GPU (TimeStepDFSPH.cpp:117-249)
+class TimeStepDFSPH_GB300 : public TimeStep {
+public:
+    // parameter ids (TimeStepDFSPH.h:57-64)
+    static int SOLVER_ITERATIONS;
+    static int MIN_ITERATIONS;
+    static int MAX_ITERATIONS;
+    static int MAX_ERROR;
+    static int SOLVER_ITERATIONS_V;
+    static int MAX_ITERATIONS_V;
+    static int MAX_ERROR_V;
+    static int USE_DIVERGENCE_SOLVER;
+    static const std::string METHOD_NAME;   // "DFSPH"
+
+    TimeStepDFSPH_GB300(FluidModel &model, BoundaryModel_Akinci2012 &boundary, const SimulationParameters &sim,
+                        Viscosity_Weiler2018_GB300 *viscosity = nullptr, int device = 0, bool useGraph = true);
+    ~TimeStepDFSPH_GB300() override;
+    TimeStepDFSPH_GB300(const TimeStepDFSPH_GB300 &) = delete;
+    TimeStepDFSPH_GB300 &operator=(const TimeStepDFSPH_GB300 &) = delete;
+
+    std::string getMethodName() override { return METHOD_NAME; }
+    void step() override;
+    void reset() override;
+    void init() override { m_dirty = true; }
+    void resize() override;
+    void emittedParticles(FluidModel *model, const unsigned int startIndex) override;
+    void performNeighborhoodSearchSort() override { m_dirty = true; }
+    int getNumIterations() override { return (int)m_iterations; }
+
+    // ParameterObject-style access by id or by the reference's parameter name
+    double getValue(int id) const;
+    void setValue(int id, double value);
+    static int getParameterId(const std::string &name);
+
+    // DFSPH fields by particle index (SimulationDataDFSPH.h:55-120, fields of TimeStepDFSPH.cpp:49-53)
+    Real &getFactor(unsigned int i) { return m_factor[i]; }
+    Real &getDensityAdv(unsigned int i) { return m_densityAdv[i]; }
+    Real &getPressureRho2(unsigned int i) { return m_pressureRho2[i]; }
+    Real &getPressureRho2_V(unsigned int i) { return m_pressureRho2V[i]; }
+    Vector3r &getPressureAccel(unsigned int i) { return m_pressureAccel[i]; }
+
+    // TimeManager
+    Real getTimeStepSize() const { return m_dt; }
+    void setTimeStepSize(Real dt);
+    Real getTime() const { return m_time; }
+
+    // download the fields after every step (default, drop-in safe) or only on syncToHost()
+    void setHostSync(bool on) { m_hostSync = on; }
+    void syncToHost();
+    unsigned int getNumIterationsV() const { return m_iterationsV; }
+    const sphgb_stats &lastStats() const { return m_stats; }
+    sphgb_ctx *context() { return m_ctx; }
+
+protected:
+    void check(int rc, const char *what);
+    void upload();
+    void applyParameters();
+
+    FluidModel &m_model;
+    BoundaryModel_Akinci2012 &m_boundary;
+    SimulationParameters m_sim;
+    Viscosity_Weiler2018_GB300 *m_visco;
+    sphgb_ctx *m_ctx = nullptr;
+    bool m_dirty = true, m_boundaryDirty = true, m_hostSync = true;
+    // DFSPH parameters (TimeStepDFSPH.cpp:77-114 defaults)
+    unsigned int m_minIterations = 2, m_maxIterations = 100, m_maxIterationsV = 100;
+    Real m_maxError = Real(0.01), m_maxErrorV = Real(0.1);
+    bool m_enableDivergenceSolver = true;
+    unsigned int m_iterations = 0, m_iterationsV = 0;
+    Real m_dt = Real(0.001), m_time = 0;
+    sphgb_stats m_stats{};
+    std::vector<Real> m_factor, m_densityAdv, m_pressureRho2, m_pressureRho2V;
+    std::vector<Vector3r> m_pressureAccel;
+};
+
+}  // namespace sphgb_host

@@ -1,0 +1,94 @@
+// Runs a scene through the C++ host classes (sphgb_host.h) the way a SPlisHSPlasH
+// simulator drives its time step: build the models, construct the time step, call step()
+// repeatedly and read the fields back from the host vectors.
+//
+//   sphgb_host_demo <scene.bin> <out.bin>
+//
+// scene.bin (little endian): uint32 n, nb, steps, lanes (0 = autotune), viscosity (0/1);
+// float64 particle radius; float64 x[n][3], v[n][3], xb[nb][3].
+// out.bin: per step uint32 iterations, iterationsV, viscoIterations and float64 time;
+// then float64 x[n][3], v[n][3], density[n], p / rho^2 [n], boundary volume[nb].
+#include <cstdint>
+#include <cstdio>
+#include <vector>
+
+#include "sphgb_host.h"
+
+using namespace sphgb_host;
+
+namespace {
+
+template <class T> bool rd(FILE *f, T *p, size_t n) { return fread(p, sizeof(T), n, f) == n; }
+template <class T> void wr(FILE *f, const T *p, size_t n) { fwrite(p, sizeof(T), n, f); }
+
+std::vector<Vector3r> to_vec(const std::vector<double> &a)
+{
+    std::vector<Vector3r> v(a.size() / 3);
+    for (size_t i = 0; i < v.size(); i++) v[i] = Vector3r((Real)a[3 * i], (Real)a[3 * i + 1], (Real)a[3 * i + 2]);
+    return v;
+}
+
+}  // namespace
+
+int main(int argc, char **argv)
+{
+    if (argc != 3) {
+        fprintf(stderr, "usage: %s scene.bin out.bin\n", argv[0]);
+        return 2;
+    }
+    FILE *f = fopen(argv[1], "rb");
+    if (!f) return 2;
+    uint32_t hdr[5];
+    double radius;
+    if (!rd(f, hdr, 5) || !rd(f, &radius, 1)) return 2;
+    const uint32_t n = hdr[0], nb = hdr[1], steps = hdr[2], lanes = hdr[3], visc = hdr[4];
+    std::vector<double> x(3 * (size_t)n), v(3 * (size_t)n), xb(3 * (size_t)nb);
+    if (!rd(f, x.data(), x.size()) || !rd(f, v.data(), v.size()) || !rd(f, xb.data(), xb.size())) return 2;
+    fclose(f);
+
+    try {
+        // the parameter block of the scenes (scene-file defaults of the dam-break configs)
+        SimulationParameters sp;
+        sp.particleRadius = (Real)radius;
+        sp.cflFactor = 1;
+        sp.viscosityMethod = visc ? 6 : 0;
+        FluidModel model;
+        const std::vector<Vector3r> xv = to_vec(x), vv = to_vec(v), xbv = to_vec(xb);
+        model.initModel("Fluid", n, xv.data(), vv.data());
+        BoundaryModel_Akinci2012 boundary;
+        boundary.initModel(nb, xbv.data());
+        Viscosity_Weiler2018_GB300 viscosity;
+        viscosity.m_maxError = Real(1e-3);
+        TimeStepDFSPH_GB300 ts(model, boundary, sp, visc ? &viscosity : nullptr);
+        sphgb_set_lanes_per_particle(ts.context(), lanes);
+        ts.resize();
+
+        FILE *o = fopen(argv[2], "wb");
+        if (!o) return 2;
+        for (uint32_t k = 0; k < steps; k++) {
+            ts.step();
+            const uint32_t it[3] = {(uint32_t)ts.getValue(TimeStepDFSPH_GB300::SOLVER_ITERATIONS),
+                                    (uint32_t)ts.getValue(TimeStepDFSPH_GB300::SOLVER_ITERATIONS_V),
+                                    visc ? (uint32_t)ts.getValue(Viscosity_Weiler2018_GB300::ITERATIONS) : 0u};
+            const double t = ts.getTime();
+            wr(o, it, 3);
+            wr(o, &t, 1);
+        }
+        std::vector<double> out;
+        for (uint32_t i = 0; i < n; i++)
+            for (int c = 0; c < 3; c++) out.push_back(model.getPosition(i)[c]);
+        for (uint32_t i = 0; i < n; i++)
+            for (int c = 0; c < 3; c++) out.push_back(model.getVelocity(i)[c]);
+        for (uint32_t i = 0; i < n; i++) out.push_back(model.getDensity(i));
+        for (uint32_t i = 0; i < n; i++) out.push_back(ts.getPressureRho2(i));
+        for (uint32_t i = 0; i < nb; i++) out.push_back(boundary.getVolume(i));
+        wr(o, out.data(), out.size());
+        fclose(o);
+        printf("%s: %u steps, %u fluid + %u boundary particles, time %.6f\n", ts.getMethodName().c_str(), steps, n, nb,
+               (double)ts.getTime());
+    } catch (const Error &e) {
+        fprintf(stderr, "error %d: %s\n", e.code, e.what());
+        return 1;
+    }
+    return 0;
+}

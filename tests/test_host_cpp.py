@@ -1,0 +1,91 @@
+"""The C++ host layer (splishsplash_gb300/host): the reference's TimeStep / FluidModel /
+Akinci2012 / Weiler2018 plugin interface over the C ABI.  The driver runs a scene through the
+C++ classes; on the GPU its results must equal the Python mirror's bit for bit (same library,
+same inputs, same lanes per particle)."""
+import os
+import struct
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+from splishsplash_gb300 import build, scenes
+from splishsplash_gb300.dfsph import TimeStepDFSPH
+
+
+def _write_scene(path, sc, steps, lanes, visc):
+    with open(path, "wb") as f:
+        f.write(struct.pack("<5I", sc.n, sc.nb, steps, lanes, 1 if visc else 0))
+        f.write(struct.pack("<d", sc.params.particleRadius))
+        for a in (sc.x, sc.v, sc.xb):
+            f.write(np.ascontiguousarray(a, "<f8").tobytes())
+
+
+def _read_out(path, n, nb, steps):
+    raw = open(path, "rb").read()
+    per = []
+    off = 0
+    for _ in range(steps):
+        it = struct.unpack_from("<3I", raw, off)
+        t = struct.unpack_from("<d", raw, off + 12)[0]
+        per.append((it, t))
+        off += 20
+    a = np.frombuffer(raw, "<f8", offset=off)
+    x = a[:3 * n].reshape(n, 3)
+    v = a[3 * n:6 * n].reshape(n, 3)
+    rho = a[6 * n:7 * n]
+    kp = a[7 * n:8 * n]
+    vb = a[8 * n:8 * n + nb]
+    return per, x, v, rho, kp, vb
+
+
+def test_host_layer_is_built_and_fails_cleanly_without_a_device():
+    build.build()
+    assert os.path.exists(build.HOST_LIB) and os.path.exists(build.HOST_DEMO)
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a device is present: covered by the GPU test")
+    sc = scenes.small_block(counts=(4, 4, 4))
+    with tempfile.TemporaryDirectory() as d:
+        _write_scene(os.path.join(d, "s.bin"), sc, 1, 0, False)
+        r = subprocess.run([build.HOST_DEMO, os.path.join(d, "s.bin"), os.path.join(d, "o.bin")],
+                           capture_output=True, text=True, timeout=120)
+    assert r.returncode == 1 and "sphgb_create failed" in r.stderr
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("visc", [False, True])
+def test_cpp_host_layer_matches_python_mirror(visc):
+    sc = scenes.small_block(counts=(10, 12, 10), box=(0.8, 1.0, 0.8), viscosity=visc,
+                            velocity=(0.3, 0.0, -0.2)).as_float32()
+    # the C++ layer holds every real parameter in Real (float), like the reference's FP32 build
+    f32 = lambda a: float(np.float32(a))
+    p = sc.params
+    for name in ("particleRadius", "density0", "cflFactor", "cflMinTimeStepSize", "cflMaxTimeStepSize", "maxError",
+                 "maxErrorV", "xsph", "xsphBoundary", "viscosity", "viscosityBoundary", "timeStepSize"):
+        setattr(p, name, f32(getattr(p, name)))
+    p.gravitation = tuple(f32(g) for g in p.gravitation)
+    p.viscoMaxError = f32(1e-3)
+    steps, lanes = 12, 1
+    with tempfile.TemporaryDirectory() as d:
+        _write_scene(os.path.join(d, "s.bin"), sc, steps, lanes, visc)
+        r = subprocess.run([build.HOST_DEMO, os.path.join(d, "s.bin"), os.path.join(d, "o.bin")],
+                           capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stderr
+        assert r.stdout.startswith("DFSPH:")
+        per, x, v, rho, kp, vb = _read_out(os.path.join(d, "o.bin"), sc.n, sc.nb, steps)
+    ts = TimeStepDFSPH(sc)
+    ts.ctx.set_lanes_per_particle(lanes)
+    for k in range(steps):
+        st = ts.step()
+        assert per[k][0] == (st["iterations"], st["iterations_v"], st["visco_iterations"] if visc else 0)
+        assert per[k][1] == pytest.approx(st["time"], rel=1e-6)
+    m = ts.getFluidModel()
+    # the C++ layer stores Real = float: compare in float32
+    np.testing.assert_array_equal(x.astype(np.float32), m.getFieldBuffer("position", np.float32))
+    np.testing.assert_array_equal(v.astype(np.float32), m.getFieldBuffer("velocity", np.float32))
+    np.testing.assert_array_equal(rho.astype(np.float32), m.getFieldBuffer("density", np.float32))
+    np.testing.assert_array_equal(kp.astype(np.float32), m.getFieldBuffer("p / rho^2", np.float32))
+    np.testing.assert_array_equal(vb.astype(np.float32), ts.ctx.download("boundary volume", np.float32))
+    ts.close()
