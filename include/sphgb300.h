@@ -125,6 +125,10 @@ typedef struct sphgb_stats {
 #define SPHGB_FIELD_BOUNDARY_VOLUME 14         /* boundary "volume" V_b (nb entries) */
 #define SPHGB_FIELD_BOUNDARY_POSITION 15       /* boundary "position" (nb x 3) */
 #define SPHGB_FIELD_FEATURES 16                /* warm-start network inputs of the last step (n x 10) */
+#define SPHGB_FIELD_POSITION_HI 17             /* position as stored: the high part of the FP32 double-float
+                                                  position (FP64 mode: the position), 3 */
+#define SPHGB_FIELD_POSITION_LO 18             /* the low part of the FP32 double-float position (FP64 mode:
+                                                  zero); HI + LO = "position" exactly, 3 */
 
 #define SPHGB_DTYPE_F32 0
 #define SPHGB_DTYPE_F64 1
@@ -169,6 +173,27 @@ int sphgb_upload_field(sphgb_ctx *ctx, int field, const void *src, int dtype);
  * ids.  kind 0 = fluid-fluid, 1 = fluid-boundary (boundary indices in upload order).  Pass
  * indices == NULL to query offsets only. */
 int sphgb_neighbors(sphgb_ctx *ctx, int kind, uint32_t *offsets, uint32_t *indices, size_t capacity);
+
+/* ---- particle export and state files (the reference's exporters and state files,
+ * Simulator/Exporter/ParticleExporter_VTK.cpp:25-266, SimulatorBase.cpp:1689-1870, run from
+ * the device copy) ----
+ * sphgb_export_vtk writes one legacy VTK 4.1 file (big-endian binary, unstructured grid of
+ * vertex cells) of all fluid particles in particle-id order, like ParticleExporter_VTK:
+ * POINTS (position), CELLS / CELL_TYPES, POINT_DATA "id", then a FIELD block with one array per
+ * entry of `fields` (field ids above, names with white space replaced by '_').  The device
+ * scatters and byte-swaps the data on its own stream and copies it to pinned host memory
+ * asynchronously; a host thread writes the file.  wait = 0 returns at once (the next steps
+ * overlap the copy and the write); sphgb_export_wait blocks until the last export is on disk
+ * and returns its status.  A new export or sphgb_destroy waits for the previous one. */
+int sphgb_export_vtk(sphgb_ctx *ctx, const char *path, const int *fields, uint32_t nfields, int wait);
+int sphgb_export_wait(sphgb_ctx *ctx);
+/* The simulation state of the context in a binary file, exactly as held on the device (the
+ * double-float positions in both parts, velocities, velocity differences, both warm starts,
+ * per-scene step size and time, the boundary particles, the parameters and the lanes per
+ * particle in use): sphgb_load_state re-creates the scenes from it, and stepping continues bit
+ * for bit as if the context had not been interrupted. */
+int sphgb_save_state(sphgb_ctx *ctx, const char *path);
+int sphgb_load_state(sphgb_ctx *ctx, const char *path);
 
 /* counts (all scenes of a batch) */
 int sphgb_num_particles(const sphgb_ctx *ctx, uint32_t *n, uint32_t *nb);

@@ -19,6 +19,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/sphgb300.h"
@@ -41,6 +42,7 @@ struct SceneHost {
     int dim[3] = {1, 1, 1};
     uint32_t cell_off = 0;
     double dt = 0.001, time = 0.0;     // host copies, valid while no step is pending
+    unsigned prev_iters = 0;           // pressure iterations of the last step (CFL method 2)
 };
 }  // namespace
 
@@ -104,6 +106,14 @@ struct sphgb_ctx {
     uint32_t lpp_fixed = 0;            // 0: autotune on the first step after an upload
     bool tuned = false;
     float tune_ms[3] = {0, 0, 0};      // trial step times of lanes per particle 1, 2, 4
+    // particle export: own stream, device and pinned staging, one writer thread
+    cudaStream_t export_stream = nullptr;
+    cudaEvent_t export_scattered = nullptr, export_copied = nullptr, export_start = nullptr;
+    void *export_dev = nullptr, *export_host = nullptr;
+    size_t export_dev_bytes = 0, export_host_bytes = 0;
+    std::thread export_thread;
+    int export_rc = 0;
+    std::string export_err;
     float *feat = nullptr, *mlp_x = nullptr, *mlp_y = nullptr;
     void *kl = nullptr, *pa2 = nullptr;
     // per-kernel CUDA-event timing (host-loop mode only)
@@ -230,6 +240,7 @@ void free_prepared(sphgb_ctx *c)
 
 void free_all(sphgb_ctx *c)
 {
+    if (c->export_stream) cudaStreamSynchronize(c->export_stream);   // an export may still read the state
     free_prepared(c);
     for (void *p : c->allocs) cudaFree(p);
     c->allocs.clear();
@@ -412,6 +423,7 @@ int upload_scalars(sphgb_ctx *c)
         c->hsc[s].dt = dt;
         c->hsc[s].dt_next = dt;
         c->hsc[s].time = t;
+        c->hsc[s].prev_iters = c->scn.empty() ? 0u : c->scn[s].prev_iters;
     }
     CK(cudaMemcpy(c->sc, c->hsc, (S + 1) * sizeof(StepScalars), cudaMemcpyHostToDevice));
     c->scalars_dirty = false;
@@ -856,6 +868,7 @@ int fill_stats(sphgb_ctx *c, sphgb_stats *st)
         for (uint32_t s = 0; s < c->scn.size(); s++) {
             c->scn[s].dt = c->hsc[s].dt;
             c->scn[s].time = c->hsc[s].time;
+            c->scn[s].prev_iters = c->hsc[s].prev_iters;
         }
         c->step_pending = false;
     }
@@ -1099,6 +1112,7 @@ int field_components(int field)
     switch (field) {
     case SPHGB_FIELD_POSITION: case SPHGB_FIELD_VELOCITY: case SPHGB_FIELD_ACCELERATION:
     case SPHGB_FIELD_PRESSURE_ACCEL: case SPHGB_FIELD_VDIFF: case SPHGB_FIELD_BOUNDARY_POSITION:
+    case SPHGB_FIELD_POSITION_HI: case SPHGB_FIELD_POSITION_LO:
         return 3;
     case SPHGB_FIELD_FEATURES:
         return 10;
@@ -1178,8 +1192,15 @@ int sphgb_destroy(sphgb_ctx *c)
     if (!c) return SPHGB_ERR_ARGUMENT;
     cudaSetDevice(c->cfg.device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->export_thread.joinable()) c->export_thread.join();
+    if (c->export_stream) cudaStreamSynchronize(c->export_stream);
     free_all(c);
     if (c->hsc) cudaFreeHost(c->hsc);
+    if (c->export_dev) cudaFree(c->export_dev);
+    if (c->export_host) cudaFreeHost(c->export_host);
+    for (cudaEvent_t e : {c->export_scattered, c->export_copied, c->export_start})
+        if (e) cudaEventDestroy(e);
+    if (c->export_stream) cudaStreamDestroy(c->export_stream);
     if (c->mlp_p) cudaFree(c->mlp_p);
     if (c->mlp_w) cudaFree(c->mlp_w);
     for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
@@ -1482,7 +1503,7 @@ int sphgb_num_particles(const sphgb_ctx *c, uint32_t *n, uint32_t *nb)
 int sphgb_download(sphgb_ctx *c, int field, void *dst, int dtype)
 {
     if (!c || !dst) return SPHGB_ERR_ARGUMENT;
-    if (field < 0 || field > SPHGB_FIELD_FEATURES) return fail(c, SPHGB_ERR_ARGUMENT, "unknown field");
+    if (field < 0 || field > SPHGB_FIELD_POSITION_LO) return fail(c, SPHGB_ERR_ARGUMENT, "unknown field");
     if (field == SPHGB_FIELD_FEATURES && !c->mlp_x) return fail(c, SPHGB_ERR_STATE, "features are not computed");
     if (dtype < SPHGB_DTYPE_F32 || dtype > SPHGB_DTYPE_U32) return fail(c, SPHGB_ERR_ARGUMENT, "unknown dtype");
     if (!c->have_fluid) return fail(c, SPHGB_ERR_STATE, "no fluid uploaded");
@@ -1516,7 +1537,8 @@ int sphgb_upload_field(sphgb_ctx *c, int field, const void *src, int dtype)
 {
     if (!c || !src) return SPHGB_ERR_ARGUMENT;
     if (field != SPHGB_FIELD_POSITION && field != SPHGB_FIELD_VELOCITY && field != SPHGB_FIELD_VDIFF &&
-        field != SPHGB_FIELD_PRESSURE_RHO2 && field != SPHGB_FIELD_PRESSURE_RHO2_V)
+        field != SPHGB_FIELD_PRESSURE_RHO2 && field != SPHGB_FIELD_PRESSURE_RHO2_V &&
+        field != SPHGB_FIELD_POSITION_HI && field != SPHGB_FIELD_POSITION_LO)
         return fail(c, SPHGB_ERR_ARGUMENT, "field is not uploadable");
     if (dtype != SPHGB_DTYPE_F32 && dtype != SPHGB_DTYPE_F64) return fail(c, SPHGB_ERR_ARGUMENT, "bad dtype");
     if (!c->have_fluid) return fail(c, SPHGB_ERR_STATE, "no fluid uploaded");
@@ -1577,6 +1599,418 @@ int sphgb_neighbors(sphgb_ctx *c, int kind, uint32_t *offsets, uint32_t *indices
     CK(cudaStreamSynchronize(c->stream));
     dfree(c->allocs, dout);
     dfree(c->allocs, doff);
+    return SPHGB_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Particle export (legacy VTK, ParticleExporter_VTK.cpp:25-266) from the device copy
+// ===========================================================================
+namespace {
+
+// the reference's field names (FluidModel.cpp:61-67, TimeStepDFSPH.cpp:49-53, Viscosity_Weiler2018.cpp:33)
+const char *field_name(int f)
+{
+    switch (f) {
+    case SPHGB_FIELD_POSITION: return "position";
+    case SPHGB_FIELD_VELOCITY: return "velocity";
+    case SPHGB_FIELD_ACCELERATION: return "acceleration";
+    case SPHGB_FIELD_DENSITY: return "density";
+    case SPHGB_FIELD_FACTOR: return "factor";
+    case SPHGB_FIELD_DENSITY_ADV: return "advected density";
+    case SPHGB_FIELD_PRESSURE_RHO2: return "p / rho^2";
+    case SPHGB_FIELD_PRESSURE_RHO2_V: return "p_v / rho^2";
+    case SPHGB_FIELD_PRESSURE_ACCEL: return "pressure acceleration";
+    case SPHGB_FIELD_VDIFF: return "velocity difference";
+    case SPHGB_FIELD_PARTICLE_ID: return "id";
+    case SPHGB_FIELD_FACTOR_RAW: return "factor raw";
+    case SPHGB_FIELD_NUM_FLUID_NEIGHBORS: return "fluid neighbors";
+    case SPHGB_FIELD_NUM_BOUNDARY_NEIGHBORS: return "boundary neighbors";
+    case SPHGB_FIELD_FEATURES: return "features";
+    case SPHGB_FIELD_POSITION_HI: return "position high";
+    case SPHGB_FIELD_POSITION_LO: return "position low";
+    default: return nullptr;
+    }
+}
+
+bool is_uint_field(int f)
+{
+    return f == SPHGB_FIELD_PARTICLE_ID || f == SPHGB_FIELD_NUM_FLUID_NEIGHBORS || f == SPHGB_FIELD_NUM_BOUNDARY_NEIGHBORS;
+}
+
+std::string vtk_name(const char *name)
+{
+    std::string out;
+    for (const char *p = name; *p; p++) out += (*p == ' ' || *p == '\t' || *p == '\n') ? '_' : *p;
+    return out;
+}
+
+uint32_t be32(uint32_t v)
+{
+    return ((v & 0xffu) << 24) | ((v & 0xff00u) << 8) | ((v >> 8) & 0xff00u) | (v >> 24);
+}
+
+struct ExportChunk {
+    int field;          // -1: positions
+    size_t offset;      // bytes into the staging buffer
+    size_t count;       // words
+    int word;           // bytes per word
+    int comps;
+};
+
+// Writer thread: waits for the device copy, then writes the file from pinned memory.
+void write_vtk(sphgb_ctx *c, std::string path, uint32_t n, std::vector<ExportChunk> chunks, bool real64)
+{
+    if (cudaEventSynchronize(c->export_copied) != cudaSuccess) {
+        c->export_rc = SPHGB_ERR_CUDA;
+        c->export_err = "export: device copy failed";
+        return;
+    }
+    FILE *f = fopen(path.c_str(), "wb");
+    if (!f) {
+        c->export_rc = SPHGB_ERR_ARGUMENT;
+        c->export_err = "export: cannot open " + path;
+        return;
+    }
+    const char *real_str = real64 ? " double\n" : " float\n";
+    const char *base = static_cast<const char *>(c->export_host);
+    fprintf(f, "# vtk DataFile Version 4.1\nSPlisHSPlasH particle data\nBINARY\nDATASET UNSTRUCTURED_GRID\n");
+    fprintf(f, "POINTS %u%s", n, real_str);
+    fwrite(base + chunks[0].offset, 1, chunks[0].count * chunks[0].word, f);
+    fprintf(f, "\nCELLS %u %u\n", n, 2 * n);
+    // particles are vertex cells (1, index); written in pieces
+    std::vector<uint32_t> buf;
+    const uint32_t piece = 1u << 16;
+    const uint32_t one = be32(1u);
+    for (uint32_t a = 0; a < n; a += piece) {
+        const uint32_t b = std::min(n, a + piece);
+        buf.resize(2 * (size_t)(b - a));
+        for (uint32_t i = a; i < b; i++) { buf[2 * (size_t)(i - a)] = one; buf[2 * (size_t)(i - a) + 1] = be32(i); }
+        fwrite(buf.data(), 4, buf.size(), f);
+    }
+    fprintf(f, "\nCELL_TYPES %u\n", n);
+    buf.assign(std::min<size_t>(n, piece), one);
+    for (uint32_t a = 0; a < n; a += piece) fwrite(buf.data(), 4, std::min(n, a + piece) - a, f);
+    fprintf(f, "\nPOINT_DATA %u\nSCALARS id unsigned_int 1\nLOOKUP_TABLE id_table\n", n);
+    fwrite(base + chunks[1].offset, 1, chunks[1].count * chunks[1].word, f);
+    fprintf(f, "\nFIELD FieldData %zu\n", chunks.size() - 2);
+    for (size_t k = 2; k < chunks.size(); k++) {
+        const ExportChunk &ch = chunks[k];
+        fprintf(f, "%s %d %u%s", vtk_name(field_name(ch.field)).c_str(), ch.comps, n,
+                is_uint_field(ch.field) ? " unsigned_int\n" : real_str);
+        fwrite(base + ch.offset, 1, ch.count * ch.word, f);
+        fprintf(f, "\n");
+    }
+    if (fclose(f) != 0) {
+        c->export_rc = SPHGB_ERR_ARGUMENT;
+        c->export_err = "export: write failed for " + path;
+    }
+}
+
+int export_join(sphgb_ctx *c)
+{
+    if (c->export_thread.joinable()) c->export_thread.join();
+    const int rc = c->export_rc;
+    if (rc) c->err = c->export_err;
+    c->export_rc = SPHGB_OK;
+    return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sphgb_export_wait(sphgb_ctx *c)
+{
+    if (!c) return SPHGB_ERR_ARGUMENT;
+    return export_join(c);
+}
+
+int sphgb_export_vtk(sphgb_ctx *c, const char *path, const int *fields, uint32_t nfields, int wait)
+{
+    if (!c || !path || (nfields && !fields)) return SPHGB_ERR_ARGUMENT;
+    if (!c->have_fluid) return fail(c, SPHGB_ERR_STATE, "no fluid uploaded");
+    cudaSetDevice(c->cfg.device);
+    int rc = export_join(c);   // one export in flight at a time
+    if (rc) return rc;
+    for (uint32_t k = 0; k < nfields; k++) {
+        const int f = fields[k];
+        if (!field_name(f) || f == SPHGB_FIELD_POSITION)
+            return fail(c, SPHGB_ERR_ARGUMENT, "field cannot be exported (boundary fields, or position twice)");
+        if (f == SPHGB_FIELD_FEATURES && !c->mlp_x) return fail(c, SPHGB_ERR_STATE, "features are not computed");
+    }
+    if (c->step_pending) {
+        sphgb_stats st;
+        fill_stats(c, &st);
+    }
+    const uint32_t n = c->n;
+    const int rword = c->fp64 ? 8 : 4;
+    // staging layout: positions, ids, then the requested fields; every chunk 256-byte aligned
+    std::vector<ExportChunk> chunks;
+    size_t off = 0;
+    auto add = [&](int field, int comps, int word) {
+        chunks.push_back({field, off, (size_t)n * comps, word, comps});
+        off += ((size_t)n * comps * word + 255) / 256 * 256;
+    };
+    add(-1, 3, rword);
+    add(SPHGB_FIELD_PARTICLE_ID, 1, 4);
+    for (uint32_t k = 0; k < nfields; k++)
+        add(fields[k], field_components(fields[k]), is_uint_field(fields[k]) ? 4 : rword);
+    const size_t bytes = std::max<size_t>(off, 256);
+    if (c->export_dev_bytes < bytes) {
+        if (c->export_dev) cudaFree(c->export_dev);
+        c->export_dev = nullptr;
+        c->export_dev_bytes = 0;
+        CK(cudaMalloc(&c->export_dev, bytes));
+        c->export_dev_bytes = bytes;
+    }
+    if (c->export_host_bytes < bytes) {
+        if (c->export_host) cudaFreeHost(c->export_host);
+        c->export_host = nullptr;
+        c->export_host_bytes = 0;
+        CK(cudaMallocHost(&c->export_host, bytes));
+        c->export_host_bytes = bytes;
+    }
+    if (!c->export_stream) {
+        CK(cudaStreamCreateWithFlags(&c->export_stream, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&c->export_start, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&c->export_scattered, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&c->export_copied, cudaEventDisableTiming));
+    }
+    // the export reads the state the last step left; it follows that step on its own stream
+    CK(cudaEventRecord(c->export_start, c->stream));
+    CK(cudaStreamWaitEvent(c->export_stream, c->export_start, 0));
+    char *dev = static_cast<char *>(c->export_dev);
+    for (const ExportChunk &ch : chunks) {
+        const int field = ch.field < 0 ? SPHGB_FIELD_POSITION : ch.field;
+        const int dt = is_uint_field(field) ? SPHGB_DTYPE_U32 : (c->fp64 ? SPHGB_DTYPE_F64 : SPHGB_DTYPE_F32);
+        if (c->fp64) {
+            launch_scatter_field<double>(make_params<double>(c), make_bufs<double>(c, 0), field, dev + ch.offset, dt,
+                                         c->export_stream);
+        } else {
+            launch_scatter_field<float>(make_params<float>(c), make_bufs<float>(c, 0), field, dev + ch.offset, dt,
+                                        c->export_stream);
+        }
+        launch_byteswap(dev + ch.offset, ch.count, ch.word, c->export_stream);
+    }
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(c->export_scattered, c->export_stream));
+    // later steps write the state set only after the scatter has read it
+    CK(cudaStreamWaitEvent(c->stream, c->export_scattered, 0));
+    CK(cudaMemcpyAsync(c->export_host, c->export_dev, off, cudaMemcpyDeviceToHost, c->export_stream));
+    CK(cudaEventRecord(c->export_copied, c->export_stream));
+    c->export_rc = SPHGB_OK;
+    c->export_thread = std::thread(write_vtk, c, std::string(path), n, chunks, c->fp64);
+    return wait ? export_join(c) : SPHGB_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// State files (SimulatorBase::saveState / loadState, SimulatorBase.cpp:1689-1870), written
+// from and read into the device copy.  Little-endian binary:
+//   "SPHGBST1", uint32 abi, precision, scenes S, lanes_log2 (0xffffffff: not chosen yet),
+//   sphgb_params, per scene {uint32 n, nb, prev_iters, pad; double dt, time, fmin[3], fmax[3]},
+//   double boundary positions [nb x 3] (upload order),
+//   uint32 ids [n] in device slot order, then in device slot order: position high part [n x 3]
+//   (float in FP32 mode, double in FP64 mode), position low part [n x 3] (float), velocity,
+//   velocity difference [n x 3], p / rho^2, p_v / rho^2 [n] (Real).
+// Saving the slot order and the grid extents keeps the next radix sort and cell grid identical,
+// so a loaded context continues bit for bit.
+// ===========================================================================
+namespace {
+
+constexpr char kStateMagic[8] = {'S', 'P', 'H', 'G', 'B', 'S', 'T', '1'};
+
+struct StateScene {
+    uint32_t n, nb, prev_iters, pad;
+    double dt, time, fmin[3], fmax[3];
+};
+
+// device slot order of the particles: the id of every occupied slot, scene by scene
+int slot_ids(sphgb_ctx *c, std::vector<uint32_t> &ids)
+{
+    ids.resize(c->n);
+    const uint32_t *dev = c->set_id[c->parity];
+    if (c->scn.size() <= 1) {
+        if (c->n) CK(cudaMemcpy(ids.data(), dev, (size_t)c->n * 4, cudaMemcpyDeviceToHost));
+        return SPHGB_OK;
+    }
+    for (const SceneHost &h : c->scn)
+        CK(cudaMemcpy(ids.data() + h.ustart, dev + h.pstart, (size_t)h.n * 4, cudaMemcpyDeviceToHost));
+    return SPHGB_OK;
+}
+
+template <class V> bool put_vec(FILE *f, const std::vector<V> &v) { return fwrite(v.data(), sizeof(V), v.size(), f) == v.size(); }
+template <class V> bool get_vec(FILE *f, std::vector<V> &v) { return fread(v.data(), sizeof(V), v.size(), f) == v.size(); }
+
+// field in id order -> the same field in slot order
+template <class V> std::vector<V> to_slots(const std::vector<V> &byid, const std::vector<uint32_t> &ids, int comps)
+{
+    std::vector<V> out(byid.size());
+    for (size_t k = 0; k < ids.size(); k++)
+        for (int q = 0; q < comps; q++) out[k * comps + q] = byid[(size_t)ids[k] * comps + q];
+    return out;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sphgb_save_state(sphgb_ctx *c, const char *path)
+{
+    if (!c || !path) return SPHGB_ERR_ARGUMENT;
+    if (!c->have_fluid) return fail(c, SPHGB_ERR_STATE, "no fluid uploaded");
+    cudaSetDevice(c->cfg.device);
+    int rc;
+    if (c->step_pending) {
+        sphgb_stats st;
+        fill_stats(c, &st);
+    }
+    const uint32_t n = c->n;
+    std::vector<uint32_t> ids;
+    if ((rc = slot_ids(c, ids))) return rc;
+    const int rdt = c->fp64 ? SPHGB_DTYPE_F64 : SPHGB_DTYPE_F32;
+    // fields in id order (Real or float), reordered to slot order
+    auto grab_real = [&](int field, int comps, std::vector<char> &out) -> int {
+        const size_t w = c->fp64 ? 8 : 4;
+        std::vector<char> byid((size_t)n * comps * w);
+        int r = n ? sphgb_download(c, field, byid.data(), rdt) : SPHGB_OK;
+        if (r) return r;
+        out.resize(byid.size());
+        for (size_t k = 0; k < n; k++)
+            std::memcpy(out.data() + k * comps * w, byid.data() + (size_t)ids[k] * comps * w, comps * w);
+        return SPHGB_OK;
+    };
+    std::vector<char> xhi, vel, vdiff, kp, kv;
+    std::vector<float> xlo_id((size_t)n * 3);
+    if ((rc = grab_real(SPHGB_FIELD_POSITION_HI, 3, xhi))) return rc;
+    if (n && (rc = sphgb_download(c, SPHGB_FIELD_POSITION_LO, xlo_id.data(), SPHGB_DTYPE_F32))) return rc;
+    if ((rc = grab_real(SPHGB_FIELD_VELOCITY, 3, vel))) return rc;
+    if ((rc = grab_real(SPHGB_FIELD_VDIFF, 3, vdiff))) return rc;
+    if ((rc = grab_real(SPHGB_FIELD_PRESSURE_RHO2, 1, kp))) return rc;
+    if ((rc = grab_real(SPHGB_FIELD_PRESSURE_RHO2_V, 1, kv))) return rc;
+    const std::vector<float> xlo = to_slots(xlo_id, ids, 3);
+
+    FILE *f = fopen(path, "wb");
+    if (!f) return fail(c, SPHGB_ERR_ARGUMENT, std::string("cannot open ") + path);
+    const uint32_t S = (uint32_t)c->scn.size();
+    const uint32_t hdr[4] = {SPHGB_ABI_VERSION, c->fp64 ? 1u : 0u, S, c->tuned ? c->lpp_log2 : 0xffffffffu};
+    bool ok = fwrite(kStateMagic, 1, 8, f) == 8 && fwrite(hdr, 4, 4, f) == 4 && fwrite(&c->prm, sizeof(sphgb_params), 1, f) == 1;
+    for (uint32_t s = 0; s < S && ok; s++) {
+        const SceneHost &h = c->scn[s];
+        StateScene r{h.n, h.nb, h.prev_iters, 0, h.dt, h.time, {h.fmin[0], h.fmin[1], h.fmin[2]},
+                     {h.fmax[0], h.fmax[1], h.fmax[2]}};
+        ok = fwrite(&r, sizeof r, 1, f) == 1;
+    }
+    ok = ok && put_vec(f, c->hb) && put_vec(f, ids) && put_vec(f, xhi) && put_vec(f, xlo) && put_vec(f, vel) &&
+         put_vec(f, vdiff) && put_vec(f, kp) && put_vec(f, kv);
+    if (fclose(f) != 0) ok = false;
+    return ok ? SPHGB_OK : fail(c, SPHGB_ERR_ARGUMENT, std::string("write failed: ") + path);
+}
+
+int sphgb_load_state(sphgb_ctx *c, const char *path)
+{
+    if (!c || !path) return SPHGB_ERR_ARGUMENT;
+    cudaSetDevice(c->cfg.device);
+    FILE *f = fopen(path, "rb");
+    if (!f) return fail(c, SPHGB_ERR_ARGUMENT, std::string("cannot open ") + path);
+    struct Closer { FILE *f; ~Closer() { fclose(f); } } closer{f};
+    char magic[8];
+    uint32_t hdr[4];
+    sphgb_params prm;
+    if (fread(magic, 1, 8, f) != 8 || std::memcmp(magic, kStateMagic, 8) != 0 || fread(hdr, 4, 4, f) != 4 ||
+        fread(&prm, sizeof prm, 1, f) != 1)
+        return fail(c, SPHGB_ERR_ARGUMENT, "not a state file of this library");
+    if (hdr[0] != SPHGB_ABI_VERSION) return fail(c, SPHGB_ERR_ARGUMENT, "state file of another ABI version");
+    if ((hdr[1] != 0) != c->fp64) return fail(c, SPHGB_ERR_ARGUMENT, "state file of the other precision");
+    const uint32_t S = hdr[2];
+    if (S == 0 || S > (1u << 24)) return fail(c, SPHGB_ERR_ARGUMENT, "bad scene count in state file");
+    std::vector<StateScene> sc(S);
+    if (!get_vec(f, sc)) return fail(c, SPHGB_ERR_ARGUMENT, "truncated state file");
+    size_t n = 0, nb = 0;
+    std::vector<uint32_t> counts(S), bcounts(S);
+    for (uint32_t s = 0; s < S; s++) {
+        counts[s] = sc[s].n;
+        bcounts[s] = sc[s].nb;
+        n += sc[s].n;
+        nb += sc[s].nb;
+    }
+    if (n >= 0xffffffffull || nb >= 0xffffffffull) return fail(c, SPHGB_ERR_ARGUMENT, "bad particle counts in state file");
+    const size_t w = c->fp64 ? 8 : 4;
+    std::vector<double> hb(nb * 3);
+    std::vector<uint32_t> ids(n);
+    std::vector<char> xhi(n * 3 * w), vel(n * 3 * w), vdiff(n * 3 * w), kp(n * w), kv(n * w);
+    std::vector<float> xlo(n * 3);
+    if (!get_vec(f, hb) || !get_vec(f, ids) || !get_vec(f, xhi) || !get_vec(f, xlo) || !get_vec(f, vel) ||
+        !get_vec(f, vdiff) || !get_vec(f, kp) || !get_vec(f, kv))
+        return fail(c, SPHGB_ERR_ARGUMENT, "truncated state file");
+    std::vector<char> seen(n, 0);
+    for (uint32_t id : ids) {
+        if (id >= n || seen[id]) return fail(c, SPHGB_ERR_ARGUMENT, "particle ids in the state file are not a permutation");
+        seen[id] = 1;
+    }
+    int rc;
+    if ((rc = sphgb_set_params(c, &prm))) return rc;
+    // fluid in the saved slot order with the saved ids (positions / velocities as double)
+    std::vector<double> x(n * 3), v(n * 3);
+    for (size_t k = 0; k < n * 3; k++) {
+        double hi, vv;
+        if (c->fp64) { std::memcpy(&hi, xhi.data() + k * 8, 8); std::memcpy(&vv, vel.data() + k * 8, 8); }
+        else {
+            float a, b;
+            std::memcpy(&a, xhi.data() + k * 4, 4);
+            std::memcpy(&b, vel.data() + k * 4, 4);
+            hi = a;
+            vv = b;
+        }
+        x[k] = hi;
+        v[k] = vv;
+    }
+    c->scn.clear();
+    c->hb.clear();
+    c->nb = 0;
+    c->have_boundary = false;
+    rc = c->fp64 ? init_scenes<double>(c, x.data(), v.data(), ids.data(), counts)
+                 : init_scenes<float>(c, x.data(), v.data(), ids.data(), counts);
+    if (rc) return rc;
+    static const double kNone[3] = {0, 0, 0};
+    if ((rc = set_boundary(c, nb ? hb.data() : kNone, bcounts))) return rc;
+    // exact fields in id order
+    auto by_id = [&](const std::vector<char> &slots, int comps) {
+        std::vector<char> out(slots.size());
+        const size_t e = comps * w;
+        for (size_t k = 0; k < n; k++) std::memcpy(out.data() + (size_t)ids[k] * e, slots.data() + k * e, e);
+        return out;
+    };
+    std::vector<float> xlo_id(n * 3);
+    for (size_t k = 0; k < n; k++)
+        for (int q = 0; q < 3; q++) xlo_id[(size_t)ids[k] * 3 + q] = xlo[k * 3 + q];
+    const int rdt = c->fp64 ? SPHGB_DTYPE_F64 : SPHGB_DTYPE_F32;
+    if (n) {
+        const std::vector<char> a = by_id(xhi, 3), b = by_id(vdiff, 3), d = by_id(kp, 1), e = by_id(kv, 1);
+        if ((rc = sphgb_upload_field(c, SPHGB_FIELD_POSITION_HI, a.data(), rdt))) return rc;
+        if ((rc = sphgb_upload_field(c, SPHGB_FIELD_POSITION_LO, xlo_id.data(), SPHGB_DTYPE_F32))) return rc;
+        if ((rc = sphgb_upload_field(c, SPHGB_FIELD_VDIFF, b.data(), rdt))) return rc;
+        if ((rc = sphgb_upload_field(c, SPHGB_FIELD_PRESSURE_RHO2, d.data(), rdt))) return rc;
+        if ((rc = sphgb_upload_field(c, SPHGB_FIELD_PRESSURE_RHO2_V, e.data(), rdt))) return rc;
+    }
+    // per-scene step size, time, CFL history and the grid extents fixed at the original upload
+    for (uint32_t s = 0; s < S; s++) {
+        SceneHost &h = c->scn[s];
+        h.dt = sc[s].dt;
+        h.time = sc[s].time;
+        h.prev_iters = sc[s].prev_iters;
+        for (int d = 0; d < 3; d++) { h.fmin[d] = sc[s].fmin[d]; h.fmax[d] = sc[s].fmax[d]; }
+    }
+    if (hdr[3] <= 2) {   // the lanes per particle the saved context ran with
+        c->lpp_log2 = hdr[3];
+        c->tuned = true;
+    }
+    c->dt = c->scn[0].dt;
+    c->scalars_dirty = true;
+    invalidate_graphs(c);
     return SPHGB_OK;
 }
 

@@ -1647,6 +1647,14 @@ __global__ void k_scatter_field(DevParams<T> P, DevBufs<T> B, int field, void *o
         if (B.mlp_x)
             for (int c = 0; c < 10; c++) put<T>(out, odt, 10 * (size_t)d + c, (double)B.mlp_x[(size_t)k * 10 + c]);
         break;
+    case SPHGB_FIELD_POSITION_HI: vec(B.x, nullptr); break;
+    case SPHGB_FIELD_POSITION_LO: {
+        const float4 l = B.xlo ? B.xlo[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+        put<T>(out, odt, 3 * (size_t)d, (double)l.x);
+        put<T>(out, odt, 3 * (size_t)d + 1, (double)l.y);
+        put<T>(out, odt, 3 * (size_t)d + 2, (double)l.z);
+        break;
+    }
     default: break;
     }
 }
@@ -1671,7 +1679,37 @@ __global__ void k_upload_field(DevParams<T> P, DevBufs<T> B, int field, const vo
     case SPHGB_FIELD_VDIFF: vec(B.vdiff, nullptr); break;
     case SPHGB_FIELD_PRESSURE_RHO2: B.kappa[k] = (T)get<T>(in, idt, d); break;
     case SPHGB_FIELD_PRESSURE_RHO2_V: B.kappa_v[k] = (T)get<T>(in, idt, d); break;
+    case SPHGB_FIELD_POSITION_HI: {   // the stored high part; the low part is left as it is
+        v4_t<T> a = ldv(B.x, k);
+        a.x = (T)get<T>(in, idt, 3 * (size_t)d);
+        a.y = (T)get<T>(in, idt, 3 * (size_t)d + 1);
+        a.z = (T)get<T>(in, idt, 3 * (size_t)d + 2);
+        stv(B.x, k, a);
+        break;
+    }
+    case SPHGB_FIELD_POSITION_LO:
+        if (B.xlo)
+            B.xlo[k] = make_float4((float)get<T>(in, idt, 3 * (size_t)d), (float)get<T>(in, idt, 3 * (size_t)d + 1),
+                                   (float)get<T>(in, idt, 3 * (size_t)d + 2), 0.f);
+        break;
     default: break;
+    }
+}
+
+// Big-endian copy of n words of `bytes` bytes each (4 or 8), in place (file formats such as
+// legacy VTK store big-endian binary data)
+__global__ void k_byteswap(void *data, size_t n, int bytes)
+{
+    const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    if (bytes == 8) {
+        unsigned long long *p = static_cast<unsigned long long *>(data) + k;
+        const unsigned long long v = *p;
+        const uint32_t lo = (uint32_t)v, hi = (uint32_t)(v >> 32);
+        *p = ((unsigned long long)__byte_perm(lo, 0, 0x0123) << 32) | (unsigned long long)__byte_perm(hi, 0, 0x0123);
+    } else {
+        uint32_t *p = static_cast<uint32_t *>(data) + k;
+        *p = __byte_perm(*p, 0, 0x0123);
     }
 }
 
@@ -1877,6 +1915,10 @@ template <class T> void launch_inverse_perm(const DevParams<T> &P, const uint32_
     if (P.np) k_inverse_perm<T><<<grid_for(P.np), kBlock, 0, s>>>(P, id, inv);
 }
 void launch_delay(cudaStream_t s, unsigned ns) { k_delay<<<1, 32, 0, s>>>(ns); }
+void launch_byteswap(void *data, size_t n, int bytes, cudaStream_t s)
+{
+    if (n) k_byteswap<<<(unsigned)((n + kBlock - 1) / kBlock), kBlock, 0, s>>>(data, n, bytes);
+}
 
 void launch_lists_to_ids(const uint32_t *list, const uint32_t *cnt, uint32_t cap, const uint32_t *id, const uint32_t *inv,
                          const uint32_t *bid, int kind, uint32_t lpp_log2, const uint32_t *offsets, uint32_t *out,

@@ -191,6 +191,7 @@ void launch_lists_to_ids(const uint32_t *list, const uint32_t *cnt, uint32_t cap
                          const uint32_t *inv, const uint32_t *bid, int kind, uint32_t lpp_log2,
                          const uint32_t *offsets, uint32_t *out, uint32_t n, cudaStream_t s);
 void launch_delay(cudaStream_t s, unsigned ns);
+void launch_byteswap(void *data, size_t n, int bytes, cudaStream_t s);
 
 // radix sort of (key, value) pairs, LSD, 8-bit digits, stable.  keys/vals are
 // ping-ponged with keys2/vals2; returns true if the result ended in keys2/vals2.

@@ -37,6 +37,8 @@ FIELDS = {
     "boundary volume": (14, 1),
     "boundary position": (15, 3),
     "features": (16, 10),
+    "position high": (17, 3),
+    "position low": (18, 3),
 }
 DTYPE_F32, DTYPE_F64, DTYPE_U32 = 0, 1, 2
 
@@ -120,6 +122,7 @@ EXPORTS = [
     "sphgb_num_particles", "sphgb_get_stream", "sphgb_profile_enable", "sphgb_profile_reset", "sphgb_profile_read",
     "sphgb_set_warmstart_mlp", "sphgb_set_feature_output", "sphgb_upload_scenes", "sphgb_num_scenes",
     "sphgb_scene_stats", "sphgb_set_warmstart_gate", "sphgb_set_lanes_per_particle", "sphgb_get_lanes_per_particle",
+    "sphgb_export_vtk", "sphgb_export_wait", "sphgb_save_state", "sphgb_load_state",
 ]
 
 _lib = None
@@ -170,6 +173,10 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.sphgb_set_warmstart_gate.argtypes = [vp, u32, u32]
     L.sphgb_set_lanes_per_particle.argtypes = [vp, u32]
     L.sphgb_get_lanes_per_particle.argtypes = [vp, ctypes.POINTER(u32), vp]
+    L.sphgb_export_vtk.argtypes = [vp, ctypes.c_char_p, vp, u32, i32]
+    L.sphgb_export_wait.argtypes = [vp]
+    L.sphgb_save_state.argtypes = [vp, ctypes.c_char_p]
+    L.sphgb_load_state.argtypes = [vp, ctypes.c_char_p]
     L.sphgb_profile_enable.argtypes = [vp, i32]
     L.sphgb_profile_reset.argtypes = [vp]
     L.sphgb_profile_read.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_uint64),
@@ -448,6 +455,22 @@ class Context:
         t = np.zeros(3, np.float32)
         self._check(self.L.sphgb_get_lanes_per_particle(self.h, ctypes.byref(k), _p(t)))
         return int(k.value), [float(v) for v in t]
+
+    def export_vtk(self, path: str, fields=(), wait: bool = True):
+        """Legacy VTK file of all fluid particles (positions, ids and the named fields), written
+        from the device copy; with wait=False the copy and the write overlap the next steps."""
+        ids = np.array([FIELDS[f][0] for f in fields], np.int32)
+        self._check(self.L.sphgb_export_vtk(self.h, os.fsencode(path), _p(ids) if ids.size else None, ids.size,
+                                            int(wait)))
+
+    def export_wait(self):
+        self._check(self.L.sphgb_export_wait(self.h))
+
+    def save_state(self, path: str):
+        self._check(self.L.sphgb_save_state(self.h, os.fsencode(path)))
+
+    def load_state(self, path: str):
+        self._check(self.L.sphgb_load_state(self.h, os.fsencode(path)))
 
     def set_feature_output(self, on: bool = True):
         self._check(self.L.sphgb_set_feature_output(self.h, int(on)))
