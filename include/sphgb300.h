@@ -290,6 +290,28 @@ int sphgb_set_lanes_per_particle(sphgb_ctx *ctx, uint32_t lanes);
 /* the lanes in use and the autotuner's trial step times in ms for 1, 2, 4 lanes (zeros when fixed) */
 int sphgb_get_lanes_per_particle(const sphgb_ctx *ctx, uint32_t *lanes, float trial_ms[3]);
 
+/* Dynamic boundary bodies: the forces and torques the fluid exerts on them, the device-side
+ * counterpart of BoundaryModel::addForce / getForceAndTorque / clearForceAndTorque
+ * (SPlisHSPlasH/BoundaryModel.h:38-49, 86-87; read and cleared by the boundary simulator each
+ * step, Simulator/BoundarySimulator.cpp:8-25).  body[k] < nbodies is the body of boundary
+ * particle k in upload order (a batch: all scenes' boundaries in scene order); center[3 b] is
+ * body b's reference point for torques (RigidBodyObject::getPosition); dynamic[b] != 0 marks a
+ * body that collects forces (RigidBodyObject::isDynamic), dynamic == NULL marks every body
+ * dynamic.  Every step adds, for each dynamic body, the boundary terms of the divergence and
+ * pressure solves' final pressure accelerations (TimeStepDFSPH.cpp:359, 514), of XSPH
+ * (XSPH.cpp:183-203) and of Weiler2018 viscosity (Viscosity_Weiler2018.cpp:960-975): force
+ * sum f and torque sum (x_b - center) x f, summed in FP64 in a fixed order (deterministic).
+ * The boundary stays static (v_b = 0); moving a body is the caller's rigid-body solver, which
+ * re-uploads the boundary.  Setting the bodies (nbodies == 0 removes them) zeroes the
+ * accumulators; uploading a boundary of another particle count removes them. */
+int sphgb_set_boundary_bodies(sphgb_ctx *ctx, const uint32_t *body, uint32_t nbodies, const double *center,
+                              const int *dynamic);
+/* the sums since the last clear, force[3 nbodies] and torque[3 nbodies] (either may be NULL;
+ * zeros for static bodies); waits for the context's stream */
+int sphgb_boundary_forces(sphgb_ctx *ctx, double *force, double *torque);
+/* zero the sums, ordered after the steps already enqueued */
+int sphgb_clear_boundary_forces(sphgb_ctx *ctx);
+
 /* the cudaStream_t every kernel of this context is launched on (for event timing by callers) */
 int sphgb_get_stream(const sphgb_ctx *ctx, void **stream);
 

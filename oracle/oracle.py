@@ -80,6 +80,12 @@ class OrcState(ctypes.Structure):
         ("density_adv_v", ctypes.c_void_p),
         ("num_fluid_neighbors", ctypes.c_void_p),
         ("num_boundary_neighbors", ctypes.c_void_p),
+        ("body", ctypes.c_void_p),
+        ("nbodies", ctypes.c_uint),
+        ("body_center", ctypes.c_void_p),
+        ("body_dynamic", ctypes.c_void_p),
+        ("body_force", ctypes.c_void_p),
+        ("body_torque", ctypes.c_void_p),
     ]
 
 
@@ -165,8 +171,9 @@ class OracleSim:
         self.cp = make_params(scene.params, fp32_predicate, num_threads)
         n, nb = scene.n, scene.nb
         self.n, self.nb = n, nb
-        self.x = np.ascontiguousarray(scene.x, dtype=dt)
-        self.v = np.ascontiguousarray(scene.v, dtype=dt)
+        # own copies: stepping must not write into the scene's arrays
+        self.x = np.array(scene.x, dtype=dt, order="C", copy=True)
+        self.v = np.array(scene.v, dtype=dt, order="C", copy=True)
         self.a = np.zeros((n, 3), dt)
         self.density = np.zeros(n, dt)
         self.factor = np.zeros(n, dt)
@@ -175,7 +182,7 @@ class OracleSim:
         self.kappa_v = np.zeros(n, dt)
         self.pressure_accel = np.zeros((n, 3), dt)
         self.vdiff = np.zeros((n, 3), dt)
-        self.xb = np.ascontiguousarray(scene.xb, dtype=dt)
+        self.xb = np.array(scene.xb, dtype=dt, order="C", copy=True)
         self.Vb = np.zeros(nb, dt)
         self.factor_raw = np.zeros(n, dt)
         self.density_adv_v = np.zeros(n, dt)
@@ -194,6 +201,26 @@ class OracleSim:
         self.st.num_boundary_neighbors = _ptr(self.nbn)
         self.st.dt = scene.params.timeStepSize
         self.st.time = 0.0
+
+    def set_bodies(self, body, center, dynamic=None):
+        """Bodies of the boundary particles (upload order), reference points and dynamic flags;
+        forces accumulate in body_force / body_torque until clear_forces()."""
+        self.body = np.ascontiguousarray(body, np.uint32)
+        self.body_center = np.ascontiguousarray(center, np.float64).reshape(-1, 3)
+        nbodies = self.body_center.shape[0]
+        self.body_dynamic = np.ones(nbodies, np.int32) if dynamic is None else np.ascontiguousarray(dynamic, np.int32)
+        self.body_force = np.zeros((nbodies, 3), np.float64)
+        self.body_torque = np.zeros((nbodies, 3), np.float64)
+        self.st.body = _ptr(self.body)
+        self.st.nbodies = nbodies
+        self.st.body_center = _ptr(self.body_center)
+        self.st.body_dynamic = _ptr(self.body_dynamic)
+        self.st.body_force = _ptr(self.body_force)
+        self.st.body_torque = _ptr(self.body_torque)
+
+    def clear_forces(self):
+        self.body_force[:] = 0.0
+        self.body_torque[:] = 0.0
 
     def step(self):
         rc = self.lib.orc_step(ctypes.byref(self.st), ctypes.byref(self.cp))

@@ -444,6 +444,44 @@ static void pressure_accel(ctx_t *c, const real *kap)
     }
 }
 
+/* BoundaryModel::addForce (BoundaryModel.h:38-49): force f at x_b on the body of boundary
+ * particle j, torque (x_b - c) x f; only dynamic bodies collect.  Serial (deterministic). */
+static void add_force(orc_state *s, unsigned j, const double f[3])
+{
+    if (!s->body || !s->body_force) return;
+    const unsigned b = s->body[j];
+    if (b >= s->nbodies || (s->body_dynamic && !s->body_dynamic[b])) return;
+    const double *c = s->body_center + 3 * (size_t)b;
+    const double r[3] = {(double)s->xb[3 * (size_t)j] - c[0], (double)s->xb[3 * (size_t)j + 1] - c[1],
+                         (double)s->xb[3 * (size_t)j + 2] - c[2]};
+    double *F = s->body_force + 3 * (size_t)b, *T = s->body_torque + 3 * (size_t)b;
+    F[0] += f[0]; F[1] += f[1]; F[2] += f[2];
+    T[0] += r[1] * f[2] - r[2] * f[1];
+    T[1] += r[2] * f[0] - r[0] * f[2];
+    T[2] += r[0] * f[1] - r[1] * f[0];
+}
+
+/* computePressureAccel with applyBoundaryForces (TimeStepDFSPH.cpp:1337-1344):
+ * a = kappa_i (-V_b gradW_ib), force on the boundary -m_i a. */
+static void boundary_pressure_forces(ctx_t *c, const real *kap)
+{
+    orc_state *s = c->s;
+    if (!s->body || !s->body_force) return;
+    for (long i = 0; i < (long)s->n; i++) {
+        const double pi = (double)kap[i];
+        if (!(fabs(pi) > c->eps)) continue;
+        for (unsigned k = c->B.off[i]; k < c->B.off[i + 1]; k++) {
+            const unsigned j = c->B.idx[k];
+            double r[3], g[3], f[3];
+            diffv(s->x + 3 * i, s->xb + 3 * (size_t)j, r);
+            kGradW(&c->K, r, g);
+            const double Vj = (double)s->Vb[j];
+            for (int d = 0; d < 3; d++) f[d] = -c->mass * (pi * (-Vj * g[d]));
+            add_force(s, j, f);
+        }
+    }
+}
+
 /* compute_aij_pj, scalar path (TimeStepDFSPH.cpp:1370-1420). */
 static double aij_pj(const ctx_t *c, long i)
 {
@@ -521,6 +559,7 @@ static void divergence_solve(ctx_t *c, double h, double *err_buf)
     s->iterations_v = it;
     s->avg_density_err_v = avg;
     pressure_accel(c, s->kappa_v);
+    boundary_pressure_forces(c, s->kappa_v);
 #pragma omp parallel for schedule(static)
     for (long i = 0; i < n; i++) {
         for (int d = 0; d < 3; d++)
@@ -573,6 +612,7 @@ static void pressure_solve(ctx_t *c, double h, double *err_buf)
     s->iterations = it;
     s->avg_density_err = avg;
     pressure_accel(c, s->kappa);
+    boundary_pressure_forces(c, s->kappa);
 #pragma omp parallel for schedule(static)
     for (long i = 0; i < n; i++)
         for (int d = 0; d < 3; d++)
@@ -611,6 +651,20 @@ static void xsph(ctx_t *c, double h)
         }
         for (int d = 0; d < 3; d++) s->a[3 * i + d] = (real)((double)s->a[3 * i + d] + ai[d]);
     }
+    /* boundary feedback of the XSPH boundary term (XSPH.cpp:183-203): force -m_i a_ib */
+    if (cb != 0.0 && s->body && s->body_force)
+        for (long i = 0; i < (long)s->n; i++) {
+            const real *xi = s->x + 3 * i, *vi = s->v + 3 * i;
+            const double rhoi = (double)s->density[i];
+            for (unsigned k = c->B.off[i]; k < c->B.off[i + 1]; k++) {
+                const unsigned j = c->B.idx[k];
+                double r[3], f[3];
+                diffv(xi, s->xb + 3 * (size_t)j, r);
+                const double w = invH * cb * (c->rho0 * (double)s->Vb[j] / rhoi) * kW(&c->K, sqrt(dot3(r, r)));
+                for (int d = 0; d < 3; d++) f[d] = -c->mass * (-w * (double)vi[d]);
+                add_force(s, j, f);
+            }
+        }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -836,6 +890,25 @@ static int viscosity_weiler(ctx_t *c, double dt)
         const double dv = (double)x[k] - (double)s->v[k];
         s->a[k] = (real)((double)s->a[k] + (1.0 / dt) * dv);
         s->vdiff[k] = (real)dv;
+    }
+    /* boundary feedback of applyForces (Viscosity_Weiler2018.cpp:960-975), static v_b = 0:
+     * a = d mub (rho0 V_b / rho_i) (v_i'.x_ib) / (|x_ib|^2 + 0.01 h^2) gradW_ib, force -m_i / rho_i a */
+    const double mub = c->p->viscosity_boundary * c->rho0;
+    if (mub != 0.0 && s->body && s->body_force) {
+        const double h2 = c->K.h * c->K.h;
+        for (long i = 0; i < (long)s->n; i++) {
+            const double rhoi = (double)s->density[i];
+            const double nv[3] = {(double)x[3 * i], (double)x[3 * i + 1], (double)x[3 * i + 2]};
+            for (unsigned k = c->B.off[i]; k < c->B.off[i + 1]; k++) {
+                const unsigned j = c->B.idx[k];
+                double r[3], g[3], f[3];
+                diffv(s->x + 3 * i, s->xb + 3 * (size_t)j, r);
+                kGradW(&c->K, r, g);
+                const double coef = 10.0 * mub * (c->rho0 * (double)s->Vb[j] / rhoi) * dot3(nv, r) / (dot3(r, r) + 0.01 * h2);
+                for (int d = 0; d < 3; d++) f[d] = -c->mass / rhoi * (coef * g[d]);
+                add_force(s, j, f);
+            }
+        }
     }
     free(b); free(x); free(inv9);
     return rc;

@@ -70,6 +70,19 @@ typedef struct orc_state {
     orc_real *factor_raw;                 /* alpha right after computeDFSPHFactor */
     orc_real *density_adv_v;              /* divergence source (unclamped) */
     unsigned *num_fluid_neighbors, *num_boundary_neighbors;
+    /* optional dynamic-boundary feedback (BoundaryModel::addForce, BoundaryModel.h:38-49):
+     * body index of every boundary particle, the bodies' reference points (rigid-body
+     * positions) and dynamic flags.  orc_step adds to body_force / body_torque (the caller
+     * clears them, like clearForceAndTorque) the forces the fluid exerts on the dynamic bodies
+     * during the step: the final pressure
+     * accelerations of both solvers (TimeStepDFSPH.cpp:359, 514 with :1342-1343), the XSPH
+     * boundary term (XSPH.cpp:183-203) and the Weiler2018 boundary term
+     * (Viscosity_Weiler2018.cpp:960-975); torque about the reference point. */
+    const unsigned *body;
+    unsigned nbodies;
+    const double *body_center;            /* 3 nbodies */
+    const int *body_dynamic;              /* nbodies */
+    double *body_force, *body_torque;     /* 3 nbodies */
 } orc_state;
 
 /* Cubic spline (SPHKernels.h:16-91). */

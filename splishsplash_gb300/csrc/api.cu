@@ -116,6 +116,15 @@ struct sphgb_ctx {
     std::string export_err;
     float *feat = nullptr, *mlp_x = nullptr, *mlp_y = nullptr;
     void *kl = nullptr, *pa2 = nullptr;
+    // dynamic boundary bodies: body of each boundary particle (upload order), reference points and
+    // flags on the host; accumulators (own allocations, kept across uploads) and the slot tables
+    // (prepared set, rebuilt with the boundary sort)
+    std::vector<uint32_t> body_of;
+    std::vector<double> body_center;
+    std::vector<int> body_dynamic;
+    uint32_t nbodies = 0;
+    std::vector<void *> body_allocs;
+    BodyDev bodies{};
     // per-kernel CUDA-event timing (host-loop mode only)
     bool profile = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -132,13 +141,13 @@ namespace {
 enum KernelId {
     K_STEP_BEGIN, K_KEYS, K_SORT, K_GATHER, K_CELL_RANGES, K_BUILD, K_LOOP_BEGIN, K_PRESSURE_ACCEL, K_JACOBI,
     K_SOLVER_FINALIZE, K_XSPH, K_VISC_SETUP, K_CG_MATVEC, K_CG_UPDATE, K_CG_P, K_KICK, K_PRESS_INIT, K_INTEGRATE,
-    K_FEATURES, K_MLP, K_WS_SELECT,
+    K_FEATURES, K_MLP, K_WS_SELECT, K_BODY_FORCES,
     K_COUNT
 };
 const char *kKernelNames[K_COUNT] = {
     "step_begin", "keys", "radix_sort", "gather", "cell_ranges", "build_lists_density_alpha", "loop_begin",
     "pressure_accel", "jacobi_update", "solver_finalize", "xsph_gravity", "visc_setup", "cg_matvec", "cg_update",
-    "cg_p", "kick_cfl", "press_init", "integrate", "features", "mlp_infer", "warmstart_select",
+    "cg_p", "kick_cfl", "press_init", "integrate", "features", "mlp_infer", "warmstart_select", "body_forces",
 };
 
 // Brackets the launches of one kernel class with events on the context stream
@@ -235,7 +244,37 @@ void free_prepared(sphgb_ctx *c)
     c->cstart = c->cend = c->bcstart = c->bcend = nullptr;
     c->xb = c->bscratch = nullptr;
     c->bid = c->bscene = nullptr;
+    c->bodies.slot = nullptr;
+    c->bodies.blk = nullptr;
+    c->bodies.body_nblk = nullptr;
+    c->bodies.partials = nullptr;
+    c->bodies.nblk = 0;
     c->prepared = false;
+}
+
+// the slot tables of the bodies (part of the prepared set)
+void drop_body_tables(sphgb_ctx *c)
+{
+    for (void *p : {(void *)c->bodies.slot, (void *)c->bodies.blk, (void *)c->bodies.body_nblk,
+                    (void *)c->bodies.partials})
+        if (p) dfree(c->prep_allocs, p);
+    c->bodies.slot = nullptr;
+    c->bodies.blk = nullptr;
+    c->bodies.body_nblk = nullptr;
+    c->bodies.partials = nullptr;
+    c->bodies.nblk = 0;
+}
+
+void free_bodies(sphgb_ctx *c)
+{
+    drop_body_tables(c);
+    for (void *p : c->body_allocs) cudaFree(p);
+    c->body_allocs.clear();
+    c->bodies = BodyDev{};
+    c->body_of.clear();
+    c->body_center.clear();
+    c->body_dynamic.clear();
+    c->nbodies = 0;
 }
 
 void free_all(sphgb_ctx *c)
@@ -437,6 +476,56 @@ int bits_for(size_t v)
     return b;
 }
 
+// Slot tables of the dynamic bodies after the boundary sort: the sorted boundary slots whose
+// particle belongs to a dynamic body, grouped by body (counting sort, slot order kept within a
+// body), and the block table of the force gather (blocks of kBlock entries, never two bodies).
+int build_body_tables(sphgb_ctx *c)
+{
+    c->bodies.nblk = 0;
+    if (c->nbodies == 0 || c->nb == 0) return SPHGB_OK;
+    std::vector<uint32_t> bid(c->nb);
+    CK(cudaMemcpy(bid.data(), c->bid, (size_t)c->nb * 4, cudaMemcpyDeviceToHost));
+    const uint32_t B = c->nbodies;
+    std::vector<uint32_t> count(B + 1, 0);
+    for (uint32_t k = 0; k < c->nb; k++) {
+        const uint32_t b = c->body_of[bid[k]];
+        if (c->body_dynamic[b]) count[b + 1]++;
+    }
+    for (uint32_t b = 0; b < B; b++) count[b + 1] += count[b];
+    const uint32_t entries = count[B];
+    if (entries == 0) return SPHGB_OK;
+    std::vector<uint32_t> slot(entries), fill(count.begin(), count.end() - 1);
+    for (uint32_t k = 0; k < c->nb; k++) {
+        const uint32_t b = c->body_of[bid[k]];
+        if (c->body_dynamic[b]) slot[fill[b]++] = k;
+    }
+    std::vector<uint4> blk;
+    std::vector<uint32_t> nblk(B, 0);
+    for (uint32_t b = 0; b < B; b++) {
+        const uint32_t first = (uint32_t)blk.size();
+        for (uint32_t e = count[b]; e < count[b + 1]; e += kBlock)
+            blk.push_back(make_uint4(b, e, std::min(e + (uint32_t)kBlock, count[b + 1]), first));
+        nblk[b] = (uint32_t)blk.size() - first;
+    }
+    uint32_t *d_slot, *d_nblk;
+    uint4 *d_blk;
+    double *d_part;
+    int rc;
+    if ((rc = palloc(c, &d_slot, (size_t)entries * 4))) return rc;
+    if ((rc = palloc(c, &d_blk, blk.size() * sizeof(uint4)))) return rc;
+    if ((rc = palloc(c, &d_nblk, (size_t)B * 4))) return rc;
+    if ((rc = palloc(c, &d_part, blk.size() * 6 * sizeof(double)))) return rc;
+    CK(cudaMemcpy(d_slot, slot.data(), (size_t)entries * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_blk, blk.data(), blk.size() * sizeof(uint4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_nblk, nblk.data(), (size_t)B * 4, cudaMemcpyHostToDevice));
+    c->bodies.slot = d_slot;
+    c->bodies.blk = d_blk;
+    c->bodies.body_nblk = d_nblk;
+    c->bodies.partials = d_part;
+    c->bodies.nblk = (uint32_t)blk.size();
+    return SPHGB_OK;
+}
+
 // Build each scene's cell grid over the union of its fluid and boundary extents,
 // sort the boundary particles into it and compute their Akinci2012 volumes.
 template <class T> int prepare(sphgb_ctx *c)
@@ -530,6 +619,7 @@ template <class T> int prepare(sphgb_ctx *c)
                         (void *)cells, (void *)hist})
             if (p) dfree(c->prep_allocs, p);
     }
+    if ((rc = build_body_tables(c))) return rc;
     c->prepared = true;
     return SPHGB_OK;
 }
@@ -570,6 +660,13 @@ int read_cont(sphgb_ctx *c, unsigned *cont)
     CK(cudaStreamSynchronize(c->stream));
     *cont = hg->cont;
     return SPHGB_OK;
+}
+
+// The body-force gather before the kick has terms to collect: the divergence solve's pressure,
+// the XSPH boundary term or the Weiler2018 boundary term.
+template <class T> bool body_phase0(const sphgb_ctx *c, const DevParams<T> &P)
+{
+    return c->bodies.nblk && (P.div_on || P.xsph_b != T(0) || (P.visc_on && P.mub != T(0)));
 }
 
 // Enqueue the launches that precede the solver loops.
@@ -642,9 +739,11 @@ template <class T> int step_host_loop(sphgb_ctx *c)
             { PROF(K_CG_P, s); launch_cg_p<T>(P, B1, s); }
         }
     }
+    if (body_phase0(c, P)) { PROF(K_BODY_FORCES, s); launch_body_forces<T>(P, B1, c->bodies, 0, s); }
     { PROF(K_KICK, s); launch_kick<T>(P, B1, s); }
     { PROF(K_PRESS_INIT, s); launch_press_init<T>(P, B1, s); }
     if ((rc = solve(false))) return rc;
+    { PROF(K_BODY_FORCES, s); launch_body_forces<T>(P, B1, c->bodies, 1, s); }
     { PROF(K_INTEGRATE, s); launch_integrate<T>(P, B1, s); }
     CK(cudaGetLastError());
     prof_resolve(c);
@@ -741,9 +840,11 @@ template <class T> int build_graph(sphgb_ctx *c, int parity, cudaGraphExec_t *ou
             });
         }
     }
+    if (body_phase0(c, P)) launch_body_forces<T>(P, B1, c->bodies, 0, s);
     launch_kick<T>(P, B1, s);
     launch_press_init<T>(P, B1, s);
     solve(false);
+    launch_body_forces<T>(P, B1, c->bodies, 1, s);
     launch_integrate<T>(P, B1, s);
     cudaGraph_t done = nullptr;
     cudaError_t e2 = cudaStreamEndCapture(s, &done);
@@ -768,6 +869,10 @@ template <class T> int autotune(sphgb_ctx *c)
     std::vector<StepScalars> saved(S + 1);
     CK(cudaStreamSynchronize(c->stream));
     CK(cudaMemcpy(saved.data(), c->sc, (S + 1) * sizeof(StepScalars), cudaMemcpyDeviceToHost));
+    // the trial steps also add to the body accumulators
+    std::vector<double> saved_acc(6 * (size_t)c->nbodies);
+    if (c->nbodies)
+        CK(cudaMemcpy(saved_acc.data(), c->bodies.acc, saved_acc.size() * sizeof(double), cudaMemcpyDeviceToHost));
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
@@ -792,6 +897,8 @@ template <class T> int autotune(sphgb_ctx *c)
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc) return rc;
+    if (c->nbodies)
+        CK(cudaMemcpy(c->bodies.acc, saved_acc.data(), saved_acc.size() * sizeof(double), cudaMemcpyHostToDevice));
     CK(cudaGetLastError());
     uint32_t pick = 2;
     for (uint32_t lg = 0; lg <= 2; lg++) {
@@ -1075,6 +1182,11 @@ int set_boundary(sphgb_ctx *c, const double *xb, const std::vector<uint32_t> &co
     if (total > 0xffffffffull) return fail(c, SPHGB_ERR_ARGUMENT, "too many boundary particles");
     c->hb.assign(xb, xb + 3 * total);
     c->nb = (uint32_t)total;
+    // bodies are given per boundary particle: a boundary of another size drops them
+    if (c->nbodies && c->body_of.size() != total) {
+        if (c->stream) cudaStreamSynchronize(c->stream);
+        free_bodies(c);
+    }
     if (c->scn.size() < counts.size()) c->scn.resize(counts.size());
     uint32_t b = 0;
     for (uint32_t s = 0; s < c->scn.size(); s++) {
@@ -1195,6 +1307,7 @@ int sphgb_destroy(sphgb_ctx *c)
     if (c->export_thread.joinable()) c->export_thread.join();
     if (c->export_stream) cudaStreamSynchronize(c->export_stream);
     free_all(c);
+    free_bodies(c);
     if (c->hsc) cudaFreeHost(c->hsc);
     if (c->export_dev) cudaFree(c->export_dev);
     if (c->export_host) cudaFreeHost(c->export_host);
@@ -1459,6 +1572,73 @@ int sphgb_get_lanes_per_particle(const sphgb_ctx *c, uint32_t *lanes, float tria
     *lanes = 1u << c->lpp_log2;
     if (trial_ms)
         for (int k = 0; k < 3; k++) trial_ms[k] = c->tune_ms[k];
+    return SPHGB_OK;
+}
+
+int sphgb_set_boundary_bodies(sphgb_ctx *c, const uint32_t *body, uint32_t nbodies, const double *center,
+                              const int *dynamic)
+{
+    if (!c) return SPHGB_ERR_ARGUMENT;
+    if (nbodies && (!body || !center)) return SPHGB_ERR_ARGUMENT;
+    if (nbodies && !c->have_boundary) return fail(c, SPHGB_ERR_STATE, "no boundary uploaded");
+    for (uint32_t k = 0; nbodies && k < c->nb; k++)
+        if (body[k] >= nbodies) return fail(c, SPHGB_ERR_ARGUMENT, "body index out of range");
+    int rc;
+    if (nbodies && (rc = check_finite(c, center, 3 * (size_t)nbodies, "body reference point"))) return rc;
+    cudaSetDevice(c->cfg.device);
+    CK(cudaStreamSynchronize(c->stream));
+    free_bodies(c);
+    invalidate_graphs(c);
+    if (nbodies == 0) return SPHGB_OK;
+    c->body_of.assign(body, body + c->nb);
+    c->body_center.assign(center, center + 3 * (size_t)nbodies);
+    c->body_dynamic.assign(nbodies, 1);
+    if (dynamic)
+        for (uint32_t b = 0; b < nbodies; b++) c->body_dynamic[b] = dynamic[b] != 0;
+    c->nbodies = nbodies;
+    double *acc, *cen;
+    unsigned *cnt;
+    if ((rc = dalloc_into(c, c->body_allocs, &acc, 6 * (size_t)nbodies * sizeof(double))) ||
+        (rc = dalloc_into(c, c->body_allocs, &cen, 3 * (size_t)nbodies * sizeof(double))) ||
+        (rc = dalloc_into(c, c->body_allocs, &cnt, (size_t)nbodies * sizeof(unsigned)))) {
+        free_bodies(c);
+        return rc;
+    }
+    CK(cudaMemset(acc, 0, 6 * (size_t)nbodies * sizeof(double)));
+    CK(cudaMemset(cnt, 0, (size_t)nbodies * sizeof(unsigned)));
+    CK(cudaMemcpy(cen, center, 3 * (size_t)nbodies * sizeof(double), cudaMemcpyHostToDevice));
+    c->bodies.acc = acc;
+    c->bodies.center = cen;
+    c->bodies.counters = cnt;
+    if (c->prepared && (rc = build_body_tables(c))) {
+        free_bodies(c);
+        return rc;
+    }
+    return SPHGB_OK;
+}
+
+int sphgb_boundary_forces(sphgb_ctx *c, double *force, double *torque)
+{
+    if (!c) return SPHGB_ERR_ARGUMENT;
+    if (c->nbodies == 0) return SPHGB_OK;
+    cudaSetDevice(c->cfg.device);
+    std::vector<double> acc(6 * (size_t)c->nbodies);
+    CK(cudaMemcpyAsync(acc.data(), c->bodies.acc, acc.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (uint32_t b = 0; b < c->nbodies; b++)
+        for (int d = 0; d < 3; d++) {
+            if (force) force[3 * (size_t)b + d] = acc[6 * (size_t)b + d];
+            if (torque) torque[3 * (size_t)b + d] = acc[6 * (size_t)b + 3 + d];
+        }
+    return SPHGB_OK;
+}
+
+int sphgb_clear_boundary_forces(sphgb_ctx *c)
+{
+    if (!c) return SPHGB_ERR_ARGUMENT;
+    if (c->nbodies == 0) return SPHGB_OK;
+    cudaSetDevice(c->cfg.device);
+    CK(cudaMemsetAsync(c->bodies.acc, 0, 6 * (size_t)c->nbodies * sizeof(double), c->stream));
     return SPHGB_OK;
 }
 

@@ -1247,6 +1247,113 @@ __global__ void __launch_bounds__(kBlock) k_integrate(DevParams<T> P, DevBufs<T>
 }
 
 // ==========================================================================
+// forces of the fluid on dynamic boundary bodies
+// ==========================================================================
+// BoundaryModel::addForce (BoundaryModel.h:38-49) collects for each dynamic body the force
+// F = sum f and the torque T = sum (x_b - c) x f over the forces f that the fluid exerts on
+// its boundary particles.  One thread per boundary particle of a dynamic body gathers the
+// forces of its fluid neighbours: it walks the same cell grid and applies the same distance
+// predicate, pair_d2(x_i, x_b) < h^2, as the fluid-to-boundary lists, so its pairs are
+// exactly the pairs of those lists.  Blocks never span two bodies, and the body's last block
+// sums the block partials in block order: the sums are deterministic.
+//   phase 0, before the kick (positions, densities and the divergence solve's kappa_v in
+//   xk.w, v after the divergence solve, the viscosity solution in cg_x):
+//     divergence solve's final pressure term  f = m kappa_v_i V_b gradW_ib
+//         (TimeStepDFSPH.cpp:514 with computePressureAccel :1337-1344),
+//     XSPH boundary term  f = m (c_b / h) (rho0 V_b / rho_i) W_ib v_i   (XSPH.cpp:183-203),
+//     Weiler2018 boundary term  f = -(m / rho_i) d mub (rho0 V_b / rho_i) (v'_i . x_ib) /
+//         (|x_ib|^2 + 0.01 h_s^2) gradW_ib   (Viscosity_Weiler2018.cpp:960-975);
+//   phase 1, after the pressure solve's last iteration (kappa in xk.w):
+//     pressure term  f = m kappa_i V_b gradW_ib   (TimeStepDFSPH.cpp:359).
+// Boundary particles are static (v_b = 0).
+template <class T, int PHASE>
+__global__ void __launch_bounds__(kBlock) k_body_forces(DevParams<T> P, DevBufs<T> B, BodyDev D)
+{
+    count_launch(&B.gsc->launches);
+    const uint4 bk = D.blk[blockIdx.x];
+    const uint32_t body = bk.x;
+    const uint32_t e = bk.y + threadIdx.x;
+    DSum<6> mine;
+#pragma unroll
+    for (int k = 0; k < 6; k++) mine.v[k] = 0.0;
+    if (e < bk.z) {
+        const uint32_t j = D.slot[e];
+        const v4_t<T> xb = ldv(B.xb, j);
+        const uint32_t s = B.bscene ? B.bscene[j] : 0u;
+        const SceneDev<T> S = scene_get(P, s);
+        const StepScalars *sc = B.sc + s;
+        const T Vb = (T)xb.w;
+        const bool press = PHASE == 1 || P.div_on;
+        const bool xs = PHASE == 0 && P.xsph_b != T(0);
+        const bool visc = PHASE == 0 && P.visc_on && P.mub != T(0) && sc->cg_state != 2u;
+        const T xs_c = xs ? P.xsph_b / (T)sc->dt * P.rho0 * Vb : T(0);
+        const T vi_c = P.vd * P.mub * P.rho0 * Vb;
+        const T eps2 = T(0.01) * P.h2;
+        double f[3] = {0.0, 0.0, 0.0};
+        int cx, cy, cz;
+        cell_of(S, xb, cx, cy, cz);
+        for (int dz = -1; dz <= 1; dz++) {
+            const int z = cz + dz;
+            if (z < 0 || z >= S.dimz) continue;
+            for (int dy = -1; dy <= 1; dy++) {
+                const int y = cy + dy;
+                if (y < 0 || y >= S.dimy) continue;
+                for (int dx = -1; dx <= 1; dx++) {
+                    const int x = cx + dx;
+                    if (x < 0 || x >= S.dimx) continue;
+                    const uint32_t c = S.cell_off + local_cell(S, x, y, z);
+                    const uint32_t st = B.cstart[c];
+                    if (st == kEmpty) continue;
+                    const uint32_t en = B.cend[c];
+                    for (uint32_t i = st; i < en; i++) {
+                        const v4_t<T> xk = ldv(B.xk, i);
+                        T rx, ry, rz;
+                        const T d2 = pair_d2(xk, xb, rx, ry, rz);
+                        if (!(d2 < P.K.h2)) continue;
+                        const V3<T> r = mk3<T>(rx, ry, rz);
+                        const T gc = grad_coef_d2(P.K, d2);
+                        V3<T> fi = mk3<T>(0, 0, 0);
+                        if (press) {
+                            const T kap = (T)xk.w;
+                            if (fabs(kap) > P.eps) fi = scl(r, P.mass * kap * Vb * gc);
+                        }
+                        if (xs || visc) {
+                            const T rhoi = B.density[i];
+                            if (xs) {
+                                const T w = P.mass * xs_c / rhoi * kernel_W(P.K, dev_sqrt(d2));
+                                fi = add(fi, scl(xyz<T>(ldv(B.v, i)), w));
+                            }
+                            if (visc) {
+                                const V3<T> nv = xyz<T>(ldv(B.cg_x, i));
+                                const T a = vi_c / rhoi * dot(nv, r) / (d2 + eps2) * gc;
+                                fi = sub(fi, scl(r, P.mass / rhoi * a));
+                            }
+                        }
+                        f[0] += (double)fi.x;
+                        f[1] += (double)fi.y;
+                        f[2] += (double)fi.z;
+                    }
+                }
+            }
+        }
+        const double *cc = D.center + 3 * (size_t)body;
+        const double px = (double)xb.x - cc[0], py = (double)xb.y - cc[1], pz = (double)xb.z - cc[2];
+        mine.v[0] = f[0];
+        mine.v[1] = f[1];
+        mine.v[2] = f[2];
+        mine.v[3] = py * f[2] - pz * f[1];
+        mine.v[4] = pz * f[0] - px * f[2];
+        mine.v[5] = px * f[1] - py * f[0];
+    }
+    const ReduceSlot rs{D.partials, D.counters + body, bk.w, D.body_nblk[body]};
+    double *const acc = D.acc + 6 * (size_t)body;
+    grid_sum_finalize<6>(mine, rs, [&](const DSum<6> &tot) {
+#pragma unroll
+        for (int k = 0; k < 6; k++) acc[k] += tot.v[k];
+    });
+}
+
+// ==========================================================================
 // learned warm start
 // ==========================================================================
 // Network inputs (10, all dimensionless): the raw features f0..f4 of particle i, with f3
@@ -1872,6 +1979,13 @@ void launch_warmstart_select(const DevParams<T> &P, const DevBufs<T> &B, bool di
         k_ws_apply<T, false><<<g, kBlock, 0, s>>>(P, B);
     }
 }
+template <class T>
+void launch_body_forces(const DevParams<T> &P, const DevBufs<T> &B, const BodyDev &D, int phase, cudaStream_t s)
+{
+    if (!D.nblk) return;
+    if (phase == 0) k_body_forces<T, 0><<<D.nblk, kBlock, 0, s>>>(P, B, D);
+    else k_body_forces<T, 1><<<D.nblk, kBlock, 0, s>>>(P, B, D);
+}
 template <class T> void launch_boundary_keys(const DevParams<T> &P, const v4_t<T> *xb_in, const uint32_t *bscene_in,
                                              uint32_t *keys, uint32_t *vals, cudaStream_t s)
 {
@@ -1940,6 +2054,7 @@ void launch_lists_to_ids(const uint32_t *list, const uint32_t *cnt, uint32_t cap
     template void launch_loop_begin<T>(const DevParams<T> &, const DevBufs<T> &, bool, cudaStream_t);               \
     template void launch_step_begin<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                     \
     template void launch_features<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                       \
+    template void launch_body_forces<T>(const DevParams<T> &, const DevBufs<T> &, const BodyDev &, int, cudaStream_t); \
     template void launch_warmstart_select<T>(const DevParams<T> &, const DevBufs<T> &, bool, unsigned,              \
                                              cudaGraphConditionalHandle, bool, cudaStream_t);                       \
     template void launch_xsph<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                           \

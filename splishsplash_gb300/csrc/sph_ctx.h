@@ -144,6 +144,20 @@ template <class T> struct DevBufs {
     uint32_t *hist;
 };
 
+// Dynamic boundary bodies (force feedback of BoundaryModel::addForce): the boundary slots of
+// the dynamic bodies grouped by body, a block table whose blocks never span two bodies, and
+// the per-body accumulators.
+struct BodyDev {
+    const uint32_t *slot;        // [entries] sorted boundary slots, grouped by body, slot order within a body
+    const uint4 *blk;            // [nblk] (body, first entry, end entry, first block of the body)
+    const uint32_t *body_nblk;   // [nbodies] blocks of each body
+    const double *center;        // [3 nbodies] reference points of the torques
+    double *acc;                 // [6 nbodies] force xyz, torque xyz, accumulated until cleared
+    double *partials;            // [6][nblk] block partial sums
+    unsigned *counters;          // [nbodies] last-block counters, zero between launches
+    uint32_t nblk;
+};
+
 // ---- launchers (defined in kernels.cu / sort.cu, instantiated for float and double)
 template <class T> void launch_keys(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
 template <class T> void launch_gather(const DevParams<T> &P, const DevBufs<T> &B, const uint32_t *perm, cudaStream_t s);
@@ -169,6 +183,10 @@ template <class T> void launch_step_begin(const DevParams<T> &P, const DevBufs<T
 template <class T> void launch_loop_begin(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s);
 template <class T> void launch_boundary_volume(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
 template <class T> void launch_features(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
+// forces of the fluid on the dynamic bodies: phase 0 before the kick (divergence, XSPH and
+// viscosity boundary terms), phase 1 after the pressure solve (pressure term)
+template <class T> void launch_body_forces(const DevParams<T> &P, const DevBufs<T> &B, const BodyDev &D, int phase,
+                                           cudaStream_t s);
 // Learned warm start of one solver: both candidates, their first `sweeps` Jacobi iterations,
 // the choice and the loop decision after them (needs 1 <= sweeps <= max_iter of that solver).
 template <class T> void launch_warmstart_select(const DevParams<T> &P, const DevBufs<T> &B, bool div, unsigned sweeps,

@@ -123,6 +123,7 @@ EXPORTS = [
     "sphgb_set_warmstart_mlp", "sphgb_set_feature_output", "sphgb_upload_scenes", "sphgb_num_scenes",
     "sphgb_scene_stats", "sphgb_set_warmstart_gate", "sphgb_set_lanes_per_particle", "sphgb_get_lanes_per_particle",
     "sphgb_export_vtk", "sphgb_export_wait", "sphgb_save_state", "sphgb_load_state",
+    "sphgb_set_boundary_bodies", "sphgb_boundary_forces", "sphgb_clear_boundary_forces",
 ]
 
 _lib = None
@@ -177,6 +178,9 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.sphgb_export_wait.argtypes = [vp]
     L.sphgb_save_state.argtypes = [vp, ctypes.c_char_p]
     L.sphgb_load_state.argtypes = [vp, ctypes.c_char_p]
+    L.sphgb_set_boundary_bodies.argtypes = [vp, vp, u32, vp, vp]
+    L.sphgb_boundary_forces.argtypes = [vp, vp, vp]
+    L.sphgb_clear_boundary_forces.argtypes = [vp]
     L.sphgb_profile_enable.argtypes = [vp, i32]
     L.sphgb_profile_reset.argtypes = [vp]
     L.sphgb_profile_read.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_uint64),
@@ -455,6 +459,37 @@ class Context:
         t = np.zeros(3, np.float32)
         self._check(self.L.sphgb_get_lanes_per_particle(self.h, ctypes.byref(k), _p(t)))
         return int(k.value), [float(v) for v in t]
+
+    def set_boundary_bodies(self, body, center, dynamic=None):
+        """Bodies of the boundary particles (BoundaryModel per rigid body): body[k] is the body of
+        boundary particle k in upload order, center (nbodies x 3) the bodies' reference points
+        for torques, dynamic (nbodies) which bodies collect forces (default all).  The fluid's
+        forces on the dynamic bodies accumulate every step until clear_boundary_forces()."""
+        center = np.ascontiguousarray(center, np.float64).reshape(-1, 3)
+        nb = int(center.shape[0])
+        if nb == 0:
+            self._check(self.L.sphgb_set_boundary_bodies(self.h, None, 0, None, None))
+            self._nbodies = 0
+            return
+        body = np.ascontiguousarray(body, np.uint32)
+        dyn = None if dynamic is None else np.ascontiguousarray(dynamic, np.int32)
+        if dyn is not None and dyn.size != nb:
+            raise ValueError("dynamic needs one flag per body")
+        self._check(self.L.sphgb_set_boundary_bodies(self.h, _p(body), nb, _p(center), _p(dyn)))
+        self._nbodies = nb
+
+    def boundary_forces(self):
+        """(force, torque), each nbodies x 3 float64: BoundaryModel::getForceAndTorque per body."""
+        n = getattr(self, "_nbodies", 0)
+        f = np.zeros((n, 3), np.float64)
+        t = np.zeros((n, 3), np.float64)
+        if n:
+            self._check(self.L.sphgb_boundary_forces(self.h, _p(f), _p(t)))
+        return f, t
+
+    def clear_boundary_forces(self):
+        """BoundaryModel::clearForceAndTorque for every body."""
+        self._check(self.L.sphgb_clear_boundary_forces(self.h))
 
     def export_vtk(self, path: str, fields=(), wait: bool = True):
         """Legacy VTK file of all fluid particles (positions, ids and the named fields), written
