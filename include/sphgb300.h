@@ -309,8 +309,8 @@ int sphgb_set_boundary_bodies(sphgb_ctx *ctx, const uint32_t *body, uint32_t nbo
 /* the sums since the last clear, force[3 nbodies] and torque[3 nbodies] (either may be NULL;
  * zeros for static bodies); waits for the context's stream */
 int sphgb_boundary_forces(sphgb_ctx *ctx, double *force, double *torque);
-/* zero the sums, ordered after the steps already enqueued */
-int sphgb_clear_boundary_forces(sphgb_ctx *ctx);
+/* zero the sums of one body (body < 0: of every body), ordered after the steps already enqueued */
+int sphgb_clear_boundary_forces(sphgb_ctx *ctx, int32_t body);
 
 /* the cudaStream_t every kernel of this context is launched on (for event timing by callers) */
 int sphgb_get_stream(const sphgb_ctx *ctx, void **stream);

@@ -1633,12 +1633,14 @@ int sphgb_boundary_forces(sphgb_ctx *c, double *force, double *torque)
     return SPHGB_OK;
 }
 
-int sphgb_clear_boundary_forces(sphgb_ctx *c)
+int sphgb_clear_boundary_forces(sphgb_ctx *c, int32_t body)
 {
     if (!c) return SPHGB_ERR_ARGUMENT;
+    if (body >= 0 && (uint32_t)body >= c->nbodies) return fail(c, SPHGB_ERR_ARGUMENT, "body index out of range");
     if (c->nbodies == 0) return SPHGB_OK;
     cudaSetDevice(c->cfg.device);
-    CK(cudaMemsetAsync(c->bodies.acc, 0, 6 * (size_t)c->nbodies * sizeof(double), c->stream));
+    if (body < 0) CK(cudaMemsetAsync(c->bodies.acc, 0, 6 * (size_t)c->nbodies * sizeof(double), c->stream));
+    else CK(cudaMemsetAsync(c->bodies.acc + 6 * (size_t)body, 0, 6 * sizeof(double), c->stream));
     return SPHGB_OK;
 }
 

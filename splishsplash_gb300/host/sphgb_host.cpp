@@ -82,11 +82,39 @@ void BoundaryModel_Akinci2012::initModel(unsigned int n, const Vector3r *x)
     m_V.assign(n, Real(0));
 }
 
+void BoundaryModel_Akinci2012::getForceAndTorque(Vector3r &force, Vector3r &torque)
+{
+    force = torque = Vector3r();
+    if (m_owner && m_rigidBody.isDynamic()) m_owner->bodyForceAndTorque(m_index, force, torque);
+}
+
+void BoundaryModel_Akinci2012::clearForceAndTorque()
+{
+    if (m_owner && m_rigidBody.isDynamic()) m_owner->clearBodyForceAndTorque(m_index);
+}
+
 TimeStepDFSPH_GB300::TimeStepDFSPH_GB300(FluidModel &model, BoundaryModel_Akinci2012 &boundary,
                                          const SimulationParameters &sim, Viscosity_Weiler2018_GB300 *viscosity,
                                          int device, bool useGraph)
-    : m_model(model), m_boundary(boundary), m_sim(sim), m_visco(viscosity)
+    : m_model(model), m_boundaries{&boundary}, m_sim(sim), m_visco(viscosity)
 {
+    createContext(device, useGraph);
+}
+
+TimeStepDFSPH_GB300::TimeStepDFSPH_GB300(FluidModel &model, const std::vector<BoundaryModel_Akinci2012 *> &boundaries,
+                                         const SimulationParameters &sim, Viscosity_Weiler2018_GB300 *viscosity,
+                                         int device, bool useGraph)
+    : m_model(model), m_boundaries(boundaries), m_sim(sim), m_visco(viscosity)
+{
+    createContext(device, useGraph);
+}
+
+void TimeStepDFSPH_GB300::createContext(int device, bool useGraph)
+{
+    for (unsigned int k = 0; k < m_boundaries.size(); k++) {
+        if (!m_boundaries[k]) throw Error(SPHGB_ERR_ARGUMENT, "null boundary model");
+        if (m_boundaries[k]->m_owner) throw Error(SPHGB_ERR_STATE, "boundary model already belongs to a time step");
+    }
     sphgb_config cfg{};
     cfg.abi_version = SPHGB_ABI_VERSION;
     cfg.device = device;
@@ -98,11 +126,32 @@ TimeStepDFSPH_GB300::TimeStepDFSPH_GB300(FluidModel &model, BoundaryModel_Akinci
     m_model.m_V = Real(0.8) * d * d * d;
     m_model.m_density0 = m_sim.density0;
     applyParameters();
+    for (unsigned int k = 0; k < m_boundaries.size(); k++) {
+        m_boundaries[k]->m_owner = this;
+        m_boundaries[k]->m_index = k;
+    }
 }
 
 TimeStepDFSPH_GB300::~TimeStepDFSPH_GB300()
 {
+    for (BoundaryModel_Akinci2012 *b : m_boundaries) b->m_owner = nullptr;
     if (m_ctx) sphgb_destroy(m_ctx);
+}
+
+void TimeStepDFSPH_GB300::bodyForceAndTorque(unsigned int body, Vector3r &force, Vector3r &torque)
+{
+    if (!m_bodiesSet) return;
+    std::vector<double> f(3 * m_boundaries.size()), t(3 * m_boundaries.size());
+    check(sphgb_boundary_forces(m_ctx, f.data(), t.data()), "sphgb_boundary_forces");
+    for (int d = 0; d < 3; d++) {
+        force[d] = (Real)f[3 * body + d];
+        torque[d] = (Real)t[3 * body + d];
+    }
+}
+
+void TimeStepDFSPH_GB300::clearBodyForceAndTorque(unsigned int body)
+{
+    if (m_bodiesSet) check(sphgb_clear_boundary_forces(m_ctx, (int32_t)body), "sphgb_clear_boundary_forces");
 }
 
 void TimeStepDFSPH_GB300::check(int rc, const char *what)
@@ -180,8 +229,26 @@ void TimeStepDFSPH_GB300::upload()
     const unsigned int n = m_model.numParticles();
     if (m_factor.size() != n) resize();
     if (m_boundaryDirty) {
-        const std::vector<double> xb = to_double(m_boundary.m_x);
-        check(sphgb_upload_boundary(m_ctx, xb.data(), m_boundary.numberOfParticles()), "sphgb_upload_boundary");
+        // the boundary models' particles in model order; model k is body k
+        std::vector<double> xb, center;
+        std::vector<uint32_t> body;
+        std::vector<int> dynamic;
+        bool anyDynamic = false;
+        for (unsigned int k = 0; k < m_boundaries.size(); k++) {
+            const BoundaryModel_Akinci2012 &bm = *m_boundaries[k];
+            const std::vector<double> x = to_double(bm.m_x);
+            xb.insert(xb.end(), x.begin(), x.end());
+            body.insert(body.end(), bm.numberOfParticles(), k);
+            for (int d = 0; d < 3; d++) center.push_back((double)bm.m_rigidBody.getPosition()[d]);
+            dynamic.push_back(bm.m_rigidBody.isDynamic() ? 1 : 0);
+            anyDynamic = anyDynamic || bm.m_rigidBody.isDynamic();
+        }
+        check(sphgb_upload_boundary(m_ctx, xb.data(), (uint32_t)body.size()), "sphgb_upload_boundary");
+        // bodies only where one collects forces: no extra launches otherwise
+        check(sphgb_set_boundary_bodies(m_ctx, body.data(), anyDynamic ? (uint32_t)m_boundaries.size() : 0u,
+                                        center.data(), dynamic.data()),
+              "sphgb_set_boundary_bodies");
+        m_bodiesSet = anyDynamic;
         m_boundaryDirty = false;
     }
     const std::vector<double> x = to_double(m_model.m_x), v = to_double(m_model.m_v);
@@ -224,8 +291,17 @@ void TimeStepDFSPH_GB300::syncToHost()
     dl(SPHGB_FIELD_PRESSURE_RHO2_V, m_pressureRho2V.data(), "download p_v / rho^2");
     dl(SPHGB_FIELD_PRESSURE_ACCEL, &m_pressureAccel[0][0], "download pressure acceleration");
     if (m_visco) dl(SPHGB_FIELD_VDIFF, &m_visco->m_vDiff[0][0], "download velocity difference");
-    const unsigned int nb = m_boundary.numberOfParticles();
-    if (nb) dl(SPHGB_FIELD_BOUNDARY_VOLUME, m_boundary.m_V.data(), "download boundary volume");
+    // boundary volumes of all models in model order, split per model
+    size_t nb = 0;
+    for (const BoundaryModel_Akinci2012 *bm : m_boundaries) nb += bm->numberOfParticles();
+    if (nb == 0) return;
+    std::vector<Real> vol(nb);
+    dl(SPHGB_FIELD_BOUNDARY_VOLUME, vol.data(), "download boundary volume");
+    size_t off = 0;
+    for (BoundaryModel_Akinci2012 *bm : m_boundaries) {
+        std::copy(vol.begin() + off, vol.begin() + off + bm->numberOfParticles(), bm->m_V.begin());
+        off += bm->numberOfParticles();
+    }
 }
 
 int TimeStepDFSPH_GB300::getParameterId(const std::string &name)

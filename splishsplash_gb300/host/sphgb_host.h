@@ -8,6 +8,7 @@
 //   DFSPH fields               TimeStepDFSPH.cpp:49-53, SimulationDataDFSPH.h:55-120
 //   FluidModel field layout    SPlisHSPlasH/FluidModel.h:113-124, 247-300
 //   Akinci2012 boundary        SPlisHSPlasH/BoundaryModel_Akinci2012.h:32-35
+//   forces on boundary bodies  SPlisHSPlasH/BoundaryModel.h:38-49, 86-87; RigidBodyObject.h
 //   Weiler2018 viscosity       SPlisHSPlasH/Viscosity/Viscosity_Weiler2018.h:44-48, .cpp:33,47-73
 //   time step size             SPlisHSPlasH/TimeManager.h
 // The host vectors are the system of record, as in the reference: step() uploads them when
@@ -89,15 +90,42 @@ private:
     std::string m_id;
 };
 
-// Static boundary sampled with particles; volumes computed on the device (BoundaryModel_Akinci2012.cpp:48-75)
+// The rigid body behind a boundary model, as far as the fluid step needs it
+// (RigidBodyObject.h: getPosition, isDynamic): the reference point of the torques and
+// whether the body collects the fluid's forces.
+struct RigidBodyObject {
+    Vector3r m_position;
+    bool m_isDynamic = false;
+    const Vector3r &getPosition() const { return m_position; }
+    void setPosition(const Vector3r &x) { m_position = x; }
+    bool isDynamic() const { return m_isDynamic; }
+    void setDynamic(bool d) { m_isDynamic = d; }
+};
+
+class TimeStepDFSPH_GB300;
+
+// Static boundary of one body sampled with particles; volumes computed on the device
+// (BoundaryModel_Akinci2012.cpp:48-75).  The forces the fluid exerted on a dynamic body
+// accumulate until clearForceAndTorque (BoundaryModel.h:86-87), as the boundary simulator
+// reads them (Simulator/BoundarySimulator.cpp:8-25).
 class BoundaryModel_Akinci2012 {
 public:
     std::vector<Vector3r> m_x;
     std::vector<Real> m_V;
+    RigidBodyObject m_rigidBody;
     void initModel(unsigned int numBoundaryParticles, const Vector3r *boundaryParticles);
     unsigned int numberOfParticles() const { return (unsigned int)m_x.size(); }
     Vector3r &getPosition(unsigned int i) { return m_x[i]; }
     Real getVolume(unsigned int i) const { return m_V[i]; }
+    RigidBodyObject *getRigidBodyObject() { return &m_rigidBody; }
+    // zero until the model belongs to a time step and its body is dynamic
+    void getForceAndTorque(Vector3r &force, Vector3r &torque);
+    void clearForceAndTorque();
+
+private:
+    friend class TimeStepDFSPH_GB300;
+    TimeStepDFSPH_GB300 *m_owner = nullptr;
+    unsigned int m_index = 0;
 };
 
 // TimeStep.h:13-59
@@ -149,6 +177,10 @@ public:
 
     TimeStepDFSPH_GB300(FluidModel &model, BoundaryModel_Akinci2012 &boundary, const SimulationParameters &sim,
                         Viscosity_Weiler2018_GB300 *viscosity = nullptr, int device = 0, bool useGraph = true);
+    // one boundary model per rigid body (Simulation::numberOfBoundaryModels)
+    TimeStepDFSPH_GB300(FluidModel &model, const std::vector<BoundaryModel_Akinci2012 *> &boundaries,
+                        const SimulationParameters &sim, Viscosity_Weiler2018_GB300 *viscosity = nullptr,
+                        int device = 0, bool useGraph = true);
     ~TimeStepDFSPH_GB300() override;
     TimeStepDFSPH_GB300(const TimeStepDFSPH_GB300 &) = delete;
     TimeStepDFSPH_GB300 &operator=(const TimeStepDFSPH_GB300 &) = delete;
@@ -160,6 +192,8 @@ public:
     void resize() override;
     void emittedParticles(FluidModel *model, const unsigned int startIndex) override;
     void performNeighborhoodSearchSort() override { m_dirty = true; }
+    // the boundary models' particles or rigid bodies changed: upload them before the next step
+    void updateBoundary() { m_boundaryDirty = m_dirty = true; }
     int getNumIterations() override { return (int)m_iterations; }
 
     // ParameterObject-style access by id or by the reference's parameter name
@@ -187,12 +221,17 @@ public:
     sphgb_ctx *context() { return m_ctx; }
 
 protected:
+    friend class BoundaryModel_Akinci2012;
     void check(int rc, const char *what);
     void upload();
     void applyParameters();
+    void createContext(int device, bool useGraph);
+    void bodyForceAndTorque(unsigned int body, Vector3r &force, Vector3r &torque);
+    void clearBodyForceAndTorque(unsigned int body);
 
     FluidModel &m_model;
-    BoundaryModel_Akinci2012 &m_boundary;
+    std::vector<BoundaryModel_Akinci2012 *> m_boundaries;
+    bool m_bodiesSet = false;
     SimulationParameters m_sim;
     Viscosity_Weiler2018_GB300 *m_visco;
     sphgb_ctx *m_ctx = nullptr;

@@ -4,10 +4,14 @@
 //
 //   sphgb_host_demo <scene.bin> <out.bin>
 //
-// scene.bin (little endian): uint32 n, nb, steps, lanes (0 = autotune), viscosity (0/1);
-// float64 particle radius; float64 x[n][3], v[n][3], xb[nb][3].
+// scene.bin (little endian): uint32 n, nb, steps, lanes (0 = autotune), viscosity (0/1),
+// bodies (0/1); float64 particle radius; float64 x[n][3], v[n][3], xb[nb][3]; with bodies:
+// uint32 body[nb] (0: the dynamic body, 1: static walls) and float64 position[3] of the
+// dynamic body.
 // out.bin: per step uint32 iterations, iterationsV, viscoIterations and float64 time;
-// then float64 x[n][3], v[n][3], density[n], p / rho^2 [n], boundary volume[nb].
+// then float64 x[n][3], v[n][3], density[n], p / rho^2 [n], boundary volume[nb] (in the
+// order of the boundary models: body 0's particles first), force[3], torque[3] of body 0
+// summed over all steps (getForceAndTorque; zeros without bodies).
 #include <cstdint>
 #include <cstdio>
 #include <vector>
@@ -38,12 +42,15 @@ int main(int argc, char **argv)
     }
     FILE *f = fopen(argv[1], "rb");
     if (!f) return 2;
-    uint32_t hdr[5];
+    uint32_t hdr[6];
     double radius;
-    if (!rd(f, hdr, 5) || !rd(f, &radius, 1)) return 2;
-    const uint32_t n = hdr[0], nb = hdr[1], steps = hdr[2], lanes = hdr[3], visc = hdr[4];
+    if (!rd(f, hdr, 6) || !rd(f, &radius, 1)) return 2;
+    const uint32_t n = hdr[0], nb = hdr[1], steps = hdr[2], lanes = hdr[3], visc = hdr[4], bodies = hdr[5];
     std::vector<double> x(3 * (size_t)n), v(3 * (size_t)n), xb(3 * (size_t)nb);
     if (!rd(f, x.data(), x.size()) || !rd(f, v.data(), v.size()) || !rd(f, xb.data(), xb.size())) return 2;
+    std::vector<uint32_t> body(nb, 1u);
+    double pos[3] = {0, 0, 0};
+    if (bodies && (!rd(f, body.data(), body.size()) || !rd(f, pos, 3))) return 2;
     fclose(f);
 
     try {
@@ -55,11 +62,20 @@ int main(int argc, char **argv)
         FluidModel model;
         const std::vector<Vector3r> xv = to_vec(x), vv = to_vec(v), xbv = to_vec(xb);
         model.initModel("Fluid", n, xv.data(), vv.data());
-        BoundaryModel_Akinci2012 boundary;
-        boundary.initModel(nb, xbv.data());
+        // one boundary model per body: the dynamic body (body 0) and the static walls
+        std::vector<Vector3r> part[2];
+        for (uint32_t k = 0; k < nb; k++) part[body[k] == 0 ? 0 : 1].push_back(xbv[k]);
+        BoundaryModel_Akinci2012 models[2];
+        std::vector<BoundaryModel_Akinci2012 *> boundaries;
+        for (int b = 0; b < 2; b++) {
+            models[b].initModel((unsigned int)part[b].size(), part[b].data());
+            if (!part[b].empty()) boundaries.push_back(&models[b]);
+        }
+        models[0].getRigidBodyObject()->setPosition(Vector3r((Real)pos[0], (Real)pos[1], (Real)pos[2]));
+        models[0].getRigidBodyObject()->setDynamic(bodies != 0);
         Viscosity_Weiler2018_GB300 viscosity;
         viscosity.m_maxError = Real(1e-3);
-        TimeStepDFSPH_GB300 ts(model, boundary, sp, visc ? &viscosity : nullptr);
+        TimeStepDFSPH_GB300 ts(model, boundaries, sp, visc ? &viscosity : nullptr);
         sphgb_set_lanes_per_particle(ts.context(), lanes);
         ts.resize();
 
@@ -81,7 +97,12 @@ int main(int argc, char **argv)
             for (int c = 0; c < 3; c++) out.push_back(model.getVelocity(i)[c]);
         for (uint32_t i = 0; i < n; i++) out.push_back(model.getDensity(i));
         for (uint32_t i = 0; i < n; i++) out.push_back(ts.getPressureRho2(i));
-        for (uint32_t i = 0; i < nb; i++) out.push_back(boundary.getVolume(i));
+        for (BoundaryModel_Akinci2012 *bm : boundaries)
+            for (uint32_t i = 0; i < bm->numberOfParticles(); i++) out.push_back(bm->getVolume(i));
+        Vector3r force, torque;
+        models[0].getForceAndTorque(force, torque);
+        for (int c = 0; c < 3; c++) out.push_back(force[c]);
+        for (int c = 0; c < 3; c++) out.push_back(torque[c]);
         wr(o, out.data(), out.size());
         fclose(o);
         printf("%s: %u steps, %u fluid + %u boundary particles, time %.6f\n", ts.getMethodName().c_str(), steps, n, nb,

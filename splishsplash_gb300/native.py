@@ -180,7 +180,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.sphgb_load_state.argtypes = [vp, ctypes.c_char_p]
     L.sphgb_set_boundary_bodies.argtypes = [vp, vp, u32, vp, vp]
     L.sphgb_boundary_forces.argtypes = [vp, vp, vp]
-    L.sphgb_clear_boundary_forces.argtypes = [vp]
+    L.sphgb_clear_boundary_forces.argtypes = [vp, i32]
     L.sphgb_profile_enable.argtypes = [vp, i32]
     L.sphgb_profile_reset.argtypes = [vp]
     L.sphgb_profile_read.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_uint64),
@@ -487,9 +487,9 @@ class Context:
             self._check(self.L.sphgb_boundary_forces(self.h, _p(f), _p(t)))
         return f, t
 
-    def clear_boundary_forces(self):
-        """BoundaryModel::clearForceAndTorque for every body."""
-        self._check(self.L.sphgb_clear_boundary_forces(self.h))
+    def clear_boundary_forces(self, body: int = -1):
+        """BoundaryModel::clearForceAndTorque of one body (default: every body)."""
+        self._check(self.L.sphgb_clear_boundary_forces(self.h, int(body)))
 
     def export_vtk(self, path: str, fields=(), wait: bool = True):
         """Legacy VTK file of all fluid particles (positions, ids and the named fields), written

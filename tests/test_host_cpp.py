@@ -2,6 +2,7 @@
 Akinci2012 / Weiler2018 plugin interface over the C ABI.  The driver runs a scene through the
 C++ classes; on the GPU its results must equal the Python mirror's bit for bit (same library,
 same inputs, same lanes per particle)."""
+import dataclasses
 import os
 import struct
 import subprocess
@@ -14,12 +15,15 @@ from splishsplash_gb300 import build, scenes
 from splishsplash_gb300.dfsph import TimeStepDFSPH
 
 
-def _write_scene(path, sc, steps, lanes, visc):
+def _write_scene(path, sc, steps, lanes, visc, body=None, position=None):
     with open(path, "wb") as f:
-        f.write(struct.pack("<5I", sc.n, sc.nb, steps, lanes, 1 if visc else 0))
+        f.write(struct.pack("<6I", sc.n, sc.nb, steps, lanes, 1 if visc else 0, 0 if body is None else 1))
         f.write(struct.pack("<d", sc.params.particleRadius))
         for a in (sc.x, sc.v, sc.xb):
             f.write(np.ascontiguousarray(a, "<f8").tobytes())
+        if body is not None:
+            f.write(np.ascontiguousarray(body, "<u4").tobytes())
+            f.write(np.ascontiguousarray(position, "<f8").tobytes())
 
 
 def _read_out(path, n, nb, steps):
@@ -37,7 +41,9 @@ def _read_out(path, n, nb, steps):
     rho = a[6 * n:7 * n]
     kp = a[7 * n:8 * n]
     vb = a[8 * n:8 * n + nb]
-    return per, x, v, rho, kp, vb
+    force = a[8 * n + nb:8 * n + nb + 3]
+    torque = a[8 * n + nb + 3:8 * n + nb + 6]
+    return per, x, v, rho, kp, vb, force, torque
 
 
 def test_host_layer_is_built_and_fails_cleanly_without_a_device():
@@ -55,8 +61,8 @@ def test_host_layer_is_built_and_fails_cleanly_without_a_device():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("visc", [False, True])
-def test_cpp_host_layer_matches_python_mirror(visc):
+@pytest.mark.parametrize("visc,bodies", [(False, False), (True, False), (True, True)])
+def test_cpp_host_layer_matches_python_mirror(visc, bodies):
     sc = scenes.small_block(counts=(10, 12, 10), box=(0.8, 1.0, 0.8), viscosity=visc,
                             velocity=(0.3, 0.0, -0.2)).as_float32()
     # the C++ layer holds every real parameter in Real (float), like the reference's FP32 build
@@ -68,15 +74,26 @@ def test_cpp_host_layer_matches_python_mirror(visc):
     p.gravitation = tuple(f32(g) for g in p.gravitation)
     p.viscoMaxError = f32(1e-3)
     steps, lanes = 12, 1
+    body = position = None
+    if bodies:
+        # the floor is a dynamic body (boundary model 0), the other walls are static (model 1)
+        body = np.where(sc.xb[:, 1] < 1e-9, 0, 1).astype(np.uint32)
+        position = np.array([0.375, 0.0, 0.4375], np.float64)   # exact in float (the C++ layer holds Real)
     with tempfile.TemporaryDirectory() as d:
-        _write_scene(os.path.join(d, "s.bin"), sc, steps, lanes, visc)
+        _write_scene(os.path.join(d, "s.bin"), sc, steps, lanes, visc, body, position)
         r = subprocess.run([build.HOST_DEMO, os.path.join(d, "s.bin"), os.path.join(d, "o.bin")],
                            capture_output=True, text=True, timeout=300)
         assert r.returncode == 0, r.stderr
         assert r.stdout.startswith("DFSPH:")
-        per, x, v, rho, kp, vb = _read_out(os.path.join(d, "o.bin"), sc.n, sc.nb, steps)
+        per, x, v, rho, kp, vb, force, torque = _read_out(os.path.join(d, "o.bin"), sc.n, sc.nb, steps)
+    if bodies:
+        # the C++ layer uploads the boundary models in order: body 0's particles first
+        order = np.concatenate([np.flatnonzero(body == 0), np.flatnonzero(body != 0)])
+        sc = dataclasses.replace(sc, xb=sc.xb[order])
     ts = TimeStepDFSPH(sc)
     ts.ctx.set_lanes_per_particle(lanes)
+    if bodies:
+        ts.ctx.set_boundary_bodies(np.sort(body), np.stack([position, np.zeros(3)]), [1, 0])
     for k in range(steps):
         st = ts.step()
         assert per[k][0] == (st["iterations"], st["iterations_v"], st["visco_iterations"] if visc else 0)
@@ -88,4 +105,11 @@ def test_cpp_host_layer_matches_python_mirror(visc):
     np.testing.assert_array_equal(rho.astype(np.float32), m.getFieldBuffer("density", np.float32))
     np.testing.assert_array_equal(kp.astype(np.float32), m.getFieldBuffer("p / rho^2", np.float32))
     np.testing.assert_array_equal(vb.astype(np.float32), ts.ctx.download("boundary volume", np.float32))
+    if bodies:
+        f, t = ts.ctx.boundary_forces()
+        assert np.abs(f[0]).max() > 0.1 and np.all(f[1] == 0.0)   # the block reaches the floor
+        np.testing.assert_array_equal(force.astype(np.float32), f[0].astype(np.float32))
+        np.testing.assert_array_equal(torque.astype(np.float32), t[0].astype(np.float32))
+    else:
+        assert np.all(force == 0.0) and np.all(torque == 0.0)
     ts.close()
