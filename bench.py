@@ -282,6 +282,8 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip the learned-warm-start and ensemble lines")
     ap.add_argument("--lanes", type=int, default=0, choices=[0, 1, 2, 4],
                     help="lanes per particle of the neighbour passes (0: the library's autotuner)")
+    ap.add_argument("--staging", type=int, default=0, choices=[0, 1, 2],
+                    help="shared-memory staging of the solver passes: 0 autotuned, 1 off, 2 on")
     ap.add_argument("--learned-steps", type=int, default=300)
     ap.add_argument("--ensemble-steps", type=int, default=60)
     args = ap.parse_args()
@@ -308,6 +310,7 @@ def main():
     scene = scenes.dambreak_1m(nz=args.nz)
     ts = TimeStepDFSPH(scene, precision="fp32", use_graph=not args.host_loops, device=local)
     ts.ctx.set_lanes_per_particle(args.lanes)
+    ts.ctx.set_neighbor_staging(args.staging)
     ext = torch.cuda.ExternalStream(ts.ctx.stream())
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
 
@@ -345,10 +348,12 @@ def main():
         dist.barrier()
     value = world * scene.n * args.steps / t_max
     lanes, trial_ms = ts.ctx.lanes_per_particle()
+    staged, staged_frac, staged_trial_ms = ts.ctx.neighbor_staging()
     if args.only_timed:
         if rank == 0:
             print(json.dumps({"metric": baseline_metric(), "value": value, "unit": UNIT, "steps": args.steps,
                               "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
+                              "lanes_per_particle": lanes, "staged": staged, "staged_block_fraction": staged_frac,
                               "note": "timed steps only"}), flush=True)
         ts.close()
         return
@@ -361,6 +366,7 @@ def main():
     hrho, hk, hkv = pin((n,), torch.float32), pin((n,), torch.float32), pin((n,), torch.float32)
     te = TimeStepDFSPH(scene, precision="fp32", use_graph=not args.host_loops, device=local)
     te.ctx.set_lanes_per_particle(args.lanes)
+    te.ctx.set_neighbor_staging(args.staging)
     for _ in range(args.warmup):
         te.step()
     te.ctx.download("position", out=hx)
@@ -447,7 +453,9 @@ def main():
             "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam break)",
             "config": {**workload_config(scene), "lanes_per_particle": lanes,
-                       "lanes_autotune_trial_ms": dict(zip(("1", "2", "4"), trial_ms)) if args.lanes == 0 else None},
+                       "lanes_autotune_trial_ms": dict(zip(("1", "2", "4"), trial_ms)) if args.lanes == 0 else None,
+                       "staged_solver_passes": staged, "staged_block_fraction": round(staged_frac, 4),
+                       "staged_autotune_trial_ms": staged_trial_ms or None},
             "e2e": e2e, "gpu_launches": launches,
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
             "wall_ms_per_step": 1e3 * wall / args.steps,

@@ -290,6 +290,19 @@ int sphgb_set_lanes_per_particle(sphgb_ctx *ctx, uint32_t lanes);
 /* the lanes in use and the autotuner's trial step times in ms for 1, 2, 4 lanes (zeros when fixed) */
 int sphgb_get_lanes_per_particle(const sphgb_ctx *ctx, uint32_t *lanes, float trial_ms[3]);
 
+/* Neighbourhood staging of the two solver passes (FP32 contexts, one lane per particle): every
+ * block of 256 particles copies the records of the cells around its particles into shared
+ * memory once per pass and walks 16-bit local lists written by the list build in the order of
+ * the fluid lists, so the results are bitwise those of the unstaged passes.  Blocks whose
+ * neighbourhood exceeds 2048 particles read from global memory.  mode 0 (default): the
+ * autotuner times it as a fourth candidate (and a fixed lane count of 1 uses it); 1: off;
+ * 2: on.  No reference counterpart. */
+int sphgb_set_neighbor_staging(sphgb_ctx *ctx, int mode);
+/* whether the passes run staged, the fraction of the last step's blocks that were staged
+ * (waits for the stream) and the autotuner's staged trial step time in ms (0 when not timed);
+ * each pointer may be NULL */
+int sphgb_get_neighbor_staging(sphgb_ctx *ctx, int *active, float *staged_fraction, float *trial_ms);
+
 /* Dynamic boundary bodies: the forces and torques the fluid exerts on them, the device-side
  * counterpart of BoundaryModel::addForce / getForceAndTorque / clearForceAndTorque
  * (SPlisHSPlasH/BoundaryModel.h:38-49, 86-87; read and cleared by the boundary simulator each

@@ -105,7 +105,14 @@ struct sphgb_ctx {
     uint32_t lpp_log2 = 2;
     uint32_t lpp_fixed = 0;            // 0: autotune on the first step after an upload
     bool tuned = false;
-    float tune_ms[3] = {0, 0, 0};      // trial step times of lanes per particle 1, 2, 4
+    float tune_ms[4] = {0, 0, 0, 0};   // trial step times of lanes per particle 1, 2, 4 and of staged passes
+    // neighbourhood staging of the solver passes (FP32, one lane per particle)
+    int stage_mode = 0;                // 0: the autotuner decides, 1: off, 2: on
+    bool staged = false;               // in use
+    uint2 *stage_hdr = nullptr;
+    uint32_t *stage_cell = nullptr;
+    uint16_t *stage_off = nullptr, *ll = nullptr;
+    uint32_t *stage_src = nullptr;
     // particle export: own stream, device and pinned staging, one writer thread
     cudaStream_t export_stream = nullptr;
     cudaEvent_t export_scattered = nullptr, export_copied = nullptr, export_start = nullptr;
@@ -141,13 +148,14 @@ namespace {
 enum KernelId {
     K_STEP_BEGIN, K_KEYS, K_SORT, K_GATHER, K_CELL_RANGES, K_BUILD, K_LOOP_BEGIN, K_PRESSURE_ACCEL, K_JACOBI,
     K_SOLVER_FINALIZE, K_XSPH, K_VISC_SETUP, K_CG_MATVEC, K_CG_UPDATE, K_CG_P, K_KICK, K_PRESS_INIT, K_INTEGRATE,
-    K_FEATURES, K_MLP, K_WS_SELECT, K_BODY_FORCES,
+    K_FEATURES, K_MLP, K_WS_SELECT, K_BODY_FORCES, K_STAGE_TABLE,
     K_COUNT
 };
 const char *kKernelNames[K_COUNT] = {
     "step_begin", "keys", "radix_sort", "gather", "cell_ranges", "build_lists_density_alpha", "loop_begin",
     "pressure_accel", "jacobi_update", "solver_finalize", "xsph_gravity", "visc_setup", "cg_matvec", "cg_update",
     "cg_p", "kick_cfl", "press_init", "integrate", "features", "mlp_infer", "warmstart_select", "body_forces",
+    "stage_table",
 };
 
 // Brackets the launches of one kernel class with events on the context stream
@@ -368,6 +376,7 @@ template <class T> DevParams<T> make_params(const sphgb_ctx *c)
     P.capf = c->cfg.max_fluid_neighbors;
     P.capb = c->cfg.max_boundary_neighbors;
     P.lpp_log2 = c->lpp_log2;
+    P.staged = (c->staged && !c->fp64 && c->lpp_log2 == 0 && c->ll) ? 1 : 0;
     return P;
 }
 
@@ -405,6 +414,11 @@ template <class T> DevBufs<T> make_bufs(const sphgb_ctx *c, int view)
     B.nbn = c->nbc;
     B.lf = c->lf;
     B.lb = c->lb;
+    B.stage_hdr = c->stage_hdr;
+    B.stage_cell = c->stage_cell;
+    B.stage_off = c->stage_off;
+    B.stage_src = c->stage_src;
+    B.ll = c->ll;
     B.key = c->key;
     B.key2 = c->key2;
     B.perm = c->perm;
@@ -687,6 +701,7 @@ template <class T> void enqueue_prologue(sphgb_ctx *c, const DevParams<T> &P, co
         cudaMemsetAsync(c->cstart, 0xff, c->ncell * 4, s);
         launch_cell_ranges<T>(P, B1, s);
     }
+    if (P.staged) { PROF(K_STAGE_TABLE, s); launch_stage_table<T>(P, B1, s); }
     { PROF(K_BUILD, s); launch_build<T>(P, B1, s); }
     if (P.feat_on) { PROF(K_FEATURES, s); launch_features<T>(P, B1, s); }
     if (P.learned) { PROF(K_MLP, s); mlp_infer_device(c->mlp_x, c->np, c->mlp_w, c->mlp_p, c->mlp_y, s); }
@@ -863,6 +878,9 @@ template <class T> int build_graph(sphgb_ctx *c, int parity, cudaGraphExec_t *ou
 // timing one trial step per candidate (1, 2 and 4 lanes, twice each, the faster of the two
 // kept) from the current state.  A step never writes the state set it starts from (it
 // gathers into the other set), so a trial is undone by restoring the step scalars.
+// staged solver passes: FP32 and not switched off
+bool staging_possible(const sphgb_ctx *c) { return !c->fp64 && c->stage_mode != 1 && c->ll != nullptr; }
+
 template <class T> int autotune(sphgb_ctx *c)
 {
     const uint32_t S = c->nscenes();
@@ -878,18 +896,24 @@ template <class T> int autotune(sphgb_ctx *c)
     CK(cudaEventCreate(&e1));
     const bool prof = c->profile;
     c->profile = false;
-    float best[3] = {1e30f, 1e30f, 1e30f};
+    // candidates 0..2: 1, 2, 4 lanes per particle; 3: one lane with staged solver passes
+    float best[4] = {1e30f, 1e30f, 1e30f, 1e30f};
+    bool cand[4] = {c->stage_mode != 2, c->stage_mode != 2, c->stage_mode != 2, staging_possible(c)};
+    if (!cand[3]) cand[0] = cand[1] = cand[2] = true;
     int rc = SPHGB_OK;
     for (int rep = 0; rep < 2 && rc == SPHGB_OK; rep++)
-        for (uint32_t lg = 0; lg <= 2 && rc == SPHGB_OK; lg++) {
+        for (uint32_t k = 0; k < 4 && rc == SPHGB_OK; k++) {
+            if (!cand[k]) continue;
+            const uint32_t lg = k == 3 ? 0u : k;
             c->lpp_log2 = lg;
+            c->staged = k == 3;
             cudaEventRecord(e0, c->stream);
             rc = step_host_loop<T>(c);
             cudaEventRecord(e1, c->stream);
             cudaEventSynchronize(e1);
             float ms = 0.f;
             cudaEventElapsedTime(&ms, e0, e1);
-            best[lg] = std::min(best[lg], ms);
+            best[k] = std::min(best[k], ms);
             if (cudaMemcpy(c->sc, saved.data(), (S + 1) * sizeof(StepScalars), cudaMemcpyHostToDevice) != cudaSuccess)
                 rc = fail(c, SPHGB_ERR_CUDA, "autotune: restoring the step scalars");
         }
@@ -900,12 +924,13 @@ template <class T> int autotune(sphgb_ctx *c)
     if (c->nbodies)
         CK(cudaMemcpy(c->bodies.acc, saved_acc.data(), saved_acc.size() * sizeof(double), cudaMemcpyHostToDevice));
     CK(cudaGetLastError());
-    uint32_t pick = 2;
-    for (uint32_t lg = 0; lg <= 2; lg++) {
-        c->tune_ms[lg] = best[lg];
-        if (best[lg] < best[pick]) pick = lg;
+    uint32_t pick = 0;
+    for (uint32_t k = 0; k < 4; k++) {
+        c->tune_ms[k] = cand[k] ? best[k] : 0.0f;
+        if (cand[k] && (!cand[pick] || best[k] < best[pick])) pick = k;
     }
-    c->lpp_log2 = pick;
+    c->lpp_log2 = pick == 3 ? 0u : pick;
+    c->staged = pick == 3;
     c->tuned = true;
     invalidate_graphs(c);
     return SPHGB_OK;
@@ -919,6 +944,7 @@ template <class T> int do_step(sphgb_ctx *c)
     if (!c->tuned) {
         if (c->lpp_fixed) {
             c->lpp_log2 = c->lpp_fixed == 1 ? 0u : (c->lpp_fixed == 2 ? 1u : 2u);
+            c->staged = c->lpp_log2 == 0 && staging_possible(c);
             c->tuned = true;
             invalidate_graphs(c);
         } else if ((rc = autotune<T>(c))) {
@@ -1090,6 +1116,18 @@ template <class T> int init_scenes(sphgb_ctx *c, const double *x, const double *
     const size_t NW = (N + 31) / 32 * 32;
     if ((rc = dalloc(c, &c->lf, NW * c->cfg.max_fluid_neighbors * 4))) return rc;
     if ((rc = dalloc(c, &c->lb, NW * c->cfg.max_boundary_neighbors * 4))) return rc;
+    c->ll = c->stage_off = nullptr;
+    c->stage_hdr = nullptr;
+    c->stage_cell = nullptr;
+    c->stage_src = nullptr;
+    if (!c->fp64) {
+        const size_t nblk = (N + kBlock - 1) / kBlock;
+        if ((rc = dalloc(c, &c->ll, NW * c->cfg.max_fluid_neighbors * 2))) return rc;
+        if ((rc = dalloc(c, &c->stage_hdr, nblk * sizeof(uint2)))) return rc;
+        if ((rc = dalloc(c, &c->stage_cell, nblk * kStageCells * 4))) return rc;
+        if ((rc = dalloc(c, &c->stage_off, nblk * kStageCells * 2))) return rc;
+        if ((rc = dalloc(c, &c->stage_src, nblk * kStageCap * 4))) return rc;
+    }
     if ((rc = dalloc(c, &c->key, NR * 4))) return rc;
     if ((rc = dalloc(c, &c->key2, NR * 4))) return rc;
     if ((rc = dalloc(c, &c->perm, NR * 4))) return rc;
@@ -1288,6 +1326,7 @@ int sphgb_create(const sphgb_config *cfg, sphgb_ctx **out)
     cudaError_t e = cudaSetDevice(cfg->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->body_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = configure_staged_kernels();
     if (e == cudaSuccess && ensure_scalar_mirror(c, 2) != SPHGB_OK) e = cudaErrorMemoryAllocation;
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -1563,6 +1602,47 @@ int sphgb_set_lanes_per_particle(sphgb_ctx *c, uint32_t lanes)
     c->lpp_fixed = lanes;
     c->tuned = false;
     invalidate_graphs(c);
+    return SPHGB_OK;
+}
+
+int sphgb_set_neighbor_staging(sphgb_ctx *c, int mode)
+{
+    if (!c || mode < 0 || mode > 2) return SPHGB_ERR_ARGUMENT;
+    sphgb_stats st;
+    if (c->step_pending) fill_stats(c, &st);
+    c->stage_mode = mode;
+    c->tuned = false;
+    invalidate_graphs(c);
+    return SPHGB_OK;
+}
+
+int sphgb_get_neighbor_staging(sphgb_ctx *c, int *active, float *staged_fraction, float *trial_ms)
+{
+    if (!c) return SPHGB_ERR_ARGUMENT;
+    const bool on = c->staged && !c->fp64 && c->lpp_log2 == 0 && c->ll;
+    if (active) *active = on ? 1 : 0;
+    if (trial_ms) *trial_ms = c->tune_ms[3];
+    if (staged_fraction) {
+        *staged_fraction = 0.0f;
+        if (on && c->np) {
+            // blocks of the last step's stage tables that hold particles, and how many were staged
+            cudaSetDevice(c->cfg.device);
+            const size_t nblk = (c->np + kBlock - 1) / kBlock;
+            std::vector<uint2> hdr(nblk);
+            CK(cudaStreamSynchronize(c->stream));
+            CK(cudaMemcpy(hdr.data(), c->stage_hdr, nblk * sizeof(uint2), cudaMemcpyDeviceToHost));
+            size_t used = 0, staged = 0;
+            for (uint32_t s = 0; s < c->nscenes(); s++) {
+                const uint32_t b0 = c->scn.empty() ? 0u : c->scn[s].pstart / kBlock;
+                const uint32_t n = c->scn.empty() ? c->n : c->scn[s].n;
+                for (uint32_t b = b0; b < b0 + (n + kBlock - 1) / kBlock && b < nblk; b++) {
+                    used++;
+                    staged += hdr[b].x != 0;
+                }
+            }
+            *staged_fraction = used ? (float)staged / (float)used : 0.0f;
+        }
+    }
     return SPHGB_OK;
 }
 
@@ -2188,6 +2268,7 @@ int sphgb_load_state(sphgb_ctx *c, const char *path)
     }
     if (hdr[3] <= 2) {   // the lanes per particle the saved context ran with
         c->lpp_log2 = hdr[3];
+        c->staged = c->lpp_log2 == 0 && staging_possible(c);
         c->tuned = true;
     }
     c->dt = c->scn[0].dt;

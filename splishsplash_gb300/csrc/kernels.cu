@@ -125,6 +125,11 @@ __device__ __forceinline__ uint32_t *list_ptr(uint32_t *L, uint32_t i, uint32_t 
 {
     return L + (size_t)(i >> 5) * cap * 32u + (i & 31u);
 }
+// local fluid lists (staged passes): the warp-interleaved layout, entry k at + 32 k
+__device__ __forceinline__ const uint16_t *ll_ptr(const uint16_t *L, uint32_t i, uint32_t cap)
+{
+    return L + (size_t)(i >> 5) * cap * 32u + (i & 31u);
+}
 // Fluid lists in the layout of the neighbour passes' lanes per particle (lpp = 1 << lpp_log2):
 // entry k of particle i at (i / G) G cap + 32 (k / lpp) + lpp (i % G) + k % lpp, G = 32 / lpp,
 // so that one step of a warp (G particles x lpp entries) reads 32 consecutive words; lpp = 1
@@ -198,9 +203,10 @@ template <class T> __device__ __forceinline__ V3<T> diff3(const v4_t<T> &a, cons
 }
 
 // Neighbour loop with U independent index loads, then U dependent gathers, then
-// U computations, so that each thread keeps several loads in flight.
-template <int U, uint32_t STRIDE = 32u, class Ld, class Cp>
-__device__ __forceinline__ void nbr_loop(const uint32_t *__restrict__ L, uint32_t cnt, Ld ld, Cp cp)
+// U computations, so that each thread keeps several loads in flight.  Idx: uint32_t for
+// the lists of global slots, uint16_t for the local lists of the staged passes.
+template <int U, uint32_t STRIDE = 32u, class Idx, class Ld, class Cp>
+__device__ __forceinline__ void nbr_loop(const Idx *__restrict__ L, uint32_t cnt, Ld ld, Cp cp)
 {
     uint32_t k = 0;
     for (; k + U <= cnt; k += U) {
@@ -346,6 +352,149 @@ __global__ void __launch_bounds__(kBlock) k_cell_ranges_flat(const uint32_t *__r
     if (k == n - 1 || cellid[k + 1] != c) cend[c] = k + 1;
 }
 
+// ---- neighbourhood staging ----------------------------------------------------
+// Exclusive block scan (kBlock threads) of two counters, with their block totals.
+__device__ __forceinline__ void block_scan2(uint32_t a, uint32_t b, uint32_t &ea, uint32_t &eb, uint32_t &ta,
+                                            uint32_t &tb)
+{
+    __shared__ uint32_t wa[kBlock / 32], wb[kBlock / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t ia = a, ib = b;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t ya = __shfl_up_sync(0xffffffffu, ia, o), yb = __shfl_up_sync(0xffffffffu, ib, o);
+        if (lane >= o) { ia += ya; ib += yb; }
+    }
+    if (lane == 31) { wa[warp] = ia; wb[warp] = ib; }
+    __syncthreads();
+    uint32_t oa = 0, ob = 0;
+    ta = tb = 0;
+#pragma unroll
+    for (int w = 0; w < kBlock / 32; w++) {
+        if (w < warp) { oa += wa[w]; ob += wb[w]; }
+        ta += wa[w];
+        tb += wb[w];
+    }
+    ea = oa + ia - a;
+    eb = ob + ib - b;
+    __syncthreads();
+}
+
+// Stage table of a block of kBlock slots (one lane per particle): the cells of the union of its
+// particles' 27-cell neighbourhoods that hold fluid, in ascending cell index, with the offset of
+// each cell's first particle in the block's staged array.  The union is marked in a bitmap over
+// the block's bounding box of cells dilated by one cell; a block over the limits of kStageCap,
+// kStageCells or kStageBoxCells gets cells = 0 (not staged).
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_stage_table(DevParams<T> P, DevBufs<T> B)
+{
+    count_launch(&B.gsc->launches);
+    const SlotInfo q = slot_info(P);
+    const SceneDev<T> S = scene_get(P, q.s);
+    __shared__ int box[6];
+    __shared__ uint32_t bits[kStageBoxCells / 32];
+    if (threadIdx.x < 3) {
+        box[threadIdx.x] = 0x7fffffff;
+        box[3 + threadIdx.x] = -1;
+    }
+    __syncthreads();
+    int cx = 0, cy = 0, cz = 0;
+    if (q.act) {
+        cell_coords(B.cellid[q.i] - S.cell_off, S.dimx, S.dimy, cx, cy, cz);
+        atomicMin(&box[0], cx);
+        atomicMin(&box[1], cy);
+        atomicMin(&box[2], cz);
+        atomicMax(&box[3], cx);
+        atomicMax(&box[4], cy);
+        atomicMax(&box[5], cz);
+    }
+    __syncthreads();
+    uint32_t vol = 0;
+    int lx = 0, ly = 0, lz = 0, ex = 0, ey = 0;
+    if (box[3] >= 0) {
+        lx = max(box[0] - 1, 0);
+        ly = max(box[1] - 1, 0);
+        lz = max(box[2] - 1, 0);
+        ex = min(box[3] + 1, S.dimx - 1) - lx + 1;
+        ey = min(box[4] + 1, S.dimy - 1) - ly + 1;
+        const int ez = min(box[5] + 1, S.dimz - 1) - lz + 1;
+        vol = (uint32_t)ex * (uint32_t)ey * (uint32_t)ez;
+    }
+    if (vol == 0 || vol > kStageBoxCells) {   // block uniform
+        if (threadIdx.x == 0) B.stage_hdr[blockIdx.x] = make_uint2(0u, 0u);
+        return;
+    }
+    for (uint32_t w = threadIdx.x; w < kStageBoxCells / 32; w += kBlock) bits[w] = 0u;
+    __syncthreads();
+    if (q.act) {
+        for (int dz = -1; dz <= 1; dz++)
+            for (int dy = -1; dy <= 1; dy++)
+                for (int dx = -1; dx <= 1; dx++) {
+                    const int x = cx + dx - lx, y = cy + dy - ly, z = cz + dz - lz;
+                    // outside the dilated box means outside the grid
+                    if (x < 0 || y < 0 || z < 0 || x >= ex || y >= ey || (uint32_t)((z * ey + y) * ex + x) >= vol)
+                        continue;
+                    const uint32_t b = (uint32_t)((z * ey + y) * ex + x);
+                    atomicOr(&bits[b >> 5], 1u << (b & 31u));
+                }
+    }
+    __syncthreads();
+    // each thread takes kStageBoxCells / kBlock consecutive box cells: count, scan, write
+    constexpr uint32_t PER = kStageBoxCells / kBlock;
+    const uint32_t b0 = threadIdx.x * PER;
+    auto cell_at = [&](uint32_t b) {
+        const uint32_t x = b % (uint32_t)ex, t = b / (uint32_t)ex;
+        return S.cell_off + local_cell(S, lx + (int)x, ly + (int)(t % (uint32_t)ey), lz + (int)(t / (uint32_t)ey));
+    };
+    uint32_t nc = 0, nr = 0;
+    for (uint32_t k = 0; k < PER; k++) {
+        const uint32_t b = b0 + k;
+        if (b >= vol) break;
+        if (!((bits[b >> 5] >> (b & 31u)) & 1u)) continue;
+        const uint32_t c = cell_at(b);
+        const uint32_t st = B.cstart[c];
+        if (st == kEmpty) continue;
+        nc++;
+        nr += B.cend[c] - st;
+    }
+    uint32_t pc, pr, tc, tr;
+    block_scan2(nc, nr, pc, pr, tc, tr);
+    if (tc == 0 || tc > kStageCells || tr > kStageCap) {   // block uniform
+        if (threadIdx.x == 0) B.stage_hdr[blockIdx.x] = make_uint2(0u, 0u);
+        return;
+    }
+    uint32_t *cells = B.stage_cell + (size_t)blockIdx.x * kStageCells;
+    uint16_t *offs = B.stage_off + (size_t)blockIdx.x * kStageCells;
+    uint32_t *src = B.stage_src + (size_t)blockIdx.x * kStageCap;
+    for (uint32_t k = 0; k < PER; k++) {
+        const uint32_t b = b0 + k;
+        if (b >= vol) break;
+        if (!((bits[b >> 5] >> (b & 31u)) & 1u)) continue;
+        const uint32_t c = cell_at(b);
+        const uint32_t st = B.cstart[c];
+        if (st == kEmpty) continue;
+        const uint32_t en = B.cend[c];
+        cells[pc] = c;
+        offs[pc] = (uint16_t)pr;
+        for (uint32_t j = st; j < en; j++) src[pr + (j - st)] = j;
+        pc++;
+        pr += en - st;
+    }
+    if (threadIdx.x == 0) B.stage_hdr[blockIdx.x] = make_uint2(tc, tr);
+}
+
+// position of cell c in a block's stage table (ascending cell ids; c is present)
+__device__ __forceinline__ uint32_t stage_find(const uint32_t *cells, uint32_t n, uint32_t c)
+{
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (cells[mid] <= c) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
 // Build the fluid and boundary neighbour lists of particle i and, in the same
 // kernel, compute (TimeStep.cpp:116-169) the density, (TimeStepDFSPH.cpp:1106-1186)
 // the DFSPH factor alpha, (TimeStepDFSPH.cpp:1247-1295) the divergence source and
@@ -355,9 +504,12 @@ __global__ void __launch_bounds__(kBlock) k_cell_ranges_flat(const uint32_t *__r
 // accepted indices to the lists (cells whose box is farther than h are skipped).
 // Phase 2 walks the fresh lists densely for the kernel sums, so the kernel math
 // does not run inside the divergent candidate loop.
+// With the block's stage table (tn cells, in shared memory) phase 1 also writes the local
+// list: the same entries as the fluid list, as indices into the block's staged array.
 template <class T>
 __device__ __forceinline__ void build_one(const DevParams<T> &P, const DevBufs<T> &B, const SceneDev<T> &S,
-                                          StepScalars *sc, uint32_t i, uint32_t &nf_out, uint32_t &nb_out)
+                                          StepScalars *sc, uint32_t i, uint32_t &nf_out, uint32_t &nb_out,
+                                          const uint32_t *tcell, const uint16_t *toff, uint32_t tn)
 {
     const v4_t<T> xi = ldv(B.x, i);
     int cx, cy, cz;
@@ -380,6 +532,7 @@ __device__ __forceinline__ void build_one(const DevParams<T> &P, const DevBufs<T
 
     uint32_t *Lf = B.lf + fl_index(i, 0, P.capf, P.lpp_log2);   // entry k at fl_index(i, k, ...)
     uint32_t *Lb = list_ptr(B.lb, i, P.capb);
+    uint16_t *Ll = tn ? B.ll + (size_t)(i >> 5) * P.capf * 32u + (i & 31u) : nullptr;   // one lane per particle
     const uint32_t lpp = 1u << P.lpp_log2;
     uint32_t nf = 0, nb = 0;
     for (int dz = -1; dz <= 1; dz++) {
@@ -402,10 +555,26 @@ __device__ __forceinline__ void build_one(const DevParams<T> &P, const DevBufs<T
                 uint32_t s = B.cstart[c];
                 if (s != kEmpty) {
                     const uint32_t e = B.cend[c];
+                    // staged index of slot j: lbase + j.  The stage table holds every fluid cell
+                    // this loop visits; should a cell be missing, the block falls back to the
+                    // unstaged passes (its stage header is cleared) and no local index is used.
+                    uint32_t lbase = 0u;
+                    if (Ll) {
+                        const uint32_t pos = stage_find(tcell, tn, c);
+                        if (tcell[pos] == c) {
+                            lbase = (uint32_t)toff[pos] - s;
+                        } else {
+                            B.stage_hdr[blockIdx.x] = make_uint2(0u, 0u);
+                            Ll = nullptr;
+                        }
+                    }
                     for (uint32_t j = s; j < e; j++) {
                         T ddx, ddy, ddz;
                         if (j != i && pair_d2(xi, ldv(B.x, j), ddx, ddy, ddz) < P.K.h2) {
-                            if (nf < P.capf) Lf[32u * (nf >> P.lpp_log2) + (nf & (lpp - 1u))] = j;
+                            if (nf < P.capf) {
+                                Lf[32u * (nf >> P.lpp_log2) + (nf & (lpp - 1u))] = j;
+                                if (Ll) Ll[32u * nf] = (uint16_t)(lbase + j);
+                            }
                             nf++;
                         }
                     }
@@ -510,8 +679,19 @@ __global__ void __launch_bounds__(kBlock) k_build(DevParams<T> P, DevBufs<T> B)
     count_launch(&B.gsc->launches);
     const SlotInfo q = slot_info(P);
     StepScalars *const sc = B.sc + q.s;
+    __shared__ uint32_t tcell[kStageCells];
+    __shared__ uint16_t toff[kStageCells];
+    uint32_t tn = 0;
+    if (P.staged) {   // block uniform
+        tn = B.stage_hdr[blockIdx.x].x;
+        for (uint32_t k = threadIdx.x; k < tn; k += kBlock) {
+            tcell[k] = B.stage_cell[(size_t)blockIdx.x * kStageCells + k];
+            toff[k] = B.stage_off[(size_t)blockIdx.x * kStageCells + k];
+        }
+        __syncthreads();
+    }
     uint32_t nf = 0, nb = 0;
-    if (q.act) build_one(P, B, scene_get(P, q.s), sc, q.i, nf, nb);
+    if (q.act) build_one(P, B, scene_get(P, q.s), sc, q.i, nf, nb, tcell, toff, tn);
     block_max_atomic(nf, nb, &sc->max_nf, &sc->max_nb);
 }
 
@@ -525,8 +705,11 @@ __global__ void __launch_bounds__(kBlock) k_build(DevParams<T> P, DevBufs<T> B)
 // a_i = -V sum_j [|k_i + k_j| > eps] (k_i + k_j) gradW_ij - [|k_i| > eps] k_i sum_b V_b gradW_ib
 // with kappa of the running solver read from xk.w and the boundary sum from bg.
 // Every lane of the particle returns the full acceleration.
+// Staged (sx != null, one lane per particle): the neighbours' xk records come from the block's
+// shared copy through the local list, in the order of the fluid list, so the sums are the same.
 template <int LPP, class T>
-__device__ __forceinline__ V3<T> pressure_accel_g(const DevParams<T> &P, const DevBufs<T> &B, const SlotInfo &q)
+__device__ __forceinline__ V3<T> pressure_accel_g(const DevParams<T> &P, const DevBufs<T> &B, const SlotInfo &q,
+                                                  const v4_t<T> *sx = nullptr)
 {
     V3<T> acc = mk3<T>(0, 0, 0);
     T pi = T(0);
@@ -534,20 +717,56 @@ __device__ __forceinline__ V3<T> pressure_accel_g(const DevParams<T> &P, const D
     if (q.act) {
         xi = ldv(B.xk, q.i);
         pi = (T)xi.w;
-        fluid_loop<LPP, kUnroll>(P, B, q.i, q.l, [&](uint32_t j) { return ldv(B.xk, j); },
-                                 [&](uint32_t, const v4_t<T> &xj) {
-                                     const T psum = pi + (T)xj.w;
-                                     if (fabs(psum) > P.eps) {
-                                         const V3<T> r = diff3<T>(xi, xj);
-                                         const T c = grad_coef_d2(P.K, dot(r, r)) * psum;
-                                         acc = add(acc, scl(r, c));
-                                     }
-                                 });
+        auto cp = [&](uint32_t, const v4_t<T> &xj) {
+            const T psum = pi + (T)xj.w;
+            if (fabs(psum) > P.eps) {
+                const V3<T> r = diff3<T>(xi, xj);
+                const T c = grad_coef_d2(P.K, dot(r, r)) * psum;
+                acc = add(acc, scl(r, c));
+            }
+        };
+        if (LPP == 1 && sx)
+            nbr_loop<kUnroll>(ll_ptr(B.ll, q.i, P.capf), min(B.nf[q.i], P.capf), [&](uint32_t m) { return sx[m]; }, cp);
+        else
+            fluid_loop<LPP, kUnroll>(P, B, q.i, q.l, [&](uint32_t j) { return ldv(B.xk, j); }, cp);
     }
     acc = gsum3<LPP>(acc);
     V3<T> ai = scl(acc, -P.V);
     if (q.act && fabs(pi) > P.eps) ai = sub(ai, scl(xyz<T>(ldv(B.bg, q.i)), pi));
     return ai;
+}
+
+// resident blocks per SM the FP32 one-lane pressure-acceleration pass is compiled for (a register
+// cap of 42): measured 11 % faster at 1M particles than the unconstrained 43-44 registers (5
+// blocks); tighter caps spill
+template <class T, int LPP> constexpr int kPressureMinBlocks = (sizeof(T) == 4 && LPP == 1) ? 6 : 1;
+
+// Copy the block's staged records to shared memory: rec = load(slot) for every slot of the
+// block's staged list, then store(local index, rec); CH loads in flight per thread.  Returns
+// false, without copying, for a block that is not staged or has more than cap records.  Every
+// thread of the block calls it (it synchronises the block).
+template <class Ld, class St>
+__device__ __forceinline__ bool stage_in(const DevBufs<float> &B, uint32_t cap, Ld load, St store)
+{
+    const uint2 hdr = B.stage_hdr[blockIdx.x];
+    if (hdr.x == 0 || hdr.y > cap) return false;   // block uniform
+    const uint32_t *src = B.stage_src + (size_t)blockIdx.x * kStageCap;
+    constexpr uint32_t CH = 4;
+#pragma unroll 1
+    for (uint32_t base = threadIdx.x; base < hdr.y; base += CH * kBlock) {
+        uint32_t slot[CH];
+#pragma unroll
+        for (uint32_t r = 0; r < CH; r++) slot[r] = base + r * kBlock < hdr.y ? src[base + r * kBlock] : 0u;
+        decltype(load(0u)) rec[CH];
+#pragma unroll
+        for (uint32_t r = 0; r < CH; r++)
+            if (base + r * kBlock < hdr.y) rec[r] = load(slot[r]);
+#pragma unroll
+        for (uint32_t r = 0; r < CH; r++)
+            if (base + r * kBlock < hdr.y) store(base + r * kBlock, rec[r]);
+    }
+    __syncthreads();
+    return true;
 }
 
 // Termination guard of a device-side loop: the first kernel of every loop body
@@ -591,14 +810,25 @@ __device__ __forceinline__ F8 ld_f8(const float4 *p)
 // Pressure accelerations of the running solver.  FP32: also the (x_i, a_i) record that the
 // Jacobi pass gathers with one 256-bit load per neighbour.
 template <class T, int LPP>
-__global__ void __launch_bounds__(kBlock) k_pressure_accel(DevParams<T> P, DevBufs<T> B, unsigned limit,
+__global__ void __launch_bounds__(kBlock, kPressureMinBlocks<T, LPP>) k_pressure_accel(DevParams<T> P, DevBufs<T> B,
+                                                                                      unsigned limit,
                                                             cudaGraphConditionalHandle h, int use_handle)
 {
     count_launch(&B.gsc->launches);
     loop_guard(B.gsc, limit, h, use_handle);
     const SlotInfo q = slot_info<LPP>(P);
-    if (!scene_live(P, B.sc + q.s)) return;
-    const V3<T> a = pressure_accel_g<LPP>(P, B, q);
+    if (!scene_live(P, B.sc + q.s)) return;   // block uniform
+    V3<T> a;
+    if constexpr (LPP == 1 && sizeof(T) == 4) {
+        extern __shared__ float4 stage_f4[];   // kStageCap records when staged
+        if (P.staged && stage_in(B, kStageCap, [&](uint32_t j) { return ldv(B.xk, j); },
+                                 [&](uint32_t m, const float4 &r) { stage_f4[m] = r; }))
+            a = pressure_accel_g<LPP>(P, B, q, stage_f4);
+        else
+            a = pressure_accel_g<LPP>(P, B, q);
+    } else {
+        a = pressure_accel_g<LPP>(P, B, q);
+    }
     if (!q.act || q.l != 0) return;
     if constexpr (sizeof(T) == 4) {
         B.xa[2 * (size_t)q.i] = ldv(B.x, q.i);
@@ -610,9 +840,13 @@ __global__ void __launch_bounds__(kBlock) k_pressure_accel(DevParams<T> P, DevBu
 
 // compute_aij_pj, scalar path (TimeStepDFSPH.cpp:1370-1420):
 // V sum_j (a_i - a_j).gradW_ij + a_i . sum_b V_b gradW_ib, on every lane of the particle.
-// FP32: x_j and a_j from the packed record, one 256-bit load per neighbour.
+// FP32: x_j and a_j from the packed record, one 256-bit load per neighbour; staged (s0 != null,
+// one lane per particle): from the block's shared copy, three float2 arrays (x, y), (z, a_x),
+// (a_y, a_z), through the local list.
 template <int LPP>
-__device__ __forceinline__ float aij_pj_g(const DevParams<float> &P, const DevBufs<float> &B, const SlotInfo &q)
+__device__ __forceinline__ float aij_pj_g(const DevParams<float> &P, const DevBufs<float> &B, const SlotInfo &q,
+                                          const float2 *s0 = nullptr, const float2 *s1 = nullptr,
+                                          const float2 *s2 = nullptr)
 {
     float accf = 0.0f;
     V3<float> ai = mk3<float>(0, 0, 0);
@@ -620,12 +854,23 @@ __device__ __forceinline__ float aij_pj_g(const DevParams<float> &P, const DevBu
         const F8 me = ld_f8(B.xa + 2 * (size_t)q.i);
         const float4 xi = me.a;
         ai = xyz<float>(me.b);
-        fluid_loop<LPP, kUnroll>(P, B, q.i, q.l, [&](uint32_t j) { return ld_f8(B.xa + 2 * (size_t)j); },
-                                 [&](uint32_t, const F8 &d) {
-                                     const V3<float> r = diff3<float>(xi, d.a);
-                                     const float c = grad_coef_d2(P.K, dot(r, r));
-                                     accf += c * dot(sub(ai, xyz<float>(d.b)), r);
-                                 });
+        auto cp = [&](uint32_t, const F8 &d) {
+            const V3<float> r = diff3<float>(xi, d.a);
+            const float c = grad_coef_d2(P.K, dot(r, r));
+            accf += c * dot(sub(ai, xyz<float>(d.b)), r);
+        };
+        if (LPP == 1 && s0)
+            nbr_loop<kUnroll>(ll_ptr(B.ll, q.i, P.capf), min(B.nf[q.i], P.capf),
+                              [&](uint32_t m) {
+                                  const float2 u = s0[m], v = s1[m], w = s2[m];
+                                  F8 r;
+                                  r.a = make_float4(u.x, u.y, v.x, 0.0f);
+                                  r.b = make_float4(v.y, w.x, w.y, 0.0f);
+                                  return r;
+                              },
+                              cp);
+        else
+            fluid_loop<LPP, kUnroll>(P, B, q.i, q.l, [&](uint32_t j) { return ld_f8(B.xa + 2 * (size_t)j); }, cp);
     }
     accf = gsum<LPP>(accf);
     return q.act ? accf * P.V + dot(ai, xyz<float>(ldv(B.bg, q.i))) : 0.0f;
@@ -689,8 +934,23 @@ __global__ void __launch_bounds__(kBlock) k_jacobi(DevParams<T> P, DevBufs<T> B,
     StepScalars *const sc = B.sc + q.s;
     const bool live = scene_live(P, sc);
     double err = 0.0;
-    if (live) {
-        T apj = aij_pj_g<LPP>(P, B, q);
+    if (live) {   // block uniform
+        T apj;
+        if constexpr (LPP == 1 && sizeof(T) == 4) {
+            extern __shared__ float2 stage_f2[];   // 3 x kStageCapJacobi when staged
+            float2 *s0 = stage_f2, *s1 = stage_f2 + kStageCapJacobi, *s2 = stage_f2 + 2 * kStageCapJacobi;
+            if (P.staged && stage_in(B, kStageCapJacobi, [&](uint32_t j) { return ld_f8(B.xa + 2 * (size_t)j); },
+                                     [&](uint32_t m, const F8 &r) {
+                                         s0[m] = make_float2(r.a.x, r.a.y);
+                                         s1[m] = make_float2(r.a.z, r.b.x);
+                                         s2[m] = make_float2(r.b.y, r.b.z);
+                                     }))
+                apj = aij_pj_g<LPP>(P, B, q, s0, s1, s2);
+            else
+                apj = aij_pj_g<LPP>(P, B, q);
+        } else {
+            apj = aij_pj_g<LPP>(P, B, q);
+        }
         if (q.act && q.l == 0) {
             const uint32_t i = q.i;
             const double hd = DIV ? sc->dt : sc->dt_next;
@@ -1863,6 +2123,14 @@ inline unsigned grid_lpp(uint32_t n, int lpp) { return (n + kBlock / lpp - 1) / 
         }                                                                                                          \
     } while (0)
 
+// dynamic shared memory of the staged solver passes (FP32, one lane per particle)
+constexpr size_t kStageBytesPressure = kStageCap * sizeof(float4);
+constexpr size_t kStageBytesJacobi = 3 * kStageCapJacobi * sizeof(float2);
+template <class T> size_t stage_bytes(const DevParams<T> &P, int lpp, size_t bytes)
+{
+    return (sizeof(T) == 4 && lpp == 1 && P.staged) ? bytes : 0;
+}
+
 template <class T> void launch_keys(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {
     if (P.np) k_keys<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
@@ -1875,6 +2143,10 @@ template <class T> void launch_cell_ranges(const DevParams<T> &P, const DevBufs<
 {
     if (P.np) k_cell_ranges<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
 }
+template <class T> void launch_stage_table(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
+{
+    if (P.np && P.staged) k_stage_table<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
+}
 template <class T> void launch_build(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {
     if (P.np) k_build<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
@@ -1884,7 +2156,8 @@ template <class T> void launch_pressure_accel(const DevParams<T> &P, const DevBu
 {
     const unsigned limit = (div ? P.max_iter_v : P.max_iter) + 1;
     if (P.np)
-        LPP_DISPATCH(P, (k_pressure_accel<T, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B, limit, h, use_handle ? 1 : 0)));
+        LPP_DISPATCH(P, (k_pressure_accel<T, L><<<grid_lpp(P.np, L), kBlock, stage_bytes(P, L, kStageBytesPressure), s>>>(
+                            P, B, limit, h, use_handle ? 1 : 0)));
 }
 template <class T>
 void launch_jacobi(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaGraphConditionalHandle h, bool use_handle,
@@ -1892,8 +2165,12 @@ void launch_jacobi(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaGra
 {
     if (!P.np) return;
     const int uh = use_handle ? 1 : 0;
-    if (div) LPP_DISPATCH(P, (k_jacobi<T, true, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B, h, uh)));
-    else LPP_DISPATCH(P, (k_jacobi<T, false, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B, h, uh)));
+    if (div)
+        LPP_DISPATCH(P, (k_jacobi<T, true, L><<<grid_lpp(P.np, L), kBlock, stage_bytes(P, L, kStageBytesJacobi), s>>>(
+                            P, B, h, uh)));
+    else
+        LPP_DISPATCH(P, (k_jacobi<T, false, L><<<grid_lpp(P.np, L), kBlock, stage_bytes(P, L, kStageBytesJacobi), s>>>(
+                            P, B, h, uh)));
 }
 template <class T> void launch_solver_finalize(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s)
 {
@@ -2046,6 +2323,7 @@ void launch_lists_to_ids(const uint32_t *list, const uint32_t *cnt, uint32_t cap
     template void launch_gather<T>(const DevParams<T> &, const DevBufs<T> &, const uint32_t *, cudaStream_t);       \
     template void launch_cell_ranges<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                    \
     template void launch_build<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                          \
+    template void launch_stage_table<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                    \
     template void launch_pressure_accel<T>(const DevParams<T> &, const DevBufs<T> &, bool, cudaStream_t,            \
                                            cudaGraphConditionalHandle, bool);                                       \
     template void launch_jacobi<T>(const DevParams<T> &, const DevBufs<T> &, bool, cudaGraphConditionalHandle, bool, \
@@ -2082,5 +2360,18 @@ void launch_lists_to_ids(const uint32_t *list, const uint32_t *cnt, uint32_t cap
 
 SPHGB_INSTANTIATE(float)
 SPHGB_INSTANTIATE(double)
+
+cudaError_t configure_staged_kernels()
+{
+    cudaError_t e = cudaFuncSetAttribute(k_jacobi<float, true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kStageBytesJacobi);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_jacobi<float, false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kStageBytesJacobi);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_pressure_accel<float, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kStageBytesPressure);
+    return e;
+}
 
 }  // namespace sphgb

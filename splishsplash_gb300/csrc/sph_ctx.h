@@ -86,7 +86,20 @@ template <class T> struct DevParams {
     uint32_t capf, capb;
     uint32_t lpp_log2;            // lanes per particle of the neighbour passes (1, 2 or 4) = 1 << lpp_log2;
                                   // also fixes the layout of the fluid lists
+    int staged;                   // FP32, one lane per particle: the solver passes read their block's
+                                  // neighbourhood from shared memory (stage tables, local lists)
 };
+
+// Neighbourhood staging of the solver passes.  For every block of kBlock slots the step's
+// stage table lists the cells of the union of its particles' 27-cell neighbourhoods (ascending
+// cell index) with the offset of each cell's first particle in the block's staged array; the
+// local fluid lists hold, per neighbour, its index in that array.  A block whose neighbourhood
+// has more than kStageCells cells, more than kStageCap particles or a bounding box of more than
+// kStageBoxCells cells is not staged and reads its neighbours from global memory.
+constexpr uint32_t kStageCap = 2048;        // staged particles per block (16-bit local indices)
+constexpr uint32_t kStageCapJacobi = 1536;  // ... that the Jacobi pass stages (24 B each; 6 blocks per SM)
+constexpr uint32_t kStageCells = 384;       // staged cells per block
+constexpr uint32_t kStageBoxCells = 4096;   // cells of the block's dilated bounding box (bitmap)
 
 // Scene descriptor by value: a kernel parameter for a single scene, a (cached) global load otherwise.
 template <class T> __device__ __forceinline__ SceneDev<T> scene_get(const DevParams<T> &P, uint32_t s)
@@ -116,6 +129,14 @@ template <class T> struct DevBufs {
     T *density, *factor, *dadv;
     uint32_t *nf, *nbn;
     uint32_t *lf, *lb;
+    // neighbourhood staging (staged mode): per block (cells, particles) with cells = 0 for a block
+    // that is not staged, the cell ids and offsets, and the local fluid lists (warp-interleaved,
+    // the layout of lf with one lane per particle)
+    uint2 *stage_hdr;
+    uint32_t *stage_cell;
+    uint16_t *stage_off;
+    uint32_t *stage_src;         // [blocks][kStageCap] slot of every staged particle
+    uint16_t *ll;
     // cell grid
     uint32_t *key, *key2, *perm, *perm2, *cellid, *cellid2;
     uint32_t *cstart, *cend;
@@ -163,6 +184,10 @@ template <class T> void launch_keys(const DevParams<T> &P, const DevBufs<T> &B, 
 template <class T> void launch_gather(const DevParams<T> &P, const DevBufs<T> &B, const uint32_t *perm, cudaStream_t s);
 template <class T> void launch_cell_ranges(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
 template <class T> void launch_build(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
+// stage tables of the step (staged mode; after the cell ranges, before the list build)
+template <class T> void launch_stage_table(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
+// shared-memory limits of the staged solver passes; call once per device before their first launch
+cudaError_t configure_staged_kernels();
 template <class T> void launch_pressure_accel(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s,
                                               cudaGraphConditionalHandle h = 0, bool use_handle = false);
 template <class T> void launch_jacobi(const DevParams<T> &P, const DevBufs<T> &B, bool div,

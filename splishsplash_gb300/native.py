@@ -124,6 +124,7 @@ EXPORTS = [
     "sphgb_scene_stats", "sphgb_set_warmstart_gate", "sphgb_set_lanes_per_particle", "sphgb_get_lanes_per_particle",
     "sphgb_export_vtk", "sphgb_export_wait", "sphgb_save_state", "sphgb_load_state",
     "sphgb_set_boundary_bodies", "sphgb_boundary_forces", "sphgb_clear_boundary_forces",
+    "sphgb_set_neighbor_staging", "sphgb_get_neighbor_staging",
 ]
 
 _lib = None
@@ -181,6 +182,9 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.sphgb_set_boundary_bodies.argtypes = [vp, vp, u32, vp, vp]
     L.sphgb_boundary_forces.argtypes = [vp, vp, vp]
     L.sphgb_clear_boundary_forces.argtypes = [vp, i32]
+    L.sphgb_set_neighbor_staging.argtypes = [vp, i32]
+    L.sphgb_get_neighbor_staging.argtypes = [vp, ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_float),
+                                             ctypes.POINTER(ctypes.c_float)]
     L.sphgb_profile_enable.argtypes = [vp, i32]
     L.sphgb_profile_reset.argtypes = [vp]
     L.sphgb_profile_read.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_uint64),
@@ -490,6 +494,18 @@ class Context:
     def clear_boundary_forces(self, body: int = -1):
         """BoundaryModel::clearForceAndTorque of one body (default: every body)."""
         self._check(self.L.sphgb_clear_boundary_forces(self.h, int(body)))
+
+    def set_neighbor_staging(self, mode: int = 0):
+        """Shared-memory staging of the solver passes: 0 autotuned (default), 1 off, 2 on."""
+        self._check(self.L.sphgb_set_neighbor_staging(self.h, int(mode)))
+
+    def neighbor_staging(self):
+        """(in use, fraction of the last step's blocks staged, autotuner trial step ms)."""
+        a = ctypes.c_int()
+        f = ctypes.c_float()
+        t = ctypes.c_float()
+        self._check(self.L.sphgb_get_neighbor_staging(self.h, ctypes.byref(a), ctypes.byref(f), ctypes.byref(t)))
+        return bool(a.value), float(f.value), float(t.value)
 
     def export_vtk(self, path: str, fields=(), wait: bool = True):
         """Legacy VTK file of all fluid particles (positions, ids and the named fields), written
