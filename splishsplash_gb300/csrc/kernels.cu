@@ -31,6 +31,7 @@ inline unsigned grid_for(uint32_t n) { return (n + kBlock - 1) / kBlock; }
 // interleaved parts of its fluid list and combine their partial sums with warp
 // shuffles.  A block never spans two scenes (scenes start at multiples of kBlock).
 struct SlotInfo {
+    uint32_t b;            // block (units of kBlock / LPP slots)
     uint32_t s;            // scene
     uint32_t i;            // slot
     uint32_t l;            // lane of the particle (0 .. LPP-1)
@@ -42,10 +43,11 @@ template <int LPP = 1, class T> __device__ __forceinline__ SlotInfo slot_info(co
 {
     constexpr uint32_t SPB = kBlock / LPP;
     SlotInfo q;
-    q.i = blockIdx.x * SPB + threadIdx.x / LPP;
+    q.b = blockIdx.x;
+    q.i = q.b * SPB + threadIdx.x / LPP;
     q.l = threadIdx.x % LPP;
     if (P.nscenes > 1) {
-        const uint4 b = __ldg(P.blk + blockIdx.x / LPP);
+        const uint4 b = __ldg(P.blk + q.b / LPP);
         q.s = b.x;
         q.begin = b.y;
         q.end = b.z;
@@ -421,7 +423,7 @@ __global__ void __launch_bounds__(kBlock) k_stage_table(DevParams<T> P, DevBufs<
         vol = (uint32_t)ex * (uint32_t)ey * (uint32_t)ez;
     }
     if (vol == 0 || vol > kStageBoxCells) {   // block uniform
-        if (threadIdx.x == 0) B.stage_hdr[blockIdx.x] = make_uint2(0u, 0u);
+        if (threadIdx.x == 0) B.stage_hdr[q.b] = make_uint2(0u, 0u);
         return;
     }
     for (uint32_t w = threadIdx.x; w < kStageBoxCells / 32; w += kBlock) bits[w] = 0u;
@@ -460,12 +462,12 @@ __global__ void __launch_bounds__(kBlock) k_stage_table(DevParams<T> P, DevBufs<
     uint32_t pc, pr, tc, tr;
     block_scan2(nc, nr, pc, pr, tc, tr);
     if (tc == 0 || tc > kStageCells || tr > kStageCap) {   // block uniform
-        if (threadIdx.x == 0) B.stage_hdr[blockIdx.x] = make_uint2(0u, 0u);
+        if (threadIdx.x == 0) B.stage_hdr[q.b] = make_uint2(0u, 0u);
         return;
     }
-    uint32_t *cells = B.stage_cell + (size_t)blockIdx.x * kStageCells;
-    uint16_t *offs = B.stage_off + (size_t)blockIdx.x * kStageCells;
-    uint32_t *src = B.stage_src + (size_t)blockIdx.x * kStageCap;
+    uint32_t *cells = B.stage_cell + (size_t)q.b * kStageCells;
+    uint16_t *offs = B.stage_off + (size_t)q.b * kStageCells;
+    uint32_t *src = B.stage_src + (size_t)q.b * kStageCap;
     for (uint32_t k = 0; k < PER; k++) {
         const uint32_t b = b0 + k;
         if (b >= vol) break;
@@ -480,7 +482,7 @@ __global__ void __launch_bounds__(kBlock) k_stage_table(DevParams<T> P, DevBufs<
         pc++;
         pr += en - st;
     }
-    if (threadIdx.x == 0) B.stage_hdr[blockIdx.x] = make_uint2(tc, tr);
+    if (threadIdx.x == 0) B.stage_hdr[q.b] = make_uint2(tc, tr);
 }
 
 // position of cell c in a block's stage table (ascending cell ids; c is present)
@@ -564,7 +566,7 @@ __device__ __forceinline__ void build_one(const DevParams<T> &P, const DevBufs<T
                         if (tcell[pos] == c) {
                             lbase = (uint32_t)toff[pos] - s;
                         } else {
-                            B.stage_hdr[blockIdx.x] = make_uint2(0u, 0u);
+                            B.stage_hdr[i / kBlock] = make_uint2(0u, 0u);   // the block of slot i
                             Ll = nullptr;
                         }
                     }
@@ -683,10 +685,10 @@ __global__ void __launch_bounds__(kBlock) k_build(DevParams<T> P, DevBufs<T> B)
     __shared__ uint16_t toff[kStageCells];
     uint32_t tn = 0;
     if (P.staged) {   // block uniform
-        tn = B.stage_hdr[blockIdx.x].x;
+        tn = B.stage_hdr[q.b].x;
         for (uint32_t k = threadIdx.x; k < tn; k += kBlock) {
-            tcell[k] = B.stage_cell[(size_t)blockIdx.x * kStageCells + k];
-            toff[k] = B.stage_off[(size_t)blockIdx.x * kStageCells + k];
+            tcell[k] = B.stage_cell[(size_t)q.b * kStageCells + k];
+            toff[k] = B.stage_off[(size_t)q.b * kStageCells + k];
         }
         __syncthreads();
     }
@@ -746,11 +748,11 @@ template <class T, int LPP> constexpr int kPressureMinBlocks = (sizeof(T) == 4 &
 // false, without copying, for a block that is not staged or has more than cap records.  Every
 // thread of the block calls it (it synchronises the block).
 template <class Ld, class St>
-__device__ __forceinline__ bool stage_in(const DevBufs<float> &B, uint32_t cap, Ld load, St store)
+__device__ __forceinline__ bool stage_in(const DevBufs<float> &B, uint32_t blk, uint32_t cap, Ld load, St store)
 {
-    const uint2 hdr = B.stage_hdr[blockIdx.x];
+    const uint2 hdr = B.stage_hdr[blk];
     if (hdr.x == 0 || hdr.y > cap) return false;   // block uniform
-    const uint32_t *src = B.stage_src + (size_t)blockIdx.x * kStageCap;
+    const uint32_t *src = B.stage_src + (size_t)blk * kStageCap;
     constexpr uint32_t CH = 4;
 #pragma unroll 1
     for (uint32_t base = threadIdx.x; base < hdr.y; base += CH * kBlock) {
@@ -821,7 +823,7 @@ __global__ void __launch_bounds__(kBlock, kPressureMinBlocks<T, LPP>) k_pressure
     V3<T> a;
     if constexpr (LPP == 1 && sizeof(T) == 4) {
         extern __shared__ float4 stage_f4[];   // kStageCap records when staged
-        if (P.staged && stage_in(B, kStageCap, [&](uint32_t j) { return ldv(B.xk, j); },
+        if (P.staged && stage_in(B, q.b, kStageCap, [&](uint32_t j) { return ldv(B.xk, j); },
                                  [&](uint32_t m, const float4 &r) { stage_f4[m] = r; }))
             a = pressure_accel_g<LPP>(P, B, q, stage_f4);
         else
@@ -939,7 +941,7 @@ __global__ void __launch_bounds__(kBlock) k_jacobi(DevParams<T> P, DevBufs<T> B,
         if constexpr (LPP == 1 && sizeof(T) == 4) {
             extern __shared__ float2 stage_f2[];   // 3 x kStageCapJacobi when staged
             float2 *s0 = stage_f2, *s1 = stage_f2 + kStageCapJacobi, *s2 = stage_f2 + 2 * kStageCapJacobi;
-            if (P.staged && stage_in(B, kStageCapJacobi, [&](uint32_t j) { return ld_f8(B.xa + 2 * (size_t)j); },
+            if (P.staged && stage_in(B, q.b, kStageCapJacobi, [&](uint32_t j) { return ld_f8(B.xa + 2 * (size_t)j); },
                                      [&](uint32_t m, const F8 &r) {
                                          s0[m] = make_float2(r.a.x, r.a.y);
                                          s1[m] = make_float2(r.a.z, r.b.x);
