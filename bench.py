@@ -207,6 +207,59 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def config_table(args):
+    """Config 0 (the 8k dam break, 500 steps) on the GPU and on the host cores, and config 3
+    (the 256-scene ensemble) stepped scene by scene on the host cores, as the reference would
+    run it (one Simulation per process).  CPU legs: the FP32 build of the CPU restatement."""
+    import torch
+
+    from splishsplash_gb300 import scenes
+    from splishsplash_gb300.dfsph import TimeStepDFSPH
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    threads = cpu_cores()
+    sc = scenes.dambreak_8k()
+    ts = TimeStepDFSPH(sc, use_graph=True)
+    ts.step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(499):
+        ts.step()
+    torch.cuda.synchronize()
+    gpu_s = time.perf_counter() - t0
+    ts.close()
+    sim = oracle.OracleSim(sc, precision="f32", num_threads=threads)
+    t0 = time.perf_counter()
+    cpu_steps = 0
+    while cpu_steps < 500 and time.perf_counter() - t0 < args.cpu_budget:
+        sim.step()
+        cpu_steps += 1
+    cpu_s = time.perf_counter() - t0
+    ens = scenes.ensemble(num_scenes=256)
+    t0 = time.perf_counter()
+    done, parts = 0, 0
+    for e in ens:
+        s1 = oracle.OracleSim(e, precision="f32", num_threads=threads)
+        s1.step()
+        parts += e.n
+        done += 1
+        if time.perf_counter() - t0 > 3 * args.cpu_budget:
+            break
+    ens_s = time.perf_counter() - t0
+    return {
+        "config0": {"workload": f"{sc.name}: {sc.n} fluid + {sc.nb} boundary particles",
+                    "gpu": {"value": sc.n * 499 / gpu_s, "unit": UNIT, "steps": 499,
+                            "timing": "wall clock over steps 2..500, one graph launch and a statistics read per step"},
+                    "cpu": {"value": sc.n * cpu_steps / cpu_s, "unit": UNIT, "steps": cpu_steps, "cores": threads,
+                            "kind": "port"}},
+        "config3_cpu_sequential": {"value": parts / ens_s, "unit": UNIT, "cores": threads, "kind": "port",
+                                   "sample": f"first step of {done} of 256 scenes, one after the other, including "
+                                             f"each scene's set-up ({ens_s:.1f} s)"},
+    }
+
+
 def learned_line(steps):
     """The 2,097,152-lattice sphere scene with the classic and the learned warm start."""
     from splishsplash_gb300 import learned, scenes
@@ -284,6 +337,8 @@ def main():
                     help="lanes per particle of the neighbour passes (0: the library's autotuner)")
     ap.add_argument("--staging", type=int, default=0, choices=[0, 1, 2],
                     help="shared-memory staging of the solver passes: 0 autotuned, 1 off, 2 on")
+    ap.add_argument("--config-table", action="store_true",
+                    help="print configs 0 and 3 (GPU and host cores) as one JSON line and exit")
     ap.add_argument("--learned-steps", type=int, default=300)
     ap.add_argument("--ensemble-steps", type=int, default=60)
     args = ap.parse_args()
@@ -291,6 +346,9 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.config_table:
+        print(json.dumps({"config_table": config_table(args)}), flush=True)
         return
 
     import torch

@@ -294,7 +294,8 @@ int sphgb_get_lanes_per_particle(const sphgb_ctx *ctx, uint32_t *lanes, float tr
  * block of 256 particles copies the records of the cells around its particles into shared
  * memory once per pass and walks 16-bit local lists written by the list build in the order of
  * the fluid lists, so the results are bitwise those of the unstaged passes.  Blocks whose
- * neighbourhood exceeds 2048 particles read from global memory.  mode 0 (default): the
+ * neighbourhood exceeds 2048 particles (1536 in the Jacobi pass) read from global memory.
+ * mode 0 (default): the
  * autotuner times it as a fourth candidate (and a fixed lane count of 1 uses it); 1: off;
  * 2: on.  No reference counterpart. */
 int sphgb_set_neighbor_staging(sphgb_ctx *ctx, int mode);
