@@ -159,7 +159,11 @@ int sphgb_set_time_step(sphgb_ctx *ctx, double dt);
 int sphgb_get_time_step(const sphgb_ctx *ctx, double *dt);
 int sphgb_set_time(sphgb_ctx *ctx, double t);
 
-/* one TimeStepDFSPH::step(); stats may be NULL (then the call does not wait for the GPU) */
+/* one TimeStepDFSPH::step(); stats may be NULL (then the call does not wait for the GPU).
+ * SPHGB_ERR_STATE before an upload or for a fluid model without particles; SPHGB_ERR_GRID when a
+ * scene spans more than 1024 cells of 4.004 r per axis; SPHGB_ERR_CAPACITY when a neighbour list
+ * overflowed (the step's results are then incomplete); SPHGB_ERR_NONFINITE for a non-finite
+ * velocity. */
 int sphgb_step(sphgb_ctx *ctx, sphgb_stats *stats);
 /* blocks until the last step finished and fills stats */
 int sphgb_sync(sphgb_ctx *ctx, sphgb_stats *stats);

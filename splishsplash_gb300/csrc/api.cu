@@ -1525,6 +1525,7 @@ int sphgb_step(sphgb_ctx *c, sphgb_stats *stats)
 {
     if (!c) return SPHGB_ERR_ARGUMENT;
     if (!c->have_fluid) return fail(c, SPHGB_ERR_STATE, "sphgb_step before sphgb_upload_fluid");
+    if (c->n == 0) return fail(c, SPHGB_ERR_STATE, "sphgb_step of a fluid model without particles");
     cudaSetDevice(c->cfg.device);
     if (c->step_pending && c->scalars_dirty) {
         sphgb_stats st;
