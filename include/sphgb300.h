@@ -330,6 +330,40 @@ int sphgb_boundary_forces(sphgb_ctx *ctx, double *force, double *torque);
 /* zero the sums of one body (body < 0: of every body), ordered after the steps already enqueued */
 int sphgb_clear_boundary_forces(sphgb_ctx *ctx, int32_t body);
 
+/* Bender2019 boundaries (BoundaryModel_Bender2019, the reference's default boundary handling,
+ * Simulation.cpp:88): static bodies given as volume maps instead of boundary particles.
+ * A map is Discregrid's cubic Lagrange grid restated: res cells per axis over the body's box, the
+ * 32-node cubic serendipity element per cell, two fields per node, the signed distance phi (positive
+ * on the fluid side) and the boundary volume.  Every step samples each body at
+ * R^T (x_i - translation) and treats x_j = x_i - max(phi + r / 2, 2 r) n with volume V_j, for
+ * 0 < phi < 4 r, as one boundary particle per body in all DFSPH, XSPH sums
+ * (TimeStep::computeVolumeAndBoundaryX, TimeStep.cpp:219-340); a particle found inside a body
+ * is moved back by min(2 r - phi, r / 10) and stopped, as in the reference.  Supported: one
+ * scene, static bodies, no boundary particles uploaded, no boundary viscosity, no force
+ * feedback (other combinations fail at the step with SPHGB_ERR_STATE / SPHGB_ERR_ARGUMENT).
+ *
+ * sphgb_add_volume_map builds a map on the GPU in FP64 from a closed triangle mesh in body
+ * coordinates, as SimulatorBase::initVolumeMap does (SimulatorBase.cpp:2512-2660): box = mesh box
+ * grown by 8 h + thickness (h = 4 r of the current parameters), phi = sign (d - thickness) with d
+ * the pseudo-normal signed mesh distance and sign = -1 when invert (a container), volume = 0.8 x
+ * the Gauss-Legendre integral (order; 0 = 30, the reference's) over the support of the clipped
+ * kernel-weighted indicator.  rotation (row-major) / translation NULL = identity / 0.  body
+ * receives the map's index.  sphgb_add_volume_map_values adds a map from node values (as a
+ * reference "mapFile"); sphgb_get_volume_map reads one back (node count = (rx+1)(ry+1)(rz+1) +
+ * 2 rx(ry+1)(rz+1) + 2 (rx+1) ry (rz+1) + 2 (rx+1)(ry+1) rz; distance / volume may be NULL).
+ * sphgb_set_boundary_method: 0 Akinci2012 boundary particles (default), 2 Bender2019 maps
+ * ("boundaryHandlingMethod", Simulation.cpp:88). */
+int sphgb_add_volume_map(sphgb_ctx *ctx, const double *vertices, uint32_t nv, const uint32_t *faces, uint32_t nf,
+                         const uint32_t resolution[3], double thickness, int invert, const double rotation[9],
+                         const double translation[3], uint32_t order, uint32_t *body);
+int sphgb_add_volume_map_values(sphgb_ctx *ctx, const uint32_t resolution[3], const double box_min[3],
+                                const double box_max[3], const double *distance, const double *volume,
+                                const double rotation[9], const double translation[3], uint32_t *body);
+int sphgb_get_volume_map(sphgb_ctx *ctx, uint32_t body, uint32_t resolution[3], double box_min[3], double box_max[3],
+                         double *distance, double *volume);
+int sphgb_clear_volume_maps(sphgb_ctx *ctx);
+int sphgb_set_boundary_method(sphgb_ctx *ctx, int method);
+
 /* the cudaStream_t every kernel of this context is launched on (for event timing by callers) */
 int sphgb_get_stream(const sphgb_ctx *ctx, void **stream);
 

@@ -48,6 +48,18 @@ class OrcParams(ctypes.Structure):
         ("visco_max_error", ctypes.c_double),
         ("fp32_predicate", ctypes.c_int),
         ("num_threads", ctypes.c_int),
+        ("boundary_method", ctypes.c_int),
+    ]
+
+
+class OrcVmap(ctypes.Structure):
+    _fields_ = [
+        ("dmin", ctypes.c_double * 3),
+        ("dmax", ctypes.c_double * 3),
+        ("res", ctypes.c_uint * 3),
+        ("field", ctypes.c_void_p * 2),
+        ("R", ctypes.c_double * 9),
+        ("t", ctypes.c_double * 3),
     ]
 
 
@@ -86,6 +98,8 @@ class OrcState(ctypes.Structure):
         ("body_dynamic", ctypes.c_void_p),
         ("body_force", ctypes.c_void_p),
         ("body_torque", ctypes.c_void_p),
+        ("vmaps", ctypes.c_void_p),
+        ("nvmaps", ctypes.c_uint),
     ]
 
 
@@ -123,6 +137,16 @@ def lib(precision: str = "f64") -> ctypes.CDLL:
                                        ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint),
                                        ctypes.POINTER(ctypes.c_double)]
         L.orc_weiler_solve.restype = ctypes.c_int
+        L.orc_vmap_nodes.argtypes = [ctypes.c_void_p]
+        L.orc_vmap_nodes.restype = ctypes.c_size_t
+        L.orc_vmap_node_position.argtypes = [ctypes.POINTER(OrcVmap), ctypes.c_size_t, ctypes.c_void_p]
+        L.orc_vmap_node_position.restype = None
+        L.orc_vmap_interpolate.argtypes = [ctypes.POINTER(OrcVmap), ctypes.c_int, ctypes.c_void_p,
+                                           ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]
+        L.orc_vmap_interpolate.restype = ctypes.c_int
+        L.orc_vmap_build.argtypes = [ctypes.POINTER(OrcVmap), ctypes.c_void_p, ctypes.c_uint, ctypes.c_void_p,
+                                     ctypes.c_uint, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_uint]
+        L.orc_vmap_build.restype = ctypes.c_int
         _LIBS[precision] = L
     return _LIBS[precision]
 
@@ -157,6 +181,57 @@ def make_params(p, fp32_predicate: bool = True, num_threads: int = 0) -> OrcPara
 
 def _ptr(a: np.ndarray):
     return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+class VolumeMap:
+    """A Bender2019 volume map of one static body (oracle/vmap.c): signed distance and volume
+    on the cubic serendipity grid, built from a triangle mesh or given node values."""
+
+    def __init__(self, res, dmin=None, dmax=None, rotation=None, translation=None):
+        self.L = lib("f64")
+        self.m = OrcVmap()
+        self.m.res = (ctypes.c_uint * 3)(*[int(r) for r in res])
+        self.nodes = int(self.L.orc_vmap_nodes(_ptr(np.array(res, np.uint32))))
+        self.fields = [np.zeros(self.nodes, np.float64), np.zeros(self.nodes, np.float64)]
+        self.m.field = (ctypes.c_void_p * 2)(_ptr(self.fields[0]).value, _ptr(self.fields[1]).value)
+        if dmin is not None:
+            self.m.dmin = (ctypes.c_double * 3)(*dmin)
+            self.m.dmax = (ctypes.c_double * 3)(*dmax)
+        R = np.eye(3) if rotation is None else np.asarray(rotation, np.float64)
+        self.m.R = (ctypes.c_double * 9)(*R.ravel())
+        self.m.t = (ctypes.c_double * 3)(*(np.zeros(3) if translation is None else translation))
+
+    def build(self, vertices, faces, support, thickness=0.0, invert=False, order=30):
+        v = np.ascontiguousarray(vertices, np.float64)
+        f = np.ascontiguousarray(faces, np.uint32)
+        rc = self.L.orc_vmap_build(ctypes.byref(self.m), _ptr(v), v.shape[0], _ptr(f), f.shape[0], support,
+                                   thickness, int(invert), order)
+        if rc != 0:
+            raise RuntimeError(f"orc_vmap_build failed: {rc}")
+        return self
+
+    def set_values(self, dmin, dmax, sdf, volume):
+        self.m.dmin = (ctypes.c_double * 3)(*dmin)
+        self.m.dmax = (ctypes.c_double * 3)(*dmax)
+        self.fields[0][:] = sdf
+        self.fields[1][:] = volume
+        return self
+
+    def node_positions(self):
+        out = np.zeros((self.nodes, 3))
+        p = np.zeros(3)
+        for k in range(self.nodes):
+            self.L.orc_vmap_node_position(ctypes.byref(self.m), k, _ptr(p))
+            out[k] = p
+        return out
+
+    def interpolate(self, field, x):
+        """(value, gradient) at body-local point x, or None outside the grid."""
+        x = np.ascontiguousarray(x, np.float64)
+        v = ctypes.c_double()
+        g = np.zeros(3)
+        ok = self.L.orc_vmap_interpolate(ctypes.byref(self.m), int(field), _ptr(x), ctypes.byref(v), _ptr(g))
+        return (v.value, g) if ok else None
 
 
 class OracleSim:
@@ -217,6 +292,14 @@ class OracleSim:
         self.st.body_dynamic = _ptr(self.body_dynamic)
         self.st.body_force = _ptr(self.body_force)
         self.st.body_torque = _ptr(self.body_torque)
+
+    def set_volume_maps(self, maps):
+        """Bender2019 boundary: the bodies' VolumeMaps replace the boundary particles."""
+        self._vmaps = list(maps)
+        self._vmap_arr = (OrcVmap * max(1, len(self._vmaps)))(*[m.m for m in self._vmaps])
+        self.st.vmaps = ctypes.cast(self._vmap_arr, ctypes.c_void_p)
+        self.st.nvmaps = len(self._vmaps)
+        self.cp.boundary_method = 2
 
     def clear_forces(self):
         self.body_force[:] = 0.0

@@ -509,9 +509,11 @@ static double aij_pj(const ctx_t *c, long i)
     return acc;
 }
 
+/* neighbours of all point sets (TimeStepDFSPH.cpp:421-423); volume maps are no point set */
 static inline unsigned num_neighbors(const ctx_t *c, long i)
 {
-    return (c->F.off[i + 1] - c->F.off[i]) + (c->B.off[i + 1] - c->B.off[i]);
+    const unsigned nb = c->p->boundary_method == 2 ? 0u : (c->B.off[i + 1] - c->B.off[i]);
+    return (c->F.off[i + 1] - c->F.off[i]) + nb;
 }
 
 /* TimeStepDFSPH::divergenceSolve (TimeStepDFSPH.cpp:386-541) with
@@ -946,6 +948,71 @@ static double update_time_step(const ctx_t *c, double h)
     return hn;
 }
 
+/* TimeStep::computeVolumeAndBoundaryX (TimeStep.cpp:219-340) for static bodies (v_b = 0): for
+ * every particle and body (in body order, so a particle moved by one body is seen moved by the
+ * next, as in the reference), the boundary point x_j = x_i - max(phi + r / 2, 2 r) n and volume
+ * V_j of the particle's volume-map sample, and, for a particle inside a body (phi <= 0), its move
+ * of min(2 r - phi, r / 10) along n with v_i = 0.  The samples with V_j > 0 become the
+ * particle's boundary "neighbours" i * nbodies + b, so the Akinci2012 sums of the step apply to
+ * them unchanged, as forall_volume_maps does (Simulation.h:79-89). */
+static int volume_maps_boundary(ctx_t *c, real **xb_out, real **Vb_out)
+{
+    orc_state *s = c->s;
+    const unsigned nbod = s->nvmaps;
+    const long n = (long)s->n;
+    const double r = c->p->radius, hs = c->K.h;
+    real *xb = (real *)calloc(3 * (size_t)n * nbod + 1, sizeof(real));
+    real *Vb = (real *)calloc((size_t)n * nbod + 1, sizeof(real));
+    c->B.off = (unsigned *)calloc((size_t)n + 1, sizeof(unsigned));
+    c->B.idx = (unsigned *)malloc(((size_t)n * nbod + 1) * sizeof(unsigned));
+    if (!xb || !Vb || !c->B.off || !c->B.idx) { free(xb); free(Vb); return -2; }
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < n; i++) {
+        unsigned cnt = 0;
+        for (unsigned b = 0; b < nbod; b++) {
+            const orc_vmap *m = s->vmaps + b;
+            real *xr = s->x + 3 * i;
+            const double xi[3] = {(double)xr[0], (double)xr[1], (double)xr[2]};
+            double dx[3], local[3], gl[3] = {0, 0, 0}, nrm[3];
+            for (int d = 0; d < 3; d++) dx[d] = xi[d] - m->t[d];
+            for (int k = 0; k < 3; k++) local[k] = m->R[k] * dx[0] + m->R[3 + k] * dx[1] + m->R[6 + k] * dx[2];
+            double dist = DBL_MAX;
+            orc_vmap_interpolate(m, 0, local, &dist, gl);
+            for (int k = 0; k < 3; k++) nrm[k] = m->R[3 * k] * gl[0] + m->R[3 * k + 1] * gl[1] + m->R[3 * k + 2] * gl[2];
+            const double nl = sqrt(nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2]);
+            double V = 0.0, xj[3] = {0, 0, 0};
+            if (dist > 0.0 && dist < hs) {
+                double vol = DBL_MAX;
+                if (orc_vmap_interpolate(m, 1, local, &vol, NULL) && vol > 0.0 && vol != DBL_MAX && nl > 1.0e-9) {
+                    const double dd = fmax(dist + 0.5 * r, 2.0 * r);
+                    for (int d = 0; d < 3; d++) xj[d] = xi[d] - dd * (nrm[d] / nl);
+                    V = vol;
+                }
+            } else if (dist <= 0.0 && nl > 1.0e-5) {
+                const double delta = fmin(2.0 * r - dist, 0.1 * r);
+                for (int d = 0; d < 3; d++) {
+                    xr[d] = (real)(xi[d] + delta * (nrm[d] / nl));
+                    s->v[3 * i + d] = 0;
+                }
+            }
+            const size_t e = (size_t)i * nbod + b;
+            for (int d = 0; d < 3; d++) xb[3 * e + d] = (real)xj[d];
+            Vb[e] = (real)V;
+            if (Vb[e] > 0) cnt++;
+        }
+        c->B.off[i + 1] = cnt;
+    }
+    for (long i = 0; i < n; i++) c->B.off[i + 1] += c->B.off[i];
+    for (long i = 0; i < n; i++) {
+        unsigned k = c->B.off[i];
+        for (unsigned b = 0; b < nbod; b++)
+            if (Vb[(size_t)i * nbod + b] > 0) c->B.idx[k++] = (unsigned)((size_t)i * nbod + b);
+    }
+    *xb_out = xb;
+    *Vb_out = Vb;
+    return 0;
+}
+
 int orc_step(orc_state *s, const orc_params *p)
 {
 #ifdef _OPENMP
@@ -965,14 +1032,38 @@ int orc_step(orc_state *s, const orc_params *p)
     const long n = (long)s->n;
     int rc = 0;
 
+    /* Bender2019: static bodies without force feedback or boundary viscosity */
+    const int vmaps = p->boundary_method == 2;
+    if (vmaps && ((s->body && s->body_force) || (p->viscosity_method == 6 && p->viscosity_boundary != 0.0)))
+        return -5;
+    real *xb_saved = s->xb, *Vb_saved = s->Vb, *vxb = NULL, *vVb = NULL;
+    const unsigned nb_saved = s->nb;
     if (lists_build(&c.F, s->n, s->x, s->n, s->x, c.K.h, 1, p->fp32_predicate) != 0) return -1;
-    if (lists_build(&c.B, s->n, s->x, s->nb, s->xb, c.K.h, 0, p->fp32_predicate) != 0) { lists_free(&c.F); return -1; }
+    if (vmaps) {
+        /* after the neighbourhood search, before the densities (TimeStepDFSPH.cpp:141-142) */
+        if (volume_maps_boundary(&c, &vxb, &vVb) != 0) { lists_free(&c.F); lists_free(&c.B); return -2; }
+        s->xb = vxb;
+        s->Vb = vVb;
+        s->nb = s->n * s->nvmaps;
+    } else if (lists_build(&c.B, s->n, s->x, s->nb, s->xb, c.K.h, 0, p->fp32_predicate) != 0) {
+        lists_free(&c.F);
+        return -1;
+    }
     if (s->num_fluid_neighbors)
         for (long i = 0; i < n; i++) s->num_fluid_neighbors[i] = c.F.off[i + 1] - c.F.off[i];
     if (s->num_boundary_neighbors)
-        for (long i = 0; i < n; i++) s->num_boundary_neighbors[i] = c.B.off[i + 1] - c.B.off[i];
+        for (long i = 0; i < n; i++) s->num_boundary_neighbors[i] = vmaps ? 0u : c.B.off[i + 1] - c.B.off[i];
     double *err_buf = (double *)malloc(((size_t)n + 1) * sizeof(double));
-    if (!err_buf) { lists_free(&c.F); lists_free(&c.B); return -2; }
+    if (!err_buf) {
+        lists_free(&c.F);
+        lists_free(&c.B);
+        s->xb = xb_saved;
+        s->Vb = Vb_saved;
+        s->nb = nb_saved;
+        free(vxb);
+        free(vVb);
+        return -2;
+    }
 
     compute_densities(&c);
     compute_factor(&c);
@@ -1005,6 +1096,11 @@ int orc_step(orc_state *s, const orc_params *p)
     free(err_buf);
     lists_free(&c.F);
     lists_free(&c.B);
+    s->xb = xb_saved;
+    s->Vb = Vb_saved;
+    s->nb = nb_saved;
+    free(vxb);
+    free(vVb);
     return rc;
 }
 

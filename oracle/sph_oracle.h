@@ -26,6 +26,8 @@
 #ifndef SPH_ORACLE_H
 #define SPH_ORACLE_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -53,7 +55,21 @@ typedef struct orc_params {
     double visco_max_error;                    /* Weiler viscoMaxError */
     int fp32_predicate;          /* evaluate |xi-xj|^2 < h^2 in float (as the FP32 device path) */
     int num_threads;             /* OpenMP threads (0 = runtime default) */
+    int boundary_method;         /* Simulation "boundaryHandlingMethod": 0 Akinci2012 (boundary particles
+                                    xb, Vb), 2 Bender2019 (volume maps of orc_state.vmaps) */
 } orc_params;
+
+/* Volume map of one Bender2019 boundary body: Discregrid's CubicLagrangeDiscreteGrid (the
+ * cubic serendipity element of 32 nodes per cell: 8 vertices and 2 nodes at 1/3 and 2/3 of each
+ * edge, shared between cells) restated, with two fields: 0 signed distance, 1 boundary volume.
+ * The grid lies in body-local coordinates over [dmin, dmax] with res cells per axis; a point x
+ * of the scene is looked up at R^T (x - t). */
+typedef struct orc_vmap {
+    double dmin[3], dmax[3];
+    unsigned res[3];
+    double *field[2];            /* orc_vmap_nodes(res) values each */
+    double R[9], t[3];           /* rotation (row-major) and position of the body */
+} orc_vmap;
 
 typedef struct orc_state {
     unsigned n, nb;
@@ -83,6 +99,9 @@ typedef struct orc_state {
     const double *body_center;            /* 3 nbodies */
     const int *body_dynamic;              /* nbodies */
     double *body_force, *body_torque;     /* 3 nbodies */
+    /* Bender2019 boundary (boundary_method 2): one volume map per body */
+    const orc_vmap *vmaps;
+    unsigned nvmaps;
 } orc_state;
 
 /* Cubic spline (SPHKernels.h:16-91). */
@@ -104,6 +123,24 @@ int orc_boundary_volume(unsigned nb, const orc_real *xb, double support, int fp3
 
 /* One TimeStepDFSPH::step() (TimeStepDFSPH.cpp:117-249). */
 int orc_step(orc_state *s, const orc_params *p);
+
+/* ---- Bender2019 volume maps (vmap.c) ---- */
+/* nodes of a grid of res cells: vertices, then the x-, y- and z-edge nodes */
+size_t orc_vmap_nodes(const unsigned res[3]);
+void orc_vmap_node_position(const orc_vmap *m, size_t node, double p[3]);
+/* DiscreteGrid::interpolate with its gradient: 0 (value untouched) outside [dmin, dmax] */
+int orc_vmap_interpolate(const orc_vmap *m, int field, const double xl[3], double *value, double grad[3]);
+/* SimulatorBase::initVolumeMap (SimulatorBase.cpp:2512-2660): the domain is the mesh's box grown
+ * by 8 h + thickness; field 0 = sign (d - thickness), d the signed distance to the triangle mesh
+ * (positive outside, pseudo-normal sign), sign -1 when invert; field 1 = 0 where field 0 > 2 h,
+ * else 0.8 x the Gauss-Legendre integral (order, GaussQuadrature.cpp:5930-5962) over [-h, h]^3 of
+ * gamma(phi(x + y)) for |y| < h, gamma = 1 inside, W(phi) / W(0) within h, 0 beyond.  field[0]
+ * and field[1] must hold orc_vmap_nodes(res) values; R and t are left to the caller. */
+int orc_vmap_build(orc_vmap *m, const double *vert, unsigned nv, const unsigned *tri, unsigned nt,
+                   double support, double thickness, int invert, unsigned order);
+/* the domain orc_vmap_build uses, for sizing field arrays before the call */
+void orc_vmap_domain(const double *vert, unsigned nv, double support, double thickness, double dmin[3],
+                     double dmax[3]);
 
 /* Weiler2018 operator pieces for the CG pin (Viscosity_Weiler2018.cpp:271-443,
  * 605-742).  Lists are rebuilt from state positions. */

@@ -106,6 +106,18 @@ struct sphgb_ctx {
     uint32_t lpp_fixed = 0;            // 0: autotune on the first step after an upload
     bool tuned = false;
     float tune_ms[4] = {0, 0, 0, 0};   // trial step times of lanes per particle 1, 2, 4 and of staged passes
+    // Bender2019 boundary: volume maps of static bodies (own allocations, kept across uploads)
+    struct VMap {
+        uint32_t res[3];
+        double dmin[3], dmax[3], R[9], t[3];
+        double support;                // support radius the map was built for
+        double *f0 = nullptr, *f1 = nullptr;   // node fields (FP64)
+        void *coef = nullptr;                  // per-cell coefficients in the context's precision
+    };
+    int boundary_method = 0;           // 0 Akinci2012, 2 Bender2019
+    std::vector<VMap> vmaps;
+    void *d_vmaps = nullptr;           // VMapDev<T>[vmaps.size()]
+    void *bx = nullptr;                // prepared set: [maps][np] boundary points
     // neighbourhood staging of the solver passes (FP32, one lane per particle)
     int stage_mode = 0;                // 0: the autotuner decides, 1: off, 2: on
     bool staged = false;               // in use
@@ -148,14 +160,14 @@ namespace {
 enum KernelId {
     K_STEP_BEGIN, K_KEYS, K_SORT, K_GATHER, K_CELL_RANGES, K_BUILD, K_LOOP_BEGIN, K_PRESSURE_ACCEL, K_JACOBI,
     K_SOLVER_FINALIZE, K_XSPH, K_VISC_SETUP, K_CG_MATVEC, K_CG_UPDATE, K_CG_P, K_KICK, K_PRESS_INIT, K_INTEGRATE,
-    K_FEATURES, K_MLP, K_WS_SELECT, K_BODY_FORCES, K_STAGE_TABLE,
+    K_FEATURES, K_MLP, K_WS_SELECT, K_BODY_FORCES, K_STAGE_TABLE, K_VMAP_BOUNDARY,
     K_COUNT
 };
 const char *kKernelNames[K_COUNT] = {
     "step_begin", "keys", "radix_sort", "gather", "cell_ranges", "build_lists_density_alpha", "loop_begin",
     "pressure_accel", "jacobi_update", "solver_finalize", "xsph_gravity", "visc_setup", "cg_matvec", "cg_update",
     "cg_p", "kick_cfl", "press_init", "integrate", "features", "mlp_infer", "warmstart_select", "body_forces",
-    "stage_table",
+    "stage_table", "vmap_boundary",
 };
 
 // Brackets the launches of one kernel class with events on the context stream
@@ -257,7 +269,18 @@ void free_prepared(sphgb_ctx *c)
     c->bodies.body_nblk = nullptr;
     c->bodies.partials = nullptr;
     c->bodies.nblk = 0;
+    c->bx = nullptr;
     c->prepared = false;
+}
+
+void free_vmaps(sphgb_ctx *c)
+{
+    for (auto &m : c->vmaps)
+        for (void *p : {(void *)m.f0, (void *)m.f1, m.coef})
+            if (p) cudaFree(p);
+    c->vmaps.clear();
+    if (c->d_vmaps) cudaFree(c->d_vmaps);
+    c->d_vmaps = nullptr;
 }
 
 // the slot tables of the bodies (part of the prepared set)
@@ -377,6 +400,8 @@ template <class T> DevParams<T> make_params(const sphgb_ctx *c)
     P.capb = c->cfg.max_boundary_neighbors;
     P.lpp_log2 = c->lpp_log2;
     P.staged = (c->staged && !c->fp64 && c->lpp_log2 == 0 && c->ll) ? 1 : 0;
+    P.nvmaps = (c->boundary_method == 2 && c->bx) ? (uint32_t)c->vmaps.size() : 0u;
+    P.vmaps = static_cast<const VMapDev<T> *>(c->d_vmaps);
     return P;
 }
 
@@ -418,6 +443,7 @@ template <class T> DevBufs<T> make_bufs(const sphgb_ctx *c, int view)
     B.stage_cell = c->stage_cell;
     B.stage_off = c->stage_off;
     B.stage_src = c->stage_src;
+    B.bx = (v4 *)c->bx;
     B.ll = c->ll;
     B.key = c->key;
     B.key2 = c->key2;
@@ -634,6 +660,8 @@ template <class T> int prepare(sphgb_ctx *c)
             if (p) dfree(c->prep_allocs, p);
     }
     if ((rc = build_body_tables(c))) return rc;
+    if (c->boundary_method == 2 && !c->vmaps.empty())
+        if ((rc = palloc(c, &c->bx, (size_t)std::max(c->np, 1u) * c->vmaps.size() * vec_size(c)))) return rc;
     c->prepared = true;
     return SPHGB_OK;
 }
@@ -701,6 +729,7 @@ template <class T> void enqueue_prologue(sphgb_ctx *c, const DevParams<T> &P, co
         cudaMemsetAsync(c->cstart, 0xff, c->ncell * 4, s);
         launch_cell_ranges<T>(P, B1, s);
     }
+    if (P.nvmaps) { PROF(K_VMAP_BOUNDARY, s); launch_vmap_boundary<T>(P, B1, s); }
     if (P.staged) { PROF(K_STAGE_TABLE, s); launch_stage_table<T>(P, B1, s); }
     { PROF(K_BUILD, s); launch_build<T>(P, B1, s); }
     if (P.feat_on) { PROF(K_FEATURES, s); launch_features<T>(P, B1, s); }
@@ -936,9 +965,53 @@ template <class T> int autotune(sphgb_ctx *c)
     return SPHGB_OK;
 }
 
+// The Bender2019 configurations this path supports: one scene, static bodies given only as volume
+// maps built for the current support radius, no boundary viscosity, no force feedback.
+int check_boundary_method(sphgb_ctx *c)
+{
+    if (c->boundary_method != 2) return SPHGB_OK;
+    if (c->vmaps.empty()) return fail(c, SPHGB_ERR_STATE, "Bender2019 boundary without volume maps");
+    if (c->scn.size() > 1) return fail(c, SPHGB_ERR_STATE, "volume maps serve a single scene, not a batch");
+    if (c->nb) return fail(c, SPHGB_ERR_STATE, "the Bender2019 boundary takes no boundary particles");
+    if (c->nbodies) return fail(c, SPHGB_ERR_ARGUMENT, "force feedback is not available for volume maps");
+    if (c->prm.viscosity_method == 6 && c->prm.viscosity_boundary != 0.0)
+        return fail(c, SPHGB_ERR_ARGUMENT, "boundary viscosity is not available for volume maps");
+    for (const auto &m : c->vmaps)
+        if (m.support != 4.0 * c->prm.particle_radius)
+            return fail(c, SPHGB_ERR_STATE, "a volume map was built for another particle radius");
+    return SPHGB_OK;
+}
+
+// the maps as the step reads them (VMapDev<T>), uploaded after any change
+template <class T> int upload_vmaps(sphgb_ctx *c)
+{
+    if (c->d_vmaps) cudaFree(c->d_vmaps);
+    c->d_vmaps = nullptr;
+    if (c->vmaps.empty()) return SPHGB_OK;
+    std::vector<VMapDev<T>> h(c->vmaps.size());
+    for (size_t b = 0; b < c->vmaps.size(); b++) {
+        const auto &m = c->vmaps[b];
+        VMapDev<T> &d = h[b];
+        for (int k = 0; k < 3; k++) {
+            d.dmin[k] = (T)m.dmin[k];
+            d.dmax[k] = (T)m.dmax[k];
+            d.cs[k] = (T)((m.dmax[k] - m.dmin[k]) / (double)m.res[k]);
+            d.t[k] = (T)m.t[k];
+            d.res[k] = m.res[k];
+        }
+        for (int k = 0; k < 9; k++) d.R[k] = (T)m.R[k];
+        d.pad = 0;
+        d.coef = static_cast<const T *>(m.coef);
+    }
+    CK(cudaMalloc(&c->d_vmaps, h.size() * sizeof(VMapDev<T>)));
+    CK(cudaMemcpy(c->d_vmaps, h.data(), h.size() * sizeof(VMapDev<T>), cudaMemcpyHostToDevice));
+    return SPHGB_OK;
+}
+
 template <class T> int do_step(sphgb_ctx *c)
 {
     int rc;
+    if ((rc = check_boundary_method(c))) return rc;
     if (!c->prepared && (rc = prepare<T>(c))) return rc;
     if ((rc = upload_scalars(c))) return rc;
     if (!c->tuned) {
@@ -1347,6 +1420,7 @@ int sphgb_destroy(sphgb_ctx *c)
     if (c->export_stream) cudaStreamSynchronize(c->export_stream);
     free_all(c);
     free_bodies(c);
+    free_vmaps(c);
     if (c->hsc) cudaFreeHost(c->hsc);
     if (c->export_dev) cudaFree(c->export_dev);
     if (c->export_host) cudaFreeHost(c->export_host);
@@ -1722,6 +1796,146 @@ int sphgb_clear_boundary_forces(sphgb_ctx *c, int32_t body)
     cudaSetDevice(c->cfg.device);
     if (body < 0) CK(cudaMemsetAsync(c->bodies.acc, 0, 6 * (size_t)c->nbodies * sizeof(double), c->stream));
     else CK(cudaMemsetAsync(c->bodies.acc + 6 * (size_t)body, 0, 6 * sizeof(double), c->stream));
+    return SPHGB_OK;
+}
+
+namespace {
+// register a map whose node fields f0 / f1 (device, FP64) are filled: per-cell coefficients and
+// the device table; the prepared set is rebuilt at the next step
+int add_vmap(sphgb_ctx *c, sphgb_ctx::VMap &m, uint32_t *body)
+{
+    const VMapLayout L(m.res[0], m.res[1], m.res[2]);
+    const size_t bytes = (size_t)L.cells() * 64 * real_size(c);
+    cudaError_t e = cudaMalloc(&m.coef, bytes);
+    if (e == cudaSuccess)
+        e = c->fp64 ? vmap_expand_device<double>(m.res, m.f0, m.f1, (double *)m.coef, c->stream)
+                    : vmap_expand_device<float>(m.res, m.f0, m.f1, (float *)m.coef, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        for (void *p : {(void *)m.f0, (void *)m.f1, m.coef})
+            if (p) cudaFree(p);
+        return fail(c, SPHGB_ERR_CUDA, std::string("volume map: ") + cudaGetErrorString(e));
+    }
+    c->vmaps.push_back(m);
+    if (body) *body = (uint32_t)c->vmaps.size() - 1;
+    const int rc = c->fp64 ? upload_vmaps<double>(c) : upload_vmaps<float>(c);
+    c->prepared = false;
+    invalidate_graphs(c);
+    return rc;
+}
+
+int vmap_init(sphgb_ctx *c, sphgb_ctx::VMap &m, const uint32_t res[3], const double *rotation, const double *translation)
+{
+    uint64_t cells = 1;
+    for (int k = 0; k < 3; k++) {
+        if (res[k] == 0 || res[k] > 1024) return fail(c, SPHGB_ERR_ARGUMENT, "map resolution must be 1..1024 per axis");
+        m.res[k] = res[k];
+        cells *= res[k];
+    }
+    const VMapLayout L(res[0], res[1], res[2]);
+    if (L.nodes() >= 0x7fffffffull || cells >= 0x7fffffffull) return fail(c, SPHGB_ERR_ARGUMENT, "map too large");
+    static const double kI[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1}, kZ[3] = {0, 0, 0};
+    std::memcpy(m.R, rotation ? rotation : kI, sizeof(m.R));
+    std::memcpy(m.t, translation ? translation : kZ, sizeof(m.t));
+    if (cudaMalloc(&m.f0, L.nodes() * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&m.f1, L.nodes() * sizeof(double)) != cudaSuccess) {
+        if (m.f0) cudaFree(m.f0);
+        cudaGetLastError();
+        return fail(c, SPHGB_ERR_CUDA, "cudaMalloc of a volume map");
+    }
+    return SPHGB_OK;
+}
+}  // namespace
+
+int sphgb_add_volume_map(sphgb_ctx *c, const double *vertices, uint32_t nv, const uint32_t *faces, uint32_t nf,
+                         const uint32_t resolution[3], double thickness, int invert, const double rotation[9],
+                         const double translation[3], uint32_t order, uint32_t *body)
+{
+    if (!c || !vertices || !faces || nv == 0 || nf == 0 || !resolution) return SPHGB_ERR_ARGUMENT;
+    for (size_t k = 0; k < 3 * (size_t)nf; k++)
+        if (faces[k] >= nv) return fail(c, SPHGB_ERR_ARGUMENT, "face index out of range");
+    int rc = check_finite(c, vertices, 3 * (size_t)nv, "mesh vertex");
+    if (rc) return rc;
+    if (!std::isfinite(thickness)) return fail(c, SPHGB_ERR_NONFINITE, "non-finite map thickness");
+    cudaSetDevice(c->cfg.device);
+    sphgb_ctx::VMap m;
+    if ((rc = vmap_init(c, m, resolution, rotation, translation))) return rc;
+    m.support = 4.0 * c->prm.particle_radius;
+    vmap_domain(vertices, nv, m.support, thickness, m.dmin, m.dmax);
+    cudaError_t e = vmap_build_device(vertices, nv, faces, nf, m.res, m.support, thickness, invert, order ? order : 30u,
+                                      m.f0, m.f1, m.dmin, m.dmax, c->stream);
+    if (e != cudaSuccess) {
+        cudaFree(m.f0);
+        cudaFree(m.f1);
+        return fail(c, SPHGB_ERR_CUDA, std::string("volume map construction: ") + cudaGetErrorString(e));
+    }
+    return add_vmap(c, m, body);
+}
+
+int sphgb_add_volume_map_values(sphgb_ctx *c, const uint32_t resolution[3], const double dmin[3], const double dmax[3],
+                                const double *distance, const double *volume, const double rotation[9],
+                                const double translation[3], uint32_t *body)
+{
+    if (!c || !resolution || !dmin || !dmax || !distance || !volume) return SPHGB_ERR_ARGUMENT;
+    for (int k = 0; k < 3; k++)
+        if (!(dmax[k] > dmin[k])) return fail(c, SPHGB_ERR_ARGUMENT, "empty map box");
+    cudaSetDevice(c->cfg.device);
+    sphgb_ctx::VMap m;
+    int rc = vmap_init(c, m, resolution, rotation, translation);
+    if (rc) return rc;
+    const size_t nodes = VMapLayout(m.res[0], m.res[1], m.res[2]).nodes();
+    if ((rc = check_finite(c, distance, nodes, "map distance")) || (rc = check_finite(c, volume, nodes, "map volume"))) {
+        cudaFree(m.f0);
+        cudaFree(m.f1);
+        return rc;
+    }
+    std::memcpy(m.dmin, dmin, sizeof(m.dmin));
+    std::memcpy(m.dmax, dmax, sizeof(m.dmax));
+    m.support = 4.0 * c->prm.particle_radius;
+    if (cudaMemcpy(m.f0, distance, nodes * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(m.f1, volume, nodes * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(m.f0);
+        cudaFree(m.f1);
+        return fail(c, SPHGB_ERR_CUDA, "volume map upload");
+    }
+    return add_vmap(c, m, body);
+}
+
+int sphgb_get_volume_map(sphgb_ctx *c, uint32_t body, uint32_t resolution[3], double dmin[3], double dmax[3],
+                         double *distance, double *volume)
+{
+    if (!c || body >= c->vmaps.size()) return SPHGB_ERR_ARGUMENT;
+    const auto &m = c->vmaps[body];
+    for (int k = 0; k < 3; k++) {
+        if (resolution) resolution[k] = m.res[k];
+        if (dmin) dmin[k] = m.dmin[k];
+        if (dmax) dmax[k] = m.dmax[k];
+    }
+    const size_t nodes = VMapLayout(m.res[0], m.res[1], m.res[2]).nodes();
+    cudaSetDevice(c->cfg.device);
+    if (distance) CK(cudaMemcpy(distance, m.f0, nodes * sizeof(double), cudaMemcpyDeviceToHost));
+    if (volume) CK(cudaMemcpy(volume, m.f1, nodes * sizeof(double), cudaMemcpyDeviceToHost));
+    return SPHGB_OK;
+}
+
+int sphgb_clear_volume_maps(sphgb_ctx *c)
+{
+    if (!c) return SPHGB_ERR_ARGUMENT;
+    cudaSetDevice(c->cfg.device);
+    CK(cudaStreamSynchronize(c->stream));
+    free_vmaps(c);
+    c->prepared = false;
+    invalidate_graphs(c);
+    return SPHGB_OK;
+}
+
+int sphgb_set_boundary_method(sphgb_ctx *c, int method)
+{
+    if (!c || (method != 0 && method != 2)) return SPHGB_ERR_ARGUMENT;
+    if (method == c->boundary_method) return SPHGB_OK;
+    c->boundary_method = method;
+    c->prepared = false;
+    invalidate_graphs(c);
     return SPHGB_OK;
 }
 

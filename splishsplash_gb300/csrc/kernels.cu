@@ -497,6 +497,66 @@ __device__ __forceinline__ uint32_t stage_find(const uint32_t *cells, uint32_t n
     return lo;
 }
 
+// TimeStep::computeVolumeAndBoundaryX (TimeStep.cpp:219-340), static bodies: for every body in
+// turn, the volume-map sample at R^T (x_i - t) gives the distance phi, its gradient (the normal
+// n = R grad phi / |.|) and the volume V.  For 0 < phi < h and V > 0 the particle gets the boundary
+// point x_j = x_i - max(phi + r / 2, 2 r) n with volume V_j = V; a particle inside a body
+// (phi <= 0) is moved by min(2 r - phi, r / 10) along n and stops (the reference's fallback for
+// too large steps), and the next body sees it moved.  The boundary sums of the step then treat
+// (x_j, V_j) like one boundary particle per body (forall_volume_maps, Simulation.h:79-89).
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_vmap_boundary(DevParams<T> P, DevBufs<T> B)
+{
+    count_launch(&B.gsc->launches);
+    const SlotInfo q = slot_info(P);
+    if (!q.act) return;
+    const uint32_t i = q.i;
+    const T r = (T)P.radius, hs = P.K.h;
+    for (uint32_t b = 0; b < P.nvmaps; b++) {
+        const VMapDev<T> &m = P.vmaps[b];
+        v4_t<T> x = ldv(B.x, i);
+        const T dx[3] = {(T)x.x - m.t[0], (T)x.y - m.t[1], (T)x.z - m.t[2]};
+        T local[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) local[k] = m.R[k] * dx[0] + m.R[3 + k] * dx[1] + m.R[6 + k] * dx[2];
+        T sdf = T(0), vol = T(0), g[3] = {T(0), T(0), T(0)};
+        V3<T> xj = mk3<T>(0, 0, 0);
+        T V = T(0);
+        if (vmap_sample<T>(m, local, sdf, g, vol)) {
+            const V3<T> nrm = mk3<T>(m.R[0] * g[0] + m.R[1] * g[1] + m.R[2] * g[2],
+                                     m.R[3] * g[0] + m.R[4] * g[1] + m.R[5] * g[2],
+                                     m.R[6] * g[0] + m.R[7] * g[1] + m.R[8] * g[2]);
+            const T nl = dev_sqrt(dot(nrm, nrm));
+            if (sdf > T(0) && sdf < hs) {
+                if (vol > T(0) && nl > T(1.0e-9)) {
+                    const T d = fmax(sdf + T(0.5) * r, T(2) * r);
+                    xj = sub(xyz<T>(x), scl(nrm, d / nl));
+                    V = vol;
+                }
+            } else if (sdf <= T(0) && nl > T(1.0e-5)) {
+                const T delta = fmin(T(2) * r - sdf, T(0.1) * r);
+                const V3<T> mv = scl(nrm, delta / nl);
+                if (B.xlo) {   // double-float position
+                    const float4 lo = B.xlo[i];
+                    const double px = (double)x.x + (double)lo.x + (double)mv.x;
+                    const double py = (double)x.y + (double)lo.y + (double)mv.y;
+                    const double pz = (double)x.z + (double)lo.z + (double)mv.z;
+                    x.x = (T)px; x.y = (T)py; x.z = (T)pz;
+                    B.xlo[i] = make_float4((float)(px - (double)x.x), (float)(py - (double)x.y),
+                                           (float)(pz - (double)x.z), 0.f);
+                } else {
+                    x.x += mv.x; x.y += mv.y; x.z += mv.z;
+                }
+                stv(B.x, i, x);
+                v4_t<T> v = ldv(B.v, i);
+                v.x = T(0); v.y = T(0); v.z = T(0);
+                stv(B.v, i, v);
+            }
+        }
+        stv(B.bx, b * P.np + i, pack(xj, V));
+    }
+}
+
 // Build the fluid and boundary neighbour lists of particle i and, in the same
 // kernel, compute (TimeStep.cpp:116-169) the density, (TimeStepDFSPH.cpp:1106-1186)
 // the DFSPH factor alpha, (TimeStepDFSPH.cpp:1247-1295) the divergence source and
@@ -618,17 +678,22 @@ __device__ __forceinline__ void build_one(const DevParams<T> &P, const DevBufs<T
                               gf = add(gf, g);
                               divf += dot(sub(vi, xyz<T>(d.v)), g);
                           });
-    nbr_loop<kUnroll>(Lb, min(nb, P.capb), [&](uint32_t j) { return ldv(B.xb, j); },
-                      [&](uint32_t, const v4_t<T> &xj) {
-                          const V3<T> r = diff3<T>(xi, xj);
-                          T W, c;
-                          kernel_W_coef_d2(P.K, dot(r, r), W, c);
-                          const T Vb = (T)xj.w;
-                          wb += Vb * W;
-                          const V3<T> g = scl(r, c * Vb);
-                          gb = add(gb, g);
-                          divb += dot(vi, g);
-                      });
+    auto boundary_term = [&](uint32_t, const v4_t<T> &xj) {
+        const V3<T> r = diff3<T>(xi, xj);
+        T W, c;
+        kernel_W_coef_d2(P.K, dot(r, r), W, c);
+        const T Vb = (T)xj.w;
+        wb += Vb * W;
+        const V3<T> g = scl(r, c * Vb);
+        gb = add(gb, g);
+        divb += dot(vi, g);
+    };
+    nbr_loop<kUnroll>(Lb, min(nb, P.capb), [&](uint32_t j) { return ldv(B.xb, j); }, boundary_term);
+    // Bender2019: the volume-map sample of each body, x_j with V_j in w, where V_j > 0
+    for (uint32_t b = 0; b < P.nvmaps; b++) {
+        const v4_t<T> xj = ldv(B.bx, b * P.np + i);
+        if ((T)xj.w > T(0)) boundary_term(b, xj);
+    }
     B.nf[i] = nf;
     B.nbn[i] = nb;
     if (nf > P.capf || nb > P.capb) atomicOr(&sc->flags, kFlagOverflow);
@@ -1018,6 +1083,7 @@ __global__ void k_step_begin(StepScalars *sc, StepScalars *gsc, uint32_t nscenes
         r.max_nf = 0;
         r.max_nb = 0;
         r.maxvel_bits = 0;
+        r.maxvel_bits64 = 0ull;
         r.iters_cg = 0;
         r.cg_err = 0.0;
         r.cg_state = 1;
@@ -1362,7 +1428,7 @@ __global__ void __launch_bounds__(kBlock) k_kick(DevParams<T> P, DevBufs<T> B)
     count_launch(&B.gsc->launches);
     const SlotInfo q = slot_info(P);
     StepScalars *const sc = B.sc + q.s;
-    float m = 0.0f;
+    T m = T(0);                  // |v + a h|^2 in the context's precision
     const double hd = sc->dt;
     if (q.act) {
         const uint32_t i = q.i;
@@ -1380,24 +1446,25 @@ __global__ void __launch_bounds__(kBlock) k_kick(DevParams<T> P, DevBufs<T> B)
         const V3<T> vn = add(v, scl(a, h));
         const T m2 = dot(vn, vn);
         if (!(m2 <= T(3.0e38))) atomicOr(&sc->flags, kFlagNonFinite);
-        m = (float)m2;
-        if (!(m >= 0.0f)) m = 0.0f;
+        m = m2;
+        if (!(m >= T(0))) m = T(0);
         v4.x = vn.x; v4.y = vn.y; v4.z = vn.z;
         stv(B.v, i, v4);
     }
-    // block max -> atomicMax on the float bits (non-negative floats order like uint)
+    // block max -> atomicMax on the bits (non-negative floats / doubles order like unsigned integers)
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
-    __shared__ float wm[32];
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+    __shared__ T wm[32];
     __shared__ bool amLast;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0) wm[warp] = m;
     __syncthreads();
     const ReduceSlot rs = scene_reduce(P, B, q);
     if (threadIdx.x == 0) {
-        float bm = 0.0f;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) bm = fmaxf(bm, wm[w]);
-        atomicMax(&sc->maxvel_bits, __float_as_uint(bm));
+        T bm = T(0);
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) bm = fmax(bm, wm[w]);
+        if constexpr (sizeof(T) == 8) atomicMax(&sc->maxvel_bits64, (unsigned long long)__double_as_longlong((double)bm));
+        else atomicMax(&sc->maxvel_bits, __float_as_uint((float)bm));
         __threadfence();
         const unsigned t = atomicAdd(rs.counter, 1u);
         amLast = (t == rs.count - 1);
@@ -1405,8 +1472,14 @@ __global__ void __launch_bounds__(kBlock) k_kick(DevParams<T> P, DevBufs<T> B)
     __syncthreads();
     if (amLast && threadIdx.x == 0) {
         __threadfence();
-        double maxVel = (double)__uint_as_float(atomicAdd(&sc->maxvel_bits, 0u));
-        sc->maxvel_bits = 0;
+        double maxVel;
+        if constexpr (sizeof(T) == 8) {
+            maxVel = __longlong_as_double((long long)atomicAdd(&sc->maxvel_bits64, 0ull));
+            sc->maxvel_bits64 = 0ull;
+        } else {
+            maxVel = (double)__uint_as_float(atomicAdd(&sc->maxvel_bits, 0u));
+            sc->maxvel_bits = 0;
+        }
         *rs.counter = 0;
         double hn = hd;
         if (P.cfl_method != 0) {
@@ -2145,6 +2218,10 @@ template <class T> void launch_cell_ranges(const DevParams<T> &P, const DevBufs<
 {
     if (P.np) k_cell_ranges<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
 }
+template <class T> void launch_vmap_boundary(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
+{
+    if (P.np && P.nvmaps) k_vmap_boundary<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
+}
 template <class T> void launch_stage_table(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {
     if (P.np && P.staged) k_stage_table<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
@@ -2326,6 +2403,7 @@ void launch_lists_to_ids(const uint32_t *list, const uint32_t *cnt, uint32_t cap
     template void launch_cell_ranges<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                    \
     template void launch_build<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                          \
     template void launch_stage_table<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                    \
+    template void launch_vmap_boundary<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                  \
     template void launch_pressure_accel<T>(const DevParams<T> &, const DevBufs<T> &, bool, cudaStream_t,            \
                                            cudaGraphConditionalHandle, bool);                                       \
     template void launch_jacobi<T>(const DevParams<T> &, const DevBufs<T> &, bool, cudaGraphConditionalHandle, bool, \

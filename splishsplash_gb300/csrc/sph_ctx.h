@@ -13,6 +13,7 @@
 #include <stdint.h>
 
 #include "sph_common.cuh"
+#include "vmap.cuh"
 
 namespace sphgb {
 
@@ -40,6 +41,7 @@ struct StepScalars {
     unsigned launches;     // kernels launched in the current step (global record)
     unsigned ws_used;      // bit 0: learned warm start used by the divergence solve, bit 1: pressure solve
     unsigned pad[2];
+    unsigned long long maxvel_bits64;   // FP64 contexts: max |v + a h|^2 as the bits of a non-negative double
 };
 
 constexpr unsigned kFlagOverflow = 1u;
@@ -86,6 +88,8 @@ template <class T> struct DevParams {
     uint32_t capf, capb;
     uint32_t lpp_log2;            // lanes per particle of the neighbour passes (1, 2 or 4) = 1 << lpp_log2;
                                   // also fixes the layout of the fluid lists
+    uint32_t nvmaps;              // Bender2019 boundary: volume maps (bodies); 0 = Akinci2012 particles
+    const VMapDev<T> *vmaps;      // device array [nvmaps]
     int staged;                   // FP32, one lane per particle: the solver passes read their block's
                                   // neighbourhood from shared memory (stage tables, local lists)
 };
@@ -126,6 +130,7 @@ template <class T> struct DevBufs {
                                  // written by the pressure-acceleration pass, read by the Jacobi pass
     v4 *xk;                      // x_i with the running solver's kappa_i in w (one gather per pair)
     v4 *bg;                      // per-particle boundary sums: xyz = sum_b V_b gradW_ib, w = sum_b V_b W_ib
+    v4 *bx;                      // Bender2019: [nvmaps][np] boundary point x_j of each particle's map sample, w = V_j
     T *density, *factor, *dadv;
     uint32_t *nf, *nbn;
     uint32_t *lf, *lb;
@@ -179,11 +184,25 @@ struct BodyDev {
     uint32_t nblk;
 };
 
+// ---- Bender2019 volume maps (vmap.cu) ----
+// the grid box of a map: the mesh's bounding box grown by 8 support + thickness
+void vmap_domain(const double *vert, uint32_t nv, double support, double thickness, double dmin[3], double dmax[3]);
+// node fields (device, FP64, VMapLayout(res).nodes() each) of the map of a triangle mesh; waits for the stream
+cudaError_t vmap_build_device(const double *vert, uint32_t nv, const uint32_t *tri, uint32_t nt, const uint32_t res[3],
+                              double support, double thickness, int invert, uint32_t order, double *f0, double *f1,
+                              const double dmin[3], const double dmax[3], cudaStream_t s);
+// the per-cell coefficient layout the step reads (VMapDev::coef)
+template <class T>
+cudaError_t vmap_expand_device(const uint32_t res[3], const double *f0, const double *f1, T *coef, cudaStream_t s);
+
 // ---- launchers (defined in kernels.cu / sort.cu, instantiated for float and double)
 template <class T> void launch_keys(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
 template <class T> void launch_gather(const DevParams<T> &P, const DevBufs<T> &B, const uint32_t *perm, cudaStream_t s);
 template <class T> void launch_cell_ranges(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
 template <class T> void launch_build(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
+// Bender2019: each particle's boundary points and volumes, particles inside a body moved out
+// (after the cell ranges, before the list build)
+template <class T> void launch_vmap_boundary(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
 // stage tables of the step (staged mode; after the cell ranges, before the list build)
 template <class T> void launch_stage_table(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
 // shared-memory limits of the staged solver passes; call once per device before their first launch

@@ -125,6 +125,8 @@ EXPORTS = [
     "sphgb_export_vtk", "sphgb_export_wait", "sphgb_save_state", "sphgb_load_state",
     "sphgb_set_boundary_bodies", "sphgb_boundary_forces", "sphgb_clear_boundary_forces",
     "sphgb_set_neighbor_staging", "sphgb_get_neighbor_staging",
+    "sphgb_add_volume_map", "sphgb_add_volume_map_values", "sphgb_get_volume_map", "sphgb_clear_volume_maps",
+    "sphgb_set_boundary_method",
 ]
 
 _lib = None
@@ -183,6 +185,11 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.sphgb_boundary_forces.argtypes = [vp, vp, vp]
     L.sphgb_clear_boundary_forces.argtypes = [vp, i32]
     L.sphgb_set_neighbor_staging.argtypes = [vp, i32]
+    L.sphgb_add_volume_map.argtypes = [vp, vp, u32, vp, u32, vp, dbl, i32, vp, vp, u32, ctypes.POINTER(u32)]
+    L.sphgb_add_volume_map_values.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, ctypes.POINTER(u32)]
+    L.sphgb_get_volume_map.argtypes = [vp, u32, vp, vp, vp, vp, vp]
+    L.sphgb_clear_volume_maps.argtypes = [vp]
+    L.sphgb_set_boundary_method.argtypes = [vp, i32]
     L.sphgb_get_neighbor_staging.argtypes = [vp, ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_float),
                                              ctypes.POINTER(ctypes.c_float)]
     L.sphgb_profile_enable.argtypes = [vp, i32]
@@ -494,6 +501,58 @@ class Context:
     def clear_boundary_forces(self, body: int = -1):
         """BoundaryModel::clearForceAndTorque of one body (default: every body)."""
         self._check(self.L.sphgb_clear_boundary_forces(self.h, int(body)))
+
+    # ---- Bender2019 volume maps ------------------------------------------------
+    @staticmethod
+    def volume_map_nodes(res):
+        nx, ny, nz = (int(r) for r in res)
+        return ((nx + 1) * (ny + 1) * (nz + 1) + 2 * nx * (ny + 1) * (nz + 1) + 2 * (nx + 1) * ny * (nz + 1)
+                + 2 * (nx + 1) * (ny + 1) * nz)
+
+    def add_volume_map(self, vertices, faces, res, thickness=0.0, invert=False, rotation=None, translation=None,
+                       order=0):
+        """Build the volume map of a static body from its triangle mesh; returns the body index."""
+        v = np.ascontiguousarray(vertices, np.float64)
+        f = np.ascontiguousarray(faces, np.uint32)
+        r = np.ascontiguousarray(res, np.uint32)
+        R = None if rotation is None else np.ascontiguousarray(rotation, np.float64)
+        t = None if translation is None else np.ascontiguousarray(translation, np.float64)
+        body = ctypes.c_uint32()
+        self._check(self.L.sphgb_add_volume_map(self.h, _p(v), v.shape[0], _p(f), f.shape[0], _p(r), float(thickness),
+                                                int(invert), _p(R), _p(t), int(order), ctypes.byref(body)))
+        return int(body.value)
+
+    def add_volume_map_values(self, res, box_min, box_max, distance, volume, rotation=None, translation=None):
+        r = np.ascontiguousarray(res, np.uint32)
+        lo = np.ascontiguousarray(box_min, np.float64)
+        hi = np.ascontiguousarray(box_max, np.float64)
+        d = np.ascontiguousarray(distance, np.float64)
+        vol = np.ascontiguousarray(volume, np.float64)
+        R = None if rotation is None else np.ascontiguousarray(rotation, np.float64)
+        t = None if translation is None else np.ascontiguousarray(translation, np.float64)
+        body = ctypes.c_uint32()
+        self._check(self.L.sphgb_add_volume_map_values(self.h, _p(r), _p(lo), _p(hi), _p(d), _p(vol), _p(R), _p(t),
+                                                       ctypes.byref(body)))
+        return int(body.value)
+
+    def volume_map(self, body):
+        """(res, box_min, box_max, distance, volume) of a map; node values in FP64."""
+        r = np.zeros(3, np.uint32)
+        lo = np.zeros(3)
+        hi = np.zeros(3)
+        self._check(self.L.sphgb_get_volume_map(self.h, int(body), _p(r), _p(lo), _p(hi), None, None))
+        n = self.volume_map_nodes(r)
+        d = np.zeros(n)
+        vol = np.zeros(n)
+        self._check(self.L.sphgb_get_volume_map(self.h, int(body), None, None, None, _p(d), _p(vol)))
+        return r, lo, hi, d, vol
+
+    def clear_volume_maps(self):
+        self._check(self.L.sphgb_clear_volume_maps(self.h))
+
+    def set_boundary_method(self, method: int):
+        """0 Akinci2012 boundary particles, 2 Bender2019 volume maps."""
+        self._check(self.L.sphgb_set_boundary_method(self.h, int(method)))
 
     def set_neighbor_staging(self, mode: int = 0):
         """Shared-memory staging of the solver passes: 0 autotuned (default), 1 off, 2 on."""

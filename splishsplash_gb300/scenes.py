@@ -126,6 +126,18 @@ def box_walls(box_min, box_max, spacing):
     return box_min + idx * step
 
 
+def box_mesh(box_min, box_max):
+    """Closed triangle mesh of an axis-aligned box: 8 vertices, 12 triangles wound
+    counter-clockwise seen from outside (outward normals), for volume-map boundaries."""
+    lo = np.asarray(box_min, dtype=np.float64)
+    hi = np.asarray(box_max, dtype=np.float64)
+    v = np.array([[hi[0] if i & 1 else lo[0], hi[1] if i & 2 else lo[1], hi[2] if i & 4 else lo[2]]
+                  for i in range(8)])
+    f = np.array([[0, 2, 3], [0, 3, 1], [4, 5, 7], [4, 7, 6], [0, 1, 5], [0, 5, 4],
+                  [2, 6, 7], [2, 7, 3], [0, 4, 6], [0, 6, 2], [1, 3, 7], [1, 7, 5]], dtype=np.uint32)
+    return v, f
+
+
 def sphere_surface(center, radius, spacing):
     """Fibonacci sampling of a sphere surface at roughly the given spacing."""
     area = 4.0 * math.pi * radius * radius

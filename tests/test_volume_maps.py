@@ -1,0 +1,209 @@
+"""Bender2019 volume-map boundaries (the reference's default boundary handling).
+
+CPU (oracle/vmap.c): the cubic serendipity grid reproduces linear fields exactly and its shape
+functions sum to one; the signed distance of a box mesh equals the analytic one; the volume
+saturates near 0.8 x the support ball; a resting column stays in a volume-mapped box with the
+average density error under the solver tolerance.
+
+GPU: the map the device builds (FP64) equals the oracle's node by node; one step from the same
+state matches the oracle (the parity bars of test_gpu_parity); a particle found inside a body is
+moved back as the oracle moves it; a resting column behaves as in the oracle; unsupported
+combinations are refused with their status codes.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from splishsplash_gb300 import native, scenes
+from splishsplash_gb300.dfsph import BatchedTimeStepDFSPH, TimeStepDFSPH
+
+from test_gpu_parity import compare, f32, relv
+
+BOX = (0.8, 1.0, 0.8)
+RES = (10, 12, 10)
+
+
+def box_sdf_inside(p, lo, hi):
+    """analytic distance to the box surface, positive inside"""
+    lo, hi = np.asarray(lo, float), np.asarray(hi, float)
+    d_in = np.minimum(p - lo, hi - p).min(axis=1)
+    d_out = np.linalg.norm(np.maximum(np.maximum(lo - p, p - hi), 0.0), axis=1)
+    inside = np.all((p >= lo) & (p <= hi), axis=1)
+    return np.where(inside, d_in, -d_out)
+
+
+def container_map(support, res=RES, box=BOX):
+    v, f = scenes.box_mesh((0, 0, 0), box)
+    return oracle.VolumeMap(res).build(v, f, support, invert=True)
+
+
+def vmap_scene(counts=(10, 10, 10), seed=7, velocity=None):
+    sc = scenes.small_block(counts=counts, box=BOX, seed=seed, velocity=velocity).as_float32()
+    sc.xb = np.zeros((0, 3))
+    return sc
+
+
+# --------------------------------------------------------------------- oracle
+def test_oracle_grid_interpolation_is_exact_for_linear_fields():
+    m = oracle.VolumeMap((3, 4, 5), dmin=(-1.0, -2.0, 0.0), dmax=(2.0, 2.0, 3.0))
+    p = m.node_positions()
+    a = np.array([0.3, -1.2, 0.7])
+    m.fields[0][:] = p @ a + 0.5
+    m.fields[1][:] = 1.0
+    rng = np.random.default_rng(0)
+    for x in rng.uniform((-1, -2, 0), (2, 2, 3), size=(50, 3)):
+        val, g = m.interpolate(0, x)
+        assert abs(val - (x @ a + 0.5)) < 1e-12
+        np.testing.assert_allclose(g, a, atol=1e-11)
+        one, g1 = m.interpolate(1, x)
+        assert abs(one - 1.0) < 1e-13 and np.abs(g1).max() < 1e-11
+    assert m.interpolate(0, np.array([2.5, 0.0, 0.0])) is None
+
+
+def test_oracle_box_map_distance_and_volume():
+    h = 0.1
+    m = container_map(h)
+    p = m.node_positions()
+    np.testing.assert_allclose(m.fields[0], box_sdf_inside(p, (0, 0, 0), BOX), atol=1e-12)
+    vol = m.fields[1]
+    ball = 0.8 * 4.0 / 3.0 * np.pi * h ** 3
+    assert np.all(vol >= 0.0) and abs(vol.max() / ball - 1.0) < 0.05
+    assert np.all(vol[m.fields[0] > 2 * h] == 0.0)
+    # a node a full support radius inside the wall sees the whole ball
+    deep = (m.fields[0] < -1.2 * h) & (m.fields[0] > -2.0 * h)
+    np.testing.assert_allclose(vol[deep], vol.max(), rtol=1e-9)
+
+
+def test_oracle_resting_column_in_a_volume_mapped_box():
+    sc = scenes.small_block(counts=(11, 6, 11), box=(0.6, 0.8, 0.6), corner=(0.05, 0.05, 0.05)).as_float32()
+    sc.xb = np.zeros((0, 3))
+    sim = oracle.OracleSim(sc)
+    sim.set_volume_maps([container_map(4 * sc.params.particleRadius, (12, 16, 12), (0.6, 0.8, 0.6))])
+    for _ in range(150):
+        sim.step()
+        assert sim.stats()["avg_density_err"] <= 0.01 * 0.01 * 1000.0 + 1e-12
+    assert sim.x.min() > 0.02 and np.all(sim.x.max(0) < np.array([0.58, 0.8, 0.58]))
+
+
+# --------------------------------------------------------------------- device
+def device_context(sc, precision="fp32", res=RES, use_graph=False):
+    ts = TimeStepDFSPH(sc, precision=precision, use_graph=use_graph)
+    v, f = scenes.box_mesh((0, 0, 0), BOX)
+    ts.ctx.add_volume_map(v, f, res, invert=True)
+    ts.ctx.set_boundary_method(2)
+    return ts
+
+
+@pytest.mark.gpu
+def test_device_map_matches_oracle():
+    sc = vmap_scene()
+    ts = device_context(sc)
+    res, lo, hi, dist, vol = ts.ctx.volume_map(0)
+    ref = container_map(4 * sc.params.particleRadius)
+    np.testing.assert_array_equal(res, RES)
+    np.testing.assert_allclose(lo, ref.m.dmin[:], atol=1e-15)
+    np.testing.assert_allclose(hi, ref.m.dmax[:], atol=1e-15)
+    assert np.abs(dist - ref.fields[0]).max() < 1e-12
+    assert np.abs(vol - ref.fields[1]).max() < 1e-12 * max(1.0, ref.fields[1].max() * 1e3)
+    ts.close()
+
+
+def oracle_with_map(sc, ts, state=None):
+    res, lo, hi, dist, vol = ts.ctx.volume_map(0)
+    m = oracle.VolumeMap(res).set_values(lo, hi, dist, vol)
+    sim = oracle.OracleSim(sc)
+    sim.set_volume_maps([m])
+    if state is not None:
+        sim.x[:] = state["x"]
+        sim.v[:] = state["v"]
+        sim.kappa[:] = state["kappa"]
+        sim.kappa_v[:] = state["kappa_v"]
+        sim.dt = state["dt"]
+    return sim
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol_scale", [("fp32", 1.0), ("fp64", 1e-4)])
+def test_step_matches_oracle(precision, tol_scale):
+    """FP64 bar 1e-4 of the FP32 one (velocity 1e-8): the map samples sum 32 products per field,
+    contracted to fused multiply-adds on the device and not in the oracle, and the solver
+    iterations carry those last-bit differences to about 5e-9 in the velocities."""
+    sc = vmap_scene(velocity=(0.3, -0.5, 0.2))
+    probe = device_context(sc)
+    pre = oracle_with_map(sc, probe)
+    probe.close()
+    for _ in range(40):    # a compressed state against the walls
+        pre.step()
+    state = dict(x=f32(pre.x), v=f32(pre.v), kappa=f32(pre.kappa), kappa_v=f32(pre.kappa_v), dt=pre.dt)
+    ts = device_context(sc, precision)
+    m = ts.getFluidModel()
+    m.setFieldBuffer("position", state["x"])
+    m.setFieldBuffer("velocity", state["v"])
+    m.setFieldBuffer("p / rho^2", state["kappa"])
+    m.setFieldBuffer("p_v / rho^2", state["kappa_v"])
+    ts.setTimeStepSize(state["dt"])
+    sim = oracle_with_map(sc, ts, state)
+    st = ts.step()
+    sim.step()
+    assert st["max_boundary_neighbors"] == 0
+    assert sim.stats()["iterations"] >= 2
+    compare(ts, sim, st, tol_scale=tol_scale)
+    ts.close()
+
+
+@pytest.mark.gpu
+def test_particle_inside_a_body_is_moved_back_like_the_oracle():
+    sc = vmap_scene(counts=(6, 6, 6))
+    sc.x = np.concatenate([sc.x, [[-0.004, 0.5, 0.4]]])    # inside the wall, far from the fluid
+    sc.v = np.concatenate([sc.v, [[-1.0, 0.0, 0.0]]])
+    ts = device_context(sc, "fp64")
+    sim = oracle_with_map(sc, ts)
+    ts.step()
+    sim.step()
+    x = ts.getFluidModel().getFieldBuffer("position")
+    assert np.abs(x[-1] - sim.x[-1]).max() < 1e-12
+    assert x[-1, 0] > -0.004                                  # moved toward the fluid side
+    ts.close()
+
+
+@pytest.mark.gpu
+def test_resting_column_in_a_volume_mapped_box():
+    sc = scenes.small_block(counts=(11, 6, 11), box=(0.6, 0.8, 0.6), corner=(0.05, 0.05, 0.05)).as_float32()
+    sc.xb = np.zeros((0, 3))
+    ts = TimeStepDFSPH(sc, use_graph=True)
+    v, f = scenes.box_mesh((0, 0, 0), (0.6, 0.8, 0.6))
+    ts.ctx.add_volume_map(v, f, (12, 16, 12), invert=True)
+    ts.ctx.set_boundary_method(2)
+    for _ in range(150):
+        st = ts.step()
+        assert st["avg_density_err"] <= 0.01 * 0.01 * 1000.0 + 1e-9
+    x = ts.getFluidModel().getFieldBuffer("position")
+    assert x.min() > 0.02 and np.all(x.max(0) < np.array([0.58, 0.8, 0.58]))
+    ts.close()
+
+
+@pytest.mark.gpu
+def test_unsupported_combinations_are_refused():
+    def code(fn):
+        with pytest.raises(native.SphgbError) as e:
+            fn()
+        return native.ERR_NAMES[e.value.code]
+
+    sc = vmap_scene(counts=(6, 6, 6))
+    ts = TimeStepDFSPH(sc, use_graph=False)
+    ts.ctx.set_boundary_method(2)
+    assert code(ts.step) == "STATE"                           # no map
+    v, f = scenes.box_mesh((0, 0, 0), BOX)
+    ts.ctx.add_volume_map(v, f, RES, invert=True)
+    ts.ctx.upload_boundary(scenes.small_block(counts=(2, 2, 2)).xb)
+    assert code(ts.step) == "STATE"                           # boundary particles as well
+    ts.ctx.upload_boundary(np.zeros((0, 3)))
+    p = sc.params
+    p.viscosityMethod, p.viscosityBoundary = 6, 0.1
+    ts.ctx.set_params(p)
+    assert code(ts.step) == "ARGUMENT"                        # boundary viscosity
+    p.viscosityBoundary = 0.0
+    p.particleRadius = 0.02
+    ts.ctx.set_params(p)
+    assert code(ts.step) == "STATE"                           # map built for another radius
+    ts.close()
