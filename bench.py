@@ -280,6 +280,51 @@ def learned_line(steps):
             "network": "splishsplash_gb300/data/warmstart_mlp.npz (python -m splishsplash_gb300.learned)"}
 
 
+def bender2019_line(steps, device):
+    """The 1M dam break with its 6x3x3 m container given as a Bender2019 volume map (the
+    reference's default boundary handling) instead of 625,002 boundary particles: map
+    construction time and particle-steps/s over `steps` steps after 10 warm-up steps."""
+    import torch
+
+    from splishsplash_gb300 import native, scenes
+    from splishsplash_gb300.dfsph import TimeStepDFSPH
+
+    sc = scenes.dambreak_1m()
+    sc.xb = np.zeros((0, 3))
+    h = 4 * sc.params.particleRadius
+    # cells of about 2 h over the map box (the container grown by 8 h on every side)
+    ext = np.array([6.0, 3.0, 3.0]) + 16 * h
+    res = np.maximum(1, np.round(ext / (2 * h))).astype(np.uint32)
+    ts = TimeStepDFSPH(sc, use_graph=True, device=device)
+    v, f = scenes.box_mesh((0, 0, 0), (6.0, 3.0, 3.0))
+    t0 = time.perf_counter()
+    ts.ctx.add_volume_map(v, f, res, invert=True)
+    build_s = time.perf_counter() - t0
+    ts.ctx.set_boundary_method(2)
+    for _ in range(10):
+        ts.step()
+    ext_s = torch.cuda.ExternalStream(ts.ctx.stream())
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    its = []
+    torch.cuda.synchronize()
+    for k in range(steps):
+        with torch.cuda.stream(ext_s):
+            evs[k][0].record(ext_s)
+        st = ts.step()
+        with torch.cuda.stream(ext_s):
+            evs[k][1].record(ext_s)
+        its.append((st["iterations"], st["iterations_v"]))
+    torch.cuda.synchronize()
+    dev_s = sum(a.elapsed_time(b) for a, b in evs) / 1e3
+    ts.close()
+    it = np.array(its)
+    return {"workload": f"dambreak_1m fluid ({sc.n} particles) in a volume-mapped 6x3x3 m box, map {res.tolist()} cells",
+            "value": sc.n * steps / dev_s, "unit": UNIT, "steps": steps, "warmup": 10,
+            "ms_per_step": 1e3 * dev_s / steps, "map_build_s": build_s,
+            "map_nodes": int(native.Context.volume_map_nodes(res)),
+            "iterations_mean": {"pressure": float(it[:, 0].mean()), "divergence": float(it[:, 1].mean())}}
+
+
 def ensemble_line(steps, device):
     """256 independent dam breaks (N_i log-uniform in [2000, 60000]) in one batched context:
     particle-steps/s over `steps` steps after 10 warm-up steps (inputs far larger than L2)."""
@@ -341,6 +386,8 @@ def main():
                     help="print configs 0 and 3 (GPU and host cores) as one JSON line and exit")
     ap.add_argument("--learned-steps", type=int, default=300)
     ap.add_argument("--ensemble-steps", type=int, default=60)
+    ap.add_argument("--bender-steps", type=int, default=60)
+    ap.add_argument("--only-bender", action="store_true", help="print the volume-map boundary line alone and exit")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -349,6 +396,9 @@ def main():
         return
     if args.config_table:
         print(json.dumps({"config_table": config_table(args)}), flush=True)
+        return
+    if args.only_bender:
+        print(json.dumps({"boundary_bender2019": bender2019_line(args.bender_steps, 0)}), flush=True)
         return
 
     import torch
@@ -503,6 +553,7 @@ def main():
     if rank == 0 and world == 1 and not args.no_extras:
         extras["learned_warmstart"] = learned_line(args.learned_steps)
         extras["ensemble"] = ensemble_line(args.ensemble_steps, local)
+        extras["boundary_bender2019"] = bender2019_line(args.bender_steps, local)
 
     if rank == 0:
         it = np.array(iters)
