@@ -109,6 +109,16 @@ TimeStepDFSPH_GB300::TimeStepDFSPH_GB300(FluidModel &model, const std::vector<Bo
     createContext(device, useGraph);
 }
 
+TimeStepDFSPH_GB300::TimeStepDFSPH_GB300(FluidModel &model, const std::vector<BoundaryModel_Bender2019 *> &volumeMaps,
+                                         const SimulationParameters &sim, Viscosity_Weiler2018_GB300 *viscosity,
+                                         int device, bool useGraph)
+    : m_model(model), m_volumeMaps(volumeMaps), m_sim(sim), m_visco(viscosity)
+{
+    for (BoundaryModel_Bender2019 *b : m_volumeMaps)
+        if (!b) throw Error(SPHGB_ERR_ARGUMENT, "null boundary model");
+    createContext(device, useGraph);
+}
+
 void TimeStepDFSPH_GB300::createContext(int device, bool useGraph)
 {
     for (unsigned int k = 0; k < m_boundaries.size(); k++) {
@@ -228,6 +238,24 @@ void TimeStepDFSPH_GB300::upload()
 {
     const unsigned int n = m_model.numParticles();
     if (m_factor.size() != n) resize();
+    if (m_boundaryDirty && !m_volumeMaps.empty()) {
+        // Bender2019: no boundary particles; one map per body, built for the current parameters
+        check(sphgb_upload_boundary(m_ctx, nullptr, 0), "sphgb_upload_boundary");
+        check(sphgb_clear_volume_maps(m_ctx), "sphgb_clear_volume_maps");
+        for (BoundaryModel_Bender2019 *bm : m_volumeMaps) {
+            const std::vector<double> v = to_double(bm->m_vertices);
+            double R[9], t[3];
+            for (int k = 0; k < 9; k++) R[k] = (double)bm->m_rotation[k];
+            for (int k = 0; k < 3; k++) t[k] = (double)bm->m_rigidBody.getPosition()[k];
+            uint32_t body;
+            check(sphgb_add_volume_map(m_ctx, v.data(), (uint32_t)bm->m_vertices.size(), bm->m_faces.data(),
+                                       (uint32_t)(bm->m_faces.size() / 3), bm->m_mapResolution, (double)bm->m_mapThickness,
+                                       bm->m_mapInvert ? 1 : 0, R, t, 0, &body),
+                  "sphgb_add_volume_map");
+        }
+        check(sphgb_set_boundary_method(m_ctx, 2), "sphgb_set_boundary_method");
+        m_boundaryDirty = false;
+    }
     if (m_boundaryDirty) {
         // the boundary models' particles in model order; model k is body k
         std::vector<double> xb, center;

@@ -9,6 +9,7 @@
 //   FluidModel field layout    SPlisHSPlasH/FluidModel.h:113-124, 247-300
 //   Akinci2012 boundary        SPlisHSPlasH/BoundaryModel_Akinci2012.h:32-35
 //   forces on boundary bodies  SPlisHSPlasH/BoundaryModel.h:38-49, 86-87; RigidBodyObject.h
+//   Bender2019 volume maps     SPlisHSPlasH/BoundaryModel_Bender2019.h, SimulatorBase.cpp:2512-2660
 //   Weiler2018 viscosity       SPlisHSPlasH/Viscosity/Viscosity_Weiler2018.h:44-48, .cpp:33,47-73
 //   time step size             SPlisHSPlasH/TimeManager.h
 // The host vectors are the system of record, as in the reference: step() uploads them when
@@ -161,6 +162,26 @@ public:
     Vector3r &getVDiff(unsigned int i) { return m_vDiff[i]; }
 };
 
+// Static body given as a volume map (BoundaryModel_Bender2019, the reference's default boundary
+// handling): its closed triangle mesh in body coordinates and the scene's map parameters
+// ("mapResolution", "mapThickness", "mapInvert"); the map itself is built on the GPU.
+class BoundaryModel_Bender2019 {
+public:
+    std::vector<Vector3r> m_vertices;
+    std::vector<unsigned int> m_faces;   // 3 per triangle
+    unsigned int m_mapResolution[3] = {20, 20, 20};
+    Real m_mapThickness = 0;
+    bool m_mapInvert = false;
+    Real m_rotation[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};   // body rotation (row-major)
+    RigidBodyObject m_rigidBody;                         // position: the body's translation
+    void initModel(unsigned int nVertices, const Vector3r *vertices, unsigned int nFaces, const unsigned int *faces)
+    {
+        m_vertices.assign(vertices, vertices + nVertices);
+        m_faces.assign(faces, faces + 3 * (size_t)nFaces);
+    }
+    RigidBodyObject *getRigidBodyObject() { return &m_rigidBody; }
+};
+
 // The DFSPH time step on the GPU (TimeStepDFSPH.cpp:117-249)
 class TimeStepDFSPH_GB300 : public TimeStep {
 public:
@@ -179,6 +200,10 @@ public:
                         Viscosity_Weiler2018_GB300 *viscosity = nullptr, int device = 0, bool useGraph = true);
     // one boundary model per rigid body (Simulation::numberOfBoundaryModels)
     TimeStepDFSPH_GB300(FluidModel &model, const std::vector<BoundaryModel_Akinci2012 *> &boundaries,
+                        const SimulationParameters &sim, Viscosity_Weiler2018_GB300 *viscosity = nullptr,
+                        int device = 0, bool useGraph = true);
+    // Bender2019 boundary ("boundaryHandlingMethod" 2): one volume map per static body
+    TimeStepDFSPH_GB300(FluidModel &model, const std::vector<BoundaryModel_Bender2019 *> &volumeMaps,
                         const SimulationParameters &sim, Viscosity_Weiler2018_GB300 *viscosity = nullptr,
                         int device = 0, bool useGraph = true);
     ~TimeStepDFSPH_GB300() override;
@@ -231,6 +256,7 @@ protected:
 
     FluidModel &m_model;
     std::vector<BoundaryModel_Akinci2012 *> m_boundaries;
+    std::vector<BoundaryModel_Bender2019 *> m_volumeMaps;
     bool m_bodiesSet = false;
     SimulationParameters m_sim;
     Viscosity_Weiler2018_GB300 *m_visco;

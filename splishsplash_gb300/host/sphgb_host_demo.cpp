@@ -5,15 +5,17 @@
 //   sphgb_host_demo <scene.bin> <out.bin>
 //
 // scene.bin (little endian): uint32 n, nb, steps, lanes (0 = autotune), viscosity (0/1),
-// bodies (0/1); float64 particle radius; float64 x[n][3], v[n][3], xb[nb][3]; with bodies:
-// uint32 body[nb] (0: the dynamic body, 1: static walls) and float64 position[3] of the
-// dynamic body.
+// bodies (0/1), volume map (0/1); float64 particle radius; float64 x[n][3], v[n][3], xb[nb][3];
+// with bodies: uint32 body[nb] (0: the dynamic body, 1: static walls) and float64 position[3]
+// of the dynamic body; with a volume map (then nb = 0): uint32 nv, nf, resolution[3], invert,
+// float64 vertices[nv][3], uint32 faces[nf][3] of the container (Bender2019 boundary).
 // out.bin: per step uint32 iterations, iterationsV, viscoIterations and float64 time;
 // then float64 x[n][3], v[n][3], density[n], p / rho^2 [n], boundary volume[nb] (in the
 // order of the boundary models: body 0's particles first), force[3], torque[3] of body 0
 // summed over all steps (getForceAndTorque; zeros without bodies).
 #include <cstdint>
 #include <cstdio>
+#include <memory>
 #include <vector>
 
 #include "sphgb_host.h"
@@ -42,15 +44,25 @@ int main(int argc, char **argv)
     }
     FILE *f = fopen(argv[1], "rb");
     if (!f) return 2;
-    uint32_t hdr[6];
+    uint32_t hdr[7];
     double radius;
-    if (!rd(f, hdr, 6) || !rd(f, &radius, 1)) return 2;
-    const uint32_t n = hdr[0], nb = hdr[1], steps = hdr[2], lanes = hdr[3], visc = hdr[4], bodies = hdr[5];
+    if (!rd(f, hdr, 7) || !rd(f, &radius, 1)) return 2;
+    const uint32_t n = hdr[0], nb = hdr[1], steps = hdr[2], lanes = hdr[3], visc = hdr[4], bodies = hdr[5],
+                   vmap = hdr[6];
     std::vector<double> x(3 * (size_t)n), v(3 * (size_t)n), xb(3 * (size_t)nb);
     if (!rd(f, x.data(), x.size()) || !rd(f, v.data(), v.size()) || !rd(f, xb.data(), xb.size())) return 2;
     std::vector<uint32_t> body(nb, 1u);
     double pos[3] = {0, 0, 0};
     if (bodies && (!rd(f, body.data(), body.size()) || !rd(f, pos, 3))) return 2;
+    uint32_t mh[6] = {0, 0, 0, 0, 0, 0};
+    std::vector<double> mv;
+    std::vector<uint32_t> mf;
+    if (vmap) {
+        if (!rd(f, mh, 6)) return 2;
+        mv.resize(3 * (size_t)mh[0]);
+        mf.resize(3 * (size_t)mh[1]);
+        if (!rd(f, mv.data(), mv.size()) || !rd(f, mf.data(), mf.size())) return 2;
+    }
     fclose(f);
 
     try {
@@ -75,7 +87,19 @@ int main(int argc, char **argv)
         models[0].getRigidBodyObject()->setDynamic(bodies != 0);
         Viscosity_Weiler2018_GB300 viscosity;
         viscosity.m_maxError = Real(1e-3);
-        TimeStepDFSPH_GB300 ts(model, boundaries, sp, visc ? &viscosity : nullptr);
+        // Bender2019: the container as a volume map instead of boundary particles
+        BoundaryModel_Bender2019 container;
+        if (vmap) {
+            const std::vector<Vector3r> mvv = to_vec(mv);
+            container.initModel(mh[0], mvv.data(), mh[1], mf.data());
+            for (int k = 0; k < 3; k++) container.m_mapResolution[k] = mh[2 + k];
+            container.m_mapInvert = mh[5] != 0;
+        }
+        std::unique_ptr<TimeStepDFSPH_GB300> tsp(
+            vmap ? new TimeStepDFSPH_GB300(model, std::vector<BoundaryModel_Bender2019 *>{&container}, sp,
+                                           visc ? &viscosity : nullptr)
+                 : new TimeStepDFSPH_GB300(model, boundaries, sp, visc ? &viscosity : nullptr));
+        TimeStepDFSPH_GB300 &ts = *tsp;
         sphgb_set_lanes_per_particle(ts.context(), lanes);
         ts.resize();
 

@@ -15,15 +15,21 @@ from splishsplash_gb300 import build, scenes
 from splishsplash_gb300.dfsph import TimeStepDFSPH
 
 
-def _write_scene(path, sc, steps, lanes, visc, body=None, position=None):
+def _write_scene(path, sc, steps, lanes, visc, body=None, position=None, vmap=None):
     with open(path, "wb") as f:
-        f.write(struct.pack("<6I", sc.n, sc.nb, steps, lanes, 1 if visc else 0, 0 if body is None else 1))
+        f.write(struct.pack("<7I", sc.n, sc.nb, steps, lanes, 1 if visc else 0, 0 if body is None else 1,
+                            0 if vmap is None else 1))
         f.write(struct.pack("<d", sc.params.particleRadius))
         for a in (sc.x, sc.v, sc.xb):
             f.write(np.ascontiguousarray(a, "<f8").tobytes())
         if body is not None:
             f.write(np.ascontiguousarray(body, "<u4").tobytes())
             f.write(np.ascontiguousarray(position, "<f8").tobytes())
+        if vmap is not None:
+            verts, faces, res = vmap
+            f.write(struct.pack("<6I", len(verts), len(faces), *[int(r) for r in res], 1))
+            f.write(np.ascontiguousarray(verts, "<f8").tobytes())
+            f.write(np.ascontiguousarray(faces, "<u4").tobytes())
 
 
 def _read_out(path, n, nb, steps):
@@ -61,8 +67,9 @@ def test_host_layer_is_built_and_fails_cleanly_without_a_device():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("visc,bodies", [(False, False), (True, False), (True, True)])
-def test_cpp_host_layer_matches_python_mirror(visc, bodies):
+@pytest.mark.parametrize("visc,bodies,vmap", [(False, False, False), (True, False, False), (True, True, False),
+                                              (True, False, True)])
+def test_cpp_host_layer_matches_python_mirror(visc, bodies, vmap):
     sc = scenes.small_block(counts=(10, 12, 10), box=(0.8, 1.0, 0.8), viscosity=visc,
                             velocity=(0.3, 0.0, -0.2)).as_float32()
     # the C++ layer holds every real parameter in Real (float), like the reference's FP32 build
@@ -79,8 +86,14 @@ def test_cpp_host_layer_matches_python_mirror(visc, bodies):
         # the floor is a dynamic body (boundary model 0), the other walls are static (model 1)
         body = np.where(sc.xb[:, 1] < 1e-9, 0, 1).astype(np.uint32)
         position = np.array([0.375, 0.0, 0.4375], np.float64)   # exact in float (the C++ layer holds Real)
+    mesh = None
+    if vmap:
+        # the container as a Bender2019 volume map instead of boundary particles
+        sc = dataclasses.replace(sc, xb=np.zeros((0, 3)))
+        verts, faces = scenes.box_mesh((0, 0, 0), (0.75, 1.0, 0.75))   # exact in float (the C++ Real)
+        mesh = (verts, faces, (8, 10, 8))
     with tempfile.TemporaryDirectory() as d:
-        _write_scene(os.path.join(d, "s.bin"), sc, steps, lanes, visc, body, position)
+        _write_scene(os.path.join(d, "s.bin"), sc, steps, lanes, visc, body, position, mesh)
         r = subprocess.run([build.HOST_DEMO, os.path.join(d, "s.bin"), os.path.join(d, "o.bin")],
                            capture_output=True, text=True, timeout=300)
         assert r.returncode == 0, r.stderr
@@ -92,6 +105,9 @@ def test_cpp_host_layer_matches_python_mirror(visc, bodies):
         sc = dataclasses.replace(sc, xb=sc.xb[order])
     ts = TimeStepDFSPH(sc)
     ts.ctx.set_lanes_per_particle(lanes)
+    if vmap:
+        ts.ctx.add_volume_map(mesh[0], mesh[1], mesh[2], invert=True)
+        ts.ctx.set_boundary_method(2)
     if bodies:
         ts.ctx.set_boundary_bodies(np.sort(body), np.stack([position, np.zeros(3)]), [1, 0])
     for k in range(steps):
