@@ -321,7 +321,9 @@ int sphgb_get_neighbor_staging(sphgb_ctx *ctx, int *active, float *staged_fracti
  * sum f and torque sum (x_b - center) x f, summed in FP64 in a fixed order (deterministic).
  * The boundary stays static (v_b = 0); moving a body is the caller's rigid-body solver, which
  * re-uploads the boundary.  Setting the bodies (nbodies == 0 removes them) zeroes the
- * accumulators; uploading a boundary of another particle count removes them. */
+ * accumulators; uploading a boundary of another particle count removes them.  With volume maps
+ * (sphgb_set_boundary_method 2) body b is map b, body may be NULL, and the forces of the same
+ * terms act at the particles' boundary points x_j (TimeStepDFSPH.cpp:1355-1364, XSPH.cpp:196-204). */
 int sphgb_set_boundary_bodies(sphgb_ctx *ctx, const uint32_t *body, uint32_t nbodies, const double *center,
                               const int *dynamic);
 /* the sums since the last clear, force[3 nbodies] and torque[3 nbodies] (either may be NULL;
@@ -339,8 +341,9 @@ int sphgb_clear_boundary_forces(sphgb_ctx *ctx, int32_t body);
  * 0 < phi < 4 r, as one boundary particle per body in all DFSPH, XSPH sums
  * (TimeStep::computeVolumeAndBoundaryX, TimeStep.cpp:219-340); a particle found inside a body
  * is moved back by min(2 r - phi, r / 10) and stopped, as in the reference.  Supported: one
- * scene, static bodies, no boundary particles uploaded, no boundary viscosity, no force
- * feedback (other combinations fail at the step with SPHGB_ERR_STATE / SPHGB_ERR_ARGUMENT).
+ * scene, static bodies, no boundary particles uploaded, no boundary viscosity; force feedback
+ * with one body per map (sphgb_set_boundary_bodies); other combinations fail at the step with
+ * SPHGB_ERR_STATE / SPHGB_ERR_ARGUMENT.
  *
  * sphgb_add_volume_map builds a map on the GPU in FP64 from a closed triangle mesh in body
  * coordinates, as SimulatorBase::initVolumeMap does (SimulatorBase.cpp:2512-2660): box = mesh box

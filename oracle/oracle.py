@@ -280,7 +280,7 @@ class OracleSim:
     def set_bodies(self, body, center, dynamic=None):
         """Bodies of the boundary particles (upload order), reference points and dynamic flags;
         forces accumulate in body_force / body_torque until clear_forces()."""
-        self.body = np.ascontiguousarray(body, np.uint32)
+        self.body = None if body is None else np.ascontiguousarray(body, np.uint32)   # None: map b is body b
         self.body_center = np.ascontiguousarray(center, np.float64).reshape(-1, 3)
         nbodies = self.body_center.shape[0]
         self.body_dynamic = np.ones(nbodies, np.int32) if dynamic is None else np.ascontiguousarray(dynamic, np.int32)

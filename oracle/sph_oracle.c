@@ -444,16 +444,25 @@ static void pressure_accel(ctx_t *c, const real *kap)
     }
 }
 
+/* Forces are collected when body_force is given and, for boundary particles, their bodies; with
+ * volume maps the boundary "neighbour" j = i * nbodies + b belongs to map b. */
+static inline int collects_forces(const orc_state *s, int vmaps)
+{
+    return s->body_force && (vmaps || s->body);
+}
+
 /* BoundaryModel::addForce (BoundaryModel.h:38-49): force f at x_b on the body of boundary
  * particle j, torque (x_b - c) x f; only dynamic bodies collect.  Serial (deterministic). */
-static void add_force(orc_state *s, unsigned j, const double f[3])
+static void add_force(const ctx_t *c, unsigned j, const double f[3])
 {
-    if (!s->body || !s->body_force) return;
-    const unsigned b = s->body[j];
+    orc_state *s = c->s;
+    const int vmaps = c->p->boundary_method == 2;
+    if (!collects_forces(s, vmaps)) return;
+    const unsigned b = vmaps ? j % s->nvmaps : s->body[j];
     if (b >= s->nbodies || (s->body_dynamic && !s->body_dynamic[b])) return;
-    const double *c = s->body_center + 3 * (size_t)b;
-    const double r[3] = {(double)s->xb[3 * (size_t)j] - c[0], (double)s->xb[3 * (size_t)j + 1] - c[1],
-                         (double)s->xb[3 * (size_t)j + 2] - c[2]};
+    const double *cen = s->body_center + 3 * (size_t)b;
+    const double r[3] = {(double)s->xb[3 * (size_t)j] - cen[0], (double)s->xb[3 * (size_t)j + 1] - cen[1],
+                         (double)s->xb[3 * (size_t)j + 2] - cen[2]};
     double *F = s->body_force + 3 * (size_t)b, *T = s->body_torque + 3 * (size_t)b;
     F[0] += f[0]; F[1] += f[1]; F[2] += f[2];
     T[0] += r[1] * f[2] - r[2] * f[1];
@@ -466,7 +475,7 @@ static void add_force(orc_state *s, unsigned j, const double f[3])
 static void boundary_pressure_forces(ctx_t *c, const real *kap)
 {
     orc_state *s = c->s;
-    if (!s->body || !s->body_force) return;
+    if (!collects_forces(s, c->p->boundary_method == 2)) return;
     for (long i = 0; i < (long)s->n; i++) {
         const double pi = (double)kap[i];
         if (!(fabs(pi) > c->eps)) continue;
@@ -477,7 +486,7 @@ static void boundary_pressure_forces(ctx_t *c, const real *kap)
             kGradW(&c->K, r, g);
             const double Vj = (double)s->Vb[j];
             for (int d = 0; d < 3; d++) f[d] = -c->mass * (pi * (-Vj * g[d]));
-            add_force(s, j, f);
+            add_force(c, j, f);
         }
     }
 }
@@ -654,7 +663,7 @@ static void xsph(ctx_t *c, double h)
         for (int d = 0; d < 3; d++) s->a[3 * i + d] = (real)((double)s->a[3 * i + d] + ai[d]);
     }
     /* boundary feedback of the XSPH boundary term (XSPH.cpp:183-203): force -m_i a_ib */
-    if (cb != 0.0 && s->body && s->body_force)
+    if (cb != 0.0 && collects_forces(s, c->p->boundary_method == 2))
         for (long i = 0; i < (long)s->n; i++) {
             const real *xi = s->x + 3 * i, *vi = s->v + 3 * i;
             const double rhoi = (double)s->density[i];
@@ -664,7 +673,7 @@ static void xsph(ctx_t *c, double h)
                 diffv(xi, s->xb + 3 * (size_t)j, r);
                 const double w = invH * cb * (c->rho0 * (double)s->Vb[j] / rhoi) * kW(&c->K, sqrt(dot3(r, r)));
                 for (int d = 0; d < 3; d++) f[d] = -c->mass * (-w * (double)vi[d]);
-                add_force(s, j, f);
+                add_force(c, j, f);
             }
         }
 }
@@ -908,7 +917,7 @@ static int viscosity_weiler(ctx_t *c, double dt)
                 kGradW(&c->K, r, g);
                 const double coef = 10.0 * mub * (c->rho0 * (double)s->Vb[j] / rhoi) * dot3(nv, r) / (dot3(r, r) + 0.01 * h2);
                 for (int d = 0; d < 3; d++) f[d] = -c->mass / rhoi * (coef * g[d]);
-                add_force(s, j, f);
+                add_force(c, j, f);
             }
         }
     }
@@ -1034,7 +1043,7 @@ int orc_step(orc_state *s, const orc_params *p)
 
     /* Bender2019: static bodies without force feedback or boundary viscosity */
     const int vmaps = p->boundary_method == 2;
-    if (vmaps && ((s->body && s->body_force) || (p->viscosity_method == 6 && p->viscosity_boundary != 0.0)))
+    if (vmaps && (s->body || (p->viscosity_method == 6 && p->viscosity_boundary != 0.0)))
         return -5;
     real *xb_saved = s->xb, *Vb_saved = s->Vb, *vxb = NULL, *vVb = NULL;
     const unsigned nb_saved = s->nb;

@@ -99,7 +99,9 @@ typedef struct orc_state {
     const double *body_center;            /* 3 nbodies */
     const int *body_dynamic;              /* nbodies */
     double *body_force, *body_torque;     /* 3 nbodies */
-    /* Bender2019 boundary (boundary_method 2): one volume map per body */
+    /* Bender2019 boundary (boundary_method 2): one volume map per body.  With body == NULL and
+     * body_force given, map b is body b (centres, dynamic flags and sums as above), its force
+     * applied at the particle's boundary point x_j (addForce(xj, ...) of the Bender2019 branches). */
     const orc_vmap *vmaps;
     unsigned nvmaps;
 } orc_state;

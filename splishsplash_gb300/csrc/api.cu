@@ -269,6 +269,7 @@ void free_prepared(sphgb_ctx *c)
     c->bodies.body_nblk = nullptr;
     c->bodies.partials = nullptr;
     c->bodies.nblk = 0;
+    c->bodies.vpartials = nullptr;
     c->bx = nullptr;
     c->prepared = false;
 }
@@ -660,8 +661,13 @@ template <class T> int prepare(sphgb_ctx *c)
             if (p) dfree(c->prep_allocs, p);
     }
     if ((rc = build_body_tables(c))) return rc;
-    if (c->boundary_method == 2 && !c->vmaps.empty())
+    if (c->boundary_method == 2 && !c->vmaps.empty()) {
         if ((rc = palloc(c, &c->bx, (size_t)std::max(c->np, 1u) * c->vmaps.size() * vec_size(c)))) return rc;
+        if (c->nbodies) {   // block partials of the volume-map body forces
+            const size_t nblk = (std::max(c->np, 1u) + kBlock - 1) / kBlock;
+            if ((rc = palloc(c, &c->bodies.vpartials, (size_t)c->nbodies * 6 * nblk * sizeof(double)))) return rc;
+        }
+    }
     c->prepared = true;
     return SPHGB_OK;
 }
@@ -708,7 +714,8 @@ int read_cont(sphgb_ctx *c, unsigned *cont)
 // the XSPH boundary term or the Weiler2018 boundary term.
 template <class T> bool body_phase0(const sphgb_ctx *c, const DevParams<T> &P)
 {
-    return c->bodies.nblk && (P.div_on || P.xsph_b != T(0) || (P.visc_on && P.mub != T(0)));
+    const bool bodies = c->bodies.nblk || (P.nvmaps && c->bodies.nbodies && c->bodies.vpartials);
+    return bodies && (P.div_on || P.xsph_b != T(0) || (P.visc_on && P.mub != T(0)));
 }
 
 // Enqueue the launches that precede the solver loops.
@@ -783,11 +790,19 @@ template <class T> int step_host_loop(sphgb_ctx *c)
             { PROF(K_CG_P, s); launch_cg_p<T>(P, B1, s); }
         }
     }
-    if (body_phase0(c, P)) { PROF(K_BODY_FORCES, s); launch_body_forces<T>(P, B1, c->bodies, 0, s); }
+    if (body_phase0(c, P)) {
+        PROF(K_BODY_FORCES, s);
+        launch_body_forces<T>(P, B1, c->bodies, 0, s);
+        launch_vmap_forces<T>(P, B1, c->bodies, 0, s);
+    }
     { PROF(K_KICK, s); launch_kick<T>(P, B1, s); }
     { PROF(K_PRESS_INIT, s); launch_press_init<T>(P, B1, s); }
     if ((rc = solve(false))) return rc;
-    { PROF(K_BODY_FORCES, s); launch_body_forces<T>(P, B1, c->bodies, 1, s); }
+    {
+        PROF(K_BODY_FORCES, s);
+        launch_body_forces<T>(P, B1, c->bodies, 1, s);
+        launch_vmap_forces<T>(P, B1, c->bodies, 1, s);
+    }
     { PROF(K_INTEGRATE, s); launch_integrate<T>(P, B1, s); }
     CK(cudaGetLastError());
     prof_resolve(c);
@@ -884,11 +899,15 @@ template <class T> int build_graph(sphgb_ctx *c, int parity, cudaGraphExec_t *ou
             });
         }
     }
-    if (body_phase0(c, P)) launch_body_forces<T>(P, B1, c->bodies, 0, s);
+    if (body_phase0(c, P)) {
+        launch_body_forces<T>(P, B1, c->bodies, 0, s);
+        launch_vmap_forces<T>(P, B1, c->bodies, 0, s);
+    }
     launch_kick<T>(P, B1, s);
     launch_press_init<T>(P, B1, s);
     solve(false);
     launch_body_forces<T>(P, B1, c->bodies, 1, s);
+    launch_vmap_forces<T>(P, B1, c->bodies, 1, s);
     launch_integrate<T>(P, B1, s);
     cudaGraph_t done = nullptr;
     cudaError_t e2 = cudaStreamEndCapture(s, &done);
@@ -973,7 +992,8 @@ int check_boundary_method(sphgb_ctx *c)
     if (c->vmaps.empty()) return fail(c, SPHGB_ERR_STATE, "Bender2019 boundary without volume maps");
     if (c->scn.size() > 1) return fail(c, SPHGB_ERR_STATE, "volume maps serve a single scene, not a batch");
     if (c->nb) return fail(c, SPHGB_ERR_STATE, "the Bender2019 boundary takes no boundary particles");
-    if (c->nbodies) return fail(c, SPHGB_ERR_ARGUMENT, "force feedback is not available for volume maps");
+    if (c->nbodies && c->nbodies != c->vmaps.size())
+        return fail(c, SPHGB_ERR_ARGUMENT, "with volume maps the bodies are the maps: one body per map");
     if (c->prm.viscosity_method == 6 && c->prm.viscosity_boundary != 0.0)
         return fail(c, SPHGB_ERR_ARGUMENT, "boundary viscosity is not available for volume maps");
     for (const auto &m : c->vmaps)
@@ -1734,7 +1754,7 @@ int sphgb_set_boundary_bodies(sphgb_ctx *c, const uint32_t *body, uint32_t nbodi
                               const int *dynamic)
 {
     if (!c) return SPHGB_ERR_ARGUMENT;
-    if (nbodies && (!body || !center)) return SPHGB_ERR_ARGUMENT;
+    if (nbodies && ((!body && c->nb) || !center)) return SPHGB_ERR_ARGUMENT;
     if (nbodies && !c->have_boundary) return fail(c, SPHGB_ERR_STATE, "no boundary uploaded");
     for (uint32_t k = 0; nbodies && k < c->nb; k++)
         if (body[k] >= nbodies) return fail(c, SPHGB_ERR_ARGUMENT, "body index out of range");
@@ -1745,7 +1765,7 @@ int sphgb_set_boundary_bodies(sphgb_ctx *c, const uint32_t *body, uint32_t nbodi
     free_bodies(c);
     invalidate_graphs(c);
     if (nbodies == 0) return SPHGB_OK;
-    c->body_of.assign(body, body + c->nb);
+    c->body_of.assign(body, body + (body ? c->nb : 0u));
     c->body_center.assign(center, center + 3 * (size_t)nbodies);
     c->body_dynamic.assign(nbodies, 1);
     if (dynamic)
@@ -1753,18 +1773,24 @@ int sphgb_set_boundary_bodies(sphgb_ctx *c, const uint32_t *body, uint32_t nbodi
     c->nbodies = nbodies;
     double *acc, *cen;
     unsigned *cnt;
+    int *dyn;
     if ((rc = dalloc_into(c, c->body_allocs, &acc, 6 * (size_t)nbodies * sizeof(double))) ||
         (rc = dalloc_into(c, c->body_allocs, &cen, 3 * (size_t)nbodies * sizeof(double))) ||
-        (rc = dalloc_into(c, c->body_allocs, &cnt, (size_t)nbodies * sizeof(unsigned)))) {
+        (rc = dalloc_into(c, c->body_allocs, &cnt, (size_t)nbodies * sizeof(unsigned))) ||
+        (rc = dalloc_into(c, c->body_allocs, &dyn, (size_t)nbodies * sizeof(int)))) {
         free_bodies(c);
         return rc;
     }
     CK(cudaMemset(acc, 0, 6 * (size_t)nbodies * sizeof(double)));
     CK(cudaMemset(cnt, 0, (size_t)nbodies * sizeof(unsigned)));
     CK(cudaMemcpy(cen, center, 3 * (size_t)nbodies * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dyn, c->body_dynamic.data(), (size_t)nbodies * sizeof(int), cudaMemcpyHostToDevice));
     c->bodies.acc = acc;
     c->bodies.center = cen;
     c->bodies.counters = cnt;
+    c->bodies.dynamic = dyn;
+    c->bodies.nbodies = nbodies;
+    if (c->boundary_method == 2) c->prepared = false;   // block partials of the volume-map forces
     if (c->prepared && (rc = build_body_tables(c))) {
         free_bodies(c);
         return rc;

@@ -1688,6 +1688,77 @@ __global__ void __launch_bounds__(kBlock) k_body_forces(DevParams<T> P, DevBufs<
     });
 }
 
+// Forces of the fluid on dynamic volume-map bodies (Bender2019): the branches of the same places
+// call addForce(x_j, f) with the particle's boundary point x_j of the body
+// (TimeStepDFSPH.cpp:1355-1364 in computePressureAccel, XSPH.cpp:196-204).  Body by body (block
+// uniform), each thread forms its particle's force and torque, the block sums them and writes its
+// partial; the last block adds the blocks' partials in block order (deterministic).
+template <class T, int PHASE>
+__global__ void __launch_bounds__(kBlock) k_vmap_forces(DevParams<T> P, DevBufs<T> B, BodyDev D)
+{
+    count_launch(&B.gsc->launches);
+    const SlotInfo q = slot_info(P);
+    const bool press = PHASE == 1 || P.div_on;
+    const bool xs = PHASE == 0 && P.xsph_b != T(0);
+    for (uint32_t b = 0; b < D.nbodies; b++) {   // block uniform
+        DSum<6> mine;
+#pragma unroll
+        for (int k = 0; k < 6; k++) mine.v[k] = 0.0;
+        if (q.act && D.dynamic[b]) {
+            const uint32_t i = q.i;
+            const v4_t<T> xj = ldv(B.bx, b * P.np + i);
+            const T Vj = (T)xj.w;
+            if (Vj > T(0)) {
+                const v4_t<T> xk = ldv(B.xk, i);
+                const T kap = (T)xk.w;
+                const V3<T> r = diff3<T>(xk, xj);
+                const T d2 = dot(r, r);
+                V3<T> f = mk3<T>(0, 0, 0);
+                if (press && fabs(kap) > P.eps) f = scl(r, P.mass * kap * Vj * grad_coef_d2(P.K, d2));
+                if (xs) {
+                    const T w = P.mass * P.xsph_b / (T)B.sc[q.s].dt * P.rho0 * Vj / B.density[i] *
+                                kernel_W(P.K, dev_sqrt(d2));
+                    f = add(f, scl(xyz<T>(ldv(B.v, i)), w));
+                }
+                const double *c = D.center + 3 * (size_t)b;
+                const double px = (double)xj.x - c[0], py = (double)xj.y - c[1], pz = (double)xj.z - c[2];
+                const double fx = (double)f.x, fy = (double)f.y, fz = (double)f.z;
+                mine.v[0] = fx;
+                mine.v[1] = fy;
+                mine.v[2] = fz;
+                mine.v[3] = py * fz - pz * fy;
+                mine.v[4] = pz * fx - px * fz;
+                mine.v[5] = px * fy - py * fx;
+            }
+        }
+        const DSum<6> bs = block_sum<6>(mine);
+        if (threadIdx.x == 0)
+#pragma unroll
+            for (int k = 0; k < 6; k++) D.vpartials[((size_t)b * 6 + k) * gridDim.x + blockIdx.x] = bs.v[k];
+    }
+    __shared__ bool amLast;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        amLast = atomicAdd(D.counters, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!amLast) return;
+    __threadfence();
+    for (uint32_t b = 0; b < D.nbodies; b++) {
+        DSum<6> part;
+#pragma unroll
+        for (int k = 0; k < 6; k++) part.v[k] = 0.0;
+        for (uint32_t g = threadIdx.x; g < gridDim.x; g += blockDim.x)
+#pragma unroll
+            for (int k = 0; k < 6; k++) part.v[k] += __ldcg(&D.vpartials[((size_t)b * 6 + k) * gridDim.x + g]);
+        const DSum<6> tot = block_sum<6>(part);
+        if (threadIdx.x == 0)
+#pragma unroll
+            for (int k = 0; k < 6; k++) D.acc[6 * (size_t)b + k] += tot.v[k];
+    }
+    if (threadIdx.x == 0) *D.counters = 0u;
+}
+
 // ==========================================================================
 // learned warm start
 // ==========================================================================
@@ -2342,6 +2413,13 @@ void launch_body_forces(const DevParams<T> &P, const DevBufs<T> &B, const BodyDe
     if (phase == 0) k_body_forces<T, 0><<<D.nblk, kBlock, 0, s>>>(P, B, D);
     else k_body_forces<T, 1><<<D.nblk, kBlock, 0, s>>>(P, B, D);
 }
+template <class T>
+void launch_vmap_forces(const DevParams<T> &P, const DevBufs<T> &B, const BodyDev &D, int phase, cudaStream_t s)
+{
+    if (!P.np || !P.nvmaps || !D.nbodies || !D.vpartials) return;
+    if (phase == 0) k_vmap_forces<T, 0><<<grid_for(P.np), kBlock, 0, s>>>(P, B, D);
+    else k_vmap_forces<T, 1><<<grid_for(P.np), kBlock, 0, s>>>(P, B, D);
+}
 template <class T> void launch_boundary_keys(const DevParams<T> &P, const v4_t<T> *xb_in, const uint32_t *bscene_in,
                                              uint32_t *keys, uint32_t *vals, cudaStream_t s)
 {
@@ -2413,6 +2491,7 @@ void launch_lists_to_ids(const uint32_t *list, const uint32_t *cnt, uint32_t cap
     template void launch_step_begin<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                     \
     template void launch_features<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                       \
     template void launch_body_forces<T>(const DevParams<T> &, const DevBufs<T> &, const BodyDev &, int, cudaStream_t); \
+    template void launch_vmap_forces<T>(const DevParams<T> &, const DevBufs<T> &, const BodyDev &, int, cudaStream_t); \
     template void launch_warmstart_select<T>(const DevParams<T> &, const DevBufs<T> &, bool, unsigned,              \
                                              cudaGraphConditionalHandle, bool, cudaStream_t);                       \
     template void launch_xsph<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                           \

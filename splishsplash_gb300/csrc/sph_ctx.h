@@ -182,6 +182,10 @@ struct BodyDev {
     double *partials;            // [6][nblk] block partial sums
     unsigned *counters;          // [nbodies] last-block counters, zero between launches
     uint32_t nblk;
+    // volume-map bodies (Bender2019): body b is map b
+    const int *dynamic;          // [nbodies] 1 if the body collects forces
+    double *vpartials;           // [nbodies][6][blocks of the particle launch]
+    uint32_t nbodies;
 };
 
 // ---- Bender2019 volume maps (vmap.cu) ----
@@ -230,6 +234,9 @@ template <class T> void launch_features(const DevParams<T> &P, const DevBufs<T> 
 // forces of the fluid on the dynamic bodies: phase 0 before the kick (divergence, XSPH and
 // viscosity boundary terms), phase 1 after the pressure solve (pressure term)
 template <class T> void launch_body_forces(const DevParams<T> &P, const DevBufs<T> &B, const BodyDev &D, int phase,
+                                           cudaStream_t s);
+// the same for volume-map bodies, from each particle's boundary points
+template <class T> void launch_vmap_forces(const DevParams<T> &P, const DevBufs<T> &B, const BodyDev &D, int phase,
                                            cudaStream_t s);
 // Learned warm start of one solver: both candidates, their first `sweeps` Jacobi iterations,
 // the choice and the loop decision after them (needs 1 <= sweeps <= max_iter of that solver).

@@ -482,7 +482,7 @@ class Context:
             self._check(self.L.sphgb_set_boundary_bodies(self.h, None, 0, None, None))
             self._nbodies = 0
             return
-        body = np.ascontiguousarray(body, np.uint32)
+        body = None if body is None else np.ascontiguousarray(body, np.uint32)   # None: volume-map bodies
         dyn = None if dynamic is None else np.ascontiguousarray(dynamic, np.int32)
         if dyn is not None and dyn.size != nb:
             raise ValueError("dynamic needs one flag per body")

@@ -207,3 +207,96 @@ def test_unsupported_combinations_are_refused():
     ts.ctx.set_params(p)
     assert code(ts.step) == "STATE"                           # map built for another radius
     ts.close()
+
+
+# ------------------------------------------------- forces on volume-map bodies
+MAP_CENTER = np.array([[0.4, 0.0, 0.4]])
+
+
+def column_scene():
+    """a block filling the floor of a 0.6 x 0.8 x 0.6 box at the rest spacing, no XSPH (which does
+    not conserve momentum exactly), so that the box carries all the fluid's momentum change"""
+    sc = scenes.small_block(counts=(11, 6, 11), box=(0.6, 0.8, 0.6), corner=(0.05, 0.05, 0.05)).as_float32()
+    sc.xb = np.zeros((0, 3))
+    sc.params.xsph = 0.0
+    return sc
+
+
+def momentum_balance(sc, forces_sum, p0, p1, steps, dt):
+    """sum of the per-step forces on the body against K M g - (P1 - P0) / h (fluid-fluid pressure
+    terms cancel pairwise, so the boundary takes the whole change of momentum besides gravity)"""
+    M = sc.n * sc.params.volume * sc.params.density0
+    expect = steps * M * np.asarray(sc.params.gravitation) - (p1 - p0) / dt
+    return forces_sum, expect, abs(steps * M * sc.params.gravitation[1])
+
+
+def test_oracle_momentum_balance_of_a_volume_mapped_box():
+    sc = column_scene()
+    sim = oracle.OracleSim(sc)
+    sim.set_volume_maps([container_map(4 * sc.params.particleRadius, (12, 16, 12), (0.6, 0.8, 0.6))])
+    sim.set_bodies(None, MAP_CENTER)
+    for _ in range(60):
+        sim.step()
+    m = sc.params.volume * sc.params.density0
+    sim.clear_forces()
+    p0 = m * sim.v.sum(0)
+    steps = 40
+    for _ in range(steps):
+        sim.step()
+        assert sim.stats()["dt_old"] == 0.005 and sim.stats()["dt"] == 0.005   # CFL at its cap
+    got, expect, scale = momentum_balance(sc, sim.body_force[0], p0, m * sim.v.sum(0), steps, 0.005)
+    assert np.abs(got - expect).max() < 1e-6 * scale, (got, expect)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol", [("fp32", 2e-3), ("fp64", 1e-8)])
+def test_map_body_forces_match_oracle(precision, tol):
+    sc = vmap_scene(velocity=(0.3, -0.5, 0.2))
+    sc.params.xsphBoundary = 0.1
+    probe = device_context(sc)
+    pre = oracle_with_map(sc, probe)
+    probe.close()
+    for _ in range(40):
+        pre.step()
+    state = dict(x=f32(pre.x), v=f32(pre.v), kappa=f32(pre.kappa), kappa_v=f32(pre.kappa_v), dt=pre.dt)
+    ts = device_context(sc, precision)
+    m = ts.getFluidModel()
+    m.setFieldBuffer("position", state["x"])
+    m.setFieldBuffer("velocity", state["v"])
+    m.setFieldBuffer("p / rho^2", state["kappa"])
+    m.setFieldBuffer("p_v / rho^2", state["kappa_v"])
+    ts.setTimeStepSize(state["dt"])
+    ts.ctx.set_boundary_bodies(None, MAP_CENTER)
+    sim = oracle_with_map(sc, ts, state)
+    sim.set_bodies(None, MAP_CENTER)
+    ts.step()
+    sim.step()
+    f, t = ts.ctx.boundary_forces()
+    scale_f, scale_t = np.abs(sim.body_force).max(), np.abs(sim.body_torque).max()
+    assert scale_f > 10.0
+    assert np.abs(f - sim.body_force).max() < tol * scale_f, (f, sim.body_force)
+    assert np.abs(t - sim.body_torque).max() < tol * scale_t, (t, sim.body_torque)
+    ts.close()
+
+
+@pytest.mark.gpu
+def test_momentum_balance_of_a_volume_mapped_box():
+    sc = column_scene()
+    ts = TimeStepDFSPH(sc, use_graph=True, precision="fp64")
+    v, f = scenes.box_mesh((0, 0, 0), (0.6, 0.8, 0.6))
+    ts.ctx.add_volume_map(v, f, (12, 16, 12), invert=True)
+    ts.ctx.set_boundary_method(2)
+    ts.ctx.set_boundary_bodies(None, MAP_CENTER)
+    for _ in range(60):
+        ts.step()
+    m = sc.params.volume * sc.params.density0
+    ts.ctx.clear_boundary_forces()
+    p0 = m * ts.getFluidModel().getFieldBuffer("velocity").sum(0)
+    steps = 40
+    for _ in range(steps):
+        st = ts.step()
+        assert st["dt_used"] == 0.005 and st["dt_next"] == 0.005
+    p1 = m * ts.getFluidModel().getFieldBuffer("velocity").sum(0)
+    got, expect, scale = momentum_balance(sc, ts.ctx.boundary_forces()[0][0], p0, p1, steps, 0.005)
+    assert np.abs(got - expect).max() < 1e-6 * scale, (got, expect)
+    ts.close()
