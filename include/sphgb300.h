@@ -340,10 +340,12 @@ int sphgb_clear_boundary_forces(sphgb_ctx *ctx, int32_t body);
  * R^T (x_i - translation) and treats x_j = x_i - max(phi + r / 2, 2 r) n with volume V_j, for
  * 0 < phi < 4 r, as one boundary particle per body in all DFSPH, XSPH sums
  * (TimeStep::computeVolumeAndBoundaryX, TimeStep.cpp:219-340); a particle found inside a body
- * is moved back by min(2 r - phi, r / 10) and stopped, as in the reference.  Supported: one
- * scene, static bodies, no boundary particles uploaded, no boundary viscosity; force feedback
- * with one body per map (sphgb_set_boundary_bodies); other combinations fail at the step with
- * SPHGB_ERR_STATE / SPHGB_ERR_ARGUMENT.
+ * is moved back by min(2 r - phi, r / 10) and stopped, as in the reference.  The Weiler2018
+ * boundary viscosity samples each x_j at the four points x_j -+ t1 h / 2, x_j -+ t2 h / 2 of the
+ * tangent plane, a quarter of V_j each (Viscosity_Weiler2018.cpp:205-255).  Supported: one
+ * scene, static bodies, no boundary particles uploaded; force feedback with one body per map
+ * (sphgb_set_boundary_bodies); other combinations fail at the step with SPHGB_ERR_STATE /
+ * SPHGB_ERR_ARGUMENT.
  *
  * sphgb_add_volume_map builds a map on the GPU in FP64 from a closed triangle mesh in body
  * coordinates, as SimulatorBase::initVolumeMap does (SimulatorBase.cpp:2512-2660): box = mesh box

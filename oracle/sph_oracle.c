@@ -451,9 +451,9 @@ static inline int collects_forces(const orc_state *s, int vmaps)
     return s->body_force && (vmaps || s->body);
 }
 
-/* BoundaryModel::addForce (BoundaryModel.h:38-49): force f at x_b on the body of boundary
- * particle j, torque (x_b - c) x f; only dynamic bodies collect.  Serial (deterministic). */
-static void add_force(const ctx_t *c, unsigned j, const double f[3])
+/* BoundaryModel::addForce (BoundaryModel.h:38-49): force f at point p on the body of boundary
+ * particle j, torque (p - c) x f; only dynamic bodies collect.  Serial (deterministic). */
+static void add_force_at(const ctx_t *c, unsigned j, const double p[3], const double f[3])
 {
     orc_state *s = c->s;
     const int vmaps = c->p->boundary_method == 2;
@@ -461,13 +461,47 @@ static void add_force(const ctx_t *c, unsigned j, const double f[3])
     const unsigned b = vmaps ? j % s->nvmaps : s->body[j];
     if (b >= s->nbodies || (s->body_dynamic && !s->body_dynamic[b])) return;
     const double *cen = s->body_center + 3 * (size_t)b;
-    const double r[3] = {(double)s->xb[3 * (size_t)j] - cen[0], (double)s->xb[3 * (size_t)j + 1] - cen[1],
-                         (double)s->xb[3 * (size_t)j + 2] - cen[2]};
+    const double r[3] = {p[0] - cen[0], p[1] - cen[1], p[2] - cen[2]};
     double *F = s->body_force + 3 * (size_t)b, *T = s->body_torque + 3 * (size_t)b;
     F[0] += f[0]; F[1] += f[1]; F[2] += f[2];
     T[0] += r[1] * f[2] - r[2] * f[1];
     T[1] += r[2] * f[0] - r[0] * f[2];
     T[2] += r[0] * f[1] - r[1] * f[0];
+}
+
+/* ... at the boundary particle (or volume-map boundary point) x_j itself */
+static void add_force(const ctx_t *c, unsigned j, const double f[3])
+{
+    const real *xb = c->s->xb + 3 * (size_t)j;
+    const double p[3] = {(double)xb[0], (double)xb[1], (double)xb[2]};
+    add_force_at(c, j, p, f);
+}
+
+/* The four samples that stand for a volume-map boundary point in the Weiler2018 boundary term
+ * (Viscosity_Weiler2018.cpp:205-255, 383-430, 697-740, 1031-1080): x_j -+ t1 d and x_j -+ t2 d
+ * with d = 0.5 h (m_tangentialDistanceFactor, :29) and t1, t2 from
+ * MathFunctions::getOrthogonalVectors (MathFunctions.cpp:234-247) of n = (x_j - x_i) / |.|;
+ * each carries a quarter of V_j.  0 when |x_i - x_j| <= 1e-4. */
+static int vmap_samples(const real *xi, const real *xj, double h, double xs[4][3])
+{
+    double n[3] = {(double)xj[0] - (double)xi[0], (double)xj[1] - (double)xi[1], (double)xj[2] - (double)xi[2]};
+    const double nl = sqrt(dot3(n, n));
+    if (!(nl > 1.0e-4)) return 0;
+    for (int d = 0; d < 3; d++) n[d] /= nl;
+    double v[3] = {1.0, 0.0, 0.0};
+    if (fabs(dot3(v, n)) > 0.999) { v[0] = 0.0; v[1] = 1.0; }
+    double t1[3] = {n[1] * v[2] - n[2] * v[1], n[2] * v[0] - n[0] * v[2], n[0] * v[1] - n[1] * v[0]};
+    double t2[3] = {n[1] * t1[2] - n[2] * t1[1], n[2] * t1[0] - n[0] * t1[2], n[0] * t1[1] - n[1] * t1[0]};
+    const double l1 = sqrt(dot3(t1, t1)), l2 = sqrt(dot3(t2, t2));
+    for (int d = 0; d < 3; d++) { t1[d] /= l1; t2[d] /= l2; }
+    const double dist = 0.5 * h;
+    for (int d = 0; d < 3; d++) {
+        xs[0][d] = (double)xj[d] - t1[d] * dist;
+        xs[1][d] = (double)xj[d] + t1[d] * dist;
+        xs[2][d] = (double)xj[d] - t2[d] * dist;
+        xs[3][d] = (double)xj[d] + t2[d] * dist;
+    }
+    return 1;
 }
 
 /* computePressureAccel with applyBoundaryForces (TimeStepDFSPH.cpp:1337-1344):
@@ -722,6 +756,19 @@ static void visc_matvec(const visc_t *w, const real *vec, real *result)
             const double v3[3] = {(double)vi[0], (double)vi[1], (double)vi[2]};
             for (unsigned k = c->B.off[i]; k < c->B.off[i + 1]; k++) {
                 const unsigned j = c->B.idx[k];
+                if (c->p->boundary_method == 2) {   /* four samples, a quarter of V_j each, no rho0 / rho_i */
+                    double xs[4][3];
+                    if (!vmap_samples(xi, s->xb + 3 * (size_t)j, c->K.h, xs)) continue;
+                    const double vol = 0.25 * (double)s->Vb[j];
+                    for (int q = 0; q < 4; q++) {
+                        double r[3], g[3];
+                        for (int d = 0; d < 3; d++) r[d] = (double)xi[d] - xs[q][d];
+                        kGradW(&c->K, r, g);
+                        const double f = w->d * w->mub * vol * dot3(v3, r) / (dot3(r, r) + 0.01 * w->h2);
+                        ai[0] += f * g[0]; ai[1] += f * g[1]; ai[2] += f * g[2];
+                    }
+                    continue;
+                }
                 double r[3], g[3];
                 diffv(xi, s->xb + 3 * (size_t)j, r);
                 kGradW(&c->K, r, g);
@@ -759,6 +806,20 @@ static void visc_diag_inverse(const visc_t *w, real *diag9, real *inv9)
         if (w->mub != 0.0) {
             for (unsigned k = c->B.off[i]; k < c->B.off[i + 1]; k++) {
                 const unsigned j = c->B.idx[k];
+                if (c->p->boundary_method == 2) {
+                    double xs[4][3];
+                    if (!vmap_samples(xi, s->xb + 3 * (size_t)j, c->K.h, xs)) continue;
+                    const double vol = 0.25 * (double)s->Vb[j];
+                    for (int q = 0; q < 4; q++) {
+                        double r[3], g[3];
+                        for (int d = 0; d < 3; d++) r[d] = (double)xi[d] - xs[q][d];
+                        kGradW(&c->K, r, g);
+                        const double f = w->d * w->mub * vol / (dot3(r, r) + 0.01 * w->h2);
+                        for (int a = 0; a < 3; a++)
+                            for (int b = 0; b < 3; b++) R[3 * a + b] += f * g[a] * r[b];
+                    }
+                    continue;
+                }
                 double r[3], g[3];
                 diffv(xi, s->xb + 3 * (size_t)j, r);
                 kGradW(&c->K, r, g);
@@ -905,13 +966,27 @@ static int viscosity_weiler(ctx_t *c, double dt)
     /* boundary feedback of applyForces (Viscosity_Weiler2018.cpp:960-975), static v_b = 0:
      * a = d mub (rho0 V_b / rho_i) (v_i'.x_ib) / (|x_ib|^2 + 0.01 h^2) gradW_ib, force -m_i / rho_i a */
     const double mub = c->p->viscosity_boundary * c->rho0;
-    if (mub != 0.0 && s->body && s->body_force) {
+    if (mub != 0.0 && collects_forces(s, c->p->boundary_method == 2)) {
         const double h2 = c->K.h * c->K.h;
         for (long i = 0; i < (long)s->n; i++) {
             const double rhoi = (double)s->density[i];
             const double nv[3] = {(double)x[3 * i], (double)x[3 * i + 1], (double)x[3 * i + 2]};
             for (unsigned k = c->B.off[i]; k < c->B.off[i + 1]; k++) {
                 const unsigned j = c->B.idx[k];
+                if (c->p->boundary_method == 2) {   /* at the four samples (:1031-1080) */
+                    double xs[4][3];
+                    if (!vmap_samples(s->x + 3 * i, s->xb + 3 * (size_t)j, c->K.h, xs)) continue;
+                    const double vol = 0.25 * (double)s->Vb[j];
+                    for (int q = 0; q < 4; q++) {
+                        double r[3], g[3], f[3];
+                        for (int d = 0; d < 3; d++) r[d] = (double)s->x[3 * i + d] - xs[q][d];
+                        kGradW(&c->K, r, g);
+                        const double coef = 10.0 * mub * vol * dot3(nv, r) / (dot3(r, r) + 0.01 * h2);
+                        for (int d = 0; d < 3; d++) f[d] = -c->mass / rhoi * (coef * g[d]);
+                        add_force_at(c, j, xs[q], f);
+                    }
+                    continue;
+                }
                 double r[3], g[3], f[3];
                 diffv(s->x + 3 * i, s->xb + 3 * (size_t)j, r);
                 kGradW(&c->K, r, g);
@@ -1043,8 +1118,7 @@ int orc_step(orc_state *s, const orc_params *p)
 
     /* Bender2019: static bodies without force feedback or boundary viscosity */
     const int vmaps = p->boundary_method == 2;
-    if (vmaps && (s->body || (p->viscosity_method == 6 && p->viscosity_boundary != 0.0)))
-        return -5;
+    if (vmaps && s->body) return -5;
     real *xb_saved = s->xb, *Vb_saved = s->Vb, *vxb = NULL, *vVb = NULL;
     const unsigned nb_saved = s->nb;
     if (lists_build(&c.F, s->n, s->x, s->n, s->x, c.K.h, 1, p->fp32_predicate) != 0) return -1;

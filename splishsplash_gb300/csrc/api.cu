@@ -994,8 +994,6 @@ int check_boundary_method(sphgb_ctx *c)
     if (c->nb) return fail(c, SPHGB_ERR_STATE, "the Bender2019 boundary takes no boundary particles");
     if (c->nbodies && c->nbodies != c->vmaps.size())
         return fail(c, SPHGB_ERR_ARGUMENT, "with volume maps the bodies are the maps: one body per map");
-    if (c->prm.viscosity_method == 6 && c->prm.viscosity_boundary != 0.0)
-        return fail(c, SPHGB_ERR_ARGUMENT, "boundary viscosity is not available for volume maps");
     for (const auto &m : c->vmaps)
         if (m.support != 4.0 * c->prm.particle_radius)
             return fail(c, SPHGB_ERR_STATE, "a volume map was built for another particle radius");

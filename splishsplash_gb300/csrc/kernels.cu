@@ -1168,6 +1168,31 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams<T> P, DevBufs<T> B, i
 // w_j travels in the w lane of the CG direction p (and of the warm start in cg_x), so one
 // 16-byte gather per neighbour gives both the vector and the weight.
 
+// The four samples that stand for a volume-map boundary point x_j in the Weiler2018 boundary term
+// (Viscosity_Weiler2018.cpp:205-255, 383-430, 697-740, 1031-1080): x_j -+ t1 h/2 and x_j -+ t2 h/2
+// with t1 = n x v / |.|, t2 = n x t1 / |.|, n = (x_j - x_i) / |.| and v = e_x, or e_y when
+// |n . e_x| > 0.999 (MathFunctions::getOrthogonalVectors, MathFunctions.cpp:234-247); each stands
+// for a quarter of V_j.  visit(x_k) for each; none when |x_i - x_j| <= 1e-4.
+template <class T, class Vis>
+__device__ __forceinline__ void vmap_samples(const v4_t<T> &xi, const v4_t<T> &xj, T h, Vis visit)
+{
+    V3<T> n = sub(xyz<T>(xj), xyz<T>(xi));
+    const T nl = dev_sqrt(dot(n, n));
+    if (!(nl > T(1.0e-4))) return;
+    n = scl(n, T(1) / nl);
+    const V3<T> v = fabs(n.x) > T(0.999) ? mk3<T>(0, 1, 0) : mk3<T>(1, 0, 0);
+    V3<T> t1 = mk3<T>(n.y * v.z - n.z * v.y, n.z * v.x - n.x * v.z, n.x * v.y - n.y * v.x);
+    V3<T> t2 = mk3<T>(n.y * t1.z - n.z * t1.y, n.z * t1.x - n.x * t1.z, n.x * t1.y - n.y * t1.x);
+    t1 = scl(t1, T(1) / dev_sqrt(dot(t1, t1)));
+    t2 = scl(t2, T(1) / dev_sqrt(dot(t2, t2)));
+    const T d = T(0.5) * h;
+    const V3<T> c = xyz<T>(xj);
+    visit(sub(c, scl(t1, d)));
+    visit(add(c, scl(t1, d)));
+    visit(sub(c, scl(t2, d)));
+    visit(add(c, scl(t2, d)));
+}
+
 // Boundary term of the operator (mub != 0), this lane's share:
 // sum_b d mub (rho0 V_b / rho_i) (v_i.x_ib) / (...) gradW_ib.
 template <int LPP, class T>
@@ -1182,6 +1207,20 @@ __device__ __forceinline__ V3<T> weiler_boundary(const DevParams<T> &P, const De
         const T f = P.vd * P.mub * (P.rho0 * (T)xj.w / rhoi) * dot(vi, r) / (r2 + eps2);
         acc = add(acc, scl(r, grad_coef_d2(P.K, r2) * f));
     });
+    // volume maps: four samples per body, a quarter of V_j each and no rho0 / rho_i factor (as in
+    // the reference's Bender2019 branches); lane 0 only, the lanes' shares are summed
+    if (q.l == 0)
+        for (uint32_t b = 0; b < P.nvmaps; b++) {
+            const v4_t<T> xj = ldv(B.bx, b * P.np + q.i);
+            if (!((T)xj.w > T(0))) continue;
+            const T vol = T(0.25) * (T)xj.w;
+            vmap_samples<T>(xi, xj, P.K.h, [&](const V3<T> &xk) {
+                const V3<T> r = sub(xyz<T>(xi), xk);
+                const T r2 = dot(r, r);
+                const T f = P.vd * P.mub * vol * dot(vi, r) / (r2 + eps2);
+                acc = add(acc, scl(r, grad_coef_d2(P.K, r2) * f));
+            });
+        }
     return acc;
 }
 
@@ -1236,6 +1275,19 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T
                 m[0] += f * r.x * r.x; m[1] += f * r.x * r.y; m[2] += f * r.x * r.z;
                 m[3] += f * r.y * r.y; m[4] += f * r.y * r.z; m[5] += f * r.z * r.z;
             });
+            if (q.l == 0)   // volume maps: the four samples of each body (diagonalMatrixElement :697-740)
+                for (uint32_t b = 0; b < P.nvmaps; b++) {
+                    const v4_t<T> xj = ldv(B.bx, b * P.np + i);
+                    if (!((T)xj.w > T(0))) continue;
+                    const T vol = T(0.25) * (T)xj.w;
+                    vmap_samples<T>(xi, xj, P.K.h, [&](const V3<T> &xk) {
+                        const V3<T> r = sub(xyz<T>(xi), xk);
+                        const T r2 = dot(r, r);
+                        const T f = P.vd * P.mub * vol / (r2 + eps2) * grad_coef_d2(P.K, r2);
+                        m[0] += f * r.x * r.x; m[1] += f * r.x * r.y; m[2] += f * r.x * r.z;
+                        m[3] += f * r.y * r.y; m[4] += f * r.y * r.z; m[5] += f * r.z * r.z;
+                    });
+                }
             acc = add(acc, weiler_boundary<LPP>(P, B, q, xi, rhoi, gi));
         }
     }
@@ -1729,6 +1781,25 @@ __global__ void __launch_bounds__(kBlock) k_vmap_forces(DevParams<T> P, DevBufs<
                 mine.v[3] = py * fz - pz * fy;
                 mine.v[4] = pz * fx - px * fz;
                 mine.v[5] = px * fy - py * fx;
+                // Weiler2018 applyForces at the four samples (Viscosity_Weiler2018.cpp:1031-1080)
+                if (PHASE == 0 && P.visc_on && P.mub != T(0) && B.sc[q.s].cg_state != 2u) {
+                    const V3<T> nv = xyz<T>(ldv(B.cg_x, i));
+                    const T rhoi = B.density[i], vol = T(0.25) * Vj, eps2 = T(0.01) * P.h2;
+                    vmap_samples<T>(xk, xj, P.K.h, [&](const V3<T> &xs4) {
+                        const V3<T> r4 = sub(xyz<T>(xk), xs4);
+                        const T r2 = dot(r4, r4);
+                        const T a = P.vd * P.mub * vol * dot(nv, r4) / (r2 + eps2) * grad_coef_d2(P.K, r2);
+                        const V3<T> g = scl(r4, -P.mass / rhoi * a);
+                        const double gx = (double)g.x, gy = (double)g.y, gz = (double)g.z;
+                        const double qx = (double)xs4.x - c[0], qy = (double)xs4.y - c[1], qz = (double)xs4.z - c[2];
+                        mine.v[0] += gx;
+                        mine.v[1] += gy;
+                        mine.v[2] += gz;
+                        mine.v[3] += qy * gz - qz * gy;
+                        mine.v[4] += qz * gx - qx * gz;
+                        mine.v[5] += qx * gy - qy * gx;
+                    });
+                }
             }
         }
         const DSum<6> bs = block_sum<6>(mine);
