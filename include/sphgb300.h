@@ -191,6 +191,22 @@ int sphgb_neighbors(sphgb_ctx *ctx, int kind, uint32_t *offsets, uint32_t *indic
  * and returns its status.  A new export or sphgb_destroy waits for the previous one. */
 int sphgb_export_vtk(sphgb_ctx *ctx, const char *path, const int *fields, uint32_t nfields, int wait);
 int sphgb_export_wait(sphgb_ctx *ctx);
+/* sphgb_export_bgeo writes one partio BGEO file of all fluid particles in particle-id order, as
+ * ParticleExporter_Partio::writeParticlesPartio does through partio
+ * (Simulator/Exporter/ParticleExporter_Partio.cpp:67-201): the attribute "position" (float x 3,
+ * stored with w = 1), "id" (INT), then one attribute per entry of `fields` under its field name
+ * (scalar fields FLOAT, uint fields INT, 3-vectors VECTOR; other fields SPHGB_ERR_ARGUMENT).
+ * Values are stored as 32-bit floats in both precisions, as the reference casts them.  level:
+ * -1 (zlib's default, partio's choice) or 1-9 writes the file as one gzip member, as the
+ * reference's Partio::write(..., true) does, compressed on all host cores but one; 0 writes it plain.
+ * The device packs the big-endian records on the export stream and copies them to pinned
+ * memory; wait and sphgb_export_wait as for sphgb_export_vtk.  SPHGB_ERR_STATE when zlib
+ * (libz.so.1) cannot be loaded for a compressed file. */
+int sphgb_export_bgeo(sphgb_ctx *ctx, const char *path, const int *fields, uint32_t nfields, int level, int wait);
+/* the field id of a fluid field name as the reference's FieldDescription names it ("velocity",
+ * "p / rho^2", ...; FluidModel.cpp:61-67, TimeStepDFSPH.cpp:49-53), for exporters that take the
+ * names of SimulatorBase's particleAttributes; -1 for an unknown name */
+int sphgb_field_id(const char *name);
 /* The simulation state of the context in a binary file, exactly as held on the device (the
  * double-float positions in both parts, velocities, velocity differences, both warm starts,
  * per-scene step size and time, the boundary particles, the parameters and the lanes per

@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "../../include/sphgb300.h"
+#include "bgeo.h"
 #include "mlp.cuh"
 #include "sph_ctx.h"
 
@@ -2209,6 +2210,22 @@ void write_vtk(sphgb_ctx *c, std::string path, uint32_t n, std::vector<ExportChu
     }
 }
 
+// Writer thread of the BGEO export: waits for the device copy of the packed records
+void write_bgeo(sphgb_ctx *c, std::string path, uint32_t n, uint32_t words, std::vector<BgeoAttr> attrs, int level)
+{
+    if (cudaEventSynchronize(c->export_copied) != cudaSuccess) {
+        c->export_rc = SPHGB_ERR_CUDA;
+        c->export_err = "export: device copy failed";
+        return;
+    }
+    std::string err;
+    const int rc = write_bgeo_file(path, c->export_host, n, words, attrs, level, err);
+    if (rc) {
+        c->export_rc = rc;
+        c->export_err = err;
+    }
+}
+
 int export_join(sphgb_ctx *c)
 {
     if (c->export_thread.joinable()) c->export_thread.join();
@@ -2303,6 +2320,109 @@ int sphgb_export_vtk(sphgb_ctx *c, const char *path, const int *fields, uint32_t
     CK(cudaEventRecord(c->export_copied, c->export_stream));
     c->export_rc = SPHGB_OK;
     c->export_thread = std::thread(write_vtk, c, std::string(path), n, chunks, c->fp64);
+    return wait ? export_join(c) : SPHGB_OK;
+}
+
+int sphgb_field_id(const char *name)
+{
+    if (!name) return -1;
+    for (int f = 0; f <= SPHGB_FIELD_POSITION_LO; f++) {
+        const char *fn = field_name(f);
+        if (fn && std::strcmp(fn, name) == 0) return f;
+    }
+    return -1;
+}
+
+int sphgb_export_bgeo(sphgb_ctx *c, const char *path, const int *fields, uint32_t nfields, int level, int wait)
+{
+    if (!c || !path || (nfields && !fields)) return SPHGB_ERR_ARGUMENT;
+    if (level < -1 || level > 9) return fail(c, SPHGB_ERR_ARGUMENT, "compression level must be -1 .. 9");
+    if (!c->have_fluid) return fail(c, SPHGB_ERR_STATE, "no fluid uploaded");
+    if (level != 0 && !bgeo_compression_available())
+        return fail(c, SPHGB_ERR_STATE, "compressed BGEO needs zlib (libz.so.1), which could not be loaded");
+    cudaSetDevice(c->cfg.device);
+    int rc = export_join(c);   // one export in flight at a time
+    if (rc) return rc;
+    if (nfields + 2 > kBgeoMaxColumns) return fail(c, SPHGB_ERR_ARGUMENT, "too many fields");
+    uint32_t words = 5;   // x, y, z, 1, id
+    for (uint32_t k = 0; k < nfields; k++) {
+        const int f = fields[k];
+        if (!field_name(f) || f == SPHGB_FIELD_POSITION || f == SPHGB_FIELD_PARTICLE_ID)
+            return fail(c, SPHGB_ERR_ARGUMENT, "field cannot be exported (boundary fields, position or id twice)");
+        const int comps = field_components(f);
+        if (comps != 1 && comps != 3)
+            return fail(c, SPHGB_ERR_ARGUMENT, "BGEO carries scalar and 3-vector fields only");
+        words += (uint32_t)comps;
+    }
+    if (c->step_pending) {
+        sphgb_stats st;
+        fill_stats(c, &st);
+    }
+    const uint32_t n = c->n;
+    const int rword = c->fp64 ? 8 : 4;
+    // device staging: the fields in particle-id order (256-byte aligned chunks), then the records
+    std::vector<ExportChunk> chunks;
+    size_t off = 0;
+    auto add = [&](int field, int comps, int word) {
+        chunks.push_back({field, off, (size_t)n * comps, word, comps});
+        off += ((size_t)n * comps * word + 255) / 256 * 256;
+    };
+    add(-1, 3, rword);
+    add(SPHGB_FIELD_PARTICLE_ID, 1, 4);
+    for (uint32_t k = 0; k < nfields; k++)
+        add(fields[k], field_components(fields[k]), is_uint_field(fields[k]) ? 4 : rword);
+    const size_t rec_off = off, rec_bytes = (size_t)n * words * 4u;
+    const size_t bytes = std::max<size_t>(rec_off + rec_bytes, 256);
+    if (c->export_dev_bytes < bytes) {
+        if (c->export_dev) cudaFree(c->export_dev);
+        c->export_dev = nullptr;
+        c->export_dev_bytes = 0;
+        CK(cudaMalloc(&c->export_dev, bytes));
+        c->export_dev_bytes = bytes;
+    }
+    if (c->export_host_bytes < std::max<size_t>(rec_bytes, 256)) {
+        if (c->export_host) cudaFreeHost(c->export_host);
+        c->export_host = nullptr;
+        c->export_host_bytes = 0;
+        CK(cudaMallocHost(&c->export_host, std::max<size_t>(rec_bytes, 256)));
+        c->export_host_bytes = std::max<size_t>(rec_bytes, 256);
+    }
+    if (!c->export_stream) {
+        CK(cudaStreamCreateWithFlags(&c->export_stream, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&c->export_start, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&c->export_scattered, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&c->export_copied, cudaEventDisableTiming));
+    }
+    CK(cudaEventRecord(c->export_start, c->stream));
+    CK(cudaStreamWaitEvent(c->export_stream, c->export_start, 0));
+    char *dev = static_cast<char *>(c->export_dev);
+    std::vector<BgeoColumn> cols;
+    std::vector<BgeoAttr> attrs;
+    for (const ExportChunk &ch : chunks) {
+        const int field = ch.field < 0 ? SPHGB_FIELD_POSITION : ch.field;
+        const bool u = is_uint_field(field);
+        const int dt = u ? SPHGB_DTYPE_U32 : (c->fp64 ? SPHGB_DTYPE_F64 : SPHGB_DTYPE_F32);
+        if (c->fp64) {
+            launch_scatter_field<double>(make_params<double>(c), make_bufs<double>(c, 0), field, dev + ch.offset, dt,
+                                         c->export_stream);
+        } else {
+            launch_scatter_field<float>(make_params<float>(c), make_bufs<float>(c, 0), field, dev + ch.offset, dt,
+                                        c->export_stream);
+        }
+        cols.push_back({dev + ch.offset, (uint32_t)ch.comps, u ? 2u : (c->fp64 ? 1u : 0u)});
+        if (ch.field < 0) cols.push_back({nullptr, 1u, 3u});   // the position's w = 1
+        else attrs.push_back({ch.field == SPHGB_FIELD_PARTICLE_ID ? std::string("id") : std::string(field_name(ch.field)),
+                              (uint32_t)ch.comps, u});
+    }
+    launch_bgeo_pack(cols.data(), (uint32_t)cols.size(), n, reinterpret_cast<uint32_t *>(dev + rec_off),
+                     c->export_stream);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(c->export_scattered, c->export_stream));
+    CK(cudaStreamWaitEvent(c->stream, c->export_scattered, 0));
+    if (rec_bytes) CK(cudaMemcpyAsync(c->export_host, dev + rec_off, rec_bytes, cudaMemcpyDeviceToHost, c->export_stream));
+    CK(cudaEventRecord(c->export_copied, c->export_stream));
+    c->export_rc = SPHGB_OK;
+    c->export_thread = std::thread(write_bgeo, c, std::string(path), n, words, attrs, level);
     return wait ? export_join(c) : SPHGB_OK;
 }
 

@@ -122,7 +122,7 @@ EXPORTS = [
     "sphgb_num_particles", "sphgb_get_stream", "sphgb_profile_enable", "sphgb_profile_reset", "sphgb_profile_read",
     "sphgb_set_warmstart_mlp", "sphgb_set_feature_output", "sphgb_upload_scenes", "sphgb_num_scenes",
     "sphgb_scene_stats", "sphgb_set_warmstart_gate", "sphgb_set_lanes_per_particle", "sphgb_get_lanes_per_particle",
-    "sphgb_export_vtk", "sphgb_export_wait", "sphgb_save_state", "sphgb_load_state",
+    "sphgb_export_vtk", "sphgb_export_wait", "sphgb_export_bgeo", "sphgb_field_id", "sphgb_save_state", "sphgb_load_state",
     "sphgb_set_boundary_bodies", "sphgb_boundary_forces", "sphgb_clear_boundary_forces",
     "sphgb_set_neighbor_staging", "sphgb_get_neighbor_staging",
     "sphgb_add_volume_map", "sphgb_add_volume_map_values", "sphgb_get_volume_map", "sphgb_clear_volume_maps",
@@ -179,6 +179,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.sphgb_get_lanes_per_particle.argtypes = [vp, ctypes.POINTER(u32), vp]
     L.sphgb_export_vtk.argtypes = [vp, ctypes.c_char_p, vp, u32, i32]
     L.sphgb_export_wait.argtypes = [vp]
+    L.sphgb_export_bgeo.argtypes = [vp, ctypes.c_char_p, vp, u32, i32, i32]
+    L.sphgb_field_id.argtypes = [ctypes.c_char_p]
     L.sphgb_save_state.argtypes = [vp, ctypes.c_char_p]
     L.sphgb_load_state.argtypes = [vp, ctypes.c_char_p]
     L.sphgb_set_boundary_bodies.argtypes = [vp, vp, u32, vp, vp]
@@ -572,6 +574,13 @@ class Context:
         ids = np.array([FIELDS[f][0] for f in fields], np.int32)
         self._check(self.L.sphgb_export_vtk(self.h, os.fsencode(path), _p(ids) if ids.size else None, ids.size,
                                             int(wait)))
+
+    def export_bgeo(self, path: str, fields=(), level: int = -1, wait: bool = True):
+        """Partio BGEO file of all fluid particles (position, id and the named scalar / vector
+        fields), gzip-compressed at zlib level `level` (-1: zlib's default) or plain (0)."""
+        ids = np.array([FIELDS[f][0] for f in fields], np.int32)
+        self._check(self.L.sphgb_export_bgeo(self.h, os.fsencode(path), _p(ids) if ids.size else None, ids.size,
+                                             int(level), int(wait)))
 
     def export_wait(self):
         self._check(self.L.sphgb_export_wait(self.h))

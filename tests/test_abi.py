@@ -44,3 +44,16 @@ def test_python_mirror_fails_loudly_without_gpu():
     from splishsplash_gb300 import native
     with pytest.raises(native.SphgbError):
         native.Context()
+
+
+def test_field_ids_of_the_reference_field_names():
+    """sphgb_field_id maps the reference's field names to the ids of the header (a host-only call)"""
+    from splishsplash_gb300 import native
+    L = ctypes.CDLL(b.build())
+    L.sphgb_field_id.argtypes = [ctypes.c_char_p]
+    L.sphgb_field_id.restype = ctypes.c_int
+    for name, (fid, _) in native.FIELDS.items():
+        if fid <= 18 and fid not in (14, 15):      # fluid fields; 14, 15 are boundary fields
+            assert L.sphgb_field_id(name.encode()) == fid, name
+    assert L.sphgb_field_id(b"velocity") == 1 and L.sphgb_field_id(b"p / rho^2") == 6
+    assert L.sphgb_field_id(b"no such field") == -1 and L.sphgb_field_id(None) == -1

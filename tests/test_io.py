@@ -1,8 +1,10 @@
-"""Particle export (legacy VTK, like the reference's ParticleExporter_VTK) and state files,
-both produced from the device copy.  A state file restores a context exactly: the loaded
-context continues bit for bit."""
+"""Particle export (legacy VTK, like the reference's ParticleExporter_VTK; partio BGEO, like
+ParticleExporter_Partio) and state files, all produced from the device copy.  A state file
+restores a context exactly: the loaded context continues bit for bit."""
+import gzip
 import os
 import re
+import struct
 import tempfile
 
 import numpy as np
@@ -60,6 +62,117 @@ def read_vtk(path):
         line()
     assert pos == len(raw)
     return out
+
+
+def read_bgeo(path):
+    """partio's classic BGEO (version 5), plain or one gzip member: {name: array, "_types": ...}"""
+    raw = open(path, "rb").read()
+    compressed = raw[:2] == b"\x1f\x8b"
+    if compressed:
+        raw = gzip.decompress(raw)      # checks the member's CRC-32 and length
+    magic, vc, version = struct.unpack_from(">icI", raw, 0)
+    assert magic == 0x4267656F and vc == b"V" and version == 5
+    n, nprim, npg, nprg, npa, nva, nra, nda = struct.unpack_from(">8I", raw, 9)
+    assert (nprim, npg, nprg, nva, nra, nda) == (0, 0, 0, 0, 0, 0)
+    pos = 9 + 32
+    attrs = []
+    for _ in range(npa):
+        (ln,) = struct.unpack_from(">H", raw, pos)
+        name = raw[pos + 2:pos + 2 + ln].decode()
+        pos += 2 + ln
+        size, typ = struct.unpack_from(">Hi", raw, pos)
+        pos += 6
+        assert struct.unpack_from(f">{size}i", raw, pos) == (0,) * size     # defaults
+        pos += 4 * size
+        attrs.append((name, size, typ))
+    words = 4 + sum(a[1] for a in attrs)
+    rec = np.frombuffer(raw, dtype=">u4", count=n * words, offset=pos).reshape(n, words)
+    pos += rec.nbytes
+    assert raw[pos:] == b"\x00\xff"
+    out = {"_types": {a[0]: (a[1], a[2]) for a in attrs}, "_compressed": compressed}
+    out["position"] = rec[:, :3].view(">f4").astype(np.float32)
+    assert (rec[:, 3].view(">f4") == 1.0).all()
+    col = 4
+    for name, size, typ in attrs:
+        a = rec[:, col:col + size]
+        a = a.view(">i4").astype(np.int64) if typ == 1 else a.view(">f4").astype(np.float32)
+        out[name] = a if size > 1 else a[:, 0]
+        col += size
+    return out
+
+
+BGEO_FIELDS = ("density", "velocity", "p / rho^2", "fluid neighbors")
+
+
+def check_bgeo(b, ref, n):
+    assert b["_types"] == {"id": (1, 1), "density": (1, 0), "velocity": (3, 5), "p / rho^2": (1, 0),
+                           "fluid neighbors": (1, 1)}
+    np.testing.assert_array_equal(b["id"], np.arange(n))
+    for f in ("position",) + BGEO_FIELDS:
+        np.testing.assert_array_equal(b[f], ref[f])
+
+
+def bgeo_reference(ts):
+    m = ts.getFluidModel()
+    ref = {f: m.getFieldBuffer(f, np.float32) for f in ("position", "density", "velocity", "p / rho^2")}
+    ref["fluid neighbors"] = ts.ctx.download("fluid neighbors").astype(np.int64)
+    return ref
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_bgeo_export_matches_downloads(precision):
+    """plain and compressed, waited and overlapping a step; FP64 values are stored as floats"""
+    sc = scenes.small_block(counts=(10, 10, 10), box=(0.8, 0.8, 0.8), velocity=(0.2, 0.0, 0.0))
+    ts = TimeStepDFSPH(sc, precision=precision)
+    for _ in range(5):
+        ts.step()
+    ref = bgeo_reference(ts)
+    with tempfile.TemporaryDirectory() as d:
+        paths = [os.path.join(d, f"ParticleData_Fluid_{k}.bgeo") for k in range(3)]
+        ts.ctx.export_bgeo(paths[0], BGEO_FIELDS, level=-1)
+        ts.ctx.export_bgeo(paths[1], BGEO_FIELDS, level=0)
+        ts.ctx.export_bgeo(paths[2], BGEO_FIELDS, level=6, wait=False)   # overlaps the next step
+        ts.step()
+        ts.ctx.export_wait()
+        for p, comp in zip(paths, (True, False, True)):
+            b = read_bgeo(p)
+            assert b["_compressed"] == comp
+            check_bgeo(b, ref, sc.n)
+        assert not np.array_equal(read_bgeo(paths[2])["position"], bgeo_reference(ts)["position"])
+    ts.close()
+
+
+def test_bgeo_export_of_many_pieces():
+    """about 3.6 MB of records: several compression pieces joined into one gzip member; levels 1 and
+    9 give the same content, and the file is smaller than the plain one"""
+    sc = scenes.small_block(counts=(50, 40, 50), radius=0.01, box=(1.2, 1.0, 1.2), velocity=(0.1, 0.0, 0.2))
+    ts = TimeStepDFSPH(sc)
+    ts.step()
+    ref = bgeo_reference(ts)
+    with tempfile.TemporaryDirectory() as d:
+        sizes = {}
+        for level in (0, 1, 9):
+            p = os.path.join(d, f"l{level}.bgeo")
+            ts.ctx.export_bgeo(p, BGEO_FIELDS, level=level)
+            check_bgeo(read_bgeo(p), ref, sc.n)
+            sizes[level] = os.path.getsize(p)
+        assert sizes[0] > 3_000_000 and sizes[9] <= sizes[1] < sizes[0]
+    ts.close()
+
+
+def test_bgeo_export_refusals():
+    sc = scenes.small_block(counts=(4, 4, 4))
+    ts = TimeStepDFSPH(sc)
+    ts.step()
+    with tempfile.TemporaryDirectory() as d:
+        p = os.path.join(d, "x.bgeo")
+        for kwargs in (dict(level=10), dict(level=-2), dict(fields=("position",)), dict(fields=("id",))):
+            with pytest.raises(native.SphgbError) as e:
+                ts.ctx.export_bgeo(p, **kwargs)
+            assert native.ERR_NAMES[e.value.code] == "ARGUMENT"
+        with pytest.raises(native.SphgbError):
+            ts.ctx.export_bgeo(os.path.join(d, "missing", "x.bgeo"))
+    ts.close()
 
 
 def test_vtk_export_matches_downloads_and_overlaps_a_step():
