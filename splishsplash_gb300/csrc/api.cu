@@ -986,7 +986,7 @@ template <class T> int autotune(sphgb_ctx *c)
 }
 
 // The Bender2019 configurations this path supports: one scene, static bodies given only as volume
-// maps built for the current support radius, no boundary viscosity, no force feedback.
+// maps built for the current support radius, forces collected with one body per map.
 int check_boundary_method(sphgb_ctx *c)
 {
     if (c->boundary_method != 2) return SPHGB_OK;
