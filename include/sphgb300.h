@@ -349,7 +349,7 @@ int sphgb_boundary_forces(sphgb_ctx *ctx, double *force, double *torque);
 int sphgb_clear_boundary_forces(sphgb_ctx *ctx, int32_t body);
 
 /* Bender2019 boundaries (BoundaryModel_Bender2019, the reference's default boundary handling,
- * Simulation.cpp:88): static bodies given as volume maps instead of boundary particles.
+ * Simulation.cpp:88): bodies given as volume maps instead of boundary particles.
  * A map is Discregrid's cubic Lagrange grid restated: res cells per axis over the body's box, the
  * 32-node cubic serendipity element per cell, two fields per node, the signed distance phi (positive
  * on the fluid side) and the boundary volume.  Every step samples each body at
@@ -359,7 +359,8 @@ int sphgb_clear_boundary_forces(sphgb_ctx *ctx, int32_t body);
  * is moved back by min(2 r - phi, r / 10) and stopped, as in the reference.  The Weiler2018
  * boundary viscosity samples each x_j at the four points x_j -+ t1 h / 2, x_j -+ t2 h / 2 of the
  * tangent plane, a quarter of V_j each (Viscosity_Weiler2018.cpp:205-255).  Supported: one
- * scene, static bodies, no boundary particles uploaded; force feedback with one body per map
+ * scene, no boundary particles uploaded; moving bodies through sphgb_set_volume_map_motion; force
+ * feedback with one body per map
  * (sphgb_set_boundary_bodies); other combinations fail at the step with SPHGB_ERR_STATE /
  * SPHGB_ERR_ARGUMENT.
  *
@@ -384,6 +385,18 @@ int sphgb_get_volume_map(sphgb_ctx *ctx, uint32_t body, uint32_t resolution[3], 
                          double *distance, double *volume);
 int sphgb_clear_volume_maps(sphgb_ctx *ctx);
 int sphgb_set_boundary_method(sphgb_ctx *ctx, int method);
+/* Pose and velocity of the body of volume map `body` for the following steps, as the reference
+ * reads them from the map's rigid body every step (BoundaryModel_Bender2019 with a dynamic or
+ * animated RigidBodyObject): the map is sampled at R^T (x - t) (TimeStep.cpp:219-340), and the
+ * velocity of a body point p, w x (p - t) + v (BoundaryModel::getPointVelocity,
+ * BoundaryModel.h:78-84), enters every boundary term as v_i - v_p: the divergence source and the
+ * density advection (TimeStepDFSPH.cpp:1218-1238, 1273-1293), XSPH (XSPH.cpp:119-128),
+ * Weiler2018's right-hand side at its four samples (Viscosity_Weiler2018.cpp:1191-1243) and the
+ * forces on the body (its torque taken about t).  rotation (row-major) / translation NULL keep
+ * the current ones; velocity / omega NULL are zero.  Moving the body is the caller's rigid-body
+ * solver's job: call this before each step. */
+int sphgb_set_volume_map_motion(sphgb_ctx *ctx, uint32_t body, const double rotation[9], const double translation[3],
+                                const double velocity[3], const double omega[3]);
 
 /* the cudaStream_t every kernel of this context is launched on (for event timing by callers) */
 int sphgb_get_stream(const sphgb_ctx *ctx, void **stream);

@@ -60,6 +60,8 @@ class OrcVmap(ctypes.Structure):
         ("field", ctypes.c_void_p * 2),
         ("R", ctypes.c_double * 9),
         ("t", ctypes.c_double * 3),
+        ("v", ctypes.c_double * 3),
+        ("w", ctypes.c_double * 3),
     ]
 
 
@@ -300,6 +302,19 @@ class OracleSim:
         self.st.vmaps = ctypes.cast(self._vmap_arr, ctypes.c_void_p)
         self.st.nvmaps = len(self._vmaps)
         self.cp.boundary_method = 2
+
+    def set_map_motion(self, b, rotation=None, translation=None, velocity=(0, 0, 0), omega=(0, 0, 0)):
+        """pose and velocity of the body of volume map b for the next steps; a body's force center
+        follows its position"""
+        m = self._vmap_arr[b]
+        if rotation is not None:
+            m.R = (ctypes.c_double * 9)(*np.asarray(rotation, np.float64).ravel())
+        if translation is not None:
+            m.t = (ctypes.c_double * 3)(*np.asarray(translation, np.float64))
+            if getattr(self, "body_center", None) is not None and b < len(self.body_center):
+                self.body_center[b] = translation
+        m.v = (ctypes.c_double * 3)(*np.asarray(velocity, np.float64))
+        m.w = (ctypes.c_double * 3)(*np.asarray(omega, np.float64))
 
     def clear_forces(self):
         self.body_force[:] = 0.0

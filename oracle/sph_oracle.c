@@ -380,6 +380,29 @@ static void compute_factor(ctx_t *c)
 /* Fluid + boundary velocity divergence sum: the loops of computeDensityChange
  * (TimeStepDFSPH.cpp:1247-1295) and computeDensityAdv (:1190-1243); boundary
  * velocity is zero for static Akinci2012 walls. */
+/* BoundaryModel::getPointVelocity (BoundaryModel.h:78-84): the velocity w x (p - t) + v of point p
+ * of the body of boundary entry j; with volume maps the entry j = i * nbodies + b belongs to map b.
+ * Boundary particles are static walls here: zero. */
+static void boundary_point_velocity(const ctx_t *c, unsigned j, const double p[3], double out[3])
+{
+    const orc_state *s = c->s;
+    out[0] = out[1] = out[2] = 0.0;
+    if (c->p->boundary_method != 2 || !s->nvmaps) return;
+    const orc_vmap *m = s->vmaps + (j % s->nvmaps);
+    const double d[3] = {p[0] - m->t[0], p[1] - m->t[1], p[2] - m->t[2]};
+    out[0] = m->w[1] * d[2] - m->w[2] * d[1] + m->v[0];
+    out[1] = m->w[2] * d[0] - m->w[0] * d[2] + m->v[1];
+    out[2] = m->w[0] * d[1] - m->w[1] * d[0] + m->v[2];
+}
+
+/* ... at the boundary point x_j itself */
+static void boundary_velocity(const ctx_t *c, unsigned j, double out[3])
+{
+    const real *xb = c->s->xb + 3 * (size_t)j;
+    const double p[3] = {(double)xb[0], (double)xb[1], (double)xb[2]};
+    boundary_point_velocity(c, j, p, out);
+}
+
 static double velocity_divergence(const ctx_t *c, long i)
 {
     const orc_state *s = c->s;
@@ -394,12 +417,14 @@ static double velocity_divergence(const ctx_t *c, long i)
         acc += dot3(dv, g);
     }
     acc *= c->V;
+    /* (v_i - v_b) . gradW_ib, v_b the boundary point's velocity (TimeStepDFSPH.cpp:1218-1238) */
     for (unsigned k = c->B.off[i]; k < c->B.off[i + 1]; k++) {
         const unsigned j = c->B.idx[k];
-        double r[3], g[3];
+        double r[3], g[3], vb[3];
         diffv(xi, s->xb + 3 * (size_t)j, r);
         kGradW(&c->K, r, g);
-        const double dv[3] = {(double)vi[0], (double)vi[1], (double)vi[2]};
+        boundary_velocity(c, j, vb);
+        const double dv[3] = {(double)vi[0] - vb[0], (double)vi[1] - vb[1], (double)vi[2] - vb[2]};
         acc += (double)s->Vb[j] * dot3(dv, g);
     }
     return acc;
@@ -691,7 +716,9 @@ static void xsph(ctx_t *c, double h)
                 double r[3];
                 diffv(xi, s->xb + 3 * (size_t)j, r);
                 const double w = invH * cb * (c->rho0 * (double)s->Vb[j] / rhoi) * kW(&c->K, sqrt(dot3(r, r)));
-                for (int d = 0; d < 3; d++) ai[d] -= w * (double)vi[d];
+                double vb[3];
+                boundary_velocity(c, j, vb);
+                for (int d = 0; d < 3; d++) ai[d] -= w * ((double)vi[d] - vb[d]);
             }
         }
         for (int d = 0; d < 3; d++) s->a[3 * i + d] = (real)((double)s->a[3 * i + d] + ai[d]);
@@ -706,7 +733,9 @@ static void xsph(ctx_t *c, double h)
                 double r[3], f[3];
                 diffv(xi, s->xb + 3 * (size_t)j, r);
                 const double w = invH * cb * (c->rho0 * (double)s->Vb[j] / rhoi) * kW(&c->K, sqrt(dot3(r, r)));
-                for (int d = 0; d < 3; d++) f[d] = -c->mass * (-w * (double)vi[d]);
+                double vb[3];
+                boundary_velocity(c, j, vb);
+                for (int d = 0; d < 3; d++) f[d] = -c->mass * (-w * ((double)vi[d] - vb[d]));
                 add_force(c, j, f);
             }
         }
@@ -854,14 +883,38 @@ static void visc_diag_inverse(const visc_t *w, real *diag9, real *inv9)
     }
 }
 
-/* computeRHS (Viscosity_Weiler2018.cpp:1091-1254): b = v (static boundary
- * velocity is zero, so the boundary term vanishes), warm start g = v + vDiff. */
+/* computeRHS (Viscosity_Weiler2018.cpp:1091-1254): b = v - dt / rho_i sum_b (boundary term of
+ * the boundary's velocity), warm start g = v + vDiff.  Boundary particles are static walls (the
+ * term vanishes); a moving volume-map body contributes at its four samples per boundary point
+ * (:1191-1243). */
 static void visc_rhs(const visc_t *w, real *b, real *g)
 {
-    const orc_state *s = w->c->s;
+    const ctx_t *c = w->c;
+    const orc_state *s = c->s;
     for (size_t i = 0; i < 3 * (size_t)s->n; i++) {
         b[i] = s->v[i];
         g[i] = (real)((double)s->v[i] + (double)s->vdiff[i]);
+    }
+    if (w->mub == 0.0 || c->p->boundary_method != 2) return;
+    for (long i = 0; i < (long)s->n; i++) {
+        const real *xi = s->x + 3 * i;
+        double bi[3] = {0, 0, 0};
+        for (unsigned k = c->B.off[i]; k < c->B.off[i + 1]; k++) {
+            const unsigned j = c->B.idx[k];
+            double xs[4][3];
+            if (!vmap_samples(xi, s->xb + 3 * (size_t)j, c->K.h, xs)) continue;
+            const double vol = 0.25 * (double)s->Vb[j];
+            for (int q = 0; q < 4; q++) {
+                double r[3], gw[3], vk[3];
+                for (int d = 0; d < 3; d++) r[d] = (double)xi[d] - xs[q][d];
+                kGradW(&c->K, r, gw);
+                boundary_point_velocity(c, j, xs[q], vk);
+                const double f = w->d * w->mub * vol * dot3(vk, r) / (dot3(r, r) + 0.01 * w->h2);
+                for (int d = 0; d < 3; d++) bi[d] += f * gw[d];
+            }
+        }
+        const double rhoi = (double)s->density[i];
+        for (int d = 0; d < 3; d++) b[3 * i + d] = (real)((double)s->v[3 * i + d] - w->dt / rhoi * bi[d]);
     }
 }
 
@@ -978,10 +1031,12 @@ static int viscosity_weiler(ctx_t *c, double dt)
                     if (!vmap_samples(s->x + 3 * i, s->xb + 3 * (size_t)j, c->K.h, xs)) continue;
                     const double vol = 0.25 * (double)s->Vb[j];
                     for (int q = 0; q < 4; q++) {
-                        double r[3], g[3], f[3];
+                        double r[3], g[3], f[3], vk[3];
                         for (int d = 0; d < 3; d++) r[d] = (double)s->x[3 * i + d] - xs[q][d];
                         kGradW(&c->K, r, g);
-                        const double coef = 10.0 * mub * vol * dot3(nv, r) / (dot3(r, r) + 0.01 * h2);
+                        boundary_point_velocity(c, j, xs[q], vk);
+                        const double dv[3] = {nv[0] - vk[0], nv[1] - vk[1], nv[2] - vk[2]};
+                        const double coef = 10.0 * mub * vol * dot3(dv, r) / (dot3(r, r) + 0.01 * h2);
                         for (int d = 0; d < 3; d++) f[d] = -c->mass / rhoi * (coef * g[d]);
                         add_force_at(c, j, xs[q], f);
                     }

@@ -69,6 +69,9 @@ typedef struct orc_vmap {
     unsigned res[3];
     double *field[2];            /* orc_vmap_nodes(res) values each */
     double R[9], t[3];           /* rotation (row-major) and position of the body */
+    double v[3], w[3];           /* its linear and angular velocity: the velocity of a point p of the
+                                    body is w x (p - t) + v (BoundaryModel::getPointVelocity,
+                                    BoundaryModel.h:78-84); zero for a static body */
 } orc_vmap;
 
 typedef struct orc_state {

@@ -107,10 +107,11 @@ struct sphgb_ctx {
     uint32_t lpp_fixed = 0;            // 0: autotune on the first step after an upload
     bool tuned = false;
     float tune_ms[4] = {0, 0, 0, 0};   // trial step times of lanes per particle 1, 2, 4 and of staged passes
-    // Bender2019 boundary: volume maps of static bodies (own allocations, kept across uploads)
+    // Bender2019 boundary: volume maps of the bodies (own allocations, kept across uploads)
     struct VMap {
         uint32_t res[3];
         double dmin[3], dmax[3], R[9], t[3];
+        double v[3] = {0, 0, 0}, w[3] = {0, 0, 0};   // the body's velocity and angular velocity
         double support;                // support radius the map was built for
         double *f0 = nullptr, *f1 = nullptr;   // node fields (FP64)
         void *coef = nullptr;                  // per-cell coefficients in the context's precision
@@ -119,6 +120,9 @@ struct sphgb_ctx {
     std::vector<VMap> vmaps;
     void *d_vmaps = nullptr;           // VMapDev<T>[vmaps.size()]
     void *bx = nullptr;                // prepared set: [maps][np] boundary points
+    void *bv = nullptr;                // prepared set: [np] boundary velocity sums of moving maps
+    bool vmove = false;                // some map has a velocity
+    bool vmaps_dirty = false;          // poses or velocities changed since the device copy
     // neighbourhood staging of the solver passes (FP32, one lane per particle)
     int stage_mode = 0;                // 0: the autotuner decides, 1: off, 2: on
     bool staged = false;               // in use
@@ -272,6 +276,7 @@ void free_prepared(sphgb_ctx *c)
     c->bodies.nblk = 0;
     c->bodies.vpartials = nullptr;
     c->bx = nullptr;
+    c->bv = nullptr;
     c->prepared = false;
 }
 
@@ -404,6 +409,7 @@ template <class T> DevParams<T> make_params(const sphgb_ctx *c)
     P.staged = (c->staged && !c->fp64 && c->lpp_log2 == 0 && c->ll) ? 1 : 0;
     P.nvmaps = (c->boundary_method == 2 && c->bx) ? (uint32_t)c->vmaps.size() : 0u;
     P.vmaps = static_cast<const VMapDev<T> *>(c->d_vmaps);
+    P.vmove = (P.nvmaps && c->vmove && c->bv) ? 1 : 0;
     return P;
 }
 
@@ -446,6 +452,7 @@ template <class T> DevBufs<T> make_bufs(const sphgb_ctx *c, int view)
     B.stage_off = c->stage_off;
     B.stage_src = c->stage_src;
     B.bx = (v4 *)c->bx;
+    B.bv = (v4 *)c->bv;
     B.ll = c->ll;
     B.key = c->key;
     B.key2 = c->key2;
@@ -664,6 +671,7 @@ template <class T> int prepare(sphgb_ctx *c)
     if ((rc = build_body_tables(c))) return rc;
     if (c->boundary_method == 2 && !c->vmaps.empty()) {
         if ((rc = palloc(c, &c->bx, (size_t)std::max(c->np, 1u) * c->vmaps.size() * vec_size(c)))) return rc;
+        if ((rc = palloc(c, &c->bv, (size_t)std::max(c->np, 1u) * vec_size(c)))) return rc;
         if (c->nbodies) {   // block partials of the volume-map body forces
             const size_t nblk = (std::max(c->np, 1u) + kBlock - 1) / kBlock;
             if ((rc = palloc(c, &c->bodies.vpartials, (size_t)c->nbodies * 6 * nblk * sizeof(double)))) return rc;
@@ -985,7 +993,7 @@ template <class T> int autotune(sphgb_ctx *c)
     return SPHGB_OK;
 }
 
-// The Bender2019 configurations this path supports: one scene, static bodies given only as volume
+// The Bender2019 configurations this path supports: one scene, bodies given only as volume
 // maps built for the current support radius, forces collected with one body per map.
 int check_boundary_method(sphgb_ctx *c)
 {
@@ -1001,12 +1009,9 @@ int check_boundary_method(sphgb_ctx *c)
     return SPHGB_OK;
 }
 
-// the maps as the step reads them (VMapDev<T>), uploaded after any change
-template <class T> int upload_vmaps(sphgb_ctx *c)
+// the maps as the step reads them (VMapDev<T>)
+template <class T> std::vector<VMapDev<T>> vmap_dev_array(const sphgb_ctx *c)
 {
-    if (c->d_vmaps) cudaFree(c->d_vmaps);
-    c->d_vmaps = nullptr;
-    if (c->vmaps.empty()) return SPHGB_OK;
     std::vector<VMapDev<T>> h(c->vmaps.size());
     for (size_t b = 0; b < c->vmaps.size(); b++) {
         const auto &m = c->vmaps[b];
@@ -1016,14 +1021,38 @@ template <class T> int upload_vmaps(sphgb_ctx *c)
             d.dmax[k] = (T)m.dmax[k];
             d.cs[k] = (T)((m.dmax[k] - m.dmin[k]) / (double)m.res[k]);
             d.t[k] = (T)m.t[k];
+            d.v[k] = (T)m.v[k];
+            d.w[k] = (T)m.w[k];
             d.res[k] = m.res[k];
         }
         for (int k = 0; k < 9; k++) d.R[k] = (T)m.R[k];
         d.pad = 0;
         d.coef = static_cast<const T *>(m.coef);
     }
+    return h;
+}
+
+// uploaded after a map is added or removed
+template <class T> int upload_vmaps(sphgb_ctx *c)
+{
+    if (c->d_vmaps) cudaFree(c->d_vmaps);
+    c->d_vmaps = nullptr;
+    c->vmaps_dirty = false;
+    if (c->vmaps.empty()) return SPHGB_OK;
+    const std::vector<VMapDev<T>> h = vmap_dev_array<T>(c);
     CK(cudaMalloc(&c->d_vmaps, h.size() * sizeof(VMapDev<T>)));
     CK(cudaMemcpy(c->d_vmaps, h.data(), h.size() * sizeof(VMapDev<T>), cudaMemcpyHostToDevice));
+    return SPHGB_OK;
+}
+
+// new poses and velocities, copied in place on the step stream before the next step (captured
+// graphs keep the array's address)
+template <class T> int refresh_vmaps(sphgb_ctx *c)
+{
+    c->vmaps_dirty = false;
+    if (!c->d_vmaps || c->vmaps.empty()) return SPHGB_OK;
+    const std::vector<VMapDev<T>> h = vmap_dev_array<T>(c);
+    CK(cudaMemcpyAsync(c->d_vmaps, h.data(), h.size() * sizeof(VMapDev<T>), cudaMemcpyHostToDevice, c->stream));
     return SPHGB_OK;
 }
 
@@ -1032,6 +1061,7 @@ template <class T> int do_step(sphgb_ctx *c)
     int rc;
     if ((rc = check_boundary_method(c))) return rc;
     if (!c->prepared && (rc = prepare<T>(c))) return rc;
+    if (c->vmaps_dirty && (rc = refresh_vmaps<T>(c))) return rc;
     if ((rc = upload_scalars(c))) return rc;
     if (!c->tuned) {
         if (c->lpp_fixed) {
@@ -1951,6 +1981,46 @@ int sphgb_clear_volume_maps(sphgb_ctx *c)
     free_vmaps(c);
     c->prepared = false;
     invalidate_graphs(c);
+    return SPHGB_OK;
+}
+
+int sphgb_set_volume_map_motion(sphgb_ctx *c, uint32_t body, const double rotation[9], const double translation[3],
+                                const double velocity[3], const double omega[3])
+{
+    if (!c) return SPHGB_ERR_ARGUMENT;
+    if (body >= c->vmaps.size()) return fail(c, SPHGB_ERR_ARGUMENT, "no such volume map");
+    int rc;
+    if ((rotation && (rc = check_finite(c, rotation, 9, "map rotation"))) ||
+        (translation && (rc = check_finite(c, translation, 3, "map translation"))) ||
+        (velocity && (rc = check_finite(c, velocity, 3, "body velocity"))) ||
+        (omega && (rc = check_finite(c, omega, 3, "body angular velocity"))))
+        return rc;
+    if (c->step_pending) {
+        sphgb_stats st;
+        fill_stats(c, &st);
+    }
+    cudaSetDevice(c->cfg.device);
+    sphgb_ctx::VMap &m = c->vmaps[body];
+    if (rotation) std::copy(rotation, rotation + 9, m.R);
+    if (translation) std::copy(translation, translation + 3, m.t);
+    for (int k = 0; k < 3; k++) {
+        m.v[k] = velocity ? velocity[k] : 0.0;
+        m.w[k] = omega ? omega[k] : 0.0;
+    }
+    bool move = false;
+    for (const auto &q : c->vmaps)
+        for (int k = 0; k < 3; k++) move = move || q.v[k] != 0.0 || q.w[k] != 0.0;
+    if (move != c->vmove) {   // the kernels' parameters change
+        c->vmove = move;
+        invalidate_graphs(c);
+    }
+    c->vmaps_dirty = true;
+    // a body's torque is taken about its position
+    if (translation && c->nbodies == c->vmaps.size() && c->bodies.center) {
+        std::copy(translation, translation + 3, c->body_center.begin() + 3 * (size_t)body);
+        CK(cudaMemcpyAsync(const_cast<double *>(c->bodies.center) + 3 * (size_t)body, c->body_center.data() + 3 * (size_t)body,
+                           3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    }
     return SPHGB_OK;
 }
 

@@ -557,6 +557,15 @@ __global__ void __launch_bounds__(kBlock) k_vmap_boundary(DevParams<T> P, DevBuf
     }
 }
 
+// BoundaryModel::getPointVelocity (BoundaryModel.h:78-84): velocity w x (p - t) + v of point p of
+// the body of volume map m
+template <class T> __device__ __forceinline__ V3<T> vmap_point_velocity(const VMapDev<T> &m, const V3<T> &p)
+{
+    const T dx = p.x - m.t[0], dy = p.y - m.t[1], dz = p.z - m.t[2];
+    return mk3<T>(m.w[1] * dz - m.w[2] * dy + m.v[0], m.w[2] * dx - m.w[0] * dz + m.v[1],
+                  m.w[0] * dy - m.w[1] * dx + m.v[2]);
+}
+
 // Build the fluid and boundary neighbour lists of particle i and, in the same
 // kernel, compute (TimeStep.cpp:116-169) the density, (TimeStepDFSPH.cpp:1106-1186)
 // the DFSPH factor alpha, (TimeStepDFSPH.cpp:1247-1295) the divergence source and
@@ -689,10 +698,28 @@ __device__ __forceinline__ void build_one(const DevParams<T> &P, const DevBufs<T
         divb += dot(vi, g);
     };
     nbr_loop<kUnroll>(Lb, min(nb, P.capb), [&](uint32_t j) { return ldv(B.xb, j); }, boundary_term);
-    // Bender2019: the volume-map sample of each body, x_j with V_j in w, where V_j > 0
+    // Bender2019: the volume-map sample of each body, x_j with V_j in w, where V_j > 0; a moving
+    // body's point velocity v_j enters as sum V_j v_j . gradW (divergence source, density
+    // advection) and sum V_j W v_j (XSPH), both fixed for the step
+    V3<T> bvw = mk3<T>(0, 0, 0);
+    T bvg = T(0);
     for (uint32_t b = 0; b < P.nvmaps; b++) {
         const v4_t<T> xj = ldv(B.bx, b * P.np + i);
-        if ((T)xj.w > T(0)) boundary_term(b, xj);
+        if ((T)xj.w > T(0)) {
+            boundary_term(b, xj);
+            if (P.vmove) {
+                const V3<T> vj = vmap_point_velocity<T>(P.vmaps[b], xyz<T>(xj));
+                const V3<T> r = diff3<T>(xi, xj);
+                T W, c;
+                kernel_W_coef_d2(P.K, dot(r, r), W, c);
+                bvw = add(bvw, scl(vj, (T)xj.w * W));
+                bvg += dot(vj, scl(r, c * (T)xj.w));
+            }
+        }
+    }
+    if (P.vmove) {
+        divb -= bvg;
+        stv(B.bv, i, pack(bvw, bvg));
     }
     B.nf[i] = nf;
     B.nbn[i] = nb;
@@ -1148,7 +1175,12 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams<T> P, DevBufs<T> B, i
     if (P.xsph_b != T(0)) {
         // sum_b (rho0 V_b / rho_i) W_ib from the per-step boundary sum
         const T wsum = P.rho0 * (T)ldv(B.bg, i).w / B.density[i];
-        ai = sub(ai, scl(vi, invH * P.xsph_b * wsum));
+        if (P.vmove) {   // moving volume-map bodies: (v_i - v_b) W
+            const V3<T> dv = sub(scl(vi, (T)ldv(B.bg, i).w), xyz<T>(ldv(B.bv, i)));
+            ai = sub(ai, scl(dv, invH * P.xsph_b * P.rho0 / B.density[i]));
+        } else {
+            ai = sub(ai, scl(vi, invH * P.xsph_b * wsum));
+        }
     }
     stv(B.a, i, pack(ai, T(0)));
     if (div_on) B.kappa_v[i] *= h;
@@ -1246,6 +1278,7 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T
     mine.v[0] = mine.v[1] = mine.v[2] = 0.0;
     T m[6] = {0, 0, 0, 0, 0, 0};   // m00 m01 m02 m11 m12 m22
     V3<T> acc = mk3<T>(0, 0, 0);
+    V3<T> bb = mk3<T>(0, 0, 0);    // moving volume-map bodies: boundary term of the right-hand side (lane 0)
     v4_t<T> xi{}, gi4{};
     T rhoi = T(1);
     if (q.act) {
@@ -1286,6 +1319,8 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T
                         const T f = P.vd * P.mub * vol / (r2 + eps2) * grad_coef_d2(P.K, r2);
                         m[0] += f * r.x * r.x; m[1] += f * r.x * r.y; m[2] += f * r.x * r.z;
                         m[3] += f * r.y * r.y; m[4] += f * r.y * r.z; m[5] += f * r.z * r.z;
+                        // computeRHS (:1191-1243): the samples' velocities
+                        if (P.vmove) bb = add(bb, scl(r, f * dot(vmap_point_velocity<T>(P.vmaps[b], xk), r)));
                     });
                 }
             acc = add(acc, weiler_boundary<LPP>(P, B, q, xi, rhoi, gi));
@@ -1310,7 +1345,8 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T
         stv(B.inv0, i, i0);
         stv(B.inv1, i, i1);
 
-        const V3<T> vi = xyz<T>(ldv(B.v, i));
+        V3<T> vi = xyz<T>(ldv(B.v, i));   // b = v_i - dt / rho_i (boundary velocity term)
+        if (P.vmove) vi = sub(vi, scl(bb, s));
         const V3<T> Ag = sub(gi, scl(acc, s));
         const V3<T> r = sub(vi, Ag);
         const V3<T> p = sym_mul<T>(i0, i1, r);
@@ -1575,7 +1611,8 @@ __global__ void __launch_bounds__(kBlock) k_press_init(DevParams<T> P, DevBufs<T
     if (!q.act || q.l != 0) return;
     const uint32_t i = q.i;
     const T h = (T)B.sc[q.s].dt_next;
-    const T accb = dot(vi, xyz<T>(ldv(B.bg, i)));
+    T accb = dot(vi, xyz<T>(ldv(B.bg, i)));
+    if (P.vmove) accb -= (T)ldv(B.bv, i).w;   // moving volume-map bodies: (v_i - v_b) . gradW
     const T dadv = B.density[i] / P.rho0 + h * (accf * P.V + accb);
     B.dadv[i] = dadv;
     const T invH2 = T(1) / (h * h);
@@ -1767,10 +1804,13 @@ __global__ void __launch_bounds__(kBlock) k_vmap_forces(DevParams<T> P, DevBufs<
                 const T d2 = dot(r, r);
                 V3<T> f = mk3<T>(0, 0, 0);
                 if (press && fabs(kap) > P.eps) f = scl(r, P.mass * kap * Vj * grad_coef_d2(P.K, d2));
+                const VMapDev<T> &mp = P.vmaps[b];
                 if (xs) {
                     const T w = P.mass * P.xsph_b / (T)B.sc[q.s].dt * P.rho0 * Vj / B.density[i] *
                                 kernel_W(P.K, dev_sqrt(d2));
-                    f = add(f, scl(xyz<T>(ldv(B.v, i)), w));
+                    V3<T> dv = xyz<T>(ldv(B.v, i));
+                    if (P.vmove) dv = sub(dv, vmap_point_velocity<T>(mp, xyz<T>(xj)));
+                    f = add(f, scl(dv, w));
                 }
                 const double *c = D.center + 3 * (size_t)b;
                 const double px = (double)xj.x - c[0], py = (double)xj.y - c[1], pz = (double)xj.z - c[2];
@@ -1788,7 +1828,9 @@ __global__ void __launch_bounds__(kBlock) k_vmap_forces(DevParams<T> P, DevBufs<
                     vmap_samples<T>(xk, xj, P.K.h, [&](const V3<T> &xs4) {
                         const V3<T> r4 = sub(xyz<T>(xk), xs4);
                         const T r2 = dot(r4, r4);
-                        const T a = P.vd * P.mub * vol * dot(nv, r4) / (r2 + eps2) * grad_coef_d2(P.K, r2);
+                        V3<T> dv = nv;
+                        if (P.vmove) dv = sub(dv, vmap_point_velocity<T>(mp, xs4));
+                        const T a = P.vd * P.mub * vol * dot(dv, r4) / (r2 + eps2) * grad_coef_d2(P.K, r2);
                         const V3<T> g = scl(r4, -P.mass / rhoi * a);
                         const double gx = (double)g.x, gy = (double)g.y, gz = (double)g.z;
                         const double qx = (double)xs4.x - c[0], qy = (double)xs4.y - c[1], qz = (double)xs4.z - c[2];

@@ -90,6 +90,7 @@ template <class T> struct DevParams {
                                   // also fixes the layout of the fluid lists
     uint32_t nvmaps;              // Bender2019 boundary: volume maps (bodies); 0 = Akinci2012 particles
     const VMapDev<T> *vmaps;      // device array [nvmaps]
+    int vmove;                    // some volume-map body moves: boundary terms use v_i - v_b
     int staged;                   // FP32, one lane per particle: the solver passes read their block's
                                   // neighbourhood from shared memory (stage tables, local lists)
 };
@@ -131,6 +132,8 @@ template <class T> struct DevBufs {
     v4 *xk;                      // x_i with the running solver's kappa_i in w (one gather per pair)
     v4 *bg;                      // per-particle boundary sums: xyz = sum_b V_b gradW_ib, w = sum_b V_b W_ib
     v4 *bx;                      // Bender2019: [nvmaps][np] boundary point x_j of each particle's map sample, w = V_j
+    v4 *bv;                      // moving volume-map bodies, per particle: xyz = sum_b V_b W_ib v_b,
+                                 // w = sum_b V_b v_b . gradW_ib (fixed for the step, like bg)
     T *density, *factor, *dadv;
     uint32_t *nf, *nbn;
     uint32_t *lf, *lb;

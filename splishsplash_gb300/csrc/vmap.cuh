@@ -122,11 +122,12 @@ __host__ __device__ __forceinline__ bool vmap_locate(const T dmin[3], const T dm
     return true;
 }
 
-// Volume map of one static body as the per-step kernel reads it: the 32 (distance, volume)
+// Volume map of one body as the per-step kernel reads it: the 32 (distance, volume)
 // coefficients of each cell stored together.
 template <class T> struct VMapDev {
     T dmin[3], dmax[3], cs[3];   // body-local grid box and cell size
     T R[9], t[3];                // rotation (row-major) and position: x_local = R^T (x - t)
+    T v[3], w[3];                // linear and angular velocity of the body: point p moves at w x (p - t) + v
     uint32_t res[3];
     uint32_t pad;
     const T *coef;               // [cells][32][2]

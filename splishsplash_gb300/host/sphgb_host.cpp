@@ -93,6 +93,17 @@ void BoundaryModel_Akinci2012::clearForceAndTorque()
     if (m_owner && m_rigidBody.isDynamic()) m_owner->clearBodyForceAndTorque(m_index);
 }
 
+void BoundaryModel_Bender2019::getForceAndTorque(Vector3r &force, Vector3r &torque)
+{
+    force = torque = Vector3r();
+    if (m_owner && m_rigidBody.isDynamic()) m_owner->bodyForceAndTorque(m_index, force, torque);
+}
+
+void BoundaryModel_Bender2019::clearForceAndTorque()
+{
+    if (m_owner && m_rigidBody.isDynamic()) m_owner->clearBodyForceAndTorque(m_index);
+}
+
 TimeStepDFSPH_GB300::TimeStepDFSPH_GB300(FluidModel &model, BoundaryModel_Akinci2012 &boundary,
                                          const SimulationParameters &sim, Viscosity_Weiler2018_GB300 *viscosity,
                                          int device, bool useGraph)
@@ -114,9 +125,15 @@ TimeStepDFSPH_GB300::TimeStepDFSPH_GB300(FluidModel &model, const std::vector<Bo
                                          int device, bool useGraph)
     : m_model(model), m_volumeMaps(volumeMaps), m_sim(sim), m_visco(viscosity)
 {
-    for (BoundaryModel_Bender2019 *b : m_volumeMaps)
+    for (BoundaryModel_Bender2019 *b : m_volumeMaps) {
         if (!b) throw Error(SPHGB_ERR_ARGUMENT, "null boundary model");
+        if (b->m_owner) throw Error(SPHGB_ERR_STATE, "boundary model already belongs to a time step");
+    }
     createContext(device, useGraph);
+    for (unsigned int k = 0; k < m_volumeMaps.size(); k++) {
+        m_volumeMaps[k]->m_owner = this;
+        m_volumeMaps[k]->m_index = k;
+    }
 }
 
 void TimeStepDFSPH_GB300::createContext(int device, bool useGraph)
@@ -145,13 +162,14 @@ void TimeStepDFSPH_GB300::createContext(int device, bool useGraph)
 TimeStepDFSPH_GB300::~TimeStepDFSPH_GB300()
 {
     for (BoundaryModel_Akinci2012 *b : m_boundaries) b->m_owner = nullptr;
+    for (BoundaryModel_Bender2019 *b : m_volumeMaps) b->m_owner = nullptr;
     if (m_ctx) sphgb_destroy(m_ctx);
 }
 
 void TimeStepDFSPH_GB300::bodyForceAndTorque(unsigned int body, Vector3r &force, Vector3r &torque)
 {
     if (!m_bodiesSet) return;
-    std::vector<double> f(3 * m_boundaries.size()), t(3 * m_boundaries.size());
+    std::vector<double> f(3 * (size_t)numberOfBodies()), t(3 * (size_t)numberOfBodies());
     check(sphgb_boundary_forces(m_ctx, f.data(), t.data()), "sphgb_boundary_forces");
     for (int d = 0; d < 3; d++) {
         force[d] = (Real)f[3 * body + d];
@@ -254,6 +272,19 @@ void TimeStepDFSPH_GB300::upload()
                   "sphgb_add_volume_map");
         }
         check(sphgb_set_boundary_method(m_ctx, 2), "sphgb_set_boundary_method");
+        // map k is body k; forces only where a body is dynamic
+        std::vector<double> center;
+        std::vector<int> dynamic;
+        bool anyDynamic = false;
+        for (BoundaryModel_Bender2019 *bm : m_volumeMaps) {
+            for (int d = 0; d < 3; d++) center.push_back((double)bm->m_rigidBody.getPosition()[d]);
+            dynamic.push_back(bm->m_rigidBody.isDynamic() ? 1 : 0);
+            anyDynamic = anyDynamic || bm->m_rigidBody.isDynamic();
+        }
+        check(sphgb_set_boundary_bodies(m_ctx, nullptr, anyDynamic ? (uint32_t)m_volumeMaps.size() : 0u, center.data(),
+                                        dynamic.data()),
+              "sphgb_set_boundary_bodies");
+        m_bodiesSet = anyDynamic;
         m_boundaryDirty = false;
     }
     if (m_boundaryDirty) {
@@ -292,9 +323,28 @@ void TimeStepDFSPH_GB300::upload()
     m_dirty = false;
 }
 
+// the current pose and velocities of every dynamic or animated volume-map body
+// (TimeStep.cpp:238-240 reads R and t from the rigid body each step; BoundaryModel.h:78-84)
+void TimeStepDFSPH_GB300::pushBodyMotion()
+{
+    for (unsigned int k = 0; k < m_volumeMaps.size(); k++) {
+        const RigidBodyObject &rb = m_volumeMaps[k]->m_rigidBody;
+        if (!rb.isDynamic() && !rb.isAnimated()) continue;
+        double R[9], t[3], v[3], w[3];
+        for (int q = 0; q < 9; q++) R[q] = (double)m_volumeMaps[k]->m_rotation[q];
+        for (int d = 0; d < 3; d++) {
+            t[d] = (double)rb.getPosition()[d];
+            v[d] = (double)rb.getVelocity()[d];
+            w[d] = (double)rb.getAngularVelocity()[d];
+        }
+        check(sphgb_set_volume_map_motion(m_ctx, k, R, t, v, w), "sphgb_set_volume_map_motion");
+    }
+}
+
 void TimeStepDFSPH_GB300::step()
 {
     if (m_dirty) upload();
+    pushBodyMotion();
     check(sphgb_step(m_ctx, &m_stats), "sphgb_step");
     m_iterations = m_stats.iterations;
     m_iterationsV = m_stats.iterations_v;

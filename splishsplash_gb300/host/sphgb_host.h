@@ -95,12 +95,18 @@ private:
 // (RigidBodyObject.h: getPosition, isDynamic): the reference point of the torques and
 // whether the body collects the fluid's forces.
 struct RigidBodyObject {
-    Vector3r m_position;
-    bool m_isDynamic = false;
+    Vector3r m_position, m_velocity, m_angularVelocity;
+    bool m_isDynamic = false, m_isAnimated = false;
     const Vector3r &getPosition() const { return m_position; }
     void setPosition(const Vector3r &x) { m_position = x; }
+    const Vector3r &getVelocity() const { return m_velocity; }
+    void setVelocity(const Vector3r &v) { m_velocity = v; }
+    const Vector3r &getAngularVelocity() const { return m_angularVelocity; }
+    void setAngularVelocity(const Vector3r &w) { m_angularVelocity = w; }
     bool isDynamic() const { return m_isDynamic; }
     void setDynamic(bool d) { m_isDynamic = d; }
+    bool isAnimated() const { return m_isAnimated; }
+    void setAnimated(bool a) { m_isAnimated = a; }
 };
 
 class TimeStepDFSPH_GB300;
@@ -180,6 +186,16 @@ public:
         m_faces.assign(faces, faces + 3 * (size_t)nFaces);
     }
     RigidBodyObject *getRigidBodyObject() { return &m_rigidBody; }
+    // forces of a dynamic body (BoundaryModel.h:86-87); a dynamic or animated body's pose
+    // (m_rotation, position) and velocities are handed to the device before every step, as the
+    // reference reads them from the rigid body
+    void getForceAndTorque(Vector3r &force, Vector3r &torque);
+    void clearForceAndTorque();
+
+private:
+    friend class TimeStepDFSPH_GB300;
+    TimeStepDFSPH_GB300 *m_owner = nullptr;
+    unsigned int m_index = 0;
 };
 
 // The DFSPH time step on the GPU (TimeStepDFSPH.cpp:117-249)
@@ -247,11 +263,17 @@ public:
 
 protected:
     friend class BoundaryModel_Akinci2012;
+    friend class BoundaryModel_Bender2019;
     void check(int rc, const char *what);
     void upload();
     void applyParameters();
     void createContext(int device, bool useGraph);
     void bodyForceAndTorque(unsigned int body, Vector3r &force, Vector3r &torque);
+    unsigned int numberOfBodies() const
+    {
+        return (unsigned int)(m_volumeMaps.empty() ? m_boundaries.size() : m_volumeMaps.size());
+    }
+    void pushBodyMotion();
     void clearBodyForceAndTorque(unsigned int body);
 
     FluidModel &m_model;

@@ -8,11 +8,13 @@
 // bodies (0/1), volume map (0/1); float64 particle radius; float64 x[n][3], v[n][3], xb[nb][3];
 // with bodies: uint32 body[nb] (0: the dynamic body, 1: static walls) and float64 position[3]
 // of the dynamic body; with a volume map (then nb = 0): uint32 nv, nf, resolution[3], invert,
-// float64 vertices[nv][3], uint32 faces[nf][3] of the container (Bender2019 boundary).
+// float64 vertices[nv][3], uint32 faces[nf][3] of the container (Bender2019 boundary); with a
+// volume map and bodies, the container is a dynamic body at the position above moving with
+// float64 velocity[3] and angular velocity[3] (its pose is held, so the run stays comparable).
 // out.bin: per step uint32 iterations, iterationsV, viscoIterations and float64 time;
 // then float64 x[n][3], v[n][3], density[n], p / rho^2 [n], boundary volume[nb] (in the
-// order of the boundary models: body 0's particles first), force[3], torque[3] of body 0
-// summed over all steps (getForceAndTorque; zeros without bodies).
+// order of the boundary models: body 0's particles first), force[3], torque[3] of body 0 (the
+// container with a volume map) summed over all steps (getForceAndTorque; zeros without bodies).
 #include <cstdint>
 #include <cstdio>
 #include <memory>
@@ -57,11 +59,13 @@ int main(int argc, char **argv)
     uint32_t mh[6] = {0, 0, 0, 0, 0, 0};
     std::vector<double> mv;
     std::vector<uint32_t> mf;
+    double bvel[6] = {0, 0, 0, 0, 0, 0};
     if (vmap) {
         if (!rd(f, mh, 6)) return 2;
         mv.resize(3 * (size_t)mh[0]);
         mf.resize(3 * (size_t)mh[1]);
         if (!rd(f, mv.data(), mv.size()) || !rd(f, mf.data(), mf.size())) return 2;
+        if (bodies && !rd(f, bvel, 6)) return 2;
     }
     fclose(f);
 
@@ -94,6 +98,13 @@ int main(int argc, char **argv)
             container.initModel(mh[0], mvv.data(), mh[1], mf.data());
             for (int k = 0; k < 3; k++) container.m_mapResolution[k] = mh[2 + k];
             container.m_mapInvert = mh[5] != 0;
+            if (bodies) {
+                RigidBodyObject *rb = container.getRigidBodyObject();
+                rb->setPosition(Vector3r((Real)pos[0], (Real)pos[1], (Real)pos[2]));
+                rb->setDynamic(true);
+                rb->setVelocity(Vector3r((Real)bvel[0], (Real)bvel[1], (Real)bvel[2]));
+                rb->setAngularVelocity(Vector3r((Real)bvel[3], (Real)bvel[4], (Real)bvel[5]));
+            }
         }
         std::unique_ptr<TimeStepDFSPH_GB300> tsp(
             vmap ? new TimeStepDFSPH_GB300(model, std::vector<BoundaryModel_Bender2019 *>{&container}, sp,
@@ -124,7 +135,10 @@ int main(int argc, char **argv)
         for (BoundaryModel_Akinci2012 *bm : boundaries)
             for (uint32_t i = 0; i < bm->numberOfParticles(); i++) out.push_back(bm->getVolume(i));
         Vector3r force, torque;
-        models[0].getForceAndTorque(force, torque);
+        if (vmap)
+            container.getForceAndTorque(force, torque);
+        else
+            models[0].getForceAndTorque(force, torque);
         for (int c = 0; c < 3; c++) out.push_back(force[c]);
         for (int c = 0; c < 3; c++) out.push_back(torque[c]);
         wr(o, out.data(), out.size());

@@ -15,7 +15,7 @@ from splishsplash_gb300 import build, scenes
 from splishsplash_gb300.dfsph import TimeStepDFSPH
 
 
-def _write_scene(path, sc, steps, lanes, visc, body=None, position=None, vmap=None):
+def _write_scene(path, sc, steps, lanes, visc, body=None, position=None, vmap=None, motion=None):
     with open(path, "wb") as f:
         f.write(struct.pack("<7I", sc.n, sc.nb, steps, lanes, 1 if visc else 0, 0 if body is None else 1,
                             0 if vmap is None else 1))
@@ -30,6 +30,8 @@ def _write_scene(path, sc, steps, lanes, visc, body=None, position=None, vmap=No
             f.write(struct.pack("<6I", len(verts), len(faces), *[int(r) for r in res], 1))
             f.write(np.ascontiguousarray(verts, "<f8").tobytes())
             f.write(np.ascontiguousarray(faces, "<u4").tobytes())
+            if body is not None:
+                f.write(np.ascontiguousarray(motion, "<f8").tobytes())
 
 
 def _read_out(path, n, nb, steps):
@@ -68,8 +70,10 @@ def test_host_layer_is_built_and_fails_cleanly_without_a_device():
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("visc,bodies,vmap", [(False, False, False), (True, False, False), (True, True, False),
-                                              (True, False, True)])
+                                              (True, False, True), (True, True, True)])
 def test_cpp_host_layer_matches_python_mirror(visc, bodies, vmap):
+    """with a volume map and bodies the container is a dynamic body with a velocity and an angular
+    velocity (pose held): the C++ layer hands them to the device before every step"""
     sc = scenes.small_block(counts=(10, 12, 10), box=(0.8, 1.0, 0.8), viscosity=visc,
                             velocity=(0.3, 0.0, -0.2)).as_float32()
     # the C++ layer holds every real parameter in Real (float), like the reference's FP32 build
@@ -81,8 +85,12 @@ def test_cpp_host_layer_matches_python_mirror(visc, bodies, vmap):
     p.gravitation = tuple(f32(g) for g in p.gravitation)
     p.viscoMaxError = f32(1e-3)
     steps, lanes = 12, 1
-    body = position = None
-    if bodies:
+    body = position = motion = None
+    if bodies and vmap:
+        body = np.zeros(0, np.uint32)
+        position = np.zeros(3)
+        motion = np.array([0.125, 0.0, -0.0625, 0.0, 0.25, 0.0])   # exact in float
+    elif bodies:
         # the floor is a dynamic body (boundary model 0), the other walls are static (model 1)
         body = np.where(sc.xb[:, 1] < 1e-9, 0, 1).astype(np.uint32)
         position = np.array([0.375, 0.0, 0.4375], np.float64)   # exact in float (the C++ layer holds Real)
@@ -93,13 +101,13 @@ def test_cpp_host_layer_matches_python_mirror(visc, bodies, vmap):
         verts, faces = scenes.box_mesh((0, 0, 0), (0.75, 1.0, 0.75))   # exact in float (the C++ Real)
         mesh = (verts, faces, (8, 10, 8))
     with tempfile.TemporaryDirectory() as d:
-        _write_scene(os.path.join(d, "s.bin"), sc, steps, lanes, visc, body, position, mesh)
+        _write_scene(os.path.join(d, "s.bin"), sc, steps, lanes, visc, body, position, mesh, motion)
         r = subprocess.run([build.HOST_DEMO, os.path.join(d, "s.bin"), os.path.join(d, "o.bin")],
                            capture_output=True, text=True, timeout=300)
         assert r.returncode == 0, r.stderr
         assert r.stdout.startswith("DFSPH:")
         per, x, v, rho, kp, vb, force, torque = _read_out(os.path.join(d, "o.bin"), sc.n, sc.nb, steps)
-    if bodies:
+    if bodies and not vmap:
         # the C++ layer uploads the boundary models in order: body 0's particles first
         order = np.concatenate([np.flatnonzero(body == 0), np.flatnonzero(body != 0)])
         sc = dataclasses.replace(sc, xb=sc.xb[order])
@@ -108,9 +116,13 @@ def test_cpp_host_layer_matches_python_mirror(visc, bodies, vmap):
     if vmap:
         ts.ctx.add_volume_map(mesh[0], mesh[1], mesh[2], invert=True)
         ts.ctx.set_boundary_method(2)
-    if bodies:
+    if bodies and vmap:
+        ts.ctx.set_boundary_bodies(None, position.reshape(1, 3))
+    elif bodies:
         ts.ctx.set_boundary_bodies(np.sort(body), np.stack([position, np.zeros(3)]), [1, 0])
     for k in range(steps):
+        if bodies and vmap:
+            ts.ctx.set_volume_map_motion(0, np.eye(3), position, motion[:3], motion[3:])
         st = ts.step()
         assert per[k][0] == (st["iterations"], st["iterations_v"], st["visco_iterations"] if visc else 0)
         assert per[k][1] == pytest.approx(st["time"], rel=1e-6)
@@ -121,7 +133,12 @@ def test_cpp_host_layer_matches_python_mirror(visc, bodies, vmap):
     np.testing.assert_array_equal(rho.astype(np.float32), m.getFieldBuffer("density", np.float32))
     np.testing.assert_array_equal(kp.astype(np.float32), m.getFieldBuffer("p / rho^2", np.float32))
     np.testing.assert_array_equal(vb.astype(np.float32), ts.ctx.download("boundary volume", np.float32))
-    if bodies:
+    if bodies and vmap:
+        f, t = ts.ctx.boundary_forces()
+        assert np.abs(f[0]).max() > 0.1
+        np.testing.assert_array_equal(force.astype(np.float32), f[0].astype(np.float32))
+        np.testing.assert_array_equal(torque.astype(np.float32), t[0].astype(np.float32))
+    elif bodies:
         f, t = ts.ctx.boundary_forces()
         assert np.abs(f[0]).max() > 0.1 and np.all(f[1] == 0.0)   # the block reaches the floor
         np.testing.assert_array_equal(force.astype(np.float32), f[0].astype(np.float32))

@@ -109,6 +109,48 @@ def test_oracle_boundary_viscosity_of_a_map_brakes_tangential_motion():
     assert abs(out[0][1]) < 0.1 * abs(out[0][0]) and abs(out[0][2]) < 1e-6 * abs(out[0][0])
 
 
+def moving_container_run(u, steps=15, precision="f64"):
+    """a column in a volume-mapped box translating at velocity u (the fluid starting at u as well),
+    with XSPH, Weiler2018 and both boundary terms on and a fixed step size; the box's pose and
+    velocity are set before every step, as a rigid-body solver would.  The column starts 0.07
+    from the walls, where the coarse map's distance is positive (a particle found inside a body is
+    stopped, v = 0, which no frame change carries), and the viscous solve converges fully (its
+    stopping rule is relative to |b|, which depends on the frame)."""
+    sc = scenes.small_block(counts=(8, 6, 8), box=(0.6, 0.8, 0.6), corner=(0.07, 0.07, 0.07),
+                            viscosity=True).as_float32()
+    sc.xb = np.zeros((0, 3))
+    sc.params.cflMethod = 0
+    sc.params.xsphBoundary = 0.1
+    sc.params.viscosityBoundary = 0.05
+    sc.params.viscoMaxError = 1e-12
+    sc.params.viscoMaxIter = 1000
+    sc.v = sc.v + np.asarray(u)
+    sim = oracle.OracleSim(sc, precision=precision, fp32_predicate=False)
+    sim.set_volume_maps([container_map(4 * sc.params.particleRadius, (12, 16, 12), (0.6, 0.8, 0.6))])
+    sim.set_bodies(None, np.zeros((1, 3)))
+    for _ in range(steps):
+        sim.set_map_motion(0, translation=np.asarray(u) * sim.st.time, velocity=u)
+        sim.step()
+    return sim
+
+
+def test_oracle_moving_container_is_galilean_invariant():
+    """a uniformly translating box carrying its fluid along evolves as the same fluid at rest in
+    the box at rest: every boundary term uses v_i - v_b (divergence source, density advection,
+    XSPH, Weiler2018's right-hand side and its force), and the forces and torques on the box (about
+    its moving position) agree"""
+    u = np.array([0.4, 0.0, -0.25])
+    a, b = moving_container_run(np.zeros(3)), moving_container_run(u)
+    T = b.st.time
+    assert abs(T - a.st.time) < 1e-15 and b.stats()["iterations"] >= 2
+    assert np.abs(b.x - u * T - a.x).max() < 1e-9
+    assert np.abs(b.v - u - a.v).max() < 1e-9
+    scale = np.abs(a.body_force).max()
+    assert scale > 1.0
+    assert np.abs(b.body_force - a.body_force).max() < 1e-9 * scale
+    assert np.abs(b.body_torque - a.body_torque).max() < 1e-9 * max(1.0, np.abs(a.body_torque).max())
+
+
 # --------------------------------------------------------------------- device
 def device_context(sc, precision="fp32", res=RES, use_graph=False):
     ts = TimeStepDFSPH(sc, precision=precision, use_graph=use_graph)
@@ -331,4 +373,102 @@ def test_momentum_balance_of_a_volume_mapped_box():
     p1 = m * ts.getFluidModel().getFieldBuffer("velocity").sum(0)
     got, expect, scale = momentum_balance(sc, ts.ctx.boundary_forces()[0][0], p0, p1, steps, 0.005)
     assert np.abs(got - expect).max() < 1e-6 * scale, (got, expect)
+    ts.close()
+
+
+# ------------------------------------------------------------- moving volume-map bodies
+def rotation_y(angle):
+    c, s = np.cos(angle), np.sin(angle)
+    return np.array([[c, 0.0, s], [0.0, 1.0, 0.0], [-s, 0.0, c]])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol_scale,ftol", [("fp32", 1.0, 2e-3), ("fp64", 1e-4, 1e-8)])
+def test_moving_map_step_and_forces_match_oracle(precision, tol_scale, ftol):
+    """one step with the container turned by 0.02 rad about its centre, translating and spinning,
+    with XSPH and Weiler2018 and both boundary terms: fields and the forces on the box against the
+    oracle at the bars of the static case"""
+    sc = vmap_scene(velocity=(0.3, -0.5, 0.2), viscosity=True)
+    sc.params.xsphBoundary = 0.1
+    probe = device_context(sc)
+    pre = oracle_with_map(sc, probe)
+    probe.close()
+    for _ in range(40):
+        pre.step()
+    state = dict(x=f32(pre.x), v=f32(pre.v), kappa=f32(pre.kappa), kappa_v=f32(pre.kappa_v), dt=pre.dt)
+    centre = 0.5 * np.asarray(BOX)
+    R = rotation_y(0.02)
+    t = centre - R @ centre
+    vel, omega = np.array([0.2, 0.05, -0.1]), np.array([0.0, 0.8, 0.3])
+    ts = device_context(sc, precision)
+    m = ts.getFluidModel()
+    m.setFieldBuffer("position", state["x"])
+    m.setFieldBuffer("velocity", state["v"])
+    m.setFieldBuffer("p / rho^2", state["kappa"])
+    m.setFieldBuffer("p_v / rho^2", state["kappa_v"])
+    ts.setTimeStepSize(state["dt"])
+    ts.ctx.set_boundary_bodies(None, t.reshape(1, 3))
+    ts.ctx.set_volume_map_motion(0, R, t, vel, omega)
+    sim = oracle_with_map(sc, ts, state)
+    sim.set_bodies(None, t.reshape(1, 3))
+    sim.set_map_motion(0, R, t, vel, omega)
+    st = ts.step()
+    sim.step()
+    assert sim.stats()["iterations"] >= 2
+    compare(ts, sim, st, tol_scale=tol_scale if precision == "fp64" else 3.0)
+    f, tq = ts.ctx.boundary_forces()
+    scale_f, scale_t = np.abs(sim.body_force).max(), np.abs(sim.body_torque).max()
+    assert scale_f > 10.0
+    assert np.abs(f - sim.body_force).max() < ftol * scale_f, (f, sim.body_force)
+    assert np.abs(tq - sim.body_torque).max() < ftol * scale_t, (tq, sim.body_torque)
+    ts.close()
+
+
+@pytest.mark.gpu
+def test_device_moving_container_is_galilean_invariant():
+    """the oracle's invariance check on the device (FP64): a box translating with its fluid, its
+    pose and velocity set before every step, evolves as the box at rest"""
+    u = np.array([0.4, 0.0, -0.25])
+    out = []
+    for uu in (np.zeros(3), u):
+        sc = scenes.small_block(counts=(8, 6, 8), box=(0.6, 0.8, 0.6), corner=(0.07, 0.07, 0.07),
+                                viscosity=True).as_float32()
+        sc.xb = np.zeros((0, 3))
+        sc.params.cflMethod = 0
+        sc.params.xsphBoundary = 0.1
+        sc.params.viscosityBoundary = 0.05
+        sc.params.viscoMaxError = 1e-12
+        sc.params.viscoMaxIter = 1000
+        sc.v = sc.v + uu
+        ts = TimeStepDFSPH(sc, precision="fp64", use_graph=True)
+        v, f = scenes.box_mesh((0, 0, 0), (0.6, 0.8, 0.6))
+        ts.ctx.add_volume_map(v, f, (12, 16, 12), invert=True)
+        ts.ctx.set_boundary_method(2)
+        ts.ctx.set_boundary_bodies(None, np.zeros((1, 3)))
+        time = 0.0
+        for _ in range(15):
+            ts.ctx.set_volume_map_motion(0, None, uu * time, uu)
+            st = ts.step()
+            time = st["time"]
+        m = ts.getFluidModel()
+        out.append((m.getFieldBuffer("position"), m.getFieldBuffer("velocity"), ts.ctx.boundary_forces(), time))
+        ts.close()
+    (xa, va, (fa, ta), Ta), (xb, vb, (fb, tb), Tb) = out
+    assert Ta == Tb
+    assert np.abs(xb - u * Tb - xa).max() < 1e-8
+    assert np.abs(vb - u - va).max() < 1e-8
+    assert np.abs(fb - fa).max() < 1e-8 * np.abs(fa).max()
+    assert np.abs(tb - ta).max() < 1e-8 * max(1.0, np.abs(ta).max())
+
+
+@pytest.mark.gpu
+def test_map_motion_refusals():
+    sc = vmap_scene(counts=(4, 4, 4))
+    ts = device_context(sc)
+    with pytest.raises(native.SphgbError) as e:
+        ts.ctx.set_volume_map_motion(1, None, (0, 0, 0))
+    assert native.ERR_NAMES[e.value.code] == "ARGUMENT"
+    with pytest.raises(native.SphgbError) as e:
+        ts.ctx.set_volume_map_motion(0, None, (np.nan, 0, 0))
+    assert native.ERR_NAMES[e.value.code] == "NONFINITE"
     ts.close()
