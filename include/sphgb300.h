@@ -392,7 +392,10 @@ int sphgb_set_boundary_method(sphgb_ctx *ctx, int method);
  * BoundaryModel.h:78-84), enters every boundary term as v_i - v_p: the divergence source and the
  * density advection (TimeStepDFSPH.cpp:1218-1238, 1273-1293), XSPH (XSPH.cpp:119-128),
  * Weiler2018's right-hand side at its four samples (Viscosity_Weiler2018.cpp:1191-1243) and the
- * forces on the body (its torque taken about t).  rotation (row-major) / translation NULL keep
+ * forces on the body (its torque taken about t); the CFL step size also bounds the body's speed
+ * |w x (maxDist, 0, 0) + v| (Simulation.cpp:466-476, SimulatorBase.cpp:1670-1687), maxDist the
+ * largest distance of a mesh vertex from the vertices' mean (0 for a map given by node values).
+ * rotation (row-major) / translation NULL keep
  * the current ones; velocity / omega NULL are zero.  Moving the body is the caller's rigid-body
  * solver's job: call this before each step. */
 int sphgb_set_volume_map_motion(sphgb_ctx *ctx, uint32_t body, const double rotation[9], const double translation[3],

@@ -62,6 +62,7 @@ class OrcVmap(ctypes.Structure):
         ("t", ctypes.c_double * 3),
         ("v", ctypes.c_double * 3),
         ("w", ctypes.c_double * 3),
+        ("max_dist", ctypes.c_double),
     ]
 
 
@@ -303,10 +304,12 @@ class OracleSim:
         self.st.nvmaps = len(self._vmaps)
         self.cp.boundary_method = 2
 
-    def set_map_motion(self, b, rotation=None, translation=None, velocity=(0, 0, 0), omega=(0, 0, 0)):
+    def set_map_motion(self, b, rotation=None, translation=None, velocity=(0, 0, 0), omega=(0, 0, 0), max_dist=None):
         """pose and velocity of the body of volume map b for the next steps; a body's force center
-        follows its position"""
+        follows its position; max_dist: the body's CFL radius (mesh vertices from their mean)"""
         m = self._vmap_arr[b]
+        if max_dist is not None:
+            m.max_dist = float(max_dist)
         if rotation is not None:
             m.R = (ctypes.c_double * 9)(*np.asarray(rotation, np.float64).ravel())
         if translation is not None:

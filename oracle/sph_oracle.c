@@ -1071,6 +1071,16 @@ static double update_time_step(const ctx_t *c, double h)
         }
         if (m > maxVel) maxVel = m;
     }
+    /* a moving volume-map body: |w x (maxDist, 0, 0) + v| (SimulatorBase::updateVMVelocity,
+     * SimulatorBase.cpp:1670-1687), taken into the maximum of the squared fluid speeds as it is
+     * (Simulation.cpp:466-476) */
+    if (p->boundary_method == 2)
+        for (unsigned b = 0; b < s->nvmaps; b++) {
+            const orc_vmap *m = s->vmaps + b;
+            const double vel[3] = {m->v[0], m->v[1] + m->w[2] * m->max_dist, m->v[2] - m->w[1] * m->max_dist};
+            const double speed = sqrt(vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]);
+            if (speed > maxVel) maxVel = speed;
+        }
     if (maxVel < 1.0e-9) maxVel = 1.0e-9;
     double hn = p->cfl_factor * 0.4 * (2.0 * p->radius / sqrt(maxVel));
     if (hn > p->cfl_max) hn = p->cfl_max;

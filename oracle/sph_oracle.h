@@ -72,6 +72,8 @@ typedef struct orc_vmap {
     double v[3], w[3];           /* its linear and angular velocity: the velocity of a point p of the
                                     body is w x (p - t) + v (BoundaryModel::getPointVelocity,
                                     BoundaryModel.h:78-84); zero for a static body */
+    double max_dist;             /* largest distance of a mesh vertex from the vertices' mean
+                                    (SimulatorBase.cpp:2706-2729), for the CFL bound of a moving body */
 } orc_vmap;
 
 typedef struct orc_state {

@@ -112,6 +112,7 @@ struct sphgb_ctx {
         uint32_t res[3];
         double dmin[3], dmax[3], R[9], t[3];
         double v[3] = {0, 0, 0}, w[3] = {0, 0, 0};   // the body's velocity and angular velocity
+        double max_dist = 0;                         // CFL radius: mesh vertices from their mean (0 without a mesh)
         double support;                // support radius the map was built for
         double *f0 = nullptr, *f1 = nullptr;   // node fields (FP64)
         void *coef = nullptr;                  // per-cell coefficients in the context's precision
@@ -1023,6 +1024,7 @@ template <class T> std::vector<VMapDev<T>> vmap_dev_array(const sphgb_ctx *c)
             d.t[k] = (T)m.t[k];
             d.v[k] = (T)m.v[k];
             d.w[k] = (T)m.w[k];
+            d.max_dist = (T)m.max_dist;
             d.res[k] = m.res[k];
         }
         for (int k = 0; k < 9; k++) d.R[k] = (T)m.R[k];
@@ -1917,6 +1919,17 @@ int sphgb_add_volume_map(sphgb_ctx *c, const double *vertices, uint32_t nv, cons
     if ((rc = vmap_init(c, m, resolution, rotation, translation))) return rc;
     m.support = 4.0 * c->prm.particle_radius;
     vmap_domain(vertices, nv, m.support, thickness, m.dmin, m.dmax);
+    {   // the CFL radius of a moving body (SimulatorBase.cpp:2706-2729)
+        double com[3] = {0, 0, 0};
+        for (uint32_t k = 0; k < nv; k++)
+            for (int d = 0; d < 3; d++) com[d] += vertices[3 * (size_t)k + d];
+        for (int d = 0; d < 3; d++) com[d] /= (double)nv;
+        for (uint32_t k = 0; k < nv; k++) {
+            const double dx = vertices[3 * (size_t)k] - com[0], dy = vertices[3 * (size_t)k + 1] - com[1],
+                         dz = vertices[3 * (size_t)k + 2] - com[2];
+            m.max_dist = std::max(m.max_dist, std::sqrt(dx * dx + dy * dy + dz * dz));
+        }
+    }
     cudaError_t e = vmap_build_device(vertices, nv, faces, nf, m.res, m.support, thickness, invert, order ? order : 30u,
                                       m.f0, m.f1, m.dmin, m.dmax, c->stream);
     if (e != cudaSuccess) {

@@ -1571,6 +1571,15 @@ __global__ void __launch_bounds__(kBlock) k_kick(DevParams<T> P, DevBufs<T> B)
         *rs.counter = 0;
         double hn = hd;
         if (P.cfl_method != 0) {
+            // moving volume-map bodies: |w x (maxDist, 0, 0) + v| against the squared fluid speeds,
+            // as the reference compares them (Simulation.cpp:466-476, SimulatorBase.cpp:1670-1687)
+            if (P.vmove)
+                for (uint32_t b = 0; b < P.nvmaps; b++) {
+                    const VMapDev<T> &m = P.vmaps[b];
+                    const double vx = (double)m.v[0], vy = (double)m.v[1] + (double)m.w[2] * (double)m.max_dist,
+                                 vz = (double)m.v[2] - (double)m.w[1] * (double)m.max_dist;
+                    maxVel = fmax(maxVel, sqrt(vx * vx + vy * vy + vz * vz));
+                }
             if (maxVel < 1.0e-9) maxVel = 1.0e-9;
             hn = P.cfl_factor * 0.4 * (2.0 * P.radius / sqrt(maxVel));
             hn = fmin(hn, P.cfl_max);

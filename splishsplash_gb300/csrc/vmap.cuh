@@ -128,6 +128,7 @@ template <class T> struct VMapDev {
     T dmin[3], dmax[3], cs[3];   // body-local grid box and cell size
     T R[9], t[3];                // rotation (row-major) and position: x_local = R^T (x - t)
     T v[3], w[3];                // linear and angular velocity of the body: point p moves at w x (p - t) + v
+    T max_dist;                  // largest distance of a mesh vertex from the vertices' mean (CFL bound)
     uint32_t res[3];
     uint32_t pad;
     const T *coef;               // [cells][32][2]

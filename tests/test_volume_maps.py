@@ -411,7 +411,9 @@ def test_moving_map_step_and_forces_match_oracle(precision, tol_scale, ftol):
     ts.ctx.set_volume_map_motion(0, R, t, vel, omega)
     sim = oracle_with_map(sc, ts, state)
     sim.set_bodies(None, t.reshape(1, 3))
-    sim.set_map_motion(0, R, t, vel, omega)
+    verts = scenes.box_mesh((0, 0, 0), BOX)[0]
+    max_dist = np.linalg.norm(verts - verts.mean(0), axis=1).max()   # the CFL radius the device takes from the mesh
+    sim.set_map_motion(0, R, t, vel, omega, max_dist=max_dist)
     st = ts.step()
     sim.step()
     assert sim.stats()["iterations"] >= 2
@@ -421,6 +423,31 @@ def test_moving_map_step_and_forces_match_oracle(precision, tol_scale, ftol):
     assert scale_f > 10.0
     assert np.abs(f - sim.body_force).max() < ftol * scale_f, (f, sim.body_force)
     assert np.abs(tq - sim.body_torque).max() < ftol * scale_t, (tq, sim.body_torque)
+    ts.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_moving_body_bounds_the_cfl_step(precision):
+    """fluid at rest in a box moving at 0.5 m/s and turning: the next step size follows the box's
+    bound |w x (maxDist, 0, 0) + v| (taken as it is against the squared fluid speeds, as the
+    reference does), on the device as in the oracle"""
+    sc = vmap_scene(counts=(6, 6, 6))
+    sc.params.cflMaxTimeStepSize = 0.1
+    vel, omega = np.array([0.5, 0.0, 0.0]), np.array([0.0, 0.2, 0.1])
+    ts = device_context(sc, precision)
+    ts.ctx.set_volume_map_motion(0, None, None, vel, omega)
+    sim = oracle_with_map(sc, ts)
+    verts = scenes.box_mesh((0, 0, 0), BOX)[0]
+    max_dist = np.linalg.norm(verts - verts.mean(0), axis=1).max()
+    sim.set_map_motion(0, None, None, vel, omega, max_dist=max_dist)
+    st = ts.step()
+    sim.step()
+    speed = np.linalg.norm(vel + np.cross(omega, [max_dist, 0.0, 0.0]))
+    assert speed > (np.abs(sim.v).max() * 3) ** 2
+    expect = sc.params.cflFactor * 0.4 * 2 * sc.params.particleRadius / np.sqrt(speed)
+    assert sim.stats()["dt"] == pytest.approx(expect, rel=1e-12)
+    assert st["dt_next"] == pytest.approx(expect, rel=1e-6)
     ts.close()
 
 
