@@ -342,6 +342,20 @@ int sphgb_get_neighbor_staging(sphgb_ctx *ctx, int *active, float *staged_fracti
  * terms act at the particles' boundary points x_j (TimeStepDFSPH.cpp:1355-1364, XSPH.cpp:196-204). */
 int sphgb_set_boundary_bodies(sphgb_ctx *ctx, const uint32_t *body, uint32_t nbodies, const double *center,
                               const int *dynamic);
+/* Pose and velocity of boundary body `body` (of sphgb_set_boundary_bodies) for the following
+ * steps: its particles, uploaded in body coordinates (the reference's getPosition0), are placed at
+ * R x0 + t and move at w x (R x0) + v, as SimulatorBase::updateBoundaryParticles does every step
+ * (SimulatorBase.cpp:1620-1645).  From the first call on, the boundary particles are placed and
+ * sorted into the grid at the start of every step, their velocities enter every boundary term as
+ * v_i - v_b (divergence source and density advection, TimeStepDFSPH.cpp:1218-1223, 1273-1278;
+ * XSPH, XSPH.cpp:176-183; Weiler2018's right-hand side and force, Viscosity_Weiler2018.cpp:
+ * 1130-1138, 966-975), their squared speeds the CFL maximum (Simulation.cpp:442-458), and the
+ * body's torque is taken about t.  The volumes stay those computed for the uploaded shape.
+ * Bodies without a call stay in their uploaded pose at rest.  rotation (row-major) / translation
+ * NULL keep the current ones; velocity / omega NULL are zero.  One scene (SPHGB_ERR_STATE for a
+ * batch); volume-map bodies move with sphgb_set_volume_map_motion. */
+int sphgb_set_body_motion(sphgb_ctx *ctx, uint32_t body, const double rotation[9], const double translation[3],
+                          const double velocity[3], const double omega[3]);
 /* the sums since the last clear, force[3 nbodies] and torque[3 nbodies] (either may be NULL;
  * zeros for static bodies); waits for the context's stream */
 int sphgb_boundary_forces(sphgb_ctx *ctx, double *force, double *torque);

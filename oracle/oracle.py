@@ -103,6 +103,7 @@ class OrcState(ctypes.Structure):
         ("body_torque", ctypes.c_void_p),
         ("vmaps", ctypes.c_void_p),
         ("nvmaps", ctypes.c_uint),
+        ("vb", ctypes.c_void_p),
     ]
 
 
@@ -266,6 +267,7 @@ class OracleSim:
         self.density_adv_v = np.zeros(n, dt)
         self.nf = np.zeros(n, np.uint32)
         self.nbn = np.zeros(n, np.uint32)
+        self._support, self._fp32_predicate = scene.params.supportRadius, int(fp32_predicate)
         rc = self.lib.orc_boundary_volume(nb, _ptr(self.xb), scene.params.supportRadius,
                                           int(fp32_predicate), _ptr(self.Vb))
         if rc != 0:
@@ -289,12 +291,29 @@ class OracleSim:
         self.body_dynamic = np.ones(nbodies, np.int32) if dynamic is None else np.ascontiguousarray(dynamic, np.int32)
         self.body_force = np.zeros((nbodies, 3), np.float64)
         self.body_torque = np.zeros((nbodies, 3), np.float64)
+        if self.body is not None:
+            self._grouped_volumes(self.body, self.body_dynamic)
         self.st.body = _ptr(self.body)
         self.st.nbodies = nbodies
         self.st.body_center = _ptr(self.body_center)
         self.st.body_dynamic = _ptr(self.body_dynamic)
         self.st.body_force = _ptr(self.body_force)
         self.st.body_torque = _ptr(self.body_torque)
+
+    def _grouped_volumes(self, body, dynamic):
+        """Akinci2012 volumes as Simulation::updateBoundaryVolume computes them
+        (Simulation.cpp:700-746): the static bodies' particles together, every dynamic body's alone"""
+        groups = np.where(np.asarray(dynamic)[body] != 0, body.astype(np.int64) + 1, 0)
+        if not groups.any():
+            return
+        for g in np.unique(groups):
+            idx = np.flatnonzero(groups == g)
+            sub = np.ascontiguousarray(self.xb[idx])
+            vol = np.zeros(len(idx), self.Vb.dtype)
+            rc = self.lib.orc_boundary_volume(len(idx), _ptr(sub), self._support, self._fp32_predicate, _ptr(vol))
+            if rc != 0:
+                raise RuntimeError(f"orc_boundary_volume failed: {rc}")
+            self.Vb[idx] = vol
 
     def set_volume_maps(self, maps):
         """Bender2019 boundary: the bodies' VolumeMaps replace the boundary particles."""
@@ -318,6 +337,13 @@ class OracleSim:
                 self.body_center[b] = translation
         m.v = (ctypes.c_double * 3)(*np.asarray(velocity, np.float64))
         m.w = (ctypes.c_double * 3)(*np.asarray(omega, np.float64))
+
+    def set_boundary_state(self, xb, vb):
+        """positions and velocities of the boundary particles for the next steps (moving
+        Akinci2012 bodies; the volumes stay those of the initial shape, as for a rigid body)"""
+        self.xb[:] = xb
+        self.vb = np.array(vb, dtype=self.xb.dtype, order="C", copy=True).reshape(self.xb.shape)
+        self.st.vb = _ptr(self.vb)
 
     def clear_forces(self):
         self.body_force[:] = 0.0

@@ -382,12 +382,17 @@ static void compute_factor(ctx_t *c)
  * velocity is zero for static Akinci2012 walls. */
 /* BoundaryModel::getPointVelocity (BoundaryModel.h:78-84): the velocity w x (p - t) + v of point p
  * of the body of boundary entry j; with volume maps the entry j = i * nbodies + b belongs to map b.
- * Boundary particles are static walls here: zero. */
+ * A boundary particle has its own velocity (s->vb; none: a static wall). */
 static void boundary_point_velocity(const ctx_t *c, unsigned j, const double p[3], double out[3])
 {
     const orc_state *s = c->s;
     out[0] = out[1] = out[2] = 0.0;
-    if (c->p->boundary_method != 2 || !s->nvmaps) return;
+    if (c->p->boundary_method != 2) {   /* boundary particle j of a moving body */
+        if (s->vb)
+            for (int d = 0; d < 3; d++) out[d] = (double)s->vb[3 * (size_t)j + d];
+        return;
+    }
+    if (!s->nvmaps) return;
     const orc_vmap *m = s->vmaps + (j % s->nvmaps);
     const double d[3] = {p[0] - m->t[0], p[1] - m->t[1], p[2] - m->t[2]};
     out[0] = m->w[1] * d[2] - m->w[2] * d[1] + m->v[0];
@@ -895,7 +900,26 @@ static void visc_rhs(const visc_t *w, real *b, real *g)
         b[i] = s->v[i];
         g[i] = (real)((double)s->v[i] + (double)s->vdiff[i]);
     }
-    if (w->mub == 0.0 || c->p->boundary_method != 2) return;
+    if (w->mub == 0.0) return;
+    if (c->p->boundary_method != 2) {   /* moving boundary particles (:1130-1138) */
+        if (!s->vb) return;
+        for (long i = 0; i < (long)s->n; i++) {
+            const real *xi = s->x + 3 * i;
+            const double rhoi = (double)s->density[i];
+            double bi[3] = {0, 0, 0};
+            for (unsigned k = c->B.off[i]; k < c->B.off[i + 1]; k++) {
+                const unsigned j = c->B.idx[k];
+                double r[3], gw[3], vj[3];
+                diffv(xi, s->xb + 3 * (size_t)j, r);
+                kGradW(&c->K, r, gw);
+                boundary_velocity(c, j, vj);
+                const double f = w->d * w->mub * (c->rho0 * (double)s->Vb[j] / rhoi) * dot3(vj, r) / (dot3(r, r) + 0.01 * w->h2);
+                for (int d = 0; d < 3; d++) bi[d] += f * gw[d];
+            }
+            for (int d = 0; d < 3; d++) b[3 * i + d] = (real)((double)s->v[3 * i + d] - w->dt / rhoi * bi[d]);
+        }
+        return;
+    }
     for (long i = 0; i < (long)s->n; i++) {
         const real *xi = s->x + 3 * i;
         double bi[3] = {0, 0, 0};
@@ -1042,10 +1066,12 @@ static int viscosity_weiler(ctx_t *c, double dt)
                     }
                     continue;
                 }
-                double r[3], g[3], f[3];
+                double r[3], g[3], f[3], vj[3];
                 diffv(s->x + 3 * i, s->xb + 3 * (size_t)j, r);
                 kGradW(&c->K, r, g);
-                const double coef = 10.0 * mub * (c->rho0 * (double)s->Vb[j] / rhoi) * dot3(nv, r) / (dot3(r, r) + 0.01 * h2);
+                boundary_velocity(c, j, vj);
+                const double dv[3] = {nv[0] - vj[0], nv[1] - vj[1], nv[2] - vj[2]};
+                const double coef = 10.0 * mub * (c->rho0 * (double)s->Vb[j] / rhoi) * dot3(dv, r) / (dot3(r, r) + 0.01 * h2);
                 for (int d = 0; d < 3; d++) f[d] = -c->mass / rhoi * (coef * g[d]);
                 add_force(c, j, f);
             }
@@ -1071,6 +1097,13 @@ static double update_time_step(const ctx_t *c, double h)
         }
         if (m > maxVel) maxVel = m;
     }
+    /* the boundary particles of moving bodies (Simulation.cpp:442-458) */
+    if (p->boundary_method != 2 && s->vb)
+        for (unsigned j = 0; j < s->nb; j++) {
+            double m = 0.0;
+            for (int d = 0; d < 3; d++) m += (double)s->vb[3 * (size_t)j + d] * (double)s->vb[3 * (size_t)j + d];
+            if (m > maxVel) maxVel = m;
+        }
     /* a moving volume-map body: |w x (maxDist, 0, 0) + v| (SimulatorBase::updateVMVelocity,
      * SimulatorBase.cpp:1670-1687), taken into the maximum of the squared fluid speeds as it is
      * (Simulation.cpp:466-476) */

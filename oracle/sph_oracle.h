@@ -81,7 +81,7 @@ typedef struct orc_state {
     orc_real *x, *v, *a;                  /* 3n, AoS (x0,y0,z0,x1,...) like Vector3r */
     orc_real *density, *factor, *density_adv, *kappa, *kappa_v;   /* n */
     orc_real *pressure_accel, *vdiff;     /* 3n */
-    orc_real *xb, *Vb;                    /* 3nb, nb (static boundary, v_b = 0) */
+    orc_real *xb, *Vb;                    /* 3nb, nb (boundary particles and their volumes) */
     double dt, time;
     /* written by orc_step */
     unsigned iterations, iterations_v, visco_iterations;
@@ -109,6 +109,9 @@ typedef struct orc_state {
      * applied at the particle's boundary point x_j (addForce(xj, ...) of the Bender2019 branches). */
     const orc_vmap *vmaps;
     unsigned nvmaps;
+    /* velocities of the boundary particles [nb][3] (BoundaryModel_Akinci2012::getVelocity of a
+     * moving body, SimulatorBase.cpp:1620-1645); NULL: static walls */
+    const orc_real *vb;
 } orc_state;
 
 /* Cubic spline (SPHKernels.h:16-91). */

@@ -124,6 +124,17 @@ struct sphgb_ctx {
     void *bv = nullptr;                // prepared set: [np] boundary velocity sums of moving maps
     bool vmove = false;                // some map has a velocity
     bool vmaps_dirty = false;          // poses or velocities changed since the device copy
+    // moving boundary bodies (sphgb_set_body_motion): particles placed and re-sorted every step
+    bool bmotion = false, bmot_dirty = false, bm_ready = false;
+    std::vector<double> bmot;          // [nbodies][18]: R (row-major), t, v, w
+    uint32_t bm_nb = 0;                // boundary count the buffers below were made for (body allocations)
+    void *d_bmot = nullptr, *bm_x0 = nullptr, *bm_V0 = nullptr, *bm_xtmp = nullptr, *bm_vtmp = nullptr;
+    void *vbs = nullptr;               // velocities of the sorted boundary particles
+    uint32_t *bm_body = nullptr, *bm_k1 = nullptr, *bm_k2 = nullptr, *bm_v1 = nullptr, *bm_v2 = nullptr;
+    uint32_t *bm_cells = nullptr, *bm_hist = nullptr;
+    uint32_t *binv = nullptr;          // prepared set: sorted slot of boundary particle u
+    uint32_t *bgroup = nullptr;        // prepared set: volume group of boundary particle u (null: one group)
+    std::vector<char> body_moves;      // a motion was set for the body (its particles form their own group)
     // neighbourhood staging of the solver passes (FP32, one lane per particle)
     int stage_mode = 0;                // 0: the autotuner decides, 1: off, 2: on
     bool staged = false;               // in use
@@ -166,14 +177,14 @@ namespace {
 enum KernelId {
     K_STEP_BEGIN, K_KEYS, K_SORT, K_GATHER, K_CELL_RANGES, K_BUILD, K_LOOP_BEGIN, K_PRESSURE_ACCEL, K_JACOBI,
     K_SOLVER_FINALIZE, K_XSPH, K_VISC_SETUP, K_CG_MATVEC, K_CG_UPDATE, K_CG_P, K_KICK, K_PRESS_INIT, K_INTEGRATE,
-    K_FEATURES, K_MLP, K_WS_SELECT, K_BODY_FORCES, K_STAGE_TABLE, K_VMAP_BOUNDARY,
+    K_FEATURES, K_MLP, K_WS_SELECT, K_BODY_FORCES, K_STAGE_TABLE, K_VMAP_BOUNDARY, K_BOUNDARY_MOVE,
     K_COUNT
 };
 const char *kKernelNames[K_COUNT] = {
     "step_begin", "keys", "radix_sort", "gather", "cell_ranges", "build_lists_density_alpha", "loop_begin",
     "pressure_accel", "jacobi_update", "solver_finalize", "xsph_gravity", "visc_setup", "cg_matvec", "cg_update",
     "cg_p", "kick_cfl", "press_init", "integrate", "features", "mlp_infer", "warmstart_select", "body_forces",
-    "stage_table", "vmap_boundary",
+    "stage_table", "vmap_boundary", "boundary_move",
 };
 
 // Brackets the launches of one kernel class with events on the context stream
@@ -270,6 +281,9 @@ void free_prepared(sphgb_ctx *c)
     c->cstart = c->cend = c->bcstart = c->bcend = nullptr;
     c->xb = c->bscratch = nullptr;
     c->bid = c->bscene = nullptr;
+    c->binv = nullptr;
+    c->bgroup = nullptr;
+    c->bm_ready = false;   // the rest shapes and volumes are read again from the new layout
     c->bodies.slot = nullptr;
     c->bodies.blk = nullptr;
     c->bodies.body_nblk = nullptr;
@@ -314,6 +328,13 @@ void free_bodies(sphgb_ctx *c)
     c->body_center.clear();
     c->body_dynamic.clear();
     c->nbodies = 0;
+    c->bmotion = c->bmot_dirty = c->bm_ready = false;
+    c->bmot.clear();
+    c->body_moves.clear();
+    c->bm_nb = 0;
+    c->d_bmot = c->bm_x0 = c->bm_V0 = c->bm_xtmp = c->bm_vtmp = c->vbs = nullptr;
+    c->bm_body = c->bm_k1 = c->bm_k2 = c->bm_v1 = c->bm_v2 = c->bm_cells = c->bm_hist = nullptr;
+    invalidate_graphs(c);
 }
 
 void free_all(sphgb_ctx *c)
@@ -411,6 +432,7 @@ template <class T> DevParams<T> make_params(const sphgb_ctx *c)
     P.nvmaps = (c->boundary_method == 2 && c->bx) ? (uint32_t)c->vmaps.size() : 0u;
     P.vmaps = static_cast<const VMapDev<T> *>(c->d_vmaps);
     P.vmove = (P.nvmaps && c->vmove && c->bv) ? 1 : 0;
+    P.bmove = (c->bmotion && c->bm_ready && c->nb && c->boundary_method == 0 && c->nscenes() == 1 && c->bv) ? 1 : 0;
     return P;
 }
 
@@ -454,6 +476,9 @@ template <class T> DevBufs<T> make_bufs(const sphgb_ctx *c, int view)
     B.stage_src = c->stage_src;
     B.bx = (v4 *)c->bx;
     B.bv = (v4 *)c->bv;
+    B.vbs = (v4 *)c->vbs;
+    B.binv = c->binv;
+    B.bgroup = c->bgroup;
     B.ll = c->ll;
     B.key = c->key;
     B.key2 = c->key2;
@@ -533,21 +558,21 @@ int build_body_tables(sphgb_ctx *c)
 {
     c->bodies.nblk = 0;
     if (c->nbodies == 0 || c->nb == 0) return SPHGB_OK;
-    std::vector<uint32_t> bid(c->nb);
-    CK(cudaMemcpy(bid.data(), c->bid, (size_t)c->nb * 4, cudaMemcpyDeviceToHost));
+    // each dynamic body's particles in upload order; the kernel finds their sorted slots through
+    // binv, so the tables hold when moving bodies are re-sorted every step
     const uint32_t B = c->nbodies;
     std::vector<uint32_t> count(B + 1, 0);
-    for (uint32_t k = 0; k < c->nb; k++) {
-        const uint32_t b = c->body_of[bid[k]];
+    for (uint32_t u = 0; u < c->nb; u++) {
+        const uint32_t b = c->body_of[u];
         if (c->body_dynamic[b]) count[b + 1]++;
     }
     for (uint32_t b = 0; b < B; b++) count[b + 1] += count[b];
     const uint32_t entries = count[B];
     if (entries == 0) return SPHGB_OK;
     std::vector<uint32_t> slot(entries), fill(count.begin(), count.end() - 1);
-    for (uint32_t k = 0; k < c->nb; k++) {
-        const uint32_t b = c->body_of[bid[k]];
-        if (c->body_dynamic[b]) slot[fill[b]++] = k;
+    for (uint32_t u = 0; u < c->nb; u++) {
+        const uint32_t b = c->body_of[u];
+        if (c->body_dynamic[b]) slot[fill[b]++] = u;
     }
     std::vector<uint4> blk;
     std::vector<uint32_t> nblk(B, 0);
@@ -624,6 +649,23 @@ template <class T> int prepare(sphgb_ctx *c)
     const uint32_t nb = c->nb;
     if ((rc = palloc(c, &c->xb, (size_t)std::max(nb, 1u) * vec_size(c)))) return rc;
     if ((rc = palloc(c, &c->bid, (size_t)std::max(nb, 1u) * 4))) return rc;
+    if ((rc = palloc(c, &c->binv, (size_t)std::max(nb, 1u) * 4))) return rc;
+    if (nb && c->nbodies && c->body_of.size() == nb) {
+        // volume groups: the static bodies together, every dynamic or moving body alone
+        std::vector<uint32_t> g(nb, 0u);
+        bool any = false;
+        for (uint32_t u = 0; u < nb; u++) {
+            const uint32_t b = c->body_of[u];
+            if (c->body_dynamic[b] || (b < c->body_moves.size() && c->body_moves[b])) {
+                g[u] = 1u + b;
+                any = true;
+            }
+        }
+        if (any) {
+            if ((rc = palloc(c, &c->bgroup, (size_t)nb * 4))) return rc;
+            CK(cudaMemcpy(c->bgroup, g.data(), (size_t)nb * 4, cudaMemcpyHostToDevice));
+        }
+    }
     if ((rc = palloc(c, &c->bscratch, (size_t)std::max(nb, 1u) * real_size(c)))) return rc;
     if (c->scn.size() > 1 && (rc = palloc(c, &c->bscene, (size_t)std::max(nb, 1u) * 4))) return rc;
     if (nb > 0) {
@@ -670,6 +712,9 @@ template <class T> int prepare(sphgb_ctx *c)
             if (p) dfree(c->prep_allocs, p);
     }
     if ((rc = build_body_tables(c))) return rc;
+    if (c->boundary_method == 0 && c->nb) {   // boundary velocity sums of moving bodies
+        if ((rc = palloc(c, &c->bv, (size_t)std::max(c->np, 1u) * vec_size(c)))) return rc;
+    }
     if (c->boundary_method == 2 && !c->vmaps.empty()) {
         if ((rc = palloc(c, &c->bx, (size_t)std::max(c->np, 1u) * c->vmaps.size() * vec_size(c)))) return rc;
         if ((rc = palloc(c, &c->bv, (size_t)std::max(c->np, 1u) * vec_size(c)))) return rc;
@@ -728,11 +773,33 @@ template <class T> bool body_phase0(const sphgb_ctx *c, const DevParams<T> &P)
     return bodies && (P.div_on || P.xsph_b != T(0) || (P.visc_on && P.mub != T(0)));
 }
 
+template <class T> BoundaryMoveDev<T> boundary_move_dev(const sphgb_ctx *c)
+{
+    BoundaryMoveDev<T> M;
+    M.x0 = static_cast<const v4_t<T> *>(c->bm_x0);
+    M.V0 = static_cast<const T *>(c->bm_V0);
+    M.body = c->bm_body;
+    M.motion = static_cast<const BodyMotionDev<T> *>(c->d_bmot);
+    M.xtmp = static_cast<v4_t<T> *>(c->bm_xtmp);
+    M.vtmp = static_cast<v4_t<T> *>(c->bm_vtmp);
+    return M;
+}
+
 // Enqueue the launches that precede the solver loops.
 template <class T> void enqueue_prologue(sphgb_ctx *c, const DevParams<T> &P, const DevBufs<T> &B0, const DevBufs<T> &B1,
                                          cudaStream_t s)
 {
     { PROF(K_STEP_BEGIN, s); launch_step_begin<T>(P, B1, s); }
+    if (P.bmove) {   // moving bodies: place, sort and bin the boundary particles (after the CFL reset)
+        PROF(K_BOUNDARY_MOVE, s);
+        const BoundaryMoveDev<T> M = boundary_move_dev<T>(c);
+        launch_boundary_move<T>(P, B1, M, c->bm_k1, c->bm_v1, s);
+        const uint32_t btiles = (c->nb + kSortTile - 1) / kSortTile;
+        const bool bsw = radix_sort_pairs(c->bm_k1, c->bm_v1, c->bm_k2, c->bm_v2, c->nb, c->key_bits, c->bm_hist,
+                                          btiles, s, &B1.gsc->launches);
+        cudaMemsetAsync(c->bcstart, 0xff, c->ncell * 4, s);
+        launch_boundary_regather<T>(P, B1, M, bsw ? c->bm_v2 : c->bm_v1, c->bm_cells, s);
+    }
     { PROF(K_KEYS, s); launch_keys<T>(P, B0, s); }
     const uint32_t tiles = (c->n + kSortTile - 1) / kSortTile;
     bool sw;
@@ -1058,12 +1125,76 @@ template <class T> int refresh_vmaps(sphgb_ctx *c)
     return SPHGB_OK;
 }
 
+// Buffers of the moving bodies (body allocations, made once per boundary count) and their
+// contents from the prepared layout: rest positions (the uploaded positions, body coordinates),
+// volumes (computed for the rest shape: a rigid body's particles keep them) and bodies, upload order.
+template <class T> int prepare_body_motion(sphgb_ctx *c)
+{
+    if (!c->bmotion || c->bm_ready || !c->nb || !c->nbodies) return SPHGB_OK;
+    const uint32_t nb = c->nb;
+    int rc;
+    if (c->bm_nb != nb) {
+        const size_t vs = sizeof(v4_t<T>), tiles = (nb + kSortTile - 1) / kSortTile;
+        auto al = [&](auto **p, size_t bytes) { return dalloc_into(c, c->body_allocs, p, bytes); };
+        if ((rc = al(&c->d_bmot, (size_t)c->nbodies * sizeof(BodyMotionDev<T>))) || (rc = al(&c->bm_x0, nb * vs)) ||
+            (rc = al(&c->bm_V0, nb * sizeof(T))) || (rc = al(&c->bm_xtmp, nb * vs)) || (rc = al(&c->bm_vtmp, nb * vs)) ||
+            (rc = al(&c->vbs, nb * vs)) || (rc = al(&c->bm_body, nb * 4)) || (rc = al(&c->bm_k1, nb * 4)) ||
+            (rc = al(&c->bm_k2, nb * 4)) || (rc = al(&c->bm_v1, nb * 4)) || (rc = al(&c->bm_v2, nb * 4)) ||
+            (rc = al(&c->bm_cells, nb * 4)) || (rc = al(&c->bm_hist, tiles * 256 * 4)))
+            return rc;
+        c->bm_nb = nb;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    std::vector<v4_t<T>> x0(nb), xs(nb);
+    std::vector<uint32_t> bid(nb);
+    std::vector<T> V0(nb);
+    CK(cudaMemcpy(xs.data(), c->xb, nb * sizeof(v4_t<T>), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(bid.data(), c->bid, nb * 4, cudaMemcpyDeviceToHost));
+    for (uint32_t k = 0; k < nb; k++) V0[bid[k]] = (T)xs[k].w;
+    for (uint32_t u = 0; u < nb; u++) {
+        const double *p = c->hb.data() + 3 * (size_t)u;
+        x0[u].x = (T)p[0];
+        x0[u].y = (T)p[1];
+        x0[u].z = (T)p[2];
+        x0[u].w = T(0);
+    }
+    CK(cudaMemcpy(c->bm_x0, x0.data(), nb * sizeof(v4_t<T>), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->bm_V0, V0.data(), nb * sizeof(T), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->bm_body, c->body_of.data(), nb * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemset(c->vbs, 0, nb * sizeof(v4_t<T>)));
+    c->bm_ready = true;
+    c->bmot_dirty = true;
+    invalidate_graphs(c);
+    return SPHGB_OK;
+}
+
+// the bodies' poses and velocities, copied in place on the step stream before the next step
+template <class T> int refresh_body_motion(sphgb_ctx *c)
+{
+    c->bmot_dirty = false;
+    if (!c->d_bmot) return SPHGB_OK;
+    std::vector<BodyMotionDev<T>> h(c->nbodies);
+    for (uint32_t b = 0; b < c->nbodies; b++) {
+        const double *q = c->bmot.data() + 18 * (size_t)b;
+        for (int k = 0; k < 9; k++) h[b].R[k] = (T)q[k];
+        for (int k = 0; k < 3; k++) {
+            h[b].t[k] = (T)q[9 + k];
+            h[b].v[k] = (T)q[12 + k];
+            h[b].w[k] = (T)q[15 + k];
+        }
+    }
+    CK(cudaMemcpyAsync(c->d_bmot, h.data(), h.size() * sizeof(BodyMotionDev<T>), cudaMemcpyHostToDevice, c->stream));
+    return SPHGB_OK;
+}
+
 template <class T> int do_step(sphgb_ctx *c)
 {
     int rc;
     if ((rc = check_boundary_method(c))) return rc;
     if (!c->prepared && (rc = prepare<T>(c))) return rc;
     if (c->vmaps_dirty && (rc = refresh_vmaps<T>(c))) return rc;
+    if ((rc = prepare_body_motion<T>(c))) return rc;
+    if (c->bmot_dirty && c->bm_ready && (rc = refresh_body_motion<T>(c))) return rc;
     if ((rc = upload_scalars(c))) return rc;
     if (!c->tuned) {
         if (c->lpp_fixed) {
@@ -1795,6 +1926,9 @@ int sphgb_set_boundary_bodies(sphgb_ctx *c, const uint32_t *body, uint32_t nbodi
     CK(cudaStreamSynchronize(c->stream));
     free_bodies(c);
     invalidate_graphs(c);
+    // prepared again at the next step: the volume groups and the body tables (and, with volume
+    // maps, the block partials of their forces)
+    c->prepared = false;
     if (nbodies == 0) return SPHGB_OK;
     c->body_of.assign(body, body + (body ? c->nb : 0u));
     c->body_center.assign(center, center + 3 * (size_t)nbodies);
@@ -1802,6 +1936,10 @@ int sphgb_set_boundary_bodies(sphgb_ctx *c, const uint32_t *body, uint32_t nbodi
     if (dynamic)
         for (uint32_t b = 0; b < nbodies; b++) c->body_dynamic[b] = dynamic[b] != 0;
     c->nbodies = nbodies;
+    c->body_moves.assign(nbodies, 0);
+    c->bmot.assign(18 * (size_t)nbodies, 0.0);   // every body at rest in its uploaded pose
+    for (uint32_t b = 0; b < nbodies; b++)
+        for (int k = 0; k < 3; k++) c->bmot[18 * (size_t)b + 4 * k] = 1.0;
     double *acc, *cen;
     unsigned *cnt;
     int *dyn;
@@ -1821,11 +1959,6 @@ int sphgb_set_boundary_bodies(sphgb_ctx *c, const uint32_t *body, uint32_t nbodi
     c->bodies.counters = cnt;
     c->bodies.dynamic = dyn;
     c->bodies.nbodies = nbodies;
-    if (c->boundary_method == 2) c->prepared = false;   // block partials of the volume-map forces
-    if (c->prepared && (rc = build_body_tables(c))) {
-        free_bodies(c);
-        return rc;
-    }
     return SPHGB_OK;
 }
 
@@ -1994,6 +2127,52 @@ int sphgb_clear_volume_maps(sphgb_ctx *c)
     free_vmaps(c);
     c->prepared = false;
     invalidate_graphs(c);
+    return SPHGB_OK;
+}
+
+int sphgb_set_body_motion(sphgb_ctx *c, uint32_t body, const double rotation[9], const double translation[3],
+                          const double velocity[3], const double omega[3])
+{
+    if (!c) return SPHGB_ERR_ARGUMENT;
+    if (c->boundary_method == 2)
+        return fail(c, SPHGB_ERR_ARGUMENT, "volume-map bodies move with sphgb_set_volume_map_motion");
+    if (body >= c->nbodies || c->nb == 0)
+        return fail(c, SPHGB_ERR_ARGUMENT, "no such body of boundary particles (sphgb_set_boundary_bodies)");
+    if (c->nscenes() > 1) return fail(c, SPHGB_ERR_STATE, "moving boundary bodies serve a single scene, not a batch");
+    int rc;
+    if ((rotation && (rc = check_finite(c, rotation, 9, "body rotation"))) ||
+        (translation && (rc = check_finite(c, translation, 3, "body translation"))) ||
+        (velocity && (rc = check_finite(c, velocity, 3, "body velocity"))) ||
+        (omega && (rc = check_finite(c, omega, 3, "body angular velocity"))))
+        return rc;
+    if (c->step_pending) {
+        sphgb_stats st;
+        fill_stats(c, &st);
+    }
+    cudaSetDevice(c->cfg.device);
+    if (!c->body_moves[body]) {   // a body that moves has its own volume group from now on
+        c->body_moves[body] = 1;
+        if (!c->body_dynamic[body]) c->prepared = false;
+    }
+    double *q = c->bmot.data() + 18 * (size_t)body;
+    if (rotation) std::copy(rotation, rotation + 9, q);
+    if (translation) std::copy(translation, translation + 3, q + 9);
+    for (int k = 0; k < 3; k++) {
+        q[12 + k] = velocity ? velocity[k] : 0.0;
+        q[15 + k] = omega ? omega[k] : 0.0;
+    }
+    if (!c->bmotion) {   // from now on the boundary particles are placed and sorted every step
+        c->bmotion = true;
+        c->bm_ready = false;
+        invalidate_graphs(c);
+    }
+    c->bmot_dirty = true;
+    if (translation && c->bodies.center) {   // the body's torque is taken about its position
+        std::copy(translation, translation + 3, c->body_center.begin() + 3 * (size_t)body);
+        CK(cudaMemcpyAsync(const_cast<double *>(c->bodies.center) + 3 * (size_t)body,
+                           c->body_center.data() + 3 * (size_t)body, 3 * sizeof(double), cudaMemcpyHostToDevice,
+                           c->stream));
+    }
     return SPHGB_OK;
 }
 

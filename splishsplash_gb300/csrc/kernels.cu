@@ -687,7 +687,11 @@ __device__ __forceinline__ void build_one(const DevParams<T> &P, const DevBufs<T
                               gf = add(gf, g);
                               divf += dot(sub(vi, xyz<T>(d.v)), g);
                           });
-    auto boundary_term = [&](uint32_t, const v4_t<T> &xj) {
+    // moving boundaries: sum V_j W v_j (XSPH) and sum V_j v_j . gradW (divergence source, density
+    // advection), both fixed for the step
+    V3<T> bvw = mk3<T>(0, 0, 0);
+    T bvg = T(0);
+    auto boundary_term = [&](uint32_t j, const v4_t<T> &xj) {
         const V3<T> r = diff3<T>(xi, xj);
         T W, c;
         kernel_W_coef_d2(P.K, dot(r, r), W, c);
@@ -696,13 +700,15 @@ __device__ __forceinline__ void build_one(const DevParams<T> &P, const DevBufs<T
         const V3<T> g = scl(r, c * Vb);
         gb = add(gb, g);
         divb += dot(vi, g);
+        if (P.bmove) {   // boundary particle j of a moving body
+            const V3<T> vj = xyz<T>(ldv(B.vbs, j));
+            bvw = add(bvw, scl(vj, Vb * W));
+            bvg += dot(vj, g);
+        }
     };
     nbr_loop<kUnroll>(Lb, min(nb, P.capb), [&](uint32_t j) { return ldv(B.xb, j); }, boundary_term);
     // Bender2019: the volume-map sample of each body, x_j with V_j in w, where V_j > 0; a moving
-    // body's point velocity v_j enters as sum V_j v_j . gradW (divergence source, density
-    // advection) and sum V_j W v_j (XSPH), both fixed for the step
-    V3<T> bvw = mk3<T>(0, 0, 0);
-    T bvg = T(0);
+    // body's point velocity v_j enters the same sums
     for (uint32_t b = 0; b < P.nvmaps; b++) {
         const v4_t<T> xj = ldv(B.bx, b * P.np + i);
         if ((T)xj.w > T(0)) {
@@ -717,7 +723,7 @@ __device__ __forceinline__ void build_one(const DevParams<T> &P, const DevBufs<T
             }
         }
     }
-    if (P.vmove) {
+    if (P.vmove || P.bmove) {
         divb -= bvg;
         stv(B.bv, i, pack(bvw, bvg));
     }
@@ -1175,7 +1181,7 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams<T> P, DevBufs<T> B, i
     if (P.xsph_b != T(0)) {
         // sum_b (rho0 V_b / rho_i) W_ib from the per-step boundary sum
         const T wsum = P.rho0 * (T)ldv(B.bg, i).w / B.density[i];
-        if (P.vmove) {   // moving volume-map bodies: (v_i - v_b) W
+        if (P.vmove || P.bmove) {   // moving boundaries: (v_i - v_b) W
             const V3<T> dv = sub(scl(vi, (T)ldv(B.bg, i).w), xyz<T>(ldv(B.bv, i)));
             ai = sub(ai, scl(dv, invH * P.xsph_b * P.rho0 / B.density[i]));
         } else {
@@ -1301,12 +1307,14 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T
                                      acc = add(acc, scl(r, f * dot(sub(gi, xyz<T>(d.g)), r)));
                                  });
         if (P.mub != T(0)) {
-            boundary_loop<LPP>(P, B, i, q.l, [&](uint32_t, const v4_t<T> &xj) {
+            boundary_loop<LPP>(P, B, i, q.l, [&](uint32_t j, const v4_t<T> &xj) {
                 const V3<T> r = diff3<T>(xi, xj);
                 const T r2 = dot(r, r);
                 const T f = P.vd * P.mub * (P.rho0 * (T)xj.w / rhoi) / (r2 + eps2) * grad_coef_d2(P.K, r2);
                 m[0] += f * r.x * r.x; m[1] += f * r.x * r.y; m[2] += f * r.x * r.z;
                 m[3] += f * r.y * r.y; m[4] += f * r.y * r.z; m[5] += f * r.z * r.z;
+                // computeRHS (:1130-1138): the boundary particle's velocity
+                if (P.bmove) bb = add(bb, scl(r, f * dot(xyz<T>(ldv(B.vbs, j)), r)));
             });
             if (q.l == 0)   // volume maps: the four samples of each body (diagonalMatrixElement :697-740)
                 for (uint32_t b = 0; b < P.nvmaps; b++) {
@@ -1329,6 +1337,7 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T
 #pragma unroll
     for (int k = 0; k < 6; k++) m[k] = gsum<LPP>(m[k]);
     acc = gsum3<LPP>(acc);
+    if (P.bmove) bb = gsum3<LPP>(bb);   // the lanes' shares of the boundary list
     if (q.act && q.l == 0) {
         const uint32_t i = q.i;
         const T dt = (T)sc->dt;
@@ -1346,7 +1355,7 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T
         stv(B.inv1, i, i1);
 
         V3<T> vi = xyz<T>(ldv(B.v, i));   // b = v_i - dt / rho_i (boundary velocity term)
-        if (P.vmove) vi = sub(vi, scl(bb, s));
+        if (P.vmove || P.bmove) vi = sub(vi, scl(bb, s));
         const V3<T> Ag = sub(gi, scl(acc, s));
         const V3<T> r = sub(vi, Ag);
         const V3<T> p = sym_mul<T>(i0, i1, r);
@@ -1621,7 +1630,7 @@ __global__ void __launch_bounds__(kBlock) k_press_init(DevParams<T> P, DevBufs<T
     const uint32_t i = q.i;
     const T h = (T)B.sc[q.s].dt_next;
     T accb = dot(vi, xyz<T>(ldv(B.bg, i)));
-    if (P.vmove) accb -= (T)ldv(B.bv, i).w;   // moving volume-map bodies: (v_i - v_b) . gradW
+    if (P.vmove || P.bmove) accb -= (T)ldv(B.bv, i).w;   // moving boundaries: (v_i - v_b) . gradW
     const T dadv = B.density[i] / P.rho0 + h * (accf * P.V + accb);
     B.dadv[i] = dadv;
     const T invH2 = T(1) / (h * h);
@@ -1710,8 +1719,9 @@ __global__ void __launch_bounds__(kBlock) k_body_forces(DevParams<T> P, DevBufs<
 #pragma unroll
     for (int k = 0; k < 6; k++) mine.v[k] = 0.0;
     if (e < bk.z) {
-        const uint32_t j = D.slot[e];
+        const uint32_t j = B.binv[D.slot[e]];   // the body's particles in upload order
         const v4_t<T> xb = ldv(B.xb, j);
+        const V3<T> vbj = P.bmove ? xyz<T>(ldv(B.vbs, j)) : mk3<T>(0, 0, 0);   // a moving body's particle
         const uint32_t s = B.bscene ? B.bscene[j] : 0u;
         const SceneDev<T> S = scene_get(P, s);
         const StepScalars *sc = B.sc + s;
@@ -1754,10 +1764,13 @@ __global__ void __launch_bounds__(kBlock) k_body_forces(DevParams<T> P, DevBufs<
                             const T rhoi = B.density[i];
                             if (xs) {
                                 const T w = P.mass * xs_c / rhoi * kernel_W(P.K, dev_sqrt(d2));
-                                fi = add(fi, scl(xyz<T>(ldv(B.v, i)), w));
+                                V3<T> dv = xyz<T>(ldv(B.v, i));
+                                if (P.bmove) dv = sub(dv, vbj);
+                                fi = add(fi, scl(dv, w));
                             }
                             if (visc) {
-                                const V3<T> nv = xyz<T>(ldv(B.cg_x, i));
+                                V3<T> nv = xyz<T>(ldv(B.cg_x, i));
+                                if (P.bmove) nv = sub(nv, vbj);
                                 const T a = vi_c / rhoi * dot(nv, r) / (d2 + eps2) * gc;
                                 fi = sub(fi, scl(r, P.mass / rhoi * a));
                             }
@@ -2126,6 +2139,7 @@ __global__ void __launch_bounds__(kBlock) k_boundary_gather(DevParams<T> P, DevB
     x.w = 0;
     stv(B.xb, k, x);
     B.bid[k] = src;
+    if (B.binv) B.binv[src] = k;   // contexts keep the inverse map; the allocation-free path has none
     const uint32_t s = bscene_in ? bscene_in[src] : 0u;
     if (B.bscene) B.bscene[k] = s;
     const SceneDev<T> S = scene_get(P, s);
@@ -2134,8 +2148,77 @@ __global__ void __launch_bounds__(kBlock) k_boundary_gather(DevParams<T> P, DevB
     cells[k] = S.cell_off + local_cell(S, cx, cy, cz);
 }
 
+// Moving boundary bodies, every step before the neighbour search (SimulatorBase::updateBoundaryParticles,
+// SimulatorBase.cpp:1620-1645): particle u of body b at R_b x0_u + t_b, moving at
+// w_b x (R_b x0_u) + v_b; its sort key; the squared speeds enter the step's CFL maximum as the
+// reference adds those of moving bodies' particles (Simulation.cpp:442-458).  One scene.
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_boundary_move(DevParams<T> P, DevBufs<T> B, BoundaryMoveDev<T> M,
+                                                           uint32_t *keys, uint32_t *vals)
+{
+    count_launch(&B.gsc->launches);
+    const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+    T sp = T(0);
+    if (u < P.nb) {
+        const v4_t<T> x0 = ldv(M.x0, u);
+        const BodyMotionDev<T> &m = M.motion[M.body[u]];
+        const V3<T> r = mk3<T>(m.R[0] * (T)x0.x + m.R[1] * (T)x0.y + m.R[2] * (T)x0.z,
+                               m.R[3] * (T)x0.x + m.R[4] * (T)x0.y + m.R[5] * (T)x0.z,
+                               m.R[6] * (T)x0.x + m.R[7] * (T)x0.y + m.R[8] * (T)x0.z);
+        const V3<T> x = add(r, mk3<T>(m.t[0], m.t[1], m.t[2]));
+        const V3<T> v = mk3<T>(m.w[1] * r.z - m.w[2] * r.y + m.v[0], m.w[2] * r.x - m.w[0] * r.z + m.v[1],
+                               m.w[0] * r.y - m.w[1] * r.x + m.v[2]);
+        const v4_t<T> xp = pack(x, M.V0[u]);
+        stv(M.xtmp, u, xp);
+        stv(M.vtmp, u, pack(v, T(0)));
+        const SceneDev<T> &S = P.s0;
+        int cx, cy, cz;
+        cell_of(S, xp, cx, cy, cz);
+        keys[u] = S.key_prefix | morton3((uint32_t)cx, (uint32_t)cy, (uint32_t)cz);
+        vals[u] = u;
+        sp = dot(v, v);
+    }
+    // block maximum, one atomic per block, in the encoding of the kick's fluid maximum
+    __shared__ T wmax[kBlock / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sp = fmax(sp, __shfl_xor_sync(0xffffffffu, sp, o));
+    if ((threadIdx.x & 31u) == 0) wmax[threadIdx.x >> 5] = sp;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        T bm = T(0);
+        for (int k = 0; k < kBlock / 32; k++) bm = fmax(bm, wmax[k]);
+        if (bm > T(0)) {
+            StepScalars *sc = B.sc;
+            if constexpr (sizeof(T) == 8) atomicMax(&sc->maxvel_bits64, (unsigned long long)__double_as_longlong((double)bm));
+            else atomicMax(&sc->maxvel_bits, __float_as_uint((float)bm));
+        }
+    }
+}
+
+// ... sorted into the boundary grid: positions (w = V), velocities, slot maps, cells
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_boundary_regather(DevParams<T> P, DevBufs<T> B, BoundaryMoveDev<T> M,
+                                                               const uint32_t *__restrict__ perm, uint32_t *cells)
+{
+    count_launch(&B.gsc->launches);
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= P.nb) return;
+    const uint32_t src = perm[k];
+    const v4_t<T> x = ldv(M.xtmp, src);
+    stv(B.xb, k, x);
+    stv(B.vbs, k, ldv(M.vtmp, src));
+    B.bid[k] = src;
+    B.binv[src] = k;
+    const SceneDev<T> &S = P.s0;
+    int cx, cy, cz;
+    cell_of(S, x, cx, cy, cz);
+    cells[k] = S.cell_off + local_cell(S, cx, cy, cz);
+}
+
 // BoundaryModel_Akinci2012::computeBoundaryVolume (BoundaryModel_Akinci2012.cpp:48-75):
-// V_b = 1 / (W0 + sum over boundary neighbours of the same scene of W)
+// V_b = 1 / (W0 + sum over boundary neighbours of the same scene and volume group of W); the
+// static bodies form one group, every dynamic or moving body its own, as
+// Simulation::updateBoundaryVolume activates them (Simulation.cpp:700-746)
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_boundary_volume(DevParams<T> P, DevBufs<T> B)
 {
@@ -2143,6 +2226,7 @@ __global__ void __launch_bounds__(kBlock) k_boundary_volume(DevParams<T> P, DevB
     if (i >= P.nb) return;
     const SceneDev<T> S = scene_get(P, B.bscene ? B.bscene[i] : 0u);
     v4_t<T> xi = ldv(B.xb, i);
+    const uint32_t gi = B.bgroup ? B.bgroup[B.bid[i]] : 0u;
     int cx, cy, cz;
     cell_of(S, xi, cx, cy, cz);
     T delta = P.K.w0;
@@ -2160,7 +2244,7 @@ __global__ void __launch_bounds__(kBlock) k_boundary_volume(DevParams<T> P, DevB
                 if (s == kEmpty) continue;
                 const uint32_t e = B.bcend[c];
                 for (uint32_t j = s; j < e; j++) {
-                    if (j == i) continue;
+                    if (j == i || (B.bgroup && B.bgroup[B.bid[j]] != gi)) continue;
                     T ddx, ddy, ddz;
                     const T d2 = pair_d2(xi, ldv(B.xb, j), ddx, ddy, ddz);
                     if (d2 < P.K.h2) delta += kernel_W(P.K, dev_sqrt(d2));
@@ -2555,6 +2639,20 @@ template <class T> void launch_boundary_gather(const DevParams<T> &P, const DevB
     k_boundary_gather<T><<<grid_for(P.nb), kBlock, 0, s>>>(P, B, xb_in, bscene_in, perm, cells);
     k_cell_ranges_flat<<<grid_for(P.nb), kBlock, 0, s>>>(cells, B.bcstart, B.bcend, P.nb);
 }
+template <class T>
+void launch_boundary_move(const DevParams<T> &P, const DevBufs<T> &B, const BoundaryMoveDev<T> &M, uint32_t *keys,
+                          uint32_t *vals, cudaStream_t s)
+{
+    if (P.nb) k_boundary_move<T><<<grid_for(P.nb), kBlock, 0, s>>>(P, B, M, keys, vals);
+}
+template <class T>
+void launch_boundary_regather(const DevParams<T> &P, const DevBufs<T> &B, const BoundaryMoveDev<T> &M,
+                              const uint32_t *perm, uint32_t *cells, cudaStream_t s)
+{
+    if (!P.nb) return;
+    k_boundary_regather<T><<<grid_for(P.nb), kBlock, 0, s>>>(P, B, M, perm, cells);
+    k_cell_ranges_flat<<<grid_for(P.nb), kBlock, 0, s>>>(cells, B.bcstart, B.bcend, P.nb);
+}
 template <class T> void launch_boundary_volume(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {
     if (!P.nb) return;
@@ -2631,6 +2729,10 @@ void launch_lists_to_ids(const uint32_t *list, const uint32_t *cnt, uint32_t cap
                                           uint32_t *, cudaStream_t);                                                \
     template void launch_boundary_gather<T>(const DevParams<T> &, const DevBufs<T> &, const v4_t<T> *,              \
                                             const uint32_t *, const uint32_t *, uint32_t *, cudaStream_t);          \
+    template void launch_boundary_move<T>(const DevParams<T> &, const DevBufs<T> &, const BoundaryMoveDev<T> &,    \
+                                          uint32_t *, uint32_t *, cudaStream_t);                                    \
+    template void launch_boundary_regather<T>(const DevParams<T> &, const DevBufs<T> &, const BoundaryMoveDev<T> &, \
+                                              const uint32_t *, uint32_t *, cudaStream_t);                          \
     template void launch_boundary_volume<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                \
     template void launch_scatter_field<T>(const DevParams<T> &, const DevBufs<T> &, int, void *, int, cudaStream_t); \
     template void launch_upload_field<T>(const DevParams<T> &, const DevBufs<T> &, int, const void *, int,          \

@@ -91,6 +91,8 @@ template <class T> struct DevParams {
     uint32_t nvmaps;              // Bender2019 boundary: volume maps (bodies); 0 = Akinci2012 particles
     const VMapDev<T> *vmaps;      // device array [nvmaps]
     int vmove;                    // some volume-map body moves: boundary terms use v_i - v_b
+    int bmove;                    // boundary particles move with their bodies: placed and re-sorted every
+                                  // step, with velocities (one scene)
     int staged;                   // FP32, one lane per particle: the solver passes read their block's
                                   // neighbourhood from shared memory (stage tables, local lists)
 };
@@ -132,6 +134,10 @@ template <class T> struct DevBufs {
     v4 *xk;                      // x_i with the running solver's kappa_i in w (one gather per pair)
     v4 *bg;                      // per-particle boundary sums: xyz = sum_b V_b gradW_ib, w = sum_b V_b W_ib
     v4 *bx;                      // Bender2019: [nvmaps][np] boundary point x_j of each particle's map sample, w = V_j
+    v4 *vbs;                     // moving boundary bodies: velocity of sorted boundary particle k
+    uint32_t *binv;              // sorted slot of boundary particle u (upload order)
+    const uint32_t *bgroup;      // volume group of boundary particle u (upload order): 0 the static bodies,
+                                 // 1 + b a dynamic or moving body b; null: one group
     v4 *bv;                      // moving volume-map bodies, per particle: xyz = sum_b V_b W_ib v_b,
                                  // w = sum_b V_b v_b . gradW_ib (fixed for the step, like bg)
     T *density, *factor, *dadv;
@@ -214,6 +220,26 @@ template <class T> void launch_vmap_boundary(const DevParams<T> &P, const DevBuf
 template <class T> void launch_stage_table(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
 // shared-memory limits of the staged solver passes; call once per device before their first launch
 cudaError_t configure_staged_kernels();
+// Pose and velocity of one boundary body (rotation row-major, position, velocity, angular velocity)
+template <class T> struct BodyMotionDev {
+    T R[9], t[3], v[3], w[3];
+};
+// Per-step placement of the boundary particles of moving bodies, upload order: rest positions x0
+// (body coordinates) and volumes, each particle's body, the bodies' motions, and the placed
+// positions (w = V) and velocities before they are sorted
+template <class T> struct BoundaryMoveDev {
+    const v4_t<T> *x0;
+    const T *V0;
+    const uint32_t *body;
+    const BodyMotionDev<T> *motion;
+    v4_t<T> *xtmp, *vtmp;
+};
+template <class T>
+void launch_boundary_move(const DevParams<T> &P, const DevBufs<T> &B, const BoundaryMoveDev<T> &M, uint32_t *keys,
+                          uint32_t *vals, cudaStream_t s);
+template <class T>
+void launch_boundary_regather(const DevParams<T> &P, const DevBufs<T> &B, const BoundaryMoveDev<T> &M,
+                              const uint32_t *perm, uint32_t *cells, cudaStream_t s);
 template <class T> void launch_pressure_accel(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s,
                                               cudaGraphConditionalHandle h = 0, bool use_handle = false);
 template <class T> void launch_jacobi(const DevParams<T> &P, const DevBufs<T> &B, bool div,

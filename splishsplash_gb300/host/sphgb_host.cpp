@@ -300,10 +300,10 @@ void TimeStepDFSPH_GB300::upload()
             body.insert(body.end(), bm.numberOfParticles(), k);
             for (int d = 0; d < 3; d++) center.push_back((double)bm.m_rigidBody.getPosition()[d]);
             dynamic.push_back(bm.m_rigidBody.isDynamic() ? 1 : 0);
-            anyDynamic = anyDynamic || bm.m_rigidBody.isDynamic();
+            // bodies where one collects forces or moves: no extra launches otherwise
+            anyDynamic = anyDynamic || bm.m_rigidBody.isDynamic() || bm.m_rigidBody.isAnimated();
         }
         check(sphgb_upload_boundary(m_ctx, xb.data(), (uint32_t)body.size()), "sphgb_upload_boundary");
-        // bodies only where one collects forces: no extra launches otherwise
         check(sphgb_set_boundary_bodies(m_ctx, body.data(), anyDynamic ? (uint32_t)m_boundaries.size() : 0u,
                                         center.data(), dynamic.data()),
               "sphgb_set_boundary_bodies");
@@ -323,10 +323,23 @@ void TimeStepDFSPH_GB300::upload()
     m_dirty = false;
 }
 
-// the current pose and velocities of every dynamic or animated volume-map body
-// (TimeStep.cpp:238-240 reads R and t from the rigid body each step; BoundaryModel.h:78-84)
+// the current pose and velocities of every dynamic or animated body: boundary particles placed at
+// R x0 + t (SimulatorBase.cpp:1620-1645), volume maps sampled at R^T (x - t) (TimeStep.cpp:238-240),
+// both moving at w x (p - t) + v (BoundaryModel.h:78-84)
 void TimeStepDFSPH_GB300::pushBodyMotion()
 {
+    for (unsigned int k = 0; k < m_boundaries.size() && m_bodiesSet; k++) {
+        const RigidBodyObject &rb = m_boundaries[k]->m_rigidBody;
+        if (!rb.isDynamic() && !rb.isAnimated()) continue;
+        double R[9], t[3], v[3], w[3];
+        for (int q = 0; q < 9; q++) R[q] = (double)rb.getRotation()[q];
+        for (int d = 0; d < 3; d++) {
+            t[d] = (double)rb.getPosition()[d];
+            v[d] = (double)rb.getVelocity()[d];
+            w[d] = (double)rb.getAngularVelocity()[d];
+        }
+        check(sphgb_set_body_motion(m_ctx, k, R, t, v, w), "sphgb_set_body_motion");
+    }
     for (unsigned int k = 0; k < m_volumeMaps.size(); k++) {
         const RigidBodyObject &rb = m_volumeMaps[k]->m_rigidBody;
         if (!rb.isDynamic() && !rb.isAnimated()) continue;

@@ -96,7 +96,13 @@ private:
 // whether the body collects the fluid's forces.
 struct RigidBodyObject {
     Vector3r m_position, m_velocity, m_angularVelocity;
+    Real m_rotation[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};   // row-major
     bool m_isDynamic = false, m_isAnimated = false;
+    const Real *getRotation() const { return m_rotation; }
+    void setRotation(const Real R[9])
+    {
+        for (int k = 0; k < 9; k++) m_rotation[k] = R[k];
+    }
     const Vector3r &getPosition() const { return m_position; }
     void setPosition(const Vector3r &x) { m_position = x; }
     const Vector3r &getVelocity() const { return m_velocity; }
@@ -111,8 +117,10 @@ struct RigidBodyObject {
 
 class TimeStepDFSPH_GB300;
 
-// Static boundary of one body sampled with particles; volumes computed on the device
-// (BoundaryModel_Akinci2012.cpp:48-75).  The forces the fluid exerted on a dynamic body
+// Boundary of one body sampled with particles; volumes computed on the device
+// (BoundaryModel_Akinci2012.cpp:48-75).  The particles of a dynamic or animated body are its rest
+// shape in body coordinates (getPosition0): every step places them at R x0 + t and moves them with
+// the body's velocities, as SimulatorBase::updateBoundaryParticles does (SimulatorBase.cpp:1620-1645).  The forces the fluid exerted on a dynamic body
 // accumulate until clearForceAndTorque (BoundaryModel.h:86-87), as the boundary simulator
 // reads them (Simulator/BoundarySimulator.cpp:8-25).
 class BoundaryModel_Akinci2012 {

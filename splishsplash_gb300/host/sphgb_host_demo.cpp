@@ -6,11 +6,11 @@
 //
 // scene.bin (little endian): uint32 n, nb, steps, lanes (0 = autotune), viscosity (0/1),
 // bodies (0/1), volume map (0/1); float64 particle radius; float64 x[n][3], v[n][3], xb[nb][3];
-// with bodies: uint32 body[nb] (0: the dynamic body, 1: static walls) and float64 position[3]
-// of the dynamic body; with a volume map (then nb = 0): uint32 nv, nf, resolution[3], invert,
-// float64 vertices[nv][3], uint32 faces[nf][3] of the container (Bender2019 boundary); with a
-// volume map and bodies, the container is a dynamic body at the position above moving with
-// float64 velocity[3] and angular velocity[3] (its pose is held, so the run stays comparable).
+// with bodies: uint32 body[nb] (0: the dynamic body, 1: static walls), float64 position[3],
+// velocity[3] and angular velocity[3] of the dynamic body (its pose is held, so that the run stays
+// comparable; its particles are given in the scene's frame and handed over in body coordinates);
+// with a volume map (then nb = 0): uint32 nv, nf, resolution[3], invert, float64 vertices[nv][3],
+// uint32 faces[nf][3] of the container (Bender2019 boundary), which is then the dynamic body.
 // out.bin: per step uint32 iterations, iterationsV, viscoIterations and float64 time;
 // then float64 x[n][3], v[n][3], density[n], p / rho^2 [n], boundary volume[nb] (in the
 // order of the boundary models: body 0's particles first), force[3], torque[3] of body 0 (the
@@ -54,18 +54,16 @@ int main(int argc, char **argv)
     std::vector<double> x(3 * (size_t)n), v(3 * (size_t)n), xb(3 * (size_t)nb);
     if (!rd(f, x.data(), x.size()) || !rd(f, v.data(), v.size()) || !rd(f, xb.data(), xb.size())) return 2;
     std::vector<uint32_t> body(nb, 1u);
-    double pos[3] = {0, 0, 0};
-    if (bodies && (!rd(f, body.data(), body.size()) || !rd(f, pos, 3))) return 2;
+    double pos[3] = {0, 0, 0}, bvel[6] = {0, 0, 0, 0, 0, 0};
+    if (bodies && (!rd(f, body.data(), body.size()) || !rd(f, pos, 3) || !rd(f, bvel, 6))) return 2;
     uint32_t mh[6] = {0, 0, 0, 0, 0, 0};
     std::vector<double> mv;
     std::vector<uint32_t> mf;
-    double bvel[6] = {0, 0, 0, 0, 0, 0};
     if (vmap) {
         if (!rd(f, mh, 6)) return 2;
         mv.resize(3 * (size_t)mh[0]);
         mf.resize(3 * (size_t)mh[1]);
         if (!rd(f, mv.data(), mv.size()) || !rd(f, mf.data(), mf.size())) return 2;
-        if (bodies && !rd(f, bvel, 6)) return 2;
     }
     fclose(f);
 
@@ -80,7 +78,14 @@ int main(int argc, char **argv)
         model.initModel("Fluid", n, xv.data(), vv.data());
         // one boundary model per body: the dynamic body (body 0) and the static walls
         std::vector<Vector3r> part[2];
-        for (uint32_t k = 0; k < nb; k++) part[body[k] == 0 ? 0 : 1].push_back(xbv[k]);
+        for (uint32_t k = 0; k < nb; k++) {
+            if (body[k] != 0) {
+                part[1].push_back(xbv[k]);
+            } else {   // the dynamic body's rest shape in body coordinates
+                const double *p = xb.data() + 3 * (size_t)k;
+                part[0].push_back(Vector3r((Real)(p[0] - pos[0]), (Real)(p[1] - pos[1]), (Real)(p[2] - pos[2])));
+            }
+        }
         BoundaryModel_Akinci2012 models[2];
         std::vector<BoundaryModel_Akinci2012 *> boundaries;
         for (int b = 0; b < 2; b++) {
@@ -89,6 +94,8 @@ int main(int argc, char **argv)
         }
         models[0].getRigidBodyObject()->setPosition(Vector3r((Real)pos[0], (Real)pos[1], (Real)pos[2]));
         models[0].getRigidBodyObject()->setDynamic(bodies != 0);
+        models[0].getRigidBodyObject()->setVelocity(Vector3r((Real)bvel[0], (Real)bvel[1], (Real)bvel[2]));
+        models[0].getRigidBodyObject()->setAngularVelocity(Vector3r((Real)bvel[3], (Real)bvel[4], (Real)bvel[5]));
         Viscosity_Weiler2018_GB300 viscosity;
         viscosity.m_maxError = Real(1e-3);
         // Bender2019: the container as a volume map instead of boundary particles

@@ -126,7 +126,7 @@ EXPORTS = [
     "sphgb_set_boundary_bodies", "sphgb_boundary_forces", "sphgb_clear_boundary_forces",
     "sphgb_set_neighbor_staging", "sphgb_get_neighbor_staging",
     "sphgb_add_volume_map", "sphgb_add_volume_map_values", "sphgb_get_volume_map", "sphgb_clear_volume_maps",
-    "sphgb_set_boundary_method", "sphgb_set_volume_map_motion",
+    "sphgb_set_boundary_method", "sphgb_set_volume_map_motion", "sphgb_set_body_motion",
 ]
 
 _lib = None
@@ -193,6 +193,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.sphgb_clear_volume_maps.argtypes = [vp]
     L.sphgb_set_boundary_method.argtypes = [vp, i32]
     L.sphgb_set_volume_map_motion.argtypes = [vp, u32, vp, vp, vp, vp]
+    L.sphgb_set_body_motion.argtypes = [vp, u32, vp, vp, vp, vp]
     L.sphgb_get_neighbor_staging.argtypes = [vp, ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_float),
                                              ctypes.POINTER(ctypes.c_float)]
     L.sphgb_profile_enable.argtypes = [vp, i32]
@@ -566,6 +567,16 @@ class Context:
             if a is not None and a.size != n:
                 raise ValueError("rotation needs 9 values, translation / velocity / omega 3")
         self._check(self.L.sphgb_set_volume_map_motion(self.h, int(body), *[None if a is None else _p(a) for a in arrs]))
+
+    def set_body_motion(self, body: int, rotation=None, translation=None, velocity=None, omega=None):
+        """Pose and velocity of boundary body `body` (its particles uploaded in body coordinates) for
+        the next steps; None keeps the pose, zero velocities."""
+        arrs = [None if a is None else np.ascontiguousarray(a, np.float64).ravel()
+                for a in (rotation, translation, velocity, omega)]
+        for a, n in zip(arrs, (9, 3, 3, 3)):
+            if a is not None and a.size != n:
+                raise ValueError("rotation needs 9 values, translation / velocity / omega 3")
+        self._check(self.L.sphgb_set_body_motion(self.h, int(body), *[None if a is None else _p(a) for a in arrs]))
 
     def set_neighbor_staging(self, mode: int = 0):
         """Shared-memory staging of the solver passes: 0 autotuned (default), 1 off, 2 on."""

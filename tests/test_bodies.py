@@ -19,7 +19,7 @@ import oracle
 from splishsplash_gb300 import native, scenes
 from splishsplash_gb300.dfsph import BatchedTimeStepDFSPH, TimeStepDFSPH
 
-from test_gpu_parity import advanced_state, gpu_from_state, oracle_from_state
+from test_gpu_parity import advanced_state, compare, gpu_from_state, oracle_from_state
 
 CENTERS = np.array([[0.4, 0.0, 0.4], [0.4, 0.5, 0.4], [0.0, 0.0, 0.0]])
 DYNAMIC = [1, 1, 0]
@@ -78,6 +78,47 @@ def test_oracle_accumulates_until_cleared():
 
 
 # ------------------------------------------------------------------- device
+def moving_box_oracle(u, steps=15):
+    """a column in a box of boundary particles (one dynamic body) translating at u, the fluid
+    starting at u too, with XSPH, Weiler2018 and both boundary terms, a fixed step size and a fully
+    converged viscous solve (its stopping rule is relative to |b|, which depends on the frame); the
+    box's particles are placed at x0 + t with velocity u before every step, as
+    SimulatorBase::updateBoundaryParticles does (SimulatorBase.cpp:1620-1645)"""
+    sc = scenes.small_block(counts=(8, 6, 8), box=(0.6, 0.8, 0.6), corner=(0.05, 0.05, 0.05),
+                            viscosity=True).as_float32()
+    sc.params.cflMethod = 0
+    sc.params.xsphBoundary = 0.1
+    sc.params.viscosityBoundary = 0.05
+    sc.params.viscoMaxError = 1e-12
+    sc.params.viscoMaxIter = 1000
+    sc.v = sc.v + np.asarray(u)
+    sim = oracle.OracleSim(sc, fp32_predicate=False)
+    xb0 = sim.xb.copy()
+    sim.set_bodies(np.zeros(sc.nb, np.uint32), np.zeros((1, 3)))
+    for _ in range(steps):
+        t = np.asarray(u) * sim.st.time
+        sim.set_boundary_state(xb0 + t, np.broadcast_to(np.asarray(u, float), xb0.shape))
+        sim.body_center[0] = t
+        sim.step()
+    return sim
+
+
+def test_oracle_moving_particle_box_is_galilean_invariant():
+    """a translating box of boundary particles carrying its fluid evolves as the box at rest: every
+    Akinci2012 term uses v_i - v_b (divergence source, density advection, XSPH, Weiler2018's
+    right-hand side and force), and the forces and torques on the box agree"""
+    u = np.array([0.4, 0.0, -0.25])
+    a, b = moving_box_oracle(np.zeros(3)), moving_box_oracle(u)
+    T = b.st.time
+    assert abs(T - a.st.time) < 1e-15 and b.stats()["iterations"] >= 2
+    assert np.abs(b.x - u * T - a.x).max() < 1e-9
+    assert np.abs(b.v - u - a.v).max() < 1e-9
+    scale = np.abs(a.body_force).max()
+    assert scale > 1.0
+    assert np.abs(b.body_force - a.body_force).max() < 1e-9 * scale
+    assert np.abs(b.body_torque - a.body_torque).max() < 1e-9 * max(1.0, np.abs(a.body_torque).max())
+
+
 def device_forces(ctx):
     f, t = ctx.boundary_forces()
     return f.copy(), t.copy()
@@ -218,3 +259,108 @@ def test_api_errors_and_reset():
     f, t = device_forces(ts.ctx)
     assert f.shape == (0, 3)
     ts.close()
+
+
+# ------------------------------------------------------------- moving particle bodies
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol", [("fp32", 2e-3), ("fp64", 1e-8)])
+def test_moving_body_step_and_forces_match_oracle(precision, tol):
+    """one step with the floor (body 0) lifted, sliding and spinning about its position, with every
+    boundary term on: fields and forces against the oracle, which gets the same placed particles
+    and their velocities w x (x0) + v"""
+    sc = all_terms_scene()
+    state = advanced_state(sc, 40)
+    body = container_bodies(sc.xb, 1.0)
+    t = np.array([0.0, 0.002, 0.0])
+    vel, omega = np.array([0.3, 0.1, 0.0]), np.array([0.0, 0.5, 0.0])
+    ts = gpu_from_state(sc, state, precision=precision)
+    ts.ctx.set_boundary_bodies(body, CENTERS, DYNAMIC)
+    ts.ctx.set_body_motion(0, np.eye(3), t, vel, omega)
+    dt = np.float32 if precision == "fp32" else np.float64
+    x0 = sc.xb.astype(dt)
+    xb = np.where((body == 0)[:, None], x0 + t.astype(dt), x0).astype(np.float64)   # the device's arithmetic
+    vb = np.where((body == 0)[:, None], np.cross(omega, sc.xb) + vel, 0.0)
+    sim = oracle_from_state(sc, state)
+    sim.set_bodies(body, CENTERS, DYNAMIC)
+    sim.body_center[0] = t
+    sim.set_boundary_state(xb, vb)
+    st = ts.step()
+    sim.step()
+    np.testing.assert_array_equal(ts.ctx.download("boundary position"), xb)
+    compare(ts, sim, st, tol_scale=1.0 if precision == "fp32" else 1e-4)
+    f, tq = device_forces(ts.ctx)
+    scale_f, scale_t = np.abs(sim.body_force).max(), np.abs(sim.body_torque).max()
+    assert scale_f > 100.0
+    assert np.abs(f - sim.body_force).max() < tol * scale_f, (f, sim.body_force)
+    assert np.abs(tq - sim.body_torque).max() < tol * scale_t, (tq, sim.body_torque)
+    ts.close()
+
+
+@pytest.mark.gpu
+def test_device_moving_particle_box_is_galilean_invariant():
+    """the oracle's invariance check on the device (FP64): the box of boundary particles translating
+    with its fluid, placed before every step, evolves as the box at rest"""
+    u = np.array([0.4, 0.0, -0.25])
+    out = []
+    for uu in (np.zeros(3), u):
+        sc = scenes.small_block(counts=(8, 6, 8), box=(0.6, 0.8, 0.6), corner=(0.05, 0.05, 0.05),
+                                viscosity=True).as_float32()
+        sc.params.cflMethod = 0
+        sc.params.xsphBoundary = 0.1
+        sc.params.viscosityBoundary = 0.05
+        sc.params.viscoMaxError = 1e-12
+        sc.params.viscoMaxIter = 1000
+        sc.v = sc.v + uu
+        ts = TimeStepDFSPH(sc, precision="fp64", use_graph=True)
+        ts.ctx.set_boundary_bodies(np.zeros(sc.nb, np.uint32), np.zeros((1, 3)))
+        time = 0.0
+        for _ in range(15):
+            ts.ctx.set_body_motion(0, None, uu * time, uu)
+            st = ts.step()
+            time = st["time"]
+        m = ts.getFluidModel()
+        out.append((m.getFieldBuffer("position"), m.getFieldBuffer("velocity"), device_forces(ts.ctx), time))
+        ts.close()
+    (xa, va, (fa, ta), Ta), (xb, vb, (fb, tb), Tb) = out
+    assert Ta == Tb
+    assert np.abs(xb - u * Tb - xa).max() < 1e-8
+    assert np.abs(vb - u - va).max() < 1e-8
+    assert np.abs(fb - fa).max() < 1e-8 * np.abs(fa).max()
+    assert np.abs(tb - ta).max() < 1e-8 * max(1.0, np.abs(ta).max())
+
+
+@pytest.mark.gpu
+def test_moving_body_bounds_the_cfl_step():
+    """fluid at rest, its floor moving at 1 m/s: the step size follows the boundary particles'
+    speed (|v_b|^2 in the CFL maximum)"""
+    sc = resting_scene()
+    sc.params.cflMaxTimeStepSize = 0.1
+    body = container_bodies(sc.xb, 0.8)
+    ts = TimeStepDFSPH(sc)
+    ts.ctx.set_boundary_bodies(body, CENTERS, DYNAMIC)
+    ts.ctx.set_body_motion(0, None, None, (1.0, 0.0, 0.0))
+    st = ts.step()
+    expect = sc.params.cflFactor * 0.4 * 2 * sc.params.particleRadius / 1.0
+    assert st["dt_next"] == pytest.approx(expect, rel=1e-6)
+    ts.close()
+
+
+@pytest.mark.gpu
+def test_body_motion_refusals():
+    def code(fn):
+        with pytest.raises(native.SphgbError) as e:
+            fn()
+        return native.ERR_NAMES[e.value.code]
+
+    sc = scenes.small_block(counts=(4, 4, 4))
+    ts = TimeStepDFSPH(sc)
+    assert code(lambda: ts.ctx.set_body_motion(0, None, (0, 0, 0))) == "ARGUMENT"          # no bodies
+    ts.ctx.set_boundary_bodies(np.zeros(sc.nb, np.uint32), np.zeros((1, 3)))
+    assert code(lambda: ts.ctx.set_body_motion(1, None, (0, 0, 0))) == "ARGUMENT"          # no such body
+    assert code(lambda: ts.ctx.set_body_motion(0, None, (np.inf, 0, 0))) == "NONFINITE"
+    ts.close()
+    a, b = scenes.small_block(counts=(4, 4, 4)), scenes.small_block(counts=(5, 4, 4))
+    bt = BatchedTimeStepDFSPH([a, b])
+    bt.ctx.set_boundary_bodies(np.zeros(a.nb + b.nb, np.uint32), np.zeros((1, 3)))
+    assert code(lambda: bt.ctx.set_body_motion(0, None, (0, 0, 0))) == "STATE"            # a batch
+    bt.close()

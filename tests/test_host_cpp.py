@@ -25,13 +25,12 @@ def _write_scene(path, sc, steps, lanes, visc, body=None, position=None, vmap=No
         if body is not None:
             f.write(np.ascontiguousarray(body, "<u4").tobytes())
             f.write(np.ascontiguousarray(position, "<f8").tobytes())
+            f.write(np.ascontiguousarray(motion, "<f8").tobytes())
         if vmap is not None:
             verts, faces, res = vmap
             f.write(struct.pack("<6I", len(verts), len(faces), *[int(r) for r in res], 1))
             f.write(np.ascontiguousarray(verts, "<f8").tobytes())
             f.write(np.ascontiguousarray(faces, "<u4").tobytes())
-            if body is not None:
-                f.write(np.ascontiguousarray(motion, "<f8").tobytes())
 
 
 def _read_out(path, n, nb, steps):
@@ -91,9 +90,11 @@ def test_cpp_host_layer_matches_python_mirror(visc, bodies, vmap):
         position = np.zeros(3)
         motion = np.array([0.125, 0.0, -0.0625, 0.0, 0.25, 0.0])   # exact in float
     elif bodies:
-        # the floor is a dynamic body (boundary model 0), the other walls are static (model 1)
+        # the floor is a dynamic body (boundary model 0) sliding along x, the other walls are static
+        # (model 1)
         body = np.where(sc.xb[:, 1] < 1e-9, 0, 1).astype(np.uint32)
         position = np.array([0.375, 0.0, 0.4375], np.float64)   # exact in float (the C++ layer holds Real)
+        motion = np.array([0.125, 0.0, 0.0, 0.0, 0.0, 0.0])
     mesh = None
     if vmap:
         # the container as a Bender2019 volume map instead of boundary particles
@@ -108,9 +109,12 @@ def test_cpp_host_layer_matches_python_mirror(visc, bodies, vmap):
         assert r.stdout.startswith("DFSPH:")
         per, x, v, rho, kp, vb, force, torque = _read_out(os.path.join(d, "o.bin"), sc.n, sc.nb, steps)
     if bodies and not vmap:
-        # the C++ layer uploads the boundary models in order: body 0's particles first
+        # the C++ layer uploads the boundary models in order: body 0's particles first, in body
+        # coordinates (placed at x0 + position every step)
         order = np.concatenate([np.flatnonzero(body == 0), np.flatnonzero(body != 0)])
-        sc = dataclasses.replace(sc, xb=sc.xb[order])
+        xb = sc.xb[order].copy()
+        xb[body[order] == 0] -= position
+        sc = dataclasses.replace(sc, xb=xb)
     ts = TimeStepDFSPH(sc)
     ts.ctx.set_lanes_per_particle(lanes)
     if vmap:
@@ -123,6 +127,8 @@ def test_cpp_host_layer_matches_python_mirror(visc, bodies, vmap):
     for k in range(steps):
         if bodies and vmap:
             ts.ctx.set_volume_map_motion(0, np.eye(3), position, motion[:3], motion[3:])
+        elif bodies:
+            ts.ctx.set_body_motion(0, np.eye(3), position, motion[:3], motion[3:])
         st = ts.step()
         assert per[k][0] == (st["iterations"], st["iterations_v"], st["visco_iterations"] if visc else 0)
         assert per[k][1] == pytest.approx(st["time"], rel=1e-6)
