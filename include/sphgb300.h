@@ -354,6 +354,18 @@ int sphgb_set_boundary_bodies(sphgb_ctx *ctx, const uint32_t *body, uint32_t nbo
  * Bodies without a call stay in their uploaded pose at rest.  rotation (row-major) / translation
  * NULL keep the current ones; velocity / omega NULL are zero.  One scene (SPHGB_ERR_STATE for a
  * batch); volume-map bodies move with sphgb_set_volume_map_motion. */
+/* Several fluid phases in one scene, as the reference's multiphase scenes hold several FluidModels
+ * of different rest density: the uploaded particles in particle-id order form nphases consecutive
+ * groups of counts[k] particles with rest density density0[k] (mass V density0[k]; the particle
+ * volume V is common).  Every particle's density and density error use its own rest density, the
+ * pressure acceleration sums kappa_i + (density0_j / density0_i) kappa_j (TimeStepDFSPH.cpp:1312),
+ * XSPH weighs neighbours by their own mass, and each solver iteration visits the phases in turn,
+ * each against its own tolerance (:322-339, :476-495), so a phase sees the kappa the phases before
+ * it updated in the same iteration.  nphases <= 1 returns to one phase of sphgb_params.density0.
+ * At the step: SPHGB_ERR_STATE when the counts do not add up to the fluid or for a batch;
+ * SPHGB_ERR_ARGUMENT with Weiler2018 viscosity (the reference solves it per model over same-phase
+ * neighbours) or the learned warm start.  Up to 8 phases. */
+int sphgb_set_fluid_phases(sphgb_ctx *ctx, uint32_t nphases, const uint32_t *counts, const double *density0);
 int sphgb_set_body_motion(sphgb_ctx *ctx, uint32_t body, const double rotation[9], const double translation[3],
                           const double velocity[3], const double omega[3]);
 /* the sums since the last clear, force[3 nbodies] and torque[3 nbodies] (either may be NULL;

@@ -104,6 +104,9 @@ class OrcState(ctypes.Structure):
         ("vmaps", ctypes.c_void_p),
         ("nvmaps", ctypes.c_uint),
         ("vb", ctypes.c_void_p),
+        ("nphase", ctypes.c_uint),
+        ("phase_count", ctypes.c_void_p),
+        ("phase_density0", ctypes.c_void_p),
     ]
 
 
@@ -337,6 +340,15 @@ class OracleSim:
                 self.body_center[b] = translation
         m.v = (ctypes.c_double * 3)(*np.asarray(velocity, np.float64))
         m.w = (ctypes.c_double * 3)(*np.asarray(omega, np.float64))
+
+    def set_phases(self, counts, density0):
+        """several fluid models: the particles in index order form len(counts) phases with the given
+        rest densities"""
+        self._phase_count = np.ascontiguousarray(counts, np.uint32)
+        self._phase_density0 = np.ascontiguousarray(density0, np.float64)
+        self.st.nphase = len(self._phase_count)
+        self.st.phase_count = _ptr(self._phase_count)
+        self.st.phase_density0 = _ptr(self._phase_density0)
 
     def set_boundary_state(self, xb, vb):
         """positions and velocities of the boundary particles for the next steps (moving

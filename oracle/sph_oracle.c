@@ -303,7 +303,16 @@ typedef struct {
     kern K;
     olist F, B;           /* fluid-fluid, fluid-boundary */
     double V, mass, rho0, eps;
+    /* several fluid phases: rest density and phase of each particle, phases, their sizes */
+    double *r0;
+    int *ph;
+    unsigned nph;
 } ctx_t;
+
+/* rest density and mass of particle i: those of its fluid model (FluidModel::getDensity0,
+ * getMass = V density0, FluidModel.cpp:234-253) */
+static inline double rho0_of(const ctx_t *c, long i) { return c->r0 ? c->r0[i] : c->rho0; }
+static inline double mass_of(const ctx_t *c, long i) { return c->V * rho0_of(c, i); }
 
 static inline void diffv(const real *a, const real *b, double r[3])
 {
@@ -343,7 +352,7 @@ static void compute_densities(ctx_t *c)
             diffv(xi, s->xb + 3 * (size_t)j, r);
             dens += (double)s->Vb[j] * kW(&c->K, sqrt(dot3(r, r)));
         }
-        s->density[i] = (real)(dens * c->rho0);
+        s->density[i] = (real)(dens * rho0_of(c, i));
     }
 }
 
@@ -435,18 +444,22 @@ static double velocity_divergence(const ctx_t *c, long i)
     return acc;
 }
 
-/* computePressureAccel, scalar path (TimeStepDFSPH.cpp:1299-1367). */
-static void pressure_accel(ctx_t *c, const real *kap)
+/* computePressureAccel, scalar path (TimeStepDFSPH.cpp:1299-1367), for the particles of one
+ * phase (phase < 0: all). */
+static void pressure_accel(ctx_t *c, const real *kap, int phase)
 {
     orc_state *s = c->s;
 #pragma omp parallel for schedule(static)
     for (long i = 0; i < (long)s->n; i++) {
+        if (phase >= 0 && c->ph[i] != phase) continue;
         const real *xi = s->x + 3 * i;
         const double pi = (double)kap[i];
         double ai[3] = {0, 0, 0};
         for (unsigned k = c->F.off[i]; k < c->F.off[i + 1]; k++) {
             const unsigned j = c->F.idx[k];
-            const double psum = pi + 1.0 * (double)kap[j];  /* density0_j / density0_i = 1 */
+            /* kappa_i + density0_j / density0_i kappa_j (:1312) */
+            const double ratio = c->r0 ? c->r0[j] / c->r0[i] : 1.0;
+            const double psum = pi + ratio * (double)kap[j];
             if (fabs(psum) > c->eps) {
                 double r[3], g[3];
                 diffv(xi, s->x + 3 * (size_t)j, r);
@@ -549,7 +562,7 @@ static void boundary_pressure_forces(ctx_t *c, const real *kap)
             diffv(s->x + 3 * i, s->xb + 3 * (size_t)j, r);
             kGradW(&c->K, r, g);
             const double Vj = (double)s->Vb[j];
-            for (int d = 0; d < 3; d++) f[d] = -c->mass * (pi * (-Vj * g[d]));
+            for (int d = 0; d < 3; d++) f[d] = -mass_of(c, i) * (pi * (-Vj * g[d]));
             add_force(c, j, f);
         }
     }
@@ -614,26 +627,34 @@ static void divergence_solve(ctx_t *c, double h, double *err_buf)
     unsigned it = 0;
     double avg = 0.0;
     int chk = 0;
-    const double eta = invH * c->p->max_error_v * 0.01 * c->rho0;
+    /* one iteration visits the fluid models in turn, each with its own tolerance (:476-495) */
+    const int nph = c->r0 ? (int)c->nph : 1;
     while ((!chk || it < 1) && it < c->p->max_iterations_v) {
-        pressure_accel(c, s->kappa_v);
+        chk = 1;
+        for (int k = 0; k < nph; k++) {
+            const int phase = c->r0 ? k : -1;
+            pressure_accel(c, s->kappa_v, phase);
 #pragma omp parallel for schedule(static)
-        for (long i = 0; i < n; i++) {
-            const double apj = aij_pj(c, i) * h;
-            const double si = -(double)s->density_adv[i];
-            double residuum = si - apj < 0.0 ? si - apj : 0.0;
-            if (num_neighbors(c, i) < 20) residuum = 0.0;
-            double kv = (double)s->kappa_v[i] - 0.5 * (si - apj) * (double)s->factor[i];
-            s->kappa_v[i] = (real)(kv > 0.0 ? kv : 0.0);
-            err_buf[i] = -c->rho0 * residuum;
+            for (long i = 0; i < n; i++) {
+                if (phase >= 0 && c->ph[i] != phase) { err_buf[i] = 0.0; continue; }
+                const double apj = aij_pj(c, i) * h;
+                const double si = -(double)s->density_adv[i];
+                double residuum = si - apj < 0.0 ? si - apj : 0.0;
+                if (num_neighbors(c, i) < 20) residuum = 0.0;
+                double kv = (double)s->kappa_v[i] - 0.5 * (si - apj) * (double)s->factor[i];
+                s->kappa_v[i] = (real)(kv > 0.0 ? kv : 0.0);
+                err_buf[i] = -rho0_of(c, i) * residuum;
+            }
+            const double cnt = phase >= 0 ? (double)s->phase_count[k] : (double)n;
+            const double rho0k = phase >= 0 ? s->phase_density0[k] : c->rho0;
+            avg = serial_sum(err_buf, (size_t)n) / cnt;
+            chk = chk && avg <= invH * c->p->max_error_v * 0.01 * rho0k;
         }
-        avg = serial_sum(err_buf, (size_t)n) / (double)n;
-        chk = avg <= eta;
         it++;
     }
     s->iterations_v = it;
     s->avg_density_err_v = avg;
-    pressure_accel(c, s->kappa_v);
+    pressure_accel(c, s->kappa_v, -1);
     boundary_pressure_forces(c, s->kappa_v);
 #pragma omp parallel for schedule(static)
     for (long i = 0; i < n; i++) {
@@ -656,7 +677,7 @@ static void pressure_solve(ctx_t *c, double h, double *err_buf)
     for (long i = 0; i < n; i++) {
         /* computeDensityAdv (:1190-1243) */
         const double delta = velocity_divergence(c, i);
-        s->density_adv[i] = (real)((double)s->density[i] / c->rho0 + h * delta);
+        s->density_adv[i] = (real)((double)s->density[i] / rho0_of(c, i) + h * delta);
         s->factor[i] = (real)((double)s->factor[i] * invH2);
         if ((double)s->density_adv[i] > 1.0) {
             const double k = (double)s->kappa[i];
@@ -668,25 +689,33 @@ static void pressure_solve(ctx_t *c, double h, double *err_buf)
     unsigned it = 0;
     double avg = 0.0;
     int chk = 0;
-    const double eta = c->p->max_error * 0.01 * c->rho0;
+    /* one iteration visits the fluid models in turn, each with its own tolerance (:322-339) */
+    const int nph = c->r0 ? (int)c->nph : 1;
     while ((!chk || it < c->p->min_iterations) && it < c->p->max_iterations) {
-        pressure_accel(c, s->kappa);
+        chk = 1;
+        for (int m = 0; m < nph; m++) {
+            const int phase = c->r0 ? m : -1;
+            pressure_accel(c, s->kappa, phase);
 #pragma omp parallel for schedule(static)
-        for (long i = 0; i < n; i++) {
-            const double apj = aij_pj(c, i) * h * h;
-            const double si = 1.0 - (double)s->density_adv[i];
-            const double residuum = si - apj < 0.0 ? si - apj : 0.0;
-            const double k = (double)s->kappa[i] - 0.5 * (si - apj) * (double)s->factor[i];
-            s->kappa[i] = (real)(k > 0.0 ? k : 0.0);
-            err_buf[i] = -c->rho0 * residuum;
+            for (long i = 0; i < n; i++) {
+                if (phase >= 0 && c->ph[i] != phase) { err_buf[i] = 0.0; continue; }
+                const double apj = aij_pj(c, i) * h * h;
+                const double si = 1.0 - (double)s->density_adv[i];
+                const double residuum = si - apj < 0.0 ? si - apj : 0.0;
+                const double k = (double)s->kappa[i] - 0.5 * (si - apj) * (double)s->factor[i];
+                s->kappa[i] = (real)(k > 0.0 ? k : 0.0);
+                err_buf[i] = -rho0_of(c, i) * residuum;
+            }
+            const double cnt = phase >= 0 ? (double)s->phase_count[m] : (double)n;
+            const double rho0m = phase >= 0 ? s->phase_density0[m] : c->rho0;
+            avg = serial_sum(err_buf, (size_t)n) / cnt;
+            chk = chk && avg <= c->p->max_error * 0.01 * rho0m;
         }
-        avg = serial_sum(err_buf, (size_t)n) / (double)n;
-        chk = avg <= eta;
         it++;
     }
     s->iterations = it;
     s->avg_density_err = avg;
-    pressure_accel(c, s->kappa);
+    pressure_accel(c, s->kappa, -1);
     boundary_pressure_forces(c, s->kappa);
 #pragma omp parallel for schedule(static)
     for (long i = 0; i < n; i++)
@@ -711,7 +740,7 @@ static void xsph(ctx_t *c, double h)
             double r[3], dv[3];
             diffv(xi, s->x + 3 * (size_t)j, r);
             diffv(vi, s->v + 3 * (size_t)j, dv);
-            const double w = invH * cf * (c->mass / (double)s->density[j]) * kW(&c->K, sqrt(dot3(r, r)));
+            const double w = invH * cf * (mass_of(c, j) / (double)s->density[j]) * kW(&c->K, sqrt(dot3(r, r)));
             ai[0] -= w * dv[0]; ai[1] -= w * dv[1]; ai[2] -= w * dv[2];
         }
         if (cb != 0.0) {
@@ -720,7 +749,7 @@ static void xsph(ctx_t *c, double h)
                 const unsigned j = c->B.idx[k];
                 double r[3];
                 diffv(xi, s->xb + 3 * (size_t)j, r);
-                const double w = invH * cb * (c->rho0 * (double)s->Vb[j] / rhoi) * kW(&c->K, sqrt(dot3(r, r)));
+                const double w = invH * cb * (rho0_of(c, i) * (double)s->Vb[j] / rhoi) * kW(&c->K, sqrt(dot3(r, r)));
                 double vb[3];
                 boundary_velocity(c, j, vb);
                 for (int d = 0; d < 3; d++) ai[d] -= w * ((double)vi[d] - vb[d]);
@@ -737,10 +766,10 @@ static void xsph(ctx_t *c, double h)
                 const unsigned j = c->B.idx[k];
                 double r[3], f[3];
                 diffv(xi, s->xb + 3 * (size_t)j, r);
-                const double w = invH * cb * (c->rho0 * (double)s->Vb[j] / rhoi) * kW(&c->K, sqrt(dot3(r, r)));
+                const double w = invH * cb * (rho0_of(c, i) * (double)s->Vb[j] / rhoi) * kW(&c->K, sqrt(dot3(r, r)));
                 double vb[3];
                 boundary_velocity(c, j, vb);
-                for (int d = 0; d < 3; d++) f[d] = -c->mass * (-w * ((double)vi[d] - vb[d]));
+                for (int d = 0; d < 3; d++) f[d] = -mass_of(c, i) * (-w * ((double)vi[d] - vb[d]));
                 add_force(c, j, f);
             }
         }
@@ -1214,20 +1243,45 @@ int orc_step(orc_state *s, const orc_params *p)
     const long n = (long)s->n;
     int rc = 0;
 
-    /* Bender2019: static bodies without force feedback or boundary viscosity */
+    /* Bender2019: the bodies are the maps (no body array) */
     const int vmaps = p->boundary_method == 2;
     if (vmaps && s->body) return -5;
+    /* several fluid phases: each particle's rest density; Weiler2018 solves per fluid model over
+     * same-phase neighbours, which this restatement does not cover */
+    if (s->nphase > 1) {
+        if (p->viscosity_method == 6) return -6;
+        unsigned total = 0;
+        for (unsigned k = 0; k < s->nphase; k++) total += s->phase_count[k];
+        if (total != s->n) return -6;
+        c.r0 = (double *)malloc(((size_t)n + 1) * sizeof(double));
+        c.ph = (int *)malloc(((size_t)n + 1) * sizeof(int));
+        if (!c.r0 || !c.ph) { free(c.r0); free(c.ph); return -2; }
+        c.nph = s->nphase;
+        long i = 0;
+        for (unsigned k = 0; k < s->nphase; k++)
+            for (unsigned q = 0; q < s->phase_count[k]; q++, i++) {
+                c.r0[i] = s->phase_density0[k];
+                c.ph[i] = (int)k;
+            }
+    }
     real *xb_saved = s->xb, *Vb_saved = s->Vb, *vxb = NULL, *vVb = NULL;
     const unsigned nb_saved = s->nb;
-    if (lists_build(&c.F, s->n, s->x, s->n, s->x, c.K.h, 1, p->fp32_predicate) != 0) return -1;
+    if (lists_build(&c.F, s->n, s->x, s->n, s->x, c.K.h, 1, p->fp32_predicate) != 0) {
+        free(c.r0); free(c.ph);
+        return -1;
+    }
     if (vmaps) {
         /* after the neighbourhood search, before the densities (TimeStepDFSPH.cpp:141-142) */
-        if (volume_maps_boundary(&c, &vxb, &vVb) != 0) { lists_free(&c.F); lists_free(&c.B); return -2; }
+        if (volume_maps_boundary(&c, &vxb, &vVb) != 0) {
+            lists_free(&c.F); lists_free(&c.B); free(c.r0); free(c.ph);
+            return -2;
+        }
         s->xb = vxb;
         s->Vb = vVb;
         s->nb = s->n * s->nvmaps;
     } else if (lists_build(&c.B, s->n, s->x, s->nb, s->xb, c.K.h, 0, p->fp32_predicate) != 0) {
         lists_free(&c.F);
+        free(c.r0); free(c.ph);
         return -1;
     }
     if (s->num_fluid_neighbors)
@@ -1243,6 +1297,7 @@ int orc_step(orc_state *s, const orc_params *p)
         s->nb = nb_saved;
         free(vxb);
         free(vVb);
+        free(c.r0); free(c.ph);
         return -2;
     }
 
@@ -1282,6 +1337,8 @@ int orc_step(orc_state *s, const orc_params *p)
     s->nb = nb_saved;
     free(vxb);
     free(vVb);
+    free(c.r0);
+    free(c.ph);
     return rc;
 }
 

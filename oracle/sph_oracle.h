@@ -112,6 +112,12 @@ typedef struct orc_state {
     /* velocities of the boundary particles [nb][3] (BoundaryModel_Akinci2012::getVelocity of a
      * moving body, SimulatorBase.cpp:1620-1645); NULL: static walls */
     const orc_real *vb;
+    /* fluid phases (several FluidModels in one simulation): the particles in index order form
+     * nphase consecutive groups of phase_count[k] particles with rest density phase_density0[k];
+     * nphase <= 1: one model of density0 */
+    unsigned nphase;
+    const unsigned *phase_count;
+    const double *phase_density0;
 } orc_state;
 
 /* Cubic spline (SPHKernels.h:16-91). */

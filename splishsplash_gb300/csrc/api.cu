@@ -124,6 +124,11 @@ struct sphgb_ctx {
     void *bv = nullptr;                // prepared set: [np] boundary velocity sums of moving maps
     bool vmove = false;                // some map has a velocity
     bool vmaps_dirty = false;          // poses or velocities changed since the device copy
+    // fluid phases (sphgb_set_fluid_phases): particles in id order, count and rest density per phase
+    std::vector<uint32_t> phase_counts;
+    std::vector<double> phase_rho0;
+    void *r0 = nullptr;                // prepared set: rest density per slot
+    uint32_t *ph = nullptr;            // prepared set: phase per slot
     // moving boundary bodies (sphgb_set_body_motion): particles placed and re-sorted every step
     bool bmotion = false, bmot_dirty = false, bm_ready = false;
     std::vector<double> bmot;          // [nbodies][18]: R (row-major), t, v, w
@@ -283,6 +288,8 @@ void free_prepared(sphgb_ctx *c)
     c->bid = c->bscene = nullptr;
     c->binv = nullptr;
     c->bgroup = nullptr;
+    c->r0 = nullptr;
+    c->ph = nullptr;
     c->bm_ready = false;   // the rest shapes and volumes are read again from the new layout
     c->bodies.slot = nullptr;
     c->bodies.blk = nullptr;
@@ -433,6 +440,19 @@ template <class T> DevParams<T> make_params(const sphgb_ctx *c)
     P.vmaps = static_cast<const VMapDev<T> *>(c->d_vmaps);
     P.vmove = (P.nvmaps && c->vmove && c->bv) ? 1 : 0;
     P.bmove = (c->bmotion && c->bm_ready && c->nb && c->boundary_method == 0 && c->nscenes() == 1 && c->bv) ? 1 : 0;
+    P.nphase = 1;
+    if (c->phase_counts.size() > 1 && c->r0) {
+        P.nphase = (uint32_t)c->phase_counts.size();
+        uint32_t end = 0;
+        for (uint32_t k = 0; k < 8; k++) {
+            const bool has = k < P.nphase;
+            P.phase_count[k] = has ? c->phase_counts[k] : 0u;
+            end += P.phase_count[k];
+            P.phase_end[k] = end;
+            P.phase_rho0[k] = has ? (T)c->phase_rho0[k] : P.rho0;
+        }
+        P.staged = 0;   // the staged passes read one rest density
+    }
     return P;
 }
 
@@ -479,6 +499,8 @@ template <class T> DevBufs<T> make_bufs(const sphgb_ctx *c, int view)
     B.vbs = (v4 *)c->vbs;
     B.binv = c->binv;
     B.bgroup = c->bgroup;
+    B.r0 = (T *)c->r0;
+    B.ph = c->ph;
     B.ll = c->ll;
     B.key = c->key;
     B.key2 = c->key2;
@@ -712,6 +734,10 @@ template <class T> int prepare(sphgb_ctx *c)
             if (p) dfree(c->prep_allocs, p);
     }
     if ((rc = build_body_tables(c))) return rc;
+    if (c->phase_counts.size() > 1) {   // fluid phases: rest density and phase per slot (set by the gather)
+        if ((rc = palloc(c, &c->r0, (size_t)std::max(c->np, 1u) * real_size(c)))) return rc;
+        if ((rc = palloc(c, &c->ph, (size_t)std::max(c->np, 1u) * 4))) return rc;
+    }
     if (c->boundary_method == 0 && c->nb) {   // boundary velocity sums of moving bodies
         if ((rc = palloc(c, &c->bv, (size_t)std::max(c->np, 1u) * vec_size(c)))) return rc;
     }
@@ -744,13 +770,18 @@ unsigned gate_sweeps(const sphgb_ctx *c, bool div)
 template <class T> void enqueue_solver_loop_body(sphgb_ctx *c, const DevParams<T> &P, const DevBufs<T> &B, bool div,
                                                  cudaGraphConditionalHandle h, bool use_handle, cudaStream_t s)
 {
-    {
-        PROF(K_PRESSURE_ACCEL, s);
-        launch_pressure_accel<T>(P, B, div, s, h, use_handle);
-    }
-    {
-        PROF(K_JACOBI, s);
-        launch_jacobi<T>(P, B, div, h, use_handle, s);
+    // one iteration: with fluid phases, both passes for each phase in turn (TimeStepDFSPH.cpp:322-339)
+    const int nph = P.nphase > 1 ? (int)P.nphase : 1;
+    for (int k = 0; k < nph; k++) {
+        const int phase = P.nphase > 1 ? k : -1;
+        {
+            PROF(K_PRESSURE_ACCEL, s);
+            launch_pressure_accel<T>(P, B, div, phase, s, h, use_handle);
+        }
+        {
+            PROF(K_JACOBI, s);
+            launch_jacobi<T>(P, B, div, phase, h, use_handle, s);
+        }
     }
 }
 
@@ -1012,10 +1043,17 @@ template <class T> int autotune(sphgb_ctx *c)
     std::vector<StepScalars> saved(S + 1);
     CK(cudaStreamSynchronize(c->stream));
     CK(cudaMemcpy(saved.data(), c->sc, (S + 1) * sizeof(StepScalars), cudaMemcpyDeviceToHost));
-    // the trial steps also add to the body accumulators
+    // the trial steps also add to the body accumulators, and leave their pressure accelerations,
+    // which the next step carries over for fluid phases
     std::vector<double> saved_acc(6 * (size_t)c->nbodies);
     if (c->nbodies)
         CK(cudaMemcpy(saved_acc.data(), c->bodies.acc, saved_acc.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    const size_t pa_bytes = (size_t)std::max(c->np, 1u) * sizeof(v4_t<T>);
+    void *saved_pa = nullptr;
+    if (c->phase_counts.size() > 1) {
+        CK(cudaMalloc(&saved_pa, pa_bytes));
+        CK(cudaMemcpy(saved_pa, c->pa, pa_bytes, cudaMemcpyDeviceToDevice));
+    }
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
@@ -1045,6 +1083,11 @@ template <class T> int autotune(sphgb_ctx *c)
     c->profile = prof;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (saved_pa) {
+        const cudaError_t e = cudaMemcpy(c->pa, saved_pa, pa_bytes, cudaMemcpyDeviceToDevice);
+        cudaFree(saved_pa);
+        if (e != cudaSuccess && !rc) rc = fail(c, SPHGB_ERR_CUDA, "autotune: restoring the pressure accelerations");
+    }
     if (rc) return rc;
     if (c->nbodies)
         CK(cudaMemcpy(c->bodies.acc, saved_acc.data(), saved_acc.size() * sizeof(double), cudaMemcpyHostToDevice));
@@ -1187,10 +1230,27 @@ template <class T> int refresh_body_motion(sphgb_ctx *c)
     return SPHGB_OK;
 }
 
+// Fluid phases: their particle counts cover the fluid; one scene; Weiler2018 (a system per fluid
+// model over same-phase neighbours) and the learned warm start (trained on one rest density) are
+// not available with several phases.
+int check_phases(sphgb_ctx *c)
+{
+    if (c->phase_counts.size() <= 1) return SPHGB_OK;
+    uint64_t total = 0;
+    for (uint32_t n : c->phase_counts) total += n;
+    if (total != c->n) return fail(c, SPHGB_ERR_STATE, "the fluid phases do not cover the uploaded fluid");
+    if (c->nscenes() > 1) return fail(c, SPHGB_ERR_STATE, "fluid phases serve a single scene, not a batch");
+    if (c->prm.viscosity_method == 6)
+        return fail(c, SPHGB_ERR_ARGUMENT, "Weiler2018 viscosity with several fluid phases is not supported");
+    if (c->learned) return fail(c, SPHGB_ERR_ARGUMENT, "the learned warm start takes one fluid phase");
+    return SPHGB_OK;
+}
+
 template <class T> int do_step(sphgb_ctx *c)
 {
     int rc;
     if ((rc = check_boundary_method(c))) return rc;
+    if ((rc = check_phases(c))) return rc;
     if (!c->prepared && (rc = prepare<T>(c))) return rc;
     if (c->vmaps_dirty && (rc = refresh_vmaps<T>(c))) return rc;
     if ((rc = prepare_body_motion<T>(c))) return rc;
@@ -2126,6 +2186,28 @@ int sphgb_clear_volume_maps(sphgb_ctx *c)
     CK(cudaStreamSynchronize(c->stream));
     free_vmaps(c);
     c->prepared = false;
+    invalidate_graphs(c);
+    return SPHGB_OK;
+}
+
+int sphgb_set_fluid_phases(sphgb_ctx *c, uint32_t nphases, const uint32_t *counts, const double *density0)
+{
+    if (!c || nphases > 8 || (nphases > 1 && (!counts || !density0))) return SPHGB_ERR_ARGUMENT;
+    for (uint32_t k = 0; k < nphases && nphases > 1; k++)
+        if (!(std::isfinite(density0[k]) && density0[k] > 0.0))
+            return fail(c, SPHGB_ERR_ARGUMENT, "a phase's rest density must be positive");
+    if (c->step_pending) {
+        sphgb_stats st;
+        fill_stats(c, &st);
+    }
+    if (nphases > 1) {
+        c->phase_counts.assign(counts, counts + nphases);
+        c->phase_rho0.assign(density0, density0 + nphases);
+    } else {
+        c->phase_counts.clear();
+        c->phase_rho0.clear();
+    }
+    c->prepared = false;   // the per-slot rest densities
     invalidate_graphs(c);
     return SPHGB_OK;
 }

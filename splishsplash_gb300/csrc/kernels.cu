@@ -199,6 +199,24 @@ __device__ __forceinline__ void kernel_W_coef_d2(const Kernel<double> &K, double
     c = kernel_gradW_coef(K, rl);
 }
 
+// rest density of the particle in slot i: its fluid phase's (FluidModel::getDensity0), else density0
+template <class T> __device__ __forceinline__ T rho0_at(const DevParams<T> &P, const DevBufs<T> &B, uint32_t i)
+{
+    return P.nphase > 1 ? B.r0[i] : P.rho0;
+}
+// particles of phase k (counted, rest density) without dynamic indexing of the parameter arrays
+template <class T> __device__ __forceinline__ void phase_info(const DevParams<T> &P, int k, uint32_t &count, T &rho0)
+{
+    count = P.phase_count[0];
+    rho0 = P.phase_rho0[0];
+#pragma unroll
+    for (int q = 1; q < 8; q++)
+        if (q == k) {
+            count = P.phase_count[q];
+            rho0 = P.phase_rho0[q];
+        }
+}
+
 template <class T> __device__ __forceinline__ V3<T> diff3(const v4_t<T> &a, const v4_t<T> &b)
 {
     return V3<T>{(T)a.x - (T)b.x, (T)a.y - (T)b.y, (T)a.z - (T)b.z};
@@ -328,6 +346,20 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevParams<T> P, DevBufs<T> B,
     B.kappa_v2[k] = B.kappa_v[s];
     B.id2[k] = B.id[s];
     B.cellid2[k] = B.cellid[s];
+    if (P.nphase > 1) {   // the phase and rest density of the particle now in slot k
+        stv(B.a, k, ldv(B.pa, s));   // its last pressure acceleration, put back by the list build
+        const uint32_t id = B.id[s];
+        uint32_t ph = 0;
+        T r0 = P.phase_rho0[0];
+#pragma unroll
+        for (int q = 0; q < 7; q++)
+            if (q + 1 < (int)P.nphase && id >= P.phase_end[q]) {
+                ph = (uint32_t)(q + 1);
+                r0 = P.phase_rho0[q + 1];
+            }
+        B.ph[k] = ph;
+        B.r0[k] = r0;
+    }
 }
 
 // first / one-past-last slot of every non-empty cell (cells of a scene are sorted within the scene's slots)
@@ -734,7 +766,7 @@ __device__ __forceinline__ void build_one(const DevParams<T> &P, const DevBufs<T
     nb_out = nb;
 
     // density: rho0 * (V W0 + sum_f V W + sum_b Vb W)
-    const T rho = P.rho0 * (P.V * P.K.w0 + P.V * wf + wb);
+    const T rho = rho0_at(P, B, i) * (P.V * P.K.w0 + P.V * wf + wb);
     B.density[i] = rho;
     // factor: 1 / (sum_f |V gradW|^2 + |sum_f V gradW + sum_b Vb gradW|^2)
     const V3<T> gpi = add(scl(gf, P.V), gb);
@@ -771,6 +803,14 @@ __device__ __forceinline__ void build_one(const DevParams<T> &P, const DevBufs<T
     v4_t<T> xk = xi;
     xk.w = kv;
     stv(B.xk, i, xk);
+    if (P.nphase > 1) {   // fluid phases: each particle's last pressure acceleration, in its new slot
+        const v4_t<T> a = ldv(B.a, i);
+        stv(B.pa, i, a);
+        if constexpr (sizeof(T) == 4) {   // the whole (x, a) record: a pass writes only its own phase's
+            B.xa[2 * (size_t)i] = ldv(B.x, i);
+            B.xa[2 * (size_t)i + 1] = make_float4((float)a.x, (float)a.y, (float)a.z, 0.0f);
+        }
+    }
 }
 
 template <class T>
@@ -807,7 +847,7 @@ __global__ void __launch_bounds__(kBlock) k_build(DevParams<T> P, DevBufs<T> B)
 // Every lane of the particle returns the full acceleration.
 // Staged (sx != null, one lane per particle): the neighbours' xk records come from the block's
 // shared copy through the local list, in the order of the fluid list, so the sums are the same.
-template <int LPP, class T>
+template <int LPP, bool MP = false, class T>
 __device__ __forceinline__ V3<T> pressure_accel_g(const DevParams<T> &P, const DevBufs<T> &B, const SlotInfo &q,
                                                   const v4_t<T> *sx = nullptr)
 {
@@ -817,8 +857,10 @@ __device__ __forceinline__ V3<T> pressure_accel_g(const DevParams<T> &P, const D
     if (q.act) {
         xi = ldv(B.xk, q.i);
         pi = (T)xi.w;
-        auto cp = [&](uint32_t, const v4_t<T> &xj) {
-            const T psum = pi + (T)xj.w;
+        const T r0i = MP ? B.r0[q.i] : T(1);
+        auto cp = [&](uint32_t j, const v4_t<T> &xj) {
+            // kappa_i + density0_j / density0_i kappa_j (TimeStepDFSPH.cpp:1312); one phase: ratio 1
+            const T psum = MP ? pi + (B.r0[j] / r0i) * (T)xj.w : pi + (T)xj.w;
             if (fabs(psum) > P.eps) {
                 const V3<T> r = diff3<T>(xi, xj);
                 const T c = grad_coef_d2(P.K, dot(r, r)) * psum;
@@ -909,25 +951,27 @@ __device__ __forceinline__ F8 ld_f8(const float4 *p)
 
 // Pressure accelerations of the running solver.  FP32: also the (x_i, a_i) record that the
 // Jacobi pass gathers with one 256-bit load per neighbour.
-template <class T, int LPP>
+template <class T, int LPP, bool MP = false>
 __global__ void __launch_bounds__(kBlock, kPressureMinBlocks<T, LPP>) k_pressure_accel(DevParams<T> P, DevBufs<T> B,
                                                                                       unsigned limit,
-                                                            cudaGraphConditionalHandle h, int use_handle)
+                                                            cudaGraphConditionalHandle h, int use_handle, int phase)
 {
     count_launch(&B.gsc->launches);
-    loop_guard(B.gsc, limit, h, use_handle);
-    const SlotInfo q = slot_info<LPP>(P);
+    if (phase <= 0) loop_guard(B.gsc, limit, h, use_handle);   // once per loop body
+    SlotInfo q = slot_info<LPP>(P);
     if (!scene_live(P, B.sc + q.s)) return;   // block uniform
+    // fluid phases: this launch updates the particles of one phase; the others keep their last a
+    if (phase >= 0 && q.act && B.ph[q.i] != (uint32_t)phase) q.act = false;
     V3<T> a;
     if constexpr (LPP == 1 && sizeof(T) == 4) {
         extern __shared__ float4 stage_f4[];   // kStageCap records when staged
         if (P.staged && stage_in(B, q.b, kStageCap, [&](uint32_t j) { return ldv(B.xk, j); },
                                  [&](uint32_t m, const float4 &r) { stage_f4[m] = r; }))
-            a = pressure_accel_g<LPP>(P, B, q, stage_f4);
+            a = pressure_accel_g<LPP, MP>(P, B, q, stage_f4);
         else
-            a = pressure_accel_g<LPP>(P, B, q);
+            a = pressure_accel_g<LPP, MP>(P, B, q);
     } else {
-        a = pressure_accel_g<LPP>(P, B, q);
+        a = pressure_accel_g<LPP, MP>(P, B, q);
     }
     if (!q.act || q.l != 0) return;
     if constexpr (sizeof(T) == 4) {
@@ -1001,8 +1045,10 @@ __device__ __forceinline__ double aij_pj_g(const DevParams<double> &P, const Dev
 // the while conditions of TimeStepDFSPH.cpp:477 (divergence: at least one iteration, error
 // below maxErrorV percent of rho0 per second) and :324 (pressure: at least minIterations,
 // error below maxError percent of rho0), both capped by the maximum iteration count.
+// With fluid phases the caller passes chk = every phase met its tolerance (phase_chk = 0 or 1).
 template <class T, bool DIV>
-__device__ __forceinline__ void solver_decide(const DevParams<T> &P, StepScalars *sc, double avg, unsigned inc = 1)
+__device__ __forceinline__ void solver_decide(const DevParams<T> &P, StepScalars *sc, double avg, unsigned inc = 1,
+                                              int phase_chk = -1)
 {
     unsigned it;
     bool cont;
@@ -1010,13 +1056,13 @@ __device__ __forceinline__ void solver_decide(const DevParams<T> &P, StepScalars
         it = (sc->iters_v += inc);
         sc->avg_err_v = avg;
         const double eta = (1.0 / sc->dt) * P.max_error_v * 0.01 * (double)P.rho0;
-        const bool chk = avg <= eta;
+        const bool chk = phase_chk >= 0 ? phase_chk != 0 : avg <= eta;
         cont = (!chk || it < 1u) && it < P.max_iter_v;
     } else {
         it = (sc->iters += inc);
         sc->avg_err = avg;
         const double eta = P.max_error * 0.01 * (double)P.rho0;
-        const bool chk = avg <= eta;
+        const bool chk = phase_chk >= 0 ? phase_chk != 0 : avg <= eta;
         cont = (!chk || it < P.min_iter) && it < P.max_iter;
     }
     sc->cont = cont ? 1u : 0u;
@@ -1027,10 +1073,12 @@ __device__ __forceinline__ void solver_decide(const DevParams<T> &P, StepScalars
 // loop decision (the while conditions of :477 and :324), per scene.
 template <class T, bool DIV, int LPP>
 __global__ void __launch_bounds__(kBlock) k_jacobi(DevParams<T> P, DevBufs<T> B, cudaGraphConditionalHandle handle,
-                                                     int use_handle)
+                                                     int use_handle, int phase)
 {
     count_launch(&B.gsc->launches);
-    const SlotInfo q = slot_info<LPP>(P);
+    SlotInfo q = slot_info<LPP>(P);
+    // fluid phases: this launch updates the particles of one phase (TimeStepDFSPH.cpp:322-339)
+    if (phase >= 0 && q.act && B.ph[q.i] != (uint32_t)phase) q.act = false;
     StepScalars *const sc = B.sc + q.s;
     const bool live = scene_live(P, sc);
     double err = 0.0;
@@ -1065,7 +1113,7 @@ __global__ void __launch_bounds__(kBlock) k_jacobi(DevParams<T> P, DevBufs<T> B,
                 const T kv = kap[i] - T(0.5) * (si - apj) * fac;
                 kap[i] = kv > T(0) ? kv : T(0);
                 store_w(B.xk, i, kap[i]);
-                err = -(double)P.rho0 * (double)residuum;
+                err = -(double)rho0_at(P, B, i) * (double)residuum;
             } else {
                 apj *= h * h;
                 const T si = T(1) - B.dadv[i];
@@ -1074,7 +1122,7 @@ __global__ void __launch_bounds__(kBlock) k_jacobi(DevParams<T> P, DevBufs<T> B,
                 const T kv = kap[i] - T(0.5) * (si - apj) * fac;
                 kap[i] = kv > T(0) ? kv : T(0);
                 store_w(B.xk, i, kap[i]);
-                err = -(double)P.rho0 * (double)residuum;
+                err = -(double)rho0_at(P, B, i) * (double)residuum;
             }
         }
     }
@@ -1083,9 +1131,24 @@ __global__ void __launch_bounds__(kBlock) k_jacobi(DevParams<T> P, DevBufs<T> B,
     const DevParams<T> &PP = P;
     const DevBufs<T> &BB = B;
     const uint32_t n_s = q.end - q.begin;
+    const int ph = phase;
     grid_sum_finalize<1>(mine, scene_reduce<LPP>(P, B, q), [&](const DSum<1> &tot) {
-        if (live) solver_decide<T, DIV>(PP, sc, n_s ? tot.v[0] / (double)n_s : 0.0);
-        batch_decide(PP, BB, handle, use_handle);
+        if (ph < 0) {
+            if (live) solver_decide<T, DIV>(PP, sc, n_s ? tot.v[0] / (double)n_s : 0.0);
+            batch_decide(PP, BB, handle, use_handle);
+        } else {   // one phase's average error against its own tolerance; the last phase decides
+            uint32_t cnt;
+            T r0;
+            phase_info(PP, ph, cnt, r0);
+            const double avg = cnt ? tot.v[0] / (double)cnt : 0.0;
+            const double eta = DIV ? (1.0 / sc->dt) * PP.max_error_v * 0.01 * (double)r0 : PP.max_error * 0.01 * (double)r0;
+            const unsigned ok = avg <= eta ? (1u << ph) : 0u;
+            sc->phase_ok = ph == 0 ? ok : (sc->phase_ok | ok);
+            if (ph + 1 == (int)PP.nphase) {
+                solver_decide<T, DIV>(PP, sc, avg, 1u, sc->phase_ok == (1u << PP.nphase) - 1u);
+                batch_decide(PP, BB, handle, use_handle);
+            }
+        }
     });
 }
 
@@ -1096,7 +1159,10 @@ __global__ void __launch_bounds__(kBlock) k_solver_finalize(DevParams<T> P, DevB
 {
     count_launch(&B.gsc->launches);
     const SlotInfo q = slot_info<LPP>(P);
-    const V3<T> a = pressure_accel_g<LPP>(P, B, q);
+    const V3<T> a = P.nphase > 1 ? pressure_accel_g<LPP, true>(P, B, q) : pressure_accel_g<LPP>(P, B, q);
+    // fluid phases: the next solver's first iteration reads the other phases' last a in the record
+    if constexpr (sizeof(T) == 4)
+        if (P.nphase > 1 && q.act && q.l == 0) B.xa[2 * (size_t)q.i + 1] = make_float4(a.x, a.y, a.z, 0.0f);
     if (!q.act || q.l != 0) return;
     const StepScalars *sc = B.sc + q.s;
     const T h = (T)(DIV ? sc->dt : sc->dt_next);
@@ -1164,9 +1230,10 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams<T> P, DevBufs<T> B, i
             T rho;
         };
         fluid_loop<LPP, kUnroll>(P, B, q.i, q.l, [&](uint32_t j) { return XVR{ldv(B.x, j), ldv(B.v, j), B.density[j]}; },
-                                 [&](uint32_t, const XVR &d) {
+                                 [&](uint32_t j, const XVR &d) {
                                      const V3<T> r = diff3<T>(xi, d.x);
-                                     const T w = (P.mass / d.rho) * kernel_W(P.K, dev_sqrt(dot(r, r)));
+                                     const T mj = P.nphase > 1 ? P.V * B.r0[j] : P.mass;
+                                     const T w = (mj / d.rho) * kernel_W(P.K, dev_sqrt(dot(r, r)));
                                      acc = add(acc, scl(sub(vi, xyz<T>(d.v)), w));
                                  });
     }
@@ -1180,10 +1247,11 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams<T> P, DevBufs<T> B, i
     if (P.xsph != T(0)) ai = sub(ai, scl(acc, invH * P.xsph));
     if (P.xsph_b != T(0)) {
         // sum_b (rho0 V_b / rho_i) W_ib from the per-step boundary sum
-        const T wsum = P.rho0 * (T)ldv(B.bg, i).w / B.density[i];
+        const T r0i = rho0_at(P, B, i);
+        const T wsum = r0i * (T)ldv(B.bg, i).w / B.density[i];
         if (P.vmove || P.bmove) {   // moving boundaries: (v_i - v_b) W
             const V3<T> dv = sub(scl(vi, (T)ldv(B.bg, i).w), xyz<T>(ldv(B.bv, i)));
-            ai = sub(ai, scl(dv, invH * P.xsph_b * P.rho0 / B.density[i]));
+            ai = sub(ai, scl(dv, invH * P.xsph_b * r0i / B.density[i]));
         } else {
             ai = sub(ai, scl(vi, invH * P.xsph_b * wsum));
         }
@@ -1631,7 +1699,7 @@ __global__ void __launch_bounds__(kBlock) k_press_init(DevParams<T> P, DevBufs<T
     const T h = (T)B.sc[q.s].dt_next;
     T accb = dot(vi, xyz<T>(ldv(B.bg, i)));
     if (P.vmove || P.bmove) accb -= (T)ldv(B.bv, i).w;   // moving boundaries: (v_i - v_b) . gradW
-    const T dadv = B.density[i] / P.rho0 + h * (accf * P.V + accb);
+    const T dadv = B.density[i] / rho0_at(P, B, i) + h * (accf * P.V + accb);
     B.dadv[i] = dadv;
     const T invH2 = T(1) / (h * h);
     const T k = B.kappa[i];
@@ -1756,14 +1824,17 @@ __global__ void __launch_bounds__(kBlock) k_body_forces(DevParams<T> P, DevBufs<
                         const V3<T> r = mk3<T>(rx, ry, rz);
                         const T gc = grad_coef_d2(P.K, d2);
                         V3<T> fi = mk3<T>(0, 0, 0);
+                        // fluid phases: the neighbour's mass and rest density
+                        const T mi = P.nphase > 1 ? P.V * B.r0[i] : P.mass;
                         if (press) {
                             const T kap = (T)xk.w;
-                            if (fabs(kap) > P.eps) fi = scl(r, P.mass * kap * Vb * gc);
+                            if (fabs(kap) > P.eps) fi = scl(r, mi * kap * Vb * gc);
                         }
                         if (xs || visc) {
                             const T rhoi = B.density[i];
                             if (xs) {
-                                const T w = P.mass * xs_c / rhoi * kernel_W(P.K, dev_sqrt(d2));
+                                const T xsc = P.nphase > 1 ? xs_c * (B.r0[i] / P.rho0) : xs_c;
+                                const T w = mi * xsc / rhoi * kernel_W(P.K, dev_sqrt(d2));
                                 V3<T> dv = xyz<T>(ldv(B.v, i));
                                 if (P.bmove) dv = sub(dv, vbj);
                                 fi = add(fi, scl(dv, w));
@@ -1825,10 +1896,11 @@ __global__ void __launch_bounds__(kBlock) k_vmap_forces(DevParams<T> P, DevBufs<
                 const V3<T> r = diff3<T>(xk, xj);
                 const T d2 = dot(r, r);
                 V3<T> f = mk3<T>(0, 0, 0);
-                if (press && fabs(kap) > P.eps) f = scl(r, P.mass * kap * Vj * grad_coef_d2(P.K, d2));
+                const T mi = P.nphase > 1 ? P.V * B.r0[i] : P.mass;   // fluid phases
+                if (press && fabs(kap) > P.eps) f = scl(r, mi * kap * Vj * grad_coef_d2(P.K, d2));
                 const VMapDev<T> &mp = P.vmaps[b];
                 if (xs) {
-                    const T w = P.mass * P.xsph_b / (T)B.sc[q.s].dt * P.rho0 * Vj / B.density[i] *
+                    const T w = mi * P.xsph_b / (T)B.sc[q.s].dt * rho0_at(P, B, i) * Vj / B.density[i] *
                                 kernel_W(P.K, dev_sqrt(d2));
                     V3<T> dv = xyz<T>(ldv(B.v, i));
                     if (P.vmove) dv = sub(dv, vmap_point_velocity<T>(mp, xyz<T>(xj)));
@@ -2507,26 +2579,32 @@ template <class T> void launch_build(const DevParams<T> &P, const DevBufs<T> &B,
 {
     if (P.np) k_build<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
 }
-template <class T> void launch_pressure_accel(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s,
+template <class T> void launch_pressure_accel(const DevParams<T> &P, const DevBufs<T> &B, bool div, int phase, cudaStream_t s,
                                               cudaGraphConditionalHandle h, bool use_handle)
 {
     const unsigned limit = (div ? P.max_iter_v : P.max_iter) + 1;
     if (P.np)
-        LPP_DISPATCH(P, (k_pressure_accel<T, L><<<grid_lpp(P.np, L), kBlock, stage_bytes(P, L, kStageBytesPressure), s>>>(
-                            P, B, limit, h, use_handle ? 1 : 0)));
+    {
+        if (P.nphase > 1)   // fluid phases: the rest-density ratio in the pressure term
+            LPP_DISPATCH(P, (k_pressure_accel<T, L, true><<<grid_lpp(P.np, L), kBlock, 0, s>>>(
+                                P, B, limit, h, use_handle ? 1 : 0, phase)));
+        else
+            LPP_DISPATCH(P, (k_pressure_accel<T, L><<<grid_lpp(P.np, L), kBlock, stage_bytes(P, L, kStageBytesPressure), s>>>(
+                                P, B, limit, h, use_handle ? 1 : 0, phase)));
+    }
 }
 template <class T>
-void launch_jacobi(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaGraphConditionalHandle h, bool use_handle,
-                   cudaStream_t s)
+void launch_jacobi(const DevParams<T> &P, const DevBufs<T> &B, bool div, int phase, cudaGraphConditionalHandle h,
+                   bool use_handle, cudaStream_t s)
 {
     if (!P.np) return;
     const int uh = use_handle ? 1 : 0;
     if (div)
         LPP_DISPATCH(P, (k_jacobi<T, true, L><<<grid_lpp(P.np, L), kBlock, stage_bytes(P, L, kStageBytesJacobi), s>>>(
-                            P, B, h, uh)));
+                            P, B, h, uh, phase)));
     else
         LPP_DISPATCH(P, (k_jacobi<T, false, L><<<grid_lpp(P.np, L), kBlock, stage_bytes(P, L, kStageBytesJacobi), s>>>(
-                            P, B, h, uh)));
+                            P, B, h, uh, phase)));
 }
 template <class T> void launch_solver_finalize(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s)
 {
@@ -2702,10 +2780,10 @@ void launch_lists_to_ids(const uint32_t *list, const uint32_t *cnt, uint32_t cap
     template void launch_build<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                          \
     template void launch_stage_table<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                    \
     template void launch_vmap_boundary<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                  \
-    template void launch_pressure_accel<T>(const DevParams<T> &, const DevBufs<T> &, bool, cudaStream_t,            \
+    template void launch_pressure_accel<T>(const DevParams<T> &, const DevBufs<T> &, bool, int, cudaStream_t,       \
                                            cudaGraphConditionalHandle, bool);                                       \
-    template void launch_jacobi<T>(const DevParams<T> &, const DevBufs<T> &, bool, cudaGraphConditionalHandle, bool, \
-                                   cudaStream_t);                                                                   \
+    template void launch_jacobi<T>(const DevParams<T> &, const DevBufs<T> &, bool, int, cudaGraphConditionalHandle,  \
+                                   bool, cudaStream_t);                                                             \
     template void launch_solver_finalize<T>(const DevParams<T> &, const DevBufs<T> &, bool, cudaStream_t);          \
     template void launch_loop_begin<T>(const DevParams<T> &, const DevBufs<T> &, bool, cudaStream_t);               \
     template void launch_step_begin<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                     \

@@ -42,6 +42,7 @@ struct StepScalars {
     unsigned ws_used;      // bit 0: learned warm start used by the divergence solve, bit 1: pressure solve
     unsigned pad[2];
     unsigned long long maxvel_bits64;   // FP64 contexts: max |v + a h|^2 as the bits of a non-negative double
+    unsigned phase_ok;  // fluid phases: bit k set when phase k met its tolerance in the running iteration
 };
 
 constexpr unsigned kFlagOverflow = 1u;
@@ -91,6 +92,11 @@ template <class T> struct DevParams {
     uint32_t nvmaps;              // Bender2019 boundary: volume maps (bodies); 0 = Akinci2012 particles
     const VMapDev<T> *vmaps;      // device array [nvmaps]
     int vmove;                    // some volume-map body moves: boundary terms use v_i - v_b
+    // fluid phases (several fluid models of one scene): particle ids [phase_end[k-1], phase_end[k])
+    // form phase k of rest density phase_rho0[k] and phase_count[k] particles; nphase <= 1: one model
+    uint32_t nphase;
+    uint32_t phase_end[8], phase_count[8];
+    T phase_rho0[8];
     int bmove;                    // boundary particles move with their bodies: placed and re-sorted every
                                   // step, with velocities (one scene)
     int staged;                   // FP32, one lane per particle: the solver passes read their block's
@@ -134,6 +140,8 @@ template <class T> struct DevBufs {
     v4 *xk;                      // x_i with the running solver's kappa_i in w (one gather per pair)
     v4 *bg;                      // per-particle boundary sums: xyz = sum_b V_b gradW_ib, w = sum_b V_b W_ib
     v4 *bx;                      // Bender2019: [nvmaps][np] boundary point x_j of each particle's map sample, w = V_j
+    T *r0;                       // fluid phases: rest density of slot i
+    uint32_t *ph;                // fluid phases: phase of slot i
     v4 *vbs;                     // moving boundary bodies: velocity of sorted boundary particle k
     uint32_t *binv;              // sorted slot of boundary particle u (upload order)
     const uint32_t *bgroup;      // volume group of boundary particle u (upload order): 0 the static bodies,
@@ -240,9 +248,10 @@ void launch_boundary_move(const DevParams<T> &P, const DevBufs<T> &B, const Boun
 template <class T>
 void launch_boundary_regather(const DevParams<T> &P, const DevBufs<T> &B, const BoundaryMoveDev<T> &M,
                               const uint32_t *perm, uint32_t *cells, cudaStream_t s);
-template <class T> void launch_pressure_accel(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s,
+// phase: with fluid phases, the phase whose particles the pass updates (-1: all particles)
+template <class T> void launch_pressure_accel(const DevParams<T> &P, const DevBufs<T> &B, bool div, int phase, cudaStream_t s,
                                               cudaGraphConditionalHandle h = 0, bool use_handle = false);
-template <class T> void launch_jacobi(const DevParams<T> &P, const DevBufs<T> &B, bool div,
+template <class T> void launch_jacobi(const DevParams<T> &P, const DevBufs<T> &B, bool div, int phase,
                                       cudaGraphConditionalHandle h, bool use_handle, cudaStream_t s);
 template <class T> void launch_solver_finalize(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s);
 template <class T> void launch_xsph(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);

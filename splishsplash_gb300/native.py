@@ -126,7 +126,7 @@ EXPORTS = [
     "sphgb_set_boundary_bodies", "sphgb_boundary_forces", "sphgb_clear_boundary_forces",
     "sphgb_set_neighbor_staging", "sphgb_get_neighbor_staging",
     "sphgb_add_volume_map", "sphgb_add_volume_map_values", "sphgb_get_volume_map", "sphgb_clear_volume_maps",
-    "sphgb_set_boundary_method", "sphgb_set_volume_map_motion", "sphgb_set_body_motion",
+    "sphgb_set_boundary_method", "sphgb_set_volume_map_motion", "sphgb_set_body_motion", "sphgb_set_fluid_phases",
 ]
 
 _lib = None
@@ -194,6 +194,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.sphgb_set_boundary_method.argtypes = [vp, i32]
     L.sphgb_set_volume_map_motion.argtypes = [vp, u32, vp, vp, vp, vp]
     L.sphgb_set_body_motion.argtypes = [vp, u32, vp, vp, vp, vp]
+    L.sphgb_set_fluid_phases.argtypes = [vp, u32, vp, vp]
     L.sphgb_get_neighbor_staging.argtypes = [vp, ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_float),
                                              ctypes.POINTER(ctypes.c_float)]
     L.sphgb_profile_enable.argtypes = [vp, i32]
@@ -567,6 +568,15 @@ class Context:
             if a is not None and a.size != n:
                 raise ValueError("rotation needs 9 values, translation / velocity / omega 3")
         self._check(self.L.sphgb_set_volume_map_motion(self.h, int(body), *[None if a is None else _p(a) for a in arrs]))
+
+    def set_fluid_phases(self, counts=(), density0=()):
+        """Fluid phases: the particles in id order form len(counts) phases of the given rest
+        densities; () returns to one phase."""
+        c = np.ascontiguousarray(counts, np.uint32)
+        d = np.ascontiguousarray(density0, np.float64)
+        if c.size != d.size:
+            raise ValueError("one rest density per phase")
+        self._check(self.L.sphgb_set_fluid_phases(self.h, c.size, _p(c) if c.size else None, _p(d) if d.size else None))
 
     def set_body_motion(self, body: int, rotation=None, translation=None, velocity=None, omega=None):
         """Pose and velocity of boundary body `body` (its particles uploaded in body coordinates) for
