@@ -1154,15 +1154,15 @@ __global__ void __launch_bounds__(kBlock) k_jacobi(DevParams<T> P, DevBufs<T> B,
 
 // final pressure acceleration and velocity update of both solvers
 // (TimeStepDFSPH.cpp:500-520 and :345-363)
-template <class T, bool DIV, int LPP>
+template <class T, bool DIV, int LPP, bool MP = false>
 __global__ void __launch_bounds__(kBlock) k_solver_finalize(DevParams<T> P, DevBufs<T> B)
 {
     count_launch(&B.gsc->launches);
     const SlotInfo q = slot_info<LPP>(P);
-    const V3<T> a = P.nphase > 1 ? pressure_accel_g<LPP, true>(P, B, q) : pressure_accel_g<LPP>(P, B, q);
+    const V3<T> a = pressure_accel_g<LPP, MP>(P, B, q);
     // fluid phases: the next solver's first iteration reads the other phases' last a in the record
-    if constexpr (sizeof(T) == 4)
-        if (P.nphase > 1 && q.act && q.l == 0) B.xa[2 * (size_t)q.i + 1] = make_float4(a.x, a.y, a.z, 0.0f);
+    if constexpr (sizeof(T) == 4 && MP)
+        if (q.act && q.l == 0) B.xa[2 * (size_t)q.i + 1] = make_float4(a.x, a.y, a.z, 0.0f);
     if (!q.act || q.l != 0) return;
     const StepScalars *sc = B.sc + q.s;
     const T h = (T)(DIV ? sc->dt : sc->dt_next);
@@ -2609,8 +2609,13 @@ void launch_jacobi(const DevParams<T> &P, const DevBufs<T> &B, bool div, int pha
 template <class T> void launch_solver_finalize(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s)
 {
     if (!P.np) return;
-    if (div) LPP_DISPATCH(P, (k_solver_finalize<T, true, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B)));
-    else LPP_DISPATCH(P, (k_solver_finalize<T, false, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B)));
+    if (P.nphase > 1) {   // fluid phases: the rest-density ratio
+        if (div) LPP_DISPATCH(P, (k_solver_finalize<T, true, L, true><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B)));
+        else LPP_DISPATCH(P, (k_solver_finalize<T, false, L, true><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B)));
+    } else {
+        if (div) LPP_DISPATCH(P, (k_solver_finalize<T, true, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B)));
+        else LPP_DISPATCH(P, (k_solver_finalize<T, false, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B)));
+    }
 }
 template <class T> void launch_step_begin(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {
