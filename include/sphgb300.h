@@ -385,7 +385,8 @@ int sphgb_clear_boundary_forces(sphgb_ctx *ctx, int32_t body);
  * is moved back by min(2 r - phi, r / 10) and stopped, as in the reference.  The Weiler2018
  * boundary viscosity samples each x_j at the four points x_j -+ t1 h / 2, x_j -+ t2 h / 2 of the
  * tangent plane, a quarter of V_j each (Viscosity_Weiler2018.cpp:205-255).  Supported: one
- * scene, no boundary particles uploaded; moving bodies through sphgb_set_volume_map_motion; force
+ * no boundary particles uploaded; in a batch every map belongs to one scene
+ * (sphgb_set_volume_map_scene); moving bodies through sphgb_set_volume_map_motion; force
  * feedback with one body per map
  * (sphgb_set_boundary_bodies); other combinations fail at the step with SPHGB_ERR_STATE /
  * SPHGB_ERR_ARGUMENT.
@@ -411,6 +412,10 @@ int sphgb_get_volume_map(sphgb_ctx *ctx, uint32_t body, uint32_t resolution[3], 
                          double *distance, double *volume);
 int sphgb_clear_volume_maps(sphgb_ctx *ctx);
 int sphgb_set_boundary_method(sphgb_ctx *ctx, int method);
+/* The scene of a batch (sphgb_upload_scenes) that volume map `body` belongs to (default 0): the
+ * particles of each scene see only the maps of their scene, and a scene's step size only its
+ * moving maps.  SPHGB_ERR_ARGUMENT at the step for a scene that is not uploaded. */
+int sphgb_set_volume_map_scene(sphgb_ctx *ctx, uint32_t body, uint32_t scene);
 /* Pose and velocity of the body of volume map `body` for the following steps, as the reference
  * reads them from the map's rigid body every step (BoundaryModel_Bender2019 with a dynamic or
  * animated RigidBodyObject): the map is sampled at R^T (x - t) (TimeStep.cpp:219-340), and the

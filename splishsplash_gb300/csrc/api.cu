@@ -113,13 +113,17 @@ struct sphgb_ctx {
         double dmin[3], dmax[3], R[9], t[3];
         double v[3] = {0, 0, 0}, w[3] = {0, 0, 0};   // the body's velocity and angular velocity
         double max_dist = 0;                         // CFL radius: mesh vertices from their mean (0 without a mesh)
+        uint32_t scene = 0;                          // the scene of a batch the body belongs to
         double support;                // support radius the map was built for
         double *f0 = nullptr, *f1 = nullptr;   // node fields (FP64)
         void *coef = nullptr;                  // per-cell coefficients in the context's precision
     };
     int boundary_method = 0;           // 0 Akinci2012, 2 Bender2019
     std::vector<VMap> vmaps;
-    void *d_vmaps = nullptr;           // VMapDev<T>[vmaps.size()]
+    void *d_vmaps = nullptr;           // VMapDev<T>[vmaps.size()], ordered by scene
+    void *d_vmap_range = nullptr;      // batches: uint2 per scene (first map, count)
+    void *d_vmap_info = nullptr;       // batches: uint4 per map (body, scene, slot, 0)
+    uint32_t vmap_max = 0;             // maps of the scene with the most
     void *bx = nullptr;                // prepared set: [maps][np] boundary points
     void *bv = nullptr;                // prepared set: [np] boundary velocity sums of moving maps
     bool vmove = false;                // some map has a velocity
@@ -308,8 +312,11 @@ void free_vmaps(sphgb_ctx *c)
         for (void *p : {(void *)m.f0, (void *)m.f1, m.coef})
             if (p) cudaFree(p);
     c->vmaps.clear();
-    if (c->d_vmaps) cudaFree(c->d_vmaps);
-    c->d_vmaps = nullptr;
+    for (void **p : {&c->d_vmaps, &c->d_vmap_range, &c->d_vmap_info}) {
+        if (*p) cudaFree(*p);
+        *p = nullptr;
+    }
+    c->vmap_max = 0;
 }
 
 // the slot tables of the bodies (part of the prepared set)
@@ -438,6 +445,9 @@ template <class T> DevParams<T> make_params(const sphgb_ctx *c)
     P.staged = (c->staged && !c->fp64 && c->lpp_log2 == 0 && c->ll) ? 1 : 0;
     P.nvmaps = (c->boundary_method == 2 && c->bx) ? (uint32_t)c->vmaps.size() : 0u;
     P.vmaps = static_cast<const VMapDev<T> *>(c->d_vmaps);
+    P.vmap_range = static_cast<const uint2 *>(c->d_vmap_range);
+    P.vmap_info = static_cast<const uint4 *>(c->d_vmap_info);
+    P.vmap_max = P.nvmaps ? c->vmap_max : 0u;
     P.vmove = (P.nvmaps && c->vmove && c->bv) ? 1 : 0;
     P.bmove = (c->bmotion && c->bm_ready && c->nb && c->boundary_method == 0 && c->nscenes() == 1 && c->bv) ? 1 : 0;
     P.nphase = 1;
@@ -623,6 +633,8 @@ int build_body_tables(sphgb_ctx *c)
     return SPHGB_OK;
 }
 
+template <class T> int upload_vmaps(sphgb_ctx *c);
+
 // Build each scene's cell grid over the union of its fluid and boundary extents,
 // sort the boundary particles into it and compute their Akinci2012 volumes.
 template <class T> int prepare(sphgb_ctx *c)
@@ -742,11 +754,13 @@ template <class T> int prepare(sphgb_ctx *c)
         if ((rc = palloc(c, &c->bv, (size_t)std::max(c->np, 1u) * vec_size(c)))) return rc;
     }
     if (c->boundary_method == 2 && !c->vmaps.empty()) {
-        if ((rc = palloc(c, &c->bx, (size_t)std::max(c->np, 1u) * c->vmaps.size() * vec_size(c)))) return rc;
+        // the maps for the current scenes; each particle keeps one boundary point per map of its scene
+        if ((rc = c->fp64 ? upload_vmaps<double>(c) : upload_vmaps<float>(c))) return rc;
+        if ((rc = palloc(c, &c->bx, (size_t)std::max(c->np, 1u) * c->vmap_max * vec_size(c)))) return rc;
         if ((rc = palloc(c, &c->bv, (size_t)std::max(c->np, 1u) * vec_size(c)))) return rc;
         if (c->nbodies) {   // block partials of the volume-map body forces
             const size_t nblk = (std::max(c->np, 1u) + kBlock - 1) / kBlock;
-            if ((rc = palloc(c, &c->bodies.vpartials, (size_t)c->nbodies * 6 * nblk * sizeof(double)))) return rc;
+            if ((rc = palloc(c, &c->bodies.vpartials, (size_t)c->vmap_max * 6 * nblk * sizeof(double)))) return rc;
         }
     }
     c->prepared = true;
@@ -1104,13 +1118,14 @@ template <class T> int autotune(sphgb_ctx *c)
     return SPHGB_OK;
 }
 
-// The Bender2019 configurations this path supports: one scene, bodies given only as volume
-// maps built for the current support radius, forces collected with one body per map.
+// The Bender2019 configurations this path supports: bodies given only as volume maps built for
+// the current support radius, each in one scene of the batch, forces collected with one body per map.
 int check_boundary_method(sphgb_ctx *c)
 {
     if (c->boundary_method != 2) return SPHGB_OK;
     if (c->vmaps.empty()) return fail(c, SPHGB_ERR_STATE, "Bender2019 boundary without volume maps");
-    if (c->scn.size() > 1) return fail(c, SPHGB_ERR_STATE, "volume maps serve a single scene, not a batch");
+    for (const auto &m : c->vmaps)
+        if (m.scene >= c->nscenes()) return fail(c, SPHGB_ERR_ARGUMENT, "a volume map belongs to a scene that is not uploaded");
     if (c->nb) return fail(c, SPHGB_ERR_STATE, "the Bender2019 boundary takes no boundary particles");
     if (c->nbodies && c->nbodies != c->vmaps.size())
         return fail(c, SPHGB_ERR_ARGUMENT, "with volume maps the bodies are the maps: one body per map");
@@ -1120,13 +1135,23 @@ int check_boundary_method(sphgb_ctx *c)
     return SPHGB_OK;
 }
 
-// the maps as the step reads them (VMapDev<T>)
+// the bodies (maps in the order they were added) in scene order, stable within a scene
+std::vector<uint32_t> vmap_order(const sphgb_ctx *c)
+{
+    std::vector<uint32_t> o(c->vmaps.size());
+    for (uint32_t b = 0; b < o.size(); b++) o[b] = b;
+    std::stable_sort(o.begin(), o.end(), [&](uint32_t a, uint32_t b) { return c->vmaps[a].scene < c->vmaps[b].scene; });
+    return o;
+}
+
+// the maps as the step reads them (VMapDev<T>), in scene order
 template <class T> std::vector<VMapDev<T>> vmap_dev_array(const sphgb_ctx *c)
 {
+    const std::vector<uint32_t> order = vmap_order(c);
     std::vector<VMapDev<T>> h(c->vmaps.size());
-    for (size_t b = 0; b < c->vmaps.size(); b++) {
-        const auto &m = c->vmaps[b];
-        VMapDev<T> &d = h[b];
+    for (size_t q = 0; q < c->vmaps.size(); q++) {
+        const auto &m = c->vmaps[order[q]];
+        VMapDev<T> &d = h[q];
         for (int k = 0; k < 3; k++) {
             d.dmin[k] = (T)m.dmin[k];
             d.dmax[k] = (T)m.dmax[k];
@@ -1144,16 +1169,37 @@ template <class T> std::vector<VMapDev<T>> vmap_dev_array(const sphgb_ctx *c)
     return h;
 }
 
-// uploaded after a map is added or removed
+// uploaded after a map is added or removed or changes scene, and when the context is prepared:
+// the maps in scene order and, for a batch, each scene's range and each map's body, scene and slot
 template <class T> int upload_vmaps(sphgb_ctx *c)
 {
-    if (c->d_vmaps) cudaFree(c->d_vmaps);
-    c->d_vmaps = nullptr;
+    for (void **p : {&c->d_vmaps, &c->d_vmap_range, &c->d_vmap_info}) {
+        if (*p) cudaFree(*p);
+        *p = nullptr;
+    }
     c->vmaps_dirty = false;
+    c->vmap_max = 0;
     if (c->vmaps.empty()) return SPHGB_OK;
     const std::vector<VMapDev<T>> h = vmap_dev_array<T>(c);
     CK(cudaMalloc(&c->d_vmaps, h.size() * sizeof(VMapDev<T>)));
     CK(cudaMemcpy(c->d_vmaps, h.data(), h.size() * sizeof(VMapDev<T>), cudaMemcpyHostToDevice));
+    const uint32_t S = c->nscenes();
+    std::vector<uint2> range(S, make_uint2(0u, 0u));
+    std::vector<uint4> info(c->vmaps.size());
+    const std::vector<uint32_t> order = vmap_order(c);
+    for (uint32_t q = 0; q < order.size(); q++) {
+        const uint32_t s = std::min(c->vmaps[order[q]].scene, S - 1);
+        if (range[s].y == 0) range[s].x = q;
+        info[q] = make_uint4(order[q], s, range[s].y, 0u);
+        range[s].y++;
+    }
+    for (const uint2 &r : range) c->vmap_max = std::max(c->vmap_max, r.y);
+    if (S > 1) {
+        CK(cudaMalloc(&c->d_vmap_range, range.size() * sizeof(uint2)));
+        CK(cudaMemcpy(c->d_vmap_range, range.data(), range.size() * sizeof(uint2), cudaMemcpyHostToDevice));
+        CK(cudaMalloc(&c->d_vmap_info, info.size() * sizeof(uint4)));
+        CK(cudaMemcpy(c->d_vmap_info, info.data(), info.size() * sizeof(uint4), cudaMemcpyHostToDevice));
+    }
     return SPHGB_OK;
 }
 
@@ -2255,6 +2301,20 @@ int sphgb_set_body_motion(sphgb_ctx *c, uint32_t body, const double rotation[9],
                            c->body_center.data() + 3 * (size_t)body, 3 * sizeof(double), cudaMemcpyHostToDevice,
                            c->stream));
     }
+    return SPHGB_OK;
+}
+
+int sphgb_set_volume_map_scene(sphgb_ctx *c, uint32_t body, uint32_t scene)
+{
+    if (!c) return SPHGB_ERR_ARGUMENT;
+    if (body >= c->vmaps.size()) return fail(c, SPHGB_ERR_ARGUMENT, "no such volume map");
+    if (c->step_pending) {
+        sphgb_stats st;
+        fill_stats(c, &st);
+    }
+    c->vmaps[body].scene = scene;
+    c->prepared = false;   // the scene-ordered maps and the boundary points per particle
+    invalidate_graphs(c);
     return SPHGB_OK;
 }
 

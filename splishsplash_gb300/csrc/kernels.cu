@@ -286,6 +286,12 @@ template <class T> __device__ __forceinline__ void cell_of(const SceneDev<T> &S,
     cz = min(max(cz, 0), S.dimz - 1);
 }
 
+// the maps of scene s: first map and count in the scene-ordered map array
+template <class T> __device__ __forceinline__ uint2 scene_maps(const DevParams<T> &P, uint32_t s)
+{
+    return P.vmap_range ? P.vmap_range[s] : make_uint2(0u, P.nvmaps);
+}
+
 template <class T> __device__ __forceinline__ uint32_t local_cell(const SceneDev<T> &S, int cx, int cy, int cz)
 {
     return ((uint32_t)cz * (uint32_t)S.dimy + (uint32_t)cy) * (uint32_t)S.dimx + (uint32_t)cx;
@@ -544,8 +550,9 @@ __global__ void __launch_bounds__(kBlock) k_vmap_boundary(DevParams<T> P, DevBuf
     if (!q.act) return;
     const uint32_t i = q.i;
     const T r = (T)P.radius, hs = P.K.h;
-    for (uint32_t b = 0; b < P.nvmaps; b++) {
-        const VMapDev<T> &m = P.vmaps[b];
+    const uint2 mr = scene_maps(P, q.s);
+    for (uint32_t b = 0; b < mr.y; b++) {   // b: the map's slot among the scene's maps
+        const VMapDev<T> &m = P.vmaps[mr.x + b];
         v4_t<T> x = ldv(B.x, i);
         const T dx[3] = {(T)x.x - m.t[0], (T)x.y - m.t[1], (T)x.z - m.t[2]};
         T local[3];
@@ -611,7 +618,7 @@ template <class T> __device__ __forceinline__ V3<T> vmap_point_velocity(const VM
 // list: the same entries as the fluid list, as indices into the block's staged array.
 template <class T>
 __device__ __forceinline__ void build_one(const DevParams<T> &P, const DevBufs<T> &B, const SceneDev<T> &S,
-                                          StepScalars *sc, uint32_t i, uint32_t &nf_out, uint32_t &nb_out,
+                                          uint32_t scene, StepScalars *sc, uint32_t i, uint32_t &nf_out, uint32_t &nb_out,
                                           const uint32_t *tcell, const uint16_t *toff, uint32_t tn)
 {
     const v4_t<T> xi = ldv(B.x, i);
@@ -741,12 +748,13 @@ __device__ __forceinline__ void build_one(const DevParams<T> &P, const DevBufs<T
     nbr_loop<kUnroll>(Lb, min(nb, P.capb), [&](uint32_t j) { return ldv(B.xb, j); }, boundary_term);
     // Bender2019: the volume-map sample of each body, x_j with V_j in w, where V_j > 0; a moving
     // body's point velocity v_j enters the same sums
-    for (uint32_t b = 0; b < P.nvmaps; b++) {
+    const uint2 mr = scene_maps(P, scene);
+    for (uint32_t b = 0; b < mr.y; b++) {
         const v4_t<T> xj = ldv(B.bx, b * P.np + i);
         if ((T)xj.w > T(0)) {
             boundary_term(b, xj);
             if (P.vmove) {
-                const V3<T> vj = vmap_point_velocity<T>(P.vmaps[b], xyz<T>(xj));
+                const V3<T> vj = vmap_point_velocity<T>(P.vmaps[mr.x + b], xyz<T>(xj));
                 const V3<T> r = diff3<T>(xi, xj);
                 T W, c;
                 kernel_W_coef_d2(P.K, dot(r, r), W, c);
@@ -831,7 +839,7 @@ __global__ void __launch_bounds__(kBlock) k_build(DevParams<T> P, DevBufs<T> B)
         __syncthreads();
     }
     uint32_t nf = 0, nb = 0;
-    if (q.act) build_one(P, B, scene_get(P, q.s), sc, q.i, nf, nb, tcell, toff, tn);
+    if (q.act) build_one(P, B, scene_get(P, q.s), q.s, sc, q.i, nf, nb, tcell, toff, tn);
     block_max_atomic(nf, nb, &sc->max_nf, &sc->max_nb);
 }
 
@@ -1315,8 +1323,9 @@ __device__ __forceinline__ V3<T> weiler_boundary(const DevParams<T> &P, const De
     });
     // volume maps: four samples per body, a quarter of V_j each and no rho0 / rho_i factor (as in
     // the reference's Bender2019 branches); lane 0 only, the lanes' shares are summed
+    const uint2 mr = scene_maps(P, q.s);
     if (q.l == 0)
-        for (uint32_t b = 0; b < P.nvmaps; b++) {
+        for (uint32_t b = 0; b < mr.y; b++) {
             const v4_t<T> xj = ldv(B.bx, b * P.np + q.i);
             if (!((T)xj.w > T(0))) continue;
             const T vol = T(0.25) * (T)xj.w;
@@ -1384,8 +1393,9 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T
                 // computeRHS (:1130-1138): the boundary particle's velocity
                 if (P.bmove) bb = add(bb, scl(r, f * dot(xyz<T>(ldv(B.vbs, j)), r)));
             });
+            const uint2 mr = scene_maps(P, q.s);
             if (q.l == 0)   // volume maps: the four samples of each body (diagonalMatrixElement :697-740)
-                for (uint32_t b = 0; b < P.nvmaps; b++) {
+                for (uint32_t b = 0; b < mr.y; b++) {
                     const v4_t<T> xj = ldv(B.bx, b * P.np + i);
                     if (!((T)xj.w > T(0))) continue;
                     const T vol = T(0.25) * (T)xj.w;
@@ -1396,7 +1406,7 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T
                         m[0] += f * r.x * r.x; m[1] += f * r.x * r.y; m[2] += f * r.x * r.z;
                         m[3] += f * r.y * r.y; m[4] += f * r.y * r.z; m[5] += f * r.z * r.z;
                         // computeRHS (:1191-1243): the samples' velocities
-                        if (P.vmove) bb = add(bb, scl(r, f * dot(vmap_point_velocity<T>(P.vmaps[b], xk), r)));
+                        if (P.vmove) bb = add(bb, scl(r, f * dot(vmap_point_velocity<T>(P.vmaps[mr.x + b], xk), r)));
                     });
                 }
             acc = add(acc, weiler_boundary<LPP>(P, B, q, xi, rhoi, gi));
@@ -1650,13 +1660,15 @@ __global__ void __launch_bounds__(kBlock) k_kick(DevParams<T> P, DevBufs<T> B)
         if (P.cfl_method != 0) {
             // moving volume-map bodies: |w x (maxDist, 0, 0) + v| against the squared fluid speeds,
             // as the reference compares them (Simulation.cpp:466-476, SimulatorBase.cpp:1670-1687)
-            if (P.vmove)
-                for (uint32_t b = 0; b < P.nvmaps; b++) {
+            if (P.vmove) {
+                const uint2 mr = scene_maps(P, q.s);
+                for (uint32_t b = mr.x; b < mr.x + mr.y; b++) {
                     const VMapDev<T> &m = P.vmaps[b];
                     const double vx = (double)m.v[0], vy = (double)m.v[1] + (double)m.w[2] * (double)m.max_dist,
                                  vz = (double)m.v[2] - (double)m.w[1] * (double)m.max_dist;
                     maxVel = fmax(maxVel, sqrt(vx * vx + vy * vy + vz * vz));
                 }
+            }
             if (maxVel < 1.0e-9) maxVel = 1.0e-9;
             hn = P.cfl_factor * 0.4 * (2.0 * P.radius / sqrt(maxVel));
             hn = fmin(hn, P.cfl_max);
@@ -1882,11 +1894,14 @@ __global__ void __launch_bounds__(kBlock) k_vmap_forces(DevParams<T> P, DevBufs<
     const SlotInfo q = slot_info(P);
     const bool press = PHASE == 1 || P.div_on;
     const bool xs = PHASE == 0 && P.xsph_b != T(0);
-    for (uint32_t b = 0; b < D.nbodies; b++) {   // block uniform
+    // partials per slot among the block's scene's maps (one scene: the slot is the body)
+    const uint2 mr = scene_maps(P, q.s);
+    for (uint32_t b = 0; b < P.vmap_max; b++) {   // block uniform
         DSum<6> mine;
 #pragma unroll
         for (int k = 0; k < 6; k++) mine.v[k] = 0.0;
-        if (q.act && D.dynamic[b]) {
+        const uint32_t body = b < mr.y ? (P.vmap_info ? P.vmap_info[mr.x + b].x : b) : 0u;
+        if (q.act && b < mr.y && D.dynamic[body]) {
             const uint32_t i = q.i;
             const v4_t<T> xj = ldv(B.bx, b * P.np + i);
             const T Vj = (T)xj.w;
@@ -1898,7 +1913,7 @@ __global__ void __launch_bounds__(kBlock) k_vmap_forces(DevParams<T> P, DevBufs<
                 V3<T> f = mk3<T>(0, 0, 0);
                 const T mi = P.nphase > 1 ? P.V * B.r0[i] : P.mass;   // fluid phases
                 if (press && fabs(kap) > P.eps) f = scl(r, mi * kap * Vj * grad_coef_d2(P.K, d2));
-                const VMapDev<T> &mp = P.vmaps[b];
+                const VMapDev<T> &mp = P.vmaps[mr.x + b];
                 if (xs) {
                     const T w = mi * P.xsph_b / (T)B.sc[q.s].dt * rho0_at(P, B, i) * Vj / B.density[i] *
                                 kernel_W(P.K, dev_sqrt(d2));
@@ -1906,7 +1921,7 @@ __global__ void __launch_bounds__(kBlock) k_vmap_forces(DevParams<T> P, DevBufs<
                     if (P.vmove) dv = sub(dv, vmap_point_velocity<T>(mp, xyz<T>(xj)));
                     f = add(f, scl(dv, w));
                 }
-                const double *c = D.center + 3 * (size_t)b;
+                const double *c = D.center + 3 * (size_t)body;
                 const double px = (double)xj.x - c[0], py = (double)xj.y - c[1], pz = (double)xj.z - c[2];
                 const double fx = (double)f.x, fy = (double)f.y, fz = (double)f.z;
                 mine.v[0] = fx;
@@ -1951,17 +1966,26 @@ __global__ void __launch_bounds__(kBlock) k_vmap_forces(DevParams<T> P, DevBufs<
     __syncthreads();
     if (!amLast) return;
     __threadfence();
-    for (uint32_t b = 0; b < D.nbodies; b++) {
+    for (uint32_t m = 0; m < P.nvmaps; m++) {   // every map: its body, scene and slot
+        uint32_t body = m, slot = m, g0 = 0u, g1 = gridDim.x;
+        if (P.vmap_info) {   // a batch: the blocks of the map's scene
+            const uint4 inf = P.vmap_info[m];
+            const SceneDev<T> S = scene_get(P, inf.y);
+            body = inf.x;
+            slot = inf.z;
+            g0 = S.pstart / kBlock;
+            g1 = (S.pstart + S.n + kBlock - 1) / kBlock;
+        }
         DSum<6> part;
 #pragma unroll
         for (int k = 0; k < 6; k++) part.v[k] = 0.0;
-        for (uint32_t g = threadIdx.x; g < gridDim.x; g += blockDim.x)
+        for (uint32_t g = g0 + threadIdx.x; g < g1; g += blockDim.x)
 #pragma unroll
-            for (int k = 0; k < 6; k++) part.v[k] += __ldcg(&D.vpartials[((size_t)b * 6 + k) * gridDim.x + g]);
+            for (int k = 0; k < 6; k++) part.v[k] += __ldcg(&D.vpartials[((size_t)slot * 6 + k) * gridDim.x + g]);
         const DSum<6> tot = block_sum<6>(part);
         if (threadIdx.x == 0)
 #pragma unroll
-            for (int k = 0; k < 6; k++) D.acc[6 * (size_t)b + k] += tot.v[k];
+            for (int k = 0; k < 6; k++) D.acc[6 * (size_t)body + k] += tot.v[k];
     }
     if (threadIdx.x == 0) *D.counters = 0u;
 }

@@ -90,7 +90,10 @@ template <class T> struct DevParams {
     uint32_t lpp_log2;            // lanes per particle of the neighbour passes (1, 2 or 4) = 1 << lpp_log2;
                                   // also fixes the layout of the fluid lists
     uint32_t nvmaps;              // Bender2019 boundary: volume maps (bodies); 0 = Akinci2012 particles
-    const VMapDev<T> *vmaps;      // device array [nvmaps]
+    const VMapDev<T> *vmaps;      // device array [nvmaps], ordered by scene
+    const uint2 *vmap_range;      // batches: per scene, first map and map count (null: one scene, all maps)
+    const uint4 *vmap_info;       // batches: per map, (body, scene, slot within the scene's maps, 0)
+    uint32_t vmap_max;            // maps of the scene with the most (per-particle boundary points)
     int vmove;                    // some volume-map body moves: boundary terms use v_i - v_b
     // fluid phases (several fluid models of one scene): particle ids [phase_end[k-1], phase_end[k])
     // form phase k of rest density phase_rho0[k] and phase_count[k] particles; nphase <= 1: one model

@@ -127,6 +127,7 @@ EXPORTS = [
     "sphgb_set_neighbor_staging", "sphgb_get_neighbor_staging",
     "sphgb_add_volume_map", "sphgb_add_volume_map_values", "sphgb_get_volume_map", "sphgb_clear_volume_maps",
     "sphgb_set_boundary_method", "sphgb_set_volume_map_motion", "sphgb_set_body_motion", "sphgb_set_fluid_phases",
+    "sphgb_set_volume_map_scene",
 ]
 
 _lib = None
@@ -195,6 +196,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.sphgb_set_volume_map_motion.argtypes = [vp, u32, vp, vp, vp, vp]
     L.sphgb_set_body_motion.argtypes = [vp, u32, vp, vp, vp, vp]
     L.sphgb_set_fluid_phases.argtypes = [vp, u32, vp, vp]
+    L.sphgb_set_volume_map_scene.argtypes = [vp, u32, u32]
     L.sphgb_get_neighbor_staging.argtypes = [vp, ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_float),
                                              ctypes.POINTER(ctypes.c_float)]
     L.sphgb_profile_enable.argtypes = [vp, i32]
@@ -558,6 +560,10 @@ class Context:
     def set_boundary_method(self, method: int):
         """0 Akinci2012 boundary particles, 2 Bender2019 volume maps."""
         self._check(self.L.sphgb_set_boundary_method(self.h, int(method)))
+
+    def set_volume_map_scene(self, body: int, scene: int):
+        """the scene of a batch that volume map `body` belongs to (default 0)"""
+        self._check(self.L.sphgb_set_volume_map_scene(self.h, int(body), int(scene)))
 
     def set_volume_map_motion(self, body: int, rotation=None, translation=None, velocity=None, omega=None):
         """Pose (row-major rotation, translation) and velocity / angular velocity of the body of

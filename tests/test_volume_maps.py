@@ -278,6 +278,10 @@ def test_unsupported_combinations_are_refused():
     p.particleRadius = 0.02
     ts.ctx.set_params(p)
     assert code(ts.step) == "STATE"                           # map built for another radius
+    p.particleRadius = sc.params.particleRadius
+    ts.ctx.set_params(p)
+    ts.ctx.set_volume_map_scene(0, 3)
+    assert code(ts.step) == "ARGUMENT"                        # a scene that is not uploaded
     ts.close()
 
 
@@ -499,3 +503,57 @@ def test_map_motion_refusals():
         ts.ctx.set_volume_map_motion(0, None, (np.nan, 0, 0))
     assert native.ERR_NAMES[e.value.code] == "NONFINITE"
     ts.close()
+
+
+# ------------------------------------------------------------------- batches
+@pytest.mark.gpu
+@pytest.mark.parametrize("moving", [False, True])
+def test_batch_with_volume_maps_matches_separate_contexts(moving):
+    """two scenes, each in its own volume-mapped box (the second one moving), forces on both boxes:
+    the batch equals the scenes run in separate contexts bit for bit"""
+    a = scenes.small_block(counts=(9, 6, 9), box=(0.6, 0.8, 0.6), corner=(0.07, 0.07, 0.07)).as_float32()
+    b = scenes.small_block(counts=(8, 9, 7), box=BOX, seed=11, velocity=(0.2, 0.0, -0.1)).as_float32()
+    b.params = a.params
+    boxes = [(0.6, 0.8, 0.6), BOX]
+    res = [(12, 16, 12), RES]
+    for sc in (a, b):
+        sc.xb = np.zeros((0, 3))
+    motion = (None, np.array([0.05, 0.0, 0.0]), np.array([0.0, 0.2, 0.0])) if moving else None
+    centers = np.array([[0.3, 0.0, 0.3], [0.4, 0.0, 0.4]])
+
+    def setup(ctx, maps):
+        ctx.set_lanes_per_particle(1)   # the summation order depends on the lanes per particle
+        ctx.set_neighbor_staging(1)
+        for k, scene in maps:
+            v, f = scenes.box_mesh((0, 0, 0), boxes[k])
+            ctx.add_volume_map(v, f, res[k], invert=True)
+        for body, (k, scene) in enumerate(maps):
+            ctx.set_volume_map_scene(body, scene)
+        ctx.set_boundary_method(2)
+
+    batch = BatchedTimeStepDFSPH([a, b])
+    setup(batch.ctx, [(0, 0), (1, 1)])
+    batch.ctx.set_boundary_bodies(None, centers)
+    for _ in range(20):
+        if moving:
+            batch.ctx.set_volume_map_motion(1, *motion)
+        batch.step()
+    xs, vs = batch.getFieldBuffer("position"), batch.getFieldBuffer("velocity")
+    fb, tb = batch.ctx.boundary_forces()
+    batch.close()
+    for k, sc in enumerate((a, b)):
+        ts = TimeStepDFSPH(sc)
+        setup(ts.ctx, [(k, 0)])
+        ts.ctx.set_boundary_bodies(None, centers[k:k + 1])
+        for _ in range(20):
+            if moving and k == 1:
+                ts.ctx.set_volume_map_motion(0, *motion)
+            ts.step()
+        m = ts.getFluidModel()
+        np.testing.assert_array_equal(xs[k], m.getFieldBuffer("position"))
+        np.testing.assert_array_equal(vs[k], m.getFieldBuffer("velocity"))
+        f, t = ts.ctx.boundary_forces()
+        assert np.abs(f).max() > 1.0
+        np.testing.assert_array_equal(fb[k], f[0])
+        np.testing.assert_array_equal(tb[k], t[0])
+        ts.close()
