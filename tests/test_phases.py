@@ -124,3 +124,34 @@ def test_phase_refusals():
     ts.ctx.set_fluid_phases()                                         # back to one phase
     ts.step()
     ts.close()
+
+
+@pytest.mark.gpu
+def test_two_phase_step_in_a_volume_mapped_box_matches_oracle():
+    """the phases with the Bender2019 boundary (FP64): iteration counts equal, fields at the bars"""
+    sc, counts, state = two_phase_state()
+    sc.xb = np.zeros((0, 3))
+    ts = TimeStepDFSPH(sc, precision="fp64")
+    v, f = scenes.box_mesh((0, 0, 0), (0.6, 0.8, 0.6))
+    ts.ctx.add_volume_map(v, f, (12, 16, 12), invert=True)
+    ts.ctx.set_boundary_method(2)
+    ts.ctx.set_fluid_phases(counts, RHO)
+    m = ts.getFluidModel()
+    m.setFieldBuffer("position", state["x"])
+    m.setFieldBuffer("velocity", state["v"])
+    m.setFieldBuffer("p / rho^2", state["kappa"])
+    m.setFieldBuffer("p_v / rho^2", state["kappa_v"])
+    ts.setTimeStepSize(state["dt"])
+    res, lo, hi, dist, vol = ts.ctx.volume_map(0)
+    sim = oracle.OracleSim(sc)
+    sim.set_volume_maps([oracle.VolumeMap(res).set_values(lo, hi, dist, vol)])
+    sim.set_phases(counts, RHO)
+    sim.x[:] = state["x"]
+    sim.v[:] = state["v"]
+    sim.kappa[:] = state["kappa"]
+    sim.kappa_v[:] = state["kappa_v"]
+    sim.dt = state["dt"]
+    st = ts.step()
+    sim.step()
+    compare(ts, sim, st, tol_scale=1e-4)
+    ts.close()
