@@ -352,8 +352,8 @@ int sphgb_set_boundary_bodies(sphgb_ctx *ctx, const uint32_t *body, uint32_t nbo
  * 1130-1138, 966-975), their squared speeds the CFL maximum (Simulation.cpp:442-458), and the
  * body's torque is taken about t.  The volumes stay those computed for the uploaded shape.
  * Bodies without a call stay in their uploaded pose at rest.  rotation (row-major) / translation
- * NULL keep the current ones; velocity / omega NULL are zero.  One scene (SPHGB_ERR_STATE for a
- * batch); volume-map bodies move with sphgb_set_volume_map_motion. */
+ * NULL keep the current ones; velocity / omega NULL are zero.  In a batch a body's particles stay
+ * in their scene; volume-map bodies move with sphgb_set_volume_map_motion. */
 /* Several fluid phases in one scene, as the reference's multiphase scenes hold several FluidModels
  * of different rest density: the uploaded particles in particle-id order form nphases consecutive
  * groups of counts[k] particles with rest density density0[k] (mass V density0[k]; the particle

@@ -139,7 +139,7 @@ struct sphgb_ctx {
     uint32_t bm_nb = 0;                // boundary count the buffers below were made for (body allocations)
     void *d_bmot = nullptr, *bm_x0 = nullptr, *bm_V0 = nullptr, *bm_xtmp = nullptr, *bm_vtmp = nullptr;
     void *vbs = nullptr;               // velocities of the sorted boundary particles
-    uint32_t *bm_body = nullptr, *bm_k1 = nullptr, *bm_k2 = nullptr, *bm_v1 = nullptr, *bm_v2 = nullptr;
+    uint32_t *bm_body = nullptr, *bm_scene = nullptr, *bm_k1 = nullptr, *bm_k2 = nullptr, *bm_v1 = nullptr, *bm_v2 = nullptr;
     uint32_t *bm_cells = nullptr, *bm_hist = nullptr;
     uint32_t *binv = nullptr;          // prepared set: sorted slot of boundary particle u
     uint32_t *bgroup = nullptr;        // prepared set: volume group of boundary particle u (null: one group)
@@ -347,7 +347,7 @@ void free_bodies(sphgb_ctx *c)
     c->body_moves.clear();
     c->bm_nb = 0;
     c->d_bmot = c->bm_x0 = c->bm_V0 = c->bm_xtmp = c->bm_vtmp = c->vbs = nullptr;
-    c->bm_body = c->bm_k1 = c->bm_k2 = c->bm_v1 = c->bm_v2 = c->bm_cells = c->bm_hist = nullptr;
+    c->bm_body = c->bm_scene = c->bm_k1 = c->bm_k2 = c->bm_v1 = c->bm_v2 = c->bm_cells = c->bm_hist = nullptr;
     invalidate_graphs(c);
 }
 
@@ -449,7 +449,7 @@ template <class T> DevParams<T> make_params(const sphgb_ctx *c)
     P.vmap_info = static_cast<const uint4 *>(c->d_vmap_info);
     P.vmap_max = P.nvmaps ? c->vmap_max : 0u;
     P.vmove = (P.nvmaps && c->vmove && c->bv) ? 1 : 0;
-    P.bmove = (c->bmotion && c->bm_ready && c->nb && c->boundary_method == 0 && c->nscenes() == 1 && c->bv) ? 1 : 0;
+    P.bmove = (c->bmotion && c->bm_ready && c->nb && c->boundary_method == 0 && c->bv) ? 1 : 0;
     P.nphase = 1;
     if (c->phase_counts.size() > 1 && c->r0) {
         P.nphase = (uint32_t)c->phase_counts.size();
@@ -824,6 +824,7 @@ template <class T> BoundaryMoveDev<T> boundary_move_dev(const sphgb_ctx *c)
     M.x0 = static_cast<const v4_t<T> *>(c->bm_x0);
     M.V0 = static_cast<const T *>(c->bm_V0);
     M.body = c->bm_body;
+    M.scene = c->nscenes() > 1 ? c->bm_scene : nullptr;
     M.motion = static_cast<const BodyMotionDev<T> *>(c->d_bmot);
     M.xtmp = static_cast<v4_t<T> *>(c->bm_xtmp);
     M.vtmp = static_cast<v4_t<T> *>(c->bm_vtmp);
@@ -1229,7 +1230,8 @@ template <class T> int prepare_body_motion(sphgb_ctx *c)
             (rc = al(&c->bm_V0, nb * sizeof(T))) || (rc = al(&c->bm_xtmp, nb * vs)) || (rc = al(&c->bm_vtmp, nb * vs)) ||
             (rc = al(&c->vbs, nb * vs)) || (rc = al(&c->bm_body, nb * 4)) || (rc = al(&c->bm_k1, nb * 4)) ||
             (rc = al(&c->bm_k2, nb * 4)) || (rc = al(&c->bm_v1, nb * 4)) || (rc = al(&c->bm_v2, nb * 4)) ||
-            (rc = al(&c->bm_cells, nb * 4)) || (rc = al(&c->bm_hist, tiles * 256 * 4)))
+            (rc = al(&c->bm_cells, nb * 4)) || (rc = al(&c->bm_hist, tiles * 256 * 4)) ||
+            (rc = al(&c->bm_scene, nb * 4)))
             return rc;
         c->bm_nb = nb;
     }
@@ -1250,6 +1252,10 @@ template <class T> int prepare_body_motion(sphgb_ctx *c)
     CK(cudaMemcpy(c->bm_x0, x0.data(), nb * sizeof(v4_t<T>), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(c->bm_V0, V0.data(), nb * sizeof(T), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(c->bm_body, c->body_of.data(), nb * 4, cudaMemcpyHostToDevice));
+    std::vector<uint32_t> bs(nb, 0u);   // each boundary particle's scene (upload order)
+    for (uint32_t s = 0; s < c->scn.size(); s++)
+        for (uint32_t k = 0; k < c->scn[s].nb; k++) bs[c->scn[s].bstart + k] = s;
+    CK(cudaMemcpy(c->bm_scene, bs.data(), nb * 4, cudaMemcpyHostToDevice));
     CK(cudaMemset(c->vbs, 0, nb * sizeof(v4_t<T>)));
     c->bm_ready = true;
     c->bmot_dirty = true;
@@ -2266,7 +2272,6 @@ int sphgb_set_body_motion(sphgb_ctx *c, uint32_t body, const double rotation[9],
         return fail(c, SPHGB_ERR_ARGUMENT, "volume-map bodies move with sphgb_set_volume_map_motion");
     if (body >= c->nbodies || c->nb == 0)
         return fail(c, SPHGB_ERR_ARGUMENT, "no such body of boundary particles (sphgb_set_boundary_bodies)");
-    if (c->nscenes() > 1) return fail(c, SPHGB_ERR_STATE, "moving boundary bodies serve a single scene, not a batch");
     int rc;
     if ((rotation && (rc = check_finite(c, rotation, 9, "body rotation"))) ||
         (translation && (rc = check_finite(c, translation, 3, "body translation"))) ||

@@ -2247,7 +2247,7 @@ __global__ void __launch_bounds__(kBlock) k_boundary_gather(DevParams<T> P, DevB
 // Moving boundary bodies, every step before the neighbour search (SimulatorBase::updateBoundaryParticles,
 // SimulatorBase.cpp:1620-1645): particle u of body b at R_b x0_u + t_b, moving at
 // w_b x (R_b x0_u) + v_b; its sort key; the squared speeds enter the step's CFL maximum as the
-// reference adds those of moving bodies' particles (Simulation.cpp:442-458).  One scene.
+// reference adds those of moving bodies' particles (Simulation.cpp:442-458), per scene.
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_boundary_move(DevParams<T> P, DevBufs<T> B, BoundaryMoveDev<T> M,
                                                            uint32_t *keys, uint32_t *vals)
@@ -2255,6 +2255,7 @@ __global__ void __launch_bounds__(kBlock) k_boundary_move(DevParams<T> P, DevBuf
     count_launch(&B.gsc->launches);
     const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
     T sp = T(0);
+    const uint32_t scene = (M.scene && u < P.nb) ? M.scene[u] : 0u;
     if (u < P.nb) {
         const v4_t<T> x0 = ldv(M.x0, u);
         const BodyMotionDev<T> &m = M.motion[M.body[u]];
@@ -2267,27 +2268,28 @@ __global__ void __launch_bounds__(kBlock) k_boundary_move(DevParams<T> P, DevBuf
         const v4_t<T> xp = pack(x, M.V0[u]);
         stv(M.xtmp, u, xp);
         stv(M.vtmp, u, pack(v, T(0)));
-        const SceneDev<T> &S = P.s0;
+        const SceneDev<T> S = scene_get(P, scene);
         int cx, cy, cz;
         cell_of(S, xp, cx, cy, cz);
         keys[u] = S.key_prefix | morton3((uint32_t)cx, (uint32_t)cy, (uint32_t)cz);
         vals[u] = u;
         sp = dot(v, v);
     }
-    // block maximum, one atomic per block, in the encoding of the kick's fluid maximum
-    __shared__ T wmax[kBlock / 32];
+    // the scene's maximum, in the encoding of the kick's fluid maximum: one atomic per warp of one
+    // scene (the scenes' particles are contiguous), one per lane otherwise
+    auto publish = [&](T m, uint32_t s) {
+        if (!(m > T(0))) return;
+        StepScalars *sc = B.sc + s;
+        if constexpr (sizeof(T) == 8) atomicMax(&sc->maxvel_bits64, (unsigned long long)__double_as_longlong((double)m));
+        else atomicMax(&sc->maxvel_bits, __float_as_uint((float)m));
+    };
+    const uint32_t s0 = __shfl_sync(0xffffffffu, scene, 0);
+    if (__all_sync(0xffffffffu, scene == s0)) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) sp = fmax(sp, __shfl_xor_sync(0xffffffffu, sp, o));
-    if ((threadIdx.x & 31u) == 0) wmax[threadIdx.x >> 5] = sp;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        T bm = T(0);
-        for (int k = 0; k < kBlock / 32; k++) bm = fmax(bm, wmax[k]);
-        if (bm > T(0)) {
-            StepScalars *sc = B.sc;
-            if constexpr (sizeof(T) == 8) atomicMax(&sc->maxvel_bits64, (unsigned long long)__double_as_longlong((double)bm));
-            else atomicMax(&sc->maxvel_bits, __float_as_uint((float)bm));
-        }
+        for (int o = 16; o > 0; o >>= 1) sp = fmax(sp, __shfl_xor_sync(0xffffffffu, sp, o));
+        if ((threadIdx.x & 31u) == 0) publish(sp, s0);
+    } else {
+        publish(sp, scene);
     }
 }
 
@@ -2305,7 +2307,9 @@ __global__ void __launch_bounds__(kBlock) k_boundary_regather(DevParams<T> P, De
     stv(B.vbs, k, ldv(M.vtmp, src));
     B.bid[k] = src;
     B.binv[src] = k;
-    const SceneDev<T> &S = P.s0;
+    const uint32_t sn = M.scene ? M.scene[src] : 0u;
+    if (B.bscene) B.bscene[k] = sn;
+    const SceneDev<T> S = scene_get(P, sn);
     int cx, cy, cz;
     cell_of(S, x, cx, cy, cz);
     cells[k] = S.cell_off + local_cell(S, cx, cy, cz);

@@ -242,6 +242,7 @@ template <class T> struct BoundaryMoveDev {
     const v4_t<T> *x0;
     const T *V0;
     const uint32_t *body;
+    const uint32_t *scene;        // batches: each particle's scene (null: one scene)
     const BodyMotionDev<T> *motion;
     v4_t<T> *xtmp, *vtmp;
 };

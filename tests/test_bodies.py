@@ -359,8 +359,39 @@ def test_body_motion_refusals():
     assert code(lambda: ts.ctx.set_body_motion(1, None, (0, 0, 0))) == "ARGUMENT"          # no such body
     assert code(lambda: ts.ctx.set_body_motion(0, None, (np.inf, 0, 0))) == "NONFINITE"
     ts.close()
-    a, b = scenes.small_block(counts=(4, 4, 4)), scenes.small_block(counts=(5, 4, 4))
-    bt = BatchedTimeStepDFSPH([a, b])
-    bt.ctx.set_boundary_bodies(np.zeros(a.nb + b.nb, np.uint32), np.zeros((1, 3)))
-    assert code(lambda: bt.ctx.set_body_motion(0, None, (0, 0, 0))) == "STATE"            # a batch
-    bt.close()
+
+
+@pytest.mark.gpu
+def test_batch_with_moving_bodies_matches_separate_contexts():
+    """two scenes whose floors slide at different speeds (bodies 0 and 3, one per scene): the batch
+    equals the scenes run in separate contexts bit for bit, forces included"""
+    a = all_terms_scene()
+    b = scenes.small_block(counts=(8, 12, 8), box=(0.8, 1.0, 0.8), seed=11, viscosity=True).as_float32()
+    b.params = a.params
+    ba, bb = container_bodies(a.xb, 1.0), container_bodies(b.xb, 1.0) + 3
+    centers = np.concatenate([CENTERS, CENTERS + 0.1])
+    dyn = DYNAMIC + DYNAMIC
+    speeds = ((0.3, 0.0, 0.0), (0.0, 0.0, -0.2))
+    batch = BatchedTimeStepDFSPH([a, b])
+    batch.ctx.set_lanes_per_particle(1)
+    batch.ctx.set_boundary_bodies(np.concatenate([ba, bb]), centers, dyn)
+    for _ in range(10):
+        batch.ctx.set_body_motion(0, None, None, speeds[0])
+        batch.ctx.set_body_motion(3, None, None, speeds[1])
+        batch.step()
+    xs = batch.getFieldBuffer("position")
+    fb, tb = device_forces(batch.ctx)
+    batch.close()
+    for k, (sc, body) in enumerate(((a, ba), (b, bb - 3))):
+        ts = TimeStepDFSPH(sc)
+        ts.ctx.set_lanes_per_particle(1)
+        ts.ctx.set_boundary_bodies(body, centers[3 * k:3 * k + 3], DYNAMIC)
+        for _ in range(10):
+            ts.ctx.set_body_motion(0, None, None, speeds[k])
+            ts.step()
+        np.testing.assert_array_equal(xs[k], ts.getFluidModel().getFieldBuffer("position"))
+        f, t = device_forces(ts.ctx)
+        ts.close()
+        assert np.abs(f[0]).max() > 1.0
+        np.testing.assert_array_equal(fb[3 * k:3 * k + 3], f)
+        np.testing.assert_array_equal(tb[3 * k:3 * k + 3], t)
