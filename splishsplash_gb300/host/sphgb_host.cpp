@@ -152,6 +152,7 @@ void TimeStepDFSPH_GB300::createContext(int device, bool useGraph)
     const Real d = Real(2) * m_sim.particleRadius;
     m_model.m_V = Real(0.8) * d * d * d;
     m_model.m_density0 = m_sim.density0;
+    m_fluids.assign(1, &m_model);
     applyParameters();
     for (unsigned int k = 0; k < m_boundaries.size(); k++) {
         m_boundaries[k]->m_owner = this;
@@ -216,9 +217,18 @@ void TimeStepDFSPH_GB300::applyParameters()
     check(sphgb_set_params(m_ctx, &p), "sphgb_set_params");
 }
 
+void TimeStepDFSPH_GB300::addFluidModel(FluidModel &model)
+{
+    for (FluidModel *f : m_fluids)
+        if (f == &model) throw Error(SPHGB_ERR_ARGUMENT, "fluid model added twice");
+    model.m_V = m_model.m_V;   // the particle volume follows the radius, common to all models
+    m_fluids.push_back(&model);
+    resize();
+}
+
 void TimeStepDFSPH_GB300::resize()
 {
-    const unsigned int n = m_model.numParticles();
+    const unsigned int n = totalParticles();
     m_factor.resize(n, Real(0));
     m_densityAdv.resize(n, Real(0));
     m_pressureRho2.resize(n, Real(0));
@@ -254,7 +264,7 @@ void TimeStepDFSPH_GB300::setTimeStepSize(Real dt)
 // host indices, so downloads come back in host order.
 void TimeStepDFSPH_GB300::upload()
 {
-    const unsigned int n = m_model.numParticles();
+    const unsigned int n = totalParticles();
     if (m_factor.size() != n) resize();
     if (m_boundaryDirty && !m_volumeMaps.empty()) {
         // Bender2019: no boundary particles; one map per body, built for the current parameters
@@ -310,8 +320,21 @@ void TimeStepDFSPH_GB300::upload()
         m_bodiesSet = anyDynamic;
         m_boundaryDirty = false;
     }
-    const std::vector<double> x = to_double(m_model.m_x), v = to_double(m_model.m_v);
+    // the fluid models concatenated in model order; several models are phases of their own rest density
+    std::vector<double> x, v;
+    std::vector<uint32_t> counts;
+    std::vector<double> rho0;
+    for (FluidModel *f : m_fluids) {
+        const std::vector<double> xf = to_double(f->m_x), vf = to_double(f->m_v);
+        x.insert(x.end(), xf.begin(), xf.end());
+        v.insert(v.end(), vf.begin(), vf.end());
+        counts.push_back(f->numParticles());
+        rho0.push_back((double)f->m_density0);
+    }
     check(sphgb_upload_fluid(m_ctx, x.data(), v.data(), nullptr, n), "sphgb_upload_fluid");
+    check(sphgb_set_fluid_phases(m_ctx, m_fluids.size() > 1 ? (uint32_t)m_fluids.size() : 0u, counts.data(),
+                                 rho0.data()),
+          "sphgb_set_fluid_phases");
     if (n) {
         check(sphgb_upload_field(m_ctx, SPHGB_FIELD_PRESSURE_RHO2, m_pressureRho2.data(), kDtype), "upload p / rho^2");
         check(sphgb_upload_field(m_ctx, SPHGB_FIELD_PRESSURE_RHO2_V, m_pressureRho2V.data(), kDtype), "upload p_v / rho^2");
@@ -369,13 +392,25 @@ void TimeStepDFSPH_GB300::step()
 
 void TimeStepDFSPH_GB300::syncToHost()
 {
-    const unsigned int n = m_model.numParticles();
+    const unsigned int n = totalParticles();
     if (n == 0) return;
     auto dl = [&](int field, void *dst, const char *what) { check(sphgb_download(m_ctx, field, dst, kDtype), what); };
-    dl(SPHGB_FIELD_POSITION, &m_model.m_x[0][0], "download position");
-    dl(SPHGB_FIELD_VELOCITY, &m_model.m_v[0][0], "download velocity");
-    dl(SPHGB_FIELD_ACCELERATION, &m_model.m_a[0][0], "download acceleration");
-    dl(SPHGB_FIELD_DENSITY, m_model.m_density.data(), "download density");
+    // the models' own fields: all models downloaded together, handed back model by model
+    std::vector<Vector3r> x(n), v(n), a(n);
+    std::vector<Real> rho(n);
+    dl(SPHGB_FIELD_POSITION, &x[0][0], "download position");
+    dl(SPHGB_FIELD_VELOCITY, &v[0][0], "download velocity");
+    dl(SPHGB_FIELD_ACCELERATION, &a[0][0], "download acceleration");
+    dl(SPHGB_FIELD_DENSITY, rho.data(), "download density");
+    size_t off = 0;
+    for (FluidModel *f : m_fluids) {
+        const size_t m = f->numParticles();
+        std::copy(x.begin() + off, x.begin() + off + m, f->m_x.begin());
+        std::copy(v.begin() + off, v.begin() + off + m, f->m_v.begin());
+        std::copy(a.begin() + off, a.begin() + off + m, f->m_a.begin());
+        std::copy(rho.begin() + off, rho.begin() + off + m, f->m_density.begin());
+        off += m;
+    }
     dl(SPHGB_FIELD_FACTOR, m_factor.data(), "download factor");
     dl(SPHGB_FIELD_DENSITY_ADV, m_densityAdv.data(), "download advected density");
     dl(SPHGB_FIELD_PRESSURE_RHO2, m_pressureRho2.data(), "download p / rho^2");
@@ -388,7 +423,7 @@ void TimeStepDFSPH_GB300::syncToHost()
     if (nb == 0) return;
     std::vector<Real> vol(nb);
     dl(SPHGB_FIELD_BOUNDARY_VOLUME, vol.data(), "download boundary volume");
-    size_t off = 0;
+    off = 0;
     for (BoundaryModel_Akinci2012 *bm : m_boundaries) {
         std::copy(vol.begin() + off, vol.begin() + off + bm->numberOfParticles(), bm->m_V.begin());
         off += bm->numberOfParticles();

@@ -244,18 +244,30 @@ public:
     // the boundary models' particles or rigid bodies changed: upload them before the next step
     void updateBoundary() { m_boundaryDirty = m_dirty = true; }
     int getNumIterations() override { return (int)m_iterations; }
+    // a further fluid model (Simulation::numberOfFluidModels > 1), before the first step: the
+    // models are phases of their own rest density (FluidModel::m_density0); the particle volume
+    // is common.  getFluidModel(k) returns model k, the first being the constructor's.
+    void addFluidModel(FluidModel &model);
+    unsigned int numberOfFluidModels() const { return (unsigned int)m_fluids.size(); }
+    FluidModel *getFluidModel(unsigned int k) { return m_fluids[k]; }
 
     // ParameterObject-style access by id or by the reference's parameter name
     double getValue(int id) const;
     void setValue(int id, double value);
     static int getParameterId(const std::string &name);
 
-    // DFSPH fields by particle index (SimulationDataDFSPH.h:55-120, fields of TimeStepDFSPH.cpp:49-53)
+    // DFSPH fields by particle index (SimulationDataDFSPH.h:55-120, fields of TimeStepDFSPH.cpp:49-53);
+    // with several fluid models by (model, index), as SimulationDataDFSPH holds them
     Real &getFactor(unsigned int i) { return m_factor[i]; }
     Real &getDensityAdv(unsigned int i) { return m_densityAdv[i]; }
     Real &getPressureRho2(unsigned int i) { return m_pressureRho2[i]; }
     Real &getPressureRho2_V(unsigned int i) { return m_pressureRho2V[i]; }
     Vector3r &getPressureAccel(unsigned int i) { return m_pressureAccel[i]; }
+    Real &getFactor(unsigned int k, unsigned int i) { return m_factor[offset(k) + i]; }
+    Real &getDensityAdv(unsigned int k, unsigned int i) { return m_densityAdv[offset(k) + i]; }
+    Real &getPressureRho2(unsigned int k, unsigned int i) { return m_pressureRho2[offset(k) + i]; }
+    Real &getPressureRho2_V(unsigned int k, unsigned int i) { return m_pressureRho2V[offset(k) + i]; }
+    Vector3r &getPressureAccel(unsigned int k, unsigned int i) { return m_pressureAccel[offset(k) + i]; }
 
     // TimeManager
     Real getTimeStepSize() const { return m_dt; }
@@ -283,8 +295,16 @@ protected:
     }
     void pushBodyMotion();
     void clearBodyForceAndTorque(unsigned int body);
+    unsigned int offset(unsigned int k) const   // first index of model k in the concatenated fields
+    {
+        unsigned int o = 0;
+        for (unsigned int q = 0; q < k; q++) o += m_fluids[q]->numParticles();
+        return o;
+    }
+    unsigned int totalParticles() const { return offset((unsigned int)m_fluids.size()); }
 
     FluidModel &m_model;
+    std::vector<FluidModel *> m_fluids;   // every fluid model, the first being m_model
     std::vector<BoundaryModel_Akinci2012 *> m_boundaries;
     std::vector<BoundaryModel_Bender2019 *> m_volumeMaps;
     bool m_bodiesSet = false;

@@ -5,7 +5,9 @@
 //   sphgb_host_demo <scene.bin> <out.bin>
 //
 // scene.bin (little endian): uint32 n, nb, steps, lanes (0 = autotune), viscosity (0/1),
-// bodies (0/1), volume map (0/1); float64 particle radius; float64 x[n][3], v[n][3], xb[nb][3];
+// bodies (0/1), volume map (0/1), phase0 (0: one fluid model; else the first phase0 particles are
+// the first model and the rest a second one); float64 particle radius; with phase0 > 0 float64
+// rest density of the second model; float64 x[n][3], v[n][3], xb[nb][3];
 // with bodies: uint32 body[nb] (0: the dynamic body, 1: static walls), float64 position[3],
 // velocity[3] and angular velocity[3] of the dynamic body (its pose is held, so that the run stays
 // comparable; its particles are given in the scene's frame and handed over in body coordinates);
@@ -46,11 +48,12 @@ int main(int argc, char **argv)
     }
     FILE *f = fopen(argv[1], "rb");
     if (!f) return 2;
-    uint32_t hdr[7];
-    double radius;
-    if (!rd(f, hdr, 7) || !rd(f, &radius, 1)) return 2;
+    uint32_t hdr[8];
+    double radius, rho1 = 0;
+    if (!rd(f, hdr, 8) || !rd(f, &radius, 1)) return 2;
     const uint32_t n = hdr[0], nb = hdr[1], steps = hdr[2], lanes = hdr[3], visc = hdr[4], bodies = hdr[5],
-                   vmap = hdr[6];
+                   vmap = hdr[6], phase0 = hdr[7];
+    if (phase0 && (phase0 >= n || !rd(f, &rho1, 1))) return 2;
     std::vector<double> x(3 * (size_t)n), v(3 * (size_t)n), xb(3 * (size_t)nb);
     if (!rd(f, x.data(), x.size()) || !rd(f, v.data(), v.size()) || !rd(f, xb.data(), xb.size())) return 2;
     std::vector<uint32_t> body(nb, 1u);
@@ -73,9 +76,14 @@ int main(int argc, char **argv)
         sp.particleRadius = (Real)radius;
         sp.cflFactor = 1;
         sp.viscosityMethod = visc ? 6 : 0;
-        FluidModel model;
+        FluidModel model, second;
         const std::vector<Vector3r> xv = to_vec(x), vv = to_vec(v), xbv = to_vec(xb);
-        model.initModel("Fluid", n, xv.data(), vv.data());
+        const uint32_t n0 = phase0 ? phase0 : n;
+        model.initModel("Fluid", n0, xv.data(), vv.data());
+        if (phase0) {   // a second fluid model (a phase of its own rest density)
+            second.initModel("Fluid2", n - n0, xv.data() + n0, vv.data() + n0);
+            second.m_density0 = (Real)rho1;
+        }
         // one boundary model per body: the dynamic body (body 0) and the static walls
         std::vector<Vector3r> part[2];
         for (uint32_t k = 0; k < nb; k++) {
@@ -118,6 +126,7 @@ int main(int argc, char **argv)
                                            visc ? &viscosity : nullptr)
                  : new TimeStepDFSPH_GB300(model, boundaries, sp, visc ? &viscosity : nullptr));
         TimeStepDFSPH_GB300 &ts = *tsp;
+        if (phase0) ts.addFluidModel(second);
         sphgb_set_lanes_per_particle(ts.context(), lanes);
         ts.resize();
 
@@ -132,13 +141,15 @@ int main(int argc, char **argv)
             wr(o, it, 3);
             wr(o, &t, 1);
         }
-        std::vector<double> out;
-        for (uint32_t i = 0; i < n; i++)
-            for (int c = 0; c < 3; c++) out.push_back(model.getPosition(i)[c]);
-        for (uint32_t i = 0; i < n; i++)
-            for (int c = 0; c < 3; c++) out.push_back(model.getVelocity(i)[c]);
-        for (uint32_t i = 0; i < n; i++) out.push_back(model.getDensity(i));
-        for (uint32_t i = 0; i < n; i++) out.push_back(ts.getPressureRho2(i));
+        std::vector<double> out;   // every fluid model in model order
+        auto each = [&](auto fn) {
+            for (unsigned int k = 0; k < ts.numberOfFluidModels(); k++)
+                for (uint32_t i = 0; i < ts.getFluidModel(k)->numParticles(); i++) fn(k, i);
+        };
+        each([&](unsigned k, uint32_t i) { for (int c = 0; c < 3; c++) out.push_back(ts.getFluidModel(k)->getPosition(i)[c]); });
+        each([&](unsigned k, uint32_t i) { for (int c = 0; c < 3; c++) out.push_back(ts.getFluidModel(k)->getVelocity(i)[c]); });
+        each([&](unsigned k, uint32_t i) { out.push_back(ts.getFluidModel(k)->getDensity(i)); });
+        each([&](unsigned k, uint32_t i) { out.push_back(ts.getPressureRho2(k, i)); });
         for (BoundaryModel_Akinci2012 *bm : boundaries)
             for (uint32_t i = 0; i < bm->numberOfParticles(); i++) out.push_back(bm->getVolume(i));
         Vector3r force, torque;

@@ -15,11 +15,13 @@ from splishsplash_gb300 import build, scenes
 from splishsplash_gb300.dfsph import TimeStepDFSPH
 
 
-def _write_scene(path, sc, steps, lanes, visc, body=None, position=None, vmap=None, motion=None):
+def _write_scene(path, sc, steps, lanes, visc, body=None, position=None, vmap=None, motion=None, phases=None):
     with open(path, "wb") as f:
-        f.write(struct.pack("<7I", sc.n, sc.nb, steps, lanes, 1 if visc else 0, 0 if body is None else 1,
-                            0 if vmap is None else 1))
+        f.write(struct.pack("<8I", sc.n, sc.nb, steps, lanes, 1 if visc else 0, 0 if body is None else 1,
+                            0 if vmap is None else 1, 0 if phases is None else phases[0]))
         f.write(struct.pack("<d", sc.params.particleRadius))
+        if phases is not None:
+            f.write(struct.pack("<d", phases[1]))
         for a in (sc.x, sc.v, sc.xb):
             f.write(np.ascontiguousarray(a, "<f8").tobytes())
         if body is not None:
@@ -68,9 +70,10 @@ def test_host_layer_is_built_and_fails_cleanly_without_a_device():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("visc,bodies,vmap", [(False, False, False), (True, False, False), (True, True, False),
-                                              (True, False, True), (True, True, True)])
-def test_cpp_host_layer_matches_python_mirror(visc, bodies, vmap):
+@pytest.mark.parametrize("visc,bodies,vmap,phases", [(False, False, False, False), (True, False, False, False),
+                                                     (True, True, False, False), (True, False, True, False),
+                                                     (True, True, True, False), (False, False, False, True)])
+def test_cpp_host_layer_matches_python_mirror(visc, bodies, vmap, phases):
     """with a volume map and bodies the container is a dynamic body with a velocity and an angular
     velocity (pose held): the C++ layer hands them to the device before every step"""
     sc = scenes.small_block(counts=(10, 12, 10), box=(0.8, 1.0, 0.8), viscosity=visc,
@@ -101,8 +104,14 @@ def test_cpp_host_layer_matches_python_mirror(visc, bodies, vmap):
         sc = dataclasses.replace(sc, xb=np.zeros((0, 3)))
         verts, faces = scenes.box_mesh((0, 0, 0), (0.75, 1.0, 0.75))   # exact in float (the C++ Real)
         mesh = (verts, faces, (8, 10, 8))
+    ph = None
+    if phases:
+        # a second fluid model of half the rest density above the first one (TimeStepDFSPH_GB300::addFluidModel)
+        order = np.argsort(sc.x[:, 1], kind="stable")
+        sc = dataclasses.replace(sc, x=sc.x[order].copy(), v=sc.v[order].copy())
+        ph = (sc.n // 2, 500.0)
     with tempfile.TemporaryDirectory() as d:
-        _write_scene(os.path.join(d, "s.bin"), sc, steps, lanes, visc, body, position, mesh, motion)
+        _write_scene(os.path.join(d, "s.bin"), sc, steps, lanes, visc, body, position, mesh, motion, ph)
         r = subprocess.run([build.HOST_DEMO, os.path.join(d, "s.bin"), os.path.join(d, "o.bin")],
                            capture_output=True, text=True, timeout=300)
         assert r.returncode == 0, r.stderr
@@ -117,6 +126,8 @@ def test_cpp_host_layer_matches_python_mirror(visc, bodies, vmap):
         sc = dataclasses.replace(sc, xb=xb)
     ts = TimeStepDFSPH(sc)
     ts.ctx.set_lanes_per_particle(lanes)
+    if phases:
+        ts.ctx.set_fluid_phases((ph[0], sc.n - ph[0]), (sc.params.density0, ph[1]))
     if vmap:
         ts.ctx.add_volume_map(mesh[0], mesh[1], mesh[2], invert=True)
         ts.ctx.set_boundary_method(2)
