@@ -361,10 +361,12 @@ int sphgb_set_boundary_bodies(sphgb_ctx *ctx, const uint32_t *body, uint32_t nbo
  * pressure acceleration sums kappa_i + (density0_j / density0_i) kappa_j (TimeStepDFSPH.cpp:1312),
  * XSPH weighs neighbours by their own mass, and each solver iteration visits the phases in turn,
  * each against its own tolerance (:322-339, :476-495), so a phase sees the kappa the phases before
- * it updated in the same iteration.  nphases <= 1 returns to one phase of sphgb_params.density0.
- * At the step: SPHGB_ERR_STATE when the counts do not add up to the fluid or for a batch;
- * SPHGB_ERR_ARGUMENT with Weiler2018 viscosity (the reference solves it per model over same-phase
- * neighbours) or the learned warm start.  Up to 8 phases. */
+ * it updated in the same iteration.  Weiler2018 viscosity solves one system per phase, in phase
+ * order, over same-phase fluid neighbours with mu = viscosity density0[k] and mub =
+ * viscosity_boundary density0[k] (Viscosity_Weiler2018.cpp:288-289, a per-model force); the step's
+ * visco_iterations is the phases' sum and visco_error their largest.  nphases <= 1 returns to one
+ * phase of sphgb_params.density0.  At the step: SPHGB_ERR_STATE when the counts do not add up to
+ * the fluid or for a batch; SPHGB_ERR_ARGUMENT with the learned warm start.  Up to 8 phases. */
 int sphgb_set_fluid_phases(sphgb_ctx *ctx, uint32_t nphases, const uint32_t *counts, const double *density0);
 int sphgb_set_body_motion(sphgb_ctx *ctx, uint32_t body, const double rotation[9], const double translation[3],
                           const double velocity[3], const double omega[3]);

@@ -778,22 +778,34 @@ static void xsph(ctx_t *c, double h)
 /* ------------------------------------------------------------------------ */
 /* Weiler et al. 2018 implicit viscosity (Viscosity_Weiler2018.cpp).          */
 /* ------------------------------------------------------------------------ */
+/* One system per fluid model (Viscosity_Weiler2018 is a per-model NonPressureForceBase, its
+ * sums run over forall_fluid_neighbors_in_same_phase): the particles [lo, hi) of phase ph
+ * (-1: the one model), its rest density rho0 and mu = nu rho0, mub = nu_b rho0. */
 typedef struct {
     ctx_t *c;
-    double dt, mu, mub, h2, d;
+    double dt, mu, mub, h2, d, rho0;
+    long lo, hi;
+    int ph;
 } visc_t;
 
-static visc_t visc_make(ctx_t *c, double dt)
+static visc_t visc_make(ctx_t *c, double dt, int ph, long lo, long hi)
 {
     visc_t w;
     w.c = c;
     w.dt = dt;
-    w.mu = c->p->viscosity * c->rho0;            /* :288 */
-    w.mub = c->p->viscosity_boundary * c->rho0;  /* :289 */
+    w.rho0 = ph >= 0 ? c->s->phase_density0[ph] : c->rho0;
+    w.mu = c->p->viscosity * w.rho0;             /* :288 */
+    w.mub = c->p->viscosity_boundary * w.rho0;   /* :289 */
     w.h2 = c->K.h * c->K.h;
     w.d = 10.0;                                  /* 3D, :292-294 */
+    w.lo = lo;
+    w.hi = hi;
+    w.ph = ph;
     return w;
 }
+
+/* a fluid neighbour of another phase takes no part in the phase's system */
+static inline int visc_skip(const visc_t *w, unsigned j) { return w->ph >= 0 && w->c->ph[j] != w->ph; }
 
 /* matrixVecProd, scalar path (Viscosity_Weiler2018.cpp:271-443). */
 static void visc_matvec(const visc_t *w, const real *vec, real *result)
@@ -801,18 +813,19 @@ static void visc_matvec(const visc_t *w, const real *vec, real *result)
     const ctx_t *c = w->c;
     const orc_state *s = c->s;
 #pragma omp parallel for schedule(static)
-    for (long i = 0; i < (long)s->n; i++) {
+    for (long i = w->lo; i < w->hi; i++) {
         const real *xi = s->x + 3 * i;
         const double rhoi = (double)s->density[i];
         const real *vi = vec + 3 * i;
         double ai[3] = {0, 0, 0};
         for (unsigned k = c->F.off[i]; k < c->F.off[i + 1]; k++) {
             const unsigned j = c->F.idx[k];
+            if (visc_skip(w, j)) continue;
             double r[3], g[3], dv[3];
             diffv(xi, s->x + 3 * (size_t)j, r);
             kGradW(&c->K, r, g);
             diffv(vi, vec + 3 * (size_t)j, dv);
-            const double f = w->d * w->mu * (c->mass / (double)s->density[j]) * dot3(dv, r) / (dot3(r, r) + 0.01 * w->h2);
+            const double f = w->d * w->mu * (mass_of(c, j) / (double)s->density[j]) * dot3(dv, r) / (dot3(r, r) + 0.01 * w->h2);
             ai[0] += f * g[0]; ai[1] += f * g[1]; ai[2] += f * g[2];
         }
         if (w->mub != 0.0) {
@@ -835,7 +848,7 @@ static void visc_matvec(const visc_t *w, const real *vec, real *result)
                 double r[3], g[3];
                 diffv(xi, s->xb + 3 * (size_t)j, r);
                 kGradW(&c->K, r, g);
-                const double f = w->d * w->mub * (c->rho0 * (double)s->Vb[j] / rhoi) * dot3(v3, r) / (dot3(r, r) + 0.01 * w->h2);
+                const double f = w->d * w->mub * (w->rho0 * (double)s->Vb[j] / rhoi) * dot3(v3, r) / (dot3(r, r) + 0.01 * w->h2);
                 ai[0] += f * g[0]; ai[1] += f * g[1]; ai[2] += f * g[2];
             }
         }
@@ -853,16 +866,17 @@ static void visc_diag_inverse(const visc_t *w, real *diag9, real *inv9)
     const ctx_t *c = w->c;
     const orc_state *s = c->s;
 #pragma omp parallel for schedule(static)
-    for (long i = 0; i < (long)s->n; i++) {
+    for (long i = w->lo; i < w->hi; i++) {
         const real *xi = s->x + 3 * i;
         const double rhoi = (double)s->density[i];
         double R[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
         for (unsigned k = c->F.off[i]; k < c->F.off[i + 1]; k++) {
             const unsigned j = c->F.idx[k];
+            if (visc_skip(w, j)) continue;
             double r[3], g[3];
             diffv(xi, s->x + 3 * (size_t)j, r);
             kGradW(&c->K, r, g);
-            const double f = w->d * w->mu * (c->mass / (double)s->density[j]) / (dot3(r, r) + 0.01 * w->h2);
+            const double f = w->d * w->mu * (mass_of(c, j) / (double)s->density[j]) / (dot3(r, r) + 0.01 * w->h2);
             for (int a = 0; a < 3; a++)
                 for (int b = 0; b < 3; b++) R[3 * a + b] += f * g[a] * r[b];
         }
@@ -886,7 +900,7 @@ static void visc_diag_inverse(const visc_t *w, real *diag9, real *inv9)
                 double r[3], g[3];
                 diffv(xi, s->xb + 3 * (size_t)j, r);
                 kGradW(&c->K, r, g);
-                const double f = w->d * w->mub * (c->rho0 * (double)s->Vb[j] / rhoi) / (dot3(r, r) + 0.01 * w->h2);
+                const double f = w->d * w->mub * (w->rho0 * (double)s->Vb[j] / rhoi) / (dot3(r, r) + 0.01 * w->h2);
                 for (int a = 0; a < 3; a++)
                     for (int b = 0; b < 3; b++) R[3 * a + b] += f * g[a] * r[b];
             }
@@ -925,14 +939,14 @@ static void visc_rhs(const visc_t *w, real *b, real *g)
 {
     const ctx_t *c = w->c;
     const orc_state *s = c->s;
-    for (size_t i = 0; i < 3 * (size_t)s->n; i++) {
+    for (size_t i = 3 * (size_t)w->lo; i < 3 * (size_t)w->hi; i++) {
         b[i] = s->v[i];
         g[i] = (real)((double)s->v[i] + (double)s->vdiff[i]);
     }
     if (w->mub == 0.0) return;
     if (c->p->boundary_method != 2) {   /* moving boundary particles (:1130-1138) */
         if (!s->vb) return;
-        for (long i = 0; i < (long)s->n; i++) {
+        for (long i = w->lo; i < w->hi; i++) {
             const real *xi = s->x + 3 * i;
             const double rhoi = (double)s->density[i];
             double bi[3] = {0, 0, 0};
@@ -942,14 +956,14 @@ static void visc_rhs(const visc_t *w, real *b, real *g)
                 diffv(xi, s->xb + 3 * (size_t)j, r);
                 kGradW(&c->K, r, gw);
                 boundary_velocity(c, j, vj);
-                const double f = w->d * w->mub * (c->rho0 * (double)s->Vb[j] / rhoi) * dot3(vj, r) / (dot3(r, r) + 0.01 * w->h2);
+                const double f = w->d * w->mub * (w->rho0 * (double)s->Vb[j] / rhoi) * dot3(vj, r) / (dot3(r, r) + 0.01 * w->h2);
                 for (int d = 0; d < 3; d++) bi[d] += f * gw[d];
             }
             for (int d = 0; d < 3; d++) b[3 * i + d] = (real)((double)s->v[3 * i + d] - w->dt / rhoi * bi[d]);
         }
         return;
     }
-    for (long i = 0; i < (long)s->n; i++) {
+    for (long i = w->lo; i < w->hi; i++) {
         const real *xi = s->x + 3 * i;
         double bi[3] = {0, 0, 0};
         for (unsigned k = c->B.off[i]; k < c->B.off[i + 1]; k++) {
@@ -978,10 +992,10 @@ static double vdot(const real *a, const real *b, size_t n)
     return s;
 }
 
-static void precond_apply(const real *inv9, const real *r, real *z, unsigned n)
+static void precond_apply(const real *inv9, const real *r, real *z, long lo, long hi)
 {
 #pragma omp parallel for schedule(static)
-    for (long i = 0; i < (long)n; i++)
+    for (long i = lo; i < hi; i++)
         for (int a = 0; a < 3; a++)
             z[3 * i + a] = (real)((double)inv9[9 * i + 3 * a + 0] * (double)r[3 * i + 0] +
                                   (double)inv9[9 * i + 3 * a + 1] * (double)r[3 * i + 1] +
@@ -996,16 +1010,17 @@ static int visc_cg(const visc_t *w, const real *b, real *x, const real *inv9,
 {
     const unsigned n = w->c->s->n;
     const size_t N = 3 * (size_t)n;
+    const size_t k0 = 3 * (size_t)w->lo, k1 = 3 * (size_t)w->hi, M = k1 - k0;   /* the phase's rows */
     real *r = (real *)malloc(N * sizeof(real));
     real *p = (real *)malloc(N * sizeof(real));
     real *z = (real *)malloc(N * sizeof(real));
     real *t = (real *)malloc(N * sizeof(real));
     if (!r || !p || !z || !t) { free(r); free(p); free(z); free(t); return -2; }
     visc_matvec(w, x, t);
-    for (size_t k = 0; k < N; k++) r[k] = (real)((double)b[k] - (double)t[k]);
-    const double rhsNorm2 = vdot(b, b, N);
+    for (size_t k = k0; k < k1; k++) r[k] = (real)((double)b[k] - (double)t[k]);
+    const double rhsNorm2 = vdot(b + k0, b + k0, M);
     if (rhsNorm2 == 0.0) {
-        for (size_t k = 0; k < N; k++) x[k] = 0;
+        for (size_t k = k0; k < k1; k++) x[k] = 0;
         *iters_out = 0;
         *err_out = 0.0;
         free(r); free(p); free(z); free(t);
@@ -1014,30 +1029,30 @@ static int visc_cg(const visc_t *w, const real *b, real *x, const real *inv9,
     const double considerAsZero = (sizeof(real) == sizeof(double)) ? DBL_MIN : (double)FLT_MIN;
     double threshold = tol * tol * rhsNorm2;
     if (threshold < considerAsZero) threshold = considerAsZero;
-    double resNorm2 = vdot(r, r, N);
+    double resNorm2 = vdot(r + k0, r + k0, M);
     if (resNorm2 < threshold) {
         *iters_out = 0;
         *err_out = sqrt(resNorm2 / rhsNorm2);
         free(r); free(p); free(z); free(t);
         return 0;
     }
-    precond_apply(inv9, r, p, n);
-    double absNew = vdot(r, p, N);
+    precond_apply(inv9, r, p, w->lo, w->hi);
+    double absNew = vdot(r + k0, p + k0, M);
     unsigned i = 0;
     while (i < max_iters) {
         visc_matvec(w, p, t);
-        const double alpha = absNew / vdot(p, t, N);
-        for (size_t k = 0; k < N; k++) {
+        const double alpha = absNew / vdot(p + k0, t + k0, M);
+        for (size_t k = k0; k < k1; k++) {
             x[k] = (real)((double)x[k] + alpha * (double)p[k]);
             r[k] = (real)((double)r[k] - alpha * (double)t[k]);
         }
-        resNorm2 = vdot(r, r, N);
+        resNorm2 = vdot(r + k0, r + k0, M);
         if (resNorm2 < threshold) break;
-        precond_apply(inv9, r, z, n);
+        precond_apply(inv9, r, z, w->lo, w->hi);
         const double absOld = absNew;
-        absNew = vdot(r, z, N);
+        absNew = vdot(r + k0, z + k0, M);
         const double beta = absNew / absOld;
-        for (size_t k = 0; k < N; k++) p[k] = (real)((double)z[k] + beta * (double)p[k]);
+        for (size_t k = k0; k < k1; k++) p[k] = (real)((double)z[k] + beta * (double)p[k]);
         i++;
     }
     *iters_out = i;
@@ -1046,36 +1061,48 @@ static int visc_cg(const visc_t *w, const real *b, real *x, const real *inv9,
     return 0;
 }
 
-/* Viscosity_Weiler2018::step + applyForces (Viscosity_Weiler2018.cpp:891-936). */
+/* Viscosity_Weiler2018::step + applyForces (Viscosity_Weiler2018.cpp:891-936), once per fluid
+ * model in model order (TimeStepDFSPH.cpp:172-173 runs each model's non-pressure forces); the
+ * reported iterations are the models' sum, the error their largest. */
 static int viscosity_weiler(ctx_t *c, double dt)
 {
     orc_state *s = c->s;
     const size_t N = 3 * (size_t)s->n;
     if (s->n == 0) return 0;
-    visc_t w = visc_make(c, dt);
     real *b = (real *)malloc(N * sizeof(real));
     real *x = (real *)malloc(N * sizeof(real));
     real *inv9 = (real *)malloc(3 * N * sizeof(real));
     if (!b || !x || !inv9) { free(b); free(x); free(inv9); return -2; }
-    visc_diag_inverse(&w, NULL, inv9);
-    visc_rhs(&w, b, x);
-    unsigned it = 0;
-    double err = 0.0;
-    int rc = visc_cg(&w, b, x, inv9, c->p->visco_max_iter, c->p->visco_max_error, &it, &err);
-    s->visco_iterations = it;
-    s->visco_error = err;
+    const int nph = c->r0 ? (int)c->nph : 1;
+    int rc = 0;
+    long lo = 0;
+    s->visco_iterations = 0;
+    s->visco_error = 0.0;
+    for (int ph = 0; ph < nph && rc == 0; ph++) {
+        const long hi = c->r0 ? lo + (long)s->phase_count[ph] : (long)s->n;
+        visc_t w = visc_make(c, dt, c->r0 ? ph : -1, lo, hi);
+        visc_diag_inverse(&w, NULL, inv9);
+        visc_rhs(&w, b, x);
+        unsigned it = 0;
+        double err = 0.0;
+        rc = visc_cg(&w, b, x, inv9, c->p->visco_max_iter, c->p->visco_max_error, &it, &err);
+        s->visco_iterations += it;
+        if (err > s->visco_error) s->visco_error = err;
+        lo = hi;
+    }
     for (size_t k = 0; k < N; k++) {
         const double dv = (double)x[k] - (double)s->v[k];
         s->a[k] = (real)((double)s->a[k] + (1.0 / dt) * dv);
         s->vdiff[k] = (real)dv;
     }
     /* boundary feedback of applyForces (Viscosity_Weiler2018.cpp:960-975), static v_b = 0:
-     * a = d mub (rho0 V_b / rho_i) (v_i'.x_ib) / (|x_ib|^2 + 0.01 h^2) gradW_ib, force -m_i / rho_i a */
-    const double mub = c->p->viscosity_boundary * c->rho0;
-    if (mub != 0.0 && collects_forces(s, c->p->boundary_method == 2)) {
+     * a = d mub (rho0 V_b / rho_i) (v_i'.x_ib) / (|x_ib|^2 + 0.01 h^2) gradW_ib, force -m_i / rho_i a,
+     * rho0, mub and m_i those of the particle's model */
+    if (c->p->viscosity_boundary != 0.0 && collects_forces(s, c->p->boundary_method == 2)) {
         const double h2 = c->K.h * c->K.h;
         for (long i = 0; i < (long)s->n; i++) {
             const double rhoi = (double)s->density[i];
+            const double r0 = rho0_of(c, i), mub = c->p->viscosity_boundary * r0, mi = mass_of(c, i);
             const double nv[3] = {(double)x[3 * i], (double)x[3 * i + 1], (double)x[3 * i + 2]};
             for (unsigned k = c->B.off[i]; k < c->B.off[i + 1]; k++) {
                 const unsigned j = c->B.idx[k];
@@ -1090,7 +1117,7 @@ static int viscosity_weiler(ctx_t *c, double dt)
                         boundary_point_velocity(c, j, xs[q], vk);
                         const double dv[3] = {nv[0] - vk[0], nv[1] - vk[1], nv[2] - vk[2]};
                         const double coef = 10.0 * mub * vol * dot3(dv, r) / (dot3(r, r) + 0.01 * h2);
-                        for (int d = 0; d < 3; d++) f[d] = -c->mass / rhoi * (coef * g[d]);
+                        for (int d = 0; d < 3; d++) f[d] = -mi / rhoi * (coef * g[d]);
                         add_force_at(c, j, xs[q], f);
                     }
                     continue;
@@ -1100,8 +1127,8 @@ static int viscosity_weiler(ctx_t *c, double dt)
                 kGradW(&c->K, r, g);
                 boundary_velocity(c, j, vj);
                 const double dv[3] = {nv[0] - vj[0], nv[1] - vj[1], nv[2] - vj[2]};
-                const double coef = 10.0 * mub * (c->rho0 * (double)s->Vb[j] / rhoi) * dot3(dv, r) / (dot3(r, r) + 0.01 * h2);
-                for (int d = 0; d < 3; d++) f[d] = -c->mass / rhoi * (coef * g[d]);
+                const double coef = 10.0 * mub * (r0 * (double)s->Vb[j] / rhoi) * dot3(dv, r) / (dot3(r, r) + 0.01 * h2);
+                for (int d = 0; d < 3; d++) f[d] = -mi / rhoi * (coef * g[d]);
                 add_force(c, j, f);
             }
         }
@@ -1246,10 +1273,8 @@ int orc_step(orc_state *s, const orc_params *p)
     /* Bender2019: the bodies are the maps (no body array) */
     const int vmaps = p->boundary_method == 2;
     if (vmaps && s->body) return -5;
-    /* several fluid phases: each particle's rest density; Weiler2018 solves per fluid model over
-     * same-phase neighbours, which this restatement does not cover */
+    /* several fluid phases: each particle's rest density */
     if (s->nphase > 1) {
-        if (p->viscosity_method == 6) return -6;
         unsigned total = 0;
         for (unsigned k = 0; k < s->nphase; k++) total += s->phase_count[k];
         if (total != s->n) return -6;
@@ -1365,7 +1390,7 @@ int orc_weiler_system(const orc_state *s, const orc_params *p, double dt, real *
 {
     ctx_t c;
     if (ctx_for_state(&c, s, p) != 0) return -1;
-    visc_t w = visc_make(&c, dt);
+    visc_t w = visc_make(&c, dt, -1, 0, (long)s->n);
     visc_diag_inverse(&w, diag9, NULL);
     visc_rhs(&w, b, g);
     lists_free(&c.F);
@@ -1377,7 +1402,7 @@ int orc_weiler_matvec(const orc_state *s, const orc_params *p, double dt, const 
 {
     ctx_t c;
     if (ctx_for_state(&c, s, p) != 0) return -1;
-    visc_t w = visc_make(&c, dt);
+    visc_t w = visc_make(&c, dt, -1, 0, (long)s->n);
     visc_matvec(&w, vec, result);
     lists_free(&c.F);
     lists_free(&c.B);
@@ -1388,7 +1413,7 @@ int orc_weiler_solve(const orc_state *s, const orc_params *p, double dt, real *x
 {
     ctx_t c;
     if (ctx_for_state(&c, s, p) != 0) return -1;
-    visc_t w = visc_make(&c, dt);
+    visc_t w = visc_make(&c, dt, -1, 0, (long)s->n);
     const size_t N = 3 * (size_t)s->n;
     real *b = (real *)malloc(N * sizeof(real));
     real *inv9 = (real *)malloc(3 * N * sizeof(real));

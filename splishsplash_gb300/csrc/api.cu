@@ -412,6 +412,8 @@ template <class T> DevParams<T> make_params(const sphgb_ctx *c)
     P.xsph_b = (T)q.xsph_boundary;
     P.mu = (T)(q.viscosity * q.density0);
     P.mub = (T)(q.viscosity_boundary * q.density0);
+    P.visc_nu = (T)q.viscosity;
+    P.visc_nub = (T)q.viscosity_boundary;
     P.vd = (T)10.0;
     P.h2 = (T)(h * h);
     P.max_error = q.max_error;
@@ -832,6 +834,20 @@ template <class T> BoundaryMoveDev<T> boundary_move_dev(const sphgb_ctx *c)
 }
 
 // Enqueue the launches that precede the solver loops.
+// Weiler2018 with fluid phases: one system per phase in phase order (the reference's viscosity is a
+// per-model force, Viscosity_Weiler2018.cpp:891-936 run for each FluidModel); phase k's system
+// takes mub = nu_b rho0 and rho0 of that phase in its boundary terms.  -1: one system over all.
+template <class T> int visc_systems(const DevParams<T> &P) { return P.nphase > 1 ? (int)P.nphase : 1; }
+template <class T> DevParams<T> visc_system_params(const sphgb_ctx *c, const DevParams<T> &P, int k, int &phase)
+{
+    phase = P.nphase > 1 ? k : -1;
+    if (phase < 0) return P;
+    DevParams<T> Q = P;
+    Q.mub = (T)(c->prm.viscosity_boundary * c->phase_rho0[k]);
+    Q.rho0 = (T)c->phase_rho0[k];
+    return Q;
+}
+
 template <class T> void enqueue_prologue(sphgb_ctx *c, const DevParams<T> &P, const DevBufs<T> &B0, const DevBufs<T> &B1,
                                          cudaStream_t s)
 {
@@ -902,15 +918,19 @@ template <class T> int step_host_loop(sphgb_ctx *c)
     if (P.div_on && (rc = solve(true))) return rc;
     { PROF(K_XSPH, s); launch_xsph<T>(P, B1, s); }
     if (P.visc_on) {
-        { PROF(K_VISC_SETUP, s); launch_visc_setup<T>(P, B1, 0, false, s); }
-        if ((rc = read_cont(c, &cont))) return rc;
-        unsigned guard = 0;
-        while (cont && guard++ <= P.visc_max_iter) {
-            { PROF(K_CG_MATVEC, s); launch_cg_matvec<T>(P, B1, s); }
-            { PROF(K_CG_UPDATE, s); launch_cg_update<T>(P, B1, 0, false, s); }
+        for (int k = 0; k < visc_systems(P); k++) {
+            int ph;
+            const DevParams<T> Q = visc_system_params(c, P, k, ph);
+            { PROF(K_VISC_SETUP, s); launch_visc_setup<T>(Q, B1, 0, false, s, ph); }
             if ((rc = read_cont(c, &cont))) return rc;
-            if (!cont) break;
-            { PROF(K_CG_P, s); launch_cg_p<T>(P, B1, s); }
+            unsigned guard = 0;
+            while (cont && guard++ <= P.visc_max_iter) {
+                { PROF(K_CG_MATVEC, s); launch_cg_matvec<T>(Q, B1, s, 0, false, ph); }
+                { PROF(K_CG_UPDATE, s); launch_cg_update<T>(Q, B1, 0, false, s, ph); }
+                if ((rc = read_cont(c, &cont))) return rc;
+                if (!cont) break;
+                { PROF(K_CG_P, s); launch_cg_p<T>(Q, B1, s, ph); }
+            }
         }
     }
     if (body_phase0(c, P)) {
@@ -1009,16 +1029,18 @@ template <class T> int build_graph(sphgb_ctx *c, int parity, cudaGraphExec_t *ou
     };
     if (P.div_on) solve(true);
     launch_xsph<T>(P, B1, s);
-    if (P.visc_on && e == cudaSuccess) {
-        // the set-up kernel sets the CG loop's condition
+    for (int k = 0; P.visc_on && e == cudaSuccess && k < visc_systems(P); k++) {
+        // the set-up kernel sets the CG loop's condition; one loop per system
+        int ph;
+        const DevParams<T> Q = visc_system_params(c, P, k, ph);
         cudaGraphConditionalHandle hcg = 0;
         e = make_handle(c, &hcg, 0u);
         if (e == cudaSuccess) {
-            launch_visc_setup<T>(P, B1, hcg, true, s);
+            launch_visc_setup<T>(Q, B1, hcg, true, s, ph);
             e = add_while_node(c, hcg, [&](cudaStream_t bs, cudaGraphConditionalHandle hh) {
-                launch_cg_matvec<T>(P, B1, bs, hh, true);
-                launch_cg_update<T>(P, B1, hh, true, bs);
-                launch_cg_p<T>(P, B1, bs);
+                launch_cg_matvec<T>(Q, B1, bs, hh, true, ph);
+                launch_cg_update<T>(Q, B1, hh, true, bs, ph);
+                launch_cg_p<T>(Q, B1, bs, ph);
             });
         }
     }
@@ -1292,8 +1314,6 @@ int check_phases(sphgb_ctx *c)
     for (uint32_t n : c->phase_counts) total += n;
     if (total != c->n) return fail(c, SPHGB_ERR_STATE, "the fluid phases do not cover the uploaded fluid");
     if (c->nscenes() > 1) return fail(c, SPHGB_ERR_STATE, "fluid phases serve a single scene, not a batch");
-    if (c->prm.viscosity_method == 6)
-        return fail(c, SPHGB_ERR_ARGUMENT, "Weiler2018 viscosity with several fluid phases is not supported");
     if (c->learned) return fail(c, SPHGB_ERR_ARGUMENT, "the learned warm start takes one fluid phase");
     return SPHGB_OK;
 }
@@ -1340,13 +1360,15 @@ void scene_stats(const sphgb_ctx *c, const StepScalars &h, const StepScalars &g,
 {
     st->iterations = h.iters;
     st->iterations_v = h.iters_v;
-    st->visco_iterations = c->prm.viscosity_method == 6 ? h.iters_cg : 0;
+    // fluid phases: the phases' systems' iterations summed, their largest final error
+    const bool phases = c->phase_counts.size() > 1;
+    st->visco_iterations = c->prm.viscosity_method == 6 ? (phases ? h.iters_cg_tot : h.iters_cg) : 0;
     st->max_fluid_neighbors = h.max_nf;
     st->max_boundary_neighbors = h.max_nb;
     st->flags = h.flags | g.flags;
     st->avg_density_err = h.avg_err;
     st->avg_density_err_v = h.avg_err_v;
-    st->visco_error = c->prm.viscosity_method == 6 ? h.cg_err : 0.0;
+    st->visco_error = c->prm.viscosity_method == 6 ? (phases ? std::max(h.cg_err_max, h.cg_err) : h.cg_err) : 0.0;
     st->dt_used = h.dt_used;
     st->dt_next = h.dt_next;
     st->time = h.time;

@@ -1269,7 +1269,15 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams<T> P, DevBufs<T> B, i
     if (P.visc_on) {
         // Weiler2018 warm start g = v + vDiff (Viscosity_Weiler2018.cpp:1247-1250) with the
         // operator weight d mu m_i / rho_i in w
-        stv(B.cg_x, i, pack(add(vi, xyz<T>(ldv(B.vdiff, i))), P.vd * P.mu * P.mass / B.density[i]));
+        // (fluid phases: mu = nu rho0 and m_i = V rho0 of the particle's phase)
+        T wi;
+        if (P.nphase > 1) {
+            const T r0 = B.r0[i];
+            wi = P.vd * (P.visc_nu * r0) * (P.V * r0) / B.density[i];
+        } else {
+            wi = P.vd * P.mu * P.mass / B.density[i];
+        }
+        stv(B.cg_x, i, pack(add(vi, xyz<T>(ldv(B.vdiff, i))), wi));
     }
 }
 
@@ -1350,12 +1358,20 @@ template <class T> __device__ __forceinline__ V3<T> sym_mul(const v4_t<T> &a, co
 // diagonal blocks (inverse taken in MatrixFreeSolver.h:231-244), b = v (computeRHS :1091-1254,
 // static boundary), warm start g = v + vDiff (already in cg_x), r = b - A g, p = M^-1 r, and
 // the first reductions of Eigen's conjugate_gradient (ConjugateGradient.h:29-70), one pass.
-template <class T, int LPP>
+// MP (fluid phases): the system of phase `phase` alone (Viscosity_Weiler2018 is per fluid model and
+// sums over forall_fluid_neighbors_in_same_phase); the other phases' particles get p = 0 with
+// weight 0, so the matrix-vector passes of this phase need no neighbour test.
+template <class T, int LPP, bool MP = false>
 __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T> B, cudaGraphConditionalHandle handle,
-                                                        int use_handle)
+                                                        int use_handle, int phase)
 {
     count_launch(&B.gsc->launches);
-    const SlotInfo q = slot_info<LPP>(P);
+    SlotInfo q = slot_info<LPP>(P);
+    bool other = false;   // a slot of another phase
+    if (MP && q.act && B.ph[q.i] != (uint32_t)phase) {
+        other = true;
+        q.act = false;
+    }
     StepScalars *const sc = B.sc + q.s;
     DSum<3> mine;
     mine.v[0] = mine.v[1] = mine.v[2] = 0.0;
@@ -1375,7 +1391,8 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T
             v4_t<T> x, g;
         };
         fluid_loop<LPP, kUnroll>(P, B, i, q.l, [&](uint32_t j) { return XG{ldv(B.x, j), ldv(B.cg_x, j)}; },
-                                 [&](uint32_t, const XG &d) {
+                                 [&](uint32_t j, const XG &d) {
+                                     if (MP && B.ph[j] != (uint32_t)phase) return;
                                      const V3<T> r = diff3<T>(xi, d.x);
                                      const T r2 = dot(r, r);
                                      const T f = (T)d.g.w / (r2 + eps2) * grad_coef_d2(P.K, r2);
@@ -1443,17 +1460,26 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T
         mine.v[1] = (double)dot(r, r);
         mine.v[2] = (double)dot(r, p);
     }
+    if (MP && other && q.l == 0) stv(B.cg_p, q.i, pack(mk3<T>(0, 0, 0), T(0)));
     const double tol = P.visc_tol;
     const unsigned maxit = P.visc_max_iter;
     const DevParams<T> &PP = P;
     const DevBufs<T> &BB = B;
     grid_sum_finalize<3>(mine, scene_reduce<LPP>(P, B, q), [&](const DSum<3> &tot) {
+        if (phase <= 0) {   // the step's first system
+            sc->iters_cg_tot = 0;
+            sc->cg_zero = 0;
+            sc->cg_err_max = 0.0;
+        } else if (sc->cg_err > sc->cg_err_max) {   // the phase before this one
+            sc->cg_err_max = sc->cg_err;
+        }
         sc->cg_rhs2 = tot.v[0];
         sc->iters_cg = 0;
         sc->cg_err = 0.0;
         BB.gsc->loop_guard = 0;
         if (tot.v[0] == 0.0) {
             sc->cg_state = 2;
+            if (phase >= 0) sc->cg_zero |= 1u << phase;
         } else {
             double thr = tol * tol * tot.v[0];
             if (thr < 2.2250738585072014e-308) thr = 2.2250738585072014e-308;
@@ -1477,11 +1503,12 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T
 // tmp = A p and p.tmp -> alpha (ConjugateGradient.h:74-76)
 template <class T, int LPP>
 __global__ void __launch_bounds__(kBlock) k_cg_matvec(DevParams<T> P, DevBufs<T> B, cudaGraphConditionalHandle h,
-                                                       int use_handle)
+                                                       int use_handle, int phase)
 {
     count_launch(&B.gsc->launches);
     loop_guard(B.gsc, P.visc_max_iter + 1, h, use_handle);
-    const SlotInfo q = slot_info<LPP>(P);
+    SlotInfo q = slot_info<LPP>(P);
+    if (phase >= 0 && q.act && B.ph[q.i] != (uint32_t)phase) q.act = false;   // fluid phases
     StepScalars *const sc = B.sc + q.s;
     const bool live = scene_live(P, sc);
     DSum<1> mine;
@@ -1524,10 +1551,11 @@ __global__ void __launch_bounds__(kBlock) k_cg_matvec(DevParams<T> P, DevBufs<T>
 // Element arithmetic in the bulk precision, sums accumulated in FP64.
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_cg_update(DevParams<T> P, DevBufs<T> B, cudaGraphConditionalHandle handle,
-                                                       int use_handle)
+                                                       int use_handle, int phase)
 {
     count_launch(&B.gsc->launches);
-    const SlotInfo q = slot_info(P);
+    SlotInfo q = slot_info(P);
+    if (phase >= 0 && q.act && B.ph[q.i] != (uint32_t)phase) q.act = false;   // fluid phases
     StepScalars *const sc = B.sc + q.s;
     const bool live = scene_live(P, sc);
     DSum<2> mine;
@@ -1564,6 +1592,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(DevParams<T> P, DevBufs<T>
                 sc->cg_absnew = tot.v[1];
                 sc->cg_beta = tot.v[1] / absOld;
                 sc->iters_cg += 1;
+                sc->iters_cg_tot += 1;
                 cont = sc->iters_cg < maxit;
             }
             sc->cont = cont ? 1u : 0u;
@@ -1574,11 +1603,12 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(DevParams<T> P, DevBufs<T>
 
 // p = z + beta p (ConjugateGradient.h:88) for scenes whose CG continues; the weight in p.w is kept
 template <class T>
-__global__ void __launch_bounds__(kBlock) k_cg_p(DevParams<T> P, DevBufs<T> B)
+__global__ void __launch_bounds__(kBlock) k_cg_p(DevParams<T> P, DevBufs<T> B, int phase)
 {
     count_launch(&B.gsc->launches);
     const SlotInfo q = slot_info(P);
     if (!q.act) return;
+    if (phase >= 0 && B.ph[q.i] != (uint32_t)phase) return;   // fluid phases
     const StepScalars *sc = B.sc + q.s;
     if (sc->cg_state != 0 || sc->cont == 0) return;
     const uint32_t i = q.i;
@@ -1612,7 +1642,9 @@ __global__ void __launch_bounds__(kBlock) k_kick(DevParams<T> P, DevBufs<T> B)
         v4_t<T> v4 = ldv(B.v, i);
         const V3<T> v = xyz<T>(v4);
         if (P.visc_on) {
-            const V3<T> x = sc->cg_state == 2 ? mk3<T>(0, 0, 0) : xyz<T>(ldv(B.cg_x, i));
+            // a zero right-hand side has the solution 0 (per phase with fluid phases)
+            const bool zero = P.nphase > 1 ? ((sc->cg_zero >> B.ph[i]) & 1u) != 0u : sc->cg_state == 2;
+            const V3<T> x = zero ? mk3<T>(0, 0, 0) : xyz<T>(ldv(B.cg_x, i));
             const V3<T> dv = sub(x, v);
             a = add(a, scl(dv, T(1) / h));
             stv(B.vdiff, i, pack(dv, T(0)));
@@ -1808,7 +1840,8 @@ __global__ void __launch_bounds__(kBlock) k_body_forces(DevParams<T> P, DevBufs<
         const T Vb = (T)xb.w;
         const bool press = PHASE == 1 || P.div_on;
         const bool xs = PHASE == 0 && P.xsph_b != T(0);
-        const bool visc = PHASE == 0 && P.visc_on && P.mub != T(0) && sc->cg_state != 2u;
+        // (fluid phases: per particle, below)
+        const bool visc = PHASE == 0 && P.visc_on && P.mub != T(0) && (P.nphase > 1 || sc->cg_state != 2u);
         const T xs_c = xs ? P.xsph_b / (T)sc->dt * P.rho0 * Vb : T(0);
         const T vi_c = P.vd * P.mub * P.rho0 * Vb;
         const T eps2 = T(0.01) * P.h2;
@@ -1851,11 +1884,13 @@ __global__ void __launch_bounds__(kBlock) k_body_forces(DevParams<T> P, DevBufs<
                                 if (P.bmove) dv = sub(dv, vbj);
                                 fi = add(fi, scl(dv, w));
                             }
-                            if (visc) {
+                            if (visc && !(P.nphase > 1 && ((sc->cg_zero >> B.ph[i]) & 1u))) {
                                 V3<T> nv = xyz<T>(ldv(B.cg_x, i));
                                 if (P.bmove) nv = sub(nv, vbj);
-                                const T a = vi_c / rhoi * dot(nv, r) / (d2 + eps2) * gc;
-                                fi = sub(fi, scl(r, P.mass / rhoi * a));
+                                // fluid phases: mub = nu_b rho0 and rho0 of the particle's phase
+                                const T vc = P.nphase > 1 ? P.vd * (P.visc_nub * B.r0[i]) * B.r0[i] * Vb : vi_c;
+                                const T a = vc / rhoi * dot(nv, r) / (d2 + eps2) * gc;
+                                fi = sub(fi, scl(r, mi / rhoi * a));
                             }
                         }
                         f[0] += (double)fi.x;
@@ -1931,16 +1966,18 @@ __global__ void __launch_bounds__(kBlock) k_vmap_forces(DevParams<T> P, DevBufs<
                 mine.v[4] = pz * fx - px * fz;
                 mine.v[5] = px * fy - py * fx;
                 // Weiler2018 applyForces at the four samples (Viscosity_Weiler2018.cpp:1031-1080)
-                if (PHASE == 0 && P.visc_on && P.mub != T(0) && B.sc[q.s].cg_state != 2u) {
+                const bool zero = P.nphase > 1 ? ((B.sc[q.s].cg_zero >> B.ph[i]) & 1u) != 0u : B.sc[q.s].cg_state == 2u;
+                if (PHASE == 0 && P.visc_on && P.mub != T(0) && !zero) {
                     const V3<T> nv = xyz<T>(ldv(B.cg_x, i));
                     const T rhoi = B.density[i], vol = T(0.25) * Vj, eps2 = T(0.01) * P.h2;
+                    const T mub = P.nphase > 1 ? P.visc_nub * B.r0[i] : P.mub;   // the particle's phase
                     vmap_samples<T>(xk, xj, P.K.h, [&](const V3<T> &xs4) {
                         const V3<T> r4 = sub(xyz<T>(xk), xs4);
                         const T r2 = dot(r4, r4);
                         V3<T> dv = nv;
                         if (P.vmove) dv = sub(dv, vmap_point_velocity<T>(mp, xs4));
-                        const T a = P.vd * P.mub * vol * dot(dv, r4) / (r2 + eps2) * grad_coef_d2(P.K, r2);
-                        const V3<T> g = scl(r4, -P.mass / rhoi * a);
+                        const T a = P.vd * mub * vol * dot(dv, r4) / (r2 + eps2) * grad_coef_d2(P.K, r2);
+                        const V3<T> g = scl(r4, -mi / rhoi * a);
                         const double gx = (double)g.x, gy = (double)g.y, gz = (double)g.z;
                         const double qx = (double)xs4.x - c[0], qy = (double)xs4.y - c[1], qz = (double)xs4.z - c[2];
                         mine.v[0] += gx;
@@ -2659,24 +2696,29 @@ template <class T> void launch_xsph(const DevParams<T> &P, const DevBufs<T> &B, 
 }
 template <class T>
 void launch_visc_setup(const DevParams<T> &P, const DevBufs<T> &B, cudaGraphConditionalHandle h, bool use_handle,
-                       cudaStream_t s)
+                       cudaStream_t s, int phase)
 {
-    if (P.np) LPP_DISPATCH(P, (k_visc_setup<T, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B, h, use_handle ? 1 : 0)));
+    if (!P.np) return;
+    if (phase >= 0)
+        LPP_DISPATCH(P, (k_visc_setup<T, L, true><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B, h, use_handle ? 1 : 0, phase)));
+    else
+        LPP_DISPATCH(P, (k_visc_setup<T, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B, h, use_handle ? 1 : 0, phase)));
 }
 template <class T> void launch_cg_matvec(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s,
-                                         cudaGraphConditionalHandle h, bool use_handle)
+                                         cudaGraphConditionalHandle h, bool use_handle, int phase)
 {
-    if (P.np) LPP_DISPATCH(P, (k_cg_matvec<T, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B, h, use_handle ? 1 : 0)));
+    if (P.np)
+        LPP_DISPATCH(P, (k_cg_matvec<T, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B, h, use_handle ? 1 : 0, phase)));
 }
 template <class T>
 void launch_cg_update(const DevParams<T> &P, const DevBufs<T> &B, cudaGraphConditionalHandle h, bool use_handle,
-                      cudaStream_t s)
+                      cudaStream_t s, int phase)
 {
-    if (P.np) k_cg_update<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B, h, use_handle ? 1 : 0);
+    if (P.np) k_cg_update<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B, h, use_handle ? 1 : 0, phase);
 }
-template <class T> void launch_cg_p(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
+template <class T> void launch_cg_p(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s, int phase)
 {
-    if (P.np) k_cg_p<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
+    if (P.np) k_cg_p<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B, phase);
 }
 template <class T> void launch_kick(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {
@@ -2827,12 +2869,12 @@ void launch_lists_to_ids(const uint32_t *list, const uint32_t *cnt, uint32_t cap
                                              cudaGraphConditionalHandle, bool, cudaStream_t);                       \
     template void launch_xsph<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                           \
     template void launch_visc_setup<T>(const DevParams<T> &, const DevBufs<T> &, cudaGraphConditionalHandle, bool,  \
-                                       cudaStream_t);                                                               \
+                                       cudaStream_t, int);                                                          \
     template void launch_cg_matvec<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t,                       \
-                                      cudaGraphConditionalHandle, bool);                                            \
+                                      cudaGraphConditionalHandle, bool, int);                                       \
     template void launch_cg_update<T>(const DevParams<T> &, const DevBufs<T> &, cudaGraphConditionalHandle, bool,   \
-                                      cudaStream_t);                                                                \
-    template void launch_cg_p<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                           \
+                                      cudaStream_t, int);                                                           \
+    template void launch_cg_p<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t, int);                      \
     template void launch_kick<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                           \
     template void launch_press_init<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                     \
     template void launch_integrate<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                      \

@@ -43,6 +43,11 @@ struct StepScalars {
     unsigned pad[2];
     unsigned long long maxvel_bits64;   // FP64 contexts: max |v + a h|^2 as the bits of a non-negative double
     unsigned phase_ok;  // fluid phases: bit k set when phase k met its tolerance in the running iteration
+    // Weiler2018 with fluid phases, one CG system per phase: iterations summed over the phases,
+    // the largest final residual of the phases before the running one, bit k: phase k had a zero
+    // right-hand side (solution 0)
+    unsigned iters_cg_tot, cg_zero;
+    double cg_err_max;
 };
 
 constexpr unsigned kFlagOverflow = 1u;
@@ -71,6 +76,7 @@ template <class T> struct DevParams {
     T gx, gy, gz;
     T xsph, xsph_b;
     T mu, mub, vd, h2;            // Weiler: mu = nu rho0, d = 10, h^2 (support)
+    T visc_nu, visc_nub;          // Weiler: nu and nu_b (fluid phases: mu = nu rho0 of the particle's phase)
     double max_error, max_error_v;
     double cfl_factor, cfl_min, cfl_max, radius;
     double visc_tol;
@@ -259,13 +265,17 @@ template <class T> void launch_jacobi(const DevParams<T> &P, const DevBufs<T> &B
                                       cudaGraphConditionalHandle h, bool use_handle, cudaStream_t s);
 template <class T> void launch_solver_finalize(const DevParams<T> &P, const DevBufs<T> &B, bool div, cudaStream_t s);
 template <class T> void launch_xsph(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
+// The Weiler2018 CG passes; phase >= 0 restricts them to that fluid phase's particles and
+// same-phase neighbours (P then carries the phase's mub and rho0), -1 runs one system over all.
 template <class T> void launch_visc_setup(const DevParams<T> &P, const DevBufs<T> &B,
-                                          cudaGraphConditionalHandle h, bool use_handle, cudaStream_t s);
+                                          cudaGraphConditionalHandle h, bool use_handle, cudaStream_t s,
+                                          int phase = -1);
 template <class T> void launch_cg_matvec(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s,
-                                         cudaGraphConditionalHandle h = 0, bool use_handle = false);
+                                         cudaGraphConditionalHandle h = 0, bool use_handle = false, int phase = -1);
 template <class T> void launch_cg_update(const DevParams<T> &P, const DevBufs<T> &B,
-                                         cudaGraphConditionalHandle h, bool use_handle, cudaStream_t s);
-template <class T> void launch_cg_p(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
+                                         cudaGraphConditionalHandle h, bool use_handle, cudaStream_t s,
+                                         int phase = -1);
+template <class T> void launch_cg_p(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s, int phase = -1);
 template <class T> void launch_kick(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
 template <class T> void launch_press_init(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);
 template <class T> void launch_integrate(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s);

@@ -3,9 +3,15 @@ reference's multiphase scenes use them): per-particle rest density and mass, the
 term kappa_i + (rho0_j / rho0_i) kappa_j, and solver iterations that visit the models in turn,
 each against its own tolerance (TimeStepDFSPH.cpp:322-339, 476-495).
 
-CPU: a heavy phase under a light one settles, each at its own rest density, in the oracle.
+Weiler2018 viscosity solves one system per phase over same-phase neighbours (the reference's
+viscosity is a per-model force, Viscosity_Weiler2018.cpp:288-289, 891-936).
+
+CPU: a heavy phase under a light one settles, each at its own rest density, in the oracle; two
+far-apart copies of one block as two phases of equal rest density step as one phase does, Weiler
+iterations doubled.
 GPU: one step from the same two-phase state meets the oracle at the standard bars (iteration
-counts equal), FP32 and FP64; unsupported combinations are refused."""
+counts equal), FP32 and FP64, with and without Weiler2018 viscosity; unsupported combinations are
+refused."""
 import numpy as np
 import pytest
 
@@ -18,10 +24,10 @@ from test_gpu_parity import compare, f32
 RHO = (1000.0, 500.0)
 
 
-def layered_scene(counts=(11, 8, 11), velocity=None):
+def layered_scene(counts=(11, 8, 11), velocity=None, viscosity=False):
     """a column whose lower half is phase 0 and upper half phase 1: particles ordered by height"""
     sc = scenes.small_block(counts=counts, box=(0.6, 0.8, 0.6), corner=(0.05, 0.05, 0.05),
-                            velocity=velocity).as_float32()
+                            velocity=velocity, viscosity=viscosity).as_float32()
     order = np.argsort(sc.x[:, 1], kind="stable")
     sc.x, sc.v = sc.x[order].copy(), sc.v[order].copy()
     n0 = sc.n // 2
@@ -44,8 +50,38 @@ def test_oracle_two_phase_column_settles_at_each_rest_density():
     assert np.median(sim.x[:counts[0], 1]) < np.median(sim.x[counts[0]:, 1])
 
 
-def two_phase_state(counts_xyz=(11, 8, 11), steps=40):
-    sc, counts = layered_scene(counts_xyz, velocity=(0.2, -0.3, 0.1))
+def test_oracle_weiler_far_apart_copies_step_as_one_phase():
+    """two copies of one block, farther apart than the support radius, without walls: as two phases
+    of equal rest density their Weiler systems are the one system's two halves (each reaches the
+    same iteration count, the sum is twice it), and the step agrees with the one-phase step up to
+    the summation order of the CG reductions"""
+    sc = scenes.small_block(counts=(6, 6, 6), viscosity=True).as_float32()
+    sc.params.viscosity = 0.05
+    rng = np.random.default_rng(3)
+    v0 = rng.normal(0.0, 0.3, sc.x.shape).astype(np.float32)
+    shift = np.array([0.0, 0.0, 1.0], np.float32)      # 1.0 >> support radius
+    sc.x = np.concatenate([sc.x, sc.x + shift]).astype(np.float32)
+    sc.v = np.concatenate([v0, v0]).astype(np.float32)
+    sc.xb = np.zeros((0, 3))
+    one = oracle.OracleSim(sc)
+    two = oracle.OracleSim(sc)
+    two.set_phases((sc.n // 2, sc.n // 2), (1000.0, 1000.0))
+    for _ in range(3):
+        one.step()
+        two.step()
+        s1, s2 = one.stats(), two.stats()
+        assert s1["visco_iterations"] > 0
+        assert s2["visco_iterations"] == 2 * s1["visco_iterations"]
+        assert (s2["iterations"], s2["iterations_v"]) == (s1["iterations"], s1["iterations_v"])
+    assert np.abs(two.x - one.x).max() < 1e-6
+    assert np.abs(two.v - one.v).max() < 1e-4
+
+
+def two_phase_state(counts_xyz=(11, 8, 11), steps=40, viscosity=False):
+    sc, counts = layered_scene(counts_xyz, velocity=(0.2, -0.3, 0.1), viscosity=viscosity)
+    if viscosity:
+        sc.params.viscosity = 0.05
+        sc.params.viscosityBoundary = 0.02
     pre = oracle.OracleSim(sc)
     pre.set_phases(counts, RHO)
     for _ in range(steps):
@@ -114,13 +150,6 @@ def test_phase_refusals():
     ts.ctx.set_fluid_phases((counts[0], counts[1] - 1), RHO)
     assert code(ts.step) == "STATE"                                   # counts do not cover the fluid
     assert code(lambda: ts.ctx.set_fluid_phases(counts, (1000.0, -1.0))) == "ARGUMENT"
-    p = sc.params
-    p.viscosityMethod = 6
-    ts.ctx.set_params(p)
-    ts.ctx.set_fluid_phases(counts, RHO)
-    assert code(ts.step) == "ARGUMENT"                                # Weiler2018 per fluid model
-    p.viscosityMethod = 0
-    ts.ctx.set_params(p)
     ts.ctx.set_fluid_phases()                                         # back to one phase
     ts.step()
     ts.close()
@@ -155,3 +184,56 @@ def test_two_phase_step_in_a_volume_mapped_box_matches_oracle():
     sim.step()
     compare(ts, sim, st, tol_scale=1e-4)
     ts.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol_scale", [("fp32", 15.0), ("fp64", 1e-4)])
+def test_two_phase_weiler_step_matches_oracle(precision, tol_scale):
+    """Weiler2018 with boundary viscosity on the layered column, one system per phase over
+    same-phase neighbours: pressure and viscosity iteration counts equal (the viscosity's the
+    phases' sum).  FP64 at the tight bars (velocity measured 2.3e-12 of the speed); FP32 at 15x
+    the standard bars: the velocity of a slow particle differs by 1.5e-3 of its speed (2.6e-6
+    absolute, the relative bar's floor is 1e-3) while the viscous velocity change agrees to
+    1.7e-5, the rounding of an FP32 CG that the FP64 run shows is not a difference of terms"""
+    sc, counts, state = two_phase_state(viscosity=True)
+    ts = TimeStepDFSPH(sc, precision=precision)
+    ts.ctx.set_fluid_phases(counts, RHO)
+    m = ts.getFluidModel()
+    m.setFieldBuffer("position", state["x"])
+    m.setFieldBuffer("velocity", state["v"])
+    m.setFieldBuffer("p / rho^2", state["kappa"])
+    m.setFieldBuffer("p_v / rho^2", state["kappa_v"])
+    ts.setTimeStepSize(state["dt"])
+    sim = oracle.OracleSim(sc)
+    sim.set_phases(counts, RHO)
+    sim.x[:] = state["x"]
+    sim.v[:] = state["v"]
+    sim.kappa[:] = state["kappa"]
+    sim.kappa_v[:] = state["kappa_v"]
+    sim.dt = state["dt"]
+    st = ts.step()
+    sim.step()
+    so = sim.stats()
+    assert so["visco_iterations"] > 0
+    assert st["visco_iterations"] == so["visco_iterations"]
+    assert st["visco_error"] == pytest.approx(so["visco_error"], rel=1e-2 if precision == "fp32" else 1e-6)
+    compare(ts, sim, st, tol_scale=tol_scale)
+    ts.close()
+
+
+@pytest.mark.gpu
+def test_two_phase_weiler_graph_and_host_loops_agree():
+    """the captured step (one conditional CG loop per phase) and the host-driven loops give the
+    same bits over several steps (FP64)"""
+    out = []
+    for graph in (True, False):
+        sc, counts = layered_scene(velocity=(0.2, -0.3, 0.1), viscosity=True)
+        sc.params.viscosity = 0.05
+        ts = TimeStepDFSPH(sc, precision="fp64", use_graph=graph)
+        ts.ctx.set_lanes_per_particle(1)   # the same summation order in both runs
+        ts.ctx.set_fluid_phases(counts, RHO)
+        its = [ts.step()["visco_iterations"] for _ in range(4)]
+        out.append((its, ts.getFluidModel().getFieldBuffer("position").copy()))
+        ts.close()
+    assert out[0][0] == out[1][0]
+    assert np.array_equal(out[0][1], out[1][1])
