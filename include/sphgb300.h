@@ -368,6 +368,14 @@ int sphgb_set_boundary_bodies(sphgb_ctx *ctx, const uint32_t *body, uint32_t nbo
  * phase of sphgb_params.density0.  At the step: SPHGB_ERR_STATE when the counts do not add up to
  * the fluid or for a batch; SPHGB_ERR_ARGUMENT with the learned warm start.  Up to 8 phases. */
 int sphgb_set_fluid_phases(sphgb_ctx *ctx, uint32_t nphases, const uint32_t *counts, const double *density0);
+
+/* Weiler2018 coefficients per fluid phase, as each FluidModel of the reference carries its own
+ * viscosity and viscosityBoundary (Viscosity_Weiler2018.cpp:288-289): phase k's system takes mu =
+ * viscosity[k] density0[k] and mub = viscosity_boundary[k] density0[k].  Phases beyond nphases
+ * (and every phase after nphases = 0) take sphgb_params.viscosity / viscosity_boundary.
+ * SPHGB_ERR_ARGUMENT for a negative or non-finite value or more than 8 phases. */
+int sphgb_set_fluid_phase_viscosity(sphgb_ctx *ctx, uint32_t nphases, const double *viscosity,
+                                    const double *viscosity_boundary);
 int sphgb_set_body_motion(sphgb_ctx *ctx, uint32_t body, const double rotation[9], const double translation[3],
                           const double velocity[3], const double omega[3]);
 /* the sums since the last clear, force[3 nbodies] and torque[3 nbodies] (either may be NULL;

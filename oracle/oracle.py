@@ -107,6 +107,8 @@ class OrcState(ctypes.Structure):
         ("nphase", ctypes.c_uint),
         ("phase_count", ctypes.c_void_p),
         ("phase_density0", ctypes.c_void_p),
+        ("phase_viscosity", ctypes.c_void_p),
+        ("phase_viscosity_boundary", ctypes.c_void_p),
     ]
 
 
@@ -349,6 +351,13 @@ class OracleSim:
         self.st.nphase = len(self._phase_count)
         self.st.phase_count = _ptr(self._phase_count)
         self.st.phase_density0 = _ptr(self._phase_density0)
+
+    def set_phase_viscosity(self, viscosity, viscosity_boundary):
+        """Weiler2018 nu and nu_b of each fluid model"""
+        self._phase_nu = np.ascontiguousarray(viscosity, np.float64)
+        self._phase_nub = np.ascontiguousarray(viscosity_boundary, np.float64)
+        self.st.phase_viscosity = _ptr(self._phase_nu)
+        self.st.phase_viscosity_boundary = _ptr(self._phase_nub)
 
     def set_boundary_state(self, xb, vb):
         """positions and velocities of the boundary particles for the next steps (moving

@@ -788,14 +788,24 @@ typedef struct {
     int ph;
 } visc_t;
 
+/* nu and nu_b of phase ph (-1: the one model) */
+static double phase_nu(const ctx_t *c, int ph)
+{
+    return (ph >= 0 && c->s->phase_viscosity) ? c->s->phase_viscosity[ph] : c->p->viscosity;
+}
+static double phase_nub(const ctx_t *c, int ph)
+{
+    return (ph >= 0 && c->s->phase_viscosity_boundary) ? c->s->phase_viscosity_boundary[ph] : c->p->viscosity_boundary;
+}
+
 static visc_t visc_make(ctx_t *c, double dt, int ph, long lo, long hi)
 {
     visc_t w;
     w.c = c;
     w.dt = dt;
     w.rho0 = ph >= 0 ? c->s->phase_density0[ph] : c->rho0;
-    w.mu = c->p->viscosity * w.rho0;             /* :288 */
-    w.mub = c->p->viscosity_boundary * w.rho0;   /* :289 */
+    w.mu = phase_nu(c, ph) * w.rho0;             /* :288 */
+    w.mub = phase_nub(c, ph) * w.rho0;           /* :289 */
     w.h2 = c->K.h * c->K.h;
     w.d = 10.0;                                  /* 3D, :292-294 */
     w.lo = lo;
@@ -1098,11 +1108,13 @@ static int viscosity_weiler(ctx_t *c, double dt)
     /* boundary feedback of applyForces (Viscosity_Weiler2018.cpp:960-975), static v_b = 0:
      * a = d mub (rho0 V_b / rho_i) (v_i'.x_ib) / (|x_ib|^2 + 0.01 h^2) gradW_ib, force -m_i / rho_i a,
      * rho0, mub and m_i those of the particle's model */
-    if (c->p->viscosity_boundary != 0.0 && collects_forces(s, c->p->boundary_method == 2)) {
+    int any_mub = 0;
+    for (int ph = 0; ph < nph; ph++) any_mub |= phase_nub(c, c->r0 ? ph : -1) != 0.0;
+    if (any_mub && collects_forces(s, c->p->boundary_method == 2)) {
         const double h2 = c->K.h * c->K.h;
         for (long i = 0; i < (long)s->n; i++) {
             const double rhoi = (double)s->density[i];
-            const double r0 = rho0_of(c, i), mub = c->p->viscosity_boundary * r0, mi = mass_of(c, i);
+            const double r0 = rho0_of(c, i), mub = phase_nub(c, c->r0 ? c->ph[i] : -1) * r0, mi = mass_of(c, i);
             const double nv[3] = {(double)x[3 * i], (double)x[3 * i + 1], (double)x[3 * i + 2]};
             for (unsigned k = c->B.off[i]; k < c->B.off[i + 1]; k++) {
                 const unsigned j = c->B.idx[k];

@@ -118,6 +118,9 @@ typedef struct orc_state {
     unsigned nphase;
     const unsigned *phase_count;
     const double *phase_density0;
+    /* Weiler2018 nu and nu_b per phase (each FluidModel's own, Viscosity_Weiler2018.cpp:288-289);
+     * NULL: the parameters' viscosity / viscosity_boundary for every phase */
+    const double *phase_viscosity, *phase_viscosity_boundary;
 } orc_state;
 
 /* Cubic spline (SPHKernels.h:16-91). */

@@ -131,6 +131,7 @@ struct sphgb_ctx {
     // fluid phases (sphgb_set_fluid_phases): particles in id order, count and rest density per phase
     std::vector<uint32_t> phase_counts;
     std::vector<double> phase_rho0;
+    std::vector<double> phase_nu, phase_nub;   // Weiler per phase; empty or short: the shared parameters
     void *r0 = nullptr;                // prepared set: rest density per slot
     uint32_t *ph = nullptr;            // prepared set: phase per slot
     // moving boundary bodies (sphgb_set_body_motion): particles placed and re-sorted every step
@@ -387,6 +388,13 @@ template <class T> SceneDev<T> scene_dev(const sphgb_ctx *c, uint32_t s)
     return S;
 }
 
+// Weiler2018 coefficients of fluid phase k: sphgb_set_fluid_phase_viscosity's, else the shared ones
+double phase_nu(const sphgb_ctx *c, uint32_t k) { return k < c->phase_nu.size() ? c->phase_nu[k] : c->prm.viscosity; }
+double phase_nub(const sphgb_ctx *c, uint32_t k)
+{
+    return k < c->phase_nub.size() ? c->phase_nub[k] : c->prm.viscosity_boundary;
+}
+
 template <class T> DevParams<T> make_params(const sphgb_ctx *c)
 {
     DevParams<T> P{};
@@ -412,8 +420,6 @@ template <class T> DevParams<T> make_params(const sphgb_ctx *c)
     P.xsph_b = (T)q.xsph_boundary;
     P.mu = (T)(q.viscosity * q.density0);
     P.mub = (T)(q.viscosity_boundary * q.density0);
-    P.visc_nu = (T)q.viscosity;
-    P.visc_nub = (T)q.viscosity_boundary;
     P.vd = (T)10.0;
     P.h2 = (T)(h * h);
     P.max_error = q.max_error;
@@ -462,6 +468,10 @@ template <class T> DevParams<T> make_params(const sphgb_ctx *c)
             end += P.phase_count[k];
             P.phase_end[k] = end;
             P.phase_rho0[k] = has ? (T)c->phase_rho0[k] : P.rho0;
+            P.phase_nu[k] = (T)phase_nu(c, k);
+            P.phase_nub[k] = (T)phase_nub(c, k);
+            // the boundary-viscosity switch of the whole step: any phase's mu_b
+            if (has && P.mub == T(0)) P.mub = (T)(phase_nub(c, k) * c->phase_rho0[k]);
         }
         P.staged = 0;   // the staged passes read one rest density
     }
@@ -843,7 +853,7 @@ template <class T> DevParams<T> visc_system_params(const sphgb_ctx *c, const Dev
     phase = P.nphase > 1 ? k : -1;
     if (phase < 0) return P;
     DevParams<T> Q = P;
-    Q.mub = (T)(c->prm.viscosity_boundary * c->phase_rho0[k]);
+    Q.mub = (T)(phase_nub(c, k) * c->phase_rho0[k]);
     Q.rho0 = (T)c->phase_rho0[k];
     return Q;
 }
@@ -2260,6 +2270,24 @@ int sphgb_clear_volume_maps(sphgb_ctx *c)
     CK(cudaStreamSynchronize(c->stream));
     free_vmaps(c);
     c->prepared = false;
+    invalidate_graphs(c);
+    return SPHGB_OK;
+}
+
+int sphgb_set_fluid_phase_viscosity(sphgb_ctx *c, uint32_t nphases, const double *viscosity,
+                                    const double *viscosity_boundary)
+{
+    if (!c || nphases > 8 || (nphases > 0 && (!viscosity || !viscosity_boundary))) return SPHGB_ERR_ARGUMENT;
+    for (uint32_t k = 0; k < nphases; k++)
+        if (!(std::isfinite(viscosity[k]) && viscosity[k] >= 0.0 && std::isfinite(viscosity_boundary[k]) &&
+              viscosity_boundary[k] >= 0.0))
+            return fail(c, SPHGB_ERR_ARGUMENT, "a phase's viscosity must be finite and non-negative");
+    if (c->step_pending) {
+        sphgb_stats st;
+        fill_stats(c, &st);
+    }
+    c->phase_nu.assign(viscosity, viscosity + nphases);
+    c->phase_nub.assign(viscosity_boundary, viscosity_boundary + nphases);
     invalidate_graphs(c);
     return SPHGB_OK;
 }

@@ -204,6 +204,18 @@ template <class T> __device__ __forceinline__ T rho0_at(const DevParams<T> &P, c
 {
     return P.nphase > 1 ? B.r0[i] : P.rho0;
 }
+// Weiler2018 coefficients nu, nu_b of phase k, without dynamic indexing of the parameter arrays
+template <class T> __device__ __forceinline__ void phase_visc(const DevParams<T> &P, uint32_t k, T &nu, T &nub)
+{
+    nu = P.phase_nu[0];
+    nub = P.phase_nub[0];
+#pragma unroll
+    for (uint32_t q = 1; q < 8; q++)
+        if (q == k) {
+            nu = P.phase_nu[q];
+            nub = P.phase_nub[q];
+        }
+}
 // particles of phase k (counted, rest density) without dynamic indexing of the parameter arrays
 template <class T> __device__ __forceinline__ void phase_info(const DevParams<T> &P, int k, uint32_t &count, T &rho0)
 {
@@ -1273,7 +1285,9 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams<T> P, DevBufs<T> B, i
         T wi;
         if (P.nphase > 1) {
             const T r0 = B.r0[i];
-            wi = P.vd * (P.visc_nu * r0) * (P.V * r0) / B.density[i];
+            T nu, nub;
+            phase_visc(P, B.ph[i], nu, nub);
+            wi = P.vd * (nu * r0) * (P.V * r0) / B.density[i];
         } else {
             wi = P.vd * P.mu * P.mass / B.density[i];
         }
@@ -1888,7 +1902,12 @@ __global__ void __launch_bounds__(kBlock) k_body_forces(DevParams<T> P, DevBufs<
                                 V3<T> nv = xyz<T>(ldv(B.cg_x, i));
                                 if (P.bmove) nv = sub(nv, vbj);
                                 // fluid phases: mub = nu_b rho0 and rho0 of the particle's phase
-                                const T vc = P.nphase > 1 ? P.vd * (P.visc_nub * B.r0[i]) * B.r0[i] * Vb : vi_c;
+                                T vc = vi_c;
+                                if (P.nphase > 1) {
+                                    T nu, nub;
+                                    phase_visc(P, B.ph[i], nu, nub);
+                                    vc = P.vd * (nub * B.r0[i]) * B.r0[i] * Vb;
+                                }
                                 const T a = vc / rhoi * dot(nv, r) / (d2 + eps2) * gc;
                                 fi = sub(fi, scl(r, mi / rhoi * a));
                             }
@@ -1970,7 +1989,12 @@ __global__ void __launch_bounds__(kBlock) k_vmap_forces(DevParams<T> P, DevBufs<
                 if (PHASE == 0 && P.visc_on && P.mub != T(0) && !zero) {
                     const V3<T> nv = xyz<T>(ldv(B.cg_x, i));
                     const T rhoi = B.density[i], vol = T(0.25) * Vj, eps2 = T(0.01) * P.h2;
-                    const T mub = P.nphase > 1 ? P.visc_nub * B.r0[i] : P.mub;   // the particle's phase
+                    T mub = P.mub;
+                    if (P.nphase > 1) {   // the particle's phase
+                        T nu, nub;
+                        phase_visc(P, B.ph[i], nu, nub);
+                        mub = nub * B.r0[i];
+                    }
                     vmap_samples<T>(xk, xj, P.K.h, [&](const V3<T> &xs4) {
                         const V3<T> r4 = sub(xyz<T>(xk), xs4);
                         const T r2 = dot(r4, r4);

@@ -76,7 +76,6 @@ template <class T> struct DevParams {
     T gx, gy, gz;
     T xsph, xsph_b;
     T mu, mub, vd, h2;            // Weiler: mu = nu rho0, d = 10, h^2 (support)
-    T visc_nu, visc_nub;          // Weiler: nu and nu_b (fluid phases: mu = nu rho0 of the particle's phase)
     double max_error, max_error_v;
     double cfl_factor, cfl_min, cfl_max, radius;
     double visc_tol;
@@ -106,6 +105,7 @@ template <class T> struct DevParams {
     uint32_t nphase;
     uint32_t phase_end[8], phase_count[8];
     T phase_rho0[8];
+    T phase_nu[8], phase_nub[8];  // Weiler per phase: nu and nu_b (mu = nu rho0 of the particle's phase)
     int bmove;                    // boundary particles move with their bodies: placed and re-sorted every
                                   // step, with velocities (one scene)
     int staged;                   // FP32, one lane per particle: the solver passes read their block's

@@ -237,3 +237,53 @@ def test_two_phase_weiler_graph_and_host_loops_agree():
         ts.close()
     assert out[0][0] == out[1][0]
     assert np.array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol_scale", [("fp32", 15.0), ("fp64", 1e-4)])
+def test_two_phase_weiler_with_own_coefficients_matches_oracle(precision, tol_scale):
+    """each model with its own Weiler2018 nu and nu_b (a viscous heavy phase with boundary viscosity
+    under a thin light one without): iteration counts equal, fields at the bars of the shared case"""
+    sc, counts, state = two_phase_state(viscosity=True)
+    nu, nub = (0.08, 0.005), (0.03, 0.0)
+    ts = TimeStepDFSPH(sc, precision=precision)
+    ts.ctx.set_fluid_phases(counts, RHO)
+    ts.ctx.set_fluid_phase_viscosity(nu, nub)
+    m = ts.getFluidModel()
+    m.setFieldBuffer("position", state["x"])
+    m.setFieldBuffer("velocity", state["v"])
+    m.setFieldBuffer("p / rho^2", state["kappa"])
+    m.setFieldBuffer("p_v / rho^2", state["kappa_v"])
+    ts.setTimeStepSize(state["dt"])
+    sim = oracle.OracleSim(sc)
+    sim.set_phases(counts, RHO)
+    sim.set_phase_viscosity(nu, nub)
+    sim.x[:] = state["x"]
+    sim.v[:] = state["v"]
+    sim.kappa[:] = state["kappa"]
+    sim.kappa_v[:] = state["kappa_v"]
+    sim.dt = state["dt"]
+    st = ts.step()
+    sim.step()
+    so = sim.stats()
+    assert st["visco_iterations"] == so["visco_iterations"] > 0
+    compare(ts, sim, st, tol_scale=tol_scale)
+    with pytest.raises(native.SphgbError):
+        ts.ctx.set_fluid_phase_viscosity((0.01, -1.0), (0.0, 0.0))
+    ts.close()
+
+
+def test_oracle_phase_viscosity_defaults_to_the_shared_coefficients():
+    """per-model coefficients equal to the shared ones give the shared run's bits"""
+    sc, counts = layered_scene((6, 6, 6), velocity=(0.2, -0.3, 0.1), viscosity=True)
+    sc.params.viscosity = 0.05
+    sc.params.viscosityBoundary = 0.02
+    a, b = oracle.OracleSim(sc), oracle.OracleSim(sc)
+    for sim in (a, b):
+        sim.set_phases(counts, RHO)
+    b.set_phase_viscosity((0.05, 0.05), (0.02, 0.02))
+    for _ in range(3):
+        a.step()
+        b.step()
+    assert a.stats()["visco_iterations"] > 0
+    assert np.array_equal(a.x, b.x) and np.array_equal(a.v, b.v)
