@@ -376,6 +376,12 @@ int sphgb_set_fluid_phases(sphgb_ctx *ctx, uint32_t nphases, const uint32_t *cou
  * SPHGB_ERR_ARGUMENT for a negative or non-finite value or more than 8 phases. */
 int sphgb_set_fluid_phase_viscosity(sphgb_ctx *ctx, uint32_t nphases, const double *viscosity,
                                     const double *viscosity_boundary);
+
+/* XSPH coefficients per fluid phase, as each FluidModel's XSPH carries its own xsph and
+ * xsphBoundary (XSPH.cpp:19-39): a particle's filter takes its phase's coefficients, over the
+ * neighbours of every phase.  Phases beyond nphases take sphgb_params.xsph / xsph_boundary.
+ * SPHGB_ERR_ARGUMENT for a non-finite value or more than 8 phases. */
+int sphgb_set_fluid_phase_xsph(sphgb_ctx *ctx, uint32_t nphases, const double *xsph, const double *xsph_boundary);
 int sphgb_set_body_motion(sphgb_ctx *ctx, uint32_t body, const double rotation[9], const double translation[3],
                           const double velocity[3], const double omega[3]);
 /* the sums since the last clear, force[3 nbodies] and torque[3 nbodies] (either may be NULL;

@@ -109,6 +109,8 @@ class OrcState(ctypes.Structure):
         ("phase_density0", ctypes.c_void_p),
         ("phase_viscosity", ctypes.c_void_p),
         ("phase_viscosity_boundary", ctypes.c_void_p),
+        ("phase_xsph", ctypes.c_void_p),
+        ("phase_xsph_boundary", ctypes.c_void_p),
     ]
 
 
@@ -358,6 +360,13 @@ class OracleSim:
         self._phase_nub = np.ascontiguousarray(viscosity_boundary, np.float64)
         self.st.phase_viscosity = _ptr(self._phase_nu)
         self.st.phase_viscosity_boundary = _ptr(self._phase_nub)
+
+    def set_phase_xsph(self, xsph, xsph_boundary):
+        """XSPH fluid and boundary coefficients of each fluid model"""
+        self._phase_xs = np.ascontiguousarray(xsph, np.float64)
+        self._phase_xsb = np.ascontiguousarray(xsph_boundary, np.float64)
+        self.st.phase_xsph = _ptr(self._phase_xs)
+        self.st.phase_xsph_boundary = _ptr(self._phase_xsb)
 
     def set_boundary_state(self, xb, vb):
         """positions and velocities of the boundary particles for the next steps (moving

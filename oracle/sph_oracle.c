@@ -726,14 +726,26 @@ static void pressure_solve(ctx_t *c, double h, double *err_buf)
 }
 
 /* XSPH::step, scalar path (XSPH.cpp:138-211); static boundary => v_b = 0. */
+/* XSPH coefficients of particle i's model (each FluidModel's XSPH has its own, XSPH.cpp:19-39) */
+static double xsph_cf(const ctx_t *c, long i)
+{
+    return (c->r0 && c->s->phase_xsph) ? c->s->phase_xsph[c->ph[i]] : c->p->xsph_fluid;
+}
+static double xsph_cb(const ctx_t *c, long i)
+{
+    return (c->r0 && c->s->phase_xsph_boundary) ? c->s->phase_xsph_boundary[c->ph[i]] : c->p->xsph_boundary;
+}
+
 static void xsph(ctx_t *c, double h)
 {
     orc_state *s = c->s;
     const double invH = 1.0 / h;
-    const double cf = c->p->xsph_fluid, cb = c->p->xsph_boundary;
+    int any_cb = 0;
+    for (long i = 0; i < (long)s->n; i++) any_cb |= xsph_cb(c, i) != 0.0;
 #pragma omp parallel for schedule(static)
     for (long i = 0; i < (long)s->n; i++) {
         const real *xi = s->x + 3 * i, *vi = s->v + 3 * i;
+        const double cf = xsph_cf(c, i), cb = xsph_cb(c, i);
         double ai[3] = {0, 0, 0};
         for (unsigned k = c->F.off[i]; k < c->F.off[i + 1]; k++) {
             const unsigned j = c->F.idx[k];
@@ -758,10 +770,10 @@ static void xsph(ctx_t *c, double h)
         for (int d = 0; d < 3; d++) s->a[3 * i + d] = (real)((double)s->a[3 * i + d] + ai[d]);
     }
     /* boundary feedback of the XSPH boundary term (XSPH.cpp:183-203): force -m_i a_ib */
-    if (cb != 0.0 && collects_forces(s, c->p->boundary_method == 2))
+    if (any_cb && collects_forces(s, c->p->boundary_method == 2))
         for (long i = 0; i < (long)s->n; i++) {
             const real *xi = s->x + 3 * i, *vi = s->v + 3 * i;
-            const double rhoi = (double)s->density[i];
+            const double rhoi = (double)s->density[i], cb = xsph_cb(c, i);
             for (unsigned k = c->B.off[i]; k < c->B.off[i + 1]; k++) {
                 const unsigned j = c->B.idx[k];
                 double r[3], f[3];
@@ -1351,7 +1363,8 @@ int orc_step(orc_state *s, const orc_params *p)
     s->visco_iterations = 0;
     s->visco_error = 0.0;
     if (p->viscosity_method == 6) rc = viscosity_weiler(&c, h);
-    if (p->xsph_fluid != 0.0 || p->xsph_boundary != 0.0) xsph(&c, h);
+    if (p->xsph_fluid != 0.0 || p->xsph_boundary != 0.0 || (c.r0 && (s->phase_xsph || s->phase_xsph_boundary)))
+        xsph(&c, h);
 
     const double hnew = update_time_step(&c, h);
 

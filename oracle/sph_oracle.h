@@ -121,6 +121,9 @@ typedef struct orc_state {
     /* Weiler2018 nu and nu_b per phase (each FluidModel's own, Viscosity_Weiler2018.cpp:288-289);
      * NULL: the parameters' viscosity / viscosity_boundary for every phase */
     const double *phase_viscosity, *phase_viscosity_boundary;
+    /* XSPH fluid and boundary coefficients per phase (each FluidModel's own, XSPH.cpp:19-39);
+     * NULL: the parameters' xsph_fluid / xsph_boundary for every phase */
+    const double *phase_xsph, *phase_xsph_boundary;
 } orc_state;
 
 /* Cubic spline (SPHKernels.h:16-91). */

@@ -132,6 +132,7 @@ struct sphgb_ctx {
     std::vector<uint32_t> phase_counts;
     std::vector<double> phase_rho0;
     std::vector<double> phase_nu, phase_nub;   // Weiler per phase; empty or short: the shared parameters
+    std::vector<double> phase_xs, phase_xsb;   // XSPH per phase; likewise
     void *r0 = nullptr;                // prepared set: rest density per slot
     uint32_t *ph = nullptr;            // prepared set: phase per slot
     // moving boundary bodies (sphgb_set_body_motion): particles placed and re-sorted every step
@@ -470,6 +471,11 @@ template <class T> DevParams<T> make_params(const sphgb_ctx *c)
             P.phase_rho0[k] = has ? (T)c->phase_rho0[k] : P.rho0;
             P.phase_nu[k] = (T)phase_nu(c, k);
             P.phase_nub[k] = (T)phase_nub(c, k);
+            P.phase_xs[k] = (T)(k < c->phase_xs.size() ? c->phase_xs[k] : q.xsph);
+            P.phase_xsb[k] = (T)(k < c->phase_xsb.size() ? c->phase_xsb[k] : q.xsph_boundary);
+            // the XSPH switches of the whole step: any phase's coefficient
+            if (has && P.xsph == T(0)) P.xsph = P.phase_xs[k];
+            if (has && P.xsph_b == T(0)) P.xsph_b = P.phase_xsb[k];
             // the boundary-viscosity switch of the whole step: any phase's mu_b
             if (has && P.mub == T(0)) P.mub = (T)(phase_nub(c, k) * c->phase_rho0[k]);
         }
@@ -2288,6 +2294,22 @@ int sphgb_set_fluid_phase_viscosity(sphgb_ctx *c, uint32_t nphases, const double
     }
     c->phase_nu.assign(viscosity, viscosity + nphases);
     c->phase_nub.assign(viscosity_boundary, viscosity_boundary + nphases);
+    invalidate_graphs(c);
+    return SPHGB_OK;
+}
+
+int sphgb_set_fluid_phase_xsph(sphgb_ctx *c, uint32_t nphases, const double *xsph, const double *xsph_boundary)
+{
+    if (!c || nphases > 8 || (nphases > 0 && (!xsph || !xsph_boundary))) return SPHGB_ERR_ARGUMENT;
+    for (uint32_t k = 0; k < nphases; k++)
+        if (!(std::isfinite(xsph[k]) && std::isfinite(xsph_boundary[k])))
+            return fail(c, SPHGB_ERR_ARGUMENT, "a phase's XSPH coefficient must be finite");
+    if (c->step_pending) {
+        sphgb_stats st;
+        fill_stats(c, &st);
+    }
+    c->phase_xs.assign(xsph, xsph + nphases);
+    c->phase_xsb.assign(xsph_boundary, xsph_boundary + nphases);
     invalidate_graphs(c);
     return SPHGB_OK;
 }

@@ -216,6 +216,18 @@ template <class T> __device__ __forceinline__ void phase_visc(const DevParams<T>
             nub = P.phase_nub[q];
         }
 }
+// XSPH coefficients of phase k (fluid, boundary)
+template <class T> __device__ __forceinline__ void phase_xsph(const DevParams<T> &P, uint32_t k, T &xs, T &xsb)
+{
+    xs = P.phase_xs[0];
+    xsb = P.phase_xsb[0];
+#pragma unroll
+    for (uint32_t q = 1; q < 8; q++)
+        if (q == k) {
+            xs = P.phase_xs[q];
+            xsb = P.phase_xsb[q];
+        }
+}
 // particles of phase k (counted, rest density) without dynamic indexing of the parameter arrays
 template <class T> __device__ __forceinline__ void phase_info(const DevParams<T> &P, int k, uint32_t &count, T &rho0)
 {
@@ -1242,7 +1254,9 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams<T> P, DevBufs<T> B, i
     count_launch(&B.gsc->launches);
     const SlotInfo q = slot_info<LPP>(P);
     V3<T> acc = mk3<T>(0, 0, 0);
-    if (q.act && P.xsph != T(0)) {
+    T xs = P.xsph, xsb = P.xsph_b;   // fluid phases: the particle's model's coefficients
+    if (P.nphase > 1 && q.act) phase_xsph(P, B.ph[q.i], xs, xsb);
+    if (q.act && xs != T(0)) {
         const v4_t<T> xi = ldv(B.x, q.i);
         const V3<T> vi = xyz<T>(ldv(B.v, q.i));
         struct XVR {
@@ -1264,16 +1278,16 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams<T> P, DevBufs<T> B, i
     const T invH = T(1) / h;
     const V3<T> vi = xyz<T>(ldv(B.v, i));
     V3<T> ai = mk3<T>(P.gx, P.gy, P.gz);
-    if (P.xsph != T(0)) ai = sub(ai, scl(acc, invH * P.xsph));
-    if (P.xsph_b != T(0)) {
+    if (xs != T(0)) ai = sub(ai, scl(acc, invH * xs));
+    if (xsb != T(0)) {
         // sum_b (rho0 V_b / rho_i) W_ib from the per-step boundary sum
         const T r0i = rho0_at(P, B, i);
         const T wsum = r0i * (T)ldv(B.bg, i).w / B.density[i];
         if (P.vmove || P.bmove) {   // moving boundaries: (v_i - v_b) W
             const V3<T> dv = sub(scl(vi, (T)ldv(B.bg, i).w), xyz<T>(ldv(B.bv, i)));
-            ai = sub(ai, scl(dv, invH * P.xsph_b * r0i / B.density[i]));
+            ai = sub(ai, scl(dv, invH * xsb * r0i / B.density[i]));
         } else {
-            ai = sub(ai, scl(vi, invH * P.xsph_b * wsum));
+            ai = sub(ai, scl(vi, invH * xsb * wsum));
         }
     }
     stv(B.a, i, pack(ai, T(0)));
@@ -1892,7 +1906,12 @@ __global__ void __launch_bounds__(kBlock) k_body_forces(DevParams<T> P, DevBufs<
                         if (xs || visc) {
                             const T rhoi = B.density[i];
                             if (xs) {
-                                const T xsc = P.nphase > 1 ? xs_c * (B.r0[i] / P.rho0) : xs_c;
+                                T xsc = xs_c;
+                                if (P.nphase > 1) {   // the particle's model's coefficient and rest density
+                                    T xf, xb;
+                                    phase_xsph(P, B.ph[i], xf, xb);
+                                    xsc = xb / (T)sc->dt * B.r0[i] * Vb;
+                                }
                                 const T w = mi * xsc / rhoi * kernel_W(P.K, dev_sqrt(d2));
                                 V3<T> dv = xyz<T>(ldv(B.v, i));
                                 if (P.bmove) dv = sub(dv, vbj);
@@ -1969,7 +1988,12 @@ __global__ void __launch_bounds__(kBlock) k_vmap_forces(DevParams<T> P, DevBufs<
                 if (press && fabs(kap) > P.eps) f = scl(r, mi * kap * Vj * grad_coef_d2(P.K, d2));
                 const VMapDev<T> &mp = P.vmaps[mr.x + b];
                 if (xs) {
-                    const T w = mi * P.xsph_b / (T)B.sc[q.s].dt * rho0_at(P, B, i) * Vj / B.density[i] *
+                    T xsb = P.xsph_b;
+                    if (P.nphase > 1) {   // the particle's model's coefficient
+                        T xf;
+                        phase_xsph(P, B.ph[i], xf, xsb);
+                    }
+                    const T w = mi * xsb / (T)B.sc[q.s].dt * rho0_at(P, B, i) * Vj / B.density[i] *
                                 kernel_W(P.K, dev_sqrt(d2));
                     V3<T> dv = xyz<T>(ldv(B.v, i));
                     if (P.vmove) dv = sub(dv, vmap_point_velocity<T>(mp, xyz<T>(xj)));

@@ -106,6 +106,7 @@ template <class T> struct DevParams {
     uint32_t phase_end[8], phase_count[8];
     T phase_rho0[8];
     T phase_nu[8], phase_nub[8];  // Weiler per phase: nu and nu_b (mu = nu rho0 of the particle's phase)
+    T phase_xs[8], phase_xsb[8];  // XSPH per phase: fluid and boundary coefficients
     int bmove;                    // boundary particles move with their bodies: placed and re-sorted every
                                   // step, with velocities (one scene)
     int staged;                   // FP32, one lane per particle: the solver passes read their block's

@@ -127,7 +127,7 @@ EXPORTS = [
     "sphgb_set_neighbor_staging", "sphgb_get_neighbor_staging",
     "sphgb_add_volume_map", "sphgb_add_volume_map_values", "sphgb_get_volume_map", "sphgb_clear_volume_maps",
     "sphgb_set_boundary_method", "sphgb_set_volume_map_motion", "sphgb_set_body_motion", "sphgb_set_fluid_phases",
-    "sphgb_set_fluid_phase_viscosity",
+    "sphgb_set_fluid_phase_viscosity", "sphgb_set_fluid_phase_xsph",
     "sphgb_set_volume_map_scene",
 ]
 
@@ -198,6 +198,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.sphgb_set_body_motion.argtypes = [vp, u32, vp, vp, vp, vp]
     L.sphgb_set_fluid_phases.argtypes = [vp, u32, vp, vp]
     L.sphgb_set_fluid_phase_viscosity.argtypes = [vp, u32, vp, vp]
+    L.sphgb_set_fluid_phase_xsph.argtypes = [vp, u32, vp, vp]
     L.sphgb_set_volume_map_scene.argtypes = [vp, u32, u32]
     L.sphgb_get_neighbor_staging.argtypes = [vp, ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_float),
                                              ctypes.POINTER(ctypes.c_float)]
@@ -595,6 +596,16 @@ class Context:
             raise ValueError("one boundary viscosity per phase")
         self._check(self.L.sphgb_set_fluid_phase_viscosity(self.h, a.size, _p(a) if a.size else None,
                                                            _p(b) if b.size else None))
+
+    def set_fluid_phase_xsph(self, xsph=(), xsph_boundary=()):
+        """XSPH fluid and boundary coefficients per fluid phase (each model's own); () returns to
+        the shared parameters."""
+        a = np.ascontiguousarray(xsph, np.float64)
+        b = np.ascontiguousarray(xsph_boundary, np.float64)
+        if a.size != b.size:
+            raise ValueError("one boundary coefficient per phase")
+        self._check(self.L.sphgb_set_fluid_phase_xsph(self.h, a.size, _p(a) if a.size else None,
+                                                      _p(b) if b.size else None))
 
     def set_body_motion(self, body: int, rotation=None, translation=None, velocity=None, omega=None):
         """Pose and velocity of boundary body `body` (its particles uploaded in body coordinates) for

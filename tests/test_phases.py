@@ -287,3 +287,51 @@ def test_oracle_phase_viscosity_defaults_to_the_shared_coefficients():
         b.step()
     assert a.stats()["visco_iterations"] > 0
     assert np.array_equal(a.x, b.x) and np.array_equal(a.v, b.v)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol_scale", [("fp32", 2.0), ("fp64", 1e-4)])
+def test_two_phase_xsph_with_own_coefficients_matches_oracle(precision, tol_scale):
+    """each model with its own XSPH fluid and boundary coefficients, the filter over the
+    neighbours of every model: iteration counts equal, fields at the bars of the shared case"""
+    sc, counts, state = two_phase_state()
+    xs, xsb = (0.2, 0.0), (0.05, 0.3)
+    ts = TimeStepDFSPH(sc, precision=precision)
+    ts.ctx.set_fluid_phases(counts, RHO)
+    ts.ctx.set_fluid_phase_xsph(xs, xsb)
+    m = ts.getFluidModel()
+    m.setFieldBuffer("position", state["x"])
+    m.setFieldBuffer("velocity", state["v"])
+    m.setFieldBuffer("p / rho^2", state["kappa"])
+    m.setFieldBuffer("p_v / rho^2", state["kappa_v"])
+    ts.setTimeStepSize(state["dt"])
+    sim = oracle.OracleSim(sc)
+    sim.set_phases(counts, RHO)
+    sim.set_phase_xsph(xs, xsb)
+    sim.x[:] = state["x"]
+    sim.v[:] = state["v"]
+    sim.kappa[:] = state["kappa"]
+    sim.kappa_v[:] = state["kappa_v"]
+    sim.dt = state["dt"]
+    st = ts.step()
+    sim.step()
+    compare(ts, sim, st, tol_scale=tol_scale)
+    ts.close()
+
+
+def test_oracle_phase_xsph_equal_to_the_shared_coefficients_gives_the_shared_bits():
+    """per-model XSPH coefficients equal to the shared ones give the shared run's bits, and a
+    different coefficient on one model changes the run"""
+    sc, counts = layered_scene((6, 6, 6), velocity=(0.2, -0.3, 0.1))
+    sc.params.xsph = 0.2
+    sc.params.xsphBoundary = 0.1
+    a, b, c = oracle.OracleSim(sc), oracle.OracleSim(sc), oracle.OracleSim(sc)
+    for sim in (a, b, c):
+        sim.set_phases(counts, RHO)
+    b.set_phase_xsph((0.2, 0.2), (0.1, 0.1))
+    c.set_phase_xsph((0.2, 0.6), (0.1, 0.1))
+    for _ in range(3):
+        for sim in (a, b, c):
+            sim.step()
+    assert np.array_equal(a.x, b.x) and np.array_equal(a.v, b.v)
+    assert np.abs(a.v - c.v).max() > 1e-6
