@@ -335,6 +335,23 @@ void TimeStepDFSPH_GB300::upload()
     check(sphgb_set_fluid_phases(m_ctx, m_fluids.size() > 1 ? (uint32_t)m_fluids.size() : 0u, counts.data(),
                                  rho0.data()),
           "sphgb_set_fluid_phases");
+    {   // per-model coefficients, where a model sets its own
+        bool own = false;
+        std::vector<double> nu, nub, xs, xsb;
+        const auto pick = [&](Real mine, double shared) {
+            own |= mine >= Real(0);
+            return mine >= Real(0) ? (double)mine : shared;
+        };
+        for (FluidModel *f : m_fluids) {
+            nu.push_back(pick(f->m_viscosity, m_visco ? (double)m_visco->m_viscosity : 0.0));
+            nub.push_back(pick(f->m_viscosityBoundary, m_visco ? (double)m_visco->m_boundaryViscosity : 0.0));
+            xs.push_back(pick(f->m_xsph, (double)m_sim.xsph));
+            xsb.push_back(pick(f->m_xsphBoundary, (double)m_sim.xsphBoundary));
+        }
+        const uint32_t k = (own && m_fluids.size() > 1) ? (uint32_t)m_fluids.size() : 0u;
+        check(sphgb_set_fluid_phase_viscosity(m_ctx, k, nu.data(), nub.data()), "sphgb_set_fluid_phase_viscosity");
+        check(sphgb_set_fluid_phase_xsph(m_ctx, k, xs.data(), xsb.data()), "sphgb_set_fluid_phase_xsph");
+    }
     if (n) {
         check(sphgb_upload_field(m_ctx, SPHGB_FIELD_PRESSURE_RHO2, m_pressureRho2.data(), kDtype), "upload p / rho^2");
         check(sphgb_upload_field(m_ctx, SPHGB_FIELD_PRESSURE_RHO2_V, m_pressureRho2V.data(), kDtype), "upload p_v / rho^2");

@@ -73,6 +73,9 @@ public:
     std::vector<unsigned int> m_particleId;
     Real m_V = 0;
     Real m_density0 = Real(1000);
+    // Per-model Weiler2018 viscosity and XSPH coefficients, as each reference FluidModel owns its
+    // viscosity and XSPH objects; negative: the time step's shared settings.
+    Real m_viscosity = Real(-1), m_viscosityBoundary = Real(-1), m_xsph = Real(-1), m_xsphBoundary = Real(-1);
 
     void initModel(const std::string &id, unsigned int nFluidParticles, const Vector3r *fluidParticles,
                    const Vector3r *fluidVelocities);

@@ -53,7 +53,8 @@ int main(int argc, char **argv)
     if (!rd(f, hdr, 8) || !rd(f, &radius, 1)) return 2;
     const uint32_t n = hdr[0], nb = hdr[1], steps = hdr[2], lanes = hdr[3], visc = hdr[4], bodies = hdr[5],
                    vmap = hdr[6], phase0 = hdr[7];
-    if (phase0 && (phase0 >= n || !rd(f, &rho1, 1))) return 2;
+    double own1[4] = {-1, -1, -1, -1};   // the second model's nu, nu_b, xsph, xsph_b (negative: shared)
+    if (phase0 && (phase0 >= n || !rd(f, &rho1, 1) || !rd(f, own1, 4))) return 2;
     std::vector<double> x(3 * (size_t)n), v(3 * (size_t)n), xb(3 * (size_t)nb);
     if (!rd(f, x.data(), x.size()) || !rd(f, v.data(), v.size()) || !rd(f, xb.data(), xb.size())) return 2;
     std::vector<uint32_t> body(nb, 1u);
@@ -83,6 +84,10 @@ int main(int argc, char **argv)
         if (phase0) {   // a second fluid model (a phase of its own rest density)
             second.initModel("Fluid2", n - n0, xv.data() + n0, vv.data() + n0);
             second.m_density0 = (Real)rho1;
+            second.m_viscosity = (Real)own1[0];
+            second.m_viscosityBoundary = (Real)own1[1];
+            second.m_xsph = (Real)own1[2];
+            second.m_xsphBoundary = (Real)own1[3];
         }
         // one boundary model per body: the dynamic body (body 0) and the static walls
         std::vector<Vector3r> part[2];

@@ -20,8 +20,8 @@ def _write_scene(path, sc, steps, lanes, visc, body=None, position=None, vmap=No
         f.write(struct.pack("<8I", sc.n, sc.nb, steps, lanes, 1 if visc else 0, 0 if body is None else 1,
                             0 if vmap is None else 1, 0 if phases is None else phases[0]))
         f.write(struct.pack("<d", sc.params.particleRadius))
-        if phases is not None:
-            f.write(struct.pack("<d", phases[1]))
+        if phases is not None:   # the second model's rest density and own nu, nu_b, xsph, xsph_b (-1: shared)
+            f.write(struct.pack("<5d", phases[1], *phases[2]))
         for a in (sc.x, sc.v, sc.xb):
             f.write(np.ascontiguousarray(a, "<f8").tobytes())
         if body is not None:
@@ -72,7 +72,8 @@ def test_host_layer_is_built_and_fails_cleanly_without_a_device():
 @pytest.mark.gpu
 @pytest.mark.parametrize("visc,bodies,vmap,phases", [(False, False, False, False), (True, False, False, False),
                                                      (True, True, False, False), (True, False, True, False),
-                                                     (True, True, True, False), (False, False, False, True)])
+                                                     (True, True, True, False), (False, False, False, True),
+                                                     (True, False, False, "own")])
 def test_cpp_host_layer_matches_python_mirror(visc, bodies, vmap, phases):
     """with a volume map and bodies the container is a dynamic body with a velocity and an angular
     velocity (pose held): the C++ layer hands them to the device before every step"""
@@ -109,7 +110,8 @@ def test_cpp_host_layer_matches_python_mirror(visc, bodies, vmap, phases):
         # a second fluid model of half the rest density above the first one (TimeStepDFSPH_GB300::addFluidModel)
         order = np.argsort(sc.x[:, 1], kind="stable")
         sc = dataclasses.replace(sc, x=sc.x[order].copy(), v=sc.v[order].copy())
-        ph = (sc.n // 2, 500.0)
+        # "own": the second model with its own Weiler and XSPH coefficients
+        ph = (sc.n // 2, 500.0, (0.05, 0.02, 0.1, 0.05) if phases == "own" else (-1.0, -1.0, -1.0, -1.0))
     with tempfile.TemporaryDirectory() as d:
         _write_scene(os.path.join(d, "s.bin"), sc, steps, lanes, visc, body, position, mesh, motion, ph)
         r = subprocess.run([build.HOST_DEMO, os.path.join(d, "s.bin"), os.path.join(d, "o.bin")],
@@ -128,6 +130,10 @@ def test_cpp_host_layer_matches_python_mirror(visc, bodies, vmap, phases):
     ts.ctx.set_lanes_per_particle(lanes)
     if phases:
         ts.ctx.set_fluid_phases((ph[0], sc.n - ph[0]), (sc.params.density0, ph[1]))
+        if phases == "own":
+            p = sc.params
+            ts.ctx.set_fluid_phase_viscosity((p.viscosity, ph[2][0]), (p.viscosityBoundary, ph[2][1]))
+            ts.ctx.set_fluid_phase_xsph((p.xsph, ph[2][2]), (p.xsphBoundary, ph[2][3]))
     if vmap:
         ts.ctx.add_volume_map(mesh[0], mesh[1], mesh[2], invert=True)
         ts.ctx.set_boundary_method(2)
