@@ -1,0 +1,291 @@
+// Test infrastructure: a C interface around the reference's own DFSPH time step,
+// compiled from the reference's sources (SPlisHSPlasH/*.cpp, DFSPH/, Viscosity/, ...)
+// against the stand-ins in oracle/shims/ by oracle/build_ref.sh.  It is the oracle
+// pin: the reference's Simulation, FluidModel, BoundaryModel_Akinci2012,
+// TimeStepDFSPH, XSPH and Viscosity_Weiler2018 run unchanged; this file only sets a
+// scene up the way the reference's simulator does and reads fields back by particle id.
+//
+// Set-up order follows Simulator/SimulatorBase.cpp:432-577 (initSimulation,
+// buildModel, readParameters, deferredInit) and
+// Simulator/StaticBoundarySimulator.cpp:58-190 (static Akinci2012 boundary,
+// updateBoundaryVolume).  The simulation method is set after the fluid model
+// exists, as readParameters does (Simulation.cpp:535-602), which forces the
+// precomputed kernel; `analytic_kernel` then selects the analytic cubic spline
+// (setKernel(0); setGradKernel(0)), as the FP64 oracle protocol asks.
+// Only tests/ and bench.py's CPU legs load the library built from this file.
+#include "SPlisHSPlasH/Common.h"
+#include "SPlisHSPlasH/Simulation.h"
+#include "SPlisHSPlasH/TimeManager.h"
+#include "SPlisHSPlasH/FluidModel.h"
+#include "SPlisHSPlasH/BoundaryModel_Akinci2012.h"
+#include "SPlisHSPlasH/StaticRigidBody.h"
+#include "SPlisHSPlasH/TimeStep.h"
+#include "SPlisHSPlasH/DFSPH/TimeStepDFSPH.h"
+#include "SPlisHSPlasH/XSPH.h"
+#include "SPlisHSPlasH/Viscosity/Viscosity_Weiler2018.h"
+#include "Utilities/Timing.h"
+#include "Utilities/Counting.h"
+#include "Utilities/Logger.h"
+
+#include <chrono>
+#include <cstring>
+#include <string>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+INIT_LOGGING
+INIT_TIMING
+INIT_COUNTING
+
+using namespace SPH;
+
+extern "C" {
+
+struct RefParams {
+    double particleRadius, density0, gravitation[3], timeStepSize;
+    int cflMethod;
+    double cflFactor, cflMinTimeStepSize, cflMaxTimeStepSize;
+    int minIterations, maxIterations;
+    double maxError;
+    int enableDivergenceSolver, maxIterationsV;
+    double maxErrorV;
+    double xsph, xsphBoundary;
+    int viscosityMethod;   // 0 none, 6 Weiler et al. 2018
+    double viscosity, viscosityBoundary;
+    int viscoMaxIter;
+    double viscoMaxError;
+    int analyticKernel;    // 1: setKernel(0); setGradKernel(0) after the parameters
+    int numThreads;        // 0: OpenMP default
+};
+
+struct RefStats {
+    unsigned int iterations, iterationsV, viscoIterations, pad;
+    double dtOld, dt, time, stepSeconds;
+};
+
+}  // extern "C"
+
+namespace {
+StaticRigidBody *g_body = nullptr;
+std::vector<Vector3r> g_x, g_v, g_xb;
+std::vector<unsigned int> g_objectIds;
+
+int method_index(std::vector<Simulation::NonPressureForceMethod> &methods, const std::string &name)
+{
+    for (unsigned int i = 0; i < methods.size(); i++)
+        if (methods[i].m_name == name) return methods[i].m_id;
+    return -1;
+}
+
+FluidModel *model0() { return Simulation::getCurrent()->getFluidModel(0); }
+
+// field -> (pointer getter, components); the names are the reference's field names
+Real *field_ptr(FluidModel *fm, int field, unsigned int i, int &dim)
+{
+    dim = 1;
+    switch (field) {
+    case 0: dim = 3; return &fm->getPosition(i)[0];
+    case 1: dim = 3; return &fm->getVelocity(i)[0];
+    case 2: return &fm->getDensity(i);
+    case 3: dim = 3; return &fm->getAcceleration(i)[0];
+    default: break;
+    }
+    static const char *names[] = {"factor", "advected density", "p / rho^2", "p_v / rho^2", "pressure acceleration",
+                                  "velocity difference"};
+    const int k = field - 4;
+    if (k < 0 || k >= 6) return nullptr;
+    const FieldDescription &fd = fm->getField(names[k]);
+    if (fd.name != names[k]) return nullptr;
+    dim = fd.type == FieldType::Vector3 ? 3 : 1;
+    return static_cast<Real *>(fd.getFct(i));
+}
+}  // namespace
+
+extern "C" {
+
+/** Builds the scene: n fluid particles (positions x, velocities v, AoS FP64, id = index)
+ *  and nb static Akinci2012 boundary particles xb.  Returns 0 on success. */
+int ref_create(const RefParams *p, unsigned int n, const double *x, const double *v, unsigned int nb,
+               const double *xb)
+{
+#ifdef _OPENMP
+    if (p->numThreads > 0) omp_set_num_threads(p->numThreads);
+#endif
+    Utilities::Timing::m_dontPrintTimes = true;
+    Simulation *sim = Simulation::getCurrent();
+    sim->init(static_cast<Real>(p->particleRadius), false);
+    sim->setBoundaryHandlingMethod(BoundaryHandlingMethods::Akinci2012);
+
+    g_x.resize(n);
+    g_v.resize(n);
+    g_objectIds.assign(n, 0u);
+    for (unsigned int i = 0; i < n; i++) {
+        g_x[i] = Vector3r(static_cast<Real>(x[3 * i]), static_cast<Real>(x[3 * i + 1]), static_cast<Real>(x[3 * i + 2]));
+        g_v[i] = Vector3r(static_cast<Real>(v[3 * i]), static_cast<Real>(v[3 * i + 1]), static_cast<Real>(v[3 * i + 2]));
+    }
+    // SimulatorBase::buildModel -> initFluidData: one fluid model, no emitter reserve
+    sim->addFluidModel("Fluid", n, g_x.data(), g_v.data(), g_objectIds.data(), 0u);
+    sim->setValue(Simulation::KERNEL_METHOD, Simulation::ENUM_KERNEL_PRECOMPUTED_CUBIC);
+    sim->setValue(Simulation::GRAD_KERNEL_METHOD, Simulation::ENUM_GRADKERNEL_PRECOMPUTED_CUBIC);
+
+    // SimulatorBase::readParameters: Configuration block, then the material
+    Real g[3] = {static_cast<Real>(p->gravitation[0]), static_cast<Real>(p->gravitation[1]),
+                 static_cast<Real>(p->gravitation[2])};
+    sim->setVecValue<Real>(Simulation::GRAVITATION, g);
+    sim->setValue<int>(Simulation::CFL_METHOD, p->cflMethod);
+    sim->setValue<Real>(Simulation::CFL_FACTOR, static_cast<Real>(p->cflFactor));
+    sim->setValue<Real>(Simulation::CFL_MIN_TIMESTEPSIZE, static_cast<Real>(p->cflMinTimeStepSize));
+    sim->setValue<Real>(Simulation::CFL_MAX_TIMESTEPSIZE, static_cast<Real>(p->cflMaxTimeStepSize));
+    sim->setValue<int>(Simulation::SIMULATION_METHOD, static_cast<int>(SimulationMethods::DFSPH));
+    TimeStep *ts = sim->getTimeStep();
+    ts->setValue<unsigned int>(TimeStepDFSPH::MIN_ITERATIONS, static_cast<unsigned int>(p->minIterations));
+    ts->setValue<unsigned int>(TimeStepDFSPH::MAX_ITERATIONS, static_cast<unsigned int>(p->maxIterations));
+    ts->setValue<Real>(TimeStepDFSPH::MAX_ERROR, static_cast<Real>(p->maxError));
+    ts->setValue<bool>(TimeStepDFSPH::USE_DIVERGENCE_SOLVER, p->enableDivergenceSolver != 0);
+    ts->setValue<unsigned int>(TimeStepDFSPH::MAX_ITERATIONS_V, static_cast<unsigned int>(p->maxIterationsV));
+    ts->setValue<Real>(TimeStepDFSPH::MAX_ERROR_V, static_cast<Real>(p->maxErrorV));
+
+    FluidModel *fm = model0();
+    fm->setValue<Real>(FluidModel::DENSITY0, static_cast<Real>(p->density0));
+    int vm = 0;
+    if (p->viscosityMethod == 6) vm = method_index(sim->getViscosityMethods(), Viscosity_Weiler2018::METHOD_NAME);
+    else vm = method_index(sim->getViscosityMethods(), "None");
+    if (vm < 0) return 2;
+    fm->setValue<int>(FluidModel::VISCOSITY_METHOD, vm);
+    if (p->viscosityMethod == 6) {
+        NonPressureForceBase *visc = fm->getViscosityBase();
+        if (!visc) return 3;
+        visc->setValue<Real>(Viscosity_Weiler2018::VISCOSITY_COEFFICIENT, static_cast<Real>(p->viscosity));
+        visc->setValue<Real>(Viscosity_Weiler2018::VISCOSITY_COEFFICIENT_BOUNDARY,
+                             static_cast<Real>(p->viscosityBoundary));
+        visc->setValue<unsigned int>(Viscosity_Weiler2018::MAX_ITERATIONS, static_cast<unsigned int>(p->viscoMaxIter));
+        visc->setValue<Real>(Viscosity_Weiler2018::MAX_ERROR, static_cast<Real>(p->viscoMaxError));
+    }
+    XSPH *xs = fm->getXSPH();
+    if (!xs) return 4;
+    xs->setValue<Real>(XSPH::FLUID_COEFFICIENT, static_cast<Real>(p->xsph));
+    xs->setValue<Real>(XSPH::BOUNDARY_COEFFICIENT, static_cast<Real>(p->xsphBoundary));
+
+    // StaticBoundarySimulator::initBoundaryData: one static body at the identity pose
+    g_xb.resize(nb);
+    for (unsigned int i = 0; i < nb; i++)
+        g_xb[i] = Vector3r(static_cast<Real>(xb[3 * i]), static_cast<Real>(xb[3 * i + 1]),
+                           static_cast<Real>(xb[3 * i + 2]));
+    if (nb > 0) {
+        g_body = new StaticRigidBody();
+        g_body->setPosition0(Vector3r::Zero());
+        g_body->setPosition(Vector3r::Zero());
+        g_body->setRotation0(Quaternionr::Identity());
+        g_body->setRotation(Quaternionr::Identity());
+        BoundaryModel_Akinci2012 *bm = new BoundaryModel_Akinci2012();
+        bm->initModel(g_body, nb, g_xb.data());
+        sim->addBoundaryModel(bm);
+    }
+    TimeManager::getCurrent()->setTimeStepSize(static_cast<Real>(p->timeStepSize));
+    TimeManager::getCurrent()->setTime(0.0);
+
+    // SimulatorBase::deferredInit -> Simulation::deferredInit, StaticBoundarySimulator::deferredInit
+    sim->deferredInit();
+    sim->performNeighborhoodSearchSort();
+    if (nb > 0) sim->updateBoundaryVolume();
+    sim->setSimulationInitialized(true);
+    if (p->analyticKernel) {
+        sim->setKernel(Simulation::ENUM_KERNEL_CUBIC);
+        sim->setGradKernel(Simulation::ENUM_GRADKERNEL_CUBIC);
+    }
+    return 0;
+}
+
+/** One TimeStep::step() of the reference. */
+int ref_step(RefStats *out)
+{
+    Simulation *sim = Simulation::getCurrent();
+    TimeManager *tm = TimeManager::getCurrent();
+    const double h0 = tm->getTimeStepSize();
+    const auto t0 = std::chrono::steady_clock::now();
+    sim->getTimeStep()->step();
+    const auto t1 = std::chrono::steady_clock::now();
+    if (out) {
+        TimeStep *ts = sim->getTimeStep();
+        out->iterations = ts->getValue<unsigned int>(TimeStepDFSPH::SOLVER_ITERATIONS);
+        out->iterationsV = ts->getValue<unsigned int>(TimeStepDFSPH::SOLVER_ITERATIONS_V);
+        NonPressureForceBase *visc = model0()->getViscosityBase();
+        out->viscoIterations = visc ? visc->getValue<unsigned int>(Viscosity_Weiler2018::ITERATIONS) : 0u;
+        out->dtOld = h0;
+        out->dt = tm->getTimeStepSize();
+        out->time = tm->getTime();
+        out->stepSeconds = std::chrono::duration<double>(t1 - t0).count();
+    }
+    return 0;
+}
+
+/** Field of the fluid model in particle-id order (FP64, AoS).  field: 0 position,
+ *  1 velocity, 2 density, 3 acceleration, 4 factor, 5 advected density, 6 p / rho^2,
+ *  7 p_v / rho^2, 8 pressure acceleration, 9 velocity difference.  Returns the number
+ *  of components, or a negative value for an unknown field. */
+int ref_get(int field, double *out)
+{
+    FluidModel *fm = model0();
+    const unsigned int n = fm->numActiveParticles();
+    int dim = 0;
+    for (unsigned int i = 0; i < n; i++) {
+        Real *p = field_ptr(fm, field, i, dim);
+        if (!p) return -1;
+        const unsigned int id = fm->getParticleId(i);
+        for (int d = 0; d < dim; d++) out[(size_t)id * dim + d] = static_cast<double>(p[d]);
+    }
+    return dim;
+}
+
+/** Overwrites a field in particle-id order (same numbering as ref_get). */
+int ref_set(int field, const double *in)
+{
+    FluidModel *fm = model0();
+    const unsigned int n = fm->numActiveParticles();
+    int dim = 0;
+    for (unsigned int i = 0; i < n; i++) {
+        Real *p = field_ptr(fm, field, i, dim);
+        if (!p) return -1;
+        const unsigned int id = fm->getParticleId(i);
+        for (int d = 0; d < dim; d++) p[d] = static_cast<Real>(in[(size_t)id * dim + d]);
+    }
+    return dim;
+}
+
+/** Akinci2012 boundary volumes in boundary upload order. */
+int ref_boundary_volume(double *out)
+{
+    Simulation *sim = Simulation::getCurrent();
+    if (sim->numberOfBoundaryModels() == 0) return 0;
+    BoundaryModel_Akinci2012 *bm = static_cast<BoundaryModel_Akinci2012 *>(sim->getBoundaryModel(0));
+    for (unsigned int i = 0; i < bm->numberOfParticles(); i++) out[i] = static_cast<double>(bm->getVolume(i));
+    return 0;
+}
+
+/** Fluid and boundary neighbour counts of the last neighbourhood search, by particle id. */
+int ref_neighbor_counts(unsigned int *nf, unsigned int *nb)
+{
+    Simulation *sim = Simulation::getCurrent();
+    FluidModel *fm = model0();
+    const unsigned int n = fm->numActiveParticles();
+    for (unsigned int i = 0; i < n; i++) {
+        const unsigned int id = fm->getParticleId(i);
+        nf[id] = sim->numberOfNeighbors(0, 0, i);
+        nb[id] = sim->numberOfPointSets() > 1 ? sim->numberOfNeighbors(0, 1, i) : 0u;
+    }
+    return 0;
+}
+
+void ref_set_time_step(double dt) { TimeManager::getCurrent()->setTimeStepSize(static_cast<Real>(dt)); }
+
+int ref_precision() { return static_cast<int>(sizeof(Real)); }
+
+void ref_destroy()
+{
+    if (Simulation::hasCurrent()) delete Simulation::getCurrent();
+    g_body = nullptr;   // the boundary model does not own it; freed with the process
+}
+
+}  // extern "C"

@@ -1,0 +1,139 @@
+"""Generate one-step fixtures from the reference's own DFSPH time step.
+
+The reference's SPlisHSPlasH sources are compiled by oracle/build_ref.sh into
+oracle/_ref/libref_f64.so (FP64, analytic cubic spline, the oracle protocol) and
+driven through oracle/refsim.py.  Run in a checkout that has the reference tree:
+
+    oracle/build_ref.sh && python tests/golden/gen_ref_steps.py
+
+Each case advances a seeded scene with the reference for `warm` steps, rounds the
+state to float32 (the state the FP32 device path can hold exactly), builds a fresh
+reference simulation from that state and records one reference step.  Written next
+to this script, by particle id:
+  ref_step_<case>.npz   inputs: x, v, kappa, kappa_v, vdiff (float32), dt, xb
+                        (float32), params (JSON); outputs (float64): density,
+                        factor, density_adv, kappa, kappa_v, v, x, vdiff, dt_next,
+                        time step counts (iterations, iterations_v, visco_iterations)
+  ref_kernel_table_delta.json  the same config-0 step with the reference's default
+                        PrecomputedKernel<CubicKernel, 10000> against the analytic
+                        kernel: max and mean relative difference per field
+"""
+import dataclasses
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import refsim  # noqa: E402
+from splishsplash_gb300 import scenes  # noqa: E402
+
+OUT_FIELDS = ("density", "factor", "advected density", "p / rho^2", "p_v / rho^2", "velocity", "position",
+              "velocity difference")
+KEYS = {"density": "density", "factor": "factor", "advected density": "density_adv", "p / rho^2": "kappa",
+        "p_v / rho^2": "kappa_v", "velocity": "v", "position": "x", "velocity difference": "vdiff"}
+
+
+def f32(a):
+    return np.asarray(a, np.float64).astype(np.float32).astype(np.float64)
+
+
+def advanced_state(scene, warm):
+    """The scene after `warm` reference steps, rounded to float32."""
+    visc = scene.params.viscosityMethod == 6
+    with refsim.RefSim(scene) as r:
+        for _ in range(warm):
+            r.step()
+        st = dict(x=f32(r.get("position")), v=f32(r.get("velocity")), kappa=f32(r.get("p / rho^2")),
+                  kappa_v=f32(r.get("p_v / rho^2")),
+                  vdiff=f32(r.get("velocity difference")) if visc else np.zeros((scene.n, 3)),
+                  dt=float(r.stats()["dt"]) if warm else scene.params.timeStepSize)
+    return st
+
+
+def step_from(scene, st, analytic=True):
+    """One reference step from state st; outputs by particle id."""
+    sc = dataclasses.replace(scene, x=st["x"], v=st["v"])
+    visc = scene.params.viscosityMethod == 6
+    with refsim.RefSim(sc, analytic_kernel=analytic) as r:
+        r.set("p / rho^2", st["kappa"])
+        r.set("p_v / rho^2", st["kappa_v"])
+        if visc:
+            r.set("velocity difference", st["vdiff"])
+        r.set_time_step(st["dt"])
+        s = r.step()
+        out = {KEYS[f]: r.get(f) for f in OUT_FIELDS if visc or f != "velocity difference"}
+    out["dt_next"] = s["dt"]
+    out["iterations"] = s["iterations"]
+    out["iterations_v"] = s["iterations_v"]
+    out["visco_iterations"] = s["visco_iterations"]
+    return out
+
+
+def viscous_column():
+    """A 10x20x10 column with a shear velocity field and nu = 1, so that one step runs
+    tens of pressure iterations and about ten Weiler2018 CG iterations."""
+    sc = scenes.small_block(counts=(10, 20, 10), box=(0.6, 1.4, 0.6), viscosity=True)
+    sc.v[:, 0] = 1.0 * (sc.x[:, 1] - sc.x[:, 1].mean())
+    sc.v[:, 2] = 0.5 * np.sin(8.0 * sc.x[:, 0])
+    sc.params.viscosity = 1.0
+    return sc
+
+
+def cases():
+    return {
+        "block12": (scenes.small_block(counts=(12, 12, 12), box=(0.8, 0.8, 0.8), velocity=(0.3, 0.0, -0.2)), 30),
+        "column_visc": (viscous_column(), 70),
+        "dambreak8k_step203": (scenes.dambreak_8k(), 202),
+    }
+
+
+def main():
+    for name, (scene, warm) in cases().items():
+        scene = scene.as_float32()
+        st = advanced_state(scene, warm)
+        out = step_from(scene, st)
+        params = dataclasses.asdict(scene.params)
+        np.savez_compressed(
+            os.path.join(HERE, f"ref_step_{name}.npz"),
+            params=json.dumps(params), warm=warm,
+            x=st["x"].astype(np.float32), v=st["v"].astype(np.float32), kappa=st["kappa"].astype(np.float32),
+            kappa_v=st["kappa_v"].astype(np.float32), vdiff=st["vdiff"].astype(np.float32), dt=st["dt"],
+            xb=scene.xb.astype(np.float32), box_min=scene.box_min, box_max=scene.box_max,
+            **{f"out_{k}": v for k, v in out.items()})
+        print(name, scene.n, "particles, warm", warm, "iterations", out["iterations"], out["iterations_v"],
+              out["visco_iterations"])
+    # lookup-table kernel against the analytic kernel, on the config-0 step above
+    scene, warm = cases()["dambreak8k_step203"]
+    scene = scene.as_float32()
+    st = advanced_state(scene, warm)
+    a = step_from(scene, st, analytic=True)
+    t = step_from(scene, st, analytic=False)
+    delta = {"case": f"dambreak_8k, one step after {warm} steps, FP64 reference build",
+             "iterations": {"analytic": [a["iterations"], a["iterations_v"]],
+                            "table": [t["iterations"], t["iterations_v"]]}}
+    for k in ("density", "factor", "kappa", "kappa_v", "v", "x"):
+        ra, rt = np.asarray(a[k]), np.asarray(t[k])
+        if ra.ndim == 2:
+            d = np.linalg.norm(rt - ra, axis=1)
+            den = np.maximum(np.linalg.norm(ra, axis=1), 1e-3 if k == "v" else 1e-12)
+        else:
+            d = np.abs(rt - ra)
+            floor = {"density": 1e-3, "factor": float(np.median(np.abs(ra))),
+                     "kappa": 1e-3 * float(np.max(np.abs(ra))) or 1e-30,
+                     "kappa_v": 1e-3 * float(np.max(np.abs(ra))) or 1e-30}[k]
+            den = np.maximum(np.abs(ra), floor)
+        rel = d / den
+        delta[k] = {"max_rel": float(rel.max()), "mean_rel": float(rel.mean())}
+    with open(os.path.join(HERE, "ref_kernel_table_delta.json"), "w") as f:
+        json.dump(delta, f, indent=1)
+    print(json.dumps(delta))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,59 @@
+"""One-step fixtures recorded from the reference's own DFSPH time step (tests/golden/
+ref_step_*.npz, made by tests/golden/gen_ref_steps.py), and the bars they are held to."""
+import dataclasses
+import json
+import os
+
+import numpy as np
+
+from splishsplash_gb300 import scenes
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CASES = ("block12", "column_visc", "dambreak8k_step203")
+
+
+def load_case(name):
+    """(scene, state, reference outputs) of a fixture; state arrays are float32 values."""
+    g = np.load(os.path.join(GOLDEN, f"ref_step_{name}.npz"))
+    params = scenes.SPHParams(**{k: (tuple(v) if isinstance(v, list) else v)
+                                 for k, v in json.loads(str(g["params"])).items()})
+    x = g["x"].astype(np.float64)
+    scene = scenes.Scene(f"ref_{name}", x, g["v"].astype(np.float64), g["xb"].astype(np.float64), params,
+                         np.asarray(g["box_min"]), np.asarray(g["box_max"]))
+    state = dict(x=x, v=g["v"].astype(np.float64), kappa=g["kappa"].astype(np.float64),
+                 kappa_v=g["kappa_v"].astype(np.float64), vdiff=g["vdiff"].astype(np.float64), dt=float(g["dt"]))
+    out = {k[4:]: (g[k] if g[k].ndim else g[k].item()) for k in g.files if k.startswith("out_")}
+    return scene, state, out
+
+
+def rel_scalar(a, b, floor):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), floor)))
+
+
+def rel_vec(a, b, floor):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    d = np.linalg.norm(a - b, axis=-1)
+    return float(np.max(d / np.maximum(np.linalg.norm(b, axis=-1), floor)))
+
+
+def field_errors(got, ref):
+    """Max relative error per field against the reference's step, with the floors of the
+    comparison protocol: rho0 1e-6 for density, the median |alpha| for alpha, 1e-3 of the
+    largest |kappa| for kappa and kappa_v, 1e-3 m/s for velocity."""
+    e = {
+        "density": rel_scalar(got["density"], ref["density"], 1e-3),
+        "factor": rel_scalar(got["factor"], ref["factor"], float(np.median(np.abs(ref["factor"])))),
+        "v": rel_vec(got["v"], ref["v"], 1e-3),
+        "x": float(np.max(np.abs(np.asarray(got["x"]) - ref["x"]))),
+    }
+    for k in ("kappa", "kappa_v"):
+        m = float(np.max(np.abs(ref[k])))
+        e[k] = float(np.max(np.abs(np.asarray(got[k]) - ref[k]))) / m if m > 0 else 0.0
+    if "vdiff" in ref and "vdiff" in got:
+        e["vdiff"] = rel_vec(got["vdiff"], ref["vdiff"], 1e-3)
+    return e
+
+
+def with_state(scene, state):
+    return dataclasses.replace(scene, x=state["x"], v=state["v"])

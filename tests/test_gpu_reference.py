@@ -1,0 +1,66 @@
+"""The CUDA path against the reference's own DFSPH time step.
+
+Fixtures (tests/golden/ref_step_*.npz) hold a float32 state and one step of the
+reference's TimeStepDFSPH built from its own sources in FP64 with the analytic cubic
+spline (tests/golden/gen_ref_steps.py).  The device starts from the same state and dt,
+through the C ABI, and must reproduce the step by particle id:
+  * pressure, divergence and Weiler2018 CG iteration counts identical;
+  * FP32 bulk: density 1e-5, velocity 1e-4 (floor 1e-3 m/s), alpha 1e-4 (floor: the
+    median alpha), kappa and kappa_v 1e-3 of their largest value, dt of the next step
+    1e-5, all relative;
+  * FP64 device mode: 1e-9 on the same fields.
+"""
+import numpy as np
+import pytest
+
+import ref_cases
+from splishsplash_gb300.dfsph import TimeStepDFSPH
+
+pytestmark = pytest.mark.gpu
+
+BARS_FP32 = dict(density=1e-5, factor=1e-4, v=1e-4, kappa=1e-3, kappa_v=1e-3, vdiff=1e-3)
+
+
+def device_step(scene, state, precision, use_graph):
+    ts = TimeStepDFSPH(ref_cases.with_state(scene, state), precision=precision, use_graph=use_graph)
+    try:
+        m = ts.getFluidModel()
+        m.setFieldBuffer("p / rho^2", state["kappa"])
+        m.setFieldBuffer("p_v / rho^2", state["kappa_v"])
+        m.setFieldBuffer("velocity difference", state["vdiff"])
+        ts.setTimeStepSize(state["dt"])
+        st = ts.step()
+        got = dict(density=m.getFieldBuffer("density"), factor=m.getFieldBuffer("factor raw"),
+                   kappa=m.getFieldBuffer("p / rho^2"), kappa_v=m.getFieldBuffer("p_v / rho^2"),
+                   v=m.getFieldBuffer("velocity"), x=m.getFieldBuffer("position"))
+        if scene.params.viscosityMethod == 6:
+            got["vdiff"] = m.getFieldBuffer("velocity difference")
+        return got, st
+    finally:
+        ts.close()
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+@pytest.mark.parametrize("case", ref_cases.CASES)
+def test_fp32_step_matches_reference(case, use_graph):
+    scene, state, ref = ref_cases.load_case(case)
+    got, st = device_step(scene, state, "fp32", use_graph)
+    assert (st["iterations"], st["iterations_v"], st["visco_iterations"]) == \
+        (ref["iterations"], ref["iterations_v"], ref["visco_iterations"])
+    err = ref_cases.field_errors(got, ref)
+    for k, bar in BARS_FP32.items():
+        if k in err:
+            assert err[k] <= bar, (case, k, err[k])
+    assert err["x"] <= 1e-6 * float(np.max(np.abs(ref["x"])))
+    assert st["dt_next"] == pytest.approx(ref["dt_next"], rel=1e-5)
+
+
+@pytest.mark.parametrize("case", ref_cases.CASES)
+def test_fp64_step_matches_reference(case):
+    scene, state, ref = ref_cases.load_case(case)
+    got, st = device_step(scene, state, "fp64", False)
+    assert (st["iterations"], st["iterations_v"], st["visco_iterations"]) == \
+        (ref["iterations"], ref["iterations_v"], ref["visco_iterations"])
+    for k, e in ref_cases.field_errors(got, ref).items():
+        assert e <= 1e-9 * (float(np.max(np.abs(ref["x"]))) if k == "x" else 1.0), (case, k, e)
+    assert st["dt_next"] == pytest.approx(ref["dt_next"], rel=1e-12)

@@ -1,0 +1,153 @@
+"""Pins the CPU oracle to the reference's own DFSPH time step.
+
+The reference's SPlisHSPlasH sources (TimeStep, DFSPH, Simulation, FluidModel,
+BoundaryModel_Akinci2012, XSPH, Viscosity_Weiler2018, SPHKernels, ...) are compiled by
+oracle/build_ref.sh against the stand-ins of oracle/shims/ and driven through
+oracle/refsim.py.  The one-step fixtures in tests/golden/ref_step_*.npz were recorded
+from that build (FP64, analytic cubic spline) by tests/golden/gen_ref_steps.py.
+
+* The FP64 oracle (oracle/sph_oracle.c) is held to the fixtures at 1e-10 with equal
+  pressure, divergence and Weiler2018 CG iteration counts.  These tests need only the
+  committed fixtures.
+* Where the reference tree is present, the reference build itself is run: it must
+  reproduce the fixtures, follow the oracle step by step over many steps, and its
+  FP32 AVX build (the CPU baseline, x86-64) must run the benchmark's kind of scene.
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+import ref_cases
+import refsim
+from splishsplash_gb300 import scenes
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_TOL = 1e-10
+
+
+def reference_tree():
+    env = os.environ.get("SPH_REFERENCE_ROOT")
+    p = env if env else os.path.join(ROOT, "..", "reference")
+    return p if os.path.isfile(os.path.join(p, "SPlisHSPlasH", "TimeStep.cpp")) else None
+
+
+@pytest.fixture(scope="module")
+def ref_build():
+    """The reference library (oracle/_ref/libref_f64.so), built on demand; skips where the
+    reference tree is absent."""
+    if not refsim.available("f64"):
+        tree = reference_tree()
+        if tree is None:
+            pytest.skip("reference tree not present (set SPH_REFERENCE_ROOT)")
+        subprocess.run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh")], check=True,
+                       env={**os.environ, "SPH_REFERENCE_ROOT": tree}, capture_output=True)
+    if not refsim.available("f64"):
+        pytest.skip("reference build unavailable")
+    return True
+
+
+def oracle_step(scene, state):
+    sim = oracle.OracleSim(ref_cases.with_state(scene, state), fp32_predicate=False)
+    sim.kappa[:] = state["kappa"]
+    sim.kappa_v[:] = state["kappa_v"]
+    sim.vdiff[:] = state["vdiff"]
+    sim.dt = state["dt"]
+    sim.step()
+    got = dict(density=sim.density.copy(), factor=sim.factor.copy(), kappa=sim.kappa.copy(),
+               kappa_v=sim.kappa_v.copy(), v=sim.v.copy(), x=sim.x.copy(), vdiff=sim.vdiff.copy())
+    return got, sim.stats()
+
+
+@pytest.mark.parametrize("case", ref_cases.CASES)
+def test_oracle_matches_reference_step(case):
+    scene, state, ref = ref_cases.load_case(case)
+    got, st = oracle_step(scene, state)
+    assert (st["iterations"], st["iterations_v"], st["visco_iterations"]) == \
+        (ref["iterations"], ref["iterations_v"], ref["visco_iterations"])
+    err = ref_cases.field_errors(got, ref)
+    for k, e in err.items():
+        bound = ORACLE_TOL * (np.max(np.abs(ref["x"])) if k == "x" else 1.0)
+        assert e <= bound, (case, k, e)
+    assert st["dt"] == pytest.approx(ref["dt_next"], rel=1e-12)
+
+
+def test_fixtures_exercise_the_solvers():
+    its = {c: ref_cases.load_case(c)[2] for c in ref_cases.CASES}
+    assert max(o["iterations"] for o in its.values()) >= 10            # pressure solve
+    assert max(o["iterations_v"] for o in its.values()) >= 5           # divergence solve
+    assert max(o["visco_iterations"] for o in its.values()) >= 5       # Weiler2018 CG
+
+
+@pytest.mark.parametrize("case", ref_cases.CASES)
+def test_reference_build_reproduces_fixture(ref_build, case):
+    scene, state, ref = ref_cases.load_case(case)
+    visc = scene.params.viscosityMethod == 6
+    with refsim.RefSim(ref_cases.with_state(scene, state)) as r:
+        r.set("p / rho^2", state["kappa"])
+        r.set("p_v / rho^2", state["kappa_v"])
+        if visc:
+            r.set("velocity difference", state["vdiff"])
+        r.set_time_step(state["dt"])
+        s = r.step()
+        got = dict(density=r.get("density"), factor=r.get("factor"), kappa=r.get("p / rho^2"),
+                   kappa_v=r.get("p_v / rho^2"), v=r.get("velocity"), x=r.get("position"))
+    assert (s["iterations"], s["iterations_v"], s["visco_iterations"]) == \
+        (ref["iterations"], ref["iterations_v"], ref["visco_iterations"])
+    for k, e in ref_cases.field_errors(got, ref).items():
+        assert e <= 1e-13 * (np.max(np.abs(ref["x"])) if k == "x" else 1.0), (case, k, e)
+
+
+def test_oracle_follows_reference_over_steps(ref_build):
+    """40 steps of a viscous shear column: oracle and reference agree after every step."""
+    sc = scenes.small_block(counts=(8, 14, 8), box=(0.5, 1.0, 0.5), viscosity=True)
+    sc.v[:, 0] = sc.x[:, 1] - sc.x[:, 1].mean()
+    sc.params.viscosity = 0.5
+    sc = sc.as_float32()
+    o = oracle.OracleSim(sc, fp32_predicate=False)
+    with refsim.RefSim(sc) as r:
+        np.testing.assert_allclose(r.boundary_volume(), o.Vb, rtol=1e-13)
+        for k in range(40):
+            sr = r.step()
+            o.step()
+            so = o.stats()
+            assert (sr["iterations"], sr["iterations_v"], sr["visco_iterations"]) == \
+                (so["iterations"], so["iterations_v"], so["visco_iterations"]), k
+            assert sr["dt"] == pytest.approx(so["dt"], rel=1e-12)
+            got = dict(density=r.get("density"), factor=r.get("factor"), kappa=r.get("p / rho^2"),
+                       kappa_v=r.get("p_v / rho^2"), v=r.get("velocity"), x=r.get("position"),
+                       vdiff=r.get("velocity difference"))
+            ref = dict(density=o.density, factor=o.factor, kappa=o.kappa, kappa_v=o.kappa_v, v=o.v, x=o.x,
+                       vdiff=o.vdiff)
+            for name, e in ref_cases.field_errors(got, ref).items():
+                assert e <= ORACLE_TOL, (k, name, e)
+
+
+def test_reference_neighbor_counts_match_oracle(ref_build):
+    sc = scenes.small_block(counts=(10, 8, 10), box=(0.8, 0.8, 0.8)).as_float32()
+    with refsim.RefSim(sc) as r:
+        r.step()
+        nf, nb = r.neighbor_counts()
+    h = sc.params.supportRadius
+    off_f, _ = oracle.neighbors(sc.x, sc.x, h, True, fp32=False)
+    off_b, _ = oracle.neighbors(sc.x, sc.xb, h, False, fp32=False)
+    np.testing.assert_array_equal(nf, np.diff(off_f))
+    np.testing.assert_array_equal(nb, np.diff(off_b))
+
+
+def test_reference_fp32_avx_build_runs(ref_build):
+    """The reference's FP32 AVX build with precomputeValues (the CPU baseline) runs a few
+    steps of a dam break and stays close to the FP64 oracle (its fluid sums use
+    CubicKernel_AVX, its boundary volumes the lookup-table kernel)."""
+    if not refsim.available("f32"):
+        pytest.skip("FP32 AVX build is x86-64 only")
+    sc = scenes.small_block(counts=(12, 12, 12), box=(0.8, 0.8, 0.8)).as_float32()
+    o = oracle.OracleSim(sc, fp32_predicate=False)
+    with refsim.RefSim(sc, precision="f32", analytic_kernel=False) as r:
+        for _ in range(5):
+            r.step()
+            o.step()
+        rho = r.get("density")
+    assert ref_cases.rel_scalar(rho, o.density, 1.0) < 1e-3
