@@ -750,7 +750,7 @@ template <class T> int prepare(sphgb_ctx *c)
         if ((rc = palloc(c, &v1, (size_t)nb * 4))) return rc;
         if ((rc = palloc(c, &v2, (size_t)nb * 4))) return rc;
         if ((rc = palloc(c, &cells, (size_t)nb * 4))) return rc;
-        if ((rc = palloc(c, &hist, (size_t)tiles * 256 * 4))) return rc;
+        if ((rc = palloc(c, &hist, (size_t)(tiles + 1) * 256 * 4))) return rc;
         const DevParams<T> P = make_params<T>(c);
         const DevBufs<T> B = make_bufs<T>(c, 1);
         launch_boundary_keys<T>(P, (const v4_t<T> *)xb_raw, bscene_raw, k1, v1, c->stream);
@@ -1268,7 +1268,7 @@ template <class T> int prepare_body_motion(sphgb_ctx *c)
             (rc = al(&c->bm_V0, nb * sizeof(T))) || (rc = al(&c->bm_xtmp, nb * vs)) || (rc = al(&c->bm_vtmp, nb * vs)) ||
             (rc = al(&c->vbs, nb * vs)) || (rc = al(&c->bm_body, nb * 4)) || (rc = al(&c->bm_k1, nb * 4)) ||
             (rc = al(&c->bm_k2, nb * 4)) || (rc = al(&c->bm_v1, nb * 4)) || (rc = al(&c->bm_v2, nb * 4)) ||
-            (rc = al(&c->bm_cells, nb * 4)) || (rc = al(&c->bm_hist, tiles * 256 * 4)) ||
+            (rc = al(&c->bm_cells, nb * 4)) || (rc = al(&c->bm_hist, (tiles + 1) * 256 * 4)) ||
             (rc = al(&c->bm_scene, nb * 4)))
             return rc;
         c->bm_nb = nb;
@@ -1553,7 +1553,7 @@ template <class T> int init_scenes(sphgb_ctx *c, const double *x, const double *
     CK(cudaMemset(c->sc, 0, nrec * sizeof(StepScalars)));
     if ((rc = ensure_scalar_mirror(c, nrec))) return rc;
     const size_t tiles = (NR + kSortTile - 1) / kSortTile;
-    if ((rc = dalloc(c, &c->hist, tiles * 256 * 4))) return rc;
+    if ((rc = dalloc(c, &c->hist, (tiles + 1) * 256 * 4))) return rc;
     if ((rc = dalloc(c, &c->inv_perm, NR * 4))) return rc;
     if (S > 1) {
         if ((rc = dalloc(c, &c->d_scenes, S * sizeof(SceneDev<T>)))) return rc;

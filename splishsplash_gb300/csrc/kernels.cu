@@ -835,13 +835,14 @@ __device__ __forceinline__ void build_one(const DevParams<T> &P, const DevBufs<T
     v4_t<T> xk = xi;
     xk.w = kv;
     stv(B.xk, i, xk);
+    // FP32: the position half of the Jacobi pass's (x, a) record, fixed for the step; the
+    // pressure-acceleration passes write only the acceleration half
+    if constexpr (sizeof(T) == 4) B.xa[2 * (size_t)i] = xi;
     if (P.nphase > 1) {   // fluid phases: each particle's last pressure acceleration, in its new slot
         const v4_t<T> a = ldv(B.a, i);
         stv(B.pa, i, a);
-        if constexpr (sizeof(T) == 4) {   // the whole (x, a) record: a pass writes only its own phase's
-            B.xa[2 * (size_t)i] = ldv(B.x, i);
+        if constexpr (sizeof(T) == 4)   // a pass writes only its own phase's accelerations
             B.xa[2 * (size_t)i + 1] = make_float4((float)a.x, (float)a.y, (float)a.z, 0.0f);
-        }
     }
 }
 
@@ -981,8 +982,8 @@ __device__ __forceinline__ F8 ld_f8(const float4 *p)
     return r;
 }
 
-// Pressure accelerations of the running solver.  FP32: also the (x_i, a_i) record that the
-// Jacobi pass gathers with one 256-bit load per neighbour.
+// Pressure accelerations of the running solver.  FP32: the acceleration half of the (x_i, a_i)
+// record that the Jacobi pass gathers with one 256-bit load per neighbour.
 template <class T, int LPP, bool MP = false>
 __global__ void __launch_bounds__(kBlock, kPressureMinBlocks<T, LPP>) k_pressure_accel(DevParams<T> P, DevBufs<T> B,
                                                                                       unsigned limit,
@@ -1007,8 +1008,7 @@ __global__ void __launch_bounds__(kBlock, kPressureMinBlocks<T, LPP>) k_pressure
     }
     if (!q.act || q.l != 0) return;
     if constexpr (sizeof(T) == 4) {
-        B.xa[2 * (size_t)q.i] = ldv(B.x, q.i);
-        B.xa[2 * (size_t)q.i + 1] = make_float4(a.x, a.y, a.z, 0.0f);
+        B.xa[2 * (size_t)q.i + 1] = make_float4(a.x, a.y, a.z, 0.0f);   // x half: written by the list build
     } else {
         stv(B.pa, q.i, pack(a, T(0)));
     }

@@ -40,7 +40,7 @@ constexpr size_t kOffKeys2 = kOffVals + (size_t)kMaxB * 4;
 constexpr size_t kOffVals2 = kOffKeys2 + (size_t)kMaxB * 4;
 constexpr size_t kOffCells = kOffVals2 + (size_t)kMaxB * 4;
 constexpr size_t kOffHist = kOffCells + (size_t)kMaxB * 4;
-constexpr size_t kOffStart = kOffHist + (size_t)kMaxTiles * 256 * 4;
+constexpr size_t kOffStart = kOffHist + (size_t)(kMaxTiles + 1) * 256 * 4;   // tile rows + digit totals
 constexpr size_t kOffEnd = kOffStart + (size_t)kMaxCells * 4;
 constexpr size_t kScratchBytes = kOffEnd + (size_t)kMaxCells * 4;
 static_assert(kScratchBytes % 256 == 0, "scratch layout must stay 256-byte aligned");

@@ -1,10 +1,11 @@
 // Stable LSD radix sort of (uint32 key, uint32 value) pairs with 8-bit digits.
 // Used to order particles by the Morton code of their cell every step.
 //
-// Per pass: (1) per-tile digit histograms, stored digit-major so that one
-// exclusive scan over [digit][tile] yields every tile's global base per digit
-// in stable order; (2) a single-block scan; (3) a stable scatter that ranks the
-// items of a tile with warp match masks and per-warp digit counts.
+// Per pass: (1) per-tile digit histograms, stored digit-major; (2) an exclusive scan
+// of each digit's row over the tiles, one block per digit, with the row totals; (3) a
+// stable scatter whose tiles add the scan of the digit totals to their row offsets, and
+// rank the items of a tile with warp match masks and per-warp digit counts.
+// The histogram buffer holds 256 x (tiles + 1) words: the rows, then the digit totals.
 #include "sph_ctx.h"
 
 namespace sphgb {
@@ -33,59 +34,68 @@ __global__ void __launch_bounds__(kSortThreads) k_hist(const uint32_t *__restric
     hist[(size_t)threadIdx.x * num_tiles + blockIdx.x] = h[threadIdx.x];
 }
 
-// Exclusive scan of m entries by one block of 32 warps.  Warp w owns the
-// contiguous chunk [w*C, (w+1)*C) and walks it 32 entries at a time with
-// coalesced loads and warp shuffles; a scan of the 32 chunk totals gives each
-// warp its base.
-__global__ void __launch_bounds__(1024) k_scan(uint32_t *__restrict__ data, uint32_t m, unsigned *lc)
+// Exclusive scan of each digit's row of tile counts, one block per digit: row d of the
+// digit-major histogram (num_tiles entries) becomes the per-tile offsets within digit d,
+// and dtot[d] receives the row total.  Each thread scans a contiguous chunk serially; a
+// block scan of the chunk totals gives each chunk its base.
+__global__ void __launch_bounds__(kSortThreads) k_scan_rows(uint32_t *__restrict__ hist, uint32_t num_tiles,
+                                                           uint32_t *__restrict__ dtot, unsigned *lc)
 {
     count_launch(lc);
-    __shared__ uint32_t tot[32];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t C = ((m + 31) / 32 + 31) / 32 * 32;   // chunk per warp, multiple of 32
-    const uint32_t lo = min((uint32_t)warp * C, m), hi = min(lo + C, m);
+    __shared__ uint32_t wsum[kWarps];
+    uint32_t *row = hist + (size_t)blockIdx.x * num_tiles;
+    const uint32_t per = (num_tiles + kSortThreads - 1) / kSortThreads;
+    const uint32_t lo = min(threadIdx.x * per, num_tiles), hi = min(lo + per, num_tiles);
     uint32_t s = 0;
-    for (uint32_t i = lo + lane; i < hi; i += 32) s += data[i];
+    for (uint32_t i = lo; i < hi; i++) s += row[i];
+    // block-wide exclusive scan of the chunk totals
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t v = s;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) tot[warp] = s;
-    __syncthreads();
-    if (warp == 0) {
-        uint32_t v = tot[lane];
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t u = __shfl_up_sync(0xffffffffu, v, o);
-            if (lane >= o) v += u;
-        }
-        tot[lane] = v - tot[lane];   // exclusive
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += u;
     }
+    if (lane == 31) wsum[warp] = v;
     __syncthreads();
-    uint32_t run = tot[warp];
-    for (uint32_t base = lo; base < hi; base += 32) {
-        const uint32_t i = base + lane;
-        const uint32_t x = i < hi ? data[i] : 0u;
+    uint32_t wbase = 0;
+    for (int w = 0; w < warp; w++) wbase += wsum[w];
+    uint32_t run = wbase + v - s;
+    for (uint32_t i = lo; i < hi; i++) {
+        const uint32_t x = row[i];
+        row[i] = run;
+        run += x;
+    }
+    if (threadIdx.x == kSortThreads - 1) dtot[blockIdx.x] = wbase + v;
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_scatter(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin,
+                                                         uint32_t *__restrict__ kout, uint32_t *__restrict__ vout,
+                                                         uint32_t n, int shift, const uint32_t *__restrict__ scanned,
+                                                         const uint32_t *__restrict__ dtot, uint32_t num_tiles,
+                                                         unsigned *lc)
+{
+    count_launch(lc);
+    __shared__ uint32_t base[kRadix];
+    __shared__ uint32_t run[kRadix];
+    __shared__ uint32_t wcnt[kWarps][kRadix];
+    __shared__ uint32_t wsum[kWarps];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    // digit base: exclusive scan of the digit totals, then this tile's offset within the digit
+    {
+        const uint32_t x = dtot[t];
         uint32_t v = x;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const uint32_t u = __shfl_up_sync(0xffffffffu, v, o);
             if (lane >= o) v += u;
         }
-        if (i < hi) data[i] = run + v - x;
-        run += __shfl_sync(0xffffffffu, v, 31);
+        if (lane == 31) wsum[warp] = v;
+        __syncthreads();
+        uint32_t wb = 0;
+        for (int w = 0; w < warp; w++) wb += wsum[w];
+        base[t] = wb + v - x + scanned[(size_t)t * num_tiles + blockIdx.x];
     }
-}
-
-__global__ void __launch_bounds__(kSortThreads) k_scatter(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin,
-                                                         uint32_t *__restrict__ kout, uint32_t *__restrict__ vout,
-                                                         uint32_t n, int shift, const uint32_t *__restrict__ scanned,
-                                                         uint32_t num_tiles, unsigned *lc)
-{
-    count_launch(lc);
-    __shared__ uint32_t base[kRadix];
-    __shared__ uint32_t run[kRadix];
-    __shared__ uint32_t wcnt[kWarps][kRadix];
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    base[t] = scanned[(size_t)t * num_tiles + blockIdx.x];
     run[t] = 0;
 #pragma unroll
     for (int w = 0; w < kWarps; w++) wcnt[w][t] = 0;
@@ -130,12 +140,13 @@ bool radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *keys2, uint32_t 
     if (n == 0) return false;
     const uint32_t tiles = (n + kSortTile - 1) / kSortTile;
     (void)num_tiles;
+    uint32_t *dtot = hist + (size_t)kRadix * tiles;   // digit totals after the tile histograms
     bool swapped = false;
     uint32_t *ki = keys, *vi = vals, *ko = keys2, *vo = vals2;
     for (int shift = 0; shift < key_bits; shift += 8) {
         k_hist<<<tiles, kSortThreads, 0, s>>>(ki, n, shift, hist, tiles, lc);
-        k_scan<<<1, 1024, 0, s>>>(hist, kRadix * tiles, lc);
-        k_scatter<<<tiles, kSortThreads, 0, s>>>(ki, vi, ko, vo, n, shift, hist, tiles, lc);
+        k_scan_rows<<<kRadix, kSortThreads, 0, s>>>(hist, tiles, dtot, lc);
+        k_scatter<<<tiles, kSortThreads, 0, s>>>(ki, vi, ko, vo, n, shift, hist, dtot, tiles, lc);
         uint32_t *tk = ki, *tv = vi;
         ki = ko; vi = vo; ko = tk; vo = tv;
         swapped = !swapped;

