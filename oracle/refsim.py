@@ -51,9 +51,12 @@ def available(precision: str = "f64") -> bool:
     return os.path.exists(os.path.join(REF_DIR, f"libref_{precision}.so"))
 
 
-def lib(precision: str = "f64") -> ctypes.CDLL:
-    if precision not in _LIBS:
-        path = os.path.join(REF_DIR, f"libref_{precision}.so")
+def lib(precision: str = "f64", path: str = None) -> ctypes.CDLL:
+    """The reference build of the given precision, or the library at `path` that links the
+    same reference objects and driver (tests of the reference-side plugin)."""
+    key = path or precision
+    if key not in _LIBS:
+        path = path or os.path.join(REF_DIR, f"libref_{precision}.so")
         if not os.path.exists(path):
             raise FileNotFoundError(f"{path} is missing: run oracle/build_ref.sh where the reference tree is present")
         L = ctypes.CDLL(path, mode=ctypes.RTLD_LOCAL)
@@ -72,8 +75,8 @@ def lib(precision: str = "f64") -> ctypes.CDLL:
         L.ref_set_time_step.restype = None
         L.ref_precision.restype = ctypes.c_int
         L.ref_destroy.restype = None
-        _LIBS[precision] = L
-    return _LIBS[precision]
+        _LIBS[key] = L
+    return _LIBS[key]
 
 
 def _dp(a):
@@ -87,10 +90,11 @@ class RefSim:
 
     _alive = False
 
-    def __init__(self, scene, precision: str = "f64", analytic_kernel: bool = True, num_threads: int = 0):
+    def __init__(self, scene, precision: str = "f64", analytic_kernel: bool = True, num_threads: int = 0,
+                 library: str = None):
         if RefSim._alive:
             raise RuntimeError("the reference's Simulation is a singleton: close the other RefSim first")
-        self.L = lib(precision)
+        self.L = lib(precision, library)
         self.n, self.nb = scene.n, scene.nb
         p = scene.params
         rp = RefParams()

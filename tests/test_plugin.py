@@ -1,0 +1,135 @@
+"""The reference-side plugin (splishsplash_gb300/plugin/) compiled against the reference's
+own headers and run inside the reference's own Simulation.
+
+* TimeStepDFSPH_GB300, Viscosity_Weiler2018_GB300 and SimulationGB300 are compiled with the
+  reference's SPlisHSPlasH headers (and the stand-ins of oracle/shims/ for its absent external
+  projects), and linked with the reference's library objects (oracle/build_ref.sh).
+* Linked against the real libsphgb300.so, every C-ABI symbol the plugin calls resolves
+  (link check; running it needs a GPU and the reference tree, which a GPU host here lacks).
+* Linked against tests/plugin/fake_sphgb300.cpp, a CPU stand-in of the same C ABI over the FP64
+  oracle, the plugin drives the reference's Simulation through TimeStep::step(): the scene,
+  parameters, warm starts, velocity differences, step sizes and time pass through the plugin's
+  upload and download, and ten steps of the dam break of config 0 and of a viscous block match
+  the reference's own TimeStepDFSPH step by step (iteration counts equal, fields to 1e-10).
+These tests need the reference tree (SPH_REFERENCE_ROOT) and skip without it.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import ref_cases
+import refsim
+from splishsplash_gb300 import scenes
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PLUGIN = os.path.join(ROOT, "splishsplash_gb300", "plugin")
+OUT = os.path.join(ROOT, "oracle", "_ref", "plugin_test")
+
+
+def reference_tree():
+    env = os.environ.get("SPH_REFERENCE_ROOT")
+    p = env if env else os.path.join(ROOT, "..", "reference")
+    return os.path.abspath(p) if os.path.isfile(os.path.join(p, "SPlisHSPlasH", "TimeStep.cpp")) else None
+
+
+def run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(" ".join(cmd) + "\n" + r.stdout[-3000:] + r.stderr[-3000:])
+
+
+@pytest.fixture(scope="module")
+def builds():
+    tree = reference_tree()
+    if tree is None:
+        pytest.skip("reference tree not present (set SPH_REFERENCE_ROOT)")
+    if not refsim.available("f64"):
+        run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh")])
+    obj_dir = os.path.join(ROOT, "oracle", "_ref", "obj_ref_f64")
+    os.makedirs(OUT, exist_ok=True)
+    inc = ["-include", "cfloat", "-include", "memory", "-I", os.path.join(ROOT, "oracle", "shims"), "-I", tree,
+           "-I", os.path.join(tree, "extern", "eigen"), "-I", os.path.join(tree, "extern"),
+           "-I", os.path.join(ROOT, "include"), "-I", PLUGIN, "-I", os.path.join(ROOT, "oracle")]
+    cxx = ["g++", "-std=c++17", "-O2", "-fPIC", "-fopenmp", "-ffp-contract=off", "-DUSE_DOUBLE", "-w"]
+    objs = {}
+    for name, src in (("plugin", os.path.join(PLUGIN, "TimeStepDFSPH_GB300.cpp")),
+                      ("glue", os.path.join(ROOT, "tests", "plugin", "plugin_glue.cpp")),
+                      ("fake", os.path.join(ROOT, "tests", "plugin", "fake_sphgb300.cpp"))):
+        objs[name] = os.path.join(OUT, name + ".o")
+        run(cxx + inc + ["-c", src, "-o", objs[name]])
+    for name in ("sph_oracle", "vmap"):
+        objs[name] = os.path.join(OUT, name + ".o")
+        run(["gcc", "-std=c11", "-O2", "-fPIC", "-fopenmp", "-ffp-contract=off", "-DORC_REAL=double", "-c",
+             os.path.join(ROOT, "oracle", name + ".c"), "-o", objs[name]])
+    ref_objs = sorted(os.path.join(obj_dir, f) for f in os.listdir(obj_dir) if f.endswith(".o"))
+    lib = os.path.join(OUT, "libplugin_fake_abi.so")
+    run(["g++", "-shared", "-fopenmp", "-Wl,--no-undefined", "-o", lib, *ref_objs, objs["plugin"], objs["glue"],
+         objs["fake"], objs["sph_oracle"], objs["vmap"], "-lm"])
+    return dict(lib=lib, objs=objs, ref_objs=ref_objs)
+
+
+def test_plugin_links_against_the_c_abi(builds):
+    """Every sphgb_* symbol the plugin calls is exported by the real libsphgb300.so."""
+    from splishsplash_gb300 import build as b
+    if not os.path.exists(b.LIB):
+        pytest.skip("libsphgb300.so not built")
+    out = os.path.join(OUT, "libplugin_gb300.so")
+    run(["g++", "-shared", "-fopenmp", "-Wl,--no-undefined", "-o", out, *builds["ref_objs"], builds["objs"]["plugin"],
+         builds["objs"]["glue"], "-L", os.path.dirname(b.LIB), "-lsphgb300", "-lm"])
+    assert os.path.exists(out)
+
+
+def plugin_run(lib_path, scene, steps):
+    L = refsim.lib("f64", lib_path)
+    L.plugin_use_gb300_simulation.restype = ctypes.c_int
+    L.plugin_install.restype = ctypes.c_int
+    L.plugin_destroy.restype = None
+    assert L.plugin_use_gb300_simulation() == 0
+    r = refsim.RefSim(scene, library=lib_path)
+    try:
+        assert L.plugin_install() == 0
+        return [r.step() for _ in range(steps)], fields(r, scene)
+    finally:
+        L.plugin_destroy()
+        refsim.RefSim._alive = False
+
+
+def reference_run(scene, steps):
+    with refsim.RefSim(scene) as r:
+        return [r.step() for _ in range(steps)], fields(r, scene)
+
+
+def fields(r, scene):
+    f = dict(density=r.get("density"), factor=r.get("factor"), kappa=r.get("p / rho^2"),
+             kappa_v=r.get("p_v / rho^2"), v=r.get("velocity"), x=r.get("position"))
+    if scene.params.viscosityMethod == 6:
+        f["vdiff"] = r.get("velocity difference")
+    return f
+
+
+def viscous_block():
+    sc = scenes.small_block(counts=(8, 12, 8), box=(0.5, 0.9, 0.5), viscosity=True)
+    sc.v[:, 0] = sc.x[:, 1] - sc.x[:, 1].mean()
+    sc.params.viscosity = 0.5
+    return sc.as_float32()
+
+
+@pytest.mark.parametrize("name", ["dambreak_8k", "viscous_block"])
+def test_plugin_steps_match_reference_time_step(builds, name):
+    scene = scenes.dambreak_8k().as_float32() if name == "dambreak_8k" else viscous_block()
+    steps = 10
+    st_p, f_p = plugin_run(builds["lib"], scene, steps)
+    st_r, f_r = reference_run(scene, steps)
+    for k, (a, b) in enumerate(zip(st_p, st_r)):
+        assert (a["iterations"], a["iterations_v"], a["visco_iterations"]) == \
+            (b["iterations"], b["iterations_v"], b["visco_iterations"]), k
+        assert a["dt"] == pytest.approx(b["dt"], rel=1e-12)
+        assert a["time"] == pytest.approx(b["time"], rel=1e-12)
+    err = ref_cases.field_errors(f_p, f_r)
+    for k, e in err.items():
+        assert e <= 1e-10 * (np.max(np.abs(f_r["x"])) if k == "x" else 1.0), (name, k, e)
+    if name == "viscous_block":
+        assert max(s["visco_iterations"] for s in st_r) > 0
