@@ -127,6 +127,10 @@ typedef struct sphgb_stats {
 #define SPHGB_FIELD_FEATURES 16                /* warm-start network inputs of the last step (n x 10) */
 #define SPHGB_FIELD_POSITION_HI 17             /* position as stored: the high part of the FP32 double-float
                                                   position (FP64 mode: the position), 3 */
+#define SPHGB_FIELD_STATE 19                   /* FluidModel "state" (ParticleState, FluidModel.cpp:62), uint32:
+                                                  0 = Active for every particle the device steps */
+#define SPHGB_FIELD_OBJECT_ID 20               /* FluidModel "object_id" (FluidModel.cpp:63), uint32: 0 (the
+                                                  device keeps no object ids) */
 #define SPHGB_FIELD_POSITION_LO 18             /* the low part of the FP32 double-float position (FP64 mode:
                                                   zero); HI + LO = "position" exactly, 3 */
 
@@ -214,6 +218,24 @@ int sphgb_field_id(const char *name);
  * for bit as if the context had not been interrupted. */
 int sphgb_save_state(sphgb_ctx *ctx, const char *path);
 int sphgb_load_state(sphgb_ctx *ctx, const char *path);
+/* The particle file of the reference's state (SimulatorBase::writeFluidParticlesState,
+ * Simulator/SimulatorBase.cpp:2062-2127, called per fluid model by saveState :1689-1770): a
+ * partio BGEO file holding the fluid model's fields that the reference marks storeData, under
+ * their names, in particle-id order: "id", "state", "object_id", "position", "velocity",
+ * "p / rho^2", "p_v / rho^2" and, with Weiler2018 viscosity, "velocity difference"
+ * (FluidModel.cpp:61-66, TimeStepDFSPH.cpp:51-52, Viscosity_Weiler2018.cpp:33); values as 32-bit
+ * floats and ints, as the reference stores them.  level as for sphgb_export_bgeo (the reference
+ * writes it compressed).  The time and step size of the state are sphgb_get_time_step and the
+ * last step's time; the simulator-level part of the reference's .bin state file stays the
+ * simulator's.  One fluid model, one scene. */
+int sphgb_save_particle_state(sphgb_ctx *ctx, const char *path, int level);
+/* Reads such a file (SimulatorBase::readFluidParticlesState, :2130-2192), plain or compressed:
+ * every attribute named like a field of this path -- "position", "velocity", "p / rho^2",
+ * "p_v / rho^2", "velocity difference" -- is set for the particle whose "id" the record carries
+ * (record order when there is no "id").  The file must hold as many points as the context has
+ * fluid particles, and a "state" attribute must mark every particle Active (0).  The boundary,
+ * the parameters and the step size stay as they are. */
+int sphgb_load_particle_state(sphgb_ctx *ctx, const char *path);
 
 /* counts (all scenes of a batch) */
 int sphgb_num_particles(const sphgb_ctx *ctx, uint32_t *n, uint32_t *nb);
@@ -293,8 +315,11 @@ int sphgb_set_feature_output(sphgb_ctx *ctx, int on);
  * nb <= SPHGB_NOALLOC_MAX_BOUNDARY (else SPHGB_ERR_CAPACITY) and at most
  * SPHGB_NOALLOC_MAX_CELLS grid cells of 1.001 x 4 r (else SPHGB_ERR_GRID).  The first call on a
  * device looks up the scratch address (cudaGetSymbolAddress) and should be made before any
- * stream capture.  Calls share the scratch: calls that overlap on the GPU (other streams,
- * other host threads) race; serialise them.  Returns without waiting for the GPU. */
+ * stream capture; the address is looked up through the CUDA runtime, so it is that of the
+ * device's primary context (callers on a non-primary driver-API context of the same device are
+ * not supported).  Calls share the scratch: calls that overlap on the GPU (other streams,
+ * other host threads) race; serialise them.  Non-finite box values or radius:
+ * SPHGB_ERR_ARGUMENT.  Returns without waiting for the GPU. */
 #define SPHGB_NOALLOC_MAX_BOUNDARY 65536
 #define SPHGB_NOALLOC_MAX_CELLS 262144
 int sphgb_boundary_volume_noalloc(const float *xb, uint32_t nb, double particle_radius,

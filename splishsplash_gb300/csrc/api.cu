@@ -2486,7 +2486,7 @@ int sphgb_num_particles(const sphgb_ctx *c, uint32_t *n, uint32_t *nb)
 int sphgb_download(sphgb_ctx *c, int field, void *dst, int dtype)
 {
     if (!c || !dst) return SPHGB_ERR_ARGUMENT;
-    if (field < 0 || field > SPHGB_FIELD_POSITION_LO) return fail(c, SPHGB_ERR_ARGUMENT, "unknown field");
+    if (field < 0 || field > SPHGB_FIELD_OBJECT_ID) return fail(c, SPHGB_ERR_ARGUMENT, "unknown field");
     if (field == SPHGB_FIELD_FEATURES && !c->mlp_x) return fail(c, SPHGB_ERR_STATE, "features are not computed");
     if (dtype < SPHGB_DTYPE_F32 || dtype > SPHGB_DTYPE_U32) return fail(c, SPHGB_ERR_ARGUMENT, "unknown dtype");
     if (!c->have_fluid) return fail(c, SPHGB_ERR_STATE, "no fluid uploaded");
@@ -2613,13 +2613,16 @@ const char *field_name(int f)
     case SPHGB_FIELD_FEATURES: return "features";
     case SPHGB_FIELD_POSITION_HI: return "position high";
     case SPHGB_FIELD_POSITION_LO: return "position low";
+    case SPHGB_FIELD_STATE: return "state";
+    case SPHGB_FIELD_OBJECT_ID: return "object_id";
     default: return nullptr;
     }
 }
 
 bool is_uint_field(int f)
 {
-    return f == SPHGB_FIELD_PARTICLE_ID || f == SPHGB_FIELD_NUM_FLUID_NEIGHBORS || f == SPHGB_FIELD_NUM_BOUNDARY_NEIGHBORS;
+    return f == SPHGB_FIELD_PARTICLE_ID || f == SPHGB_FIELD_NUM_FLUID_NEIGHBORS || f == SPHGB_FIELD_NUM_BOUNDARY_NEIGHBORS ||
+           f == SPHGB_FIELD_STATE || f == SPHGB_FIELD_OBJECT_ID;
 }
 
 std::string vtk_name(const char *name)
@@ -2807,7 +2810,7 @@ int sphgb_export_vtk(sphgb_ctx *c, const char *path, const int *fields, uint32_t
 int sphgb_field_id(const char *name)
 {
     if (!name) return -1;
-    for (int f = 0; f <= SPHGB_FIELD_POSITION_LO; f++) {
+    for (int f = 0; f <= SPHGB_FIELD_OBJECT_ID; f++) {
         const char *fn = field_name(f);
         if (fn && std::strcmp(fn, name) == 0) return f;
     }
@@ -3114,6 +3117,79 @@ int sphgb_load_state(sphgb_ctx *c, const char *path)
     c->dt = c->scn[0].dt;
     c->scalars_dirty = true;
     invalidate_graphs(c);
+    return SPHGB_OK;
+}
+
+int sphgb_save_particle_state(sphgb_ctx *c, const char *path, int level)
+{
+    if (!c || !path) return SPHGB_ERR_ARGUMENT;
+    if (!c->have_fluid) return fail(c, SPHGB_ERR_STATE, "no fluid uploaded");
+    if (c->nscenes() != 1 || c->phase_counts.size() > 1)
+        return fail(c, SPHGB_ERR_STATE, "a particle state file holds one fluid model of one scene");
+    // the storeData fields of FluidModel, TimeStepDFSPH and Viscosity_Weiler2018, in that order
+    // (FluidModel.cpp:61-66, TimeStepDFSPH.cpp:51-52, Viscosity_Weiler2018.cpp:33); the position
+    // and "id" are the exporter's first attributes
+    std::vector<int> fields = {SPHGB_FIELD_STATE, SPHGB_FIELD_OBJECT_ID, SPHGB_FIELD_VELOCITY,
+                               SPHGB_FIELD_PRESSURE_RHO2, SPHGB_FIELD_PRESSURE_RHO2_V};
+    if (c->prm.viscosity_method == 6) fields.push_back(SPHGB_FIELD_VDIFF);
+    return sphgb_export_bgeo(c, path, fields.data(), (uint32_t)fields.size(), level, 1);
+}
+
+int sphgb_load_particle_state(sphgb_ctx *c, const char *path)
+{
+    if (!c || !path) return SPHGB_ERR_ARGUMENT;
+    if (!c->have_fluid) return fail(c, SPHGB_ERR_STATE, "no fluid uploaded");
+    if (c->nscenes() != 1 || c->phase_counts.size() > 1)
+        return fail(c, SPHGB_ERR_STATE, "a particle state file holds one fluid model of one scene");
+    BgeoPoints pts;
+    std::string err;
+    int rc = read_bgeo_file(path, pts, err);
+    if (rc) return fail(c, rc, err.c_str());
+    const uint32_t n = c->n;
+    if (pts.n != n) return fail(c, SPHGB_ERR_ARGUMENT, "the file's point count differs from the fluid's");
+    // record r -> particle id (the "id" attribute; the record order without one)
+    std::vector<uint32_t> id(n);
+    for (uint32_t r = 0; r < n; r++) id[r] = r;
+    auto find = [&](const char *name, uint32_t comps, bool integer) -> const std::vector<uint32_t> * {
+        for (size_t a = 0; a < pts.attrs.size(); a++)
+            if (pts.attrs[a].name == name && pts.attrs[a].comps == comps && pts.attrs[a].integer == integer)
+                return &pts.values[a];
+        return nullptr;
+    };
+    if (const std::vector<uint32_t> *ids = find("id", 1, true)) {
+        std::vector<char> seen(n, 0);
+        for (uint32_t r = 0; r < n; r++) {
+            const uint32_t d = (*ids)[r];
+            if (d >= n || seen[d]) return fail(c, SPHGB_ERR_ARGUMENT, "the file's ids are not a permutation of 0 .. n-1");
+            seen[d] = 1;
+            id[r] = d;
+        }
+    }
+    if (const std::vector<uint32_t> *state = find("state", 1, true))
+        for (uint32_t r = 0; r < n; r++)
+            if ((*state)[r] != 0u) return fail(c, SPHGB_ERR_ARGUMENT, "only Active particles (state 0) are supported");
+    std::vector<double> buf;
+    auto put = [&](int field, const std::vector<uint32_t> &v, uint32_t comps) -> int {
+        buf.assign((size_t)n * comps, 0.0);
+        for (uint32_t r = 0; r < n; r++)
+            for (uint32_t k = 0; k < comps; k++) {
+                float x;
+                std::memcpy(&x, &v[(size_t)r * comps + k], 4);
+                buf[(size_t)id[r] * comps + k] = (double)x;
+            }
+        return sphgb_upload_field(c, field, buf.data(), SPHGB_DTYPE_F64);
+    };
+    {
+        std::vector<uint32_t> pos(pts.position.size());
+        std::memcpy(pos.data(), pts.position.data(), pos.size() * 4);
+        if ((rc = put(SPHGB_FIELD_POSITION, pos, 3))) return rc;
+    }
+    const struct { const char *name; int field; uint32_t comps; } map[] = {
+        {"velocity", SPHGB_FIELD_VELOCITY, 3}, {"p / rho^2", SPHGB_FIELD_PRESSURE_RHO2, 1},
+        {"p_v / rho^2", SPHGB_FIELD_PRESSURE_RHO2_V, 1}, {"velocity difference", SPHGB_FIELD_VDIFF, 3}};
+    for (const auto &m : map)
+        if (const std::vector<uint32_t> *v = find(m.name, m.comps, false))
+            if ((rc = put(m.field, *v, m.comps))) return rc;
     return SPHGB_OK;
 }
 

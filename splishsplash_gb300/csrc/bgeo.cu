@@ -1,9 +1,10 @@
 // Partio BGEO particle files: the record packing on the device and the file writer.
 //
 // The layout is the one partio's BGEO writer produces for the reference's
-// ParticleExporter_Partio (Simulator/Exporter/ParticleExporter_Partio.cpp:67-201); partio
-// itself is not part of the reference tree, so its published format is restated here.  All
-// numbers are big-endian:
+// ParticleExporter_Partio (Simulator/Exporter/ParticleExporter_Partio.cpp:67-201) and its
+// particle state files (Simulator/SimulatorBase.cpp:2062-2192); partio is vendored in the
+// reference tree (extern/partio), and the format is restated here in this project's own code.
+// All numbers are big-endian:
 //   int32 magic "Bgeo", char 'V', int32 version 5, int32 points, primitives 0, point groups 0,
 //   primitive groups 0, point attributes, vertex attributes 0, primitive attributes 0,
 //   detail attributes 0;
@@ -136,7 +137,12 @@ struct ZlibApi {
     uLong (*deflate_bound)(z_streamp, uLong) = nullptr;
     uLong (*crc)(uLong, const Bytef *, uInt) = nullptr;
     uLong (*crc_combine)(uLong, uLong, z_off_t) = nullptr;
+    int (*inflate_init2)(z_streamp, int, const char *, int) = nullptr;
+    int (*inflate_)(z_streamp, int) = nullptr;
+    int (*inflate_end)(z_streamp) = nullptr;
+    int (*inflate_reset)(z_streamp) = nullptr;
     bool ok = false;
+    bool inflate_ok = false;
 };
 
 const ZlibApi &zlib_api()
@@ -153,6 +159,11 @@ const ZlibApi &zlib_api()
         a.crc = reinterpret_cast<decltype(a.crc)>(dlsym(h, "crc32"));
         a.crc_combine = reinterpret_cast<decltype(a.crc_combine)>(dlsym(h, "crc32_combine"));
         a.ok = a.deflate_init2 && a.deflate_ && a.deflate_end && a.deflate_bound && a.crc && a.crc_combine;
+        a.inflate_init2 = reinterpret_cast<decltype(a.inflate_init2)>(dlsym(h, "inflateInit2_"));
+        a.inflate_ = reinterpret_cast<decltype(a.inflate_)>(dlsym(h, "inflate"));
+        a.inflate_end = reinterpret_cast<decltype(a.inflate_end)>(dlsym(h, "inflateEnd"));
+        a.inflate_reset = reinterpret_cast<decltype(a.inflate_reset)>(dlsym(h, "inflateReset"));
+        a.inflate_ok = a.inflate_init2 && a.inflate_ && a.inflate_end && a.inflate_reset;
         return a;
     }();
     return api;
@@ -281,6 +292,159 @@ int write_bgeo_file(const std::string &path, const void *records, uint32_t n, ui
     if (!ok) {
         err = "export: write failed for " + path;
         return SPHGB_ERR_ARGUMENT;
+    }
+    return SPHGB_OK;
+}
+
+namespace {
+
+// the gzip members of a file, inflated one after another (zlib detects each gzip header)
+bool gunzip_all(const std::vector<unsigned char> &in, std::vector<unsigned char> &out, std::string &err)
+{
+#if SPHGB_HAVE_ZLIB
+    const ZlibApi &z = zlib_api();
+    if (!z.inflate_ok) {
+        err = "reading a compressed BGEO needs zlib (libz.so.1), which could not be loaded";
+        return false;
+    }
+    z_stream s;
+    std::memset(&s, 0, sizeof s);
+    if (z.inflate_init2(&s, 15 + 16, ZLIB_VERSION, (int)sizeof(z_stream)) != Z_OK) {
+        err = "inflateInit2 failed";
+        return false;
+    }
+    s.next_in = const_cast<Bytef *>(in.data());
+    s.avail_in = (uInt)in.size();
+    std::vector<unsigned char> buf(1u << 20);
+    bool ok = true;
+    while (true) {
+        s.next_out = buf.data();
+        s.avail_out = (uInt)buf.size();
+        const int r = z.inflate_(&s, Z_NO_FLUSH);
+        out.insert(out.end(), buf.data(), buf.data() + (buf.size() - s.avail_out));
+        if (r == Z_STREAM_END) {
+            if (s.avail_in == 0) break;
+            z.inflate_reset(&s);   // another member follows
+            continue;
+        }
+        if (r != Z_OK && r != Z_BUF_ERROR) { ok = false; break; }
+        if (r == Z_BUF_ERROR && s.avail_in == 0) { ok = false; break; }
+    }
+    z.inflate_end(&s);
+    if (!ok) err = "corrupt gzip data";
+    return ok;
+#else
+    (void)in;
+    (void)out;
+    err = "reading a compressed BGEO needs zlib, which this build does not have";
+    return false;
+#endif
+}
+
+struct BeReader {
+    const unsigned char *p, *end;
+    bool ok = true;
+    uint32_t u32()
+    {
+        if (end - p < 4) { ok = false; return 0; }
+        const uint32_t v = ((uint32_t)p[0] << 24) | ((uint32_t)p[1] << 16) | ((uint32_t)p[2] << 8) | p[3];
+        p += 4;
+        return v;
+    }
+    uint16_t u16()
+    {
+        if (end - p < 2) { ok = false; return 0; }
+        const uint16_t v = (uint16_t)((p[0] << 8) | p[1]);
+        p += 2;
+        return v;
+    }
+    uint8_t u8()
+    {
+        if (end - p < 1) { ok = false; return 0; }
+        return *p++;
+    }
+    std::string str()
+    {
+        const uint16_t len = u16();
+        if (!ok || end - p < len) { ok = false; return {}; }
+        std::string s(reinterpret_cast<const char *>(p), len);
+        p += len;
+        return s;
+    }
+};
+
+}  // namespace
+
+int read_bgeo_file(const std::string &path, BgeoPoints &out, std::string &err)
+{
+    FILE *f = fopen(path.c_str(), "rb");
+    if (!f) {
+        err = "cannot open " + path;
+        return SPHGB_ERR_ARGUMENT;
+    }
+    std::vector<unsigned char> raw;
+    unsigned char chunk[1 << 16];
+    for (size_t got; (got = fread(chunk, 1, sizeof chunk, f)) > 0;) raw.insert(raw.end(), chunk, chunk + got);
+    fclose(f);
+    std::vector<unsigned char> plain;
+    if (raw.size() >= 2 && raw[0] == 0x1f && raw[1] == 0x8b) {
+        if (!gunzip_all(raw, plain, err)) return SPHGB_ERR_ARGUMENT;
+    } else {
+        plain.swap(raw);
+    }
+    BeReader r{plain.data(), plain.data() + plain.size()};
+    const uint32_t magic = r.u32();
+    const uint8_t vchar = r.u8();
+    const uint32_t version = r.u32();
+    if (!r.ok || magic != 0x4267656fu || vchar != 'V' || version != 5u) {
+        err = path + " is not a version-5 BGEO file";
+        return SPHGB_ERR_ARGUMENT;
+    }
+    const uint32_t npoints = r.u32(), nprims = r.u32(), npgroups = r.u32(), nprgroups = r.u32();
+    const uint32_t npattr = r.u32(), nvattr = r.u32(), nprattr = r.u32(), ndetail = r.u32();
+    (void)npgroups;
+    (void)nprgroups;
+    (void)nvattr;
+    (void)nprattr;
+    (void)ndetail;
+    if (!r.ok || nprims != 0) {
+        err = path + ": not a particle file (primitives present)";
+        return SPHGB_ERR_ARGUMENT;
+    }
+    out = BgeoPoints{};
+    out.n = npoints;
+    uint32_t words = 4;   // x, y, z, w
+    for (uint32_t a = 0; a < npattr; a++) {
+        BgeoAttr at;
+        at.name = r.str();
+        at.comps = r.u16();
+        const uint32_t type = r.u32();
+        if (!r.ok || (type != 0 && type != 1 && type != 5)) {
+            err = path + ": unsupported point attribute type (only float, int and vector)";
+            return SPHGB_ERR_ARGUMENT;
+        }
+        at.integer = type == 1;
+        for (uint32_t k = 0; k < at.comps; k++) r.u32();   // defaults
+        out.attrs.push_back(at);
+        words += at.comps;
+    }
+    if (!r.ok || (size_t)(r.end - r.p) < (size_t)npoints * words * 4u) {
+        err = path + ": truncated point data";
+        return SPHGB_ERR_ARGUMENT;
+    }
+    out.position.resize((size_t)npoints * 3);
+    out.values.assign(out.attrs.size(), {});
+    for (size_t a = 0; a < out.attrs.size(); a++) out.values[a].resize((size_t)npoints * out.attrs[a].comps);
+    for (uint32_t i = 0; i < npoints; i++) {
+        for (int d = 0; d < 3; d++) {
+            const uint32_t w = r.u32();
+            float x;
+            std::memcpy(&x, &w, 4);
+            out.position[(size_t)i * 3 + d] = x;
+        }
+        r.u32();   // homogeneous coordinate
+        for (size_t a = 0; a < out.attrs.size(); a++)
+            for (uint32_t k = 0; k < out.attrs[a].comps; k++) out.values[a][(size_t)i * out.attrs[a].comps + k] = r.u32();
     }
     return SPHGB_OK;
 }

@@ -39,4 +39,17 @@ int write_bgeo_file(const std::string &path, const void *records, uint32_t n, ui
 // whether zlib could be loaded (levels 1-9 need it)
 bool bgeo_compression_available();
 
+// the points of a BGEO particle file: positions and every point attribute (host-order words)
+struct BgeoPoints {
+    uint32_t n = 0;
+    std::vector<float> position;                 // n x 3
+    std::vector<BgeoAttr> attrs;                 // besides the position, in file order
+    std::vector<std::vector<uint32_t>> values;   // per attribute: n x comps words (float or int bits)
+};
+
+// Reads a version-5 BGEO particle file, plain or gzip-compressed (any number of members), as
+// partio's reader does for point attributes of type float, int and vector.  Detail attributes
+// after the points are not read.  Returns an SPHGB status; err gets the message.
+int read_bgeo_file(const std::string &path, BgeoPoints &out, std::string &err);
+
 }  // namespace sphgb

@@ -39,6 +39,8 @@ FIELDS = {
     "features": (16, 10),
     "position high": (17, 3),
     "position low": (18, 3),
+    "state": (19, 1),
+    "object_id": (20, 1),
 }
 DTYPE_F32, DTYPE_F64, DTYPE_U32 = 0, 1, 2
 
@@ -128,7 +130,7 @@ EXPORTS = [
     "sphgb_add_volume_map", "sphgb_add_volume_map_values", "sphgb_get_volume_map", "sphgb_clear_volume_maps",
     "sphgb_set_boundary_method", "sphgb_set_volume_map_motion", "sphgb_set_body_motion", "sphgb_set_fluid_phases",
     "sphgb_set_fluid_phase_viscosity", "sphgb_set_fluid_phase_xsph",
-    "sphgb_set_volume_map_scene",
+    "sphgb_set_volume_map_scene", "sphgb_save_particle_state", "sphgb_load_particle_state",
 ]
 
 _lib = None
@@ -185,6 +187,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.sphgb_field_id.argtypes = [ctypes.c_char_p]
     L.sphgb_save_state.argtypes = [vp, ctypes.c_char_p]
     L.sphgb_load_state.argtypes = [vp, ctypes.c_char_p]
+    L.sphgb_save_particle_state.argtypes = [vp, ctypes.c_char_p, i32]
+    L.sphgb_load_particle_state.argtypes = [vp, ctypes.c_char_p]
     L.sphgb_set_boundary_bodies.argtypes = [vp, vp, u32, vp, vp]
     L.sphgb_boundary_forces.argtypes = [vp, vp, vp]
     L.sphgb_clear_boundary_forces.argtypes = [vp, i32]
@@ -441,7 +445,7 @@ class Context:
         fid, comp = FIELDS[name]
         n, nb = self.num_particles()
         m = nb if name.startswith("boundary") and name != "boundary neighbors" else n
-        if name in ("id", "fluid neighbors", "boundary neighbors"):
+        if name in ("id", "fluid neighbors", "boundary neighbors", "state", "object_id"):
             dtype = np.uint32
         if out is None:
             out = np.zeros((m, comp) if comp > 1 else (m,), dtype=dtype)
@@ -648,6 +652,16 @@ class Context:
 
     def save_state(self, path: str):
         self._check(self.L.sphgb_save_state(self.h, os.fsencode(path)))
+
+    def save_particle_state(self, path: str, level: int = -1):
+        """The reference's per-fluid-model state file (SimulatorBase::writeFluidParticlesState):
+        partio BGEO with id, state, object_id, position, velocity, p / rho^2, p_v / rho^2 and,
+        with Weiler2018, velocity difference."""
+        self._check(self.L.sphgb_save_particle_state(self.h, os.fsencode(path), int(level)))
+
+    def load_particle_state(self, path: str):
+        """Reads such a file (SimulatorBase::readFluidParticlesState) into the fluid, by id."""
+        self._check(self.L.sphgb_load_particle_state(self.h, os.fsencode(path)))
 
     def load_state(self, path: str):
         self._check(self.L.sphgb_load_state(self.h, os.fsencode(path)))

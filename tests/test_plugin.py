@@ -15,71 +15,35 @@ These tests need the reference tree (SPH_REFERENCE_ROOT) and skip without it.
 """
 import ctypes
 import os
-import subprocess
 
 import numpy as np
 import pytest
 
 import ref_cases
+import refbuild
 import refsim
 from splishsplash_gb300 import scenes
 
-ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-PLUGIN = os.path.join(ROOT, "splishsplash_gb300", "plugin")
-OUT = os.path.join(ROOT, "oracle", "_ref", "plugin_test")
 
-
-def reference_tree():
-    env = os.environ.get("SPH_REFERENCE_ROOT")
-    p = env if env else os.path.join(ROOT, "..", "reference")
-    return os.path.abspath(p) if os.path.isfile(os.path.join(p, "SPlisHSPlasH", "TimeStep.cpp")) else None
-
-
-def run(cmd):
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(" ".join(cmd) + "\n" + r.stdout[-3000:] + r.stderr[-3000:])
+@pytest.fixture(scope="module")
+def tree():
+    t = refbuild.reference_tree()
+    if t is None:
+        pytest.skip("reference tree not present (set SPH_REFERENCE_ROOT)")
+    return t
 
 
 @pytest.fixture(scope="module")
-def builds():
-    tree = reference_tree()
-    if tree is None:
-        pytest.skip("reference tree not present (set SPH_REFERENCE_ROOT)")
-    if not refsim.available("f64"):
-        run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh")])
-    obj_dir = os.path.join(ROOT, "oracle", "_ref", "obj_ref_f64")
-    os.makedirs(OUT, exist_ok=True)
-    inc = ["-include", "cfloat", "-include", "memory", "-I", os.path.join(ROOT, "oracle", "shims"), "-I", tree,
-           "-I", os.path.join(tree, "extern", "eigen"), "-I", os.path.join(tree, "extern"),
-           "-I", os.path.join(ROOT, "include"), "-I", PLUGIN, "-I", os.path.join(ROOT, "oracle")]
-    cxx = ["g++", "-std=c++17", "-O2", "-fPIC", "-fopenmp", "-ffp-contract=off", "-DUSE_DOUBLE", "-w"]
-    objs = {}
-    for name, src in (("plugin", os.path.join(PLUGIN, "TimeStepDFSPH_GB300.cpp")),
-                      ("glue", os.path.join(ROOT, "tests", "plugin", "plugin_glue.cpp")),
-                      ("fake", os.path.join(ROOT, "tests", "plugin", "fake_sphgb300.cpp"))):
-        objs[name] = os.path.join(OUT, name + ".o")
-        run(cxx + inc + ["-c", src, "-o", objs[name]])
-    for name in ("sph_oracle", "vmap"):
-        objs[name] = os.path.join(OUT, name + ".o")
-        run(["gcc", "-std=c11", "-O2", "-fPIC", "-fopenmp", "-ffp-contract=off", "-DORC_REAL=double", "-c",
-             os.path.join(ROOT, "oracle", name + ".c"), "-o", objs[name]])
-    ref_objs = sorted(os.path.join(obj_dir, f) for f in os.listdir(obj_dir) if f.endswith(".o"))
-    lib = os.path.join(OUT, "libplugin_fake_abi.so")
-    run(["g++", "-shared", "-fopenmp", "-Wl,--no-undefined", "-o", lib, *ref_objs, objs["plugin"], objs["glue"],
-         objs["fake"], objs["sph_oracle"], objs["vmap"], "-lm"])
-    return dict(lib=lib, objs=objs, ref_objs=ref_objs)
+def fake_lib(tree):
+    return refbuild.plugin_fake_abi(tree)
 
 
-def test_plugin_links_against_the_c_abi(builds):
+def test_plugin_links_against_the_c_abi(tree):
     """Every sphgb_* symbol the plugin calls is exported by the real libsphgb300.so."""
     from splishsplash_gb300 import build as b
     if not os.path.exists(b.LIB):
         pytest.skip("libsphgb300.so not built")
-    out = os.path.join(OUT, "libplugin_gb300.so")
-    run(["g++", "-shared", "-fopenmp", "-Wl,--no-undefined", "-o", out, *builds["ref_objs"], builds["objs"]["plugin"],
-         builds["objs"]["glue"], "-L", os.path.dirname(b.LIB), "-lsphgb300", "-lm"])
-    assert os.path.exists(out)
+    assert os.path.exists(refbuild.link_plugin_against(tree, os.path.dirname(b.LIB)))
 
 
 def plugin_run(lib_path, scene, steps):
@@ -118,10 +82,10 @@ def viscous_block():
 
 
 @pytest.mark.parametrize("name", ["dambreak_8k", "viscous_block"])
-def test_plugin_steps_match_reference_time_step(builds, name):
+def test_plugin_steps_match_reference_time_step(fake_lib, name):
     scene = scenes.dambreak_8k().as_float32() if name == "dambreak_8k" else viscous_block()
     steps = 10
-    st_p, f_p = plugin_run(builds["lib"], scene, steps)
+    st_p, f_p = plugin_run(fake_lib, scene, steps)
     st_r, f_r = reference_run(scene, steps)
     for k, (a, b) in enumerate(zip(st_p, st_r)):
         assert (a["iterations"], a["iterations_v"], a["visco_iterations"]) == \
