@@ -324,16 +324,13 @@ template <class T> __device__ __forceinline__ uint32_t local_cell(const SceneDev
 // block-wide max of two counters, one atomic per block (all threads of the block call it)
 __device__ __forceinline__ void block_max_atomic(uint32_t a, uint32_t b, unsigned *da, unsigned *db)
 {
-    __shared__ uint32_t sa[32], sb[32];
+    // per warp, without a block barrier (the warps of the list build finish at very different
+    // times); the atomic only where the warp's maximum exceeds the value already there
     a = __reduce_max_sync(0xffffffffu, a);
     b = __reduce_max_sync(0xffffffffu, b);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) { sa[warp] = a; sb[warp] = b; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int w = 1; w < (int)(blockDim.x >> 5); w++) { a = max(a, sa[w]); b = max(b, sb[w]); }
-        atomicMax(da, a);
-        atomicMax(db, b);
+    if ((threadIdx.x & 31) == 0) {
+        if (a > __ldcg(da)) atomicMax(da, a);
+        if (b > __ldcg(db)) atomicMax(db, b);
     }
 }
 
@@ -1103,9 +1100,14 @@ __device__ __forceinline__ void solver_decide(const DevParams<T> &P, StepScalars
 // divergenceSolveIteration (TimeStepDFSPH.cpp:621-706) / pressureSolveIteration (:544-619):
 // Jacobi update of kappa_v / kappa plus the FP64 average-error reduction and the
 // loop decision (the while conditions of :477 and :324), per scene.
+// resident blocks per SM the FP32 one-lane Jacobi pass is compiled for (a register cap of 40):
+// measured 0.6 % faster per step on the 1M dam break than the unconstrained 44 registers (5 blocks)
+template <class T, int LPP> constexpr int kJacobiMinBlocks = (sizeof(T) == 4 && LPP == 1) ? 6 : 1;
+
 template <class T, bool DIV, int LPP>
-__global__ void __launch_bounds__(kBlock) k_jacobi(DevParams<T> P, DevBufs<T> B, cudaGraphConditionalHandle handle,
-                                                     int use_handle, int phase)
+__global__ void __launch_bounds__(kBlock, kJacobiMinBlocks<T, LPP>) k_jacobi(DevParams<T> P, DevBufs<T> B,
+                                                                           cudaGraphConditionalHandle handle,
+                                                                           int use_handle, int phase)
 {
     count_launch(&B.gsc->launches);
     SlotInfo q = slot_info<LPP>(P);
@@ -2552,6 +2554,10 @@ __global__ void k_scatter_field(DevParams<T> P, DevBufs<T> B, int field, void *o
             for (int c = 0; c < 10; c++) put<T>(out, odt, 10 * (size_t)d + c, (double)B.mlp_x[(size_t)k * 10 + c]);
         break;
     case SPHGB_FIELD_POSITION_HI: vec(B.x, nullptr); break;
+    case SPHGB_FIELD_STATE:       // every particle the device steps is Active (ParticleState 0)
+    case SPHGB_FIELD_OBJECT_ID:   // the device keeps no object ids
+        put<T>(out, odt, d, 0.0);
+        break;
     case SPHGB_FIELD_POSITION_LO: {
         const float4 l = B.xlo ? B.xlo[k] : make_float4(0.f, 0.f, 0.f, 0.f);
         put<T>(out, odt, 3 * (size_t)d, (double)l.x);

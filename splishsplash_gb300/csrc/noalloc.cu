@@ -103,11 +103,15 @@ extern "C" int sphgb_boundary_volume_noalloc(const float *xb, uint32_t nb, doubl
     int dim[3];
     size_t ncell = 1;
     int maxdim = 1;
+    if (!std::isfinite(particle_radius)) return SPHGB_ERR_ARGUMENT;
     for (int d = 0; d < 3; d++) {
-        if (!(box_max[d] >= box_min[d])) return SPHGB_ERR_ARGUMENT;
+        if (!std::isfinite(box_min[d]) || !std::isfinite(box_max[d]) || !(box_max[d] >= box_min[d]))
+            return SPHGB_ERR_ARGUMENT;
         org[d] = box_min[d] - cell;
-        dim[d] = (int)std::floor((box_max[d] - org[d]) / cell) + 2;
-        if (dim[d] > 1024) return SPHGB_ERR_GRID;
+        // the cell count in double first: an extent far beyond the grid never reaches the int
+        const double cells = std::floor((box_max[d] - org[d]) / cell) + 2.0;
+        if (!(cells <= 1024.0)) return SPHGB_ERR_GRID;
+        dim[d] = (int)cells;
         maxdim = dim[d] > maxdim ? dim[d] : maxdim;
         ncell *= (size_t)dim[d];
     }
