@@ -25,9 +25,11 @@ learned warm start (committed network), iterations and device time per step at
 the same tolerance.  `ensemble` = 256 independent dam breaks advanced by one
 batched context (one launch per kernel, one graph per step).
 
---impl reference times that CPU restatement of the reference's step (the
-reference library itself cannot be built: its build needs external projects
-that are not in its tree) on the same workload, all host threads.
+--impl reference times the CPU implementation of the reference's step on the same
+workload and step window, all host threads: the reference's own FP32 AVX build
+(oracle/_ref/libref_f32.so, compiled from its sources by oracle/build_ref.sh) where
+it is present, else the FP32 build of the CPU restatement (oracle/sph_oracle.c) --
+the reference's sources are not on every host, and its AVX path is x86-64 only.
 
 --gpus N > 1 (torchrun): independent replicas, one per GPU (the step does not
 shard); value = total particle-steps / max time over ranks.
@@ -137,11 +139,30 @@ def cpu_cores():
         return os.cpu_count() or 1
 
 
-def run_oracle_sample(scene, state, budget_s, threads):
-    """FP32 CPU restatement from `state`; at least one step, then as many as fit in budget_s."""
+def cpu_stepper(scene, threads, state=None, prefer="auto"):
+    """The CPU implementation of the reference's step for the CPU legs: the reference's own FP32
+    AVX build (oracle/_ref/libref_f32.so, from its sources; x86-64 hosts with the reference tree)
+    when it is present, else the FP32 build of the CPU restatement (oracle/sph_oracle.c).
+    Returns (step function, close function, kind, description, the RefSim or None)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import refsim
+    if prefer == "reference" and not refsim.available("f32"):
+        raise RuntimeError("the reference's FP32 build (oracle/_ref/libref_f32.so) is not present")
+    if prefer != "port" and refsim.available("f32"):
+        import dataclasses
+        sc = scene if state is None else dataclasses.replace(scene, x=state["x"], v=state["v"])
+        r = refsim.RefSim(sc, precision="f32", analytic_kernel=False, num_threads=threads)
+        if state is not None:
+            r.set("p / rho^2", state["kappa"])
+            r.set("p_v / rho^2", state["kappa_v"])
+            if scene.params.viscosityMethod == 6:
+                r.set("velocity difference", state["vdiff"])
+            r.set_time_step(state["dt"])
+        r.ns_ms = lambda: r.timing("neighborhood_search")[0]
+        return (lambda: r.step(), r.close, "reference",
+                "the reference's TimeStepDFSPH built from its sources, FP32 AVX with precomputeValues, OpenMP; "
+                "its neighbour search is this project's stand-in for CompactNSearch", r)
     import oracle  # CPU baseline only
-
     sim = oracle.OracleSim(scene, precision="f32", num_threads=threads)
     if state is not None:
         sim.x[:] = state["x"]
@@ -150,21 +171,35 @@ def run_oracle_sample(scene, state, budget_s, threads):
         sim.kappa_v[:] = state["kappa_v"]
         sim.vdiff[:] = state["vdiff"]
         sim.dt = state["dt"]
+
+    def step():
+        sim.step()
+        return sim.stats()
+    return (step, lambda: None, "port",
+            "FP32 build of the CPU restatement of the reference's step (oracle/sph_oracle.c), OpenMP; the "
+            "reference's own build needs its source tree, which this host does not hold", None)
+
+
+def run_oracle_sample(scene, state, budget_s, threads, prefer="auto"):
+    """CPU leg from `state`: at least one step, then as many as fit in budget_s."""
+    step, close, kind, desc, _ = cpu_stepper(scene, threads, state, prefer)
     t0 = time.perf_counter()
     steps = 0
     iters = []
     while True:
-        sim.step()
+        st = step()
         steps += 1
-        st = sim.stats()
         iters.append((st["iterations"], st["iterations_v"], st["visco_iterations"]))
         if time.perf_counter() - t0 >= budget_s:
             break
     dt = time.perf_counter() - t0
-    return scene.n * steps / dt, steps, dt, iters
+    close()
+    return scene.n * steps / dt, steps, dt, iters, kind, desc
 
 
 def run_reference(args):
+    """The reference arm: the CPU implementation of the step on all host threads, on this
+    benchmark's workload and step window (warm-up steps, then the timed steps)."""
     from splishsplash_gb300 import scenes
 
     rank = int(os.environ.get("RANK", "0"))
@@ -172,38 +207,40 @@ def run_reference(args):
         return
     scene = scenes.dambreak_1m()
     threads = cpu_cores()
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
-
-    sim = oracle.OracleSim(scene, precision="f32", num_threads=threads)
+    step, close, kind, desc, ref = cpu_stepper(scene, threads, prefer=args.cpu_impl)
     t_w = time.perf_counter()
     warm_done = 0
     for _ in range(args.warmup):
-        sim.step()
+        step()
         warm_done += 1
-        if time.perf_counter() - t_w > args.cpu_warmup_budget:
+        if time.perf_counter() - t_w > args.ref_budget:
             break
+    ns0 = ref.ns_ms() if ref is not None else 0.0
     t0 = time.perf_counter()
     steps = 0
     for _ in range(args.steps):
-        sim.step()
+        step()
         steps += 1
-        if time.perf_counter() - t0 > args.cpu_budget:
+        if time.perf_counter() - t0 > args.ref_budget:
             break
     el = time.perf_counter() - t0
+    ns_s = (ref.ns_ms() - ns0) * 1e-3 if ref is not None else None
+    close()
     value = scene.n * steps / el
-    sample = (f"{steps} of {args.steps} requested steps after {warm_done} warm-up steps of the full {scene.n}-particle "
-              f"scene (stops once {args.cpu_budget:.0f} s of timed CPU work is exceeded)")
+    sample = (f"{steps} of {args.steps} requested steps after {warm_done} of {args.warmup} warm-up steps of the full "
+              f"{scene.n}-particle scene from rest (the timed window of the GPU arm)")
     line = {
         "impl": "reference", "metric": baseline_metric(), "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": steps, "warmup": warm_done, "ms_per_step": 1e3 * el / max(steps, 1), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam break)",
         "config": workload_config(scene),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "CPU restatement of the reference DFSPH step (oracle/sph_oracle.c, FP32 build, OpenMP); the "
-                "reference library itself needs external projects absent from its tree and is not built",
+        "note": desc,
     }
+    if ns_s is not None:
+        line["without_neighbor_search"] = {"value": scene.n * steps / max(el - ns_s, 1e-9), "unit": UNIT,
+                                           "neighbor_search_s": ns_s}
     print(json.dumps(line), flush=True)
 
 
@@ -261,22 +298,28 @@ def config_table(args):
 
 
 def learned_line(steps):
-    """The 2,097,152-lattice sphere scene with the classic and the learned warm start."""
+    """The 2,097,152-lattice sphere scene with the classic and the learned warm start, the
+    latter with the library's default gate (1 divergence / 4 pressure Jacobi sweeps of both
+    candidates) and with the initial-residual gate (1 / 1).  Iterations are reported as the
+    solves count them and booked: with the losing candidate's gate sweeps added."""
     from splishsplash_gb300 import learned, scenes
 
     sc = scenes.learned_2m()
     net = learned.load()
-    res = learned.evaluate(sc, net, steps=steps, strict=False)
+    res = learned.evaluate(sc, net, steps=steps, strict=True)
     net.close()
-    keep = ("pressure_iterations_mean", "divergence_iterations_mean", "solver_iterations_total", "ms_per_step",
-            "final_avg_density_error_percent", "max_avg_density_error_percent", "learned_used_pressure_fraction",
-            "learned_used_div_fraction")
+    keep = ("pressure_iterations_mean", "divergence_iterations_mean", "solver_iterations_total",
+            "solver_iterations_total_booked", "gate_sweeps", "ms_per_step", "final_avg_density_error_percent",
+            "max_avg_density_error_percent", "learned_used_pressure_fraction", "learned_used_div_fraction")
     return {"workload": f"{sc.name}: {sc.n} fluid + {sc.nb} boundary particles, r=0.01, unit-sphere obstacle, "
                         f"{steps} steps from rest, maxError 0.01%",
             "plain": {k: res["plain"][k] for k in keep}, "learned": {k: res["learned"][k] for k in keep},
+            "learned_initial_residual_gate": {k: res["learned_initial_residual_gate"][k] for k in keep},
             "iteration_reduction": res["gain"]["iteration_reduction"],
+            "iteration_reduction_booked": res["gain"]["iteration_reduction_booked"],
             "time_per_step_reduction": res["gain"]["time_per_step_reduction"],
-            "gate": "1 divergence / 4 pressure Jacobi iterations of both candidates (default)",
+            "initial_residual_gate": res["gain_initial_residual_gate"],
+            "gate": "default: 1 divergence / 4 pressure Jacobi sweeps of both candidates; initial-residual gate: 1 / 1",
             "network": "splishsplash_gb300/data/warmstart_mlp.npz (python -m splishsplash_gb300.learned)"}
 
 
@@ -369,7 +412,10 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=0, help="0: as many as --steps")
     ap.add_argument("--profile-steps", type=int, default=4)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
-    ap.add_argument("--cpu-warmup-budget", type=float, default=60.0)
+    ap.add_argument("--cpu-impl", default="auto", choices=["auto", "reference", "port"],
+                    help="CPU legs: the reference's own FP32 build (where present; auto) or the CPU restatement")
+    ap.add_argument("--ref-budget", type=float, default=900.0,
+                    help="--impl reference: seconds after which the warm-up or the timed steps stop early")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--nz", type=int, default=128,
                     help="fluid block depth (128 = the 1M workload; smaller for multi-pass profiler captures)")
@@ -544,10 +590,11 @@ def main():
                                                      ("kappa_v", "p_v / rho^2"), ("vdiff", "velocity difference"))}
         state["dt"] = ts.getTimeStepSize()
         threads = cpu_cores()
-        v_cpu, s_cpu, t_cpu, it_cpu = run_oracle_sample(scene, state, args.cpu_budget, threads)
-        cpu = {"value": v_cpu, "unit": UNIT, "cores": threads, "kind": "port",
+        v_cpu, s_cpu, t_cpu, it_cpu, kind, desc = run_oracle_sample(scene, state, args.cpu_budget, threads,
+                                                                    args.cpu_impl)
+        cpu = {"value": v_cpu, "unit": UNIT, "cores": threads, "kind": kind,
                "sample": f"{s_cpu} step(s) of the full scene from the GPU state after the timed region, {t_cpu:.1f} s "
-                         f"(FP32 build of the CPU restatement, OpenMP); solver iterations {it_cpu}"}
+                         f"({desc}); solver iterations {it_cpu}"}
 
     extras = {}
     if rank == 0 and world == 1 and not args.no_extras:

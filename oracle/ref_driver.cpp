@@ -280,6 +280,22 @@ int ref_neighbor_counts(unsigned int *nf, unsigned int *nb)
 
 void ref_set_time_step(double dt) { TimeManager::getCurrent()->setTimeStepSize(static_cast<Real>(dt)); }
 
+/** Total milliseconds and count of the reference's own timer `name` (START_TIMING /
+ *  STOP_TIMING_AVG, e.g. "neighborhood_search", "pressureSolve") since the library loaded;
+ *  returns 0 when the timer has not run. */
+int ref_timing(const char *name, double *total_ms, unsigned int *count)
+{
+    for (const auto &kv : Utilities::Timing::m_averageTimes)
+        if (kv.second.name == name) {
+            *total_ms = kv.second.totalTime;
+            *count = kv.second.counter;
+            return 1;
+        }
+    *total_ms = 0.0;
+    *count = 0;
+    return 0;
+}
+
 int ref_precision() { return static_cast<int>(sizeof(Real)); }
 
 void ref_destroy()

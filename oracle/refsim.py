@@ -74,6 +74,8 @@ def lib(precision: str = "f64", path: str = None) -> ctypes.CDLL:
         L.ref_set_time_step.argtypes = [ctypes.c_double]
         L.ref_set_time_step.restype = None
         L.ref_precision.restype = ctypes.c_int
+        L.ref_timing.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint)]
+        L.ref_timing.restype = ctypes.c_int
         L.ref_destroy.restype = None
         _LIBS[key] = L
     return _LIBS[key]
@@ -168,6 +170,12 @@ class RefSim:
         self.L.ref_neighbor_counts(nf.ctypes.data_as(ctypes.POINTER(ctypes.c_uint)),
                                    nb.ctypes.data_as(ctypes.POINTER(ctypes.c_uint)))
         return nf, nb
+
+    def timing(self, name: str):
+        """(total ms, count) of the reference's own timer `name` since the library loaded."""
+        t, c = ctypes.c_double(), ctypes.c_uint()
+        self.L.ref_timing(name.encode(), ctypes.byref(t), ctypes.byref(c))
+        return t.value, c.value
 
     def set_time_step(self, dt: float) -> None:
         self.L.ref_set_time_step(float(dt))

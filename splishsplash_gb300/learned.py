@@ -157,7 +157,11 @@ def run(scene, steps, net=None, warmup=0, use_graph=True, gate=(0, 0)):
     return stats, ms, rho
 
 
-def summarize(stats, ms, rho, rho0=1000.0):
+def summarize(stats, ms, rho, rho0=1000.0, gate=None):
+    """Per-run summary.  gate = (divergence, pressure) Jacobi sweeps that the network's warm-start
+    selection runs for both candidates, or None for the classic warm start: the losing
+    candidate's sweeps are work the GPU did, and `solver_iterations_total_booked` adds them
+    (gate sweeps per gated solve) to the iterations of the solves themselves."""
     it = np.array([[s["iterations"], s["iterations_v"]] for s in stats], float)
     used = np.array([s["learned_used"] for s in stats])
     rc = np.array([s["ws_residual_classic"] for s in stats], float)
@@ -169,6 +173,8 @@ def summarize(stats, ms, rho, rho0=1000.0):
         "pressure_iterations_mean": float(it[:, 0].mean()),
         "divergence_iterations_mean": float(it[:, 1].mean()),
         "solver_iterations_total": float(it.sum()),
+        "solver_iterations_total_booked": float(it.sum() + (0 if gate is None else len(stats) * (gate[0] + gate[1]))),
+        "gate_sweeps": None if gate is None else list(gate),
         "ms_per_step": float(np.mean(ms)),
         "final_avg_density_error_percent": float(stats[-1]["avg_density_err"] / rho0 * 100.0),
         "max_avg_density_error_percent": float(max(s["avg_density_err"] for s in stats) / rho0 * 100.0),
@@ -181,8 +187,17 @@ def summarize(stats, ms, rho, rho0=1000.0):
 def _gain(plain, learned):
     return {
         "iteration_reduction": 1.0 - learned["solver_iterations_total"] / max(plain["solver_iterations_total"], 1.0),
+        "iteration_reduction_booked": 1.0 - learned["solver_iterations_total_booked"] /
+        max(plain["solver_iterations_total_booked"], 1.0),
         "time_per_step_reduction": 1.0 - learned["ms_per_step"] / plain["ms_per_step"],
     }
+
+
+def default_gate(params):
+    """The gate sweeps sphgb_set_warmstart_gate(0, 0) selects: 1 for the divergence solve,
+    max(minIterations, 4) for the pressure solve, never more than the solvers' caps."""
+    return (min(1, params.maxIterationsV) if params.enableDivergenceSolver else 0,
+            min(max(4, params.minIterations), params.maxIterations))
 
 
 def evaluate(scene, net, steps=300, warmup=0, strict=True):
@@ -190,11 +205,12 @@ def evaluate(scene, net, steps=300, warmup=0, strict=True):
     by the candidates' initial residuals alone (gate 1 for both solvers)."""
     sp, mp, rp = run(scene, steps, None, warmup)
     sl, ml, rl = run(scene, steps, net, warmup)
-    plain, learned = summarize(sp, mp, rp), summarize(sl, ml, rl)
+    plain, learned = summarize(sp, mp, rp), summarize(sl, ml, rl, gate=default_gate(scene.params))
     out = {"plain": plain, "learned": learned, "gain": _gain(plain, learned)}
     if strict:
         ss, ms, rs = run(scene, steps, net, warmup, gate=(1, 1))
-        out["learned_initial_residual_gate"] = summarize(ss, ms, rs)
+        strict_gate = (1 if scene.params.enableDivergenceSolver else 0, 1)
+        out["learned_initial_residual_gate"] = summarize(ss, ms, rs, gate=strict_gate)
         out["gain_initial_residual_gate"] = _gain(plain, out["learned_initial_residual_gate"])
     return out
 
