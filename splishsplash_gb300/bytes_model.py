@@ -38,6 +38,10 @@ def per_particle(kernel: str, nf: float, nb: float, visc_boundary: bool = False)
         # x_i, warm start g_i (+ weight), v_i, density_i, counts, lists; writes 2 symmetric
         # inverse rows, r, p
         "visc_setup": 3 * V4 + S + counts + lists_f + 2 * V4 + 2 * V4,
+        # the two passes above fused (one fluid phase with viscosity): x_i, v_i, vDiff_i (rho_i
+        # in w), density_i, counts, one walk of the lists; writes a_i, kappa_v r/w, the warm
+        # start, 2 symmetric inverse rows, r, p
+        "xsph_visc_setup": 3 * V4 + S + counts + lists_f + V4 + 2 * S + V4 + 2 * V4 + 2 * V4,
         # x_i, p_i, density_i, counts, lists; writes t_i
         "cg_matvec": 2 * V4 + S + counts + lists_f + V4,
         # p, t, x, r, 2 inverse rows; writes x, r, z

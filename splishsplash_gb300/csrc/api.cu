@@ -189,13 +189,13 @@ enum KernelId {
     K_STEP_BEGIN, K_KEYS, K_SORT, K_GATHER, K_CELL_RANGES, K_BUILD, K_LOOP_BEGIN, K_PRESSURE_ACCEL, K_JACOBI,
     K_SOLVER_FINALIZE, K_XSPH, K_VISC_SETUP, K_CG_MATVEC, K_CG_UPDATE, K_CG_P, K_KICK, K_PRESS_INIT, K_INTEGRATE,
     K_FEATURES, K_MLP, K_WS_SELECT, K_BODY_FORCES, K_STAGE_TABLE, K_VMAP_BOUNDARY, K_BOUNDARY_MOVE,
-    K_COUNT
+    K_XSPH_VISC_SETUP, K_COUNT
 };
 const char *kKernelNames[K_COUNT] = {
     "step_begin", "keys", "radix_sort", "gather", "cell_ranges", "build_lists_density_alpha", "loop_begin",
     "pressure_accel", "jacobi_update", "solver_finalize", "xsph_gravity", "visc_setup", "cg_matvec", "cg_update",
     "cg_p", "kick_cfl", "press_init", "integrate", "features", "mlp_infer", "warmstart_select", "body_forces",
-    "stage_table", "vmap_boundary", "boundary_move",
+    "stage_table", "vmap_boundary", "boundary_move", "xsph_visc_setup",
 };
 
 // Brackets the launches of one kernel class with events on the context stream
@@ -854,6 +854,8 @@ template <class T> BoundaryMoveDev<T> boundary_move_dev(const sphgb_ctx *c)
 // per-model force, Viscosity_Weiler2018.cpp:891-936 run for each FluidModel); phase k's system
 // takes mub = nu_b rho0 and rho0 of that phase in its boundary terms.  -1: one system over all.
 template <class T> int visc_systems(const DevParams<T> &P) { return P.nphase > 1 ? (int)P.nphase : 1; }
+// one fluid phase with viscosity: the XSPH pass runs fused into the viscosity set-up pass
+template <class T> bool fused_xsph_visc(const DevParams<T> &P) { return P.visc_on && P.nphase <= 1; }
 template <class T> DevParams<T> visc_system_params(const sphgb_ctx *c, const DevParams<T> &P, int k, int &phase)
 {
     phase = P.nphase > 1 ? k : -1;
@@ -932,12 +934,14 @@ template <class T> int step_host_loop(sphgb_ctx *c)
         return SPHGB_OK;
     };
     if (P.div_on && (rc = solve(true))) return rc;
-    { PROF(K_XSPH, s); launch_xsph<T>(P, B1, s); }
+    const bool fused = fused_xsph_visc(P);
+    if (!fused) { PROF(K_XSPH, s); launch_xsph<T>(P, B1, s); }
     if (P.visc_on) {
         for (int k = 0; k < visc_systems(P); k++) {
             int ph;
             const DevParams<T> Q = visc_system_params(c, P, k, ph);
-            { PROF(K_VISC_SETUP, s); launch_visc_setup<T>(Q, B1, 0, false, s, ph); }
+            if (fused) { PROF(K_XSPH_VISC_SETUP, s); launch_xsph_visc_setup<T>(Q, B1, 0, false, s); }
+            else { PROF(K_VISC_SETUP, s); launch_visc_setup<T>(Q, B1, 0, false, s, ph); }
             if ((rc = read_cont(c, &cont))) return rc;
             unsigned guard = 0;
             while (cont && guard++ <= P.visc_max_iter) {
@@ -1044,7 +1048,8 @@ template <class T> int build_graph(sphgb_ctx *c, int parity, cudaGraphExec_t *ou
         launch_solver_finalize<T>(P, B1, div, s);
     };
     if (P.div_on) solve(true);
-    launch_xsph<T>(P, B1, s);
+    const bool fused = fused_xsph_visc(P);
+    if (!fused) launch_xsph<T>(P, B1, s);
     for (int k = 0; P.visc_on && e == cudaSuccess && k < visc_systems(P); k++) {
         // the set-up kernel sets the CG loop's condition; one loop per system
         int ph;
@@ -1052,7 +1057,8 @@ template <class T> int build_graph(sphgb_ctx *c, int parity, cudaGraphExec_t *ou
         cudaGraphConditionalHandle hcg = 0;
         e = make_handle(c, &hcg, 0u);
         if (e == cudaSuccess) {
-            launch_visc_setup<T>(Q, B1, hcg, true, s, ph);
+            if (fused) launch_xsph_visc_setup<T>(Q, B1, hcg, true, s);
+            else launch_visc_setup<T>(Q, B1, hcg, true, s, ph);
             e = add_while_node(c, hcg, [&](cudaStream_t bs, cudaGraphConditionalHandle hh) {
                 launch_cg_matvec<T>(Q, B1, bs, hh, true, ph);
                 launch_cg_update<T>(Q, B1, hh, true, bs, ph);

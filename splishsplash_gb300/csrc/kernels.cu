@@ -797,6 +797,9 @@ __device__ __forceinline__ void build_one(const DevParams<T> &P, const DevBufs<T
     // density: rho0 * (V W0 + sum_f V W + sum_b Vb W)
     const T rho = rho0_at(P, B, i) * (P.V * P.K.w0 + P.V * wf + wb);
     B.density[i] = rho;
+    // the fused XSPH and viscosity set-up pass gathers rho_j in the w lane of the
+    // velocity-difference record (the kick overwrites it at the end of the step)
+    if (P.visc_on) store_w(B.vdiff, i, rho);
     // factor: 1 / (sum_f |V gradW|^2 + |sum_f V gradW + sum_b Vb gradW|^2)
     const V3<T> gpi = add(scl(gf, P.V), gb);
     const T sum_grad = P.V * P.V * gsq + dot(gpi, gpi);
@@ -1250,33 +1253,13 @@ __global__ void k_loop_begin(StepScalars *sc, StepScalars *gsc, uint32_t nscenes
 // clearAccelerations (TimeStep.cpp:35-50) + XSPH::step scalar path (XSPH.cpp:138-211).
 // Also finishes the divergence solve's kappa_v *= h (TimeStepDFSPH.cpp:522-540),
 // which must wait until no thread reads kappa_v of its neighbours any more.
-template <class T, int LPP>
-__global__ void __launch_bounds__(kBlock) k_xsph(DevParams<T> P, DevBufs<T> B, int div_on)
+// Gravity plus the XSPH acceleration of particle i from its fluid sum acc (XSPH.cpp:138-216),
+// kappa_v h (divergence solve on) and, with viscosity, the Weiler2018 warm start in cg_x.
+template <class T>
+__device__ __forceinline__ void xsph_finish(const DevParams<T> &P, const DevBufs<T> &B, uint32_t s, uint32_t i,
+                                            V3<T> acc, T xs, T xsb, int div_on)
 {
-    count_launch(&B.gsc->launches);
-    const SlotInfo q = slot_info<LPP>(P);
-    V3<T> acc = mk3<T>(0, 0, 0);
-    T xs = P.xsph, xsb = P.xsph_b;   // fluid phases: the particle's model's coefficients
-    if (P.nphase > 1 && q.act) phase_xsph(P, B.ph[q.i], xs, xsb);
-    if (q.act && xs != T(0)) {
-        const v4_t<T> xi = ldv(B.x, q.i);
-        const V3<T> vi = xyz<T>(ldv(B.v, q.i));
-        struct XVR {
-            v4_t<T> x, v;
-            T rho;
-        };
-        fluid_loop<LPP, kUnroll>(P, B, q.i, q.l, [&](uint32_t j) { return XVR{ldv(B.x, j), ldv(B.v, j), B.density[j]}; },
-                                 [&](uint32_t j, const XVR &d) {
-                                     const V3<T> r = diff3<T>(xi, d.x);
-                                     const T mj = P.nphase > 1 ? P.V * B.r0[j] : P.mass;
-                                     const T w = (mj / d.rho) * kernel_W(P.K, dev_sqrt(dot(r, r)));
-                                     acc = add(acc, scl(sub(vi, xyz<T>(d.v)), w));
-                                 });
-    }
-    acc = gsum3<LPP>(acc);
-    if (!q.act || q.l != 0) return;
-    const uint32_t i = q.i;
-    const T h = (T)B.sc[q.s].dt;
+    const T h = (T)B.sc[s].dt;
     const T invH = T(1) / h;
     const V3<T> vi = xyz<T>(ldv(B.v, i));
     V3<T> ai = mk3<T>(P.gx, P.gy, P.gz);
@@ -1309,6 +1292,34 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams<T> P, DevBufs<T> B, i
         }
         stv(B.cg_x, i, pack(add(vi, xyz<T>(ldv(B.vdiff, i))), wi));
     }
+}
+
+template <class T, int LPP>
+__global__ void __launch_bounds__(kBlock) k_xsph(DevParams<T> P, DevBufs<T> B, int div_on)
+{
+    count_launch(&B.gsc->launches);
+    const SlotInfo q = slot_info<LPP>(P);
+    V3<T> acc = mk3<T>(0, 0, 0);
+    T xs = P.xsph, xsb = P.xsph_b;   // fluid phases: the particle's model's coefficients
+    if (P.nphase > 1 && q.act) phase_xsph(P, B.ph[q.i], xs, xsb);
+    if (q.act && xs != T(0)) {
+        const v4_t<T> xi = ldv(B.x, q.i);
+        const V3<T> vi = xyz<T>(ldv(B.v, q.i));
+        struct XVR {
+            v4_t<T> x, v;
+            T rho;
+        };
+        fluid_loop<LPP, kUnroll>(P, B, q.i, q.l, [&](uint32_t j) { return XVR{ldv(B.x, j), ldv(B.v, j), B.density[j]}; },
+                                 [&](uint32_t j, const XVR &d) {
+                                     const V3<T> r = diff3<T>(xi, d.x);
+                                     const T mj = P.nphase > 1 ? P.V * B.r0[j] : P.mass;
+                                     const T w = (mj / d.rho) * kernel_W(P.K, dev_sqrt(dot(r, r)));
+                                     acc = add(acc, scl(sub(vi, xyz<T>(d.v)), w));
+                                 });
+    }
+    acc = gsum3<LPP>(acc);
+    if (!q.act || q.l != 0) return;
+    xsph_finish(P, B, q.s, q.i, acc, xs, xsb, div_on);
 }
 
 // ---- Weiler et al. 2018 ---------------------------------------------------
@@ -1391,10 +1402,15 @@ template <class T> __device__ __forceinline__ V3<T> sym_mul(const v4_t<T> &a, co
 // MP (fluid phases): the system of phase `phase` alone (Viscosity_Weiler2018 is per fluid model and
 // sums over forall_fluid_neighbors_in_same_phase); the other phases' particles get p = 0 with
 // weight 0, so the matrix-vector passes of this phase need no neighbour test.
-template <class T, int LPP, bool MP = false>
+// XS (one fluid phase): the XSPH pass fused in.  The neighbours' warm start g_j = v_j + vDiff_j and
+// weight w_j = d mu m / rho_j are formed here, with the same operations as k_xsph stores them in
+// cg_x, from one walk of the list that gathers (x_j, v_j, vDiff_j | rho_j); the XSPH sum takes v_j
+// and rho_j from the same records, and the particle's own XSPH results are written as k_xsph does.
+template <class T, int LPP, bool MP = false, bool XS = false>
 __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T> B, cudaGraphConditionalHandle handle,
                                                         int use_handle, int phase)
 {
+    static_assert(!(MP && XS), "the fused XSPH pass serves a single fluid phase");
     count_launch(&B.gsc->launches);
     SlotInfo q = slot_info<LPP>(P);
     bool other = false;   // a slot of another phase
@@ -1408,6 +1424,7 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T
     T m[6] = {0, 0, 0, 0, 0, 0};   // m00 m01 m02 m11 m12 m22
     V3<T> acc = mk3<T>(0, 0, 0);
     V3<T> bb = mk3<T>(0, 0, 0);    // moving volume-map bodies: boundary term of the right-hand side (lane 0)
+    V3<T> axs = mk3<T>(0, 0, 0);   // XS: the XSPH sum
     v4_t<T> xi{}, gi4{};
     T rhoi = T(1);
     if (q.act) {
@@ -1415,21 +1432,47 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T
         xi = ldv(B.x, i);
         rhoi = B.density[i];
         const T eps2 = T(0.01) * P.h2;
-        gi4 = ldv(B.cg_x, i);
-        const V3<T> gi = xyz<T>(gi4);
-        struct XG {
-            v4_t<T> x, g;
+        // the operator term of neighbour j with its warm start g_j and weight w_j
+        auto op = [&](const V3<T> &r, T r2, T wj, const V3<T> &gi, const V3<T> &gj) {
+            const T f = wj / (r2 + eps2) * grad_coef_d2(P.K, r2);
+            m[0] += f * r.x * r.x; m[1] += f * r.x * r.y; m[2] += f * r.x * r.z;
+            m[3] += f * r.y * r.y; m[4] += f * r.y * r.z; m[5] += f * r.z * r.z;
+            acc = add(acc, scl(r, f * dot(sub(gi, gj), r)));
         };
-        fluid_loop<LPP, kUnroll>(P, B, i, q.l, [&](uint32_t j) { return XG{ldv(B.x, j), ldv(B.cg_x, j)}; },
-                                 [&](uint32_t j, const XG &d) {
-                                     if (MP && B.ph[j] != (uint32_t)phase) return;
-                                     const V3<T> r = diff3<T>(xi, d.x);
-                                     const T r2 = dot(r, r);
-                                     const T f = (T)d.g.w / (r2 + eps2) * grad_coef_d2(P.K, r2);
-                                     m[0] += f * r.x * r.x; m[1] += f * r.x * r.y; m[2] += f * r.x * r.z;
-                                     m[3] += f * r.y * r.y; m[4] += f * r.y * r.z; m[5] += f * r.z * r.z;
-                                     acc = add(acc, scl(r, f * dot(sub(gi, xyz<T>(d.g)), r)));
-                                 });
+        if constexpr (XS) {
+            const V3<T> vi = xyz<T>(ldv(B.v, i));
+            gi4 = pack(add(vi, xyz<T>(ldv(B.vdiff, i))), P.vd * P.mu * P.mass / rhoi);
+            const V3<T> gi = xyz<T>(gi4);
+            const bool xs_on = P.xsph != T(0);
+            struct XVD {
+                v4_t<T> x, v, d;
+            };
+            fluid_loop<LPP, kUnroll>(P, B, i, q.l,
+                                     [&](uint32_t j) { return XVD{ldv(B.x, j), ldv(B.v, j), ldv(B.vdiff, j)}; },
+                                     [&](uint32_t, const XVD &d) {
+                                         const V3<T> r = diff3<T>(xi, d.x);
+                                         const T r2 = dot(r, r);
+                                         const T rhoj = (T)d.d.w;
+                                         if (xs_on) {
+                                             const T w = (P.mass / rhoj) * kernel_W(P.K, dev_sqrt(r2));
+                                             axs = add(axs, scl(sub(vi, xyz<T>(d.v)), w));
+                                         }
+                                         op(r, r2, P.vd * P.mu * P.mass / rhoj, gi,
+                                            add(xyz<T>(d.v), xyz<T>(d.d)));
+                                     });
+        } else {
+            gi4 = ldv(B.cg_x, i);
+            const V3<T> gi = xyz<T>(gi4);
+            struct XG {
+                v4_t<T> x, g;
+            };
+            fluid_loop<LPP, kUnroll>(P, B, i, q.l, [&](uint32_t j) { return XG{ldv(B.x, j), ldv(B.cg_x, j)}; },
+                                     [&](uint32_t j, const XG &d) {
+                                         if (MP && B.ph[j] != (uint32_t)phase) return;
+                                         const V3<T> r = diff3<T>(xi, d.x);
+                                         op(r, dot(r, r), (T)d.g.w, gi, xyz<T>(d.g));
+                                     });
+        }
         if (P.mub != T(0)) {
             boundary_loop<LPP>(P, B, i, q.l, [&](uint32_t j, const v4_t<T> &xj) {
                 const V3<T> r = diff3<T>(xi, xj);
@@ -1456,15 +1499,17 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T
                         if (P.vmove) bb = add(bb, scl(r, f * dot(vmap_point_velocity<T>(P.vmaps[mr.x + b], xk), r)));
                     });
                 }
-            acc = add(acc, weiler_boundary<LPP>(P, B, q, xi, rhoi, gi));
+            acc = add(acc, weiler_boundary<LPP>(P, B, q, xi, rhoi, xyz<T>(gi4)));
         }
     }
 #pragma unroll
     for (int k = 0; k < 6; k++) m[k] = gsum<LPP>(m[k]);
     acc = gsum3<LPP>(acc);
     if (P.bmove) bb = gsum3<LPP>(bb);   // the lanes' shares of the boundary list
+    if constexpr (XS) axs = gsum3<LPP>(axs);
     if (q.act && q.l == 0) {
         const uint32_t i = q.i;
+        if constexpr (XS) xsph_finish(P, B, q.s, i, axs, P.xsph, P.xsph_b, P.div_on);
         const T dt = (T)sc->dt;
         const V3<T> gi = xyz<T>(gi4);
         const T s = dt / rhoi;
@@ -1785,33 +1830,69 @@ __global__ void __launch_bounds__(kBlock) k_press_init(DevParams<T> P, DevBufs<T
 // x += h_old v (TimeStepDFSPH.cpp:220-237) accumulated in FP64 (double-float
 // compensated positions in FP32 mode), kappa *= h_new^2 (:365-383); the scene's
 // last block advances its time (:248) and makes dt_next its next step size.
+// (s, e) with s + e = a + b exactly (Knuth's TwoSum)
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// (x, lo) <- x + lo + (hh + hl) v in double-float arithmetic: the product hh v exactly (p + pe,
+// FMA), x + p exactly (TwoSum), the small terms in FP32 and a final TwoSum; the new pair holds
+// the sum to about 2^-47 of |x| (FP64 rounding of the same sum: 2^-53)
+__device__ __forceinline__ void df_advance(float &x, float &lo, float hh, float hl, float v)
+{
+    const float p = __fmul_rn(hh, v);
+    const float pe = __fmaf_rn(hh, v, -p);
+    float s, e;
+    two_sum(x, p, s, e);
+    const float t = __fadd_rn(e, __fadd_rn(lo, __fadd_rn(pe, __fmul_rn(hl, v))));
+    two_sum(s, t, x, lo);
+}
+
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_integrate(DevParams<T> P, DevBufs<T> B)
 {
     count_launch(&B.gsc->launches);
     const SlotInfo q = slot_info(P);
     StepScalars *const sc = B.sc + q.s;
-    const double h = sc->dt;
-    const double hn = sc->dt_next;
+    // FP32: the step sizes as float pairs, split once per block (FP64 runs at a small fraction
+    // of the FP32 rate on this part)
+    __shared__ float hsplit[4];
+    if (sizeof(T) == 4 && threadIdx.x == 0) {
+        const double h = sc->dt, hn2 = sc->dt_next * sc->dt_next;
+        hsplit[0] = (float)h;
+        hsplit[1] = (float)(h - (double)hsplit[0]);
+        hsplit[2] = (float)hn2;
+        hsplit[3] = (float)(hn2 - (double)hsplit[2]);
+    }
+    __syncthreads();
     if (q.act) {
         const uint32_t i = q.i;
         v4_t<T> x = ldv(B.x, i);
         const v4_t<T> v = ldv(B.v, i);
-        if (B.xlo) {
-            const float4 lo = B.xlo[i];
-            const double px = (double)x.x + (double)lo.x + h * (double)v.x;
-            const double py = (double)x.y + (double)lo.y + h * (double)v.y;
-            const double pz = (double)x.z + (double)lo.z + h * (double)v.z;
-            x.x = (T)px; x.y = (T)py; x.z = (T)pz;
-            B.xlo[i] = make_float4((float)(px - (double)x.x), (float)(py - (double)x.y), (float)(pz - (double)x.z), 0.f);
+        if constexpr (sizeof(T) == 4) {
+            float4 lo = B.xlo[i];
+            df_advance(x.x, lo.x, hsplit[0], hsplit[1], v.x);
+            df_advance(x.y, lo.y, hsplit[0], hsplit[1], v.y);
+            df_advance(x.z, lo.z, hsplit[0], hsplit[1], v.z);
+            lo.w = 0.f;
+            B.xlo[i] = lo;
+            // kappa h_new^2 with h_new^2 as a float pair
+            const float k = B.kappa[i];
+            B.kappa[i] = __fmaf_rn(k, hsplit[2], __fmul_rn(k, hsplit[3]));
         } else {
-            x.x = (T)((double)x.x + h * (double)v.x);
-            x.y = (T)((double)x.y + h * (double)v.y);
-            x.z = (T)((double)x.z + h * (double)v.z);
+            const double h = sc->dt, hn = sc->dt_next;
+            x.x = x.x + h * v.x;
+            x.y = x.y + h * v.y;
+            x.z = x.z + h * v.z;
+            B.kappa[i] = B.kappa[i] * (hn * hn);
         }
         stv(B.x, i, x);
-        B.kappa[i] = (T)((double)B.kappa[i] * (hn * hn));
     }
+    const double h = sc->dt;
+    const double hn = sc->dt_next;
     __shared__ bool amLast;
     __syncthreads();
     const ReduceSlot rs = scene_reduce(P, B, q);
@@ -2758,6 +2839,14 @@ void launch_visc_setup(const DevParams<T> &P, const DevBufs<T> &B, cudaGraphCond
     else
         LPP_DISPATCH(P, (k_visc_setup<T, L><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B, h, use_handle ? 1 : 0, phase)));
 }
+template <class T>
+void launch_xsph_visc_setup(const DevParams<T> &P, const DevBufs<T> &B, cudaGraphConditionalHandle h, bool use_handle,
+                            cudaStream_t s)
+{
+    if (P.np)
+        LPP_DISPATCH(P, (k_visc_setup<T, L, false, true><<<grid_lpp(P.np, L), kBlock, 0, s>>>(P, B, h, use_handle ? 1 : 0,
+                                                                                             -1)));
+}
 template <class T> void launch_cg_matvec(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s,
                                          cudaGraphConditionalHandle h, bool use_handle, int phase)
 {
@@ -2924,6 +3013,8 @@ void launch_lists_to_ids(const uint32_t *list, const uint32_t *cnt, uint32_t cap
     template void launch_xsph<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                           \
     template void launch_visc_setup<T>(const DevParams<T> &, const DevBufs<T> &, cudaGraphConditionalHandle, bool,  \
                                        cudaStream_t, int);                                                          \
+    template void launch_xsph_visc_setup<T>(const DevParams<T> &, const DevBufs<T> &, cudaGraphConditionalHandle,   \
+                                            bool, cudaStream_t);                                                    \
     template void launch_cg_matvec<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t,                       \
                                       cudaGraphConditionalHandle, bool, int);                                       \
     template void launch_cg_update<T>(const DevParams<T> &, const DevBufs<T> &, cudaGraphConditionalHandle, bool,   \

@@ -195,9 +195,25 @@ __device__ __forceinline__ void grid_sum_finalize(DSum<NV> mine, ReduceSlot slot
     DSum<NV> acc;
 #pragma unroll
     for (int k = 0; k < NV; k++) acc.v[k] = 0.0;
-    for (unsigned i = threadIdx.x; i < slot.count; i += blockDim.x) {
+    // U partials per thread in flight at a time, added in the same order as one by one (thread t
+    // sums t, t + blockDim, t + 2 blockDim, ...), so the total does not depend on U
+    constexpr unsigned U = NV <= 2 ? 8u : 4u;
+    const double *src = slot.partials + slot.first;
+    unsigned i = threadIdx.x;
+    for (; i + (U - 1u) * blockDim.x < slot.count; i += U * blockDim.x) {
+        double p[U][NV];
 #pragma unroll
-        for (int k = 0; k < NV; k++) acc.v[k] += __ldcg(&slot.partials[(size_t)k * gridDim.x + slot.first + i]);
+        for (unsigned u = 0; u < U; u++)
+#pragma unroll
+            for (int k = 0; k < NV; k++) p[u][k] = __ldcg(src + (size_t)k * gridDim.x + i + u * blockDim.x);
+#pragma unroll
+        for (unsigned u = 0; u < U; u++)
+#pragma unroll
+            for (int k = 0; k < NV; k++) acc.v[k] += p[u][k];
+    }
+    for (; i < slot.count; i += blockDim.x) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) acc.v[k] += __ldcg(src + (size_t)k * gridDim.x + i);
     }
     DSum<NV> tot = block_sum<NV>(acc);
     if (threadIdx.x == 0) {

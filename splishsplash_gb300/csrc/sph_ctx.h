@@ -271,6 +271,10 @@ template <class T> void launch_xsph(const DevParams<T> &P, const DevBufs<T> &B, 
 template <class T> void launch_visc_setup(const DevParams<T> &P, const DevBufs<T> &B,
                                           cudaGraphConditionalHandle h, bool use_handle, cudaStream_t s,
                                           int phase = -1);
+// One fluid phase with viscosity: the XSPH pass and the viscosity set-up in one pass over the
+// lists, with the results of launch_xsph followed by launch_visc_setup(phase -1).
+template <class T> void launch_xsph_visc_setup(const DevParams<T> &P, const DevBufs<T> &B,
+                                               cudaGraphConditionalHandle h, bool use_handle, cudaStream_t s);
 template <class T> void launch_cg_matvec(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s,
                                          cudaGraphConditionalHandle h = 0, bool use_handle = false, int phase = -1);
 template <class T> void launch_cg_update(const DevParams<T> &P, const DevBufs<T> &B,
