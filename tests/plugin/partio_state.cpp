@@ -7,6 +7,8 @@
 // order.  Linked with the reference's objects and oracle/ref_driver.cpp, so the reference's
 // Simulation set up by ref_create is the one saved and restored.
 #include "SPlisHSPlasH/Simulation.h"
+#include "SPlisHSPlasH/TimeManager.h"
+#include "Utilities/BinaryFileReaderWriter.h"
 #include "Partio.h"
 
 #include <vector>
@@ -81,6 +83,33 @@ int state_read(const char *path)
     }
     data->release();
     return matched;
+}
+
+/** The library's section of the simulator's .bin state file, written as SimulatorBase::saveState
+ *  writes it (Simulator/SimulatorBase.cpp:1724-1725): TimeManager::saveState, then
+ *  Simulation::saveState (time, step size, W(0), the fluid models' particle states and emitter
+ *  counts, the boundary models' sort flags and point-set indices, the time step's own state);
+ *  returns 0, or -1 when the file cannot be opened. */
+int sim_state_write(const char *path)
+{
+    BinaryFileWriter w;
+    if (!w.openFile(path)) return -1;
+    TimeManager::getCurrent()->saveState(w);
+    Simulation::getCurrent()->saveState(w);
+    w.closeFile();
+    return 0;
+}
+
+/** Reads that section back as SimulatorBase::loadState does (:1805-1806); the particle files
+ *  follow with state_read, in that order. */
+int sim_state_read(const char *path)
+{
+    BinaryFileReader r;
+    if (!r.openFile(path)) return -1;
+    TimeManager::getCurrent()->loadState(r);
+    Simulation::getCurrent()->loadState(r);
+    r.closeFile();
+    return 0;
 }
 
 /** Attribute names of a BGEO file, separated by '\n', with their partio types (F, I or V)

@@ -3,8 +3,9 @@
 * `reference_tree()`: the reference's source tree (SPH_REFERENCE_ROOT, else a "reference"
   folder beside this repository), or None.
 * `plugin_fake_abi()`: the reference's library objects (oracle/build_ref.sh) with the
-  reference-side plugin (splishsplash_gb300/plugin/), tests/plugin/plugin_glue.cpp and the
-  oracle-backed stand-in of the C ABI (tests/plugin/fake_sphgb300.cpp).
+  reference-side plugin (splishsplash_gb300/plugin/), tests/plugin/plugin_glue.cpp, the
+  oracle-backed stand-in of the C ABI (tests/plugin/fake_sphgb300.cpp) and the state-file glue
+  of `state_library()`.
 * `plugin_objects()`: the plugin's object files, for a link check against libsphgb300.so.
 * `state_library()`: the reference's library objects with oracle/ref_driver.cpp and partio
   (vendored in the reference tree, extern/partio) plus tests/plugin/partio_state.cpp: the
@@ -68,12 +69,13 @@ def plugin_fake_abi(tree):
     lib = os.path.join(out, "libplugin_fake_abi.so")
     objs = plugin_objects(tree)
     objs["fake"] = _compile(tree, out, "fake", os.path.join(ROOT, "tests", "plugin", "fake_sphgb300.cpp"))
+    objs["state"] = _compile(tree, out, "partio_state", os.path.join(ROOT, "tests", "plugin", "partio_state.cpp"))
     for name in ("sph_oracle", "vmap"):
         objs[name] = os.path.join(out, name + ".o")
         run(["gcc", "-std=c11", "-O2", "-fPIC", "-fopenmp", "-ffp-contract=off", "-DORC_REAL=double", "-c",
              os.path.join(ROOT, "oracle", name + ".c"), "-o", objs[name]])
-    run(["g++", "-shared", "-fopenmp", "-Wl,--no-undefined", "-o", lib, *_ref_objects(tree), objs["plugin"],
-         objs["glue"], objs["fake"], objs["sph_oracle"], objs["vmap"], "-lm"])
+    run(["g++", "-shared", "-fopenmp", "-Wl,--no-undefined", "-o", lib, *_ref_objects(tree), *objs.values(),
+         *_partio_objects(tree), "-lz", "-lm"])
     return lib
 
 
@@ -86,6 +88,24 @@ def link_plugin_against(tree, libdir):
     return out
 
 
+def _partio_objects(tree):
+    """partio's library objects, compiled once into oracle/_ref/partio/"""
+    out = os.path.join(REF_OUT, "partio")
+    os.makedirs(out, exist_ok=True)
+    objs = []
+    pio = os.path.join(tree, "extern", "partio", "src", "lib")
+    # partio predates C++17 (std::ios::streampos): compiled as C++11, as its own build does
+    for sub in ("core", "io"):
+        for f in sorted(os.listdir(os.path.join(pio, sub))):
+            if f.endswith(".cpp"):
+                obj = os.path.join(out, f"partio_{sub}_{f[:-4]}.o")
+                if not os.path.exists(obj):
+                    run(["g++", "-std=c++11", "-O2", "-fPIC", "-w", "-DPARTIO_USE_ZLIB", "-I", pio,
+                         "-c", os.path.join(pio, sub, f), "-o", obj])
+                objs.append(obj)
+    return objs
+
+
 def state_library(tree):
     out = os.path.join(REF_OUT, "state_test")
     os.makedirs(out, exist_ok=True)
@@ -94,19 +114,7 @@ def state_library(tree):
     src = os.path.join(ROOT, "tests", "plugin", "partio_state.cpp")
     if os.path.exists(lib) and all(os.path.getmtime(f) <= os.path.getmtime(lib) for f in ref_objs + [src]):
         return lib
-    objs = []
-    pio = os.path.join(tree, "extern", "partio", "src", "lib")
-    # partio predates C++17 (std::ios::streampos): compiled as C++11, as its own build does
-    for sub in ("core", "io"):
-        for f in sorted(os.listdir(os.path.join(pio, sub))):
-            if f.endswith(".cpp"):
-                obj = os.path.join(out, f"partio_{sub}_{f[:-4]}.o")
-                if os.path.exists(obj):
-                    objs.append(obj)
-                    continue
-                run(["g++", "-std=c++11", "-O2", "-fPIC", "-w", "-DPARTIO_USE_ZLIB", "-I", pio,
-                     "-c", os.path.join(pio, sub, f), "-o", obj])
-                objs.append(obj)
-    objs.append(_compile(tree, out, "partio_state", os.path.join(ROOT, "tests", "plugin", "partio_state.cpp")))
-    run(["g++", "-shared", "-fopenmp", "-Wl,--no-undefined", "-o", lib, *ref_objs, *objs, "-lz", "-lm"])
+    objs = [_compile(tree, out, "partio_state", src)]
+    run(["g++", "-shared", "-fopenmp", "-Wl,--no-undefined", "-o", lib, *ref_objs, *objs, *_partio_objects(tree),
+         "-lz", "-lm"])
     return lib
