@@ -96,21 +96,27 @@ template <int LPP, class T> __device__ __forceinline__ V3<T> gsum3(V3<T> v)
 // reduction, after it stored the scene's own decision in sc[s].cont; the last
 // scene to arrive stores the OR over all scenes in the global record and in the
 // graph's loop condition.  A loop stopped by the guard stays stopped.
+// The scenes that call it are every scene (all_scenes: the first kernel of a loop) or the scenes
+// live at the launch, whose number the previous decision left in the global record: the blocks
+// of a scene whose loop has stopped return before any work and never get here.  The last scene
+// to decide counts the scenes that continue for the next launch.
 template <class T>
 __device__ __forceinline__ void batch_decide(const DevParams<T> &P, const DevBufs<T> &B, cudaGraphConditionalHandle h,
-                                             int use_handle)
+                                             int use_handle, bool all_scenes)
 {
     unsigned any;
     if (P.nscenes == 1) {
         any = B.sc[0].cont;
     } else {
+        const unsigned expect = all_scenes ? P.nscenes : __ldcg(&B.gsc->live);
         __threadfence();
         const unsigned t = atomicAdd(B.counters + P.nscenes, 1u);
-        if (t != P.nscenes - 1) return;
+        if (t != expect - 1) return;
         __threadfence();
         any = 0;
-        for (uint32_t s = 0; s < P.nscenes; s++) any |= __ldcg(&B.sc[s].cont);
+        for (uint32_t s = 0; s < P.nscenes; s++) any += __ldcg(&B.sc[s].cont) != 0u ? 1u : 0u;
         B.counters[P.nscenes] = 0;
+        B.gsc->live = any;
     }
     if (B.gsc->flags & kFlagLoopGuard) any = 0;
     B.gsc->cont = any ? 1u : 0u;
@@ -699,26 +705,48 @@ __device__ __forceinline__ void build_one(const DevParams<T> &P, const DevBufs<T
                             Ll = nullptr;
                         }
                     }
-                    for (uint32_t j = s; j < e; j++) {
-                        T ddx, ddy, ddz;
-                        if (j != i && pair_d2(xi, ldv(B.x, j), ddx, ddy, ddz) < P.K.h2) {
-                            if (nf < P.capf) {
-                                Lf[32u * (nf >> P.lpp_log2) + (nf & (lpp - 1u))] = j;
-                                if (Ll) Ll[32u * nf] = (uint16_t)(lbase + j);
-                            }
-                            nf++;
+                    auto accept = [&](uint32_t j) {
+                        if (nf < P.capf) {
+                            Lf[32u * (nf >> P.lpp_log2) + (nf & (lpp - 1u))] = j;
+                            if (Ll) Ll[32u * nf] = (uint16_t)(lbase + j);
                         }
+                        nf++;
+                    };
+                    // two candidates per iteration, both loads in flight before either test; the
+                    // appends keep the order j, j + 1
+                    uint32_t j = s;
+                    for (; j + 1u < e; j += 2u) {
+                        const v4_t<T> xa = ldv(B.x, j), xb = ldv(B.x, j + 1u);
+                        T ddx, ddy, ddz;
+                        const bool ia = pair_d2(xi, xa, ddx, ddy, ddz) < P.K.h2 && j != i;
+                        const bool ib = pair_d2(xi, xb, ddx, ddy, ddz) < P.K.h2 && j + 1u != i;
+                        if (ia) accept(j);
+                        if (ib) accept(j + 1u);
+                    }
+                    if (j < e) {
+                        T ddx, ddy, ddz;
+                        if (j != i && pair_d2(xi, ldv(B.x, j), ddx, ddy, ddz) < P.K.h2) accept(j);
                     }
                 }
                 s = B.bcstart[c];
                 if (s != kEmpty) {
                     const uint32_t e = B.bcend[c];
-                    for (uint32_t j = s; j < e; j++) {
+                    auto accept = [&](uint32_t j) {
+                        if (nb < P.capb) Lb[nb * 32u] = j;
+                        nb++;
+                    };
+                    uint32_t j = s;
+                    for (; j + 1u < e; j += 2u) {
+                        const v4_t<T> xa = ldv(B.xb, j), xb = ldv(B.xb, j + 1u);
                         T ddx, ddy, ddz;
-                        if (pair_d2(xi, ldv(B.xb, j), ddx, ddy, ddz) < P.K.h2) {
-                            if (nb < P.capb) Lb[nb * 32u] = j;
-                            nb++;
-                        }
+                        const bool ia = pair_d2(xi, xa, ddx, ddy, ddz) < P.K.h2;
+                        const bool ib = pair_d2(xi, xb, ddx, ddy, ddz) < P.K.h2;
+                        if (ia) accept(j);
+                        if (ib) accept(j + 1u);
+                    }
+                    if (j < e) {
+                        T ddx, ddy, ddz;
+                        if (pair_d2(xi, ldv(B.xb, j), ddx, ddy, ddz) < P.K.h2) accept(j);
                     }
                 }
             }
@@ -1117,9 +1145,11 @@ __global__ void __launch_bounds__(kBlock, kJacobiMinBlocks<T, LPP>) k_jacobi(Dev
     // fluid phases: this launch updates the particles of one phase (TimeStepDFSPH.cpp:322-339)
     if (phase >= 0 && q.act && B.ph[q.i] != (uint32_t)phase) q.act = false;
     StepScalars *const sc = B.sc + q.s;
-    const bool live = scene_live(P, sc);
+    // a scene whose loop has stopped: its blocks return at once (block uniform; batch_decide
+    // expects only the live scenes)
+    if (!scene_live(P, sc)) return;
     double err = 0.0;
-    if (live) {   // block uniform
+    {
         T apj;
         if constexpr (LPP == 1 && sizeof(T) == 4) {
             extern __shared__ float2 stage_f2[];   // 3 x kStageCapJacobi when staged
@@ -1171,8 +1201,8 @@ __global__ void __launch_bounds__(kBlock, kJacobiMinBlocks<T, LPP>) k_jacobi(Dev
     const int ph = phase;
     grid_sum_finalize<1>(mine, scene_reduce<LPP>(P, B, q), [&](const DSum<1> &tot) {
         if (ph < 0) {
-            if (live) solver_decide<T, DIV>(PP, sc, n_s ? tot.v[0] / (double)n_s : 0.0);
-            batch_decide(PP, BB, handle, use_handle);
+            solver_decide<T, DIV>(PP, sc, n_s ? tot.v[0] / (double)n_s : 0.0);
+            batch_decide(PP, BB, handle, use_handle, false);
         } else {   // one phase's average error against its own tolerance; the last phase decides
             uint32_t cnt;
             T r0;
@@ -1183,7 +1213,7 @@ __global__ void __launch_bounds__(kBlock, kJacobiMinBlocks<T, LPP>) k_jacobi(Dev
             sc->phase_ok = ph == 0 ? ok : (sc->phase_ok | ok);
             if (ph + 1 == (int)PP.nphase) {
                 solver_decide<T, DIV>(PP, sc, avg, 1u, sc->phase_ok == (1u << PP.nphase) - 1u);
-                batch_decide(PP, BB, handle, use_handle);
+                batch_decide(PP, BB, handle, use_handle, false);
             }
         }
     });
@@ -1243,6 +1273,7 @@ __global__ void k_loop_begin(StepScalars *sc, StepScalars *gsc, uint32_t nscenes
     }
     if (threadIdx.x == 0) {
         gsc->cont = cont;
+        gsc->live = cont ? nscenes : 0u;
         gsc->loop_guard = 0;
     }
 }
@@ -1571,7 +1602,7 @@ __global__ void __launch_bounds__(kBlock) k_visc_setup(DevParams<T> P, DevBufs<T
         const bool cont = sc->cg_state == 0 && maxit > 0;
         if (sc->cg_state == 0 && maxit == 0) sc->cg_err = sqrt(tot.v[1] / tot.v[0]);
         sc->cont = cont ? 1u : 0u;
-        batch_decide(PP, BB, handle, use_handle);
+        batch_decide(PP, BB, handle, use_handle, true);
     });
 }
 
@@ -1585,10 +1616,10 @@ __global__ void __launch_bounds__(kBlock) k_cg_matvec(DevParams<T> P, DevBufs<T>
     SlotInfo q = slot_info<LPP>(P);
     if (phase >= 0 && q.act && B.ph[q.i] != (uint32_t)phase) q.act = false;   // fluid phases
     StepScalars *const sc = B.sc + q.s;
-    const bool live = scene_live(P, sc);
+    if (!scene_live(P, sc)) return;   // block uniform: a scene whose CG has stopped
     DSum<1> mine;
     mine.v[0] = 0.0;
-    if (live) {   // uniform over the block
+    {
         V3<T> acc = mk3<T>(0, 0, 0), pi = mk3<T>(0, 0, 0);
         T rhoi = T(1);
         if (q.act) {
@@ -1617,9 +1648,8 @@ __global__ void __launch_bounds__(kBlock) k_cg_matvec(DevParams<T> P, DevBufs<T>
             mine.v[0] = (double)dot(pi, t);
         }
     }
-    grid_sum_finalize<1>(mine, scene_reduce<LPP>(P, B, q), [&](const DSum<1> &tot) {
-        if (live) sc->cg_alpha = sc->cg_absnew / tot.v[0];
-    });
+    grid_sum_finalize<1>(mine, scene_reduce<LPP>(P, B, q),
+                         [&](const DSum<1> &tot) { sc->cg_alpha = sc->cg_absnew / tot.v[0]; });
 }
 
 // x += alpha p; r -= alpha tmp; |r|^2; z = M^-1 r; r.z -> beta (ConjugateGradient.h:77-88).
@@ -1632,10 +1662,10 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(DevParams<T> P, DevBufs<T>
     SlotInfo q = slot_info(P);
     if (phase >= 0 && q.act && B.ph[q.i] != (uint32_t)phase) q.act = false;   // fluid phases
     StepScalars *const sc = B.sc + q.s;
-    const bool live = scene_live(P, sc);
+    if (!scene_live(P, sc)) return;   // block uniform: a scene whose CG has stopped
     DSum<2> mine;
     mine.v[0] = mine.v[1] = 0.0;
-    if (q.act && live) {
+    if (q.act) {
         const uint32_t i = q.i;
         const T alpha = (T)sc->cg_alpha;
         const V3<T> p = xyz<T>(ldv(B.cg_p, i));
@@ -1655,7 +1685,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(DevParams<T> P, DevBufs<T>
     const DevParams<T> &PP = P;
     const DevBufs<T> &BB = B;
     grid_sum_finalize<2>(mine, scene_reduce(P, B, q), [&](const DSum<2> &tot) {
-        if (live) {
+        {
             sc->cg_res2 = tot.v[0];
             sc->cg_err = sqrt(tot.v[0] / sc->cg_rhs2);
             bool cont;
@@ -1672,7 +1702,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(DevParams<T> P, DevBufs<T>
             }
             sc->cont = cont ? 1u : 0u;
         }
-        batch_decide(PP, BB, handle, use_handle);
+        batch_decide(PP, BB, handle, use_handle, false);
     });
 }
 
@@ -2354,7 +2384,7 @@ __global__ void __launch_bounds__(kBlock) k_ws_sweep(DevParams<T> P, DevBufs<T> 
         if (learned) sc->ws_used |= (1u << k);
         else sc->ws_used &= ~(1u << k);
         solver_decide<T, DIV>(PP, sc, (learned ? tot.v[1] : tot.v[0]) * inv, sweeps);
-        batch_decide(PP, BB, handle, use_handle);
+        batch_decide(PP, BB, handle, use_handle, true);
     });
 }
 

@@ -40,7 +40,8 @@ struct StepScalars {
     unsigned loop_guard;   // body executions of the running device-side loop (global record)
     unsigned launches;     // kernels launched in the current step (global record)
     unsigned ws_used;      // bit 0: learned warm start used by the divergence solve, bit 1: pressure solve
-    unsigned pad[2];
+    unsigned live;         // scenes whose running loop continues (global record, batches)
+    unsigned pad1;
     unsigned long long maxvel_bits64;   // FP64 contexts: max |v + a h|^2 as the bits of a non-negative double
     unsigned phase_ok;  // fluid phases: bit k set when phase k met its tolerance in the running iteration
     // Weiler2018 with fluid phases, one CG system per phase: iterations summed over the phases,
