@@ -682,16 +682,28 @@ __device__ __forceinline__ void build_one(const DevParams<T> &P, const DevBufs<T
             if (y < 0 || y >= S.dimy) continue;
             const T syz = sz + (dy < 0 ? slo[1] : (dy > 0 ? shi[1] : T(0)));
             const bool inner_yz = inner_z && y > 0 && y < S.dimy - 1;
-            for (int dx = -1; dx <= 1; dx++) {
-                const int x = cx + dx;
-                if (x < 0 || x >= S.dimx) continue;
+            // the row's three cells (dx = -1, 0, 1): their fluid and boundary ranges are loaded
+            // together, so their latencies overlap; a culled or outside cell gets an empty range
+            uint32_t rc[3], rfs[3], rfe[3], rbs[3], rbe[3];
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                const int dx = k - 1, x = cx + dx;
                 // border cells may hold clamped particles outside their box: never culled
                 const bool inner = inner_yz && x > 0 && x < S.dimx - 1;
-                if (inner && syz + (dx < 0 ? slo[0] : (dx > 0 ? shi[0] : T(0))) > cull) continue;
-                const uint32_t c = S.cell_off + local_cell(S, x, y, z);
-                uint32_t s = B.cstart[c];
+                const bool use = x >= 0 && x < S.dimx &&
+                                 !(inner && syz + (dx < 0 ? slo[0] : (dx > 0 ? shi[0] : T(0))) > cull);
+                rc[k] = use ? S.cell_off + local_cell(S, x, y, z) : 0u;
+                rfs[k] = use ? B.cstart[rc[k]] : kEmpty;
+                rfe[k] = use ? B.cend[rc[k]] : 0u;
+                rbs[k] = use ? B.bcstart[rc[k]] : kEmpty;
+                rbe[k] = use ? B.bcend[rc[k]] : 0u;
+            }
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                const uint32_t c = rc[k];
+                uint32_t s = rfs[k];
                 if (s != kEmpty) {
-                    const uint32_t e = B.cend[c];
+                    const uint32_t e = rfe[k];
                     // staged index of slot j: lbase + j.  The stage table holds every fluid cell
                     // this loop visits; should a cell be missing, the block falls back to the
                     // unstaged passes (its stage header is cleared) and no local index is used.
@@ -728,9 +740,9 @@ __device__ __forceinline__ void build_one(const DevParams<T> &P, const DevBufs<T
                         if (j != i && pair_d2(xi, ldv(B.x, j), ddx, ddy, ddz) < P.K.h2) accept(j);
                     }
                 }
-                s = B.bcstart[c];
+                s = rbs[k];
                 if (s != kEmpty) {
-                    const uint32_t e = B.bcend[c];
+                    const uint32_t e = rbe[k];
                     auto accept = [&](uint32_t j) {
                         if (nb < P.capb) Lb[nb * 32u] = j;
                         nb++;
