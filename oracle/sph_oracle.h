@@ -14,14 +14,21 @@
  *     MatrixFreeSolver.h + vendored Eigen 3.4 ConjugateGradient, run on the
  *     oracle's own Weiler2018 operator (tests/golden/).
  *   - DFSPH / Akinci2012 / XSPH / Weiler2018 per-particle sums and the solver
- *     loops: parity unpinned.  The reference has no golden vectors for them and
- *     its full library cannot be built here (it needs the CompactNSearch,
- *     GenericParameters and Discregrid external projects, which are absent).
+ *     loops: pinned against the reference's own TimeStepDFSPH step.  The
+ *     reference's library sources are compiled by oracle/build_ref.sh (FP64,
+ *     analytic kernel) against stand-ins for its absent external projects
+ *     (oracle/shims/), and one reference step from three float32 states is
+ *     stored in tests/golden/ref_step_*.npz; this oracle reproduces each to
+ *     1e-10 with equal iteration counts (tests/test_reference_pin.py).
  *     Every function below cites the reference file:line it restates.
+ *   - The neighbour predicate: CompactNSearch is not in the reference tree, so
+ *     the documented |x_i - x_j|^2 < h^2 (self excluded) stands for it, here, on
+ *     the GPU and in the reference build's stand-in alike.
  *
  * Build: two precisions from one source (ORC_REAL = double | float).  The FP64
- * build is the parity oracle; the FP32 build is the CPU timing baseline (a
- * port of the reference's FP32 OpenMP path, not the reference binary).
+ * build is the parity oracle; the FP32 build is the CPU baseline where the
+ * reference's own FP32 AVX build cannot run (a port of the reference's FP32
+ * OpenMP path, not the reference binary).
  */
 #ifndef SPH_ORACLE_H
 #define SPH_ORACLE_H

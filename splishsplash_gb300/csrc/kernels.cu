@@ -252,6 +252,16 @@ template <class T> __device__ __forceinline__ V3<T> diff3(const v4_t<T> &a, cons
     return V3<T>{(T)a.x - (T)b.x, (T)a.y - (T)b.y, (T)a.z - (T)b.z};
 }
 
+// A list entry: read once per pass, so it is not kept in L1, where it would displace the
+// neighbour records that the gathers reuse
+__device__ __forceinline__ uint32_t ld_list(const uint32_t *p)
+{
+    uint32_t v;
+    asm("ld.global.nc.L1::no_allocate.u32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ uint32_t ld_list(const uint16_t *p) { return __ldg(p); }
+
 // Neighbour loop with U independent index loads, then U dependent gathers, then
 // U computations, so that each thread keeps several loads in flight.  Idx: uint32_t for
 // the lists of global slots, uint16_t for the local lists of the staged passes.
@@ -262,7 +272,7 @@ __device__ __forceinline__ void nbr_loop(const Idx *__restrict__ L, uint32_t cnt
     for (; k + U <= cnt; k += U) {
         uint32_t j[U];
 #pragma unroll
-        for (int u = 0; u < U; u++) j[u] = __ldg(L + (k + u) * STRIDE);
+        for (int u = 0; u < U; u++) j[u] = ld_list(L + (k + u) * STRIDE);
         decltype(ld(0u)) d[U];
 #pragma unroll
         for (int u = 0; u < U; u++) d[u] = ld(j[u]);
@@ -270,7 +280,7 @@ __device__ __forceinline__ void nbr_loop(const Idx *__restrict__ L, uint32_t cnt
         for (int u = 0; u < U; u++) cp(j[u], d[u]);
     }
     for (; k < cnt; k++) {
-        const uint32_t jj = __ldg(L + k * STRIDE);
+        const uint32_t jj = ld_list(L + k * STRIDE);
         cp(jj, ld(jj));
     }
 }
@@ -290,7 +300,7 @@ __device__ __forceinline__ void boundary_loop(const DevParams<T> &P, const DevBu
     const uint32_t *L = list_ptr(B.lb, i, P.capb) + 32u * l;
     const uint32_t cnt = lane_count<LPP>(nb, l);
     for (uint32_t k = 0; k < cnt; k++) {
-        const uint32_t j = __ldg(L + k * 32u * LPP);
+        const uint32_t j = ld_list(L + k * 32u * LPP);
         cp(j, ldv(B.xb, j));
     }
 }
