@@ -462,6 +462,9 @@ template <class T> DevParams<T> make_params(const sphgb_ctx *c)
     P.nphase = 1;
     if (c->phase_counts.size() > 1 && c->r0) {
         P.nphase = (uint32_t)c->phase_counts.size();
+        // the step-wide XSPH and boundary-viscosity switches follow the phases' own coefficients
+        // (which fall back to the shared ones where a phase sets none): any non-zero one
+        P.xsph = P.xsph_b = P.mub = T(0);
         uint32_t end = 0;
         for (uint32_t k = 0; k < 8; k++) {
             const bool has = k < P.nphase;
@@ -473,10 +476,8 @@ template <class T> DevParams<T> make_params(const sphgb_ctx *c)
             P.phase_nub[k] = (T)phase_nub(c, k);
             P.phase_xs[k] = (T)(k < c->phase_xs.size() ? c->phase_xs[k] : q.xsph);
             P.phase_xsb[k] = (T)(k < c->phase_xsb.size() ? c->phase_xsb[k] : q.xsph_boundary);
-            // the XSPH switches of the whole step: any phase's coefficient
             if (has && P.xsph == T(0)) P.xsph = P.phase_xs[k];
             if (has && P.xsph_b == T(0)) P.xsph_b = P.phase_xsb[k];
-            // the boundary-viscosity switch of the whole step: any phase's mu_b
             if (has && P.mub == T(0)) P.mub = (T)(phase_nub(c, k) * c->phase_rho0[k]);
         }
         P.staged = 0;   // the staged passes read one rest density

@@ -261,18 +261,31 @@ __device__ __forceinline__ uint32_t ld_list(const uint32_t *p)
     return v;
 }
 __device__ __forceinline__ uint32_t ld_list(const uint16_t *p) { return __ldg(p); }
+// ... and one that the reading thread itself wrote earlier in the same kernel (the list build):
+// a coherent load, also without L1 allocation
+__device__ __forceinline__ uint32_t ld_own_list(const uint32_t *p)
+{
+    uint32_t v;
+    asm volatile("ld.global.L1::no_allocate.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
 
 // Neighbour loop with U independent index loads, then U dependent gathers, then
 // U computations, so that each thread keeps several loads in flight.  Idx: uint32_t for
-// the lists of global slots, uint16_t for the local lists of the staged passes.
-template <int U, uint32_t STRIDE = 32u, class Idx, class Ld, class Cp>
+// the lists of global slots, uint16_t for the local lists of the staged passes.  OWN: the
+// list was written by this thread in the same kernel.
+template <int U, uint32_t STRIDE = 32u, bool OWN = false, class Idx, class Ld, class Cp>
 __device__ __forceinline__ void nbr_loop(const Idx *__restrict__ L, uint32_t cnt, Ld ld, Cp cp)
 {
+    auto idx = [&](uint32_t k) -> uint32_t {
+        if constexpr (OWN) return ld_own_list(L + k * STRIDE);
+        else return ld_list(L + k * STRIDE);
+    };
     uint32_t k = 0;
     for (; k + U <= cnt; k += U) {
         uint32_t j[U];
 #pragma unroll
-        for (int u = 0; u < U; u++) j[u] = ld_list(L + (k + u) * STRIDE);
+        for (int u = 0; u < U; u++) j[u] = idx(k + u);
         decltype(ld(0u)) d[U];
 #pragma unroll
         for (int u = 0; u < U; u++) d[u] = ld(j[u]);
@@ -280,7 +293,7 @@ __device__ __forceinline__ void nbr_loop(const Idx *__restrict__ L, uint32_t cnt
         for (int u = 0; u < U; u++) cp(j[u], d[u]);
     }
     for (; k < cnt; k++) {
-        const uint32_t jj = ld_list(L + k * STRIDE);
+        const uint32_t jj = idx(k);
         cp(jj, ld(jj));
     }
 }
@@ -785,7 +798,7 @@ __device__ __forceinline__ void build_one(const DevParams<T> &P, const DevBufs<T
     // the own list, sub-list by sub-list (entries l, l + lpp, ... are 32 words apart)
     const uint32_t nfc = min(nf, P.capf);
     for (uint32_t l = 0; l < lpp; l++)
-        nbr_loop<kUnroll>(Lf + l, nfc > l ? (nfc - l + lpp - 1u) >> P.lpp_log2 : 0u,
+        nbr_loop<kUnroll, 32u, true>(Lf + l, nfc > l ? (nfc - l + lpp - 1u) >> P.lpp_log2 : 0u,
                           [&](uint32_t j) { return XV{ldv(B.x, j), ldv(B.v, j)}; },
                           [&](uint32_t, const XV &d) {
                               const V3<T> r = diff3<T>(xi, d.x);
@@ -816,7 +829,7 @@ __device__ __forceinline__ void build_one(const DevParams<T> &P, const DevBufs<T
             bvg += dot(vj, g);
         }
     };
-    nbr_loop<kUnroll>(Lb, min(nb, P.capb), [&](uint32_t j) { return ldv(B.xb, j); }, boundary_term);
+    nbr_loop<kUnroll, 32u, true>(Lb, min(nb, P.capb), [&](uint32_t j) { return ldv(B.xb, j); }, boundary_term);
     // Bender2019: the volume-map sample of each body, x_j with V_j in w, where V_j > 0; a moving
     // body's point velocity v_j enters the same sums
     const uint2 mr = scene_maps(P, scene);
