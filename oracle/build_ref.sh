@@ -47,6 +47,10 @@ build_lib() {   # name, flags...
   # vendored third-party code the library links (extern/md5, extern/tinyexpr)
   $CXX -std=c++17 -fPIC -w -O2 -I"$REF/extern/md5" -c "$REF/extern/md5/md5.cpp" -o "$obj/extern_md5.o"
   ${CC:-gcc} -fPIC -w -O2 -c "$REF/extern/tinyexpr/tinyexpr.c" -o "$obj/extern_tinyexpr.o"
+  # the oracle's grid evaluation behind ref_driver.cpp's Discregrid grid (volume maps), with
+  # the oracle's kernel functions it uses (FP64)
+  ${CC:-gcc} -std=c11 -fPIC -fopenmp -w -O2 -ffp-contract=off -DORC_REAL=double -c "$HERE/vmap.c" -o "$obj/oracle_vmap.o"
+  ${CC:-gcc} -std=c11 -fPIC -fopenmp -w -O2 -ffp-contract=off -DORC_REAL=double -c "$HERE/sph_oracle.c" -o "$obj/oracle_sph.o"
   $CXX -shared -fopenmp -Wl,--no-undefined -o "$OUT/lib$name.so.tmp" "$obj"/*.o -lm
   mv "$OUT/lib$name.so.tmp" "$OUT/lib$name.so"
 }

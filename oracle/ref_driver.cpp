@@ -12,12 +12,19 @@
 // exists, as readParameters does (Simulation.cpp:535-602), which forces the
 // precomputed kernel; `analytic_kernel` then selects the analytic cubic spline
 // (setKernel(0); setGradKernel(0)), as the FP64 oracle protocol asks.
+// With boundaryMethod 2 the boundary is Bender2019 volume maps: each body is a
+// BoundaryModel_Bender2019 whose Discregrid::DiscreteGrid is OracleGrid below, a grid
+// evaluated by the oracle's restatement of Discregrid's cubic Lagrange grid
+// (oracle/vmap.c; Discregrid itself is not in the reference tree).  The reference's own
+// Bender2019 code then runs on it: TimeStep::computeVolumeAndBoundaryX and the Bender2019
+// branches of TimeStepDFSPH, XSPH and Viscosity_Weiler2018.
 // Only tests/ and bench.py's CPU legs load the library built from this file.
 #include "SPlisHSPlasH/Common.h"
 #include "SPlisHSPlasH/Simulation.h"
 #include "SPlisHSPlasH/TimeManager.h"
 #include "SPlisHSPlasH/FluidModel.h"
 #include "SPlisHSPlasH/BoundaryModel_Akinci2012.h"
+#include "SPlisHSPlasH/BoundaryModel_Bender2019.h"
 #include "SPlisHSPlasH/StaticRigidBody.h"
 #include "SPlisHSPlasH/TimeStep.h"
 #include "SPlisHSPlasH/DFSPH/TimeStepDFSPH.h"
@@ -29,8 +36,11 @@
 
 #include <chrono>
 #include <cstring>
+#include <limits>
 #include <string>
 #include <vector>
+
+#include "sph_oracle.h"
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -58,6 +68,7 @@ struct RefParams {
     double viscoMaxError;
     int analyticKernel;    // 1: setKernel(0); setGradKernel(0) after the parameters
     int numThreads;        // 0: OpenMP default
+    int boundaryMethod;    // 0 Akinci2012 (boundary particles), 2 Bender2019 (the volume maps registered)
 };
 
 struct RefStats {
@@ -71,6 +82,65 @@ namespace {
 StaticRigidBody *g_body = nullptr;
 std::vector<Vector3r> g_x, g_v, g_xb;
 std::vector<unsigned int> g_objectIds;
+
+// A volume map as the oracle holds it: signed distance (field 0) and volume (field 1) at the
+// nodes of the 32-node cubic serendipity grid over [dmin, dmax], body pose R (row-major), t.
+struct MapData {
+    double dmin[3], dmax[3], R[9], t[3];
+    unsigned res[3];
+    std::vector<double> f0, f1;
+};
+std::vector<MapData> g_maps;
+
+// The Discregrid grid interface that the reference's Bender2019 code calls, over a MapData.
+// determineShapeFunctions reports whether x lies in the grid; interpolate evaluates the field
+// (and its gradient) at x with the oracle's grid, so the cell, N and dN that the caller passes
+// back are not needed.  Outside the grid the value is the maximum double, as Discregrid's.
+class OracleGrid : public Discregrid::DiscreteGrid
+{
+public:
+    explicit OracleGrid(const MapData &d) : m_d(d)
+    {
+        std::memset(&m_m, 0, sizeof(m_m));
+        for (int k = 0; k < 3; k++) {
+            m_m.dmin[k] = m_d.dmin[k];
+            m_m.dmax[k] = m_d.dmax[k];
+            m_m.res[k] = m_d.res[k];
+            m_m.t[k] = m_d.t[k];
+        }
+        for (int k = 0; k < 9; k++) m_m.R[k] = m_d.R[k];
+        m_m.field[0] = m_d.f0.data();
+        m_m.field[1] = m_d.f1.data();
+    }
+    bool determineShapeFunctions(unsigned int field, Eigen::Vector3d const &x, std::array<unsigned int, 32> &,
+                                 Eigen::Vector3d &, Eigen::Matrix<double, 32, 1> &,
+                                 Eigen::Matrix<double, 32, 3> * = nullptr) const override
+    {
+        double v;
+        return orc_vmap_interpolate(&m_m, (int)field, x.data(), &v, nullptr) != 0;
+    }
+    double interpolate(unsigned int field, Eigen::Vector3d const &x, const std::array<unsigned int, 32> &,
+                       const Eigen::Vector3d &, const Eigen::Matrix<double, 32, 1> &, Eigen::Vector3d *gradient = nullptr,
+                       Eigen::Matrix<double, 32, 3> * = nullptr) const override
+    {
+        return eval(field, x, gradient);
+    }
+    double interpolate(unsigned int field, Eigen::Vector3d const &x, Eigen::Vector3d *gradient = nullptr) const override
+    {
+        return eval(field, x, gradient);
+    }
+
+private:
+    MapData m_d;
+    orc_vmap m_m;
+    double eval(unsigned int field, Eigen::Vector3d const &x, Eigen::Vector3d *gradient) const
+    {
+        double v, g[3];
+        if (!orc_vmap_interpolate(&m_m, (int)field, x.data(), &v, g)) return std::numeric_limits<double>::max();
+        if (gradient) *gradient = Eigen::Vector3d(g[0], g[1], g[2]);
+        return v;
+    }
+};
 
 int method_index(std::vector<Simulation::NonPressureForceMethod> &methods, const std::string &name)
 {
@@ -116,7 +186,9 @@ int ref_create(const RefParams *p, unsigned int n, const double *x, const double
     Utilities::Timing::m_dontPrintTimes = true;
     Simulation *sim = Simulation::getCurrent();
     sim->init(static_cast<Real>(p->particleRadius), false);
-    sim->setBoundaryHandlingMethod(BoundaryHandlingMethods::Akinci2012);
+    const bool maps = p->boundaryMethod == 2;
+    if (maps && g_maps.empty()) return 5;
+    sim->setBoundaryHandlingMethod(maps ? BoundaryHandlingMethods::Bender2019 : BoundaryHandlingMethods::Akinci2012);
 
     g_x.resize(n);
     g_v.resize(n);
@@ -173,7 +245,25 @@ int ref_create(const RefParams *p, unsigned int n, const double *x, const double
     for (unsigned int i = 0; i < nb; i++)
         g_xb[i] = Vector3r(static_cast<Real>(xb[3 * i]), static_cast<Real>(xb[3 * i + 1]),
                            static_cast<Real>(xb[3 * i + 2]));
-    if (nb > 0) {
+    if (maps) {
+        // StaticBoundarySimulator::initBoundaryData with Bender2019: one static body per map at
+        // its pose, a BoundaryModel_Bender2019 holding the map (StaticBoundarySimulator.cpp:167-174)
+        for (const MapData &d : g_maps) {
+            StaticRigidBody *rb = new StaticRigidBody();
+            Matrix3r R;
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++) R(r, c) = static_cast<Real>(d.R[3 * r + c]);
+            const Vector3r t(static_cast<Real>(d.t[0]), static_cast<Real>(d.t[1]), static_cast<Real>(d.t[2]));
+            rb->setPosition0(t);
+            rb->setPosition(t);
+            rb->setRotation0(Quaternionr(R));
+            rb->setRotation(Quaternionr(R));
+            BoundaryModel_Bender2019 *bm = new BoundaryModel_Bender2019();
+            bm->initModel(rb);
+            sim->addBoundaryModel(bm);
+            bm->setMap(new OracleGrid(d));
+        }
+    } else if (nb > 0) {
         g_body = new StaticRigidBody();
         g_body->setPosition0(Vector3r::Zero());
         g_body->setPosition(Vector3r::Zero());
@@ -189,7 +279,7 @@ int ref_create(const RefParams *p, unsigned int n, const double *x, const double
     // SimulatorBase::deferredInit -> Simulation::deferredInit, StaticBoundarySimulator::deferredInit
     sim->deferredInit();
     sim->performNeighborhoodSearchSort();
-    if (nb > 0) sim->updateBoundaryVolume();
+    if (!maps && nb > 0) sim->updateBoundaryVolume();
     sim->setSimulationInitialized(true);
     if (p->analyticKernel) {
         sim->setKernel(Simulation::ENUM_KERNEL_CUBIC);
@@ -297,6 +387,29 @@ int ref_timing(const char *name, double *total_ms, unsigned int *count)
 }
 
 int ref_precision() { return static_cast<int>(sizeof(Real)); }
+
+/** Registers a volume map for the next ref_create with boundaryMethod 2: the grid's domain and
+ *  cells per axis, the node values of the signed distance and of the volume
+ *  (orc_vmap_nodes(res) each, the node order of oracle/vmap.c) and the body's pose. */
+int ref_add_volume_map(const double *dmin, const double *dmax, const unsigned int *res, const double *f0,
+                       const double *f1, const double *R, const double *t)
+{
+    MapData d;
+    for (int k = 0; k < 3; k++) {
+        d.dmin[k] = dmin[k];
+        d.dmax[k] = dmax[k];
+        d.res[k] = res[k];
+        d.t[k] = t[k];
+    }
+    for (int k = 0; k < 9; k++) d.R[k] = R[k];
+    const size_t n = orc_vmap_nodes(d.res);
+    d.f0.assign(f0, f0 + n);
+    d.f1.assign(f1, f1 + n);
+    g_maps.push_back(std::move(d));
+    return (int)g_maps.size();
+}
+
+void ref_clear_volume_maps() { g_maps.clear(); }
 
 void ref_destroy()
 {

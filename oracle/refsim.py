@@ -35,7 +35,8 @@ class RefParams(ctypes.Structure):
                 ("maxErrorV", ctypes.c_double), ("xsph", ctypes.c_double), ("xsphBoundary", ctypes.c_double),
                 ("viscosityMethod", ctypes.c_int), ("viscosity", ctypes.c_double),
                 ("viscosityBoundary", ctypes.c_double), ("viscoMaxIter", ctypes.c_int),
-                ("viscoMaxError", ctypes.c_double), ("analyticKernel", ctypes.c_int), ("numThreads", ctypes.c_int)]
+                ("viscoMaxError", ctypes.c_double), ("analyticKernel", ctypes.c_int), ("numThreads", ctypes.c_int),
+                ("boundaryMethod", ctypes.c_int)]
 
 
 class RefStats(ctypes.Structure):
@@ -77,6 +78,10 @@ def lib(precision: str = "f64", path: str = None) -> ctypes.CDLL:
         L.ref_timing.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint)]
         L.ref_timing.restype = ctypes.c_int
         L.ref_destroy.restype = None
+        up = ctypes.POINTER(ctypes.c_uint)
+        L.ref_add_volume_map.argtypes = [dp, dp, up, dp, dp, dp, dp]
+        L.ref_add_volume_map.restype = ctypes.c_int
+        L.ref_clear_volume_maps.restype = None
         _LIBS[key] = L
     return _LIBS[key]
 
@@ -88,12 +93,14 @@ def _dp(a):
 class RefSim:
     """One scene stepped by the reference.  analytic_kernel=True selects the analytic
     cubic spline after the parameters are read (the FP64 oracle protocol); False keeps
-    the reference's default PrecomputedKernel<CubicKernel, 10000> for DFSPH."""
+    the reference's default PrecomputedKernel<CubicKernel, 10000> for DFSPH.
+    volume_maps: oracle.VolumeMap objects (static bodies): the boundary is then Bender2019
+    with those maps instead of the scene's boundary particles."""
 
     _alive = False
 
     def __init__(self, scene, precision: str = "f64", analytic_kernel: bool = True, num_threads: int = 0,
-                 library: str = None):
+                 library: str = None, volume_maps=None):
         if RefSim._alive:
             raise RuntimeError("the reference's Simulation is a singleton: close the other RefSim first")
         self.L = lib(precision, library)
@@ -123,6 +130,17 @@ class RefSim:
         rp.viscoMaxError = p.viscoMaxError
         rp.analyticKernel = int(analytic_kernel)
         rp.numThreads = num_threads
+        self.L.ref_clear_volume_maps()
+        for vm in volume_maps or ():
+            c = vm.m   # the oracle's orc_vmap: domain, cells per axis, pose
+            res = np.array(list(c.res), np.uint32)
+            arr = lambda a: np.array(list(a), np.float64)
+            self.L.ref_add_volume_map(_dp(arr(c.dmin)), _dp(arr(c.dmax)),
+                                      res.ctypes.data_as(ctypes.POINTER(ctypes.c_uint)),
+                                      _dp(np.ascontiguousarray(vm.fields[0], np.float64)),
+                                      _dp(np.ascontiguousarray(vm.fields[1], np.float64)),
+                                      _dp(arr(c.R)), _dp(arr(c.t)))
+        rp.boundaryMethod = 2 if volume_maps else 0
         x = np.ascontiguousarray(scene.x, np.float64)
         v = np.ascontiguousarray(scene.v, np.float64)
         xb = np.ascontiguousarray(scene.xb, np.float64).reshape(-1, 3)

@@ -14,6 +14,10 @@ to this script, by particle id:
                         (float32), params (JSON); outputs (float64): density,
                         factor, density_adv, kappa, kappa_v, v, x, vdiff, dt_next,
                         time step counts (iterations, iterations_v, visco_iterations)
+  The volume-map case (vmap_box) has no boundary particles: its boundary is a Bender2019
+  volume map of the box, built by the oracle (oracle/vmap.c) from the box mesh and handed to
+  the reference's Bender2019 code through the driver's Discregrid grid; the fixture records
+  the map's cells per axis and box (vmap_res, vmap_box) so that a test rebuilds it.
   ref_kernel_table_delta.json  the same config-0 step with the reference's default
                         PrecomputedKernel<CubicKernel, 10000> against the analytic
                         kernel: max and mean relative difference per field
@@ -43,10 +47,10 @@ def f32(a):
     return np.asarray(a, np.float64).astype(np.float32).astype(np.float64)
 
 
-def advanced_state(scene, warm):
+def advanced_state(scene, warm, maps=None):
     """The scene after `warm` reference steps, rounded to float32."""
     visc = scene.params.viscosityMethod == 6
-    with refsim.RefSim(scene) as r:
+    with refsim.RefSim(scene, volume_maps=maps) as r:
         for _ in range(warm):
             r.step()
         st = dict(x=f32(r.get("position")), v=f32(r.get("velocity")), kappa=f32(r.get("p / rho^2")),
@@ -56,11 +60,11 @@ def advanced_state(scene, warm):
     return st
 
 
-def step_from(scene, st, analytic=True):
+def step_from(scene, st, analytic=True, maps=None):
     """One reference step from state st; outputs by particle id."""
     sc = dataclasses.replace(scene, x=st["x"], v=st["v"])
     visc = scene.params.viscosityMethod == 6
-    with refsim.RefSim(sc, analytic_kernel=analytic) as r:
+    with refsim.RefSim(sc, analytic_kernel=analytic, volume_maps=maps) as r:
         r.set("p / rho^2", st["kappa"])
         r.set("p_v / rho^2", st["kappa_v"])
         if visc:
@@ -85,29 +89,60 @@ def viscous_column():
     return sc
 
 
+VMAP_BOX = (0.8, 1.0, 0.8)
+VMAP_RES = (10, 12, 10)
+
+
+def vmap_box():
+    """A 10x14x10 block with a shear velocity field in a volume-mapped 0.8 x 1.0 x 0.8 m box:
+    Weiler2018 (nu = 0.2) with boundary viscosity 0.05, XSPH with its boundary term."""
+    sc = scenes.small_block(counts=(10, 14, 10), box=VMAP_BOX, viscosity=True)
+    sc.v[:, 0] = 1.0 * (sc.x[:, 1] - sc.x[:, 1].mean())
+    sc.v[:, 2] = 0.5 * np.sin(8.0 * sc.x[:, 0])
+    sc.xb = np.zeros((0, 3))
+    sc.params.viscosity = 0.2
+    sc.params.viscosityBoundary = 0.05
+    sc.params.xsphBoundary = 0.1
+    return sc
+
+
+def box_volume_map(support, res=VMAP_RES, box=VMAP_BOX):
+    import oracle
+    v, f = scenes.box_mesh((0, 0, 0), box)
+    return oracle.VolumeMap(res).build(v, f, support, invert=True)
+
+
 def cases():
     return {
         "block12": (scenes.small_block(counts=(12, 12, 12), box=(0.8, 0.8, 0.8), velocity=(0.3, 0.0, -0.2)), 30),
         "column_visc": (viscous_column(), 70),
         "dambreak8k_step203": (scenes.dambreak_8k(), 202),
+        "vmap_box": (vmap_box(), 40),
     }
 
 
 def main():
+    only = set(sys.argv[1:])
     for name, (scene, warm) in cases().items():
+        if only and name not in only:
+            continue
         scene = scene.as_float32()
-        st = advanced_state(scene, warm)
-        out = step_from(scene, st)
+        maps = [box_volume_map(scene.params.supportRadius)] if name == "vmap_box" else None
+        st = advanced_state(scene, warm, maps)
+        out = step_from(scene, st, maps=maps)
         params = dataclasses.asdict(scene.params)
+        extra = dict(vmap_res=np.array(VMAP_RES), vmap_box=np.array(VMAP_BOX)) if maps else {}
         np.savez_compressed(
             os.path.join(HERE, f"ref_step_{name}.npz"),
             params=json.dumps(params), warm=warm,
             x=st["x"].astype(np.float32), v=st["v"].astype(np.float32), kappa=st["kappa"].astype(np.float32),
             kappa_v=st["kappa_v"].astype(np.float32), vdiff=st["vdiff"].astype(np.float32), dt=st["dt"],
-            xb=scene.xb.astype(np.float32), box_min=scene.box_min, box_max=scene.box_max,
+            xb=scene.xb.astype(np.float32), box_min=scene.box_min, box_max=scene.box_max, **extra,
             **{f"out_{k}": v for k, v in out.items()})
         print(name, scene.n, "particles, warm", warm, "iterations", out["iterations"], out["iterations_v"],
               out["visco_iterations"])
+    if only and "dambreak8k_step203" not in only:
+        return
     # lookup-table kernel against the analytic kernel, on the config-0 step above
     scene, warm = cases()["dambreak8k_step203"]
     scene = scene.as_float32()

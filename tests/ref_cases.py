@@ -9,7 +9,7 @@ import numpy as np
 from splishsplash_gb300 import scenes
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ("block12", "column_visc", "dambreak8k_step203")
+CASES = ("block12", "column_visc", "dambreak8k_step203", "vmap_box")
 
 
 def load_case(name):
@@ -24,6 +24,25 @@ def load_case(name):
                  kappa_v=g["kappa_v"].astype(np.float64), vdiff=g["vdiff"].astype(np.float64), dt=float(g["dt"]))
     out = {k[4:]: (g[k] if g[k].ndim else g[k].item()) for k in g.files if k.startswith("out_")}
     return scene, state, out
+
+
+def vmap_spec(name):
+    """(cells per axis, box) of a fixture whose boundary is a Bender2019 volume map of a box
+    container, or None for boundary particles"""
+    g = np.load(os.path.join(GOLDEN, f"ref_step_{name}.npz"))
+    if "vmap_res" not in g.files:
+        return None
+    return tuple(int(r) for r in g["vmap_res"]), tuple(float(b) for b in g["vmap_box"])
+
+
+def case_maps(name, support):
+    """The oracle's volume maps of a fixture (oracle/vmap.c, from the box mesh), or None"""
+    spec = vmap_spec(name)
+    if spec is None:
+        return None
+    import oracle
+    v, f = scenes.box_mesh((0, 0, 0), spec[1])
+    return [oracle.VolumeMap(spec[0]).build(v, f, support, invert=True)]
 
 
 def rel_scalar(a, b, floor):

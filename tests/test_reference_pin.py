@@ -49,8 +49,10 @@ def ref_build():
     return True
 
 
-def oracle_step(scene, state):
+def oracle_step(scene, state, maps=None):
     sim = oracle.OracleSim(ref_cases.with_state(scene, state), fp32_predicate=False)
+    if maps:
+        sim.set_volume_maps(maps)
     sim.kappa[:] = state["kappa"]
     sim.kappa_v[:] = state["kappa_v"]
     sim.vdiff[:] = state["vdiff"]
@@ -64,7 +66,7 @@ def oracle_step(scene, state):
 @pytest.mark.parametrize("case", ref_cases.CASES)
 def test_oracle_matches_reference_step(case):
     scene, state, ref = ref_cases.load_case(case)
-    got, st = oracle_step(scene, state)
+    got, st = oracle_step(scene, state, ref_cases.case_maps(case, scene.params.supportRadius))
     assert (st["iterations"], st["iterations_v"], st["visco_iterations"]) == \
         (ref["iterations"], ref["iterations_v"], ref["visco_iterations"])
     err = ref_cases.field_errors(got, ref)
@@ -85,7 +87,8 @@ def test_fixtures_exercise_the_solvers():
 def test_reference_build_reproduces_fixture(ref_build, case):
     scene, state, ref = ref_cases.load_case(case)
     visc = scene.params.viscosityMethod == 6
-    with refsim.RefSim(ref_cases.with_state(scene, state)) as r:
+    maps = ref_cases.case_maps(case, scene.params.supportRadius)
+    with refsim.RefSim(ref_cases.with_state(scene, state), volume_maps=maps) as r:
         r.set("p / rho^2", state["kappa"])
         r.set("p_v / rho^2", state["kappa_v"])
         if visc:
@@ -123,6 +126,40 @@ def test_oracle_follows_reference_over_steps(ref_build):
                        vdiff=o.vdiff)
             for name, e in ref_cases.field_errors(got, ref).items():
                 assert e <= ORACLE_TOL, (k, name, e)
+
+
+def test_oracle_follows_reference_in_a_volume_mapped_box(ref_build):
+    """Bender2019: 30 steps of the fixture's viscous block in a volume-mapped box.  The map is
+    the oracle's (oracle/vmap.c); the reference evaluates it through its own Bender2019 code
+    (TimeStep::computeVolumeAndBoundaryX, the Bender2019 branches of the DFSPH step, XSPH and
+    Weiler2018's four-sample boundary term); both agree after every step."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("gen_ref_steps", os.path.join(ROOT, "tests", "golden",
+                                                                                 "gen_ref_steps.py"))
+    gen = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(gen)
+    sc = gen.vmap_box().as_float32()
+    maps = [gen.box_volume_map(sc.params.supportRadius)]
+    o = oracle.OracleSim(sc, fp32_predicate=False)
+    o.set_volume_maps(maps)
+    cg = 0
+    with refsim.RefSim(sc, volume_maps=maps) as r:
+        for k in range(30):
+            sr = r.step()
+            o.step()
+            so = o.stats()
+            cg += sr["visco_iterations"]
+            assert (sr["iterations"], sr["iterations_v"], sr["visco_iterations"]) == \
+                (so["iterations"], so["iterations_v"], so["visco_iterations"]), k
+            assert sr["dt"] == pytest.approx(so["dt"], rel=1e-12)
+            got = dict(density=r.get("density"), factor=r.get("factor"), kappa=r.get("p / rho^2"),
+                       kappa_v=r.get("p_v / rho^2"), v=r.get("velocity"), x=r.get("position"),
+                       vdiff=r.get("velocity difference"))
+            ref = dict(density=o.density, factor=o.factor, kappa=o.kappa, kappa_v=o.kappa_v, v=o.v, x=o.x,
+                       vdiff=o.vdiff)
+            for name, e in ref_cases.field_errors(got, ref).items():
+                assert e <= ORACLE_TOL, (k, name, e)
+    assert cg > 0
 
 
 def test_reference_neighbor_counts_match_oracle(ref_build):
