@@ -92,6 +92,12 @@ struct MapData {
 };
 std::vector<MapData> g_maps;
 
+// Several fluid models (ref_set_phases): the particles in id order form consecutive groups of
+// g_phaseCount[m] particles, model m of rest density g_phaseRho0[m]; the per-model viscosity and
+// XSPH coefficients default to the shared parameters where a list is empty.
+std::vector<unsigned int> g_phaseCount;
+std::vector<double> g_phaseRho0, g_phaseNu, g_phaseNub, g_phaseXs, g_phaseXsb;
+
 // The Discregrid grid interface that the reference's Bender2019 code calls, over a MapData.
 // determineShapeFunctions reports whether x lies in the grid; interpolate evaluates the field
 // (and its gradient) at x with the oracle's grid, so the cell, N and dN that the caller passes
@@ -151,6 +157,20 @@ int method_index(std::vector<Simulation::NonPressureForceMethod> &methods, const
 
 FluidModel *model0() { return Simulation::getCurrent()->getFluidModel(0); }
 
+// calls f(model, local index i, particle id) for every particle of every fluid model; ids are
+// consecutive over the models in model order
+template <class F> void for_particles(F f)
+{
+    Simulation *sim = Simulation::getCurrent();
+    unsigned int off = 0;
+    for (unsigned int m = 0; m < sim->numberOfFluidModels(); m++) {
+        FluidModel *fm = sim->getFluidModel(m);
+        const unsigned int n = fm->numActiveParticles();
+        for (unsigned int i = 0; i < n; i++) f(fm, i, off + fm->getParticleId(i));
+        off += n;
+    }
+}
+
 // field -> (pointer getter, components); the names are the reference's field names
 Real *field_ptr(FluidModel *fm, int field, unsigned int i, int &dim)
 {
@@ -197,8 +217,19 @@ int ref_create(const RefParams *p, unsigned int n, const double *x, const double
         g_x[i] = Vector3r(static_cast<Real>(x[3 * i]), static_cast<Real>(x[3 * i + 1]), static_cast<Real>(x[3 * i + 2]));
         g_v[i] = Vector3r(static_cast<Real>(v[3 * i]), static_cast<Real>(v[3 * i + 1]), static_cast<Real>(v[3 * i + 2]));
     }
-    // SimulatorBase::buildModel -> initFluidData: one fluid model, no emitter reserve
-    sim->addFluidModel("Fluid", n, g_x.data(), g_v.data(), g_objectIds.data(), 0u);
+    // SimulatorBase::buildModel -> initFluidData: one fluid model per phase, no emitter reserve
+    const unsigned int nmodels = g_phaseCount.size() > 1 ? (unsigned int)g_phaseCount.size() : 1u;
+    {
+        unsigned int off = 0;
+        for (unsigned int m = 0; m < nmodels; m++) {
+            const unsigned int cnt = nmodels > 1 ? g_phaseCount[m] : n;
+            if (off + cnt > n) return 6;
+            sim->addFluidModel(nmodels > 1 ? "Fluid" + std::to_string(m) : std::string("Fluid"), cnt,
+                               g_x.data() + off, g_v.data() + off, g_objectIds.data() + off, 0u);
+            off += cnt;
+        }
+        if (off != n) return 6;
+    }
     sim->setValue(Simulation::KERNEL_METHOD, Simulation::ENUM_KERNEL_PRECOMPUTED_CUBIC);
     sim->setValue(Simulation::GRAD_KERNEL_METHOD, Simulation::ENUM_GRADKERNEL_PRECOMPUTED_CUBIC);
 
@@ -219,26 +250,33 @@ int ref_create(const RefParams *p, unsigned int n, const double *x, const double
     ts->setValue<unsigned int>(TimeStepDFSPH::MAX_ITERATIONS_V, static_cast<unsigned int>(p->maxIterationsV));
     ts->setValue<Real>(TimeStepDFSPH::MAX_ERROR_V, static_cast<Real>(p->maxErrorV));
 
-    FluidModel *fm = model0();
-    fm->setValue<Real>(FluidModel::DENSITY0, static_cast<Real>(p->density0));
-    int vm = 0;
-    if (p->viscosityMethod == 6) vm = method_index(sim->getViscosityMethods(), Viscosity_Weiler2018::METHOD_NAME);
-    else vm = method_index(sim->getViscosityMethods(), "None");
-    if (vm < 0) return 2;
-    fm->setValue<int>(FluidModel::VISCOSITY_METHOD, vm);
-    if (p->viscosityMethod == 6) {
-        NonPressureForceBase *visc = fm->getViscosityBase();
-        if (!visc) return 3;
-        visc->setValue<Real>(Viscosity_Weiler2018::VISCOSITY_COEFFICIENT, static_cast<Real>(p->viscosity));
-        visc->setValue<Real>(Viscosity_Weiler2018::VISCOSITY_COEFFICIENT_BOUNDARY,
-                             static_cast<Real>(p->viscosityBoundary));
-        visc->setValue<unsigned int>(Viscosity_Weiler2018::MAX_ITERATIONS, static_cast<unsigned int>(p->viscoMaxIter));
-        visc->setValue<Real>(Viscosity_Weiler2018::MAX_ERROR, static_cast<Real>(p->viscoMaxError));
+    // each model's material block: rest density, viscosity and XSPH
+    auto pick = [&](const std::vector<double> &v, unsigned int m, double shared) {
+        return static_cast<Real>(m < v.size() ? v[m] : shared);
+    };
+    for (unsigned int m = 0; m < nmodels; m++) {
+        FluidModel *fm = sim->getFluidModel(m);
+        fm->setValue<Real>(FluidModel::DENSITY0, pick(g_phaseRho0, m, p->density0));
+        int vm = 0;
+        if (p->viscosityMethod == 6) vm = method_index(sim->getViscosityMethods(), Viscosity_Weiler2018::METHOD_NAME);
+        else vm = method_index(sim->getViscosityMethods(), "None");
+        if (vm < 0) return 2;
+        fm->setValue<int>(FluidModel::VISCOSITY_METHOD, vm);
+        if (p->viscosityMethod == 6) {
+            NonPressureForceBase *visc = fm->getViscosityBase();
+            if (!visc) return 3;
+            visc->setValue<Real>(Viscosity_Weiler2018::VISCOSITY_COEFFICIENT, pick(g_phaseNu, m, p->viscosity));
+            visc->setValue<Real>(Viscosity_Weiler2018::VISCOSITY_COEFFICIENT_BOUNDARY,
+                                 pick(g_phaseNub, m, p->viscosityBoundary));
+            visc->setValue<unsigned int>(Viscosity_Weiler2018::MAX_ITERATIONS,
+                                         static_cast<unsigned int>(p->viscoMaxIter));
+            visc->setValue<Real>(Viscosity_Weiler2018::MAX_ERROR, static_cast<Real>(p->viscoMaxError));
+        }
+        XSPH *xs = fm->getXSPH();
+        if (!xs) return 4;
+        xs->setValue<Real>(XSPH::FLUID_COEFFICIENT, pick(g_phaseXs, m, p->xsph));
+        xs->setValue<Real>(XSPH::BOUNDARY_COEFFICIENT, pick(g_phaseXsb, m, p->xsphBoundary));
     }
-    XSPH *xs = fm->getXSPH();
-    if (!xs) return 4;
-    xs->setValue<Real>(XSPH::FLUID_COEFFICIENT, static_cast<Real>(p->xsph));
-    xs->setValue<Real>(XSPH::BOUNDARY_COEFFICIENT, static_cast<Real>(p->xsphBoundary));
 
     // StaticBoundarySimulator::initBoundaryData: one static body at the identity pose
     g_xb.resize(nb);
@@ -301,8 +339,11 @@ int ref_step(RefStats *out)
         TimeStep *ts = sim->getTimeStep();
         out->iterations = ts->getValue<unsigned int>(TimeStepDFSPH::SOLVER_ITERATIONS);
         out->iterationsV = ts->getValue<unsigned int>(TimeStepDFSPH::SOLVER_ITERATIONS_V);
-        NonPressureForceBase *visc = model0()->getViscosityBase();
-        out->viscoIterations = visc ? visc->getValue<unsigned int>(Viscosity_Weiler2018::ITERATIONS) : 0u;
+        out->viscoIterations = 0u;   // summed over the fluid models (one system each)
+        for (unsigned int m = 0; m < sim->numberOfFluidModels(); m++) {
+            NonPressureForceBase *visc = sim->getFluidModel(m)->getViscosityBase();
+            if (visc) out->viscoIterations += visc->getValue<unsigned int>(Viscosity_Weiler2018::ITERATIONS);
+        }
         out->dtOld = h0;
         out->dt = tm->getTimeStepSize();
         out->time = tm->getTime();
@@ -317,31 +358,27 @@ int ref_step(RefStats *out)
  *  of components, or a negative value for an unknown field. */
 int ref_get(int field, double *out)
 {
-    FluidModel *fm = model0();
-    const unsigned int n = fm->numActiveParticles();
     int dim = 0;
-    for (unsigned int i = 0; i < n; i++) {
+    bool ok = true;
+    for_particles([&](FluidModel *fm, unsigned int i, unsigned int id) {
         Real *p = field_ptr(fm, field, i, dim);
-        if (!p) return -1;
-        const unsigned int id = fm->getParticleId(i);
+        if (!p) { ok = false; return; }
         for (int d = 0; d < dim; d++) out[(size_t)id * dim + d] = static_cast<double>(p[d]);
-    }
-    return dim;
+    });
+    return ok ? dim : -1;
 }
 
 /** Overwrites a field in particle-id order (same numbering as ref_get). */
 int ref_set(int field, const double *in)
 {
-    FluidModel *fm = model0();
-    const unsigned int n = fm->numActiveParticles();
     int dim = 0;
-    for (unsigned int i = 0; i < n; i++) {
+    bool ok = true;
+    for_particles([&](FluidModel *fm, unsigned int i, unsigned int id) {
         Real *p = field_ptr(fm, field, i, dim);
-        if (!p) return -1;
-        const unsigned int id = fm->getParticleId(i);
+        if (!p) { ok = false; return; }
         for (int d = 0; d < dim; d++) p[d] = static_cast<Real>(in[(size_t)id * dim + d]);
-    }
-    return dim;
+    });
+    return ok ? dim : -1;
 }
 
 /** Akinci2012 boundary volumes in boundary upload order. */
@@ -358,12 +395,17 @@ int ref_boundary_volume(double *out)
 int ref_neighbor_counts(unsigned int *nf, unsigned int *nb)
 {
     Simulation *sim = Simulation::getCurrent();
-    FluidModel *fm = model0();
-    const unsigned int n = fm->numActiveParticles();
-    for (unsigned int i = 0; i < n; i++) {
-        const unsigned int id = fm->getParticleId(i);
-        nf[id] = sim->numberOfNeighbors(0, 0, i);
-        nb[id] = sim->numberOfPointSets() > 1 ? sim->numberOfNeighbors(0, 1, i) : 0u;
+    const unsigned int nm = sim->numberOfFluidModels();
+    for (unsigned int m = 0, off = 0; m < nm; m++) {
+        FluidModel *fm = sim->getFluidModel(m);
+        const unsigned int n = fm->numActiveParticles();
+        for (unsigned int i = 0; i < n; i++) {
+            const unsigned int id = off + fm->getParticleId(i);
+            nf[id] = 0;
+            for (unsigned int k = 0; k < nm; k++) nf[id] += sim->numberOfNeighbors(m, k, i);
+            nb[id] = sim->numberOfPointSets() > nm ? sim->numberOfNeighbors(m, nm, i) : 0u;
+        }
+        off += n;
     }
     return 0;
 }
@@ -410,6 +452,29 @@ int ref_add_volume_map(const double *dmin, const double *dmax, const unsigned in
 }
 
 void ref_clear_volume_maps() { g_maps.clear(); }
+
+/** Several fluid models for the next ref_create: k consecutive groups of count[m] particles
+ *  (in id order), model m of rest density rho0[m]; nu, nub (Weiler2018 viscosity and boundary
+ *  viscosity) and xs, xsb (XSPH fluid and boundary coefficients) per model, or null for the
+ *  shared parameters.  k <= 1 returns to one model. */
+int ref_set_phases(unsigned int k, const unsigned int *count, const double *rho0, const double *nu, const double *nub,
+                   const double *xs, const double *xsb)
+{
+    g_phaseCount.clear();
+    g_phaseRho0.clear();
+    g_phaseNu.clear();
+    g_phaseNub.clear();
+    g_phaseXs.clear();
+    g_phaseXsb.clear();
+    if (k <= 1) return 0;
+    g_phaseCount.assign(count, count + k);
+    g_phaseRho0.assign(rho0, rho0 + k);
+    if (nu) g_phaseNu.assign(nu, nu + k);
+    if (nub) g_phaseNub.assign(nub, nub + k);
+    if (xs) g_phaseXs.assign(xs, xs + k);
+    if (xsb) g_phaseXsb.assign(xsb, xsb + k);
+    return (int)k;
+}
 
 void ref_destroy()
 {

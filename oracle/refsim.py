@@ -82,6 +82,8 @@ def lib(precision: str = "f64", path: str = None) -> ctypes.CDLL:
         L.ref_add_volume_map.argtypes = [dp, dp, up, dp, dp, dp, dp]
         L.ref_add_volume_map.restype = ctypes.c_int
         L.ref_clear_volume_maps.restype = None
+        L.ref_set_phases.argtypes = [ctypes.c_uint, up, dp, dp, dp, dp, dp]
+        L.ref_set_phases.restype = ctypes.c_int
         _LIBS[key] = L
     return _LIBS[key]
 
@@ -95,12 +97,14 @@ class RefSim:
     cubic spline after the parameters are read (the FP64 oracle protocol); False keeps
     the reference's default PrecomputedKernel<CubicKernel, 10000> for DFSPH.
     volume_maps: oracle.VolumeMap objects (static bodies): the boundary is then Bender2019
-    with those maps instead of the scene's boundary particles."""
+    with those maps instead of the scene's boundary particles.
+    phases: dict(counts=..., density0=..., and optionally viscosity, viscosity_boundary, xsph,
+    xsph_boundary per model): the particles in id order form that many fluid models."""
 
     _alive = False
 
     def __init__(self, scene, precision: str = "f64", analytic_kernel: bool = True, num_threads: int = 0,
-                 library: str = None, volume_maps=None):
+                 library: str = None, volume_maps=None, phases=None):
         if RefSim._alive:
             raise RuntimeError("the reference's Simulation is a singleton: close the other RefSim first")
         self.L = lib(precision, library)
@@ -141,6 +145,16 @@ class RefSim:
                                       _dp(np.ascontiguousarray(vm.fields[1], np.float64)),
                                       _dp(arr(c.R)), _dp(arr(c.t)))
         rp.boundaryMethod = 2 if volume_maps else 0
+        self._phase_arrays = []
+        if phases:
+            cnt = np.ascontiguousarray(phases["counts"], np.uint32)
+            arrs = [np.ascontiguousarray(phases[k], np.float64) if phases.get(k) is not None else None
+                    for k in ("density0", "viscosity", "viscosity_boundary", "xsph", "xsph_boundary")]
+            self._phase_arrays = [cnt] + arrs
+            self.L.ref_set_phases(len(cnt), cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_uint)),
+                                  *[(_dp(a) if a is not None else None) for a in arrs])
+        else:
+            self.L.ref_set_phases(0, None, None, None, None, None, None)
         x = np.ascontiguousarray(scene.x, np.float64)
         v = np.ascontiguousarray(scene.v, np.float64)
         xb = np.ascontiguousarray(scene.xb, np.float64).reshape(-1, 3)

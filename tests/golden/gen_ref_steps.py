@@ -18,6 +18,10 @@ to this script, by particle id:
   volume map of the box, built by the oracle (oracle/vmap.c) from the box mesh and handed to
   the reference's Bender2019 code through the driver's Discregrid grid; the fixture records
   the map's cells per axis and box (vmap_res, vmap_box) so that a test rebuilds it.
+  The two-model case (phases_visc) is a column of two fluid models (rest densities 1000 and
+  500, the heavy one below) with their own Weiler2018 and XSPH coefficients; the fixture
+  records the models (phase_counts, phase_density0, phase_viscosity, phase_viscosity_boundary,
+  phase_xsph, phase_xsph_boundary).
   ref_kernel_table_delta.json  the same config-0 step with the reference's default
                         PrecomputedKernel<CubicKernel, 10000> against the analytic
                         kernel: max and mean relative difference per field
@@ -47,10 +51,10 @@ def f32(a):
     return np.asarray(a, np.float64).astype(np.float32).astype(np.float64)
 
 
-def advanced_state(scene, warm, maps=None):
+def advanced_state(scene, warm, maps=None, phases=None):
     """The scene after `warm` reference steps, rounded to float32."""
     visc = scene.params.viscosityMethod == 6
-    with refsim.RefSim(scene, volume_maps=maps) as r:
+    with refsim.RefSim(scene, volume_maps=maps, phases=phases) as r:
         for _ in range(warm):
             r.step()
         st = dict(x=f32(r.get("position")), v=f32(r.get("velocity")), kappa=f32(r.get("p / rho^2")),
@@ -60,11 +64,11 @@ def advanced_state(scene, warm, maps=None):
     return st
 
 
-def step_from(scene, st, analytic=True, maps=None):
+def step_from(scene, st, analytic=True, maps=None, phases=None):
     """One reference step from state st; outputs by particle id."""
     sc = dataclasses.replace(scene, x=st["x"], v=st["v"])
     visc = scene.params.viscosityMethod == 6
-    with refsim.RefSim(sc, analytic_kernel=analytic, volume_maps=maps) as r:
+    with refsim.RefSim(sc, analytic_kernel=analytic, volume_maps=maps, phases=phases) as r:
         r.set("p / rho^2", st["kappa"])
         r.set("p_v / rho^2", st["kappa_v"])
         if visc:
@@ -112,12 +116,28 @@ def box_volume_map(support, res=VMAP_RES, box=VMAP_BOX):
     return oracle.VolumeMap(res).build(v, f, support, invert=True)
 
 
+PHASES = dict(density0=(1000.0, 500.0), viscosity=(0.3, 0.05), viscosity_boundary=(0.05, 0.0),
+              xsph=(0.01, 0.1), xsph_boundary=(0.1, 0.0))
+
+
+def phases_visc():
+    """An 8x10x8 column, its lower half fluid model 0 (rest density 1000) and upper half model 1
+    (500), particles ordered by height; Weiler2018 and XSPH with per-model coefficients."""
+    sc = scenes.small_block(counts=(8, 10, 8), box=(0.6, 0.8, 0.6), corner=(0.05, 0.05, 0.05),
+                            velocity=(0.2, -0.3, 0.1), viscosity=True)
+    order = np.argsort(sc.x[:, 1], kind="stable")
+    sc.x, sc.v = sc.x[order].copy(), sc.v[order].copy()
+    n0 = sc.n // 2
+    return sc, dict(counts=(n0, sc.n - n0), **PHASES)
+
+
 def cases():
     return {
         "block12": (scenes.small_block(counts=(12, 12, 12), box=(0.8, 0.8, 0.8), velocity=(0.3, 0.0, -0.2)), 30),
         "column_visc": (viscous_column(), 70),
         "dambreak8k_step203": (scenes.dambreak_8k(), 202),
         "vmap_box": (vmap_box(), 40),
+        "phases_visc": (phases_visc()[0], 30),
     }
 
 
@@ -128,10 +148,13 @@ def main():
             continue
         scene = scene.as_float32()
         maps = [box_volume_map(scene.params.supportRadius)] if name == "vmap_box" else None
-        st = advanced_state(scene, warm, maps)
-        out = step_from(scene, st, maps=maps)
+        phases = phases_visc()[1] if name == "phases_visc" else None
+        st = advanced_state(scene, warm, maps, phases)
+        out = step_from(scene, st, maps=maps, phases=phases)
         params = dataclasses.asdict(scene.params)
         extra = dict(vmap_res=np.array(VMAP_RES), vmap_box=np.array(VMAP_BOX)) if maps else {}
+        if phases:
+            extra = {f"phase_{k}": np.array(v) for k, v in phases.items()}
         np.savez_compressed(
             os.path.join(HERE, f"ref_step_{name}.npz"),
             params=json.dumps(params), warm=warm,

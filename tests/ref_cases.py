@@ -9,7 +9,7 @@ import numpy as np
 from splishsplash_gb300 import scenes
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ("block12", "column_visc", "dambreak8k_step203", "vmap_box")
+CASES = ("block12", "column_visc", "dambreak8k_step203", "vmap_box", "phases_visc")
 
 
 def load_case(name):
@@ -43,6 +43,17 @@ def case_maps(name, support):
     import oracle
     v, f = scenes.box_mesh((0, 0, 0), spec[1])
     return [oracle.VolumeMap(spec[0]).build(v, f, support, invert=True)]
+
+
+def case_phases(name):
+    """The fluid models of a fixture (counts, density0 and per-model viscosity and XSPH
+    coefficients, as refsim.RefSim takes them), or None for one model"""
+    g = np.load(os.path.join(GOLDEN, f"ref_step_{name}.npz"))
+    if "phase_counts" not in g.files:
+        return None
+    out = {k[6:]: g[k] for k in g.files if k.startswith("phase_")}
+    out["counts"] = tuple(int(c) for c in out["counts"])
+    return out
 
 
 def rel_scalar(a, b, floor):

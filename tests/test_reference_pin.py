@@ -49,10 +49,18 @@ def ref_build():
     return True
 
 
-def oracle_step(scene, state, maps=None):
+def oracle_phases(sim, ph):
+    sim.set_phases(ph["counts"], ph["density0"])
+    sim.set_phase_viscosity(ph["viscosity"], ph["viscosity_boundary"])
+    sim.set_phase_xsph(ph["xsph"], ph["xsph_boundary"])
+
+
+def oracle_step(scene, state, maps=None, phases=None):
     sim = oracle.OracleSim(ref_cases.with_state(scene, state), fp32_predicate=False)
     if maps:
         sim.set_volume_maps(maps)
+    if phases:
+        oracle_phases(sim, phases)
     sim.kappa[:] = state["kappa"]
     sim.kappa_v[:] = state["kappa_v"]
     sim.vdiff[:] = state["vdiff"]
@@ -66,7 +74,8 @@ def oracle_step(scene, state, maps=None):
 @pytest.mark.parametrize("case", ref_cases.CASES)
 def test_oracle_matches_reference_step(case):
     scene, state, ref = ref_cases.load_case(case)
-    got, st = oracle_step(scene, state, ref_cases.case_maps(case, scene.params.supportRadius))
+    got, st = oracle_step(scene, state, ref_cases.case_maps(case, scene.params.supportRadius),
+                          ref_cases.case_phases(case))
     assert (st["iterations"], st["iterations_v"], st["visco_iterations"]) == \
         (ref["iterations"], ref["iterations_v"], ref["visco_iterations"])
     err = ref_cases.field_errors(got, ref)
@@ -88,7 +97,7 @@ def test_reference_build_reproduces_fixture(ref_build, case):
     scene, state, ref = ref_cases.load_case(case)
     visc = scene.params.viscosityMethod == 6
     maps = ref_cases.case_maps(case, scene.params.supportRadius)
-    with refsim.RefSim(ref_cases.with_state(scene, state), volume_maps=maps) as r:
+    with refsim.RefSim(ref_cases.with_state(scene, state), volume_maps=maps, phases=ref_cases.case_phases(case)) as r:
         r.set("p / rho^2", state["kappa"])
         r.set("p_v / rho^2", state["kappa_v"])
         if visc:
@@ -145,6 +154,39 @@ def test_oracle_follows_reference_in_a_volume_mapped_box(ref_build):
     cg = 0
     with refsim.RefSim(sc, volume_maps=maps) as r:
         for k in range(30):
+            sr = r.step()
+            o.step()
+            so = o.stats()
+            cg += sr["visco_iterations"]
+            assert (sr["iterations"], sr["iterations_v"], sr["visco_iterations"]) == \
+                (so["iterations"], so["iterations_v"], so["visco_iterations"]), k
+            assert sr["dt"] == pytest.approx(so["dt"], rel=1e-12)
+            got = dict(density=r.get("density"), factor=r.get("factor"), kappa=r.get("p / rho^2"),
+                       kappa_v=r.get("p_v / rho^2"), v=r.get("velocity"), x=r.get("position"),
+                       vdiff=r.get("velocity difference"))
+            ref = dict(density=o.density, factor=o.factor, kappa=o.kappa, kappa_v=o.kappa_v, v=o.v, x=o.x,
+                       vdiff=o.vdiff)
+            for name, e in ref_cases.field_errors(got, ref).items():
+                assert e <= ORACLE_TOL, (k, name, e)
+    assert cg > 0
+
+
+def test_oracle_follows_reference_with_two_fluid_models(ref_build):
+    """20 steps of the fixture's two-model column (rest densities 1000 and 500, per-model
+    Weiler2018 and XSPH coefficients): the reference runs two FluidModels, the oracle two phases;
+    iteration counts equal and fields at 1e-10 after every step."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("gen_ref_steps", os.path.join(ROOT, "tests", "golden",
+                                                                                 "gen_ref_steps.py"))
+    gen = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(gen)
+    sc, ph = gen.phases_visc()
+    sc = sc.as_float32()
+    o = oracle.OracleSim(sc, fp32_predicate=False)
+    oracle_phases(o, ph)
+    cg = 0
+    with refsim.RefSim(sc, phases=ph) as r:
+        for k in range(20):
             sr = r.step()
             o.step()
             so = o.stats()
