@@ -298,29 +298,12 @@ class OracleSim:
         self.body_dynamic = np.ones(nbodies, np.int32) if dynamic is None else np.ascontiguousarray(dynamic, np.int32)
         self.body_force = np.zeros((nbodies, 3), np.float64)
         self.body_torque = np.zeros((nbodies, 3), np.float64)
-        if self.body is not None:
-            self._grouped_volumes(self.body, self.body_dynamic)
         self.st.body = _ptr(self.body)
         self.st.nbodies = nbodies
         self.st.body_center = _ptr(self.body_center)
         self.st.body_dynamic = _ptr(self.body_dynamic)
         self.st.body_force = _ptr(self.body_force)
         self.st.body_torque = _ptr(self.body_torque)
-
-    def _grouped_volumes(self, body, dynamic):
-        """Akinci2012 volumes as Simulation::updateBoundaryVolume computes them
-        (Simulation.cpp:700-746): the static bodies' particles together, every dynamic body's alone"""
-        groups = np.where(np.asarray(dynamic)[body] != 0, body.astype(np.int64) + 1, 0)
-        if not groups.any():
-            return
-        for g in np.unique(groups):
-            idx = np.flatnonzero(groups == g)
-            sub = np.ascontiguousarray(self.xb[idx])
-            vol = np.zeros(len(idx), self.Vb.dtype)
-            rc = self.lib.orc_boundary_volume(len(idx), _ptr(sub), self._support, self._fp32_predicate, _ptr(vol))
-            if rc != 0:
-                raise RuntimeError(f"orc_boundary_volume failed: {rc}")
-            self.Vb[idx] = vol
 
     def set_volume_maps(self, maps):
         """Bender2019 boundary: the bodies' VolumeMaps replace the boundary particles."""

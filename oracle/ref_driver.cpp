@@ -98,6 +98,21 @@ std::vector<MapData> g_maps;
 std::vector<unsigned int> g_phaseCount;
 std::vector<double> g_phaseRho0, g_phaseNu, g_phaseNub, g_phaseXs, g_phaseXsb;
 
+// Akinci2012 boundary split into bodies (ref_set_bodies): body of every boundary particle, the
+// bodies' reference points and dynamic flags.  A dynamic body is HeldBody: dynamic for
+// BoundaryModel::addForce (forces and torques about its position accumulate), but nothing
+// integrates its motion, so it stays where it is (the caller's rigid-body solver would move it).
+std::vector<unsigned int> g_bodyOf;
+std::vector<double> g_bodyCenter;
+std::vector<int> g_bodyDynamic;
+std::vector<std::vector<Vector3r>> g_bodyX;
+
+class HeldBody : public StaticRigidBody
+{
+public:
+    bool isDynamic() const override { return true; }
+};
+
 // The Discregrid grid interface that the reference's Bender2019 code calls, over a MapData.
 // determineShapeFunctions reports whether x lies in the grid; interpolate evaluates the field
 // (and its gradient) at x with the oracle's grid, so the cell, N and dN that the caller passes
@@ -301,6 +316,28 @@ int ref_create(const RefParams *p, unsigned int n, const double *x, const double
             sim->addBoundaryModel(bm);
             bm->setMap(new OracleGrid(d));
         }
+    } else if (nb > 0 && !g_bodyDynamic.empty()) {
+        // one BoundaryModel_Akinci2012 per body, its particles in upload order, the body's rigid
+        // body at its reference point (the torque's centre, BoundaryModel.h:38-49)
+        const unsigned int nbodies = (unsigned int)g_bodyDynamic.size();
+        g_bodyX.assign(nbodies, {});
+        for (unsigned int i = 0; i < nb; i++) {
+            if (g_bodyOf[i] >= nbodies) return 7;
+            g_bodyX[g_bodyOf[i]].push_back(g_xb[i]);
+        }
+        for (unsigned int b = 0; b < nbodies; b++) {
+            if (g_bodyX[b].empty()) return 7;
+            StaticRigidBody *rb = g_bodyDynamic[b] ? new HeldBody() : new StaticRigidBody();
+            const Vector3r c(static_cast<Real>(g_bodyCenter[3 * b]), static_cast<Real>(g_bodyCenter[3 * b + 1]),
+                             static_cast<Real>(g_bodyCenter[3 * b + 2]));
+            rb->setPosition0(c);
+            rb->setPosition(c);
+            rb->setRotation0(Quaternionr::Identity());
+            rb->setRotation(Quaternionr::Identity());
+            BoundaryModel_Akinci2012 *bm = new BoundaryModel_Akinci2012();
+            bm->initModel(rb, (unsigned int)g_bodyX[b].size(), g_bodyX[b].data());
+            sim->addBoundaryModel(bm);
+        }
     } else if (nb > 0) {
         g_body = new StaticRigidBody();
         g_body->setPosition0(Vector3r::Zero());
@@ -386,9 +423,61 @@ int ref_boundary_volume(double *out)
 {
     Simulation *sim = Simulation::getCurrent();
     if (sim->numberOfBoundaryModels() == 0) return 0;
+    if (!g_bodyDynamic.empty()) {   // bodies: back to upload order
+        std::vector<unsigned int> next(sim->numberOfBoundaryModels(), 0u);
+        for (size_t i = 0; i < g_bodyOf.size(); i++) {
+            const unsigned int b = g_bodyOf[i];
+            BoundaryModel_Akinci2012 *bm = static_cast<BoundaryModel_Akinci2012 *>(sim->getBoundaryModel(b));
+            out[i] = static_cast<double>(bm->getVolume(next[b]++));
+        }
+        return 0;
+    }
     BoundaryModel_Akinci2012 *bm = static_cast<BoundaryModel_Akinci2012 *>(sim->getBoundaryModel(0));
     for (unsigned int i = 0; i < bm->numberOfParticles(); i++) out[i] = static_cast<double>(bm->getVolume(i));
     return 0;
+}
+
+/** Bodies of the Akinci2012 boundary for the next ref_create: body[i] of boundary particle i,
+ *  center (3 per body: the body's position, the torque's centre) and dynamic flags.
+ *  nbodies 0 returns to one static body. */
+int ref_set_bodies(unsigned int nbodies, unsigned int nb, const unsigned int *body, const double *center,
+                   const int *dynamic)
+{
+    g_bodyOf.clear();
+    g_bodyCenter.clear();
+    g_bodyDynamic.clear();
+    if (nbodies == 0) return 0;
+    g_bodyOf.assign(body, body + nb);
+    g_bodyCenter.assign(center, center + 3 * (size_t)nbodies);
+    g_bodyDynamic.assign(dynamic, dynamic + nbodies);
+    return (int)nbodies;
+}
+
+/** Force and torque that the fluid exerted on each body since the last clear
+ *  (BoundaryModel::getForceAndTorque, summed over the threads); 3 values per body each. */
+int ref_body_forces(double *force, double *torque)
+{
+    Simulation *sim = Simulation::getCurrent();
+    for (unsigned int b = 0; b < sim->numberOfBoundaryModels(); b++) {
+        Vector3r f, t;
+        f.setZero();
+        t.setZero();
+        if (sim->getBoundaryModel(b)->getRigidBodyObject()->isDynamic())
+            sim->getBoundaryModel(b)->getForceAndTorque(f, t);
+        for (int d = 0; d < 3; d++) {
+            force[3 * b + d] = static_cast<double>(f[d]);
+            torque[3 * b + d] = static_cast<double>(t[d]);
+        }
+    }
+    return (int)sim->numberOfBoundaryModels();
+}
+
+/** BoundaryModel::clearForceAndTorque of every dynamic body. */
+void ref_clear_body_forces()
+{
+    Simulation *sim = Simulation::getCurrent();
+    for (unsigned int b = 0; b < sim->numberOfBoundaryModels(); b++)
+        if (sim->getBoundaryModel(b)->getRigidBodyObject()->isDynamic()) sim->getBoundaryModel(b)->clearForceAndTorque();
 }
 
 /** Fluid and boundary neighbour counts of the last neighbourhood search, by particle id. */
@@ -403,7 +492,8 @@ int ref_neighbor_counts(unsigned int *nf, unsigned int *nb)
             const unsigned int id = off + fm->getParticleId(i);
             nf[id] = 0;
             for (unsigned int k = 0; k < nm; k++) nf[id] += sim->numberOfNeighbors(m, k, i);
-            nb[id] = sim->numberOfPointSets() > nm ? sim->numberOfNeighbors(m, nm, i) : 0u;
+            nb[id] = 0;
+            for (unsigned int k = nm; k < sim->numberOfPointSets(); k++) nb[id] += sim->numberOfNeighbors(m, k, i);
         }
         off += n;
     }

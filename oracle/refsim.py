@@ -84,6 +84,11 @@ def lib(precision: str = "f64", path: str = None) -> ctypes.CDLL:
         L.ref_clear_volume_maps.restype = None
         L.ref_set_phases.argtypes = [ctypes.c_uint, up, dp, dp, dp, dp, dp]
         L.ref_set_phases.restype = ctypes.c_int
+        L.ref_set_bodies.argtypes = [ctypes.c_uint, ctypes.c_uint, up, dp, ctypes.POINTER(ctypes.c_int)]
+        L.ref_set_bodies.restype = ctypes.c_int
+        L.ref_body_forces.argtypes = [dp, dp]
+        L.ref_body_forces.restype = ctypes.c_int
+        L.ref_clear_body_forces.restype = None
         _LIBS[key] = L
     return _LIBS[key]
 
@@ -99,12 +104,15 @@ class RefSim:
     volume_maps: oracle.VolumeMap objects (static bodies): the boundary is then Bender2019
     with those maps instead of the scene's boundary particles.
     phases: dict(counts=..., density0=..., and optionally viscosity, viscosity_boundary, xsph,
-    xsph_boundary per model): the particles in id order form that many fluid models."""
+    xsph_boundary per model): the particles in id order form that many fluid models.
+    bodies: dict(body=..., center=..., dynamic=...): the boundary particles split into one
+    Akinci2012 body each (body index per particle, reference points, dynamic flags); the forces on
+    the dynamic ones accumulate (body_forces / clear_body_forces)."""
 
     _alive = False
 
     def __init__(self, scene, precision: str = "f64", analytic_kernel: bool = True, num_threads: int = 0,
-                 library: str = None, volume_maps=None, phases=None):
+                 library: str = None, volume_maps=None, phases=None, bodies=None):
         if RefSim._alive:
             raise RuntimeError("the reference's Simulation is a singleton: close the other RefSim first")
         self.L = lib(precision, library)
@@ -155,6 +163,17 @@ class RefSim:
                                   *[(_dp(a) if a is not None else None) for a in arrs])
         else:
             self.L.ref_set_phases(0, None, None, None, None, None, None)
+        self.nbodies = 0
+        if bodies:
+            self._body = np.ascontiguousarray(bodies["body"], np.uint32)
+            self._center = np.ascontiguousarray(bodies["center"], np.float64).reshape(-1, 3)
+            self._dyn = np.ascontiguousarray(bodies["dynamic"], np.int32)
+            self.nbodies = self._center.shape[0]
+            self.L.ref_set_bodies(self.nbodies, self._body.size,
+                                  self._body.ctypes.data_as(ctypes.POINTER(ctypes.c_uint)), _dp(self._center),
+                                  self._dyn.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+        else:
+            self.L.ref_set_bodies(0, 0, None, None, None)
         x = np.ascontiguousarray(scene.x, np.float64)
         v = np.ascontiguousarray(scene.v, np.float64)
         xb = np.ascontiguousarray(scene.xb, np.float64).reshape(-1, 3)
@@ -195,6 +214,16 @@ class RefSim:
         out = np.zeros(max(1, self.nb), np.float64)
         self.L.ref_boundary_volume(_dp(out))
         return out[: self.nb]
+
+    def body_forces(self):
+        """(force, torque) per body since the last clear, nbodies x 3 each"""
+        f = np.zeros((max(1, self.nbodies), 3))
+        t = np.zeros((max(1, self.nbodies), 3))
+        self.L.ref_body_forces(_dp(f), _dp(t))
+        return f[: self.nbodies], t[: self.nbodies]
+
+    def clear_body_forces(self) -> None:
+        self.L.ref_clear_body_forces()
 
     def neighbor_counts(self):
         nf = np.zeros(self.n, np.uint32)

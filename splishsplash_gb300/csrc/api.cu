@@ -144,8 +144,6 @@ struct sphgb_ctx {
     uint32_t *bm_body = nullptr, *bm_scene = nullptr, *bm_k1 = nullptr, *bm_k2 = nullptr, *bm_v1 = nullptr, *bm_v2 = nullptr;
     uint32_t *bm_cells = nullptr, *bm_hist = nullptr;
     uint32_t *binv = nullptr;          // prepared set: sorted slot of boundary particle u
-    uint32_t *bgroup = nullptr;        // prepared set: volume group of boundary particle u (null: one group)
-    std::vector<char> body_moves;      // a motion was set for the body (its particles form their own group)
     // neighbourhood staging of the solver passes (FP32, one lane per particle)
     int stage_mode = 0;                // 0: the autotuner decides, 1: off, 2: on
     bool staged = false;               // in use
@@ -293,7 +291,6 @@ void free_prepared(sphgb_ctx *c)
     c->xb = c->bscratch = nullptr;
     c->bid = c->bscene = nullptr;
     c->binv = nullptr;
-    c->bgroup = nullptr;
     c->r0 = nullptr;
     c->ph = nullptr;
     c->bm_ready = false;   // the rest shapes and volumes are read again from the new layout
@@ -346,7 +343,6 @@ void free_bodies(sphgb_ctx *c)
     c->nbodies = 0;
     c->bmotion = c->bmot_dirty = c->bm_ready = false;
     c->bmot.clear();
-    c->body_moves.clear();
     c->bm_nb = 0;
     c->d_bmot = c->bm_x0 = c->bm_V0 = c->bm_xtmp = c->bm_vtmp = c->vbs = nullptr;
     c->bm_body = c->bm_scene = c->bm_k1 = c->bm_k2 = c->bm_v1 = c->bm_v2 = c->bm_cells = c->bm_hist = nullptr;
@@ -527,7 +523,6 @@ template <class T> DevBufs<T> make_bufs(const sphgb_ctx *c, int view)
     B.bv = (v4 *)c->bv;
     B.vbs = (v4 *)c->vbs;
     B.binv = c->binv;
-    B.bgroup = c->bgroup;
     B.r0 = (T *)c->r0;
     B.ph = c->ph;
     B.ll = c->ll;
@@ -703,22 +698,6 @@ template <class T> int prepare(sphgb_ctx *c)
     if ((rc = palloc(c, &c->xb, (size_t)std::max(nb, 1u) * vec_size(c)))) return rc;
     if ((rc = palloc(c, &c->bid, (size_t)std::max(nb, 1u) * 4))) return rc;
     if ((rc = palloc(c, &c->binv, (size_t)std::max(nb, 1u) * 4))) return rc;
-    if (nb && c->nbodies && c->body_of.size() == nb) {
-        // volume groups: the static bodies together, every dynamic or moving body alone
-        std::vector<uint32_t> g(nb, 0u);
-        bool any = false;
-        for (uint32_t u = 0; u < nb; u++) {
-            const uint32_t b = c->body_of[u];
-            if (c->body_dynamic[b] || (b < c->body_moves.size() && c->body_moves[b])) {
-                g[u] = 1u + b;
-                any = true;
-            }
-        }
-        if (any) {
-            if ((rc = palloc(c, &c->bgroup, (size_t)nb * 4))) return rc;
-            CK(cudaMemcpy(c->bgroup, g.data(), (size_t)nb * 4, cudaMemcpyHostToDevice));
-        }
-    }
     if ((rc = palloc(c, &c->bscratch, (size_t)std::max(nb, 1u) * real_size(c)))) return rc;
     if (c->scn.size() > 1 && (rc = palloc(c, &c->bscene, (size_t)std::max(nb, 1u) * 4))) return rc;
     if (nb > 0) {
@@ -2083,8 +2062,8 @@ int sphgb_set_boundary_bodies(sphgb_ctx *c, const uint32_t *body, uint32_t nbodi
     CK(cudaStreamSynchronize(c->stream));
     free_bodies(c);
     invalidate_graphs(c);
-    // prepared again at the next step: the volume groups and the body tables (and, with volume
-    // maps, the block partials of their forces)
+    // prepared again at the next step: the body tables (and, with volume maps, the block partials
+    // of their forces)
     c->prepared = false;
     if (nbodies == 0) return SPHGB_OK;
     c->body_of.assign(body, body + (body ? c->nb : 0u));
@@ -2093,7 +2072,6 @@ int sphgb_set_boundary_bodies(sphgb_ctx *c, const uint32_t *body, uint32_t nbodi
     if (dynamic)
         for (uint32_t b = 0; b < nbodies; b++) c->body_dynamic[b] = dynamic[b] != 0;
     c->nbodies = nbodies;
-    c->body_moves.assign(nbodies, 0);
     c->bmot.assign(18 * (size_t)nbodies, 0.0);   // every body at rest in its uploaded pose
     for (uint32_t b = 0; b < nbodies; b++)
         for (int k = 0; k < 3; k++) c->bmot[18 * (size_t)b + 4 * k] = 1.0;
@@ -2362,10 +2340,6 @@ int sphgb_set_body_motion(sphgb_ctx *c, uint32_t body, const double rotation[9],
         fill_stats(c, &st);
     }
     cudaSetDevice(c->cfg.device);
-    if (!c->body_moves[body]) {   // a body that moves has its own volume group from now on
-        c->body_moves[body] = 1;
-        if (!c->body_dynamic[body]) c->prepared = false;
-    }
     double *q = c->bmot.data() + 18 * (size_t)body;
     if (rotation) std::copy(rotation, rotation + 9, q);
     if (translation) std::copy(translation, translation + 3, q + 9);

@@ -2549,9 +2549,11 @@ __global__ void __launch_bounds__(kBlock) k_boundary_regather(DevParams<T> P, De
 }
 
 // BoundaryModel_Akinci2012::computeBoundaryVolume (BoundaryModel_Akinci2012.cpp:48-75):
-// V_b = 1 / (W0 + sum over boundary neighbours of the same scene and volume group of W); the
-// static bodies form one group, every dynamic or moving body its own, as
-// Simulation::updateBoundaryVolume activates them (Simulation.cpp:700-746)
+// V_b = 1 / (W0 + sum over the boundary neighbours of the same scene of W), over the particles
+// of every body together.  Simulation::updateBoundaryVolume (Simulation.cpp:700-746) activates
+// the static bodies, then each dynamic or animated body, with set_active(i, true, true), and a
+// point set activated so searches every other point set: each body's sum covers the boundary
+// particles of all bodies.
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_boundary_volume(DevParams<T> P, DevBufs<T> B)
 {
@@ -2559,7 +2561,6 @@ __global__ void __launch_bounds__(kBlock) k_boundary_volume(DevParams<T> P, DevB
     if (i >= P.nb) return;
     const SceneDev<T> S = scene_get(P, B.bscene ? B.bscene[i] : 0u);
     v4_t<T> xi = ldv(B.xb, i);
-    const uint32_t gi = B.bgroup ? B.bgroup[B.bid[i]] : 0u;
     int cx, cy, cz;
     cell_of(S, xi, cx, cy, cz);
     T delta = P.K.w0;
@@ -2577,7 +2578,7 @@ __global__ void __launch_bounds__(kBlock) k_boundary_volume(DevParams<T> P, DevB
                 if (s == kEmpty) continue;
                 const uint32_t e = B.bcend[c];
                 for (uint32_t j = s; j < e; j++) {
-                    if (j == i || (B.bgroup && B.bgroup[B.bid[j]] != gi)) continue;
+                    if (j == i) continue;
                     T ddx, ddy, ddz;
                     const T d2 = pair_d2(xi, ldv(B.xb, j), ddx, ddy, ddz);
                     if (d2 < P.K.h2) delta += kernel_W(P.K, dev_sqrt(d2));

@@ -155,8 +155,6 @@ template <class T> struct DevBufs {
     uint32_t *ph;                // fluid phases: phase of slot i
     v4 *vbs;                     // moving boundary bodies: velocity of sorted boundary particle k
     uint32_t *binv;              // sorted slot of boundary particle u (upload order)
-    const uint32_t *bgroup;      // volume group of boundary particle u (upload order): 0 the static bodies,
-                                 // 1 + b a dynamic or moving body b; null: one group
     v4 *bv;                      // moving volume-map bodies, per particle: xyz = sum_b V_b W_ib v_b,
                                  // w = sum_b V_b v_b . gradW_ib (fixed for the step, like bg)
     T *density, *factor, *dadv;

@@ -204,6 +204,45 @@ def test_oracle_follows_reference_with_two_fluid_models(ref_build):
     assert cg > 0
 
 
+def test_body_forces_follow_the_reference(ref_build):
+    """BoundaryModel::addForce on dynamic Akinci2012 bodies: the container split into a dynamic
+    floor, dynamic side walls and a static ceiling (tests/test_bodies.py's all-terms scene: both
+    solvers' pressure, XSPH boundary and Weiler2018 boundary terms).  The reference holds one
+    BoundaryModel_Akinci2012 per body, the dynamic ones on a rigid body that nothing moves.  Over
+    40 steps the boundary volumes, the force and torque on every body in every step, the fields
+    and the iteration counts agree with the oracle at 1e-10."""
+    from test_bodies import CENTERS, DYNAMIC, all_terms_scene, container_bodies
+    sc = all_terms_scene()
+    sc.v[:, 0] = 0.5 * (sc.x[:, 1] - sc.x[:, 1].mean())   # shear: the viscosity solve iterates
+    body = container_bodies(sc.xb, 1.0)
+    o = oracle.OracleSim(sc, fp32_predicate=False)
+    o.set_bodies(body, CENTERS, DYNAMIC)
+    cg = 0
+    with refsim.RefSim(sc, bodies=dict(body=body, center=CENTERS, dynamic=DYNAMIC)) as r:
+        np.testing.assert_allclose(r.boundary_volume(), o.Vb, rtol=1e-13)
+        for k in range(40):
+            r.clear_body_forces()
+            o.clear_forces()
+            sr = r.step()
+            o.step()
+            so = o.stats()
+            cg += sr["visco_iterations"]
+            assert (sr["iterations"], sr["iterations_v"], sr["visco_iterations"]) == \
+                (so["iterations"], so["iterations_v"], so["visco_iterations"]), k
+            fr, tr = r.body_forces()
+            scale_f = max(float(np.abs(o.body_force).max()), 1e-30)
+            scale_t = max(float(np.abs(o.body_torque).max()), 1e-30)
+            assert float(np.abs(fr - o.body_force).max()) <= ORACLE_TOL * scale_f, k
+            assert float(np.abs(tr - o.body_torque).max()) <= ORACLE_TOL * scale_t, k
+            assert not np.any(o.body_force[2]) and not np.any(fr[2])   # the static ceiling
+            got = dict(density=r.get("density"), factor=r.get("factor"), kappa=r.get("p / rho^2"),
+                       kappa_v=r.get("p_v / rho^2"), v=r.get("velocity"), x=r.get("position"))
+            ref = dict(density=o.density, factor=o.factor, kappa=o.kappa, kappa_v=o.kappa_v, v=o.v, x=o.x)
+            for name, e in ref_cases.field_errors(got, ref).items():
+                assert e <= ORACLE_TOL, (k, name, e)
+    assert cg > 0 and float(np.abs(o.body_force[0]).max()) > 0
+
+
 def test_reference_neighbor_counts_match_oracle(ref_build):
     sc = scenes.small_block(counts=(10, 8, 10), box=(0.8, 0.8, 0.8)).as_float32()
     with refsim.RefSim(sc) as r:
