@@ -530,15 +530,12 @@ def main():
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
+    inputs = {"position": hx, "velocity": hv}
+    outputs = {"position": hx, "velocity": hv, "density": hrho, "p / rho^2": hk, "p_v / rho^2": hkv}
     for _ in range(e2e_steps):
-        te.ctx.upload_field("position", hx)
-        te.ctx.upload_field("velocity", hv)
+        te.ctx.upload_fields(inputs)
         te.step()
-        te.ctx.download("position", out=hx)
-        te.ctx.download("velocity", out=hv)
-        te.ctx.download("density", out=hrho)
-        te.ctx.download("p / rho^2", out=hk)
-        te.ctx.download("p_v / rho^2", out=hkv)
+        te.ctx.download_fields(outputs)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     te.close()

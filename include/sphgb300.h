@@ -176,6 +176,12 @@ int sphgb_sync(sphgb_ctx *ctx, sphgb_stats *stats);
  * boundary fields) x components */
 int sphgb_download(sphgb_ctx *ctx, int field, void *dst, int dtype);
 int sphgb_upload_field(sphgb_ctx *ctx, int field, const void *src, int dtype);
+/* several fields in one call (no counterpart in the reference, whose host vectors are read
+ * field by field): the same fields, layouts and checks as above, dsts[k] / srcs[k] for
+ * fields[k], all in one dtype; the transfers are queued back to back on the context's stream
+ * and the call waits once.  Uploads compute the slot of each particle id once for all fields. */
+int sphgb_download_fields(sphgb_ctx *ctx, uint32_t count, const int *fields, void *const *dsts, int dtype);
+int sphgb_upload_fields(sphgb_ctx *ctx, uint32_t count, const int *fields, const void *const *srcs, int dtype);
 
 /* neighbour lists of the last step in particle-id order, CSR: offsets[n+1], indices are particle
  * ids.  kind 0 = fluid-fluid, 1 = fluid-boundary (boundary indices in upload order).  Pass

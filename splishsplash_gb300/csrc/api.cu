@@ -2464,35 +2464,97 @@ int sphgb_num_particles(const sphgb_ctx *c, uint32_t *n, uint32_t *nb)
     return SPHGB_OK;
 }
 
-int sphgb_download(sphgb_ctx *c, int field, void *dst, int dtype)
+int sphgb_download_fields(sphgb_ctx *c, uint32_t count, const int *fields, void *const *dsts, int dtype)
 {
-    if (!c || !dst) return SPHGB_ERR_ARGUMENT;
-    if (field < 0 || field > SPHGB_FIELD_OBJECT_ID) return fail(c, SPHGB_ERR_ARGUMENT, "unknown field");
-    if (field == SPHGB_FIELD_FEATURES && !c->mlp_x) return fail(c, SPHGB_ERR_STATE, "features are not computed");
+    if (!c || (count && (!fields || !dsts))) return SPHGB_ERR_ARGUMENT;
     if (dtype < SPHGB_DTYPE_F32 || dtype > SPHGB_DTYPE_U32) return fail(c, SPHGB_ERR_ARGUMENT, "unknown dtype");
     if (!c->have_fluid) return fail(c, SPHGB_ERR_STATE, "no fluid uploaded");
+    // checks, and each field's bytes and place in the staging buffer
+    std::vector<size_t> off(count + 1, 0);
+    bool bfields = false;
+    for (uint32_t k = 0; k < count; k++) {
+        const int field = fields[k];
+        if (!dsts[k]) return SPHGB_ERR_ARGUMENT;
+        if (field < 0 || field > SPHGB_FIELD_OBJECT_ID) return fail(c, SPHGB_ERR_ARGUMENT, "unknown field");
+        if (field == SPHGB_FIELD_FEATURES && !c->mlp_x) return fail(c, SPHGB_ERR_STATE, "features are not computed");
+        const bool bfield = field == SPHGB_FIELD_BOUNDARY_VOLUME || field == SPHGB_FIELD_BOUNDARY_POSITION;
+        bfields = bfields || bfield;
+        const size_t m = bfield ? c->nb : c->n;
+        off[k + 1] = off[k] + ((m * field_components(field) * dtype_size(dtype) + 255) & ~(size_t)255);
+    }
     cudaSetDevice(c->cfg.device);
-    const bool bfield = field == SPHGB_FIELD_BOUNDARY_VOLUME || field == SPHGB_FIELD_BOUNDARY_POSITION;
-    if (bfield && !c->prepared) {
+    if (bfields && !c->prepared) {
         int rc = c->fp64 ? prepare<double>(c) : prepare<float>(c);
         if (rc) return rc;
     }
-    const size_t m = bfield ? c->nb : c->n;
-    const size_t bytes = m * field_components(field) * dtype_size(dtype);
-    if (bytes == 0) return SPHGB_OK;
-    int rc = ensure_staging(c, bytes);
+    if (off[count] == 0) return SPHGB_OK;
+    int rc = ensure_staging(c, off[count]);
     if (rc) return rc;
-    if (c->fp64) {
-        DevParams<double> P = make_params<double>(c);
-        DevBufs<double> B = make_bufs<double>(c, 0);
-        launch_scatter_field<double>(P, B, field, c->staging, dtype, c->stream);
-    } else {
-        DevParams<float> P = make_params<float>(c);
-        DevBufs<float> B = make_bufs<float>(c, 0);
-        launch_scatter_field<float>(P, B, field, c->staging, dtype, c->stream);
+    // every field scattered to particle-id order and copied out, queued back to back; one wait
+    for (uint32_t k = 0; k < count; k++) {
+        const int field = fields[k];
+        const bool bfield = field == SPHGB_FIELD_BOUNDARY_VOLUME || field == SPHGB_FIELD_BOUNDARY_POSITION;
+        const size_t bytes = (size_t)(bfield ? c->nb : c->n) * field_components(field) * dtype_size(dtype);
+        if (bytes == 0) continue;
+        char *st = static_cast<char *>(c->staging) + off[k];
+        if (c->fp64) {
+            DevParams<double> P = make_params<double>(c);
+            DevBufs<double> B = make_bufs<double>(c, 0);
+            launch_scatter_field<double>(P, B, field, st, dtype, c->stream);
+        } else {
+            DevParams<float> P = make_params<float>(c);
+            DevBufs<float> B = make_bufs<float>(c, 0);
+            launch_scatter_field<float>(P, B, field, st, dtype, c->stream);
+        }
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(dsts[k], st, bytes, cudaMemcpyDeviceToHost, c->stream));
     }
+    CK(cudaStreamSynchronize(c->stream));
+    return SPHGB_OK;
+}
+
+int sphgb_download(sphgb_ctx *c, int field, void *dst, int dtype)
+{
+    if (!c || !dst) return SPHGB_ERR_ARGUMENT;
+    return sphgb_download_fields(c, 1u, &field, &dst, dtype);
+}
+
+int sphgb_upload_fields(sphgb_ctx *c, uint32_t count, const int *fields, const void *const *srcs, int dtype)
+{
+    if (!c || (count && (!fields || !srcs))) return SPHGB_ERR_ARGUMENT;
+    for (uint32_t k = 0; k < count; k++) {
+        const int field = fields[k];
+        if (!srcs[k]) return SPHGB_ERR_ARGUMENT;
+        if (field != SPHGB_FIELD_POSITION && field != SPHGB_FIELD_VELOCITY && field != SPHGB_FIELD_VDIFF &&
+            field != SPHGB_FIELD_PRESSURE_RHO2 && field != SPHGB_FIELD_PRESSURE_RHO2_V &&
+            field != SPHGB_FIELD_POSITION_HI && field != SPHGB_FIELD_POSITION_LO)
+            return fail(c, SPHGB_ERR_ARGUMENT, "field is not uploadable");
+    }
+    if (dtype != SPHGB_DTYPE_F32 && dtype != SPHGB_DTYPE_F64) return fail(c, SPHGB_ERR_ARGUMENT, "bad dtype");
+    if (!c->have_fluid) return fail(c, SPHGB_ERR_STATE, "no fluid uploaded");
+    cudaSetDevice(c->cfg.device);
+    sphgb_stats st;
+    if (c->step_pending) fill_stats(c, &st);
+    std::vector<size_t> off(count + 1, 0);
+    for (uint32_t k = 0; k < count; k++)
+        off[k + 1] = off[k] + (((size_t)c->n * field_components(fields[k]) * dtype_size(dtype) + 255) & ~(size_t)255);
+    if (c->n == 0 || off[count] == 0) return SPHGB_OK;
+    int rc = ensure_staging(c, off[count]);
+    if (rc) return rc;
+    // every field copied in, the inverse permutation once, then each field written by id; one wait
+    for (uint32_t k = 0; k < count; k++)
+        CK(cudaMemcpyAsync(static_cast<char *>(c->staging) + off[k], srcs[k],
+                           (size_t)c->n * field_components(fields[k]) * dtype_size(dtype), cudaMemcpyHostToDevice,
+                           c->stream));
+    auto write = [&](auto P, auto B) {
+        launch_inverse_perm(P, B.id, c->inv_perm, c->stream);
+        for (uint32_t k = 0; k < count; k++)
+            launch_upload_field(P, B, fields[k], static_cast<const char *>(c->staging) + off[k], dtype, c->inv_perm,
+                                c->stream);
+    };
+    if (c->fp64) write(make_params<double>(c), make_bufs<double>(c, 0));
+    else write(make_params<float>(c), make_bufs<float>(c, 0));
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(dst, c->staging, bytes, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return SPHGB_OK;
 }
@@ -2500,34 +2562,7 @@ int sphgb_download(sphgb_ctx *c, int field, void *dst, int dtype)
 int sphgb_upload_field(sphgb_ctx *c, int field, const void *src, int dtype)
 {
     if (!c || !src) return SPHGB_ERR_ARGUMENT;
-    if (field != SPHGB_FIELD_POSITION && field != SPHGB_FIELD_VELOCITY && field != SPHGB_FIELD_VDIFF &&
-        field != SPHGB_FIELD_PRESSURE_RHO2 && field != SPHGB_FIELD_PRESSURE_RHO2_V &&
-        field != SPHGB_FIELD_POSITION_HI && field != SPHGB_FIELD_POSITION_LO)
-        return fail(c, SPHGB_ERR_ARGUMENT, "field is not uploadable");
-    if (dtype != SPHGB_DTYPE_F32 && dtype != SPHGB_DTYPE_F64) return fail(c, SPHGB_ERR_ARGUMENT, "bad dtype");
-    if (!c->have_fluid) return fail(c, SPHGB_ERR_STATE, "no fluid uploaded");
-    cudaSetDevice(c->cfg.device);
-    sphgb_stats st;
-    if (c->step_pending) fill_stats(c, &st);
-    const size_t bytes = (size_t)c->n * field_components(field) * dtype_size(dtype);
-    if (bytes == 0) return SPHGB_OK;
-    int rc = ensure_staging(c, bytes);
-    if (rc) return rc;
-    CK(cudaMemcpyAsync(c->staging, src, bytes, cudaMemcpyHostToDevice, c->stream));
-    if (c->fp64) {
-        DevParams<double> P = make_params<double>(c);
-        DevBufs<double> B = make_bufs<double>(c, 0);
-        launch_inverse_perm<double>(P, B.id, c->inv_perm, c->stream);
-        launch_upload_field<double>(P, B, field, c->staging, dtype, c->inv_perm, c->stream);
-    } else {
-        DevParams<float> P = make_params<float>(c);
-        DevBufs<float> B = make_bufs<float>(c, 0);
-        launch_inverse_perm<float>(P, B.id, c->inv_perm, c->stream);
-        launch_upload_field<float>(P, B, field, c->staging, dtype, c->inv_perm, c->stream);
-    }
-    CK(cudaGetLastError());
-    CK(cudaStreamSynchronize(c->stream));
-    return SPHGB_OK;
+    return sphgb_upload_fields(c, 1u, &field, &src, dtype);
 }
 
 int sphgb_neighbors(sphgb_ctx *c, int kind, uint32_t *offsets, uint32_t *indices, size_t capacity)

@@ -121,6 +121,7 @@ EXPORTS = [
     "sphgb_set_params", "sphgb_get_params", "sphgb_upload_boundary", "sphgb_upload_boundary_f32",
     "sphgb_upload_fluid", "sphgb_upload_fluid_f32", "sphgb_set_time_step", "sphgb_get_time_step",
     "sphgb_set_time", "sphgb_step", "sphgb_sync", "sphgb_download", "sphgb_upload_field", "sphgb_neighbors",
+    "sphgb_download_fields", "sphgb_upload_fields",
     "sphgb_num_particles", "sphgb_get_stream", "sphgb_profile_enable", "sphgb_profile_reset", "sphgb_profile_read",
     "sphgb_set_warmstart_mlp", "sphgb_set_feature_output", "sphgb_upload_scenes", "sphgb_num_scenes",
     "sphgb_scene_stats", "sphgb_set_warmstart_gate", "sphgb_set_lanes_per_particle", "sphgb_get_lanes_per_particle",
@@ -170,6 +171,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.sphgb_sync.argtypes = [vp, ctypes.POINTER(Stats)]
     L.sphgb_download.argtypes = [vp, i32, vp, i32]
     L.sphgb_upload_field.argtypes = [vp, i32, vp, i32]
+    L.sphgb_download_fields.argtypes = [vp, ctypes.c_uint32, vp, vp, i32]
+    L.sphgb_upload_fields.argtypes = [vp, ctypes.c_uint32, vp, vp, i32]
     L.sphgb_neighbors.argtypes = [vp, i32, vp, vp, ctypes.c_size_t]
     L.sphgb_num_particles.argtypes = [vp, ctypes.POINTER(u32), ctypes.POINTER(u32)]
     L.sphgb_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
@@ -464,6 +467,35 @@ class Context:
             a = np.ascontiguousarray(a, dtype=np.float64)
         dt = DTYPE_F32 if a.dtype == np.float32 else DTYPE_F64
         self._check(self.L.sphgb_upload_field(self.h, fid, _p(a), dt))
+
+    def download_fields(self, outs: dict) -> dict:
+        """Several fields in one call: {name: out} with C-contiguous float32 (or all float64)
+        targets of n x components elements (e.g. pinned buffers), filled in place."""
+        names = list(outs)
+        arrs = [outs[k] for k in names]
+        dtypes = {a.dtype for a in arrs}
+        if len(dtypes) != 1 or next(iter(dtypes)) not in (np.dtype(np.float32), np.dtype(np.float64)):
+            raise ValueError("download_fields targets must all be float32 or all float64")
+        n, _ = self.num_particles()
+        for k, a in zip(names, arrs):
+            if not a.flags["C_CONTIGUOUS"] or a.size != n * FIELDS[k][1]:
+                raise ValueError(f"download target {k!r} must be C-contiguous with n x components elements")
+        fids = np.array([FIELDS[k][0] for k in names], np.int32)
+        ptrs = (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+        dt = DTYPE_F32 if arrs[0].dtype == np.float32 else DTYPE_F64
+        self._check(self.L.sphgb_download_fields(self.h, len(arrs), _p(fids), ptrs, dt))
+        return outs
+
+    def upload_fields(self, values: dict):
+        """Several fields in one call: {name: particle-id ordered values}, all float32 or all float64."""
+        names = list(values)
+        arrs = [np.asarray(values[k]) for k in names]
+        f32 = all(a.dtype == np.float32 and a.flags["C_CONTIGUOUS"] for a in arrs)
+        if not f32:
+            arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in arrs]
+        fids = np.array([FIELDS[k][0] for k in names], np.int32)
+        ptrs = (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+        self._check(self.L.sphgb_upload_fields(self.h, len(arrs), _p(fids), ptrs, DTYPE_F32 if f32 else DTYPE_F64))
 
     def set_warmstart_mlp(self, mlp):
         """Use a trained network for both warm starts (None: classic warm start only)."""

@@ -9,6 +9,7 @@
 #include "Utilities/Counting.h"
 
 #include <algorithm>
+#include <functional>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -180,44 +181,58 @@ void TimeStepDFSPH_GB300::download()
 	Simulation *sim = Simulation::getCurrent();
 	uint32_t n = 0;
 	check(m_ctx, sphgb_num_particles(m_ctx, &n, nullptr));
-	std::vector<Real> buf(3 * static_cast<size_t>(n));
-	auto field = [&](int f, int comps, auto store) {
-		check(m_ctx, sphgb_download(m_ctx, f, buf.data(), kDtype));
+	// every field in one call (one wait), then handed to the models: model by model in id order
+	using Store = std::function<void(FluidModel *, unsigned int, unsigned int, const Real *)>;
+	struct Column { int field; int comps; Store store; };
+	std::vector<Column> cols = {
+		{SPHGB_FIELD_POSITION, 3, [](FluidModel *fm, unsigned, unsigned i, const Real *s) {
+			fm->getPosition(i) = Vector3r(s[0], s[1], s[2]); }},
+		{SPHGB_FIELD_VELOCITY, 3, [](FluidModel *fm, unsigned, unsigned i, const Real *s) {
+			fm->getVelocity(i) = Vector3r(s[0], s[1], s[2]); }},
+		{SPHGB_FIELD_ACCELERATION, 3, [](FluidModel *fm, unsigned, unsigned i, const Real *s) {
+			fm->getAcceleration(i) = Vector3r(s[0], s[1], s[2]); }},
+		{SPHGB_FIELD_DENSITY, 1, [](FluidModel *fm, unsigned, unsigned i, const Real *s) { fm->getDensity(i) = s[0]; }},
+		{SPHGB_FIELD_FACTOR, 1, [this](FluidModel *, unsigned k, unsigned i, const Real *s) {
+			m_simulationData.getFactor(k, i) = s[0]; }},
+		{SPHGB_FIELD_DENSITY_ADV, 1, [this](FluidModel *, unsigned k, unsigned i, const Real *s) {
+			m_simulationData.getDensityAdv(k, i) = s[0]; }},
+		{SPHGB_FIELD_PRESSURE_RHO2, 1, [this](FluidModel *, unsigned k, unsigned i, const Real *s) {
+			m_simulationData.getPressureRho2(k, i) = s[0]; }},
+		{SPHGB_FIELD_PRESSURE_RHO2_V, 1, [this](FluidModel *, unsigned k, unsigned i, const Real *s) {
+			m_simulationData.getPressureRho2_V(k, i) = s[0]; }},
+		{SPHGB_FIELD_PRESSURE_ACCEL, 3, [this](FluidModel *, unsigned k, unsigned i, const Real *s) {
+			m_simulationData.getPressureAccel(k, i) = Vector3r(s[0], s[1], s[2]); }},
+	};
+	bool anyWeiler = false;
+	for (unsigned int k = 0; k < sim->numberOfFluidModels(); k++)
+		anyWeiler = anyWeiler || weiler(sim->getFluidModel(k)) != nullptr;
+	if (anyWeiler)
+		cols.push_back({SPHGB_FIELD_VDIFF, 3, [](FluidModel *fm, unsigned, unsigned i, const Real *s) {
+			if (Viscosity_Weiler2018 *w = weiler(fm))
+				w->getVDiff(i) = Vector3r(s[0], s[1], s[2]);
+		}});
+	std::vector<std::vector<Real>> bufs(cols.size());
+	std::vector<int> ids(cols.size());
+	std::vector<void *> dsts(cols.size());
+	for (size_t c = 0; c < cols.size(); c++)
+	{
+		bufs[c].resize(static_cast<size_t>(n) * cols[c].comps);
+		ids[c] = cols[c].field;
+		dsts[c] = bufs[c].data();
+	}
+	check(m_ctx, sphgb_download_fields(m_ctx, static_cast<uint32_t>(cols.size()), ids.data(), dsts.data(), kDtype));
+	for (size_t c = 0; c < cols.size(); c++)
+	{
 		size_t off = 0;
 		for (unsigned int k = 0; k < sim->numberOfFluidModels(); k++)
 		{
 			FluidModel *fm = sim->getFluidModel(k);
 			const unsigned int m = fm->numActiveParticles();
 			for (unsigned int i = 0; i < m; i++)
-				store(fm, k, i, &buf[off + static_cast<size_t>(i) * comps]);
-			off += static_cast<size_t>(m) * comps;
+				cols[c].store(fm, k, i, &bufs[c][off + static_cast<size_t>(i) * cols[c].comps]);
+			off += static_cast<size_t>(m) * cols[c].comps;
 		}
-	};
-	field(SPHGB_FIELD_POSITION, 3, [](FluidModel *fm, unsigned, unsigned i, const Real *s) {
-		fm->getPosition(i) = Vector3r(s[0], s[1], s[2]); });
-	field(SPHGB_FIELD_VELOCITY, 3, [](FluidModel *fm, unsigned, unsigned i, const Real *s) {
-		fm->getVelocity(i) = Vector3r(s[0], s[1], s[2]); });
-	field(SPHGB_FIELD_ACCELERATION, 3, [](FluidModel *fm, unsigned, unsigned i, const Real *s) {
-		fm->getAcceleration(i) = Vector3r(s[0], s[1], s[2]); });
-	field(SPHGB_FIELD_DENSITY, 1, [](FluidModel *fm, unsigned, unsigned i, const Real *s) { fm->getDensity(i) = s[0]; });
-	field(SPHGB_FIELD_FACTOR, 1, [this](FluidModel *, unsigned k, unsigned i, const Real *s) {
-		m_simulationData.getFactor(k, i) = s[0]; });
-	field(SPHGB_FIELD_DENSITY_ADV, 1, [this](FluidModel *, unsigned k, unsigned i, const Real *s) {
-		m_simulationData.getDensityAdv(k, i) = s[0]; });
-	field(SPHGB_FIELD_PRESSURE_RHO2, 1, [this](FluidModel *, unsigned k, unsigned i, const Real *s) {
-		m_simulationData.getPressureRho2(k, i) = s[0]; });
-	field(SPHGB_FIELD_PRESSURE_RHO2_V, 1, [this](FluidModel *, unsigned k, unsigned i, const Real *s) {
-		m_simulationData.getPressureRho2_V(k, i) = s[0]; });
-	field(SPHGB_FIELD_PRESSURE_ACCEL, 3, [this](FluidModel *, unsigned k, unsigned i, const Real *s) {
-		m_simulationData.getPressureAccel(k, i) = Vector3r(s[0], s[1], s[2]); });
-	bool anyWeiler = false;
-	for (unsigned int k = 0; k < sim->numberOfFluidModels(); k++)
-		anyWeiler = anyWeiler || weiler(sim->getFluidModel(k)) != nullptr;
-	if (anyWeiler)
-		field(SPHGB_FIELD_VDIFF, 3, [](FluidModel *fm, unsigned, unsigned i, const Real *s) {
-			if (Viscosity_Weiler2018 *w = weiler(fm))
-				w->getVDiff(i) = Vector3r(s[0], s[1], s[2]);
-		});
+	}
 }
 
 void TimeStepDFSPH_GB300::step()

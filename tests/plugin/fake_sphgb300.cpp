@@ -126,6 +126,15 @@ int sphgb_download(sphgb_ctx *ctx, int field, void *dst, int dtype)
     }
     return SPHGB_OK;
 }
+
+int sphgb_download_fields(sphgb_ctx *ctx, uint32_t count, const int *fields, void *const *dsts, int dtype)
+{
+    for (uint32_t k = 0; k < count; k++) {
+        const int rc = sphgb_download(ctx, fields[k], dsts[k], dtype);
+        if (rc) return rc;
+    }
+    return SPHGB_OK;
+}
 int sphgb_set_fluid_phases(sphgb_ctx *ctx, uint32_t nphases, const uint32_t *, const double *)
 {
     return nphases <= 1 ? SPHGB_OK : fail(ctx, SPHGB_ERR_ARGUMENT, "one fluid model in the stand-in");

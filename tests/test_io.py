@@ -244,3 +244,31 @@ def test_state_file_restores_a_batch():
     np.testing.assert_array_equal(a.ctx.download("position"), b.download("position"))
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_batched_field_transfers_equal_single_ones(precision):
+    """sphgb_download_fields / sphgb_upload_fields: the same values as one call per field, in
+    float32 and float64 targets; an unknown or non-uploadable field is refused."""
+    sc = scenes.small_block(counts=(9, 8, 7), viscosity=True, velocity=(0.2, 0.0, -0.1)).as_float32()
+    ts = TimeStepDFSPH(sc, precision=precision)
+    try:
+        for _ in range(4):
+            ts.step()
+        ctx = ts.ctx
+        names = ("position", "velocity", "density", "p / rho^2", "p_v / rho^2", "velocity difference")
+        for dt in (np.float32, np.float64):
+            single = {k: ctx.download(k, dtype=dt) for k in names}
+            many = ctx.download_fields({k: np.zeros_like(v) for k, v in single.items()})
+            for k in names:
+                np.testing.assert_array_equal(many[k], single[k])
+        rng = np.random.default_rng(5)
+        new = {"velocity": rng.uniform(-1, 1, (sc.n, 3)).astype(np.float32),
+               "p / rho^2": rng.uniform(0, 1e-4, sc.n).astype(np.float32)}
+        ctx.upload_fields(new)
+        for k, v in new.items():
+            np.testing.assert_array_equal(ctx.download(k, dtype=np.float32), v)
+        with pytest.raises(native.SphgbError):
+            ctx.upload_fields({"density": np.zeros(sc.n, np.float32)})
+    finally:
+        ts.close()
