@@ -197,6 +197,23 @@ def run_oracle_sample(scene, state, budget_s, threads, prefer="auto"):
     return scene.n * steps / dt, steps, dt, iters, kind, desc
 
 
+def max_over_ranks(x: float, dist, device) -> float:
+    """The largest x over the ranks (the slowest replica's time); x itself without a process
+    group.  device: the tensor's device for the group's backend (cuda for NCCL, cpu for gloo)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(world: int, n: int, steps: int, seconds: float) -> float:
+    """Whole-job particle-steps/s of `world` replicas, each advancing n particles `steps` times,
+    timed by the slowest replica's `seconds` (replicas only: no data-path collective)."""
+    return world * n * steps / seconds
+
+
 def run_reference(args):
     """The reference arm: the CPU implementation of the step on all host threads, on this
     benchmark's workload and step window (warm-up steps, then the timed steps)."""
@@ -494,13 +511,10 @@ def main():
     wall = time.perf_counter() - t_wall
     clk = clocks.stop()
     dev_s = sum(a.elapsed_time(b) for a, b in evs) / 1e3
-    t_max = dev_s
+    t_max = max_over_ranks(dev_s, dist, f"cuda:{local}")
     if dist:
-        t = torch.tensor([dev_s], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
         dist.barrier()
-    value = world * scene.n * args.steps / t_max
+    value = replica_rate(world, scene.n, args.steps, t_max)
     lanes, trial_ms = ts.ctx.lanes_per_particle()
     staged, staged_frac, staged_trial_ms = ts.ctx.neighbor_staging()
     if args.only_timed:
@@ -539,11 +553,8 @@ def main():
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     te.close()
-    if dist:
-        t = torch.tensor([e2e_s], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = {"value": world * n * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 2 * n * 3 * 4,
+    e2e_s = max_over_ranks(e2e_s, dist, f"cuda:{local}")
+    e2e = {"value": replica_rate(world, n, e2e_steps, e2e_s), "unit": UNIT, "h2d_bytes_per_step": 2 * n * 3 * 4,
            "d2h_bytes_per_step": 2 * n * 3 * 4 + 3 * n * 4, "steps": e2e_steps,
            "region": f"steps {args.warmup + 1}..{args.warmup + e2e_steps} of a fresh context (same as the timed run)"}
 
