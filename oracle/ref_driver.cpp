@@ -472,6 +472,60 @@ int ref_body_forces(double *force, double *torque)
     return (int)sim->numberOfBoundaryModels();
 }
 
+/** Moves body b (ref_set_bodies) for the next step: rotation R (row-major), position t, linear
+ *  velocity v and angular velocity w of its rigid body, then its particles as the simulator places
+ *  them before every step (SimulatorBase::updateBoundaryParticles, SimulatorBase.cpp:1617-1645):
+ *  x_j = R x0_j + t, v_j = w x (x_j - t) + v.  The body counts as animated from then on. */
+int ref_set_body_motion(unsigned int b, const double *R, const double *t, const double *v, const double *w)
+{
+    Simulation *sim = Simulation::getCurrent();
+    if (b >= sim->numberOfBoundaryModels()) return -1;
+    BoundaryModel_Akinci2012 *bm = dynamic_cast<BoundaryModel_Akinci2012 *>(sim->getBoundaryModel(b));
+    if (!bm) return -1;
+    RigidBodyObject *rbo = bm->getRigidBodyObject();
+    rbo->setIsAnimated(true);
+    Matrix3r Rm;
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) Rm(r, c) = static_cast<Real>(R[3 * r + c]);
+    rbo->setRotation(Quaternionr(Rm));
+    rbo->setPosition(Vector3r(static_cast<Real>(t[0]), static_cast<Real>(t[1]), static_cast<Real>(t[2])));
+    rbo->setVelocity(Vector3r(static_cast<Real>(v[0]), static_cast<Real>(v[1]), static_cast<Real>(v[2])));
+    rbo->setAngularVelocity(Vector3r(static_cast<Real>(w[0]), static_cast<Real>(w[1]), static_cast<Real>(w[2])));
+    const Matrix3r Rq = rbo->getRotation().toRotationMatrix();
+    for (unsigned int j = 0; j < bm->numberOfParticles(); j++) {
+        bm->getPosition(j) = Rq * bm->getPosition0(j) + rbo->getPosition();
+        bm->getVelocity(j) = rbo->getAngularVelocity().cross(bm->getPosition(j) - rbo->getPosition()) + rbo->getVelocity();
+    }
+    return 0;
+}
+
+/** Moves the body of volume map b (boundaryMethod 2) for the next step: its rigid body's rotation
+ *  R (row-major), position t, linear velocity v and angular velocity w, the body's CFL radius
+ *  max_dist, and its CFL speed bound as the simulator sets it before every step
+ *  (SimulatorBase::updateVMVelocity, SimulatorBase.cpp:1670-1687): |w x (max_dist, 0, 0) + v|.
+ *  The body counts as animated from then on. */
+int ref_set_map_motion(unsigned int b, const double *R, const double *t, const double *v, const double *w,
+                       double max_dist)
+{
+    Simulation *sim = Simulation::getCurrent();
+    if (b >= sim->numberOfBoundaryModels()) return -1;
+    BoundaryModel_Bender2019 *bm = dynamic_cast<BoundaryModel_Bender2019 *>(sim->getBoundaryModel(b));
+    if (!bm) return -1;
+    RigidBodyObject *rbo = bm->getRigidBodyObject();
+    rbo->setIsAnimated(true);
+    Matrix3r Rm;
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) Rm(r, c) = static_cast<Real>(R[3 * r + c]);
+    rbo->setRotation(Quaternionr(Rm));
+    rbo->setPosition(Vector3r(static_cast<Real>(t[0]), static_cast<Real>(t[1]), static_cast<Real>(t[2])));
+    rbo->setVelocity(Vector3r(static_cast<Real>(v[0]), static_cast<Real>(v[1]), static_cast<Real>(v[2])));
+    rbo->setAngularVelocity(Vector3r(static_cast<Real>(w[0]), static_cast<Real>(w[1]), static_cast<Real>(w[2])));
+    bm->setMaxDist(static_cast<Real>(max_dist));
+    const Vector3r x(bm->getMaxDist(), 0.0, 0.0);
+    bm->setMaxVel((rbo->getAngularVelocity().cross(x) + rbo->getVelocity()).norm());
+    return 0;
+}
+
 /** BoundaryModel::clearForceAndTorque of every dynamic body. */
 void ref_clear_body_forces()
 {

@@ -89,6 +89,10 @@ def lib(precision: str = "f64", path: str = None) -> ctypes.CDLL:
         L.ref_body_forces.argtypes = [dp, dp]
         L.ref_body_forces.restype = ctypes.c_int
         L.ref_clear_body_forces.restype = None
+        L.ref_set_body_motion.argtypes = [ctypes.c_uint, dp, dp, dp, dp]
+        L.ref_set_body_motion.restype = ctypes.c_int
+        L.ref_set_map_motion.argtypes = [ctypes.c_uint, dp, dp, dp, dp, ctypes.c_double]
+        L.ref_set_map_motion.restype = ctypes.c_int
         _LIBS[key] = L
     return _LIBS[key]
 
@@ -224,6 +228,19 @@ class RefSim:
 
     def clear_body_forces(self) -> None:
         self.L.ref_clear_body_forces()
+
+    def set_body_motion(self, b, rotation, translation, velocity, omega) -> None:
+        """Pose and velocity of body b for the next step; its particles are placed as the
+        simulator places them (x = R x0 + t, v = w x (x - t) + v)."""
+        a = [np.ascontiguousarray(q, np.float64).reshape(-1) for q in (rotation, translation, velocity, omega)]
+        if self.L.ref_set_body_motion(int(b), *[_dp(q) for q in a]) != 0:
+            raise RuntimeError("ref_set_body_motion failed")
+
+    def set_map_motion(self, b, rotation, translation, velocity, omega, max_dist=0.0) -> None:
+        """Pose, velocity and CFL radius of the body of volume map b for the next step."""
+        a = [np.ascontiguousarray(q, np.float64).reshape(-1) for q in (rotation, translation, velocity, omega)]
+        if self.L.ref_set_map_motion(int(b), *[_dp(q) for q in a], float(max_dist)) != 0:
+            raise RuntimeError("ref_set_map_motion failed")
 
     def neighbor_counts(self):
         nf = np.zeros(self.n, np.uint32)

@@ -243,6 +243,84 @@ def test_body_forces_follow_the_reference(ref_build):
     assert cg > 0 and float(np.abs(o.body_force[0]).max()) > 0
 
 
+def test_moving_body_follows_the_reference(ref_build):
+    """A moving Akinci2012 body: the floor of the all-terms scene slides at 4.6 m/s (fast enough for
+    its particles to set the CFL step) and spins about its position.  Before every step the
+    reference's rigid body gets its pose and velocity and the driver places the floor's particles
+    as the simulator does (x = R x0 + t, v = w x (x - t) + v); the oracle gets the same particles
+    and velocities.  Over 15 steps the step sizes, iteration counts, fields, and the force and
+    torque on every body agree at 1e-10."""
+    from test_bodies import CENTERS, DYNAMIC, all_terms_scene, container_bodies
+    sc = all_terms_scene()
+    sc.v[:, 0] = 0.5 * (sc.x[:, 1] - sc.x[:, 1].mean())
+    body = container_bodies(sc.xb, 1.0)
+    u, w = np.array([4.5, 0.0, -1.0]), np.array([0.0, 0.8, 0.0])
+    o = oracle.OracleSim(sc, fp32_predicate=False)
+    o.set_bodies(body, CENTERS, DYNAMIC)
+    x0, floor = o.xb.copy(), (body == 0)[:, None]
+    capped = False
+    with refsim.RefSim(sc, bodies=dict(body=body, center=CENTERS, dynamic=DYNAMIC)) as r:
+        for k in range(15):
+            t = u * o.st.time
+            r.set_body_motion(0, np.eye(3), t, u, w)
+            xb = np.where(floor, x0 + t, x0)
+            o.set_boundary_state(xb, np.where(floor, np.cross(w, xb - t) + u, 0.0))
+            o.body_center[0] = t
+            r.clear_body_forces()
+            o.clear_forces()
+            sr = r.step()
+            o.step()
+            so = o.stats()
+            capped = capped or sr["dt"] < sc.params.cflMaxTimeStepSize
+            assert (sr["iterations"], sr["iterations_v"], sr["visco_iterations"]) == \
+                (so["iterations"], so["iterations_v"], so["visco_iterations"]), k
+            assert sr["dt"] == pytest.approx(so["dt"], rel=1e-12), k
+            fr, tr = r.body_forces()
+            assert float(np.abs(fr - o.body_force).max()) <= ORACLE_TOL * float(np.abs(o.body_force).max()), k
+            assert float(np.abs(tr - o.body_torque).max()) <= ORACLE_TOL * float(np.abs(o.body_torque).max()), k
+            got = dict(density=r.get("density"), factor=r.get("factor"), kappa=r.get("p / rho^2"),
+                       kappa_v=r.get("p_v / rho^2"), v=r.get("velocity"), x=r.get("position"))
+            ref = dict(density=o.density, factor=o.factor, kappa=o.kappa, kappa_v=o.kappa_v, v=o.v, x=o.x)
+            for name, e in ref_cases.field_errors(got, ref).items():
+                assert e <= ORACLE_TOL, (k, name, e)
+    assert capped   # the moving particles set the CFL step
+
+
+def test_moving_volume_map_follows_the_reference(ref_build):
+    """A moving Bender2019 body: the volume-mapped box of the vmap_box fixture translates at
+    (2, 0, 0.5) m/s and turns about the vertical axis.  Before every step the reference's rigid
+    body gets the pose and velocity, and its CFL bound as the simulator's updateVMVelocity sets it;
+    the oracle's map gets the same.  Over 15 steps iteration counts and fields agree at 1e-10."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("gen_ref_steps", os.path.join(ROOT, "tests", "golden",
+                                                                                 "gen_ref_steps.py"))
+    gen = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(gen)
+    sc = gen.vmap_box().as_float32()
+    maps = [gen.box_volume_map(sc.params.supportRadius)]
+    u, w, max_dist = np.array([2.0, 0.0, 0.5]), np.array([0.0, 0.6, 0.0]), 0.7
+    o = oracle.OracleSim(sc, fp32_predicate=False)
+    o.set_volume_maps(maps)
+    with refsim.RefSim(sc, volume_maps=maps) as r:
+        for k in range(15):
+            time = o.st.time
+            c, s_ = np.cos(w[1] * time), np.sin(w[1] * time)
+            R = np.array([[c, 0.0, s_], [0.0, 1.0, 0.0], [-s_, 0.0, c]])
+            r.set_map_motion(0, R, u * time, u, w, max_dist)
+            o.set_map_motion(0, R, u * time, u, w, max_dist)
+            sr = r.step()
+            o.step()
+            so = o.stats()
+            assert (sr["iterations"], sr["iterations_v"], sr["visco_iterations"]) == \
+                (so["iterations"], so["iterations_v"], so["visco_iterations"]), k
+            assert sr["dt"] == pytest.approx(so["dt"], rel=1e-12), k
+            got = dict(density=r.get("density"), factor=r.get("factor"), kappa=r.get("p / rho^2"),
+                       kappa_v=r.get("p_v / rho^2"), v=r.get("velocity"), x=r.get("position"))
+            ref = dict(density=o.density, factor=o.factor, kappa=o.kappa, kappa_v=o.kappa_v, v=o.v, x=o.x)
+            for name, e in ref_cases.field_errors(got, ref).items():
+                assert e <= ORACLE_TOL, (k, name, e)
+
+
 def test_reference_neighbor_counts_match_oracle(ref_build):
     sc = scenes.small_block(counts=(10, 8, 10), box=(0.8, 0.8, 0.8)).as_float32()
     with refsim.RefSim(sc) as r:
