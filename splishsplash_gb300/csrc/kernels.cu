@@ -909,12 +909,20 @@ __device__ __forceinline__ void build_one(const DevParams<T> &P, const DevBufs<T
     }
 }
 
-template <class T>
+// ST: the instance that may write the staged passes' local lists.  Without staging the instance
+// compiled without that code is used (0.49 against 0.53 ms at 1M particles).
+template <class T, bool ST>
 __global__ void __launch_bounds__(kBlock) k_build(DevParams<T> P, DevBufs<T> B)
 {
     count_launch(&B.gsc->launches);
     const SlotInfo q = slot_info(P);
     StepScalars *const sc = B.sc + q.s;
+    if constexpr (!ST) {
+        uint32_t nf = 0, nb = 0;
+        if (q.act) build_one(P, B, scene_get(P, q.s), q.s, sc, q.i, nf, nb, nullptr, nullptr, 0u);
+        block_max_atomic(nf, nb, &sc->max_nf, &sc->max_nb);
+        return;
+    }
     __shared__ uint32_t tcell[kStageCells];
     __shared__ uint16_t toff[kStageCells];
     uint32_t tn = 0;
@@ -2843,7 +2851,8 @@ template <class T> void launch_stage_table(const DevParams<T> &P, const DevBufs<
 }
 template <class T> void launch_build(const DevParams<T> &P, const DevBufs<T> &B, cudaStream_t s)
 {
-    if (P.np) k_build<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
+    if (P.np && P.staged) k_build<T, true><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
+    else if (P.np) k_build<T, false><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
 }
 template <class T> void launch_pressure_accel(const DevParams<T> &P, const DevBufs<T> &B, bool div, int phase, cudaStream_t s,
                                               cudaGraphConditionalHandle h, bool use_handle)
