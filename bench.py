@@ -408,7 +408,8 @@ def ensemble_line(steps, device):
         with torch.cuda.stream(ext):
             evs[k][1].record(ext)
         per = b.scene_stats()
-        it.append((st["iterations"], float(np.mean([p["iterations"] for p in per]))))
+        it.append((st["iterations"], float(np.mean([p["iterations"] for p in per])),
+                   st["iterations_v"], float(np.mean([p["iterations_v"] for p in per]))))
     torch.cuda.synchronize()
     dev_s = sum(a.elapsed_time(c) for a, c in evs) / 1e3
     n = int(b.sizes.sum())
@@ -417,7 +418,9 @@ def ensemble_line(steps, device):
     return {"workload": f"256 dam-break scenes, {n} fluid particles in total, r=0.025, per-scene CFL dt",
             "value": n * steps / dev_s, "unit": UNIT, "steps": steps, "warmup": 10,
             "ms_per_step": 1e3 * dev_s / steps,
-            "pressure_iterations": {"batch_loop_mean": float(it[:, 0].mean()), "scene_mean": float(it[:, 1].mean())}}
+            "pressure_iterations": {"batch_loop_mean": float(it[:, 0].mean()), "scene_mean": float(it[:, 1].mean())},
+            "divergence_iterations": {"batch_loop_mean": float(it[:, 2].mean()),
+                                      "scene_mean": float(it[:, 3].mean())}}
 
 
 def main():

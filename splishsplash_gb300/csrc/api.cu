@@ -1722,6 +1722,8 @@ int sphgb_create(const sphgb_config *cfg, sphgb_ctx **out)
     if (e != cudaSuccess) {
         cudaGetLastError();
         if (c->hsc) cudaFreeHost(c->hsc);
+        if (c->stream) cudaStreamDestroy(c->stream);
+        if (c->body_stream) cudaStreamDestroy(c->body_stream);
         delete c;
         return SPHGB_ERR_CUDA;
     }
