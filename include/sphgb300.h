@@ -179,7 +179,10 @@ int sphgb_upload_field(sphgb_ctx *ctx, int field, const void *src, int dtype);
 /* several fields in one call (no counterpart in the reference, whose host vectors are read
  * field by field): the same fields, layouts and checks as above, dsts[k] / srcs[k] for
  * fields[k], all in one dtype; the transfers are queued back to back on the context's stream
- * and the call waits once.  Uploads compute the slot of each particle id once for all fields. */
+ * and the call waits once.  Uploads compute the slot of each particle id once for all fields.
+ * A fluid field whose buffer is page-locked host memory mapped into the device's address space
+ * (cudaHostAlloc, cudaHostRegister) is read or written by the device itself, in particle-id
+ * order, with no staging copy; other buffers are staged in device memory and copied. */
 int sphgb_download_fields(sphgb_ctx *ctx, uint32_t count, const int *fields, void *const *dsts, int dtype);
 int sphgb_upload_fields(sphgb_ctx *ctx, uint32_t count, const int *fields, const void *const *srcs, int dtype);
 

@@ -2466,14 +2466,30 @@ int sphgb_num_particles(const sphgb_ctx *c, uint32_t *n, uint32_t *nb)
     return SPHGB_OK;
 }
 
+// The device's address of page-locked host memory mapped into its address space (cudaHostAlloc,
+// cudaHostRegister on a unified address space), else null: such a buffer is read or written by
+// the transfer kernels themselves, with no staging copy.
+void *mapped_host(const void *p)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 int sphgb_download_fields(sphgb_ctx *c, uint32_t count, const int *fields, void *const *dsts, int dtype)
 {
     if (!c || (count && (!fields || !dsts))) return SPHGB_ERR_ARGUMENT;
     if (dtype < SPHGB_DTYPE_F32 || dtype > SPHGB_DTYPE_U32) return fail(c, SPHGB_ERR_ARGUMENT, "unknown dtype");
     if (!c->have_fluid) return fail(c, SPHGB_ERR_STATE, "no fluid uploaded");
-    // checks, and each field's bytes and place in the staging buffer
+    cudaSetDevice(c->cfg.device);
+    // checks; fluid fields into mapped host memory are written in particle-id order by the device,
+    // the others get a place in the staging buffer
     std::vector<size_t> off(count + 1, 0);
-    bool bfields = false;
+    std::vector<void *> direct(count, nullptr);
+    bool bfields = false, any_direct = false;
     for (uint32_t k = 0; k < count; k++) {
         const int field = fields[k];
         if (!dsts[k]) return SPHGB_ERR_ARGUMENT;
@@ -2481,36 +2497,45 @@ int sphgb_download_fields(sphgb_ctx *c, uint32_t count, const int *fields, void 
         if (field == SPHGB_FIELD_FEATURES && !c->mlp_x) return fail(c, SPHGB_ERR_STATE, "features are not computed");
         const bool bfield = field == SPHGB_FIELD_BOUNDARY_VOLUME || field == SPHGB_FIELD_BOUNDARY_POSITION;
         bfields = bfields || bfield;
+        if (!bfield) direct[k] = mapped_host(dsts[k]);
+        any_direct = any_direct || direct[k];
         const size_t m = bfield ? c->nb : c->n;
-        off[k + 1] = off[k] + ((m * field_components(field) * dtype_size(dtype) + 255) & ~(size_t)255);
+        off[k + 1] = off[k] + (direct[k] ? 0 : ((m * field_components(field) * dtype_size(dtype) + 255) & ~(size_t)255));
     }
-    cudaSetDevice(c->cfg.device);
     if (bfields && !c->prepared) {
         int rc = c->fp64 ? prepare<double>(c) : prepare<float>(c);
         if (rc) return rc;
     }
-    if (off[count] == 0) return SPHGB_OK;
-    int rc = ensure_staging(c, off[count]);
-    if (rc) return rc;
-    // every field scattered to particle-id order and copied out, queued back to back; one wait
-    for (uint32_t k = 0; k < count; k++) {
-        const int field = fields[k];
-        const bool bfield = field == SPHGB_FIELD_BOUNDARY_VOLUME || field == SPHGB_FIELD_BOUNDARY_POSITION;
-        const size_t bytes = (size_t)(bfield ? c->nb : c->n) * field_components(field) * dtype_size(dtype);
-        if (bytes == 0) continue;
-        char *st = static_cast<char *>(c->staging) + off[k];
-        if (c->fp64) {
-            DevParams<double> P = make_params<double>(c);
-            DevBufs<double> B = make_bufs<double>(c, 0);
-            launch_scatter_field<double>(P, B, field, st, dtype, c->stream);
-        } else {
-            DevParams<float> P = make_params<float>(c);
-            DevBufs<float> B = make_bufs<float>(c, 0);
-            launch_scatter_field<float>(P, B, field, st, dtype, c->stream);
-        }
-        CK(cudaGetLastError());
-        CK(cudaMemcpyAsync(dsts[k], st, bytes, cudaMemcpyDeviceToHost, c->stream));
+    if (off[count] == 0 && (!any_direct || c->n == 0)) return SPHGB_OK;
+    if (off[count]) {
+        int rc = ensure_staging(c, off[count]);
+        if (rc) return rc;
     }
+    // every field queued back to back, one wait: written straight to mapped host memory, or
+    // scattered to particle-id order in the staging buffer and copied out
+    auto emit = [&](auto P, auto B) -> int {
+        if (any_direct && c->n) launch_inverse_perm(P, B.id, c->inv_perm, c->stream);
+        for (uint32_t k = 0; k < count; k++) {
+            const int field = fields[k];
+            const bool bfield = field == SPHGB_FIELD_BOUNDARY_VOLUME || field == SPHGB_FIELD_BOUNDARY_POSITION;
+            const size_t bytes = (size_t)(bfield ? c->nb : c->n) * field_components(field) * dtype_size(dtype);
+            if (bytes == 0) continue;
+            if (direct[k]) {
+                launch_gather_field(P, B, field, direct[k], dtype, c->inv_perm, (uint32_t)field_components(field),
+                                    c->stream);
+                CK(cudaGetLastError());
+                continue;
+            }
+            char *st = static_cast<char *>(c->staging) + off[k];
+            launch_scatter_field(P, B, field, st, dtype, c->stream);
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(dsts[k], st, bytes, cudaMemcpyDeviceToHost, c->stream));
+        }
+        return SPHGB_OK;
+    };
+    const int rc = c->fp64 ? emit(make_params<double>(c), make_bufs<double>(c, 0))
+                           : emit(make_params<float>(c), make_bufs<float>(c, 0));
+    if (rc) return rc;
     CK(cudaStreamSynchronize(c->stream));
     return SPHGB_OK;
 }
@@ -2537,22 +2562,31 @@ int sphgb_upload_fields(sphgb_ctx *c, uint32_t count, const int *fields, const v
     cudaSetDevice(c->cfg.device);
     sphgb_stats st;
     if (c->step_pending) fill_stats(c, &st);
+    // fields in mapped host memory are read by the device directly, the others staged
     std::vector<size_t> off(count + 1, 0);
-    for (uint32_t k = 0; k < count; k++)
-        off[k + 1] = off[k] + (((size_t)c->n * field_components(fields[k]) * dtype_size(dtype) + 255) & ~(size_t)255);
-    if (c->n == 0 || off[count] == 0) return SPHGB_OK;
-    int rc = ensure_staging(c, off[count]);
-    if (rc) return rc;
-    // every field copied in, the inverse permutation once, then each field written by id; one wait
-    for (uint32_t k = 0; k < count; k++)
-        CK(cudaMemcpyAsync(static_cast<char *>(c->staging) + off[k], srcs[k],
+    std::vector<const void *> in(count, nullptr);
+    for (uint32_t k = 0; k < count; k++) {
+        in[k] = mapped_host(srcs[k]);
+        off[k + 1] = off[k] + (in[k] ? 0 : (((size_t)c->n * field_components(fields[k]) * dtype_size(dtype) + 255) &
+                                            ~(size_t)255));
+    }
+    if (c->n == 0 || count == 0) return SPHGB_OK;
+    if (off[count]) {
+        int rc = ensure_staging(c, off[count]);
+        if (rc) return rc;
+    }
+    // every staged field copied in, the inverse permutation once, then each field written by id;
+    // one wait
+    for (uint32_t k = 0; k < count; k++) {
+        if (in[k]) continue;
+        in[k] = static_cast<const char *>(c->staging) + off[k];
+        CK(cudaMemcpyAsync(const_cast<void *>(in[k]), srcs[k],
                            (size_t)c->n * field_components(fields[k]) * dtype_size(dtype), cudaMemcpyHostToDevice,
                            c->stream));
+    }
     auto write = [&](auto P, auto B) {
         launch_inverse_perm(P, B.id, c->inv_perm, c->stream);
-        for (uint32_t k = 0; k < count; k++)
-            launch_upload_field(P, B, fields[k], static_cast<const char *>(c->staging) + off[k], dtype, c->inv_perm,
-                                c->stream);
+        for (uint32_t k = 0; k < count; k++) launch_upload_field(P, B, fields[k], in[k], dtype, c->inv_perm, c->stream);
     };
     if (c->fp64) write(make_params<double>(c), make_bufs<double>(c, 0));
     else write(make_params<float>(c), make_bufs<float>(c, 0));

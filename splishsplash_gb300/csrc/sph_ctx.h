@@ -307,6 +307,10 @@ template <class T> void launch_boundary_gather(const DevParams<T> &P, const DevB
                                                cudaStream_t s);
 template <class T> void launch_scatter_field(const DevParams<T> &P, const DevBufs<T> &B, int field, void *out,
                                              int out_dtype, cudaStream_t s);
+// a fluid field (comps components) in particle-id order from slot inv[id], written as contiguous
+// ranges (host memory the device maps)
+template <class T> void launch_gather_field(const DevParams<T> &P, const DevBufs<T> &B, int field, void *out, int odt,
+                                            const uint32_t *inv, uint32_t comps, cudaStream_t s);
 template <class T> void launch_upload_field(const DevParams<T> &P, const DevBufs<T> &B, int field, const void *in,
                                             int in_dtype, const uint32_t *inv, cudaStream_t s);
 template <class T> void launch_init_state(const DevParams<T> &P, const DevBufs<T> &B, const double *x,

@@ -272,3 +272,42 @@ def test_batched_field_transfers_equal_single_ones(precision):
             ctx.upload_fields({"density": np.zeros(sc.n, np.float32)})
     finally:
         ts.close()
+
+
+@pytest.mark.parametrize("batch", [False, True])
+def test_transfers_through_mapped_host_memory_match_staged_ones(batch):
+    """Fields to and from page-locked host buffers are written and read by the device directly,
+    in particle-id order; the values equal those of the staged copies into pageable buffers, in
+    float32 and float64, for one scene and for a batch of scenes."""
+    torch = pytest.importorskip("torch")
+    if batch:
+        sc = [scenes.small_block(counts=(9, 8, 7), seed=1, velocity=(0.2, 0.0, -0.1)).as_float32(),
+              scenes.small_block(counts=(6, 6, 6), seed=2, velocity=(-0.1, 0.3, 0.0)).as_float32()]
+        ts = BatchedTimeStepDFSPH(sc)
+    else:
+        sc = scenes.small_block(counts=(9, 8, 7), viscosity=True, velocity=(0.2, 0.0, -0.1)).as_float32()
+        ts = TimeStepDFSPH(sc)
+    try:
+        for _ in range(3):
+            ts.step()
+        ctx = ts.ctx
+        n, _ = ctx.num_particles()
+        names = ("position", "velocity", "density", "p / rho^2", "p_v / rho^2", "factor")
+        shape = {k: (n, 3) if k in ("position", "velocity") else (n,) for k in names}
+        pin = lambda shp, dt: torch.empty(shp, dtype=dt, pin_memory=True).numpy()
+        for dt, tdt in ((np.float32, torch.float32), (np.float64, torch.float64)):
+            staged = ctx.download_fields({k: np.zeros(shape[k], dt) for k in names})
+            direct = ctx.download_fields({k: pin(shape[k], tdt) for k in names})
+            for k in names:
+                np.testing.assert_array_equal(direct[k], staged[k], err_msg=k)
+        rng = np.random.default_rng(11)
+        v = rng.uniform(-1, 1, (n, 3)).astype(np.float32)
+        kap = rng.uniform(0, 1e-4, n).astype(np.float32)
+        vp, kp = pin((n, 3), torch.float32), pin((n,), torch.float32)
+        vp[:] = v
+        kp[:] = kap
+        ctx.upload_fields({"velocity": vp, "p / rho^2": kp})
+        np.testing.assert_array_equal(ctx.download("velocity", dtype=np.float32), v)
+        np.testing.assert_array_equal(ctx.download("p / rho^2", dtype=np.float32), kap)
+    finally:
+        ts.close()
