@@ -22,6 +22,12 @@ to this script, by particle id:
   500, the heavy one below) with their own Weiler2018 and XSPH coefficients; the fixture
   records the models (phase_counts, phase_density0, phase_viscosity, phase_viscosity_boundary,
   phase_xsph, phase_xsph_boundary).
+  The solver-parameter cases: caps_cfl_iter (iteration caps below what the solvers need and the
+  iteration-adapted CFL step size) and fixed_dt_nodiv (fixed step size, no divergence solve,
+  a pressure-iteration minimum, XSPH with its boundary term).
+  ref_run_cfl_iter.npz  25 steps of a compressed block with the iteration-adapted CFL step
+                        size from its initial state: iteration counts and step sizes per step,
+                        the final fields
   ref_kernel_table_delta.json  the same config-0 step with the reference's default
                         PrecomputedKernel<CubicKernel, 10000> against the analytic
                         kernel: max and mean relative difference per field
@@ -131,14 +137,76 @@ def phases_visc():
     return sc, dict(counts=(n0, sc.n - n0), **PHASES)
 
 
+def block12():
+    return scenes.small_block(counts=(12, 12, 12), box=(0.8, 0.8, 0.8), velocity=(0.3, 0.0, -0.2))
+
+
+def caps_cfl_iter():
+    """The viscous column with the solvers capped below what they need (4 pressure, 2 divergence
+    and 4 CG iterations) and the iteration-adapted CFL step size (cflMethod 2)."""
+    sc = viscous_column()
+    p = sc.params
+    p.maxIterations, p.maxIterationsV, p.viscoMaxIter, p.cflMethod = 4, 2, 4, 2
+    return sc
+
+
+def fixed_dt_nodiv():
+    """The 12^3 block at a fixed step size (cflMethod 0, 2 ms), without the divergence solver,
+    at least 5 pressure iterations, XSPH 0.05 with a boundary term of 0.1 and no viscosity."""
+    sc = block12()
+    p = sc.params
+    p.cflMethod, p.timeStepSize, p.enableDivergenceSolver, p.minIterations = 0, 0.002, False, 5
+    p.xsph, p.xsphBoundary = 0.05, 0.1
+    return sc
+
+
 def cases():
     return {
-        "block12": (scenes.small_block(counts=(12, 12, 12), box=(0.8, 0.8, 0.8), velocity=(0.3, 0.0, -0.2)), 30),
+        "block12": (block12(), 30),
         "column_visc": (viscous_column(), 70),
         "dambreak8k_step203": (scenes.dambreak_8k(), 202),
         "vmap_box": (vmap_box(), 40),
         "phases_visc": (phases_visc()[0], 30),
+        "caps_cfl_iter": (caps_cfl_iter(), 40),
+        "fixed_dt_nodiv": (fixed_dt_nodiv(), 30),
     }
+
+
+RUN_STEPS = 25
+
+
+def cfl_iter_block():
+    """A 12^3 block compressed to 0.84 of its spacing (30 % over the rest density) with the
+    iteration-adapted CFL step size (cflMethod 2): tens of pressure iterations in its first
+    steps shrink the step size (x 0.9 after more than 10), the expanding block then limits it by
+    the velocity CFL, and the few iterations after grow it (x 1.1 after fewer than 5)."""
+    sc = scenes.small_block(counts=(12, 12, 12), box=(1.0, 1.0, 1.0), corner=(0.2, 0.2, 0.2))
+    c = sc.x.mean(axis=0)
+    sc.x = c + 0.84 * (sc.x - c)
+    sc.params.cflMethod = 2
+    return sc
+
+
+def run_fixture():
+    """ref_run_cfl_iter.npz: RUN_STEPS reference steps of cfl_iter_block from its float32
+    initial state, each step's iteration counts and step sizes, and the final fields, so that a
+    run (the CFL adaptation reads the previous step's pressure iterations) can be followed."""
+    scene = cfl_iter_block().as_float32()
+    its, dts = [], []
+    with refsim.RefSim(scene) as r:
+        for _ in range(RUN_STEPS):
+            s = r.step()
+            its.append((s["iterations"], s["iterations_v"], s["visco_iterations"]))
+            dts.append((s["dt_old"], s["dt"]))
+        visc = scene.params.viscosityMethod == 6
+        out = {KEYS[f]: r.get(f) for f in OUT_FIELDS
+               if f != "advected density" and (visc or f != "velocity difference")}
+    np.savez_compressed(
+        os.path.join(HERE, "ref_run_cfl_iter.npz"), params=json.dumps(dataclasses.asdict(scene.params)),
+        x=scene.x.astype(np.float32), v=scene.v.astype(np.float32), xb=scene.xb.astype(np.float32),
+        box_min=scene.box_min, box_max=scene.box_max, iterations=np.array(its), dt=np.array(dts),
+        **{f"out_{k}": v for k, v in out.items()})
+    print("run cfl_iter", scene.n, "particles", RUN_STEPS, "steps; iterations", its[-1], "dt", dts[-1])
 
 
 def main():
@@ -164,6 +232,8 @@ def main():
             **{f"out_{k}": v for k, v in out.items()})
         print(name, scene.n, "particles, warm", warm, "iterations", out["iterations"], out["iterations_v"],
               out["visco_iterations"])
+    if not only or "run_cfl_iter" in only:
+        run_fixture()
     if only and "dambreak8k_step203" not in only:
         return
     # lookup-table kernel against the analytic kernel, on the config-0 step above

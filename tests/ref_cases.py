@@ -9,7 +9,7 @@ import numpy as np
 from splishsplash_gb300 import scenes
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ("block12", "column_visc", "dambreak8k_step203", "vmap_box", "phases_visc")
+CASES = ("block12", "column_visc", "dambreak8k_step203", "vmap_box", "phases_visc", "caps_cfl_iter", "fixed_dt_nodiv")
 
 
 def load_case(name):
@@ -24,6 +24,19 @@ def load_case(name):
                  kappa_v=g["kappa_v"].astype(np.float64), vdiff=g["vdiff"].astype(np.float64), dt=float(g["dt"]))
     out = {k[4:]: (g[k] if g[k].ndim else g[k].item()) for k in g.files if k.startswith("out_")}
     return scene, state, out
+
+
+def load_run(name):
+    """(scene, per-step iteration counts [steps, 3], per-step (dt used, dt next) [steps, 2], final
+    reference fields) of a run fixture (tests/golden/ref_run_<name>.npz): the reference's steps
+    from the scene's float32 initial state."""
+    g = np.load(os.path.join(GOLDEN, f"ref_run_{name}.npz"))
+    params = scenes.SPHParams(**{k: (tuple(v) if isinstance(v, list) else v)
+                                 for k, v in json.loads(str(g["params"])).items()})
+    scene = scenes.Scene(f"ref_run_{name}", g["x"].astype(np.float64), g["v"].astype(np.float64),
+                         g["xb"].astype(np.float64), params, np.asarray(g["box_min"]), np.asarray(g["box_max"]))
+    out = {k[4:]: g[k] for k in g.files if k.startswith("out_")}
+    return scene, g["iterations"], g["dt"], out
 
 
 def vmap_spec(name):

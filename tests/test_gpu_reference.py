@@ -21,6 +21,14 @@ boundary point, and in FP32 their rounding reaches the velocity through the CG a
 solves (the device measured 1.5e-4; FP64 mode 4e-13).
 The two-model column (phases_visc) runs the reference's two FluidModels as two phases of one
 context, each with its own Weiler2018 and XSPH coefficients, at the standard bars.
+The solver-parameter cases run the viscous column with its solvers capped below what they need
+and the iteration-adapted CFL step size (caps_cfl_iter), and a block at a fixed step size with no
+divergence solve, a pressure-iteration minimum and XSPH with its boundary term (fixed_dt_nodiv).
+The run fixture (ref_run_cfl_iter) is 25 reference steps of a compressed block with the
+iteration-adapted step size: the device takes the same iteration counts in every step and ends
+on the reference's fields (FP32: step sizes 1e-5, density 1e-4, velocity 5e-4 after the 25
+steps, where an FP32 restatement of the step on the CPU measured 2.4e-6, 4.3e-5 and 2.1e-4;
+FP64 device mode: 1e-12 and 1e-9).
 """
 import numpy as np
 import pytest
@@ -79,6 +87,27 @@ def test_fp32_step_matches_reference(case, use_graph):
             assert err[k] <= bar, (case, k, err[k])
     assert err["x"] <= 1e-6 * float(np.max(np.abs(ref["x"])))
     assert st["dt_next"] == pytest.approx(ref["dt_next"], rel=1e-5)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_run_with_adapted_step_size_follows_reference(precision):
+    scene, its, dts, ref = ref_cases.load_run("cfl_iter")
+    ts = TimeStepDFSPH(scene, precision=precision)
+    try:
+        for k in range(len(its)):
+            st = ts.step()
+            assert (st["iterations"], st["iterations_v"], st["visco_iterations"]) == tuple(its[k]), (precision, k)
+            assert st["dt_next"] == pytest.approx(dts[k][1], rel=1e-5 if precision == "fp32" else 1e-12), k
+        m = ts.getFluidModel()
+        got = dict(density=m.getFieldBuffer("density"), factor=m.getFieldBuffer("factor"),
+                   kappa=m.getFieldBuffer("p / rho^2"), kappa_v=m.getFieldBuffer("p_v / rho^2"),
+                   v=m.getFieldBuffer("velocity"), x=m.getFieldBuffer("position"))
+    finally:
+        ts.close()
+    bars = dict(density=1e-4, v=5e-4, x=1e-5) if precision == "fp32" else dict(density=1e-9, v=1e-9, x=1e-9)
+    err = ref_cases.field_errors(got, ref)
+    for k, bar in bars.items():
+        assert err[k] <= bar * (float(np.max(np.abs(ref["x"]))) if k == "x" else 1.0), (precision, k, err[k])
 
 
 @pytest.mark.parametrize("case", ref_cases.CASES)

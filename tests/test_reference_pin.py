@@ -85,6 +85,24 @@ def test_oracle_matches_reference_step(case):
     assert st["dt"] == pytest.approx(ref["dt_next"], rel=1e-12)
 
 
+def test_oracle_follows_reference_run_with_adapted_step_size():
+    """25 steps of a compressed block with the iteration-adapted CFL step size (cflMethod 2):
+    the oracle takes the reference's iteration counts and step sizes in every step (the step
+    size shrinks after steps of more than 10 pressure iterations and grows after fewer than 5)
+    and ends on its fields."""
+    scene, its, dts, ref = ref_cases.load_run("cfl_iter")
+    sim = oracle.OracleSim(scene, fp32_predicate=False)
+    for k in range(len(its)):
+        sim.step()
+        st = sim.stats()
+        assert (st["iterations"], st["iterations_v"], st["visco_iterations"]) == tuple(its[k]), k
+        assert st["dt"] == pytest.approx(dts[k][1], rel=1e-12), k
+    got = dict(density=sim.density, factor=sim.factor, kappa=sim.kappa, kappa_v=sim.kappa_v, v=sim.v, x=sim.x)
+    for k, e in ref_cases.field_errors(got, ref).items():
+        assert e <= ORACLE_TOL * (np.max(np.abs(ref["x"])) if k == "x" else 1.0), (k, e)
+    assert its[:, 0].max() > 10 and its[:, 0].min() < 5 and len({round(d, 9) for d in dts[:, 1]}) > 10
+
+
 def test_fixtures_exercise_the_solvers():
     its = {c: ref_cases.load_case(c)[2] for c in ref_cases.CASES}
     assert max(o["iterations"] for o in its.values()) >= 10            # pressure solve
