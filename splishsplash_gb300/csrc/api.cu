@@ -2514,18 +2514,27 @@ int sphgb_download_fields(sphgb_ctx *c, uint32_t count, const int *fields, void 
     // every field queued back to back, one wait: written straight to mapped host memory, or
     // scattered to particle-id order in the staging buffer and copied out
     auto emit = [&](auto P, auto B) -> int {
-        if (any_direct && c->n) launch_inverse_perm(P, B.id, c->inv_perm, c->stream);
+        if (any_direct && c->n) {   // the mapped fields, up to kFieldSetMax per launch
+            launch_inverse_perm(P, B.id, c->inv_perm, c->stream);
+            FieldSet F{};
+            for (uint32_t k = 0; k <= count; k++) {
+                if (F.n == kFieldSetMax || (k == count && F.n)) {
+                    launch_gather_fields(P, B, F, dtype, c->inv_perm, c->stream);
+                    CK(cudaGetLastError());
+                    F.n = 0;
+                }
+                if (k == count || !direct[k]) continue;
+                F.ptr[F.n] = direct[k];
+                F.field[F.n] = fields[k];
+                F.comps[F.n] = (uint32_t)field_components(fields[k]);
+                F.n++;
+            }
+        }
         for (uint32_t k = 0; k < count; k++) {
             const int field = fields[k];
             const bool bfield = field == SPHGB_FIELD_BOUNDARY_VOLUME || field == SPHGB_FIELD_BOUNDARY_POSITION;
             const size_t bytes = (size_t)(bfield ? c->nb : c->n) * field_components(field) * dtype_size(dtype);
-            if (bytes == 0) continue;
-            if (direct[k]) {
-                launch_gather_field(P, B, field, direct[k], dtype, c->inv_perm, (uint32_t)field_components(field),
-                                    c->stream);
-                CK(cudaGetLastError());
-                continue;
-            }
+            if (bytes == 0 || direct[k]) continue;
             char *st = static_cast<char *>(c->staging) + off[k];
             launch_scatter_field(P, B, field, st, dtype, c->stream);
             CK(cudaGetLastError());
@@ -2586,7 +2595,16 @@ int sphgb_upload_fields(sphgb_ctx *c, uint32_t count, const int *fields, const v
     }
     auto write = [&](auto P, auto B) {
         launch_inverse_perm(P, B.id, c->inv_perm, c->stream);
-        for (uint32_t k = 0; k < count; k++) launch_upload_field(P, B, fields[k], in[k], dtype, c->inv_perm, c->stream);
+        FieldSet F{};   // up to kFieldSetMax fields per launch, in the order given
+        for (uint32_t k = 0; k < count; k++) {
+            F.ptr[F.n] = const_cast<void *>(in[k]);
+            F.field[F.n] = fields[k];
+            F.comps[F.n] = (uint32_t)field_components(fields[k]);
+            if (++F.n == kFieldSetMax || k + 1 == count) {
+                launch_upload_fields(P, B, F, dtype, c->inv_perm, c->stream);
+                F.n = 0;
+            }
+        }
     };
     if (c->fp64) write(make_params<double>(c), make_bufs<double>(c, 0));
     else write(make_params<float>(c), make_bufs<float>(c, 0));

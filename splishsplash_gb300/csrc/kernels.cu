@@ -2730,67 +2730,47 @@ __global__ void k_scatter_field(DevParams<T> P, DevBufs<T> B, int field, void *o
     emit_field(P, B, field, out, odt, q.i, B.id[q.i], q.s);
 }
 
-// ... in particle-id order into host memory the device maps: thread t of a block takes particle
-// d0 + t from its slot inv[d], stages its values in shared memory, and the block writes its
-// particles' values out as one contiguous range, with 16-byte stores where that range is 16-byte
-// aligned (whole lines over the host link instead of strided 4-byte pieces)
-constexpr uint32_t kGatherMaxComps = 10;   // components of the widest field (network features)
+// ... in particle-id order into host memory the device maps, several fields per launch: thread t
+// of a block takes particle d0 + t from its slot inv[d] once; for each field it stages the value
+// in shared memory, and the block writes its particles' values out as one contiguous range, with
+// 16-byte stores where that range is 16-byte aligned (whole lines over the host link instead of
+// strided 4-byte pieces)
 template <class T>
-__global__ void __launch_bounds__(kBlock) k_gather_field(DevParams<T> P, DevBufs<T> B, int field, void *out, int odt,
-                                                         const uint32_t *__restrict__ inv, uint32_t comps)
+__global__ void __launch_bounds__(kBlock) k_gather_fields(DevParams<T> P, DevBufs<T> B, FieldSet F, int odt,
+                                                          const uint32_t *__restrict__ inv)
 {
-    __shared__ __align__(16) unsigned char buf[kBlock * kGatherMaxComps * 8];
+    __shared__ __align__(16) unsigned char buf[kBlock * kFieldSetMaxComps * 8];
     const uint32_t d0 = blockIdx.x * kBlock, d = d0 + threadIdx.x;
+    uint32_t k = 0u, sc = 0u;
     if (d < P.nreal) {
-        const uint32_t k = inv[d];
-        const uint32_t sc = P.nscenes > 1 ? __ldg(P.blk + k / kBlock).x : 0u;
-        emit_field(P, B, field, buf, odt, k, threadIdx.x, sc);
+        k = inv[d];
+        sc = P.nscenes > 1 ? __ldg(P.blk + k / kBlock).x : 0u;
     }
-    __syncthreads();
     const size_t es = odt == SPHGB_DTYPE_F64 ? 8 : 4;
     const uint32_t cnt = min((uint32_t)kBlock, P.nreal - d0);   // every launched block holds a particle
-    const size_t bytes = (size_t)cnt * comps * es;
-    unsigned char *dst = static_cast<unsigned char *>(out) + (size_t)d0 * comps * es;
-    size_t done = 0;
-    if ((reinterpret_cast<uintptr_t>(dst) & 15u) == 0) {
-        const size_t nv = bytes / 16;
-        for (size_t i = threadIdx.x; i < nv; i += kBlock)
-            reinterpret_cast<float4 *>(dst)[i] = reinterpret_cast<const float4 *>(buf)[i];
-        done = nv * 16;
-    }
-    for (size_t i = done / 4 + threadIdx.x; i < bytes / 4; i += kBlock)
-        reinterpret_cast<uint32_t *>(dst)[i] = reinterpret_cast<const uint32_t *>(buf)[i];
-}
-
-template <class T>
-__global__ void __launch_bounds__(kBlock) k_upload_field(DevParams<T> P, DevBufs<T> B, int field, const void *src,
-                                                         int idt, const uint32_t *__restrict__ inv, uint32_t comps)
-{
-    // the block's particles' values (one contiguous range of the particle-id ordered input, which
-    // may be host memory the device maps) read into shared memory with 16-byte loads where the
-    // range is 16-byte aligned; thread t then takes particle d0 + t's values at t * comps
-    __shared__ __align__(16) unsigned char buf[kBlock * 3 * 8];
-    const uint32_t d0 = blockIdx.x * kBlock;
-    {
-        const size_t es = idt == SPHGB_DTYPE_F64 ? 8 : 4;
-        const uint32_t cnt = min((uint32_t)kBlock, P.nreal - d0);   // every launched block holds a particle
-        const size_t bytes = (size_t)cnt * comps * es;
-        const unsigned char *s = static_cast<const unsigned char *>(src) + (size_t)d0 * comps * es;
+    for (uint32_t f = 0; f < F.n; f++) {
+        if (d < P.nreal) emit_field(P, B, F.field[f], buf, odt, k, threadIdx.x, sc);
+        __syncthreads();
+        const size_t bytes = (size_t)cnt * F.comps[f] * es;
+        unsigned char *dst = static_cast<unsigned char *>(F.ptr[f]) + (size_t)d0 * F.comps[f] * es;
         size_t done = 0;
-        if ((reinterpret_cast<uintptr_t>(s) & 15u) == 0) {
+        if ((reinterpret_cast<uintptr_t>(dst) & 15u) == 0) {
             const size_t nv = bytes / 16;
             for (size_t i = threadIdx.x; i < nv; i += kBlock)
-                reinterpret_cast<float4 *>(buf)[i] = reinterpret_cast<const float4 *>(s)[i];
+                reinterpret_cast<float4 *>(dst)[i] = reinterpret_cast<const float4 *>(buf)[i];
             done = nv * 16;
         }
         for (size_t i = done / 4 + threadIdx.x; i < bytes / 4; i += kBlock)
-            reinterpret_cast<uint32_t *>(buf)[i] = reinterpret_cast<const uint32_t *>(s)[i];
+            reinterpret_cast<uint32_t *>(dst)[i] = reinterpret_cast<const uint32_t *>(buf)[i];
+        __syncthreads();   // the next field reuses the staging buffer
     }
-    __syncthreads();
-    const void *in = buf;
-    const uint32_t d = threadIdx.x;   // index into the staged values; particle id d0 + d
-    if (d0 + d >= P.nreal) return;
-    const uint32_t k = inv[d0 + d];
+}
+
+// value d of an uploaded field (particle-id ordered input `in`) written to slot k
+template <class T>
+__device__ __forceinline__ void apply_field(const DevBufs<T> &B, int field, const void *in, int idt, uint32_t k,
+                                            uint32_t d)
+{
     auto vec = [&](v4_t<T> *arr, float4 *lo) {
         const double ax = get<T>(in, idt, 3 * (size_t)d), ay = get<T>(in, idt, 3 * (size_t)d + 1),
                      az = get<T>(in, idt, 3 * (size_t)d + 2);
@@ -2819,6 +2799,38 @@ __global__ void __launch_bounds__(kBlock) k_upload_field(DevParams<T> P, DevBufs
                                    (float)get<T>(in, idt, 3 * (size_t)d + 2), 0.f);
         break;
     default: break;
+    }
+}
+
+// Uploaded fields in particle-id order, several per launch.  For each field the block reads its
+// particles' values (one contiguous range of the input, which may be host memory the device
+// maps) into shared memory, with 16-byte loads where the range is 16-byte aligned; thread t then
+// writes particle d0 + t's values to its slot inv[d0 + t].
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_upload_fields(DevParams<T> P, DevBufs<T> B, FieldSet F, int idt,
+                                                          const uint32_t *__restrict__ inv)
+{
+    __shared__ __align__(16) unsigned char buf[kBlock * 3 * 8];   // uploadable fields: at most 3 components
+    const uint32_t d0 = blockIdx.x * kBlock;
+    const size_t es = idt == SPHGB_DTYPE_F64 ? 8 : 4;
+    const uint32_t cnt = min((uint32_t)kBlock, P.nreal - d0);   // every launched block holds a particle
+    const bool mine = d0 + threadIdx.x < P.nreal;
+    const uint32_t k = mine ? inv[d0 + threadIdx.x] : 0u;
+    for (uint32_t f = 0; f < F.n; f++) {
+        const size_t bytes = (size_t)cnt * F.comps[f] * es;
+        const unsigned char *src = static_cast<const unsigned char *>(F.ptr[f]) + (size_t)d0 * F.comps[f] * es;
+        size_t done = 0;
+        if ((reinterpret_cast<uintptr_t>(src) & 15u) == 0) {
+            const size_t nv = bytes / 16;
+            for (size_t i = threadIdx.x; i < nv; i += kBlock)
+                reinterpret_cast<float4 *>(buf)[i] = reinterpret_cast<const float4 *>(src)[i];
+            done = nv * 16;
+        }
+        for (size_t i = done / 4 + threadIdx.x; i < bytes / 4; i += kBlock)
+            reinterpret_cast<uint32_t *>(buf)[i] = reinterpret_cast<const uint32_t *>(src)[i];
+        __syncthreads();
+        if (mine) apply_field(B, F.field[f], buf, idt, k, threadIdx.x);
+        __syncthreads();   // the next field reuses the staging buffer
     }
 }
 
@@ -3100,17 +3112,15 @@ template <class T> void launch_scatter_field(const DevParams<T> &P, const DevBuf
         k_scatter_field<T><<<grid_for(P.np), kBlock, 0, s>>>(P, B, field, out, odt);
     }
 }
-template <class T> void launch_gather_field(const DevParams<T> &P, const DevBufs<T> &B, int field, void *out, int odt,
-                                            const uint32_t *inv, uint32_t comps, cudaStream_t s)
+template <class T> void launch_gather_fields(const DevParams<T> &P, const DevBufs<T> &B, const FieldSet &F, int odt,
+                                             const uint32_t *inv, cudaStream_t s)
 {
-    if (P.nreal && comps <= kGatherMaxComps)
-        k_gather_field<T><<<grid_for(P.nreal), kBlock, 0, s>>>(P, B, field, out, odt, inv, comps);
+    if (P.nreal && F.n) k_gather_fields<T><<<grid_for(P.nreal), kBlock, 0, s>>>(P, B, F, odt, inv);
 }
-template <class T> void launch_upload_field(const DevParams<T> &P, const DevBufs<T> &B, int field, const void *in,
-                                            int idt, const uint32_t *inv, cudaStream_t s)
+template <class T> void launch_upload_fields(const DevParams<T> &P, const DevBufs<T> &B, const FieldSet &F, int idt,
+                                             const uint32_t *inv, cudaStream_t s)
 {
-    const uint32_t comps = (field == SPHGB_FIELD_PRESSURE_RHO2 || field == SPHGB_FIELD_PRESSURE_RHO2_V) ? 1u : 3u;
-    if (P.nreal) k_upload_field<T><<<grid_for(P.nreal), kBlock, 0, s>>>(P, B, field, in, idt, inv, comps);
+    if (P.nreal && F.n) k_upload_fields<T><<<grid_for(P.nreal), kBlock, 0, s>>>(P, B, F, idt, inv);
 }
 template <class T> void launch_init_state(const DevParams<T> &P, const DevBufs<T> &B, const double *x, const double *v,
                                           const uint32_t *id, cudaStream_t s)
@@ -3176,10 +3186,10 @@ void launch_lists_to_ids(const uint32_t *list, const uint32_t *cnt, uint32_t cap
                                               const uint32_t *, uint32_t *, cudaStream_t);                          \
     template void launch_boundary_volume<T>(const DevParams<T> &, const DevBufs<T> &, cudaStream_t);                \
     template void launch_scatter_field<T>(const DevParams<T> &, const DevBufs<T> &, int, void *, int, cudaStream_t); \
-    template void launch_gather_field<T>(const DevParams<T> &, const DevBufs<T> &, int, void *, int, const uint32_t *, \
-                                         uint32_t, cudaStream_t);                                                   \
-    template void launch_upload_field<T>(const DevParams<T> &, const DevBufs<T> &, int, const void *, int,          \
-                                         const uint32_t *, cudaStream_t);                                           \
+    template void launch_gather_fields<T>(const DevParams<T> &, const DevBufs<T> &, const FieldSet &, int,          \
+                                          const uint32_t *, cudaStream_t);                                          \
+    template void launch_upload_fields<T>(const DevParams<T> &, const DevBufs<T> &, const FieldSet &, int,          \
+                                          const uint32_t *, cudaStream_t);                                          \
     template void launch_init_state<T>(const DevParams<T> &, const DevBufs<T> &, const double *, const double *,    \
                                        const uint32_t *, cudaStream_t);                                             \
     template void launch_inverse_perm<T>(const DevParams<T> &, const uint32_t *, uint32_t *, cudaStream_t);

@@ -307,12 +307,22 @@ template <class T> void launch_boundary_gather(const DevParams<T> &P, const DevB
                                                cudaStream_t s);
 template <class T> void launch_scatter_field(const DevParams<T> &P, const DevBufs<T> &B, int field, void *out,
                                              int out_dtype, cudaStream_t s);
-// a fluid field (comps components) in particle-id order from slot inv[id], written as contiguous
-// ranges (host memory the device maps)
-template <class T> void launch_gather_field(const DevParams<T> &P, const DevBufs<T> &B, int field, void *out, int odt,
-                                            const uint32_t *inv, uint32_t comps, cudaStream_t s);
-template <class T> void launch_upload_field(const DevParams<T> &P, const DevBufs<T> &B, int field, const void *in,
-                                            int in_dtype, const uint32_t *inv, cudaStream_t s);
+// Fluid fields moved in particle-id order by one launch: field[k] (comps[k] components) to or
+// from ptr[k], a buffer in host memory the device maps or in device memory
+constexpr uint32_t kFieldSetMax = 8;
+constexpr uint32_t kFieldSetMaxComps = 10;   // components of the widest field (network features)
+struct FieldSet {
+    void *ptr[kFieldSetMax];
+    int field[kFieldSetMax];
+    uint32_t comps[kFieldSetMax];
+    uint32_t n;
+};
+// the fields of F from slot inv[id], each written as contiguous ranges
+template <class T> void launch_gather_fields(const DevParams<T> &P, const DevBufs<T> &B, const FieldSet &F, int odt,
+                                             const uint32_t *inv, cudaStream_t s);
+// the fields of F (sources in particle-id order) written to slot inv[id], in the order of F
+template <class T> void launch_upload_fields(const DevParams<T> &P, const DevBufs<T> &B, const FieldSet &F, int in_dtype,
+                                             const uint32_t *inv, cudaStream_t s);
 template <class T> void launch_init_state(const DevParams<T> &P, const DevBufs<T> &B, const double *x,
                                           const double *v, const uint32_t *id, cudaStream_t s);
 template <class T> void launch_inverse_perm(const DevParams<T> &P, const uint32_t *id, uint32_t *inv, cudaStream_t s);
