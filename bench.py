@@ -550,9 +550,12 @@ def main():
     inputs = {"position": hx, "velocity": hv}
     outputs = {"position": hx, "velocity": hv, "density": hrho, "p / rho^2": hk, "p_v / rho^2": hkv}
     for _ in range(e2e_steps):
+        # as the reference-side plugin steps: the step is queued, the download waits for it and
+        # its fields, then the step's statistics are read on the host
         te.ctx.upload_fields(inputs)
-        te.step()
+        te.ctx.step(wait=False)
         te.ctx.download_fields(outputs)
+        te.ctx.sync()
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     te.close()

@@ -245,7 +245,11 @@ void TimeStepDFSPH_GB300::step()
 		setParams();
 	check(m_ctx, sphgb_set_time_step(m_ctx, tm->getTimeStepSize()));
 	check(m_ctx, sphgb_set_time(m_ctx, tm->getTime()));
-	check(m_ctx, sphgb_step(m_ctx, &m_stats));
+	// the step is queued without a wait; the download waits for it and its fields in one go,
+	// after which the step's statistics are on the host
+	check(m_ctx, sphgb_step(m_ctx, nullptr));
+	download();   // the host vectors stay the system of record
+	check(m_ctx, sphgb_sync(m_ctx, &m_stats));
 	m_iterations = m_stats.iterations;
 	m_iterationsV = m_stats.iterations_v;
 	INCREASE_COUNTER("DFSPH - iterations", static_cast<Real>(m_iterations));
@@ -253,7 +257,6 @@ void TimeStepDFSPH_GB300::step()
 	for (unsigned int k = 0; k < sim->numberOfFluidModels(); k++)
 		if (Viscosity_Weiler2018_GB300 *w = dynamic_cast<Viscosity_Weiler2018_GB300 *>(sim->getFluidModel(k)->getViscosityBase()))
 			w->setIterations(m_stats.visco_iterations);
-	download();   // the host vectors stay the system of record
 	// Simulation::updateTimeStepSize ran on the device (Simulation.cpp:395-493)
 	tm->setTimeStepSize(static_cast<Real>(m_stats.dt_next));
 	tm->setTime(static_cast<Real>(m_stats.time));

@@ -15,6 +15,7 @@ struct sphgb_ctx {
     std::vector<double> x, v, a, density, factor, density_adv, kappa, kappa_v, pressure_accel, vdiff, xb, Vb;
     unsigned n = 0, nb = 0;
     double dt = 0.001, time = 0.0;
+    sphgb_stats last{};   // statistics of the last step (sphgb_sync)
     std::string err;
 };
 
@@ -204,18 +205,26 @@ int sphgb_step(sphgb_ctx *ctx, sphgb_stats *stats)
     if (orc_step(&s, &p) != 0) return fail(ctx, SPHGB_ERR_STATE, "oracle step failed");
     ctx->dt = s.dt;
     ctx->time = s.time;
-    if (stats) {
-        std::memset(stats, 0, sizeof(*stats));
-        stats->iterations = s.iterations;
-        stats->iterations_v = s.iterations_v;
-        stats->visco_iterations = s.visco_iterations;
-        stats->avg_density_err = s.avg_density_err;
-        stats->avg_density_err_v = s.avg_density_err_v;
-        stats->visco_error = s.visco_error;
-        stats->dt_used = s.dt_old;
-        stats->dt_next = s.dt;
-        stats->time = s.time;
-    }
+    sphgb_stats &st = ctx->last;
+    std::memset(&st, 0, sizeof(st));
+    st.iterations = s.iterations;
+    st.iterations_v = s.iterations_v;
+    st.visco_iterations = s.visco_iterations;
+    st.avg_density_err = s.avg_density_err;
+    st.avg_density_err_v = s.avg_density_err_v;
+    st.visco_error = s.visco_error;
+    st.dt_used = s.dt_old;
+    st.dt_next = s.dt;
+    st.time = s.time;
+    if (stats) *stats = st;
+    return SPHGB_OK;
+}
+
+// the step ran to completion inside sphgb_step: its statistics
+int sphgb_sync(sphgb_ctx *ctx, sphgb_stats *stats)
+{
+    if (!ctx) return SPHGB_ERR_ARGUMENT;
+    if (stats) *stats = ctx->last;
     return SPHGB_OK;
 }
 
