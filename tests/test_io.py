@@ -295,19 +295,24 @@ def test_transfers_through_mapped_host_memory_match_staged_ones(batch):
         names = ("position", "velocity", "density", "p / rho^2", "p_v / rho^2", "factor")
         shape = {k: (n, 3) if k in ("position", "velocity") else (n,) for k in names}
         pin = lambda shp, dt: torch.empty(shp, dtype=dt, pin_memory=True).numpy()
+        # a buffer one element past a 16-byte boundary takes the 4-byte path of the same kernels
+        off = lambda shp, dt: pin(int(np.prod(shp)) + 1, dt)[1:].reshape(shp)
         for dt, tdt in ((np.float32, torch.float32), (np.float64, torch.float64)):
             staged = ctx.download_fields({k: np.zeros(shape[k], dt) for k in names})
-            direct = ctx.download_fields({k: pin(shape[k], tdt) for k in names})
-            for k in names:
-                np.testing.assert_array_equal(direct[k], staged[k], err_msg=k)
+            for make in (pin, off):
+                direct = ctx.download_fields({k: make(shape[k], tdt) for k in names})
+                for k in names:
+                    np.testing.assert_array_equal(direct[k], staged[k], err_msg=k)
         rng = np.random.default_rng(11)
         v = rng.uniform(-1, 1, (n, 3)).astype(np.float32)
         kap = rng.uniform(0, 1e-4, n).astype(np.float32)
-        vp, kp = pin((n, 3), torch.float32), pin((n,), torch.float32)
-        vp[:] = v
-        kp[:] = kap
-        ctx.upload_fields({"velocity": vp, "p / rho^2": kp})
-        np.testing.assert_array_equal(ctx.download("velocity", dtype=np.float32), v)
-        np.testing.assert_array_equal(ctx.download("p / rho^2", dtype=np.float32), kap)
+        for make in (pin, off):
+            vp, kp = make((n, 3), torch.float32), make((n,), torch.float32)
+            vp[:] = v
+            kp[:] = kap
+            ctx.upload_fields({"velocity": vp, "p / rho^2": kp})
+            np.testing.assert_array_equal(ctx.download("velocity", dtype=np.float32), v)
+            np.testing.assert_array_equal(ctx.download("p / rho^2", dtype=np.float32), kap)
+            v, kap = v[::-1].copy(), kap[::-1].copy()
     finally:
         ts.close()
