@@ -181,8 +181,10 @@ int sphgb_upload_field(sphgb_ctx *ctx, int field, const void *src, int dtype);
  * fields[k], all in one dtype; the transfers are queued back to back on the context's stream
  * and the call waits once.  Uploads compute the slot of each particle id once for all fields.
  * A fluid field whose buffer is page-locked host memory mapped into the device's address space
- * (cudaHostAlloc, cudaHostRegister) is read or written by the device itself, in particle-id
- * order, with no staging copy; other buffers are staged in device memory and copied. */
+ * (cudaHostAlloc, cudaHostRegister) or memory of the context's device is read or written by the
+ * device itself, in particle-id order, with no staging copy; other buffers are staged in device
+ * memory and copied.  The transfers run on the context's stream: a device buffer written on
+ * another stream must be complete before the call. */
 int sphgb_download_fields(sphgb_ctx *ctx, uint32_t count, const int *fields, void *const *dsts, int dtype);
 int sphgb_upload_fields(sphgb_ctx *ctx, uint32_t count, const int *fields, const void *const *srcs, int dtype);
 

@@ -2466,17 +2466,20 @@ int sphgb_num_particles(const sphgb_ctx *c, uint32_t *n, uint32_t *nb)
     return SPHGB_OK;
 }
 
-// The device's address of page-locked host memory mapped into its address space (cudaHostAlloc,
-// cudaHostRegister on a unified address space), else null: such a buffer is read or written by
-// the transfer kernels themselves, with no staging copy.
-void *mapped_host(const void *p)
+// The device's address of a buffer its kernels can read and write: page-locked host memory
+// mapped into its address space (cudaHostAlloc, cudaHostRegister on a unified address space) or
+// memory of the context's own device, else null.  Such a buffer is read or written by the
+// transfer kernels themselves, with no staging copy.
+void *device_addressable(const void *p, int device)
 {
     cudaPointerAttributes a{};
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
         return nullptr;
     }
-    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+    if (a.type == cudaMemoryTypeHost) return a.devicePointer;
+    if (a.type == cudaMemoryTypeDevice && a.device == device) return a.devicePointer;
+    return nullptr;
 }
 
 int sphgb_download_fields(sphgb_ctx *c, uint32_t count, const int *fields, void *const *dsts, int dtype)
@@ -2485,8 +2488,8 @@ int sphgb_download_fields(sphgb_ctx *c, uint32_t count, const int *fields, void 
     if (dtype < SPHGB_DTYPE_F32 || dtype > SPHGB_DTYPE_U32) return fail(c, SPHGB_ERR_ARGUMENT, "unknown dtype");
     if (!c->have_fluid) return fail(c, SPHGB_ERR_STATE, "no fluid uploaded");
     cudaSetDevice(c->cfg.device);
-    // checks; fluid fields into mapped host memory are written in particle-id order by the device,
-    // the others get a place in the staging buffer
+    // checks; fluid fields into mapped host memory or device memory are written in particle-id
+    // order by the device, the others get a place in the staging buffer
     std::vector<size_t> off(count + 1, 0);
     std::vector<void *> direct(count, nullptr);
     bool bfields = false, any_direct = false;
@@ -2497,7 +2500,7 @@ int sphgb_download_fields(sphgb_ctx *c, uint32_t count, const int *fields, void 
         if (field == SPHGB_FIELD_FEATURES && !c->mlp_x) return fail(c, SPHGB_ERR_STATE, "features are not computed");
         const bool bfield = field == SPHGB_FIELD_BOUNDARY_VOLUME || field == SPHGB_FIELD_BOUNDARY_POSITION;
         bfields = bfields || bfield;
-        if (!bfield) direct[k] = mapped_host(dsts[k]);
+        if (!bfield) direct[k] = device_addressable(dsts[k], c->cfg.device);
         any_direct = any_direct || direct[k];
         const size_t m = bfield ? c->nb : c->n;
         off[k + 1] = off[k] + (direct[k] ? 0 : ((m * field_components(field) * dtype_size(dtype) + 255) & ~(size_t)255));
@@ -2511,8 +2514,8 @@ int sphgb_download_fields(sphgb_ctx *c, uint32_t count, const int *fields, void 
         int rc = ensure_staging(c, off[count]);
         if (rc) return rc;
     }
-    // every field queued back to back, one wait: written straight to mapped host memory, or
-    // scattered to particle-id order in the staging buffer and copied out
+    // every field queued back to back, one wait: written straight to mapped host or device
+    // memory, or scattered to particle-id order in the staging buffer and copied out
     auto emit = [&](auto P, auto B) -> int {
         if (any_direct && c->n) {   // the mapped fields, up to kFieldSetMax per launch
             launch_inverse_perm(P, B.id, c->inv_perm, c->stream);
@@ -2571,11 +2574,12 @@ int sphgb_upload_fields(sphgb_ctx *c, uint32_t count, const int *fields, const v
     cudaSetDevice(c->cfg.device);
     sphgb_stats st;
     if (c->step_pending) fill_stats(c, &st);
-    // fields in mapped host memory are read by the device directly, the others staged
+    // fields in mapped host memory or device memory are read by the device directly, the others
+    // staged
     std::vector<size_t> off(count + 1, 0);
     std::vector<const void *> in(count, nullptr);
     for (uint32_t k = 0; k < count; k++) {
-        in[k] = mapped_host(srcs[k]);
+        in[k] = device_addressable(srcs[k], c->cfg.device);
         off[k + 1] = off[k] + (in[k] ? 0 : (((size_t)c->n * field_components(fields[k]) * dtype_size(dtype) + 255) &
                                             ~(size_t)255));
     }

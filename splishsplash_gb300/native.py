@@ -338,6 +338,21 @@ class Mlp:
         return losses
 
 
+def _is_tensor(a) -> bool:
+    return hasattr(a, "data_ptr") and hasattr(a, "is_contiguous") and hasattr(a, "numel")
+
+
+def _buffer(a):
+    """(address, elements, numpy dtype, C-contiguous) of a numpy array or a torch tensor (host or
+    device memory)"""
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data, a.size, a.dtype, bool(a.flags["C_CONTIGUOUS"])
+    if _is_tensor(a):
+        dt = {"torch.float32": np.dtype(np.float32), "torch.float64": np.dtype(np.float64)}.get(str(a.dtype))
+        return a.data_ptr(), a.numel(), dt, bool(a.is_contiguous())
+    raise TypeError(f"expected a numpy array or a torch tensor, got {type(a).__name__}")
+
+
 class Context:
     """One device-resident fluid model + static boundary (one sphgb_ctx)."""
 
@@ -470,32 +485,44 @@ class Context:
 
     def download_fields(self, outs: dict) -> dict:
         """Several fields in one call: {name: out} with C-contiguous float32 (or all float64)
-        targets of n x components elements (e.g. pinned buffers), filled in place."""
+        targets of n x components elements, filled in place: numpy arrays, or torch tensors on
+        the host (pinned ones are written by the device directly) or on the context's device."""
         names = list(outs)
-        arrs = [outs[k] for k in names]
-        dtypes = {a.dtype for a in arrs}
+        bufs = [_buffer(outs[k]) for k in names]
+        dtypes = {b[2] for b in bufs}
         if len(dtypes) != 1 or next(iter(dtypes)) not in (np.dtype(np.float32), np.dtype(np.float64)):
             raise ValueError("download_fields targets must all be float32 or all float64")
         n, _ = self.num_particles()
-        for k, a in zip(names, arrs):
-            if not a.flags["C_CONTIGUOUS"] or a.size != n * FIELDS[k][1]:
+        for k, b in zip(names, bufs):
+            if not b[3] or b[1] != n * FIELDS[k][1]:
                 raise ValueError(f"download target {k!r} must be C-contiguous with n x components elements")
         fids = np.array([FIELDS[k][0] for k in names], np.int32)
-        ptrs = (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
-        dt = DTYPE_F32 if arrs[0].dtype == np.float32 else DTYPE_F64
-        self._check(self.L.sphgb_download_fields(self.h, len(arrs), _p(fids), ptrs, dt))
+        ptrs = (ctypes.c_void_p * len(bufs))(*[b[0] for b in bufs])
+        dt = DTYPE_F32 if bufs[0][2] == np.float32 else DTYPE_F64
+        self._check(self.L.sphgb_download_fields(self.h, len(bufs), _p(fids), ptrs, dt))
         return outs
 
     def upload_fields(self, values: dict):
-        """Several fields in one call: {name: particle-id ordered values}, all float32 or all float64."""
+        """Several fields in one call: {name: particle-id ordered values}, all float32 or all float64:
+        numpy arrays (others are converted), or C-contiguous torch tensors on the host or on the
+        context's device."""
         names = list(values)
-        arrs = [np.asarray(values[k]) for k in names]
-        f32 = all(a.dtype == np.float32 and a.flags["C_CONTIGUOUS"] for a in arrs)
-        if not f32:
-            arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in arrs]
+        vals = [values[k] if _is_tensor(values[k]) else np.asarray(values[k]) for k in names]
+        bufs = [_buffer(v) for v in vals]
+        f32 = all(b[2] == np.float32 and b[3] for b in bufs)
+        if not f32 and any(_is_tensor(v) for v in vals):
+            if not all(b[2] == np.float64 and b[3] for b in bufs):
+                raise ValueError("upload_fields tensors must be C-contiguous and all float32 or all float64")
+        elif not f32:
+            vals = [np.ascontiguousarray(v, dtype=np.float64) for v in vals]
+            bufs = [_buffer(v) for v in vals]
+        n, _ = self.num_particles()
+        for k, b in zip(names, bufs):
+            if b[1] != n * FIELDS[k][1]:
+                raise ValueError(f"upload source {k!r} must hold n x components elements")
         fids = np.array([FIELDS[k][0] for k in names], np.int32)
-        ptrs = (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
-        self._check(self.L.sphgb_upload_fields(self.h, len(arrs), _p(fids), ptrs, DTYPE_F32 if f32 else DTYPE_F64))
+        ptrs = (ctypes.c_void_p * len(bufs))(*[b[0] for b in bufs])
+        self._check(self.L.sphgb_upload_fields(self.h, len(bufs), _p(fids), ptrs, DTYPE_F32 if f32 else DTYPE_F64))
 
     def set_warmstart_mlp(self, mlp):
         """Use a trained network for both warm starts (None: classic warm start only)."""

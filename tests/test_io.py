@@ -276,9 +276,10 @@ def test_batched_field_transfers_equal_single_ones(precision):
 
 @pytest.mark.parametrize("batch", [False, True])
 def test_transfers_through_mapped_host_memory_match_staged_ones(batch):
-    """Fields to and from page-locked host buffers are written and read by the device directly,
-    in particle-id order; the values equal those of the staged copies into pageable buffers, in
-    float32 and float64, for one scene and for a batch of scenes."""
+    """Fields to and from page-locked host buffers and the context's device memory are written
+    and read by the device directly, in particle-id order; the values equal those of the staged
+    copies into pageable buffers, in float32 and float64, for one scene and for a batch of
+    scenes, also for buffers off a 16-byte boundary."""
     torch = pytest.importorskip("torch")
     if batch:
         sc = [scenes.small_block(counts=(9, 8, 7), seed=1, velocity=(0.2, 0.0, -0.1)).as_float32(),
@@ -297,19 +298,22 @@ def test_transfers_through_mapped_host_memory_match_staged_ones(batch):
         pin = lambda shp, dt: torch.empty(shp, dtype=dt, pin_memory=True).numpy()
         # a buffer one element past a 16-byte boundary takes the 4-byte path of the same kernels
         off = lambda shp, dt: pin(int(np.prod(shp)) + 1, dt)[1:].reshape(shp)
+        dev = lambda shp, dt: torch.empty(shp, dtype=dt, device="cuda")
+        host = lambda a: a.cpu().numpy() if hasattr(a, "cpu") else a
         for dt, tdt in ((np.float32, torch.float32), (np.float64, torch.float64)):
             staged = ctx.download_fields({k: np.zeros(shape[k], dt) for k in names})
-            for make in (pin, off):
+            for make in (pin, off, dev):
                 direct = ctx.download_fields({k: make(shape[k], tdt) for k in names})
                 for k in names:
-                    np.testing.assert_array_equal(direct[k], staged[k], err_msg=k)
+                    np.testing.assert_array_equal(host(direct[k]), staged[k], err_msg=k)
         rng = np.random.default_rng(11)
         v = rng.uniform(-1, 1, (n, 3)).astype(np.float32)
         kap = rng.uniform(0, 1e-4, n).astype(np.float32)
-        for make in (pin, off):
+        for make in (pin, off, dev):
             vp, kp = make((n, 3), torch.float32), make((n,), torch.float32)
-            vp[:] = v
-            kp[:] = kap
+            vp[:] = torch.from_numpy(v) if make is dev else v
+            kp[:] = torch.from_numpy(kap) if make is dev else kap
+            torch.cuda.synchronize()   # device buffers are read on the context's stream
             ctx.upload_fields({"velocity": vp, "p / rho^2": kp})
             np.testing.assert_array_equal(ctx.download("velocity", dtype=np.float32), v)
             np.testing.assert_array_equal(ctx.download("p / rho^2", dtype=np.float32), kap)
