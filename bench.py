@@ -520,12 +520,13 @@ def main():
     value = replica_rate(world, scene.n, args.steps, t_max)
     lanes, trial_ms = ts.ctx.lanes_per_particle()
     staged, staged_frac, staged_trial_ms = ts.ctx.neighbor_staging()
+    block_threads, block_trial_ms = ts.ctx.solver_block_threads()
     if args.only_timed:
         if rank == 0:
             print(json.dumps({"metric": baseline_metric(), "value": value, "unit": UNIT, "steps": args.steps,
                               "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
                               "lanes_per_particle": lanes, "staged": staged, "staged_block_fraction": staged_frac,
-                              "note": "timed steps only"}), flush=True)
+                              "solver_block_threads": block_threads, "note": "timed steps only"}), flush=True)
         ts.close()
         return
 
@@ -625,7 +626,10 @@ def main():
             "config": {**workload_config(scene), "lanes_per_particle": lanes,
                        "lanes_autotune_trial_ms": dict(zip(("1", "2", "4"), trial_ms)) if args.lanes == 0 else None,
                        "staged_solver_passes": staged, "staged_block_fraction": round(staged_frac, 4),
-                       "staged_autotune_trial_ms": staged_trial_ms or None},
+                       "staged_autotune_trial_ms": staged_trial_ms or None,
+                       "solver_block_threads": block_threads,
+                       "block_threads_autotune_trial_ms": dict(zip(("128", "256", "512"), block_trial_ms))
+                       if args.lanes == 0 else None},
             "e2e": e2e, "gpu_launches": launches,
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
             "wall_ms_per_step": 1e3 * wall / args.steps,

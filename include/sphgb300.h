@@ -346,6 +346,17 @@ int sphgb_set_lanes_per_particle(sphgb_ctx *ctx, uint32_t lanes);
 /* the lanes in use and the autotuner's trial step times in ms for 1, 2, 4 lanes (zeros when fixed) */
 int sphgb_get_lanes_per_particle(const sphgb_ctx *ctx, uint32_t *lanes, float trial_ms[3]);
 
+/* Threads per block of the two solver passes (pressure acceleration, Jacobi update) when they run
+ * one lane per particle, unstaged: 128, 256 or 512 (512 for one scene only; a batch's blocks
+ * never span two scenes' 256-slot tiles).  The resident threads per SM are the same at every
+ * size.  0 (default): the autotuner times 128 and 512 beside 256 on the first step after an
+ * upload.  Results do not depend on it but for the order of the FP64 error sums.  No reference
+ * counterpart. */
+int sphgb_set_solver_block_threads(sphgb_ctx *ctx, uint32_t threads);
+/* the threads per block in use and the autotuner's trial step times in ms for 128, 256, 512 (zeros
+ * where not timed) */
+int sphgb_get_solver_block_threads(const sphgb_ctx *ctx, uint32_t *threads, float trial_ms[3]);
+
 /* Neighbourhood staging of the two solver passes (FP32 contexts, one lane per particle): every
  * block of 256 particles copies the records of the cells around its particles into shared
  * memory once per pass and walks 16-bit local lists written by the list build in the order of

@@ -39,15 +39,18 @@ struct SlotInfo {
     bool act;              // slot i holds a particle
 };
 
-template <int LPP = 1, class T> __device__ __forceinline__ SlotInfo slot_info(const DevParams<T> &P)
+// NT: threads per block (kBlock except in the two solver passes, which may run 128 or 512); a
+// block of 512 covers two scene tiles and runs for one scene only.
+template <int LPP = 1, int NT = kBlock, class T> __device__ __forceinline__ SlotInfo slot_info(const DevParams<T> &P)
 {
-    constexpr uint32_t SPB = kBlock / LPP;
+    constexpr uint32_t SPB = NT / LPP;                            // slots per block
+    constexpr uint32_t PER = SPB <= kBlock ? kBlock / SPB : 1u;   // blocks per scene-table entry
     SlotInfo q;
     q.b = blockIdx.x;
     q.i = q.b * SPB + threadIdx.x / LPP;
     q.l = threadIdx.x % LPP;
-    if (P.nscenes > 1) {
-        const uint4 b = __ldg(P.blk + q.b / LPP);
+    if (SPB <= kBlock && P.nscenes > 1) {
+        const uint4 b = __ldg(P.blk + q.b / PER);
         q.s = b.x;
         q.begin = b.y;
         q.end = b.z;
@@ -61,18 +64,19 @@ template <int LPP = 1, class T> __device__ __forceinline__ SlotInfo slot_info(co
 }
 
 // reduction slot of the scene of this block
-template <int LPP = 1, class T>
+template <int LPP = 1, int NT = kBlock, class T>
 __device__ __forceinline__ ReduceSlot scene_reduce(const DevParams<T> &P, const DevBufs<T> &B, const SlotInfo &q)
 {
-    constexpr uint32_t SPB = kBlock / LPP;
+    constexpr uint32_t SPB = NT / LPP;
+    constexpr uint32_t PER = SPB <= kBlock ? kBlock / SPB : 1u;
     ReduceSlot r;
     r.partials = B.partials;
     r.counter = B.counters + q.s;
-    if (P.nscenes > 1) {
+    if (SPB <= kBlock && P.nscenes > 1) {
         // every block of the scene's padded slot range [begin, begin + kBlock * ceil(n / kBlock))
         // takes part, also those that hold no particle
         r.first = q.begin / SPB;
-        r.count = (q.end - q.begin + kBlock - 1) / kBlock * LPP;
+        r.count = (q.end - q.begin + kBlock - 1) / kBlock * PER;
     } else {
         r.first = 0;
         r.count = gridDim.x;
@@ -1055,19 +1059,21 @@ __device__ __forceinline__ F8 ld_f8(const float4 *p)
 
 // Pressure accelerations of the running solver.  FP32: the acceleration half of the (x_i, a_i)
 // record that the Jacobi pass gathers with one 256-bit load per neighbour.
-template <class T, int LPP, bool MP = false>
-__global__ void __launch_bounds__(kBlock, kPressureMinBlocks<T, LPP>) k_pressure_accel(DevParams<T> P, DevBufs<T> B,
-                                                                                      unsigned limit,
-                                                            cudaGraphConditionalHandle h, int use_handle, int phase)
+// NT: threads per block (the same resident threads per SM at every size); the staged variant runs
+// with kBlock only
+template <class T, int LPP, bool MP = false, int NT = kBlock>
+__global__ void __launch_bounds__(NT, kPressureMinBlocks<T, LPP> * kBlock / NT)
+    k_pressure_accel(DevParams<T> P, DevBufs<T> B, unsigned limit, cudaGraphConditionalHandle h, int use_handle,
+                     int phase)
 {
     count_launch(&B.gsc->launches);
     if (phase <= 0) loop_guard(B.gsc, limit, h, use_handle);   // once per loop body
-    SlotInfo q = slot_info<LPP>(P);
+    SlotInfo q = slot_info<LPP, NT>(P);
     if (!scene_live(P, B.sc + q.s)) return;   // block uniform
     // fluid phases: this launch updates the particles of one phase; the others keep their last a
     if (phase >= 0 && q.act && B.ph[q.i] != (uint32_t)phase) q.act = false;
     V3<T> a;
-    if constexpr (LPP == 1 && sizeof(T) == 4) {
+    if constexpr (LPP == 1 && sizeof(T) == 4 && NT == kBlock) {
         extern __shared__ float4 stage_f4[];   // kStageCap records when staged
         if (P.staged && stage_in(B, q.b, kStageCap, [&](uint32_t j) { return ldv(B.xk, j); },
                                  [&](uint32_t m, const float4 &r) { stage_f4[m] = r; }))
@@ -1178,13 +1184,12 @@ __device__ __forceinline__ void solver_decide(const DevParams<T> &P, StepScalars
 // measured 0.6 % faster per step on the 1M dam break than the unconstrained 44 registers (5 blocks)
 template <class T, int LPP> constexpr int kJacobiMinBlocks = (sizeof(T) == 4 && LPP == 1) ? 6 : 1;
 
-template <class T, bool DIV, int LPP>
-__global__ void __launch_bounds__(kBlock, kJacobiMinBlocks<T, LPP>) k_jacobi(DevParams<T> P, DevBufs<T> B,
-                                                                           cudaGraphConditionalHandle handle,
-                                                                           int use_handle, int phase)
+template <class T, bool DIV, int LPP, int NT = kBlock>
+__global__ void __launch_bounds__(NT, kJacobiMinBlocks<T, LPP> * kBlock / NT)
+    k_jacobi(DevParams<T> P, DevBufs<T> B, cudaGraphConditionalHandle handle, int use_handle, int phase)
 {
     count_launch(&B.gsc->launches);
-    SlotInfo q = slot_info<LPP>(P);
+    SlotInfo q = slot_info<LPP, NT>(P);
     // fluid phases: this launch updates the particles of one phase (TimeStepDFSPH.cpp:322-339)
     if (phase >= 0 && q.act && B.ph[q.i] != (uint32_t)phase) q.act = false;
     StepScalars *const sc = B.sc + q.s;
@@ -1194,7 +1199,7 @@ __global__ void __launch_bounds__(kBlock, kJacobiMinBlocks<T, LPP>) k_jacobi(Dev
     double err = 0.0;
     {
         T apj;
-        if constexpr (LPP == 1 && sizeof(T) == 4) {
+        if constexpr (LPP == 1 && sizeof(T) == 4 && NT == kBlock) {
             extern __shared__ float2 stage_f2[];   // 3 x kStageCapJacobi when staged
             float2 *s0 = stage_f2, *s1 = stage_f2 + kStageCapJacobi, *s2 = stage_f2 + 2 * kStageCapJacobi;
             if (P.staged && stage_in(B, q.b, kStageCapJacobi, [&](uint32_t j) { return ld_f8(B.xa + 2 * (size_t)j); },
@@ -1242,7 +1247,7 @@ __global__ void __launch_bounds__(kBlock, kJacobiMinBlocks<T, LPP>) k_jacobi(Dev
     const DevBufs<T> &BB = B;
     const uint32_t n_s = q.end - q.begin;
     const int ph = phase;
-    grid_sum_finalize<1>(mine, scene_reduce<LPP>(P, B, q), [&](const DSum<1> &tot) {
+    grid_sum_finalize<1>(mine, scene_reduce<LPP, NT>(P, B, q), [&](const DSum<1> &tot) {
         if (ph < 0) {
             solver_decide<T, DIV>(PP, sc, n_s ? tot.v[0] / (double)n_s : 0.0);
             batch_decide(PP, BB, handle, use_handle, false);
@@ -2927,11 +2932,30 @@ template <class T> void launch_build(const DevParams<T> &P, const DevBufs<T> &B,
     if (P.np && P.staged) k_build<T, true><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
     else if (P.np) k_build<T, false><<<grid_for(P.np), kBlock, 0, s>>>(P, B);
 }
+// The two solver passes with one lane per particle, unstaged, may run 128 or 512 threads per
+// block (P.solver_nt, chosen by the autotuner; 512 for one scene only)
+#define NT_DISPATCH(P, CALL)                                                                                       \
+    do {                                                                                                           \
+        if ((P).solver_nt == 128u) { constexpr int NT = 128; CALL; }                                               \
+        else { constexpr int NT = 512; CALL; }                                                                     \
+    } while (0)
+template <class T> bool solver_nt_other(const DevParams<T> &P)
+{
+    return P.solver_nt != (uint32_t)kBlock && P.lpp_log2 == 0 && !P.staged &&
+           (P.solver_nt == 128u || (P.solver_nt == 512u && P.nscenes == 1));
+}
+
 template <class T> void launch_pressure_accel(const DevParams<T> &P, const DevBufs<T> &B, bool div, int phase, cudaStream_t s,
                                               cudaGraphConditionalHandle h, bool use_handle)
 {
     const unsigned limit = (div ? P.max_iter_v : P.max_iter) + 1;
-    if (P.np)
+    if (P.np && solver_nt_other(P)) {
+        const int uh = use_handle ? 1 : 0;
+        if (P.nphase > 1)
+            NT_DISPATCH(P, (k_pressure_accel<T, 1, true, NT><<<(P.np + NT - 1) / NT, NT, 0, s>>>(P, B, limit, h, uh, phase)));
+        else
+            NT_DISPATCH(P, (k_pressure_accel<T, 1, false, NT><<<(P.np + NT - 1) / NT, NT, 0, s>>>(P, B, limit, h, uh, phase)));
+    } else if (P.np)
     {
         if (P.nphase > 1)   // fluid phases: the rest-density ratio in the pressure term
             LPP_DISPATCH(P, (k_pressure_accel<T, L, true><<<grid_lpp(P.np, L), kBlock, 0, s>>>(
@@ -2947,7 +2971,10 @@ void launch_jacobi(const DevParams<T> &P, const DevBufs<T> &B, bool div, int pha
 {
     if (!P.np) return;
     const int uh = use_handle ? 1 : 0;
-    if (div)
+    if (solver_nt_other(P)) {
+        if (div) NT_DISPATCH(P, (k_jacobi<T, true, 1, NT><<<(P.np + NT - 1) / NT, NT, 0, s>>>(P, B, h, uh, phase)));
+        else NT_DISPATCH(P, (k_jacobi<T, false, 1, NT><<<(P.np + NT - 1) / NT, NT, 0, s>>>(P, B, h, uh, phase)));
+    } else if (div)
         LPP_DISPATCH(P, (k_jacobi<T, true, L><<<grid_lpp(P.np, L), kBlock, stage_bytes(P, L, kStageBytesJacobi), s>>>(
                             P, B, h, uh, phase)));
     else

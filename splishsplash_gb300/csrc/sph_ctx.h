@@ -112,6 +112,8 @@ template <class T> struct DevParams {
                                   // step, with velocities (one scene)
     int staged;                   // FP32, one lane per particle: the solver passes read their block's
                                   // neighbourhood from shared memory (stage tables, local lists)
+    uint32_t solver_nt;           // threads per block of the two solver passes with one lane per particle,
+                                  // unstaged: 128, 256 or 512 (one scene)
 };
 
 // Neighbourhood staging of the solver passes.  For every block of kBlock slots the step's

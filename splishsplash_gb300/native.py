@@ -127,7 +127,8 @@ EXPORTS = [
     "sphgb_scene_stats", "sphgb_set_warmstart_gate", "sphgb_set_lanes_per_particle", "sphgb_get_lanes_per_particle",
     "sphgb_export_vtk", "sphgb_export_wait", "sphgb_export_bgeo", "sphgb_field_id", "sphgb_save_state", "sphgb_load_state",
     "sphgb_set_boundary_bodies", "sphgb_boundary_forces", "sphgb_clear_boundary_forces",
-    "sphgb_set_neighbor_staging", "sphgb_get_neighbor_staging",
+    "sphgb_set_neighbor_staging", "sphgb_get_neighbor_staging", "sphgb_set_solver_block_threads",
+    "sphgb_get_solver_block_threads",
     "sphgb_add_volume_map", "sphgb_add_volume_map_values", "sphgb_get_volume_map", "sphgb_clear_volume_maps",
     "sphgb_set_boundary_method", "sphgb_set_volume_map_motion", "sphgb_set_body_motion", "sphgb_set_fluid_phases",
     "sphgb_set_fluid_phase_viscosity", "sphgb_set_fluid_phase_xsph",
@@ -184,6 +185,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.sphgb_set_warmstart_gate.argtypes = [vp, u32, u32]
     L.sphgb_set_lanes_per_particle.argtypes = [vp, u32]
     L.sphgb_get_lanes_per_particle.argtypes = [vp, ctypes.POINTER(u32), vp]
+    L.sphgb_set_solver_block_threads.argtypes = [vp, u32]
+    L.sphgb_get_solver_block_threads.argtypes = [vp, ctypes.POINTER(u32), vp]
     L.sphgb_export_vtk.argtypes = [vp, ctypes.c_char_p, vp, u32, i32]
     L.sphgb_export_wait.argtypes = [vp]
     L.sphgb_export_bgeo.argtypes = [vp, ctypes.c_char_p, vp, u32, i32, i32]
@@ -542,6 +545,17 @@ class Context:
         k = ctypes.c_uint32()
         t = np.zeros(3, np.float32)
         self._check(self.L.sphgb_get_lanes_per_particle(self.h, ctypes.byref(k), _p(t)))
+        return int(k.value), [float(v) for v in t]
+
+    def set_solver_block_threads(self, threads: int = 0):
+        """Threads per block of the one-lane solver passes: 128, 256, 512 (one scene), 0 = autotune."""
+        self._check(self.L.sphgb_set_solver_block_threads(self.h, int(threads)))
+
+    def solver_block_threads(self):
+        """(threads per block in use, autotuner trial step times in ms for 128, 256, 512)."""
+        k = ctypes.c_uint32()
+        t = np.zeros(3, np.float32)
+        self._check(self.L.sphgb_get_solver_block_threads(self.h, ctypes.byref(k), _p(t)))
         return int(k.value), [float(v) for v in t]
 
     def set_boundary_bodies(self, body, center, dynamic=None):
