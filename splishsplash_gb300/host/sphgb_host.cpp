@@ -398,13 +398,20 @@ void TimeStepDFSPH_GB300::step()
 {
     if (m_dirty) upload();
     pushBodyMotion();
-    check(sphgb_step(m_ctx, &m_stats), "sphgb_step");
+    if (m_hostSync) {
+        // the step is queued without a wait; the download waits for it and its fields together,
+        // after which the step's statistics are on the host
+        check(sphgb_step(m_ctx, nullptr), "sphgb_step");
+        syncToHost();
+        check(sphgb_sync(m_ctx, &m_stats), "sphgb_sync");
+    } else {
+        check(sphgb_step(m_ctx, &m_stats), "sphgb_step");
+    }
     m_iterations = m_stats.iterations;
     m_iterationsV = m_stats.iterations_v;
     if (m_visco) m_visco->m_iterations = m_stats.visco_iterations;
     m_dt = (Real)m_stats.dt_next;   // TimeManager::setTimeStepSize of the CFL update
     m_time = (Real)m_stats.time;
-    if (m_hostSync) syncToHost();
 }
 
 void TimeStepDFSPH_GB300::syncToHost()
@@ -412,13 +419,21 @@ void TimeStepDFSPH_GB300::syncToHost()
     const unsigned int n = totalParticles();
     if (n == 0) return;
     auto dl = [&](int field, void *dst, const char *what) { check(sphgb_download(m_ctx, field, dst, kDtype), what); };
-    // the models' own fields: all models downloaded together, handed back model by model
+    // the fluid fields in one call (one wait): the models' own fields of all models together,
+    // handed back model by model, and the solver's fields
     std::vector<Vector3r> x(n), v(n), a(n);
     std::vector<Real> rho(n);
-    dl(SPHGB_FIELD_POSITION, &x[0][0], "download position");
-    dl(SPHGB_FIELD_VELOCITY, &v[0][0], "download velocity");
-    dl(SPHGB_FIELD_ACCELERATION, &a[0][0], "download acceleration");
-    dl(SPHGB_FIELD_DENSITY, rho.data(), "download density");
+    std::vector<int> ids = {SPHGB_FIELD_POSITION, SPHGB_FIELD_VELOCITY, SPHGB_FIELD_ACCELERATION, SPHGB_FIELD_DENSITY,
+                            SPHGB_FIELD_FACTOR, SPHGB_FIELD_DENSITY_ADV, SPHGB_FIELD_PRESSURE_RHO2,
+                            SPHGB_FIELD_PRESSURE_RHO2_V, SPHGB_FIELD_PRESSURE_ACCEL};
+    std::vector<void *> dsts = {&x[0][0], &v[0][0], &a[0][0], rho.data(), m_factor.data(), m_densityAdv.data(),
+                                m_pressureRho2.data(), m_pressureRho2V.data(), &m_pressureAccel[0][0]};
+    if (m_visco) {
+        ids.push_back(SPHGB_FIELD_VDIFF);
+        dsts.push_back(&m_visco->m_vDiff[0][0]);
+    }
+    check(sphgb_download_fields(m_ctx, static_cast<uint32_t>(ids.size()), ids.data(), dsts.data(), kDtype),
+          "download fields");
     size_t off = 0;
     for (FluidModel *f : m_fluids) {
         const size_t m = f->numParticles();
@@ -428,12 +443,6 @@ void TimeStepDFSPH_GB300::syncToHost()
         std::copy(rho.begin() + off, rho.begin() + off + m, f->m_density.begin());
         off += m;
     }
-    dl(SPHGB_FIELD_FACTOR, m_factor.data(), "download factor");
-    dl(SPHGB_FIELD_DENSITY_ADV, m_densityAdv.data(), "download advected density");
-    dl(SPHGB_FIELD_PRESSURE_RHO2, m_pressureRho2.data(), "download p / rho^2");
-    dl(SPHGB_FIELD_PRESSURE_RHO2_V, m_pressureRho2V.data(), "download p_v / rho^2");
-    dl(SPHGB_FIELD_PRESSURE_ACCEL, &m_pressureAccel[0][0], "download pressure acceleration");
-    if (m_visco) dl(SPHGB_FIELD_VDIFF, &m_visco->m_vDiff[0][0], "download velocity difference");
     // boundary volumes of all models in model order, split per model
     size_t nb = 0;
     for (const BoundaryModel_Akinci2012 *bm : m_boundaries) nb += bm->numberOfParticles();
