@@ -108,3 +108,22 @@ def test_solver_block_sizes_agree(batch):
         np.testing.assert_allclose(r[1], runs[0][1], rtol=0, atol=tol[0])
         np.testing.assert_allclose(r[2], runs[0][2], rtol=0, atol=tol[1])
         np.testing.assert_allclose(r[3], runs[0][3], rtol=tol[2], atol=tol[2] * float(np.max(np.abs(runs[0][3]))))
+
+
+def test_solver_block_threads_are_checked():
+    """Sizes other than 0, 128, 256 and 512 are refused, and 512 on a batch (its blocks would span
+    two scenes' tiles); the refusals leave the context usable."""
+    from splishsplash_gb300 import native
+    ts = TimeStepDFSPH(scenes.small_block(counts=(6, 6, 6)))
+    with pytest.raises(native.SphgbError):
+        ts.ctx.set_solver_block_threads(100)
+    ts.ctx.set_solver_block_threads(512)
+    ts.step()
+    assert ts.ctx.solver_block_threads()[0] in (256, 512)
+    ts.close()
+    b = BatchedTimeStepDFSPH(scenes.ensemble(num_scenes=2, seed=4, n_min=2000, n_max=3000))
+    with pytest.raises(native.SphgbError):
+        b.ctx.set_solver_block_threads(512)
+    b.ctx.set_solver_block_threads(128)
+    b.step()
+    b.close()
