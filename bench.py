@@ -399,7 +399,7 @@ def bender2019_line(steps, device):
             "iterations_mean": {"pressure": float(it[:, 0].mean()), "divergence": float(it[:, 1].mean())}}
 
 
-def ensemble_line(steps, device):
+def ensemble_line(steps, device, use_graph=True):
     """256 independent dam breaks (N_i log-uniform in [2000, 60000]) in one batched context:
     particle-steps/s over `steps` steps after 10 warm-up steps (inputs far larger than L2)."""
     import torch
@@ -408,7 +408,7 @@ def ensemble_line(steps, device):
     from splishsplash_gb300.dfsph import BatchedTimeStepDFSPH
 
     ens = scenes.ensemble(num_scenes=256)
-    b = BatchedTimeStepDFSPH(ens, use_graph=True, device=device)
+    b = BatchedTimeStepDFSPH(ens, use_graph=use_graph, device=device)
     for _ in range(10):
         b.step()
     ext = torch.cuda.ExternalStream(b.ctx.stream())
@@ -468,6 +468,9 @@ def main():
     ap.add_argument("--ensemble-steps", type=int, default=60)
     ap.add_argument("--bender-steps", type=int, default=60)
     ap.add_argument("--only-bender", action="store_true", help="print the volume-map boundary line alone and exit")
+    ap.add_argument("--only-ensemble", action="store_true",
+                    help="print the 256-scene ensemble line alone and exit (with --host-loops: host-driven solver "
+                         "loops, so that a profiler sees every kernel)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -479,6 +482,10 @@ def main():
         return
     if args.only_bender:
         print(json.dumps({"boundary_bender2019": bender2019_line(args.bender_steps, 0)}), flush=True)
+        return
+    if args.only_ensemble:
+        print(json.dumps({"ensemble": ensemble_line(args.ensemble_steps, 0, use_graph=not args.host_loops)}),
+              flush=True)
         return
 
     import torch
