@@ -37,6 +37,7 @@ shard); value = total particle-steps / max time over ranks.
 from __future__ import annotations
 
 import argparse
+import datetime
 import json
 import os
 import statistics
@@ -86,24 +87,32 @@ def workload_config(scene):
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling every 50 ms, started before the warm-up; the samples whose timestamps
+    fall in the timed region (mark() to stop()) are kept, or the one just before a region shorter
+    than the period."""
 
     def __init__(self, index=0):
         self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
         self.p = None
         self.index = index
+        self.t0 = None
 
     def start(self):
-        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
-             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-             "clocks_event_reasons.sw_power_cap")
+        q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}", "--format=csv,noheader,nounits",
-                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+                                       "-lms", "50"], stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.p = None
 
+    def mark(self):
+        """The timed region starts."""
+        self.t0 = time.time()
+
     def stop(self):
+        t1 = time.time()
         if self.p is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.p.terminate()
@@ -113,22 +122,25 @@ class Clocks:
             self.p.kill()
         self.f.flush()
         self.f.seek(0)
-        sm, mx, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        rows = []
         for line in self.f.read().splitlines():
             parts = [x.strip() for x in line.split(",")]
-            if len(parts) < 9:
+            if len(parts) < 10:
                 continue
             try:
-                sm.append(float(parts[1]))
-                mx.append(float(parts[2]))
+                ts = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                rows.append((ts, float(parts[2]), float(parts[3]), parts[6:10]))
             except ValueError:
                 continue
-            for nm, val in zip(names, parts[5:9]):
-                if val.lower().startswith("active"):
-                    reasons.add(nm)
         os.unlink(self.f.name)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+        t0 = self.t0 if self.t0 is not None else t1
+        keep = [r for r in rows if t0 - 0.01 <= r[0] <= t1 + 0.01]
+        if not keep:
+            keep = [r for r in rows if r[0] < t0][-1:]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = {nm for r in keep for nm, val in zip(names, r[3]) if val.lower().startswith("active")}
+        sm = [r[1] for r in keep]
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max((r[2] for r in keep), default=None),
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
@@ -509,18 +521,19 @@ def main():
     ext = torch.cuda.ExternalStream(ts.ctx.stream())
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
 
+    clocks = Clocks(local)
+    clocks.start()   # sampling from before the warm-up; mark() keeps the timed region's samples
     for _ in range(args.warmup):
         ts.step()
 
     # ---------------- device-resident timed region ----------------
-    clocks = Clocks(local)
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     iters = []
     launches = 0
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    clocks.start()
+    clocks.mark()
     t_wall = time.perf_counter()
     for k in range(args.steps):
         with torch.cuda.stream(ext):
